@@ -1,0 +1,286 @@
+"""Benchmark of the marker-in-cell hot path on one GB300 (markers/s, MIC transfer + RK4).
+
+A step is one marker cycle of the 40M-marker rifting model (2001x801 basic
+nodes, 25 markers per cell): inside flags, cell location and the cell-sorted
+marker list, heat and Stokes marker->grid averaging, post-Stokes marker
+gathers, subgrid stress and temperature diffusion, the stress and temperature
+corrections, fused RK4 advection with stress rotation, and the strain update.
+Every field is larger than L2 (40M x 8 B = 320 MB), so no L2 flush is needed.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference] [--workload NAME]
+
+Prints one JSON line.  ``value`` is markers/s with the model resident in HBM;
+``e2e`` is the same metric through the C-ABI with host buffers: each step
+uploads the marker state from pinned host memory and downloads the updated
+state.  ``--impl reference`` times the CPU restatement of the reference (the
+EarthBox.jl functions in plain C, OpenMP across the loops the reference runs
+with Threads.@threads, serial scatters as in the reference) on a bounded strip
+of the same model.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import pathlib
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = pathlib.Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+from __graft_entry__ import load_oracle, load_package  # noqa: E402
+
+METRIC = "markers/s (MIC transfer+RK4)"
+UNIT = "markers/s"
+
+# Bytes per marker each kernel must move (reads + writes of marker arrays), and
+# grid bytes per call; the dominant-kernel roofline uses these.
+ALGO_BYTES_PER_MARKER = {
+    "k_cells<stokes>": 4 + 4 + 8 + 1 + 4 + 8 * 8 + 4 + 4,   # perm, xn, fx/fy, flags, matid, 8 f64, 2 f32
+    "k_cells<heat>": 4 + 8 + 1 + 4 + 5 * 8,
+    "k_cells<denominators>": 4 + 4 + 8 + 1,
+    "k_cells<subgrid_stress>": 4 + 8 + 8 + 1 + 4 + 8 + 2 * 16,
+    "k_cells<subgrid_heat>": 4 + 8 + 8 + 1 + 16 + 8,
+    "k_advect": 8 + 8 + 1 + 16 + 16 + 24 + 32,             # xn/yn, fx/fy, flags, rw x/y, w vx/vy/spin, rw sxx/sxy
+    "k_post_stokes": 8 + 8 + 1 + 4 + 8 + 4 * 8,
+    "k_locate_count": 16 + 1 + 8 + 8 + 1 + 4,               # x,y, inside, w xn/yn, fx/fy, flags, count atomics
+}
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="rift_40M")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    return ap.parse_args()
+
+
+def dist_info():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class Clocks:
+    """nvidia-smi sampling of SM clocks and throttle reasons during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        self.lines = []
+        if self.proc:
+            self.proc.terminate()
+            try:
+                out, _ = self.proc.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+                out, _ = self.proc.communicate()
+            self.lines = [ln for ln in out.splitlines() if ln.strip()]
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in getattr(self, "lines", []):
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx = float(parts[1])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[3:7]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": mx, "reasons": ["unsampled"]}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+E2E_IN = ["x", "y", "matid", "rho", "cohesion", "fric", "eta", "eta_flow", "sxx", "sxy", "pfailure", "dilatation",
+          "meltfrac", "tk", "kt", "rhocp", "ha", "serp_hr", "gii", "strain_plastic"]
+E2E_OUT = ["x", "y", "sxx", "sxy", "tk", "exx", "exy", "pr", "sr_ratio", "gii", "strain_plastic",
+           "strain_rate_plastic"]
+
+
+def cpu_baseline(eb, oracle, steps: int = 2):
+    """The reference's algorithms (C restatement, OpenMP where the reference threads) on a strip
+    of the 40M-marker model: 101x801 nodes at the same spacing, 25 markers per cell (2M markers)."""
+    model = eb.synthetic.rift(101, 801, 5, width=25e3)
+    ref = oracle.OracleMIC(model)
+    ref.marker_cycle()  # warm-up
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        ref.marker_cycle()
+    dt = (time.perf_counter() - t0) / steps
+    return {"value": model.marknum / dt, "unit": UNIT, "cores": oracle.threads(), "kind": "port",
+            "sample": f"{model.marknum} markers (101x801-node strip of the 2001x801 model, same spacing), "
+                      f"{steps} marker cycles after one warm-up; {dt:.3f} s per cycle"}
+
+
+def run_reference(args):
+    rank, world, _ = dist_info()
+    if rank != 0:
+        return
+    eb = load_package()
+    oracle = load_oracle()
+    model = eb.synthetic.rift(101, 801, 5, width=25e3)
+    ref = oracle.OracleMIC(model)
+    for _ in range(args.warmup):
+        ref.marker_cycle()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        ref.marker_cycle()
+    dt = (time.perf_counter() - t0) / max(args.steps, 1)
+    value = model.marknum / dt
+    sample = (f"{model.marknum} markers per step (101x801-node strip of the 2001x801, 25 markers/cell model, "
+              f"same spacing); {dt:.3f} s per marker cycle")
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "impl": "reference", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": args.workload, "sample": "rift strip 101x801 nodes, 2.0M markers"},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": oracle.threads(), "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    rank, world, local = dist_info()
+    import torch
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    eb = load_package()
+    eb.build()
+    t_gen = time.perf_counter()
+    model = eb.synthetic.config(args.workload, seed=100 + rank)   # each replica its own seeded model
+    t_gen = time.perf_counter() - t_gen
+    mic = eb.MarkerInCell(local)
+    mic.load_model(model)
+    stream = torch.cuda.ExternalStream(mic.stream, device=local)
+    M = model.marknum
+
+    def step():
+        mic.marker_cycle()
+
+    for _ in range(max(args.warmup, 3)):
+        step()
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    launches0 = mic.launch_count
+    mic.profile_enable(True)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with Clocks(local) as clk:
+        ev0.record(stream)
+        for _ in range(args.steps):
+            step()
+        ev1.record(stream)
+        torch.cuda.synchronize()
+    ms = ev0.elapsed_time(ev1) / args.steps
+    prof = mic.profile()
+    mic.profile_enable(False)
+    launches = mic.launch_count - launches0
+    ms_t = torch.tensor([ms], device=f"cuda:{local}")
+    if world > 1:
+        torch.distributed.all_reduce(ms_t, op=torch.distributed.ReduceOp.MAX)
+    ms = float(ms_t.item())
+    value = M * world / (ms * 1e-3)
+
+    # dominant kernel: live per-kernel CUDA-event times on the library's stream
+    kern = {k: (t / n, n) for k, (t, n) in prof.items()}
+    dom = max(prof, key=lambda k: prof[k][0])
+    dom_ms, dom_n = kern[dom]
+    peak, peak_kind = peaks()
+    bpm = ALGO_BYTES_PER_MARKER.get(dom)
+    roofline = None
+    if bpm is not None:
+        achieved = bpm * M / (dom_ms * 1e-3) / 1e9
+        roofline = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                    "frac": achieved / peak, "peak_kind": peak_kind, "traffic": None,
+                    "bytes_per_marker": bpm, "launch_ms": dom_ms}
+
+    # e2e: host buffers through the C-ABI, copies inside the timed region
+    e2e = None
+    if not args.no_e2e:
+        pinned_in = {k: torch.from_numpy(np.ascontiguousarray(model.markers[k])).pin_memory().numpy() for k in E2E_IN}
+        pinned_out = {k: torch.empty(M, dtype={"f8": torch.float64, "f4": torch.float32}[
+            eb._abi.MARKER_DTYPE[k]]).pin_memory().numpy() for k in E2E_OUT}
+        h2d = sum(a.nbytes for a in pinned_in.values())
+        d2h = sum(a.nbytes for a in pinned_out.values())
+        reps = max(2, min(args.steps, 5))
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            for k, a in pinned_in.items():
+                mic.upload_marker(k, a)
+            step()
+            for k, a in pinned_out.items():
+                mic._check(mic._lib.eb_marker_download(mic._ctx, eb._abi.MARKER_ID[k], a.ctypes.data))
+        torch.cuda.synchronize()
+        te = (time.perf_counter() - t0) / reps
+        e2e = {"value": M * world / te, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+               "ms_per_step": te * 1e3}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        try:
+            cpu = cpu_baseline(eb, load_oracle())
+        except Exception as exc:  # the baseline is reported, not required
+            cpu = {"value": None, "unit": UNIT, "cores": 0, "kind": "port", "sample": f"failed: {exc}"}
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+                "warmup": max(args.warmup, 3), "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f64 storage, f32 weights/sums", "data": "synthetic",
+                "config": {"workload": args.workload, "markers": M, "xnum": model.grid.xnum, "ynum": model.grid.ynum,
+                           "markers_per_cell": 25 if args.workload == "rift_40M" else None,
+                           "l2": "inputs larger than L2 (each marker field 320 MB)", "parallelism": "replicas"},
+                "gpu_launches": launches, "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
+                "clocks": clk.summary(),
+                "kernels_ms": {k: round(v[0], 4) for k, v in sorted(kern.items(), key=lambda kv: -kv[1][0] * kv[1][1])},
+                "generate_s": round(t_gen, 2)}
+        print(json.dumps(line))
+    mic.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

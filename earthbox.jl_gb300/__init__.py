@@ -1,0 +1,264 @@
+"""GB300 (sm_103a) marker-in-cell hot path for EarthBox.jl -- host-side mirror.
+
+``MarkerInCell`` drives libebgpu.so through its C-ABI (include/ebgpu.h).  Its
+methods carry the names of the EarthBox.jl functions they replace (the Julia
+``!`` dropped), take no arguments beyond the model state the context already
+holds, and raise ``EarthBoxGPUError`` with the library's message on any
+non-zero status, like the reference raises a Julia error.
+
+Typical use, one time step of the marker path::
+
+    mic = MarkerInCell()
+    mic.load_model(model)                       # grid, materials, params, markers, grids
+    mic.get_marker_inside_flags()               # GridFuncs.get_marker_inside_flags
+    mic.initialize_bilinear_interpolation()     # Interpolation.initialize_bilinear_interpolation!
+    mic.interpolate_marker_heat_parameters_to_grid()
+    mic.update_marker_rheology()
+    mic.update_marker_viscoplastic_viscosity(use_marker_plasticity=True)
+    mic.interpolate_marker_stokes_parameters_to_grid()
+    ...                                         # Stokes solve (grid side)
+    mic.post_stokes_marker_gathers()
+    mic.update_subgrid_stress(); mic.apply_marker_stress_correction()
+    mic.subgrid_heat_diffusion_update(); mic.add_remaining_grid_change_to_marker_temperature()
+    mic.advect_markers_and_rotate_stress(); mic.update_marker_strain()
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _abi
+from . import synthetic
+from .build import build
+
+__all__ = ["MarkerInCell", "EarthBoxGPUError", "build", "synthetic"]
+
+
+class EarthBoxGPUError(RuntimeError):
+    def __init__(self, code: int, message: str):
+        super().__init__(f"[status {code}] {message}")
+        self.code = code
+
+
+def _ptr(a: np.ndarray) -> int:
+    return a.ctypes.data
+
+
+class MarkerInCell:
+    """One device context: marker SoA, staggered grids and material tables on one GPU."""
+
+    def __init__(self, device: int = 0):
+        self._lib = _abi.load()
+        self._ctx = C.c_void_p()
+        rc = self._lib.eb_create(C.byref(self._ctx), int(device))
+        if rc != _abi.EB_OK:
+            raise EarthBoxGPUError(rc, "eb_create failed (no CUDA device?)")
+        self.xnum = self.ynum = 0
+        self.marknum = 0
+
+    # ------------------------------------------------------------ plumbing --
+    def _check(self, rc: int) -> None:
+        if rc != _abi.EB_OK:
+            msg = self._lib.eb_last_error(self._ctx)
+            raise EarthBoxGPUError(rc, msg.decode() if msg else "unknown error")
+
+    def close(self) -> None:
+        if self._ctx:
+            self._lib.eb_destroy(self._ctx)
+            self._ctx = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def stream(self) -> int:
+        """The context's cudaStream_t (as an integer) for event timing."""
+        return int(self._lib.eb_stream(self._ctx) or 0)
+
+    @property
+    def launch_count(self) -> int:
+        return int(self._lib.eb_launch_count(self._ctx))
+
+    def profile_enable(self, on: bool = True) -> None:
+        """Time every kernel with CUDA events on the context's stream (clears the counters)."""
+        self._check(self._lib.eb_profile_enable(self._ctx, int(bool(on))))
+
+    def profile(self) -> dict:
+        """{kernel name: (total device ms, launches)} since the last profile_enable."""
+        out = {}
+        buf = C.create_string_buffer(128)
+        for i in range(self._lib.eb_profile_count(self._ctx)):
+            ms, n = C.c_double(), C.c_int64()
+            self._check(self._lib.eb_profile_entry(self._ctx, i, buf, 128, C.byref(ms), C.byref(n)))
+            out[buf.value.decode()] = (ms.value, n.value)
+        return out
+
+    # --------------------------------------------------------------- set-up --
+    def set_grid(self, g: "synthetic.Grid") -> None:
+        self._grid_keep = [np.ascontiguousarray(getattr(g, n), dtype=np.float64) for n in
+                           ("gridx_b", "gridy_b", "xstp_b", "ystp_b", "gridx_vy", "xstp_vy", "gridy_vx", "ystp_vx")]
+        d = _abi.GridDesc(g.xnum, g.ynum, *[_ptr(a) for a in self._grid_keep],
+                          g.xmin, g.xmax, g.ymin, g.ymax, g.xstpavg, g.ystpavg)
+        self._check(self._lib.eb_set_grid(self._ctx, C.byref(d)))
+        self.xnum, self.ynum = int(g.xnum), int(g.ynum)
+
+    def set_materials(self, m: "synthetic.Materials") -> None:
+        keep = [np.ascontiguousarray(m.mat_mu, np.float64), np.ascontiguousarray(m.mat_hr, np.float64),
+                np.ascontiguousarray(m.mat_flow_type, np.int64),
+                np.asfortranarray(m.mat_flow, np.float64).ravel(order="F"),
+                np.asfortranarray(m.mat_plastic, np.float64).ravel(order="F"),
+                np.ascontiguousarray(m.mat_rho, np.float64)]
+        d = _abi.MaterialDesc(len(keep[0]), *[_ptr(a) for a in keep])
+        self._check(self._lib.eb_set_materials(self._ctx, C.byref(d)))
+
+    def set_params(self, params: dict) -> None:
+        p = _abi.Params()
+        for name, _ in _abi.Params._fields_:
+            if name in params:
+                setattr(p, name, params[name])
+        self._params = dict(params)
+        self._check(self._lib.eb_set_params(self._ctx, C.byref(p)))
+
+    def resize_markers(self, marknum: int) -> None:
+        self._check(self._lib.eb_resize_markers(self._ctx, int(marknum)))
+        self.marknum = int(marknum)
+
+    def upload_marker(self, name: str, values: np.ndarray) -> None:
+        a = np.ascontiguousarray(values, dtype=_abi.MARKER_DTYPE[name])
+        if a.shape != (self.marknum,):
+            raise ValueError(f"{name}: expected {self.marknum} values, got {a.shape}")
+        self._check(self._lib.eb_marker_upload(self._ctx, _abi.MARKER_ID[name], _ptr(a)))
+
+    def download_marker(self, name: str) -> np.ndarray:
+        a = np.empty(self.marknum, dtype=_abi.MARKER_DTYPE[name])
+        self._check(self._lib.eb_marker_download(self._ctx, _abi.MARKER_ID[name], _ptr(a)))
+        return a
+
+    def upload_grid(self, name: str, values: np.ndarray) -> None:
+        shape = _abi.grid_shape(name, self.xnum, self.ynum)
+        a = np.asfortranarray(values, dtype=np.float64)
+        if a.shape != shape:
+            raise ValueError(f"{name}: expected shape {shape}, got {a.shape}")
+        self._check(self._lib.eb_grid_upload(self._ctx, _abi.GRID_ID[name], _ptr(a)))
+
+    def download_grid(self, name: str) -> np.ndarray:
+        a = np.empty(_abi.grid_shape(name, self.xnum, self.ynum), dtype=np.float64, order="F")
+        self._check(self._lib.eb_grid_download(self._ctx, _abi.GRID_ID[name], _ptr(a)))
+        return a
+
+    def marker_device_ptr(self, name: str) -> int:
+        p = C.c_void_p()
+        self._check(self._lib.eb_marker_device_ptr(self._ctx, _abi.MARKER_ID[name], C.byref(p)))
+        return int(p.value or 0)
+
+    def grid_device_ptr(self, name: str) -> int:
+        p = C.c_void_p()
+        self._check(self._lib.eb_grid_device_ptr(self._ctx, _abi.GRID_ID[name], C.byref(p)))
+        return int(p.value or 0)
+
+    def load_model(self, model: "synthetic.Model", grids: bool = True) -> None:
+        """Upload a whole model: grid geometry, materials, parameters, markers and grid fields."""
+        self.set_grid(model.grid)
+        self.set_materials(model.mats)
+        self.set_params(model.params)
+        self.resize_markers(model.marknum)
+        for k, v in model.markers.items():
+            if k in ("xn", "yn", "xn_vy", "yn_vy"):
+                continue
+            self.upload_marker(k, v)
+        if grids:
+            for k, v in model.grids.items():
+                self.upload_grid(k, v)
+
+    # --------------------------------------------------- hot-path steps ---
+    def _call(self, name: str) -> None:
+        self._check(getattr(self._lib, name)(self._ctx))
+
+    def get_marker_inside_flags(self) -> None:
+        """GridFuncs.get_marker_inside_flags (src/utils/GridFuncs.jl:54-80)."""
+        self._call("eb_get_marker_inside_flags")
+
+    def initialize_bilinear_interpolation(self) -> None:
+        """InitializeInterpolation.initialize_bilinear_interpolation! (InitializeInterpolation.jl:63-82)."""
+        self._call("eb_initialize_bilinear_interpolation")
+
+    def interpolate_marker_stokes_parameters_to_grid(self) -> None:
+        """MarkersToStokesArrays.interpolate_markers_to_transport_arrays! (MarkersToStokesArrays.jl:39-45)."""
+        self._call("eb_interpolate_marker_stokes_parameters_to_grid")
+
+    def interpolate_marker_heat_parameters_to_grid(self) -> None:
+        """MarkerToHeatArrays.interpolate_markers_to_transport_arrays! (MarkerToHeatArrays.jl:29-35)."""
+        self._call("eb_interpolate_marker_heat_parameters_to_grid")
+
+    def backup_and_clear_viscosity_transport_arrays(self) -> None:
+        """BackupTransportArrays.backup_and_clear_viscosity_transport_arrays! (BackupTransportArrays.jl:105-137)."""
+        self._call("eb_backup_and_clear_viscosity_transport_arrays")
+
+    def interpolate_viscosity_to_transport_arrays(self) -> None:
+        """MarkersToStokesArrays.interpolate_viscosity_to_transport_arrays! (MarkersToStokesArrays.jl:60-64)."""
+        self._call("eb_interpolate_viscosity_to_transport_arrays")
+
+    def interpolate_temperature_to_markers(self) -> None:
+        """GridTemperatureToMarkers.interpolate! (GridTemperatureToMarkers.jl:18-45)."""
+        self._call("eb_interpolate_temperature_to_markers")
+
+    def update_marker_rheology(self) -> None:
+        """Rheology.update_marker_rheology! (src/rheology/Rheology.jl:37-56)."""
+        self._call("eb_update_marker_rheology")
+
+    def update_marker_viscoplastic_viscosity(self, use_marker_plasticity: bool = True) -> None:
+        """Rheology.update_marker_viscoplastic_viscosity! (Rheology.jl:70-107)."""
+        self._check(self._lib.eb_update_marker_viscoplastic_viscosity(self._ctx, int(bool(use_marker_plasticity))))
+
+    def update_plastic_yielding(self) -> None:
+        """MarkerPlasticity.update_plastic_yielding! (ViscoelasticForecast.jl:11-123)."""
+        self._call("eb_update_plastic_yielding")
+
+    def post_stokes_marker_gathers(self) -> None:
+        """Marker part of StokesContinuitySolver.execute_post_stokes_solver_steps! (StokesContinuitySolver.jl:283-290)."""
+        self._call("eb_post_stokes_marker_gathers")
+
+    def update_subgrid_stress(self) -> None:
+        """SubGridStress.Update.update_subgrid_stress! (subgrid_stress/update/Update.jl:69-87)."""
+        self._call("eb_update_subgrid_stress")
+
+    def apply_marker_stress_correction(self) -> None:
+        """StressCorrection.apply_marker_stress_correction_for_remaining_grid_stress! (StressCorrection.jl:35-82)."""
+        self._call("eb_apply_marker_stress_correction")
+
+    def subgrid_heat_diffusion_update(self) -> None:
+        """SubgridDiffusion.subgrid_heat_diffusion_update! + remove_subgrid_effects_from_grid_changes!."""
+        self._call("eb_subgrid_heat_diffusion_update")
+
+    def add_remaining_grid_change_to_marker_temperature(self) -> None:
+        """MarkerTemperature.add_remaining_grid_change_to_marker_temperature! (MarkerTemperature.jl:18-45)."""
+        self._call("eb_add_remaining_grid_change_to_marker_temperature")
+
+    def advect_markers_and_rotate_stress(self) -> None:
+        """Advection.advect_markers_and_rotate_stress_tensor! (src/advection/Advection.jl:109-114)."""
+        self._call("eb_advect_markers_and_rotate_stress")
+
+    def update_marker_strain(self) -> None:
+        """Advection.update_marker_strain! (Advection.jl:169-178)."""
+        self._call("eb_update_marker_strain")
+
+    # ----------------------------------------------------- step sequences --
+    def marker_cycle(self) -> None:
+        """The marker-in-cell transfer + RK4 sequence of one time step (no Stokes/heat solve):
+        locate, heat and Stokes scatters, post-Stokes gathers, subgrid stress and temperature,
+        stress and temperature corrections, RK4 advection and the strain update."""
+        self.get_marker_inside_flags()
+        self.initialize_bilinear_interpolation()
+        self.interpolate_marker_heat_parameters_to_grid()
+        self.interpolate_marker_stokes_parameters_to_grid()
+        self.post_stokes_marker_gathers()
+        self.update_subgrid_stress()
+        self.apply_marker_stress_correction()
+        self.subgrid_heat_diffusion_update()
+        self.add_remaining_grid_change_to_marker_temperature()
+        self.advect_markers_and_rotate_stress()
+        self.update_marker_strain()

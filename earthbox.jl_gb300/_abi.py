@@ -1,0 +1,148 @@
+"""ctypes binding of include/ebgpu.h (the C-ABI of libebgpu.so).
+
+This is the same binding a Julia host writes with ``ccall``; the field and
+status enumerations mirror the header one to one.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import pathlib
+
+PKG = pathlib.Path(__file__).resolve().parent
+LIB_PATH = PKG / "_build" / "libebgpu.so"
+
+EB_OK, EB_NOT_CONVERGED, EB_NAN, EB_BAD_INPUT, EB_CUDA_ERROR, EB_NOT_READY = range(6)
+
+MARKER_FIELDS = [
+    "x", "y", "matid", "rho", "cohesion", "fric", "fric_ini", "eta", "eta_flow", "preexp",
+    "sxx", "sxy", "exx", "exy", "pr", "sr_ratio", "gii", "strain_plastic", "strain_rate_plastic",
+    "tk", "kt", "rhocp", "ha", "meltfrac", "melt_damage", "serp_hr", "pfailure", "dilatation",
+    "vx", "vy", "spin", "subgrid_dt", "xn", "yn", "xn_vy", "yn_vy", "inside",
+]
+MARKER_ID = {n: i for i, n in enumerate(MARKER_FIELDS)}
+MARKER_DTYPE = {n: "f8" for n in MARKER_FIELDS}
+MARKER_DTYPE.update({"matid": "i2", "pfailure": "f4", "dilatation": "f4", "xn": "i4", "yn": "i4",
+                     "xn_vy": "i4", "yn_vy": "i4", "inside": "i1"})
+
+GRID_FIELDS = [
+    # basic (ynum, xnum)
+    "rho1", "rho0", "etas1", "etas0", "eta_flow", "eta_flow0", "mus1", "mus0", "sxy1", "sxy0",
+    "plastics", "plastics0", "cohesion_grid", "cohesion_grid0", "fric_degrees_grid", "fric_degrees_grid0",
+    "wtnodes", "wtetas", "tk1", "tk0", "tk2", "kt1", "kt0", "rhocp1", "rhocp0", "hr1", "hr0", "ha1", "ha0",
+    "exy", "esp", "sxy2", "dsxy", "dsxyn", "dtk1", "dtkn", "plastic_yield",
+    # pressure (ynum-1, xnum-1)
+    "etan1", "etan0", "mun1", "mun0", "sxx1", "sxx0", "plasticn", "plasticn0", "dilatation_grid",
+    "dilatation_grid0", "extractable_meltfrac_grid", "extractable_meltfrac_grid0", "wtetan", "exx",
+    "sxx2", "dsxx", "dsxxn", "pr1",
+    # vx / vy
+    "vx1", "vy1", "rho1_vy", "rho0_vy", "wtnodes_vy",
+    # thermal BC coefficients
+    "btopt", "bbottomt", "bleftt", "brightt",
+]
+GRID_ID = {n: i for i, n in enumerate(GRID_FIELDS)}
+
+
+def grid_shape(name: str, xnum: int, ynum: int) -> tuple[int, int]:
+    i = GRID_ID[name]
+    if i <= GRID_ID["plastic_yield"]:
+        return (ynum, xnum)
+    if i <= GRID_ID["pr1"]:
+        return (ynum - 1, xnum - 1)
+    if name == "vx1":
+        return (ynum + 1, xnum)
+    if i <= GRID_ID["wtnodes_vy"]:
+        return (ynum, xnum + 1)
+    if name in ("btopt", "bbottomt"):
+        return (xnum, 2)
+    return (ynum, 2)
+
+
+class GridDesc(C.Structure):
+    _fields_ = [("xnum", C.c_int64), ("ynum", C.c_int64)] + [
+        (n, C.c_void_p) for n in ("gridx_b", "gridy_b", "xstp_b", "ystp_b", "gridx_vy", "xstp_vy", "gridy_vx", "ystp_vx")
+    ] + [(n, C.c_double) for n in ("xmin", "xmax", "ymin", "ymax", "xstpavg", "ystpavg")]
+
+
+class MaterialDesc(C.Structure):
+    _fields_ = [("nmat", C.c_int64)] + [
+        (n, C.c_void_p) for n in ("mat_mu", "mat_hr", "mat_flow_type", "mat_flow", "mat_plastic", "mat_rho")
+    ]
+
+
+class Params(C.Structure):
+    _fields_ = [
+        ("timestep", C.c_double), ("ntimestep", C.c_int64), ("temperature_top", C.c_double),
+        ("viscosity_min", C.c_double), ("viscosity_max", C.c_double), ("powerlaw_stress_min", C.c_double),
+        ("yield_stress_min", C.c_double), ("yield_stress_max", C.c_double), ("gas_constant", C.c_double),
+        ("iuse_viscous_strain_soft", C.c_int64), ("vsoftfac", C.c_double),
+        ("iuse_fluid_pressure_for_yield", C.c_int64), ("y_sealevel", C.c_double),
+        ("itype_global", C.c_int64), ("no_yielding_in_mobile_wall", C.c_int64),
+        ("matid_sticky_air", C.c_int64), ("matid_mobile_wall", C.c_int64), ("matid_plate_extension", C.c_int64),
+        ("plastic_healing_rate", C.c_double), ("subgrid_diff_coef_stress", C.c_double),
+        ("subgrid_diff_coef_temp", C.c_double), ("iuse_melt_damage", C.c_int64),
+        ("iuse_serpentinization", C.c_int64), ("iuse_topo", C.c_int64),
+        ("matid_sticky_air_rho", C.c_int64), ("matid_sticky_water_rho", C.c_int64),
+        ("runge_kutta_order", C.c_int64),
+    ]
+
+
+ENTRY_POINTS = [
+    "eb_get_marker_inside_flags", "eb_initialize_bilinear_interpolation",
+    "eb_interpolate_marker_stokes_parameters_to_grid", "eb_interpolate_marker_heat_parameters_to_grid",
+    "eb_backup_and_clear_viscosity_transport_arrays", "eb_interpolate_viscosity_to_transport_arrays",
+    "eb_interpolate_temperature_to_markers", "eb_update_marker_rheology", "eb_update_plastic_yielding",
+    "eb_post_stokes_marker_gathers", "eb_update_subgrid_stress", "eb_apply_marker_stress_correction",
+    "eb_subgrid_heat_diffusion_update", "eb_add_remaining_grid_change_to_marker_temperature",
+    "eb_advect_markers_and_rotate_stress", "eb_update_marker_strain",
+]
+ALL_SYMBOLS = [
+    "eb_create", "eb_destroy", "eb_last_error", "eb_set_grid", "eb_set_materials", "eb_set_params",
+    "eb_resize_markers", "eb_marker_upload", "eb_marker_download", "eb_grid_upload", "eb_grid_download",
+    "eb_marker_device_ptr", "eb_grid_device_ptr", "eb_stream", "eb_launch_count",
+    "eb_update_marker_viscoplastic_viscosity", "eb_profile_enable", "eb_profile_count", "eb_profile_entry",
+] + ENTRY_POINTS
+
+_lib = None
+
+
+def load(path: pathlib.Path | str | None = None) -> C.CDLL:
+    """Load libebgpu.so and declare its signatures.  Raises if it is missing."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = pathlib.Path(path) if path else LIB_PATH
+    if not p.exists():
+        raise RuntimeError(f"libebgpu.so not built ({p}); run earthbox_gb300.build.build()")
+    lib = C.CDLL(str(p))
+    vp = C.c_void_p
+    lib.eb_create.argtypes = [C.POINTER(vp), C.c_int]
+    lib.eb_destroy.argtypes = [vp]
+    lib.eb_last_error.argtypes = [vp]
+    lib.eb_last_error.restype = C.c_char_p
+    lib.eb_set_grid.argtypes = [vp, C.POINTER(GridDesc)]
+    lib.eb_set_materials.argtypes = [vp, C.POINTER(MaterialDesc)]
+    lib.eb_set_params.argtypes = [vp, C.POINTER(Params)]
+    lib.eb_resize_markers.argtypes = [vp, C.c_int64]
+    lib.eb_marker_upload.argtypes = [vp, C.c_int, vp]
+    lib.eb_marker_download.argtypes = [vp, C.c_int, vp]
+    lib.eb_grid_upload.argtypes = [vp, C.c_int, vp]
+    lib.eb_grid_download.argtypes = [vp, C.c_int, vp]
+    lib.eb_marker_device_ptr.argtypes = [vp, C.c_int, C.POINTER(vp)]
+    lib.eb_grid_device_ptr.argtypes = [vp, C.c_int, C.POINTER(vp)]
+    lib.eb_stream.argtypes = [vp]
+    lib.eb_stream.restype = vp
+    lib.eb_launch_count.argtypes = [vp]
+    lib.eb_launch_count.restype = C.c_int64
+    lib.eb_update_marker_viscoplastic_viscosity.argtypes = [vp, C.c_int]
+    lib.eb_profile_enable.argtypes = [vp, C.c_int]
+    lib.eb_profile_count.argtypes = [vp]
+    lib.eb_profile_entry.argtypes = [vp, C.c_int, C.c_char_p, C.c_int, C.POINTER(C.c_double),
+                                     C.POINTER(C.c_int64)]
+    for name in ENTRY_POINTS:
+        getattr(lib, name).argtypes = [vp]
+    for name in ALL_SYMBOLS:
+        if name not in ("eb_last_error", "eb_stream", "eb_launch_count"):
+            getattr(lib, name).restype = C.c_int
+    if path is None:
+        _lib = lib
+    return lib

@@ -1,0 +1,187 @@
+// eb_advect.cu -- fused RK4 advection, stress rotation and strain update.
+//
+// Reference: Advection.advect_markers_and_rotate_stress_tensor! (src/advection/Advection.jl:109-114):
+//   VelocityAndSpin.update_marker_velocity_and_spin_using_runge_kutta! (VelocityAndSpin.jl:45-129,
+//     rk_update :131, interpolate_vx :343, interpolate_vy :373, interpolate_spin :402),
+//   RungeKutta.jl:9-69, MarkersLocation.update! (MarkersLocation.jl:11-39),
+//   MarkersStressRotation.rotate_marker_stress (MarkersStressRotation.jl:59-75);
+// and MarkersStrain.update_total_strain! / update_plastic_strain! (MarkersStrain.jl:11-136).
+// The reference runs three passes through marker_vx/vy/spin buffers; here one
+// pass does all four RK stages, the move and the rotation.
+//
+// Precision: the intermediate RK positions are carried in FP32 relative to the
+// marker's upper-left basic node (offsets below a few cells, so the FP32 error
+// is ~1e-7 of a cell); the interpolated velocities are FP32; the final position
+// update x + dt*v and the stress update are done in FP64.  A cell choice that
+// differs from the reference at an intermediate stage (a point within FP32
+// rounding of a grid line) does not change the velocity, because the bilinear
+// interpolant is continuous across cell edges.
+#include "eb_internal.h"
+
+namespace {
+
+constexpr int kBlock = 256;
+
+__global__ void k_to_float(const double* __restrict__ a, float* __restrict__ b, int64_t n) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) b[i] = (float)a[i];
+}
+
+struct VelGrids {
+  const float *vx1, *vy1, *esp;
+  float dt;
+  double dtd;  // the same time step in FP64 for the position update
+  int order;   // 1 or 4
+};
+
+// Locate a point given as an FP32 offset (px, py) from basic node (ix0, iy0):
+// walk to the basic cell that contains it (searchsortedlast + clamp semantics)
+// and return the offsets (ux, uy) from that cell's upper-left node.
+__device__ __forceinline__ void walk_x(const DevGrid& g, int32_t ix0, float px, int32_t& j, float& u) {
+  j = ix0;
+  float o = 0.f;
+  while (j < g.xnum - 1 && px >= o + __ldg(&g.sxf[j - 1])) { o += __ldg(&g.sxf[j - 1]); ++j; }
+  while (j > 1 && px < o) { --j; o -= __ldg(&g.sxf[j - 1]); }
+  u = px - o;
+}
+__device__ __forceinline__ void walk_y(const DevGrid& g, int32_t iy0, float py, int32_t& i, float& u) {
+  i = iy0;
+  float o = 0.f;
+  while (i < g.ynum - 1 && py >= o + __ldg(&g.syf[i - 1])) { o += __ldg(&g.syf[i - 1]); ++i; }
+  while (i > 1 && py < o) { --i; o -= __ldg(&g.syf[i - 1]); }
+  u = py - o;
+}
+
+// VelocityAndSpin.interpolate_vx / interpolate_vy / interpolate_spin at a point
+// with offsets (ux, uy) inside basic cell (jx, jy).
+__device__ __forceinline__ void vel_spin(const DevGrid& g, const VelGrids& V, int32_t jx, int32_t jy, float ux,
+                                         float uy, float& vx, float& vy, float& sp) {
+  const float dx = ux * __ldg(&g.rsxf[jx - 1]);
+  const float dy = uy * __ldg(&g.rsyf[jy - 1]);
+  // vx grid: x from the basic cell, y row yi = jy + (y > gridy_vx[jy+1])
+  const float vhi = __ldg(&g.vxoff_hi[jy - 1]);
+  const int32_t yi = (uy > vhi) ? jy + 1 : jy;
+  const float dyv = (uy - ((yi == jy) ? __ldg(&g.vxoff_lo[jy - 1]) : vhi)) * __ldg(&g.rsyvxf[yi - 1]);
+  vx = gather4f(V.vx1, g.ynum + 1, yi, jx, dx, dyv);
+  // vy grid: column xi = jx + (x > gridx_vy[jx+1]), y from the basic cell
+  const float hhi = __ldg(&g.vyoff_hi[jx - 1]);
+  const int32_t xi = (ux > hhi) ? jx + 1 : jx;
+  const float dxv = (ux - ((xi == jx) ? __ldg(&g.vyoff_lo[jx - 1]) : hhi)) * __ldg(&g.rsxvyf[xi - 1]);
+  vy = gather4f(V.vy1, g.ynum, jy, xi, dxv, dy);
+  // basic grid spin
+  sp = gather4f(V.esp, g.ynum, jy, jx, dx, dy);
+}
+
+__global__ void k_advect(DevMarkers mk, DevGrid g, VelGrids V) {
+  const int64_t m = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= mk.M) return;
+  if (!(mk.mflags[m] & MF_INSIDE)) {
+    mk.vx[m] = 0.0; mk.vy[m] = 0.0; mk.spin[m] = 0.0;
+    return;
+  }
+  const int32_t ix0 = mk.xn[m], iy0 = mk.yn[m];
+  const float lx0 = mk.fx[m] * __ldg(&g.sxf[ix0 - 1]);
+  const float ly0 = mk.fy[m] * __ldg(&g.syf[iy0 - 1]);
+  const float h = V.dt;
+  float v1x, v1y, s1;
+  vel_spin(g, V, ix0, iy0, lx0, ly0, v1x, v1y, s1);
+  float vxm = v1x, vym = v1y, spm = s1;
+  if (V.order == 4) {
+    float v2x, v2y, s2, v3x, v3y, s3, v4x, v4y, s4, ux, uy;
+    int32_t jx, jy;
+    walk_x(g, ix0, lx0 + (h * 0.5f) * v1x, jx, ux);
+    walk_y(g, iy0, ly0 + (h * 0.5f) * v1y, jy, uy);
+    vel_spin(g, V, jx, jy, ux, uy, v2x, v2y, s2);
+    walk_x(g, ix0, lx0 + (h * 0.5f) * v2x, jx, ux);
+    walk_y(g, iy0, ly0 + (h * 0.5f) * v2y, jy, uy);
+    vel_spin(g, V, jx, jy, ux, uy, v3x, v3y, s3);
+    walk_x(g, ix0, lx0 + h * v3x, jx, ux);
+    walk_y(g, iy0, ly0 + h * v3y, jy, uy);
+    vel_spin(g, V, jx, jy, ux, uy, v4x, v4y, s4);
+    // RungeKutta.apply_4th_order_runge_kutta
+    vxm = (v1x + 2.f * v2x + 2.f * v3x + v4x) / 6.f;
+    vym = (v1y + 2.f * v2y + 2.f * v3y + v4y) / 6.f;
+    spm = (s1 + 2.f * s2 + 2.f * s3 + s4) / 6.f;
+  }
+  mk.vx[m] = (double)vxm;
+  mk.vy[m] = (double)vym;
+  mk.spin[m] = (double)spm;
+  // MarkersLocation.advect_marker: x + timestep * v (FP64)
+  mk.x[m] = fma(V.dtd, (double)vxm, mk.x[m]);
+  mk.y[m] = fma(V.dtd, (double)vym, mk.y[m]);
+  // MarkersStressRotation.rotate_marker_stress, written as increments:
+  //   sxy' = sxy + sxx sin(2w) + sxy (cos(2w) - 1),  sxx' = sxx + sxx (cos(2w) - 1) - sxy sin(2w)
+  // with cos(2w) - 1 = -2 sin(w)^2 evaluated without cancellation.
+  const float w = spm * V.dt;
+  const float s2w = sinf(2.f * w), sw = sinf(w);
+  const float c2m1 = -2.f * sw * sw;
+  const double sxx = mk.sxx[m], sxy = mk.sxy[m];
+  const float fxx = (float)sxx, fxy = (float)sxy;
+  mk.sxy[m] = sxy + (double)(fxx * s2w + fxy * c2m1);
+  mk.sxx[m] = sxx + (double)(fxx * c2m1 - fxy * s2w);
+}
+
+// MarkersStrain.update_total_strain! and update_plastic_strain!
+__global__ void k_strain(DevMarkers mk, double dt, double healing) {
+  const int64_t m = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= mk.M || mk.inside[m] != 1) return;
+  const float eii = hypotf((float)mk.exx[m], (float)mk.exy[m]);
+  mk.gii[m] = fma(dt, (double)eii, mk.gii[m]);
+  if (mk.pfailure[m] != 1.0f) return;
+  const double eta = mk.eta[m], eta_flow = mk.eta_flow[m];
+  const float sii = hypotf((float)mk.sxx[m], (float)mk.sxy[m]);
+  // 0.5 sii (1/eta - 1/eta_flow) = 0.5 sii ((eta_flow - eta) / eta) / eta_flow
+  const float d = (float)(eta_flow - eta);
+  float rate = 0.5f * sii * ((d / (float)eta) / (float)eta_flow);
+  rate = fmaxf(0.f, rate);
+  double sp = mk.sp[m] + dt * (double)rate - healing * dt;
+  mk.sp[m] = sp > 0.0 ? sp : 0.0;
+  mk.srp[m] = (double)rate;
+}
+
+}  // namespace
+
+int launch_advect(eb_ctx* c) {
+  const int64_t order = c->P.runge_kutta_order;
+  if (order <= 0) return EB_OK;  // NoMotion: markers fixed (Advection options)
+  if (order != 1 && order != 4) return eb_fail(c, EB_BAD_INPUT, "runge_kutta_order must be 0, 1 or 4");
+  int rc;
+  const int mf[] = {EB_M_X, EB_M_Y, EB_M_VX, EB_M_VY, EB_M_SPIN, EB_M_SXX, EB_M_SXY};
+  for (int f : mf) if ((rc = ensure_marker_field(c, f))) return rc;
+  if ((rc = ensure_grid_field(c, EB_G_VX1)) || (rc = ensure_grid_field(c, EB_G_VY1)) || (rc = ensure_grid_field(c, EB_G_ESP)))
+    return rc;
+  const int64_t nvx = grid_field_count(c, EB_G_VX1), nvy = grid_field_count(c, EB_G_VY1), nb = grid_field_count(c, EB_G_ESP);
+  if (!c->vx1f) {
+    EB_CK(c, cudaMalloc(&c->vx1f, nvx * sizeof(float)));
+    EB_CK(c, cudaMalloc(&c->vy1f, nvy * sizeof(float)));
+    EB_CK(c, cudaMalloc(&c->espf, nb * sizeof(float)));
+  }
+  EB_PROF(c, "k_to_float");
+  k_to_float<<<(unsigned)((nvx + 255) / 256), 256, 0, c->stream>>>(c->gf[EB_G_VX1], c->vx1f, nvx);
+  EB_LAUNCHED(c);
+  EB_PROF(c, "k_to_float");
+  k_to_float<<<(unsigned)((nvy + 255) / 256), 256, 0, c->stream>>>(c->gf[EB_G_VY1], c->vy1f, nvy);
+  EB_LAUNCHED(c);
+  EB_PROF(c, "k_to_float");
+  k_to_float<<<(unsigned)((nb + 255) / 256), 256, 0, c->stream>>>(c->gf[EB_G_ESP], c->espf, nb);
+  EB_LAUNCHED(c);
+  if (c->M == 0) return EB_OK;
+  VelGrids V{c->vx1f, c->vy1f, c->espf, (float)c->P.timestep, c->P.timestep, (int)order};
+  EB_PROF(c, "k_advect");
+  k_advect<<<(unsigned)((c->M + kBlock - 1) / kBlock), kBlock, 0, c->stream>>>(dev_markers(c), c->g, V);
+  EB_LAUNCHED(c);
+  return EB_OK;
+}
+
+int launch_update_strain(eb_ctx* c) {
+  int rc;
+  const int mf[] = {EB_M_INSIDE, EB_M_EXX, EB_M_EXY, EB_M_GII, EB_M_PFAILURE, EB_M_ETA, EB_M_ETA_FLOW,
+                    EB_M_SXX, EB_M_SXY, EB_M_STRAIN_PLASTIC, EB_M_STRAIN_RATE_PLASTIC};
+  for (int f : mf) if ((rc = ensure_marker_field(c, f))) return rc;
+  if (c->M == 0) return EB_OK;
+  EB_PROF(c, "k_strain");
+  k_strain<<<(unsigned)((c->M + kBlock - 1) / kBlock), kBlock, 0, c->stream>>>(dev_markers(c), c->P.timestep,
+                                                                                c->P.plastic_healing_rate);
+  EB_LAUNCHED(c);
+  return EB_OK;
+}

@@ -1,0 +1,135 @@
+// eb_gather.cu -- grid -> marker bilinear gathers (coalesced SoA passes).
+//
+// Reference: GridToMarker.get_marker_value (src/interpolation/utils/GridToMarker.jl:190-226),
+// GridTemperatureToMarkers.interpolate! (GridTemperatureToMarkers.jl:18-45),
+// MarkerStrainRate.jl:23-69, MarkerStrainRateRatio.jl:191-322, MarkerPressure.jl:17-54,
+// StressCorrection.jl:35-82, MarkerTemperature.jl:18-45.
+// The post-Stokes marker gathers (strain rate, strain-rate ratio, pressure) are
+// one pass here instead of three.  Weights and sums run in FP32 on FP64 grid
+// values; results are stored in FP64.
+#include "eb_internal.h"
+
+namespace {
+
+constexpr int kBlock = 256;
+
+// Pressure-grid bilinear gather (GridToMarker.jl:104-153, MarkerGridMapping.jl:311-350).
+__device__ __forceinline__ float gather_p(const double* __restrict__ pg, const DevGrid& g, int32_t ix, int32_t iy,
+                                          float lx, float ly) {
+  const float hx = __ldg(&g.vyoff_hi[ix - 1]), hy = __ldg(&g.vxoff_hi[iy - 1]);
+  const int32_t xp = clamp_i((lx < hx) ? ix - 1 : ix, 1, g.xnum - 2);
+  const int32_t yp = clamp_i((ly < hy) ? iy - 1 : iy, 1, g.ynum - 2);
+  const float ox = (xp + 1 == ix) ? __ldg(&g.vyoff_lo[ix - 1]) : hx;
+  const float oy = (yp + 1 == iy) ? __ldg(&g.vxoff_lo[iy - 1]) : hy;
+  return gather4(pg, g.ynum - 1, yp, xp, (lx - ox) * __ldg(&g.rsxvyf[xp]), (ly - oy) * __ldg(&g.rsyvxf[yp]));
+}
+
+__global__ void k_gather_temperature(DevMarkers mk, DevGrid g, const double* __restrict__ tk1) {
+  const int64_t m = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= mk.M || !(mk.mflags[m] & MF_INSIDE)) return;
+  mk.tk[m] = (double)gather4(tk1, g.ynum, mk.yn[m], mk.xn[m], mk.fx[m], mk.fy[m]);
+}
+
+struct PostStokesGrids {
+  const double *exx, *exy, *sxx2, *sxy2, *dsxx, *dsxy, *pr1, *mat_mu;
+  float dt;
+};
+
+__global__ void k_post_stokes(DevMarkers mk, DevGrid g, PostStokesGrids G) {
+  const int64_t m = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= mk.M || !(mk.mflags[m] & MF_INSIDE)) return;
+  const int32_t ix = mk.xn[m], iy = mk.yn[m];
+  const float fx = mk.fx[m], fy = mk.fy[m];
+  const float lx = fx * __ldg(&g.sxf[ix - 1]), ly = fy * __ldg(&g.syf[iy - 1]);
+  // MarkerStrainRate.calculate_marker_strain_rate!
+  const float exx = gather_p(G.exx, g, ix, iy, lx, ly);
+  const float exy = gather4(G.exy, g.ynum, iy, ix, fx, fy);
+  mk.exx[m] = (double)exx;
+  mk.exy[m] = (double)exy;
+  // MarkerStrainRateRatio.calculate_marker_strain_rate_ratio! / marker_strain_rate_ratio
+  const float sxx2 = gather_p(G.sxx2, g, ix, iy, lx, ly);
+  const float sxy2 = gather4(G.sxy2, g.ynum, iy, ix, fx, fy);
+  const float dsxx = gather_p(G.dsxx, g, ix, iy, lx, ly);
+  const float dsxy = gather4(G.dsxy, g.ynum, iy, ix, fx, fy);
+  const float mu = (float)__ldg(&G.mat_mu[mk.matid[m] - 1]);
+  const float eta = (float)mk.eta[m];
+  const float eii = hypotf(exx, exy);
+  float r = 1.f;
+  if (eii > 0.f) {
+    const float tf = 1.f / (G.dt * mu);
+    const float a = 0.5f * (sxx2 / eta + dsxx * tf);
+    const float b = 0.5f * (sxy2 / eta + dsxy * tf);
+    r = hypotf(a, b) / eii;
+  }
+  mk.sr_ratio[m] = (double)r;
+  // MarkerPressure.calculate_marker_pressure!
+  mk.pr[m] = (double)gather_p(G.pr1, g, ix, iy, lx, ly);
+}
+
+__global__ void k_stress_correction(DevMarkers mk, DevGrid g, const double* __restrict__ dsxy,
+                                    const double* __restrict__ dsxx) {
+  const int64_t m = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= mk.M || !(mk.mflags[m] & MF_INSIDE)) return;
+  const int32_t ix = mk.xn[m], iy = mk.yn[m];
+  const float fx = mk.fx[m], fy = mk.fy[m];
+  const float lx = fx * __ldg(&g.sxf[ix - 1]), ly = fy * __ldg(&g.syf[iy - 1]);
+  mk.sxy[m] = mk.sxy[m] + (double)gather4(dsxy, g.ynum, iy, ix, fx, fy);
+  mk.sxx[m] = mk.sxx[m] + (double)gather_p(dsxx, g, ix, iy, lx, ly);
+}
+
+__global__ void k_add_dt(DevMarkers mk, DevGrid g, const double* __restrict__ dtk1) {
+  const int64_t m = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= mk.M || !(mk.mflags[m] & MF_INSIDE)) return;
+  mk.tk[m] = mk.tk[m] + (double)gather4(dtk1, g.ynum, mk.yn[m], mk.xn[m], mk.fx[m], mk.fy[m]);
+}
+
+unsigned mblocks(const eb_ctx* c) { return (unsigned)((c->M + kBlock - 1) / kBlock); }
+
+}  // namespace
+
+int launch_gather_temperature(eb_ctx* c) {
+  int rc;
+  if ((rc = ensure_marker_field(c, EB_M_TK)) || (rc = ensure_grid_field(c, EB_G_TK1))) return rc;
+  if (c->M == 0) return EB_OK;
+  EB_PROF(c, "k_gather_temperature");
+  k_gather_temperature<<<mblocks(c), kBlock, 0, c->stream>>>(dev_markers(c), c->g, c->gf[EB_G_TK1]);
+  EB_LAUNCHED(c);
+  return EB_OK;
+}
+
+int launch_post_stokes_gathers(eb_ctx* c) {
+  int rc;
+  const int mf[] = {EB_M_EXX, EB_M_EXY, EB_M_SR_RATIO, EB_M_PR, EB_M_ETA, EB_M_MATID};
+  for (int f : mf) if ((rc = ensure_marker_field(c, f))) return rc;
+  const int gfs[] = {EB_G_EXX, EB_G_EXY, EB_G_SXX2, EB_G_SXY2, EB_G_DSXX, EB_G_DSXY, EB_G_PR1};
+  for (int f : gfs) if ((rc = ensure_grid_field(c, f))) return rc;
+  if (c->M == 0) return EB_OK;
+  PostStokesGrids G{c->gf[EB_G_EXX], c->gf[EB_G_EXY], c->gf[EB_G_SXX2], c->gf[EB_G_SXY2], c->gf[EB_G_DSXX],
+                    c->gf[EB_G_DSXY], c->gf[EB_G_PR1], c->mats.mu, (float)c->P.timestep};
+  EB_PROF(c, "k_post_stokes");
+  k_post_stokes<<<mblocks(c), kBlock, 0, c->stream>>>(dev_markers(c), c->g, G);
+  EB_LAUNCHED(c);
+  return EB_OK;
+}
+
+int launch_stress_correction(eb_ctx* c) {
+  int rc;
+  if ((rc = ensure_marker_field(c, EB_M_SXX)) || (rc = ensure_marker_field(c, EB_M_SXY)) ||
+      (rc = ensure_grid_field(c, EB_G_DSXY)) || (rc = ensure_grid_field(c, EB_G_DSXX)))
+    return rc;
+  if (c->M == 0) return EB_OK;
+  EB_PROF(c, "k_stress_correction");
+  k_stress_correction<<<mblocks(c), kBlock, 0, c->stream>>>(dev_markers(c), c->g, c->gf[EB_G_DSXY], c->gf[EB_G_DSXX]);
+  EB_LAUNCHED(c);
+  return EB_OK;
+}
+
+int launch_add_remaining_dt(eb_ctx* c) {
+  int rc;
+  if ((rc = ensure_marker_field(c, EB_M_TK)) || (rc = ensure_grid_field(c, EB_G_DTK1))) return rc;
+  if (c->M == 0) return EB_OK;
+  EB_PROF(c, "k_add_dt");
+  k_add_dt<<<mblocks(c), kBlock, 0, c->stream>>>(dev_markers(c), c->g, c->gf[EB_G_DTK1]);
+  EB_LAUNCHED(c);
+  return EB_OK;
+}

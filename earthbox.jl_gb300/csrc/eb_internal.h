@@ -1,0 +1,147 @@
+// eb_internal.h -- context layout and kernel launchers shared by the .cu files.
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <map>
+#include <string>
+#include <vector>
+#include "../../include/ebgpu.h"
+#include "eb_common.cuh"
+
+// Device-side grid tables (all pointers are device pointers).
+struct DevGrid {
+  int32_t xnum, ynum;
+  const double *gx, *gy, *sx, *sy;       // basic coordinates / spacings (FP64)
+  const double *rsx, *rsy;                // 1/xstp_b, 1/ystp_b (FP64)
+  Axis ax, ay, axvy;                      // exact search tables
+  // FP32 per-basic-index tables, index j-1 for 1-based j
+  const float *sxf, *rsxf;                // [xnum-1] xstp_b, 1/xstp_b
+  const float *syf, *rsyf;                // [ynum-1]
+  const float *vyoff_lo, *vyoff_hi;       // [xnum-1] gridx_vy[j]-gx[j], gridx_vy[j+1]-gx[j]
+  const float *vxoff_lo, *vxoff_hi;       // [ynum-1] gridy_vx[i]-gy[i], gridy_vx[i+1]-gy[i]
+  const float *rsxvyf;                    // [xnum]   1/xstp_vy
+  const float *rsyvxf;                    // [ynum]   1/ystp_vx
+  uint64_t kxmin, kxmax, kymin, kymax;    // order keys of the domain limits
+  double xstpavg, ystpavg;
+};
+
+struct DevMats {
+  int32_t nmat;
+  const double *mu, *hr, *flow, *plastic, *rho;
+  const int32_t* flow_type;
+};
+
+// Marker SoA pointers handed to kernels.
+struct DevMarkers {
+  int64_t M;
+  double *x, *y;
+  int32_t* matid;
+  double *rho, *cohesion, *fric, *fric_ini, *eta, *eta_flow, *preexp;
+  double *sxx, *sxy, *exx, *exy, *pr, *sr_ratio, *gii, *sp, *srp;
+  double *tk, *kt, *rhocp, *ha, *melt, *melt_damage, *serp_hr;
+  float *pfailure, *dilat;
+  double *vx, *vy, *spin, *subgrid_dt;
+  int32_t *xn, *yn;
+  int8_t* inside;
+  float *fx, *fy;   // FP32 normalised distances from the upper-left basic node
+  uint8_t* mflags;  // MF_* bits
+};
+
+struct CellSort {
+  int32_t ncells;        // (ynum-1)*(xnum-1)
+  int32_t* count;        // [ncells+1]
+  int32_t* start;        // [ncells+1] exclusive scan of count
+  int32_t* cursor;       // [ncells]
+  int32_t* perm;         // [M] marker indices grouped by cell, ascending within a cell
+  int32_t* perm_tmp;     // [M] placement buffer before the per-cell sort
+  int32_t* scan_tmp;     // block sums for the scan
+  int32_t scan_blocks;
+};
+
+// Per-kernel timing with CUDA events on the context's stream (off by default).
+struct Profiler {
+  bool on = false;
+  std::vector<cudaEvent_t> pool;                 // reused event pairs
+  size_t used = 0;                               // events handed out since the last resolve
+  std::vector<std::pair<std::string, size_t>> pending;  // (kernel, index of its start event)
+  std::map<std::string, std::pair<double, int64_t>> acc;  // kernel -> (total ms, launches)
+  const char* open_name = nullptr;
+};
+
+struct eb_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  std::string err;
+  int64_t launches = 0;
+  eb_params P{};
+  bool have_params = false, have_grid = false, have_mats = false, located = false;
+  // grid
+  int32_t xnum = 0, ynum = 0;
+  std::vector<void*> grid_allocs;  // coordinate tables
+  DevGrid g{};
+  double* gf[EB_G_NFIELDS] = {};
+  float *vx1f = nullptr, *vy1f = nullptr, *espf = nullptr;  // FP32 copies for RK4
+  // materials
+  std::vector<void*> mat_allocs;
+  DevMats mats{};
+  std::vector<double> h_mat_rho, h_mat_plastic;  // host copies used by launch set-up
+  // markers
+  int64_t M = 0;
+  int32_t matid_max = 0;  // largest uploaded marker_matid (checked against nmat before use)
+  void* mf[EB_M_NFIELDS] = {};
+  float *fx = nullptr, *fy = nullptr;
+  uint8_t* mflags = nullptr;
+  // cell sort and per-cell partial sums
+  CellSort cs{};
+  float* part = nullptr;     // [kMaxSlots * ncells]
+  int32_t* dflag = nullptr;  // device status word written by kernels (0 = ok)
+  Profiler prof;
+};
+
+constexpr int kMaxSlots = 48;
+
+// error helpers
+int eb_fail(eb_ctx* c, int code, const std::string& msg);
+int eb_cuda(eb_ctx* c, cudaError_t e, const char* what);
+#define EB_CK(ctx, call)                                  \
+  do {                                                    \
+    cudaError_t _e = (call);                              \
+    if (_e != cudaSuccess) return eb_cuda(ctx, _e, #call); \
+  } while (0)
+// Every kernel launch is bracketed by EB_PROF(ctx, "name") before and EB_LAUNCHED(ctx) after.
+void prof_begin(eb_ctx* c, const char* name);
+void prof_end(eb_ctx* c);
+void prof_resolve(eb_ctx* c);
+#define EB_PROF(ctx, name) prof_begin(ctx, name)
+#define EB_LAUNCHED(ctx)                                                    \
+  do {                                                                      \
+    (ctx)->launches++;                                                      \
+    prof_end(ctx);                                                          \
+    cudaError_t _e = cudaGetLastError();                                    \
+    if (_e != cudaSuccess) return eb_cuda(ctx, _e, "kernel launch");        \
+  } while (0)
+
+// field helpers (eb_ctx.cu)
+int ensure_grid_field(eb_ctx* c, int f);
+int ensure_marker_field(eb_ctx* c, int f);
+DevMarkers dev_markers(eb_ctx* c);
+size_t grid_field_count(const eb_ctx* c, int f);
+
+// launchers
+int launch_inside_flags(eb_ctx* c);
+int launch_locate_and_sort(eb_ctx* c);
+int launch_denominators(eb_ctx* c);
+int launch_scatter_stokes(eb_ctx* c);
+int launch_scatter_heat(eb_ctx* c);
+int launch_scatter_viscosity(eb_ctx* c);
+int launch_subgrid_stress(eb_ctx* c);
+int launch_subgrid_heat(eb_ctx* c);
+int launch_gather_temperature(eb_ctx* c);
+int launch_post_stokes_gathers(eb_ctx* c);
+int launch_stress_correction(eb_ctx* c);
+int launch_add_remaining_dt(eb_ctx* c);
+int launch_advect(eb_ctx* c);
+int launch_update_strain(eb_ctx* c);
+int launch_rheology(eb_ctx* c);
+int launch_viscoplastic(eb_ctx* c, int use_marker_plasticity);
+int launch_plastic_yielding(eb_ctx* c);

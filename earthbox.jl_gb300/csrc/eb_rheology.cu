@@ -1,0 +1,277 @@
+// eb_rheology.cu -- per-marker failure properties, composite creep viscosity and
+// Drucker-Prager marker yielding.
+//
+// Reference (src/rheology):
+//   FailureProperties.calculate_failure_properties_loop!   plastic_failure/failure_properties/FailureProperties.jl:19-161
+//   CompositeViscosity.update_marker_flow_viscosity!        flow_viscosity/update/types/composite_viscosity/CompositeViscosity.jl:133-418
+//   CompositeCreep / CreepStrainRate / ExponentialTerm / PeierlsCreep   composite_creep/*.jl
+//   ViscousStrainSoftening                                   viscous_strain_softening/ViscousStrainSoftening.jl:14-39
+//   ViscoplasticViscosity.update_marker_viscoplastic_viscosity!  viscoplastic_viscosity/ViscoplasticViscosity.jl:21-60
+//   ViscoelasticForecast.update_plastic_yielding!            plastic_failure/markers/update/types/ViscoelasticForecast.jl:11-181
+//   YieldStress / FluidPressure / Limits / YieldCheck / CheckYield   plastic_failure/utils/*.jl, markers/update/utils/*.jl
+// These kernels run in FP64 end to end: the bisection's stopping test
+// (|dsigma| <= 1 Pa) and its branch decisions must follow the reference's
+// FP64 path to keep the flow viscosity within tolerance.
+#include "eb_internal.h"
+
+namespace {
+
+constexpr int kBlock = 128;
+constexpr double kPaToMPa = 1.0 / 1e6;
+
+__device__ __forceinline__ double MATV(const double* t, int32_t nmat, int32_t m, int k) {
+  return __ldg(&t[(size_t)(k - 1) * nmat + (m - 1)]);
+}
+
+// Julia Float64^Float64 for the exponents on this path (2 -> x*x, 3 -> x*x*x, 1 -> x).
+__device__ __forceinline__ double jl_pow(double x, double y) {
+  if (y == 2.0) return x * x;
+  if (y == 3.0) return x * x * x;
+  if (y == 1.0) return x;
+  return pow(x, y);
+}
+
+__global__ void k_failure(DevMarkers mk, DevMats mt, int melt_damage) {
+  const int64_t m = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= mk.M || mk.inside[m] != 1) return;
+  const int32_t id = mk.matid[m];
+  const double strain = mk.sp[m], sfi_m = mk.fric_ini[m];
+  const double ci = MATV(mt.plastic, mt.nmat, id, 1), cf = MATV(mt.plastic, mt.nmat, id, 2);
+  const double sfi_mat = MATV(mt.plastic, mt.nmat, id, 3), sff_mat = MATV(mt.plastic, mt.nmat, id, 4);
+  const double ei = MATV(mt.plastic, mt.nmat, id, 5), ef = MATV(mt.plastic, mt.nmat, id, 6);
+  // update_final_friction_angle
+  const double sff = (sfi_mat > 0.0 && sff_mat > 0.0) ? sfi_m * (sff_mat / sfi_mat) : sff_mat;
+  // strain_weakening_or_hardening
+  double coh = ci, sf = sfi_m;
+  if (strain >= ef) {
+    coh = cf;
+    sf = sff;
+  } else if (ei <= strain && strain < ef) {
+    coh = ci + (cf - ci) / (ef - ei) * (strain - ei);
+    sf = sfi_m + (sff - sfi_m) / (ef - ei) * (strain - ei);
+  }
+  if (melt_damage) {
+    sf = sf / mk.melt_damage[m];
+    coh = coh / mk.melt_damage[m];
+  }
+  mk.cohesion[m] = coh;
+  mk.fric[m] = sf;
+}
+
+struct CreepRow {
+  double A_disl, n_disl, Ea_disl, Va_disl, A_p, m_p, n_p, s_p, A_diff, Ea_diff, Va_diff;
+};
+
+// CompositeCreep.calculate_composite_creep_viscosity_and_strain_rate
+__device__ double composite_viscosity(const CreepRow& r, double p_mpa, double T, double R, double preexp,
+                                      double s_mpa, bool use_old, double& e_disl, double& a_p, double& e_diff) {
+  if (!use_old) e_disl = exp(-((r.Ea_disl * 1000.0 + r.Va_disl * p_mpa) * (1.0 / (R * T))));
+  const double rd = preexp * e_disl * ((r.n_disl == 1.0) ? s_mpa : jl_pow(s_mpa, r.n_disl));
+  double rp = 0.0;
+  if (r.A_p > 0.0 && T < 1200.0) {
+    if (!use_old) a_p = (r.Ea_disl * 1000.0 + r.Va_disl * p_mpa) * (1.0 / (R * T));
+    const double ratio = s_mpa / r.s_p;
+    const double tm = (r.m_p == 1.0) ? 1.0 - ratio : 1.0 - jl_pow(ratio, r.m_p);
+    const double inner = (r.n_p == 2.0) ? tm * tm : jl_pow(tm, r.n_p);
+    rp = r.A_p * exp(-a_p * inner) * (s_mpa * s_mpa);
+  }
+  double rf = 0.0;
+  if (r.A_diff > 0.0) {
+    if (!use_old) e_diff = exp(-((r.Ea_diff * 1000.0 + r.Va_diff * p_mpa) * (1.0 / (R * T))));
+    rf = r.A_diff * e_diff * s_mpa;
+  }
+  const double rate = ((rd > rp) ? rd : rp) + rf;
+  return 0.5 * (s_mpa * 1e6) / rate;
+}
+
+__device__ __forceinline__ double forecast_ve(double dt, double mu, double srr, double sxx, double sxy, double exx,
+                                              double exy, double smin, double eta) {
+  const double vef = eta / (mu * dt + eta);
+  const double fac1 = 2.0 * eta * srr;
+  const double om = 1.0 - vef;
+  const double nxx = fac1 * exx * om + sxx * vef;
+  const double nxy = fac1 * exy * om + sxy * vef;
+  const double s = sqrt(nxx * nxx + nxy * nxy);
+  return (s > smin) ? s : smin;
+}
+
+struct RheoParams {
+  double dt, T_top, eta_min, eta_max, s_min, R, vsoftfac;
+  int soft;
+};
+
+__global__ void k_flow_viscosity(DevMarkers mk, DevMats mt, RheoParams P) {
+  const int64_t m = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= mk.M || mk.inside[m] != 1) return;
+  const int32_t id = mk.matid[m];
+  const int32_t ft = __ldg(&mt.flow_type[id - 1]);
+  double eta = 0.0;
+  double A = MATV(mt.flow, mt.nmat, id, 2);
+  if (ft == 0) {
+    eta = MATV(mt.flow, mt.nmat, id, 1);
+  } else if (ft == 1 || ft == 2) {
+    CreepRow r;
+    r.n_disl = MATV(mt.flow, mt.nmat, id, 3); r.Ea_disl = MATV(mt.flow, mt.nmat, id, 4);
+    r.Va_disl = MATV(mt.flow, mt.nmat, id, 5); r.A_p = MATV(mt.flow, mt.nmat, id, 6);
+    r.m_p = MATV(mt.flow, mt.nmat, id, 7); r.n_p = MATV(mt.flow, mt.nmat, id, 8);
+    r.s_p = MATV(mt.flow, mt.nmat, id, 9); r.A_diff = MATV(mt.flow, mt.nmat, id, 10);
+    r.Ea_diff = MATV(mt.flow, mt.nmat, id, 11); r.Va_diff = MATV(mt.flow, mt.nmat, id, 12);
+    const double sxx = mk.sxx[m], sxy = mk.sxy[m], exx = mk.exx[m], exy = mk.exy[m];
+    const double strain = mk.gii[m];
+    const double p_mpa = mk.pr[m] * kPaToMPa;
+    const double srr = mk.sr_ratio[m];
+    const double T = fmax(mk.tk[m], P.T_top);
+    const double ei = MATV(mt.plastic, mt.nmat, id, 5), ef = MATV(mt.plastic, mt.nmat, id, 6);
+    const double mu = __ldg(&mt.mu[id - 1]);
+    if (P.soft) {  // ViscousStrainSoftening.update_pre_exponential_for_viscous_strain_softening
+      const double amin = A, amax = A * P.vsoftfac;
+      if (ei < strain && strain < ef) A = amin + (amax - amin) / (ef - ei) * (strain - ei);
+      if (strain >= ef) A = amax;
+    }
+    double s0 = sqrt(sxx * sxx + sxy * sxy);
+    if (s0 < P.s_min) s0 = P.s_min;
+    double e_disl = 0.0, a_p = 0.0, e_diff = 0.0;
+    eta = composite_viscosity(r, p_mpa, T, P.R, A, s0 * kPaToMPa, false, e_disl, a_p, e_diff);
+    double sf = forecast_ve(P.dt, mu, srr, sxx, sxy, exx, exy, P.s_min, eta);
+    double delta = 1e39;
+    int icount = 0;
+    while (icount < 20 && delta > 1.0) {
+      ++icount;
+      const double savg = (s0 + sf) / 2.0;
+      eta = composite_viscosity(r, p_mpa, T, P.R, A, savg * kPaToMPa, true, e_disl, a_p, e_diff);
+      const double sfu = forecast_ve(P.dt, mu, srr, sxx, sxy, exx, exy, P.s_min, eta);
+      if ((sf > s0 && sfu > savg) || (sf < s0 && sfu < savg)) s0 = savg;
+      else sf = savg;
+      delta = fabs(sf - s0);
+    }
+    eta = fmin(fmax(eta, P.eta_min), P.eta_max);
+  }
+  mk.eta_flow[m] = eta;
+  mk.preexp[m] = A;
+}
+
+__global__ void k_viscoplastic(DevMarkers mk, int64_t ntimestep, int64_t itype_global) {
+  const int64_t m = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= mk.M || mk.inside[m] != 1) return;
+  const double vf = mk.eta_flow[m];
+  double vp = mk.eta[m];
+  if (itype_global == 0) vp = vf;
+  else if (itype_global == 1 && (ntimestep == 0 || vp == 0.0)) vp = vf;
+  mk.eta[m] = vp;
+}
+
+struct YieldParams {
+  int64_t ntimestep;
+  double dt, y_sealevel, eta_min, eta_max, sy_min, sy_max;
+  int fluid, no_yield_mobile;
+  int32_t id_air, id_wall, id_plate;
+};
+
+__global__ void k_yield(DevMarkers mk, DevMats mt, YieldParams P) {
+  const int64_t m = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= mk.M || mk.inside[m] != 1) return;
+  const int32_t id = mk.matid[m];
+  const double coh = mk.cohesion[m], sf = mk.fric[m];
+  int yflag = 0;
+  if (P.ntimestep > 0 && (coh > 0.0 || sf > 0.0)) {
+    double eta = mk.eta[m];
+    const double mu = __ldg(&mt.mu[id - 1]);
+    double sxx = mk.sxx[m], sxy = mk.sxy[m];
+    const double exx = mk.exx[m], exy = mk.exy[m], srr = mk.sr_ratio[m], p = mk.pr[m];
+    const double cphi = cos(asin(sf));
+    double sy;
+    if (P.fluid == 0) {
+      sy = coh * cphi + sf * p;
+    } else {
+      const double depth = fmax(0.0, mk.y[m] - P.y_sealevel);
+      const double pf = 1000.0 * 9.81 * depth;
+      sy = (p < pf) ? coh * cphi : coh * cphi + sf * (p - pf);
+    }
+    sy = fmax(sy, 0.0);
+    sy = fmin(fmax(sy, P.sy_min), P.sy_max);
+    const double vef = eta / (eta + P.dt * mu);
+    const double nxx = sxx * vef + 2.0 * eta * exx * srr * (1.0 - vef);
+    const double nxy = sxy * vef + 2.0 * eta * exy * srr * (1.0 - vef);
+    const double sii = sqrt(nxx * nxx + nxy * nxy);
+    bool yielding = sii > sy;
+    if (P.no_yield_mobile && (id == P.id_air || id == P.id_wall || id == P.id_plate)) yielding = false;
+    if (yielding) {
+      yflag = 1;
+      const double s_old = sqrt(sxx * sxx + sxy * sxy);
+      if (s_old != 0.0) {
+        sxx = sxx * sy / s_old;
+        sxy = sxy * sy / s_old;
+      } else {
+        sxx = sy;
+        sxy = sy;
+      }
+      const double e_old = srr * sqrt(exx * exx + exy * exy);
+      eta = sy / 2.0 / e_old;
+      eta = fmin(fmax(eta, P.eta_min), P.eta_max);
+      mk.sxx[m] = sxx;
+      mk.sxy[m] = sxy;
+      mk.eta[m] = eta;
+    }
+  }
+  if (mk.pfailure[m] != 1.0f) mk.pfailure[m] = (float)yflag;
+}
+
+unsigned mblocks(const eb_ctx* c) { return (unsigned)((c->M + kBlock - 1) / kBlock); }
+
+int ensure(eb_ctx* c, std::initializer_list<int> fs) {
+  for (int f : fs) {
+    int rc = ensure_marker_field(c, f);
+    if (rc) return rc;
+  }
+  return EB_OK;
+}
+
+int yield_launch(eb_ctx* c) {
+  int rc = ensure(c, {EB_M_INSIDE, EB_M_MATID, EB_M_COHESION, EB_M_FRIC, EB_M_ETA, EB_M_SXX, EB_M_SXY, EB_M_EXX,
+                      EB_M_EXY, EB_M_SR_RATIO, EB_M_PR, EB_M_Y, EB_M_PFAILURE});
+  if (rc) return rc;
+  if (c->M == 0) return EB_OK;
+  const eb_params& p = c->P;
+  YieldParams Y{p.ntimestep, p.timestep, p.y_sealevel, p.viscosity_min, p.viscosity_max, p.yield_stress_min,
+                p.yield_stress_max, (int)(p.iuse_fluid_pressure_for_yield != 0), (int)(p.no_yielding_in_mobile_wall != 0),
+                (int32_t)p.matid_sticky_air, (int32_t)p.matid_mobile_wall, (int32_t)p.matid_plate_extension};
+  EB_PROF(c, "k_yield");
+  k_yield<<<mblocks(c), kBlock, 0, c->stream>>>(dev_markers(c), c->mats, Y);
+  EB_LAUNCHED(c);
+  return EB_OK;
+}
+
+}  // namespace
+
+int launch_rheology(eb_ctx* c) {
+  int rc = ensure(c, {EB_M_INSIDE, EB_M_MATID, EB_M_STRAIN_PLASTIC, EB_M_FRIC_INI, EB_M_COHESION, EB_M_FRIC,
+                      EB_M_SXX, EB_M_SXY, EB_M_EXX, EB_M_EXY, EB_M_TK, EB_M_PR, EB_M_GII, EB_M_SR_RATIO,
+                      EB_M_ETA_FLOW, EB_M_PREEXP});
+  if (rc) return rc;
+  const int melt = c->P.iuse_melt_damage == 1;
+  if (melt && (rc = ensure_marker_field(c, EB_M_MELT_DAMAGE))) return rc;
+  if (c->M == 0) return EB_OK;
+  EB_PROF(c, "k_failure");
+  k_failure<<<mblocks(c), kBlock, 0, c->stream>>>(dev_markers(c), c->mats, melt);
+  EB_LAUNCHED(c);
+  const eb_params& p = c->P;
+  RheoParams R{p.timestep, p.temperature_top, p.viscosity_min, p.viscosity_max, p.powerlaw_stress_min,
+               p.gas_constant, p.vsoftfac, (int)(p.iuse_viscous_strain_soft == 1)};
+  EB_PROF(c, "k_flow_viscosity");
+  k_flow_viscosity<<<mblocks(c), kBlock, 0, c->stream>>>(dev_markers(c), c->mats, R);
+  EB_LAUNCHED(c);
+  return EB_OK;
+}
+
+int launch_viscoplastic(eb_ctx* c, int use_marker_plasticity) {
+  int rc = ensure(c, {EB_M_INSIDE, EB_M_ETA, EB_M_ETA_FLOW});
+  if (rc) return rc;
+  if (c->M == 0) return EB_OK;
+  EB_PROF(c, "k_viscoplastic");
+  k_viscoplastic<<<mblocks(c), kBlock, 0, c->stream>>>(dev_markers(c), c->P.ntimestep, c->P.itype_global);
+  EB_LAUNCHED(c);
+  if (use_marker_plasticity) return yield_launch(c);
+  return EB_OK;
+}
+
+int launch_plastic_yielding(eb_ctx* c) { return yield_launch(c); }

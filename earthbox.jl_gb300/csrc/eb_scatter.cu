@@ -1,0 +1,745 @@
+// eb_scatter.cu -- marker -> grid bilinear averaging as a deterministic cell-sorted reduction.
+//
+// Reference (src/interpolation): BilinearDenominator.jl:34-157 (weight sums),
+// BilinearNumerator.jl:31-533 (numerators), BilinearAverage.jl:10-322 (averages),
+// BackupTransportArrays.jl:33-179 (backup + clear), FlattenDensity.jl:29-89,
+// ApplyThermalBC.jl:20-44, and the subgrid scatters
+// subgrid_stress/update/stress_change/*.jl and heat_solver/subgrid_heat/SubgridDiffusion.jl:126-195.
+//
+// The reference folds every marker into the grid serially in marker order.
+// Here each block owns 32 consecutive basic cells (column-major cell id); it
+// stages its markers' weights and values in shared memory (markers come from
+// the cell-sorted list, so they are read in cell order) and one warp per
+// "role" (a corner, a quadrant, the cell centre, a vy half-cell) folds the
+// markers of one cell per lane, in increasing marker index, with FP32
+// compensated sums.  The per-cell partial sums are then combined per node in
+// a fixed order.  The result is deterministic: it does not depend on thread
+// scheduling, and there are no floating-point atomics.
+#include "eb_internal.h"
+
+namespace {
+
+constexpr int kChunk = 256;  // markers staged per pass
+constexpr float kRad2Deg = 57.295779513082320876798f;
+
+enum { C_UL = 0, C_LL = 1, C_UR = 2, C_LR = 3 };
+
+__device__ __forceinline__ int32_t cell_id(int32_t ci, int32_t cj, int32_t ynum) {
+  return (cj - 1) * (ynum - 1) + (ci - 1);
+}
+
+// Weights of one marker from its stored FP32 normalised offsets.
+struct MW {
+  W4 b;       // basic UL, LL, UR, LR
+  float wc;   // central (pressure) node
+  W4 vy;      // vy-grid corners
+  int half;   // 0: vy cell = xn, 1: vy cell = xn + 1
+};
+__device__ __forceinline__ MW marker_weights(const DevGrid& g, int32_t ix, float fx, float fy, uint8_t fl) {
+  MW w;
+  w.b = wts(fx, fy);
+  w.wc = (1.f - fabsf(0.5f - fx)) * (1.f - fabsf(0.5f - fy));
+  w.half = (fl & MF_VYRIGHT) ? 1 : 0;
+  const float off = w.half ? __ldg(&g.vyoff_hi[ix - 1]) : __ldg(&g.vyoff_lo[ix - 1]);
+  const float dxv = (fx * __ldg(&g.sxf[ix - 1]) - off) * __ldg(&g.rsxvyf[ix - 1 + w.half]);
+  w.vy = wts(dxv, fy);
+  return w;
+}
+
+// exclusive-quadrant membership from the exact flags
+__device__ __forceinline__ bool in_quadrant(uint8_t fl, int q) {
+  const bool xl = fl & MF_XLE, xg = fl & MF_XGE, yl = fl & MF_YLE, yg = fl & MF_YGE;
+  return q == C_UL ? (xl && yl) : (q == C_LL ? (xl && yg) : (q == C_UR ? (xg && yl) : (xg && yg)));
+}
+
+// ---------------------------------------------------------------- staging ---
+// Stage layout indices (rows of the shared-memory table).
+enum { S_UL = 0, S_LL, S_UR, S_LR, S_WC, S_VUL, S_VLL, S_VUR, S_VLR, S_HALF, S_V0 };
+
+__device__ __forceinline__ void stage_weights(float (*sv)[kChunk], int t, const MW& w) {
+  sv[S_UL][t] = w.b.ul; sv[S_LL][t] = w.b.ll; sv[S_UR][t] = w.b.ur; sv[S_LR][t] = w.b.lr;
+  sv[S_WC][t] = w.wc;
+  sv[S_VUL][t] = w.vy.ul; sv[S_VLL][t] = w.vy.ll; sv[S_VUR][t] = w.vy.ur; sv[S_VLR][t] = w.vy.lr;
+  sv[S_HALF][t] = (float)w.half;
+}
+
+// ------------------------------------------------------------------ specs ---
+// Each spec defines: kRoles (warps), kNV (staged rows), kAcc (max accumulators
+// per thread), stage(), accum(), store().
+
+// Denominators: wtnodes (incl), wtetas (excl), wtetan (central), wtnodes_vy.
+// slots: 0-3 incl corners, 4-7 excl quadrants, 8 central, 9-16 vy half*4+corner
+struct DenomSpec {
+  static constexpr const char* kName = "k_cells<denominators>";
+  static constexpr int kRoles = 4, kNV = S_V0, kAcc = 8;
+  __device__ void stage(const DevMarkers& mk, const DevGrid& g, int32_t m, int t, float (*sv)[kChunk], uint8_t* sfl) const {
+    const uint8_t fl = mk.mflags[m];
+    stage_weights(sv, t, marker_weights(g, mk.xn[m], mk.fx[m], mk.fy[m], fl));
+    sfl[t] = fl;
+  }
+  __device__ void accum(int role, int t, float (*sv)[kChunk], const uint8_t* sfl, KSum* a) const {
+    if (role == 0) {
+      for (int k = 0; k < 4; ++k) a[k].add(sv[S_UL + k][t]);
+    } else if (role == 1) {
+      const uint8_t fl = sfl[t];
+      for (int q = 0; q < 4; ++q) if (in_quadrant(fl, q)) a[q].add(sv[S_UL + q][t]);
+    } else if (role == 2) {
+      a[0].add(sv[S_WC][t]);
+    } else {
+      const int h = (int)sv[S_HALF][t];
+      for (int k = 0; k < 4; ++k) a[h * 4 + k].add(sv[S_VUL + k][t]);
+    }
+  }
+  __device__ void store(int role, int32_t cell, int32_t nc, const KSum* a, float* part) const {
+    if (role == 0) for (int k = 0; k < 4; ++k) part[(size_t)k * nc + cell] = a[k].get();
+    else if (role == 1) for (int q = 0; q < 4; ++q) part[(size_t)(4 + q) * nc + cell] = a[q].get();
+    else if (role == 2) part[(size_t)8 * nc + cell] = a[0].get();
+    else for (int k = 0; k < 8; ++k) part[(size_t)(9 + k) * nc + cell] = a[k].get();
+  }
+};
+
+// Stokes numerators (BilinearNumerator.jl:205-454).
+// values: rho, coh, fric_deg, eta_flow, eta, mu_inv, sxy, plast, dil, melt, sxx
+enum { V_RHO = S_V0, V_COH, V_FRIC, V_ETAF, V_ETA, V_MUI, V_SXY, V_PLAST, V_DIL, V_MELT, V_SXX, V_END };
+// slots: 0-3 incl rho; 4 + 7*q + f excl (f: coh, fric, eta_flow, eta, mu_inv, sxy, plast);
+//        32-37 central (eta, mu_inv, plast, dil, melt, sxx); 38-45 vy rho half*4+corner
+struct StokesSpec {
+  static constexpr const char* kName = "k_cells<stokes>";
+  static constexpr int kRoles = 7, kNV = V_END, kAcc = 8;
+  const double* mat_mu;
+  int32_t* dflag;
+  __device__ void stage(const DevMarkers& mk, const DevGrid& g, int32_t m, int t, float (*sv)[kChunk], uint8_t* sfl) const {
+    const uint8_t fl = mk.mflags[m];
+    stage_weights(sv, t, marker_weights(g, mk.xn[m], mk.fx[m], mk.fy[m], fl));
+    sfl[t] = fl;
+    const int32_t mt = mk.matid[m];
+    const double mu = __ldg(&mat_mu[mt - 1]);
+    if ((__double_as_longlong(mu) << 1) == 0) atomicOr(dflag, 2);  // reference raises on a zero shear modulus
+    sv[V_RHO][t] = (float)mk.rho[m];
+    sv[V_COH][t] = (float)mk.cohesion[m];
+    sv[V_FRIC][t] = asinf((float)mk.fric[m]) * kRad2Deg;
+    sv[V_ETAF][t] = (float)mk.eta_flow[m];
+    sv[V_ETA][t] = (float)mk.eta[m];
+    sv[V_MUI][t] = 1.f / (float)mu;
+    sv[V_SXY][t] = (float)mk.sxy[m];
+    sv[V_PLAST][t] = mk.pfailure[m];
+    sv[V_DIL][t] = mk.dilat[m];
+    sv[V_MELT][t] = (float)mk.melt[m];
+    sv[V_SXX][t] = (float)mk.sxx[m];
+  }
+  __device__ void accum(int role, int t, float (*sv)[kChunk], const uint8_t* sfl, KSum* a) const {
+    if (role == 0) {
+      const float r = sv[V_RHO][t];
+      for (int k = 0; k < 4; ++k) a[k].add(sv[S_UL + k][t] * r);
+    } else if (role <= 4) {
+      const int q = role - 1;
+      if (!in_quadrant(sfl[t], q)) return;
+      const float w = sv[S_UL + q][t];
+      a[0].add(w * sv[V_COH][t]);
+      a[1].add(w * sv[V_FRIC][t]);
+      a[2].add(w * sv[V_ETAF][t]);
+      a[3].add(w * sv[V_ETA][t]);
+      a[4].add(w * sv[V_MUI][t]);
+      a[5].add(w * sv[V_SXY][t]);
+      a[6].add(w * sv[V_PLAST][t]);
+    } else if (role == 5) {
+      const float w = sv[S_WC][t];
+      a[0].add(w * sv[V_ETA][t]);
+      a[1].add(w * sv[V_MUI][t]);
+      a[2].add(w * sv[V_PLAST][t]);
+      a[3].add(w * sv[V_DIL][t]);
+      a[4].add(w * sv[V_MELT][t]);
+      a[5].add(w * sv[V_SXX][t]);
+    } else {
+      const int h = (int)sv[S_HALF][t];
+      const float r = sv[V_RHO][t];
+      for (int k = 0; k < 4; ++k) a[h * 4 + k].add(sv[S_VUL + k][t] * r);
+    }
+  }
+  __device__ void store(int role, int32_t cell, int32_t nc, const KSum* a, float* part) const {
+    if (role == 0) for (int k = 0; k < 4; ++k) part[(size_t)k * nc + cell] = a[k].get();
+    else if (role <= 4) for (int f = 0; f < 7; ++f) part[(size_t)(4 + 7 * (role - 1) + f) * nc + cell] = a[f].get();
+    else if (role == 5) for (int f = 0; f < 6; ++f) part[(size_t)(32 + f) * nc + cell] = a[f].get();
+    else for (int k = 0; k < 8; ++k) part[(size_t)(38 + k) * nc + cell] = a[k].get();
+  }
+};
+
+// Heat numerators (BilinearNumerator.jl:31-141): tk, kt, rhocp, hr(+serp), ha; slots 5*corner + f
+struct HeatSpec {
+  static constexpr const char* kName = "k_cells<heat>";
+  static constexpr int kRoles = 4, kNV = S_V0 + 5, kAcc = 5;
+  const double* mat_hr;
+  int use_serp;
+  __device__ void stage(const DevMarkers& mk, const DevGrid& g, int32_t m, int t, float (*sv)[kChunk], uint8_t* sfl) const {
+    const uint8_t fl = mk.mflags[m];
+    const W4 w = wts(mk.fx[m], mk.fy[m]);
+    sv[S_UL][t] = w.ul; sv[S_LL][t] = w.ll; sv[S_UR][t] = w.ur; sv[S_LR][t] = w.lr;
+    sfl[t] = fl;
+    double hr = __ldg(&mat_hr[mk.matid[m] - 1]);
+    if (use_serp) hr = hr + mk.serp_hr[m];
+    sv[S_V0 + 0][t] = (float)mk.tk[m];
+    sv[S_V0 + 1][t] = (float)mk.kt[m];
+    sv[S_V0 + 2][t] = (float)mk.rhocp[m];
+    sv[S_V0 + 3][t] = (float)hr;
+    sv[S_V0 + 4][t] = (float)mk.ha[m];
+  }
+  __device__ void accum(int role, int t, float (*sv)[kChunk], const uint8_t*, KSum* a) const {
+    const float w = sv[S_UL + role][t];
+    for (int f = 0; f < 5; ++f) a[f].add(w * sv[S_V0 + f][t]);
+  }
+  __device__ void store(int role, int32_t cell, int32_t nc, const KSum* a, float* part) const {
+    for (int f = 0; f < 5; ++f) part[(size_t)(5 * role + f) * nc + cell] = a[f].get();
+  }
+};
+
+// Viscosity re-scatter (BilinearNumerator.jl:470-533): slots 0-3 excl eta, 4 central eta
+struct ViscSpec {
+  static constexpr const char* kName = "k_cells<viscosity>";
+  static constexpr int kRoles = 2, kNV = S_V0 + 1, kAcc = 4;
+  __device__ void stage(const DevMarkers& mk, const DevGrid& g, int32_t m, int t, float (*sv)[kChunk], uint8_t* sfl) const {
+    const uint8_t fl = mk.mflags[m];
+    const float fx = mk.fx[m], fy = mk.fy[m];
+    const W4 w = wts(fx, fy);
+    sv[S_UL][t] = w.ul; sv[S_LL][t] = w.ll; sv[S_UR][t] = w.ur; sv[S_LR][t] = w.lr;
+    sv[S_WC][t] = (1.f - fabsf(0.5f - fx)) * (1.f - fabsf(0.5f - fy));
+    sfl[t] = fl;
+    sv[S_V0][t] = (float)mk.eta[m];
+  }
+  __device__ void accum(int role, int t, float (*sv)[kChunk], const uint8_t* sfl, KSum* a) const {
+    const float e = sv[S_V0][t];
+    if (role == 0) {
+      const uint8_t fl = sfl[t];
+      for (int q = 0; q < 4; ++q) if (in_quadrant(fl, q)) a[q].add(sv[S_UL + q][t] * e);
+    } else {
+      a[0].add(sv[S_WC][t] * e);
+    }
+  }
+  __device__ void store(int role, int32_t cell, int32_t nc, const KSum* a, float* part) const {
+    if (role == 0) for (int q = 0; q < 4; ++q) part[(size_t)q * nc + cell] = a[q].get();
+    else part[(size_t)4 * nc + cell] = a[0].get();
+  }
+};
+
+// Pressure-grid bilinear gather of one marker (GridToMarker.jl:104-153 with
+// MarkerGridMapping.upr_left_index_pressure / upr_left_dist_pressure, :311-350).
+__device__ __forceinline__ float gather_pressure_grid(const double* __restrict__ pg, const DevGrid& g, int32_t ix,
+                                                      int32_t iy, float fx, float fy) {
+  const float lx = fx * __ldg(&g.sxf[ix - 1]);
+  const float ly = fy * __ldg(&g.syf[iy - 1]);
+  const float hx = __ldg(&g.vyoff_hi[ix - 1]), hy = __ldg(&g.vxoff_hi[iy - 1]);
+  int32_t xp = (lx < hx) ? ix - 1 : ix;
+  int32_t yp = (ly < hy) ? iy - 1 : iy;
+  xp = clamp_i(xp, 1, g.xnum - 2);
+  yp = clamp_i(yp, 1, g.ynum - 2);
+  // staggered node xp+1 lies at offset vyoff_lo (== ix) or vyoff_hi (== ix+1) from gx[ix]
+  const float ox = (xp + 1 == ix) ? __ldg(&g.vyoff_lo[ix - 1]) : hx;
+  const float oy = (yp + 1 == iy) ? __ldg(&g.vxoff_lo[iy - 1]) : hy;
+  const float dxp = (lx - ox) * __ldg(&g.rsxvyf[xp]);
+  const float dyp = (ly - oy) * __ldg(&g.rsyvxf[yp]);
+  return gather4(pg, g.ynum - 1, yp, xp, dxp, dyp);
+}
+
+// Subgrid stress (SubgridShearStress.jl:27-96, SubgridNormalStress.jl:27-89):
+// the staging pass relaxes the marker stress and stages the relaxed change.
+// slots: 0-3 excl relax_xy*w, 4-7 excl w, 8 central relax_xx*wc, 9 central wc
+struct SubgridStressSpec {
+  static constexpr const char* kName = "k_cells<subgrid_stress>";
+  static constexpr int kRoles = 2, kNV = S_V0 + 2, kAcc = 8;
+  const double *sxy1, *sxx1, *mat_mu;
+  float dt, coef;
+  __device__ void stage(const DevMarkers& mk, const DevGrid& g, int32_t m, int t, float (*sv)[kChunk], uint8_t* sfl) const {
+    const uint8_t fl = mk.mflags[m];
+    const int32_t ix = mk.xn[m], iy = mk.yn[m];
+    const float fx = mk.fx[m], fy = mk.fy[m];
+    const W4 w = wts(fx, fy);
+    sv[S_UL][t] = w.ul; sv[S_LL][t] = w.ll; sv[S_UR][t] = w.ur; sv[S_LR][t] = w.lr;
+    sv[S_WC][t] = (1.f - fabsf(0.5f - fx)) * (1.f - fabsf(0.5f - fy));
+    sfl[t] = fl;
+    // DiffusionTerm.calculate_subgrid_stress_diffusion_term (DiffusionTerm.jl:14-29)
+    const float mu = (float)__ldg(&mat_mu[mk.matid[m] - 1]);
+    const float maxwell = (float)mk.eta[m] / mu;
+    const float sdif = fmaxf(-coef * dt / maxwell, -30.f);
+    const float term = -expm1f(sdif);  // 1 - exp(sdif), accurate for small |sdif|
+    const float sxy_g = gather4(sxy1, g.ynum, iy, ix, fx, fy);
+    const double sxy_m = mk.sxy[m];
+    const float rxy = (sxy_g - (float)sxy_m) * term;
+    mk.sxy[m] = sxy_m + (double)rxy;
+    const float sxx_g = gather_pressure_grid(sxx1, g, ix, iy, fx, fy);
+    const double sxx_m = mk.sxx[m];
+    const float rxx = (sxx_g - (float)sxx_m) * term;
+    mk.sxx[m] = sxx_m + (double)rxx;
+    sv[S_V0][t] = rxy;
+    sv[S_V0 + 1][t] = rxx;
+  }
+  __device__ void accum(int role, int t, float (*sv)[kChunk], const uint8_t* sfl, KSum* a) const {
+    if (role == 0) {
+      const uint8_t fl = sfl[t];
+      const float r = sv[S_V0][t];
+      for (int q = 0; q < 4; ++q)
+        if (in_quadrant(fl, q)) {
+          const float w = sv[S_UL + q][t];
+          a[q].add(w * r);
+          a[4 + q].add(w);
+        }
+    } else {
+      const float w = sv[S_WC][t];
+      a[0].add(w * sv[S_V0 + 1][t]);
+      a[1].add(w);
+    }
+  }
+  __device__ void store(int role, int32_t cell, int32_t nc, const KSum* a, float* part) const {
+    if (role == 0) for (int k = 0; k < 8; ++k) part[(size_t)k * nc + cell] = a[k].get();
+    else { part[(size_t)8 * nc + cell] = a[0].get(); part[(size_t)9 * nc + cell] = a[1].get(); }
+  }
+};
+
+// Subgrid heat diffusion (SubgridDiffusion.jl:67-175): slots 0-3 dT*w, 4-7 w
+struct SubgridHeatSpec {
+  static constexpr const char* kName = "k_cells<subgrid_heat>";
+  static constexpr int kRoles = 1, kNV = S_V0 + 1, kAcc = 8;
+  const double *tk1, *kt1, *rhocp1;
+  float dt, coef, inv_ts;  // inv_ts = 2/xstpavg^2 + 2/ystpavg^2
+  __device__ void stage(const DevMarkers& mk, const DevGrid& g, int32_t m, int t, float (*sv)[kChunk], uint8_t* sfl) const {
+    const int32_t ix = mk.xn[m], iy = mk.yn[m];
+    const float fx = mk.fx[m], fy = mk.fy[m];
+    const W4 w = wts(fx, fy);
+    sv[S_UL][t] = w.ul; sv[S_LL][t] = w.ll; sv[S_UR][t] = w.ur; sv[S_LR][t] = w.lr;
+    sfl[t] = mk.mflags[m];
+    const float tn = gather4(tk1, g.ynum, iy, ix, fx, fy);
+    const double tm = mk.tk[m];
+    const float k = gather4(kt1, g.ynum, iy, ix, fx, fy);
+    const float rc = gather4(rhocp1, g.ynum, iy, ix, fx, fy);
+    const float tsg = rc / k / inv_ts;
+    const float term = fmaxf(-coef * dt / tsg, -30.f);
+    const float d = (tn - (float)tm) * (-expm1f(term));
+    mk.subgrid_dt[m] = (double)d;
+    mk.tk[m] = tm + (double)d;
+    sv[S_V0][t] = d;
+  }
+  __device__ void accum(int, int t, float (*sv)[kChunk], const uint8_t*, KSum* a) const {
+    const float d = sv[S_V0][t];
+    for (int k = 0; k < 4; ++k) {
+      const float w = sv[S_UL + k][t];
+      a[k].add(w * d);
+      a[4 + k].add(w);
+    }
+  }
+  __device__ void store(int, int32_t cell, int32_t nc, const KSum* a, float* part) const {
+    for (int k = 0; k < 8; ++k) part[(size_t)k * nc + cell] = a[k].get();
+  }
+};
+
+// ------------------------------------------------------- per-cell kernel ---
+template <class S>
+__global__ void __launch_bounds__(32 * S::kRoles) k_cells(S spec, DevMarkers mk, DevGrid g,
+                                                          const int32_t* __restrict__ start,
+                                                          const int32_t* __restrict__ perm, int32_t nc,
+                                                          float* __restrict__ part) {
+  __shared__ float sv[S::kNV][kChunk];
+  __shared__ uint8_t sfl[kChunk];
+  const int lane = threadIdx.x & 31, role = threadIdx.x >> 5;
+  const int32_t c0 = blockIdx.x * 32;
+  const int32_t c1 = min(c0 + 32, nc);
+  const int32_t P0 = start[c0], P1 = start[c1];
+  const int32_t my = c0 + lane;
+  const int32_t beg = my < nc ? start[my] : P1, end = my < nc ? start[my + 1] : P1;
+  KSum acc[S::kAcc];
+#pragma unroll
+  for (int k = 0; k < S::kAcc; ++k) acc[k].init();
+  for (int32_t k0 = P0; k0 < P1; k0 += kChunk) {
+    const int32_t kn = min(kChunk, P1 - k0);
+    __syncthreads();
+    for (int t = threadIdx.x; t < kn; t += blockDim.x) spec.stage(mk, g, __ldg(&perm[k0 + t]), t, sv, sfl);
+    __syncthreads();
+    const int32_t kb = max(beg, k0), ke = min(end, k0 + kn);
+    for (int32_t k = kb; k < ke; ++k) spec.accum(role, k - k0, sv, sfl, acc);
+  }
+  if (my < nc) spec.store(role, my, nc, acc, part);
+}
+
+template <class S>
+int run_cells(eb_ctx* c, const S& spec) {
+  const int32_t nc = c->cs.ncells;
+  const unsigned blocks = (unsigned)((nc + 31) / 32);
+  EB_PROF(c, S::kName);
+  k_cells<S><<<blocks, 32 * S::kRoles, 0, c->stream>>>(spec, dev_markers(c), c->g, c->cs.start, c->cs.perm, nc, c->part);
+  EB_LAUNCHED(c);
+  return EB_OK;
+}
+
+// ---------------------------------------------------- node combination ---
+struct NodeCtx {
+  const float* part;
+  int32_t nc, ynum, xnum;
+  __device__ float p(int slot, int32_t ci, int32_t cj) const {
+    return part[(size_t)slot * nc + cell_id(ci, cj, ynum)];
+  }
+  // Sum over the cells around basic node (i, j): LR of (i-1, j-1), UR of (i, j-1),
+  // LL of (i-1, j), UL of (i, j).  slot(k) = base + stride * k.
+  __device__ float basic(int32_t i, int32_t j, int base, int stride) const {
+    KSum s; s.init();
+    if (i > 1 && j > 1) s.add(p(base + stride * C_LR, i - 1, j - 1));
+    if (i < ynum && j > 1) s.add(p(base + stride * C_UR, i, j - 1));
+    if (i > 1 && j < xnum) s.add(p(base + stride * C_LL, i - 1, j));
+    if (i < ynum && j < xnum) s.add(p(base + stride * C_UL, i, j));
+    return s.get();
+  }
+  // vy node (i, jv): vy cells (ci, cjv) are the left half of basic cell (ci, cjv)
+  // plus the right half of basic cell (ci, cjv-1).  slot = base + half*4 + corner.
+  __device__ void vycell(KSum& s, int32_t ci, int32_t cjv, int k, int base) const {
+    if (ci < 1 || ci > ynum - 1 || cjv < 1 || cjv > xnum) return;
+    if (cjv <= xnum - 1) s.add(p(base + k, ci, cjv));
+    if (cjv >= 2) s.add(p(base + 4 + k, ci, cjv - 1));
+  }
+  __device__ float vy(int32_t i, int32_t jv, int base) const {
+    KSum s; s.init();
+    vycell(s, i - 1, jv - 1, C_LR, base);
+    vycell(s, i, jv - 1, C_UR, base);
+    vycell(s, i - 1, jv, C_LL, base);
+    vycell(s, i, jv, C_UL, base);
+    return s.get();
+  }
+};
+
+__global__ void k_finish_denoms(NodeCtx n, double* wtnodes, double* wtetas, double* wtetan, double* wtnodes_vy) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t nb = (int64_t)n.ynum * n.xnum, np = (int64_t)(n.ynum - 1) * (n.xnum - 1),
+                nv = (int64_t)n.ynum * (n.xnum + 1);
+  if (t < nb) {
+    const int32_t i = (int32_t)(t % n.ynum) + 1, j = (int32_t)(t / n.ynum) + 1;
+    wtnodes[t] = (double)n.basic(i, j, 0, 1);
+    wtetas[t] = (double)n.basic(i, j, 4, 1);
+  }
+  if (t < np) wtetan[t] = (double)n.part[(size_t)8 * n.nc + t];
+  if (t < nv) {
+    const int32_t i = (int32_t)(t % n.ynum) + 1, jv = (int32_t)(t / n.ynum) + 1;
+    wtnodes_vy[t] = (double)n.vy(i, jv, 9);
+  }
+}
+
+// average with backup: den != 0 -> num/den, else the backup value
+__device__ __forceinline__ double avg_or(float num, double den, double backup) {
+  return den != 0.0 ? (double)(num / (float)den) : backup;
+}
+__device__ __forceinline__ double harm_or(float num, double den, double backup) {
+  return den != 0.0 ? (double)((float)den / num) : backup;
+}
+
+struct StokesGrids {
+  double *rho1, *rho0, *etas1, *etas0, *eta_flow, *eta_flow0, *mus1, *mus0, *sxy1, *sxy0;
+  double *plastics, *plastics0, *coh, *coh0, *fric, *fric0;
+  double *etan1, *etan0, *mun1, *mun0, *sxx1, *sxx0, *plasticn, *plasticn0, *dil, *dil0, *melt, *melt0;
+  double *rho1_vy, *rho0_vy;
+  const double *wtnodes, *wtetas, *wtetan, *wtnodes_vy, *hr1, *gy;
+  int iuse_topo;
+  double y_sealevel, rho_air, rho_water;
+};
+
+__global__ void k_finish_stokes(NodeCtx n, StokesGrids G) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t nb = (int64_t)n.ynum * n.xnum, np = (int64_t)(n.ynum - 1) * (n.xnum - 1),
+                nv = (int64_t)n.ynum * (n.xnum + 1);
+  if (t < nb) {
+    const int32_t i = (int32_t)(t % n.ynum) + 1, j = (int32_t)(t / n.ynum) + 1;
+    const double dn = G.wtnodes[t], ds = G.wtetas[t];
+    // backups (BackupTransportArrays.backup_stokes_transport_arrays!)
+    const double o_rho = G.rho1[t], o_etas = G.etas1[t], o_etaf = G.eta_flow[t], o_mus = G.mus1[t],
+                 o_sxy = G.sxy1[t], o_pl = G.plastics[t], o_coh = G.coh[t], o_fr = G.fric[t];
+    G.rho0[t] = o_rho; G.etas0[t] = o_etas; G.eta_flow0[t] = o_etaf; G.mus0[t] = o_mus;
+    G.sxy0[t] = o_sxy; G.plastics0[t] = o_pl; G.coh0[t] = o_coh; G.fric0[t] = o_fr;
+    double rho = avg_or(n.basic(i, j, 0, 1), dn, o_rho);
+    // FlattenDensity.flatten_staggered_grid_density_in_sticky_air_layer! (FlattenDensity.jl:48-66)
+    if (G.iuse_topo == 1 && G.hr1[t] == 0.0 && rho <= 1100.0) {
+      const bool above = G.gy[i - 1] < G.y_sealevel;
+      if (above && G.rho_air >= 0.0) rho = G.rho_air;
+      else if (!above && G.rho_water >= 0.0) rho = G.rho_water;
+    }
+    G.rho1[t] = rho;
+    G.coh[t] = avg_or(n.basic(i, j, 4 + 0, 7), ds, o_coh);
+    G.fric[t] = avg_or(n.basic(i, j, 4 + 1, 7), ds, o_fr);
+    G.eta_flow[t] = avg_or(n.basic(i, j, 4 + 2, 7), ds, o_etaf);
+    G.etas1[t] = avg_or(n.basic(i, j, 4 + 3, 7), ds, o_etas);
+    G.mus1[t] = harm_or(n.basic(i, j, 4 + 4, 7), ds, o_mus);
+    G.sxy1[t] = avg_or(n.basic(i, j, 4 + 5, 7), ds, o_sxy);
+    G.plastics[t] = avg_or(n.basic(i, j, 4 + 6, 7), ds, o_pl);
+  }
+  if (t < np) {
+    const double dc = G.wtetan[t];
+    const double o_etan = G.etan1[t], o_mun = G.mun1[t], o_pl = G.plasticn[t], o_dil = G.dil[t],
+                 o_melt = G.melt[t], o_sxx = G.sxx1[t];
+    G.etan0[t] = o_etan; G.mun0[t] = o_mun; G.plasticn0[t] = o_pl; G.dil0[t] = o_dil;
+    G.melt0[t] = o_melt; G.sxx0[t] = o_sxx;
+    const float* P = n.part;
+    const size_t nc = n.nc;
+    G.etan1[t] = avg_or(P[32 * nc + t], dc, o_etan);
+    G.mun1[t] = harm_or(P[33 * nc + t], dc, o_mun);
+    G.plasticn[t] = avg_or(P[34 * nc + t], dc, o_pl);
+    G.dil[t] = avg_or(P[35 * nc + t], dc, o_dil);
+    G.melt[t] = avg_or(P[36 * nc + t], dc, o_melt);
+    G.sxx1[t] = avg_or(P[37 * nc + t], dc, o_sxx);
+  }
+  if (t < nv) {
+    const int32_t i = (int32_t)(t % n.ynum) + 1, jv = (int32_t)(t / n.ynum) + 1;
+    const double o = G.rho1_vy[t];
+    G.rho0_vy[t] = o;
+    double rho = avg_or(n.vy(i, jv, 38), G.wtnodes_vy[t], o);
+    if (G.iuse_topo == 1 && rho <= 1100.0) {
+      const bool above = G.gy[i - 1] < G.y_sealevel;
+      if (above && G.rho_air >= 0.0) rho = G.rho_air;
+      else if (!above && G.rho_water >= 0.0) rho = G.rho_water;
+    }
+    G.rho1_vy[t] = rho;
+  }
+}
+
+struct HeatGrids {
+  double *tk1, *tk0, *kt1, *kt0, *rhocp1, *rhocp0, *hr1, *hr0, *ha1, *ha0;
+  const double *tk2, *wtnodes;
+};
+__global__ void k_finish_heat(NodeCtx n, HeatGrids G) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (int64_t)n.ynum * n.xnum) return;
+  const int32_t i = (int32_t)(t % n.ynum) + 1, j = (int32_t)(t / n.ynum) + 1;
+  const double dn = G.wtnodes[t];
+  const double b_tk = G.tk2[t], b_kt = G.kt1[t], b_rc = G.rhocp1[t], b_hr = G.hr1[t], b_ha = G.ha1[t];
+  G.tk0[t] = b_tk; G.kt0[t] = b_kt; G.rhocp0[t] = b_rc; G.hr0[t] = b_hr; G.ha0[t] = b_ha;
+  G.tk1[t] = avg_or(n.basic(i, j, 0, 5), dn, b_tk);
+  G.kt1[t] = avg_or(n.basic(i, j, 1, 5), dn, b_kt);
+  G.rhocp1[t] = avg_or(n.basic(i, j, 2, 5), dn, b_rc);
+  G.hr1[t] = avg_or(n.basic(i, j, 3, 5), dn, b_hr);
+  G.ha1[t] = avg_or(n.basic(i, j, 4, 5), dn, b_ha);
+}
+
+// ApplyThermalBC.apply_thermal_bc_along_boundaries! (ApplyThermalBC.jl:20-44): top/bottom rows
+// for j in 2:xnum-1, then left/right columns for every i (the column pass runs second).
+__global__ void k_thermal_bc_rows(double* tk1, const double* btop, const double* bbot, int32_t ynum, int32_t xnum) {
+  const int32_t j = blockIdx.x * blockDim.x + threadIdx.x + 2;
+  if (j > xnum - 1) return;
+  const size_t col = (size_t)(j - 1) * ynum;
+  tk1[col] = btop[j - 1] + btop[xnum + j - 1] * tk1[col + 1];
+  tk1[col + ynum - 1] = bbot[j - 1] + bbot[xnum + j - 1] * tk1[col + ynum - 2];
+}
+__global__ void k_thermal_bc_cols(double* tk1, const double* bl, const double* br, int32_t ynum, int32_t xnum) {
+  const int32_t i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  if (i > ynum) return;
+  tk1[i - 1] = bl[i - 1] + bl[ynum + i - 1] * tk1[(size_t)ynum + i - 1];
+  tk1[(size_t)(xnum - 1) * ynum + i - 1] = br[i - 1] + br[ynum + i - 1] * tk1[(size_t)(xnum - 2) * ynum + i - 1];
+}
+
+__global__ void k_finish_visc(NodeCtx n, double* etas1, const double* etas0, double* etan1, const double* etan0,
+                              const double* wtetas, const double* wtetan) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < (int64_t)n.ynum * n.xnum) {
+    const int32_t i = (int32_t)(t % n.ynum) + 1, j = (int32_t)(t / n.ynum) + 1;
+    etas1[t] = avg_or(n.basic(i, j, 0, 1), wtetas[t], etas0[t]);
+  }
+  if (t < (int64_t)(n.ynum - 1) * (n.xnum - 1)) etan1[t] = avg_or(n.part[(size_t)4 * n.nc + t], wtetan[t], etan0[t]);
+}
+
+// BilinearAverage.calc_marker_average_subgrid_stress_change! + RemainingStress (Update.jl:69-87)
+__global__ void k_finish_subgrid_stress(NodeCtx n, double* dsxyn, double* dsxxn, double* wtetas, double* wtetan,
+                                        double* dsxy, double* dsxx) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < (int64_t)n.ynum * n.xnum) {
+    const int32_t i = (int32_t)(t % n.ynum) + 1, j = (int32_t)(t / n.ynum) + 1;
+    const float num = n.basic(i, j, 0, 1), den = n.basic(i, j, 4, 1);
+    const double v = den != 0.f ? (double)(num / den) : (double)num;
+    dsxyn[t] = v;
+    wtetas[t] = (double)den;
+    dsxy[t] = dsxy[t] - v;
+  }
+  if (t < (int64_t)(n.ynum - 1) * (n.xnum - 1)) {
+    const float num = n.part[(size_t)8 * n.nc + t], den = n.part[(size_t)9 * n.nc + t];
+    const double v = den != 0.f ? (double)(num / den) : (double)num;
+    dsxxn[t] = v;
+    wtetan[t] = (double)den;
+    dsxx[t] = dsxx[t] - v;
+  }
+}
+
+// SubgridDiffusion.interpolate_subgrid_temperature_change_to_grid! + remove_subgrid_effects_from_grid_changes!
+__global__ void k_finish_subgrid_heat(NodeCtx n, double* dtkn, double* wtnodes, double* dtk1) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (int64_t)n.ynum * n.xnum) return;
+  const int32_t i = (int32_t)(t % n.ynum) + 1, j = (int32_t)(t / n.ynum) + 1;
+  const float num = n.basic(i, j, 0, 1), den = n.basic(i, j, 4, 1);
+  const double v = den != 0.f ? (double)(num / den) : (double)num;
+  dtkn[t] = v;
+  wtnodes[t] = (double)den;
+  dtk1[t] = dtk1[t] - v;
+}
+
+NodeCtx node_ctx(eb_ctx* c) { return NodeCtx{c->part, c->cs.ncells, c->ynum, c->xnum}; }
+unsigned node_blocks(eb_ctx* c, int64_t n) { return (unsigned)((n + 255) / 256); }
+
+int ensure_grids(eb_ctx* c, std::initializer_list<int> fields) {
+  for (int f : fields) {
+    int rc = ensure_grid_field(c, f);
+    if (rc) return rc;
+  }
+  return EB_OK;
+}
+int ensure_markers(eb_ctx* c, std::initializer_list<int> fields) {
+  for (int f : fields) {
+    int rc = ensure_marker_field(c, f);
+    if (rc) return rc;
+  }
+  return EB_OK;
+}
+
+}  // namespace
+
+int launch_denominators(eb_ctx* c) {
+  if (c->M > 0) {
+    int rc = run_cells(c, DenomSpec{});
+    if (rc) return rc;
+  } else {
+    EB_CK(c, cudaMemsetAsync(c->part, 0, (size_t)kMaxSlots * c->cs.ncells * sizeof(float), c->stream));
+  }
+  const int64_t n = (int64_t)c->ynum * (c->xnum + 1);
+  EB_PROF(c, "k_finish_denoms");
+  k_finish_denoms<<<node_blocks(c, n), 256, 0, c->stream>>>(node_ctx(c), c->gf[EB_G_WTNODES], c->gf[EB_G_WTETAS],
+                                                            c->gf[EB_G_WTETAN], c->gf[EB_G_WTNODES_VY]);
+  EB_LAUNCHED(c);
+  return EB_OK;
+}
+
+int launch_scatter_stokes(eb_ctx* c) {
+  int rc = ensure_markers(c, {EB_M_MATID, EB_M_RHO, EB_M_COHESION, EB_M_FRIC, EB_M_ETA_FLOW, EB_M_ETA, EB_M_SXY,
+                              EB_M_SXX, EB_M_PFAILURE, EB_M_DILATATION, EB_M_MELTFRAC});
+  if (rc) return rc;
+  rc = ensure_grids(c, {EB_G_RHO1, EB_G_RHO0, EB_G_ETAS1, EB_G_ETAS0, EB_G_ETA_FLOW, EB_G_ETA_FLOW0, EB_G_MUS1,
+                        EB_G_MUS0, EB_G_SXY1, EB_G_SXY0, EB_G_PLASTICS, EB_G_PLASTICS0, EB_G_COHESION,
+                        EB_G_COHESION0, EB_G_FRIC_DEG, EB_G_FRIC_DEG0, EB_G_ETAN1, EB_G_ETAN0, EB_G_MUN1, EB_G_MUN0,
+                        EB_G_SXX1, EB_G_SXX0, EB_G_PLASTICN, EB_G_PLASTICN0, EB_G_DILAT, EB_G_DILAT0, EB_G_MELTFRAC,
+                        EB_G_MELTFRAC0, EB_G_RHO1_VY, EB_G_RHO0_VY, EB_G_HR1});
+  if (rc) return rc;
+  EB_CK(c, cudaMemsetAsync(c->dflag, 0, sizeof(int32_t), c->stream));
+  if (c->M > 0) {
+    rc = run_cells(c, StokesSpec{c->mats.mu, c->dflag});
+    if (rc) return rc;
+  } else {
+    EB_CK(c, cudaMemsetAsync(c->part, 0, (size_t)kMaxSlots * c->cs.ncells * sizeof(float), c->stream));
+  }
+  StokesGrids G{};
+  double** gf = c->gf;
+  G.rho1 = gf[EB_G_RHO1]; G.rho0 = gf[EB_G_RHO0]; G.etas1 = gf[EB_G_ETAS1]; G.etas0 = gf[EB_G_ETAS0];
+  G.eta_flow = gf[EB_G_ETA_FLOW]; G.eta_flow0 = gf[EB_G_ETA_FLOW0]; G.mus1 = gf[EB_G_MUS1]; G.mus0 = gf[EB_G_MUS0];
+  G.sxy1 = gf[EB_G_SXY1]; G.sxy0 = gf[EB_G_SXY0]; G.plastics = gf[EB_G_PLASTICS]; G.plastics0 = gf[EB_G_PLASTICS0];
+  G.coh = gf[EB_G_COHESION]; G.coh0 = gf[EB_G_COHESION0]; G.fric = gf[EB_G_FRIC_DEG]; G.fric0 = gf[EB_G_FRIC_DEG0];
+  G.etan1 = gf[EB_G_ETAN1]; G.etan0 = gf[EB_G_ETAN0]; G.mun1 = gf[EB_G_MUN1]; G.mun0 = gf[EB_G_MUN0];
+  G.sxx1 = gf[EB_G_SXX1]; G.sxx0 = gf[EB_G_SXX0]; G.plasticn = gf[EB_G_PLASTICN]; G.plasticn0 = gf[EB_G_PLASTICN0];
+  G.dil = gf[EB_G_DILAT]; G.dil0 = gf[EB_G_DILAT0]; G.melt = gf[EB_G_MELTFRAC]; G.melt0 = gf[EB_G_MELTFRAC0];
+  G.rho1_vy = gf[EB_G_RHO1_VY]; G.rho0_vy = gf[EB_G_RHO0_VY];
+  G.wtnodes = gf[EB_G_WTNODES]; G.wtetas = gf[EB_G_WTETAS]; G.wtetan = gf[EB_G_WTETAN]; G.wtnodes_vy = gf[EB_G_WTNODES_VY];
+  G.hr1 = gf[EB_G_HR1]; G.gy = c->g.gy;
+  G.iuse_topo = (int)c->P.iuse_topo;
+  G.y_sealevel = c->P.y_sealevel;
+  auto mrho = [&](int64_t id) -> double {
+    if (id < 1 || id > (int64_t)c->h_mat_rho.size()) return -1.0;
+    return c->h_mat_rho[id - 1];
+  };
+  G.rho_air = c->P.iuse_topo == 1 ? mrho(c->P.matid_sticky_air_rho) : -1.0;
+  G.rho_water = c->P.iuse_topo == 1 ? mrho(c->P.matid_sticky_water_rho) : -1.0;
+  const int64_t n = (int64_t)c->ynum * (c->xnum + 1);
+  EB_PROF(c, "k_finish_stokes");
+  k_finish_stokes<<<node_blocks(c, n), 256, 0, c->stream>>>(node_ctx(c), G);
+  EB_LAUNCHED(c);
+  int32_t flag = 0;
+  EB_CK(c, cudaMemcpyAsync(&flag, c->dflag, sizeof(int32_t), cudaMemcpyDeviceToHost, c->stream));
+  EB_CK(c, cudaStreamSynchronize(c->stream));
+  if (flag & 2) return eb_fail(c, EB_BAD_INPUT, "Shear modulus for marker material is zero");
+  return EB_OK;
+}
+
+int launch_scatter_heat(eb_ctx* c) {
+  int rc = ensure_markers(c, {EB_M_MATID, EB_M_TK, EB_M_KT, EB_M_RHOCP, EB_M_HA, EB_M_SERP_HR});
+  if (rc) return rc;
+  rc = ensure_grids(c, {EB_G_TK1, EB_G_TK0, EB_G_TK2, EB_G_KT1, EB_G_KT0, EB_G_RHOCP1, EB_G_RHOCP0, EB_G_HR1, EB_G_HR0,
+                        EB_G_HA1, EB_G_HA0, EB_G_BTOPT, EB_G_BBOTTOMT, EB_G_BLEFTT, EB_G_BRIGHTT});
+  if (rc) return rc;
+  if (c->M > 0) {
+    rc = run_cells(c, HeatSpec{c->mats.hr, (int)(c->P.iuse_serpentinization == 1)});
+    if (rc) return rc;
+  } else {
+    EB_CK(c, cudaMemsetAsync(c->part, 0, (size_t)kMaxSlots * c->cs.ncells * sizeof(float), c->stream));
+  }
+  double** gf = c->gf;
+  HeatGrids G{gf[EB_G_TK1], gf[EB_G_TK0], gf[EB_G_KT1], gf[EB_G_KT0], gf[EB_G_RHOCP1], gf[EB_G_RHOCP0],
+              gf[EB_G_HR1], gf[EB_G_HR0], gf[EB_G_HA1], gf[EB_G_HA0], gf[EB_G_TK2], gf[EB_G_WTNODES]};
+  const int64_t n = (int64_t)c->ynum * c->xnum;
+  EB_PROF(c, "k_finish_heat");
+  k_finish_heat<<<node_blocks(c, n), 256, 0, c->stream>>>(node_ctx(c), G);
+  EB_LAUNCHED(c);
+  EB_PROF(c, "k_thermal_bc_rows");
+  k_thermal_bc_rows<<<(c->xnum + 255) / 256, 256, 0, c->stream>>>(gf[EB_G_TK1], gf[EB_G_BTOPT], gf[EB_G_BBOTTOMT], c->ynum, c->xnum);
+  EB_LAUNCHED(c);
+  EB_PROF(c, "k_thermal_bc_cols");
+  k_thermal_bc_cols<<<(c->ynum + 255) / 256, 256, 0, c->stream>>>(gf[EB_G_TK1], gf[EB_G_BLEFTT], gf[EB_G_BRIGHTT], c->ynum, c->xnum);
+  EB_LAUNCHED(c);
+  return EB_OK;
+}
+
+int launch_scatter_viscosity(eb_ctx* c) {
+  int rc = ensure_markers(c, {EB_M_ETA});
+  if (rc) return rc;
+  rc = ensure_grids(c, {EB_G_ETAS1, EB_G_ETAS0, EB_G_ETAN1, EB_G_ETAN0});
+  if (rc) return rc;
+  if (c->M > 0) {
+    rc = run_cells(c, ViscSpec{});
+    if (rc) return rc;
+  } else {
+    EB_CK(c, cudaMemsetAsync(c->part, 0, (size_t)kMaxSlots * c->cs.ncells * sizeof(float), c->stream));
+  }
+  double** gf = c->gf;
+  EB_PROF(c, "k_finish_visc");
+  k_finish_visc<<<node_blocks(c, (int64_t)c->ynum * c->xnum), 256, 0, c->stream>>>(
+      node_ctx(c), gf[EB_G_ETAS1], gf[EB_G_ETAS0], gf[EB_G_ETAN1], gf[EB_G_ETAN0], gf[EB_G_WTETAS], gf[EB_G_WTETAN]);
+  EB_LAUNCHED(c);
+  return EB_OK;
+}
+
+int launch_subgrid_stress(eb_ctx* c) {
+  if (!(c->P.subgrid_diff_coef_stress > 0)) return EB_OK;  // StokesContinuitySolver.jl:371-373
+  int rc = ensure_markers(c, {EB_M_MATID, EB_M_ETA, EB_M_SXY, EB_M_SXX});
+  if (rc) return rc;
+  rc = ensure_grids(c, {EB_G_SXY1, EB_G_SXX1, EB_G_DSXYN, EB_G_DSXXN, EB_G_DSXY, EB_G_DSXX});
+  if (rc) return rc;
+  double** gf = c->gf;
+  if (c->M > 0) {
+    SubgridStressSpec s{gf[EB_G_SXY1], gf[EB_G_SXX1], c->mats.mu, (float)c->P.timestep, (float)c->P.subgrid_diff_coef_stress};
+    rc = run_cells(c, s);
+    if (rc) return rc;
+  } else {
+    EB_CK(c, cudaMemsetAsync(c->part, 0, (size_t)kMaxSlots * c->cs.ncells * sizeof(float), c->stream));
+  }
+  EB_PROF(c, "k_finish_subgrid_stress");
+  k_finish_subgrid_stress<<<node_blocks(c, (int64_t)c->ynum * c->xnum), 256, 0, c->stream>>>(
+      node_ctx(c), gf[EB_G_DSXYN], gf[EB_G_DSXXN], gf[EB_G_WTETAS], gf[EB_G_WTETAN], gf[EB_G_DSXY], gf[EB_G_DSXX]);
+  EB_LAUNCHED(c);
+  return EB_OK;
+}
+
+int launch_subgrid_heat(eb_ctx* c) {
+  int rc = ensure_markers(c, {EB_M_TK, EB_M_SUBGRID_DT});
+  if (rc) return rc;
+  rc = ensure_grids(c, {EB_G_TK1, EB_G_KT1, EB_G_RHOCP1, EB_G_DTKN, EB_G_DTK1});
+  if (rc) return rc;
+  double** gf = c->gf;
+  // markers outside the domain get a zero subgrid change (SubgridDiffusion.jl:119-121)
+  EB_CK(c, cudaMemsetAsync(c->mf[EB_M_SUBGRID_DT], 0, c->M * sizeof(double), c->stream));
+  if (c->M > 0) {
+    const double its = 2.0 / (c->g.xstpavg * c->g.xstpavg) + 2.0 / (c->g.ystpavg * c->g.ystpavg);
+    SubgridHeatSpec s{gf[EB_G_TK1], gf[EB_G_KT1], gf[EB_G_RHOCP1], (float)c->P.timestep,
+                      (float)c->P.subgrid_diff_coef_temp, (float)its};
+    rc = run_cells(c, s);
+    if (rc) return rc;
+  } else {
+    EB_CK(c, cudaMemsetAsync(c->part, 0, (size_t)kMaxSlots * c->cs.ncells * sizeof(float), c->stream));
+  }
+  EB_PROF(c, "k_finish_subgrid_heat");
+  k_finish_subgrid_heat<<<node_blocks(c, (int64_t)c->ynum * c->xnum), 256, 0, c->stream>>>(
+      node_ctx(c), gf[EB_G_DTKN], gf[EB_G_WTNODES], gf[EB_G_DTK1]);
+  EB_LAUNCHED(c);
+  return EB_OK;
+}

@@ -1,0 +1,330 @@
+"""Seeded synthetic inputs for the marker-in-cell hot path.
+
+No dataset is involved: every model below is generated from a seed with the
+shapes, spacings, marker densities and value ranges of the three marker-path
+configurations:
+
+* ``sinking_block``  -- 101x101 basic nodes over 500x500 km, 4x4 markers per
+  cell (160,000 markers); background 1e21 Pa s / 3200 kg/m^3, a centred
+  100x100 km block of 1e27 Pa s / 3300 kg/m^3; dt = 10 kyr.
+* ``rift``           -- 500x160 km with 10 km of sticky air (1e18 Pa s, 1 kg/m^3),
+  upper crust 0-20 km (2700, wet quartzite), lower crust 20-35 km (2850,
+  plagioclase/anorthite), mantle (3300, dry olivine), power-law creep,
+  Drucker-Prager friction 30 deg -> 15 deg by strain 1.0, cohesion 10 MPa,
+  initial plastic strain U(0, 0.5) in a central 50 km zone, linear geotherm
+  0 C -> 1330 C at 120 km, +-1 cm/yr extension.  ``rift(801, 201, 4)`` is the
+  2.56M-marker case; ``rift(2001, 801, 5)`` the 40M-marker case.
+
+Flow-law constants are the values of the reference's material registry
+(src/material_library/registries/lithospheric_deformation/lithospheric_deformation_eb1.yml).
+Marker placement follows MarkersRandomized.initialize! (outer loop over x,
+inner over y: markers of a cell sit in runs along y) with independent x and y
+jitter drawn from a Philox stream (the reference draws one value for both and
+does not seed it).  Grid-side inputs of the gathers and of the advection
+(velocities, spin, strain rates, stresses, pressure) are smooth analytic
+fields with the magnitudes of a rifting model.
+"""
+from __future__ import annotations
+
+import dataclasses
+import math
+
+import numpy as np
+
+from . import _abi
+
+YEAR = 365.25 * 24.0 * 3600.0
+
+
+@dataclasses.dataclass
+class Grid:
+    xnum: int
+    ynum: int
+    gridx_b: np.ndarray
+    gridy_b: np.ndarray
+    xstp_b: np.ndarray
+    ystp_b: np.ndarray
+    gridx_vy: np.ndarray
+    xstp_vy: np.ndarray
+    gridy_vx: np.ndarray
+    ystp_vx: np.ndarray
+    xmin: float
+    xmax: float
+    ymin: float
+    ymax: float
+    xstpavg: float
+    ystpavg: float
+
+
+@dataclasses.dataclass
+class Materials:
+    mat_mu: np.ndarray
+    mat_hr: np.ndarray
+    mat_flow_type: np.ndarray
+    mat_flow: np.ndarray      # (nmat, 12), Fortran order
+    mat_plastic: np.ndarray   # (nmat, 6), Fortran order
+    mat_rho: np.ndarray
+
+    @property
+    def nmat(self) -> int:
+        return len(self.mat_mu)
+
+
+@dataclasses.dataclass
+class Model:
+    name: str
+    grid: Grid
+    mats: Materials
+    params: dict
+    markers: dict             # name -> 1-D array (dtype of _abi.MARKER_DTYPE)
+    grids: dict               # name -> 2-D Fortran-order array
+
+    @property
+    def marknum(self) -> int:
+        return len(self.markers["x"])
+
+    def copy(self) -> "Model":
+        return Model(self.name, self.grid, self.mats, dict(self.params),
+                     {k: v.copy() for k, v in self.markers.items()},
+                     {k: np.asfortranarray(v.copy()) for k, v in self.grids.items()})
+
+
+def staggered_grid(x: np.ndarray, y: np.ndarray) -> Grid:
+    """Basic coordinates -> staggered vx/vy coordinates and spacings
+    (restating VyGridTools / VxGridTools in src/staggered_grid/utils)."""
+    def stag(b):
+        n = len(b)
+        stp = np.diff(b)
+        g = np.empty(n + 1)
+        g[0] = b[0] - stp[0] / 2.0
+        g[n] = b[n - 1] + stp[n - 2] / 2.0
+        g[1:n] = (b[1:] + b[:-1]) / 2.0
+        s = np.empty(n)
+        s[0] = stp[0]
+        s[n - 1] = stp[n - 2]
+        s[1:n - 1] = (b[2:] - b[:-2]) / 2.0
+        return g, s
+    gxvy, sxvy = stag(x)
+    gyvx, syvx = stag(y)
+    return Grid(len(x), len(y), x, y, np.diff(x), np.diff(y), gxvy, sxvy, gyvx, syvx,
+                float(x[0]), float(x[-1]), float(y[0]), float(y[-1]),
+                float((x[-1] - x[0]) / (len(x) - 1)), float((y[-1] - y[0]) / (len(y) - 1)))
+
+
+def default_params(**kw) -> dict:
+    p = dict(timestep=1e4 * YEAR, ntimestep=1, temperature_top=273.15, viscosity_min=1e18, viscosity_max=1e26,
+             powerlaw_stress_min=1e4, yield_stress_min=0.0, yield_stress_max=1e12, gas_constant=8.314,
+             iuse_viscous_strain_soft=0, vsoftfac=1.0, iuse_fluid_pressure_for_yield=0, y_sealevel=10e3,
+             itype_global=0, no_yielding_in_mobile_wall=0, matid_sticky_air=-1, matid_mobile_wall=-1,
+             matid_plate_extension=-1, plastic_healing_rate=0.0, subgrid_diff_coef_stress=1.0,
+             subgrid_diff_coef_temp=1.0, iuse_melt_damage=0, iuse_serpentinization=0, iuse_topo=0,
+             matid_sticky_air_rho=-1, matid_sticky_water_rho=-1, runge_kutta_order=4)
+    p.update(kw)
+    return p
+
+
+def _markers_xy(rng, grid: Grid, mpc: int):
+    """MarkersRandomized layout: mxnum x mynum markers, x outer / y inner."""
+    W, H = grid.xmax - grid.xmin, grid.ymax - grid.ymin
+    mx, my = (grid.xnum - 1) * mpc, (grid.ynum - 1) * mpc
+    mxstep, mystep = W / mx, H / my
+    ix = np.repeat(np.arange(1, mx + 1, dtype=np.float64), my)
+    iy = np.tile(np.arange(1, my + 1, dtype=np.float64), mx)
+    rx = rng.random(mx * my)
+    ry = rng.random(mx * my)
+    x = grid.xmin + ix * mxstep - mxstep / 2.0 + (rx - 0.5) * mxstep
+    y = grid.ymin + iy * mystep - mystep / 2.0 + (ry - 0.5) * mystep
+    return x, y
+
+
+def _fields_common(rng, n: int, markers: dict) -> None:
+    markers["pfailure"] = (rng.random(n) < 0.1).astype(np.float32)
+    markers["dilatation"] = np.zeros(n, np.float32)
+    markers["meltfrac"] = np.zeros(n)
+    markers["melt_damage"] = np.ones(n)
+    markers["serp_hr"] = np.zeros(n)
+    for k in ("vx", "vy", "spin", "subgrid_dt", "strain_rate_plastic"):
+        markers[k] = np.zeros(n)
+
+
+def _analytic_grids(grid: Grid, v0: float, eta_ref: float, rho_ref: float, T0: float, T1: float,
+                    depth_T1: float, y_surface: float, g: float = 9.81) -> dict:
+    """Smooth grid-side inputs of the gathers and of the advection."""
+    X, Y = grid.xnum, grid.ynum
+    W, H = grid.xmax - grid.xmin, grid.ymax - grid.ymin
+    xb, yb = grid.gridx_b, grid.gridy_b
+    xc = grid.gridx_vy[1:X]        # pressure-node x (cell centres)
+    yc = grid.gridy_vx[1:Y]
+    kx, ky = 2.0 * math.pi / W, math.pi / H
+    A = 0.3 * v0                    # cellular perturbation amplitude
+
+    def F(a):
+        return np.asfortranarray(a)
+    # stream function psi = A/kx sin(kx x) sin(ky y) + extension: vx = dpsi/dy, vy = -dpsi/dx
+    def vx_at(x, y):
+        return v0 * (2.0 * (x - grid.xmin) / W - 1.0) + A * ky / kx * np.sin(kx * x) * np.cos(ky * y)
+    def vy_at(x, y):
+        return -2.0 * v0 / W * (y - (grid.ymin + 0.5 * H)) - A * np.cos(kx * x) * np.sin(ky * y)
+    Yvx, Xvx = np.meshgrid(grid.gridy_vx, xb, indexing="ij")
+    Yvy, Xvy = np.meshgrid(yb, grid.gridx_vy, indexing="ij")
+    Yb, Xb = np.meshgrid(yb, xb, indexing="ij")
+    Yp, Xp = np.meshgrid(yc, xc, indexing="ij")
+    out = {}
+    out["vx1"] = F(vx_at(Xvx, Yvx))
+    out["vy1"] = F(vy_at(Xvy, Yvy))
+    # spin 0.5 (dvy/dx - dvx/dy) of the perturbation
+    out["esp"] = F(0.5 * (A * kx * np.sin(kx * Xb) * np.sin(ky * Yb) + A * ky * ky / kx * np.sin(kx * Xb) * np.sin(ky * Yb)))
+    exx_p = 2.0 * v0 / W + A * ky * np.cos(kx * Xp) * np.cos(ky * Yp)
+    out["exx"] = F(exx_p)
+    out["exy"] = F(0.5 * A * (-ky * ky / kx + kx) * np.sin(kx * Xb) * np.sin(ky * Yb))
+    out["sxx2"] = F(2.0 * eta_ref * exx_p)
+    out["sxy2"] = F(2.0 * eta_ref * out["exy"])
+    out["dsxx"] = F(0.05 * out["sxx2"])
+    out["dsxy"] = F(0.05 * out["sxy2"])
+    depth_p = np.clip(Yp - y_surface, 0.0, None)
+    out["pr1"] = F(rho_ref * g * depth_p + 1e5 * np.cos(kx * Xp))
+    depth_b = np.clip(Yb - y_surface, 0.0, None)
+    Tb = T0 + (T1 - T0) * np.clip(depth_b / depth_T1, 0.0, 1.0)
+    out["tk2"] = F(Tb)
+    out["dtk1"] = F(0.5 * np.sin(kx * Xb) * np.sin(ky * Yb))
+    out["btopt"] = F(np.column_stack([np.full(X, T0), np.zeros(X)]))
+    out["bbottomt"] = F(np.column_stack([np.full(X, Tb[-1, 0]), np.zeros(X)]))
+    out["bleftt"] = F(np.column_stack([np.zeros(Y), np.ones(Y)]))
+    out["brightt"] = F(np.column_stack([np.zeros(Y), np.ones(Y)]))
+    # transport grids start from plausible values so that empty nodes keep a backup
+    for name, val in (("rho1", rho_ref), ("etas1", eta_ref), ("eta_flow", eta_ref), ("mus1", 3e10), ("sxy1", 0.0),
+                      ("plastics", 0.0), ("cohesion_grid", 1e7), ("fric_degrees_grid", 30.0), ("tk1", T0),
+                      ("kt1", 2.5), ("rhocp1", 2.5e6), ("hr1", 1e-6), ("ha1", 0.0)):
+        out[name] = F(np.full((Y, X), val))
+    for name, val in (("etan1", eta_ref), ("mun1", 3e10), ("sxx1", 0.0), ("plasticn", 0.0), ("dilatation_grid", 0.0),
+                      ("extractable_meltfrac_grid", 0.0)):
+        out[name] = F(np.full((Y - 1, X - 1), val))
+    out["rho1_vy"] = F(np.full((Y, X + 1), rho_ref))
+    # stress grids of the subgrid-stress step: interpolated marker stress, smooth
+    out["sxy1"] = F(out["sxy2"] * 0.9)
+    out["sxx1"] = F(out["sxx2"] * 0.9)
+    return out
+
+
+def sinking_block(xnum: int = 101, ynum: int = 101, mpc: int = 4, seed: int = 1) -> Model:
+    rng = np.random.Generator(np.random.Philox(seed))
+    W = H = 500e3
+    grid = staggered_grid(np.linspace(0.0, W, xnum), np.linspace(0.0, H, ynum))
+    x, y = _markers_xy(rng, grid, mpc)
+    n = len(x)
+    block = (np.abs(x - W / 2) <= 50e3) & (np.abs(y - H / 2) <= 50e3)
+    matid = np.where(block, 2, 1).astype(np.int16)
+    mats = Materials(
+        mat_mu=np.array([1e10, 1e10]), mat_hr=np.zeros(2), mat_flow_type=np.array([0, 0], np.int64),
+        mat_flow=np.asfortranarray(np.zeros((2, 12))), mat_plastic=np.asfortranarray(np.zeros((2, 6))),
+        mat_rho=np.array([3200.0, 3300.0]))
+    mats.mat_flow[:, 0] = [1e21, 1e27]
+    m = {"x": x, "y": y, "matid": matid}
+    m["rho"] = np.where(block, 3300.0, 3200.0)
+    m["eta"] = np.where(block, 1e27, 1e21)
+    m["eta_flow"] = m["eta"].copy()
+    m["cohesion"] = np.zeros(n)
+    m["fric"] = np.zeros(n)
+    m["fric_ini"] = np.zeros(n)
+    m["preexp"] = np.zeros(n)
+    m["sxx"] = rng.normal(0.0, 1e5, n)
+    m["sxy"] = rng.normal(0.0, 1e5, n)
+    m["exx"] = rng.normal(0.0, 1e-15, n)
+    m["exy"] = rng.normal(0.0, 1e-15, n)
+    m["pr"] = 3200.0 * 9.81 * y
+    m["sr_ratio"] = np.ones(n)
+    m["gii"] = np.zeros(n)
+    m["strain_plastic"] = np.zeros(n)
+    m["tk"] = 273.15 + 1000.0 * y / H
+    m["kt"] = np.full(n, 3.0)
+    m["rhocp"] = m["rho"] * 1000.0
+    m["ha"] = 3e-5 * m["tk"]
+    _fields_common(rng, n, m)
+    m["pfailure"][:] = 0.0
+    grids = _analytic_grids(grid, v0=1e-2 / YEAR, eta_ref=1e21, rho_ref=3200.0, T0=273.15, T1=1273.15,
+                            depth_T1=H, y_surface=0.0)
+    params = default_params(timestep=1e4 * YEAR, viscosity_min=1e18, viscosity_max=1e28, ntimestep=1)
+    return Model("sinking_block", grid, mats, params, m, grids)
+
+
+def rift(xnum: int = 801, ynum: int = 201, mpc: int = 4, seed: int = 2, width: float = 500e3) -> Model:
+    rng = np.random.Generator(np.random.Philox(seed))
+    W, H, air = width, 160e3, 10e3
+    grid = staggered_grid(np.linspace(0.0, W, xnum), np.linspace(0.0, H, ynum))
+    x, y = _markers_xy(rng, grid, mpc)
+    n = len(x)
+    depth = y - air
+    matid = np.full(n, 4, np.int16)
+    matid[depth < 35e3] = 3
+    matid[depth < 20e3] = 2
+    matid[depth < 0.0] = 1
+    # registry values (lithospheric_deformation_eb1.yml): air, wet quartzite, anorthite, dry olivine
+    nmat = 4
+    mat_flow = np.zeros((nmat, 12))
+    mat_flow[0, 0] = 1e18
+    mat_flow[1, [1, 2, 3, 4]] = [8.57e-4, 4.0, 223.0, 0.0]
+    mat_flow[2, [1, 2, 3, 4]] = [3.57e3, 3.0, 345.0, 38.0]
+    mat_flow[3, [1, 2, 3, 4]] = [6.51e5, 3.5, 530.0, 13.0]
+    mat_flow[3, [5, 6, 7, 8]] = [2.5e7, 1.0, 2.0, 9100.0]
+    mat_flow[3, [9, 10, 11]] = [1.04e-2, 375.0, 6.0]
+    sin30, sin15 = math.sin(math.radians(30.0)), math.sin(math.radians(15.0))
+    mat_plastic = np.zeros((nmat, 6))
+    mat_plastic[1:, :] = [10e6, 10e6, sin30, sin15, 0.0, 1.0]
+    mats = Materials(
+        mat_mu=np.array([1e20, 3.6e10, 4.0e10, 6.6e10]), mat_hr=np.array([0.0, 1.8e-6, 0.5e-6, 0.0]),
+        mat_flow_type=np.array([0, 1, 1, 1], np.int64), mat_flow=np.asfortranarray(mat_flow),
+        mat_plastic=np.asfortranarray(mat_plastic), mat_rho=np.array([1.0, 2700.0, 2850.0, 3300.0]))
+    rho_of = mats.mat_rho
+    m = {"x": x, "y": y, "matid": matid}
+    mi = matid.astype(np.int64) - 1
+    m["rho"] = rho_of[mi].copy()
+    T = 273.15 + 1330.0 * np.clip(depth / 120e3, 0.0, 1.0)
+    m["tk"] = T
+    rock = matid > 1
+    m["fric_ini"] = np.where(rock, sin30, 0.0)
+    m["strain_plastic"] = np.where(rock & (np.abs(x - W / 2) < 25e3), rng.uniform(0.0, 0.5, n), 0.0)
+    m["cohesion"] = np.where(rock, 10e6, 0.0)
+    m["fric"] = m["fric_ini"].copy()
+    m["eta"] = np.where(rock, 10.0 ** rng.uniform(20.0, 24.0, n), 1e18)
+    m["eta_flow"] = m["eta"] * np.where(rock, 10.0 ** rng.uniform(0.0, 0.5, n), 1.0)
+    m["preexp"] = mat_flow[mi, 1].copy()
+    m["sxx"] = np.where(rock, rng.normal(0.0, 5e6, n), 0.0)
+    m["sxy"] = np.where(rock, rng.normal(0.0, 5e6, n), 0.0)
+    v0 = 1e-2 / YEAR
+    m["exx"] = 2.0 * v0 / W * (1.0 + 0.3 * rng.normal(0.0, 1.0, n))
+    m["exy"] = 0.3 * 2.0 * v0 / W * rng.normal(0.0, 1.0, n)
+    m["pr"] = np.where(rock, 2900.0 * 9.81 * np.clip(depth, 0.0, None), 0.0) + 1e5
+    m["sr_ratio"] = rng.uniform(0.8, 1.2, n)
+    m["gii"] = rng.uniform(0.0, 1.0, n)
+    m["kt"] = np.where(rock, 2.5, 200.0)
+    m["rhocp"] = m["rho"] * np.where(rock, 800.0, 100.0)
+    m["ha"] = 3e-5 * T
+    _fields_common(rng, n, m)
+    grids = _analytic_grids(grid, v0=v0, eta_ref=1e22, rho_ref=2900.0, T0=273.15, T1=1603.15, depth_T1=120e3,
+                            y_surface=air)
+    params = default_params(timestep=1e4 * YEAR, y_sealevel=air, matid_sticky_air=1)
+    return Model(f"rift_{xnum}x{ynum}_{mpc}", grid, mats, params, m, grids)
+
+
+def config(name: str, seed: int | None = None) -> Model:
+    """Named workloads: sinking_block, rift_small, rift_2p5M, rift_40M."""
+    kw = {} if seed is None else {"seed": seed}
+    if name == "sinking_block":
+        return sinking_block(**kw)
+    if name == "rift_small":
+        return rift(101, 41, 4, **kw)
+    if name == "rift_2p5M":
+        return rift(801, 201, 4, **kw)
+    if name == "rift_40M":
+        return rift(2001, 801, 5, **kw)
+    if name == "rift_40M_strip":
+        return rift(101, 801, 5, width=25e3, **kw)
+    raise KeyError(name)
+
+
+def marker_arrays_for_upload(model: Model) -> dict:
+    """Marker arrays cast to the C-ABI host types."""
+    out = {}
+    for k, v in model.markers.items():
+        out[k] = np.ascontiguousarray(v, dtype=_abi.MARKER_DTYPE[k])
+    return out

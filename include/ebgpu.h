@@ -1,0 +1,253 @@
+/*
+ * ebgpu.h -- C-ABI of the GB300 (sm_103a) marker-in-cell hot path for EarthBox.jl.
+ *
+ * One opaque context (eb_ctx) per GPU holds the marker SoA, the staggered grids and
+ * the material tables device-resident.  The host (Julia through `ccall`, or any
+ * C/C++/Python caller) uploads its arrays once, calls one entry point per
+ * reference step, and copies fields back only when it needs them (output,
+ * checkpoint).  Every entry point returns an int status (EB_OK on success) and
+ * never aborts or traps; eb_last_error() gives the message of the last failure.
+ *
+ * Layout conventions are the reference's:
+ *   - grid arrays are Julia column-major Matrix{Float64} of shape (rows, cols):
+ *     element (i, j), 1-based, lives at offset (j-1)*rows + (i-1);
+ *   - marker cell indices (marker_xn/yn, marker_xn_vy/yn_vy) are 1-based Int32;
+ *   - marker_matid is accepted as Int16 (the reference's storage type) and
+ *     widened to Int32 on the device;
+ *   - material tables mat_flow (nmat x 12) and mat_plastic (nmat x 6) are
+ *     column-major, indexed by the 1-based material id.
+ * All calls are synchronous with respect to the host on return, on the
+ * context's own CUDA stream.
+ */
+#ifndef EBGPU_H
+#define EBGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes -------------------------------------------------------- */
+#define EB_OK            0
+#define EB_NOT_CONVERGED 1  /* iterative solve stopped before its tolerance     */
+#define EB_NAN           2  /* NaN/Inf found in an input or a result            */
+#define EB_BAD_INPUT     3  /* sizes, pointers or field ids out of range        */
+#define EB_CUDA_ERROR    4  /* a CUDA runtime call failed (message in last_error)*/
+#define EB_NOT_READY     5  /* a prerequisite step has not been run             */
+
+typedef struct eb_ctx eb_ctx;
+
+/* ---- grid geometry (reference: model.grids.arrays.*, model.grids.parameters.geometry) */
+typedef struct eb_grid_desc {
+  int64_t xnum, ynum;          /* basic-grid node counts                              */
+  const double* gridx_b;       /* [xnum]    basic x coordinates                       */
+  const double* gridy_b;       /* [ynum]    basic y coordinates                       */
+  const double* xstp_b;        /* [xnum-1]  basic x spacings                          */
+  const double* ystp_b;        /* [ynum-1]  basic y spacings                          */
+  const double* gridx_vy;      /* [xnum+1]  vy-grid x coordinates                     */
+  const double* xstp_vy;       /* [xnum]    vy-grid x spacings                        */
+  const double* gridy_vx;      /* [ynum+1]  vx-grid y coordinates                     */
+  const double* ystp_vx;       /* [ynum]    vx-grid y spacings                        */
+  double xmin, xmax, ymin, ymax;  /* domain limits used by the inside test           */
+  double xstpavg, ystpavg;        /* average spacings (subgrid thermal timescale)     */
+} eb_grid_desc;
+
+/* ---- material tables (reference: model.materials.arrays.*) ----------------- */
+typedef struct eb_material_desc {
+  int64_t nmat;
+  const double*  mat_mu;        /* [nmat]      shear modulus (Pa)                     */
+  const double*  mat_hr;        /* [nmat]      radiogenic heat production (W/m^3)     */
+  const int64_t* mat_flow_type; /* [nmat]      0 isoviscous, 1/2 composite creep     */
+  const double*  mat_flow;      /* [nmat x 12] column-major flow-law table            */
+  const double*  mat_plastic;   /* [nmat x 6]  column-major plasticity table          */
+  const double*  mat_rho;       /* [nmat]      first column of mat_rho (sticky flatten)*/
+} eb_material_desc;
+
+/* ---- scalar model parameters (reference parameter registry values) -------- */
+typedef struct eb_params {
+  double  timestep;                 /* s                                               */
+  int64_t ntimestep;                /* current time-step counter                       */
+  double  temperature_top;          /* K                                               */
+  double  viscosity_min, viscosity_max;
+  double  powerlaw_stress_min;      /* Pa                                              */
+  double  yield_stress_min, yield_stress_max;
+  double  gas_constant;             /* J/mol/K                                         */
+  int64_t iuse_viscous_strain_soft; double vsoftfac;
+  int64_t iuse_fluid_pressure_for_yield; double y_sealevel;
+  int64_t itype_global;             /* 0 marker Picard loop, 1 nodal Picard loop       */
+  int64_t no_yielding_in_mobile_wall;
+  int64_t matid_sticky_air, matid_mobile_wall, matid_plate_extension; /* -1 = none   */
+  double  plastic_healing_rate;     /* 1/s                                             */
+  double  subgrid_diff_coef_stress, subgrid_diff_coef_temp;
+  int64_t iuse_melt_damage;
+  int64_t iuse_serpentinization;
+  int64_t iuse_topo;                /* sticky-layer density flattening switch          */
+  int64_t matid_sticky_air_rho, matid_sticky_water_rho; /* ids for flattening, -1 none */
+  int64_t runge_kutta_order;        /* 1 or 4 (0 = markers do not move)                */
+} eb_params;
+
+/* ---- marker fields ----------------------------------------------------------
+ * Types on the host side of eb_marker_upload/download: F64 unless noted. */
+enum eb_marker_field {
+  EB_M_X = 0, EB_M_Y,                     /* marker_x, marker_y                        */
+  EB_M_MATID,                             /* marker_matid       (Int16 on the host)    */
+  EB_M_RHO, EB_M_COHESION, EB_M_FRIC, EB_M_FRIC_INI,
+  EB_M_ETA, EB_M_ETA_FLOW, EB_M_PREEXP,
+  EB_M_SXX, EB_M_SXY, EB_M_EXX, EB_M_EXY, EB_M_PR, EB_M_SR_RATIO,
+  EB_M_GII, EB_M_STRAIN_PLASTIC, EB_M_STRAIN_RATE_PLASTIC,
+  EB_M_TK, EB_M_KT, EB_M_RHOCP, EB_M_HA,
+  EB_M_MELTFRAC,                          /* marker_extractable_meltfrac               */
+  EB_M_MELT_DAMAGE, EB_M_SERP_HR,         /* melt damage factor, serpentinisation heat */
+  EB_M_PFAILURE,                          /* Float32                                   */
+  EB_M_DILATATION,                        /* Float32 marker_dilatation_angle           */
+  EB_M_VX, EB_M_VY, EB_M_SPIN,            /* RK4 velocity/spin at the marker           */
+  EB_M_SUBGRID_DT,                        /* marker_subgrid_temp_delta_buffer          */
+  EB_M_XN, EB_M_YN, EB_M_XN_VY, EB_M_YN_VY, /* Int32, 1-based, download only          */
+  EB_M_INSIDE,                            /* Int8 (+1 inside / -1 outside)             */
+  EB_M_NFIELDS
+};
+
+/* ---- grid fields ------------------------------------------------------------
+ * Shapes: B = basic (ynum, xnum); P = pressure (ynum-1, xnum-1);
+ *         VX = (ynum+1, xnum); VY = (ynum, xnum+1);
+ *         BCX = (xnum, 2) thermal top/bottom BC; BCY = (ynum, 2) left/right BC. */
+enum eb_grid_field {
+  /* basic grid */
+  EB_G_RHO1 = 0, EB_G_RHO0, EB_G_ETAS1, EB_G_ETAS0, EB_G_ETA_FLOW, EB_G_ETA_FLOW0,
+  EB_G_MUS1, EB_G_MUS0, EB_G_SXY1, EB_G_SXY0, EB_G_PLASTICS, EB_G_PLASTICS0,
+  EB_G_COHESION, EB_G_COHESION0, EB_G_FRIC_DEG, EB_G_FRIC_DEG0,
+  EB_G_WTNODES, EB_G_WTETAS,
+  EB_G_TK1, EB_G_TK0, EB_G_TK2, EB_G_KT1, EB_G_KT0, EB_G_RHOCP1, EB_G_RHOCP0,
+  EB_G_HR1, EB_G_HR0, EB_G_HA1, EB_G_HA0,
+  EB_G_EXY, EB_G_ESP, EB_G_SXY2, EB_G_DSXY, EB_G_DSXYN, EB_G_DTK1, EB_G_DTKN,
+  EB_G_PLASTIC_YIELD,
+  /* pressure grid */
+  EB_G_ETAN1, EB_G_ETAN0, EB_G_MUN1, EB_G_MUN0, EB_G_SXX1, EB_G_SXX0,
+  EB_G_PLASTICN, EB_G_PLASTICN0, EB_G_DILAT, EB_G_DILAT0, EB_G_MELTFRAC, EB_G_MELTFRAC0,
+  EB_G_WTETAN, EB_G_EXX, EB_G_SXX2, EB_G_DSXX, EB_G_DSXXN, EB_G_PR1,
+  /* vx / vy grids */
+  EB_G_VX1,
+  EB_G_VY1, EB_G_RHO1_VY, EB_G_RHO0_VY, EB_G_WTNODES_VY,
+  /* thermal boundary-condition coefficient arrays */
+  EB_G_BTOPT, EB_G_BBOTTOMT, EB_G_BLEFTT, EB_G_BRIGHTT,
+  EB_G_NFIELDS
+};
+
+/* ---- context ------------------------------------------------------------- */
+int         eb_create(eb_ctx** out, int device);
+int         eb_destroy(eb_ctx* ctx);
+const char* eb_last_error(const eb_ctx* ctx);
+int         eb_set_grid(eb_ctx* ctx, const eb_grid_desc* grid);
+int         eb_set_materials(eb_ctx* ctx, const eb_material_desc* mats);
+int         eb_set_params(eb_ctx* ctx, const eb_params* params);
+int         eb_resize_markers(eb_ctx* ctx, int64_t marknum);
+/* Copy one marker field between host memory and the device (count = marknum).  */
+int         eb_marker_upload(eb_ctx* ctx, int field, const void* host);
+int         eb_marker_download(eb_ctx* ctx, int field, void* host);
+/* Copy one grid field (count = rows*cols of the field's shape).                */
+int         eb_grid_upload(eb_ctx* ctx, int field, const double* host);
+int         eb_grid_download(eb_ctx* ctx, int field, double* host);
+/* Device pointer of a field (for callers that already hold device buffers).    */
+int         eb_marker_device_ptr(eb_ctx* ctx, int field, void** dptr);
+int         eb_grid_device_ptr(eb_ctx* ctx, int field, double** dptr);
+/* The context's CUDA stream (cudaStream_t) for event timing by the caller.     */
+void*       eb_stream(eb_ctx* ctx);
+/* Number of kernels this context has launched since creation.                  */
+int64_t     eb_launch_count(const eb_ctx* ctx);
+/* Per-kernel timing with CUDA events on the context's stream.  Enabling (or
+ * disabling) clears the counters; entries are kernels in name order, each with
+ * its summed device time and launch count since the last enable.  No
+ * counterpart in the reference (it times whole steps with @timeit_memit,
+ * src/utils/PrintFuncs.jl:46-94).                                              */
+int         eb_profile_enable(eb_ctx* ctx, int on);
+int         eb_profile_count(const eb_ctx* ctx);
+int         eb_profile_entry(const eb_ctx* ctx, int i, char* name, int name_len,
+                             double* total_ms, int64_t* launches);
+
+/* ---- hot-path entry points (one per reference step) -----------------------
+ * Each mirrors the named reference function; inside flags are the context's
+ * own (EB_M_INSIDE), set by eb_get_marker_inside_flags.                       */
+
+/* GridFuncs.get_marker_inside_flags  (src/utils/GridFuncs.jl:54-80)            */
+int eb_get_marker_inside_flags(eb_ctx* ctx);
+
+/* InitializeInterpolation.initialize_bilinear_interpolation!
+ *   (src/interpolation/initialize/InitializeInterpolation.jl:63-82):
+ * upper-left indices on basic and vy grids (MarkerGridMapping.jl:78-173),
+ * normalised distances and weights (recomputed on the fly, MarkerGridMapping.jl:185-265,
+ * MarkerGridNodeWeights.jl:68-150), the cell-sorted marker list, and the
+ * weight-sum denominators wtnodes/wtetas/wtetan/wtnodes_vy (BilinearDenominator.jl:34-157). */
+int eb_initialize_bilinear_interpolation(eb_ctx* ctx);
+
+/* MarkersToStokesArrays.interpolate_markers_to_transport_arrays!
+ *   (src/interpolation/utils/MarkersToStokesArrays.jl:39-45): backup+clear
+ * (BackupTransportArrays.jl:33-98), numerators (BilinearNumerator.jl:205-454),
+ * averages (BilinearAverage.jl:57-178), sticky-layer flattening (FlattenDensity.jl:29-89). */
+int eb_interpolate_marker_stokes_parameters_to_grid(eb_ctx* ctx);
+
+/* MarkerToHeatArrays.interpolate_markers_to_transport_arrays!
+ *   (src/interpolation/utils/MarkerToHeatArrays.jl:29-35): backup+clear,
+ * numerators (BilinearNumerator.jl:31-141), averages (BilinearAverage.jl:10-50),
+ * thermal BC rows (ApplyThermalBC.jl:20-44).                                     */
+int eb_interpolate_marker_heat_parameters_to_grid(eb_ctx* ctx);
+
+/* BackupTransportArrays.backup_and_clear_viscosity_transport_arrays!
+ *   (src/interpolation/backup/BackupTransportArrays.jl:105-137)                  */
+int eb_backup_and_clear_viscosity_transport_arrays(eb_ctx* ctx);
+
+/* MarkersToStokesArrays.interpolate_viscosity_to_transport_arrays!
+ *   (MarkersToStokesArrays.jl:60-64 -> BilinearNumerator.jl:470-533, BilinearAverage.jl:213-227) */
+int eb_interpolate_viscosity_to_transport_arrays(eb_ctx* ctx);
+
+/* GridTemperatureToMarkers.interpolate!  (GridTemperatureToMarkers.jl:18-45)     */
+int eb_interpolate_temperature_to_markers(eb_ctx* ctx);
+
+/* Rheology.update_marker_rheology!  (src/rheology/Rheology.jl:37-56):
+ * FailureProperties.calculate_failure_properties_loop! (FailureProperties.jl:19-83) and
+ * CompositeViscosity.update_marker_flow_viscosity! (CompositeViscosity.jl:133-284). */
+int eb_update_marker_rheology(eb_ctx* ctx);
+
+/* Rheology.update_marker_viscoplastic_viscosity!  (Rheology.jl:70-107):
+ * ViscoplasticViscosity.jl:21-41, then (use_marker_plasticity != 0)
+ * ViscoelasticForecast.update_plastic_yielding! (ViscoelasticForecast.jl:11-123). */
+int eb_update_marker_viscoplastic_viscosity(eb_ctx* ctx, int use_marker_plasticity);
+
+/* MarkerPlasticity.update_plastic_yielding! alone (Picard iterations >= 2,
+ * PlasticityLoopMarkers.jl:52-57) -> ViscoelasticForecast.jl:11-123.            */
+int eb_update_plastic_yielding(eb_ctx* ctx);
+
+/* StokesContinuitySolver.execute_post_stokes_solver_steps! marker part
+ * (StokesContinuitySolver.jl:286-290): MarkerStrainRate.jl:23-69,
+ * MarkerStrainRateRatio.jl:191-271, MarkerPressure.jl:17-54, fused in one pass. */
+int eb_post_stokes_marker_gathers(eb_ctx* ctx);
+
+/* SubGridStress.Update.update_subgrid_stress!  (subgrid_stress/update/Update.jl:69-87) */
+int eb_update_subgrid_stress(eb_ctx* ctx);
+
+/* StressCorrection.apply_marker_stress_correction_for_remaining_grid_stress!
+ *   (subgrid_stress/stress_correction/StressCorrection.jl:35-82)                 */
+int eb_apply_marker_stress_correction(eb_ctx* ctx);
+
+/* SubgridDiffusion.subgrid_heat_diffusion_update! and
+ * remove_subgrid_effects_from_grid_changes!  (heat_solver/subgrid_heat/SubgridDiffusion.jl:59-195) */
+int eb_subgrid_heat_diffusion_update(eb_ctx* ctx);
+
+/* MarkerTemperature.add_remaining_grid_change_to_marker_temperature!
+ *   (heat_solver/marker_temperature/MarkerTemperature.jl:18-45)                  */
+int eb_add_remaining_grid_change_to_marker_temperature(eb_ctx* ctx);
+
+/* Advection.advect_markers_and_rotate_stress_tensor!  (src/advection/Advection.jl:109-114):
+ * VelocityAndSpin.update_marker_velocity_and_spin_using_runge_kutta! (VelocityAndSpin.jl:45-129),
+ * MarkersLocation.update! (MarkersLocation.jl:11-39), MarkersStressRotation.update!
+ * (MarkersStressRotation.jl:15-75), fused into one pass over the markers.        */
+int eb_advect_markers_and_rotate_stress(eb_ctx* ctx);
+
+/* Advection.update_marker_strain!  (Advection.jl:169-178 -> MarkersStrain.jl:11-136) */
+int eb_update_marker_strain(eb_ctx* ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* EBGPU_H */

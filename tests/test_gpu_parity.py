@@ -1,0 +1,387 @@
+"""GPU parity: every hot-path entry point, called through the C-ABI, against the CPU oracle.
+
+Contract (tolerances written here, applied entry by entry):
+  * inside flags and marker->cell indices (marker_xn/yn, marker_xn_vy/yn_vy): bit-exact;
+  * floating-point fields: |gpu - oracle| <= RTOL * S with RTOL = 1e-6, where S is
+    the magnitude of what the entry is made of:
+      - marker->grid averages: the same step run by the oracle on absolute values
+        (|w1 s1| + |w2 s2| + ... over w1 + w2 + ...), the classical bound of a
+        weighted sum; for a positive field S is the value itself (plain 1e-6
+        relative);
+      - grid->marker gathers: the largest |grid value| among the nodes the
+        marker interpolates from (a 5x5-node neighbourhood of its cell, which
+        covers the staggered and the RK4 intermediate cells), the usual error
+        scale of an interpolant;
+      - marker stresses: the stress magnitude, plus the local grid stress
+        magnitude where a step mixes grid stress into the marker;
+  * zero weight sums (empty nodes, which select the backup value) identical.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+RTOL = 1e-6
+
+
+def close(got, want, name, scale=None, rtol=RTOL):
+    """|got - want| <= rtol * scale entrywise; scale defaults to |want| (plain relative error)."""
+    got = np.asarray(got, dtype=np.float64)
+    want = np.asarray(want, dtype=np.float64)
+    assert got.shape == want.shape, name
+    s = np.abs(want) if scale is None else np.maximum(np.abs(np.asarray(scale, dtype=np.float64)), np.abs(want))
+    tol = rtol * s
+    bad = ~(np.abs(got - want) <= tol)
+    if bad.any():
+        i = np.flatnonzero(bad.ravel())[0]
+        rel = np.max(np.abs(got - want) / np.maximum(s, 1e-300))
+        raise AssertionError(f"{name}: {bad.sum()} of {want.size} entries out of tolerance; worst rel {rel:.3g}; "
+                             f"first at {i}: gpu {got.ravel()[i]!r} oracle {want.ravel()[i]!r} scale {s.ravel()[i]!r}")
+
+
+SIGNED_MARKER_FIELDS = ("sxx", "sxy", "exx", "exy", "subgrid_dt")
+SIGNED_GRID_FIELDS = ("sxx1", "sxy1", "sxx0", "sxy0", "exx", "exy", "sxx2", "sxy2", "dsxx", "dsxy", "dsxxn", "dsxyn",
+                      "dtk1", "dtkn", "vx1", "vy1", "esp", "pr1")
+
+
+def local_max(grid_values, ref):
+    """Largest |value| of a grid field in the 5x5-node neighbourhood of each marker's basic cell."""
+    from scipy.ndimage import maximum_filter
+    mx = maximum_filter(np.abs(np.asarray(grid_values)), size=5, mode="nearest")
+    yn = np.clip(ref.mk["yn"].astype(np.int64) - 1, 0, mx.shape[0] - 1)
+    xn = np.clip(ref.mk["xn"].astype(np.int64) - 1, 0, mx.shape[1] - 1)
+    out = mx[yn, xn]
+    out[ref.mk["inside"] != 1] = 0.0
+    return out
+
+
+def abs_model(model):
+    """The same model with every signed marker and grid field replaced by its absolute value:
+    the oracle run on it gives the magnitude S of each weighted sum."""
+    m = model.copy()
+    for k in SIGNED_MARKER_FIELDS:
+        if k in m.markers:
+            m.markers[k] = np.abs(m.markers[k])
+    for k in SIGNED_GRID_FIELDS:
+        if k in m.grids:
+            m.grids[k] = np.asfortranarray(np.abs(m.grids[k]))
+    return m
+
+
+@pytest.fixture(scope="module", params=["sinking_block", "rift_small"])
+def pair(request, eb, oracle):
+    eb.build()
+    model = eb.synthetic.config(request.param)
+    mic = eb.MarkerInCell(0)
+    mic.load_model(model)
+    ref = oracle.OracleMIC(model)
+    yield model, mic, ref
+    mic.close()
+
+
+def fresh(eb, oracle, model):
+    mic = eb.MarkerInCell(0)
+    mic.load_model(model)
+    return mic, oracle.OracleMIC(model)
+
+
+def locate_both(mic, ref):
+    mic.get_marker_inside_flags()
+    mic.initialize_bilinear_interpolation()
+    ref.get_marker_inside_flags()
+    ref.initialize_bilinear_interpolation()
+
+
+def test_inside_flags_and_cell_indices_bit_exact(eb, oracle, pair):
+    model, _, _ = pair
+    mic, ref = fresh(eb, oracle, model)
+    locate_both(mic, ref)
+    inside = ref.mk["inside"]
+    assert np.array_equal(mic.download_marker("inside"), inside)
+    sel = inside == 1
+    for f in ("xn", "yn", "xn_vy", "yn_vy"):
+        assert np.array_equal(mic.download_marker(f)[sel], ref.mk[f][sel]), f
+    mic.close()
+
+
+def test_cell_indices_on_grid_lines_and_edges(eb, oracle):
+    """Markers exactly on grid lines, on staggered lines and on the domain edges."""
+    model = eb.synthetic.config("sinking_block")
+    g = model.grid
+    rng = np.random.default_rng(5)
+    xs = np.concatenate([g.gridx_b, g.gridx_vy[1:-1], np.nextafter(g.gridx_b, -np.inf)[1:],
+                         np.nextafter(g.gridx_b, np.inf)[:-1]])
+    ys = np.concatenate([g.gridy_b, g.gridy_vx[1:-1], np.nextafter(g.gridy_b, np.inf)[:-1]])
+    n = model.marknum
+    x = rng.choice(xs, n)
+    y = rng.choice(ys, n)
+    x[:4] = [g.xmin, g.xmax, g.xmin - 1.0, g.xmax + 1e-9]
+    y[:4] = [g.ymin, g.ymax, g.ymax, g.ymin]
+    model.markers["x"], model.markers["y"] = x, y
+    mic, ref = fresh(eb, oracle, model)
+    locate_both(mic, ref)
+    assert np.array_equal(mic.download_marker("inside"), ref.mk["inside"])
+    sel = ref.mk["inside"] == 1
+    for f in ("xn", "yn", "xn_vy", "yn_vy"):
+        assert np.array_equal(mic.download_marker(f)[sel], ref.mk[f][sel]), f
+    # exclusive quadrants decided exactly: the viscosity scatter is sensitive to them
+    mic.interpolate_marker_stokes_parameters_to_grid()
+    ref.interpolate_marker_stokes_parameters_to_grid()
+    for f in ("wtetas", "etas1"):
+        close(mic.download_grid(f), ref.gr[f], f)
+    mic.close()
+
+
+def test_denominators(eb, oracle, pair):
+    model, _, _ = pair
+    mic, ref = fresh(eb, oracle, model)
+    locate_both(mic, ref)
+    for f in ("wtnodes", "wtetas", "wtetan", "wtnodes_vy"):
+        got = mic.download_grid(f)
+        assert np.array_equal(got == 0, ref.gr[f] == 0), f
+        close(got, ref.gr[f], f)
+    mic.close()
+
+
+STOKES_GRIDS = ["rho1", "rho0", "rho1_vy", "rho0_vy", "etas1", "etas0", "eta_flow", "eta_flow0", "mus1", "mus0",
+                "sxy1", "sxy0", "plastics", "cohesion_grid", "fric_degrees_grid", "etan1", "etan0", "mun1", "mun0",
+                "sxx1", "sxx0", "plasticn", "dilatation_grid", "extractable_meltfrac_grid"]
+
+
+def oracle_pair(oracle, model, steps):
+    """Run the oracle's steps on the model and on its absolute-value twin."""
+    ref, refa = oracle.OracleMIC(model), oracle.OracleMIC(abs_model(model))
+    for o in (ref, refa):
+        for st in steps:
+            getattr(o, st)()
+    return ref, refa
+
+
+def stress_scale(ref):
+    return np.hypot(ref.mk["sxx"], ref.mk["sxy"])
+
+
+def test_scatter_stokes(eb, oracle, pair):
+    model, _, _ = pair
+    mic = fresh(eb, oracle, model)[0]
+    steps = ["get_marker_inside_flags", "initialize_bilinear_interpolation",
+             "interpolate_marker_stokes_parameters_to_grid"]
+    for st in steps:
+        getattr(mic, st)()
+    ref, refa = oracle_pair(oracle, model, steps)
+    for f in STOKES_GRIDS:
+        close(mic.download_grid(f), ref.gr[f], f, scale=refa.gr[f])
+    mic.close()
+
+
+def test_scatter_heat(eb, oracle, pair):
+    model, _, _ = pair
+    mic, ref = fresh(eb, oracle, model)
+    locate_both(mic, ref)
+    mic.interpolate_marker_heat_parameters_to_grid()
+    ref.interpolate_marker_heat_parameters_to_grid()
+    for f in ("tk1", "tk0", "kt1", "kt0", "rhocp1", "hr1", "ha1"):
+        close(mic.download_grid(f), ref.gr[f], f)
+    mic.close()
+
+
+def test_viscosity_rescatter(eb, oracle, pair):
+    model, _, _ = pair
+    mic, ref = fresh(eb, oracle, model)
+    locate_both(mic, ref)
+    eta = model.markers["eta"] * np.exp(np.sin(np.arange(model.marknum)))
+    mic.upload_marker("eta", eta)
+    ref.mk["eta"][:] = eta
+    for o in (mic, ref):
+        o.backup_and_clear_viscosity_transport_arrays()
+        o.interpolate_viscosity_to_transport_arrays()
+    for f in ("etas1", "etas0", "etan1", "etan0"):
+        close(mic.download_grid(f), ref.gr[f], f)
+    mic.close()
+
+
+def test_gathers(eb, oracle, pair):
+    model, _, _ = pair
+    mic = fresh(eb, oracle, model)[0]
+    steps = ["get_marker_inside_flags", "initialize_bilinear_interpolation", "post_stokes_marker_gathers"]
+    for st in steps:
+        getattr(mic, st)()
+    ref, refa = oracle_pair(oracle, model, steps)
+    for f in ("exx", "exy", "pr"):
+        close(mic.download_marker(f), ref.mk[f], f, scale=local_max(model.grids[f if f != "pr" else "pr1"], ref))
+    # the strain-rate ratio divides stress-based by velocity-based invariants built from
+    # gathers: its error scale is the ratio of the local magnitudes
+    e_loc = np.hypot(local_max(model.grids["exx"], ref), local_max(model.grids["exy"], ref))
+    e_here = np.maximum(np.hypot(ref.mk["exx"], ref.mk["exy"]), 1e-300)
+    close(mic.download_marker("sr_ratio"), ref.mk["sr_ratio"], "sr_ratio", scale=ref.mk["sr_ratio"] * e_loc / e_here)
+    mic.upload_grid("tk1", model.grids["tk2"])
+    ref.gr["tk1"][:] = model.grids["tk2"]
+    mic.interpolate_temperature_to_markers()
+    ref.interpolate_temperature_to_markers()
+    close(mic.download_marker("tk"), ref.mk["tk"], "tk")
+    mic.close()
+
+
+def test_subgrid_stress_and_correction(eb, oracle, pair):
+    model, _, _ = pair
+    mic = fresh(eb, oracle, model)[0]
+    steps = ["get_marker_inside_flags", "initialize_bilinear_interpolation", "update_subgrid_stress"]
+    for st in steps:
+        getattr(mic, st)()
+    ref, refa = oracle_pair(oracle, model, steps)
+    s_loc = stress_scale(ref) + np.hypot(local_max(model.grids["sxx1"], ref), local_max(model.grids["sxy1"], ref))
+    for f in ("sxx", "sxy"):
+        close(mic.download_marker(f), ref.mk[f], f, scale=s_loc)
+    for f in ("dsxyn", "dsxxn"):
+        close(mic.download_grid(f), ref.gr[f], f, scale=refa.gr[f])
+    for f, fn in (("dsxy", "dsxyn"), ("dsxx", "dsxxn")):
+        close(mic.download_grid(f), ref.gr[f], f, scale=np.abs(model.grids[f]) + refa.gr[fn])
+    for f in ("wtetas", "wtetan"):
+        close(mic.download_grid(f), ref.gr[f], f)
+    mic.apply_marker_stress_correction()
+    ref.apply_marker_stress_correction()
+    s_loc = s_loc + np.hypot(local_max(ref.gr["dsxx"], ref), local_max(ref.gr["dsxy"], ref))
+    for f in ("sxx", "sxy"):
+        close(mic.download_marker(f), ref.mk[f], f, scale=s_loc)
+    mic.close()
+
+
+def test_subgrid_heat_and_remaining_dt(eb, oracle, pair):
+    """The subgrid temperature change is a correction to the temperature: its
+    tolerance is relative to the temperature it corrects."""
+    model, _, _ = pair
+    mic, ref = fresh(eb, oracle, model)
+    locate_both(mic, ref)
+    for o in (mic, ref):
+        o.interpolate_marker_heat_parameters_to_grid()
+        o.subgrid_heat_diffusion_update()
+    close(mic.download_marker("subgrid_dt"), ref.mk["subgrid_dt"], "subgrid_dt", scale=ref.mk["tk"])
+    close(mic.download_marker("tk"), ref.mk["tk"], "tk")
+    close(mic.download_grid("wtnodes"), ref.gr["wtnodes"], "wtnodes")
+    for f in ("dtkn", "dtk1"):
+        close(mic.download_grid(f), ref.gr[f], f, scale=ref.gr["tk1"])
+    for o in (mic, ref):
+        o.add_remaining_grid_change_to_marker_temperature()
+    close(mic.download_marker("tk"), ref.mk["tk"], "tk")
+    mic.close()
+
+
+def test_advection_rk4(eb, oracle, pair):
+    model, _, _ = pair
+    mic = fresh(eb, oracle, model)[0]
+    steps = ["get_marker_inside_flags", "initialize_bilinear_interpolation", "advect_markers_and_rotate_stress"]
+    for st in steps:
+        getattr(mic, st)()
+    ref, refa = oracle_pair(oracle, model, steps)
+    vscale = {"vx": local_max(model.grids["vx1"], ref), "vy": local_max(model.grids["vy1"], ref),
+              "spin": local_max(model.grids["esp"], ref)}
+    for f in ("vx", "vy", "spin"):
+        close(mic.download_marker(f), ref.mk[f], f, scale=vscale[f])
+    # positions: the displacement dt*v within RTOL of dt times the local velocity magnitude
+    dt = model.params["timestep"]
+    for f, v in (("x", "vx"), ("y", "vy")):
+        f0 = model.markers[f]
+        close(mic.download_marker(f) - f0, ref.mk[f] - f0, f + " displacement", scale=dt * vscale[v])
+    for f in ("sxx", "sxy"):
+        close(mic.download_marker(f), ref.mk[f], f, scale=stress_scale(ref))
+    mic.close()
+
+
+def test_strain_update(eb, oracle, pair):
+    model, _, _ = pair
+    mic, ref = fresh(eb, oracle, model)
+    for o in (mic, ref):
+        o.get_marker_inside_flags()
+        o.update_marker_strain()
+    for f in ("gii", "strain_plastic", "strain_rate_plastic"):
+        close(mic.download_marker(f), ref.mk[f], f)
+    mic.close()
+
+
+def test_rheology(eb, oracle):
+    model = eb.synthetic.config("rift_small")
+    mic, ref = fresh(eb, oracle, model)
+    for o in (mic, ref):
+        o.get_marker_inside_flags()
+        o.update_marker_rheology()
+    for f in ("cohesion", "fric", "preexp"):
+        close(mic.download_marker(f), ref.mk[f], f, rtol=1e-12)
+    close(mic.download_marker("eta_flow"), ref.mk["eta_flow"], "eta_flow")
+    for o in (mic, ref):
+        o.update_marker_viscoplastic_viscosity(use_marker_plasticity=True)
+    close(mic.download_marker("eta"), ref.mk["eta"], "eta")
+    for f in ("sxx", "sxy"):
+        close(mic.download_marker(f), ref.mk[f], f, scale=stress_scale(ref))
+    assert np.array_equal(mic.download_marker("pfailure"), ref.mk["pfailure"])
+    mic.close()
+
+
+def test_full_marker_cycle(eb, oracle, pair):
+    model, _, _ = pair
+    mic = fresh(eb, oracle, model)[0]
+    mic.marker_cycle()
+    ref, refa = oracle_pair(oracle, model, ["marker_cycle"])
+    loc = {f: local_max(model.grids[g], ref) for f, g in (("vx", "vx1"), ("vy", "vy1"), ("exx", "exx"),
+                                                           ("exy", "exy"), ("pr", "pr1"))}
+    for f in ("vx", "vy", "exx", "exy", "pr"):
+        close(mic.download_marker(f), ref.mk[f], f, scale=loc[f])
+    s_loc = stress_scale(ref) + np.hypot(local_max(ref.gr["sxx1"], ref), local_max(ref.gr["sxy1"], ref)) + \
+        np.hypot(local_max(ref.gr["dsxx"], ref), local_max(ref.gr["dsxy"], ref))
+    for f in ("sxx", "sxy"):
+        close(mic.download_marker(f), ref.mk[f], f, scale=s_loc)
+    for f in ("tk", "gii"):
+        close(mic.download_marker(f), ref.mk[f], f)
+    dt = model.params["timestep"]
+    for f in ("x", "y"):
+        f0 = model.markers[f]
+        close(mic.download_marker(f) - f0, ref.mk[f] - f0, f + " displacement", scale=dt * loc["v" + f])
+    for f in ("rho1", "etas1", "etan1", "tk1"):
+        close(mic.download_grid(f), ref.gr[f], f)
+    close(mic.download_grid("dtk1"), ref.gr["dtk1"], "dtk1", scale=ref.gr["tk1"])
+    close(mic.download_grid("dsxy"), ref.gr["dsxy"], "dsxy", scale=np.abs(model.grids["dsxy"]) + refa.gr["dsxyn"])
+    mic.close()
+
+
+def test_deterministic(eb, oracle):
+    model = eb.synthetic.config("rift_small")
+    outs = []
+    for _ in range(2):
+        mic = eb.MarkerInCell(0)
+        mic.load_model(model)
+        mic.marker_cycle()
+        outs.append({f: mic.download_marker(f) for f in ("x", "y", "sxx", "tk")} |
+                    {f: mic.download_grid(f) for f in ("rho1", "etas1", "tk1", "dsxyn")})
+        mic.close()
+    for k in outs[0]:
+        assert np.array_equal(outs[0][k], outs[1][k]), k
+
+
+def test_empty_and_all_outside(eb, oracle):
+    model = eb.synthetic.config("sinking_block")
+    mic = eb.MarkerInCell(0)
+    mic.load_model(model)
+    mic.upload_marker("x", np.full(model.marknum, -1e9))  # every marker outside the domain
+    mic.marker_cycle()
+    assert np.all(mic.download_marker("inside") == -1)
+    rho_before = model.grids["rho1"]
+    np.testing.assert_array_equal(mic.download_grid("rho1"), rho_before)  # empty nodes keep the backup
+    mic.resize_markers(0)
+    mic.marker_cycle()
+    mic.close()
+
+
+def test_errors_are_reported_not_raised_on_device(eb):
+    model = eb.synthetic.config("sinking_block")
+    mic = eb.MarkerInCell(0)
+    mic.set_grid(model.grid)
+    mic.set_params(model.params)
+    with pytest.raises(eb.EarthBoxGPUError) as e:
+        mic.interpolate_marker_stokes_parameters_to_grid()  # no materials, not located
+    assert e.value.code in (3, 5)
+    mic.set_materials(model.mats)
+    mic.resize_markers(model.marknum)
+    bad = model.markers["matid"].copy()
+    bad[7] = 99
+    with pytest.raises(eb.EarthBoxGPUError):
+        mic.upload_marker("matid", bad)
+    mic.close()
