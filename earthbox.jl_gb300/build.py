@@ -16,7 +16,8 @@ ROOT = PKG.parent
 CSRC = PKG / "csrc"
 BUILD = PKG / "_build"
 LIB = BUILD / "libebgpu.so"
-SOURCES = ["eb_ctx.cu", "eb_locate.cu", "eb_scatter.cu", "eb_gather.cu", "eb_advect.cu", "eb_rheology.cu"]
+SOURCES = ["eb_ctx.cu", "eb_locate.cu", "eb_scatter.cu", "eb_gather.cu", "eb_advect.cu", "eb_rheology.cu",
+           "eb_noalloc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall"]
 

@@ -1,0 +1,242 @@
+// eb_noalloc.cu -- marker -> basic-grid bilinear average that allocates no device memory.
+//
+// Some callers cannot call cudaMalloc: a host program whose device memory is
+// owned by another allocator (a Julia or Python memory pool handing out
+// buffers), a code path that runs while allocation is forbidden or would
+// stall (a stream-ordered pipeline, a tight real-time loop), or a process
+// whose device-memory budget is fixed up front.  This entry point serves them:
+// the caller passes every input and output as device pointers, and the only
+// working memory is a file-scope static __device__ array of kNoAllocScratchBytes
+// (16 MiB).  Every GPU that loads the library holds that array until the
+// process exits.
+//
+// It computes one inclusive bilinear average on the basic grid, the operation
+// of BilinearNumerator (update_weight_inclusive!) + BilinearAverage
+// (calc_bilinear_average_arithmetic!) for a field such as density or
+// temperature, deterministically: markers are grouped by cell with their
+// marker order kept, each cell folds its markers in that order, and nodes sum
+// their four cells in a fixed order.
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include "eb_internal.h"
+
+namespace {
+
+constexpr int64_t kMaxMarkers = 1 << 19;  // 524,288 markers
+constexpr int64_t kMaxCells = 1 << 17;    // 131,072 basic cells
+// Scratch layout (bytes): per marker key/fx/fy/perm_tmp/perm (5 x 4), per cell
+// count/start/cursor (3 x 4, plus one) and 8 partial sums (8 x 4).
+constexpr size_t kMarkerBytes = (size_t)kMaxMarkers * 5 * 4;
+constexpr size_t kCellBytes = (size_t)(kMaxCells + 1) * 3 * 4 + (size_t)kMaxCells * 8 * 4;
+constexpr size_t kNoAllocScratchBytes = 16u << 20;
+static_assert(kMarkerBytes + kCellBytes + 1024 <= kNoAllocScratchBytes, "scratch layout exceeds the array");
+
+static __device__ __align__(256) unsigned char g_scratch[kNoAllocScratchBytes];
+
+struct Scratch {
+  int32_t *key, *perm_tmp, *perm, *count, *start, *cursor;
+  float *fx, *fy, *part;
+};
+
+Scratch carve(unsigned char* base) {
+  Scratch s;
+  size_t o = 0;
+  auto take = [&](size_t bytes) { unsigned char* p = base + o; o += (bytes + 255) & ~size_t(255); return p; };
+  s.key = (int32_t*)take(kMaxMarkers * 4);
+  s.fx = (float*)take(kMaxMarkers * 4);
+  s.fy = (float*)take(kMaxMarkers * 4);
+  s.perm_tmp = (int32_t*)take(kMaxMarkers * 4);
+  s.perm = (int32_t*)take(kMaxMarkers * 4);
+  s.count = (int32_t*)take((kMaxCells + 1) * 4);
+  s.start = (int32_t*)take((kMaxCells + 1) * 4);
+  s.cursor = (int32_t*)take((kMaxCells + 1) * 4);
+  s.part = (float*)take(kMaxCells * 8 * 4);
+  return s;
+}
+
+// searchsortedlast on a device coordinate array by order keys (exact).
+__device__ int32_t search(const double* __restrict__ v, int32_t n, double x) {
+  const uint64_t kx = dkey(x);
+  int32_t lo = 0, hi = n + 1;
+  while (hi - lo > 1) {
+    const int32_t mid = (lo + hi) >> 1;
+    if (kx < dkey(__ldg(&v[mid - 1]))) hi = mid; else lo = mid;
+  }
+  return lo;
+}
+
+__global__ void k_na_locate(const double* __restrict__ x, const double* __restrict__ y, int32_t M,
+                            const double* __restrict__ gx, int32_t xnum, const double* __restrict__ gy, int32_t ynum,
+                            Scratch s) {
+  const int32_t m = blockIdx.x * blockDim.x + threadIdx.x;
+  int32_t key = -1;
+  if (m < M) {
+    const double xm = x[m], ym = y[m];
+    const uint64_t kx = dkey(xm), ky = dkey(ym);
+    const bool in = dkey(gx[0]) <= kx && kx <= dkey(gx[xnum - 1]) && dkey(gy[0]) <= ky && ky <= dkey(gy[ynum - 1]);
+    if (in) {
+      const int32_t ix = clamp_i(search(gx, xnum, xm), 1, xnum - 1);
+      const int32_t iy = clamp_i(search(gy, ynum, ym), 1, ynum - 1);
+      const double x0 = gx[ix - 1], y0 = gy[iy - 1];
+      s.fx[m] = (float)((xm - x0) / (gx[ix] - x0));
+      s.fy[m] = (float)((ym - y0) / (gy[iy] - y0));
+      key = (ix - 1) * (ynum - 1) + (iy - 1);
+    }
+    s.key[m] = key;
+  }
+  const unsigned peers = __match_any_sync(0xffffffffu, key);
+  if (key >= 0 && (int)(threadIdx.x & 31) == __ffs(peers) - 1) atomicAdd(&s.count[key], __popc(peers));
+}
+
+// Exclusive scan of count[0..n) into start[0..n] by one block (n <= kMaxCells + 1).
+__global__ void k_na_scan(Scratch s, int32_t n) {
+  __shared__ int32_t warp_sums[32];
+  __shared__ int32_t carry;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  if (threadIdx.x == 0) carry = 0;
+  __syncthreads();
+  for (int32_t base = 0; base < n; base += blockDim.x) {
+    const int32_t i = base + threadIdx.x;
+    const int32_t v = i < n ? s.count[i] : 0;
+    int32_t inc = v;
+    for (int o = 1; o < 32; o <<= 1) {
+      const int32_t t = __shfl_up_sync(0xffffffffu, inc, o);
+      if (lane >= o) inc += t;
+    }
+    if (lane == 31) warp_sums[wid] = inc;
+    __syncthreads();
+    if (wid == 0) {
+      int32_t w = lane < nw ? warp_sums[lane] : 0;
+      for (int o = 1; o < 32; o <<= 1) {
+        const int32_t t = __shfl_up_sync(0xffffffffu, w, o);
+        if (lane >= o) w += t;
+      }
+      if (lane < nw) warp_sums[lane] = w;
+    }
+    __syncthreads();
+    const int32_t c0 = carry;
+    if (i < n) s.start[i] = c0 + (wid ? warp_sums[wid - 1] : 0) + inc - v;
+    __syncthreads();
+    if (threadIdx.x == 0) carry = c0 + warp_sums[nw - 1];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) s.start[n] = carry;
+}
+
+__global__ void k_na_place(int32_t M, Scratch s) {
+  const int32_t m = blockIdx.x * blockDim.x + threadIdx.x;
+  const int32_t key = m < M ? s.key[m] : -1;
+  const unsigned peers = __match_any_sync(0xffffffffu, key);
+  const int lane = threadIdx.x & 31, leader = __ffs(peers) - 1;
+  int32_t base = 0;
+  if (key >= 0 && lane == leader) base = atomicAdd(&s.cursor[key], __popc(peers));
+  base = __shfl_sync(0xffffffffu, base, leader);
+  if (key >= 0) s.perm_tmp[s.start[key] + base + __popc(peers & ((1u << lane) - 1u))] = m;
+}
+
+__global__ void k_na_sort(int32_t nc, Scratch s) {
+  const int32_t cell = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (cell >= nc) return;
+  const int32_t beg = s.start[cell], n = s.start[cell + 1] - beg;
+  for (int32_t i = lane; i < n; i += 32) {
+    const int32_t v = s.perm_tmp[beg + i];
+    int32_t r = 0;
+    for (int32_t j = 0; j < n; ++j) r += (s.perm_tmp[beg + j] < v);
+    s.perm[beg + r] = v;
+  }
+}
+
+// One thread per cell: fold the cell's markers in marker order into the four
+// corners' w*value and w sums.
+__global__ void k_na_cells(const double* __restrict__ value, int32_t nc, Scratch s) {
+  const int32_t cell = blockIdx.x * blockDim.x + threadIdx.x;
+  if (cell >= nc) return;
+  KSum a[8];
+  for (int k = 0; k < 8; ++k) a[k].init();
+  for (int32_t k = s.start[cell]; k < s.start[cell + 1]; ++k) {
+    const int32_t m = s.perm[k];
+    const W4 w = wts(s.fx[m], s.fy[m]);
+    const float v = (float)value[m];
+    a[0].add(w.ul * v); a[1].add(w.ll * v); a[2].add(w.ur * v); a[3].add(w.lr * v);
+    a[4].add(w.ul); a[5].add(w.ll); a[6].add(w.ur); a[7].add(w.lr);
+  }
+  for (int k = 0; k < 8; ++k) s.part[(size_t)k * nc + cell] = a[k].get();
+}
+
+// Node (i, j) is UL of cell (i, j), LL of (i-1, j), UR of (i, j-1), LR of (i-1, j-1).
+__global__ void k_na_finish(int32_t xnum, int32_t ynum, Scratch s, double* __restrict__ avg,
+                            double* __restrict__ wsum) {
+  const int32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= xnum * ynum) return;
+  const int32_t i = t % ynum + 1, j = t / ynum + 1, nc = (xnum - 1) * (ynum - 1);
+  KSum num, den;
+  num.init();
+  den.init();
+  auto add = [&](int32_t ci, int32_t cj, int corner) {
+    const int32_t c = (cj - 1) * (ynum - 1) + (ci - 1);
+    num.add(s.part[(size_t)corner * nc + c]);
+    den.add(s.part[(size_t)(4 + corner) * nc + c]);
+  };
+  if (i > 1 && j > 1) add(i - 1, j - 1, 3);
+  if (i < ynum && j > 1) add(i, j - 1, 2);
+  if (i > 1 && j < xnum) add(i - 1, j, 1);
+  if (i < ynum && j < xnum) add(i, j, 0);
+  const float n = num.get(), d = den.get();
+  wsum[t] = (double)d;
+  if (d != 0.f) avg[t] = (double)(n / d);  // else: keep the caller's previous value (the backup)
+}
+
+std::mutex g_mutex;
+void* g_scratch_ptr[256];  // per device, resolved once with that device current
+
+}  // namespace
+
+// Documented in include/ebgpu.h.
+extern "C" int eb_marker_to_basic_grid_average_noalloc(const double* d_marker_x, const double* d_marker_y,
+                                                       const double* d_marker_value, int64_t marknum,
+                                                       const double* d_gridx_b, int64_t xnum,
+                                                       const double* d_gridy_b, int64_t ynum, double* d_avg,
+                                                       double* d_wsum, void* stream, char* errbuf,
+                                                       size_t errlen) {
+  auto fail = [&](int code, const char* msg) {
+    if (errbuf && errlen) std::snprintf(errbuf, errlen, "%s", msg);
+    return code;
+  };
+  if (marknum < 0 || marknum > kMaxMarkers) return fail(EB_BAD_INPUT, "marknum exceeds the no-alloc limit of 524288 markers");
+  if (xnum < 2 || ynum < 2) return fail(EB_BAD_INPUT, "xnum and ynum must be >= 2");
+  if ((xnum - 1) * (ynum - 1) > kMaxCells) return fail(EB_BAD_INPUT, "(xnum-1)*(ynum-1) exceeds the no-alloc limit of 131072 cells");
+  if (!d_gridx_b || !d_gridy_b || !d_avg || !d_wsum || (marknum > 0 && (!d_marker_x || !d_marker_y || !d_marker_value)))
+    return fail(EB_BAD_INPUT, "null device pointer");
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 256) return fail(EB_CUDA_ERROR, "cudaGetDevice failed");
+  void* base = nullptr;
+  {
+    std::lock_guard<std::mutex> lock(g_mutex);
+    if (!g_scratch_ptr[dev]) {  // first call on this device: resolve the array's device address
+      void* p = nullptr;
+      const cudaError_t e = cudaGetSymbolAddress(&p, g_scratch);
+      if (e != cudaSuccess) return fail(EB_CUDA_ERROR, cudaGetErrorString(e));
+      g_scratch_ptr[dev] = p;
+    }
+    base = g_scratch_ptr[dev];
+  }
+  const Scratch s = carve((unsigned char*)base);
+  cudaStream_t st = (cudaStream_t)stream;
+  const int32_t M = (int32_t)marknum, X = (int32_t)xnum, Y = (int32_t)ynum, nc = (X - 1) * (Y - 1);
+  // the array keeps the previous call's contents: clear the counters this call accumulates into
+  if (cudaMemsetAsync(s.count, 0, (nc + 1) * sizeof(int32_t), st) != cudaSuccess ||
+      cudaMemsetAsync(s.cursor, 0, (nc + 1) * sizeof(int32_t), st) != cudaSuccess)
+    return fail(EB_CUDA_ERROR, "cudaMemsetAsync failed");
+  const unsigned mb = (unsigned)((M + 255) / 256);
+  if (M > 0) k_na_locate<<<mb, 256, 0, st>>>(d_marker_x, d_marker_y, M, d_gridx_b, X, d_gridy_b, Y, s);
+  k_na_scan<<<1, 1024, 0, st>>>(s, nc);
+  if (M > 0) k_na_place<<<mb, 256, 0, st>>>(M, s);
+  k_na_sort<<<(unsigned)(((int64_t)nc * 32 + 255) / 256), 256, 0, st>>>(nc, s);
+  k_na_cells<<<(unsigned)((nc + 255) / 256), 256, 0, st>>>(d_marker_value, nc, s);
+  k_na_finish<<<(unsigned)((X * Y + 255) / 256), 256, 0, st>>>(X, Y, s, d_avg, d_wsum);
+  const cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return fail(EB_CUDA_ERROR, cudaGetErrorString(e));
+  return EB_OK;
+}

@@ -247,6 +247,31 @@ int eb_advect_markers_and_rotate_stress(eb_ctx* ctx);
 /* Advection.update_marker_strain!  (Advection.jl:169-178 -> MarkersStrain.jl:11-136) */
 int eb_update_marker_strain(eb_ctx* ctx);
 
+/* ---- allocation-free entry point -------------------------------------------
+ * No counterpart in the reference.  For callers that cannot call cudaMalloc
+ * (their device memory belongs to another allocator, or allocating is not
+ * allowed where they run): the inclusive bilinear average of one marker field
+ * on the basic grid (the operation of BilinearNumerator's inclusive update and
+ * BilinearAverage.calc_bilinear_average_arithmetic!), computed without
+ * allocating device memory.  All pointers are device pointers owned by the
+ * caller: marker x, y and value (marknum doubles), gridx_b (xnum), gridy_b
+ * (ynum); d_avg and d_wsum are (ynum, xnum) column-major grids, written on
+ * return; nodes with a zero weight sum keep d_avg's previous value.
+ * Working memory is one static 16 MiB device array that every GPU loading the
+ * library holds until the process exits: marknum <= EB_NOALLOC_MAX_MARKERS and
+ * (xnum-1)*(ynum-1) <= EB_NOALLOC_MAX_CELLS, else EB_BAD_INPUT with a message
+ * in errbuf.  The first call on a device resolves the array's device address
+ * (cudaGetSymbolAddress) with that device current; make that first call
+ * before any stream capture.  Work is queued on `stream` (a cudaStream_t, 0 =
+ * default) without synchronising.  All calls share the one array, so calls
+ * that overlap on the GPU (different streams, or another host thread) race.  */
+#define EB_NOALLOC_MAX_MARKERS 524288
+#define EB_NOALLOC_MAX_CELLS   131072
+int eb_marker_to_basic_grid_average_noalloc(
+    const double* d_marker_x, const double* d_marker_y, const double* d_marker_value, int64_t marknum,
+    const double* d_gridx_b, int64_t xnum, const double* d_gridy_b, int64_t ynum,
+    double* d_avg, double* d_wsum, void* stream, char* errbuf, size_t errlen);
+
 #ifdef __cplusplus
 }
 #endif
