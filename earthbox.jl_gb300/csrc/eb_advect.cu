@@ -22,11 +22,6 @@ namespace {
 
 constexpr int kBlock = 256;
 
-__global__ void k_to_float(const double* __restrict__ a, float* __restrict__ b, int64_t n) {
-  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) b[i] = (float)a[i];
-}
-
 struct VelGrids {
   const float *vx1, *vy1, *esp;
   float dt;
@@ -103,12 +98,13 @@ __global__ void k_advect(DevMarkers mk, DevGrid g, VelGrids V) {
     vym = (v1y + 2.f * v2y + 2.f * v3y + v4y) / 6.f;
     spm = (s1 + 2.f * s2 + 2.f * s3 + s4) / 6.f;
   }
-  mk.vx[m] = (double)vxm;
-  mk.vy[m] = (double)vym;
-  mk.spin[m] = (double)spm;
+  const double vxd = f2d(vxm), vyd = f2d(vym);
+  mk.vx[m] = vxd;
+  mk.vy[m] = vyd;
+  mk.spin[m] = f2d(spm);
   // MarkersLocation.advect_marker: x + timestep * v (FP64)
-  mk.x[m] = fma(V.dtd, (double)vxm, mk.x[m]);
-  mk.y[m] = fma(V.dtd, (double)vym, mk.y[m]);
+  mk.x[m] = fma(V.dtd, vxd, mk.x[m]);
+  mk.y[m] = fma(V.dtd, vyd, mk.y[m]);
   // MarkersStressRotation.rotate_marker_stress, written as increments:
   //   sxy' = sxy + sxx sin(2w) + sxy (cos(2w) - 1),  sxx' = sxx + sxx (cos(2w) - 1) - sxy sin(2w)
   // with cos(2w) - 1 = -2 sin(w)^2 evaluated without cancellation.
@@ -116,27 +112,27 @@ __global__ void k_advect(DevMarkers mk, DevGrid g, VelGrids V) {
   const float s2w = sinf(2.f * w), sw = sinf(w);
   const float c2m1 = -2.f * sw * sw;
   const double sxx = mk.sxx[m], sxy = mk.sxy[m];
-  const float fxx = (float)sxx, fxy = (float)sxy;
-  mk.sxy[m] = sxy + (double)(fxx * s2w + fxy * c2m1);
-  mk.sxx[m] = sxx + (double)(fxx * c2m1 - fxy * s2w);
+  const float fxx = d2f(sxx), fxy = d2f(sxy);
+  mk.sxy[m] = sxy + f2d(fxx * s2w + fxy * c2m1);
+  mk.sxx[m] = sxx + f2d(fxx * c2m1 - fxy * s2w);
 }
 
 // MarkersStrain.update_total_strain! and update_plastic_strain!
 __global__ void k_strain(DevMarkers mk, double dt, double healing) {
   const int64_t m = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (m >= mk.M || mk.inside[m] != 1) return;
-  const float eii = hypotf((float)mk.exx[m], (float)mk.exy[m]);
-  mk.gii[m] = fma(dt, (double)eii, mk.gii[m]);
+  const float eii = hypotf(d2f(mk.exx[m]), d2f(mk.exy[m]));
+  mk.gii[m] = fma(dt, f2d(eii), mk.gii[m]);
   if (mk.pfailure[m] != 1.0f) return;
   const double eta = mk.eta[m], eta_flow = mk.eta_flow[m];
-  const float sii = hypotf((float)mk.sxx[m], (float)mk.sxy[m]);
+  const float sii = hypotf(d2f(mk.sxx[m]), d2f(mk.sxy[m]));
   // 0.5 sii (1/eta - 1/eta_flow) = 0.5 sii ((eta_flow - eta) / eta) / eta_flow
-  const float d = (float)(eta_flow - eta);
-  float rate = 0.5f * sii * ((d / (float)eta) / (float)eta_flow);
+  const float d = d2f(eta_flow - eta);
+  float rate = 0.5f * sii * ((d / d2f(eta)) / d2f(eta_flow));
   rate = fmaxf(0.f, rate);
-  double sp = mk.sp[m] + dt * (double)rate - healing * dt;
+  double sp = mk.sp[m] + dt * f2d(rate) - healing * dt;
   mk.sp[m] = sp > 0.0 ? sp : 0.0;
-  mk.srp[m] = (double)rate;
+  mk.srp[m] = f2d(rate);
 }
 
 }  // namespace
@@ -150,23 +146,10 @@ int launch_advect(eb_ctx* c) {
   for (int f : mf) if ((rc = ensure_marker_field(c, f))) return rc;
   if ((rc = ensure_grid_field(c, EB_G_VX1)) || (rc = ensure_grid_field(c, EB_G_VY1)) || (rc = ensure_grid_field(c, EB_G_ESP)))
     return rc;
-  const int64_t nvx = grid_field_count(c, EB_G_VX1), nvy = grid_field_count(c, EB_G_VY1), nb = grid_field_count(c, EB_G_ESP);
-  if (!c->vx1f) {
-    EB_CK(c, cudaMalloc(&c->vx1f, nvx * sizeof(float)));
-    EB_CK(c, cudaMalloc(&c->vy1f, nvy * sizeof(float)));
-    EB_CK(c, cudaMalloc(&c->espf, nb * sizeof(float)));
-  }
-  EB_PROF(c, "k_to_float");
-  k_to_float<<<(unsigned)((nvx + 255) / 256), 256, 0, c->stream>>>(c->gf[EB_G_VX1], c->vx1f, nvx);
-  EB_LAUNCHED(c);
-  EB_PROF(c, "k_to_float");
-  k_to_float<<<(unsigned)((nvy + 255) / 256), 256, 0, c->stream>>>(c->gf[EB_G_VY1], c->vy1f, nvy);
-  EB_LAUNCHED(c);
-  EB_PROF(c, "k_to_float");
-  k_to_float<<<(unsigned)((nb + 255) / 256), 256, 0, c->stream>>>(c->gf[EB_G_ESP], c->espf, nb);
-  EB_LAUNCHED(c);
   if (c->M == 0) return EB_OK;
-  VelGrids V{c->vx1f, c->vy1f, c->espf, (float)c->P.timestep, c->P.timestep, (int)order};
+  const float* f[3];
+  if ((rc = grid_f32(c, {EB_G_VX1, EB_G_VY1, EB_G_ESP}, f))) return rc;
+  VelGrids V{f[0], f[1], f[2], (float)c->P.timestep, c->P.timestep, (int)order};
   EB_PROF(c, "k_advect");
   k_advect<<<(unsigned)((c->M + kBlock - 1) / kBlock), kBlock, 0, c->stream>>>(dev_markers(c), c->g, V);
   EB_LAUNCHED(c);

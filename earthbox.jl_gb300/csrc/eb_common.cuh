@@ -30,6 +30,33 @@ __host__ __device__ __forceinline__ uint64_t dkey(double v) {
   return (u >> 63) ? ~u : (u | 0x8000000000000000ull);
 }
 
+// ---- FP64 <-> FP32 conversion with integer operations ---------------------------
+// On GB300 the F2F conversion instructions issue on the FP64 pipe (0.5 T op/s,
+// measured: a gather kernel doing ~33 conversions per marker ran with that pipe
+// 95% busy), so the hot kernels convert with 32-bit integer operations instead.
+// d2f rounds to nearest (a tie rounds away from zero, IEEE rounds it to even:
+// the two differ by one FP32 ulp on exact ties only); magnitudes below FLT_MIN
+// become a signed zero, above FLT_MAX infinity.  Every value on this path lies
+// well inside the FP32 range.
+EB_DEV float d2f(double d) {
+  const uint32_t hi = (uint32_t)__double2hiint(d), lo = (uint32_t)__double2loint(d);
+  const int32_t e = (int32_t)((hi >> 20) & 0x7FFu) - 896;  // FP32 exponent field
+  uint32_t bits = ((uint32_t)e << 23) + (((hi & 0xFFFFFu) << 3) | (lo >> 29)) + ((lo >> 28) & 1u);
+  bits = (e <= 0) ? 0u : ((e >= 255) ? 0x7F800000u : bits);
+  return __uint_as_float((hi & 0x80000000u) | bits);
+}
+// Exact FP32 -> FP64 widening (FP32 subnormals, never produced here, become zero).
+EB_DEV double f2d(float f) {
+  const uint32_t b = __float_as_uint(f);
+  const uint32_t ex = (b >> 23) & 0xFFu, man = b & 0x7FFFFFu;
+  uint32_t hi = b & 0x80000000u, lo = 0u;
+  if (ex != 0u) {
+    hi |= ((ex == 255u ? 2047u : ex + 896u) << 20) | (man >> 3);
+    lo = man << 29;
+  }
+  return __hiloint2double((int)hi, (int)lo);
+}
+
 // ---- exact searchsortedlast with a bucket accelerator ------------------------
 // A 1-D grid coordinate array v[1..n] (stored 0-based) is described by its keys
 // and by a table that maps a uniform bucket over [v1, vn] to the
@@ -47,7 +74,7 @@ struct Axis {
 EB_DEV int32_t axis_search(const Axis& a, double x) {
   const uint64_t kx = dkey(x);
   // clamp before the conversion (fmaxf maps NaN to 0), so b is always in [0, nb]
-  const float t = fminf(fmaxf(((float)x - a.v0) * a.inv_h, 0.f), (float)a.nb);
+  const float t = fminf(fmaxf((d2f(x) - a.v0) * a.inv_h, 0.f), (float)a.nb);
   const int32_t b = (int32_t)t;
   int32_t i = __ldg(&a.bucket[b]);
   // walk up while v[i+1] <= x, then down while v[i] > x (1-based indices)
@@ -95,10 +122,10 @@ EB_DEV float gather4(const double* __restrict__ g, int32_t rows, int32_t iy, int
                      float dy) {
   const W4 w = wts(dx, dy);
   const size_t o = (size_t)(ix - 1) * rows + (iy - 1);
-  float v = w.ul * (float)__ldg(&g[o]);
-  v = fmaf(w.ll, (float)__ldg(&g[o + 1]), v);
-  v = fmaf(w.ur, (float)__ldg(&g[o + rows]), v);
-  v = fmaf(w.lr, (float)__ldg(&g[o + rows + 1]), v);
+  float v = w.ul * d2f(__ldg(&g[o]));
+  v = fmaf(w.ll, d2f(__ldg(&g[o + 1])), v);
+  v = fmaf(w.ur, d2f(__ldg(&g[o + rows])), v);
+  v = fmaf(w.lr, d2f(__ldg(&g[o + rows + 1])), v);
   return v;
 }
 EB_DEV float gather4f(const float* __restrict__ g, int32_t rows, int32_t iy, int32_t ix, float dx,

@@ -92,6 +92,45 @@ DevMarkers dev_markers(eb_ctx* c) {
   return d;
 }
 
+// ------------------------------------------------------------ FP32 mirrors ---
+namespace {
+struct ConvJob {
+  const double* src[8];
+  float* dst[8];
+  int64_t n[8];
+  int count;
+};
+__global__ void k_grids_to_f32(ConvJob j) {
+  const int g = blockIdx.y;
+  if (g >= j.count) return;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < j.n[g]; i += (int64_t)gridDim.x * blockDim.x)
+    j.dst[g][i] = d2f(j.src[g][i]);
+}
+}  // namespace
+
+int grid_f32(eb_ctx* c, std::initializer_list<int> fields, const float** out) {
+  ConvJob job{};
+  int64_t nmax = 0;
+  for (int f : fields) {
+    if (job.count == 8) return eb_fail(c, EB_BAD_INPUT, "too many grids for one conversion");
+    int rc = ensure_grid_field(c, f);
+    if (rc) return rc;
+    const int64_t n = (int64_t)grid_field_count(c, f);
+    if (!c->gf32[f]) EB_CK(c, cudaMalloc(&c->gf32[f], n * sizeof(float)));
+    job.src[job.count] = c->gf[f];
+    job.dst[job.count] = c->gf32[f];
+    job.n[job.count] = n;
+    out[job.count] = c->gf32[f];
+    nmax = n > nmax ? n : nmax;
+    ++job.count;
+  }
+  const unsigned bx = (unsigned)((nmax + 255) / 256 < 1184 ? (nmax + 255) / 256 : 1184);
+  EB_PROF(c, "k_grids_to_f32");
+  k_grids_to_f32<<<dim3(bx, job.count), 256, 0, c->stream>>>(job);
+  EB_LAUNCHED(c);
+  return EB_OK;
+}
+
 // -------------------------------------------------------------- profiler ---
 void prof_begin(eb_ctx* c, const char* name) {
   Profiler& p = c->prof;
@@ -176,9 +215,12 @@ extern "C" int eb_create(eb_ctx** out, int device) {
 static void free_grid_tables(eb_ctx* c) {
   for (void* p : c->grid_allocs) cudaFree(p);
   c->grid_allocs.clear();
-  for (int f = 0; f < EB_G_NFIELDS; ++f) { cudaFree(c->gf[f]); c->gf[f] = nullptr; }
-  cudaFree(c->vx1f); cudaFree(c->vy1f); cudaFree(c->espf);
-  c->vx1f = c->vy1f = c->espf = nullptr;
+  for (int f = 0; f < EB_G_NFIELDS; ++f) {
+    cudaFree(c->gf[f]);
+    cudaFree(c->gf32[f]);
+    c->gf[f] = nullptr;
+    c->gf32[f] = nullptr;
+  }
   cudaFree(c->cs.count); cudaFree(c->cs.start); cudaFree(c->cs.cursor); cudaFree(c->cs.scan_tmp);
   cudaFree(c->part);
   c->cs.count = c->cs.start = c->cs.cursor = c->cs.scan_tmp = nullptr;

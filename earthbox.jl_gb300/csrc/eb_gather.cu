@@ -13,25 +13,27 @@ namespace {
 
 constexpr int kBlock = 256;
 
-// Pressure-grid bilinear gather (GridToMarker.jl:104-153, MarkerGridMapping.jl:311-350).
-__device__ __forceinline__ float gather_p(const double* __restrict__ pg, const DevGrid& g, int32_t ix, int32_t iy,
+// Pressure-grid bilinear gather (GridToMarker.jl:104-153, MarkerGridMapping.jl:311-350)
+// on an FP32 mirror of the grid.
+__device__ __forceinline__ float gather_p(const float* __restrict__ pg, const DevGrid& g, int32_t ix, int32_t iy,
                                           float lx, float ly) {
   const float hx = __ldg(&g.vyoff_hi[ix - 1]), hy = __ldg(&g.vxoff_hi[iy - 1]);
   const int32_t xp = clamp_i((lx < hx) ? ix - 1 : ix, 1, g.xnum - 2);
   const int32_t yp = clamp_i((ly < hy) ? iy - 1 : iy, 1, g.ynum - 2);
   const float ox = (xp + 1 == ix) ? __ldg(&g.vyoff_lo[ix - 1]) : hx;
   const float oy = (yp + 1 == iy) ? __ldg(&g.vxoff_lo[iy - 1]) : hy;
-  return gather4(pg, g.ynum - 1, yp, xp, (lx - ox) * __ldg(&g.rsxvyf[xp]), (ly - oy) * __ldg(&g.rsyvxf[yp]));
+  return gather4f(pg, g.ynum - 1, yp, xp, (lx - ox) * __ldg(&g.rsxvyf[xp]), (ly - oy) * __ldg(&g.rsyvxf[yp]));
 }
 
-__global__ void k_gather_temperature(DevMarkers mk, DevGrid g, const double* __restrict__ tk1) {
+__global__ void k_gather_temperature(DevMarkers mk, DevGrid g, const float* __restrict__ tk1) {
   const int64_t m = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (m >= mk.M || !(mk.mflags[m] & MF_INSIDE)) return;
-  mk.tk[m] = (double)gather4(tk1, g.ynum, mk.yn[m], mk.xn[m], mk.fx[m], mk.fy[m]);
+  mk.tk[m] = f2d(gather4f(tk1, g.ynum, mk.yn[m], mk.xn[m], mk.fx[m], mk.fy[m]));
 }
 
 struct PostStokesGrids {
-  const double *exx, *exy, *sxx2, *sxy2, *dsxx, *dsxy, *pr1, *mat_mu;
+  const float *exx, *exy, *sxx2, *sxy2, *dsxx, *dsxy, *pr1;
+  const double* mat_mu;
   float dt;
 };
 
@@ -43,16 +45,16 @@ __global__ void k_post_stokes(DevMarkers mk, DevGrid g, PostStokesGrids G) {
   const float lx = fx * __ldg(&g.sxf[ix - 1]), ly = fy * __ldg(&g.syf[iy - 1]);
   // MarkerStrainRate.calculate_marker_strain_rate!
   const float exx = gather_p(G.exx, g, ix, iy, lx, ly);
-  const float exy = gather4(G.exy, g.ynum, iy, ix, fx, fy);
-  mk.exx[m] = (double)exx;
-  mk.exy[m] = (double)exy;
+  const float exy = gather4f(G.exy, g.ynum, iy, ix, fx, fy);
+  mk.exx[m] = f2d(exx);
+  mk.exy[m] = f2d(exy);
   // MarkerStrainRateRatio.calculate_marker_strain_rate_ratio! / marker_strain_rate_ratio
   const float sxx2 = gather_p(G.sxx2, g, ix, iy, lx, ly);
-  const float sxy2 = gather4(G.sxy2, g.ynum, iy, ix, fx, fy);
+  const float sxy2 = gather4f(G.sxy2, g.ynum, iy, ix, fx, fy);
   const float dsxx = gather_p(G.dsxx, g, ix, iy, lx, ly);
-  const float dsxy = gather4(G.dsxy, g.ynum, iy, ix, fx, fy);
-  const float mu = (float)__ldg(&G.mat_mu[mk.matid[m] - 1]);
-  const float eta = (float)mk.eta[m];
+  const float dsxy = gather4f(G.dsxy, g.ynum, iy, ix, fx, fy);
+  const float mu = d2f(__ldg(&G.mat_mu[mk.matid[m] - 1]));
+  const float eta = d2f(mk.eta[m]);
   const float eii = hypotf(exx, exy);
   float r = 1.f;
   if (eii > 0.f) {
@@ -61,26 +63,26 @@ __global__ void k_post_stokes(DevMarkers mk, DevGrid g, PostStokesGrids G) {
     const float b = 0.5f * (sxy2 / eta + dsxy * tf);
     r = hypotf(a, b) / eii;
   }
-  mk.sr_ratio[m] = (double)r;
+  mk.sr_ratio[m] = f2d(r);
   // MarkerPressure.calculate_marker_pressure!
-  mk.pr[m] = (double)gather_p(G.pr1, g, ix, iy, lx, ly);
+  mk.pr[m] = f2d(gather_p(G.pr1, g, ix, iy, lx, ly));
 }
 
-__global__ void k_stress_correction(DevMarkers mk, DevGrid g, const double* __restrict__ dsxy,
-                                    const double* __restrict__ dsxx) {
+__global__ void k_stress_correction(DevMarkers mk, DevGrid g, const float* __restrict__ dsxy,
+                                    const float* __restrict__ dsxx) {
   const int64_t m = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (m >= mk.M || !(mk.mflags[m] & MF_INSIDE)) return;
   const int32_t ix = mk.xn[m], iy = mk.yn[m];
   const float fx = mk.fx[m], fy = mk.fy[m];
   const float lx = fx * __ldg(&g.sxf[ix - 1]), ly = fy * __ldg(&g.syf[iy - 1]);
-  mk.sxy[m] = mk.sxy[m] + (double)gather4(dsxy, g.ynum, iy, ix, fx, fy);
-  mk.sxx[m] = mk.sxx[m] + (double)gather_p(dsxx, g, ix, iy, lx, ly);
+  mk.sxy[m] = mk.sxy[m] + f2d(gather4f(dsxy, g.ynum, iy, ix, fx, fy));
+  mk.sxx[m] = mk.sxx[m] + f2d(gather_p(dsxx, g, ix, iy, lx, ly));
 }
 
-__global__ void k_add_dt(DevMarkers mk, DevGrid g, const double* __restrict__ dtk1) {
+__global__ void k_add_dt(DevMarkers mk, DevGrid g, const float* __restrict__ dtk1) {
   const int64_t m = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (m >= mk.M || !(mk.mflags[m] & MF_INSIDE)) return;
-  mk.tk[m] = mk.tk[m] + (double)gather4(dtk1, g.ynum, mk.yn[m], mk.xn[m], mk.fx[m], mk.fy[m]);
+  mk.tk[m] = mk.tk[m] + f2d(gather4f(dtk1, g.ynum, mk.yn[m], mk.xn[m], mk.fx[m], mk.fy[m]));
 }
 
 unsigned mblocks(const eb_ctx* c) { return (unsigned)((c->M + kBlock - 1) / kBlock); }
@@ -91,8 +93,10 @@ int launch_gather_temperature(eb_ctx* c) {
   int rc;
   if ((rc = ensure_marker_field(c, EB_M_TK)) || (rc = ensure_grid_field(c, EB_G_TK1))) return rc;
   if (c->M == 0) return EB_OK;
+  const float* tk1;
+  if ((rc = grid_f32(c, {EB_G_TK1}, &tk1))) return rc;
   EB_PROF(c, "k_gather_temperature");
-  k_gather_temperature<<<mblocks(c), kBlock, 0, c->stream>>>(dev_markers(c), c->g, c->gf[EB_G_TK1]);
+  k_gather_temperature<<<mblocks(c), kBlock, 0, c->stream>>>(dev_markers(c), c->g, tk1);
   EB_LAUNCHED(c);
   return EB_OK;
 }
@@ -104,8 +108,9 @@ int launch_post_stokes_gathers(eb_ctx* c) {
   const int gfs[] = {EB_G_EXX, EB_G_EXY, EB_G_SXX2, EB_G_SXY2, EB_G_DSXX, EB_G_DSXY, EB_G_PR1};
   for (int f : gfs) if ((rc = ensure_grid_field(c, f))) return rc;
   if (c->M == 0) return EB_OK;
-  PostStokesGrids G{c->gf[EB_G_EXX], c->gf[EB_G_EXY], c->gf[EB_G_SXX2], c->gf[EB_G_SXY2], c->gf[EB_G_DSXX],
-                    c->gf[EB_G_DSXY], c->gf[EB_G_PR1], c->mats.mu, (float)c->P.timestep};
+  const float* f[7];
+  if ((rc = grid_f32(c, {EB_G_EXX, EB_G_EXY, EB_G_SXX2, EB_G_SXY2, EB_G_DSXX, EB_G_DSXY, EB_G_PR1}, f))) return rc;
+  PostStokesGrids G{f[0], f[1], f[2], f[3], f[4], f[5], f[6], c->mats.mu, (float)c->P.timestep};
   EB_PROF(c, "k_post_stokes");
   k_post_stokes<<<mblocks(c), kBlock, 0, c->stream>>>(dev_markers(c), c->g, G);
   EB_LAUNCHED(c);
@@ -118,8 +123,10 @@ int launch_stress_correction(eb_ctx* c) {
       (rc = ensure_grid_field(c, EB_G_DSXY)) || (rc = ensure_grid_field(c, EB_G_DSXX)))
     return rc;
   if (c->M == 0) return EB_OK;
+  const float* f[2];
+  if ((rc = grid_f32(c, {EB_G_DSXY, EB_G_DSXX}, f))) return rc;
   EB_PROF(c, "k_stress_correction");
-  k_stress_correction<<<mblocks(c), kBlock, 0, c->stream>>>(dev_markers(c), c->g, c->gf[EB_G_DSXY], c->gf[EB_G_DSXX]);
+  k_stress_correction<<<mblocks(c), kBlock, 0, c->stream>>>(dev_markers(c), c->g, f[0], f[1]);
   EB_LAUNCHED(c);
   return EB_OK;
 }
@@ -128,8 +135,10 @@ int launch_add_remaining_dt(eb_ctx* c) {
   int rc;
   if ((rc = ensure_marker_field(c, EB_M_TK)) || (rc = ensure_grid_field(c, EB_G_DTK1))) return rc;
   if (c->M == 0) return EB_OK;
+  const float* dtk1;
+  if ((rc = grid_f32(c, {EB_G_DTK1}, &dtk1))) return rc;
   EB_PROF(c, "k_add_dt");
-  k_add_dt<<<mblocks(c), kBlock, 0, c->stream>>>(dev_markers(c), c->g, c->gf[EB_G_DTK1]);
+  k_add_dt<<<mblocks(c), kBlock, 0, c->stream>>>(dev_markers(c), c->g, dtk1);
   EB_LAUNCHED(c);
   return EB_OK;
 }

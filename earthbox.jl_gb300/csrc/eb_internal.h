@@ -80,7 +80,7 @@ struct eb_ctx {
   std::vector<void*> grid_allocs;  // coordinate tables
   DevGrid g{};
   double* gf[EB_G_NFIELDS] = {};
-  float *vx1f = nullptr, *vy1f = nullptr, *espf = nullptr;  // FP32 copies for RK4
+  float* gf32[EB_G_NFIELDS] = {};  // FP32 mirrors of grids read by the gathers
   // materials
   std::vector<void*> mat_allocs;
   DevMats mats{};
@@ -126,6 +126,10 @@ int ensure_grid_field(eb_ctx* c, int f);
 int ensure_marker_field(eb_ctx* c, int f);
 DevMarkers dev_markers(eb_ctx* c);
 size_t grid_field_count(const eb_ctx* c, int f);
+
+// FP32 mirrors: convert the listed grid fields (up to 8) in one launch and
+// return their device pointers in `out` (same order).
+int grid_f32(eb_ctx* c, std::initializer_list<int> fields, const float** out);
 
 // launchers
 int launch_inside_flags(eb_ctx* c);

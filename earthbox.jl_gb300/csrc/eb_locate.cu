@@ -59,8 +59,8 @@ __global__ void k_locate_count(DevMarkers mk, DevGrid g, int32_t* __restrict__ c
       const double dyd = y - __ldg(&g.gy[iy - 1]);
       // one FP64 multiply by the reciprocal spacing, rounded once to FP32:
       // |fx - fl64(dx)| <= 2^-25 fx + 2^-52, i.e. below 3e-8 on [0, 1]
-      const float fx = (float)(dxd * __ldg(&g.rsx[ix - 1]));
-      const float fy = (float)(dyd * __ldg(&g.rsy[iy - 1]));
+      const float fx = d2f(dxd * __ldg(&g.rsx[ix - 1]));
+      const float fy = d2f(dyd * __ldg(&g.rsy[iy - 1]));
       bool le, ge;
       half_tests(fx, dxd, __ldg(&g.sx[ix - 1]), le, ge);
       if (le) fl |= MF_XLE;

@@ -19,7 +19,7 @@
 
 namespace {
 
-constexpr int kChunk = 256;  // markers staged per pass
+constexpr int kChunk = 288;  // staging slots per pass (32 cells x 9)
 constexpr float kRad2Deg = 57.295779513082320876798f;
 
 enum { C_UL = 0, C_LL = 1, C_UR = 2, C_LR = 3 };
@@ -115,17 +115,17 @@ struct StokesSpec {
     const int32_t mt = mk.matid[m];
     const double mu = __ldg(&mat_mu[mt - 1]);
     if ((__double_as_longlong(mu) << 1) == 0) atomicOr(dflag, 2);  // reference raises on a zero shear modulus
-    sv[V_RHO][t] = (float)mk.rho[m];
-    sv[V_COH][t] = (float)mk.cohesion[m];
-    sv[V_FRIC][t] = asinf((float)mk.fric[m]) * kRad2Deg;
-    sv[V_ETAF][t] = (float)mk.eta_flow[m];
-    sv[V_ETA][t] = (float)mk.eta[m];
-    sv[V_MUI][t] = 1.f / (float)mu;
-    sv[V_SXY][t] = (float)mk.sxy[m];
+    sv[V_RHO][t] = d2f(mk.rho[m]);
+    sv[V_COH][t] = d2f(mk.cohesion[m]);
+    sv[V_FRIC][t] = asinf(d2f(mk.fric[m])) * kRad2Deg;
+    sv[V_ETAF][t] = d2f(mk.eta_flow[m]);
+    sv[V_ETA][t] = d2f(mk.eta[m]);
+    sv[V_MUI][t] = 1.f / d2f(mu);
+    sv[V_SXY][t] = d2f(mk.sxy[m]);
     sv[V_PLAST][t] = mk.pfailure[m];
     sv[V_DIL][t] = mk.dilat[m];
-    sv[V_MELT][t] = (float)mk.melt[m];
-    sv[V_SXX][t] = (float)mk.sxx[m];
+    sv[V_MELT][t] = d2f(mk.melt[m]);
+    sv[V_SXX][t] = d2f(mk.sxx[m]);
   }
   __device__ void accum(int role, int t, float (*sv)[kChunk], const uint8_t* sfl, KSum* a) const {
     if (role == 0) {
@@ -177,11 +177,11 @@ struct HeatSpec {
     sfl[t] = fl;
     double hr = __ldg(&mat_hr[mk.matid[m] - 1]);
     if (use_serp) hr = hr + mk.serp_hr[m];
-    sv[S_V0 + 0][t] = (float)mk.tk[m];
-    sv[S_V0 + 1][t] = (float)mk.kt[m];
-    sv[S_V0 + 2][t] = (float)mk.rhocp[m];
-    sv[S_V0 + 3][t] = (float)hr;
-    sv[S_V0 + 4][t] = (float)mk.ha[m];
+    sv[S_V0 + 0][t] = d2f(mk.tk[m]);
+    sv[S_V0 + 1][t] = d2f(mk.kt[m]);
+    sv[S_V0 + 2][t] = d2f(mk.rhocp[m]);
+    sv[S_V0 + 3][t] = d2f(hr);
+    sv[S_V0 + 4][t] = d2f(mk.ha[m]);
   }
   __device__ void accum(int role, int t, float (*sv)[kChunk], const uint8_t*, KSum* a) const {
     const float w = sv[S_UL + role][t];
@@ -203,7 +203,7 @@ struct ViscSpec {
     sv[S_UL][t] = w.ul; sv[S_LL][t] = w.ll; sv[S_UR][t] = w.ur; sv[S_LR][t] = w.lr;
     sv[S_WC][t] = (1.f - fabsf(0.5f - fx)) * (1.f - fabsf(0.5f - fy));
     sfl[t] = fl;
-    sv[S_V0][t] = (float)mk.eta[m];
+    sv[S_V0][t] = d2f(mk.eta[m]);
   }
   __device__ void accum(int role, int t, float (*sv)[kChunk], const uint8_t* sfl, KSum* a) const {
     const float e = sv[S_V0][t];
@@ -222,7 +222,7 @@ struct ViscSpec {
 
 // Pressure-grid bilinear gather of one marker (GridToMarker.jl:104-153 with
 // MarkerGridMapping.upr_left_index_pressure / upr_left_dist_pressure, :311-350).
-__device__ __forceinline__ float gather_pressure_grid(const double* __restrict__ pg, const DevGrid& g, int32_t ix,
+__device__ __forceinline__ float gather_pressure_grid(const float* __restrict__ pg, const DevGrid& g, int32_t ix,
                                                       int32_t iy, float fx, float fy) {
   const float lx = fx * __ldg(&g.sxf[ix - 1]);
   const float ly = fy * __ldg(&g.syf[iy - 1]);
@@ -236,7 +236,7 @@ __device__ __forceinline__ float gather_pressure_grid(const double* __restrict__
   const float oy = (yp + 1 == iy) ? __ldg(&g.vxoff_lo[iy - 1]) : hy;
   const float dxp = (lx - ox) * __ldg(&g.rsxvyf[xp]);
   const float dyp = (ly - oy) * __ldg(&g.rsyvxf[yp]);
-  return gather4(pg, g.ynum - 1, yp, xp, dxp, dyp);
+  return gather4f(pg, g.ynum - 1, yp, xp, dxp, dyp);
 }
 
 // Subgrid stress (SubgridShearStress.jl:27-96, SubgridNormalStress.jl:27-89):
@@ -245,7 +245,8 @@ __device__ __forceinline__ float gather_pressure_grid(const double* __restrict__
 struct SubgridStressSpec {
   static constexpr const char* kName = "k_cells<subgrid_stress>";
   static constexpr int kRoles = 2, kNV = S_V0 + 2, kAcc = 8;
-  const double *sxy1, *sxx1, *mat_mu;
+  const float *sxy1, *sxx1;  // FP32 mirrors
+  const double* mat_mu;
   float dt, coef;
   __device__ void stage(const DevMarkers& mk, const DevGrid& g, int32_t m, int t, float (*sv)[kChunk], uint8_t* sfl) const {
     const uint8_t fl = mk.mflags[m];
@@ -256,18 +257,18 @@ struct SubgridStressSpec {
     sv[S_WC][t] = (1.f - fabsf(0.5f - fx)) * (1.f - fabsf(0.5f - fy));
     sfl[t] = fl;
     // DiffusionTerm.calculate_subgrid_stress_diffusion_term (DiffusionTerm.jl:14-29)
-    const float mu = (float)__ldg(&mat_mu[mk.matid[m] - 1]);
-    const float maxwell = (float)mk.eta[m] / mu;
+    const float mu = d2f(__ldg(&mat_mu[mk.matid[m] - 1]));
+    const float maxwell = d2f(mk.eta[m]) / mu;
     const float sdif = fmaxf(-coef * dt / maxwell, -30.f);
     const float term = -expm1f(sdif);  // 1 - exp(sdif), accurate for small |sdif|
-    const float sxy_g = gather4(sxy1, g.ynum, iy, ix, fx, fy);
+    const float sxy_g = gather4f(sxy1, g.ynum, iy, ix, fx, fy);
     const double sxy_m = mk.sxy[m];
-    const float rxy = (sxy_g - (float)sxy_m) * term;
-    mk.sxy[m] = sxy_m + (double)rxy;
+    const float rxy = (sxy_g - d2f(sxy_m)) * term;
+    mk.sxy[m] = sxy_m + f2d(rxy);
     const float sxx_g = gather_pressure_grid(sxx1, g, ix, iy, fx, fy);
     const double sxx_m = mk.sxx[m];
-    const float rxx = (sxx_g - (float)sxx_m) * term;
-    mk.sxx[m] = sxx_m + (double)rxx;
+    const float rxx = (sxx_g - d2f(sxx_m)) * term;
+    mk.sxx[m] = sxx_m + f2d(rxx);
     sv[S_V0][t] = rxy;
     sv[S_V0 + 1][t] = rxx;
   }
@@ -297,7 +298,7 @@ struct SubgridStressSpec {
 struct SubgridHeatSpec {
   static constexpr const char* kName = "k_cells<subgrid_heat>";
   static constexpr int kRoles = 1, kNV = S_V0 + 1, kAcc = 8;
-  const double *tk1, *kt1, *rhocp1;
+  const float *tk1, *kt1, *rhocp1;  // FP32 mirrors
   float dt, coef, inv_ts;  // inv_ts = 2/xstpavg^2 + 2/ystpavg^2
   __device__ void stage(const DevMarkers& mk, const DevGrid& g, int32_t m, int t, float (*sv)[kChunk], uint8_t* sfl) const {
     const int32_t ix = mk.xn[m], iy = mk.yn[m];
@@ -305,15 +306,15 @@ struct SubgridHeatSpec {
     const W4 w = wts(fx, fy);
     sv[S_UL][t] = w.ul; sv[S_LL][t] = w.ll; sv[S_UR][t] = w.ur; sv[S_LR][t] = w.lr;
     sfl[t] = mk.mflags[m];
-    const float tn = gather4(tk1, g.ynum, iy, ix, fx, fy);
+    const float tn = gather4f(tk1, g.ynum, iy, ix, fx, fy);
     const double tm = mk.tk[m];
-    const float k = gather4(kt1, g.ynum, iy, ix, fx, fy);
-    const float rc = gather4(rhocp1, g.ynum, iy, ix, fx, fy);
+    const float k = gather4f(kt1, g.ynum, iy, ix, fx, fy);
+    const float rc = gather4f(rhocp1, g.ynum, iy, ix, fx, fy);
     const float tsg = rc / k / inv_ts;
     const float term = fmaxf(-coef * dt / tsg, -30.f);
-    const float d = (tn - (float)tm) * (-expm1f(term));
-    mk.subgrid_dt[m] = (double)d;
-    mk.tk[m] = tm + (double)d;
+    const float d = (tn - d2f(tm)) * (-expm1f(term));
+    mk.subgrid_dt[m] = f2d(d);
+    mk.tk[m] = tm + f2d(d);
     sv[S_V0][t] = d;
   }
   __device__ void accum(int, int t, float (*sv)[kChunk], const uint8_t*, KSum* a) const {
@@ -330,6 +331,17 @@ struct SubgridHeatSpec {
 };
 
 // ------------------------------------------------------- per-cell kernel ---
+// Block = 32 consecutive cells.  Pass p stages markers [8p, 8p+8) of every cell:
+// thread t loads marker 8p + (t & 7) of cell t >> 3, so eight consecutive
+// threads read eight consecutive entries of one cell's list (coalesced), and
+// writes it to slot (t >> 3) * 9 + (t & 7).  Then warp `role`, lane j folds
+// cell j's slots j*9 .. j*9+7 in order (stride 9 keeps the 32 lanes on 32
+// different banks).  All 32 lanes stay busy while the cells have markers left,
+// and each cell is folded in its marker order.
+constexpr int kPer = 8;             // markers per cell per pass
+constexpr int kSlotStride = kPer + 1;
+static_assert(kChunk >= 32 * kSlotStride, "staging table too small");
+
 template <class S>
 __global__ void __launch_bounds__(32 * S::kRoles) k_cells(S spec, DevMarkers mk, DevGrid g,
                                                           const int32_t* __restrict__ start,
@@ -337,24 +349,36 @@ __global__ void __launch_bounds__(32 * S::kRoles) k_cells(S spec, DevMarkers mk,
                                                           float* __restrict__ part) {
   __shared__ float sv[S::kNV][kChunk];
   __shared__ uint8_t sfl[kChunk];
+  __shared__ int32_t s_beg[32], s_cnt[32], s_max;
   const int lane = threadIdx.x & 31, role = threadIdx.x >> 5;
   const int32_t c0 = blockIdx.x * 32;
-  const int32_t c1 = min(c0 + 32, nc);
-  const int32_t P0 = start[c0], P1 = start[c1];
-  const int32_t my = c0 + lane;
-  const int32_t beg = my < nc ? start[my] : P1, end = my < nc ? start[my + 1] : P1;
+  if (threadIdx.x < 32) {
+    const int32_t cell = c0 + lane;
+    const int32_t b = cell < nc ? start[cell] : 0;
+    const int32_t n = cell < nc ? start[cell + 1] - b : 0;
+    s_beg[lane] = b;
+    s_cnt[lane] = n;
+    int32_t mx = n;
+    for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    if (lane == 0) s_max = mx;
+  }
+  __syncthreads();
+  const int32_t nmax = s_max;
+  const int32_t my_cnt = s_cnt[lane];
   KSum acc[S::kAcc];
 #pragma unroll
   for (int k = 0; k < S::kAcc; ++k) acc[k].init();
-  for (int32_t k0 = P0; k0 < P1; k0 += kChunk) {
-    const int32_t kn = min(kChunk, P1 - k0);
+  for (int32_t base = 0; base < nmax; base += kPer) {
     __syncthreads();
-    for (int t = threadIdx.x; t < kn; t += blockDim.x) spec.stage(mk, g, __ldg(&perm[k0 + t]), t, sv, sfl);
+    for (int t = threadIdx.x; t < 32 * kPer; t += blockDim.x) {
+      const int j = t >> 3, ii = t & 7, i = base + ii;
+      if (i < s_cnt[j]) spec.stage(mk, g, __ldg(&perm[s_beg[j] + i]), j * kSlotStride + ii, sv, sfl);
+    }
     __syncthreads();
-    const int32_t kb = max(beg, k0), ke = min(end, k0 + kn);
-    for (int32_t k = kb; k < ke; ++k) spec.accum(role, k - k0, sv, sfl, acc);
+    const int n = min(kPer, my_cnt - base);
+    for (int i = 0; i < n; ++i) spec.accum(role, lane * kSlotStride + i, sv, sfl, acc);
   }
-  if (my < nc) spec.store(role, my, nc, acc, part);
+  if (c0 + lane < nc) spec.store(role, c0 + lane, nc, acc, part);
 }
 
 template <class S>
@@ -407,22 +431,25 @@ __global__ void k_finish_denoms(NodeCtx n, double* wtnodes, double* wtetas, doub
                 nv = (int64_t)n.ynum * (n.xnum + 1);
   if (t < nb) {
     const int32_t i = (int32_t)(t % n.ynum) + 1, j = (int32_t)(t / n.ynum) + 1;
-    wtnodes[t] = (double)n.basic(i, j, 0, 1);
-    wtetas[t] = (double)n.basic(i, j, 4, 1);
+    wtnodes[t] = f2d(n.basic(i, j, 0, 1));
+    wtetas[t] = f2d(n.basic(i, j, 4, 1));
   }
-  if (t < np) wtetan[t] = (double)n.part[(size_t)8 * n.nc + t];
+  if (t < np) wtetan[t] = f2d(n.part[(size_t)8 * n.nc + t]);
   if (t < nv) {
     const int32_t i = (int32_t)(t % n.ynum) + 1, jv = (int32_t)(t / n.ynum) + 1;
-    wtnodes_vy[t] = (double)n.vy(i, jv, 9);
+    wtnodes_vy[t] = f2d(n.vy(i, jv, 9));
   }
 }
 
 // average with backup: den != 0 -> num/den, else the backup value
+// (weight sums are FP32 sums stored in FP64, so d2f(den) is exact)
 __device__ __forceinline__ double avg_or(float num, double den, double backup) {
-  return den != 0.0 ? (double)(num / (float)den) : backup;
+  const float d = d2f(den);
+  return d != 0.f ? f2d(num / d) : backup;
 }
 __device__ __forceinline__ double harm_or(float num, double den, double backup) {
-  return den != 0.0 ? (double)((float)den / num) : backup;
+  const float d = d2f(den);
+  return d != 0.f ? f2d(d / num) : backup;
 }
 
 struct StokesGrids {
@@ -543,16 +570,16 @@ __global__ void k_finish_subgrid_stress(NodeCtx n, double* dsxyn, double* dsxxn,
   if (t < (int64_t)n.ynum * n.xnum) {
     const int32_t i = (int32_t)(t % n.ynum) + 1, j = (int32_t)(t / n.ynum) + 1;
     const float num = n.basic(i, j, 0, 1), den = n.basic(i, j, 4, 1);
-    const double v = den != 0.f ? (double)(num / den) : (double)num;
+    const double v = f2d(den != 0.f ? num / den : num);
     dsxyn[t] = v;
-    wtetas[t] = (double)den;
+    wtetas[t] = f2d(den);
     dsxy[t] = dsxy[t] - v;
   }
   if (t < (int64_t)(n.ynum - 1) * (n.xnum - 1)) {
     const float num = n.part[(size_t)8 * n.nc + t], den = n.part[(size_t)9 * n.nc + t];
-    const double v = den != 0.f ? (double)(num / den) : (double)num;
+    const double v = f2d(den != 0.f ? num / den : num);
     dsxxn[t] = v;
-    wtetan[t] = (double)den;
+    wtetan[t] = f2d(den);
     dsxx[t] = dsxx[t] - v;
   }
 }
@@ -563,9 +590,9 @@ __global__ void k_finish_subgrid_heat(NodeCtx n, double* dtkn, double* wtnodes, 
   if (t >= (int64_t)n.ynum * n.xnum) return;
   const int32_t i = (int32_t)(t % n.ynum) + 1, j = (int32_t)(t / n.ynum) + 1;
   const float num = n.basic(i, j, 0, 1), den = n.basic(i, j, 4, 1);
-  const double v = den != 0.f ? (double)(num / den) : (double)num;
+  const double v = f2d(den != 0.f ? num / den : num);
   dtkn[t] = v;
-  wtnodes[t] = (double)den;
+  wtnodes[t] = f2d(den);
   dtk1[t] = dtk1[t] - v;
 }
 
@@ -707,7 +734,9 @@ int launch_subgrid_stress(eb_ctx* c) {
   if (rc) return rc;
   double** gf = c->gf;
   if (c->M > 0) {
-    SubgridStressSpec s{gf[EB_G_SXY1], gf[EB_G_SXX1], c->mats.mu, (float)c->P.timestep, (float)c->P.subgrid_diff_coef_stress};
+    const float* f[2];
+    if ((rc = grid_f32(c, {EB_G_SXY1, EB_G_SXX1}, f))) return rc;
+    SubgridStressSpec s{f[0], f[1], c->mats.mu, (float)c->P.timestep, (float)c->P.subgrid_diff_coef_stress};
     rc = run_cells(c, s);
     if (rc) return rc;
   } else {
@@ -730,8 +759,9 @@ int launch_subgrid_heat(eb_ctx* c) {
   EB_CK(c, cudaMemsetAsync(c->mf[EB_M_SUBGRID_DT], 0, c->M * sizeof(double), c->stream));
   if (c->M > 0) {
     const double its = 2.0 / (c->g.xstpavg * c->g.xstpavg) + 2.0 / (c->g.ystpavg * c->g.ystpavg);
-    SubgridHeatSpec s{gf[EB_G_TK1], gf[EB_G_KT1], gf[EB_G_RHOCP1], (float)c->P.timestep,
-                      (float)c->P.subgrid_diff_coef_temp, (float)its};
+    const float* f[3];
+    if ((rc = grid_f32(c, {EB_G_TK1, EB_G_KT1, EB_G_RHOCP1}, f))) return rc;
+    SubgridHeatSpec s{f[0], f[1], f[2], (float)c->P.timestep, (float)c->P.subgrid_diff_coef_temp, (float)its};
     rc = run_cells(c, s);
     if (rc) return rc;
   } else {
