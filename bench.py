@@ -49,6 +49,17 @@ ALGO_BYTES_PER_MARKER = {
     "k_locate_count": 16 + 1 + 8 + 8 + 1 + 4,               # x,y, inside, w xn/yn, fx/fy, flags, count atomics
 }
 
+# DRAM bytes per marker (dram__bytes_read.sum + dram__bytes_write.sum) from one
+# `ncu --set full` capture of each kernel on the 2.56M-marker rift
+# (profiles/marker_kernels_rift_2p5M.md); reads scale with the marker count,
+# writes that still sit in L2 at that size make these a lower bound.
+NCU_DRAM_BYTES_PER_MARKER = {
+    "k_cells<stokes>": 101.2,
+    "k_cells<subgrid_stress>": 57.3,
+    "k_advect": 83.1,
+    "k_post_stokes": 44.5,
+}
+
 
 def parse():
     ap = argparse.ArgumentParser()
@@ -235,6 +246,10 @@ def main():
         roofline = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
                     "frac": achieved / peak, "peak_kind": peak_kind, "traffic": None,
                     "bytes_per_marker": bpm, "launch_ms": dom_ms}
+        ncu_bpm = NCU_DRAM_BYTES_PER_MARKER.get(dom)
+        if ncu_bpm is not None:
+            roofline["traffic"] = ncu_bpm * M / 1e9
+            roofline["traffic_unit"] = "GB per launch (ncu DRAM bytes per marker on 2.56M markers x markers)"
 
     # e2e: host buffers through the C-ABI, copies inside the timed region
     e2e = None

@@ -64,18 +64,24 @@ __device__ __forceinline__ void stage_weights(float (*sv)[kChunk], int t, const 
 }
 
 // ------------------------------------------------------------------ specs ---
-// Each spec defines: kRoles (warps), kNV (staged rows), kAcc (max accumulators
-// per thread), stage(), accum(), store().
+// Each spec defines: kRoles (folding warps, <= 8), kNV (staged rows), kAcc
+// (accumulators per folding thread), a Raw record of the marker fields it
+// reads, load() (the global loads only, issued one pass ahead), put()
+// (arithmetic on a loaded Raw, marker write-backs, staging), accum() and
+// store().
 
 // Denominators: wtnodes (incl), wtetas (excl), wtetan (central), wtnodes_vy.
 // slots: 0-3 incl corners, 4-7 excl quadrants, 8 central, 9-16 vy half*4+corner
 struct DenomSpec {
   static constexpr const char* kName = "k_cells<denominators>";
   static constexpr int kRoles = 4, kNV = S_V0, kAcc = 8;
-  __device__ void stage(const DevMarkers& mk, const DevGrid& g, int32_t m, int t, float (*sv)[kChunk], uint8_t* sfl) const {
-    const uint8_t fl = mk.mflags[m];
-    stage_weights(sv, t, marker_weights(g, mk.xn[m], mk.fx[m], mk.fy[m], fl));
-    sfl[t] = fl;
+  struct Raw { int32_t xn; float fx, fy; uint8_t fl; };
+  __device__ Raw load(const DevMarkers& mk, int32_t m) const {
+    return Raw{mk.xn[m], mk.fx[m], mk.fy[m], mk.mflags[m]};
+  }
+  __device__ void put(const Raw& r, const DevMarkers&, const DevGrid& g, int t, float (*sv)[kChunk], uint8_t* sfl) const {
+    stage_weights(sv, t, marker_weights(g, r.xn, r.fx, r.fy, r.fl));
+    sfl[t] = r.fl;
   }
   __device__ void accum(int role, int t, float (*sv)[kChunk], const uint8_t* sfl, KSum* a) const {
     if (role == 0) {
@@ -108,24 +114,36 @@ struct StokesSpec {
   static constexpr int kRoles = 7, kNV = V_END, kAcc = 8;
   const double* mat_mu;
   int32_t* dflag;
-  __device__ void stage(const DevMarkers& mk, const DevGrid& g, int32_t m, int t, float (*sv)[kChunk], uint8_t* sfl) const {
-    const uint8_t fl = mk.mflags[m];
-    stage_weights(sv, t, marker_weights(g, mk.xn[m], mk.fx[m], mk.fy[m], fl));
-    sfl[t] = fl;
-    const int32_t mt = mk.matid[m];
-    const double mu = __ldg(&mat_mu[mt - 1]);
+  struct Raw {
+    double rho, coh, fric, etaf, eta, sxy, melt, sxx;
+    float fx, fy, plast, dil;
+    int32_t xn, mt;
+    uint8_t fl;
+  };
+  __device__ Raw load(const DevMarkers& mk, int32_t m) const {
+    Raw r;
+    r.fl = mk.mflags[m]; r.xn = mk.xn[m]; r.fx = mk.fx[m]; r.fy = mk.fy[m]; r.mt = mk.matid[m];
+    r.rho = mk.rho[m]; r.coh = mk.cohesion[m]; r.fric = mk.fric[m]; r.etaf = mk.eta_flow[m];
+    r.eta = mk.eta[m]; r.sxy = mk.sxy[m]; r.plast = mk.pfailure[m]; r.dil = mk.dilat[m];
+    r.melt = mk.melt[m]; r.sxx = mk.sxx[m];
+    return r;
+  }
+  __device__ void put(const Raw& r, const DevMarkers&, const DevGrid& g, int t, float (*sv)[kChunk], uint8_t* sfl) const {
+    stage_weights(sv, t, marker_weights(g, r.xn, r.fx, r.fy, r.fl));
+    sfl[t] = r.fl;
+    const double mu = __ldg(&mat_mu[r.mt - 1]);
     if ((__double_as_longlong(mu) << 1) == 0) atomicOr(dflag, 2);  // reference raises on a zero shear modulus
-    sv[V_RHO][t] = d2f(mk.rho[m]);
-    sv[V_COH][t] = d2f(mk.cohesion[m]);
-    sv[V_FRIC][t] = asinf(d2f(mk.fric[m])) * kRad2Deg;
-    sv[V_ETAF][t] = d2f(mk.eta_flow[m]);
-    sv[V_ETA][t] = d2f(mk.eta[m]);
+    sv[V_RHO][t] = d2f(r.rho);
+    sv[V_COH][t] = d2f(r.coh);
+    sv[V_FRIC][t] = asinf(d2f(r.fric)) * kRad2Deg;
+    sv[V_ETAF][t] = d2f(r.etaf);
+    sv[V_ETA][t] = d2f(r.eta);
     sv[V_MUI][t] = 1.f / d2f(mu);
-    sv[V_SXY][t] = d2f(mk.sxy[m]);
-    sv[V_PLAST][t] = mk.pfailure[m];
-    sv[V_DIL][t] = mk.dilat[m];
-    sv[V_MELT][t] = d2f(mk.melt[m]);
-    sv[V_SXX][t] = d2f(mk.sxx[m]);
+    sv[V_SXY][t] = d2f(r.sxy);
+    sv[V_PLAST][t] = r.plast;
+    sv[V_DIL][t] = r.dil;
+    sv[V_MELT][t] = d2f(r.melt);
+    sv[V_SXX][t] = d2f(r.sxx);
   }
   __device__ void accum(int role, int t, float (*sv)[kChunk], const uint8_t* sfl, KSum* a) const {
     if (role == 0) {
@@ -170,18 +188,24 @@ struct HeatSpec {
   static constexpr int kRoles = 4, kNV = S_V0 + 5, kAcc = 5;
   const double* mat_hr;
   int use_serp;
-  __device__ void stage(const DevMarkers& mk, const DevGrid& g, int32_t m, int t, float (*sv)[kChunk], uint8_t* sfl) const {
-    const uint8_t fl = mk.mflags[m];
-    const W4 w = wts(mk.fx[m], mk.fy[m]);
+  struct Raw { double tk, kt, rhocp, ha, serp; float fx, fy; int32_t mt; };
+  __device__ Raw load(const DevMarkers& mk, int32_t m) const {
+    Raw r;
+    r.fx = mk.fx[m]; r.fy = mk.fy[m]; r.mt = mk.matid[m];
+    r.tk = mk.tk[m]; r.kt = mk.kt[m]; r.rhocp = mk.rhocp[m]; r.ha = mk.ha[m];
+    r.serp = use_serp ? mk.serp_hr[m] : 0.0;
+    return r;
+  }
+  __device__ void put(const Raw& r, const DevMarkers&, const DevGrid&, int t, float (*sv)[kChunk], uint8_t*) const {
+    const W4 w = wts(r.fx, r.fy);
     sv[S_UL][t] = w.ul; sv[S_LL][t] = w.ll; sv[S_UR][t] = w.ur; sv[S_LR][t] = w.lr;
-    sfl[t] = fl;
-    double hr = __ldg(&mat_hr[mk.matid[m] - 1]);
-    if (use_serp) hr = hr + mk.serp_hr[m];
-    sv[S_V0 + 0][t] = d2f(mk.tk[m]);
-    sv[S_V0 + 1][t] = d2f(mk.kt[m]);
-    sv[S_V0 + 2][t] = d2f(mk.rhocp[m]);
+    double hr = __ldg(&mat_hr[r.mt - 1]);
+    if (use_serp) hr = hr + r.serp;
+    sv[S_V0 + 0][t] = d2f(r.tk);
+    sv[S_V0 + 1][t] = d2f(r.kt);
+    sv[S_V0 + 2][t] = d2f(r.rhocp);
     sv[S_V0 + 3][t] = d2f(hr);
-    sv[S_V0 + 4][t] = d2f(mk.ha[m]);
+    sv[S_V0 + 4][t] = d2f(r.ha);
   }
   __device__ void accum(int role, int t, float (*sv)[kChunk], const uint8_t*, KSum* a) const {
     const float w = sv[S_UL + role][t];
@@ -193,30 +217,31 @@ struct HeatSpec {
 };
 
 // Viscosity re-scatter (BilinearNumerator.jl:470-533): slots 0-3 excl eta, 4 central eta
+// roles 0-3: one exclusive quadrant each; role 4: the central node
 struct ViscSpec {
   static constexpr const char* kName = "k_cells<viscosity>";
-  static constexpr int kRoles = 2, kNV = S_V0 + 1, kAcc = 4;
-  __device__ void stage(const DevMarkers& mk, const DevGrid& g, int32_t m, int t, float (*sv)[kChunk], uint8_t* sfl) const {
-    const uint8_t fl = mk.mflags[m];
-    const float fx = mk.fx[m], fy = mk.fy[m];
-    const W4 w = wts(fx, fy);
+  static constexpr int kRoles = 5, kNV = S_V0 + 1, kAcc = 1;
+  struct Raw { double eta; float fx, fy; uint8_t fl; };
+  __device__ Raw load(const DevMarkers& mk, int32_t m) const {
+    return Raw{mk.eta[m], mk.fx[m], mk.fy[m], mk.mflags[m]};
+  }
+  __device__ void put(const Raw& r, const DevMarkers&, const DevGrid&, int t, float (*sv)[kChunk], uint8_t* sfl) const {
+    const W4 w = wts(r.fx, r.fy);
     sv[S_UL][t] = w.ul; sv[S_LL][t] = w.ll; sv[S_UR][t] = w.ur; sv[S_LR][t] = w.lr;
-    sv[S_WC][t] = (1.f - fabsf(0.5f - fx)) * (1.f - fabsf(0.5f - fy));
-    sfl[t] = fl;
-    sv[S_V0][t] = d2f(mk.eta[m]);
+    sv[S_WC][t] = (1.f - fabsf(0.5f - r.fx)) * (1.f - fabsf(0.5f - r.fy));
+    sfl[t] = r.fl;
+    sv[S_V0][t] = d2f(r.eta);
   }
   __device__ void accum(int role, int t, float (*sv)[kChunk], const uint8_t* sfl, KSum* a) const {
     const float e = sv[S_V0][t];
-    if (role == 0) {
-      const uint8_t fl = sfl[t];
-      for (int q = 0; q < 4; ++q) if (in_quadrant(fl, q)) a[q].add(sv[S_UL + q][t] * e);
+    if (role < 4) {
+      if (in_quadrant(sfl[t], role)) a[0].add(sv[S_UL + role][t] * e);
     } else {
       a[0].add(sv[S_WC][t] * e);
     }
   }
   __device__ void store(int role, int32_t cell, int32_t nc, const KSum* a, float* part) const {
-    if (role == 0) for (int q = 0; q < 4; ++q) part[(size_t)q * nc + cell] = a[q].get();
-    else part[(size_t)4 * nc + cell] = a[0].get();
+    part[(size_t)role * nc + cell] = a[0].get();
   }
 };
 
@@ -240,48 +265,48 @@ __device__ __forceinline__ float gather_pressure_grid(const float* __restrict__ 
 }
 
 // Subgrid stress (SubgridShearStress.jl:27-96, SubgridNormalStress.jl:27-89):
-// the staging pass relaxes the marker stress and stages the relaxed change.
+// put() relaxes the marker stress, writes it back and stages the relaxed change.
 // slots: 0-3 excl relax_xy*w, 4-7 excl w, 8 central relax_xx*wc, 9 central wc
+// roles 0-3: one exclusive quadrant each (relax_xy*w, w); role 4: the central node
 struct SubgridStressSpec {
   static constexpr const char* kName = "k_cells<subgrid_stress>";
-  static constexpr int kRoles = 2, kNV = S_V0 + 2, kAcc = 8;
+  static constexpr int kRoles = 5, kNV = S_V0 + 2, kAcc = 2;
   const float *sxy1, *sxx1;  // FP32 mirrors
   const double* mat_mu;
   float dt, coef;
-  __device__ void stage(const DevMarkers& mk, const DevGrid& g, int32_t m, int t, float (*sv)[kChunk], uint8_t* sfl) const {
-    const uint8_t fl = mk.mflags[m];
-    const int32_t ix = mk.xn[m], iy = mk.yn[m];
-    const float fx = mk.fx[m], fy = mk.fy[m];
-    const W4 w = wts(fx, fy);
+  struct Raw { double eta, sxy, sxx; int32_t m, xn, yn, mt; float fx, fy; uint8_t fl; };
+  __device__ Raw load(const DevMarkers& mk, int32_t m) const {
+    Raw r;
+    r.m = m; r.fl = mk.mflags[m]; r.xn = mk.xn[m]; r.yn = mk.yn[m]; r.fx = mk.fx[m]; r.fy = mk.fy[m];
+    r.mt = mk.matid[m]; r.eta = mk.eta[m]; r.sxy = mk.sxy[m]; r.sxx = mk.sxx[m];
+    return r;
+  }
+  __device__ void put(const Raw& r, const DevMarkers& mk, const DevGrid& g, int t, float (*sv)[kChunk], uint8_t* sfl) const {
+    const W4 w = wts(r.fx, r.fy);
     sv[S_UL][t] = w.ul; sv[S_LL][t] = w.ll; sv[S_UR][t] = w.ur; sv[S_LR][t] = w.lr;
-    sv[S_WC][t] = (1.f - fabsf(0.5f - fx)) * (1.f - fabsf(0.5f - fy));
-    sfl[t] = fl;
+    sv[S_WC][t] = (1.f - fabsf(0.5f - r.fx)) * (1.f - fabsf(0.5f - r.fy));
+    sfl[t] = r.fl;
     // DiffusionTerm.calculate_subgrid_stress_diffusion_term (DiffusionTerm.jl:14-29)
-    const float mu = d2f(__ldg(&mat_mu[mk.matid[m] - 1]));
-    const float maxwell = d2f(mk.eta[m]) / mu;
+    const float mu = d2f(__ldg(&mat_mu[r.mt - 1]));
+    const float maxwell = d2f(r.eta) / mu;
     const float sdif = fmaxf(-coef * dt / maxwell, -30.f);
     const float term = -expm1f(sdif);  // 1 - exp(sdif), accurate for small |sdif|
-    const float sxy_g = gather4f(sxy1, g.ynum, iy, ix, fx, fy);
-    const double sxy_m = mk.sxy[m];
-    const float rxy = (sxy_g - d2f(sxy_m)) * term;
-    mk.sxy[m] = sxy_m + f2d(rxy);
-    const float sxx_g = gather_pressure_grid(sxx1, g, ix, iy, fx, fy);
-    const double sxx_m = mk.sxx[m];
-    const float rxx = (sxx_g - d2f(sxx_m)) * term;
-    mk.sxx[m] = sxx_m + f2d(rxx);
+    const float sxy_g = gather4f(sxy1, g.ynum, r.yn, r.xn, r.fx, r.fy);
+    const float rxy = (sxy_g - d2f(r.sxy)) * term;
+    mk.sxy[r.m] = r.sxy + f2d(rxy);
+    const float sxx_g = gather_pressure_grid(sxx1, g, r.xn, r.yn, r.fx, r.fy);
+    const float rxx = (sxx_g - d2f(r.sxx)) * term;
+    mk.sxx[r.m] = r.sxx + f2d(rxx);
     sv[S_V0][t] = rxy;
     sv[S_V0 + 1][t] = rxx;
   }
   __device__ void accum(int role, int t, float (*sv)[kChunk], const uint8_t* sfl, KSum* a) const {
-    if (role == 0) {
-      const uint8_t fl = sfl[t];
-      const float r = sv[S_V0][t];
-      for (int q = 0; q < 4; ++q)
-        if (in_quadrant(fl, q)) {
-          const float w = sv[S_UL + q][t];
-          a[q].add(w * r);
-          a[4 + q].add(w);
-        }
+    if (role < 4) {
+      if (in_quadrant(sfl[t], role)) {
+        const float w = sv[S_UL + role][t];
+        a[0].add(w * sv[S_V0][t]);
+        a[1].add(w);
+      }
     } else {
       const float w = sv[S_WC][t];
       a[0].add(w * sv[S_V0 + 1][t]);
@@ -289,68 +314,77 @@ struct SubgridStressSpec {
     }
   }
   __device__ void store(int role, int32_t cell, int32_t nc, const KSum* a, float* part) const {
-    if (role == 0) for (int k = 0; k < 8; ++k) part[(size_t)k * nc + cell] = a[k].get();
-    else { part[(size_t)8 * nc + cell] = a[0].get(); part[(size_t)9 * nc + cell] = a[1].get(); }
+    if (role < 4) {
+      part[(size_t)role * nc + cell] = a[0].get();
+      part[(size_t)(4 + role) * nc + cell] = a[1].get();
+    } else {
+      part[(size_t)8 * nc + cell] = a[0].get();
+      part[(size_t)9 * nc + cell] = a[1].get();
+    }
   }
 };
 
 // Subgrid heat diffusion (SubgridDiffusion.jl:67-175): slots 0-3 dT*w, 4-7 w
+// roles 0-3: one corner each
 struct SubgridHeatSpec {
   static constexpr const char* kName = "k_cells<subgrid_heat>";
-  static constexpr int kRoles = 1, kNV = S_V0 + 1, kAcc = 8;
+  static constexpr int kRoles = 4, kNV = S_V0 + 1, kAcc = 2;
   const float *tk1, *kt1, *rhocp1;  // FP32 mirrors
   float dt, coef, inv_ts;  // inv_ts = 2/xstpavg^2 + 2/ystpavg^2
-  __device__ void stage(const DevMarkers& mk, const DevGrid& g, int32_t m, int t, float (*sv)[kChunk], uint8_t* sfl) const {
-    const int32_t ix = mk.xn[m], iy = mk.yn[m];
-    const float fx = mk.fx[m], fy = mk.fy[m];
-    const W4 w = wts(fx, fy);
+  struct Raw { double tk; int32_t m, xn, yn; float fx, fy; };
+  __device__ Raw load(const DevMarkers& mk, int32_t m) const {
+    return Raw{mk.tk[m], m, mk.xn[m], mk.yn[m], mk.fx[m], mk.fy[m]};
+  }
+  __device__ void put(const Raw& r, const DevMarkers& mk, const DevGrid& g, int t, float (*sv)[kChunk], uint8_t*) const {
+    const W4 w = wts(r.fx, r.fy);
     sv[S_UL][t] = w.ul; sv[S_LL][t] = w.ll; sv[S_UR][t] = w.ur; sv[S_LR][t] = w.lr;
-    sfl[t] = mk.mflags[m];
-    const float tn = gather4f(tk1, g.ynum, iy, ix, fx, fy);
-    const double tm = mk.tk[m];
-    const float k = gather4f(kt1, g.ynum, iy, ix, fx, fy);
-    const float rc = gather4f(rhocp1, g.ynum, iy, ix, fx, fy);
+    const float tn = gather4f(tk1, g.ynum, r.yn, r.xn, r.fx, r.fy);
+    const float k = gather4f(kt1, g.ynum, r.yn, r.xn, r.fx, r.fy);
+    const float rc = gather4f(rhocp1, g.ynum, r.yn, r.xn, r.fx, r.fy);
     const float tsg = rc / k / inv_ts;
     const float term = fmaxf(-coef * dt / tsg, -30.f);
-    const float d = (tn - d2f(tm)) * (-expm1f(term));
-    mk.subgrid_dt[m] = f2d(d);
-    mk.tk[m] = tm + f2d(d);
+    const float d = (tn - d2f(r.tk)) * (-expm1f(term));
+    mk.subgrid_dt[r.m] = f2d(d);
+    mk.tk[r.m] = r.tk + f2d(d);
     sv[S_V0][t] = d;
   }
-  __device__ void accum(int, int t, float (*sv)[kChunk], const uint8_t*, KSum* a) const {
-    const float d = sv[S_V0][t];
-    for (int k = 0; k < 4; ++k) {
-      const float w = sv[S_UL + k][t];
-      a[k].add(w * d);
-      a[4 + k].add(w);
-    }
+  __device__ void accum(int role, int t, float (*sv)[kChunk], const uint8_t*, KSum* a) const {
+    const float w = sv[S_UL + role][t];
+    a[0].add(w * sv[S_V0][t]);
+    a[1].add(w);
   }
-  __device__ void store(int, int32_t cell, int32_t nc, const KSum* a, float* part) const {
-    for (int k = 0; k < 8; ++k) part[(size_t)k * nc + cell] = a[k].get();
+  __device__ void store(int role, int32_t cell, int32_t nc, const KSum* a, float* part) const {
+    part[(size_t)role * nc + cell] = a[0].get();
+    part[(size_t)(4 + role) * nc + cell] = a[1].get();
   }
 };
 
 // ------------------------------------------------------- per-cell kernel ---
-// Block = 32 consecutive cells.  Pass p stages markers [8p, 8p+8) of every cell:
-// thread t loads marker 8p + (t & 7) of cell t >> 3, so eight consecutive
-// threads read eight consecutive entries of one cell's list (coalesced), and
-// writes it to slot (t >> 3) * 9 + (t & 7).  Then warp `role`, lane j folds
+// Block = 256 threads = 32 consecutive cells.  Pass p stages markers
+// [8p, 8p+8) of every cell: thread t owns marker 8p + (t & 7) of cell t >> 3,
+// so eight consecutive threads read eight consecutive entries of one cell's
+// list (coalesced), and stage it to slot (t >> 3) * 9 + (t & 7).  The global
+// loads of pass p+1 are issued into registers before the fold of pass p, so
+// their latency hides behind the fold.  Warp `role` < kRoles, lane j folds
 // cell j's slots j*9 .. j*9+7 in order (stride 9 keeps the 32 lanes on 32
-// different banks).  All 32 lanes stay busy while the cells have markers left,
-// and each cell is folded in its marker order.
+// different banks), so each cell is folded in its marker order.
+constexpr int kThreads = 256;
 constexpr int kPer = 8;             // markers per cell per pass
 constexpr int kSlotStride = kPer + 1;
 static_assert(kChunk >= 32 * kSlotStride, "staging table too small");
+static_assert(kThreads == 32 * kPer, "one staged marker per thread per pass");
 
 template <class S>
-__global__ void __launch_bounds__(32 * S::kRoles) k_cells(S spec, DevMarkers mk, DevGrid g,
-                                                          const int32_t* __restrict__ start,
-                                                          const int32_t* __restrict__ perm, int32_t nc,
-                                                          float* __restrict__ part) {
+__global__ void __launch_bounds__(kThreads) k_cells(S spec, DevMarkers mk, DevGrid g,
+                                                    const int32_t* __restrict__ start,
+                                                    const int32_t* __restrict__ perm, int32_t nc,
+                                                    float* __restrict__ part) {
+  static_assert(S::kRoles <= kThreads / 32, "one warp per role");
   __shared__ float sv[S::kNV][kChunk];
   __shared__ uint8_t sfl[kChunk];
   __shared__ int32_t s_beg[32], s_cnt[32], s_max;
   const int lane = threadIdx.x & 31, role = threadIdx.x >> 5;
+  const int sj = threadIdx.x >> 3, si = threadIdx.x & 7;  // staging cell / marker of this thread
   const int32_t c0 = blockIdx.x * 32;
   if (threadIdx.x < 32) {
     const int32_t cell = c0 + lane;
@@ -365,20 +399,26 @@ __global__ void __launch_bounds__(32 * S::kRoles) k_cells(S spec, DevMarkers mk,
   __syncthreads();
   const int32_t nmax = s_max;
   const int32_t my_cnt = s_cnt[lane];
+  const int32_t st_beg = s_beg[sj], st_cnt = s_cnt[sj];
   KSum acc[S::kAcc];
 #pragma unroll
   for (int k = 0; k < S::kAcc; ++k) acc[k].init();
+  typename S::Raw r;
+  bool have = si < st_cnt;
+  if (have) r = spec.load(mk, __ldg(&perm[st_beg + si]));
   for (int32_t base = 0; base < nmax; base += kPer) {
     __syncthreads();
-    for (int t = threadIdx.x; t < 32 * kPer; t += blockDim.x) {
-      const int j = t >> 3, ii = t & 7, i = base + ii;
-      if (i < s_cnt[j]) spec.stage(mk, g, __ldg(&perm[s_beg[j] + i]), j * kSlotStride + ii, sv, sfl);
-    }
+    if (have) spec.put(r, mk, g, sj * kSlotStride + si, sv, sfl);
     __syncthreads();
-    const int n = min(kPer, my_cnt - base);
-    for (int i = 0; i < n; ++i) spec.accum(role, lane * kSlotStride + i, sv, sfl, acc);
+    const int32_t nxt = base + kPer + si;
+    have = nxt < st_cnt;
+    if (have) r = spec.load(mk, __ldg(&perm[st_beg + nxt]));
+    if (role < S::kRoles) {
+      const int n = min(kPer, my_cnt - base);
+      for (int i = 0; i < n; ++i) spec.accum(role, lane * kSlotStride + i, sv, sfl, acc);
+    }
   }
-  if (c0 + lane < nc) spec.store(role, c0 + lane, nc, acc, part);
+  if (role < S::kRoles && c0 + lane < nc) spec.store(role, c0 + lane, nc, acc, part);
 }
 
 template <class S>
@@ -386,7 +426,7 @@ int run_cells(eb_ctx* c, const S& spec) {
   const int32_t nc = c->cs.ncells;
   const unsigned blocks = (unsigned)((nc + 31) / 32);
   EB_PROF(c, S::kName);
-  k_cells<S><<<blocks, 32 * S::kRoles, 0, c->stream>>>(spec, dev_markers(c), c->g, c->cs.start, c->cs.perm, nc, c->part);
+  k_cells<S><<<blocks, kThreads, 0, c->stream>>>(spec, dev_markers(c), c->g, c->cs.start, c->cs.perm, nc, c->part);
   EB_LAUNCHED(c);
   return EB_OK;
 }
