@@ -123,6 +123,21 @@ class MarkerInCell:
         self._params = dict(params)
         self._check(self._lib.eb_set_params(self._ctx, C.byref(p)))
 
+    def set_stokes_params(self, params: dict) -> None:
+        """Gravity, interface stabilisation, pressure boundary condition and internal velocity zone."""
+        p = _abi.StokesParams()
+        p.gravity_x = float(params.get("gravity_x", 0.0))
+        p.gravity_y = float(params.get("gravity_y", 9.81))
+        p.iuse_interface_stabilization = int(params.get("iuse_interface_stabilization", 0))
+        p.pressure_bc_mode = int(params.get("pressure_bc_mode", 0))
+        p.pressure_bc = float(params.get("pressure_bc", 0.0))
+        zone = np.asarray(params.get("bintern_zone", [-1, 0, 0, 0, -1, 0, 0, 0]), dtype=np.int64)
+        vel = np.asarray(params.get("bintern_velocity", np.zeros(8)), dtype=np.float64)
+        for k in range(8):
+            p.bintern_zone[k] = int(zone[k])
+            p.bintern_velocity[k] = float(vel[k])
+        self._check(self._lib.eb_set_stokes_params(self._ctx, C.byref(p)))
+
     def resize_markers(self, marknum: int) -> None:
         self._check(self._lib.eb_resize_markers(self._ctx, int(marknum)))
         self.marknum = int(marknum)
@@ -165,6 +180,8 @@ class MarkerInCell:
         self.set_grid(model.grid)
         self.set_materials(model.mats)
         self.set_params(model.params)
+        if "gravity_y" in model.params:
+            self.set_stokes_params(model.params)
         self.resize_markers(model.marknum)
         for k, v in model.markers.items():
             if k in ("xn", "yn", "xn_vy", "yn_vy"):
@@ -245,6 +262,88 @@ class MarkerInCell:
     def update_marker_strain(self) -> None:
         """Advection.update_marker_strain! (Advection.jl:169-178)."""
         self._call("eb_update_marker_strain")
+
+    # -------------------------------------------- Stokes-continuity step ---
+    def calc_viscoelastic_terms(self) -> None:
+        """StokesViscoelasticTerms.calc_viscoelastic_terms! (StokesViscoelasticTerms.jl:26-125)."""
+        self._call("eb_calc_viscoelastic_terms")
+
+    def viscoelastic_rhs(self) -> None:
+        """StokesContinuityRhs.viscoelastic_rhs! (StokesContinuityRhs.jl:30-190)."""
+        self._call("eb_viscoelastic_rhs")
+
+    def build_system_of_equations(self) -> None:
+        """SystemSolver.initialize_solver! + StokesBuildManager.build_system_of_equations
+        (SystemSolver.jl:99-115, StokesBuildManager.jl:661-712), kept on the device."""
+        self._call("eb_build_stokes_system")
+
+    def solve_system(self, rtol: float = 1e-8, max_iters: int = 0, restart: int = 0, mg_sweeps: int = 0,
+                     use_initial_guess: bool = False, check: bool = True) -> dict:
+        """The Stokes solve (replaces SystemSolver.solve_system_optimized, SystemSolver.jl:67-91)."""
+        o = _abi.SolveOpts(rtol, max_iters, restart, mg_sweeps, int(use_initial_guess))
+        r = _abi.SolveReport()
+        rc = self._lib.eb_solve_stokes_system(self._ctx, C.byref(o), C.byref(r))
+        rep = {"status": rc, "iterations": r.iterations, "levels": r.levels, "rel_residual": r.rel_residual,
+               "rel_residual_scaled": r.rel_residual_scaled, "seconds": r.seconds}
+        if check:
+            self._check(rc)
+        return rep
+
+    def process_stokes_solution(self) -> None:
+        """SystemSolver.process_stokes_solution! (SystemSolver.jl:141-271)."""
+        self._call("eb_process_stokes_solution")
+
+    def stokes_nonlinear_residual(self) -> np.ndarray:
+        """StokesResiduals.stokes_calc_nonlinear_system_residual_optimized! (StokesResiduals.jl:63-81)."""
+        self._call("eb_stokes_nonlinear_residual")
+        return self.download_stokes_vector("resnl")
+
+    def backup_stokes_solution(self) -> None:
+        """The S part of SystemSolver.backup_stokes_arrays! (SystemSolver.jl:306-318)."""
+        self._call("eb_backup_stokes_solution")
+
+    @property
+    def stokes_size(self) -> int:
+        return int(self._lib.eb_stokes_size(self._ctx))
+
+    @property
+    def pscale(self) -> float:
+        return float(self._lib.eb_stokes_pscale(self._ctx))
+
+    def stokes_apply(self, x: np.ndarray) -> np.ndarray:
+        """y = L x with the assembled operator (interleaved N-vectors)."""
+        a = np.ascontiguousarray(x, dtype=np.float64)
+        y = np.empty(self.stokes_size)
+        self._check(self._lib.eb_stokes_apply(self._ctx, _ptr(a), _ptr(y)))
+        return y
+
+    def download_stokes_vector(self, name: str) -> np.ndarray:
+        y = np.empty(self.stokes_size)
+        self._check(self._lib.eb_stokes_vector_download(self._ctx, _abi.STOKES_VECTORS[name], _ptr(y)))
+        return y
+
+    def upload_stokes_vector(self, name: str, values: np.ndarray) -> None:
+        a = np.ascontiguousarray(values, dtype=np.float64)
+        if a.shape != (self.stokes_size,):
+            raise ValueError(f"expected {self.stokes_size} values")
+        self._check(self._lib.eb_stokes_vector_upload(self._ctx, _abi.STOKES_VECTORS[name], _ptr(a)))
+
+    def stokes_stencil(self) -> np.ndarray:
+        """The assembled coefficients as a (27, xnum-1, ynum-1) array indexed [slot, j, i]."""
+        nx, ny = self.xnum - 1, self.ynum - 1
+        a = np.empty(27 * nx * ny)
+        self._check(self._lib.eb_stokes_stencil_download(self._ctx, _ptr(a)))
+        return a.reshape(27, nx, ny)
+
+    def solve_viscoelastic_stokes_continuity_equations(self, **solve_kw) -> dict:
+        """StokesContinuitySolver.solve_viscoelastic_stokes_continuity_equations!
+        (StokesContinuitySolver.jl:68-110): build steps, solve, unpack."""
+        self.calc_viscoelastic_terms()
+        self.viscoelastic_rhs()
+        self.build_system_of_equations()
+        rep = self.solve_system(**solve_kw)
+        self.process_stokes_solution()
+        return rep
 
     # ----------------------------------------------------- step sequences --
     def marker_cycle(self) -> None:

@@ -38,6 +38,10 @@ GRID_FIELDS = [
     "vx1", "vy1", "rho1_vy", "rho0_vy", "wtnodes_vy",
     # thermal BC coefficients
     "btopt", "bbottomt", "bleftt", "brightt",
+    # Stokes right-hand sides, plastic strain rate at pressure nodes
+    "RX1", "RY1", "RC1", "eii_plastic_pressure",
+    # velocity BC coefficients
+    "btopx", "bbottomx", "btopy", "bbottomy", "bleftx", "brightx", "blefty", "brighty",
 ]
 GRID_ID = {n: i for i, n in enumerate(GRID_FIELDS)}
 
@@ -52,9 +56,19 @@ def grid_shape(name: str, xnum: int, ynum: int) -> tuple[int, int]:
         return (ynum + 1, xnum)
     if i <= GRID_ID["wtnodes_vy"]:
         return (ynum, xnum + 1)
-    if name in ("btopt", "bbottomt"):
+    if name in ("btopt", "bbottomt", "btopx", "bbottomx"):
         return (xnum, 2)
-    return (ynum, 2)
+    if name in ("bleftt", "brightt", "blefty", "brighty"):
+        return (ynum, 2)
+    if name in ("btopy", "bbottomy"):
+        return (xnum + 1, 2)
+    if name in ("bleftx", "brightx"):
+        return (ynum + 1, 2)
+    if name == "RX1":
+        return (ynum + 1, xnum)
+    if name == "RY1":
+        return (ynum, xnum + 1)
+    return (ynum - 1, xnum - 1)   # RC1, eii_plastic_pressure
 
 
 class GridDesc(C.Structure):
@@ -86,6 +100,29 @@ class Params(C.Structure):
     ]
 
 
+class StokesParams(C.Structure):
+    _fields_ = [("gravity_x", C.c_double), ("gravity_y", C.c_double), ("iuse_interface_stabilization", C.c_int64),
+                ("pressure_bc_mode", C.c_int64), ("pressure_bc", C.c_double),
+                ("bintern_zone", C.c_int64 * 8), ("bintern_velocity", C.c_double * 8)]
+
+
+class SolveOpts(C.Structure):
+    _fields_ = [("rtol", C.c_double), ("max_iters", C.c_int32), ("restart", C.c_int32), ("mg_sweeps", C.c_int32),
+                ("use_initial_guess", C.c_int32)]
+
+
+class SolveReport(C.Structure):
+    _fields_ = [("iterations", C.c_int32), ("levels", C.c_int32), ("rel_residual", C.c_double),
+                ("rel_residual_scaled", C.c_double), ("seconds", C.c_double)]
+
+
+STOKES_VECTORS = {"solution": 0, "rhs": 1, "solution_old": 2, "resnl": 3}
+
+STOKES_ENTRY_POINTS = [
+    "eb_calc_viscoelastic_terms", "eb_viscoelastic_rhs", "eb_build_stokes_system", "eb_process_stokes_solution",
+    "eb_stokes_nonlinear_residual", "eb_backup_stokes_solution",
+]
+
 ENTRY_POINTS = [
     "eb_get_marker_inside_flags", "eb_initialize_bilinear_interpolation",
     "eb_interpolate_marker_stokes_parameters_to_grid", "eb_interpolate_marker_heat_parameters_to_grid",
@@ -100,7 +137,10 @@ ALL_SYMBOLS = [
     "eb_resize_markers", "eb_marker_upload", "eb_marker_download", "eb_grid_upload", "eb_grid_download",
     "eb_marker_device_ptr", "eb_grid_device_ptr", "eb_stream", "eb_launch_count",
     "eb_update_marker_viscoplastic_viscosity", "eb_profile_enable", "eb_profile_count", "eb_profile_entry",
-] + ENTRY_POINTS
+    "eb_set_stokes_params", "eb_solve_stokes_system", "eb_stokes_apply", "eb_stokes_vector_upload",
+    "eb_stokes_vector_download", "eb_stokes_stencil_download", "eb_stokes_pscale", "eb_stokes_size",
+    "eb_marker_to_basic_grid_average_noalloc",
+] + ENTRY_POINTS + STOKES_ENTRY_POINTS
 
 _lib = None
 
@@ -138,10 +178,22 @@ def load(path: pathlib.Path | str | None = None) -> C.CDLL:
     lib.eb_profile_count.argtypes = [vp]
     lib.eb_profile_entry.argtypes = [vp, C.c_int, C.c_char_p, C.c_int, C.POINTER(C.c_double),
                                      C.POINTER(C.c_int64)]
-    for name in ENTRY_POINTS:
+    for name in ENTRY_POINTS + STOKES_ENTRY_POINTS:
         getattr(lib, name).argtypes = [vp]
+    lib.eb_set_stokes_params.argtypes = [vp, C.POINTER(StokesParams)]
+    lib.eb_solve_stokes_system.argtypes = [vp, C.POINTER(SolveOpts), C.POINTER(SolveReport)]
+    lib.eb_stokes_apply.argtypes = [vp, vp, vp]
+    lib.eb_stokes_vector_upload.argtypes = [vp, C.c_int, vp]
+    lib.eb_stokes_vector_download.argtypes = [vp, C.c_int, vp]
+    lib.eb_stokes_stencil_download.argtypes = [vp, vp]
+    lib.eb_stokes_pscale.argtypes = [vp]
+    lib.eb_stokes_pscale.restype = C.c_double
+    lib.eb_stokes_size.argtypes = [vp]
+    lib.eb_stokes_size.restype = C.c_int64
+    lib.eb_marker_to_basic_grid_average_noalloc.argtypes = [vp, vp, vp, C.c_int64, vp, C.c_int64, vp, C.c_int64,
+                                                            vp, vp, vp, C.c_char_p, C.c_size_t]
     for name in ALL_SYMBOLS:
-        if name not in ("eb_last_error", "eb_stream", "eb_launch_count"):
+        if name not in ("eb_last_error", "eb_stream", "eb_launch_count", "eb_stokes_pscale", "eb_stokes_size"):
             getattr(lib, name).restype = C.c_int
     if path is None:
         _lib = lib

@@ -17,7 +17,10 @@ CSRC = PKG / "csrc"
 BUILD = PKG / "_build"
 LIB = BUILD / "libebgpu.so"
 SOURCES = ["eb_ctx.cu", "eb_locate.cu", "eb_scatter.cu", "eb_gather.cu", "eb_advect.cu", "eb_rheology.cu",
-           "eb_noalloc.cu"]
+           "eb_noalloc.cu", "eb_stokes_build.cu", "eb_stokes_solve.cu"]
+# The Stokes assembly reproduces the reference's FP64 coefficients operation by
+# operation, so no multiply-add contraction there.
+EXTRA_FLAGS = {"eb_stokes_build.cu": ["-fmad=false"]}
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall"]
 
@@ -49,7 +52,7 @@ def build(force: bool = False, verbose: bool = False) -> pathlib.Path:
 
     def compile_one(src: str) -> pathlib.Path:
         obj = BUILD / (pathlib.Path(src).stem + ".o")
-        cmd = [nvcc, *ARCH, *FLAGS, "-c", str(CSRC / src), "-o", str(obj)]
+        cmd = [nvcc, *ARCH, *FLAGS, *EXTRA_FLAGS.get(src, []), "-c", str(CSRC / src), "-o", str(obj)]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"nvcc failed for {src}:\n{r.stderr}")

@@ -18,14 +18,17 @@ int eb_cuda(eb_ctx* c, cudaError_t e, const char* what) {
 }
 
 // ---------------------------------------------------------------- shapes ---
-enum Shape { SH_B, SH_P, SH_VX, SH_VY, SH_BCX, SH_BCY };
+enum Shape { SH_B, SH_P, SH_VX, SH_VY, SH_BCX, SH_BCY, SH_BCX1, SH_BCY1 };
 static Shape grid_shape(int f) {
   if (f <= EB_G_PLASTIC_YIELD) return SH_B;
   if (f <= EB_G_PR1) return SH_P;
-  if (f == EB_G_VX1) return SH_VX;
-  if (f <= EB_G_WTNODES_VY) return SH_VY;
-  if (f == EB_G_BTOPT || f == EB_G_BBOTTOMT) return SH_BCX;
-  return SH_BCY;
+  if (f == EB_G_VX1 || f == EB_G_RX1) return SH_VX;
+  if (f <= EB_G_WTNODES_VY || f == EB_G_RY1) return SH_VY;
+  if (f == EB_G_RC1 || f == EB_G_EII_PLASTIC_PRESSURE) return SH_P;
+  if (f == EB_G_BTOPT || f == EB_G_BBOTTOMT || f == EB_G_BTOPX || f == EB_G_BBOTTOMX) return SH_BCX;
+  if (f == EB_G_BTOPY || f == EB_G_BBOTTOMY) return SH_BCX1;
+  if (f == EB_G_BLEFTX || f == EB_G_BRIGHTX) return SH_BCY1;
+  return SH_BCY;  // bleftt, brightt, blefty, brighty
 }
 size_t grid_field_count(const eb_ctx* c, int f) {
   const size_t X = c->xnum, Y = c->ynum;
@@ -35,6 +38,8 @@ size_t grid_field_count(const eb_ctx* c, int f) {
     case SH_VX: return (Y + 1) * X;
     case SH_VY: return Y * (X + 1);
     case SH_BCX: return X * 2;
+    case SH_BCX1: return (X + 1) * 2;
+    case SH_BCY1: return (Y + 1) * 2;
     default: return Y * 2;
   }
 }
@@ -239,6 +244,7 @@ extern "C" int eb_destroy(eb_ctx* c) {
   cudaStreamSynchronize(c->stream);
   free_grid_tables(c);
   free_markers(c);
+  stokes_free(c);
   for (void* p : c->mat_allocs) cudaFree(p);
   for (cudaEvent_t e : c->prof.pool) cudaEventDestroy(e);
   cudaFree(c->dflag);
@@ -317,6 +323,10 @@ extern "C" int eb_set_grid(eb_ctx* c, const eb_grid_desc* G) {
     for (int32_t i = 0; i < Y - 1; ++i) rsy[i] = 1.0 / G->ystp_b[i];
     if ((rc = upload_vec(c, c->grid_allocs, rsx, &g.rsx)) || (rc = upload_vec(c, c->grid_allocs, rsy, &g.rsy))) return rc;
   }
+  if ((rc = up(G->xstp_vy, X, &c->g_xstp_vy)) || (rc = up(G->ystp_vx, Y, &c->g_ystp_vx))) return rc;
+  c->h_gx.assign(G->gridx_b, G->gridx_b + X);
+  c->h_gy.assign(G->gridy_b, G->gridy_b + Y);
+  stokes_free(c);  // the Stokes system and its multigrid hierarchy follow the grid
   if ((rc = build_axis(c, G->gridx_b, X, &g.ax)) || (rc = build_axis(c, G->gridy_b, Y, &g.ay)) ||
       (rc = build_axis(c, G->gridx_vy, X + 1, &g.axvy)))
     return rc;

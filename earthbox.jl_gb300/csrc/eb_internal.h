@@ -68,6 +68,8 @@ struct Profiler {
   const char* open_name = nullptr;
 };
 
+struct StokesState;  // eb_stokes_solve.cu
+
 struct eb_ctx {
   int device = 0;
   cudaStream_t stream = nullptr;
@@ -79,6 +81,8 @@ struct eb_ctx {
   int32_t xnum = 0, ynum = 0;
   std::vector<void*> grid_allocs;  // coordinate tables
   DevGrid g{};
+  const double *g_xstp_vy = nullptr, *g_ystp_vx = nullptr;  // FP64 staggered spacings (device)
+  std::vector<double> h_gx, h_gy;                             // basic coordinates (host)
   double* gf[EB_G_NFIELDS] = {};
   float* gf32[EB_G_NFIELDS] = {};  // FP32 mirrors of grids read by the gathers
   // materials
@@ -96,7 +100,34 @@ struct eb_ctx {
   float* part = nullptr;     // [kMaxSlots * ncells]
   int32_t* dflag = nullptr;  // device status word written by kernels (0 = ok)
   Profiler prof;
+  // Stokes-continuity step
+  eb_stokes_params SP{};
+  bool have_stokes_params = false;
+  StokesState* st = nullptr;
 };
+
+// Stokes system storage shared by the assembly (eb_stokes_build.cu) and the
+// solver (eb_stokes_solve.cu).  Vectors are SoA blocks [vx | vy | p] of nc
+// cells each, cell c = j*ny + i (0-based column j, row i), i.e. the
+// reference's interleaved index 3c + {0, 1, 2}.
+constexpr int kStencilSlots = 27;  // 11 x-Stokes, 11 y-Stokes, 5 continuity
+struct StokesSystem {
+  int32_t nx = 0, ny = 0;  // cells: xnum-1, ynum-1
+  int64_t nc = 0;          // nx * ny
+  double* coef = nullptr;  // [27][nc]
+  double* rhs = nullptr;   // [3][nc]
+  double* S = nullptr;     // [3][nc] solution
+  double* S_old = nullptr; // [3][nc]
+  double* resnl = nullptr; // [3][nc]
+  double pscale = 0.0;
+  bool built = false;
+};
+StokesSystem* stokes_system(eb_ctx* c);            // allocated on first use for the current grid
+void stokes_free(eb_ctx* c);
+int launch_viscoelastic_terms(eb_ctx* c);
+int launch_viscoelastic_rhs(eb_ctx* c);
+int launch_build_stokes_system(eb_ctx* c, StokesSystem* s);
+int launch_process_stokes_solution(eb_ctx* c, const StokesSystem* s);
 
 constexpr int kMaxSlots = 48;
 

@@ -30,15 +30,17 @@ __global__ void k_inside_flags(const double* __restrict__ x, const double* __res
 // fl rounds to nearest even: fl(q) <= 0.5 <=> q <= 0.5 + 2^-54 and
 // fl(q) >= 0.5 <=> q >= 0.5 - 2^-55.  With t = d - 0.5 s (exact near the
 // boundary by Sterbenz's lemma) these become t <= s 2^-54 and t >= -s 2^-55.
-__device__ __forceinline__ void half_tests(float f, double d, double s, bool& le, bool& ge) {
-  if (fabsf(f - 0.5f) > 1e-7f) {  // the FP32 offset errs by < 3e-8
-    le = f < 0.5f;
-    ge = !le;
-  } else {
-    double t = d - 0.5 * s;
-    le = t <= s * 0x1p-54;
-    ge = t >= -s * 0x1p-55;
-  }
+// Kept out of line: only markers within 1e-7 of the half line reach it, and
+// an inlined copy would be if-converted and run on every marker's FP64 pipe.
+__device__ __noinline__ uint32_t exact_half_bits(double d, double s) {
+  const double t = d - 0.5 * s;
+  return (t <= s * 0x1p-54 ? 1u : 0u) | (t >= -s * 0x1p-55 ? 2u : 0u);
+}
+// bit 0: fl(d/s) <= 0.5, bit 1: fl(d/s) >= 0.5; the FP32 offset f errs by < 3e-8
+__device__ __forceinline__ uint32_t half_bits(float f, double d,
+                                              const double* __restrict__ s_tab, int32_t k) {
+  if (fabsf(f - 0.5f) > 1e-7f) return f < 0.5f ? 1u : 2u;
+  return exact_half_bits(d, __ldg(&s_tab[k]));
 }
 
 __global__ void k_locate_count(DevMarkers mk, DevGrid g, int32_t* __restrict__ count,
@@ -61,13 +63,12 @@ __global__ void k_locate_count(DevMarkers mk, DevGrid g, int32_t* __restrict__ c
       // |fx - fl64(dx)| <= 2^-25 fx + 2^-52, i.e. below 3e-8 on [0, 1]
       const float fx = d2f(dxd * __ldg(&g.rsx[ix - 1]));
       const float fy = d2f(dyd * __ldg(&g.rsy[iy - 1]));
-      bool le, ge;
-      half_tests(fx, dxd, __ldg(&g.sx[ix - 1]), le, ge);
-      if (le) fl |= MF_XLE;
-      if (ge) fl |= MF_XGE;
-      half_tests(fy, dyd, __ldg(&g.sy[iy - 1]), le, ge);
-      if (le) fl |= MF_YLE;
-      if (ge) fl |= MF_YGE;
+      const uint32_t hx = half_bits(fx, dxd, g.sx, ix - 1);
+      const uint32_t hy = half_bits(fy, dyd, g.sy, iy - 1);
+      if (hx & 1u) fl |= MF_XLE;
+      if (hx & 2u) fl |= MF_XGE;
+      if (hy & 1u) fl |= MF_YLE;
+      if (hy & 2u) fl |= MF_YGE;
       mk.xn[m] = ix;
       mk.yn[m] = iy;
       mk.fx[m] = fx;

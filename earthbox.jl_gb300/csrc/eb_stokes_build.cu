@@ -1,0 +1,446 @@
+// eb_stokes_build.cu -- Stokes-continuity system assembly on the GPU, FP64.
+//
+// Reference (paths under src/stokes_continuity_solver/):
+//   solver/rhs/StokesViscoelasticTerms.jl:26-125   viscoelastic viscosity/stress terms
+//   solver/rhs/StokesContinuityRhs.jl:30-190       RX1, RY1, RC1
+//   solver/system_solver/SystemSolver.jl:99-115    initialize_solver!, pscale
+//   solver/build_system/StokesBuildManager.jl:661-712 and the stencil modules
+//     discretize_{x,y}_stokes_equation/, discretize_continuity_equation/
+//   solver/system_solver/SystemSolver.jl:188-271   reload_solu_vel!, apply_vel_bc!
+//
+// The reference assembles a COO list (Li, Lj, Lv) row by row; here one thread
+// per basic cell writes that cell's three rows into a stored 27-slot stencil.
+// Every coefficient is computed with the reference's operand order and the
+// boundary folds are added in the reference's order, and this file is built
+// with -fmad=false, so each slot holds exactly the reference's Lv value (the
+// sum of the reference's duplicate entries where a fold hits an existing one).
+#include "eb_internal.h"
+
+namespace {
+
+// 1-based column-major access, as in Julia
+#define A2(a, rows, i, j) (a)[((int64_t)(j) - 1) * (int64_t)(rows) + ((int64_t)(i) - 1)]
+
+constexpr int kB = 256;
+
+// ---- StokesViscoelasticTerms.jl:51-125 --------------------------------------
+// Viscoelastic.calculate_viscoelastic_factor (utils/Viscoelastic.jl:26-38): eta / (eta + dt mu)
+__global__ void k_ve_terms(const double* __restrict__ eta1, const double* __restrict__ mu1,
+                           const double* __restrict__ s1, double* __restrict__ eta0, double* __restrict__ s0,
+                           int64_t n, double dt) {
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  const double e = eta1[k];
+  const double f = e / (e + dt * mu1[k]);
+  eta0[k] = e * (1.0 - f);
+  s0[k] = s1[k] * f;
+}
+
+// ---- StokesContinuityRhs.jl:63-157 ------------------------------------------
+// One thread per basic node (i, j), i in 2..ynum, j in 2..xnum; RY1 then RX1 rules.
+__global__ void k_rhs_xy(int32_t xnum, int32_t ynum, double gx, double gy, int32_t stab,
+                         const double* __restrict__ xstp_b, const double* __restrict__ ystp_b,
+                         const double* __restrict__ xstp_vy, const double* __restrict__ ystp_vx,
+                         const double* __restrict__ rho1, const double* __restrict__ rho1_vy,
+                         const double* __restrict__ sxx0, const double* __restrict__ sxy0,
+                         double* __restrict__ RX1, double* __restrict__ RY1) {
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= (int64_t)(xnum - 1) * (ynum - 1)) return;
+  const int32_t i = (int32_t)(k % (ynum - 1)) + 2, j = (int32_t)(k / (ynum - 1)) + 2;
+  const int32_t yp = ynum - 1;
+  if (i != ynum) {  // Domain.basic_node_along_lower_boundary
+    double r;
+    if (stab == 1) r = -gy * A2(rho1_vy, ynum, i, j);
+    else r = -gy * (A2(rho1, ynum, i, j) + A2(rho1, ynum, i, j - 1)) / 2;
+    r += (A2(sxx0, yp, i, j - 1) - A2(sxx0, yp, i - 1, j - 1)) / ystp_vx[i - 1];
+    r -= (A2(sxy0, ynum, i, j) - A2(sxy0, ynum, i, j - 1)) / xstp_b[j - 2];
+    A2(RY1, ynum, i, j) = r;
+  }
+  if (j != xnum) {  // Domain.basic_node_on_right_boundary
+    double r = -gx * (A2(rho1, ynum, i, j) + A2(rho1, ynum, i - 1, j)) / 2;
+    r -= (A2(sxx0, yp, i - 1, j) - A2(sxx0, yp, i - 1, j - 1)) / xstp_vy[j - 1];
+    r -= (A2(sxy0, ynum, i, j) - A2(sxy0, ynum, i - 1, j)) / ystp_b[i - 2];
+    A2(RX1, ynum + 1, i, j) = r;
+  }
+}
+
+// calc_plastic_volumetric_effect (StokesContinuityRhs.jl:159-190): 2 sin(dil pi/180) eii_plastic
+__global__ void k_rhs_c(const double* __restrict__ dil, const double* __restrict__ eii, double* __restrict__ RC1,
+                        int64_t n) {
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  const double rad = dil[k] * 3.14159265358979323846 / 180.0;
+  RC1[k] = 2.0 * sin(rad) * eii[k];
+}
+
+// ---- StokesBuildManager.jl:661-712 ------------------------------------------
+struct BuildIn {
+  int32_t xnum, ynum;
+  double xstpavg, ystpavg, pscale, timestep, gravity_y, pressure_bc;
+  int32_t stab, pressure_bc_mode;
+  int64_t zone[8];
+  double zvel[8];
+  const double *xstp, *ystp, *xstpc, *ystpc;
+  const double *btopx, *bbottomx, *btopy, *bbottomy, *bleftx, *brightx, *blefty, *brighty;
+  const double *etan, *etas, *rho_vy, *RX, *RY, *RC;
+};
+
+// slot numbers inside each row
+enum { X_C = 0, X_L, X_R, X_U, X_D, X_YUL, X_YUR, X_YLL, X_YLR, X_PL, X_PR };
+enum { Y_C = 0, Y_U, Y_D, Y_L, Y_R, Y_XUL, Y_XUR, Y_XLL, Y_XLR, Y_PU, Y_PD };
+enum { C_C = 0, C_XL, C_XR, C_YU, C_YD };
+
+__global__ void k_build_system(BuildIn b, double* __restrict__ coef, double* __restrict__ rhs, int64_t nc) {
+  const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= nc) return;
+  const int32_t ny = b.ynum - 1;
+  const int32_t i = (int32_t)(c % ny) + 1, j = (int32_t)(c / ny) + 1;  // 1-based cell (i, j)
+  const double *xstp = b.xstp, *ystp = b.ystp, *xstpc = b.xstpc, *ystpc = b.ystpc;
+#define ETAN(ii, jj) A2(b.etan, b.ynum - 1, ii, jj)
+#define ETAS(ii, jj) A2(b.etas, b.ynum, ii, jj)
+#define RHOVY(ii, jj) A2(b.rho_vy, b.ynum, ii, jj)
+#define BX(a, k, col) A2(b.a, b.xnum, k, col)
+#define BX1(a, k, col) A2(b.a, b.xnum + 1, k, col)
+#define BY1(a, k, col) A2(b.a, b.ynum + 1, k, col)
+#define BY(a, k, col) A2(b.a, b.ynum, k, col)
+  double x[11] = {0}, y[11] = {0}, p[5] = {0};
+  double Rx, Ry, Rc;
+  const double kbond = 2.0 * b.pscale / (b.xstpavg + b.ystpavg);
+  const bool top = (i == 1), left = (j == 1);
+  // ---- x-Stokes (StencilForVxStokesUnknown.jl) ----
+  const bool out_x = j != b.zone[0] || i < b.zone[1] || i > b.zone[2];
+  if (!(j < b.xnum - 1 && out_x)) {  // boundary/BoundaryCells.jl:64-95
+    x[X_C] = kbond;
+    Rx = out_x ? 0.0 : 2.0 * b.pscale / (b.xstpavg + b.ystpavg) * b.zvel[3];
+  } else {
+    const bool bot = i >= b.ynum - 1, right2 = j >= b.xnum - 2;
+    // CentralVelocityXNode.jl:6-45
+    x[X_C] = -2.0 * (ETAN(i, j + 1) / xstp[j] + ETAN(i, j) / xstp[j - 1]) / xstpc[j] -
+             (ETAS(i + 1, j + 1) / ystpc[i] + ETAS(i, j + 1) / ystpc[i - 1]) / ystp[i - 1];
+    Rx = A2(b.RX, b.ynum + 1, i + 1, j + 1);
+    // LeftVelocityXNode.jl:7-79
+    if (!left) {
+      x[X_L] = 2.0 * ETAN(i, j) / xstp[j - 1] / xstpc[j];
+    } else {
+      x[X_C] = x[X_C] + BY1(bleftx, i + 1, 2) * 2.0 * ETAN(i, j) / xstp[j - 1] / xstpc[j];
+      Rx = Rx - BY1(bleftx, i + 1, 1) * 2.0 * ETAN(i, j) / xstp[j - 1] / xstpc[j];
+    }
+    // RightVelocityXNode.jl:7-59
+    if (!right2) {
+      x[X_R] = 2.0 * ETAN(i, j + 1) / xstp[j] / xstpc[j];
+    } else {
+      x[X_C] = x[X_C] + BY1(brightx, i + 1, 2) * 2.0 * ETAN(i, j + 1) / xstp[j] / xstpc[j];
+      Rx = Rx - BY1(brightx, i + 1, 1) * 2.0 * ETAN(i, j + 1) / xstp[j] / xstpc[j];
+    }
+    // UpperVelocityXNode.jl:7-52
+    if (!top) {
+      x[X_U] = ETAS(i, j + 1) / ystpc[i - 1] / ystp[i - 1];
+    } else {
+      x[X_C] = x[X_C] + BX(btopx, j + 1, 2) * ETAS(i, j + 1) / ystpc[i - 1] / ystp[i - 1];
+      Rx = Rx - BX(btopx, j + 1, 1) * ETAS(i, j + 1) / ystpc[i - 1] / ystp[i - 1];
+    }
+    // BottomVelocityXNode.jl:7-52
+    if (!bot) {
+      x[X_D] = ETAS(i + 1, j + 1) / ystpc[i] / ystp[i - 1];
+    } else {
+      x[X_C] = x[X_C] + BX(bbottomx, j + 1, 2) * ETAS(i + 1, j + 1) / ystpc[i] / ystp[i - 1];
+      Rx = Rx - BX(bbottomx, j + 1, 1) * ETAS(i + 1, j + 1) / ystpc[i] / ystp[i - 1];
+    }
+    // UpperLeftVelocityYNode.jl:7-64, UpperRightVelocityYNode.jl:7-63
+    if (!top) {
+      x[X_YUL] = ETAS(i, j + 1) / xstpc[j] / ystp[i - 1];
+      x[X_YUR] = -ETAS(i, j + 1) / xstpc[j] / ystp[i - 1];
+    } else {
+      x[X_YLL] = BX1(btopy, j + 1, 2) * ETAS(i, j + 1) / xstpc[j] / ystp[i - 1];
+      Rx = Rx - BX1(btopy, j + 1, 1) * ETAS(i, j + 1) / xstpc[j] / ystp[i - 1];
+      x[X_YLR] = -BX1(btopy, j + 2, 2) * ETAS(i, j + 1) / xstpc[j] / ystp[i - 1];
+      Rx = Rx + BX1(btopy, j + 2, 1) * ETAS(i, j + 1) / xstpc[j] / ystp[i - 1];
+    }
+    // BottomLeftVelocityYNode.jl:8-72
+    if (!bot) {
+      if (!top) x[X_YLL] = -ETAS(i + 1, j + 1) / xstpc[j] / ystp[i - 1];
+      else x[X_YLL] = x[X_YLL] - ETAS(i + 1, j + 1) / xstpc[j] / ystp[i - 1];
+    } else {
+      x[X_YUL] = x[X_YUL] - BX1(bbottomy, j + 1, 2) * ETAS(i + 1, j + 1) / xstpc[j] / ystp[i - 1];
+      Rx = Rx + BX1(bbottomy, j + 1, 1) * ETAS(i + 1, j + 1) / xstpc[j] / ystp[i - 1];
+    }
+    // BottomRightVelocityYNode.jl:8-67
+    if (!bot) {
+      if (!top) x[X_YLR] = ETAS(i + 1, j + 1) / xstpc[j] / ystp[i - 1];
+      else x[X_YLR] = x[X_YLR] + ETAS(i + 1, j + 1) / xstpc[j] / ystp[i - 1];
+    } else {
+      x[X_YUR] = x[X_YUR] + BX1(bbottomy, j + 2, 2) * ETAS(i + 1, j + 1) / xstpc[j] / ystp[i - 1];
+      Rx = Rx - BX1(bbottomy, j + 2, 1) * ETAS(i + 1, j + 1) / xstpc[j] / ystp[i - 1];
+    }
+    // LeftAndRightPressureNodes.jl:6-54
+    x[X_PL] = b.pscale / xstpc[j];
+    x[X_PR] = -b.pscale / xstpc[j];
+  }
+  // ---- y-Stokes (StencilForVyStokesUnknown.jl) ----
+  const bool out_y = j != b.zone[4] || i < b.zone[5] || i > b.zone[6];
+  if (!(i < b.ynum - 1 && out_y)) {  // boundary/BoundaryCells.jl:68-99
+    y[Y_C] = kbond;
+    Ry = out_y ? 0.0 : 2.0 * b.pscale / (b.xstpavg + b.ystpavg) * b.zvel[7];
+  } else {
+    const bool bot2 = i >= b.ynum - 2, right = j >= b.xnum - 1;
+    // InternalCells.calculate_stabilization_terms (:104-175)
+    double dy = 0.0, dx = 0.0;
+    if (b.stab == 1) {
+      const double drhody = ((RHOVY(i + 2, j + 1) - RHOVY(i + 1, j + 1)) / ystp[i] +
+                             (RHOVY(i + 1, j + 1) - RHOVY(i, j + 1)) / ystp[i - 1]) / 2.0;
+      dy = drhody * b.gravity_y * b.timestep;
+      const double drhodx = ((RHOVY(i + 1, j + 2) - RHOVY(i + 1, j + 1)) / xstpc[j] +
+                             (RHOVY(i + 1, j + 1) - RHOVY(i + 1, j)) / xstpc[j - 1]) / 2.0;
+      dx = drhodx * b.gravity_y * b.timestep;
+    }
+    // CentralVelocityYNode.jl:6-44
+    y[Y_C] = -2 * (ETAN(i + 1, j) / ystp[i] + ETAN(i, j) / ystp[i - 1]) / ystpc[i] -
+             (ETAS(i + 1, j + 1) / xstpc[j] + ETAS(i + 1, j) / xstpc[j - 1]) / xstp[j - 1] - dy;
+    Ry = A2(b.RY, b.ynum, i + 1, j + 1);
+    // UpperVelocityYNode.jl:7-51
+    if (!top) {
+      y[Y_U] = 2.0 * ETAN(i, j) / ystp[i - 1] / ystpc[i];
+    } else {
+      y[Y_C] = y[Y_C] + BX1(btopy, j + 1, 2) * 2.0 * ETAN(i, j) / ystp[i - 1] / ystpc[i];
+      Ry = Ry - BX1(btopy, j + 1, 1) * 2.0 * ETAN(i, j) / ystp[i - 1] / ystpc[i];
+    }
+    // BottomVelocityYNode.jl:7-51
+    if (!bot2) {
+      y[Y_D] = 2.0 * ETAN(i + 1, j) / ystp[i] / ystpc[i];
+    } else {
+      y[Y_C] = y[Y_C] + BX1(bbottomy, j + 1, 2) * 2.0 * ETAN(i + 1, j) / ystp[i] / ystpc[i];
+      Ry = Ry - BX1(bbottomy, j + 1, 1) * 2.0 * ETAN(i + 1, j) / ystp[i] / ystpc[i];
+    }
+    // LeftVelocityYNode.jl:7-46
+    if (!left) {
+      y[Y_L] = ETAS(i + 1, j) / xstpc[j - 1] / xstp[j - 1];
+    } else {
+      y[Y_C] = y[Y_C] + BY(blefty, i + 1, 2) * ETAS(i + 1, j) / xstpc[j - 1] / xstp[j - 1];
+      Ry = Ry - BY(blefty, i + 1, 1) * ETAS(i + 1, j) / xstpc[j - 1] / xstp[j - 1];
+    }
+    // RightVelocityYNode.jl:7-47
+    if (!right) {
+      y[Y_R] = ETAS(i + 1, j + 1) / xstpc[j] / xstp[j - 1];
+    } else {
+      y[Y_C] += BY(brighty, i + 1, 2) * ETAS(i + 1, j + 1) / xstpc[j] / xstp[j - 1];
+      Ry -= BY(brighty, i + 1, 1) * ETAS(i + 1, j + 1) / xstpc[j] / xstp[j - 1];
+    }
+    // UpperLeftVelocityXNode.jl:7-78
+    if (!left) {
+      y[Y_XUL] = ETAS(i + 1, j) / ystpc[i] / xstp[j - 1] - dx / 4.0;
+    } else {
+      y[Y_XUR] = BY1(bleftx, i + 1, 2) * (ETAS(i + 1, j) / ystpc[i] / xstp[j - 1] - dx / 4.0);
+      Ry = Ry - BY1(bleftx, i + 1, 1) * (ETAS(i + 1, j) / ystpc[i] / xstp[j - 1] - dx / 4.0);
+    }
+    // BottomLeftVelocityXNode.jl:7-77
+    if (!left) {
+      y[Y_XLL] = -ETAS(i + 1, j) / ystpc[i] / xstp[j - 1] - dx / 4.0;
+    } else {
+      y[Y_XLR] = BY1(bleftx, i + 2, 2) * (-ETAS(i + 1, j) / ystpc[i] / xstp[j - 1] - dx / 4.0);
+      Ry = Ry - BY1(bleftx, i + 2, 1) * (-ETAS(i + 1, j) / ystpc[i] / xstp[j - 1] - dx / 4.0);
+    }
+    // UpperRightVelocityXNode.jl:8-80
+    if (!right) {
+      if (!left) y[Y_XUR] = -ETAS(i + 1, j + 1) / ystpc[i] / xstp[j - 1] - dx / 4.0;
+      else y[Y_XUR] = y[Y_XUR] - ETAS(i + 1, j + 1) / ystpc[i] / xstp[j - 1] - dx / 4.0;
+    } else {
+      y[Y_XUL] = y[Y_XUL] + BY1(brightx, i + 1, 2) * (-ETAS(i + 1, j + 1) / ystpc[i] / xstp[j - 1] - dx / 4.0);
+      Ry = Ry - BY1(brightx, i + 1, 1) * (-ETAS(i + 1, j + 1) / ystpc[i] / xstp[j - 1] - dx / 4.0);
+    }
+    // BottomRightVelocityXNode.jl:8-80
+    if (!right) {
+      if (!left) y[Y_XLR] = ETAS(i + 1, j + 1) / ystpc[i] / xstp[j - 1] - dx / 4.0;
+      else y[Y_XLR] = y[Y_XLR] + ETAS(i + 1, j + 1) / ystpc[i] / xstp[j - 1] - dx / 4.0;
+    } else {
+      y[Y_XLL] = y[Y_XLL] + BY1(brightx, i + 2, 2) * (ETAS(i + 1, j + 1) / ystpc[i] / xstp[j - 1] - dx / 4.0);
+      Ry = Ry - BY1(brightx, i + 2, 1) * (ETAS(i + 1, j + 1) / ystpc[i] / xstp[j - 1] - dx / 4.0);
+    }
+    // UpperAndLowerPressureNodes.jl:6-43
+    y[Y_PU] = b.pscale / ystpc[i];
+    y[Y_PD] = -b.pscale / ystpc[i];
+  }
+  // ---- continuity (StencilForPContinuityUnknown.jl:31-52) ----
+  bool internal;
+  switch (b.pressure_bc_mode) {  // Domain.found_internal_cell_continuity
+    case 0: internal = (j > 1 || i > 1); break;
+    case 1: internal = (1 < i && i < b.ynum - 1); break;
+    case 2: internal = (1 < j && j < b.xnum - 1); break;
+    default: internal = false;
+  }
+  if (!internal) {  // boundary/BoundaryCells.jl:36-203
+    const double rbc = 2.0 * b.pressure_bc / (b.xstpavg + b.ystpavg);
+    Rc = 0.0;
+    if (b.pressure_bc_mode >= 0 && b.pressure_bc_mode <= 2) {
+      p[C_C] = kbond;
+      Rc = (b.pressure_bc_mode == 0) ? rbc : (b.pressure_bc_mode == 1 ? (top ? rbc : 0.0) : (left ? rbc : 0.0));
+    }
+  } else {
+    const double ps = b.pscale;
+    const bool lower = i >= b.ynum - 1, rightb = j >= b.xnum - 1;
+    Rc = A2(b.RC, b.ynum - 1, i, j) * ps;
+    // internal/stencil_nodes/LeftVelocityXNode.jl:8-46
+    if (!left) {
+      p[C_XL] = -ps / xstp[j - 1];
+      if (rightb) {
+        p[C_XL] = p[C_XL] + BY1(brightx, i + 1, 2) * ps / xstp[j - 1];
+        Rc = Rc - BY1(brightx, i + 1, 1) * ps / xstp[j - 1];
+      }
+    }
+    // RightVelocityXNode.jl:8-45
+    if (!rightb) {
+      p[C_XR] = ps / xstp[j - 1];
+      if (left) {
+        p[C_XR] = p[C_XR] - BY1(bleftx, i + 1, 2) * ps / xstp[j - 1];
+        Rc = Rc + BY1(bleftx, i + 1, 1) * ps / xstp[j - 1];
+      }
+    }
+    // UpperVelocityYNode.jl:8-50
+    if (!top) {
+      p[C_YU] = -ps / ystp[i - 1];
+      if (lower) {
+        p[C_YU] = p[C_YU] + BX1(bbottomy, j + 1, 2) * ps / ystp[i - 1];
+        Rc = Rc - BX1(bbottomy, j + 1, 1) * ps / ystp[i - 1];
+      }
+    }
+    // BottomVelocityYNode.jl:8-44
+    if (!lower) {
+      p[C_YD] = ps / ystp[i - 1];
+      if (top) {
+        p[C_YD] = p[C_YD] - BX1(btopy, j + 1, 2) * ps / ystp[i - 1];
+        Rc = Rc + BX1(btopy, j + 1, 1) * ps / ystp[i - 1];
+      }
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < 11; ++k) coef[(int64_t)k * nc + c] = x[k];
+#pragma unroll
+  for (int k = 0; k < 11; ++k) coef[(int64_t)(11 + k) * nc + c] = y[k];
+#pragma unroll
+  for (int k = 0; k < 5; ++k) coef[(int64_t)(22 + k) * nc + c] = p[k];
+  rhs[c] = Rx;
+  rhs[nc + c] = Ry;
+  rhs[2 * nc + c] = Rc;
+#undef ETAN
+#undef ETAS
+#undef RHOVY
+#undef BX
+#undef BX1
+#undef BY1
+#undef BY
+}
+
+// ---- SystemSolver.reload_solu_vel! (:188-235) -------------------------------
+__global__ void k_reload_solution(const double* __restrict__ S, int32_t xnum, int32_t ynum, double pscale,
+                                  double* __restrict__ vx1, double* __restrict__ vy1, double* __restrict__ pr1) {
+  const int64_t nc = (int64_t)(xnum - 1) * (ynum - 1);
+  const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= nc) return;
+  const int32_t i = (int32_t)(c % (ynum - 1)) + 1, j = (int32_t)(c / (ynum - 1)) + 1;
+  if (j < xnum - 1) A2(vx1, ynum + 1, i + 1, j + 1) = S[c];
+  if (i < ynum - 1) A2(vy1, ynum, i + 1, j + 1) = S[nc + c];
+  A2(pr1, ynum - 1, i, j) = S[2 * nc + c] * pscale;
+}
+
+// ---- SystemSolver.apply_vel_bc! (:237-271), its four loops in order ---------
+__global__ void k_bc_top_bottom_vx(double* vx1, const double* btopx, const double* bbottomx, int32_t xnum, int32_t ynum) {
+  const int32_t j = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  if (j > xnum) return;
+  A2(vx1, ynum + 1, 1, j) = A2(btopx, xnum, j, 1) + A2(btopx, xnum, j, 2) * A2(vx1, ynum + 1, 2, j);
+  A2(vx1, ynum + 1, ynum + 1, j) = A2(bbottomx, xnum, j, 1) + A2(bbottomx, xnum, j, 2) * A2(vx1, ynum + 1, ynum, j);
+}
+__global__ void k_bc_top_bottom_vy(double* vy1, const double* btopy, const double* bbottomy, int32_t xnum, int32_t ynum) {
+  const int32_t j = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  if (j > xnum + 1) return;
+  A2(vy1, ynum, 1, j) = A2(btopy, xnum + 1, j, 1) + A2(btopy, xnum + 1, j, 2) * A2(vy1, ynum, 2, j);
+  A2(vy1, ynum, ynum, j) = A2(bbottomy, xnum + 1, j, 1) + A2(bbottomy, xnum + 1, j, 2) * A2(vy1, ynum, ynum - 1, j);
+}
+__global__ void k_bc_left_right_vx(double* vx1, const double* bleftx, const double* brightx, int32_t xnum, int32_t ynum) {
+  const int32_t i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  if (i > ynum + 1) return;
+  A2(vx1, ynum + 1, i, 1) = A2(bleftx, ynum + 1, i, 1) + A2(bleftx, ynum + 1, i, 2) * A2(vx1, ynum + 1, i, 2);
+  A2(vx1, ynum + 1, i, xnum) = A2(brightx, ynum + 1, i, 1) + A2(brightx, ynum + 1, i, 2) * A2(vx1, ynum + 1, i, xnum - 1);
+}
+__global__ void k_bc_left_right_vy(double* vy1, const double* blefty, const double* brighty, int32_t xnum, int32_t ynum) {
+  const int32_t i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  if (i > ynum) return;
+  A2(vy1, ynum, i, 1) = A2(blefty, ynum, i, 1) + A2(blefty, ynum, i, 2) * A2(vy1, ynum, i, 2);
+  A2(vy1, ynum, i, xnum + 1) = A2(brighty, ynum, i, 1) + A2(brighty, ynum, i, 2) * A2(vy1, ynum, i, xnum);
+}
+
+unsigned nblk(int64_t n) { return (unsigned)((n + kB - 1) / kB); }
+
+}  // namespace
+
+int launch_viscoelastic_terms(eb_ctx* c) {
+  double** g = c->gf;
+  const int64_t nb = (int64_t)c->xnum * c->ynum, np = (int64_t)(c->xnum - 1) * (c->ynum - 1);
+  EB_PROF(c, "k_ve_terms");
+  k_ve_terms<<<nblk(nb), kB, 0, c->stream>>>(g[EB_G_ETAS1], g[EB_G_MUS1], g[EB_G_SXY1], g[EB_G_ETAS0], g[EB_G_SXY0],
+                                             nb, c->P.timestep);
+  EB_LAUNCHED(c);
+  EB_PROF(c, "k_ve_terms");
+  k_ve_terms<<<nblk(np), kB, 0, c->stream>>>(g[EB_G_ETAN1], g[EB_G_MUN1], g[EB_G_SXX1], g[EB_G_ETAN0], g[EB_G_SXX0],
+                                             np, c->P.timestep);
+  EB_LAUNCHED(c);
+  return EB_OK;
+}
+
+int launch_viscoelastic_rhs(eb_ctx* c) {
+  double** g = c->gf;
+  const int32_t X = c->xnum, Y = c->ynum;
+  EB_CK(c, cudaMemsetAsync(g[EB_G_RX1], 0, sizeof(double) * (size_t)(Y + 1) * X, c->stream));
+  EB_CK(c, cudaMemsetAsync(g[EB_G_RY1], 0, sizeof(double) * (size_t)Y * (X + 1), c->stream));
+  const DevGrid& G = c->g;
+  EB_PROF(c, "k_rhs_xy");
+  k_rhs_xy<<<nblk((int64_t)(X - 1) * (Y - 1)), kB, 0, c->stream>>>(
+      X, Y, c->SP.gravity_x, c->SP.gravity_y, (int32_t)c->SP.iuse_interface_stabilization, G.sx, G.sy,
+      c->g_xstp_vy, c->g_ystp_vx, g[EB_G_RHO1], g[EB_G_RHO1_VY], g[EB_G_SXX0], g[EB_G_SXY0], g[EB_G_RX1], g[EB_G_RY1]);
+  EB_LAUNCHED(c);
+  const int64_t np = (int64_t)(X - 1) * (Y - 1);
+  EB_PROF(c, "k_rhs_c");
+  k_rhs_c<<<nblk(np), kB, 0, c->stream>>>(g[EB_G_DILAT], g[EB_G_EII_PLASTIC_PRESSURE], g[EB_G_RC1], np);
+  EB_LAUNCHED(c);
+  return EB_OK;
+}
+
+int launch_build_stokes_system(eb_ctx* c, StokesSystem* s) {
+  double** g = c->gf;
+  BuildIn b{};
+  b.xnum = c->xnum; b.ynum = c->ynum;
+  b.xstpavg = c->g.xstpavg; b.ystpavg = c->g.ystpavg;
+  b.pscale = s->pscale; b.timestep = c->P.timestep; b.gravity_y = c->SP.gravity_y; b.pressure_bc = c->SP.pressure_bc;
+  b.stab = (int32_t)c->SP.iuse_interface_stabilization; b.pressure_bc_mode = (int32_t)c->SP.pressure_bc_mode;
+  for (int k = 0; k < 8; ++k) { b.zone[k] = c->SP.bintern_zone[k]; b.zvel[k] = c->SP.bintern_velocity[k]; }
+  b.xstp = c->g.sx; b.ystp = c->g.sy; b.xstpc = c->g_xstp_vy; b.ystpc = c->g_ystp_vx;
+  b.btopx = g[EB_G_BTOPX]; b.bbottomx = g[EB_G_BBOTTOMX]; b.btopy = g[EB_G_BTOPY]; b.bbottomy = g[EB_G_BBOTTOMY];
+  b.bleftx = g[EB_G_BLEFTX]; b.brightx = g[EB_G_BRIGHTX]; b.blefty = g[EB_G_BLEFTY]; b.brighty = g[EB_G_BRIGHTY];
+  b.etan = g[EB_G_ETAN0]; b.etas = g[EB_G_ETAS0]; b.rho_vy = g[EB_G_RHO1_VY];
+  b.RX = g[EB_G_RX1]; b.RY = g[EB_G_RY1]; b.RC = g[EB_G_RC1];
+  EB_PROF(c, "k_build_system");
+  k_build_system<<<nblk(s->nc), kB, 0, c->stream>>>(b, s->coef, s->rhs, s->nc);
+  EB_LAUNCHED(c);
+  return EB_OK;
+}
+
+int launch_process_stokes_solution(eb_ctx* c, const StokesSystem* s) {
+  double** g = c->gf;
+  const int32_t X = c->xnum, Y = c->ynum;
+  EB_CK(c, cudaMemsetAsync(g[EB_G_VX1], 0, sizeof(double) * (size_t)(Y + 1) * X, c->stream));
+  EB_CK(c, cudaMemsetAsync(g[EB_G_VY1], 0, sizeof(double) * (size_t)Y * (X + 1), c->stream));
+  EB_PROF(c, "k_reload_solution");
+  k_reload_solution<<<nblk(s->nc), kB, 0, c->stream>>>(s->S, X, Y, s->pscale, g[EB_G_VX1], g[EB_G_VY1], g[EB_G_PR1]);
+  EB_LAUNCHED(c);
+  EB_PROF(c, "k_apply_vel_bc");
+  k_bc_top_bottom_vx<<<nblk(X), kB, 0, c->stream>>>(g[EB_G_VX1], g[EB_G_BTOPX], g[EB_G_BBOTTOMX], X, Y);
+  EB_LAUNCHED(c);
+  EB_PROF(c, "k_apply_vel_bc");
+  k_bc_top_bottom_vy<<<nblk(X + 1), kB, 0, c->stream>>>(g[EB_G_VY1], g[EB_G_BTOPY], g[EB_G_BBOTTOMY], X, Y);
+  EB_LAUNCHED(c);
+  EB_PROF(c, "k_apply_vel_bc");
+  k_bc_left_right_vx<<<nblk(Y + 1), kB, 0, c->stream>>>(g[EB_G_VX1], g[EB_G_BLEFTX], g[EB_G_BRIGHTX], X, Y);
+  EB_LAUNCHED(c);
+  EB_PROF(c, "k_apply_vel_bc");
+  k_bc_left_right_vy<<<nblk(Y), kB, 0, c->stream>>>(g[EB_G_VY1], g[EB_G_BLEFTY], g[EB_G_BRIGHTY], X, Y);
+  EB_LAUNCHED(c);
+  return EB_OK;
+}

@@ -1,0 +1,1285 @@
+// eb_stokes_solve.cu -- iterative solve of the Stokes-continuity system on the GPU.
+//
+// Replaces the reference's direct sparse solve (SystemSolver.solve_system_optimized,
+// src/stokes_continuity_solver/solver/system_solver/SystemSolver.jl:67-91, which
+// calls MUMPS through ParallelSolver.jl:52-126 or UMFPACK through `sparse(...) \ R`).
+//
+// Method.  FGMRES in FP64 on the symmetrically scaled system (W L W) y = W R,
+// S = W y, with W = 1/sqrt(|diag L|) on the momentum rows and sqrt(2 eta_n)/pscale
+// on the continuity rows (the inverse square root of the Schur-complement
+// diagonal), so that the residual FGMRES minimises weighs weak (sticky-air) and
+// stiff regions alike.  Right preconditioner: block upper-triangular,
+//   z_p = (2 eta_n / pscale^2) r_p   (1/L_pp on pressure-condition rows),
+//   z_u = MG(r_u - L_up z_p),
+// where MG is one V-cycle of FP32 geometric multigrid on the coupled velocity
+// block: red-black Gauss-Seidel on vx then vy, coarse levels rediscretised from
+// arithmetic averages of the viscosity on grids with every other node (the last
+// coarse cell takes three fine cells when the count is odd), linear transfer
+// operators in physical coordinates with the boundary-condition coefficients
+// folded in, and an exact dense solve on the coarsest level.  The V-cycle is
+// captured once per solve into a CUDA graph and replayed every iteration.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <vector>
+#include "eb_internal.h"
+
+namespace {
+
+constexpr int kB = 256;
+constexpr int kRmax = 8;  // restriction entries per coarse index and axis
+
+unsigned nblk(int64_t n) { return (unsigned)((n + kB - 1) / kB); }
+
+// ------------------------------------------------------- FP64 operator ---
+// y = L x on SoA vectors; optional scaling: y = w .* L (w .* x).
+__global__ void k_apply64(const double* __restrict__ coef, const double* __restrict__ x, double* __restrict__ y,
+                          const double* __restrict__ w, int32_t nx, int32_t ny, int64_t nc) {
+  const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= nc) return;
+  const int32_t i = (int32_t)(c % ny), j = (int32_t)(c / ny);
+  const double *vx = x, *vy = x + nc, *p = x + 2 * nc;
+  const double *wx = w, *wy = w ? w + nc : nullptr, *wp = w ? w + 2 * nc : nullptr;
+  auto X = [&](int64_t k) { return w ? vx[k] * wx[k] : vx[k]; };
+  auto Y = [&](int64_t k) { return w ? vy[k] * wy[k] : vy[k]; };
+  auto Pp = [&](int64_t k) { return w ? p[k] * wp[k] : p[k]; };
+  const bool hu = i > 0, hd = i < ny - 1, hl = j > 0, hr = j < nx - 1;
+  auto cf = [&](int s) { return __ldg(&coef[(int64_t)s * nc + c]); };
+  double ax = cf(0) * X(c);
+  if (hl) ax += cf(1) * X(c - ny);
+  if (hr) ax += cf(2) * X(c + ny);
+  if (hu) ax += cf(3) * X(c - 1);
+  if (hd) ax += cf(4) * X(c + 1);
+  if (hu) ax += cf(5) * Y(c - 1);
+  if (hu && hr) ax += cf(6) * Y(c + ny - 1);
+  ax += cf(7) * Y(c);
+  if (hr) ax += cf(8) * Y(c + ny);
+  ax += cf(9) * Pp(c);
+  if (hr) ax += cf(10) * Pp(c + ny);
+  double ay = cf(11) * Y(c);
+  if (hu) ay += cf(12) * Y(c - 1);
+  if (hd) ay += cf(13) * Y(c + 1);
+  if (hl) ay += cf(14) * Y(c - ny);
+  if (hr) ay += cf(15) * Y(c + ny);
+  if (hl) ay += cf(16) * X(c - ny);
+  ay += cf(17) * X(c);
+  if (hl && hd) ay += cf(18) * X(c + 1 - ny);
+  if (hd) ay += cf(19) * X(c + 1);
+  ay += cf(20) * Pp(c);
+  if (hd) ay += cf(21) * Pp(c + 1);
+  double ap = cf(22) * Pp(c);
+  if (hl) ap += cf(23) * X(c - ny);
+  ap += cf(24) * X(c);
+  if (hu) ap += cf(25) * Y(c - 1);
+  ap += cf(26) * Y(c);
+  if (w) { ax *= wx[c]; ay *= wy[c]; ap *= wp[c]; }
+  y[c] = ax;
+  y[nc + c] = ay;
+  y[2 * nc + c] = ap;
+}
+
+// W and the pressure preconditioner factor.
+__global__ void k_scaling(const double* __restrict__ coef, const double* __restrict__ etan0, double pscale,
+                          double* __restrict__ w, double* __restrict__ prep, int64_t nc) {
+  const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= nc) return;
+  w[c] = 1.0 / sqrt(fabs(coef[c]));
+  w[nc + c] = 1.0 / sqrt(fabs(coef[11 * nc + c]));
+  const double pc = coef[22 * nc + c];
+  if (pc != 0.0) {  // pressure-condition row
+    w[2 * nc + c] = 1.0 / sqrt(fabs(pc));
+    prep[c] = 1.0 / pc;
+  } else {
+    const double s = 2.0 * etan0[c] / (pscale * pscale);  // etan0 is (ynum-1, xnum-1): same cell order
+    w[2 * nc + c] = sqrt(s);
+    prep[c] = s;
+  }
+}
+
+// ------------------------------------------------------ FGMRES helpers ---
+// partial[v * nb + b] = sum over block b's chunk of V_v . u
+__global__ void k_mdot(const double* __restrict__ V, int64_t stride, const double* __restrict__ u, int64_t n,
+                       double* __restrict__ partial) {
+  const int v = blockIdx.y;
+  const double* a = V + (int64_t)v * stride;
+  double s = 0.0;
+  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x)
+    s += a[k] * u[k];
+  __shared__ double sh[kB];
+  sh[threadIdx.x] = s;
+  __syncthreads();
+  for (int o = kB / 2; o > 0; o >>= 1) {
+    if ((int)threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) partial[(int64_t)v * gridDim.x + blockIdx.x] = sh[0];
+}
+__global__ void k_mdot_final(const double* __restrict__ partial, int nb, double* __restrict__ out) {
+  const int v = blockIdx.x;
+  double s = 0.0;
+  for (int b = threadIdx.x; b < nb; b += blockDim.x) s += partial[(int64_t)v * nb + b];
+  __shared__ double sh[kB];
+  sh[threadIdx.x] = s;
+  __syncthreads();
+  for (int o = kB / 2; o > 0; o >>= 1) {
+    if ((int)threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) out[v] = sh[0];
+}
+// u -= sum_v h[v] V_v
+__global__ void k_maxpy(double* __restrict__ u, const double* __restrict__ V, int64_t stride, const double* __restrict__ h,
+                        int nv, int64_t n) {
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  double s = u[k];
+  for (int v = 0; v < nv; ++v) s -= h[v] * V[(int64_t)v * stride + k];
+  u[k] = s;
+}
+// dst may alias src (in-place scaling)
+__global__ void k_scale_copy(double* dst, const double* src, double a, int64_t n) {
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < n) dst[k] = a * src[k];
+}
+// dst = a - b (elementwise)
+__global__ void k_sub(double* __restrict__ dst, const double* __restrict__ a, const double* __restrict__ b, int64_t n) {
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < n) dst[k] = a[k] - b[k];
+}
+// dst = a .* b or a ./ b (dst may alias a)
+__global__ void k_mul(double* dst, const double* a, const double* __restrict__ b, int64_t n, int div) {
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < n) dst[k] = div ? a[k] / b[k] : a[k] * b[k];
+}
+__global__ void k_abs_sub(double* __restrict__ dst, const double* __restrict__ a, const double* __restrict__ b, int64_t n) {
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < n) dst[k] = fabs(a[k] - b[k]);
+}
+
+// interleaved host layout <-> SoA device layout
+__global__ void k_interleave(const double* __restrict__ soa, double* __restrict__ il, int64_t nc) {
+  const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= nc) return;
+  il[3 * c] = soa[c];
+  il[3 * c + 1] = soa[nc + c];
+  il[3 * c + 2] = soa[2 * nc + c];
+}
+__global__ void k_deinterleave(const double* __restrict__ il, double* __restrict__ soa, int64_t nc) {
+  const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= nc) return;
+  soa[c] = il[3 * c];
+  soa[nc + c] = il[3 * c + 1];
+  soa[2 * nc + c] = il[3 * c + 2];
+}
+
+// ----------------------------------------------------------- multigrid ---
+struct Axis2 { int32_t* idx; float* w; };   // prolongation: 2 (coarse index, weight) per fine index
+struct AxisR { int32_t* idx; float* w; };   // restriction: kRmax (fine index, weight) per coarse index
+
+struct Level {
+  int32_t nx = 0, ny = 0;
+  int64_t nc = 0;
+  float *X = nullptr, *Y = nullptr;                       // [9][nc]
+  float *ux = nullptr, *uy = nullptr, *fx = nullptr, *fy = nullptr, *rx = nullptr, *ry = nullptr;
+  float *etas = nullptr, *etan = nullptr;                 // [(ny+1)(nx+1)], [ny nx]
+  float *xstp = nullptr, *ystp = nullptr, *xstpc = nullptr, *ystpc = nullptr;
+  int32_t *kx = nullptr, *ky = nullptr;                   // nodes of this level in the finer level
+  // transfers to the next coarser level
+  Axis2 pvx_x{}, pvx_y{}, pvy_x{}, pvy_y{};
+  AxisR rvx_x{}, rvx_y{}, rvy_x{}, rvy_y{};
+  // host geometry
+  std::vector<double> x, y;                               // basic node coordinates
+};
+
+struct B2 { float topx, botx, topy, boty, leftx, rightx, lefty, righty; };
+
+// Coarse-level velocity stencil from averaged viscosity (same formulas as the
+// fine assembly, uniform boundary-condition coefficients, no stabilisation).
+__global__ void k_redisc(int32_t nx, int32_t ny, const float* __restrict__ etas, const float* __restrict__ etan,
+                         const float* __restrict__ xstp, const float* __restrict__ ystp,
+                         const float* __restrict__ xstpc, const float* __restrict__ ystpc, B2 b,
+                         float* __restrict__ X, float* __restrict__ Y) {
+  const int64_t nc = (int64_t)nx * ny;
+  const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= nc) return;
+  const int32_t i = (int32_t)(c % ny) + 1, j = (int32_t)(c / ny) + 1;  // 1-based cell
+  const int32_t xnum = nx + 1, ynum = ny + 1;
+  auto eS = [&](int ii, int jj) { return etas[(int64_t)(jj - 1) * ynum + (ii - 1)]; };
+  auto eN = [&](int ii, int jj) { return etan[(int64_t)(jj - 1) * ny + (ii - 1)]; };
+  float x[9] = {0}, y[9] = {0};
+  if (j < xnum - 1) {
+    const bool left = j == 1, right2 = j >= xnum - 2, top = i == 1, bot = i >= ynum - 1;
+    const float cL = 2.f * eN(i, j) / xstp[j - 1] / xstpc[j];
+    const float cR = 2.f * eN(i, j + 1) / xstp[j] / xstpc[j];
+    const float cU = eS(i, j + 1) / ystpc[i - 1] / ystp[i - 1];
+    const float cD = eS(i + 1, j + 1) / ystpc[i] / ystp[i - 1];
+    float C = -(cL + cR) - (cU + cD);
+    const float gUL = eS(i, j + 1) / xstpc[j] / ystp[i - 1], gUR = -gUL;
+    const float gLL = -eS(i + 1, j + 1) / xstpc[j] / ystp[i - 1], gLR = -gLL;
+    if (left) C += b.leftx * cL; else x[1] = cL;
+    if (right2) C += b.rightx * cR; else x[2] = cR;
+    if (top) C += b.topx * cU; else x[3] = cU;
+    if (bot) C += b.botx * cD; else x[4] = cD;
+    x[0] = C;
+    float vUL = 0, vUR = 0, vLL = 0, vLR = 0;
+    if (!top) { vUL = gUL; vUR = gUR; } else { vLL = b.topy * gUL; vLR = b.topy * gUR; }
+    if (!bot) { vLL += gLL; vLR += gLR; } else { vUL += b.boty * gLL; vUR += b.boty * gLR; }
+    x[5] = vUL; x[6] = vUR; x[7] = vLL; x[8] = vLR;
+  } else {
+    x[0] = 1.f;
+  }
+  if (i < ynum - 1) {
+    const bool top = i == 1, bot2 = i >= ynum - 2, left = j == 1, right = j >= xnum - 1;
+    const float cU = 2.f * eN(i, j) / ystp[i - 1] / ystpc[i];
+    const float cD = 2.f * eN(i + 1, j) / ystp[i] / ystpc[i];
+    const float cL = eS(i + 1, j) / xstpc[j - 1] / xstp[j - 1];
+    const float cR = eS(i + 1, j + 1) / xstpc[j] / xstp[j - 1];
+    float C = -(cU + cD) - (cL + cR);
+    const float hUL = eS(i + 1, j) / ystpc[i] / xstp[j - 1], hLL = -hUL;
+    const float hUR = -eS(i + 1, j + 1) / ystpc[i] / xstp[j - 1], hLR = -hUR;
+    if (top) C += b.topy * cU; else y[1] = cU;
+    if (bot2) C += b.boty * cD; else y[2] = cD;
+    if (left) C += b.lefty * cL; else y[3] = cL;
+    if (right) C += b.righty * cR; else y[4] = cR;
+    y[0] = C;
+    float xUL = 0, xUR = 0, xLL = 0, xLR = 0;
+    if (!left) { xUL = hUL; xLL = hLL; } else { xUR = b.leftx * hUL; xLR = b.leftx * hLL; }
+    if (!right) { xUR += hUR; xLR += hLR; } else { xUL += b.rightx * hUR; xLL += b.rightx * hLR; }
+    y[5] = xUL; y[6] = xUR; y[7] = xLL; y[8] = xLR;
+  } else {
+    y[0] = 1.f;
+  }
+  for (int k = 0; k < 9; ++k) { X[(int64_t)k * nc + c] = x[k]; Y[(int64_t)k * nc + c] = y[k]; }
+}
+
+// Level 0 takes the assembled FP64 velocity block.
+__global__ void k_level0(const double* __restrict__ coef, float* __restrict__ X, float* __restrict__ Y, int64_t nc) {
+  const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= nc) return;
+  for (int k = 0; k < 9; ++k) {
+    X[(int64_t)k * nc + c] = (float)coef[(int64_t)k * nc + c];
+    Y[(int64_t)k * nc + c] = (float)coef[(int64_t)(11 + k) * nc + c];
+  }
+}
+__global__ void k_to_f32(const double* __restrict__ a, float* __restrict__ b, int64_t n) {
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < n) b[k] = (float)a[k];
+}
+// Arithmetic averages of the finer level's viscosity onto this level.
+__global__ void k_coarsen_eta(const float* __restrict__ es_f, const float* __restrict__ en_f, int32_t nxf, int32_t nyf,
+                              float* __restrict__ es_c, float* __restrict__ en_c, int32_t nxc, int32_t nyc,
+                              const int32_t* __restrict__ kx, const int32_t* __restrict__ ky) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t nnode = (int64_t)(nxc + 1) * (nyc + 1);
+  if (t < nnode) {
+    const int32_t I = (int32_t)(t % (nyc + 1)), J = (int32_t)(t / (nyc + 1));
+    const int32_t fi = ky[I], fj = kx[J];
+    float s = 0.f; int n = 0;
+    for (int32_t jj = max(fj - 1, 0); jj <= min(fj + 1, nxf); ++jj)
+      for (int32_t ii = max(fi - 1, 0); ii <= min(fi + 1, nyf); ++ii) { s += es_f[(int64_t)jj * (nyf + 1) + ii]; ++n; }
+    es_c[t] = s / (float)n;
+  }
+  if (t < (int64_t)nxc * nyc) {
+    const int32_t I = (int32_t)(t % nyc), J = (int32_t)(t / nyc);
+    float s = 0.f; int n = 0;
+    for (int32_t jj = kx[J]; jj < kx[J + 1]; ++jj)
+      for (int32_t ii = ky[I]; ii < ky[I + 1]; ++ii) { s += en_f[(int64_t)jj * nyf + ii]; ++n; }
+    en_c[t] = s / (float)n;
+  }
+}
+
+// Velocity-block product of one row kind at cell c.
+__device__ __forceinline__ float rowx(const float* __restrict__ X, const float* ux, const float* uy, int64_t c, int32_t i,
+                                      int32_t j, int32_t nx, int32_t ny, int64_t nc, bool skip_center) {
+  const bool hu = i > 0, hd = i < ny - 1, hl = j > 0, hr = j < nx - 1;
+  float a = skip_center ? 0.f : X[c] * ux[c];
+  if (hl) a += X[nc + c] * ux[c - ny];
+  if (hr) a += X[2 * nc + c] * ux[c + ny];
+  if (hu) a += X[3 * nc + c] * ux[c - 1];
+  if (hd) a += X[4 * nc + c] * ux[c + 1];
+  if (hu) a += X[5 * nc + c] * uy[c - 1];
+  if (hu && hr) a += X[6 * nc + c] * uy[c + ny - 1];
+  a += X[7 * nc + c] * uy[c];
+  if (hr) a += X[8 * nc + c] * uy[c + ny];
+  return a;
+}
+__device__ __forceinline__ float rowy(const float* __restrict__ Y, const float* ux, const float* uy, int64_t c, int32_t i,
+                                      int32_t j, int32_t nx, int32_t ny, int64_t nc, bool skip_center) {
+  const bool hu = i > 0, hd = i < ny - 1, hl = j > 0, hr = j < nx - 1;
+  float a = skip_center ? 0.f : Y[c] * uy[c];
+  if (hu) a += Y[nc + c] * uy[c - 1];
+  if (hd) a += Y[2 * nc + c] * uy[c + 1];
+  if (hl) a += Y[3 * nc + c] * uy[c - ny];
+  if (hr) a += Y[4 * nc + c] * uy[c + ny];
+  if (hl) a += Y[5 * nc + c] * ux[c - ny];
+  a += Y[6 * nc + c] * ux[c];
+  if (hl && hd) a += Y[7 * nc + c] * ux[c + 1 - ny];
+  if (hd) a += Y[8 * nc + c] * ux[c + 1];
+  return a;
+}
+
+// Red-black Gauss-Seidel half sweep: comp 0 updates vx, 1 updates vy, on cells with (i + j) % 2 == color.
+__global__ void k_rbgs(const float* __restrict__ X, const float* __restrict__ Y, float* ux, float* uy,
+                       const float* __restrict__ fx, const float* __restrict__ fy, int32_t nx, int32_t ny, int comp,
+                       int color) {
+  const int64_t nc = (int64_t)nx * ny;
+  // column j holds the rows i = 2q + ((j + color) & 1) of this color, q < ceil(ny / 2)
+  const int32_t half = (ny + 1) / 2;
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int32_t j = (int32_t)(t / half);
+  if (j >= nx) return;
+  const int32_t i = 2 * (int32_t)(t - (int64_t)j * half) + ((j + color) & 1);
+  if (i >= ny) return;
+  const int64_t c = (int64_t)j * ny + i;
+  if (comp == 0) {
+    const float s = rowx(X, ux, uy, c, i, j, nx, ny, nc, true);
+    ux[c] = (fx[c] - s) / X[c];
+  } else {
+    const float s = rowy(Y, ux, uy, c, i, j, nx, ny, nc, true);
+    uy[c] = (fy[c] - s) / Y[c];
+  }
+}
+__global__ void k_resid(const float* __restrict__ X, const float* __restrict__ Y, const float* __restrict__ ux,
+                        const float* __restrict__ uy, const float* __restrict__ fx, const float* __restrict__ fy,
+                        float* __restrict__ rx, float* __restrict__ ry, int32_t nx, int32_t ny) {
+  const int64_t nc = (int64_t)nx * ny;
+  const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= nc) return;
+  const int32_t i = (int32_t)(c % ny), j = (int32_t)(c / ny);
+  rx[c] = fx[c] - rowx(X, ux, uy, c, i, j, nx, ny, nc, false);
+  ry[c] = fy[c] - rowy(Y, ux, uy, c, i, j, nx, ny, nc, false);
+}
+// coarse f = R r (per component, tensor product of the axis tables)
+__global__ void k_restrict(const float* __restrict__ rx, const float* __restrict__ ry, int32_t nyf,
+                           float* __restrict__ fxc, float* __restrict__ fyc, int32_t nxc, int32_t nyc, AxisR vxx, AxisR vxy,
+                           AxisR vyx, AxisR vyy) {
+  const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= (int64_t)nxc * nyc) return;
+  const int32_t I = (int32_t)(c % nyc), J = (int32_t)(c / nyc);
+  float sx = 0.f, sy = 0.f;
+  for (int a = 0; a < kRmax; ++a) {
+    const float wa = vxx.w[J * kRmax + a];
+    if (wa != 0.f) {
+      const int64_t col = (int64_t)vxx.idx[J * kRmax + a] * nyf;
+      for (int b = 0; b < kRmax; ++b) {
+        const float wb = vxy.w[I * kRmax + b];
+        if (wb != 0.f) sx += wa * wb * rx[col + vxy.idx[I * kRmax + b]];
+      }
+    }
+    const float va = vyx.w[J * kRmax + a];
+    if (va != 0.f) {
+      const int64_t col = (int64_t)vyx.idx[J * kRmax + a] * nyf;
+      for (int b = 0; b < kRmax; ++b) {
+        const float vb = vyy.w[I * kRmax + b];
+        if (vb != 0.f) sy += va * vb * ry[col + vyy.idx[I * kRmax + b]];
+      }
+    }
+  }
+  fxc[c] = sx;
+  fyc[c] = sy;
+}
+// fine u += P e
+__global__ void k_prolong(float* __restrict__ ux, float* __restrict__ uy, int32_t nxf, int32_t nyf,
+                          const float* __restrict__ ex, const float* __restrict__ ey, int32_t nyc, Axis2 vxx, Axis2 vxy,
+                          Axis2 vyx, Axis2 vyy) {
+  const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= (int64_t)nxf * nyf) return;
+  const int32_t i = (int32_t)(c % nyf), j = (int32_t)(c / nyf);
+  float sx = 0.f, sy = 0.f;
+  for (int a = 0; a < 2; ++a)
+    for (int b = 0; b < 2; ++b) {
+      const float w1 = vxx.w[2 * j + a] * vxy.w[2 * i + b];
+      if (w1 != 0.f) sx += w1 * ex[(int64_t)vxx.idx[2 * j + a] * nyc + vxy.idx[2 * i + b]];
+      const float w2 = vyx.w[2 * j + a] * vyy.w[2 * i + b];
+      if (w2 != 0.f) sy += w2 * ey[(int64_t)vyx.idx[2 * j + a] * nyc + vyy.idx[2 * i + b]];
+    }
+  ux[c] += sx;
+  uy[c] += sy;
+}
+// coarsest level: u = Ainv f with the dense inverse of the velocity block (n = 2 nc unknowns)
+__global__ void k_dense_solve(const float* __restrict__ Ainv, int n, const float* __restrict__ fx,
+                              const float* __restrict__ fy, float* __restrict__ ux, float* __restrict__ uy) {
+  const int half = n / 2;
+  for (int r = threadIdx.x; r < n; r += blockDim.x) {
+    float s = 0.f;
+    for (int k = 0; k < half; ++k) s += Ainv[(int64_t)r * n + k] * fx[k];
+    for (int k = 0; k < half; ++k) s += Ainv[(int64_t)r * n + half + k] * fy[k];
+    if (r < half) ux[r] = s; else uy[r - half] = s;
+  }
+}
+
+// preconditioner input: z_p = prep r_p; f = r_u - L_up z_p (FP32, level 0).  r, z are unscaled here.
+__global__ void k_prec_in(const double* __restrict__ coef, const double* __restrict__ r, const double* __restrict__ prep,
+                          double* __restrict__ zp, float* __restrict__ fx, float* __restrict__ fy, int32_t nx, int32_t ny) {
+  const int64_t nc = (int64_t)nx * ny;
+  const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= nc) return;
+  const int32_t i = (int32_t)(c % ny), j = (int32_t)(c / ny);
+  auto z = [&](int64_t k) { return prep[k] * r[2 * nc + k]; };
+  const double zc = z(c);
+  zp[c] = zc;
+  double gx = coef[9 * nc + c] * zc;
+  if (j < nx - 1) gx += coef[10 * nc + c] * z(c + ny);
+  double gy = coef[20 * nc + c] * zc;
+  if (i < ny - 1) gy += coef[21 * nc + c] * z(c + 1);
+  fx[c] = (float)(r[c] - gx);
+  fy[c] = (float)(r[nc + c] - gy);
+}
+__global__ void k_prec_out(const float* __restrict__ ux, const float* __restrict__ uy, double* __restrict__ z, int64_t nc) {
+  const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= nc) return;
+  z[c] = (double)ux[c];
+  z[nc + c] = (double)uy[c];
+}
+
+// ------------------------------------------------------ host geometry ---
+std::vector<int32_t> coarse_nodes(int32_t n_cells) {
+  const int32_t M = n_cells / 2;
+  std::vector<int32_t> k(M + 1);
+  for (int32_t m = 0; m < M; ++m) k[m] = 2 * m;
+  k[M] = n_cells;
+  return k;
+}
+void stag(const std::vector<double>& b, std::vector<double>& g, std::vector<double>& s) {
+  const size_t n = b.size();
+  g.assign(n + 1, 0.0);
+  s.assign(n, 0.0);
+  g[0] = b[0] - (b[1] - b[0]) / 2.0;
+  g[n] = b[n - 1] + (b[n - 1] - b[n - 2]) / 2.0;
+  for (size_t k = 1; k < n; ++k) g[k] = (b[k] + b[k - 1]) / 2.0;
+  s[0] = b[1] - b[0];
+  s[n - 1] = b[n - 1] - b[n - 2];
+  for (size_t k = 1; k + 1 < n; ++k) s[k] = (b[k + 1] - b[k - 1]) / 2.0;
+}
+// 1-D linear interpolation fine <- coarse.  cpos[0..m]: coarse positions where 1..m-1 are
+// unknowns (index k-1) and 0, m are boundary/ghost values equal to b2lo/b2hi times the
+// adjacent unknown.  fpos: fine positions; the last one is a dummy (zero row) if last_dummy.
+void interp1d(const std::vector<double>& fpos, bool last_dummy, const std::vector<double>& cpos, double b2lo, double b2hi,
+              std::vector<int32_t>& idx, std::vector<float>& w, std::vector<std::vector<std::pair<int32_t, double>>>* cols) {
+  const int32_t nf = (int32_t)fpos.size(), m = (int32_t)cpos.size() - 1;
+  idx.assign(2 * nf, 0);
+  w.assign(2 * nf, 0.f);
+  for (int32_t n = 0; n < nf; ++n) {
+    if (last_dummy && n == nf - 1) continue;
+    const double xv = fpos[n];
+    int32_t k = (int32_t)(std::upper_bound(cpos.begin(), cpos.end(), xv) - cpos.begin()) - 1;  // cpos[k] <= xv
+    k = std::min(std::max(k, 0), m - 1);
+    const double t = (xv - cpos[k]) / (cpos[k + 1] - cpos[k]);
+    double wt[2] = {1.0 - t, t};
+    int32_t node[2] = {k, k + 1};
+    int32_t out_i[2];
+    double out_w[2];
+    for (int a = 0; a < 2; ++a) {
+      int32_t nd = node[a];
+      double ww = wt[a];
+      if (nd == 0) { nd = 1; ww *= b2lo; }
+      else if (nd == m) { nd = m - 1; ww *= b2hi; }
+      out_i[a] = nd - 1;
+      out_w[a] = ww;
+    }
+    if (out_i[0] == out_i[1]) { out_w[0] += out_w[1]; out_w[1] = 0.0; }
+    for (int a = 0; a < 2; ++a) {
+      idx[2 * n + a] = out_i[a];
+      w[2 * n + a] = (float)out_w[a];
+    }
+  }
+  (void)cols;
+}
+// Restriction from the prolongation: R[K][n] = P[n][K] vol[n] / sum_n P[n][K] vol[n].
+bool restrict1d(const std::vector<int32_t>& pidx, const std::vector<float>& pw, const std::vector<double>& vol,
+                int32_t ncoarse, std::vector<int32_t>& ridx, std::vector<float>& rw) {
+  std::vector<std::vector<std::pair<int32_t, double>>> rows(ncoarse);
+  const int32_t nf = (int32_t)vol.size();
+  for (int32_t n = 0; n < nf; ++n)
+    for (int a = 0; a < 2; ++a) {
+      const double v = (double)pw[2 * n + a] * vol[n];
+      if (v != 0.0) rows[pidx[2 * n + a]].push_back({n, v});
+    }
+  ridx.assign((size_t)ncoarse * kRmax, 0);
+  rw.assign((size_t)ncoarse * kRmax, 0.f);
+  for (int32_t K = 0; K < ncoarse; ++K) {
+    double s = 0.0;
+    for (auto& e : rows[K]) s += e.second;
+    if ((int)rows[K].size() > kRmax) return false;
+    for (size_t a = 0; a < rows[K].size(); ++a) {
+      ridx[(size_t)K * kRmax + a] = rows[K][a].first;
+      rw[(size_t)K * kRmax + a] = (float)(rows[K][a].second / s);
+    }
+  }
+  return true;
+}
+
+// dense inverse (Gauss-Jordan with partial pivoting), row-major n x n
+bool invert_dense(std::vector<double>& A, int n, std::vector<double>& inv) {
+  inv.assign((size_t)n * n, 0.0);
+  for (int k = 0; k < n; ++k) inv[(size_t)k * n + k] = 1.0;
+  for (int col = 0; col < n; ++col) {
+    int piv = col;
+    for (int r = col + 1; r < n; ++r)
+      if (std::fabs(A[(size_t)r * n + col]) > std::fabs(A[(size_t)piv * n + col])) piv = r;
+    if (A[(size_t)piv * n + col] == 0.0) return false;
+    if (piv != col)
+      for (int k = 0; k < n; ++k) {
+        std::swap(A[(size_t)piv * n + k], A[(size_t)col * n + k]);
+        std::swap(inv[(size_t)piv * n + k], inv[(size_t)col * n + k]);
+      }
+    const double d = 1.0 / A[(size_t)col * n + col];
+    for (int k = 0; k < n; ++k) { A[(size_t)col * n + k] *= d; inv[(size_t)col * n + k] *= d; }
+    for (int r = 0; r < n; ++r) {
+      if (r == col) continue;
+      const double f = A[(size_t)r * n + col];
+      if (f == 0.0) continue;
+      for (int k = 0; k < n; ++k) {
+        A[(size_t)r * n + k] -= f * A[(size_t)col * n + k];
+        inv[(size_t)r * n + k] -= f * inv[(size_t)col * n + k];
+      }
+    }
+  }
+  return true;
+}
+
+}  // namespace
+
+// ------------------------------------------------------------ state ---
+struct StokesState {
+  StokesSystem sys;
+  std::vector<void*> allocs;         // system + solver buffers
+  std::vector<void*> level_allocs;   // multigrid buffers
+  std::vector<Level> levels;
+  float* Ainv = nullptr;
+  int n_dense = 0;
+  double *w = nullptr, *prep = nullptr;  // scaling and pressure factor
+  // FGMRES workspace
+  int m = 0;
+  double *V = nullptr, *Z = nullptr, *r = nullptr, *t = nullptr, *xs = nullptr, *bs = nullptr, *zp = nullptr;
+  double *partial = nullptr, *dots = nullptr, *hdev = nullptr;
+  int nb_dot = 0;
+  double* il = nullptr;              // interleaved staging vector (N)
+  double* tmp = nullptr;             // scratch vector (N)
+  B2 b2_levels{};                    // boundary coefficients the transfer tables were built with
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t gexec = nullptr;
+  int64_t graph_kernels = 0;
+};
+
+namespace {
+
+template <class T>
+int dalloc(eb_ctx* c, std::vector<void*>& owner, T** p, size_t n) {
+  EB_CK(c, cudaMalloc((void**)p, std::max<size_t>(n, 1) * sizeof(T)));
+  owner.push_back(*p);
+  return EB_OK;
+}
+template <class T>
+int dupload(eb_ctx* c, std::vector<void*>& owner, T** p, const std::vector<T>& h) {
+  int rc = dalloc(c, owner, p, h.size());
+  if (rc) return rc;
+  if (!h.empty()) EB_CK(c, cudaMemcpyAsync(*p, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice, c->stream));
+  return EB_OK;
+}
+
+void free_levels(StokesState* st) {
+  for (void* p : st->level_allocs) cudaFree(p);
+  st->level_allocs.clear();
+  st->levels.clear();
+  st->Ainv = nullptr;
+  if (st->gexec) cudaGraphExecDestroy(st->gexec);
+  if (st->graph) cudaGraphDestroy(st->graph);
+  st->gexec = nullptr;
+  st->graph = nullptr;
+}
+
+}  // namespace
+
+StokesSystem* stokes_system(eb_ctx* c) {
+  if (c->st) return &c->st->sys;
+  StokesState* st = new StokesState();
+  StokesSystem& s = st->sys;
+  s.nx = c->xnum - 1;
+  s.ny = c->ynum - 1;
+  s.nc = (int64_t)s.nx * s.ny;
+  const size_t nc = (size_t)s.nc;
+  if (dalloc(c, st->allocs, &s.coef, kStencilSlots * nc) || dalloc(c, st->allocs, &s.rhs, 3 * nc) ||
+      dalloc(c, st->allocs, &s.S, 3 * nc) || dalloc(c, st->allocs, &s.S_old, 3 * nc) ||
+      dalloc(c, st->allocs, &s.resnl, 3 * nc) || dalloc(c, st->allocs, &st->il, 3 * nc) ||
+      dalloc(c, st->allocs, &st->tmp, 3 * nc)) {
+    for (void* p : st->allocs) cudaFree(p);
+    delete st;
+    return nullptr;
+  }
+  cudaMemsetAsync(s.S, 0, 3 * nc * sizeof(double), c->stream);
+  cudaMemsetAsync(s.S_old, 0, 3 * nc * sizeof(double), c->stream);
+  c->st = st;
+  return &st->sys;
+}
+
+void stokes_free(eb_ctx* c) {
+  if (!c->st) return;
+  free_levels(c->st);
+  for (void* p : c->st->allocs) cudaFree(p);
+  delete c->st;
+  c->st = nullptr;
+}
+
+namespace {
+
+// Uniform boundary-condition coefficient per side: the mean of b[:, 2].
+int read_b2(eb_ctx* c, B2* b) {
+  const int ids[8] = {EB_G_BTOPX, EB_G_BBOTTOMX, EB_G_BTOPY, EB_G_BBOTTOMY, EB_G_BLEFTX, EB_G_BRIGHTX, EB_G_BLEFTY, EB_G_BRIGHTY};
+  float* out[8] = {&b->topx, &b->botx, &b->topy, &b->boty, &b->leftx, &b->rightx, &b->lefty, &b->righty};
+  for (int k = 0; k < 8; ++k) {
+    const size_t n = grid_field_count(c, ids[k]) / 2;
+    std::vector<double> h(2 * n);
+    EB_CK(c, cudaMemcpyAsync(h.data(), c->gf[ids[k]], 2 * n * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    EB_CK(c, cudaStreamSynchronize(c->stream));
+    double s = 0.0;
+    for (size_t q = 0; q < n; ++q) s += h[n + q];
+    *out[k] = (float)(s / (double)n);
+  }
+  return EB_OK;
+}
+
+// Build the level geometry, buffers and transfer tables (host), for the current grid and b2.
+int setup_levels(eb_ctx* c, StokesState* st, const B2& b2) {
+  free_levels(st);
+  std::vector<Level>& L = st->levels;
+  L.emplace_back();
+  L[0].x = c->h_gx;
+  L[0].y = c->h_gy;
+  while (true) {
+    Level& f = L.back();
+    f.nx = (int32_t)f.x.size() - 1;
+    f.ny = (int32_t)f.y.size() - 1;
+    f.nc = (int64_t)f.nx * f.ny;
+    if (std::min(f.nx, f.ny) < 4) break;
+    Level cl;
+    const std::vector<int32_t> kx = coarse_nodes(f.nx), ky = coarse_nodes(f.ny);
+    for (int32_t k : kx) cl.x.push_back(f.x[k]);
+    for (int32_t k : ky) cl.y.push_back(f.y[k]);
+    L.push_back(cl);
+    Level& cc = L.back();
+    int rc;
+    if ((rc = dupload(c, st->level_allocs, &cc.kx, kx)) || (rc = dupload(c, st->level_allocs, &cc.ky, ky))) return rc;
+  }
+  const int nlev = (int)L.size();
+  st->n_dense = 2 * (int)L.back().nc;
+  if (st->n_dense > 2048)
+    return eb_fail(c, EB_BAD_INPUT, "grid aspect ratio too large for the multigrid hierarchy (coarsest level has " +
+                                        std::to_string(L.back().nc) + " cells)");
+  for (int l = 0; l < nlev; ++l) {
+    Level& v = L[l];
+    const size_t nc = (size_t)v.nc;
+    int rc;
+    if ((rc = dalloc(c, st->level_allocs, &v.X, 9 * nc)) || (rc = dalloc(c, st->level_allocs, &v.Y, 9 * nc)) ||
+        (rc = dalloc(c, st->level_allocs, &v.ux, nc)) || (rc = dalloc(c, st->level_allocs, &v.uy, nc)) ||
+        (rc = dalloc(c, st->level_allocs, &v.fx, nc)) || (rc = dalloc(c, st->level_allocs, &v.fy, nc)) ||
+        (rc = dalloc(c, st->level_allocs, &v.rx, nc)) || (rc = dalloc(c, st->level_allocs, &v.ry, nc)) ||
+        (rc = dalloc(c, st->level_allocs, &v.etas, (size_t)(v.nx + 1) * (v.ny + 1))) ||
+        (rc = dalloc(c, st->level_allocs, &v.etan, nc)))
+      return rc;
+    // spacing tables (FP32) for the rediscretisation
+    std::vector<double> gxc, sxc, gyc, syc;
+    stag(v.x, gxc, sxc);
+    stag(v.y, gyc, syc);
+    std::vector<float> xs(v.nx), ys(v.ny), xsc(v.nx + 1), ysc(v.ny + 1);
+    for (int32_t j = 0; j < v.nx; ++j) xs[j] = (float)(v.x[j + 1] - v.x[j]);
+    for (int32_t i = 0; i < v.ny; ++i) ys[i] = (float)(v.y[i + 1] - v.y[i]);
+    for (int32_t j = 0; j <= v.nx; ++j) xsc[j] = (float)sxc[j];
+    for (int32_t i = 0; i <= v.ny; ++i) ysc[i] = (float)syc[i];
+    if ((rc = dupload(c, st->level_allocs, &v.xstp, xs)) || (rc = dupload(c, st->level_allocs, &v.ystp, ys)) ||
+        (rc = dupload(c, st->level_allocs, &v.xstpc, xsc)) || (rc = dupload(c, st->level_allocs, &v.ystpc, ysc)))
+      return rc;
+  }
+  // transfer tables between level l (fine) and l+1 (coarse)
+  for (int l = 0; l + 1 < nlev; ++l) {
+    Level& f = L[l];
+    Level& cl = L[l + 1];
+    std::vector<double> gxf, sxf, gyf, syf, gxc, sxc, gyc, syc;
+    stag(f.x, gxf, sxf);
+    stag(f.y, gyf, syf);
+    stag(cl.x, gxc, sxc);
+    stag(cl.y, gyc, syc);
+    // fine positions and control lengths
+    std::vector<double> vx_x(f.x.begin() + 1, f.x.end());           // nodes 1..nx (last: dummy)
+    std::vector<double> vx_y(gyf.begin() + 1, gyf.begin() + 1 + f.ny);  // cell centres
+    std::vector<double> vy_x(gxf.begin() + 1, gxf.begin() + 1 + f.nx);
+    std::vector<double> vy_y(f.y.begin() + 1, f.y.end());           // last: dummy
+    std::vector<double> vol_vx_x(f.nx), vol_vx_y(f.ny), vol_vy_x(f.nx), vol_vy_y(f.ny);
+    for (int32_t j = 0; j < f.nx; ++j) {
+      vol_vx_x[j] = (j == f.nx - 1) ? 0.0 : sxf[j + 1];
+      vol_vy_x[j] = f.x[j + 1] - f.x[j];
+    }
+    for (int32_t i = 0; i < f.ny; ++i) {
+      vol_vx_y[i] = f.y[i + 1] - f.y[i];
+      vol_vy_y[i] = (i == f.ny - 1) ? 0.0 : syf[i + 1];
+    }
+    // coarse positions: [boundary/ghost, unknowns..., boundary/ghost]
+    std::vector<double> c_vx_x(cl.x.begin(), cl.x.end());                  // 0..nxc
+    std::vector<double> c_vx_y(gyc.begin(), gyc.begin() + cl.ny + 2);      // ghost, centres, ghost
+    std::vector<double> c_vy_x(gxc.begin(), gxc.begin() + cl.nx + 2);
+    std::vector<double> c_vy_y(cl.y.begin(), cl.y.end());
+    std::vector<int32_t> pi[4], ri[4];
+    std::vector<float> pw[4], rw[4];
+    interp1d(vx_x, true, c_vx_x, b2.leftx, b2.rightx, pi[0], pw[0], nullptr);
+    interp1d(vx_y, false, c_vx_y, b2.topx, b2.botx, pi[1], pw[1], nullptr);
+    interp1d(vy_x, false, c_vy_x, b2.lefty, b2.righty, pi[2], pw[2], nullptr);
+    interp1d(vy_y, true, c_vy_y, b2.topy, b2.boty, pi[3], pw[3], nullptr);
+    const std::vector<double>* vols[4] = {&vol_vx_x, &vol_vx_y, &vol_vy_x, &vol_vy_y};
+    const int32_t ncs[4] = {cl.nx, cl.ny, cl.nx, cl.ny};
+    for (int a = 0; a < 4; ++a)
+      if (!restrict1d(pi[a], pw[a], *vols[a], ncs[a], ri[a], rw[a]))
+        return eb_fail(c, EB_BAD_INPUT, "multigrid restriction stencil too wide (grid spacing varies too fast)");
+    Axis2* P[4] = {&f.pvx_x, &f.pvx_y, &f.pvy_x, &f.pvy_y};
+    AxisR* R[4] = {&f.rvx_x, &f.rvx_y, &f.rvy_x, &f.rvy_y};
+    for (int a = 0; a < 4; ++a) {
+      int rc;
+      if ((rc = dupload(c, st->level_allocs, &P[a]->idx, pi[a])) || (rc = dupload(c, st->level_allocs, &P[a]->w, pw[a])) ||
+          (rc = dupload(c, st->level_allocs, &R[a]->idx, ri[a])) || (rc = dupload(c, st->level_allocs, &R[a]->w, rw[a])))
+        return rc;
+    }
+  }
+  int rc = dalloc(c, st->level_allocs, &st->Ainv, (size_t)st->n_dense * st->n_dense);
+  if (rc) return rc;
+  EB_CK(c, cudaStreamSynchronize(c->stream));
+  return EB_OK;
+}
+
+// Per-solve operators: level 0 from the FP64 stencil, coarse viscosity and stencils, coarsest inverse.
+int refresh_levels(eb_ctx* c, StokesState* st, const B2& b2) {
+  std::vector<Level>& L = st->levels;
+  const StokesSystem& s = st->sys;
+  EB_PROF(c, "k_mg_setup");
+  k_level0<<<nblk(s.nc), kB, 0, c->stream>>>(s.coef, L[0].X, L[0].Y, s.nc);
+  EB_LAUNCHED(c);
+  EB_PROF(c, "k_mg_setup");
+  k_to_f32<<<nblk((int64_t)c->xnum * c->ynum), kB, 0, c->stream>>>(c->gf[EB_G_ETAS0], L[0].etas, (int64_t)c->xnum * c->ynum);
+  EB_LAUNCHED(c);
+  EB_PROF(c, "k_mg_setup");
+  k_to_f32<<<nblk(s.nc), kB, 0, c->stream>>>(c->gf[EB_G_ETAN0], L[0].etan, s.nc);
+  EB_LAUNCHED(c);
+  for (size_t l = 1; l < L.size(); ++l) {
+    Level& f = L[l - 1];
+    Level& v = L[l];
+    const int64_t n = std::max<int64_t>((int64_t)(v.nx + 1) * (v.ny + 1), v.nc);
+    EB_PROF(c, "k_mg_setup");
+    k_coarsen_eta<<<nblk(n), kB, 0, c->stream>>>(f.etas, f.etan, f.nx, f.ny, v.etas, v.etan, v.nx, v.ny, v.kx, v.ky);
+    EB_LAUNCHED(c);
+    EB_PROF(c, "k_mg_setup");
+    k_redisc<<<nblk(v.nc), kB, 0, c->stream>>>(v.nx, v.ny, v.etas, v.etan, v.xstp, v.ystp, v.xstpc, v.ystpc, b2, v.X, v.Y);
+    EB_LAUNCHED(c);
+  }
+  // coarsest velocity block as a dense matrix on the host, inverted in FP64
+  const Level& cl = L.back();
+  const int nc = (int)cl.nc, n = 2 * nc;
+  std::vector<float> hX(9 * (size_t)nc), hY(9 * (size_t)nc);
+  EB_CK(c, cudaMemcpyAsync(hX.data(), cl.X, hX.size() * sizeof(float), cudaMemcpyDeviceToHost, c->stream));
+  EB_CK(c, cudaMemcpyAsync(hY.data(), cl.Y, hY.size() * sizeof(float), cudaMemcpyDeviceToHost, c->stream));
+  EB_CK(c, cudaStreamSynchronize(c->stream));
+  std::vector<double> A((size_t)n * n, 0.0), inv;
+  const int32_t ny = cl.ny, nx = cl.nx;
+  auto put = [&](int r, int col, double v) { if (v != 0.0) A[(size_t)r * n + col] += v; };
+  for (int cc = 0; cc < nc; ++cc) {
+    const int i = cc % ny, j = cc / ny;
+    const bool hu = i > 0, hd = i < ny - 1, hl = j > 0, hr = j < nx - 1;
+    auto Xs = [&](int k) { return (double)hX[(size_t)k * nc + cc]; };
+    auto Ys = [&](int k) { return (double)hY[(size_t)k * nc + cc]; };
+    put(cc, cc, Xs(0));
+    if (hl) put(cc, cc - ny, Xs(1));
+    if (hr) put(cc, cc + ny, Xs(2));
+    if (hu) put(cc, cc - 1, Xs(3));
+    if (hd) put(cc, cc + 1, Xs(4));
+    if (hu) put(cc, nc + cc - 1, Xs(5));
+    if (hu && hr) put(cc, nc + cc + ny - 1, Xs(6));
+    put(cc, nc + cc, Xs(7));
+    if (hr) put(cc, nc + cc + ny, Xs(8));
+    const int r = nc + cc;
+    put(r, nc + cc, Ys(0));
+    if (hu) put(r, nc + cc - 1, Ys(1));
+    if (hd) put(r, nc + cc + 1, Ys(2));
+    if (hl) put(r, nc + cc - ny, Ys(3));
+    if (hr) put(r, nc + cc + ny, Ys(4));
+    if (hl) put(r, cc - ny, Ys(5));
+    put(r, cc, Ys(6));
+    if (hl && hd) put(r, cc + 1 - ny, Ys(7));
+    if (hd) put(r, cc + 1, Ys(8));
+  }
+  if (!invert_dense(A, n, inv)) return eb_fail(c, EB_NAN, "coarsest multigrid operator is singular");
+  std::vector<float> invf(inv.size());
+  for (size_t k = 0; k < inv.size(); ++k) invf[k] = (float)inv[k];
+  EB_CK(c, cudaMemcpyAsync(st->Ainv, invf.data(), invf.size() * sizeof(float), cudaMemcpyHostToDevice, c->stream));
+  EB_CK(c, cudaStreamSynchronize(c->stream));
+  return EB_OK;
+}
+
+// One V-cycle from level 0's f into level 0's u (launches on c->stream).
+int vcycle_launch(eb_ctx* c, StokesState* st, int sweeps, int64_t* nk) {
+  std::vector<Level>& L = st->levels;
+  const int nl = (int)L.size();
+  auto rb = [&](Level& v, int comp, int color) -> int {
+    const int64_t half = (int64_t)v.nx * ((v.ny + 1) / 2);
+    k_rbgs<<<nblk(half), kB, 0, c->stream>>>(v.X, v.Y, v.ux, v.uy, v.fx, v.fy, v.nx, v.ny, comp, color);
+    ++*nk;
+    return EB_OK;
+  };
+  for (int l = 0; l < nl - 1; ++l) {
+    Level& v = L[l];
+    EB_CK(c, cudaMemsetAsync(v.ux, 0, v.nc * sizeof(float), c->stream));
+    EB_CK(c, cudaMemsetAsync(v.uy, 0, v.nc * sizeof(float), c->stream));
+    for (int s = 0; s < sweeps; ++s) { rb(v, 0, 0); rb(v, 0, 1); rb(v, 1, 0); rb(v, 1, 1); }
+    k_resid<<<nblk(v.nc), kB, 0, c->stream>>>(v.X, v.Y, v.ux, v.uy, v.fx, v.fy, v.rx, v.ry, v.nx, v.ny);
+    Level& w = L[l + 1];
+    k_restrict<<<nblk(w.nc), kB, 0, c->stream>>>(v.rx, v.ry, v.ny, w.fx, w.fy, w.nx, w.ny, v.rvx_x, v.rvx_y, v.rvy_x,
+                                                  v.rvy_y);
+    *nk += 2;
+  }
+  Level& cl = L[nl - 1];
+  k_dense_solve<<<1, 512, 0, c->stream>>>(st->Ainv, st->n_dense, cl.fx, cl.fy, cl.ux, cl.uy);
+  ++*nk;
+  for (int l = nl - 2; l >= 0; --l) {
+    Level& v = L[l];
+    Level& w = L[l + 1];
+    k_prolong<<<nblk(v.nc), kB, 0, c->stream>>>(v.ux, v.uy, v.nx, v.ny, w.ux, w.uy, w.ny, v.pvx_x, v.pvx_y, v.pvy_x,
+                                                 v.pvy_y);
+    ++*nk;
+    for (int s = 0; s < sweeps; ++s) { rb(v, 1, 1); rb(v, 1, 0); rb(v, 0, 1); rb(v, 0, 0); }
+  }
+  EB_CK(c, cudaGetLastError());
+  return EB_OK;
+}
+
+int capture_vcycle(eb_ctx* c, StokesState* st, int sweeps) {
+  if (st->gexec) { cudaGraphExecDestroy(st->gexec); st->gexec = nullptr; }
+  if (st->graph) { cudaGraphDestroy(st->graph); st->graph = nullptr; }
+  const bool prof = c->prof.on;
+  c->prof.on = false;
+  int64_t nk = 0;
+  EB_CK(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+  int rc = vcycle_launch(c, st, sweeps, &nk);
+  cudaGraph_t g = nullptr;
+  cudaError_t e = cudaStreamEndCapture(c->stream, &g);
+  c->prof.on = prof;
+  if (rc) return rc;
+  if (e != cudaSuccess) return eb_cuda(c, e, "cudaStreamEndCapture");
+  st->graph = g;
+  EB_CK(c, cudaGraphInstantiate(&st->gexec, g, 0));
+  st->graph_kernels = nk;
+  return EB_OK;
+}
+
+// z = W^-1 M^-1 W^-1 rhat  (rhat, z: SoA FP64 of 3 nc)
+int precondition(eb_ctx* c, StokesState* st, const double* rhat, double* z) {
+  const StokesSystem& s = st->sys;
+  const int64_t n3 = 3 * s.nc;
+  Level& v = st->levels[0];
+  EB_PROF(c, "k_precond");
+  k_mul<<<nblk(n3), kB, 0, c->stream>>>(st->t, rhat, st->w, n3, 1);  // r = rhat ./ w
+  EB_LAUNCHED(c);
+  EB_PROF(c, "k_precond");
+  k_prec_in<<<nblk(s.nc), kB, 0, c->stream>>>(s.coef, st->t, st->prep, z + 2 * s.nc, v.fx, v.fy, s.nx, s.ny);
+  EB_LAUNCHED(c);
+  EB_PROF(c, "vcycle_graph");
+  EB_CK(c, cudaGraphLaunch(st->gexec, c->stream));
+  c->launches += st->graph_kernels - 1;
+  EB_LAUNCHED(c);
+  EB_PROF(c, "k_precond");
+  k_prec_out<<<nblk(s.nc), kB, 0, c->stream>>>(v.ux, v.uy, z, s.nc);
+  EB_LAUNCHED(c);
+  EB_PROF(c, "k_precond");
+  k_mul<<<nblk(n3), kB, 0, c->stream>>>(z, z, st->w, n3, 1);  // z ./ w
+  EB_LAUNCHED(c);
+  return EB_OK;
+}
+
+// dots[v] = V_v . u for v < nv (device), copied to host h
+int mdot(eb_ctx* c, StokesState* st, const double* V, int64_t stride, int nv, const double* u, double* h) {
+  const int64_t n3 = 3 * st->sys.nc;
+  dim3 grid(st->nb_dot, nv);
+  EB_PROF(c, "k_mdot");
+  k_mdot<<<grid, kB, 0, c->stream>>>(V, stride, u, n3, st->partial);
+  EB_LAUNCHED(c);
+  EB_PROF(c, "k_mdot");
+  k_mdot_final<<<nv, kB, 0, c->stream>>>(st->partial, st->nb_dot, st->dots);
+  EB_LAUNCHED(c);
+  EB_CK(c, cudaMemcpyAsync(h, st->dots, nv * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  EB_CK(c, cudaStreamSynchronize(c->stream));
+  return EB_OK;
+}
+
+int apply_scaled(eb_ctx* c, StokesState* st, const double* x, double* y) {
+  const StokesSystem& s = st->sys;
+  EB_PROF(c, "k_apply64");
+  k_apply64<<<nblk(s.nc), kB, 0, c->stream>>>(s.coef, x, y, st->w, s.nx, s.ny, s.nc);
+  EB_LAUNCHED(c);
+  return EB_OK;
+}
+
+int ensure_solver(eb_ctx* c, StokesState* st, int m) {
+  if (st->m == m && st->V) return EB_OK;
+  // (re)allocate the Krylov workspace
+  for (double** p : {&st->V, &st->Z}) {
+    if (*p) {
+      cudaFree(*p);
+      st->allocs.erase(std::remove(st->allocs.begin(), st->allocs.end(), (void*)*p), st->allocs.end());
+      *p = nullptr;
+    }
+  }
+  const size_t n3 = 3 * (size_t)st->sys.nc;
+  st->m = m;
+  st->nb_dot = 2 * 152;
+  int rc;
+  if ((rc = dalloc(c, st->allocs, &st->V, (size_t)(m + 1) * n3)) || (rc = dalloc(c, st->allocs, &st->Z, (size_t)m * n3)))
+    return rc;
+  if (!st->r) {
+    if ((rc = dalloc(c, st->allocs, &st->r, n3)) || (rc = dalloc(c, st->allocs, &st->t, n3)) ||
+        (rc = dalloc(c, st->allocs, &st->xs, n3)) || (rc = dalloc(c, st->allocs, &st->bs, n3)) ||
+        (rc = dalloc(c, st->allocs, &st->w, n3)) || (rc = dalloc(c, st->allocs, &st->prep, (size_t)st->sys.nc)) ||
+        (rc = dalloc(c, st->allocs, &st->partial, (size_t)st->nb_dot * 512)) ||
+        (rc = dalloc(c, st->allocs, &st->dots, 512)) || (rc = dalloc(c, st->allocs, &st->hdev, 512)))
+      return rc;
+  }
+  return EB_OK;
+}
+
+}  // namespace
+
+// ------------------------------------------------------------ C-ABI ---
+static int need_system(eb_ctx* c, bool built) {
+  if (!c) return EB_BAD_INPUT;
+  if (!c->have_grid) return eb_fail(c, EB_NOT_READY, "eb_set_grid has not been called");
+  cudaSetDevice(c->device);
+  if (!stokes_system(c)) return eb_fail(c, EB_CUDA_ERROR, "out of device memory for the Stokes system");
+  if (built && !c->st->sys.built) return eb_fail(c, EB_NOT_READY, "eb_build_stokes_system has not been called");
+  return EB_OK;
+}
+
+extern "C" int eb_solve_stokes_system(eb_ctx* c, const eb_solve_opts* o, eb_solve_report* rep) {
+  int rc = need_system(c, true);
+  if (rc) return rc;
+  const auto t0 = std::chrono::steady_clock::now();
+  StokesState* st = c->st;
+  StokesSystem& s = st->sys;
+  eb_solve_opts opt = o ? *o : eb_solve_opts{};
+  if (opt.rtol <= 0) opt.rtol = 1e-8;
+  if (opt.max_iters <= 0) opt.max_iters = 3000;
+  if (opt.restart <= 0) opt.restart = 40;
+  if (opt.mg_sweeps <= 0) opt.mg_sweeps = 2;
+  const int m = std::min(opt.restart, 200);
+  const int64_t n3 = 3 * s.nc;
+  B2 b2;
+  if ((rc = ensure_solver(c, st, m)) || (rc = read_b2(c, &b2))) return rc;
+  if (st->levels.empty() || std::memcmp(&b2, &st->b2_levels, sizeof(B2)) != 0) {
+    if ((rc = setup_levels(c, st, b2))) return rc;
+    st->b2_levels = b2;
+  }
+  if ((rc = refresh_levels(c, st, b2)) || (rc = capture_vcycle(c, st, opt.mg_sweeps))) return rc;
+  EB_PROF(c, "k_scaling");
+  k_scaling<<<nblk(s.nc), kB, 0, c->stream>>>(s.coef, c->gf[EB_G_ETAN0], s.pscale, st->w, st->prep, s.nc);
+  EB_LAUNCHED(c);
+  // bhat = W R, xhat = W^-1 S0
+  EB_PROF(c, "k_axpy");
+  k_mul<<<nblk(n3), kB, 0, c->stream>>>(st->bs, s.rhs, st->w, n3, 0);
+  EB_LAUNCHED(c);
+  if (opt.use_initial_guess) {
+    EB_PROF(c, "k_axpy");
+    k_mul<<<nblk(n3), kB, 0, c->stream>>>(st->xs, s.S, st->w, n3, 1);
+    EB_LAUNCHED(c);
+  } else {
+    EB_CK(c, cudaMemsetAsync(st->xs, 0, n3 * sizeof(double), c->stream));
+  }
+  double bn2;
+  if ((rc = mdot(c, st, st->bs, 0, 1, st->bs, &bn2))) return rc;
+  const double bnorm = std::sqrt(bn2);
+  if (!std::isfinite(bnorm)) return eb_fail(c, EB_NAN, "right-hand side has NaN/Inf");
+  std::vector<double> H((size_t)(m + 1) * m), g(m + 1), cs(m), sn(m), hcol(m + 2), y(m);
+  int it = 0;
+  double est = 1.0;
+  bool converged = (bnorm == 0.0);
+  while (!converged && it < opt.max_iters) {
+    // r = bhat - Khat xhat
+    if ((rc = apply_scaled(c, st, st->xs, st->t))) return rc;
+    EB_PROF(c, "k_axpy");
+    k_sub<<<nblk(n3), kB, 0, c->stream>>>(st->r, st->bs, st->t, n3);
+    EB_LAUNCHED(c);
+    double beta2;
+    if ((rc = mdot(c, st, st->r, 0, 1, st->r, &beta2))) return rc;
+    const double beta = std::sqrt(beta2);
+    if (!std::isfinite(beta)) return eb_fail(c, EB_NAN, "FGMRES residual became NaN/Inf");
+    est = beta / bnorm;
+    if (est <= opt.rtol) { converged = true; break; }
+    EB_PROF(c, "k_axpy");
+    k_scale_copy<<<nblk(n3), kB, 0, c->stream>>>(st->V, st->r, 1.0 / beta, n3);
+    EB_LAUNCHED(c);
+    std::fill(g.begin(), g.end(), 0.0);
+    g[0] = beta;
+    int k = 0;
+    for (; k < m && it < opt.max_iters; ++k) {
+      double* vk = st->V + (size_t)k * n3;
+      double* zk = st->Z + (size_t)k * n3;
+      double* w = st->V + (size_t)(k + 1) * n3;
+      if ((rc = precondition(c, st, vk, zk)) || (rc = apply_scaled(c, st, zk, w))) return rc;
+      // classical Gram-Schmidt with one conditional re-orthogonalisation
+      double wn2_before;
+      if ((rc = mdot(c, st, w, 0, 1, w, &wn2_before))) return rc;
+      for (int pass = 0; pass < 2; ++pass) {
+        std::vector<double> h(k + 1);
+        if ((rc = mdot(c, st, st->V, n3, k + 1, w, h.data()))) return rc;
+        EB_CK(c, cudaMemcpyAsync(st->hdev, h.data(), (k + 1) * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+        EB_PROF(c, "k_maxpy");
+        k_maxpy<<<nblk(n3), kB, 0, c->stream>>>(w, st->V, n3, st->hdev, k + 1, n3);
+        EB_LAUNCHED(c);
+        for (int q = 0; q <= k; ++q) hcol[q] = (pass == 0 ? 0.0 : hcol[q]) + h[q];
+        double wn2;
+        if ((rc = mdot(c, st, w, 0, 1, w, &wn2))) return rc;
+        hcol[k + 1] = std::sqrt(wn2);
+        if (!std::isfinite(hcol[k + 1])) return eb_fail(c, EB_NAN, "FGMRES basis became NaN/Inf");
+        if (hcol[k + 1] > 0.7071 * std::sqrt(wn2_before)) break;
+        wn2_before = wn2;
+      }
+      // apply the previous rotations, then a new one
+      for (int q = 0; q < k; ++q) {
+        const double a = cs[q] * hcol[q] + sn[q] * hcol[q + 1];
+        hcol[q + 1] = -sn[q] * hcol[q] + cs[q] * hcol[q + 1];
+        hcol[q] = a;
+      }
+      const double d = std::hypot(hcol[k], hcol[k + 1]);
+      cs[k] = (d == 0.0) ? 1.0 : hcol[k] / d;
+      sn[k] = (d == 0.0) ? 0.0 : hcol[k + 1] / d;
+      const double hk1 = hcol[k + 1];
+      hcol[k] = d;
+      for (int q = 0; q <= k; ++q) H[(size_t)q * m + k] = hcol[q];
+      g[k + 1] = -sn[k] * g[k];
+      g[k] = cs[k] * g[k];
+      ++it;
+      est = std::fabs(g[k + 1]) / bnorm;
+      if (hk1 > 0.0) {
+        EB_PROF(c, "k_axpy");
+        k_scale_copy<<<nblk(n3), kB, 0, c->stream>>>(w, w, 1.0 / hk1, n3);
+        EB_LAUNCHED(c);
+      }
+      if (est <= opt.rtol || hk1 == 0.0) { ++k; break; }
+    }
+    // y = H^-1 g (upper triangular k x k), xhat += Z y
+    for (int q = k - 1; q >= 0; --q) {
+      double sacc = g[q];
+      for (int p = q + 1; p < k; ++p) sacc -= H[(size_t)q * m + p] * y[p];
+      y[q] = sacc / H[(size_t)q * m + q];
+    }
+    std::vector<double> negy(k);
+    for (int q = 0; q < k; ++q) negy[q] = -y[q];
+    EB_CK(c, cudaMemcpyAsync(st->hdev, negy.data(), k * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    EB_PROF(c, "k_maxpy");
+    k_maxpy<<<nblk(n3), kB, 0, c->stream>>>(st->xs, st->Z, n3, st->hdev, k, n3);
+    EB_LAUNCHED(c);
+    EB_CK(c, cudaStreamSynchronize(c->stream));
+  }
+  // S = W xhat; true residual of the unscaled system
+  EB_PROF(c, "k_axpy");
+  k_mul<<<nblk(n3), kB, 0, c->stream>>>(s.S, st->xs, st->w, n3, 0);
+  EB_LAUNCHED(c);
+  EB_PROF(c, "k_apply64");
+  k_apply64<<<nblk(s.nc), kB, 0, c->stream>>>(s.coef, s.S, st->t, nullptr, s.nx, s.ny, s.nc);
+  EB_LAUNCHED(c);
+  EB_PROF(c, "k_axpy");
+  k_sub<<<nblk(n3), kB, 0, c->stream>>>(st->r, s.rhs, st->t, n3);
+  EB_LAUNCHED(c);
+  double rr, RR, sr2;
+  if ((rc = mdot(c, st, st->r, 0, 1, st->r, &rr)) || (rc = mdot(c, st, s.rhs, 0, 1, s.rhs, &RR))) return rc;
+  // scaled residual of the final iterate
+  if ((rc = apply_scaled(c, st, st->xs, st->t))) return rc;
+  EB_PROF(c, "k_axpy");
+  k_sub<<<nblk(n3), kB, 0, c->stream>>>(st->r, st->bs, st->t, n3);
+  EB_LAUNCHED(c);
+  if ((rc = mdot(c, st, st->r, 0, 1, st->r, &sr2))) return rc;
+  prof_resolve(c);
+  const double rel = RR > 0 ? std::sqrt(rr / RR) : std::sqrt(rr);
+  const double rel_s = bnorm > 0 ? std::sqrt(sr2) / bnorm : std::sqrt(sr2);
+  if (rep) {
+    rep->iterations = it;
+    rep->levels = (int32_t)st->levels.size();
+    rep->rel_residual = rel;
+    rep->rel_residual_scaled = rel_s;
+    rep->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  }
+  if (!std::isfinite(rel)) return eb_fail(c, EB_NAN, "Stokes solution has NaN/Inf");
+  if (rel_s > opt.rtol * 1.0000001)
+    return eb_fail(c, EB_NOT_CONVERGED, "FGMRES stopped at scaled relative residual " + std::to_string(rel_s) +
+                                            " after " + std::to_string(it) + " iterations");
+  return EB_OK;
+}
+
+extern "C" int eb_set_stokes_params(eb_ctx* c, const eb_stokes_params* p) {
+  if (!c || !p) return EB_BAD_INPUT;
+  if (p->pressure_bc_mode < 0 || p->pressure_bc_mode > 2) return eb_fail(c, EB_BAD_INPUT, "pressure_bc_mode must be 0, 1 or 2");
+  c->SP = *p;
+  c->have_stokes_params = true;
+  return EB_OK;
+}
+
+static int need_fields(eb_ctx* c, std::initializer_list<int> ids) {
+  for (int f : ids) {
+    int rc = ensure_grid_field(c, f);
+    if (rc) return rc;
+  }
+  return EB_OK;
+}
+
+extern "C" int eb_calc_viscoelastic_terms(eb_ctx* c) {
+  if (!c) return EB_BAD_INPUT;
+  if (!c->have_grid || !c->have_params) return eb_fail(c, EB_NOT_READY, "eb_set_grid and eb_set_params come first");
+  cudaSetDevice(c->device);
+  int rc = need_fields(c, {EB_G_ETAS1, EB_G_MUS1, EB_G_SXY1, EB_G_ETAS0, EB_G_SXY0, EB_G_ETAN1, EB_G_MUN1, EB_G_SXX1,
+                           EB_G_ETAN0, EB_G_SXX0});
+  if (rc || (rc = launch_viscoelastic_terms(c))) return rc;
+  EB_CK(c, cudaStreamSynchronize(c->stream));
+  prof_resolve(c);
+  return EB_OK;
+}
+
+extern "C" int eb_viscoelastic_rhs(eb_ctx* c) {
+  if (!c) return EB_BAD_INPUT;
+  if (!c->have_grid || !c->have_stokes_params) return eb_fail(c, EB_NOT_READY, "eb_set_grid and eb_set_stokes_params come first");
+  cudaSetDevice(c->device);
+  int rc = need_fields(c, {EB_G_RHO1, EB_G_RHO1_VY, EB_G_SXX0, EB_G_SXY0, EB_G_DILAT, EB_G_EII_PLASTIC_PRESSURE, EB_G_RX1,
+                           EB_G_RY1, EB_G_RC1});
+  if (rc || (rc = launch_viscoelastic_rhs(c))) return rc;
+  EB_CK(c, cudaStreamSynchronize(c->stream));
+  prof_resolve(c);
+  return EB_OK;
+}
+
+extern "C" int eb_build_stokes_system(eb_ctx* c) {
+  int rc = need_system(c, false);
+  if (rc) return rc;
+  if (!c->have_params || !c->have_stokes_params) return eb_fail(c, EB_NOT_READY, "eb_set_params and eb_set_stokes_params come first");
+  if ((rc = need_fields(c, {EB_G_ETAN0, EB_G_ETAS0, EB_G_RHO1_VY, EB_G_RX1, EB_G_RY1, EB_G_RC1, EB_G_BTOPX, EB_G_BBOTTOMX,
+                            EB_G_BTOPY, EB_G_BBOTTOMY, EB_G_BLEFTX, EB_G_BRIGHTX, EB_G_BLEFTY, EB_G_BRIGHTY, EB_G_VX1,
+                            EB_G_VY1, EB_G_PR1})))
+    return rc;
+  StokesSystem* s = &c->st->sys;
+  // SystemSolver.initialize_solver!: zero vx1, vy1, pr1; pscale from etan0[1,1]
+  const int32_t X = c->xnum, Y = c->ynum;
+  EB_CK(c, cudaMemsetAsync(c->gf[EB_G_VX1], 0, sizeof(double) * (size_t)(Y + 1) * X, c->stream));
+  EB_CK(c, cudaMemsetAsync(c->gf[EB_G_VY1], 0, sizeof(double) * (size_t)Y * (X + 1), c->stream));
+  EB_CK(c, cudaMemsetAsync(c->gf[EB_G_PR1], 0, sizeof(double) * (size_t)(Y - 1) * (X - 1), c->stream));
+  double etan11;
+  EB_CK(c, cudaMemcpyAsync(&etan11, c->gf[EB_G_ETAN0], sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  EB_CK(c, cudaStreamSynchronize(c->stream));
+  s->pscale = 2.0 * etan11 / (c->g.xstpavg + c->g.ystpavg);
+  if ((rc = launch_build_stokes_system(c, s))) return rc;
+  EB_CK(c, cudaStreamSynchronize(c->stream));
+  prof_resolve(c);
+  s->built = true;
+  return EB_OK;
+}
+
+extern "C" int eb_process_stokes_solution(eb_ctx* c) {
+  int rc = need_system(c, true);
+  if (rc || (rc = need_fields(c, {EB_G_VX1, EB_G_VY1, EB_G_PR1}))) return rc;
+  if ((rc = launch_process_stokes_solution(c, &c->st->sys))) return rc;
+  EB_CK(c, cudaStreamSynchronize(c->stream));
+  prof_resolve(c);
+  return EB_OK;
+}
+
+extern "C" int eb_stokes_nonlinear_residual(eb_ctx* c) {
+  int rc = need_system(c, true);
+  if (rc) return rc;
+  StokesSystem& s = c->st->sys;
+  double* tmp = c->st->il;  // N doubles
+  EB_PROF(c, "k_apply64");
+  k_apply64<<<nblk(s.nc), kB, 0, c->stream>>>(s.coef, s.S_old, tmp, nullptr, s.nx, s.ny, s.nc);
+  EB_LAUNCHED(c);
+  EB_PROF(c, "k_axpy");
+  k_abs_sub<<<nblk(3 * s.nc), kB, 0, c->stream>>>(s.resnl, tmp, s.rhs, 3 * s.nc);
+  EB_LAUNCHED(c);
+  EB_CK(c, cudaStreamSynchronize(c->stream));
+  prof_resolve(c);
+  return EB_OK;
+}
+
+extern "C" int eb_backup_stokes_solution(eb_ctx* c) {
+  int rc = need_system(c, false);
+  if (rc) return rc;
+  StokesSystem& s = c->st->sys;
+  EB_CK(c, cudaMemcpyAsync(s.S_old, s.S, 3 * s.nc * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
+  EB_CK(c, cudaStreamSynchronize(c->stream));
+  return EB_OK;
+}
+
+static double* vector_ptr(StokesSystem& s, int which) {
+  switch (which) {
+    case EB_SV_SOLUTION: return s.S;
+    case EB_SV_RHS: return s.rhs;
+    case EB_SV_SOLUTION_OLD: return s.S_old;
+    case EB_SV_RESNL: return s.resnl;
+    default: return nullptr;
+  }
+}
+
+extern "C" int eb_stokes_vector_upload(eb_ctx* c, int which, const double* host) {
+  int rc = need_system(c, false);
+  if (rc) return rc;
+  StokesSystem& s = c->st->sys;
+  double* d = vector_ptr(s, which);
+  if (!d || !host) return eb_fail(c, EB_BAD_INPUT, "bad Stokes vector id or null pointer");
+  EB_CK(c, cudaMemcpyAsync(c->st->il, host, 3 * s.nc * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  EB_PROF(c, "k_interleave");
+  k_deinterleave<<<nblk(s.nc), kB, 0, c->stream>>>(c->st->il, d, s.nc);
+  EB_LAUNCHED(c);
+  EB_CK(c, cudaStreamSynchronize(c->stream));
+  prof_resolve(c);
+  return EB_OK;
+}
+
+extern "C" int eb_stokes_vector_download(eb_ctx* c, int which, double* host) {
+  int rc = need_system(c, false);
+  if (rc) return rc;
+  StokesSystem& s = c->st->sys;
+  double* d = vector_ptr(s, which);
+  if (!d || !host) return eb_fail(c, EB_BAD_INPUT, "bad Stokes vector id or null pointer");
+  EB_PROF(c, "k_interleave");
+  k_interleave<<<nblk(s.nc), kB, 0, c->stream>>>(d, c->st->il, s.nc);
+  EB_LAUNCHED(c);
+  EB_CK(c, cudaMemcpyAsync(host, c->st->il, 3 * s.nc * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  EB_CK(c, cudaStreamSynchronize(c->stream));
+  prof_resolve(c);
+  return EB_OK;
+}
+
+extern "C" int eb_stokes_apply(eb_ctx* c, const double* x, double* y) {
+  int rc = need_system(c, true);
+  if (rc) return rc;
+  if (!x || !y) return eb_fail(c, EB_BAD_INPUT, "null vector");
+  StokesSystem& s = c->st->sys;
+  double* xin = c->st->tmp;
+  EB_CK(c, cudaMemcpyAsync(c->st->il, x, 3 * s.nc * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  EB_PROF(c, "k_interleave");
+  k_deinterleave<<<nblk(s.nc), kB, 0, c->stream>>>(c->st->il, xin, s.nc);
+  EB_LAUNCHED(c);
+  EB_PROF(c, "k_apply64");
+  k_apply64<<<nblk(s.nc), kB, 0, c->stream>>>(s.coef, xin, c->st->il, nullptr, s.nx, s.ny, s.nc);
+  EB_LAUNCHED(c);
+  EB_PROF(c, "k_interleave");
+  k_interleave<<<nblk(s.nc), kB, 0, c->stream>>>(c->st->il, xin, s.nc);
+  EB_LAUNCHED(c);
+  EB_CK(c, cudaMemcpyAsync(y, xin, 3 * s.nc * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  EB_CK(c, cudaStreamSynchronize(c->stream));
+  prof_resolve(c);
+  return EB_OK;
+}
+
+extern "C" int eb_stokes_stencil_download(eb_ctx* c, double* host) {
+  int rc = need_system(c, true);
+  if (rc) return rc;
+  if (!host) return eb_fail(c, EB_BAD_INPUT, "null pointer");
+  StokesSystem& s = c->st->sys;
+  EB_CK(c, cudaMemcpyAsync(host, s.coef, kStencilSlots * s.nc * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  EB_CK(c, cudaStreamSynchronize(c->stream));
+  return EB_OK;
+}
+
+extern "C" double eb_stokes_pscale(const eb_ctx* c) { return (c && c->st) ? c->st->sys.pscale : 0.0; }
+extern "C" int64_t eb_stokes_size(const eb_ctx* c) {
+  return (c && c->have_grid) ? 3 * (int64_t)(c->xnum - 1) * (c->ynum - 1) : 0;
+}

@@ -206,6 +206,38 @@ def _analytic_grids(grid: Grid, v0: float, eta_ref: float, rho_ref: float, T0: f
     return out
 
 
+def velocity_bcs(grid: Grid, v_ext: float = 0.0, free_slip_bottom: bool = True) -> dict:
+    """Velocity boundary-condition coefficient arrays (the reference's vel_comp
+    arrays): ghost = b[:, 0] + b[:, 1] * interior.  Free slip on top and on the
+    sides for the tangential component; the sides move outwards at v_ext and the
+    bottom brings in the balancing inflow (zero when v_ext = 0)."""
+    X, Y = grid.xnum, grid.ynum
+    W, H = grid.xmax - grid.xmin, grid.ymax - grid.ymin
+    F = np.asfortranarray
+    v_in = -2.0 * v_ext * H / W            # upward (y grows with depth)
+    out = {}
+    out["btopx"] = F(np.column_stack([np.zeros(X), np.ones(X)]))
+    out["btopy"] = F(np.column_stack([np.zeros(X + 1), np.zeros(X + 1)]))
+    out["bbottomx"] = F(np.column_stack([np.zeros(X), np.ones(X) if free_slip_bottom else -np.ones(X)]))
+    out["bbottomy"] = F(np.column_stack([np.full(X + 1, v_in), np.zeros(X + 1)]))
+    out["bleftx"] = F(np.column_stack([np.full(Y + 1, -v_ext), np.zeros(Y + 1)]))
+    out["brightx"] = F(np.column_stack([np.full(Y + 1, v_ext), np.zeros(Y + 1)]))
+    out["blefty"] = F(np.column_stack([np.zeros(Y), np.ones(Y)]))
+    out["brighty"] = F(np.column_stack([np.zeros(Y), np.ones(Y)]))
+    out["eii_plastic_pressure"] = F(np.zeros((Y - 1, X - 1)))
+    for name, shape in (("RX1", (Y + 1, X)), ("RY1", (Y, X + 1)), ("RC1", (Y - 1, X - 1))):
+        out[name] = F(np.zeros(shape))
+    return out
+
+
+def stokes_params(**kw) -> dict:
+    """Scalar Stokes parameters (gravity, interface stabilisation, pressure BC, internal velocity zone off)."""
+    p = dict(gravity_x=0.0, gravity_y=9.81, iuse_interface_stabilization=1, pressure_bc_mode=0, pressure_bc=1e5,
+             bintern_zone=np.array([-1, 0, 0, 0, -1, 0, 0, 0], np.int64), bintern_velocity=np.zeros(8))
+    p.update(kw)
+    return p
+
+
 def sinking_block(xnum: int = 101, ynum: int = 101, mpc: int = 4, seed: int = 1) -> Model:
     rng = np.random.Generator(np.random.Philox(seed))
     W = H = 500e3
@@ -243,7 +275,9 @@ def sinking_block(xnum: int = 101, ynum: int = 101, mpc: int = 4, seed: int = 1)
     m["pfailure"][:] = 0.0
     grids = _analytic_grids(grid, v0=1e-2 / YEAR, eta_ref=1e21, rho_ref=3200.0, T0=273.15, T1=1273.15,
                             depth_T1=H, y_surface=0.0)
+    grids.update(velocity_bcs(grid))
     params = default_params(timestep=1e4 * YEAR, viscosity_min=1e18, viscosity_max=1e28, ntimestep=1)
+    params.update(stokes_params())
     return Model("sinking_block", grid, mats, params, m, grids)
 
 
@@ -302,7 +336,9 @@ def rift(xnum: int = 801, ynum: int = 201, mpc: int = 4, seed: int = 2, width: f
     _fields_common(rng, n, m)
     grids = _analytic_grids(grid, v0=v0, eta_ref=1e22, rho_ref=2900.0, T0=273.15, T1=1603.15, depth_T1=120e3,
                             y_surface=air)
+    grids.update(velocity_bcs(grid, v_ext=0.5 * v0))
     params = default_params(timestep=1e4 * YEAR, y_sealevel=air, matid_sticky_air=1)
+    params.update(stokes_params())
     return Model(f"rift_{xnum}x{ynum}_{mpc}", grid, mats, params, m, grids)
 
 

@@ -112,7 +112,8 @@ enum eb_marker_field {
 /* ---- grid fields ------------------------------------------------------------
  * Shapes: B = basic (ynum, xnum); P = pressure (ynum-1, xnum-1);
  *         VX = (ynum+1, xnum); VY = (ynum, xnum+1);
- *         BCX = (xnum, 2) thermal top/bottom BC; BCY = (ynum, 2) left/right BC. */
+ *         BCX = (xnum, 2) thermal top/bottom BC; BCY = (ynum, 2) left/right BC;
+ *         velocity BC shapes are listed beside them below. */
 enum eb_grid_field {
   /* basic grid */
   EB_G_RHO1 = 0, EB_G_RHO0, EB_G_ETAS1, EB_G_ETAS0, EB_G_ETA_FLOW, EB_G_ETA_FLOW0,
@@ -132,6 +133,13 @@ enum eb_grid_field {
   EB_G_VY1, EB_G_RHO1_VY, EB_G_RHO0_VY, EB_G_WTNODES_VY,
   /* thermal boundary-condition coefficient arrays */
   EB_G_BTOPT, EB_G_BBOTTOMT, EB_G_BLEFTT, EB_G_BRIGHTT,
+  /* Stokes right-hand sides RX1 (VX), RY1 (VY), RC1 (P); plastic strain rate (P) */
+  EB_G_RX1, EB_G_RY1, EB_G_RC1, EB_G_EII_PLASTIC_PRESSURE,
+  /* velocity boundary-condition coefficient arrays (ghost = b[:,1] + b[:,2] * interior):
+   * btopx/bbottomx (xnum, 2), btopy/bbottomy (xnum+1, 2), bleftx/brightx (ynum+1, 2),
+   * blefty/brighty (ynum, 2) */
+  EB_G_BTOPX, EB_G_BBOTTOMX, EB_G_BTOPY, EB_G_BBOTTOMY,
+  EB_G_BLEFTX, EB_G_BRIGHTX, EB_G_BLEFTY, EB_G_BRIGHTY,
   EB_G_NFIELDS
 };
 
@@ -246,6 +254,96 @@ int eb_advect_markers_and_rotate_stress(eb_ctx* ctx);
 
 /* Advection.update_marker_strain!  (Advection.jl:169-178 -> MarkersStrain.jl:11-136) */
 int eb_update_marker_strain(eb_ctx* ctx);
+
+/* ---- Stokes-continuity step --------------------------------------------------
+ * The grid-side half of StokesContinuitySolver.solve_viscoelastic_stokes_continuity_equations!
+ * (src/stokes_continuity_solver/StokesContinuitySolver.jl:68-110).  Inputs are
+ * context grid fields (eb_grid_upload): etas1, mus1, sxy1, etan1, mun1, sxx1,
+ * rho1, rho1_vy, dilatation_grid, eii_plastic_pressure and the eight velocity
+ * BC arrays; outputs are etas0, sxy0, etan0, sxx0, RX1, RY1, RC1, vx1, vy1, pr1
+ * and the solution vector S.
+ * The system has N = 3 (xnum-1)(ynum-1) unknowns interleaved per basic cell
+ * (vx, vy, p / pscale), cells column-major (GlobalIndices.jl:13-27), exactly
+ * the reference's S.  It is kept on the device as a stored 27-coefficient
+ * stencil per cell whose values are the reference's COO values (Li, Lj, Lv). */
+typedef struct eb_stokes_params {
+  double  gravity_x, gravity_y;          /* m/s^2 (model.gravity.parameters)                    */
+  int64_t iuse_interface_stabilization;  /* 1: drho/dx, drho/dy g dt terms in the y-Stokes rows  */
+  int64_t pressure_bc_mode;              /* 0 upper-left cell, 1 top/bottom rows, 2 left/right   */
+  double  pressure_bc;                   /* Pa                                                   */
+  int64_t bintern_zone[8];               /* internal prescribed-velocity zone, reference layout  */
+  double  bintern_velocity[8];
+} eb_stokes_params;
+
+/* Options of the iterative solve that replaces the direct sparse solve. */
+typedef struct eb_solve_opts {
+  double  rtol;              /* stop when ||W(R - L S)|| <= rtol ||W R|| (W: diagonal scaling); 0 -> 1e-8 */
+  int32_t max_iters;         /* FGMRES iterations; 0 -> 3000                                          */
+  int32_t restart;           /* Krylov basis size; 0 -> 40                                             */
+  int32_t mg_sweeps;         /* red-black Gauss-Seidel sweeps before/after each coarse correction; 0 -> 2 */
+  int32_t use_initial_guess; /* 1: start from the current device solution vector, 0: from zero         */
+} eb_solve_opts;
+
+typedef struct eb_solve_report {
+  int32_t iterations;        /* FGMRES iterations run                                   */
+  int32_t levels;            /* multigrid levels of the velocity preconditioner         */
+  double  rel_residual;      /* ||R - L S||_2 / ||R||_2 of the assembled (unscaled) system */
+  double  rel_residual_scaled; /* the same for the diagonally scaled system             */
+  double  seconds;           /* wall time of the solve                                  */
+} eb_solve_report;
+
+enum eb_stokes_vector {
+  EB_SV_SOLUTION = 0,        /* S (soluv1)                                  */
+  EB_SV_RHS,                 /* R (RHS)                                     */
+  EB_SV_SOLUTION_OLD,        /* S of the previous Picard iteration (soluv1_old) */
+  EB_SV_RESNL                /* |L S_old - R| (resnl)                       */
+};
+
+int eb_set_stokes_params(eb_ctx* ctx, const eb_stokes_params* p);
+
+/* StokesViscoelasticTerms.calc_viscoelastic_terms!  (solver/rhs/StokesViscoelasticTerms.jl:26-125) */
+int eb_calc_viscoelastic_terms(eb_ctx* ctx);
+
+/* StokesContinuityRhs.viscoelastic_rhs!  (solver/rhs/StokesContinuityRhs.jl:30-190) */
+int eb_viscoelastic_rhs(eb_ctx* ctx);
+
+/* SystemSolver.initialize_solver! (solver/system_solver/SystemSolver.jl:99-115: vx1, vy1, pr1
+ * zeroed, pscale = 2 etan0[1,1] / (xstpavg + ystpavg)) followed by
+ * StokesBuildManager.build_system_of_equations (solver/build_system/StokesBuildManager.jl:661-712). */
+int eb_build_stokes_system(eb_ctx* ctx);
+
+/* Replaces SystemSolver.solve_system_optimized (SystemSolver.jl:67-91), whose direct
+ * sparse solve (MUMPS, ParallelSolver.jl:52-126, or UMFPACK) becomes FGMRES in FP64,
+ * preconditioned by a block-triangular split: FP32 geometric multigrid on the velocity
+ * block and a viscosity-scaled diagonal on the pressure.  EB_NOT_CONVERGED when the
+ * tolerance is not met in max_iters (S then holds the last iterate), EB_NAN on NaN. */
+int eb_solve_stokes_system(eb_ctx* ctx, const eb_solve_opts* opts, eb_solve_report* report);
+
+/* SystemSolver.process_stokes_solution!  (SystemSolver.jl:141-271: reload_solu_vel!, apply_vel_bc!) */
+int eb_process_stokes_solution(eb_ctx* ctx);
+
+/* StokesResiduals.stokes_calc_nonlinear_system_residual_optimized!  (solver/residuals/StokesResiduals.jl:63-81):
+ * resnl = |L S_old - R|, kept as EB_SV_RESNL. */
+int eb_stokes_nonlinear_residual(eb_ctx* ctx);
+
+/* The solution-vector part of SystemSolver.backup_stokes_arrays!  (SystemSolver.jl:306-318): S_old = S. */
+int eb_backup_stokes_solution(eb_ctx* ctx);
+
+/* No counterpart in the reference (its COO product): y = L x for host vectors of N doubles. */
+int eb_stokes_apply(eb_ctx* ctx, const double* x, double* y);
+
+/* Copies of the N-vectors named by enum eb_stokes_vector (host arrays, interleaved layout). */
+int eb_stokes_vector_upload(eb_ctx* ctx, int which, const double* host);
+int eb_stokes_vector_download(eb_ctx* ctx, int which, double* host);
+
+/* The assembled coefficients: 27 slots x (xnum-1)(ynum-1) cells, slot-major, cells
+ * column-major.  Slots 0-10: x-Stokes row (vx C, L, R, U, D; vy UL, UR, LL, LR; p L, R),
+ * 11-21: y-Stokes row (vy C, U, D, L, R; vx UL, UR, LL, LR; p U, D), 22-26: continuity
+ * row (p C; vx L, R; vy U, D).  Neighbours: L/R = cell column -/+ 1, U/D = row -/+ 1. */
+int eb_stokes_stencil_download(eb_ctx* ctx, double* host);
+
+double  eb_stokes_pscale(const eb_ctx* ctx);  /* pscale of the last eb_build_stokes_system */
+int64_t eb_stokes_size(const eb_ctx* ctx);    /* N = 3 (xnum-1)(ynum-1), 0 before eb_set_grid */
 
 /* ---- allocation-free entry point -------------------------------------------
  * No counterpart in the reference.  For callers that cannot call cudaMalloc

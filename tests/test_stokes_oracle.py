@@ -1,0 +1,131 @@
+"""The Stokes oracle against analytic solutions and the reference's structure (CPU only).
+
+No reference test pins the Stokes assembly or the direct solve (the reference
+has no golden vectors for them), so the oracle is pinned here by solutions
+the discrete equations must reproduce to rounding: a hydrostatic box (v = 0,
+p = pressure_bc + rho g dy) and plane Couette flow (a linear vx profile), plus
+the structural facts of StokesBuildManager's COO list.
+"""
+import numpy as np
+import pytest
+
+from stokes_cases import couette, marker_model, random_box
+
+
+@pytest.fixture(scope="module")
+def S_mod():
+    from oracle.stokes import StokesOracle
+    return StokesOracle
+
+
+def test_hydrostatic_box(eb, S_mod):
+    m = random_box(eb)
+    o = S_mod(m)
+    o.stokes_steps()
+    S = o.solve_direct()
+    assert o.residual(S) < 1e-12
+    o.process_stokes_solution(S)
+    g = m.grid
+    v_scale = 3000.0 * 9.81 * (g.ymax - g.ymin) ** 2 / 1e21  # rho g H^2 / eta
+    assert np.abs(o.gr["vx1"]).max() < 1e-10 * v_scale
+    assert np.abs(o.gr["vy1"]).max() < 1e-10 * v_scale
+    yc = g.gridy_vx[1:g.ynum]
+    pr = 1e5 + 3000.0 * 9.81 * (yc - yc[0])
+    assert np.abs(o.gr["pr1"] - pr[:, None]).max() < 1e-12 * pr.max()
+
+
+def test_couette_flow(eb, S_mod):
+    m = random_box(eb, xnum=19, ynum=23, seed=3)
+    U = 1e-9
+    vex = couette(m, U)
+    o = S_mod(m)
+    o.stokes_steps()
+    S = o.solve_direct()
+    o.process_stokes_solution(S)
+    g = m.grid
+    assert np.abs(o.gr["vx1"] - vex(g.gridy_vx)[:, None]).max() < 1e-12 * U
+    assert np.abs(o.gr["vy1"]).max() < 1e-12 * U
+
+
+def test_coo_structure(eb, S_mod):
+    """Rows, columns and entry counts of StokesBuildManager.build_system_of_equations."""
+    m = random_box(eb, xnum=9, ynum=7)
+    o = S_mod(m)
+    Li, Lj, Lv, R = o.stokes_steps()
+    nx, ny = 8, 6
+    N = 3 * nx * ny
+    assert Li.min() >= 1 and Li.max() <= N and Lj.min() >= 1 and Lj.max() <= N
+    # entries come row by row: cells in row-major (i outer) order, rows vx, vy, p of each cell
+    cell = (Li - 1) // 3
+    j, i = cell // ny, cell % ny
+    key = i * nx + j
+    assert np.all(np.diff(key) >= 0)
+    # every momentum row has a diagonal entry; of the continuity rows (zero pressure block)
+    # only the pressure-condition row of the upper-left cell has one
+    diag = Li == Lj
+    kind_d = (Li[diag] - 1) % 3
+    assert len(np.unique(Li[diag][kind_d < 2])) == 2 * nx * ny
+    assert list(Li[diag][kind_d == 2]) == [3]
+    hs = 3 * ny
+    allowed = {0: {0, -hs, hs, -3, 3, -2, -2 + hs, 1, 1 + hs, 2, 2 + hs},
+               1: {0, -3, 3, -hs, hs, -1 - hs, -1, 2 - hs, 2, 1, 4},
+               2: {0, -2 - hs, -2, -4, -1}}
+    kind = (Li - 1) % 3
+    for k, offs in allowed.items():
+        assert set(np.unique(Lj[kind == k] - Li[kind == k])) <= offs
+    # x-Stokes rows of the last column (vx on the right boundary) and y-Stokes rows of the
+    # last row are identity rows with 2 pscale / (xstpavg + ystpavg)
+    kb = 2.0 * o.pscale / (m.grid.xstpavg + m.grid.ystpavg)
+    xrows = 3 * ((nx - 1) * ny + np.arange(ny)) + 1
+    for r in xrows:
+        sel = Li == r
+        assert sel.sum() == 1 and Lv[sel][0] == kb
+    # pressure_bc_mode 0: the upper-left cell's continuity row fixes the pressure
+    sel = Li == 3
+    assert sel.sum() == 1 and Lv[sel][0] == kb
+    assert R[2] == 2.0 * m.params["pressure_bc"] / (m.grid.xstpavg + m.grid.ystpavg)
+
+
+def test_process_solution_mapping(eb, S_mod):
+    """reload_solu_vel! and apply_vel_bc! on a random solution vector."""
+    m = random_box(eb, xnum=8, ynum=6)
+    o = S_mod(m)
+    o.stokes_steps()
+    rng = np.random.default_rng(5)
+    S = rng.normal(size=o.N)
+    o.process_stokes_solution(S)
+    X, Y = 8, 6
+    ny = Y - 1
+    vx1, vy1, pr1 = o.gr["vx1"], o.gr["vy1"], o.gr["pr1"]
+    for j in range(1, X):
+        for i in range(1, Y):
+            c = (j - 1) * ny + i
+            ivx = 3 * c - 2
+            if j < X - 1 and 1 < i + 1 < Y + 1 and 1 < j + 1 < X:
+                assert vx1[i, j] == S[ivx - 1]
+            if i < Y - 1 and 1 < i + 1 < Y and 1 < j + 1 < X + 1:
+                assert vy1[i, j] == S[ivx]
+            assert pr1[i - 1, j - 1] == S[ivx + 1] * o.pscale
+    G = o.gr
+    # free-slip top for vx (ghost = interior) and zero vy on the top boundary
+    assert np.array_equal(vx1[0, 1:-1], vx1[1, 1:-1])
+    assert np.all(vy1[0, 1:-1] == G["btopy"][1:-1, 0])
+
+
+def test_nonlinear_residual_matches_sparse_product(eb, S_mod):
+    m = marker_model(eb, "rift_small")
+    o = S_mod(m)
+    o.stokes_steps()
+    S_old = np.random.default_rng(2).normal(size=o.N) * 1e-10
+    res = o.nonlinear_residual(S_old)
+    ref = np.abs(o.matrix() @ S_old - o.coo[3])
+    assert np.allclose(res, ref, rtol=1e-12, atol=1e-12 * np.abs(ref).max())
+
+
+def test_direct_solve_of_marker_model(eb, S_mod):
+    """The rift's system (sticky air 1e18 over 1e20-1e24 rock) solves to rounding with SuperLU."""
+    m = marker_model(eb, "rift_small")
+    o = S_mod(m)
+    o.stokes_steps()
+    S = o.solve_direct()
+    assert o.residual(S) < 1e-12
