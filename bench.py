@@ -37,7 +37,7 @@ METRIC = "markers/s (MIC transfer+RK4)"
 UNIT = "markers/s"
 
 # Bytes per marker each kernel must move (reads + writes of marker arrays), and
-# grid bytes per call; the dominant-kernel roofline uses these (see DESIGN.md).
+# grid bytes per call; the dominant-kernel roofline uses these.
 ALGO_BYTES_PER_MARKER = {
     "k_cells<stokes>": 4 + 4 + 8 + 1 + 4 + 8 * 8 + 4 + 4,   # perm, xn, fx/fy, flags, matid, 8 f64, 2 f32
     "k_cells<heat>": 4 + 8 + 1 + 4 + 5 * 8,
@@ -50,8 +50,8 @@ ALGO_BYTES_PER_MARKER = {
 }
 
 # DRAM bytes per marker (dram__bytes_read.sum + dram__bytes_write.sum) from one
-# `ncu --set full` capture of each kernel on the 2.56M-marker rift
-# (profiles/marker_kernels_rift_2p5M.md); reads scale with the marker count,
+# `ncu --set full` capture of each kernel on the 2.56M-marker rift (801x201
+# nodes, 16 markers per cell); reads scale with the marker count,
 # writes that still sit in L2 at that size make these a lower bound.
 NCU_DRAM_BYTES_PER_MARKER = {
     "k_cells<stokes>": 101.2,
@@ -70,6 +70,7 @@ def parse():
     ap.add_argument("--workload", default="rift_40M")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-stokes", action="store_true")
     return ap.parse_args()
 
 
@@ -158,6 +159,59 @@ def cpu_baseline(eb, oracle, steps: int = 2):
     return {"value": model.marknum / dt, "unit": UNIT, "cores": oracle.threads(), "kind": "port",
             "sample": f"{model.marknum} markers (101x801-node strip of the 2001x801 model, same spacing), "
                       f"{steps} marker cycles after one warm-up; {dt:.3f} s per cycle"}
+
+
+STOKES_METRIC = "Stokes s/solve @1e-8 resid"
+STOKES_GRIDS = ("etas1", "etan1", "mus1", "mun1", "sxy1", "sxx1", "rho1", "rho1_vy", "dilatation_grid",
+                "eii_plastic_pressure", "btopx", "bbottomx", "btopy", "bbottomy", "bleftx", "brightx", "blefty",
+                "brighty")
+
+
+def stokes_gpu(mic, reps: int = 2):
+    """The Stokes step on the grids the context holds: build steps, solve to 1e-8, unpack.
+    One warm-up (level set-up, graph capture), then `reps` timed steps (wall clock: the
+    FGMRES loop is host-driven)."""
+    import torch
+
+    def one():
+        mic.calc_viscoelastic_terms()
+        mic.viscoelastic_rhs()
+        mic.build_system_of_equations()
+        rep = mic.solve_system(rtol=1e-8, check=False)
+        mic.process_stokes_solution()
+        return rep
+
+    one()
+    torch.cuda.synchronize()
+    mic.profile_enable(True)
+    t0 = time.perf_counter()
+    reps_out = [one() for _ in range(reps)]
+    torch.cuda.synchronize()
+    dt = (time.perf_counter() - t0) / reps
+    prof = mic.profile()
+    mic.profile_enable(False)
+    return dt, reps_out[-1], prof
+
+
+def stokes_cpu_sample(eb, oracle_mod):
+    """SuperLU (scipy) on the oracle's assembly of the 101x801 strip, standing in for the
+    reference's UMFPACK/MUMPS call; inputs are the oracle's marker averages."""
+    from oracle.stokes import StokesOracle
+    import scipy.sparse.linalg as spla
+    model = eb.synthetic.rift(101, 801, 5, width=25e3)
+    ref = oracle_mod.OracleMIC(model)
+    ref.get_marker_inside_flags()
+    ref.initialize_bilinear_interpolation()
+    ref.interpolate_marker_stokes_parameters_to_grid()
+    so = StokesOracle(model, {k: ref.gr[k] for k in STOKES_GRIDS if k in ref.gr})
+    t0 = time.perf_counter()
+    so.stokes_steps()
+    K = so.matrix().tocsc()
+    S = spla.spsolve(K, so.coo[3])
+    dt = time.perf_counter() - t0
+    return {"value": dt, "unit": "s/solve", "cores": 1, "kind": "port",
+            "sample": f"101x801-node strip, N={so.N} unknowns: oracle assembly + scipy SuperLU "
+                      f"(relative residual {so.residual(S):.1e})"}, model
 
 
 def run_reference(args):
@@ -280,6 +334,38 @@ def main():
         except Exception as exc:  # the baseline is reported, not required
             cpu = {"value": None, "unit": UNIT, "cores": 0, "kind": "port", "sample": f"failed: {exc}"}
 
+    # Stokes step of the same model: the marker cycle left the averaged grids on the device
+    stokes = None
+    if not args.no_stokes:
+        s_dt, s_rep, s_prof = stokes_gpu(mic, reps=2)
+        s_kern = {k: (t / n, n) for k, (t, n) in s_prof.items()}
+        stokes = {"metric": STOKES_METRIC, "value": s_dt, "unit": "s/solve", "higher_is_better": False,
+                  "workload": f"{args.workload}: {model.grid.xnum}x{model.grid.ynum} nodes, "
+                              f"N={3 * (model.grid.xnum - 1) * (model.grid.ynum - 1)} unknowns",
+                  "includes": "viscoelastic terms, RHS, assembly, FGMRES+MG solve, unpacking",
+                  "iterations": s_rep["iterations"], "levels": s_rep["levels"],
+                  "rel_residual": s_rep["rel_residual"], "rel_residual_scaled": s_rep["rel_residual_scaled"],
+                  "status": s_rep["status"], "solve_s": s_rep["seconds"],
+                  "reorthogonalisations": s_rep["reorthogonalisations"],
+                  "kernels_ms": {k: round(v[0] * v[1], 3) for k, v in
+                                 sorted(s_kern.items(), key=lambda kv: -kv[1][0] * kv[1][1])[:12]}}
+        if rank == 0 and world == 1 and not args.no_cpu:
+            try:
+                s_cpu, strip = stokes_cpu_sample(eb, load_oracle())
+                # the GPU on the same strip: marker averages from the GPU scatter, then the Stokes step
+                smic = eb.MarkerInCell(local)
+                smic.load_model(strip)
+                smic.get_marker_inside_flags()
+                smic.initialize_bilinear_interpolation()
+                smic.interpolate_marker_stokes_parameters_to_grid()
+                g_dt, g_rep, _ = stokes_gpu(smic, reps=2)
+                smic.close()
+                stokes["cpu_baseline"] = s_cpu
+                stokes["gpu_same_sample"] = {"value": g_dt, "unit": "s/solve", "iterations": g_rep["iterations"],
+                                             "rel_residual": g_rep["rel_residual"]}
+            except Exception as exc:
+                stokes["cpu_baseline"] = {"value": None, "sample": f"failed: {exc}"}
+
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                 "warmup": max(args.warmup, 3), "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
@@ -288,7 +374,7 @@ def main():
                            "markers_per_cell": 25 if args.workload == "rift_40M" else None,
                            "l2": "inputs larger than L2 (each marker field 320 MB)", "parallelism": "replicas"},
                 "gpu_launches": launches, "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
-                "clocks": clk.summary(),
+                "clocks": clk.summary(), "stokes": stokes,
                 "kernels_ms": {k: round(v[0], 4) for k, v in sorted(kern.items(), key=lambda kv: -kv[1][0] * kv[1][1])},
                 "generate_s": round(t_gen, 2)}
         print(json.dumps(line))

@@ -284,7 +284,8 @@ class MarkerInCell:
         r = _abi.SolveReport()
         rc = self._lib.eb_solve_stokes_system(self._ctx, C.byref(o), C.byref(r))
         rep = {"status": rc, "iterations": r.iterations, "levels": r.levels, "rel_residual": r.rel_residual,
-               "rel_residual_scaled": r.rel_residual_scaled, "seconds": r.seconds}
+               "rel_residual_scaled": r.rel_residual_scaled, "seconds": r.seconds,
+               "reorthogonalisations": r.reorthogonalisations}
         if check:
             self._check(rc)
         return rep
@@ -334,6 +335,22 @@ class MarkerInCell:
         a = np.empty(27 * nx * ny)
         self._check(self._lib.eb_stokes_stencil_download(self._ctx, _ptr(a)))
         return a.reshape(27, nx, ny)
+
+    def update_grid_strain_rate_and_spin(self) -> None:
+        """GridStrainRate.update_grid_strain_rate_and_spin! (GridStrainRate.jl:6-182): exx, exy, eii, esp."""
+        self._call("eb_update_grid_strain_rate_and_spin")
+
+    def forecast_viscoelastic_grid_stress(self) -> None:
+        """GridStress.forecast_viscoelastic_grid_stress! (GridStress.jl:30-126): sxy2, sxx2."""
+        self._call("eb_forecast_viscoelastic_grid_stress")
+
+    def calculate_deviatoric_grid_stress_change(self) -> None:
+        """GridStress.calculate_deviatoric_grid_stress_change! (GridStress.jl:128-134): dsxy, dsxx."""
+        self._call("eb_calculate_deviatoric_grid_stress_change")
+
+    def interpolate_stag_velocity_to_basic_grid(self) -> None:
+        """StokesInterpolate.interpolate_stag_velocity_to_basic_grid! (StokesInterpolate.jl:16-33): vxb, vyb."""
+        self._call("eb_interpolate_stag_velocity_to_basic_grid")
 
     def solve_viscoelastic_stokes_continuity_equations(self, **solve_kw) -> dict:
         """StokesContinuitySolver.solve_viscoelastic_stokes_continuity_equations!

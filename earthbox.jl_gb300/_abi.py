@@ -42,6 +42,8 @@ GRID_FIELDS = [
     "RX1", "RY1", "RC1", "eii_plastic_pressure",
     # velocity BC coefficients
     "btopx", "bbottomx", "btopy", "bbottomy", "bleftx", "brightx", "blefty", "brighty",
+    # post-solve grids
+    "eii", "vxb", "vyb",
 ]
 GRID_ID = {n: i for i, n in enumerate(GRID_FIELDS)}
 
@@ -68,7 +70,9 @@ def grid_shape(name: str, xnum: int, ynum: int) -> tuple[int, int]:
         return (ynum + 1, xnum)
     if name == "RY1":
         return (ynum, xnum + 1)
-    return (ynum - 1, xnum - 1)   # RC1, eii_plastic_pressure
+    if name in ("vxb", "vyb"):
+        return (ynum, xnum)
+    return (ynum - 1, xnum - 1)   # RC1, eii_plastic_pressure, eii
 
 
 class GridDesc(C.Structure):
@@ -113,14 +117,16 @@ class SolveOpts(C.Structure):
 
 class SolveReport(C.Structure):
     _fields_ = [("iterations", C.c_int32), ("levels", C.c_int32), ("rel_residual", C.c_double),
-                ("rel_residual_scaled", C.c_double), ("seconds", C.c_double)]
+                ("rel_residual_scaled", C.c_double), ("seconds", C.c_double), ("reorthogonalisations", C.c_int32)]
 
 
 STOKES_VECTORS = {"solution": 0, "rhs": 1, "solution_old": 2, "resnl": 3}
 
 STOKES_ENTRY_POINTS = [
     "eb_calc_viscoelastic_terms", "eb_viscoelastic_rhs", "eb_build_stokes_system", "eb_process_stokes_solution",
-    "eb_stokes_nonlinear_residual", "eb_backup_stokes_solution",
+    "eb_stokes_nonlinear_residual", "eb_backup_stokes_solution", "eb_update_grid_strain_rate_and_spin",
+    "eb_forecast_viscoelastic_grid_stress", "eb_calculate_deviatoric_grid_stress_change",
+    "eb_interpolate_stag_velocity_to_basic_grid",
 ]
 
 ENTRY_POINTS = [

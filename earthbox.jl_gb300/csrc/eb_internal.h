@@ -128,6 +128,10 @@ int launch_viscoelastic_terms(eb_ctx* c);
 int launch_viscoelastic_rhs(eb_ctx* c);
 int launch_build_stokes_system(eb_ctx* c, StokesSystem* s);
 int launch_process_stokes_solution(eb_ctx* c, const StokesSystem* s);
+int launch_grid_strain_rate(eb_ctx* c);
+int launch_forecast_stress(eb_ctx* c);
+int launch_stress_change(eb_ctx* c);
+int launch_stag_to_basic(eb_ctx* c);
 
 constexpr int kMaxSlots = 48;
 

@@ -46,11 +46,30 @@ __device__ __forceinline__ MW marker_weights(const DevGrid& g, int32_t ix, float
   return w;
 }
 
-// exclusive-quadrant membership from the exact flags
-__device__ __forceinline__ bool in_quadrant(uint8_t fl, int q) {
+// Bit q set when the marker belongs to exclusive quadrant q (UL, LL, UR, LR).
+// A marker exactly on a half line belongs to two (or four) quadrants.
+__device__ __forceinline__ uint32_t quadrant_mask(uint8_t fl) {
   const bool xl = fl & MF_XLE, xg = fl & MF_XGE, yl = fl & MF_YLE, yg = fl & MF_YGE;
-  return q == C_UL ? (xl && yl) : (q == C_LL ? (xl && yg) : (q == C_UR ? (xg && yl) : (xg && yg)));
+  return (xl && yl ? 1u : 0u) | (xl && yg ? 2u : 0u) | (xg && yl ? 4u : 0u) | (xg && yg ? 8u : 0u);
 }
+
+// Compensated accumulators in shared memory, indexed per lane: the (s, c) pair
+// of slot k of lane j sits at a[2k*32 + j] and a[(2k+1)*32 + j], so the 32
+// lanes of a warp use 32 different banks whichever slot each lane picks (a
+// lane's slot can depend on its marker, e.g. on the marker's quadrant).
+struct SAcc {
+  float* a;
+  __device__ __forceinline__ void add(int k, int lane, float v) const {
+    float* ps = a + 2 * k * 32 + lane;
+    const float s = ps[0];
+    const float t = s + v;
+    const float e = (fabsf(s) >= fabsf(v)) ? ((s - t) + v) : ((v - t) + s);
+    ps[32] += e;
+    ps[0] = t;
+  }
+  __device__ __forceinline__ float get(int k, int lane) const { return a[2 * k * 32 + lane] + a[(2 * k + 1) * 32 + lane]; }
+};
+constexpr int kSAccPerSlot = 64;  // floats per accumulator slot (s and c for 32 lanes)
 
 // ---------------------------------------------------------------- staging ---
 // Stage layout indices (rows of the shared-memory table).
@@ -65,16 +84,19 @@ __device__ __forceinline__ void stage_weights(float (*sv)[kChunk], int t, const 
 
 // ------------------------------------------------------------------ specs ---
 // Each spec defines: kRoles (folding warps, <= 8), kNV (staged rows), kAcc
-// (accumulators per folding thread), a Raw record of the marker fields it
-// reads, load() (the global loads only, issued one pass ahead), put()
-// (arithmetic on a loaded Raw, marker write-backs, staging), accum() and
-// store().
+// (register accumulators per folding thread), kSmem (shared-memory accumulator
+// slots, SAcc), a Raw record of the marker fields it reads, load() (the global
+// loads only, issued one pass ahead), put() (arithmetic on a loaded Raw, marker
+// write-backs, staging), accum() and store().  Every accumulator receives its
+// cell's markers in slot (marker) order.
 
 // Denominators: wtnodes (incl), wtetas (excl), wtetan (central), wtnodes_vy.
 // slots: 0-3 incl corners, 4-7 excl quadrants, 8 central, 9-16 vy half*4+corner
 struct DenomSpec {
   static constexpr const char* kName = "k_cells<denominators>";
-  static constexpr int kRoles = 4, kNV = S_V0, kAcc = 8;
+  // roles: 0 inclusive corners (registers), 1 exclusive quadrants (shared, slot q),
+  //        2 central node (registers), 3 vy corners (shared, slot 4 + half*4 + corner)
+  static constexpr int kRoles = 4, kNV = S_V0, kAcc = 4, kSmem = 12;
   struct Raw { int32_t xn; float fx, fy; uint8_t fl; };
   __device__ Raw load(const DevMarkers& mk, int32_t m) const {
     return Raw{mk.xn[m], mk.fx[m], mk.fy[m], mk.mflags[m]};
@@ -83,24 +105,26 @@ struct DenomSpec {
     stage_weights(sv, t, marker_weights(g, r.xn, r.fx, r.fy, r.fl));
     sfl[t] = r.fl;
   }
-  __device__ void accum(int role, int t, float (*sv)[kChunk], const uint8_t* sfl, KSum* a) const {
+  __device__ void accum(int role, int lane, int t, float (*sv)[kChunk], const uint8_t* sfl, KSum* a, SAcc sa) const {
     if (role == 0) {
       for (int k = 0; k < 4; ++k) a[k].add(sv[S_UL + k][t]);
     } else if (role == 1) {
-      const uint8_t fl = sfl[t];
-      for (int q = 0; q < 4; ++q) if (in_quadrant(fl, q)) a[q].add(sv[S_UL + q][t]);
+      for (uint32_t m = quadrant_mask(sfl[t]); m; m &= m - 1) {
+        const int q = __ffs(m) - 1;
+        sa.add(q, lane, sv[S_UL + q][t]);
+      }
     } else if (role == 2) {
       a[0].add(sv[S_WC][t]);
     } else {
       const int h = (int)sv[S_HALF][t];
-      for (int k = 0; k < 4; ++k) a[h * 4 + k].add(sv[S_VUL + k][t]);
+      for (int k = 0; k < 4; ++k) sa.add(4 + h * 4 + k, lane, sv[S_VUL + k][t]);
     }
   }
-  __device__ void store(int role, int32_t cell, int32_t nc, const KSum* a, float* part) const {
+  __device__ void store(int role, int lane, int32_t cell, int32_t nc, const KSum* a, SAcc sa, float* part) const {
     if (role == 0) for (int k = 0; k < 4; ++k) part[(size_t)k * nc + cell] = a[k].get();
-    else if (role == 1) for (int q = 0; q < 4; ++q) part[(size_t)(4 + q) * nc + cell] = a[q].get();
+    else if (role == 1) for (int q = 0; q < 4; ++q) part[(size_t)(4 + q) * nc + cell] = sa.get(q, lane);
     else if (role == 2) part[(size_t)8 * nc + cell] = a[0].get();
-    else for (int k = 0; k < 8; ++k) part[(size_t)(9 + k) * nc + cell] = a[k].get();
+    else for (int k = 0; k < 8; ++k) part[(size_t)(9 + k) * nc + cell] = sa.get(4 + k, lane);
   }
 };
 
@@ -111,7 +135,9 @@ enum { V_RHO = S_V0, V_COH, V_FRIC, V_ETAF, V_ETA, V_MUI, V_SXY, V_PLAST, V_DIL,
 //        32-37 central (eta, mu_inv, plast, dil, melt, sxx); 38-45 vy rho half*4+corner
 struct StokesSpec {
   static constexpr const char* kName = "k_cells<stokes>";
-  static constexpr int kRoles = 7, kNV = V_END, kAcc = 8;
+  // roles: 0 inclusive rho (registers), 1 exclusive quadrants (shared, slot 7q + f),
+  //        2 central node (registers), 3 vy rho (shared, slot 28 + half*4 + corner)
+  static constexpr int kRoles = 4, kNV = V_END, kAcc = 6, kSmem = 36;
   const double* mat_mu;
   int32_t* dflag;
   struct Raw {
@@ -145,22 +171,23 @@ struct StokesSpec {
     sv[V_MELT][t] = d2f(r.melt);
     sv[V_SXX][t] = d2f(r.sxx);
   }
-  __device__ void accum(int role, int t, float (*sv)[kChunk], const uint8_t* sfl, KSum* a) const {
+  __device__ void accum(int role, int lane, int t, float (*sv)[kChunk], const uint8_t* sfl, KSum* a, SAcc sa) const {
     if (role == 0) {
       const float r = sv[V_RHO][t];
       for (int k = 0; k < 4; ++k) a[k].add(sv[S_UL + k][t] * r);
-    } else if (role <= 4) {
-      const int q = role - 1;
-      if (!in_quadrant(sfl[t], q)) return;
-      const float w = sv[S_UL + q][t];
-      a[0].add(w * sv[V_COH][t]);
-      a[1].add(w * sv[V_FRIC][t]);
-      a[2].add(w * sv[V_ETAF][t]);
-      a[3].add(w * sv[V_ETA][t]);
-      a[4].add(w * sv[V_MUI][t]);
-      a[5].add(w * sv[V_SXY][t]);
-      a[6].add(w * sv[V_PLAST][t]);
-    } else if (role == 5) {
+    } else if (role == 1) {
+      for (uint32_t m = quadrant_mask(sfl[t]); m; m &= m - 1) {
+        const int q = __ffs(m) - 1;
+        const float w = sv[S_UL + q][t];
+        sa.add(7 * q + 0, lane, w * sv[V_COH][t]);
+        sa.add(7 * q + 1, lane, w * sv[V_FRIC][t]);
+        sa.add(7 * q + 2, lane, w * sv[V_ETAF][t]);
+        sa.add(7 * q + 3, lane, w * sv[V_ETA][t]);
+        sa.add(7 * q + 4, lane, w * sv[V_MUI][t]);
+        sa.add(7 * q + 5, lane, w * sv[V_SXY][t]);
+        sa.add(7 * q + 6, lane, w * sv[V_PLAST][t]);
+      }
+    } else if (role == 2) {
       const float w = sv[S_WC][t];
       a[0].add(w * sv[V_ETA][t]);
       a[1].add(w * sv[V_MUI][t]);
@@ -171,21 +198,21 @@ struct StokesSpec {
     } else {
       const int h = (int)sv[S_HALF][t];
       const float r = sv[V_RHO][t];
-      for (int k = 0; k < 4; ++k) a[h * 4 + k].add(sv[S_VUL + k][t] * r);
+      for (int k = 0; k < 4; ++k) sa.add(28 + h * 4 + k, lane, sv[S_VUL + k][t] * r);
     }
   }
-  __device__ void store(int role, int32_t cell, int32_t nc, const KSum* a, float* part) const {
+  __device__ void store(int role, int lane, int32_t cell, int32_t nc, const KSum* a, SAcc sa, float* part) const {
     if (role == 0) for (int k = 0; k < 4; ++k) part[(size_t)k * nc + cell] = a[k].get();
-    else if (role <= 4) for (int f = 0; f < 7; ++f) part[(size_t)(4 + 7 * (role - 1) + f) * nc + cell] = a[f].get();
-    else if (role == 5) for (int f = 0; f < 6; ++f) part[(size_t)(32 + f) * nc + cell] = a[f].get();
-    else for (int k = 0; k < 8; ++k) part[(size_t)(38 + k) * nc + cell] = a[k].get();
+    else if (role == 1) for (int k = 0; k < 28; ++k) part[(size_t)(4 + k) * nc + cell] = sa.get(k, lane);
+    else if (role == 2) for (int f = 0; f < 6; ++f) part[(size_t)(32 + f) * nc + cell] = a[f].get();
+    else for (int k = 0; k < 8; ++k) part[(size_t)(38 + k) * nc + cell] = sa.get(28 + k, lane);
   }
 };
 
 // Heat numerators (BilinearNumerator.jl:31-141): tk, kt, rhocp, hr(+serp), ha; slots 5*corner + f
 struct HeatSpec {
   static constexpr const char* kName = "k_cells<heat>";
-  static constexpr int kRoles = 4, kNV = S_V0 + 5, kAcc = 5;
+  static constexpr int kRoles = 4, kNV = S_V0 + 5, kAcc = 5, kSmem = 0;
   const double* mat_hr;
   int use_serp;
   struct Raw { double tk, kt, rhocp, ha, serp; float fx, fy; int32_t mt; };
@@ -207,20 +234,20 @@ struct HeatSpec {
     sv[S_V0 + 3][t] = d2f(hr);
     sv[S_V0 + 4][t] = d2f(r.ha);
   }
-  __device__ void accum(int role, int t, float (*sv)[kChunk], const uint8_t*, KSum* a) const {
+  __device__ void accum(int role, int, int t, float (*sv)[kChunk], const uint8_t*, KSum* a, SAcc) const {
     const float w = sv[S_UL + role][t];
     for (int f = 0; f < 5; ++f) a[f].add(w * sv[S_V0 + f][t]);
   }
-  __device__ void store(int role, int32_t cell, int32_t nc, const KSum* a, float* part) const {
+  __device__ void store(int role, int, int32_t cell, int32_t nc, const KSum* a, SAcc, float* part) const {
     for (int f = 0; f < 5; ++f) part[(size_t)(5 * role + f) * nc + cell] = a[f].get();
   }
 };
 
 // Viscosity re-scatter (BilinearNumerator.jl:470-533): slots 0-3 excl eta, 4 central eta
-// roles 0-3: one exclusive quadrant each; role 4: the central node
+// roles: 0 exclusive quadrants (shared, slot q), 1 central node (registers)
 struct ViscSpec {
   static constexpr const char* kName = "k_cells<viscosity>";
-  static constexpr int kRoles = 5, kNV = S_V0 + 1, kAcc = 1;
+  static constexpr int kRoles = 2, kNV = S_V0 + 1, kAcc = 1, kSmem = 4;
   struct Raw { double eta; float fx, fy; uint8_t fl; };
   __device__ Raw load(const DevMarkers& mk, int32_t m) const {
     return Raw{mk.eta[m], mk.fx[m], mk.fy[m], mk.mflags[m]};
@@ -232,16 +259,20 @@ struct ViscSpec {
     sfl[t] = r.fl;
     sv[S_V0][t] = d2f(r.eta);
   }
-  __device__ void accum(int role, int t, float (*sv)[kChunk], const uint8_t* sfl, KSum* a) const {
+  __device__ void accum(int role, int lane, int t, float (*sv)[kChunk], const uint8_t* sfl, KSum* a, SAcc sa) const {
     const float e = sv[S_V0][t];
-    if (role < 4) {
-      if (in_quadrant(sfl[t], role)) a[0].add(sv[S_UL + role][t] * e);
+    if (role == 0) {
+      for (uint32_t m = quadrant_mask(sfl[t]); m; m &= m - 1) {
+        const int q = __ffs(m) - 1;
+        sa.add(q, lane, sv[S_UL + q][t] * e);
+      }
     } else {
       a[0].add(sv[S_WC][t] * e);
     }
   }
-  __device__ void store(int role, int32_t cell, int32_t nc, const KSum* a, float* part) const {
-    part[(size_t)role * nc + cell] = a[0].get();
+  __device__ void store(int role, int lane, int32_t cell, int32_t nc, const KSum* a, SAcc sa, float* part) const {
+    if (role == 0) for (int q = 0; q < 4; ++q) part[(size_t)q * nc + cell] = sa.get(q, lane);
+    else part[(size_t)4 * nc + cell] = a[0].get();
   }
 };
 
@@ -267,10 +298,10 @@ __device__ __forceinline__ float gather_pressure_grid(const float* __restrict__ 
 // Subgrid stress (SubgridShearStress.jl:27-96, SubgridNormalStress.jl:27-89):
 // put() relaxes the marker stress, writes it back and stages the relaxed change.
 // slots: 0-3 excl relax_xy*w, 4-7 excl w, 8 central relax_xx*wc, 9 central wc
-// roles 0-3: one exclusive quadrant each (relax_xy*w, w); role 4: the central node
+// roles: 0 exclusive quadrants (shared, slots q: relax_xy*w, 4+q: w), 1 central node (registers)
 struct SubgridStressSpec {
   static constexpr const char* kName = "k_cells<subgrid_stress>";
-  static constexpr int kRoles = 5, kNV = S_V0 + 2, kAcc = 2;
+  static constexpr int kRoles = 2, kNV = S_V0 + 2, kAcc = 2, kSmem = 8;
   const float *sxy1, *sxx1;  // FP32 mirrors
   const double* mat_mu;
   float dt, coef;
@@ -300,12 +331,14 @@ struct SubgridStressSpec {
     sv[S_V0][t] = rxy;
     sv[S_V0 + 1][t] = rxx;
   }
-  __device__ void accum(int role, int t, float (*sv)[kChunk], const uint8_t* sfl, KSum* a) const {
-    if (role < 4) {
-      if (in_quadrant(sfl[t], role)) {
-        const float w = sv[S_UL + role][t];
-        a[0].add(w * sv[S_V0][t]);
-        a[1].add(w);
+  __device__ void accum(int role, int lane, int t, float (*sv)[kChunk], const uint8_t* sfl, KSum* a, SAcc sa) const {
+    if (role == 0) {
+      const float r = sv[S_V0][t];
+      for (uint32_t m = quadrant_mask(sfl[t]); m; m &= m - 1) {
+        const int q = __ffs(m) - 1;
+        const float w = sv[S_UL + q][t];
+        sa.add(q, lane, w * r);
+        sa.add(4 + q, lane, w);
       }
     } else {
       const float w = sv[S_WC][t];
@@ -313,10 +346,9 @@ struct SubgridStressSpec {
       a[1].add(w);
     }
   }
-  __device__ void store(int role, int32_t cell, int32_t nc, const KSum* a, float* part) const {
-    if (role < 4) {
-      part[(size_t)role * nc + cell] = a[0].get();
-      part[(size_t)(4 + role) * nc + cell] = a[1].get();
+  __device__ void store(int role, int lane, int32_t cell, int32_t nc, const KSum* a, SAcc sa, float* part) const {
+    if (role == 0) {
+      for (int k = 0; k < 8; ++k) part[(size_t)k * nc + cell] = sa.get(k, lane);
     } else {
       part[(size_t)8 * nc + cell] = a[0].get();
       part[(size_t)9 * nc + cell] = a[1].get();
@@ -328,7 +360,7 @@ struct SubgridStressSpec {
 // roles 0-3: one corner each
 struct SubgridHeatSpec {
   static constexpr const char* kName = "k_cells<subgrid_heat>";
-  static constexpr int kRoles = 4, kNV = S_V0 + 1, kAcc = 2;
+  static constexpr int kRoles = 4, kNV = S_V0 + 1, kAcc = 2, kSmem = 0;
   const float *tk1, *kt1, *rhocp1;  // FP32 mirrors
   float dt, coef, inv_ts;  // inv_ts = 2/xstpavg^2 + 2/ystpavg^2
   struct Raw { double tk; int32_t m, xn, yn; float fx, fy; };
@@ -348,12 +380,12 @@ struct SubgridHeatSpec {
     mk.tk[r.m] = r.tk + f2d(d);
     sv[S_V0][t] = d;
   }
-  __device__ void accum(int role, int t, float (*sv)[kChunk], const uint8_t*, KSum* a) const {
+  __device__ void accum(int role, int, int t, float (*sv)[kChunk], const uint8_t*, KSum* a, SAcc) const {
     const float w = sv[S_UL + role][t];
     a[0].add(w * sv[S_V0][t]);
     a[1].add(w);
   }
-  __device__ void store(int role, int32_t cell, int32_t nc, const KSum* a, float* part) const {
+  __device__ void store(int role, int, int32_t cell, int32_t nc, const KSum* a, SAcc, float* part) const {
     part[(size_t)role * nc + cell] = a[0].get();
     part[(size_t)(4 + role) * nc + cell] = a[1].get();
   }
@@ -383,6 +415,9 @@ __global__ void __launch_bounds__(kThreads) k_cells(S spec, DevMarkers mk, DevGr
   __shared__ float sv[S::kNV][kChunk];
   __shared__ uint8_t sfl[kChunk];
   __shared__ int32_t s_beg[32], s_cnt[32], s_max;
+  __shared__ float s_acc[S::kSmem > 0 ? S::kSmem * kSAccPerSlot : 1];
+  for (int k = threadIdx.x; k < S::kSmem * kSAccPerSlot; k += blockDim.x) s_acc[k] = 0.f;
+  const SAcc sa{s_acc};
   const int lane = threadIdx.x & 31, role = threadIdx.x >> 5;
   const int sj = threadIdx.x >> 3, si = threadIdx.x & 7;  // staging cell / marker of this thread
   const int32_t c0 = blockIdx.x * 32;
@@ -415,10 +450,10 @@ __global__ void __launch_bounds__(kThreads) k_cells(S spec, DevMarkers mk, DevGr
     if (have) r = spec.load(mk, __ldg(&perm[st_beg + nxt]));
     if (role < S::kRoles) {
       const int n = min(kPer, my_cnt - base);
-      for (int i = 0; i < n; ++i) spec.accum(role, lane * kSlotStride + i, sv, sfl, acc);
+      for (int i = 0; i < n; ++i) spec.accum(role, lane, lane * kSlotStride + i, sv, sfl, acc, sa);
     }
   }
-  if (role < S::kRoles && c0 + lane < nc) spec.store(role, c0 + lane, nc, acc, part);
+  if (role < S::kRoles && c0 + lane < nc) spec.store(role, lane, c0 + lane, nc, acc, sa, part);
 }
 
 template <class S>

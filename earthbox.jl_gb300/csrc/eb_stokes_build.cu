@@ -367,9 +367,114 @@ __global__ void k_bc_left_right_vy(double* vy1, const double* blefty, const doub
   A2(vy1, ynum, i, xnum + 1) = A2(brighty, ynum, i, 1) + A2(brighty, ynum, i, 2) * A2(vy1, ynum, i, xnum);
 }
 
+// ---- post-solve grid kernels ---------------------------------------------
+// GridStrainRate.jl:21-182: exx (pressure grid), exy and esp (basic grid); one thread per basic node.
+__global__ void k_grid_strain_rate(int32_t xnum, int32_t ynum, const double* __restrict__ xstp_b,
+                                   const double* __restrict__ ystp_b, const double* __restrict__ xstp_vy,
+                                   const double* __restrict__ ystp_vx, const double* __restrict__ vx1,
+                                   const double* __restrict__ vy1, double* __restrict__ exx, double* __restrict__ exy,
+                                   double* __restrict__ esp) {
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= (int64_t)xnum * ynum) return;
+  const int32_t i = (int32_t)(k % ynum) + 1, j = (int32_t)(k / ynum) + 1;
+  const int32_t yx = ynum + 1;
+  if (i < ynum && j < xnum)
+    A2(exx, ynum - 1, i, j) = 0.5 * ((A2(vx1, yx, i + 1, j + 1) - A2(vx1, yx, i + 1, j)) / xstp_b[j - 1] -
+                                     (A2(vy1, ynum, i + 1, j + 1) - A2(vy1, ynum, i, j + 1)) / ystp_b[i - 1]);
+  const double dvx = (A2(vx1, yx, i + 1, j) - A2(vx1, yx, i, j)) / ystp_vx[i - 1];
+  const double dvy = (A2(vy1, ynum, i, j + 1) - A2(vy1, ynum, i, j)) / xstp_vy[j - 1];
+  A2(exy, ynum, i, j) = 0.5 * (dvx + dvy);
+  A2(esp, ynum, i, j) = 0.5 * (dvy - dvx);
+}
+// GridStrainRate.calculate_second_invariant! (:107-131); x^2.0 is x*x in Julia
+__global__ void k_grid_eii(int32_t xnum, int32_t ynum, const double* __restrict__ exx, const double* __restrict__ exy,
+                           double* __restrict__ eii) {
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= (int64_t)(xnum - 1) * (ynum - 1)) return;
+  const int32_t i = (int32_t)(k % (ynum - 1)) + 2, j = (int32_t)(k / (ynum - 1)) + 2;
+  const double e = A2(exx, ynum - 1, i - 1, j - 1);
+  const double a = A2(exy, ynum, i - 1, j - 1), b = A2(exy, ynum, i, j - 1);
+  const double c = A2(exy, ynum, i - 1, j), d = A2(exy, ynum, i, j);
+  A2(eii, ynum - 1, i - 1, j - 1) = sqrt(e * e + (a * a + b * b + c * c + d * d) / 4.0);
+}
+// GridStress.forecast_viscoelastic_{shear,normal}_stress! (:54-126)
+__global__ void k_forecast_stress(const double* __restrict__ eta1, const double* __restrict__ mu1,
+                                  const double* __restrict__ e, const double* __restrict__ s1,
+                                  double* __restrict__ s2, int64_t n, double dt) {
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  const double eta = eta1[k];
+  const double f = eta / (eta + dt * mu1[k]);
+  s2[k] = (1.0 - f) * 2.0 * eta * e[k] + f * s1[k];
+}
+// GridStress.calculate_deviatoric_grid_stress_change! (:128-134)
+__global__ void k_stress_change(const double* __restrict__ s2, const double* __restrict__ s1, double* __restrict__ ds,
+                                int64_t n) {
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < n) ds[k] = s2[k] - s1[k];
+}
+// StokesInterpolate.interpolate_stag_velocity_to_basic_grid! (:16-33)
+__global__ void k_stag_to_basic(int32_t xnum, int32_t ynum, const double* __restrict__ vx1,
+                                const double* __restrict__ vy1, double* __restrict__ vxb, double* __restrict__ vyb) {
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= (int64_t)xnum * ynum) return;
+  const int32_t i = (int32_t)(k % ynum) + 1, j = (int32_t)(k / ynum) + 1;
+  A2(vxb, ynum, i, j) = (A2(vx1, ynum + 1, i, j) + A2(vx1, ynum + 1, i + 1, j)) / 2.0;
+  A2(vyb, ynum, i, j) = (A2(vy1, ynum, i, j) + A2(vy1, ynum, i, j + 1)) / 2.0;
+}
+
 unsigned nblk(int64_t n) { return (unsigned)((n + kB - 1) / kB); }
 
 }  // namespace
+
+int launch_grid_strain_rate(eb_ctx* c) {
+  double** g = c->gf;
+  const int32_t X = c->xnum, Y = c->ynum;
+  EB_PROF(c, "k_grid_strain_rate");
+  k_grid_strain_rate<<<nblk((int64_t)X * Y), kB, 0, c->stream>>>(X, Y, c->g.sx, c->g.sy, c->g_xstp_vy, c->g_ystp_vx,
+                                                                  g[EB_G_VX1], g[EB_G_VY1], g[EB_G_EXX], g[EB_G_EXY],
+                                                                  g[EB_G_ESP]);
+  EB_LAUNCHED(c);
+  EB_PROF(c, "k_grid_eii");
+  k_grid_eii<<<nblk((int64_t)(X - 1) * (Y - 1)), kB, 0, c->stream>>>(X, Y, g[EB_G_EXX], g[EB_G_EXY], g[EB_G_EII]);
+  EB_LAUNCHED(c);
+  return EB_OK;
+}
+
+int launch_forecast_stress(eb_ctx* c) {
+  double** g = c->gf;
+  const int64_t nb = (int64_t)c->xnum * c->ynum, np = (int64_t)(c->xnum - 1) * (c->ynum - 1);
+  EB_PROF(c, "k_forecast_stress");
+  k_forecast_stress<<<nblk(nb), kB, 0, c->stream>>>(g[EB_G_ETAS1], g[EB_G_MUS1], g[EB_G_EXY], g[EB_G_SXY1], g[EB_G_SXY2],
+                                                    nb, c->P.timestep);
+  EB_LAUNCHED(c);
+  EB_PROF(c, "k_forecast_stress");
+  k_forecast_stress<<<nblk(np), kB, 0, c->stream>>>(g[EB_G_ETAN1], g[EB_G_MUN1], g[EB_G_EXX], g[EB_G_SXX1], g[EB_G_SXX2],
+                                                    np, c->P.timestep);
+  EB_LAUNCHED(c);
+  return EB_OK;
+}
+
+int launch_stress_change(eb_ctx* c) {
+  double** g = c->gf;
+  const int64_t nb = (int64_t)c->xnum * c->ynum, np = (int64_t)(c->xnum - 1) * (c->ynum - 1);
+  EB_PROF(c, "k_stress_change");
+  k_stress_change<<<nblk(nb), kB, 0, c->stream>>>(g[EB_G_SXY2], g[EB_G_SXY1], g[EB_G_DSXY], nb);
+  EB_LAUNCHED(c);
+  EB_PROF(c, "k_stress_change");
+  k_stress_change<<<nblk(np), kB, 0, c->stream>>>(g[EB_G_SXX2], g[EB_G_SXX1], g[EB_G_DSXX], np);
+  EB_LAUNCHED(c);
+  return EB_OK;
+}
+
+int launch_stag_to_basic(eb_ctx* c) {
+  double** g = c->gf;
+  EB_PROF(c, "k_stag_to_basic");
+  k_stag_to_basic<<<nblk((int64_t)c->xnum * c->ynum), kB, 0, c->stream>>>(c->xnum, c->ynum, g[EB_G_VX1], g[EB_G_VY1],
+                                                                          g[EB_G_VXB], g[EB_G_VYB]);
+  EB_LAUNCHED(c);
+  return EB_OK;
+}
 
 int launch_viscoelastic_terms(eb_ctx* c) {
   double** g = c->gf;

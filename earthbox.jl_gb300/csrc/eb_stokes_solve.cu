@@ -29,6 +29,11 @@ namespace {
 
 constexpr int kB = 256;
 constexpr int kRmax = 8;  // restriction entries per coarse index and axis
+constexpr int kMaxRestart = 500;
+// Classical Gram-Schmidt re-orthogonalises a new direction only when the projection
+// removed all but 5% of its norm (squared ratio below).
+constexpr double kReorth2 = 0.05 * 0.05;
+constexpr int kMaxDots = kMaxRestart + 8;  // dot products per reduction
 
 unsigned nblk(int64_t n) { return (unsigned)((n + kB - 1) / kB); }
 
@@ -98,22 +103,25 @@ __global__ void k_scaling(const double* __restrict__ coef, const double* __restr
 }
 
 // ------------------------------------------------------ FGMRES helpers ---
-// partial[v * nb + b] = sum over block b's chunk of V_v . u
-__global__ void k_mdot(const double* __restrict__ V, int64_t stride, const double* __restrict__ u, int64_t n,
-                       double* __restrict__ partial) {
-  const int v = blockIdx.y;
-  const double* a = V + (int64_t)v * stride;
+// Dot products with the Krylov basis V (nv vectors of n, `stride` apart):
+// block (b, v) reduces a grid-stride slice of V_v . u, so the blocks of one
+// vector run together and stream it (u stays in L2 across vectors).
+constexpr int kDotBlocks = 2 * 152;
+__global__ void __launch_bounds__(kB) k_mdot(const double* __restrict__ V, int64_t stride, const double* __restrict__ u,
+                                             int64_t n, double* __restrict__ partial) {
+  const double* a = V + (int64_t)blockIdx.y * stride;
   double s = 0.0;
   for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x)
     s += a[k] * u[k];
-  __shared__ double sh[kB];
-  sh[threadIdx.x] = s;
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  __shared__ double sh[kB / 32];
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = s;
   __syncthreads();
-  for (int o = kB / 2; o > 0; o >>= 1) {
-    if ((int)threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
-    __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < kB / 32; ++w) t += sh[w];
+    partial[(int64_t)blockIdx.y * gridDim.x + blockIdx.x] = t;
   }
-  if (threadIdx.x == 0) partial[(int64_t)v * gridDim.x + blockIdx.x] = sh[0];
 }
 __global__ void k_mdot_final(const double* __restrict__ partial, int nb, double* __restrict__ out) {
   const int v = blockIdx.x;
@@ -128,19 +136,74 @@ __global__ void k_mdot_final(const double* __restrict__ partial, int nb, double*
   }
   if (threadIdx.x == 0) out[v] = sh[0];
 }
-// u -= sum_v h[v] V_v
-__global__ void k_maxpy(double* __restrict__ u, const double* __restrict__ V, int64_t stride, const double* __restrict__ h,
-                        int nv, int64_t n) {
-  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= n) return;
-  double s = u[k];
-  for (int v = 0; v < nv; ++v) s -= h[v] * V[(int64_t)v * stride + k];
-  u[k] = s;
+// u -= sum_v h[v] V_v.  Each thread owns kAxPer elements and streams four
+// basis vectors at a time (16 independent loads in flight).
+constexpr int kAxThreads = 256, kAxPer = 4, kAxTile = kAxThreads * kAxPer;
+__global__ void __launch_bounds__(kAxThreads) k_maxpy(double* __restrict__ u, const double* __restrict__ V,
+                                                      int64_t stride, const double* __restrict__ h, int nv,
+                                                      int64_t n) {
+  extern __shared__ double hs[];
+  for (int v = threadIdx.x; v < nv; v += blockDim.x) hs[v] = h[v];
+  __syncthreads();
+  const int64_t base = (int64_t)blockIdx.x * kAxTile;
+  const bool full = base + kAxTile <= n;
+  double ur[kAxPer];
+#pragma unroll
+  for (int q = 0; q < kAxPer; ++q) {
+    const int64_t e = base + q * kAxThreads + threadIdx.x;
+    ur[q] = (full || e < n) ? u[e] : 0.0;
+  }
+  if (full) {
+    int v = 0;
+    for (; v + 4 <= nv; v += 4) {
+      double x[4][kAxPer];
+#pragma unroll
+      for (int g = 0; g < 4; ++g)
+#pragma unroll
+        for (int q = 0; q < kAxPer; ++q) x[g][q] = __ldcs(V + (int64_t)(v + g) * stride + base + q * kAxThreads + threadIdx.x);
+#pragma unroll
+      for (int g = 0; g < 4; ++g)
+#pragma unroll
+        for (int q = 0; q < kAxPer; ++q) ur[q] -= hs[v + g] * x[g][q];
+    }
+    for (; v < nv; ++v)
+#pragma unroll
+      for (int q = 0; q < kAxPer; ++q) ur[q] -= hs[v] * V[(int64_t)v * stride + base + q * kAxThreads + threadIdx.x];
+  } else {
+    for (int v = 0; v < nv; ++v)
+#pragma unroll
+      for (int q = 0; q < kAxPer; ++q) {
+        const int64_t e = base + q * kAxThreads + threadIdx.x;
+        if (e < n) ur[q] -= hs[v] * V[(int64_t)v * stride + e];
+      }
+  }
+#pragma unroll
+  for (int q = 0; q < kAxPer; ++q) {
+    const int64_t e = base + q * kAxThreads + threadIdx.x;
+    if (full || e < n) u[e] = ur[q];
+  }
 }
 // dst may alias src (in-place scaling)
 __global__ void k_scale_copy(double* dst, const double* src, double a, int64_t n) {
   const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (k < n) dst[k] = a * src[k];
+}
+// Zk = (float) z and z = (double) Zk: the direction is kept exactly as stored
+__global__ void k_round_dir(double* __restrict__ z, float* __restrict__ Zk, int64_t n) {
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  const float f = (float)z[k];
+  Zk[k] = f;
+  z[k] = (double)f;
+}
+// u -= sum_v h[v] Z_v (FP32 directions)
+__global__ void k_maxpy_f32(double* __restrict__ u, const float* __restrict__ Z, int64_t stride,
+                            const double* __restrict__ h, int nv, int64_t n) {
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  double s = u[k];
+  for (int v = 0; v < nv; ++v) s -= h[v] * (double)Z[(int64_t)v * stride + k];
+  u[k] = s;
 }
 // dst = a - b (elementwise)
 __global__ void k_sub(double* __restrict__ dst, const double* __restrict__ a, const double* __restrict__ b, int64_t n) {
@@ -319,93 +382,142 @@ __device__ __forceinline__ float rowy(const float* __restrict__ Y, const float* 
   return a;
 }
 
-// Red-black Gauss-Seidel half sweep: comp 0 updates vx, 1 updates vy, on cells with (i + j) % 2 == color.
-__global__ void k_rbgs(const float* __restrict__ X, const float* __restrict__ Y, float* ux, float* uy,
-                       const float* __restrict__ fx, const float* __restrict__ fy, int32_t nx, int32_t ny, int comp,
-                       int color) {
-  const int64_t nc = (int64_t)nx * ny;
-  // column j holds the rows i = 2q + ((j + color) & 1) of this color, q < ceil(ny / 2)
-  const int32_t half = (ny + 1) / 2;
-  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+// Device view of one multigrid level (transfer tables point to the next coarser level).
+struct LevelDev {
+  int32_t nx, ny;
+  int64_t nc;
+  const float *X, *Y;
+  float *ux, *uy, *fx, *fy, *rx, *ry;
+  Axis2 pvx_x, pvx_y, pvy_x, pvy_y;
+  AxisR rvx_x, rvx_y, rvy_x, rvy_y;
+};
+
+// Red-black Gauss-Seidel update of the t-th cell of one color: comp 0 updates vx,
+// 1 updates vy, on cells with (i + j) % 2 == color.  Column j holds the rows
+// i = 2q + ((j + color) & 1) of that color, q < ceil(ny / 2).
+__device__ __forceinline__ void d_rbgs(const LevelDev& v, int64_t t, int comp, int color) {
+  const int32_t half = (v.ny + 1) / 2;
   const int32_t j = (int32_t)(t / half);
-  if (j >= nx) return;
+  if (j >= v.nx) return;
   const int32_t i = 2 * (int32_t)(t - (int64_t)j * half) + ((j + color) & 1);
-  if (i >= ny) return;
-  const int64_t c = (int64_t)j * ny + i;
+  if (i >= v.ny) return;
+  const int64_t c = (int64_t)j * v.ny + i;
   if (comp == 0) {
-    const float s = rowx(X, ux, uy, c, i, j, nx, ny, nc, true);
-    ux[c] = (fx[c] - s) / X[c];
+    const float s = rowx(v.X, v.ux, v.uy, c, i, j, v.nx, v.ny, v.nc, true);
+    v.ux[c] = (v.fx[c] - s) / v.X[c];
   } else {
-    const float s = rowy(Y, ux, uy, c, i, j, nx, ny, nc, true);
-    uy[c] = (fy[c] - s) / Y[c];
+    const float s = rowy(v.Y, v.ux, v.uy, c, i, j, v.nx, v.ny, v.nc, true);
+    v.uy[c] = (v.fy[c] - s) / v.Y[c];
   }
 }
-__global__ void k_resid(const float* __restrict__ X, const float* __restrict__ Y, const float* __restrict__ ux,
-                        const float* __restrict__ uy, const float* __restrict__ fx, const float* __restrict__ fy,
-                        float* __restrict__ rx, float* __restrict__ ry, int32_t nx, int32_t ny) {
-  const int64_t nc = (int64_t)nx * ny;
-  const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= nc) return;
-  const int32_t i = (int32_t)(c % ny), j = (int32_t)(c / ny);
-  rx[c] = fx[c] - rowx(X, ux, uy, c, i, j, nx, ny, nc, false);
-  ry[c] = fy[c] - rowy(Y, ux, uy, c, i, j, nx, ny, nc, false);
+__device__ __forceinline__ int64_t rb_count(const LevelDev& v) { return (int64_t)v.nx * ((v.ny + 1) / 2); }
+
+__device__ __forceinline__ void d_resid(const LevelDev& v, int64_t c) {
+  const int32_t i = (int32_t)(c % v.ny), j = (int32_t)(c / v.ny);
+  v.rx[c] = v.fx[c] - rowx(v.X, v.ux, v.uy, c, i, j, v.nx, v.ny, v.nc, false);
+  v.ry[c] = v.fy[c] - rowy(v.Y, v.ux, v.uy, c, i, j, v.nx, v.ny, v.nc, false);
 }
-// coarse f = R r (per component, tensor product of the axis tables)
-__global__ void k_restrict(const float* __restrict__ rx, const float* __restrict__ ry, int32_t nyf,
-                           float* __restrict__ fxc, float* __restrict__ fyc, int32_t nxc, int32_t nyc, AxisR vxx, AxisR vxy,
-                           AxisR vyx, AxisR vyy) {
-  const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= (int64_t)nxc * nyc) return;
-  const int32_t I = (int32_t)(c % nyc), J = (int32_t)(c / nyc);
+// coarse f = R r at coarse cell c (tensor product of the axis tables of the fine level f)
+__device__ __forceinline__ void d_restrict(const LevelDev& f, const LevelDev& cl, int64_t c) {
+  const int32_t I = (int32_t)(c % cl.ny), J = (int32_t)(c / cl.ny);
   float sx = 0.f, sy = 0.f;
   for (int a = 0; a < kRmax; ++a) {
-    const float wa = vxx.w[J * kRmax + a];
+    const float wa = f.rvx_x.w[J * kRmax + a];
     if (wa != 0.f) {
-      const int64_t col = (int64_t)vxx.idx[J * kRmax + a] * nyf;
+      const int64_t col = (int64_t)f.rvx_x.idx[J * kRmax + a] * f.ny;
       for (int b = 0; b < kRmax; ++b) {
-        const float wb = vxy.w[I * kRmax + b];
-        if (wb != 0.f) sx += wa * wb * rx[col + vxy.idx[I * kRmax + b]];
+        const float wb = f.rvx_y.w[I * kRmax + b];
+        if (wb != 0.f) sx += wa * wb * f.rx[col + f.rvx_y.idx[I * kRmax + b]];
       }
     }
-    const float va = vyx.w[J * kRmax + a];
+    const float va = f.rvy_x.w[J * kRmax + a];
     if (va != 0.f) {
-      const int64_t col = (int64_t)vyx.idx[J * kRmax + a] * nyf;
+      const int64_t col = (int64_t)f.rvy_x.idx[J * kRmax + a] * f.ny;
       for (int b = 0; b < kRmax; ++b) {
-        const float vb = vyy.w[I * kRmax + b];
-        if (vb != 0.f) sy += va * vb * ry[col + vyy.idx[I * kRmax + b]];
+        const float vb = f.rvy_y.w[I * kRmax + b];
+        if (vb != 0.f) sy += va * vb * f.ry[col + f.rvy_y.idx[I * kRmax + b]];
       }
     }
   }
-  fxc[c] = sx;
-  fyc[c] = sy;
+  cl.fx[c] = sx;
+  cl.fy[c] = sy;
 }
-// fine u += P e
-__global__ void k_prolong(float* __restrict__ ux, float* __restrict__ uy, int32_t nxf, int32_t nyf,
-                          const float* __restrict__ ex, const float* __restrict__ ey, int32_t nyc, Axis2 vxx, Axis2 vxy,
-                          Axis2 vyx, Axis2 vyy) {
-  const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= (int64_t)nxf * nyf) return;
-  const int32_t i = (int32_t)(c % nyf), j = (int32_t)(c / nyf);
+// fine u += P e at fine cell c
+__device__ __forceinline__ void d_prolong(const LevelDev& f, const LevelDev& cl, int64_t c) {
+  const int32_t i = (int32_t)(c % f.ny), j = (int32_t)(c / f.ny);
   float sx = 0.f, sy = 0.f;
   for (int a = 0; a < 2; ++a)
     for (int b = 0; b < 2; ++b) {
-      const float w1 = vxx.w[2 * j + a] * vxy.w[2 * i + b];
-      if (w1 != 0.f) sx += w1 * ex[(int64_t)vxx.idx[2 * j + a] * nyc + vxy.idx[2 * i + b]];
-      const float w2 = vyx.w[2 * j + a] * vyy.w[2 * i + b];
-      if (w2 != 0.f) sy += w2 * ey[(int64_t)vyx.idx[2 * j + a] * nyc + vyy.idx[2 * i + b]];
+      const float w1 = f.pvx_x.w[2 * j + a] * f.pvx_y.w[2 * i + b];
+      if (w1 != 0.f) sx += w1 * cl.ux[(int64_t)f.pvx_x.idx[2 * j + a] * cl.ny + f.pvx_y.idx[2 * i + b]];
+      const float w2 = f.pvy_x.w[2 * j + a] * f.pvy_y.w[2 * i + b];
+      if (w2 != 0.f) sy += w2 * cl.uy[(int64_t)f.pvy_x.idx[2 * j + a] * cl.ny + f.pvy_y.idx[2 * i + b]];
     }
-  ux[c] += sx;
-  uy[c] += sy;
+  f.ux[c] += sx;
+  f.uy[c] += sy;
 }
-// coarsest level: u = Ainv f with the dense inverse of the velocity block (n = 2 nc unknowns)
-__global__ void k_dense_solve(const float* __restrict__ Ainv, int n, const float* __restrict__ fx,
-                              const float* __restrict__ fy, float* __restrict__ ux, float* __restrict__ uy) {
-  const int half = n / 2;
-  for (int r = threadIdx.x; r < n; r += blockDim.x) {
-    float s = 0.f;
-    for (int k = 0; k < half; ++k) s += Ainv[(int64_t)r * n + k] * fx[k];
-    for (int k = 0; k < half; ++k) s += Ainv[(int64_t)r * n + half + k] * fy[k];
-    if (r < half) ux[r] = s; else uy[r - half] = s;
+
+__global__ void k_rbgs(LevelDev v, int comp, int color) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < rb_count(v)) d_rbgs(v, t, comp, color);
+}
+__global__ void k_resid(LevelDev v) {
+  const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c < v.nc) d_resid(v, c);
+}
+__global__ void k_restrict(LevelDev f, LevelDev cl) {
+  const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c < cl.nc) d_restrict(f, cl, c);
+}
+__global__ void k_prolong(LevelDev f, LevelDev cl) {
+  const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c < f.nc) d_prolong(f, cl, c);
+}
+
+// The V-cycle below level l0 (all levels small) in one thread block:
+// every step is a block-stride loop followed by __syncthreads().
+constexpr int kCoarseThreads = 1024;
+__global__ void __launch_bounds__(kCoarseThreads) k_coarse_cycle(const LevelDev* __restrict__ lv, int l0, int nl,
+                                                                  int sweeps, const float* __restrict__ Ainv, int n) {
+  auto smooth = [&](const LevelDev& v, bool pre) {
+    const int64_t cnt = rb_count(v);
+    for (int s = 0; s < sweeps; ++s)
+      for (int k = 0; k < 4; ++k) {
+        // pre: vx red, vx black, vy red, vy black; post: the reverse order
+        const int kk = pre ? k : 3 - k;
+        const int comp = kk >> 1, color = kk & 1;
+        for (int64_t t = threadIdx.x; t < cnt; t += blockDim.x) d_rbgs(v, t, comp, color);
+        __syncthreads();
+      }
+  };
+  for (int l = l0; l < nl - 1; ++l) {
+    const LevelDev v = lv[l];
+    for (int64_t c = threadIdx.x; c < v.nc; c += blockDim.x) { v.ux[c] = 0.f; v.uy[c] = 0.f; }
+    __syncthreads();
+    smooth(v, true);
+    for (int64_t c = threadIdx.x; c < v.nc; c += blockDim.x) d_resid(v, c);
+    __syncthreads();
+    const LevelDev w = lv[l + 1];
+    for (int64_t c = threadIdx.x; c < w.nc; c += blockDim.x) d_restrict(v, w, c);
+    __syncthreads();
+  }
+  {  // coarsest: u = Ainv f
+    const LevelDev cl = lv[nl - 1];
+    const int half = n / 2;
+    for (int r = threadIdx.x; r < n; r += blockDim.x) {
+      float s = 0.f;
+      for (int k = 0; k < half; ++k) s += Ainv[(int64_t)r * n + k] * cl.fx[k];
+      for (int k = 0; k < half; ++k) s += Ainv[(int64_t)r * n + half + k] * cl.fy[k];
+      if (r < half) cl.ux[r] = s; else cl.uy[r - half] = s;
+    }
+    __syncthreads();
+  }
+  for (int l = nl - 2; l >= l0; --l) {
+    const LevelDev v = lv[l];
+    const LevelDev w = lv[l + 1];
+    for (int64_t c = threadIdx.x; c < v.nc; c += blockDim.x) d_prolong(v, w, c);
+    __syncthreads();
+    smooth(v, false);
   }
 }
 
@@ -548,11 +660,13 @@ struct StokesState {
   std::vector<void*> level_allocs;   // multigrid buffers
   std::vector<Level> levels;
   float* Ainv = nullptr;
+  LevelDev* lv_dev = nullptr;        // device copies of the level descriptors
   int n_dense = 0;
   double *w = nullptr, *prep = nullptr;  // scaling and pressure factor
   // FGMRES workspace
   int m = 0;
-  double *V = nullptr, *Z = nullptr, *r = nullptr, *t = nullptr, *xs = nullptr, *bs = nullptr, *zp = nullptr;
+  double *V = nullptr, *r = nullptr, *t = nullptr, *xs = nullptr, *bs = nullptr, *zp = nullptr, *zt = nullptr;
+  float* Z = nullptr;                // preconditioned directions, stored in FP32
   double *partial = nullptr, *dots = nullptr, *hdev = nullptr;
   int nb_dot = 0;
   double* il = nullptr;              // interleaved staging vector (N)
@@ -584,6 +698,7 @@ void free_levels(StokesState* st) {
   st->level_allocs.clear();
   st->levels.clear();
   st->Ainv = nullptr;
+  st->lv_dev = nullptr;
   if (st->gexec) cudaGraphExecDestroy(st->gexec);
   if (st->graph) cudaGraphDestroy(st->graph);
   st->gexec = nullptr;
@@ -641,6 +756,8 @@ int read_b2(eb_ctx* c, B2* b) {
 }
 
 // Build the level geometry, buffers and transfer tables (host), for the current grid and b2.
+LevelDev level_dev(const Level& v);
+
 int setup_levels(eb_ctx* c, StokesState* st, const B2& b2) {
   free_levels(st);
   std::vector<Level>& L = st->levels;
@@ -741,6 +858,9 @@ int setup_levels(eb_ctx* c, StokesState* st, const B2& b2) {
   }
   int rc = dalloc(c, st->level_allocs, &st->Ainv, (size_t)st->n_dense * st->n_dense);
   if (rc) return rc;
+  std::vector<LevelDev> lv;
+  for (const Level& v : L) lv.push_back(level_dev(v));
+  if ((rc = dupload(c, st->level_allocs, &st->lv_dev, lv))) return rc;
   EB_CK(c, cudaStreamSynchronize(c->stream));
   return EB_OK;
 }
@@ -813,34 +933,46 @@ int refresh_levels(eb_ctx* c, StokesState* st, const B2& b2) {
 }
 
 // One V-cycle from level 0's f into level 0's u (launches on c->stream).
+// One V-cycle from level 0's f into level 0's u (launches on c->stream).
+LevelDev level_dev(const Level& v) {
+  LevelDev d;
+  d.nx = v.nx; d.ny = v.ny; d.nc = v.nc;
+  d.X = v.X; d.Y = v.Y;
+  d.ux = v.ux; d.uy = v.uy; d.fx = v.fx; d.fy = v.fy; d.rx = v.rx; d.ry = v.ry;
+  d.pvx_x = v.pvx_x; d.pvx_y = v.pvx_y; d.pvy_x = v.pvy_x; d.pvy_y = v.pvy_y;
+  d.rvx_x = v.rvx_x; d.rvx_y = v.rvx_y; d.rvy_x = v.rvy_x; d.rvy_y = v.rvy_y;
+  return d;
+}
+
+// One V-cycle from level 0's f into level 0's u (launches on c->stream).  Levels
+// at or below l0 (the first with at most kCoarseCells cells) run in one block.
+constexpr int64_t kCoarseCells = 8192;
 int vcycle_launch(eb_ctx* c, StokesState* st, int sweeps, int64_t* nk) {
   std::vector<Level>& L = st->levels;
   const int nl = (int)L.size();
-  auto rb = [&](Level& v, int comp, int color) -> int {
-    const int64_t half = (int64_t)v.nx * ((v.ny + 1) / 2);
-    k_rbgs<<<nblk(half), kB, 0, c->stream>>>(v.X, v.Y, v.ux, v.uy, v.fx, v.fy, v.nx, v.ny, comp, color);
+  int l0 = 0;
+  while (l0 < nl - 1 && L[l0].nc > kCoarseCells) ++l0;
+  auto rb = [&](const LevelDev& v, int comp, int color) {
+    const int64_t cnt = (int64_t)v.nx * ((v.ny + 1) / 2);
+    k_rbgs<<<nblk(cnt), kB, 0, c->stream>>>(v, comp, color);
     ++*nk;
-    return EB_OK;
   };
-  for (int l = 0; l < nl - 1; ++l) {
-    Level& v = L[l];
-    EB_CK(c, cudaMemsetAsync(v.ux, 0, v.nc * sizeof(float), c->stream));
-    EB_CK(c, cudaMemsetAsync(v.uy, 0, v.nc * sizeof(float), c->stream));
+  for (int l = 0; l < l0; ++l) {
+    const LevelDev v = level_dev(L[l]);
+    EB_CK(c, cudaMemsetAsync(L[l].ux, 0, v.nc * sizeof(float), c->stream));
+    EB_CK(c, cudaMemsetAsync(L[l].uy, 0, v.nc * sizeof(float), c->stream));
     for (int s = 0; s < sweeps; ++s) { rb(v, 0, 0); rb(v, 0, 1); rb(v, 1, 0); rb(v, 1, 1); }
-    k_resid<<<nblk(v.nc), kB, 0, c->stream>>>(v.X, v.Y, v.ux, v.uy, v.fx, v.fy, v.rx, v.ry, v.nx, v.ny);
-    Level& w = L[l + 1];
-    k_restrict<<<nblk(w.nc), kB, 0, c->stream>>>(v.rx, v.ry, v.ny, w.fx, w.fy, w.nx, w.ny, v.rvx_x, v.rvx_y, v.rvy_x,
-                                                  v.rvy_y);
+    k_resid<<<nblk(v.nc), kB, 0, c->stream>>>(v);
+    const LevelDev w = level_dev(L[l + 1]);
+    k_restrict<<<nblk(w.nc), kB, 0, c->stream>>>(v, w);
     *nk += 2;
   }
-  Level& cl = L[nl - 1];
-  k_dense_solve<<<1, 512, 0, c->stream>>>(st->Ainv, st->n_dense, cl.fx, cl.fy, cl.ux, cl.uy);
+  k_coarse_cycle<<<1, kCoarseThreads, 0, c->stream>>>(st->lv_dev, l0, nl, sweeps, st->Ainv, st->n_dense);
   ++*nk;
-  for (int l = nl - 2; l >= 0; --l) {
-    Level& v = L[l];
-    Level& w = L[l + 1];
-    k_prolong<<<nblk(v.nc), kB, 0, c->stream>>>(v.ux, v.uy, v.nx, v.ny, w.ux, w.uy, w.ny, v.pvx_x, v.pvx_y, v.pvy_x,
-                                                 v.pvy_y);
+  for (int l = l0 - 1; l >= 0; --l) {
+    const LevelDev v = level_dev(L[l]);
+    const LevelDev w = level_dev(L[l + 1]);
+    k_prolong<<<nblk(v.nc), kB, 0, c->stream>>>(v, w);
     ++*nk;
     for (int s = 0; s < sweeps; ++s) { rb(v, 1, 1); rb(v, 1, 0); rb(v, 0, 1); rb(v, 0, 0); }
   }
@@ -894,9 +1026,8 @@ int precondition(eb_ctx* c, StokesState* st, const double* rhat, double* z) {
 // dots[v] = V_v . u for v < nv (device), copied to host h
 int mdot(eb_ctx* c, StokesState* st, const double* V, int64_t stride, int nv, const double* u, double* h) {
   const int64_t n3 = 3 * st->sys.nc;
-  dim3 grid(st->nb_dot, nv);
   EB_PROF(c, "k_mdot");
-  k_mdot<<<grid, kB, 0, c->stream>>>(V, stride, u, n3, st->partial);
+  k_mdot<<<dim3(st->nb_dot, nv), kB, 0, c->stream>>>(V, stride, u, n3, st->partial);
   EB_LAUNCHED(c);
   EB_PROF(c, "k_mdot");
   k_mdot_final<<<nv, kB, 0, c->stream>>>(st->partial, st->nb_dot, st->dots);
@@ -917,25 +1048,28 @@ int apply_scaled(eb_ctx* c, StokesState* st, const double* x, double* y) {
 int ensure_solver(eb_ctx* c, StokesState* st, int m) {
   if (st->m == m && st->V) return EB_OK;
   // (re)allocate the Krylov workspace
-  for (double** p : {&st->V, &st->Z}) {
-    if (*p) {
-      cudaFree(*p);
-      st->allocs.erase(std::remove(st->allocs.begin(), st->allocs.end(), (void*)*p), st->allocs.end());
-      *p = nullptr;
-    }
-  }
+  auto drop = [&](void* p) {
+    if (!p) return;
+    cudaFree(p);
+    st->allocs.erase(std::remove(st->allocs.begin(), st->allocs.end(), p), st->allocs.end());
+  };
+  drop(st->V);
+  drop(st->Z);
+  st->V = nullptr;
+  st->Z = nullptr;
   const size_t n3 = 3 * (size_t)st->sys.nc;
   st->m = m;
-  st->nb_dot = 2 * 152;
+  st->nb_dot = kDotBlocks;
   int rc;
-  if ((rc = dalloc(c, st->allocs, &st->V, (size_t)(m + 1) * n3)) || (rc = dalloc(c, st->allocs, &st->Z, (size_t)m * n3)))
+  if ((rc = dalloc(c, st->allocs, &st->V, (size_t)(m + 2) * n3)) || (rc = dalloc(c, st->allocs, &st->Z, (size_t)m * n3)))
     return rc;
   if (!st->r) {
     if ((rc = dalloc(c, st->allocs, &st->r, n3)) || (rc = dalloc(c, st->allocs, &st->t, n3)) ||
         (rc = dalloc(c, st->allocs, &st->xs, n3)) || (rc = dalloc(c, st->allocs, &st->bs, n3)) ||
+        (rc = dalloc(c, st->allocs, &st->zt, n3)) ||
         (rc = dalloc(c, st->allocs, &st->w, n3)) || (rc = dalloc(c, st->allocs, &st->prep, (size_t)st->sys.nc)) ||
-        (rc = dalloc(c, st->allocs, &st->partial, (size_t)st->nb_dot * 512)) ||
-        (rc = dalloc(c, st->allocs, &st->dots, 512)) || (rc = dalloc(c, st->allocs, &st->hdev, 512)))
+        (rc = dalloc(c, st->allocs, &st->partial, (size_t)st->nb_dot * kMaxDots)) ||
+        (rc = dalloc(c, st->allocs, &st->dots, kMaxDots)) || (rc = dalloc(c, st->allocs, &st->hdev, kMaxDots)))
       return rc;
   }
   return EB_OK;
@@ -962,9 +1096,9 @@ extern "C" int eb_solve_stokes_system(eb_ctx* c, const eb_solve_opts* o, eb_solv
   eb_solve_opts opt = o ? *o : eb_solve_opts{};
   if (opt.rtol <= 0) opt.rtol = 1e-8;
   if (opt.max_iters <= 0) opt.max_iters = 3000;
-  if (opt.restart <= 0) opt.restart = 40;
+  if (opt.restart <= 0) opt.restart = 250;
   if (opt.mg_sweeps <= 0) opt.mg_sweeps = 2;
-  const int m = std::min(opt.restart, 200);
+  const int m = std::min(opt.restart, kMaxRestart);
   const int64_t n3 = 3 * s.nc;
   B2 b2;
   if ((rc = ensure_solver(c, st, m)) || (rc = read_b2(c, &b2))) return rc;
@@ -992,7 +1126,7 @@ extern "C" int eb_solve_stokes_system(eb_ctx* c, const eb_solve_opts* o, eb_solv
   const double bnorm = std::sqrt(bn2);
   if (!std::isfinite(bnorm)) return eb_fail(c, EB_NAN, "right-hand side has NaN/Inf");
   std::vector<double> H((size_t)(m + 1) * m), g(m + 1), cs(m), sn(m), hcol(m + 2), y(m);
-  int it = 0;
+  int it = 0, reorth = 0;
   double est = 1.0;
   bool converged = (bnorm == 0.0);
   while (!converged && it < opt.max_iters) {
@@ -1015,27 +1149,44 @@ extern "C" int eb_solve_stokes_system(eb_ctx* c, const eb_solve_opts* o, eb_solv
     int k = 0;
     for (; k < m && it < opt.max_iters; ++k) {
       double* vk = st->V + (size_t)k * n3;
-      double* zk = st->Z + (size_t)k * n3;
+      float* zk = st->Z + (size_t)k * n3;
       double* w = st->V + (size_t)(k + 1) * n3;
-      if ((rc = precondition(c, st, vk, zk)) || (rc = apply_scaled(c, st, zk, w))) return rc;
-      // classical Gram-Schmidt with one conditional re-orthogonalisation
-      double wn2_before;
-      if ((rc = mdot(c, st, w, 0, 1, w, &wn2_before))) return rc;
+      if ((rc = precondition(c, st, vk, st->zt))) return rc;
+      EB_PROF(c, "k_axpy");
+      k_round_dir<<<nblk(n3), kB, 0, c->stream>>>(st->zt, zk, n3);
+      EB_LAUNCHED(c);
+      if ((rc = apply_scaled(c, st, st->zt, w))) return rc;
+      // Classical Gram-Schmidt.  One reduction gives V^T w and |w|^2 (w is the slot after V_k);
+      // the projected norm follows from Pythagoras unless cancellation is large, in which
+      // case a second pass re-orthogonalises and the norm is measured.
+      std::vector<double> h(k + 2);
+      if ((rc = mdot(c, st, st->V, n3, k + 2, w, h.data()))) return rc;
+      double wn2_before = h[k + 1];
       for (int pass = 0; pass < 2; ++pass) {
-        std::vector<double> h(k + 1);
-        if ((rc = mdot(c, st, st->V, n3, k + 1, w, h.data()))) return rc;
         EB_CK(c, cudaMemcpyAsync(st->hdev, h.data(), (k + 1) * sizeof(double), cudaMemcpyHostToDevice, c->stream));
         EB_PROF(c, "k_maxpy");
-        k_maxpy<<<nblk(n3), kB, 0, c->stream>>>(w, st->V, n3, st->hdev, k + 1, n3);
+        k_maxpy<<<(unsigned)((n3 + kAxTile - 1) / kAxTile), kAxThreads, (size_t)(k + 1) * sizeof(double), c->stream>>>(
+            w, st->V, n3, st->hdev, k + 1, n3);
         EB_LAUNCHED(c);
-        for (int q = 0; q <= k; ++q) hcol[q] = (pass == 0 ? 0.0 : hcol[q]) + h[q];
-        double wn2;
-        if ((rc = mdot(c, st, w, 0, 1, w, &wn2))) return rc;
-        hcol[k + 1] = std::sqrt(wn2);
-        if (!std::isfinite(hcol[k + 1])) return eb_fail(c, EB_NAN, "FGMRES basis became NaN/Inf");
-        if (hcol[k + 1] > 0.7071 * std::sqrt(wn2_before)) break;
-        wn2_before = wn2;
+        double proj = 0.0;
+        for (int q = 0; q <= k; ++q) {
+          hcol[q] = (pass == 0 ? 0.0 : hcol[q]) + h[q];
+          proj += h[q] * h[q];
+        }
+        const double est = wn2_before - proj;
+        if (pass == 0 && est > kReorth2 * wn2_before) {  // no severe cancellation: keep
+          hcol[k + 1] = std::sqrt(est);
+          break;
+        }
+        ++reorth;
+        if ((rc = mdot(c, st, st->V, n3, k + 2, w, h.data()))) return rc;
+        if (pass == 1) {
+          hcol[k + 1] = std::sqrt(h[k + 1]);
+          break;
+        }
+        wn2_before = h[k + 1];
       }
+      if (!std::isfinite(hcol[k + 1])) return eb_fail(c, EB_NAN, "FGMRES basis became NaN/Inf");
       // apply the previous rotations, then a new one
       for (int q = 0; q < k; ++q) {
         const double a = cs[q] * hcol[q] + sn[q] * hcol[q + 1];
@@ -1069,7 +1220,7 @@ extern "C" int eb_solve_stokes_system(eb_ctx* c, const eb_solve_opts* o, eb_solv
     for (int q = 0; q < k; ++q) negy[q] = -y[q];
     EB_CK(c, cudaMemcpyAsync(st->hdev, negy.data(), k * sizeof(double), cudaMemcpyHostToDevice, c->stream));
     EB_PROF(c, "k_maxpy");
-    k_maxpy<<<nblk(n3), kB, 0, c->stream>>>(st->xs, st->Z, n3, st->hdev, k, n3);
+    k_maxpy_f32<<<nblk(n3), kB, 0, c->stream>>>(st->xs, st->Z, n3, st->hdev, k, n3);
     EB_LAUNCHED(c);
     EB_CK(c, cudaStreamSynchronize(c->stream));
   }
@@ -1096,6 +1247,7 @@ extern "C" int eb_solve_stokes_system(eb_ctx* c, const eb_solve_opts* o, eb_solv
   const double rel_s = bnorm > 0 ? std::sqrt(sr2) / bnorm : std::sqrt(sr2);
   if (rep) {
     rep->iterations = it;
+    rep->reorthogonalisations = reorth;
     rep->levels = (int32_t)st->levels.size();
     rep->rel_residual = rel;
     rep->rel_residual_scaled = rel_s;
@@ -1171,6 +1323,31 @@ extern "C" int eb_build_stokes_system(eb_ctx* c) {
   prof_resolve(c);
   s->built = true;
   return EB_OK;
+}
+
+static int grid_step(eb_ctx* c, std::initializer_list<int> fields, int (*launch)(eb_ctx*)) {
+  if (!c) return EB_BAD_INPUT;
+  if (!c->have_grid || !c->have_params) return eb_fail(c, EB_NOT_READY, "eb_set_grid and eb_set_params come first");
+  cudaSetDevice(c->device);
+  int rc = need_fields(c, fields);
+  if (rc || (rc = launch(c))) return rc;
+  EB_CK(c, cudaStreamSynchronize(c->stream));
+  prof_resolve(c);
+  return EB_OK;
+}
+
+extern "C" int eb_update_grid_strain_rate_and_spin(eb_ctx* c) {
+  return grid_step(c, {EB_G_VX1, EB_G_VY1, EB_G_EXX, EB_G_EXY, EB_G_ESP, EB_G_EII}, launch_grid_strain_rate);
+}
+extern "C" int eb_forecast_viscoelastic_grid_stress(eb_ctx* c) {
+  return grid_step(c, {EB_G_ETAS1, EB_G_MUS1, EB_G_EXY, EB_G_SXY1, EB_G_SXY2, EB_G_ETAN1, EB_G_MUN1, EB_G_EXX, EB_G_SXX1,
+                       EB_G_SXX2}, launch_forecast_stress);
+}
+extern "C" int eb_calculate_deviatoric_grid_stress_change(eb_ctx* c) {
+  return grid_step(c, {EB_G_SXY2, EB_G_SXY1, EB_G_DSXY, EB_G_SXX2, EB_G_SXX1, EB_G_DSXX}, launch_stress_change);
+}
+extern "C" int eb_interpolate_stag_velocity_to_basic_grid(eb_ctx* c) {
+  return grid_step(c, {EB_G_VX1, EB_G_VY1, EB_G_VXB, EB_G_VYB}, launch_stag_to_basic);
 }
 
 extern "C" int eb_process_stokes_solution(eb_ctx* c) {

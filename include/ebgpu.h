@@ -140,6 +140,8 @@ enum eb_grid_field {
    * blefty/brighty (ynum, 2) */
   EB_G_BTOPX, EB_G_BBOTTOMX, EB_G_BTOPY, EB_G_BBOTTOMY,
   EB_G_BLEFTX, EB_G_BRIGHTX, EB_G_BLEFTY, EB_G_BRIGHTY,
+  /* post-solve grids: strain-rate invariant eii (P), velocity at basic nodes vxb, vyb (B) */
+  EB_G_EII, EB_G_VXB, EB_G_VYB,
   EB_G_NFIELDS
 };
 
@@ -290,6 +292,7 @@ typedef struct eb_solve_report {
   double  rel_residual;      /* ||R - L S||_2 / ||R||_2 of the assembled (unscaled) system */
   double  rel_residual_scaled; /* the same for the diagonally scaled system             */
   double  seconds;           /* wall time of the solve                                  */
+  int32_t reorthogonalisations; /* Gram-Schmidt second passes (severe cancellation only) */
 } eb_solve_report;
 
 enum eb_stokes_vector {
@@ -328,6 +331,16 @@ int eb_stokes_nonlinear_residual(eb_ctx* ctx);
 
 /* The solution-vector part of SystemSolver.backup_stokes_arrays!  (SystemSolver.jl:306-318): S_old = S. */
 int eb_backup_stokes_solution(eb_ctx* ctx);
+
+/* Post-solve grid kernels (src/stokes_continuity_solver/utils/):
+ * GridStrainRate.update_grid_strain_rate_and_spin! (strain_rate/GridStrainRate.jl:6-182): exx, exy, eii, esp */
+int eb_update_grid_strain_rate_and_spin(eb_ctx* ctx);
+/* GridStress.forecast_viscoelastic_grid_stress! (GridStress.jl:30-126): sxy2, sxx2 */
+int eb_forecast_viscoelastic_grid_stress(eb_ctx* ctx);
+/* GridStress.calculate_deviatoric_grid_stress_change! (GridStress.jl:128-134): dsxy, dsxx */
+int eb_calculate_deviatoric_grid_stress_change(eb_ctx* ctx);
+/* StokesInterpolate.interpolate_stag_velocity_to_basic_grid! (StokesInterpolate.jl:16-33): vxb, vyb */
+int eb_interpolate_stag_velocity_to_basic_grid(eb_ctx* ctx);
 
 /* No counterpart in the reference (its COO product): y = L x for host vectors of N doubles. */
 int eb_stokes_apply(eb_ctx* ctx, const double* x, double* y);

@@ -181,3 +181,35 @@ class StokesOracle:
         lib().o_coo_residual(C.c_int64(len(Li)), _p(Li), _p(Lj), _p(Lv), _p(x), _p(R), C.c_int64(self.N),
                              _p(work), _p(resnl))
         return resnl
+
+    # ---- post-solve grid kernels ------------------------------------------------
+    def update_grid_strain_rate_and_spin(self):
+        """GridStrainRate.update_grid_strain_rate_and_spin! (utils/strain_rate/GridStrainRate.jl:6-182)."""
+        G, S = self.gr, self.spacing
+        X, Y = self.xnum, self.ynum
+        for k, sh in (("exx", (Y - 1, X - 1)), ("exy", (Y, X)), ("eii", (Y - 1, X - 1)), ("esp", (Y, X))):
+            G[k] = np.zeros(sh, order="F")
+        lib().o_grid_strain_rate_and_spin(C.c_int64(X), C.c_int64(Y), _p(S["xstp_b"]), _p(S["ystp_b"]),
+                                          _p(S["xstp_vy"]), _p(S["ystp_vx"]), _p(G["vx1"]), _p(G["vy1"]),
+                                          _p(G["exx"]), _p(G["exy"]), _p(G["eii"]), _p(G["esp"]))
+
+    def forecast_viscoelastic_grid_stress(self):
+        """GridStress.forecast_viscoelastic_grid_stress! and calculate_deviatoric_grid_stress_change!
+        (utils/GridStress.jl:30-134)."""
+        G = self.gr
+        X, Y = self.xnum, self.ynum
+        for k, sh in (("sxy2", (Y, X)), ("sxx2", (Y - 1, X - 1)), ("dsxy", (Y, X)), ("dsxx", (Y - 1, X - 1))):
+            G[k] = np.zeros(sh, order="F")
+        lib().o_forecast_grid_stress(C.c_int64(X), C.c_int64(Y), C.c_double(self.p["timestep"]), _p(G["etas1"]),
+                                     _p(G["mus1"]), _p(G["exy"]), _p(G["sxy1"]), _p(G["etan1"]), _p(G["mun1"]),
+                                     _p(G["exx"]), _p(G["sxx1"]), _p(G["sxy2"]), _p(G["sxx2"]), _p(G["dsxy"]),
+                                     _p(G["dsxx"]))
+
+    def interpolate_stag_velocity_to_basic_grid(self):
+        """StokesInterpolate.interpolate_stag_velocity_to_basic_grid! (utils/StokesInterpolate.jl:16-33)."""
+        G = self.gr
+        X, Y = self.xnum, self.ynum
+        G["vxb"] = np.zeros((Y, X), order="F")
+        G["vyb"] = np.zeros((Y, X), order="F")
+        lib().o_stag_velocity_to_basic(C.c_int64(X), C.c_int64(Y), _p(G["vx1"]), _p(G["vy1"]), _p(G["vxb"]),
+                                       _p(G["vyb"]))

@@ -431,3 +431,64 @@ void o_process_stokes_solution(int64_t xnum, int64_t ynum, double pscale, const 
     A2(vy1, ynum, i, xnum + 1) = A2(brighty, ynum, i, 1) + A2(brighty, ynum, i, 2) * A2(vy1, ynum, i, xnum);
   }
 }
+
+/* ---- post-solve grid kernels (src/stokes_continuity_solver/utils/) ---------- */
+
+/* GridStrainRate.update_grid_strain_rate_and_spin! (strain_rate/GridStrainRate.jl:6-182):
+ * exx (ynum-1, xnum-1), exy (ynum, xnum), eii (ynum-1, xnum-1), esp (ynum, xnum). */
+void o_grid_strain_rate_and_spin(int64_t xnum, int64_t ynum, const double* xstp_b, const double* ystp_b,
+                                 const double* xstp_vy, const double* ystp_vx, const double* vx1,
+                                 const double* vy1, double* exx, double* exy, double* eii, double* esp) {
+  const int64_t yp = ynum - 1, yx = ynum + 1;
+  memset(exx, 0, sizeof(double) * (size_t)(yp * (xnum - 1)));
+  for (int64_t j = 1; j < xnum; ++j)
+    for (int64_t i = 1; i < ynum; ++i)
+      A2(exx, yp, i, j) = 0.5 * ((A2(vx1, yx, i + 1, j + 1) - A2(vx1, yx, i + 1, j)) / xstp_b[j - 1] -
+                                 (A2(vy1, ynum, i + 1, j + 1) - A2(vy1, ynum, i, j + 1)) / ystp_b[i - 1]);
+  for (int64_t j = 1; j <= xnum; ++j)
+    for (int64_t i = 1; i <= ynum; ++i)
+      A2(exy, ynum, i, j) = 0.5 * ((A2(vx1, yx, i + 1, j) - A2(vx1, yx, i, j)) / ystp_vx[i - 1] +
+                                   (A2(vy1, ynum, i, j + 1) - A2(vy1, ynum, i, j)) / xstp_vy[j - 1]);
+  memset(eii, 0, sizeof(double) * (size_t)(yp * (xnum - 1)));
+  /* exx^2.0 etc.: Julia's x^2.0 is x*x */
+  for (int64_t j = 2; j <= xnum; ++j)
+    for (int64_t i = 2; i <= ynum; ++i) {
+      const double e = A2(exx, yp, i - 1, j - 1);
+      const double a = A2(exy, ynum, i - 1, j - 1), b = A2(exy, ynum, i, j - 1);
+      const double c = A2(exy, ynum, i - 1, j), d = A2(exy, ynum, i, j);
+      A2(eii, yp, i - 1, j - 1) = sqrt(e * e + (a * a + b * b + c * c + d * d) / 4.0);
+    }
+  for (int64_t j = 1; j <= xnum; ++j)
+    for (int64_t i = 1; i <= ynum; ++i)
+      A2(esp, ynum, i, j) = 0.5 * ((A2(vy1, ynum, i, j + 1) - A2(vy1, ynum, i, j)) / xstp_vy[j - 1] -
+                                   (A2(vx1, yx, i + 1, j) - A2(vx1, yx, i, j)) / ystp_vx[i - 1]);
+}
+
+/* GridStress.forecast_viscoelastic_grid_stress! (GridStress.jl:30-126) and
+ * calculate_deviatoric_grid_stress_change! (:128-134). */
+void o_forecast_grid_stress(int64_t xnum, int64_t ynum, double dt, const double* etas1, const double* mus1,
+                            const double* exy, const double* sxy1, const double* etan1, const double* mun1,
+                            const double* exx, const double* sxx1, double* sxy2, double* sxx2, double* dsxy,
+                            double* dsxx) {
+  const int64_t nb = xnum * ynum, np = (xnum - 1) * (ynum - 1);
+  for (int64_t k = 0; k < nb; ++k) {
+    const double f = ve_factor(etas1[k], mus1[k], dt);
+    sxy2[k] = (1.0 - f) * 2.0 * etas1[k] * exy[k] + f * sxy1[k];
+  }
+  for (int64_t k = 0; k < np; ++k) {
+    const double f = ve_factor(etan1[k], mun1[k], dt);
+    sxx2[k] = (1.0 - f) * 2.0 * etan1[k] * exx[k] + f * sxx1[k];
+  }
+  for (int64_t k = 0; k < nb; ++k) dsxy[k] = sxy2[k] - sxy1[k];
+  for (int64_t k = 0; k < np; ++k) dsxx[k] = sxx2[k] - sxx1[k];
+}
+
+/* StokesInterpolate.interpolate_stag_velocity_to_basic_grid! (StokesInterpolate.jl:16-33). */
+void o_stag_velocity_to_basic(int64_t xnum, int64_t ynum, const double* vx1, const double* vy1, double* vxb,
+                              double* vyb) {
+  for (int64_t j = 1; j <= xnum; ++j)
+    for (int64_t i = 1; i <= ynum; ++i) {
+      A2(vxb, ynum, i, j) = (A2(vx1, ynum + 1, i, j) + A2(vx1, ynum + 1, i + 1, j)) / 2.0;
+      A2(vyb, ynum, i, j) = (A2(vy1, ynum, i, j) + A2(vy1, ynum, i, j + 1)) / 2.0;
+    }
+}

@@ -162,3 +162,22 @@ def test_nonlinear_residual_and_backup(eb):
     scale = abs(o.matrix()) @ np.abs(S) + np.abs(o.coo[3])
     assert np.all(np.abs(res - ref) <= 1e-14 * scale + 1e-300)
     mic.close()
+
+
+@pytest.mark.parametrize("case", ["rift_small", "sinking_block"])
+def test_post_solve_grid_kernels_match_oracle(eb, case):
+    """Grid strain rate/spin, viscoelastic stress forecast and change, basic-node velocity:
+    identical to the oracle applied to the GPU's own solution."""
+    model = marker_model(eb, case)
+    o, mic, rep, S = solve_case(eb, model, 1e-8)
+    o.process_stokes_solution(S)
+    mic.update_grid_strain_rate_and_spin()
+    mic.forecast_viscoelastic_grid_stress()
+    mic.calculate_deviatoric_grid_stress_change()
+    mic.interpolate_stag_velocity_to_basic_grid()
+    o.update_grid_strain_rate_and_spin()
+    o.forecast_viscoelastic_grid_stress()
+    o.interpolate_stag_velocity_to_basic_grid()
+    for k in ("exx", "exy", "eii", "esp", "sxy2", "sxx2", "dsxy", "dsxx", "vxb", "vyb"):
+        assert np.array_equal(mic.download_grid(k), o.gr[k]), k
+    mic.close()
