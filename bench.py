@@ -71,6 +71,7 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-stokes", action="store_true")
+    ap.add_argument("--stokes-method", default="fgmres", choices=["fgmres", "bicgstab"])
     return ap.parse_args()
 
 
@@ -167,7 +168,7 @@ STOKES_GRIDS = ("etas1", "etan1", "mus1", "mun1", "sxy1", "sxx1", "rho1", "rho1_
                 "brighty")
 
 
-def stokes_gpu(mic, reps: int = 2):
+def stokes_gpu(mic, reps: int = 2, method: str = "fgmres"):
     """The Stokes step on the grids the context holds: build steps, solve to 1e-8, unpack.
     One warm-up (level set-up, graph capture), then `reps` timed steps (wall clock: the
     FGMRES loop is host-driven)."""
@@ -177,7 +178,7 @@ def stokes_gpu(mic, reps: int = 2):
         mic.calc_viscoelastic_terms()
         mic.viscoelastic_rhs()
         mic.build_system_of_equations()
-        rep = mic.solve_system(rtol=1e-8, check=False)
+        rep = mic.solve_system(rtol=1e-8, check=False, method=method)
         mic.process_stokes_solution()
         return rep
 
@@ -337,18 +338,48 @@ def main():
     # Stokes step of the same model: the marker cycle left the averaged grids on the device
     stokes = None
     if not args.no_stokes:
-        s_dt, s_rep, s_prof = stokes_gpu(mic, reps=2)
+        alt = {}
+        for meth in ("fgmres", "bicgstab"):
+            if meth != args.stokes_method:
+                a_dt, a_rep, _ = stokes_gpu(mic, reps=1, method=meth)
+                alt[meth] = {"value": a_dt, "iterations": a_rep["iterations"], "status": a_rep["status"],
+                             "rel_residual": a_rep["rel_residual"]}
+        s_dt, s_rep, s_prof = stokes_gpu(mic, reps=2, method=args.stokes_method)
         s_kern = {k: (t / n, n) for k, (t, n) in s_prof.items()}
         stokes = {"metric": STOKES_METRIC, "value": s_dt, "unit": "s/solve", "higher_is_better": False,
                   "workload": f"{args.workload}: {model.grid.xnum}x{model.grid.ynum} nodes, "
                               f"N={3 * (model.grid.xnum - 1) * (model.grid.ynum - 1)} unknowns",
-                  "includes": "viscoelastic terms, RHS, assembly, FGMRES+MG solve, unpacking",
+                  "includes": f"viscoelastic terms, RHS, assembly, {args.stokes_method}+MG solve, unpacking",
+                  "method": args.stokes_method, "other_methods": alt,
                   "iterations": s_rep["iterations"], "levels": s_rep["levels"],
                   "rel_residual": s_rep["rel_residual"], "rel_residual_scaled": s_rep["rel_residual_scaled"],
                   "status": s_rep["status"], "solve_s": s_rep["seconds"],
                   "reorthogonalisations": s_rep["reorthogonalisations"],
                   "kernels_ms": {k: round(v[0] * v[1], 3) for k, v in
                                  sorted(s_kern.items(), key=lambda kv: -kv[1][0] * kv[1][1])[:12]}}
+        # roofline of the Krylov-basis products (the solve's dominant kernels): per FGMRES
+        # iteration k of a cycle, k_mdot reads the k+2 basis vectors and k_maxpy k+1 of them
+        # plus the new direction (read and written); vectors are N doubles.
+        n_unk = 3 * (model.grid.xnum - 1) * (model.grid.ynum - 1)
+        its, m = s_rep["iterations"], 250
+        ks = [k for c0 in range(0, its, m) for k in range(min(m, its - c0))] if args.stokes_method == "fgmres" else []
+        vbytes = n_unk * 8.0
+        bytes_dot = sum(k + 2 for k in ks) * vbytes
+        bytes_axpy = sum(k + 3 for k in ks) * vbytes
+        peak, peak_kind = peaks()
+        rl = {}
+        nc_cells = n_unk // 3
+        # operator product: 27 coefficients, x and the scaling w read, y written (FP64 per cell)
+        bytes_apply = nc_cells * (27 + 3 + 3 + 3) * 8.0 * s_kern.get("k_apply64", (0, 0))[1] / 2
+        for kname, b in (("k_mdot", bytes_dot), ("k_maxpy", bytes_axpy), ("k_apply64", bytes_apply)):
+            if kname in s_kern and b > 0:
+                t = s_kern[kname][0] * s_kern[kname][1] / 2 * 1e-3  # seconds per solve (2 timed solves)
+                rl[kname] = {"achieved": b / t / 1e9, "bytes_per_solve": b, "s_per_solve": t}
+        if rl:
+            dom_k = max(rl, key=lambda k: rl[k]["s_per_solve"])
+            stokes["roofline"] = {"bound": "hbm", "kernel": dom_k, "achieved": rl[dom_k]["achieved"], "peak": peak,
+                                  "unit": "GB/s", "frac": rl[dom_k]["achieved"] / peak, "peak_kind": peak_kind,
+                                  "traffic": None, "kernels": rl}
         if rank == 0 and world == 1 and not args.no_cpu:
             try:
                 s_cpu, strip = stokes_cpu_sample(eb, load_oracle())

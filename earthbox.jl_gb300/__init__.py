@@ -278,9 +278,11 @@ class MarkerInCell:
         self._call("eb_build_stokes_system")
 
     def solve_system(self, rtol: float = 1e-8, max_iters: int = 0, restart: int = 0, mg_sweeps: int = 0,
-                     use_initial_guess: bool = False, check: bool = True) -> dict:
-        """The Stokes solve (replaces SystemSolver.solve_system_optimized, SystemSolver.jl:67-91)."""
-        o = _abi.SolveOpts(rtol, max_iters, restart, mg_sweeps, int(use_initial_guess))
+                     use_initial_guess: bool = False, method: str = "fgmres", check: bool = True) -> dict:
+        """The Stokes solve (replaces SystemSolver.solve_system_optimized, SystemSolver.jl:67-91);
+        method "fgmres" or "bicgstab"."""
+        o = _abi.SolveOpts(rtol, max_iters, restart, mg_sweeps, int(use_initial_guess),
+                           {"fgmres": 0, "bicgstab": 1}[method])
         r = _abi.SolveReport()
         rc = self._lib.eb_solve_stokes_system(self._ctx, C.byref(o), C.byref(r))
         rep = {"status": rc, "iterations": r.iterations, "levels": r.levels, "rel_residual": r.rel_residual,
@@ -299,9 +301,15 @@ class MarkerInCell:
         self._call("eb_stokes_nonlinear_residual")
         return self.download_stokes_vector("resnl")
 
-    def backup_stokes_solution(self) -> None:
-        """The S part of SystemSolver.backup_stokes_arrays! (SystemSolver.jl:306-318)."""
-        self._call("eb_backup_stokes_solution")
+    def backup_stokes_arrays(self) -> None:
+        """SystemSolver.backup_stokes_arrays! (SystemSolver.jl:306-318): S, vx1, vy1, pr1 -> *_old."""
+        self._call("eb_backup_stokes_arrays")
+
+    def calculate_stokes_norms(self) -> dict:
+        """StokesNorms.calculate_stokes_norms! solution-change norms and |resnl|_2 (StokesNorms.jl:8-160)."""
+        n = _abi.StokesNorms()
+        self._check(self._lib.eb_calculate_stokes_norms(self._ctx, C.byref(n)))
+        return {k: getattr(n, k) for k, _ in _abi.StokesNorms._fields_}
 
     @property
     def stokes_size(self) -> int:
@@ -352,15 +360,92 @@ class MarkerInCell:
         """StokesInterpolate.interpolate_stag_velocity_to_basic_grid! (StokesInterpolate.jl:16-33): vxb, vyb."""
         self._call("eb_interpolate_stag_velocity_to_basic_grid")
 
+    def interpolate_basic_viscoplastic_viscosity_to_pressure_grid(self, iuse_harmonic: int = 1) -> None:
+        """Interpolation.interpolate_basic_viscoplastic_viscosity_to_pressure_grid! (Interpolation.jl:97-108)."""
+        self._check(self._lib.eb_interpolate_basic_viscoplastic_viscosity_to_pressure_grid(self._ctx, int(iuse_harmonic)))
+
+    def update_nodes_for_plastic_yielding(self, wall: dict | None = None) -> tuple:
+        """PlasticFailureNodes.update_nodes_for_plastic_yielding (PlasticFailureNodes.jl:24-184).
+        `wall` holds the mobile-wall geometry (eb_mobile_wall fields) or None.
+        Returns (nnode_yield, global_yield_error)."""
+        n, e = C.c_int64(), C.c_double()
+        wp = None
+        if wall is not None:
+            wp = _abi.MobileWall(**{k: wall.get(k, 0) for k, _ in _abi.MobileWall._fields_})
+        self._check(self._lib.eb_update_nodes_for_plastic_yielding(self._ctx, C.byref(wp) if wp else None,
+                                                                   C.byref(n), C.byref(e)))
+        return int(n.value), float(e.value)
+
+    def apply_nodal_plastic_yielding(self) -> None:
+        """The etas1 / plastic_yield / plastic strain-rate updates of PlasticityLoopNodes.picard_loop."""
+        self._call("eb_apply_nodal_plastic_yielding")
+
+    def picard_loop_nodes(self, nglobal: int, tolerance_picard: float, iuse_harmonic: int = 1,
+                          wall: dict | None = None, **solve_kw) -> list:
+        """PlasticityLoopNodes.picard_loop (plasticity_loop_nodes/PlasticityLoopNodes.jl:36-92): solve,
+        process, nodal yield, apply it when nodes yield; stop when no node yields, at nglobal, or when
+        the yield error or dvxy_rel_L2 drops below the tolerance (check_stop_global_loop_nodes)."""
+        history = []
+        for iglobal in range(1, nglobal + 1):
+            if iglobal > 1:
+                self.interpolate_basic_viscoplastic_viscosity_to_pressure_grid(iuse_harmonic)
+            rep = self.solve_viscoelastic_stokes_continuity_equations(**solve_kw)
+            norms = self.stokes_solution_processing()
+            nnode, gerr = self.update_nodes_for_plastic_yielding(wall)
+            if nnode > 0:
+                self.apply_nodal_plastic_yielding()
+            history.append({"iglobal": iglobal, "nnode_yield": nnode, "global_yield_error": gerr, **rep, **norms})
+            if (nnode == 0 or iglobal == nglobal or gerr < tolerance_picard
+                    or norms["dvxy_rel_L2"] < tolerance_picard):
+                break
+        return history
+
     def solve_viscoelastic_stokes_continuity_equations(self, **solve_kw) -> dict:
         """StokesContinuitySolver.solve_viscoelastic_stokes_continuity_equations!
-        (StokesContinuitySolver.jl:68-110): build steps, solve, unpack."""
+        (StokesContinuitySolver.jl:68-90): build steps, solve, unpack, and the nonlinear
+        residual |L S_old - R| of calculate_residuals_optimized!."""
         self.calc_viscoelastic_terms()
         self.viscoelastic_rhs()
         self.build_system_of_equations()
         rep = self.solve_system(**solve_kw)
         self.process_stokes_solution()
+        self._call("eb_stokes_nonlinear_residual")
         return rep
+
+    def stokes_solution_processing(self) -> dict:
+        """StokesContinuitySolver.stokes_solution_processing! (StokesContinuitySolver.jl:113-136):
+        grid strain rate and spin, the post-Stokes grid and marker steps
+        (execute_post_stokes_solver_steps!: stress forecast and change, marker strain rate,
+        strain-rate ratio and pressure), the Stokes norms, and the backup of S, vx1, vy1, pr1.
+        Returns the norms."""
+        self.update_grid_strain_rate_and_spin()
+        self.forecast_viscoelastic_grid_stress()
+        self.calculate_deviatoric_grid_stress_change()
+        self.post_stokes_marker_gathers()
+        norms = self.calculate_stokes_norms()
+        self.backup_stokes_arrays()
+        return norms
+
+    def picard_loop_markers(self, nglobal: int, tolerance_picard: float, iuse_harmonic: int = 1,
+                            **solve_kw) -> list:
+        """PlasticityLoopMarkers.picard_loop (global_plasticity_loop/plasticity_loop/
+        plasticity_loop_markers/PlasticityLoopMarkers.jl:36-73): from the second iteration on,
+        re-yield the markers and re-average the viscosity; solve; process; stop at nglobal or when
+        dvxy_rel_L2 < tolerance_picard (LoopTermination.check_stop_global_loop_markers).
+        Returns one record per iteration (solve report and norms)."""
+        history = []
+        for iglobal in range(1, nglobal + 1):
+            if iglobal > 1:
+                self.backup_and_clear_viscosity_transport_arrays()
+                self.update_plastic_yielding()
+                self.interpolate_viscosity_to_transport_arrays()
+                self.interpolate_basic_viscoplastic_viscosity_to_pressure_grid(iuse_harmonic)
+            rep = self.solve_viscoelastic_stokes_continuity_equations(**solve_kw)
+            norms = self.stokes_solution_processing()
+            history.append({"iglobal": iglobal, **rep, **norms})
+            if iglobal == nglobal or norms["dvxy_rel_L2"] < tolerance_picard:
+                break
+        return history
 
     # ----------------------------------------------------- step sequences --
     def marker_cycle(self) -> None:

@@ -44,6 +44,10 @@ GRID_FIELDS = [
     "btopx", "bbottomx", "btopy", "bbottomy", "bleftx", "brightx", "blefty", "brighty",
     # post-solve grids
     "eii", "vxb", "vyb",
+    # previous Picard iterate
+    "vx1_old", "vy1_old", "pr1_old",
+    # nodal Picard variant (basic grid)
+    "etavp_buffer", "plastic_yield_buffer", "plastic_strain_rate_buffer", "yield_error", "eii_plastic_basic",
 ]
 GRID_ID = {n: i for i, n in enumerate(GRID_FIELDS)}
 
@@ -70,8 +74,13 @@ def grid_shape(name: str, xnum: int, ynum: int) -> tuple[int, int]:
         return (ynum + 1, xnum)
     if name == "RY1":
         return (ynum, xnum + 1)
-    if name in ("vxb", "vyb"):
+    if name in ("vxb", "vyb", "etavp_buffer", "plastic_yield_buffer", "plastic_strain_rate_buffer", "yield_error",
+                "eii_plastic_basic"):
         return (ynum, xnum)
+    if name == "vx1_old":
+        return (ynum + 1, xnum)
+    if name == "vy1_old":
+        return (ynum, xnum + 1)
     return (ynum - 1, xnum - 1)   # RC1, eii_plastic_pressure, eii
 
 
@@ -112,7 +121,21 @@ class StokesParams(C.Structure):
 
 class SolveOpts(C.Structure):
     _fields_ = [("rtol", C.c_double), ("max_iters", C.c_int32), ("restart", C.c_int32), ("mg_sweeps", C.c_int32),
-                ("use_initial_guess", C.c_int32)]
+                ("use_initial_guess", C.c_int32), ("method", C.c_int32)]
+
+
+class StokesNorms(C.Structure):
+    _fields_ = [(n, C.c_double) for n in (
+        "dsoluv1_abs_inf", "dsoluv1_rel_inf", "dsoluv1_abs_L2", "dsoluv1_rel_L2", "dvx1_abs_L2", "dvx1_rel_L2",
+        "dvy1_abs_L2", "dvy1_rel_L2", "dpr1_abs_L2", "dpr1_rel_L2", "dvxy_abs_inf", "dvxy_rel_inf", "dvxy_abs_L2",
+        "dvxy_rel_L2", "resnl_L2")]
+
+
+class MobileWall(C.Structure):
+    _fields_ = [(n, C.c_double) for n in (
+        "timesum", "velocity_internal_x", "x_left_mobile_wall", "x_right_mobile_wall", "y_top_mobile_wall",
+        "y_bottom_mobile_wall", "plate_extension_thickness", "plate_extension_width")] + [
+        ("no_yielding_in_plate_extension", C.c_int64)]
 
 
 class SolveReport(C.Structure):
@@ -124,9 +147,9 @@ STOKES_VECTORS = {"solution": 0, "rhs": 1, "solution_old": 2, "resnl": 3}
 
 STOKES_ENTRY_POINTS = [
     "eb_calc_viscoelastic_terms", "eb_viscoelastic_rhs", "eb_build_stokes_system", "eb_process_stokes_solution",
-    "eb_stokes_nonlinear_residual", "eb_backup_stokes_solution", "eb_update_grid_strain_rate_and_spin",
+    "eb_stokes_nonlinear_residual", "eb_backup_stokes_arrays", "eb_update_grid_strain_rate_and_spin",
     "eb_forecast_viscoelastic_grid_stress", "eb_calculate_deviatoric_grid_stress_change",
-    "eb_interpolate_stag_velocity_to_basic_grid",
+    "eb_interpolate_stag_velocity_to_basic_grid", "eb_apply_nodal_plastic_yielding",
 ]
 
 ENTRY_POINTS = [
@@ -145,6 +168,8 @@ ALL_SYMBOLS = [
     "eb_update_marker_viscoplastic_viscosity", "eb_profile_enable", "eb_profile_count", "eb_profile_entry",
     "eb_set_stokes_params", "eb_solve_stokes_system", "eb_stokes_apply", "eb_stokes_vector_upload",
     "eb_stokes_vector_download", "eb_stokes_stencil_download", "eb_stokes_pscale", "eb_stokes_size",
+    "eb_calculate_stokes_norms", "eb_interpolate_basic_viscoplastic_viscosity_to_pressure_grid",
+    "eb_update_nodes_for_plastic_yielding",
     "eb_marker_to_basic_grid_average_noalloc",
 ] + ENTRY_POINTS + STOKES_ENTRY_POINTS
 
@@ -192,6 +217,10 @@ def load(path: pathlib.Path | str | None = None) -> C.CDLL:
     lib.eb_stokes_vector_upload.argtypes = [vp, C.c_int, vp]
     lib.eb_stokes_vector_download.argtypes = [vp, C.c_int, vp]
     lib.eb_stokes_stencil_download.argtypes = [vp, vp]
+    lib.eb_calculate_stokes_norms.argtypes = [vp, C.POINTER(StokesNorms)]
+    lib.eb_interpolate_basic_viscoplastic_viscosity_to_pressure_grid.argtypes = [vp, C.c_int]
+    lib.eb_update_nodes_for_plastic_yielding.argtypes = [vp, C.POINTER(MobileWall), C.POINTER(C.c_int64),
+                                                         C.POINTER(C.c_double)]
     lib.eb_stokes_pscale.argtypes = [vp]
     lib.eb_stokes_pscale.restype = C.c_double
     lib.eb_stokes_size.argtypes = [vp]

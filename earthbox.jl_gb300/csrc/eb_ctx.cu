@@ -22,10 +22,10 @@ enum Shape { SH_B, SH_P, SH_VX, SH_VY, SH_BCX, SH_BCY, SH_BCX1, SH_BCY1 };
 static Shape grid_shape(int f) {
   if (f <= EB_G_PLASTIC_YIELD) return SH_B;
   if (f <= EB_G_PR1) return SH_P;
-  if (f == EB_G_VX1 || f == EB_G_RX1) return SH_VX;
-  if (f <= EB_G_WTNODES_VY || f == EB_G_RY1) return SH_VY;
-  if (f == EB_G_RC1 || f == EB_G_EII_PLASTIC_PRESSURE || f == EB_G_EII) return SH_P;
-  if (f == EB_G_VXB || f == EB_G_VYB) return SH_B;
+  if (f == EB_G_VX1 || f == EB_G_RX1 || f == EB_G_VX1_OLD) return SH_VX;
+  if (f <= EB_G_WTNODES_VY || f == EB_G_RY1 || f == EB_G_VY1_OLD) return SH_VY;
+  if (f == EB_G_RC1 || f == EB_G_EII_PLASTIC_PRESSURE || f == EB_G_EII || f == EB_G_PR1_OLD) return SH_P;
+  if (f == EB_G_VXB || f == EB_G_VYB || (f >= EB_G_ETAVP_BUFFER && f <= EB_G_EII_PLASTIC_BASIC)) return SH_B;
   if (f == EB_G_BTOPT || f == EB_G_BBOTTOMT || f == EB_G_BTOPX || f == EB_G_BBOTTOMX) return SH_BCX;
   if (f == EB_G_BTOPY || f == EB_G_BBOTTOMY) return SH_BCX1;
   if (f == EB_G_BLEFTX || f == EB_G_BRIGHTX) return SH_BCY1;

@@ -132,6 +132,9 @@ int launch_grid_strain_rate(eb_ctx* c);
 int launch_forecast_stress(eb_ctx* c);
 int launch_stress_change(eb_ctx* c);
 int launch_stag_to_basic(eb_ctx* c);
+int launch_harmonic_etan(eb_ctx* c);
+int launch_nodal_yield(eb_ctx* c, const eb_mobile_wall* w, double* d_partial, int* nblocks);
+int launch_apply_nodal_yield(eb_ctx* c);
 
 constexpr int kMaxSlots = 48;
 

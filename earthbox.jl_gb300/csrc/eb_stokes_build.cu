@@ -423,9 +423,182 @@ __global__ void k_stag_to_basic(int32_t xnum, int32_t ynum, const double* __rest
   A2(vyb, ynum, i, j) = (A2(vy1, ynum, i, j) + A2(vy1, ynum, i, j + 1)) / 2.0;
 }
 
+// HarmonicAverage.normal_viscosity_from_harmonic_avg_shear_viscosity! (HarmonicAverage.jl:20-51):
+// cells that yield (CheckPlasticYield.plastic_yielding, tolerance 0) take the harmonic mean of
+// their four corner etas1 (MathTools.harmonic4 with zero factors).
+__global__ void k_harmonic_etan(int32_t xnum, int32_t ynum, const double* __restrict__ etas1,
+                                const double* __restrict__ plastics, const double* __restrict__ plasticn,
+                                const double* __restrict__ pyield, double* __restrict__ etan1) {
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= (int64_t)(xnum - 1) * (ynum - 1)) return;
+  const int32_t i = (int32_t)(k % (ynum - 1)) + 1, j = (int32_t)(k / (ynum - 1)) + 1;
+  bool y = A2(plasticn, ynum - 1, i, j) > 0.0;
+  y = y || A2(plastics, ynum, i, j) > 0.0 || A2(plastics, ynum, i, j + 1) > 0.0 ||
+      A2(plastics, ynum, i + 1, j) > 0.0 || A2(plastics, ynum, i + 1, j + 1) > 0.0;
+  y = y || A2(pyield, ynum, i, j) > 0.0 || A2(pyield, ynum, i, j + 1) > 0.0 || A2(pyield, ynum, i + 1, j) > 0.0 ||
+      A2(pyield, ynum, i + 1, j + 1) > 0.0;
+  if (!y) return;
+  const double vinv = 1.0 / A2(etas1, ynum, i, j) + 1.0 / A2(etas1, ynum, i, j + 1) + 1.0 / A2(etas1, ynum, i + 1, j) +
+                      1.0 / A2(etas1, ynum, i + 1, j + 1) + 0.0 + 0.0 + 0.0 + 0.0;
+  if (vinv != 0.0) A2(etan1, ynum - 1, i, j) = 1.0 / (vinv / (4.0 + 0.0 + 0.0 + 0.0 + 0.0));
+}
+
+// ---- PlasticFailureNodes.jl:24-318 ------------------------------------------
+struct NodalYieldIn {
+  int32_t xnum, ynum;
+  int64_t ntimestep;
+  int32_t iuse_fluid, no_wall, no_plate;
+  double dt, timesum, eta_min, eta_max, y_sealevel;
+  double vix, xl, xr, yt, yb, pthick, pwidth;
+  const double *gx, *gy, *pyield, *etas1, *eta_flow, *mus1, *coh, *fric, *sxy2, *sxx2, *pr1;
+  double *yerr, *etavp, *psr, *pyield_new;
+};
+// interpolate_from_pressure_grid_to_basic_grid (:221-257)
+__device__ double p_to_basic(int32_t i, int32_t j, int32_t ynum, int32_t xnum, const double* a) {
+  const int32_t yp = ynum - 1;
+  if (1 < i && i < ynum && 1 < j && j < xnum)
+    return (A2(a, yp, i - 1, j - 1) + A2(a, yp, i, j - 1) + A2(a, yp, i - 1, j) + A2(a, yp, i, j)) / 4.0;
+  if (i == 1 && j == 1) return A2(a, yp, i, j);
+  if (i == ynum && j == 1) return A2(a, yp, i - 1, j);
+  if (i == ynum && j == xnum) return A2(a, yp, i - 1, j - 1);
+  if (i == 1 && j == xnum) return A2(a, yp, i, j - 1);
+  if (j == 1) return (A2(a, yp, i, j) + A2(a, yp, i - 1, j)) / 2.0;
+  if (j == xnum) return (A2(a, yp, i - 1, j - 1) + A2(a, yp, i, j - 1)) / 2.0;
+  if (i == 1) return (A2(a, yp, i, j) + A2(a, yp, i, j - 1)) / 2.0;
+  return (A2(a, yp, i - 1, j) + A2(a, yp, i - 1, j - 1)) / 2.0;
+}
+// One thread per basic node; per-block (count, sum err^2) in partial[2 * block].
+__global__ void k_nodal_yield(NodalYieldIn q, double* __restrict__ partial) {
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  double cnt = 0.0, esq = 0.0;
+  if (k < (int64_t)q.xnum * q.ynum) {
+    const int32_t i = (int32_t)(k % q.ynum) + 1, j = (int32_t)(k / q.ynum) + 1;
+    const int32_t Y = q.ynum;
+    const double vold = A2(q.etas1, Y, i, j), vflow = A2(q.eta_flow, Y, i, j), mu = A2(q.mus1, Y, i, j);
+    const double coh = A2(q.coh, Y, i, j);
+    const double fc = sin(A2(q.fric, Y, i, j) * (3.14159265358979323846 / 180.0));
+    double etavp = vflow, ynew = 0.0, psr = 0.0;
+    bool applicable = q.ntimestep > 0 && (coh > 0.0 || fc > 0.0);
+    const double xs = q.vix * q.timesum;
+    const double xn = q.gx[j - 1], yn = q.gy[i - 1];
+    if (q.no_wall && (q.xl + xs) <= xn && xn <= (q.xr + xs) && q.yt <= yn && yn <= q.yb) applicable = false;
+    if (q.no_plate) {
+      const double xl = q.xl + xs;
+      if (xl - q.pwidth <= xn && xn <= xl && q.yb - q.pthick <= yn && yn <= q.yb) applicable = false;
+    }
+    if (applicable) {
+      const double p = p_to_basic(i, j, Y, q.xnum, q.pr1);
+      const double sxx = p_to_basic(i, j, Y, q.xnum, q.sxx2), sxy = A2(q.sxy2, Y, i, j);
+      const double sii = sqrt(sxy * sxy + sxx * sxx);
+      const double sie = sii * (mu * q.dt + vold) / vold;
+      const double cphi = cos(asin(fc));
+      double sy;
+      if (q.iuse_fluid == 0) {
+        sy = coh * cphi + fc * p;
+      } else {
+        double depth = yn - q.y_sealevel;
+        if (depth < 0.0) depth = 0.0;
+        const double pf = 1000.0 * 9.81 * depth;
+        sy = (p < pf) ? coh * cphi : coh * cphi + fc * (p - pf);
+      }
+      if (sy < 0.0) sy = 0.0;
+      const bool at_yield = A2(q.pyield, Y, i, j) > 0;
+      bool counted = false;
+      if (at_yield) counted = true;
+      if (sy < sie) {
+        double vnew = q.dt * mu * sy / (sie - sy);
+        if (vnew < vflow) {
+          ynew = 1.0;
+          vnew = vnew > q.eta_min ? vnew : q.eta_min;
+          vnew = vnew < q.eta_max ? vnew : q.eta_max;
+          etavp = vnew;
+          psr = 0.5 * sii / vnew - 0.5 * sii / vflow;
+          counted = true;
+        }
+      }
+      if (counted) {
+        const double err = sii - sy;
+        A2(q.yerr, Y, i, j) = err;
+        cnt = 1.0;
+        esq = err * err;
+      }
+    }
+    A2(q.etavp, Y, i, j) = etavp;
+    A2(q.pyield_new, Y, i, j) = ynew;
+    A2(q.psr, Y, i, j) = psr;
+  }
+  __shared__ double sc[kB], se[kB];
+  sc[threadIdx.x] = cnt;
+  se[threadIdx.x] = esq;
+  __syncthreads();
+  for (int o = kB / 2; o > 0; o >>= 1) {
+    if ((int)threadIdx.x < o) { sc[threadIdx.x] += sc[threadIdx.x + o]; se[threadIdx.x] += se[threadIdx.x + o]; }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) { partial[2 * blockIdx.x] = sc[0]; partial[2 * blockIdx.x + 1] = se[0]; }
+}
+// PlasticStrainRateInterpolation.interpolate_at_pressure_nodes! (:13-40)
+__global__ void k_eii_plastic_pressure(int32_t xnum, int32_t ynum, const double* __restrict__ eb,
+                                       double* __restrict__ ep) {
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= (int64_t)(xnum - 1) * (ynum - 1)) return;
+  const int32_t i = (int32_t)(k % (ynum - 1)) + 1, j = (int32_t)(k / (ynum - 1)) + 1;
+  A2(ep, ynum - 1, i, j) = (A2(eb, ynum, i, j) + A2(eb, ynum, i, j + 1) + A2(eb, ynum, i + 1, j) +
+                            A2(eb, ynum, i + 1, j + 1)) / 4.0;
+}
+
 unsigned nblk(int64_t n) { return (unsigned)((n + kB - 1) / kB); }
 
 }  // namespace
+
+int launch_nodal_yield(eb_ctx* c, const eb_mobile_wall* w, double* d_partial, int* nblocks) {
+  double** g = c->gf;
+  NodalYieldIn q{};
+  q.xnum = c->xnum; q.ynum = c->ynum; q.ntimestep = c->P.ntimestep;
+  q.iuse_fluid = (int32_t)c->P.iuse_fluid_pressure_for_yield; q.no_wall = (int32_t)(c->P.no_yielding_in_mobile_wall != 0);
+  q.dt = c->P.timestep; q.eta_min = c->P.viscosity_min; q.eta_max = c->P.viscosity_max; q.y_sealevel = c->P.y_sealevel;
+  if (w) {
+    q.no_plate = (int32_t)(w->no_yielding_in_plate_extension != 0);
+    q.timesum = w->timesum; q.vix = w->velocity_internal_x;
+    q.xl = w->x_left_mobile_wall; q.xr = w->x_right_mobile_wall; q.yt = w->y_top_mobile_wall; q.yb = w->y_bottom_mobile_wall;
+    q.pthick = w->plate_extension_thickness; q.pwidth = w->plate_extension_width;
+  } else {
+    q.no_wall = 0;
+  }
+  q.gx = c->g.gx; q.gy = c->g.gy;
+  q.pyield = g[EB_G_PLASTIC_YIELD]; q.etas1 = g[EB_G_ETAS1]; q.eta_flow = g[EB_G_ETA_FLOW]; q.mus1 = g[EB_G_MUS1];
+  q.coh = g[EB_G_COHESION]; q.fric = g[EB_G_FRIC_DEG]; q.sxy2 = g[EB_G_SXY2]; q.sxx2 = g[EB_G_SXX2]; q.pr1 = g[EB_G_PR1];
+  q.yerr = g[EB_G_YIELD_ERROR]; q.etavp = g[EB_G_ETAVP_BUFFER]; q.psr = g[EB_G_PLASTIC_STRAIN_RATE_BUFFER];
+  q.pyield_new = g[EB_G_PLASTIC_YIELD_BUFFER];
+  *nblocks = (int)nblk((int64_t)c->xnum * c->ynum);
+  EB_PROF(c, "k_nodal_yield");
+  k_nodal_yield<<<*nblocks, kB, 0, c->stream>>>(q, d_partial);
+  EB_LAUNCHED(c);
+  return EB_OK;
+}
+
+int launch_apply_nodal_yield(eb_ctx* c) {
+  double** g = c->gf;
+  const size_t nb = (size_t)c->xnum * c->ynum * sizeof(double);
+  EB_CK(c, cudaMemcpyAsync(g[EB_G_ETAS1], g[EB_G_ETAVP_BUFFER], nb, cudaMemcpyDeviceToDevice, c->stream));
+  EB_CK(c, cudaMemcpyAsync(g[EB_G_PLASTIC_YIELD], g[EB_G_PLASTIC_YIELD_BUFFER], nb, cudaMemcpyDeviceToDevice, c->stream));
+  EB_CK(c, cudaMemcpyAsync(g[EB_G_EII_PLASTIC_BASIC], g[EB_G_PLASTIC_STRAIN_RATE_BUFFER], nb, cudaMemcpyDeviceToDevice,
+                           c->stream));
+  EB_PROF(c, "k_eii_plastic_pressure");
+  k_eii_plastic_pressure<<<nblk((int64_t)(c->xnum - 1) * (c->ynum - 1)), kB, 0, c->stream>>>(
+      c->xnum, c->ynum, g[EB_G_EII_PLASTIC_BASIC], g[EB_G_EII_PLASTIC_PRESSURE]);
+  EB_LAUNCHED(c);
+  return EB_OK;
+}
+
+int launch_harmonic_etan(eb_ctx* c) {
+  double** g = c->gf;
+  EB_PROF(c, "k_harmonic_etan");
+  k_harmonic_etan<<<nblk((int64_t)(c->xnum - 1) * (c->ynum - 1)), kB, 0, c->stream>>>(
+      c->xnum, c->ynum, g[EB_G_ETAS1], g[EB_G_PLASTICS], g[EB_G_PLASTICN], g[EB_G_PLASTIC_YIELD], g[EB_G_ETAN1]);
+  EB_LAUNCHED(c);
+  return EB_OK;
+}
 
 int launch_grid_strain_rate(eb_ctx* c) {
   double** g = c->gf;

@@ -188,14 +188,6 @@ __global__ void k_scale_copy(double* dst, const double* src, double a, int64_t n
   const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (k < n) dst[k] = a * src[k];
 }
-// Zk = (float) z and z = (double) Zk: the direction is kept exactly as stored
-__global__ void k_round_dir(double* __restrict__ z, float* __restrict__ Zk, int64_t n) {
-  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= n) return;
-  const float f = (float)z[k];
-  Zk[k] = f;
-  z[k] = (double)f;
-}
 // u -= sum_v h[v] Z_v (FP32 directions)
 __global__ void k_maxpy_f32(double* __restrict__ u, const float* __restrict__ Z, int64_t stride,
                             const double* __restrict__ h, int nv, int64_t n) {
@@ -204,6 +196,25 @@ __global__ void k_maxpy_f32(double* __restrict__ u, const float* __restrict__ Z,
   double s = u[k];
   for (int v = 0; v < nv; ++v) s -= h[v] * (double)Z[(int64_t)v * stride + k];
   u[k] = s;
+}
+// BiCGStab vector updates
+__global__ void k_bicg_p(double* __restrict__ p, const double* __restrict__ r, const double* __restrict__ v, double beta,
+                         double omega, int64_t n) {
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < n) p[k] = r[k] + beta * (p[k] - omega * v[k]);
+}
+__global__ void k_bicg_s(double* __restrict__ s, const double* __restrict__ r, const double* __restrict__ v, double alpha,
+                         int64_t n) {
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < n) s[k] = r[k] - alpha * v[k];
+}
+__global__ void k_bicg_xr(double* __restrict__ x, double* __restrict__ r, const double* __restrict__ ph,
+                          const double* __restrict__ sh, const double* __restrict__ s, const double* __restrict__ t,
+                          double alpha, double omega, int64_t n) {
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  x[k] += alpha * ph[k] + omega * sh[k];
+  r[k] = s[k] - omega * t[k];
 }
 // dst = a - b (elementwise)
 __global__ void k_sub(double* __restrict__ dst, const double* __restrict__ a, const double* __restrict__ b, int64_t n) {
@@ -521,28 +532,40 @@ __global__ void __launch_bounds__(kCoarseThreads) k_coarse_cycle(const LevelDev*
   }
 }
 
-// preconditioner input: z_p = prep r_p; f = r_u - L_up z_p (FP32, level 0).  r, z are unscaled here.
-__global__ void k_prec_in(const double* __restrict__ coef, const double* __restrict__ r, const double* __restrict__ prep,
-                          double* __restrict__ zp, float* __restrict__ fx, float* __restrict__ fy, int32_t nx, int32_t ny) {
+// Preconditioner input, on the scaled residual rhat (r = rhat ./ w):
+// z_p = prep r_p, stored scaled and rounded to FP32 (zhat_p = fl32(z_p / w_p));
+// level-0 right-hand side f = r_u - L_up z_p (FP32).
+__global__ void k_prec_in(const double* __restrict__ coef, const double* __restrict__ rhat,
+                          const double* __restrict__ w, const double* __restrict__ prep, double* __restrict__ zt,
+                          float* __restrict__ Zk, float* __restrict__ fx, float* __restrict__ fy, int32_t nx,
+                          int32_t ny) {
   const int64_t nc = (int64_t)nx * ny;
   const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= nc) return;
   const int32_t i = (int32_t)(c % ny), j = (int32_t)(c / ny);
-  auto z = [&](int64_t k) { return prep[k] * r[2 * nc + k]; };
+  auto z = [&](int64_t k) { return prep[k] * (rhat[2 * nc + k] / w[2 * nc + k]); };
   const double zc = z(c);
-  zp[c] = zc;
+  const float zs = (float)(zc / w[2 * nc + c]);
+  Zk[2 * nc + c] = zs;
+  zt[2 * nc + c] = (double)zs;
   double gx = coef[9 * nc + c] * zc;
   if (j < nx - 1) gx += coef[10 * nc + c] * z(c + ny);
   double gy = coef[20 * nc + c] * zc;
   if (i < ny - 1) gy += coef[21 * nc + c] * z(c + 1);
-  fx[c] = (float)(r[c] - gx);
-  fy[c] = (float)(r[nc + c] - gy);
+  fx[c] = (float)(rhat[c] / w[c] - gx);
+  fy[c] = (float)(rhat[nc + c] / w[nc + c] - gy);
 }
-__global__ void k_prec_out(const float* __restrict__ ux, const float* __restrict__ uy, double* __restrict__ z, int64_t nc) {
+// Preconditioner output: zhat_u = fl32(u / w_u), kept in FP32 (Zk) and FP64 (zt).
+__global__ void k_prec_out(const float* __restrict__ ux, const float* __restrict__ uy, const double* __restrict__ w,
+                           double* __restrict__ zt, float* __restrict__ Zk, int64_t nc) {
   const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= nc) return;
-  z[c] = (double)ux[c];
-  z[nc + c] = (double)uy[c];
+  const float zx = (float)((double)ux[c] / w[c]);
+  const float zy = (float)((double)uy[c] / w[nc + c]);
+  Zk[c] = zx;
+  Zk[nc + c] = zy;
+  zt[c] = (double)zx;
+  zt[nc + c] = (double)zy;
 }
 
 // ------------------------------------------------------ host geometry ---
@@ -999,26 +1022,20 @@ int capture_vcycle(eb_ctx* c, StokesState* st, int sweeps) {
   return EB_OK;
 }
 
-// z = W^-1 M^-1 W^-1 rhat  (rhat, z: SoA FP64 of 3 nc)
-int precondition(eb_ctx* c, StokesState* st, const double* rhat, double* z) {
+// zhat = W^-1 M^-1 W^-1 rhat (rhat: SoA FP64 of 3 nc), rounded to FP32: kept in Zk (the
+// stored direction) and zt (its FP64 copy, the input of the operator product).
+int precondition(eb_ctx* c, StokesState* st, const double* rhat, double* zt, float* Zk) {
   const StokesSystem& s = st->sys;
-  const int64_t n3 = 3 * s.nc;
   Level& v = st->levels[0];
   EB_PROF(c, "k_precond");
-  k_mul<<<nblk(n3), kB, 0, c->stream>>>(st->t, rhat, st->w, n3, 1);  // r = rhat ./ w
-  EB_LAUNCHED(c);
-  EB_PROF(c, "k_precond");
-  k_prec_in<<<nblk(s.nc), kB, 0, c->stream>>>(s.coef, st->t, st->prep, z + 2 * s.nc, v.fx, v.fy, s.nx, s.ny);
+  k_prec_in<<<nblk(s.nc), kB, 0, c->stream>>>(s.coef, rhat, st->w, st->prep, zt, Zk, v.fx, v.fy, s.nx, s.ny);
   EB_LAUNCHED(c);
   EB_PROF(c, "vcycle_graph");
   EB_CK(c, cudaGraphLaunch(st->gexec, c->stream));
   c->launches += st->graph_kernels - 1;
   EB_LAUNCHED(c);
   EB_PROF(c, "k_precond");
-  k_prec_out<<<nblk(s.nc), kB, 0, c->stream>>>(v.ux, v.uy, z, s.nc);
-  EB_LAUNCHED(c);
-  EB_PROF(c, "k_precond");
-  k_mul<<<nblk(n3), kB, 0, c->stream>>>(z, z, st->w, n3, 1);  // z ./ w
+  k_prec_out<<<nblk(s.nc), kB, 0, c->stream>>>(v.ux, v.uy, st->w, zt, Zk, s.nc);
   EB_LAUNCHED(c);
   return EB_OK;
 }
@@ -1098,7 +1115,8 @@ extern "C" int eb_solve_stokes_system(eb_ctx* c, const eb_solve_opts* o, eb_solv
   if (opt.max_iters <= 0) opt.max_iters = 3000;
   if (opt.restart <= 0) opt.restart = 250;
   if (opt.mg_sweeps <= 0) opt.mg_sweeps = 2;
-  const int m = std::min(opt.restart, kMaxRestart);
+  if (opt.method != 1) opt.method = 0;
+  const int m = std::max(std::min(opt.restart, kMaxRestart), opt.method == 1 ? 6 : 1);
   const int64_t n3 = 3 * s.nc;
   B2 b2;
   if ((rc = ensure_solver(c, st, m)) || (rc = read_b2(c, &b2))) return rc;
@@ -1129,7 +1147,55 @@ extern "C" int eb_solve_stokes_system(eb_ctx* c, const eb_solve_opts* o, eb_solv
   int it = 0, reorth = 0;
   double est = 1.0;
   bool converged = (bnorm == 0.0);
-  while (!converged && it < opt.max_iters) {
+  if (opt.method == 1 && !converged) {
+    // Right-preconditioned BiCGStab on the scaled system.  Basis slots hold its vectors:
+    // 0 r0hat, 1 r (adjacent: one reduction gives r0hat.r and r.r), 2 s, 3 t (s.t, t.t),
+    // 4 p, 5 v, 6 shat; phat is zt.  The FP32 copy of each preconditioned vector goes to Z.
+    double *rh0 = st->V, *r = st->V + n3, *sv = st->V + 2 * n3, *tv = st->V + 3 * n3, *p = st->V + 4 * n3,
+           *v = st->V + 5 * n3, *sh = st->V + 6 * n3, *ph = st->zt;
+    if ((rc = apply_scaled(c, st, st->xs, st->t))) return rc;
+    EB_PROF(c, "k_axpy");
+    k_sub<<<nblk(n3), kB, 0, c->stream>>>(r, st->bs, st->t, n3);
+    EB_LAUNCHED(c);
+    EB_CK(c, cudaMemcpyAsync(rh0, r, n3 * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
+    EB_CK(c, cudaMemsetAsync(p, 0, n3 * sizeof(double), c->stream));
+    EB_CK(c, cudaMemsetAsync(v, 0, n3 * sizeof(double), c->stream));
+    double rho = 1.0, alpha = 1.0, omega = 1.0, d2[2];
+    if ((rc = mdot(c, st, rh0, n3, 2, r, d2))) return rc;
+    double rho_new = d2[0];
+    est = std::sqrt(d2[1]) / bnorm;
+    converged = est <= opt.rtol;
+    while (!converged && it < opt.max_iters) {
+      if (rho_new == 0.0 || omega == 0.0 || !std::isfinite(rho_new))
+        return eb_fail(c, std::isfinite(rho_new) ? EB_NOT_CONVERGED : EB_NAN, "BiCGStab breakdown");
+      const double beta = (rho_new / rho) * (alpha / omega);
+      rho = rho_new;
+      EB_PROF(c, "k_axpy");
+      k_bicg_p<<<nblk(n3), kB, 0, c->stream>>>(p, r, v, beta, omega, n3);
+      EB_LAUNCHED(c);
+      if ((rc = precondition(c, st, p, ph, st->Z)) || (rc = apply_scaled(c, st, ph, v))) return rc;
+      double rv;
+      if ((rc = mdot(c, st, rh0, 0, 1, v, &rv))) return rc;
+      alpha = rho / rv;
+      EB_PROF(c, "k_axpy");
+      k_bicg_s<<<nblk(n3), kB, 0, c->stream>>>(sv, r, v, alpha, n3);
+      EB_LAUNCHED(c);
+      if ((rc = precondition(c, st, sv, sh, st->Z)) || (rc = apply_scaled(c, st, sh, tv))) return rc;
+      double st2[2];
+      if ((rc = mdot(c, st, sv, n3, 2, tv, st2))) return rc;  // s.t, t.t
+      omega = st2[1] > 0.0 ? st2[0] / st2[1] : 0.0;
+      EB_PROF(c, "k_axpy");
+      k_bicg_xr<<<nblk(n3), kB, 0, c->stream>>>(st->xs, r, ph, sh, sv, tv, alpha, omega, n3);
+      EB_LAUNCHED(c);
+      ++it;
+      if ((rc = mdot(c, st, rh0, n3, 2, r, d2))) return rc;
+      rho_new = d2[0];
+      est = std::sqrt(d2[1]) / bnorm;
+      if (!std::isfinite(est)) return eb_fail(c, EB_NAN, "BiCGStab residual became NaN/Inf");
+      converged = est <= opt.rtol;
+    }
+  }
+  while (opt.method != 1 && !converged && it < opt.max_iters) {
     // r = bhat - Khat xhat
     if ((rc = apply_scaled(c, st, st->xs, st->t))) return rc;
     EB_PROF(c, "k_axpy");
@@ -1151,11 +1217,7 @@ extern "C" int eb_solve_stokes_system(eb_ctx* c, const eb_solve_opts* o, eb_solv
       double* vk = st->V + (size_t)k * n3;
       float* zk = st->Z + (size_t)k * n3;
       double* w = st->V + (size_t)(k + 1) * n3;
-      if ((rc = precondition(c, st, vk, st->zt))) return rc;
-      EB_PROF(c, "k_axpy");
-      k_round_dir<<<nblk(n3), kB, 0, c->stream>>>(st->zt, zk, n3);
-      EB_LAUNCHED(c);
-      if ((rc = apply_scaled(c, st, st->zt, w))) return rc;
+      if ((rc = precondition(c, st, vk, st->zt, zk)) || (rc = apply_scaled(c, st, st->zt, w))) return rc;
       // Classical Gram-Schmidt.  One reduction gives V^T w and |w|^2 (w is the slot after V_k);
       // the projected norm follows from Pythagoras unless cancellation is large, in which
       // case a second pass re-orthogonalises and the norm is measured.
@@ -1346,6 +1408,43 @@ extern "C" int eb_forecast_viscoelastic_grid_stress(eb_ctx* c) {
 extern "C" int eb_calculate_deviatoric_grid_stress_change(eb_ctx* c) {
   return grid_step(c, {EB_G_SXY2, EB_G_SXY1, EB_G_DSXY, EB_G_SXX2, EB_G_SXX1, EB_G_DSXX}, launch_stress_change);
 }
+extern "C" int eb_interpolate_basic_viscoplastic_viscosity_to_pressure_grid(eb_ctx* c, int iuse_harmonic) {
+  if (iuse_harmonic != 1) return c ? EB_OK : EB_BAD_INPUT;
+  return grid_step(c, {EB_G_ETAS1, EB_G_PLASTICS, EB_G_PLASTICN, EB_G_PLASTIC_YIELD, EB_G_ETAN1}, launch_harmonic_etan);
+}
+
+extern "C" int eb_update_nodes_for_plastic_yielding(eb_ctx* c, const eb_mobile_wall* w, int64_t* nnode_yield,
+                                                    double* global_yield_error) {
+  if (!c) return EB_BAD_INPUT;
+  if (!c->have_grid || !c->have_params) return eb_fail(c, EB_NOT_READY, "eb_set_grid and eb_set_params come first");
+  cudaSetDevice(c->device);
+  int rc = need_fields(c, {EB_G_PLASTIC_YIELD, EB_G_ETAS1, EB_G_ETA_FLOW, EB_G_MUS1, EB_G_COHESION, EB_G_FRIC_DEG,
+                           EB_G_SXY2, EB_G_SXX2, EB_G_PR1, EB_G_YIELD_ERROR, EB_G_ETAVP_BUFFER,
+                           EB_G_PLASTIC_STRAIN_RATE_BUFFER, EB_G_PLASTIC_YIELD_BUFFER});
+  if (rc) return rc;
+  // per-block partial sums go to the context's per-cell scratch (kMaxSlots floats per cell,
+  // far more than 2 doubles per 256 basic nodes)
+  double* d_part = reinterpret_cast<double*>(c->part);
+  int nb = 0;
+  if ((rc = launch_nodal_yield(c, w, d_part, &nb))) return rc;
+  std::vector<double> h(2 * (size_t)nb);
+  EB_CK(c, cudaMemcpyAsync(h.data(), d_part, h.size() * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  EB_CK(c, cudaStreamSynchronize(c->stream));
+  prof_resolve(c);
+  double cnt = 0.0, esum = 0.0;
+  for (int b = 0; b < nb; ++b) { cnt += h[2 * b]; esum += h[2 * b + 1]; }
+  const int64_t n = (int64_t)cnt;
+  if (nnode_yield) *nnode_yield = n;
+  if (global_yield_error) *global_yield_error = n > 0 ? std::sqrt(esum / (double)n) : 0.0;
+  return EB_OK;
+}
+
+extern "C" int eb_apply_nodal_plastic_yielding(eb_ctx* c) {
+  return grid_step(c, {EB_G_ETAS1, EB_G_ETAVP_BUFFER, EB_G_PLASTIC_YIELD, EB_G_PLASTIC_YIELD_BUFFER,
+                       EB_G_EII_PLASTIC_BASIC, EB_G_PLASTIC_STRAIN_RATE_BUFFER, EB_G_EII_PLASTIC_PRESSURE},
+                   launch_apply_nodal_yield);
+}
+
 extern "C" int eb_interpolate_stag_velocity_to_basic_grid(eb_ctx* c) {
   return grid_step(c, {EB_G_VX1, EB_G_VY1, EB_G_VXB, EB_G_VYB}, launch_stag_to_basic);
 }
@@ -1375,12 +1474,92 @@ extern "C" int eb_stokes_nonlinear_residual(eb_ctx* c) {
   return EB_OK;
 }
 
-extern "C" int eb_backup_stokes_solution(eb_ctx* c) {
+extern "C" int eb_backup_stokes_arrays(eb_ctx* c) {
   int rc = need_system(c, false);
-  if (rc) return rc;
+  if (rc || (rc = need_fields(c, {EB_G_VX1, EB_G_VY1, EB_G_PR1, EB_G_VX1_OLD, EB_G_VY1_OLD, EB_G_PR1_OLD}))) return rc;
   StokesSystem& s = c->st->sys;
   EB_CK(c, cudaMemcpyAsync(s.S_old, s.S, 3 * s.nc * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
+  const int pairs[3][2] = {{EB_G_VX1, EB_G_VX1_OLD}, {EB_G_VY1, EB_G_VY1_OLD}, {EB_G_PR1, EB_G_PR1_OLD}};
+  for (const auto& pr : pairs)
+    EB_CK(c, cudaMemcpyAsync(c->gf[pr[1]], c->gf[pr[0]], grid_field_count(c, pr[0]) * sizeof(double),
+                             cudaMemcpyDeviceToDevice, c->stream));
   EB_CK(c, cudaStreamSynchronize(c->stream));
+  return EB_OK;
+}
+
+namespace {
+// Per block: sum (a-b)^2, max |a-b|, sum a^2, max |a| (b may be null: b = 0).
+__global__ void k_diff_norms(const double* __restrict__ a, const double* __restrict__ b, int64_t n,
+                             double* __restrict__ partial) {
+  double sd = 0.0, md = 0.0, sa = 0.0, ma = 0.0;
+  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
+    const double x = a[k], d = fabs((b ? b[k] : 0.0) - x);
+    sd += d * d;
+    md = fmax(md, d);
+    sa += x * x;
+    ma = fmax(ma, fabs(x));
+  }
+  __shared__ double sh[4][kB];
+  sh[0][threadIdx.x] = sd; sh[1][threadIdx.x] = md; sh[2][threadIdx.x] = sa; sh[3][threadIdx.x] = ma;
+  __syncthreads();
+  for (int o = kB / 2; o > 0; o >>= 1) {
+    if ((int)threadIdx.x < o) {
+      sh[0][threadIdx.x] += sh[0][threadIdx.x + o];
+      sh[1][threadIdx.x] = fmax(sh[1][threadIdx.x], sh[1][threadIdx.x + o]);
+      sh[2][threadIdx.x] += sh[2][threadIdx.x + o];
+      sh[3][threadIdx.x] = fmax(sh[3][threadIdx.x], sh[3][threadIdx.x + o]);
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x < 4) partial[(int64_t)blockIdx.x * 4 + threadIdx.x] = sh[threadIdx.x][0];
+}
+}  // namespace
+
+// {sum d^2, max d, sum a^2, max a} over the whole array, reduced on the host in block order
+static int diff_norms(eb_ctx* c, const double* a, const double* b, int64_t n, double out[4]) {
+  constexpr int nb = 2 * 152;
+  double* part = c->st->tmp;  // 3 nc >= 4 nb doubles for every grid of at least 3x3 nodes
+  EB_PROF(c, "k_diff_norms");
+  k_diff_norms<<<nb, kB, 0, c->stream>>>(a, b, n, part);
+  EB_LAUNCHED(c);
+  std::vector<double> h(4 * nb);
+  EB_CK(c, cudaMemcpyAsync(h.data(), part, h.size() * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  EB_CK(c, cudaStreamSynchronize(c->stream));
+  out[0] = out[1] = out[2] = out[3] = 0.0;
+  for (int k = 0; k < nb; ++k) {
+    out[0] += h[4 * k];
+    out[1] = std::max(out[1], h[4 * k + 1]);
+    out[2] += h[4 * k + 2];
+    out[3] = std::max(out[3], h[4 * k + 3]);
+  }
+  return EB_OK;
+}
+
+extern "C" int eb_calculate_stokes_norms(eb_ctx* c, eb_stokes_norms* o) {
+  int rc = need_system(c, false);
+  if (rc || (rc = need_fields(c, {EB_G_VX1, EB_G_VY1, EB_G_PR1, EB_G_VX1_OLD, EB_G_VY1_OLD, EB_G_PR1_OLD}))) return rc;
+  if (!o) return eb_fail(c, EB_BAD_INPUT, "null norms pointer");
+  if (3 * c->st->sys.nc < 4 * 2 * 152) return eb_fail(c, EB_BAD_INPUT, "grid too small for the norm reduction");
+  StokesSystem& s = c->st->sys;
+  double S4[4], X4[4], Y4[4], P4[4], R4[4];
+  if ((rc = diff_norms(c, s.S, s.S_old, 3 * s.nc, S4)) ||
+      (rc = diff_norms(c, c->gf[EB_G_VX1], c->gf[EB_G_VX1_OLD], (int64_t)grid_field_count(c, EB_G_VX1), X4)) ||
+      (rc = diff_norms(c, c->gf[EB_G_VY1], c->gf[EB_G_VY1_OLD], (int64_t)grid_field_count(c, EB_G_VY1), Y4)) ||
+      (rc = diff_norms(c, c->gf[EB_G_PR1], c->gf[EB_G_PR1_OLD], (int64_t)grid_field_count(c, EB_G_PR1), P4)) ||
+      (rc = diff_norms(c, s.resnl, nullptr, 3 * s.nc, R4)))
+    return rc;
+  prof_resolve(c);
+  // MathTools.get_L2_norms / get_inf_norms: rel = abs / |v|, or 1e38 when |v| = 0
+  auto rel = [](double a, double v) { return v != 0.0 ? a / v : 1e38; };
+  o->dsoluv1_abs_inf = S4[1]; o->dsoluv1_rel_inf = rel(S4[1], S4[3]);
+  o->dsoluv1_abs_L2 = std::sqrt(S4[0]); o->dsoluv1_rel_L2 = rel(std::sqrt(S4[0]), std::sqrt(S4[2]));
+  o->dvx1_abs_L2 = std::sqrt(X4[0]); o->dvx1_rel_L2 = rel(std::sqrt(X4[0]), std::sqrt(X4[2]));
+  o->dvy1_abs_L2 = std::sqrt(Y4[0]); o->dvy1_rel_L2 = rel(std::sqrt(Y4[0]), std::sqrt(Y4[2]));
+  o->dpr1_abs_L2 = std::sqrt(P4[0]); o->dpr1_rel_L2 = rel(std::sqrt(P4[0]), std::sqrt(P4[2]));
+  const double vi = std::max(X4[1], Y4[1]), vmax = std::max(X4[3], Y4[3]);
+  o->dvxy_abs_inf = vi; o->dvxy_rel_inf = rel(vi, vmax);
+  o->dvxy_abs_L2 = std::sqrt(X4[0] + Y4[0]); o->dvxy_rel_L2 = rel(std::sqrt(X4[0] + Y4[0]), std::sqrt(X4[2] + Y4[2]));
+  o->resnl_L2 = std::sqrt(R4[2]);
   return EB_OK;
 }
 

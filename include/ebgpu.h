@@ -142,6 +142,12 @@ enum eb_grid_field {
   EB_G_BLEFTX, EB_G_BRIGHTX, EB_G_BLEFTY, EB_G_BRIGHTY,
   /* post-solve grids: strain-rate invariant eii (P), velocity at basic nodes vxb, vyb (B) */
   EB_G_EII, EB_G_VXB, EB_G_VYB,
+  /* previous Picard iterate (SystemSolver.backup_stokes_arrays!): vx1_old (VX), vy1_old (VY), pr1_old (P) */
+  EB_G_VX1_OLD, EB_G_VY1_OLD, EB_G_PR1_OLD,
+  /* nodal Picard variant (all basic grid): etavp_buffer, plastic_yield_buffer,
+   * plastic_strain_rate_buffer, yield_error, eii_plastic_basic */
+  EB_G_ETAVP_BUFFER, EB_G_PLASTIC_YIELD_BUFFER, EB_G_PLASTIC_STRAIN_RATE_BUFFER, EB_G_YIELD_ERROR,
+  EB_G_EII_PLASTIC_BASIC,
   EB_G_NFIELDS
 };
 
@@ -284,6 +290,8 @@ typedef struct eb_solve_opts {
   int32_t restart;           /* Krylov basis size; 0 -> 40                                             */
   int32_t mg_sweeps;         /* red-black Gauss-Seidel sweeps before/after each coarse correction; 0 -> 2 */
   int32_t use_initial_guess; /* 1: start from the current device solution vector, 0: from zero         */
+  int32_t method;            /* 0: FGMRES (long recurrence, robust); 1: BiCGStab (short recurrence, two
+                                preconditioner applications per iteration)                           */
 } eb_solve_opts;
 
 typedef struct eb_solve_report {
@@ -329,8 +337,20 @@ int eb_process_stokes_solution(eb_ctx* ctx);
  * resnl = |L S_old - R|, kept as EB_SV_RESNL. */
 int eb_stokes_nonlinear_residual(eb_ctx* ctx);
 
-/* The solution-vector part of SystemSolver.backup_stokes_arrays!  (SystemSolver.jl:306-318): S_old = S. */
-int eb_backup_stokes_solution(eb_ctx* ctx);
+/* SystemSolver.backup_stokes_arrays!  (SystemSolver.jl:306-318): S_old = S, vx1_old = vx1,
+ * vy1_old = vy1, pr1_old = pr1 (vxy_old is vx1_old and vy1_old in row-major order). */
+int eb_backup_stokes_arrays(eb_ctx* ctx);
+
+/* StokesNorms.calculate_stokes_norms! (solver/norms/StokesNorms.jl:8-160) without the grid residual
+ * arrays: the solution-change norms of calculate_solution_norms! (:64-120, MathTools.get_L2_norms /
+ * get_inf_norms: abs = |v - v_old|, rel = abs / |v| or 1e38 when |v| = 0) and |resnl|_2. */
+typedef struct eb_stokes_norms {
+  double dsoluv1_abs_inf, dsoluv1_rel_inf, dsoluv1_abs_L2, dsoluv1_rel_L2;
+  double dvx1_abs_L2, dvx1_rel_L2, dvy1_abs_L2, dvy1_rel_L2, dpr1_abs_L2, dpr1_rel_L2;
+  double dvxy_abs_inf, dvxy_rel_inf, dvxy_abs_L2, dvxy_rel_L2;
+  double resnl_L2;
+} eb_stokes_norms;
+int eb_calculate_stokes_norms(eb_ctx* ctx, eb_stokes_norms* out);
 
 /* Post-solve grid kernels (src/stokes_continuity_solver/utils/):
  * GridStrainRate.update_grid_strain_rate_and_spin! (strain_rate/GridStrainRate.jl:6-182): exx, exy, eii, esp */
@@ -339,8 +359,36 @@ int eb_update_grid_strain_rate_and_spin(eb_ctx* ctx);
 int eb_forecast_viscoelastic_grid_stress(eb_ctx* ctx);
 /* GridStress.calculate_deviatoric_grid_stress_change! (GridStress.jl:128-134): dsxy, dsxx */
 int eb_calculate_deviatoric_grid_stress_change(eb_ctx* ctx);
+/* Interpolation.interpolate_basic_viscoplastic_viscosity_to_pressure_grid! (src/interpolation/Interpolation.jl:97-108):
+ * when iuse_harmonic (interp_options.iuse_harmonic_avg_normal_viscosity) is 1, yielding cells take
+ * etan1 = harmonic mean of their corner etas1 (HarmonicAverage.jl:20-51); otherwise nothing happens. */
+int eb_interpolate_basic_viscoplastic_viscosity_to_pressure_grid(eb_ctx* ctx, int iuse_harmonic);
 /* StokesInterpolate.interpolate_stag_velocity_to_basic_grid! (StokesInterpolate.jl:16-33): vxb, vyb */
 int eb_interpolate_stag_velocity_to_basic_grid(eb_ctx* ctx);
+
+/* Nodal Picard variant (itype_global = 1). */
+typedef struct eb_mobile_wall {
+  double  timesum;                     /* model time (s): walls move with velocity_internal_x         */
+  double  velocity_internal_x;
+  double  x_left_mobile_wall, x_right_mobile_wall, y_top_mobile_wall, y_bottom_mobile_wall;
+  double  plate_extension_thickness, plate_extension_width;
+  int64_t no_yielding_in_plate_extension;
+} eb_mobile_wall;
+
+/* PlasticFailureNodes.update_nodes_for_plastic_yielding (rheology/plastic_failure/nodes/
+ * PlasticFailureNodes.jl:24-184): Drucker-Prager yield on the basic grid from etas1, eta_flow, mus1,
+ * cohesion_grid, fric_degrees_grid, plastic_yield, sxy2, sxx2, pr1.  Writes etavp_buffer,
+ * plastic_yield_buffer, plastic_strain_rate_buffer and yield_error (at yielding nodes), and returns
+ * nnode_yield and global_yield_error = sqrt(sum err^2 / nnode_yield).  `wall` may be NULL (no mobile
+ * wall); eb_params.no_yielding_in_mobile_wall switches the wall test on. */
+int eb_update_nodes_for_plastic_yielding(eb_ctx* ctx, const eb_mobile_wall* wall, int64_t* nnode_yield,
+                                         double* global_yield_error);
+
+/* The updates PlasticityLoopNodes.picard_loop makes when nnode_yield > 0
+ * (plasticity_loop_nodes/PlasticityLoopNodes.jl:36-92, :128-152): etas1 = etavp_buffer,
+ * plastic_yield = plastic_yield_buffer, eii_plastic_basic = plastic_strain_rate_buffer, and
+ * eii_plastic_pressure = the 4-node average (PlasticStrainRateInterpolation.jl:13-40). */
+int eb_apply_nodal_plastic_yielding(eb_ctx* ctx);
 
 /* No counterpart in the reference (its COO product): y = L x for host vectors of N doubles. */
 int eb_stokes_apply(eb_ctx* ctx, const double* x, double* y);

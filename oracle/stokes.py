@@ -213,3 +213,46 @@ class StokesOracle:
         G["vyb"] = np.zeros((Y, X), order="F")
         lib().o_stag_velocity_to_basic(C.c_int64(X), C.c_int64(Y), _p(G["vx1"]), _p(G["vy1"]), _p(G["vxb"]),
                                        _p(G["vyb"]))
+
+    def interpolate_basic_viscoplastic_viscosity_to_pressure_grid(self, iuse_harmonic: int = 1):
+        """Interpolation.interpolate_basic_viscoplastic_viscosity_to_pressure_grid! (Interpolation.jl:97-108)."""
+        if iuse_harmonic != 1:
+            return
+        G = self.gr
+        lib().o_harmonic_normal_viscosity(C.c_int64(self.xnum), C.c_int64(self.ynum), _p(G["etas1"]),
+                                          _p(G["plastics"]), _p(G["plasticn"]), _p(G["plastic_yield"]),
+                                          _p(G["etan1"]))
+
+    def update_nodes_for_plastic_yielding(self, wall: dict | None = None):
+        """PlasticFailureNodes.update_nodes_for_plastic_yielding (PlasticFailureNodes.jl:24-184).
+        Returns (nnode_yield, global_yield_error); fills etavp_buffer, plastic_yield_buffer,
+        plastic_strain_rate_buffer and yield_error."""
+        G, g, p = self.gr, self.model.grid, self.p
+        X, Y = self.xnum, self.ynum
+        for k in ("etavp_buffer", "plastic_yield_buffer", "plastic_strain_rate_buffer"):
+            G[k] = np.zeros((Y, X), order="F")
+        G.setdefault("yield_error", np.zeros((Y, X), order="F"))
+        w = wall or {}
+
+        class Q(C.Structure):
+            _fields_ = [(n, C.c_int64) for n in ("ntimestep", "iuse_fluid", "no_wall", "no_plate")] + [
+                (n, C.c_double) for n in ("timestep", "timesum", "vmin", "vmax", "y_sealevel", "vix", "xl", "xr",
+                                          "yt", "yb", "pthick", "pwidth")]
+        q = Q(ntimestep=int(p["ntimestep"]), iuse_fluid=int(p["iuse_fluid_pressure_for_yield"]),
+              no_wall=int(p["no_yielding_in_mobile_wall"]) if wall else 0,
+              no_plate=int(w.get("no_yielding_in_plate_extension", 0)), timestep=p["timestep"],
+              timesum=w.get("timesum", 0.0), vmin=p["viscosity_min"], vmax=p["viscosity_max"],
+              y_sealevel=p["y_sealevel"], vix=w.get("velocity_internal_x", 0.0), xl=w.get("x_left_mobile_wall", 0.0),
+              xr=w.get("x_right_mobile_wall", 0.0), yt=w.get("y_top_mobile_wall", 0.0),
+              yb=w.get("y_bottom_mobile_wall", 0.0), pthick=w.get("plate_extension_thickness", 0.0),
+              pwidth=w.get("plate_extension_width", 0.0))
+        gx = np.ascontiguousarray(g.gridx_b, dtype=np.float64)
+        gy = np.ascontiguousarray(g.gridy_b, dtype=np.float64)
+        gerr = C.c_double()
+        f = lib().o_nodal_plastic_yielding
+        f.restype = C.c_int64
+        n = f(C.byref(q), C.c_int64(X), C.c_int64(Y), _p(gx), _p(gy), _p(G["plastic_yield"]), _p(G["etas1"]),
+              _p(G["eta_flow"]), _p(G["mus1"]), _p(G["cohesion_grid"]), _p(G["fric_degrees_grid"]), _p(G["sxy2"]),
+              _p(G["sxx2"]), _p(G["pr1"]), _p(G["yield_error"]), _p(G["etavp_buffer"]),
+              _p(G["plastic_strain_rate_buffer"]), _p(G["plastic_yield_buffer"]), C.byref(gerr))
+        return int(n), gerr.value

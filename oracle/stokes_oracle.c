@@ -492,3 +492,130 @@ void o_stag_velocity_to_basic(int64_t xnum, int64_t ynum, const double* vx1, con
       A2(vyb, ynum, i, j) = (A2(vy1, ynum, i, j) + A2(vy1, ynum, i, j + 1)) / 2.0;
     }
 }
+
+/* HarmonicAverage.normal_viscosity_from_harmonic_avg_shear_viscosity! (interpolation/utils/stokes_funcs/
+ * HarmonicAverage.jl:20-51) with CheckPlasticYield.plastic_yielding (tolerance 0) and
+ * MathTools.harmonic4 (zero factors): etan1 = 4 / sum(1 / etas1 corners) where the cell yields. */
+void o_harmonic_normal_viscosity(int64_t xnum, int64_t ynum, const double* etas1, const double* plastics,
+                                 const double* plasticn, const double* plastic_yield, double* etan1) {
+  const int64_t yp = ynum - 1;
+  for (int64_t i = 1; i <= ynum - 1; ++i)
+    for (int64_t j = 1; j <= xnum - 1; ++j) {
+      int yielding = A2(plasticn, yp, i, j) > 0.0;
+      if (A2(plastics, ynum, i, j) > 0.0 || A2(plastics, ynum, i, j + 1) > 0.0 ||
+          A2(plastics, ynum, i + 1, j) > 0.0 || A2(plastics, ynum, i + 1, j + 1) > 0.0) yielding = 1;
+      if (A2(plastic_yield, ynum, i, j) > 0.0 || A2(plastic_yield, ynum, i, j + 1) > 0.0 ||
+          A2(plastic_yield, ynum, i + 1, j) > 0.0 || A2(plastic_yield, ynum, i + 1, j + 1) > 0.0) yielding = 1;
+      if (!yielding) continue;
+      const double vinv = 1.0 / A2(etas1, ynum, i, j) + 1.0 / A2(etas1, ynum, i, j + 1) +
+                          1.0 / A2(etas1, ynum, i + 1, j) + 1.0 / A2(etas1, ynum, i + 1, j + 1) + 0.0 + 0.0 + 0.0 + 0.0;
+      if (vinv != 0.0) A2(etan1, yp, i, j) = 1.0 / (vinv / (4.0 + 0.0 + 0.0 + 0.0 + 0.0));
+    }
+}
+
+/* ---- nodal Picard variant ---------------------------------------------------- */
+
+/* PlasticFailureNodes.interpolate_from_pressure_grid_to_basic_grid (rheology/plastic_failure/nodes/
+ * PlasticFailureNodes.jl:221-257): pressure-grid value at basic node (i, j). */
+static double p_to_basic(int64_t i, int64_t j, int64_t ynum, int64_t xnum, const double* a) {
+  const int64_t yp = ynum - 1;
+  if (1 < i && i < ynum && 1 < j && j < xnum)
+    return (A2(a, yp, i - 1, j - 1) + A2(a, yp, i, j - 1) + A2(a, yp, i - 1, j) + A2(a, yp, i, j)) / 4.0;
+  if (i == 1 && j == 1) return A2(a, yp, i, j);
+  if (i == ynum && j == 1) return A2(a, yp, i - 1, j);
+  if (i == ynum && j == xnum) return A2(a, yp, i - 1, j - 1);
+  if (i == 1 && j == xnum) return A2(a, yp, i, j - 1);
+  if (j == 1) return (A2(a, yp, i, j) + A2(a, yp, i - 1, j)) / 2.0;
+  if (j == xnum) return (A2(a, yp, i - 1, j - 1) + A2(a, yp, i, j - 1)) / 2.0;
+  if (i == 1) return (A2(a, yp, i, j) + A2(a, yp, i, j - 1)) / 2.0;
+  return (A2(a, yp, i - 1, j) + A2(a, yp, i - 1, j - 1)) / 2.0;  /* i == ynum */
+}
+
+typedef struct {
+  int64_t ntimestep, iuse_fluid_pressure_for_yield, no_yielding_in_mobile_wall, no_yielding_in_plate_extension;
+  double timestep, timesum, viscosity_min, viscosity_max, y_sealevel;
+  double velocity_internal_x, x_left_mobile_wall, x_right_mobile_wall, y_top_mobile_wall, y_bottom_mobile_wall;
+  double plate_extension_thickness, plate_extension_width;
+} o_nodal_yield_in;
+
+/* PlasticFailureNodes.update_nodes_for_plastic_yielding (PlasticFailureNodes.jl:24-184) with
+ * CheckYield.check_yield_is_applicable, MobileWall.in_mobile_wall_transient /
+ * in_plate_extension_transient (src/utils/MobileWall.jl), YieldStress.calc_yield_stress
+ * (utils/YieldStress.jl:28-67, tension method 2) and the helpers :186-318.
+ * viscosity_weight_factor is 0, so the weighted viscosity is the new one.
+ * Returns nnode_yield; *gerr = sqrt(sum err^2 / nnode_yield) (0 when none). */
+int64_t o_nodal_plastic_yielding(const o_nodal_yield_in* q, int64_t xnum, int64_t ynum, const double* gridx,
+                                 const double* gridy, const double* plastic_yield, const double* etas1,
+                                 const double* eta_flow, const double* mus1, const double* cohesion_grid,
+                                 const double* fric_degrees_grid, const double* sxy2, const double* sxx2,
+                                 const double* pr1, double* yield_error, double* etavp_new,
+                                 double* plastic_strain_rate, double* plastic_yield_new, double* gerr) {
+  const double pi_term = O_PI / 180.0;
+  int64_t nnode = 0;
+  double esum = 0.0;
+  for (int64_t j = 1; j <= xnum; ++j)
+    for (int64_t i = 1; i <= ynum; ++i) {
+      const double vold = A2(etas1, ynum, i, j), vflow = A2(eta_flow, ynum, i, j), mu = A2(mus1, ynum, i, j);
+      const double coh = A2(cohesion_grid, ynum, i, j);
+      const double fc = sin(A2(fric_degrees_grid, ynum, i, j) * pi_term);
+      A2(etavp_new, ynum, i, j) = vflow;
+      A2(plastic_yield_new, ynum, i, j) = 0.0;
+      A2(plastic_strain_rate, ynum, i, j) = 0.0;
+      int applicable = q->ntimestep > 0 && (coh > 0.0 || fc > 0.0);
+      const double xs = q->velocity_internal_x * q->timesum;
+      if (q->no_yielding_in_mobile_wall) {
+        const double xl = q->x_left_mobile_wall + xs, xr = q->x_right_mobile_wall + xs;
+        if (xl <= gridx[j - 1] && gridx[j - 1] <= xr && q->y_top_mobile_wall <= gridy[i - 1] &&
+            gridy[i - 1] <= q->y_bottom_mobile_wall)
+          applicable = 0;
+      }
+      if (q->no_yielding_in_plate_extension) {
+        const double xl = q->x_left_mobile_wall + xs;
+        const double xmin = xl - q->plate_extension_width, ymin = q->y_bottom_mobile_wall - q->plate_extension_thickness;
+        if (xmin <= gridx[j - 1] && gridx[j - 1] <= xl && ymin <= gridy[i - 1] && gridy[i - 1] <= q->y_bottom_mobile_wall)
+          applicable = 0;
+      }
+      if (!applicable) continue;
+      const double p = p_to_basic(i, j, ynum, xnum, pr1);
+      const double sxx = p_to_basic(i, j, ynum, xnum, sxx2), sxy = A2(sxy2, ynum, i, j);
+      const double sii = sqrt(sxy * sxy + sxx * sxx);
+      const double sie = sii * (mu * q->timestep + vold) / vold;
+      const double cphi = cos(asin(fc));
+      double sy;
+      if (q->iuse_fluid_pressure_for_yield == 0) {
+        sy = coh * cphi + fc * p;
+      } else {
+        double depth = gridy[i - 1] - q->y_sealevel;
+        if (depth < 0.0) depth = 0.0;
+        const double pf = 1000.0 * 9.81 * depth;
+        sy = (p < pf) ? coh * cphi : coh * cphi + fc * (p - pf);
+      }
+      if (sy < 0.0) sy = 0.0;
+      const int at_yield = A2(plastic_yield, ynum, i, j) > 0;
+      if (at_yield) {
+        const double err = sii - sy;
+        esum = esum + err * err;
+        A2(yield_error, ynum, i, j) = err;
+        ++nnode;
+      }
+      if (sy < sie) {
+        double vnew = q->timestep * mu * sy / (sie - sy);
+        if (vnew < vflow) {
+          A2(plastic_yield_new, ynum, i, j) = 1.0;
+          vnew = pow(vnew, 1.0 - 0.0) * pow(vold, 0.0);
+          vnew = vnew > q->viscosity_min ? vnew : q->viscosity_min;
+          vnew = vnew < q->viscosity_max ? vnew : q->viscosity_max;
+          A2(etavp_new, ynum, i, j) = vnew;
+          A2(plastic_strain_rate, ynum, i, j) = 0.5 * sii / vnew - 0.5 * sii / vflow;
+          if (!at_yield) {
+            const double err = sii - sy;
+            esum = esum + err * err;
+            A2(yield_error, ynum, i, j) = err;
+            ++nnode;
+          }
+        }
+      }
+    }
+  *gerr = nnode > 0 ? sqrt(esum / (double)nnode) : 0.0;
+  return nnode;
+}

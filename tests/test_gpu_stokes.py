@@ -102,28 +102,30 @@ def test_operator_apply_matches_coo_product(eb, case):
     mic.close()
 
 
-def solve_case(eb, model, rtol):
+def solve_case(eb, model, rtol, method="fgmres"):
     o = oracle_for(model)
     mic = gpu_ctx(eb, model)
-    rep = mic.solve_viscoelastic_stokes_continuity_equations(rtol=rtol, max_iters=4000)
+    rep = mic.solve_viscoelastic_stokes_continuity_equations(rtol=rtol, max_iters=4000, method=method)
     S = mic.download_stokes_vector("solution")
     return o, mic, rep, S
 
 
+@pytest.mark.parametrize("method", ["fgmres", "bicgstab"])
 @pytest.mark.parametrize("case", ["rift_small", "sinking_block"])
-def test_solve_reaches_metric_tolerance(eb, case):
+def test_solve_reaches_metric_tolerance(eb, case, method):
     model = marker_model(eb, case)
-    o, mic, rep, S = solve_case(eb, model, 1e-8)
+    o, mic, rep, S = solve_case(eb, model, 1e-8, method)
     assert rep["status"] == 0
     assert rep["rel_residual"] <= 1e-8, rep
     assert o.residual(S) <= 1e-8 * 1.01
     mic.close()
 
 
+@pytest.mark.parametrize("method", ["fgmres", "bicgstab"])
 @pytest.mark.parametrize("case", ["rift_small", "sinking_block"])
-def test_solution_matches_superlu(eb, case):
+def test_solution_matches_superlu(eb, case, method):
     model = marker_model(eb, case)
-    o, mic, rep, S = solve_case(eb, model, 1e-11)
+    o, mic, rep, S = solve_case(eb, model, 1e-11, method)
     assert rep["status"] == 0, rep
     S_ref = o.solve_direct()
     for comp in range(3):
@@ -155,8 +157,10 @@ def test_couette_and_hydrostatic_on_gpu(eb):
 def test_nonlinear_residual_and_backup(eb):
     model = marker_model(eb, "rift_small")
     o, mic, rep, S = solve_case(eb, model, 1e-8)
-    mic.backup_stokes_solution()
+    mic.backup_stokes_arrays()
     assert np.array_equal(mic.download_stokes_vector("solution_old"), S)
+    for k in ("vx1", "vy1", "pr1"):
+        assert np.array_equal(mic.download_grid(k + "_old"), mic.download_grid(k))
     res = mic.stokes_nonlinear_residual()
     ref = o.nonlinear_residual(S)
     scale = abs(o.matrix()) @ np.abs(S) + np.abs(o.coo[3])
@@ -180,4 +184,118 @@ def test_post_solve_grid_kernels_match_oracle(eb, case):
     o.interpolate_stag_velocity_to_basic_grid()
     for k in ("exx", "exy", "eii", "esp", "sxy2", "sxx2", "dsxy", "dsxx", "vxb", "vyb"):
         assert np.array_equal(mic.download_grid(k), o.gr[k]), k
+    mic.close()
+
+
+def test_stokes_norms_match_numpy(eb):
+    """StokesNorms.calculate_stokes_norms! solution-change norms between two Picard iterates."""
+    model = marker_model(eb, "rift_small")
+    o, mic, rep, S0 = solve_case(eb, model, 1e-6)
+    mic.backup_stokes_arrays()
+    old = {k: mic.download_grid(k) for k in ("vx1", "vy1", "pr1")}
+    mic.solve_system(rtol=1e-10, use_initial_guess=True)
+    mic.process_stokes_solution()
+    mic.stokes_nonlinear_residual()
+    S = mic.download_stokes_vector("solution")
+    new = {k: mic.download_grid(k) for k in ("vx1", "vy1", "pr1")}
+    res = mic.download_stokes_vector("resnl")
+    got = mic.calculate_stokes_norms()
+
+    def l2(v, v0):
+        a = np.linalg.norm(np.abs(v0 - v)); n = np.linalg.norm(v)
+        return a, (a / n if n != 0 else 1e38)
+
+    def linf(v, v0):
+        a = np.max(np.abs(v0 - v)); n = np.max(np.abs(v))
+        return a, (a / n if n != 0 else 1e38)
+    vxy = np.concatenate([new["vx1"].ravel(order="C"), new["vy1"].ravel(order="C")])
+    vxy0 = np.concatenate([old["vx1"].ravel(order="C"), old["vy1"].ravel(order="C")])
+    want = {}
+    want["dsoluv1_abs_inf"], want["dsoluv1_rel_inf"] = linf(S, S0)
+    want["dsoluv1_abs_L2"], want["dsoluv1_rel_L2"] = l2(S, S0)
+    for k in ("vx1", "vy1", "pr1"):
+        want[f"d{k}_abs_L2"], want[f"d{k}_rel_L2"] = l2(new[k], old[k])
+    want["dvxy_abs_inf"], want["dvxy_rel_inf"] = linf(vxy, vxy0)
+    want["dvxy_abs_L2"], want["dvxy_rel_L2"] = l2(vxy, vxy0)
+    want["resnl_L2"] = np.linalg.norm(res)
+    for k, v in want.items():
+        assert abs(got[k] - v) <= 1e-12 * abs(v) + 1e-300, (k, got[k], v)
+    mic.close()
+
+
+@pytest.mark.parametrize("case", ["rift_small", "sinking_block"])
+def test_harmonic_normal_viscosity_matches_oracle(eb, case):
+    """HarmonicAverage.normal_viscosity_from_harmonic_avg_shear_viscosity! on yielding cells."""
+    model = marker_model(eb, case)
+    rng = np.random.default_rng(3)
+    X, Y = model.grid.xnum, model.grid.ynum
+    # mark a random subset of nodes and cells as yielding
+    model.grids["plastics"] = np.asfortranarray((rng.random((Y, X)) < 0.1).astype(float))
+    model.grids["plasticn"] = np.asfortranarray((rng.random((Y - 1, X - 1)) < 0.1).astype(float))
+    model.grids["plastic_yield"] = np.asfortranarray(np.zeros((Y, X)))
+    o = oracle_for(model)
+    mic = gpu_ctx(eb, model)
+    for k in ("plastics", "plasticn", "plastic_yield"):
+        mic.upload_grid(k, model.grids[k])
+    mic.interpolate_basic_viscoplastic_viscosity_to_pressure_grid(1)
+    o.interpolate_basic_viscoplastic_viscosity_to_pressure_grid(1)
+    assert np.array_equal(mic.download_grid("etan1"), o.gr["etan1"])
+    assert not np.array_equal(o.gr["etan1"], model.grids["etan1"])  # the update did something
+    mic.close()
+
+
+def test_picard_loop_markers_runs_and_converges(eb):
+    """The marker Picard loop on the GPU context: the first iteration equals a single Stokes step,
+    the loop stops on the reference's criterion, and every solve meets the metric tolerance."""
+    model = eb.synthetic.rift(101, 41, 4)
+    mic = eb.MarkerInCell(0)
+    mic.load_model(model)
+    mic.get_marker_inside_flags()
+    mic.initialize_bilinear_interpolation()
+    mic.interpolate_marker_stokes_parameters_to_grid()
+    mic.update_marker_rheology()
+    hist = mic.picard_loop_markers(nglobal=4, tolerance_picard=1e-3)
+    assert 1 <= len(hist) <= 4
+    for h in hist:
+        assert h["status"] == 0 and h["rel_residual"] <= 1e-8
+    assert hist[0]["dvxy_rel_L2"] == pytest.approx(1.0)  # compared with zero previous velocities
+    if len(hist) < 4:
+        assert hist[-1]["dvxy_rel_L2"] < 1e-3
+    mic.close()
+
+
+@pytest.mark.parametrize("case", ["rift_small", "sinking_block"])
+def test_nodal_plastic_yielding_matches_oracle(eb, case):
+    """PlasticFailureNodes.update_nodes_for_plastic_yielding on the GPU's own solved state."""
+    model = marker_model(eb, case)
+    o, mic, rep, S = solve_case(eb, model, 1e-8)
+    mic.update_grid_strain_rate_and_spin()
+    mic.forecast_viscoelastic_grid_stress()
+    # yield state and material strength from the same arrays on both sides
+    X, Y = model.grid.xnum, model.grid.ynum
+    rng = np.random.default_rng(11)
+    G = {"plastic_yield": (rng.random((Y, X)) < 0.2).astype(float),
+         "cohesion_grid": np.full((Y, X), 5e6), "fric_degrees_grid": rng.uniform(5.0, 30.0, (Y, X)),
+         "eta_flow": mic.download_grid("etas1") * 10.0}
+    for k, v in G.items():
+        mic.upload_grid(k, np.asfortranarray(v))
+    for k in ("etas1", "mus1", "sxy2", "sxx2", "pr1"):
+        o.gr[k] = np.asfortranarray(mic.download_grid(k))
+    for k, v in G.items():
+        o.gr[k] = np.asfortranarray(v)
+    n_gpu, e_gpu = mic.update_nodes_for_plastic_yielding()
+    n_ref, e_ref = o.update_nodes_for_plastic_yielding()
+    assert n_gpu == n_ref and n_ref > 0
+    assert e_gpu == pytest.approx(e_ref, rel=1e-12)
+    assert np.array_equal(mic.download_grid("plastic_yield_buffer"), o.gr["plastic_yield_buffer"])
+    for k in ("etavp_buffer", "plastic_strain_rate_buffer"):
+        a, b = mic.download_grid(k), o.gr[k]
+        assert np.allclose(a, b, rtol=1e-13, atol=0), k
+    yb = o.gr["plastic_yield_buffer"] > 0
+    assert np.allclose(mic.download_grid("yield_error")[yb], o.gr["yield_error"][yb], rtol=1e-12, atol=1e-6)
+    mic.apply_nodal_plastic_yielding()
+    assert np.array_equal(mic.download_grid("etas1"), mic.download_grid("etavp_buffer"))
+    eb_ = mic.download_grid("eii_plastic_basic")
+    ep = (eb_[:-1, :-1] + eb_[:-1, 1:] + eb_[1:, :-1] + eb_[1:, 1:]) / 4.0
+    assert np.allclose(mic.download_grid("eii_plastic_pressure"), ep, rtol=1e-15, atol=0)
     mic.close()
