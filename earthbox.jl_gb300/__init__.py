@@ -337,6 +337,17 @@ class MarkerInCell:
             raise ValueError(f"expected {self.stokes_size} values")
         self._check(self._lib.eb_stokes_vector_upload(self._ctx, _abi.STOKES_VECTORS[name], _ptr(a)))
 
+    def export_coo(self) -> tuple:
+        """The assembled system as the reference's (Li, Lj, Lv, R): 1-based COO in
+        StokesBuildManager's entry order, for a direct solver on the host."""
+        n = C.c_int64()
+        self._check(self._lib.eb_stokes_export_coo(self._ctx, None, None, None, 0, C.byref(n)))
+        Li = np.empty(n.value, np.int64)
+        Lj = np.empty(n.value, np.int64)
+        Lv = np.empty(n.value, np.float64)
+        self._check(self._lib.eb_stokes_export_coo(self._ctx, _ptr(Li), _ptr(Lj), _ptr(Lv), n.value, C.byref(n)))
+        return Li, Lj, Lv, self.download_stokes_vector("rhs")
+
     def stokes_stencil(self) -> np.ndarray:
         """The assembled coefficients as a (27, xnum-1, ynum-1) array indexed [slot, j, i]."""
         nx, ny = self.xnum - 1, self.ynum - 1

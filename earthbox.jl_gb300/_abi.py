@@ -169,7 +169,7 @@ ALL_SYMBOLS = [
     "eb_set_stokes_params", "eb_solve_stokes_system", "eb_stokes_apply", "eb_stokes_vector_upload",
     "eb_stokes_vector_download", "eb_stokes_stencil_download", "eb_stokes_pscale", "eb_stokes_size",
     "eb_calculate_stokes_norms", "eb_interpolate_basic_viscoplastic_viscosity_to_pressure_grid",
-    "eb_update_nodes_for_plastic_yielding",
+    "eb_update_nodes_for_plastic_yielding", "eb_stokes_export_coo",
     "eb_marker_to_basic_grid_average_noalloc",
 ] + ENTRY_POINTS + STOKES_ENTRY_POINTS
 
@@ -219,6 +219,7 @@ def load(path: pathlib.Path | str | None = None) -> C.CDLL:
     lib.eb_stokes_stencil_download.argtypes = [vp, vp]
     lib.eb_calculate_stokes_norms.argtypes = [vp, C.POINTER(StokesNorms)]
     lib.eb_interpolate_basic_viscoplastic_viscosity_to_pressure_grid.argtypes = [vp, C.c_int]
+    lib.eb_stokes_export_coo.argtypes = [vp, vp, vp, vp, C.c_int64, C.POINTER(C.c_int64)]
     lib.eb_update_nodes_for_plastic_yielding.argtypes = [vp, C.POINTER(MobileWall), C.POINTER(C.c_int64),
                                                          C.POINTER(C.c_double)]
     lib.eb_stokes_pscale.argtypes = [vp]

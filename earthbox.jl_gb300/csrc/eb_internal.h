@@ -135,6 +135,8 @@ int launch_stag_to_basic(eb_ctx* c);
 int launch_harmonic_etan(eb_ctx* c);
 int launch_nodal_yield(eb_ctx* c, const eb_mobile_wall* w, double* d_partial, int* nblocks);
 int launch_apply_nodal_yield(eb_ctx* c);
+int export_stokes_coo(eb_ctx* c, const StokesSystem* s, int64_t* Li, int64_t* Lj, double* Lv, int64_t capacity,
+                      int64_t* nnz);
 
 constexpr int kMaxSlots = 48;
 

@@ -547,9 +547,147 @@ __global__ void k_eii_plastic_pressure(int32_t xnum, int32_t ynum, const double*
                             A2(eb, ynum, i + 1, j + 1)) / 4.0;
 }
 
+// ---- the reference's COO entry order ------------------------------------------
+// Which stencil slots StokesBuildManager emits for cell (i, j), in its order (the same
+// branches as k_build_system; folds modify entries already emitted and add none).
+struct CooIn {
+  int32_t xnum, ynum, pressure_bc_mode;
+  int64_t zone[8];
+};
+struct CooEntry { int8_t slot; int64_t col; };
+__device__ int coo_entries(const CooIn& b, int32_t i, int32_t j, CooEntry* e) {
+  const int64_t ny = b.ynum - 1;
+  const int64_t c = (int64_t)(j - 1) * ny + (i - 1);
+  const bool top = i == 1, left = j == 1;
+  int n = 0;
+  auto put = [&](int slot, int64_t col) { e[n].slot = (int8_t)slot; e[n].col = col; ++n; };
+  // x-Stokes
+  const bool out_x = j != b.zone[0] || i < b.zone[1] || i > b.zone[2];
+  if (!(j < b.xnum - 1 && out_x)) {
+    put(X_C, 3 * c);
+  } else {
+    const bool bot = i >= b.ynum - 1, right2 = j >= b.xnum - 2;
+    put(X_C, 3 * c);
+    if (!left) put(X_L, 3 * (c - ny));
+    if (!right2) put(X_R, 3 * (c + ny));
+    if (!top) put(X_U, 3 * (c - 1));
+    if (!bot) put(X_D, 3 * (c + 1));
+    if (!top) put(X_YUL, 3 * (c - 1) + 1); else put(X_YLL, 3 * c + 1);
+    if (!top) put(X_YUR, 3 * (c - 1 + ny) + 1); else put(X_YLR, 3 * (c + ny) + 1);
+    if (!bot && !top) put(X_YLL, 3 * c + 1);
+    if (!bot && !top) put(X_YLR, 3 * (c + ny) + 1);
+    put(X_PL, 3 * c + 2);
+    put(X_PR, 3 * (c + ny) + 2);
+  }
+  // y-Stokes
+  const bool out_y = j != b.zone[4] || i < b.zone[5] || i > b.zone[6];
+  if (!(i < b.ynum - 1 && out_y)) {
+    put(11 + Y_C, 3 * c + 1);
+  } else {
+    const bool bot2 = i >= b.ynum - 2, right = j >= b.xnum - 1;
+    put(11 + Y_C, 3 * c + 1);
+    if (!top) put(11 + Y_U, 3 * (c - 1) + 1);
+    if (!bot2) put(11 + Y_D, 3 * (c + 1) + 1);
+    if (!left) put(11 + Y_L, 3 * (c - ny) + 1);
+    if (!right) put(11 + Y_R, 3 * (c + ny) + 1);
+    if (!left) put(11 + Y_XUL, 3 * (c - ny)); else put(11 + Y_XUR, 3 * c);
+    if (!left) put(11 + Y_XLL, 3 * (c + 1 - ny)); else put(11 + Y_XLR, 3 * (c + 1));
+    if (!right && !left) put(11 + Y_XUR, 3 * c);
+    if (!right && !left) put(11 + Y_XLR, 3 * (c + 1));
+    put(11 + Y_PU, 3 * c + 2);
+    put(11 + Y_PD, 3 * (c + 1) + 2);
+  }
+  // continuity
+  bool internal;
+  switch (b.pressure_bc_mode) {
+    case 0: internal = (j > 1 || i > 1); break;
+    case 1: internal = (1 < i && i < b.ynum - 1); break;
+    case 2: internal = (1 < j && j < b.xnum - 1); break;
+    default: internal = false;
+  }
+  if (!internal) {
+    if (b.pressure_bc_mode >= 0 && b.pressure_bc_mode <= 2) put(22 + C_C, 3 * c + 2);
+  } else {
+    const bool lower = i >= b.ynum - 1, rightb = j >= b.xnum - 1;
+    if (!left) put(22 + C_XL, 3 * (c - ny));
+    if (!rightb) put(22 + C_XR, 3 * c);
+    if (!top) put(22 + C_YU, 3 * (c - 1) + 1);
+    if (!lower) put(22 + C_YD, 3 * c + 1);
+  }
+  return n;
+}
+// Cells in the reference's build order: r = (i-1) (xnum-1) + (j-1).
+__global__ void k_coo_count(CooIn b, int32_t* __restrict__ count, int64_t nc) {
+  const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= nc) return;
+  const int32_t i = (int32_t)(r / (b.xnum - 1)) + 1, j = (int32_t)(r % (b.xnum - 1)) + 1;
+  CooEntry e[kStencilSlots];
+  count[r] = coo_entries(b, i, j, e);
+}
+__global__ void k_coo_write(CooIn b, const int64_t* __restrict__ offset, const double* __restrict__ coef, int64_t nc,
+                            int64_t* __restrict__ Li, int64_t* __restrict__ Lj, double* __restrict__ Lv) {
+  const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= nc) return;
+  const int32_t i = (int32_t)(r / (b.xnum - 1)) + 1, j = (int32_t)(r % (b.xnum - 1)) + 1;
+  const int64_t c = (int64_t)(j - 1) * (b.ynum - 1) + (i - 1);
+  CooEntry e[kStencilSlots];
+  const int n = coo_entries(b, i, j, e);
+  int64_t o = offset[r];
+  for (int k = 0; k < n; ++k, ++o) {
+    const int row_kind = e[k].slot < 11 ? 0 : (e[k].slot < 22 ? 1 : 2);
+    Li[o] = 3 * c + row_kind + 1;
+    Lj[o] = e[k].col + 1;
+    Lv[o] = coef[(int64_t)e[k].slot * nc + c];
+  }
+}
+
 unsigned nblk(int64_t n) { return (unsigned)((n + kB - 1) / kB); }
 
 }  // namespace
+
+// The system as the reference's COO list (1-based Li, Lj; Lv), in StokesBuildManager's
+// entry order.  Li/Lj/Lv null: only *nnz is returned.
+int export_stokes_coo(eb_ctx* c, const StokesSystem* s, int64_t* Li, int64_t* Lj, double* Lv, int64_t capacity,
+                      int64_t* nnz) {
+  CooIn b{c->xnum, c->ynum, (int32_t)c->SP.pressure_bc_mode, {}};
+  for (int k = 0; k < 8; ++k) b.zone[k] = c->SP.bintern_zone[k];
+  const int64_t nc = s->nc;
+  int32_t* d_count = nullptr;
+  EB_CK(c, cudaMalloc(&d_count, nc * sizeof(int32_t)));
+  k_coo_count<<<nblk(nc), kB, 0, c->stream>>>(b, d_count, nc);
+  c->launches++;
+  std::vector<int32_t> h(nc);
+  cudaError_t e = cudaMemcpyAsync(h.data(), d_count, nc * sizeof(int32_t), cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  cudaFree(d_count);
+  if (e != cudaSuccess) return eb_cuda(c, e, "COO entry count");
+  std::vector<int64_t> off(nc);
+  int64_t total = 0;
+  for (int64_t r = 0; r < nc; ++r) { off[r] = total; total += h[r]; }
+  if (nnz) *nnz = total;
+  if (!Li || !Lj || !Lv) return EB_OK;
+  if (capacity < total) return eb_fail(c, EB_BAD_INPUT, "COO arrays hold " + std::to_string(capacity) +
+                                                            " entries, the system has " + std::to_string(total));
+  int64_t *d_off = nullptr, *d_li = nullptr, *d_lj = nullptr;
+  double* d_lv = nullptr;
+  e = cudaMalloc(&d_off, nc * sizeof(int64_t));
+  if (e == cudaSuccess) e = cudaMalloc(&d_li, total * sizeof(int64_t));
+  if (e == cudaSuccess) e = cudaMalloc(&d_lj, total * sizeof(int64_t));
+  if (e == cudaSuccess) e = cudaMalloc(&d_lv, total * sizeof(double));
+  if (e == cudaSuccess) e = cudaMemcpyAsync(d_off, off.data(), nc * sizeof(int64_t), cudaMemcpyHostToDevice, c->stream);
+  if (e == cudaSuccess) {
+    k_coo_write<<<nblk(nc), kB, 0, c->stream>>>(b, d_off, s->coef, nc, d_li, d_lj, d_lv);
+    c->launches++;
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaMemcpyAsync(Li, d_li, total * sizeof(int64_t), cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(Lj, d_lj, total * sizeof(int64_t), cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(Lv, d_lv, total * sizeof(double), cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  cudaFree(d_off); cudaFree(d_li); cudaFree(d_lj); cudaFree(d_lv);
+  if (e != cudaSuccess) return eb_cuda(c, e, "COO export");
+  return EB_OK;
+}
 
 int launch_nodal_yield(eb_ctx* c, const eb_mobile_wall* w, double* d_partial, int* nblocks) {
   double** g = c->gf;

@@ -38,9 +38,10 @@ constexpr int kMaxDots = kMaxRestart + 8;  // dot products per reduction
 unsigned nblk(int64_t n) { return (unsigned)((n + kB - 1) / kB); }
 
 // ------------------------------------------------------- FP64 operator ---
-// y = L x on SoA vectors; optional scaling: y = w .* L (w .* x).
+// y = L x on SoA vectors; optional scaling: y = w .* L (w .* x); optional shift: y -= sub.
 __global__ void k_apply64(const double* __restrict__ coef, const double* __restrict__ x, double* __restrict__ y,
-                          const double* __restrict__ w, int32_t nx, int32_t ny, int64_t nc) {
+                          const double* __restrict__ w, int32_t nx, int32_t ny, int64_t nc,
+                          const double* __restrict__ sub = nullptr) {
   const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= nc) return;
   const int32_t i = (int32_t)(c % ny), j = (int32_t)(c / ny);
@@ -79,6 +80,7 @@ __global__ void k_apply64(const double* __restrict__ coef, const double* __restr
   if (hu) ap += cf(25) * Y(c - 1);
   ap += cf(26) * Y(c);
   if (w) { ax *= wx[c]; ay *= wy[c]; ap *= wp[c]; }
+  if (sub) { ax -= sub[c]; ay -= sub[nc + c]; ap -= sub[2 * nc + c]; }
   y[c] = ax;
   y[nc + c] = ay;
   y[2 * nc + c] = ap;
@@ -110,9 +112,21 @@ constexpr int kDotBlocks = 2 * 152;
 __global__ void __launch_bounds__(kB) k_mdot(const double* __restrict__ V, int64_t stride, const double* __restrict__ u,
                                              int64_t n, double* __restrict__ partial) {
   const double* a = V + (int64_t)blockIdx.y * stride;
-  double s = 0.0;
-  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x)
-    s += a[k] * u[k];
+  // four independent partial sums: eight loads in flight per thread
+  double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
+  const int64_t step = (int64_t)gridDim.x * blockDim.x;
+  int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  for (; k + 3 * step < n; k += 4 * step) {
+    const double a0 = __ldcs(a + k), a1 = __ldcs(a + k + step), a2 = __ldcs(a + k + 2 * step),
+                 a3 = __ldcs(a + k + 3 * step);
+    const double u0 = __ldg(u + k), u1 = __ldg(u + k + step), u2 = __ldg(u + k + 2 * step), u3 = __ldg(u + k + 3 * step);
+    s0 += a0 * u0;
+    s1 += a1 * u1;
+    s2 += a2 * u2;
+    s3 += a3 * u3;
+  }
+  for (; k < n; k += step) s0 += a[k] * u[k];
+  double s = (s0 + s1) + (s2 + s3);
   for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
   __shared__ double sh[kB / 32];
   if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = s;
@@ -1114,7 +1128,7 @@ extern "C" int eb_solve_stokes_system(eb_ctx* c, const eb_solve_opts* o, eb_solv
   if (opt.rtol <= 0) opt.rtol = 1e-8;
   if (opt.max_iters <= 0) opt.max_iters = 3000;
   if (opt.restart <= 0) opt.restart = 250;
-  if (opt.mg_sweeps <= 0) opt.mg_sweeps = 2;
+  if (opt.mg_sweeps <= 0) opt.mg_sweeps = 3;
   if (opt.method != 1) opt.method = 0;
   const int m = std::max(std::min(opt.restart, kMaxRestart), opt.method == 1 ? 6 : 1);
   const int64_t n3 = 3 * s.nc;
@@ -1217,8 +1231,14 @@ extern "C" int eb_solve_stokes_system(eb_ctx* c, const eb_solve_opts* o, eb_solv
       double* vk = st->V + (size_t)k * n3;
       float* zk = st->Z + (size_t)k * n3;
       double* w = st->V + (size_t)(k + 1) * n3;
-      if ((rc = precondition(c, st, vk, st->zt, zk)) || (rc = apply_scaled(c, st, st->zt, w))) return rc;
-      // Classical Gram-Schmidt.  One reduction gives V^T w and |w|^2 (w is the slot after V_k);
+      if ((rc = precondition(c, st, vk, st->zt, zk))) return rc;
+      // Shifted Arnoldi: with a good preconditioner A z_k is close to v_k, so the slot holds
+      // d = A z_k - v_k and the projection starts from d (h_kk gets the 1 back below); the
+      // cancellation that classical Gram-Schmidt suffers is then measured against |d|.
+      EB_PROF(c, "k_apply64");
+      k_apply64<<<nblk(s.nc), kB, 0, c->stream>>>(s.coef, st->zt, w, st->w, s.nx, s.ny, s.nc, vk);
+      EB_LAUNCHED(c);
+      // Classical Gram-Schmidt.  One reduction gives V^T d and |d|^2 (d is the slot after V_k);
       // the projected norm follows from Pythagoras unless cancellation is large, in which
       // case a second pass re-orthogonalises and the norm is measured.
       std::vector<double> h(k + 2);
@@ -1248,6 +1268,7 @@ extern "C" int eb_solve_stokes_system(eb_ctx* c, const eb_solve_opts* o, eb_solv
         }
         wn2_before = h[k + 1];
       }
+      hcol[k] += 1.0;
       if (!std::isfinite(hcol[k + 1])) return eb_fail(c, EB_NAN, "FGMRES basis became NaN/Inf");
       // apply the previous rotations, then a new one
       for (int q = 0; q < k; ++q) {
@@ -1623,6 +1644,12 @@ extern "C" int eb_stokes_apply(eb_ctx* c, const double* x, double* y) {
   EB_CK(c, cudaStreamSynchronize(c->stream));
   prof_resolve(c);
   return EB_OK;
+}
+
+extern "C" int eb_stokes_export_coo(eb_ctx* c, int64_t* Li, int64_t* Lj, double* Lv, int64_t capacity, int64_t* nnz) {
+  int rc = need_system(c, true);
+  if (rc) return rc;
+  return export_stokes_coo(c, &c->st->sys, Li, Lj, Lv, capacity, nnz);
 }
 
 extern "C" int eb_stokes_stencil_download(eb_ctx* c, double* host) {

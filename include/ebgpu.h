@@ -288,7 +288,7 @@ typedef struct eb_solve_opts {
   double  rtol;              /* stop when ||W(R - L S)|| <= rtol ||W R|| (W: diagonal scaling); 0 -> 1e-8 */
   int32_t max_iters;         /* FGMRES iterations; 0 -> 3000                                          */
   int32_t restart;           /* Krylov basis size; 0 -> 40                                             */
-  int32_t mg_sweeps;         /* red-black Gauss-Seidel sweeps before/after each coarse correction; 0 -> 2 */
+  int32_t mg_sweeps;         /* red-black Gauss-Seidel sweeps before/after each coarse correction; 0 -> 3 */
   int32_t use_initial_guess; /* 1: start from the current device solution vector, 0: from zero         */
   int32_t method;            /* 0: FGMRES (long recurrence, robust); 1: BiCGStab (short recurrence, two
                                 preconditioner applications per iteration)                           */
@@ -396,6 +396,14 @@ int eb_stokes_apply(eb_ctx* ctx, const double* x, double* y);
 /* Copies of the N-vectors named by enum eb_stokes_vector (host arrays, interleaved layout). */
 int eb_stokes_vector_upload(eb_ctx* ctx, int which, const double* host);
 int eb_stokes_vector_download(eb_ctx* ctx, int which, double* host);
+
+/* The assembled system as the reference's COO list: Li, Lj 1-based (Int64), Lv (Float64), in
+ * StokesBuildManager.build_system_of_equations' entry order (StokesBuildManager.jl:661-712), entry for
+ * entry the reference's system_vectors (Li_out, Lj_out, Lv_out); with the RHS from
+ * eb_stokes_vector_download(EB_SV_RHS) it is what parallel_direct_solver (ParallelSolver.jl:52) takes,
+ * so MUMPS stays usable on a GPU-assembled system.  Host arrays of `capacity` entries; with Li, Lj or
+ * Lv null only *nnz is set (size query). */
+int eb_stokes_export_coo(eb_ctx* ctx, int64_t* Li, int64_t* Lj, double* Lv, int64_t capacity, int64_t* nnz);
 
 /* The assembled coefficients: 27 slots x (xnum-1)(ynum-1) cells, slot-major, cells
  * column-major.  Slots 0-10: x-Stokes row (vx C, L, R, U, D; vy UL, UR, LL, LR; p L, R),
