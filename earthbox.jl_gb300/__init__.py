@@ -41,6 +41,16 @@ class EarthBoxGPUError(RuntimeError):
         self.code = code
 
 
+def heat_params(params: dict) -> dict:
+    """The heat-step scalars (reference parameter names) with this package's defaults."""
+    return {"timestep": float(params["timestep"]), "max_temp_change": float(params.get("max_temp_change", 20.0)),
+            "gravity_x": float(params.get("gravity_x", 0.0)), "gravity_y": float(params.get("gravity_y", 9.81)),
+            "iuse_adiabatic_heating": int(params.get("iuse_adiabatic_heating", 1)),
+            "iuse_shear_heating": int(params.get("iuse_shear_heating", 1)),
+            "iuse_heat": int(params.get("iuse_heat", 1)),
+            "subgrid_diff_coef_temp": float(params.get("subgrid_diff_coef_temp", 1.0))}
+
+
 def _ptr(a: np.ndarray) -> int:
     return a.ctypes.data
 
@@ -182,6 +192,7 @@ class MarkerInCell:
         self.set_params(model.params)
         if "gravity_y" in model.params:
             self.set_stokes_params(model.params)
+        self.heat = heat_params(model.params)
         self.resize_markers(model.marknum)
         for k, v in model.markers.items():
             if k in ("xn", "yn", "xn_vy", "yn_vy"):
@@ -457,6 +468,87 @@ class MarkerInCell:
             if iglobal == nglobal or norms["dvxy_rel_L2"] < tolerance_picard:
                 break
         return history
+
+    # ---------------------------------------------------------- heat step --
+    def _heat(self, params: dict | None) -> "_abi.HeatParams":
+        hp = heat_params(params) if params is not None else getattr(self, "heat", None)
+        if hp is None:
+            raise ValueError("heat parameters: pass params or call load_model first")
+        return _abi.HeatParams(hp["timestep"], hp["max_temp_change"], hp["gravity_x"], hp["gravity_y"],
+                               hp["iuse_adiabatic_heating"], hp["iuse_shear_heating"])
+
+    def calculate_heat_rhs_terms(self, params: dict | None = None) -> None:
+        """HeatSolver.calculate_heat_rhs_terms_grid! (heat_solver/HeatSolver.jl:139-150): RT1."""
+        hp = self._heat(params)
+        self._check(self._lib.eb_calculate_heat_rhs_terms(self._ctx, C.byref(hp)))
+
+    def initialize_old_temperature_array(self) -> None:
+        """HeatSolver.initialize_old_temperature_array! (HeatSolver.jl:199-204): tk0 = tk1."""
+        self._call("eb_initialize_old_temperature")
+
+    def build_heat_system(self, timestep_heat: float) -> None:
+        """HeatBuildManager.build_system_of_equations (HeatBuildManager.jl:44-86)."""
+        self._check(self._lib.eb_build_heat_system(self._ctx, C.c_double(timestep_heat)))
+
+    def solve_heat_system(self, rtol: float = 0.0, max_iters: int = 0, mg_sweeps: int = 0,
+                          use_initial_guess: bool = True, check: bool = True) -> dict:
+        """The solve of SystemSolver.discretize_and_solve_conductive_heat_equation
+        (heat_solver/solver/SystemSolver.jl:32-66) and reload_solu_temp: tk2."""
+        o = _abi.SolveOpts(rtol, max_iters, 0, mg_sweeps, int(use_initial_guess), 0)
+        r = _abi.SolveReport()
+        rc = self._lib.eb_solve_heat_system(self._ctx, C.byref(o), C.byref(r))
+        if check:
+            self._check(rc)
+        return {"status": rc, "iterations": r.iterations, "levels": r.levels, "rel_residual": r.rel_residual,
+                "rel_residual_scaled": r.rel_residual_scaled, "seconds": r.seconds}
+
+    def heat_residuals(self, timestep_heat: float) -> None:
+        """HeatResiduals.compute_residuals_temp! (HeatResiduals.jl:12-162): rest."""
+        self._check(self._lib.eb_heat_residuals(self._ctx, C.c_double(timestep_heat)))
+
+    def run_conductive_heat_solver_loop(self, params: dict | None = None, rtol: float = 0.0, max_iters: int = 0,
+                                        mg_sweeps: int = 0) -> dict:
+        """HeatLoop.run_conductive_heat_solver_loop! (heat_loop/HeatLoop.jl:10-79)."""
+        hp = self._heat(params)
+        o = _abi.SolveOpts(rtol, max_iters, 0, mg_sweeps, 1, 0)
+        r = _abi.HeatLoopReport()
+        self._check(self._lib.eb_run_conductive_heat_solver_loop(self._ctx, C.byref(hp), C.byref(o), C.byref(r)))
+        return {k: getattr(r, k) for k, _ in _abi.HeatLoopReport._fields_}
+
+    def calculate_grid_temp_change(self) -> None:
+        """HeatSolver.calculate_grid_temp_change! (HeatSolver.jl:211-216): dtk1 = tk2 - tk1."""
+        self._call("eb_calculate_grid_temp_change")
+
+    def export_heat_coo(self) -> tuple:
+        """The assembled heat system as the reference's (Li, Lj, Lv, R) in HeatBuildManager's order."""
+        n = C.c_int64()
+        self._check(self._lib.eb_heat_export_coo(self._ctx, None, None, None, 0, C.byref(n)))
+        Li = np.empty(n.value, np.int64)
+        Lj = np.empty(n.value, np.int64)
+        Lv = np.empty(n.value, np.float64)
+        self._check(self._lib.eb_heat_export_coo(self._ctx, _ptr(Li), _ptr(Lj), _ptr(Lv), n.value, C.byref(n)))
+        R = np.empty(int(self._lib.eb_heat_size(self._ctx)), np.float64)
+        self._check(self._lib.eb_heat_rhs_download(self._ctx, _ptr(R)))
+        return Li, Lj, Lv, R
+
+    def update_marker_temp_for_grid_and_subgrid_changes(self, params: dict | None = None,
+                                                        **solve_kw) -> dict | None:
+        """HeatSolver.update_marker_temp_for_grid_and_subgrid_changes! (HeatSolver.jl:94-122): RHS
+        terms, tk0 = tk1, the heat loop, dtk1 = tk2 - tk1, the subgrid diffusion (when its
+        coefficient is positive) and the remaining change added to the marker temperature.
+        Runs only when timestep > 0, max_temp_change > 0 and iuse_heat == 1 (use_heat_solver)."""
+        p = params if params is not None else {}
+        hp = heat_params(p) if params is not None else getattr(self, "heat", None)
+        if hp is None or not (hp["timestep"] > 0 and hp["max_temp_change"] > 0 and hp["iuse_heat"] == 1):
+            return None
+        self.calculate_heat_rhs_terms(params)
+        self.initialize_old_temperature_array()
+        rep = self.run_conductive_heat_solver_loop(params, **solve_kw)
+        self.calculate_grid_temp_change()
+        if hp["subgrid_diff_coef_temp"] > 0:
+            self.subgrid_heat_diffusion_update()
+        self.add_remaining_grid_change_to_marker_temperature()
+        return rep
 
     # ----------------------------------------------------- step sequences --
     def marker_cycle(self) -> None:

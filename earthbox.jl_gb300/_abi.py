@@ -48,6 +48,8 @@ GRID_FIELDS = [
     "vx1_old", "vy1_old", "pr1_old",
     # nodal Picard variant (basic grid)
     "etavp_buffer", "plastic_yield_buffer", "plastic_strain_rate_buffer", "yield_error", "eii_plastic_basic",
+    # heat step (basic grid)
+    "RT1", "rest",
 ]
 GRID_ID = {n: i for i, n in enumerate(GRID_FIELDS)}
 
@@ -75,7 +77,7 @@ def grid_shape(name: str, xnum: int, ynum: int) -> tuple[int, int]:
     if name == "RY1":
         return (ynum, xnum + 1)
     if name in ("vxb", "vyb", "etavp_buffer", "plastic_yield_buffer", "plastic_strain_rate_buffer", "yield_error",
-                "eii_plastic_basic"):
+                "eii_plastic_basic", "RT1", "rest"):
         return (ynum, xnum)
     if name == "vx1_old":
         return (ynum + 1, xnum)
@@ -145,6 +147,24 @@ class SolveReport(C.Structure):
 
 STOKES_VECTORS = {"solution": 0, "rhs": 1, "solution_old": 2, "resnl": 3}
 
+
+class HeatParams(C.Structure):
+    _fields_ = [("timestep", C.c_double), ("max_temp_change", C.c_double), ("gravity_x", C.c_double),
+                ("gravity_y", C.c_double), ("iuse_adiabatic_heating", C.c_int32), ("iuse_shear_heating", C.c_int32)]
+
+
+class HeatLoopReport(C.Structure):
+    _fields_ = [("substeps", C.c_int32), ("solves", C.c_int32), ("iterations", C.c_int32), ("levels", C.c_int32),
+                ("timestep_sum", C.c_double), ("timestep_heat", C.c_double), ("max_rel_residual", C.c_double),
+                ("seconds", C.c_double)]
+
+
+HEAT_ENTRY_POINTS = [
+    "eb_calculate_heat_rhs_terms", "eb_initialize_old_temperature", "eb_build_heat_system", "eb_solve_heat_system",
+    "eb_heat_residuals", "eb_run_conductive_heat_solver_loop", "eb_calculate_grid_temp_change",
+    "eb_heat_export_coo", "eb_heat_rhs_download", "eb_heat_size",
+]
+
 STOKES_ENTRY_POINTS = [
     "eb_calc_viscoelastic_terms", "eb_viscoelastic_rhs", "eb_build_stokes_system", "eb_process_stokes_solution",
     "eb_stokes_nonlinear_residual", "eb_backup_stokes_arrays", "eb_update_grid_strain_rate_and_spin",
@@ -171,7 +191,7 @@ ALL_SYMBOLS = [
     "eb_calculate_stokes_norms", "eb_interpolate_basic_viscoplastic_viscosity_to_pressure_grid",
     "eb_update_nodes_for_plastic_yielding", "eb_stokes_export_coo",
     "eb_marker_to_basic_grid_average_noalloc",
-] + ENTRY_POINTS + STOKES_ENTRY_POINTS
+] + ENTRY_POINTS + STOKES_ENTRY_POINTS + HEAT_ENTRY_POINTS
 
 _lib = None
 
@@ -228,8 +248,21 @@ def load(path: pathlib.Path | str | None = None) -> C.CDLL:
     lib.eb_stokes_size.restype = C.c_int64
     lib.eb_marker_to_basic_grid_average_noalloc.argtypes = [vp, vp, vp, C.c_int64, vp, C.c_int64, vp, C.c_int64,
                                                             vp, vp, vp, C.c_char_p, C.c_size_t]
+    lib.eb_calculate_heat_rhs_terms.argtypes = [vp, C.POINTER(HeatParams)]
+    lib.eb_initialize_old_temperature.argtypes = [vp]
+    lib.eb_build_heat_system.argtypes = [vp, C.c_double]
+    lib.eb_solve_heat_system.argtypes = [vp, C.POINTER(SolveOpts), C.POINTER(SolveReport)]
+    lib.eb_heat_residuals.argtypes = [vp, C.c_double]
+    lib.eb_run_conductive_heat_solver_loop.argtypes = [vp, C.POINTER(HeatParams), C.POINTER(SolveOpts),
+                                                       C.POINTER(HeatLoopReport)]
+    lib.eb_calculate_grid_temp_change.argtypes = [vp]
+    lib.eb_heat_export_coo.argtypes = [vp, vp, vp, vp, C.c_int64, C.POINTER(C.c_int64)]
+    lib.eb_heat_rhs_download.argtypes = [vp, vp]
+    lib.eb_heat_size.argtypes = [vp]
+    lib.eb_heat_size.restype = C.c_int64
     for name in ALL_SYMBOLS:
-        if name not in ("eb_last_error", "eb_stream", "eb_launch_count", "eb_stokes_pscale", "eb_stokes_size"):
+        if name not in ("eb_last_error", "eb_stream", "eb_launch_count", "eb_stokes_pscale", "eb_stokes_size",
+                        "eb_heat_size"):
             getattr(lib, name).restype = C.c_int
     if path is None:
         _lib = lib

@@ -26,6 +26,7 @@ static Shape grid_shape(int f) {
   if (f <= EB_G_WTNODES_VY || f == EB_G_RY1 || f == EB_G_VY1_OLD) return SH_VY;
   if (f == EB_G_RC1 || f == EB_G_EII_PLASTIC_PRESSURE || f == EB_G_EII || f == EB_G_PR1_OLD) return SH_P;
   if (f == EB_G_VXB || f == EB_G_VYB || (f >= EB_G_ETAVP_BUFFER && f <= EB_G_EII_PLASTIC_BASIC)) return SH_B;
+  if (f == EB_G_RT1 || f == EB_G_REST) return SH_B;
   if (f == EB_G_BTOPT || f == EB_G_BBOTTOMT || f == EB_G_BTOPX || f == EB_G_BBOTTOMX) return SH_BCX;
   if (f == EB_G_BTOPY || f == EB_G_BBOTTOMY) return SH_BCX1;
   if (f == EB_G_BLEFTX || f == EB_G_BRIGHTX) return SH_BCY1;
@@ -246,6 +247,7 @@ extern "C" int eb_destroy(eb_ctx* c) {
   free_grid_tables(c);
   free_markers(c);
   stokes_free(c);
+  heat_free(c);
   for (void* p : c->mat_allocs) cudaFree(p);
   for (cudaEvent_t e : c->prof.pool) cudaEventDestroy(e);
   cudaFree(c->dflag);
@@ -328,6 +330,7 @@ extern "C" int eb_set_grid(eb_ctx* c, const eb_grid_desc* G) {
   c->h_gx.assign(G->gridx_b, G->gridx_b + X);
   c->h_gy.assign(G->gridy_b, G->gridy_b + Y);
   stokes_free(c);  // the Stokes system and its multigrid hierarchy follow the grid
+  heat_free(c);
   if ((rc = build_axis(c, G->gridx_b, X, &g.ax)) || (rc = build_axis(c, G->gridy_b, Y, &g.ay)) ||
       (rc = build_axis(c, G->gridx_vy, X + 1, &g.axvy)))
     return rc;

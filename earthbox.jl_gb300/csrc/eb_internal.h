@@ -69,6 +69,7 @@ struct Profiler {
 };
 
 struct StokesState;  // eb_stokes_solve.cu
+struct HeatState;    // eb_heat.cu
 
 struct eb_ctx {
   int device = 0;
@@ -104,6 +105,8 @@ struct eb_ctx {
   eb_stokes_params SP{};
   bool have_stokes_params = false;
   StokesState* st = nullptr;
+  // conductive heat step
+  HeatState* ht = nullptr;
 };
 
 // Stokes system storage shared by the assembly (eb_stokes_build.cu) and the
@@ -137,6 +140,8 @@ int launch_nodal_yield(eb_ctx* c, const eb_mobile_wall* w, double* d_partial, in
 int launch_apply_nodal_yield(eb_ctx* c);
 int export_stokes_coo(eb_ctx* c, const StokesSystem* s, int64_t* Li, int64_t* Lj, double* Lv, int64_t capacity,
                       int64_t* nnz);
+
+void heat_free(eb_ctx* c);  // eb_heat.cu
 
 constexpr int kMaxSlots = 48;
 

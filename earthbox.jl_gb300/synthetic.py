@@ -177,8 +177,9 @@ def _analytic_grids(grid: Grid, v0: float, eta_ref: float, rho_ref: float, T0: f
     exx_p = 2.0 * v0 / W + A * ky * np.cos(kx * Xp) * np.cos(ky * Yp)
     out["exx"] = F(exx_p)
     out["exy"] = F(0.5 * A * (-ky * ky / kx + kx) * np.sin(kx * Xb) * np.sin(ky * Yb))
-    out["sxx2"] = F(2.0 * eta_ref * exx_p)
-    out["sxy2"] = F(2.0 * eta_ref * out["exy"])
+    # deviatoric stress vanishes in the sticky layer (y < y_surface)
+    out["sxx2"] = F(np.where(Yp < y_surface, 0.0, 2.0 * eta_ref * exx_p))
+    out["sxy2"] = F(np.where(Yb < y_surface, 0.0, 2.0 * eta_ref * out["exy"]))
     out["dsxx"] = F(0.05 * out["sxx2"])
     out["dsxy"] = F(0.05 * out["sxy2"])
     depth_p = np.clip(Yp - y_surface, 0.0, None)

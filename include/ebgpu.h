@@ -148,6 +148,8 @@ enum eb_grid_field {
    * plastic_strain_rate_buffer, yield_error, eii_plastic_basic */
   EB_G_ETAVP_BUFFER, EB_G_PLASTIC_YIELD_BUFFER, EB_G_PLASTIC_STRAIN_RATE_BUFFER, EB_G_YIELD_ERROR,
   EB_G_EII_PLASTIC_BASIC,
+  /* heat step (basic grid): RHS terms RT1 (HeatRhs.jl), residuals rest (HeatResiduals.jl) */
+  EB_G_RT1, EB_G_REST,
   EB_G_NFIELDS
 };
 
@@ -413,6 +415,69 @@ int eb_stokes_stencil_download(eb_ctx* ctx, double* host);
 
 double  eb_stokes_pscale(const eb_ctx* ctx);  /* pscale of the last eb_build_stokes_system */
 int64_t eb_stokes_size(const eb_ctx* ctx);    /* N = 3 (xnum-1)(ynum-1), 0 before eb_set_grid */
+
+/* ---- conductive heat step (src/heat_solver) --------------------------------
+ * Grid fields read: tk1, kt1, rhocp1, hr1, ha1, rho1, vx1, vy1, sxy2, etas1, sxx2,
+ * etan1 and the thermal BC arrays btopt, bbottomt (xnum, 2), bleftt, brightt (ynum, 2)
+ * (tk[1,j] = btopt[j,1] + btopt[j,2] tk[2,j], and so on).  Written: RT1, tk0, tk2,
+ * dtk1, rest.  The heat system has N = xnum*ynum unknowns, node (i, j) at
+ * (j-1)*ynum + i (the reference's itk, HeatBuildManager.jl:55). */
+typedef struct eb_heat_params {
+  double  timestep;                /* main time step (s): the heat loop integrates over it      */
+  double  max_temp_change;         /* K: larger grid changes shorten the heat-loop step        */
+  double  gravity_x, gravity_y;    /* adiabatic heating term (HeatRhs.jl:28-47)                */
+  int32_t iuse_adiabatic_heating;  /* 1: add alpha*T*rho*(g . v) to RT1                         */
+  int32_t iuse_shear_heating;      /* 1: add sxy2^2/etas1 + <sxx2^2/etan1> to RT1               */
+} eb_heat_params;
+
+typedef struct eb_heat_loop_report {
+  int32_t substeps;        /* passes of the heat loop                                      */
+  int32_t solves;          /* heat solves (a pass that shortens its step solves twice)     */
+  int32_t iterations;      /* conjugate-gradient iterations over all solves                */
+  int32_t levels;          /* multigrid levels of the preconditioner                       */
+  double  timestep_sum;    /* integrated heat time (s) = timestep on exit                  */
+  double  timestep_heat;   /* heat-loop step after the last pass (s)                       */
+  double  max_rel_residual;/* largest ||R - L T||_2 / ||R||_2 over the solves              */
+  double  seconds;         /* wall time of the loop                                        */
+} eb_heat_loop_report;
+
+/* HeatSolver.calculate_heat_rhs_terms_grid! (heat_solver/HeatSolver.jl:139-150):
+ * RT1 = hr1 (+ adiabatic, + shear heating terms, rhs/HeatRhs.jl:5-80).                */
+int eb_calculate_heat_rhs_terms(eb_ctx* ctx, const eb_heat_params* hp);
+/* HeatSolver.initialize_old_temperature_array! (HeatSolver.jl:199-204): tk0 = tk1.   */
+int eb_initialize_old_temperature(eb_ctx* ctx);
+/* HeatBuildManager.build_system_of_equations (solver/build_system/HeatBuildManager.jl:44-86)
+ * for the heat-loop step timestep_heat: the 5-point system in the reference's coefficients
+ * (bit-identical) from tk0, rhocp1, kt1, RT1 and the thermal BC arrays.                */
+int eb_build_heat_system(eb_ctx* ctx, double timestep_heat);
+/* The solve of SystemSolver.discretize_and_solve_conductive_heat_equation
+ * (solver/SystemSolver.jl:32-66: MUMPS or UMFPACK) and reload_solu_temp (:85-110):
+ * tk2 = L^-1 R.  The BC rows are folded into an area-scaled symmetric system on the
+ * internal nodes, solved by flexible conjugate gradients with an FP32 multigrid
+ * V-cycle; the BC rows then give the boundary values exactly.  opts: rtol (default
+ * 1e-12, on the scaled internal system), max_iters, mg_sweeps (default 2),
+ * use_initial_guess (1: start from tk0; default); restart and method are unused.
+ * report->rel_residual is ||R - L tk2||_2 / ||R||_2 of the reference's system.        */
+int eb_solve_heat_system(eb_ctx* ctx, const eb_solve_opts* opts, eb_solve_report* report);
+/* HeatResiduals.compute_residuals_temp! (solver/residuals/HeatResiduals.jl:12-162):
+ * rest from RT1, rhocp1, tk0, tk2, kt1 at the heat-loop step timestep_heat.           */
+int eb_heat_residuals(eb_ctx* ctx, double timestep_heat);
+/* HeatLoop.run_conductive_heat_solver_loop! (heat_loop/HeatLoop.jl:10-79): the
+ * adaptive heat loop over hp->timestep, each pass building, solving and computing the
+ * residuals, shortening its step to max_temp_change / max|tk2 - tk0| when the change
+ * exceeds max_temp_change, then tk0 = tk2.  Leaves dtk1 = tk2 - tk0 of the last pass's
+ * first solve, as the reference does.                                                 */
+int eb_run_conductive_heat_solver_loop(eb_ctx* ctx, const eb_heat_params* hp, const eb_solve_opts* opts,
+                                       eb_heat_loop_report* report);
+/* HeatSolver.calculate_grid_temp_change! (HeatSolver.jl:211-216): dtk1 = tk2 - tk1.   */
+int eb_calculate_grid_temp_change(eb_ctx* ctx);
+/* The assembled heat system as the reference's COO list (1-based Li, Lj; Lv) in
+ * HeatBuildManager's entry order, for parallel_direct_solver or UMFPACK on the host;
+ * with Li, Lj or Lv null only *nnz is set.                                             */
+int eb_heat_export_coo(eb_ctx* ctx, int64_t* Li, int64_t* Lj, double* Lv, int64_t capacity, int64_t* nnz);
+/* The right-hand side R of the last eb_build_heat_system (N doubles).                 */
+int eb_heat_rhs_download(eb_ctx* ctx, double* host);
+int64_t eb_heat_size(const eb_ctx* ctx);      /* N = xnum*ynum, 0 before eb_set_grid */
 
 /* ---- allocation-free entry point -------------------------------------------
  * No counterpart in the reference.  For callers that cannot call cudaMalloc

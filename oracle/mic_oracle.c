@@ -19,6 +19,7 @@
  */
 #include <math.h>
 #include <stdint.h>
+#include <stdlib.h>
 #include <string.h>
 #ifdef _OPENMP
 #include <omp.h>
@@ -576,6 +577,31 @@ void o_subgrid_stress(int64_t M, const int8_t* flags, int64_t xnum, int64_t ynum
   for (int64_t k = 0; k < np; ++k) if (wtetan[k] != 0) dsxxn[k] = dsxxn[k] / wtetan[k];
   for (int64_t k = 0; k < nb; ++k) dsxy[k] = dsxy[k] - dsxyn[k];
   for (int64_t k = 0; k < np; ++k) dsxx[k] = dsxx[k] - dsxxn[k];
+}
+
+/* Exclusive (basic grid) and central (pressure grid) weighted averages of per-marker values,
+ * with the weights of the scatters above; nodes without markers get 0.  Test-side error
+ * scales (the average of |contribution| bounds the rounding of a weighted sum). */
+void o_excl_cent_average(int64_t M, const int8_t* flags, int64_t xnum, int64_t ynum, const int32_t* xn,
+                         const int32_t* yn, const double* dx, const double* dy, const double* wUL,
+                         const double* wLL, const double* wUR, const double* wLR, const double* wC,
+                         const double* v_excl, const double* v_cent, double* avg_excl, double* avg_cent) {
+  const int64_t nb = ynum * xnum, np = (ynum - 1) * (xnum - 1);
+  double* we = (double*)calloc((size_t)nb, sizeof(double));
+  double* wc = (double*)calloc((size_t)np, sizeof(double));
+  memset(avg_excl, 0, sizeof(double) * nb);
+  memset(avg_cent, 0, sizeof(double) * np);
+  for (int64_t m = 0; m < M; ++m) {
+    if (flags[m] != 1) continue;
+    upd_excl(avg_excl, ynum, yn[m], xn[m], wUL[m], wLL[m], wUR[m], wLR[m], dx[m], dy[m], v_excl[m]);
+    upd_excl(we, ynum, yn[m], xn[m], wUL[m], wLL[m], wUR[m], wLR[m], dx[m], dy[m], 1.0);
+    upd_cent(avg_cent, ynum - 1, yn[m], xn[m], wC[m], v_cent[m]);
+    upd_cent(wc, ynum - 1, yn[m], xn[m], wC[m], 1.0);
+  }
+  for (int64_t k = 0; k < nb; ++k) if (we[k] != 0) avg_excl[k] /= we[k];
+  for (int64_t k = 0; k < np; ++k) if (wc[k] != 0) avg_cent[k] /= wc[k];
+  free(we);
+  free(wc);
 }
 
 /* StressCorrection.apply_marker_stress_correction_for_remaining_grid_stress! (StressCorrection.jl:35-82) */

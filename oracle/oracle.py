@@ -189,6 +189,19 @@ class OracleMIC:
             P(k["sxy"]), P(k["sxx"]), P(gr["dsxyn"]), P(gr["dsxxn"]), P(gr["wtetas"]), P(gr["wtetan"]),
             P(gr["dsxy"]), P(gr["dsxx"]))
 
+    def excl_cent_average(self, v_excl, v_cent):
+        """Weighted averages of per-marker values with the exclusive (basic grid) and central
+        (pressure grid) weights of the current marker positions (test-side error scales)."""
+        k, g = self.mk, self.g
+        ve = np.ascontiguousarray(v_excl, dtype=np.float64)
+        vc = np.ascontiguousarray(v_cent, dtype=np.float64)
+        ae = np.zeros((g.ynum, g.xnum), order="F")
+        ac = np.zeros((g.ynum - 1, g.xnum - 1), order="F")
+        lib().o_excl_cent_average(I(self.M), P(k["inside"]), I(g.xnum), I(g.ynum), P(k["xn"]), P(k["yn"]),
+                                  P(k["dx"]), P(k["dy"]), P(k["wUL"]), P(k["wLL"]), P(k["wUR"]), P(k["wLR"]),
+                                  P(k["wC"]), P(ve), P(vc), P(ae), P(ac))
+        return ae, ac
+
     def apply_marker_stress_correction(self):
         k, g, gr = self.mk, self.g, self.gr
         lib().o_stress_correction(I(self.M), P(k["inside"]), I(g.xnum), I(g.ynum), P(k["x"]), P(k["y"]),

@@ -161,6 +161,18 @@ def stress_scale(ref):
     return np.hypot(ref.mk["sxx"], ref.mk["sxy"])
 
 
+def subgrid_change_scale(oracle, model, steps_before):
+    """Error scales of the averaged subgrid stress changes dsxyn, dsxxn: the weighted averages
+    of |marker stress change| (the terms of each weighted sum), from an oracle run of the steps
+    before update_subgrid_stress and of that step."""
+    o = oracle.OracleMIC(model)
+    for st in steps_before:
+        getattr(o, st)()
+    sxy0, sxx0 = o.mk["sxy"].copy(), o.mk["sxx"].copy()
+    o.update_subgrid_stress()
+    return o.excl_cent_average(np.abs(o.mk["sxy"] - sxy0), np.abs(o.mk["sxx"] - sxx0))
+
+
 def test_scatter_stokes(eb, oracle, pair):
     model, _, _ = pair
     mic = fresh(eb, oracle, model)[0]
@@ -211,9 +223,17 @@ def test_gathers(eb, oracle, pair):
         close(mic.download_marker(f), ref.mk[f], f, scale=local_max(model.grids[f if f != "pr" else "pr1"], ref))
     # the strain-rate ratio divides stress-based by velocity-based invariants built from
     # gathers: its error scale is the ratio of the local magnitudes
+    # and the stress-based invariant is itself made of gathered stresses: the local stress
+    # magnitudes over the marker's viscosity (and dt*mu) set its error scale
     e_loc = np.hypot(local_max(model.grids["exx"], ref), local_max(model.grids["exy"], ref))
     e_here = np.maximum(np.hypot(ref.mk["exx"], ref.mk["exy"]), 1e-300)
-    close(mic.download_marker("sr_ratio"), ref.mk["sr_ratio"], "sr_ratio", scale=ref.mk["sr_ratio"] * e_loc / e_here)
+    mu = model.mats.mat_mu[ref.mk["matid"].astype(np.int64) - 1]
+    tf = 1.0 / (model.params["timestep"] * mu)
+    eta = ref.mk["eta"]
+    num_loc = 0.5 * np.hypot(local_max(model.grids["sxx2"], ref) / eta + local_max(model.grids["dsxx"], ref) * tf,
+                             local_max(model.grids["sxy2"], ref) / eta + local_max(model.grids["dsxy"], ref) * tf)
+    close(mic.download_marker("sr_ratio"), ref.mk["sr_ratio"], "sr_ratio",
+          scale=ref.mk["sr_ratio"] * e_loc / e_here + num_loc / e_here)
     mic.upload_grid("tk1", model.grids["tk2"])
     ref.gr["tk1"][:] = model.grids["tk2"]
     mic.interpolate_temperature_to_markers()
@@ -232,10 +252,11 @@ def test_subgrid_stress_and_correction(eb, oracle, pair):
     s_loc = stress_scale(ref) + np.hypot(local_max(model.grids["sxx1"], ref), local_max(model.grids["sxy1"], ref))
     for f in ("sxx", "sxy"):
         close(mic.download_marker(f), ref.mk[f], f, scale=s_loc)
+    sc = dict(zip(("dsxyn", "dsxxn"), subgrid_change_scale(oracle, model, steps[:-1])))
     for f in ("dsxyn", "dsxxn"):
-        close(mic.download_grid(f), ref.gr[f], f, scale=refa.gr[f])
+        close(mic.download_grid(f), ref.gr[f], f, scale=sc[f])
     for f, fn in (("dsxy", "dsxyn"), ("dsxx", "dsxxn")):
-        close(mic.download_grid(f), ref.gr[f], f, scale=np.abs(model.grids[f]) + refa.gr[fn])
+        close(mic.download_grid(f), ref.gr[f], f, scale=np.abs(model.grids[f]) + sc[fn])
     for f in ("wtetas", "wtetan"):
         close(mic.download_grid(f), ref.gr[f], f)
     mic.apply_marker_stress_correction()
@@ -338,10 +359,13 @@ def test_full_marker_cycle(eb, oracle, pair):
     for f in ("rho1", "etas1", "etan1", "tk1"):
         close(mic.download_grid(f), ref.gr[f], f)
     close(mic.download_grid("dtk1"), ref.gr["dtk1"], "dtk1", scale=ref.gr["tk1"])
-    # dsxy = input change - averaged relaxed marker stress change: its terms are as large as the
-    # marker and grid stresses being relaxed
-    close(mic.download_grid("dsxy"), ref.gr["dsxy"], "dsxy",
-          scale=np.abs(model.grids["dsxy"]) + refa.gr["sxy1"] + np.abs(ref.gr["sxy1"]))
+    # dsxy = input change - averaged relaxed marker stress change: its terms are the input and
+    # the marker stress changes being averaged
+    sc_xy, _ = subgrid_change_scale(oracle, model, ["get_marker_inside_flags", "initialize_bilinear_interpolation",
+                                                    "interpolate_marker_heat_parameters_to_grid",
+                                                    "interpolate_marker_stokes_parameters_to_grid",
+                                                    "post_stokes_marker_gathers"])
+    close(mic.download_grid("dsxy"), ref.gr["dsxy"], "dsxy", scale=np.abs(model.grids["dsxy"]) + sc_xy)
     mic.close()
 
 
