@@ -71,6 +71,7 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-stokes", action="store_true")
+    ap.add_argument("--no-heat", action="store_true")
     ap.add_argument("--stokes-method", default="fgmres", choices=["fgmres", "bicgstab"])
     return ap.parse_args()
 
@@ -192,6 +193,49 @@ def stokes_gpu(mic, reps: int = 2, method: str = "fgmres"):
     prof = mic.profile()
     mic.profile_enable(False)
     return dt, reps_out[-1], prof
+
+
+def heat_gpu(mic, reps: int = 2):
+    """The grid part of the heat step (HeatSolver.update_marker_temp_for_grid_and_subgrid_changes!
+    up to dtk1): RHS terms, tk0 = tk1, the adaptive heat loop, dtk1 = tk2 - tk1.  One warm-up
+    (level set-up, graph capture), then `reps` timed steps (wall clock: the loop is host-driven)."""
+    import torch
+
+    def one():
+        mic.calculate_heat_rhs_terms()
+        mic.initialize_old_temperature_array()
+        rep = mic.run_conductive_heat_solver_loop()
+        mic.calculate_grid_temp_change()
+        return rep
+
+    one()
+    torch.cuda.synchronize()
+    mic.profile_enable(True)
+    t0 = time.perf_counter()
+    reps_out = [one() for _ in range(reps)]
+    torch.cuda.synchronize()
+    dt = (time.perf_counter() - t0) / reps
+    prof = mic.profile()
+    mic.profile_enable(False)
+    return dt, reps_out[-1], prof
+
+
+def heat_cpu_sample(eb, oracle_mod, strip):
+    """The oracle's heat step (assembly + scipy SuperLU standing in for UMFPACK/MUMPS) on the
+    101x801 strip, inputs from the oracle's marker averages."""
+    from oracle.heat import HeatOracle, HEAT_GRIDS
+    ref = oracle_mod.OracleMIC(strip)
+    ref.get_marker_inside_flags()
+    ref.initialize_bilinear_interpolation()
+    ref.interpolate_marker_heat_parameters_to_grid()
+    ref.interpolate_marker_stokes_parameters_to_grid()
+    ho = HeatOracle(strip, {k: ref.gr[k] for k in HEAT_GRIDS if k in ref.gr})
+    t0 = time.perf_counter()
+    ho.heat_step()
+    dt = time.perf_counter() - t0
+    return {"value": dt, "unit": "s/step", "cores": 1, "kind": "port",
+            "sample": f"101x801-node strip, N={ho.N} unknowns, {ho.solves} solve(s): oracle assembly + scipy "
+                      f"SuperLU per heat-loop pass"}
 
 
 def stokes_cpu_sample(eb, oracle_mod):
@@ -397,6 +441,68 @@ def main():
             except Exception as exc:
                 stokes["cpu_baseline"] = {"value": None, "sample": f"failed: {exc}"}
 
+    # heat step of the same model (grids from the marker cycle and the Stokes step)
+    heat = None
+    if not args.no_heat:
+        h_dt, h_rep, h_prof = heat_gpu(mic, reps=2)
+        h_kern = {k: (t / n, n) for k, (t, n) in h_prof.items()}
+        n_nodes = model.grid.xnum * model.grid.ynum
+        heat = {"metric": "heat s/step", "value": h_dt, "unit": "s/step", "higher_is_better": False,
+                "workload": f"{args.workload}: {model.grid.xnum}x{model.grid.ynum} nodes, N={n_nodes} unknowns",
+                "includes": "RHS terms, tk0 = tk1, adaptive heat loop (assembly, MG-CG solve to 1e-12, residuals), "
+                            "dtk1",
+                **{k: h_rep[k] for k in ("substeps", "solves", "iterations", "levels", "max_rel_residual")},
+                "kernels_ms": {k: round(v[0] * v[1], 3) for k, v in
+                               sorted(h_kern.items(), key=lambda kv: -kv[1][0] * kv[1][1])[:10]}}
+        # roofline of the FP64 operator product (d, cx, cy, x read; y written per internal node)
+        if "k_heat_apply" in h_kern:
+            t_apply, n_apply = h_kern["k_heat_apply"]
+            nq = (model.grid.xnum - 2) * (model.grid.ynum - 2)
+            peak, peak_kind = peaks()
+            ach = nq * 5 * 8.0 / (t_apply * 1e-3) / 1e9
+            heat["roofline"] = {"bound": "hbm", "kernel": "k_heat_apply", "achieved": ach, "peak": peak,
+                                "unit": "GB/s", "frac": ach / peak, "peak_kind": peak_kind, "traffic": None,
+                                "bytes_per_node": 40, "launch_ms": t_apply}
+        if rank == 0 and world == 1 and not args.no_cpu:
+            try:
+                strip = eb.synthetic.rift(101, 801, 5, width=25e3)
+                h_cpu = heat_cpu_sample(eb, load_oracle(), strip)
+                smic = eb.MarkerInCell(local)
+                smic.load_model(strip)
+                smic.get_marker_inside_flags()
+                smic.initialize_bilinear_interpolation()
+                smic.interpolate_marker_heat_parameters_to_grid()
+                smic.interpolate_marker_stokes_parameters_to_grid()
+                g_dt, g_rep, _ = heat_gpu(smic, reps=2)
+                smic.close()
+                heat["cpu_baseline"] = h_cpu
+                heat["gpu_same_sample"] = {"value": g_dt, "unit": "s/step", "solves": g_rep["solves"],
+                                           "iterations": g_rep["iterations"]}
+            except Exception as exc:
+                heat["cpu_baseline"] = {"value": None, "sample": f"failed: {exc}"}
+
+    # one whole time step, measured: marker cycle, Stokes step, heat step back to back
+    timestep = None
+    if not args.no_stokes and not args.no_heat:
+        import torch
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(2):
+            step()
+            mic.calc_viscoelastic_terms()
+            mic.viscoelastic_rhs()
+            mic.build_system_of_equations()
+            mic.solve_system(rtol=1e-8, check=False, method=args.stokes_method)
+            mic.process_stokes_solution()
+            mic.calculate_heat_rhs_terms()
+            mic.initialize_old_temperature_array()
+            mic.run_conductive_heat_solver_loop()
+            mic.calculate_grid_temp_change()
+        torch.cuda.synchronize()
+        timestep = {"metric": "per-timestep wall time", "value": (time.perf_counter() - t0) / 2, "unit": "s/step",
+                    "higher_is_better": False,
+                    "includes": "marker cycle (transfer + RK4), Stokes step (solve to 1e-8), heat step"}
+
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                 "warmup": max(args.warmup, 3), "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
@@ -405,7 +511,7 @@ def main():
                            "markers_per_cell": 25 if args.workload == "rift_40M" else None,
                            "l2": "inputs larger than L2 (each marker field 320 MB)", "parallelism": "replicas"},
                 "gpu_launches": launches, "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
-                "clocks": clk.summary(), "stokes": stokes,
+                "clocks": clk.summary(), "stokes": stokes, "heat": heat, "timestep": timestep,
                 "kernels_ms": {k: round(v[0], 4) for k, v in sorted(kern.items(), key=lambda kv: -kv[1][0] * kv[1][1])},
                 "generate_s": round(t_gen, 2)}
         print(json.dumps(line))
