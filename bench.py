@@ -72,6 +72,8 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-stokes", action="store_true")
     ap.add_argument("--no-heat", action="store_true")
+    ap.add_argument("--circles", action="store_true",
+                    help="also time the circles_1025 Stokes benchmark (200 inclusions, 1e-10)")
     ap.add_argument("--stokes-method", default="fgmres", choices=["fgmres", "bicgstab"])
     return ap.parse_args()
 
@@ -169,7 +171,7 @@ STOKES_GRIDS = ("etas1", "etan1", "mus1", "mun1", "sxy1", "sxx1", "rho1", "rho1_
                 "brighty")
 
 
-def stokes_gpu(mic, reps: int = 2, method: str = "fgmres"):
+def stokes_gpu(mic, reps: int = 2, method: str = "fgmres", rtol: float = 1e-8):
     """The Stokes step on the grids the context holds: build steps, solve to 1e-8, unpack.
     One warm-up (level set-up, graph capture), then `reps` timed steps (wall clock: the
     FGMRES loop is host-driven)."""
@@ -179,7 +181,7 @@ def stokes_gpu(mic, reps: int = 2, method: str = "fgmres"):
         mic.calc_viscoelastic_terms()
         mic.viscoelastic_rhs()
         mic.build_system_of_equations()
-        rep = mic.solve_system(rtol=1e-8, check=False, method=method)
+        rep = mic.solve_system(rtol=rtol, check=False, method=method)
         mic.process_stokes_solution()
         return rep
 
@@ -193,6 +195,27 @@ def stokes_gpu(mic, reps: int = 2, method: str = "fgmres"):
     prof = mic.profile()
     mic.profile_enable(False)
     return dt, reps_out[-1], prof
+
+
+def link_bandwidth(device: int, nbytes: int = 1 << 30) -> dict:
+    """Host<->device copy rate of one large pinned buffer (best of 3, CUDA events), the
+    denominator of the e2e copies."""
+    import torch
+    h = torch.empty(nbytes, dtype=torch.uint8).pin_memory()
+    d = torch.empty(nbytes, dtype=torch.uint8, device=f"cuda:{device}")
+    out = {}
+    for name, dst, src in (("h2d_gbs", d, h), ("d2h_gbs", h, d)):
+        best = None
+        for _ in range(3):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            dst.copy_(src, non_blocking=True)
+            e1.record()
+            torch.cuda.synchronize()
+            t = e0.elapsed_time(e1) * 1e-3
+            best = t if best is None else min(best, t)
+        out[name] = round(nbytes / best / 1e9, 1)
+    return out
 
 
 def heat_gpu(mic, reps: int = 2):
@@ -359,6 +382,15 @@ def main():
         h2d = sum(a.nbytes for a in pinned_in.values())
         d2h = sum(a.nbytes for a in pinned_out.values())
         reps = max(2, min(args.steps, 5))
+        # one call per step with host arrays (eb_marker_cycle_host): the copies overlap the steps
+        mic.marker_cycle_host(pinned_in, pinned_out)  # warm-up
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            mic.marker_cycle_host(pinned_in, pinned_out)
+        torch.cuda.synchronize()
+        te = (time.perf_counter() - t0) / reps
+        # the same through the per-field upload/download calls and the eleven step calls
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         for _ in range(reps):
@@ -368,9 +400,14 @@ def main():
             for k, a in pinned_out.items():
                 mic._check(mic._lib.eb_marker_download(mic._ctx, eb._abi.MARKER_ID[k], a.ctypes.data))
         torch.cuda.synchronize()
-        te = (time.perf_counter() - t0) / reps
+        ts = (time.perf_counter() - t0) / reps
+        link = link_bandwidth(local)
         e2e = {"value": M * world / te, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-               "ms_per_step": te * 1e3}
+               "ms_per_step": te * 1e3, "call": "eb_marker_cycle_host (pinned host arrays in and out)",
+               "link": link,
+               "copy_bound_ms": round(max(h2d / link["h2d_gbs"], d2h / link["d2h_gbs"]) / 1e6, 2),
+               "sequential": {"value": M * world / ts, "ms_per_step": ts * 1e3,
+                              "call": "eb_marker_upload x20, 11 step calls, eb_marker_download x12"}}
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -440,6 +477,29 @@ def main():
                                              "rel_residual": g_rep["rel_residual"]}
             except Exception as exc:
                 stokes["cpu_baseline"] = {"value": None, "sample": f"failed: {exc}"}
+
+    # the circles solver benchmark: 1025 x 1025 nodes, 200 inclusions (1e18-1e27 Pa s), to 1e-10
+    stokes_circles = None
+    if not args.no_stokes and args.circles:
+        cm = eb.synthetic.config("circles_1025")
+        cmic = eb.MarkerInCell(local)
+        cmic.set_grid(cm.grid)
+        cmic.set_params(cm.params)
+        cmic.set_stokes_params(cm.params)
+        for k, v in cm.grids.items():
+            cmic.upload_grid(k, v)
+        c_dt, c_rep, c_prof = stokes_gpu(cmic, reps=2, rtol=1e-10)
+        cmic.close()
+        c_kern = {k: (t / n, n) for k, (t, n) in c_prof.items()}
+        stokes_circles = {"metric": "Stokes s/solve @1e-10 resid", "value": c_dt, "unit": "s/solve",
+                          "higher_is_better": False,
+                          "workload": "circles_1025: 1025x1025 nodes, N=3145728 unknowns, 200 circles, "
+                                      "log10 eta U(18, 27), free slip",
+                          "iterations": c_rep["iterations"], "levels": c_rep["levels"],
+                          "rel_residual": c_rep["rel_residual"], "rel_residual_scaled": c_rep["rel_residual_scaled"],
+                          "status": c_rep["status"],
+                          "kernels_ms": {k: round(v[0] * v[1], 3) for k, v in
+                                         sorted(c_kern.items(), key=lambda kv: -kv[1][0] * kv[1][1])[:8]}}
 
     # heat step of the same model (grids from the marker cycle and the Stokes step)
     heat = None
@@ -511,7 +571,8 @@ def main():
                            "markers_per_cell": 25 if args.workload == "rift_40M" else None,
                            "l2": "inputs larger than L2 (each marker field 320 MB)", "parallelism": "replicas"},
                 "gpu_launches": launches, "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
-                "clocks": clk.summary(), "stokes": stokes, "heat": heat, "timestep": timestep,
+                "clocks": clk.summary(), "stokes": stokes, "stokes_circles": stokes_circles, "heat": heat,
+                "timestep": timestep,
                 "kernels_ms": {k: round(v[0], 4) for k, v in sorted(kern.items(), key=lambda kv: -kv[1][0] * kv[1][1])},
                 "generate_s": round(t_gen, 2)}
         print(json.dumps(line))

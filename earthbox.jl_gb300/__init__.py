@@ -551,6 +551,26 @@ class MarkerInCell:
         return rep
 
     # ----------------------------------------------------- step sequences --
+    def marker_cycle_host(self, inputs: dict, outputs: dict) -> None:
+        """The marker cycle from host arrays (eb_marker_cycle_host): `inputs` maps field names to
+        host arrays copied in before the steps that read them, `outputs` maps field names to host
+        arrays filled as soon as the last step writing each has finished.  Arrays must have the
+        field's dtype and marknum elements; pinned host memory lets the copies overlap the steps."""
+        def check(name, a):
+            want = np.dtype(_abi.MARKER_DTYPE[name])
+            if a.dtype != want or a.shape != (self.marknum,) or not a.flags.c_contiguous:
+                raise ValueError(f"{name}: need a contiguous {want} array of {self.marknum} markers")
+        for k, a in inputs.items():
+            check(k, a)
+        for k, a in outputs.items():
+            check(k, a)
+        fin = (C.c_int32 * len(inputs))(*[_abi.MARKER_ID[k] for k in inputs])
+        hin = (C.c_void_p * len(inputs))(*[a.ctypes.data for a in inputs.values()])
+        fout = (C.c_int32 * len(outputs))(*[_abi.MARKER_ID[k] for k in outputs])
+        hout = (C.c_void_p * len(outputs))(*[a.ctypes.data for a in outputs.values()])
+        io = _abi.MarkerIO(len(inputs), fin, hin, len(outputs), fout, hout)
+        self._check(self._lib.eb_marker_cycle_host(self._ctx, C.byref(io)))
+
     def marker_cycle(self) -> None:
         """The marker-in-cell transfer + RK4 sequence of one time step (no Stokes/heat solve):
         locate, heat and Stokes scatters, post-Stokes gathers, subgrid stress and temperature,

@@ -148,6 +148,11 @@ class SolveReport(C.Structure):
 STOKES_VECTORS = {"solution": 0, "rhs": 1, "solution_old": 2, "resnl": 3}
 
 
+class MarkerIO(C.Structure):
+    _fields_ = [("n_in", C.c_int32), ("in_fields", C.POINTER(C.c_int32)), ("in_host", C.POINTER(C.c_void_p)),
+                ("n_out", C.c_int32), ("out_fields", C.POINTER(C.c_int32)), ("out_host", C.POINTER(C.c_void_p))]
+
+
 class HeatParams(C.Structure):
     _fields_ = [("timestep", C.c_double), ("max_temp_change", C.c_double), ("gravity_x", C.c_double),
                 ("gravity_y", C.c_double), ("iuse_adiabatic_heating", C.c_int32), ("iuse_shear_heating", C.c_int32)]
@@ -190,7 +195,7 @@ ALL_SYMBOLS = [
     "eb_stokes_vector_download", "eb_stokes_stencil_download", "eb_stokes_pscale", "eb_stokes_size",
     "eb_calculate_stokes_norms", "eb_interpolate_basic_viscoplastic_viscosity_to_pressure_grid",
     "eb_update_nodes_for_plastic_yielding", "eb_stokes_export_coo",
-    "eb_marker_to_basic_grid_average_noalloc",
+    "eb_marker_to_basic_grid_average_noalloc", "eb_marker_cycle_host",
 ] + ENTRY_POINTS + STOKES_ENTRY_POINTS + HEAT_ENTRY_POINTS
 
 _lib = None
@@ -248,6 +253,7 @@ def load(path: pathlib.Path | str | None = None) -> C.CDLL:
     lib.eb_stokes_size.restype = C.c_int64
     lib.eb_marker_to_basic_grid_average_noalloc.argtypes = [vp, vp, vp, C.c_int64, vp, C.c_int64, vp, C.c_int64,
                                                             vp, vp, vp, C.c_char_p, C.c_size_t]
+    lib.eb_marker_cycle_host.argtypes = [vp, C.POINTER(MarkerIO)]
     lib.eb_calculate_heat_rhs_terms.argtypes = [vp, C.POINTER(HeatParams)]
     lib.eb_initialize_old_temperature.argtypes = [vp]
     lib.eb_build_heat_system.argtypes = [vp, C.c_double]

@@ -85,17 +85,37 @@ EB_DEV int32_t axis_search(const Axis& a, double x) {
 
 EB_DEV int32_t clamp_i(int32_t v, int32_t lo, int32_t hi) { return v < lo ? lo : (v > hi ? hi : v); }
 
-// ---- compensated FP32 accumulation (Neumaier) ---------------------------------
+// ---- compensated FP32 accumulation ------------------------------------------------
+// Each add records its exact rounding error (Knuth's TwoSum: six additions, no
+// comparison) in a running correction c; the result is s + c.
 struct KSum {
   float s, c;
   EB_DEV void init() { s = 0.f; c = 0.f; }
   EB_DEV void add(float v) {
-    float t = s + v;
-    float e = (fabsf(s) >= fabsf(v)) ? ((s - t) + v) : ((v - t) + s);
-    c += e;
+    const float t = s + v;
+    const float z = t - s;
+    c += (s - (t - z)) + (v - z);
     s = t;
   }
   EB_DEV float get() const { return s + c; }
+};
+// Two compensated accumulators in packed FP32x2 arithmetic (TwoSum per lane of the
+// pair; a - b is computed as fma(b, -1, a), which rounds once like a subtraction).
+EB_DEV void two_sum2(float2& s, float2& c, float2 v) {
+  const float2 m1 = make_float2(-1.f, -1.f);
+  const float2 t = __fadd2_rn(s, v);
+  const float2 z = __ffma2_rn(s, m1, t);                                    // t - s
+  const float2 e = __fadd2_rn(__ffma2_rn(__ffma2_rn(z, m1, t), m1, s),      // s - (t - z)
+                              __ffma2_rn(z, m1, v));                        // v - z
+  c = __fadd2_rn(c, e);
+  s = t;
+}
+struct KSum2 {
+  float2 s, c;
+  EB_DEV void init() { s = make_float2(0.f, 0.f); c = s; }
+  EB_DEV void add(float2 v) { two_sum2(s, c, v); }
+  EB_DEV float x() const { return s.x + c.x; }
+  EB_DEV float y() const { return s.y + c.y; }
 };
 
 // ---- marker flag byte written by the locate kernel ----------------------------

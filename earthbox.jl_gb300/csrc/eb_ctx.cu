@@ -57,9 +57,54 @@ int ensure_grid_field(eb_ctx* c, int f) {
   return EB_OK;
 }
 
+// min and max of the uploaded marker_matid
+__global__ void k_matid_range(const int16_t* __restrict__ m, int64_t n, int32_t* __restrict__ mm);
+
+int launch_matid_range(eb_ctx* c, cudaStream_t s) {
+  if (!c->d_minmax) EB_CK(c, cudaMalloc(&c->d_minmax, 2 * sizeof(int32_t)));
+  const int32_t init[2] = {INT32_MAX, INT32_MIN};
+  if (!c->h_pinned) EB_CK(c, cudaMallocHost(&c->h_pinned, 64));
+  std::memcpy(c->h_pinned, init, sizeof(init));
+  EB_CK(c, cudaMemcpyAsync(c->d_minmax, c->h_pinned, sizeof(init), cudaMemcpyHostToDevice, s));
+  k_matid_range<<<(unsigned)std::min<int64_t>((c->M + 255) / 256, 4 * 152), 256, 0, s>>>(
+      (const int16_t*)c->mf[EB_M_MATID], c->M, c->d_minmax);
+  c->launches++;
+  EB_CK(c, cudaGetLastError());
+  EB_CK(c, cudaMemcpyAsync((char*)c->h_pinned + 8, c->d_minmax, 2 * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+  return EB_OK;
+}
+
+// after the stream of launch_matid_range has reached it: accept or reject the range
+int finish_matid_range(eb_ctx* c) {
+  int32_t mm[2];
+  std::memcpy(mm, (const char*)c->h_pinned + 8, sizeof(mm));
+  if (mm[0] < 1 || (c->have_mats && mm[1] > c->mats.nmat)) return eb_fail(c, EB_BAD_INPUT, "marker_matid out of range");
+  c->matid_min = mm[0];
+  c->matid_max = mm[1];
+  return EB_OK;
+}
+
+__global__ void k_matid_range(const int16_t* __restrict__ m, int64_t n, int32_t* __restrict__ mm) {
+  int32_t lo = INT32_MAX, hi = INT32_MIN;
+  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
+    const int32_t v = m[k];
+    lo = min(lo, v);
+    hi = max(hi, v);
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    lo = min(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+    hi = max(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomicMin(&mm[0], lo);
+    atomicMax(&mm[1], hi);
+  }
+}
+
 static size_t marker_elem_size(int f) {
   switch (f) {
-    case EB_M_MATID: case EB_M_XN: case EB_M_YN: case EB_M_XN_VY: case EB_M_YN_VY: return 4;
+    case EB_M_MATID: return 2;
+    case EB_M_XN: case EB_M_YN: case EB_M_XN_VY: case EB_M_YN_VY: return 4;
     case EB_M_PFAILURE: case EB_M_DILATATION: return 4;
     case EB_M_INSIDE: return 1;
     default: return 8;
@@ -83,7 +128,7 @@ DevMarkers dev_markers(eb_ctx* c) {
   d.M = c->M;
   auto D = [&](int f) { return (double*)c->mf[f]; };
   d.x = D(EB_M_X); d.y = D(EB_M_Y);
-  d.matid = (int32_t*)c->mf[EB_M_MATID];
+  d.matid = (int16_t*)c->mf[EB_M_MATID];
   d.rho = D(EB_M_RHO); d.cohesion = D(EB_M_COHESION); d.fric = D(EB_M_FRIC); d.fric_ini = D(EB_M_FRIC_INI);
   d.eta = D(EB_M_ETA); d.eta_flow = D(EB_M_ETA_FLOW); d.preexp = D(EB_M_PREEXP);
   d.sxx = D(EB_M_SXX); d.sxy = D(EB_M_SXY); d.exx = D(EB_M_EXX); d.exy = D(EB_M_EXY);
@@ -251,6 +296,11 @@ extern "C" int eb_destroy(eb_ctx* c) {
   for (void* p : c->mat_allocs) cudaFree(p);
   for (cudaEvent_t e : c->prof.pool) cudaEventDestroy(e);
   cudaFree(c->dflag);
+  cudaFree(c->d_minmax);
+  if (c->h_pinned) cudaFreeHost(c->h_pinned);
+  if (c->copy_in) cudaStreamDestroy(c->copy_in);
+  if (c->copy_out) cudaStreamDestroy(c->copy_out);
+  for (cudaEvent_t e : c->pipe_events) cudaEventDestroy(e);
   cudaStreamDestroy(c->stream);
   delete c;
   return EB_OK;
@@ -417,6 +467,7 @@ extern "C" int eb_resize_markers(eb_ctx* c, int64_t M) {
   cudaStreamSynchronize(c->stream);
   free_markers(c);
   c->M = M;
+  c->matid_min = 0;
   c->matid_max = 0;
   c->located = false;
   if (M == 0) return EB_OK;
@@ -440,18 +491,13 @@ extern "C" int eb_marker_upload(eb_ctx* c, int f, const void* host) {
   cudaSetDevice(c->device);
   if (c->M == 0) return EB_OK;
   if (f == EB_M_MATID) {
-    const int16_t* h = (const int16_t*)host;
-    std::vector<int32_t> w(c->M);
-    int32_t mx = 0;
-    for (int64_t i = 0; i < c->M; ++i) {
-      if (h[i] < 1 || (c->have_mats && h[i] > c->mats.nmat)) return eb_fail(c, EB_BAD_INPUT, "marker_matid out of range");
-      w[i] = h[i];
-      mx = w[i] > mx ? w[i] : mx;
-    }
-    c->matid_max = mx;
-    EB_CK(c, cudaMemcpyAsync(c->mf[f], w.data(), c->M * 4, cudaMemcpyHostToDevice, c->stream));
+    // copied as is (Int16, as the reference stores it); its range is checked on the device
+    c->matid_min = 0;  // unusable until the check passes
+    c->matid_max = 0;
+    EB_CK(c, cudaMemcpyAsync(c->mf[f], host, c->M * 2, cudaMemcpyHostToDevice, c->stream));
+    if ((rc = launch_matid_range(c, c->stream))) return rc;
     EB_CK(c, cudaStreamSynchronize(c->stream));
-    return EB_OK;
+    return finish_matid_range(c);
   }
   EB_CK(c, cudaMemcpyAsync(c->mf[f], host, c->M * marker_elem_size(f), cudaMemcpyHostToDevice, c->stream));
   if (f == EB_M_X || f == EB_M_Y) c->located = false;
@@ -477,11 +523,8 @@ extern "C" int eb_marker_download(eb_ctx* c, int f, void* host) {
   int rc = ensure_marker_field(c, f);
   if (rc) return rc;
   if (f == EB_M_MATID) {
-    std::vector<int32_t> w(c->M);
-    EB_CK(c, cudaMemcpyAsync(w.data(), c->mf[f], c->M * 4, cudaMemcpyDeviceToHost, c->stream));
+    EB_CK(c, cudaMemcpyAsync(host, c->mf[f], c->M * 2, cudaMemcpyDeviceToHost, c->stream));
     EB_CK(c, cudaStreamSynchronize(c->stream));
-    int16_t* h = (int16_t*)host;
-    for (int64_t i = 0; i < c->M; ++i) h[i] = (int16_t)w[i];
     return EB_OK;
   }
   EB_CK(c, cudaMemcpyAsync(host, c->mf[f], c->M * marker_elem_size(f), cudaMemcpyDeviceToHost, c->stream));
@@ -531,6 +574,8 @@ static int ready(eb_ctx* c, bool need_mats, bool need_located) {
   if (!c->have_grid) return eb_fail(c, EB_NOT_READY, "eb_set_grid has not been called");
   if (!c->have_params) return eb_fail(c, EB_NOT_READY, "eb_set_params has not been called");
   if (need_mats && !c->have_mats) return eb_fail(c, EB_NOT_READY, "eb_set_materials has not been called");
+  if (need_mats && c->M > 0 && c->matid_min < 1)
+    return eb_fail(c, EB_NOT_READY, "marker_matid has not been uploaded (or held values below 1)");
   if (need_mats && c->matid_max > c->mats.nmat) return eb_fail(c, EB_BAD_INPUT, "marker_matid exceeds the material count");
   if (need_located && !c->located)
     return eb_fail(c, EB_NOT_READY, "eb_initialize_bilinear_interpolation must run after markers move");

@@ -35,7 +35,7 @@ struct DevMats {
 struct DevMarkers {
   int64_t M;
   double *x, *y;
-  int32_t* matid;
+  int16_t* matid;  // the reference's Vector{Int16}
   double *rho, *cohesion, *fric, *fric_ini, *eta, *eta_flow, *preexp;
   double *sxx, *sxy, *exx, *exy, *pr, *sr_ratio, *gii, *sp, *srp;
   double *tk, *kt, *rhocp, *ha, *melt, *melt_damage, *serp_hr;
@@ -92,7 +92,12 @@ struct eb_ctx {
   std::vector<double> h_mat_rho, h_mat_plastic;  // host copies used by launch set-up
   // markers
   int64_t M = 0;
-  int32_t matid_max = 0;  // largest uploaded marker_matid (checked against nmat before use)
+  int32_t matid_min = 0, matid_max = 0;  // range of the uploaded marker_matid (checked before use)
+  int32_t* d_minmax = nullptr;            // device scratch of the range check
+  void* h_pinned = nullptr;               // 64 pinned host bytes for small async read-backs
+  // copy streams and events of eb_marker_cycle_host
+  cudaStream_t copy_in = nullptr, copy_out = nullptr;
+  std::vector<cudaEvent_t> pipe_events;
   void* mf[EB_M_NFIELDS] = {};
   float *fx = nullptr, *fy = nullptr;
   uint8_t* mflags = nullptr;
@@ -142,6 +147,8 @@ int export_stokes_coo(eb_ctx* c, const StokesSystem* s, int64_t* Li, int64_t* Lj
                       int64_t* nnz);
 
 void heat_free(eb_ctx* c);  // eb_heat.cu
+int launch_matid_range(eb_ctx* c, cudaStream_t s);  // eb_ctx.cu: marker_matid range check
+int finish_matid_range(eb_ctx* c);
 
 constexpr int kMaxSlots = 48;
 

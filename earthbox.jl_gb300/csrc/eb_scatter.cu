@@ -53,23 +53,31 @@ __device__ __forceinline__ uint32_t quadrant_mask(uint8_t fl) {
   return (xl && yl ? 1u : 0u) | (xl && yg ? 2u : 0u) | (xg && yl ? 4u : 0u) | (xg && yg ? 8u : 0u);
 }
 
-// Compensated accumulators in shared memory, indexed per lane: the (s, c) pair
-// of slot k of lane j sits at a[2k*32 + j] and a[(2k+1)*32 + j], so the 32
-// lanes of a warp use 32 different banks whichever slot each lane picks (a
-// lane's slot can depend on its marker, e.g. on the marker's quadrant).
+// Compensated accumulators in shared memory, indexed per lane: slot k of lane j is
+// the float4 (s0, s1, c0, c1) at a[k*32 + j] -- one accumulator pair, or one
+// accumulator in the .x/.z halves.  The 32 lanes of a warp read 32 consecutive
+// float4 whichever slot each lane picks (a lane's slot can depend on its marker,
+// e.g. on the marker's quadrant), so an add is one 128-bit load and one store.
 struct SAcc {
-  float* a;
-  __device__ __forceinline__ void add(int k, int lane, float v) const {
-    float* ps = a + 2 * k * 32 + lane;
-    const float s = ps[0];
-    const float t = s + v;
-    const float e = (fabsf(s) >= fabsf(v)) ? ((s - t) + v) : ((v - t) + s);
-    ps[32] += e;
-    ps[0] = t;
+  float4* a;
+  __device__ __forceinline__ void add2(int k, int lane, float2 v) const {
+    float4* p = a + k * 32 + lane;
+    const float4 q = *p;
+    float2 sv = make_float2(q.x, q.y), cv = make_float2(q.z, q.w);
+    two_sum2(sv, cv, v);
+    *p = make_float4(sv.x, sv.y, cv.x, cv.y);
   }
-  __device__ __forceinline__ float get(int k, int lane) const { return a[2 * k * 32 + lane] + a[(2 * k + 1) * 32 + lane]; }
+  __device__ __forceinline__ void add1(int k, int lane, float v) const {
+    float4* p = a + k * 32 + lane;
+    const float4 q = *p;
+    KSum t{q.x, q.z};
+    t.add(v);
+    p->x = t.s;
+    p->z = t.c;
+  }
+  __device__ __forceinline__ float get0(int k, int lane) const { const float4 q = a[k * 32 + lane]; return q.x + q.z; }
+  __device__ __forceinline__ float get1(int k, int lane) const { const float4 q = a[k * 32 + lane]; return q.y + q.w; }
 };
-constexpr int kSAccPerSlot = 64;  // floats per accumulator slot (s and c for 32 lanes)
 
 // ---------------------------------------------------------------- staging ---
 // Stage layout indices (rows of the shared-memory table).
@@ -84,19 +92,21 @@ __device__ __forceinline__ void stage_weights(float (*sv)[kChunk], int t, const 
 
 // ------------------------------------------------------------------ specs ---
 // Each spec defines: kRoles (folding warps, <= 8), kNV (staged rows), kAcc
-// (register accumulators per folding thread), kSmem (shared-memory accumulator
-// slots, SAcc), a Raw record of the marker fields it reads, load() (the global
-// loads only, issued one pass ahead), put() (arithmetic on a loaded Raw, marker
-// write-backs, staging), accum() and store().  Every accumulator receives its
-// cell's markers in slot (marker) order.
+// (register accumulator pairs KSum2 per folding thread), kSlots (shared-memory
+// accumulator slots, SAcc, each a pair), a Raw record of the marker fields it
+// reads, load() (the global loads only, issued one pass ahead), put() (arithmetic
+// on a loaded Raw, marker write-backs, staging), accum() and store().  Every
+// accumulator receives its cell's markers in slot (marker) order; accumulators
+// travel in pairs through packed FP32x2 arithmetic where two share a role.
 
 // Denominators: wtnodes (incl), wtetas (excl), wtetan (central), wtnodes_vy.
-// slots: 0-3 incl corners, 4-7 excl quadrants, 8 central, 9-16 vy half*4+corner
+// part slots: 0-3 incl corners, 4-7 excl quadrants, 8 central, 9-16 vy half*4+corner
 struct DenomSpec {
   static constexpr const char* kName = "k_cells<denominators>";
-  // roles: 0 inclusive corners (registers), 1 exclusive quadrants (shared, slot q),
-  //        2 central node (registers), 3 vy corners (shared, slot 4 + half*4 + corner)
-  static constexpr int kRoles = 4, kNV = S_V0, kAcc = 4, kSmem = 12;
+  // roles: 0-1 inclusive corners {0,1} / {2,3} (registers), 2 exclusive quadrants (shared
+  //        slot q), 3 central node (registers), 4-5 vy corners {0,1} / {2,3} (shared pair
+  //        slot 4 + 2*half + pair)
+  static constexpr int kRoles = 6, kNV = S_V0, kAcc = 1, kSlots = 8;
   struct Raw { int32_t xn; float fx, fy; uint8_t fl; };
   __device__ Raw load(const DevMarkers& mk, int32_t m) const {
     return Raw{mk.xn[m], mk.fx[m], mk.fy[m], mk.mflags[m]};
@@ -105,39 +115,53 @@ struct DenomSpec {
     stage_weights(sv, t, marker_weights(g, r.xn, r.fx, r.fy, r.fl));
     sfl[t] = r.fl;
   }
-  __device__ void accum(int role, int lane, int t, float (*sv)[kChunk], const uint8_t* sfl, KSum* a, SAcc sa) const {
-    if (role == 0) {
-      for (int k = 0; k < 4; ++k) a[k].add(sv[S_UL + k][t]);
-    } else if (role == 1) {
+  __device__ void accum(int role, int lane, int t, float (*sv)[kChunk], const uint8_t* sfl, KSum2* a, SAcc sa) const {
+    if (role < 2) {
+      a[0].add(make_float2(sv[S_UL + 2 * role][t], sv[S_UL + 2 * role + 1][t]));
+    } else if (role == 2) {
       for (uint32_t m = quadrant_mask(sfl[t]); m; m &= m - 1) {
         const int q = __ffs(m) - 1;
-        sa.add(q, lane, sv[S_UL + q][t]);
+        sa.add1(q, lane, sv[S_UL + q][t]);
       }
-    } else if (role == 2) {
-      a[0].add(sv[S_WC][t]);
+    } else if (role == 3) {
+      a[0].add(make_float2(sv[S_WC][t], 0.f));
     } else {
-      const int h = (int)sv[S_HALF][t];
-      for (int k = 0; k < 4; ++k) sa.add(4 + h * 4 + k, lane, sv[S_VUL + k][t]);
+      const int h = (int)sv[S_HALF][t], p = role - 4;
+      sa.add2(4 + 2 * h + p, lane, make_float2(sv[S_VUL + 2 * p][t], sv[S_VUL + 2 * p + 1][t]));
     }
   }
-  __device__ void store(int role, int lane, int32_t cell, int32_t nc, const KSum* a, SAcc sa, float* part) const {
-    if (role == 0) for (int k = 0; k < 4; ++k) part[(size_t)k * nc + cell] = a[k].get();
-    else if (role == 1) for (int q = 0; q < 4; ++q) part[(size_t)(4 + q) * nc + cell] = sa.get(q, lane);
-    else if (role == 2) part[(size_t)8 * nc + cell] = a[0].get();
-    else for (int k = 0; k < 8; ++k) part[(size_t)(9 + k) * nc + cell] = sa.get(4 + k, lane);
+  __device__ void store(int role, int lane, int32_t cell, int32_t nc, const KSum2* a, SAcc sa, float* part) const {
+    if (role < 2) {
+      part[(size_t)(2 * role) * nc + cell] = a[0].x();
+      part[(size_t)(2 * role + 1) * nc + cell] = a[0].y();
+    } else if (role == 2) {
+      for (int q = 0; q < 4; ++q) part[(size_t)(4 + q) * nc + cell] = sa.get0(q, lane);
+    } else if (role == 3) {
+      part[(size_t)8 * nc + cell] = a[0].x();
+    } else {
+      const int p = role - 4;
+      for (int h = 0; h < 2; ++h) {
+        part[(size_t)(9 + 4 * h + 2 * p) * nc + cell] = sa.get0(4 + 2 * h + p, lane);
+        part[(size_t)(9 + 4 * h + 2 * p + 1) * nc + cell] = sa.get1(4 + 2 * h + p, lane);
+      }
+    }
   }
 };
 
 // Stokes numerators (BilinearNumerator.jl:205-454).
 // values: rho, coh, fric_deg, eta_flow, eta, mu_inv, sxy, plast, dil, melt, sxx
 enum { V_RHO = S_V0, V_COH, V_FRIC, V_ETAF, V_ETA, V_MUI, V_SXY, V_PLAST, V_DIL, V_MELT, V_SXX, V_END };
-// slots: 0-3 incl rho; 4 + 7*q + f excl (f: coh, fric, eta_flow, eta, mu_inv, sxy, plast);
-//        32-37 central (eta, mu_inv, plast, dil, melt, sxx); 38-45 vy rho half*4+corner
+// part slots: 0-3 incl rho; 4 + 7*q + f excl (f: coh, fric, eta_flow, eta, mu_inv, sxy, plast);
+//             32-37 central (eta, mu_inv, plast, dil, melt, sxx); 38-45 vy rho half*4+corner
 struct StokesSpec {
   static constexpr const char* kName = "k_cells<stokes>";
-  // roles: 0 inclusive rho (registers), 1 exclusive quadrants (shared, slot 7q + f),
-  //        2 central node (registers), 3 vy rho (shared, slot 28 + half*4 + corner)
-  static constexpr int kRoles = 4, kNV = V_END, kAcc = 6, kSmem = 36;
+  // Eight roles of about equal work:
+  //   0 inclusive rho, corner pairs {UL, LL}, {UR, LR} (registers)
+  //   1-3 exclusive field pairs {coh, fric}, {eta_flow, eta}, {mu_inv, sxy} (shared pair slot 4(role-1) + q)
+  //   4 exclusive plast (shared slot 12 + q) + central {eta, mu_inv} (registers)
+  //   5 central {plast, dil}, {melt, sxx} (registers)
+  //   6-7 vy rho corner pairs {0, 1}, {2, 3} (shared pair slot 16 + 2*half + pair)
+  static constexpr int kRoles = 8, kNV = V_END, kAcc = 2, kSlots = 20;
   const double* mat_mu;
   int32_t* dflag;
   struct Raw {
@@ -171,48 +195,74 @@ struct StokesSpec {
     sv[V_MELT][t] = d2f(r.melt);
     sv[V_SXX][t] = d2f(r.sxx);
   }
-  __device__ void accum(int role, int lane, int t, float (*sv)[kChunk], const uint8_t* sfl, KSum* a, SAcc sa) const {
+  __device__ void accum(int role, int lane, int t, float (*sv)[kChunk], const uint8_t* sfl, KSum2* a, SAcc sa) const {
     if (role == 0) {
-      const float r = sv[V_RHO][t];
-      for (int k = 0; k < 4; ++k) a[k].add(sv[S_UL + k][t] * r);
-    } else if (role == 1) {
+      const float2 r = make_float2(sv[V_RHO][t], sv[V_RHO][t]);
+      a[0].add(__fmul2_rn(make_float2(sv[S_UL][t], sv[S_LL][t]), r));
+      a[1].add(__fmul2_rn(make_float2(sv[S_UR][t], sv[S_LR][t]), r));
+    } else if (role <= 4) {
+      const int f0 = 2 * (role - 1);  // exclusive fields f0, f0 + 1 (role 4: plast only)
       for (uint32_t m = quadrant_mask(sfl[t]); m; m &= m - 1) {
         const int q = __ffs(m) - 1;
         const float w = sv[S_UL + q][t];
-        sa.add(7 * q + 0, lane, w * sv[V_COH][t]);
-        sa.add(7 * q + 1, lane, w * sv[V_FRIC][t]);
-        sa.add(7 * q + 2, lane, w * sv[V_ETAF][t]);
-        sa.add(7 * q + 3, lane, w * sv[V_ETA][t]);
-        sa.add(7 * q + 4, lane, w * sv[V_MUI][t]);
-        sa.add(7 * q + 5, lane, w * sv[V_SXY][t]);
-        sa.add(7 * q + 6, lane, w * sv[V_PLAST][t]);
+        if (role < 4) {
+          sa.add2(4 * (role - 1) + q, lane,
+                  __fmul2_rn(make_float2(w, w), make_float2(sv[V_COH + f0][t], sv[V_COH + f0 + 1][t])));
+        } else {
+          sa.add1(12 + q, lane, w * sv[V_PLAST][t]);
+        }
       }
-    } else if (role == 2) {
-      const float w = sv[S_WC][t];
-      a[0].add(w * sv[V_ETA][t]);
-      a[1].add(w * sv[V_MUI][t]);
-      a[2].add(w * sv[V_PLAST][t]);
-      a[3].add(w * sv[V_DIL][t]);
-      a[4].add(w * sv[V_MELT][t]);
-      a[5].add(w * sv[V_SXX][t]);
+      if (role == 4) {
+        const float w = sv[S_WC][t];
+        a[0].add(__fmul2_rn(make_float2(w, w), make_float2(sv[V_ETA][t], sv[V_MUI][t])));
+      }
+    } else if (role == 5) {
+      const float2 w = make_float2(sv[S_WC][t], sv[S_WC][t]);
+      a[0].add(__fmul2_rn(w, make_float2(sv[V_PLAST][t], sv[V_DIL][t])));
+      a[1].add(__fmul2_rn(w, make_float2(sv[V_MELT][t], sv[V_SXX][t])));
     } else {
-      const int h = (int)sv[S_HALF][t];
+      const int h = (int)sv[S_HALF][t], p = role - 6;
       const float r = sv[V_RHO][t];
-      for (int k = 0; k < 4; ++k) sa.add(28 + h * 4 + k, lane, sv[S_VUL + k][t] * r);
+      sa.add2(16 + 2 * h + p, lane,
+              __fmul2_rn(make_float2(sv[S_VUL + 2 * p][t], sv[S_VUL + 2 * p + 1][t]), make_float2(r, r)));
     }
   }
-  __device__ void store(int role, int lane, int32_t cell, int32_t nc, const KSum* a, SAcc sa, float* part) const {
-    if (role == 0) for (int k = 0; k < 4; ++k) part[(size_t)k * nc + cell] = a[k].get();
-    else if (role == 1) for (int k = 0; k < 28; ++k) part[(size_t)(4 + k) * nc + cell] = sa.get(k, lane);
-    else if (role == 2) for (int f = 0; f < 6; ++f) part[(size_t)(32 + f) * nc + cell] = a[f].get();
-    else for (int k = 0; k < 8; ++k) part[(size_t)(38 + k) * nc + cell] = sa.get(28 + k, lane);
+  __device__ void store(int role, int lane, int32_t cell, int32_t nc, const KSum2* a, SAcc sa, float* part) const {
+    if (role == 0) {
+      part[(size_t)0 * nc + cell] = a[0].x();
+      part[(size_t)1 * nc + cell] = a[0].y();
+      part[(size_t)2 * nc + cell] = a[1].x();
+      part[(size_t)3 * nc + cell] = a[1].y();
+    } else if (role < 4) {
+      const int f0 = 2 * (role - 1);
+      for (int q = 0; q < 4; ++q) {
+        part[(size_t)(4 + 7 * q + f0) * nc + cell] = sa.get0(4 * (role - 1) + q, lane);
+        part[(size_t)(4 + 7 * q + f0 + 1) * nc + cell] = sa.get1(4 * (role - 1) + q, lane);
+      }
+    } else if (role == 4) {
+      for (int q = 0; q < 4; ++q) part[(size_t)(4 + 7 * q + 6) * nc + cell] = sa.get0(12 + q, lane);
+      part[(size_t)32 * nc + cell] = a[0].x();
+      part[(size_t)33 * nc + cell] = a[0].y();
+    } else if (role == 5) {
+      part[(size_t)34 * nc + cell] = a[0].x();
+      part[(size_t)35 * nc + cell] = a[0].y();
+      part[(size_t)36 * nc + cell] = a[1].x();
+      part[(size_t)37 * nc + cell] = a[1].y();
+    } else {
+      const int p = role - 6;
+      for (int h = 0; h < 2; ++h) {
+        part[(size_t)(38 + 4 * h + 2 * p) * nc + cell] = sa.get0(16 + 2 * h + p, lane);
+        part[(size_t)(38 + 4 * h + 2 * p + 1) * nc + cell] = sa.get1(16 + 2 * h + p, lane);
+      }
+    }
   }
 };
 
-// Heat numerators (BilinearNumerator.jl:31-141): tk, kt, rhocp, hr(+serp), ha; slots 5*corner + f
+// Heat numerators (BilinearNumerator.jl:31-141): tk, kt, rhocp, hr(+serp), ha; part slots 5*corner + f
 struct HeatSpec {
   static constexpr const char* kName = "k_cells<heat>";
-  static constexpr int kRoles = 4, kNV = S_V0 + 5, kAcc = 5, kSmem = 0;
+  // roles: corner (role & 3) x field pairs {tk, kt} + {ha} (role < 4) or {rhocp, hr} (role >= 4)
+  static constexpr int kRoles = 8, kNV = S_V0 + 5, kAcc = 2, kSlots = 0;
   const double* mat_hr;
   int use_serp;
   struct Raw { double tk, kt, rhocp, ha, serp; float fx, fy; int32_t mt; };
@@ -234,20 +284,34 @@ struct HeatSpec {
     sv[S_V0 + 3][t] = d2f(hr);
     sv[S_V0 + 4][t] = d2f(r.ha);
   }
-  __device__ void accum(int role, int, int t, float (*sv)[kChunk], const uint8_t*, KSum* a, SAcc) const {
-    const float w = sv[S_UL + role][t];
-    for (int f = 0; f < 5; ++f) a[f].add(w * sv[S_V0 + f][t]);
+  __device__ void accum(int role, int, int t, float (*sv)[kChunk], const uint8_t*, KSum2* a, SAcc) const {
+    const float w = sv[S_UL + (role & 3)][t];
+    const float2 w2 = make_float2(w, w);
+    if (role < 4) {
+      a[0].add(__fmul2_rn(w2, make_float2(sv[S_V0 + 0][t], sv[S_V0 + 1][t])));
+      a[1].add(make_float2(w * sv[S_V0 + 4][t], 0.f));
+    } else {
+      a[0].add(__fmul2_rn(w2, make_float2(sv[S_V0 + 2][t], sv[S_V0 + 3][t])));
+    }
   }
-  __device__ void store(int role, int, int32_t cell, int32_t nc, const KSum* a, SAcc, float* part) const {
-    for (int f = 0; f < 5; ++f) part[(size_t)(5 * role + f) * nc + cell] = a[f].get();
+  __device__ void store(int role, int, int32_t cell, int32_t nc, const KSum2* a, SAcc, float* part) const {
+    const int k = role & 3;
+    if (role < 4) {
+      part[(size_t)(5 * k + 0) * nc + cell] = a[0].x();
+      part[(size_t)(5 * k + 1) * nc + cell] = a[0].y();
+      part[(size_t)(5 * k + 4) * nc + cell] = a[1].x();
+    } else {
+      part[(size_t)(5 * k + 2) * nc + cell] = a[0].x();
+      part[(size_t)(5 * k + 3) * nc + cell] = a[0].y();
+    }
   }
 };
 
-// Viscosity re-scatter (BilinearNumerator.jl:470-533): slots 0-3 excl eta, 4 central eta
-// roles: 0 exclusive quadrants (shared, slot q), 1 central node (registers)
+// Viscosity re-scatter (BilinearNumerator.jl:470-533): part slots 0-3 excl eta, 4 central eta
+// roles: 0 exclusive quadrants (shared slot q), 1 central node (registers)
 struct ViscSpec {
   static constexpr const char* kName = "k_cells<viscosity>";
-  static constexpr int kRoles = 2, kNV = S_V0 + 1, kAcc = 1, kSmem = 4;
+  static constexpr int kRoles = 2, kNV = S_V0 + 1, kAcc = 1, kSlots = 4;
   struct Raw { double eta; float fx, fy; uint8_t fl; };
   __device__ Raw load(const DevMarkers& mk, int32_t m) const {
     return Raw{mk.eta[m], mk.fx[m], mk.fy[m], mk.mflags[m]};
@@ -259,22 +323,23 @@ struct ViscSpec {
     sfl[t] = r.fl;
     sv[S_V0][t] = d2f(r.eta);
   }
-  __device__ void accum(int role, int lane, int t, float (*sv)[kChunk], const uint8_t* sfl, KSum* a, SAcc sa) const {
+  __device__ void accum(int role, int lane, int t, float (*sv)[kChunk], const uint8_t* sfl, KSum2* a, SAcc sa) const {
     const float e = sv[S_V0][t];
     if (role == 0) {
       for (uint32_t m = quadrant_mask(sfl[t]); m; m &= m - 1) {
         const int q = __ffs(m) - 1;
-        sa.add(q, lane, sv[S_UL + q][t] * e);
+        sa.add1(q, lane, sv[S_UL + q][t] * e);
       }
     } else {
-      a[0].add(sv[S_WC][t] * e);
+      a[0].add(make_float2(sv[S_WC][t] * e, 0.f));
     }
   }
-  __device__ void store(int role, int lane, int32_t cell, int32_t nc, const KSum* a, SAcc sa, float* part) const {
-    if (role == 0) for (int q = 0; q < 4; ++q) part[(size_t)q * nc + cell] = sa.get(q, lane);
-    else part[(size_t)4 * nc + cell] = a[0].get();
+  __device__ void store(int role, int lane, int32_t cell, int32_t nc, const KSum2* a, SAcc sa, float* part) const {
+    if (role == 0) for (int q = 0; q < 4; ++q) part[(size_t)q * nc + cell] = sa.get0(q, lane);
+    else part[(size_t)4 * nc + cell] = a[0].x();
   }
 };
+
 
 // Pressure-grid bilinear gather of one marker (GridToMarker.jl:104-153 with
 // MarkerGridMapping.upr_left_index_pressure / upr_left_dist_pressure, :311-350).
@@ -297,11 +362,11 @@ __device__ __forceinline__ float gather_pressure_grid(const float* __restrict__ 
 
 // Subgrid stress (SubgridShearStress.jl:27-96, SubgridNormalStress.jl:27-89):
 // put() relaxes the marker stress, writes it back and stages the relaxed change.
-// slots: 0-3 excl relax_xy*w, 4-7 excl w, 8 central relax_xx*wc, 9 central wc
-// roles: 0 exclusive quadrants (shared, slots q: relax_xy*w, 4+q: w), 1 central node (registers)
+// part slots: 0-3 excl relax_xy*w, 4-7 excl w, 8 central relax_xx*wc, 9 central wc
+// roles: 0 exclusive quadrants (shared pair slot q: {relax_xy*w, w}), 1 central node (registers)
 struct SubgridStressSpec {
   static constexpr const char* kName = "k_cells<subgrid_stress>";
-  static constexpr int kRoles = 2, kNV = S_V0 + 2, kAcc = 2, kSmem = 8;
+  static constexpr int kRoles = 2, kNV = S_V0 + 2, kAcc = 1, kSlots = 4;
   const float *sxy1, *sxx1;  // FP32 mirrors
   const double* mat_mu;
   float dt, coef;
@@ -331,36 +396,37 @@ struct SubgridStressSpec {
     sv[S_V0][t] = rxy;
     sv[S_V0 + 1][t] = rxx;
   }
-  __device__ void accum(int role, int lane, int t, float (*sv)[kChunk], const uint8_t* sfl, KSum* a, SAcc sa) const {
+  __device__ void accum(int role, int lane, int t, float (*sv)[kChunk], const uint8_t* sfl, KSum2* a, SAcc sa) const {
     if (role == 0) {
       const float r = sv[S_V0][t];
       for (uint32_t m = quadrant_mask(sfl[t]); m; m &= m - 1) {
         const int q = __ffs(m) - 1;
         const float w = sv[S_UL + q][t];
-        sa.add(q, lane, w * r);
-        sa.add(4 + q, lane, w);
+        sa.add2(q, lane, make_float2(w * r, w));
       }
     } else {
       const float w = sv[S_WC][t];
-      a[0].add(w * sv[S_V0 + 1][t]);
-      a[1].add(w);
+      a[0].add(make_float2(w * sv[S_V0 + 1][t], w));
     }
   }
-  __device__ void store(int role, int lane, int32_t cell, int32_t nc, const KSum* a, SAcc sa, float* part) const {
+  __device__ void store(int role, int lane, int32_t cell, int32_t nc, const KSum2* a, SAcc sa, float* part) const {
     if (role == 0) {
-      for (int k = 0; k < 8; ++k) part[(size_t)k * nc + cell] = sa.get(k, lane);
+      for (int q = 0; q < 4; ++q) {
+        part[(size_t)q * nc + cell] = sa.get0(q, lane);
+        part[(size_t)(4 + q) * nc + cell] = sa.get1(q, lane);
+      }
     } else {
-      part[(size_t)8 * nc + cell] = a[0].get();
-      part[(size_t)9 * nc + cell] = a[1].get();
+      part[(size_t)8 * nc + cell] = a[0].x();
+      part[(size_t)9 * nc + cell] = a[0].y();
     }
   }
 };
 
-// Subgrid heat diffusion (SubgridDiffusion.jl:67-175): slots 0-3 dT*w, 4-7 w
-// roles 0-3: one corner each
+// Subgrid heat diffusion (SubgridDiffusion.jl:67-175): part slots 0-3 dT*w, 4-7 w
+// roles 0-3: one corner each, {dT*w, w} packed
 struct SubgridHeatSpec {
   static constexpr const char* kName = "k_cells<subgrid_heat>";
-  static constexpr int kRoles = 4, kNV = S_V0 + 1, kAcc = 2, kSmem = 0;
+  static constexpr int kRoles = 4, kNV = S_V0 + 1, kAcc = 1, kSlots = 0;
   const float *tk1, *kt1, *rhocp1;  // FP32 mirrors
   float dt, coef, inv_ts;  // inv_ts = 2/xstpavg^2 + 2/ystpavg^2
   struct Raw { double tk; int32_t m, xn, yn; float fx, fy; };
@@ -380,16 +446,16 @@ struct SubgridHeatSpec {
     mk.tk[r.m] = r.tk + f2d(d);
     sv[S_V0][t] = d;
   }
-  __device__ void accum(int role, int, int t, float (*sv)[kChunk], const uint8_t*, KSum* a, SAcc) const {
+  __device__ void accum(int role, int, int t, float (*sv)[kChunk], const uint8_t*, KSum2* a, SAcc) const {
     const float w = sv[S_UL + role][t];
-    a[0].add(w * sv[S_V0][t]);
-    a[1].add(w);
+    a[0].add(make_float2(w * sv[S_V0][t], w));
   }
-  __device__ void store(int role, int, int32_t cell, int32_t nc, const KSum* a, SAcc, float* part) const {
-    part[(size_t)role * nc + cell] = a[0].get();
-    part[(size_t)(4 + role) * nc + cell] = a[1].get();
+  __device__ void store(int role, int, int32_t cell, int32_t nc, const KSum2* a, SAcc, float* part) const {
+    part[(size_t)role * nc + cell] = a[0].x();
+    part[(size_t)(4 + role) * nc + cell] = a[0].y();
   }
 };
+
 
 // ------------------------------------------------------- per-cell kernel ---
 // Block = 256 threads = 32 consecutive cells.  Pass p stages markers
@@ -415,8 +481,8 @@ __global__ void __launch_bounds__(kThreads) k_cells(S spec, DevMarkers mk, DevGr
   __shared__ float sv[S::kNV][kChunk];
   __shared__ uint8_t sfl[kChunk];
   __shared__ int32_t s_beg[32], s_cnt[32], s_max;
-  __shared__ float s_acc[S::kSmem > 0 ? S::kSmem * kSAccPerSlot : 1];
-  for (int k = threadIdx.x; k < S::kSmem * kSAccPerSlot; k += blockDim.x) s_acc[k] = 0.f;
+  __shared__ float4 s_acc[S::kSlots > 0 ? S::kSlots * 32 : 1];
+  for (int k = threadIdx.x; k < S::kSlots * 32; k += blockDim.x) s_acc[k] = make_float4(0.f, 0.f, 0.f, 0.f);
   const SAcc sa{s_acc};
   const int lane = threadIdx.x & 31, role = threadIdx.x >> 5;
   const int sj = threadIdx.x >> 3, si = threadIdx.x & 7;  // staging cell / marker of this thread
@@ -435,19 +501,23 @@ __global__ void __launch_bounds__(kThreads) k_cells(S spec, DevMarkers mk, DevGr
   const int32_t nmax = s_max;
   const int32_t my_cnt = s_cnt[lane];
   const int32_t st_beg = s_beg[sj], st_cnt = s_cnt[sj];
-  KSum acc[S::kAcc];
+  KSum2 acc[S::kAcc];
 #pragma unroll
   for (int k = 0; k < S::kAcc; ++k) acc[k].init();
+  // The marker index of a staged entry is read one pass before its fields: the field
+  // loads of pass p+1 then wait for one memory latency, not for a perm load and then them.
   typename S::Raw r;
   bool have = si < st_cnt;
+  int32_t m_next = kPer + si < st_cnt ? __ldg(&perm[st_beg + kPer + si]) : -1;
   if (have) r = spec.load(mk, __ldg(&perm[st_beg + si]));
   for (int32_t base = 0; base < nmax; base += kPer) {
     __syncthreads();
     if (have) spec.put(r, mk, g, sj * kSlotStride + si, sv, sfl);
     __syncthreads();
-    const int32_t nxt = base + kPer + si;
-    have = nxt < st_cnt;
-    if (have) r = spec.load(mk, __ldg(&perm[st_beg + nxt]));
+    have = m_next >= 0;
+    if (have) r = spec.load(mk, m_next);
+    const int32_t nxt2 = base + 2 * kPer + si;
+    m_next = nxt2 < st_cnt ? __ldg(&perm[st_beg + nxt2]) : -1;
     if (role < S::kRoles) {
       const int n = min(kPer, my_cnt - base);
       for (int i = 0; i < n; ++i) spec.accum(role, lane, lane * kSlotStride + i, sv, sfl, acc, sa);

@@ -1160,6 +1160,12 @@ extern "C" int eb_solve_stokes_system(eb_ctx* c, const eb_solve_opts* o, eb_solv
   std::vector<double> H((size_t)(m + 1) * m), g(m + 1), cs(m), sn(m), hcol(m + 2), y(m);
   int it = 0, reorth = 0;
   double est = 1.0;
+  // The Krylov methods run on the scaled system, whose residual norm weights rows by W; the
+  // tolerance is on the reference's (unscaled) residual ||R - L S|| / ||R||.  When the scaled
+  // target is reached but the unscaled residual is still above rtol, the target is tightened
+  // by their ratio and the method restarts from the current iterate.
+  double target = opt.rtol, rel = 0.0, rel_s = 0.0;
+  for (int outer = 0;; ++outer) {
   bool converged = (bnorm == 0.0);
   if (opt.method == 1 && !converged) {
     // Right-preconditioned BiCGStab on the scaled system.  Basis slots hold its vectors:
@@ -1178,7 +1184,7 @@ extern "C" int eb_solve_stokes_system(eb_ctx* c, const eb_solve_opts* o, eb_solv
     if ((rc = mdot(c, st, rh0, n3, 2, r, d2))) return rc;
     double rho_new = d2[0];
     est = std::sqrt(d2[1]) / bnorm;
-    converged = est <= opt.rtol;
+    converged = est <= target;
     while (!converged && it < opt.max_iters) {
       if (rho_new == 0.0 || omega == 0.0 || !std::isfinite(rho_new))
         return eb_fail(c, std::isfinite(rho_new) ? EB_NOT_CONVERGED : EB_NAN, "BiCGStab breakdown");
@@ -1206,7 +1212,7 @@ extern "C" int eb_solve_stokes_system(eb_ctx* c, const eb_solve_opts* o, eb_solv
       rho_new = d2[0];
       est = std::sqrt(d2[1]) / bnorm;
       if (!std::isfinite(est)) return eb_fail(c, EB_NAN, "BiCGStab residual became NaN/Inf");
-      converged = est <= opt.rtol;
+      converged = est <= target;
     }
   }
   while (opt.method != 1 && !converged && it < opt.max_iters) {
@@ -1220,7 +1226,7 @@ extern "C" int eb_solve_stokes_system(eb_ctx* c, const eb_solve_opts* o, eb_solv
     const double beta = std::sqrt(beta2);
     if (!std::isfinite(beta)) return eb_fail(c, EB_NAN, "FGMRES residual became NaN/Inf");
     est = beta / bnorm;
-    if (est <= opt.rtol) { converged = true; break; }
+    if (est <= target) { converged = true; break; }
     EB_PROF(c, "k_axpy");
     k_scale_copy<<<nblk(n3), kB, 0, c->stream>>>(st->V, st->r, 1.0 / beta, n3);
     EB_LAUNCHED(c);
@@ -1291,7 +1297,7 @@ extern "C" int eb_solve_stokes_system(eb_ctx* c, const eb_solve_opts* o, eb_solv
         k_scale_copy<<<nblk(n3), kB, 0, c->stream>>>(w, w, 1.0 / hk1, n3);
         EB_LAUNCHED(c);
       }
-      if (est <= opt.rtol || hk1 == 0.0) { ++k; break; }
+      if (est <= target || hk1 == 0.0) { ++k; break; }
     }
     // y = H^-1 g (upper triangular k x k), xhat += Z y
     for (int q = k - 1; q >= 0; --q) {
@@ -1325,9 +1331,13 @@ extern "C" int eb_solve_stokes_system(eb_ctx* c, const eb_solve_opts* o, eb_solv
   k_sub<<<nblk(n3), kB, 0, c->stream>>>(st->r, st->bs, st->t, n3);
   EB_LAUNCHED(c);
   if ((rc = mdot(c, st, st->r, 0, 1, st->r, &sr2))) return rc;
+  rel = RR > 0 ? std::sqrt(rr / RR) : std::sqrt(rr);
+  rel_s = bnorm > 0 ? std::sqrt(sr2) / bnorm : std::sqrt(sr2);
+  if (!std::isfinite(rel)) break;
+  if (rel <= opt.rtol || it >= opt.max_iters || outer >= 8 || bnorm == 0.0) break;
+  target = std::min(target, rel_s) * std::max(0.5 * opt.rtol / rel, 1e-4);
+  }  // outer
   prof_resolve(c);
-  const double rel = RR > 0 ? std::sqrt(rr / RR) : std::sqrt(rr);
-  const double rel_s = bnorm > 0 ? std::sqrt(sr2) / bnorm : std::sqrt(sr2);
   if (rep) {
     rep->iterations = it;
     rep->reorthogonalisations = reorth;
@@ -1337,8 +1347,8 @@ extern "C" int eb_solve_stokes_system(eb_ctx* c, const eb_solve_opts* o, eb_solv
     rep->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
   }
   if (!std::isfinite(rel)) return eb_fail(c, EB_NAN, "Stokes solution has NaN/Inf");
-  if (rel_s > opt.rtol * 1.0000001)
-    return eb_fail(c, EB_NOT_CONVERGED, "FGMRES stopped at scaled relative residual " + std::to_string(rel_s) +
+  if (rel > opt.rtol * 1.0000001)
+    return eb_fail(c, EB_NOT_CONVERGED, "Stokes solve stopped at relative residual " + std::to_string(rel) +
                                             " after " + std::to_string(it) + " iterations");
   return EB_OK;
 }

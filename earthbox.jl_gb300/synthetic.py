@@ -343,8 +343,50 @@ def rift(xnum: int = 801, ynum: int = 201, mpc: int = 4, seed: int = 2, width: f
     return Model(f"rift_{xnum}x{ynum}_{mpc}", grid, mats, params, m, grids)
 
 
+def circles(n: int = 1025, ncircles: int = 200, seed: int = 4, width: float = 1000e3) -> Model:
+    """Grid-only Stokes benchmark: a square n x n-node box (eta = 1e21, rho = 3300) with
+    `ncircles` seeded circular inclusions, r ~ U(5, 20) km, log10 eta ~ U(18, 27) and
+    density contrast ~ U(-100, 100) kg/m^3; free slip on every side, purely viscous
+    (shear modulus 1e40).  Later circles overwrite earlier ones where they overlap.
+    Viscosity and density are evaluated at each grid's own nodes (basic, pressure, vy)."""
+    rng = np.random.Generator(np.random.Philox(seed))
+    x = np.linspace(0.0, width, n)
+    grid = staggered_grid(x, x.copy())
+    X = Y = n
+    cx = rng.uniform(0.0, width, ncircles)
+    cy = rng.uniform(0.0, width, ncircles)
+    r = rng.uniform(5e3, 20e3, ncircles)
+    leta = rng.uniform(18.0, 27.0, ncircles)
+    drho = rng.uniform(-100.0, 100.0, ncircles)
+
+    def paint(xs, ys):
+        Yg, Xg = np.meshgrid(ys, xs, indexing="ij")
+        eta = np.full(Yg.shape, 1e21)
+        rho = np.full(Yg.shape, 3300.0)
+        for k in range(ncircles):
+            inside = (Xg - cx[k]) ** 2 + (Yg - cy[k]) ** 2 <= r[k] ** 2
+            eta[inside] = 10.0 ** leta[k]
+            rho[inside] = 3300.0 + drho[k]
+        return np.asfortranarray(eta), np.asfortranarray(rho)
+
+    xb, yb = grid.gridx_b, grid.gridy_b
+    xp, yp = grid.gridx_vy[1:X], grid.gridy_vx[1:Y]
+    etas, rho = paint(xb, yb)
+    etan, _ = paint(xp, yp)
+    _, rho_vy = paint(grid.gridx_vy, yb)
+    F = np.asfortranarray
+    gr = {"etas1": etas, "etan1": etan, "rho1": rho, "rho1_vy": rho_vy,
+          "mus1": F(np.full((Y, X), 1e40)), "mun1": F(np.full((Y - 1, X - 1), 1e40)),
+          "sxy1": F(np.zeros((Y, X))), "sxx1": F(np.zeros((Y - 1, X - 1))),
+          "dilatation_grid": F(np.zeros((Y - 1, X - 1)))}
+    gr.update(velocity_bcs(grid))
+    params = default_params()
+    params.update(stokes_params())
+    return Model(f"circles_{n}", grid, None, params, {}, gr)
+
+
 def config(name: str, seed: int | None = None) -> Model:
-    """Named workloads: sinking_block, rift_small, rift_2p5M, rift_40M."""
+    """Named workloads: sinking_block, rift_small, rift_2p5M, rift_40M, rift_40M_strip, circles_1025."""
     kw = {} if seed is None else {"seed": seed}
     if name == "sinking_block":
         return sinking_block(**kw)
@@ -356,6 +398,8 @@ def config(name: str, seed: int | None = None) -> Model:
         return rift(2001, 801, 5, **kw)
     if name == "rift_40M_strip":
         return rift(101, 801, 5, width=25e3, **kw)
+    if name == "circles_1025":
+        return circles(1025, **kw)
     raise KeyError(name)
 
 

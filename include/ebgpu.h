@@ -12,8 +12,8 @@
  *   - grid arrays are Julia column-major Matrix{Float64} of shape (rows, cols):
  *     element (i, j), 1-based, lives at offset (j-1)*rows + (i-1);
  *   - marker cell indices (marker_xn/yn, marker_xn_vy/yn_vy) are 1-based Int32;
- *   - marker_matid is accepted as Int16 (the reference's storage type) and
- *     widened to Int32 on the device;
+ *   - marker_matid is Int16 (the reference's storage type) on the host and on
+ *     the device; its upload checks 1 <= matid (<= nmat once materials are set);
  *   - material tables mat_flow (nmat x 12) and mat_plastic (nmat x 6) are
  *     column-major, indexed by the 1-based material id.
  * All calls are synchronous with respect to the host on return, on the
@@ -287,7 +287,9 @@ typedef struct eb_stokes_params {
 
 /* Options of the iterative solve that replaces the direct sparse solve. */
 typedef struct eb_solve_opts {
-  double  rtol;              /* stop when ||W(R - L S)|| <= rtol ||W R|| (W: diagonal scaling); 0 -> 1e-8 */
+  double  rtol;              /* stop when ||R - L S|| <= rtol ||R|| (the reference's assembled system; the
+                                iteration runs on the W-scaled system and tightens its own target
+                                until this holds); 0 -> 1e-8                                     */
   int32_t max_iters;         /* FGMRES iterations; 0 -> 3000                                          */
   int32_t restart;           /* Krylov basis size; 0 -> 40                                             */
   int32_t mg_sweeps;         /* red-black Gauss-Seidel sweeps before/after each coarse correction; 0 -> 3 */
@@ -478,6 +480,29 @@ int eb_heat_export_coo(eb_ctx* ctx, int64_t* Li, int64_t* Lj, double* Lv, int64_
 /* The right-hand side R of the last eb_build_heat_system (N doubles).                 */
 int eb_heat_rhs_download(eb_ctx* ctx, double* host);
 int64_t eb_heat_size(const eb_ctx* ctx);      /* N = xnum*ynum, 0 before eb_set_grid */
+
+/* ---- one marker cycle from host arrays -------------------------------------
+ * No single counterpart in the reference: the sequence of eb_get_marker_inside_flags,
+ * eb_initialize_bilinear_interpolation, eb_interpolate_marker_heat_parameters_to_grid,
+ * eb_interpolate_marker_stokes_parameters_to_grid, eb_post_stokes_marker_gathers,
+ * eb_update_subgrid_stress, eb_apply_marker_stress_correction,
+ * eb_subgrid_heat_diffusion_update, eb_add_remaining_grid_change_to_marker_temperature,
+ * eb_advect_markers_and_rotate_stress and eb_update_marker_strain, with the caller's
+ * host arrays copied in before the steps that read them and out as soon as the
+ * last step writing each has finished.  The copies run on two copy streams beside
+ * the steps (host memory should be pinned for them to overlap); the call returns
+ * when everything has completed.  Fields and host types as for eb_marker_upload /
+ * eb_marker_download; inputs cannot be cell indices or inside flags, outputs cannot
+ * be marker_xn_vy/yn_vy.  marker_matid in the inputs is range-checked as on upload. */
+typedef struct eb_marker_io {
+  int32_t n_in;                 /* fields copied host -> device before their first use   */
+  const int32_t* in_fields;     /* eb_marker_field ids                                   */
+  const void* const* in_host;   /* host arrays (marknum elements each)                   */
+  int32_t n_out;                /* fields copied device -> host after their last write   */
+  const int32_t* out_fields;
+  void* const* out_host;
+} eb_marker_io;
+int eb_marker_cycle_host(eb_ctx* ctx, const eb_marker_io* io);
 
 /* ---- allocation-free entry point -------------------------------------------
  * No counterpart in the reference.  For callers that cannot call cudaMalloc

@@ -1,0 +1,49 @@
+"""eb_marker_cycle_host (one marker cycle from host arrays, copies overlapped with the
+steps) against the same cycle run entry point by entry point: identical results, since
+the same kernels run on the same data; bad inputs rejected before any step runs."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+IN = ["x", "y", "matid", "rho", "cohesion", "fric", "eta", "eta_flow", "sxx", "sxy", "pfailure", "dilatation",
+      "meltfrac", "tk", "kt", "rhocp", "ha", "serp_hr", "gii", "strain_plastic"]
+OUT = ["x", "y", "sxx", "sxy", "tk", "exx", "exy", "pr", "sr_ratio", "gii", "strain_plastic", "strain_rate_plastic",
+       "xn", "yn", "inside", "subgrid_dt", "eta"]
+
+
+@pytest.mark.parametrize("name", ["rift_small", "sinking_block"])
+def test_cycle_from_host_matches_entry_points(eb, name):
+    model = eb.synthetic.config(name)
+    ref = eb.MarkerInCell(0)
+    ref.load_model(model)
+    ref.marker_cycle()
+    want = {k: ref.download_marker(k) for k in OUT}
+    ref.close()
+    mic = eb.MarkerInCell(0)
+    mic.load_model(model)
+    # the context starts from different marker values: the call must replace them
+    mic.upload_marker("tk", np.zeros(model.marknum))
+    dt = eb._abi.MARKER_DTYPE
+    inputs = {k: np.ascontiguousarray(model.markers[k], dtype=dt[k]) for k in IN}
+    outputs = {k: np.zeros(model.marknum, dtype=dt[k]) for k in OUT}
+    mic.marker_cycle_host(inputs, outputs)
+    for k in OUT:
+        assert np.array_equal(outputs[k], want[k]), k
+    # a second call from the outputs continues the evolution like a second cycle
+    mic.close()
+
+
+def test_cycle_from_host_rejects_bad_matid(eb):
+    model = eb.synthetic.config("rift_small")
+    mic = eb.MarkerInCell(0)
+    mic.load_model(model)
+    bad = model.markers["matid"].astype(np.int16).copy()
+    bad[7] = 0
+    x0 = mic.download_marker("x")
+    with pytest.raises(RuntimeError):
+        mic.marker_cycle_host({"x": model.markers["x"], "matid": bad}, {"x": np.zeros(model.marknum)})
+    # no step ran: a valid call afterwards works
+    mic.marker_cycle_host({"matid": model.markers["matid"].astype(np.int16)}, {"x": np.zeros(model.marknum)})
+    assert x0.shape == (model.marknum,)
+    mic.close()

@@ -306,3 +306,21 @@ def test_nodal_plastic_yielding_matches_oracle(eb, case):
     ep = (eb_[:-1, :-1] + eb_[:-1, 1:] + eb_[1:, :-1] + eb_[1:, 1:]) / 4.0
     assert np.allclose(mic.download_grid("eii_plastic_pressure"), ep, rtol=1e-15, atol=0)
     mic.close()
+
+
+def test_circles_box_matches_superlu(eb):
+    """The circles solver benchmark at 129 x 129 nodes: 20 inclusions of 1e18-1e27 Pa s, solved
+    to 1e-10 (the benchmark's tolerance) and compared with SuperLU per unknown type."""
+    from oracle.stokes import StokesOracle
+    model = eb.synthetic.circles(129, 20)
+    mic = gpu_ctx(eb, model)
+    rep = mic.solve_viscoelastic_stokes_continuity_equations(rtol=1e-10)
+    assert rep["status"] == 0 and rep["rel_residual"] <= 1e-10, rep
+    o = StokesOracle(model)
+    o.stokes_steps()
+    S, S_ref = mic.download_stokes_vector("solution"), o.solve_direct()
+    assert o.residual(S) < 1e-9
+    for k in range(3):
+        err = np.max(np.abs(S[k::3] - S_ref[k::3])) / np.max(np.abs(S_ref[k::3]))
+        assert err < 1e-6, (k, err)
+    mic.close()
