@@ -469,6 +469,47 @@ class MarkerInCell:
                 break
         return history
 
+    # ------------------------------------------------------- step boundary --
+    def set_rock_tables(self, mat_rho: np.ndarray, mat_cp: np.ndarray, mat_kt: np.ndarray) -> None:
+        """Material tables of the rock-property models: mat_rho (nmat, 3), mat_cp (nmat),
+        mat_kt (nmat, 2) (model.materials.arrays)."""
+        rho = np.asfortranarray(mat_rho, dtype=np.float64)
+        cp = np.ascontiguousarray(mat_cp, dtype=np.float64)
+        kt = np.asfortranarray(mat_kt, dtype=np.float64)
+        n = cp.shape[0]
+        if rho.shape != (n, 3) or kt.shape != (n, 2):
+            raise ValueError("mat_rho must be (nmat, 3) and mat_kt (nmat, 2)")
+        d = _abi.RockDesc(n, rho.ctypes.data, cp.ctypes.data, kt.ctypes.data)
+        self._check(self._lib.eb_set_rock_tables(self._ctx, C.byref(d)))
+
+    def set_sediment_porosity(self, matids_sediments, topo_x, topo_y, conductivity_water: float,
+                              density_water: float, heat_capacity_water: float) -> None:
+        """Inputs of the sediment porosity correction (PorosityUpdate.jl)."""
+        ids = np.ascontiguousarray(matids_sediments, dtype=np.int16)
+        tx = np.ascontiguousarray(topo_x, dtype=np.float64)
+        ty = np.ascontiguousarray(topo_y, dtype=np.float64)
+        d = _abi.SedimentDesc(len(ids), ids.ctypes.data if len(ids) else None, len(tx), tx.ctypes.data,
+                              ty.ctypes.data, conductivity_water, density_water, heat_capacity_water)
+        self._check(self._lib.eb_set_sediment_porosity(self._ctx, C.byref(d)))
+
+    def update_marker_rock_properties(self, density_model: int = 0, rhocp_model: int = 0,
+                                      conductivity_model: int = 0, iuse_sed_porosity: int = 0,
+                                      maximum_heat_capacity: float = 1200.0) -> None:
+        """RockProperties.update_marker_rock_properties! (rock_properties/RockProperties.jl:99-125)."""
+        p = _abi.RockParams(density_model, rhocp_model, conductivity_model, iuse_sed_porosity,
+                            maximum_heat_capacity)
+        self._check(self._lib.eb_update_marker_rock_properties(self._ctx, C.byref(p)))
+
+    def update_model_time_step_using_displacement_limit(self, timestep: float, marker_cell_displ_max: float,
+                                                        iuse_local_adaptive_time_stepping: int = 0) -> tuple:
+        """Update.update_model_time_step_using_displacement_limit (time_step/update/Update.jl:16-33):
+        returns (new time step, updated?)."""
+        dt = C.c_double(timestep)
+        upd = C.c_int32()
+        self._check(self._lib.eb_update_model_time_step_using_displacement_limit(
+            self._ctx, marker_cell_displ_max, iuse_local_adaptive_time_stepping, C.byref(dt), C.byref(upd)))
+        return dt.value, bool(upd.value)
+
     # ---------------------------------------------------------- heat step --
     def _heat(self, params: dict | None) -> "_abi.HeatParams":
         hp = heat_params(params) if params is not None else getattr(self, "heat", None)

@@ -18,6 +18,7 @@ MARKER_FIELDS = [
     "sxx", "sxy", "exx", "exy", "pr", "sr_ratio", "gii", "strain_plastic", "strain_rate_plastic",
     "tk", "kt", "rhocp", "ha", "meltfrac", "melt_damage", "serp_hr", "pfailure", "dilatation",
     "vx", "vy", "spin", "subgrid_dt", "xn", "yn", "xn_vy", "yn_vy", "inside",
+    "porosity_initial", "decay_depth", "max_burial_depth",
 ]
 MARKER_ID = {n: i for i, n in enumerate(MARKER_FIELDS)}
 MARKER_DTYPE = {n: "f8" for n in MARKER_FIELDS}
@@ -153,6 +154,21 @@ class MarkerIO(C.Structure):
                 ("n_out", C.c_int32), ("out_fields", C.POINTER(C.c_int32)), ("out_host", C.POINTER(C.c_void_p))]
 
 
+class RockDesc(C.Structure):
+    _fields_ = [("nmat", C.c_int64), ("mat_rho", C.c_void_p), ("mat_cp", C.c_void_p), ("mat_kt", C.c_void_p)]
+
+
+class SedimentDesc(C.Structure):
+    _fields_ = [("nsed", C.c_int64), ("matids_sediments", C.c_void_p), ("ntopo", C.c_int64), ("topo_x", C.c_void_p),
+                ("topo_y", C.c_void_p), ("conductivity_water", C.c_double), ("density_water", C.c_double),
+                ("heat_capacity_water", C.c_double)]
+
+
+class RockParams(C.Structure):
+    _fields_ = [("density_model", C.c_int32), ("rhocp_model", C.c_int32), ("conductivity_model", C.c_int32),
+                ("iuse_sed_porosity", C.c_int32), ("maximum_heat_capacity", C.c_double)]
+
+
 class HeatParams(C.Structure):
     _fields_ = [("timestep", C.c_double), ("max_temp_change", C.c_double), ("gravity_x", C.c_double),
                 ("gravity_y", C.c_double), ("iuse_adiabatic_heating", C.c_int32), ("iuse_shear_heating", C.c_int32)]
@@ -195,7 +211,9 @@ ALL_SYMBOLS = [
     "eb_stokes_vector_download", "eb_stokes_stencil_download", "eb_stokes_pscale", "eb_stokes_size",
     "eb_calculate_stokes_norms", "eb_interpolate_basic_viscoplastic_viscosity_to_pressure_grid",
     "eb_update_nodes_for_plastic_yielding", "eb_stokes_export_coo",
-    "eb_marker_to_basic_grid_average_noalloc", "eb_marker_cycle_host",
+    "eb_marker_to_basic_grid_average_noalloc", "eb_marker_cycle_host", "eb_set_rock_tables",
+    "eb_set_sediment_porosity", "eb_update_marker_rock_properties",
+    "eb_update_model_time_step_using_displacement_limit",
 ] + ENTRY_POINTS + STOKES_ENTRY_POINTS + HEAT_ENTRY_POINTS
 
 _lib = None
@@ -254,6 +272,11 @@ def load(path: pathlib.Path | str | None = None) -> C.CDLL:
     lib.eb_marker_to_basic_grid_average_noalloc.argtypes = [vp, vp, vp, C.c_int64, vp, C.c_int64, vp, C.c_int64,
                                                             vp, vp, vp, C.c_char_p, C.c_size_t]
     lib.eb_marker_cycle_host.argtypes = [vp, C.POINTER(MarkerIO)]
+    lib.eb_set_rock_tables.argtypes = [vp, C.POINTER(RockDesc)]
+    lib.eb_set_sediment_porosity.argtypes = [vp, C.POINTER(SedimentDesc)]
+    lib.eb_update_marker_rock_properties.argtypes = [vp, C.POINTER(RockParams)]
+    lib.eb_update_model_time_step_using_displacement_limit.argtypes = [vp, C.c_double, C.c_int32,
+                                                                       C.POINTER(C.c_double), C.POINTER(C.c_int32)]
     lib.eb_calculate_heat_rhs_terms.argtypes = [vp, C.POINTER(HeatParams)]
     lib.eb_initialize_old_temperature.argtypes = [vp]
     lib.eb_build_heat_system.argtypes = [vp, C.c_double]

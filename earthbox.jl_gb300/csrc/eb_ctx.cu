@@ -140,6 +140,7 @@ DevMarkers dev_markers(eb_ctx* c) {
   d.vx = D(EB_M_VX); d.vy = D(EB_M_VY); d.spin = D(EB_M_SPIN); d.subgrid_dt = D(EB_M_SUBGRID_DT);
   d.xn = (int32_t*)c->mf[EB_M_XN]; d.yn = (int32_t*)c->mf[EB_M_YN];
   d.inside = (int8_t*)c->mf[EB_M_INSIDE];
+  d.por0 = D(EB_M_POROSITY_INITIAL); d.decay = D(EB_M_DECAY_DEPTH); d.burial = D(EB_M_MAX_BURIAL_DEPTH);
   d.fx = c->fx; d.fy = c->fy; d.mflags = c->mflags;
   return d;
 }
@@ -294,6 +295,8 @@ extern "C" int eb_destroy(eb_ctx* c) {
   stokes_free(c);
   heat_free(c);
   for (void* p : c->mat_allocs) cudaFree(p);
+  for (void* p : c->rock_allocs) cudaFree(p);
+  for (void* p : c->sed_allocs) cudaFree(p);
   for (cudaEvent_t e : c->prof.pool) cudaEventDestroy(e);
   cudaFree(c->dflag);
   cudaFree(c->d_minmax);
@@ -431,6 +434,8 @@ extern "C" int eb_set_materials(eb_ctx* c, const eb_material_desc* m) {
   cudaSetDevice(c->device);
   cudaStreamSynchronize(c->stream);
   for (void* p : c->mat_allocs) cudaFree(p);
+  for (void* p : c->rock_allocs) cudaFree(p);
+  for (void* p : c->sed_allocs) cudaFree(p);
   c->mat_allocs.clear();
   const int32_t n = (int32_t)m->nmat;
   DevMats& d = c->mats;

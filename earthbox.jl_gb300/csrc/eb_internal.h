@@ -43,6 +43,7 @@ struct DevMarkers {
   double *vx, *vy, *spin, *subgrid_dt;
   int32_t *xn, *yn;
   int8_t* inside;
+  double *por0, *decay, *burial;  // sediment porosity (Athy's law) inputs
   float *fx, *fy;   // FP32 normalised distances from the upper-left basic node
   uint8_t* mflags;  // MF_* bits
 };
@@ -112,6 +113,16 @@ struct eb_ctx {
   StokesState* st = nullptr;
   // conductive heat step
   HeatState* ht = nullptr;
+  // rock-property tables and sediment porosity inputs (eb_step_boundary.cu)
+  std::vector<void*> rock_allocs;
+  int64_t rock_nmat = 0;
+  const double *rock_rho = nullptr, *rock_cp = nullptr, *rock_kt = nullptr;  // [nmat x 3], [nmat], [nmat x 2]
+  std::vector<void*> sed_allocs;
+  int64_t sed_n = 0, sed_ntopo = 0;
+  const int16_t* sed_ids = nullptr;
+  const double *sed_tx = nullptr, *sed_ty = nullptr;
+  double sed_kw = 0.0, sed_rhow = 0.0, sed_cpw = 0.0;
+  bool have_sed = false;
 };
 
 // Stokes system storage shared by the assembly (eb_stokes_build.cu) and the

@@ -106,6 +106,7 @@ enum eb_marker_field {
   EB_M_SUBGRID_DT,                        /* marker_subgrid_temp_delta_buffer          */
   EB_M_XN, EB_M_YN, EB_M_XN_VY, EB_M_YN_VY, /* Int32, 1-based, download only          */
   EB_M_INSIDE,                            /* Int8 (+1 inside / -1 outside)             */
+  EB_M_POROSITY_INITIAL, EB_M_DECAY_DEPTH, EB_M_MAX_BURIAL_DEPTH, /* sediment porosity (Athy's law) */
   EB_M_NFIELDS
 };
 
@@ -480,6 +481,49 @@ int eb_heat_export_coo(eb_ctx* ctx, int64_t* Li, int64_t* Lj, double* Lv, int64_
 /* The right-hand side R of the last eb_build_heat_system (N doubles).                 */
 int eb_heat_rhs_download(eb_ctx* ctx, double* host);
 int64_t eb_heat_size(const eb_ctx* ctx);      /* N = xnum*ynum, 0 before eb_set_grid */
+
+/* ---- step boundary: rock properties and the time step ---------------------- */
+/* Material tables of the rock-property models (model.materials.arrays.*). */
+typedef struct eb_rock_desc {
+  int64_t nmat;
+  const double* mat_rho;   /* [nmat x 3] column-major: standard density, expansivity, compressibility */
+  const double* mat_cp;    /* [nmat]     heat capacity (J/kg/K; at 20 C for the Waples model)         */
+  const double* mat_kt;    /* [nmat x 2] column-major: reference conductivity, factor a              */
+} eb_rock_desc;
+int eb_set_rock_tables(eb_ctx* ctx, const eb_rock_desc* tables);
+
+/* Sediment porosity (PorosityUpdate.jl): sediment material ids, the topography
+ * (gridt rows 1 and 2: x and y of the sediment-water interface) and water properties. */
+typedef struct eb_sediment_desc {
+  int64_t nsed;
+  const int16_t* matids_sediments;   /* materials.dicts.matid_types["Sediment"]             */
+  int64_t ntopo;
+  const double* topo_x;              /* gridt[1, :] (increasing)                            */
+  const double* topo_y;              /* gridt[2, :]                                         */
+  double conductivity_water, density_water, heat_capacity_water;
+} eb_sediment_desc;
+int eb_set_sediment_porosity(eb_ctx* ctx, const eb_sediment_desc* sed);
+
+typedef struct eb_rock_params {
+  int32_t density_model;       /* DensityModel options: 0 Liao14, 1 Blankenbach89, 2 Naliboff17          */
+  int32_t rhocp_model;         /* RhoCpModel options: 0 Constant, 1 TemperatureDependentWaples           */
+  int32_t conductivity_model;  /* ThermalConductivityModel options: 0 Liao14, 1 Uniform, 2 Temperature-
+                                  Dependent, 3 Naliboff17, 4 Adiabatic, 5 SekiguchiWaples                 */
+  int32_t iuse_sed_porosity;   /* 1: porosity correction of sediment markers (eb_set_sediment_porosity)  */
+  double  maximum_heat_capacity;  /* J/kg/K cap of the Waples model                                    */
+} eb_rock_params;
+/* RockProperties.update_marker_rock_properties! (rock_properties/RockProperties.jl:99-125):
+ * marker rho, rhocp, kt and ha of inside markers from matid, x, y, pr, tk (and the
+ * porosity fields); temperature_top comes from eb_params.                            */
+int eb_update_marker_rock_properties(eb_ctx* ctx, const eb_rock_params* p);
+
+/* Update.update_model_time_step_using_displacement_limit (time_step/update/Update.jl:16-33):
+ * the new main time step from vx1, vy1 (average spacings, or every staggered node when
+ * iuse_local_adaptive_time_stepping == 1); *timestep is the old step on entry and the
+ * new one on return, *timestep_update = (new != old).                                 */
+int eb_update_model_time_step_using_displacement_limit(eb_ctx* ctx, double marker_cell_displ_max,
+                                                       int32_t iuse_local_adaptive_time_stepping,
+                                                       double* timestep, int32_t* timestep_update);
 
 /* ---- one marker cycle from host arrays -------------------------------------
  * No single counterpart in the reference: the sequence of eb_get_marker_inside_flags,

@@ -1,0 +1,83 @@
+"""CPU oracle (TEST INFRASTRUCTURE ONLY) for the step-boundary updates: the rock
+properties of the markers (rock_properties/RockProperties.jl:99-125) and the
+displacement-limited time step (time_step/update/Update.jl:16-219), restated in
+boundary_oracle.c.  Only tests/ use it."""
+from __future__ import annotations
+
+import ctypes as C
+import pathlib
+import subprocess
+
+import numpy as np
+
+HERE = pathlib.Path(__file__).resolve().parent
+BUILD = HERE / "_build"
+LIB = BUILD / "libboundary_oracle.so"
+SRC = HERE / "boundary_oracle.c"
+CFLAGS = ["-O2", "-fPIC", "-shared", "-ffp-contract=off", "-fno-fast-math", "-std=c11"]
+
+
+def build(force: bool = False) -> pathlib.Path:
+    if force or not LIB.exists() or LIB.stat().st_mtime < SRC.stat().st_mtime:
+        BUILD.mkdir(exist_ok=True)
+        tmp = BUILD / "libboundary_oracle.so.tmp"
+        subprocess.run(["gcc", *CFLAGS, str(SRC), "-o", str(tmp), "-lm"], check=True)
+        tmp.replace(LIB)
+    return LIB
+
+
+_lib = None
+
+
+def lib() -> C.CDLL:
+    global _lib
+    if _lib is None:
+        _lib = C.CDLL(str(build()))
+        _lib.o_timestep_displacement_limit.restype = C.c_double
+    return _lib
+
+
+def _p(a):
+    return C.c_void_p(a.ctypes.data) if a is not None else None
+
+
+def timestep_displacement_limit(grid, vx1, vy1, displ: float, iuse_local: int, dt_old: float) -> float:
+    vx = np.asfortranarray(vx1, dtype=np.float64)
+    vy = np.asfortranarray(vy1, dtype=np.float64)
+    xs = np.ascontiguousarray(grid.xstp_b, dtype=np.float64)
+    ys = np.ascontiguousarray(grid.ystp_b, dtype=np.float64)
+    return lib().o_timestep_displacement_limit(C.c_int64(grid.xnum), C.c_int64(grid.ynum), _p(vx), _p(vy), _p(xs),
+                                               _p(ys), C.c_double(grid.xstpavg), C.c_double(grid.ystpavg),
+                                               C.c_double(displ), C.c_int64(iuse_local), C.c_double(dt_old))
+
+
+def rock_properties(mk: dict, mat_rho, mat_cp, mat_kt, density_model, rhocp_model, cond_model, temperature_top,
+                    maximum_heat_capacity, iuse_por=0, sed=None) -> dict:
+    """Returns updated copies of rho, rhocp, kt, ha (inside markers only, as the reference)."""
+    M = len(mk["x"])
+    out = {k: np.array(mk[k], dtype=np.float64, copy=True) for k in ("rho", "rhocp", "kt", "ha")}
+    rho_t = np.asfortranarray(mat_rho, dtype=np.float64)
+    cp_t = np.ascontiguousarray(mat_cp, dtype=np.float64)
+    kt_t = np.asfortranarray(mat_kt, dtype=np.float64)
+    inside = np.ascontiguousarray(mk["inside"], dtype=np.int8)
+    matid = np.ascontiguousarray(mk["matid"], dtype=np.int16)
+    f = {k: np.ascontiguousarray(mk[k], dtype=np.float64) for k in ("x", "y", "pr", "tk")}
+    if iuse_por == 1:
+        por = [np.ascontiguousarray(mk[k], dtype=np.float64) for k in ("porosity_initial", "decay_depth",
+                                                                         "max_burial_depth")]
+        ids = np.ascontiguousarray(sed["matids"], dtype=np.int16)
+        tx = np.ascontiguousarray(sed["topo_x"], dtype=np.float64)
+        ty = np.ascontiguousarray(sed["topo_y"], dtype=np.float64)
+        wk, wr, wc = sed["conductivity_water"], sed["density_water"], sed["heat_capacity_water"]
+    else:
+        por = [None, None, None]
+        ids = tx = ty = None
+        wk = wr = wc = 0.0
+    lib().o_rock_properties(C.c_int64(M), _p(inside), _p(matid), _p(f["x"]), _p(f["y"]), _p(f["pr"]), _p(f["tk"]),
+                            _p(out["rho"]), _p(out["rhocp"]), _p(out["kt"]), _p(out["ha"]), C.c_int64(len(cp_t)),
+                            _p(rho_t), _p(cp_t), _p(kt_t), C.c_int64(density_model), C.c_int64(rhocp_model),
+                            C.c_int64(cond_model), C.c_double(temperature_top), C.c_double(maximum_heat_capacity),
+                            C.c_int64(iuse_por), _p(por[0]), _p(por[1]), _p(por[2]), _p(tx), _p(ty),
+                            C.c_int64(0 if tx is None else len(tx)), _p(ids), C.c_int64(0 if ids is None else len(ids)),
+                            C.c_double(wk), C.c_double(wr), C.c_double(wc))
+    return out

@@ -1,0 +1,76 @@
+"""GPU step-boundary updates against the oracle, through the C-ABI: rock properties of the
+markers for every density x rhocp x conductivity model (bit-identical where the formula
+has no exp; within 2e-16 relative otherwise), the sediment porosity correction, and the
+displacement-limited time step in both modes (bit-identical)."""
+import numpy as np
+import pytest
+
+from boundary_cases import porosity_fields, rock_tables, sediment
+
+pytestmark = pytest.mark.gpu
+
+
+def setup(eb, name="rift_small", nmat=4):
+    model = eb.synthetic.config(name)
+    mic = eb.MarkerInCell(0)
+    mic.load_model(model)
+    mic.get_marker_inside_flags()
+    M = model.marknum
+    mk = {k: mic.download_marker(k) for k in ("x", "y", "matid", "pr", "tk", "rho", "rhocp", "kt", "ha", "inside")}
+    por = porosity_fields(M)
+    for k, v in por.items():
+        mic.upload_marker(k, v)
+    mk.update(por)
+    tabs = rock_tables(nmat)
+    mic.set_rock_tables(*tabs)
+    return model, mic, mk, tabs
+
+
+@pytest.mark.parametrize("dm,cm,km", [(d, c, k) for d in range(3) for c in range(2) for k in range(6)])
+def test_rock_properties_match_oracle(eb, dm, cm, km):
+    from oracle import boundary as B
+    model, mic, mk, tabs = setup(eb)
+    mic.update_marker_rock_properties(dm, cm, km, 0, 1200.0)
+    want = B.rock_properties(mk, *tabs, dm, cm, km, model.params["temperature_top"], 1200.0)
+    for n in ("rho", "rhocp", "kt", "ha"):
+        got = mic.download_marker(n)
+        if km == 0 and n == "kt":
+            np.testing.assert_allclose(got, want[n], rtol=4e-16, atol=0, err_msg=n)
+        else:
+            assert np.array_equal(got, want[n]), n
+    mic.close()
+
+
+def test_rock_properties_porosity_match_oracle(eb):
+    from oracle import boundary as B
+    model, mic, mk, tabs = setup(eb)
+    sed = sediment(model.grid)
+    mic.set_sediment_porosity(sed["matids"], sed["topo_x"], sed["topo_y"], sed["conductivity_water"],
+                              sed["density_water"], sed["heat_capacity_water"])
+    mic.update_marker_rock_properties(1, 1, 2, 1, 1200.0)
+    want = B.rock_properties(mk, *tabs, 1, 1, 2, model.params["temperature_top"], 1200.0, iuse_por=1, sed=sed)
+    for n in ("rho", "rhocp", "kt", "ha"):
+        np.testing.assert_allclose(mic.download_marker(n), want[n], rtol=1e-15, atol=0, err_msg=n)
+    mic.close()
+
+
+def test_rock_properties_rejects_unknown_material(eb):
+    model, mic, mk, tabs = setup(eb, nmat=4)
+    mic.set_rock_tables(tabs[0][:2], tabs[1][:2], tabs[2][:2])  # fewer materials than the markers use
+    with pytest.raises(RuntimeError):
+        mic.update_marker_rock_properties()
+    mic.close()
+
+
+@pytest.mark.parametrize("local", [0, 1])
+def test_timestep_matches_oracle(eb, local):
+    from oracle import boundary as B
+    model = eb.synthetic.config("rift_small")
+    mic = eb.MarkerInCell(0)
+    mic.load_model(model)
+    vx, vy = model.grids["vx1"], model.grids["vy1"]
+    for dt_old in (1e9, 1e13):
+        got, upd = mic.update_model_time_step_using_displacement_limit(dt_old, 0.5, local)
+        want = B.timestep_displacement_limit(model.grid, vx, vy, 0.5, local, dt_old)
+        assert got == want and upd == (want != dt_old)
+    mic.close()
