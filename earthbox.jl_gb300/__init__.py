@@ -612,16 +612,26 @@ class MarkerInCell:
         io = _abi.MarkerIO(len(inputs), fin, hin, len(outputs), fout, hout)
         self._check(self._lib.eb_marker_cycle_host(self._ctx, C.byref(io)))
 
-    def marker_cycle(self) -> None:
+    def correct_advect_and_update_strain(self) -> None:
+        """Stress correction, remaining temperature change, RK4 advection with stress rotation
+        and the strain update in one marker pass (eb_correct_advect_and_update_strain)."""
+        self._call("eb_correct_advect_and_update_strain")
+
+    def marker_cycle(self, fused: bool = True) -> None:
         """The marker-in-cell transfer + RK4 sequence of one time step (no Stokes/heat solve):
         locate, heat and Stokes scatters, post-Stokes gathers, subgrid stress and temperature,
-        stress and temperature corrections, RK4 advection and the strain update."""
+        stress and temperature corrections, RK4 advection and the strain update.  With
+        fused=True the last four run as one pass (same results)."""
         self.get_marker_inside_flags()
         self.initialize_bilinear_interpolation()
         self.interpolate_marker_heat_parameters_to_grid()
         self.interpolate_marker_stokes_parameters_to_grid()
         self.post_stokes_marker_gathers()
         self.update_subgrid_stress()
+        if fused:
+            self.subgrid_heat_diffusion_update()
+            self.correct_advect_and_update_strain()
+            return
         self.apply_marker_stress_correction()
         self.subgrid_heat_diffusion_update()
         self.add_remaining_grid_change_to_marker_temperature()

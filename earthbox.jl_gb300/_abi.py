@@ -200,7 +200,7 @@ ENTRY_POINTS = [
     "eb_interpolate_temperature_to_markers", "eb_update_marker_rheology", "eb_update_plastic_yielding",
     "eb_post_stokes_marker_gathers", "eb_update_subgrid_stress", "eb_apply_marker_stress_correction",
     "eb_subgrid_heat_diffusion_update", "eb_add_remaining_grid_change_to_marker_temperature",
-    "eb_advect_markers_and_rotate_stress", "eb_update_marker_strain",
+    "eb_advect_markers_and_rotate_stress", "eb_update_marker_strain", "eb_correct_advect_and_update_strain",
 ]
 ALL_SYMBOLS = [
     "eb_create", "eb_destroy", "eb_last_error", "eb_set_grid", "eb_set_materials", "eb_set_params",

@@ -117,6 +117,86 @@ __global__ void k_advect(DevMarkers mk, DevGrid g, VelGrids V) {
   mk.sxx[m] = sxx + f2d(fxx * c2m1 - fxy * s2w);
 }
 
+// The last four steps of the marker cycle in one pass over the markers, each marker's
+// fields read once and written once: StressCorrection (remaining grid stress change
+// added to the marker stress, StressCorrection.jl:35-82), MarkerTemperature (remaining
+// grid temperature change, MarkerTemperature.jl:18-45), the RK4 move and rotation of
+// k_advect, and the strain update of k_strain.  Same arithmetic, same order: the
+// correction precedes the rotation and the strain update reads the rotated stress, as
+// when the four kernels run one after the other.
+struct TailGrids {
+  const float *dsxy, *dsxx, *dtk1;  // FP32 mirrors
+  double healing;
+};
+template <bool kMove>
+__global__ void k_tail(DevMarkers mk, DevGrid g, VelGrids V, TailGrids T) {
+  const int64_t m = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= mk.M) return;
+  if (!(mk.mflags[m] & MF_INSIDE)) {
+    if (kMove) { mk.vx[m] = 0.0; mk.vy[m] = 0.0; mk.spin[m] = 0.0; }
+    return;
+  }
+  const int32_t ix0 = mk.xn[m], iy0 = mk.yn[m];
+  const float fx = mk.fx[m], fy = mk.fy[m];
+  const float lx0 = fx * __ldg(&g.sxf[ix0 - 1]);
+  const float ly0 = fy * __ldg(&g.syf[iy0 - 1]);
+  // stress correction
+  double sxy = mk.sxy[m] + f2d(gather4f(T.dsxy, g.ynum, iy0, ix0, fx, fy));
+  double sxx = mk.sxx[m] + f2d(gather_p(T.dsxx, g, ix0, iy0, lx0, ly0));
+  // remaining temperature change
+  mk.tk[m] = mk.tk[m] + f2d(gather4f(T.dtk1, g.ynum, iy0, ix0, fx, fy));
+  if (kMove) {
+    const float h = V.dt;
+    float v1x, v1y, s1;
+    vel_spin(g, V, ix0, iy0, lx0, ly0, v1x, v1y, s1);
+    float vxm = v1x, vym = v1y, spm = s1;
+    if (V.order == 4) {
+      float v2x, v2y, s2, v3x, v3y, s3, v4x, v4y, s4, ux, uy;
+      int32_t jx, jy;
+      walk_x(g, ix0, lx0 + (h * 0.5f) * v1x, jx, ux);
+      walk_y(g, iy0, ly0 + (h * 0.5f) * v1y, jy, uy);
+      vel_spin(g, V, jx, jy, ux, uy, v2x, v2y, s2);
+      walk_x(g, ix0, lx0 + (h * 0.5f) * v2x, jx, ux);
+      walk_y(g, iy0, ly0 + (h * 0.5f) * v2y, jy, uy);
+      vel_spin(g, V, jx, jy, ux, uy, v3x, v3y, s3);
+      walk_x(g, ix0, lx0 + h * v3x, jx, ux);
+      walk_y(g, iy0, ly0 + h * v3y, jy, uy);
+      vel_spin(g, V, jx, jy, ux, uy, v4x, v4y, s4);
+      vxm = (v1x + 2.f * v2x + 2.f * v3x + v4x) / 6.f;
+      vym = (v1y + 2.f * v2y + 2.f * v3y + v4y) / 6.f;
+      spm = (s1 + 2.f * s2 + 2.f * s3 + s4) / 6.f;
+    }
+    const double vxd = f2d(vxm), vyd = f2d(vym);
+    mk.vx[m] = vxd;
+    mk.vy[m] = vyd;
+    mk.spin[m] = f2d(spm);
+    mk.x[m] = fma(V.dtd, vxd, mk.x[m]);
+    mk.y[m] = fma(V.dtd, vyd, mk.y[m]);
+    const float w = spm * V.dt;
+    const float s2w = sinf(2.f * w), sw = sinf(w);
+    const float c2m1 = -2.f * sw * sw;
+    const float fxx = d2f(sxx), fxy = d2f(sxy);
+    const double nxy = sxy + f2d(fxx * s2w + fxy * c2m1);
+    const double nxx = sxx + f2d(fxx * c2m1 - fxy * s2w);
+    sxy = nxy;
+    sxx = nxx;
+  }
+  mk.sxx[m] = sxx;
+  mk.sxy[m] = sxy;
+  // strain update (inside markers only, as k_strain)
+  const float eii = hypotf(d2f(mk.exx[m]), d2f(mk.exy[m]));
+  mk.gii[m] = fma(V.dtd, f2d(eii), mk.gii[m]);
+  if (mk.pfailure[m] != 1.0f) return;
+  const double eta = mk.eta[m], eta_flow = mk.eta_flow[m];
+  const float sii = hypotf(d2f(sxx), d2f(sxy));
+  const float d = d2f(eta_flow - eta);
+  float rate = 0.5f * sii * ((d / d2f(eta)) / d2f(eta_flow));
+  rate = fmaxf(0.f, rate);
+  double sp = mk.sp[m] + V.dtd * f2d(rate) - T.healing * V.dtd;
+  mk.sp[m] = sp > 0.0 ? sp : 0.0;
+  mk.srp[m] = f2d(rate);
+}
+
 // MarkersStrain.update_total_strain! and update_plastic_strain!
 __global__ void k_strain(DevMarkers mk, double dt, double healing) {
   const int64_t m = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -165,6 +245,29 @@ int launch_update_strain(eb_ctx* c) {
   EB_PROF(c, "k_strain");
   k_strain<<<(unsigned)((c->M + kBlock - 1) / kBlock), kBlock, 0, c->stream>>>(dev_markers(c), c->P.timestep,
                                                                                 c->P.plastic_healing_rate);
+  EB_LAUNCHED(c);
+  return EB_OK;
+}
+
+int launch_marker_tail(eb_ctx* c) {
+  const int64_t order = c->P.runge_kutta_order;
+  if (order != 0 && order != 1 && order != 4) return eb_fail(c, EB_BAD_INPUT, "runge_kutta_order must be 0, 1 or 4");
+  int rc;
+  const int mf[] = {EB_M_X, EB_M_Y, EB_M_VX, EB_M_VY, EB_M_SPIN, EB_M_SXX, EB_M_SXY, EB_M_TK, EB_M_INSIDE, EB_M_EXX,
+                    EB_M_EXY, EB_M_GII, EB_M_PFAILURE, EB_M_ETA, EB_M_ETA_FLOW, EB_M_STRAIN_PLASTIC,
+                    EB_M_STRAIN_RATE_PLASTIC};
+  for (int f : mf) if ((rc = ensure_marker_field(c, f))) return rc;
+  for (int f : {EB_G_VX1, EB_G_VY1, EB_G_ESP, EB_G_DSXY, EB_G_DSXX, EB_G_DTK1})
+    if ((rc = ensure_grid_field(c, f))) return rc;
+  if (c->M == 0) return EB_OK;
+  const float* f[6];
+  if ((rc = grid_f32(c, {EB_G_VX1, EB_G_VY1, EB_G_ESP, EB_G_DSXY, EB_G_DSXX, EB_G_DTK1}, f))) return rc;
+  VelGrids V{f[0], f[1], f[2], (float)c->P.timestep, c->P.timestep, (int)order};
+  TailGrids T{f[3], f[4], f[5], c->P.plastic_healing_rate};
+  EB_PROF(c, "k_tail");
+  const unsigned blocks = (unsigned)((c->M + kBlock - 1) / kBlock);
+  if (order > 0) k_tail<true><<<blocks, kBlock, 0, c->stream>>>(dev_markers(c), c->g, V, T);
+  else k_tail<false><<<blocks, kBlock, 0, c->stream>>>(dev_markers(c), c->g, V, T);
   EB_LAUNCHED(c);
   return EB_OK;
 }

@@ -703,3 +703,9 @@ extern "C" int eb_update_marker_strain(eb_ctx* c) {
   if (rc) return rc;
   return finish(c, launch_update_strain(c));
 }
+
+extern "C" int eb_correct_advect_and_update_strain(eb_ctx* c) {
+  int rc = ready(c, false, true);
+  if (rc) return rc;
+  return finish(c, launch_marker_tail(c));
+}

@@ -13,17 +13,6 @@ namespace {
 
 constexpr int kBlock = 256;
 
-// Pressure-grid bilinear gather (GridToMarker.jl:104-153, MarkerGridMapping.jl:311-350)
-// on an FP32 mirror of the grid.
-__device__ __forceinline__ float gather_p(const float* __restrict__ pg, const DevGrid& g, int32_t ix, int32_t iy,
-                                          float lx, float ly) {
-  const float hx = __ldg(&g.vyoff_hi[ix - 1]), hy = __ldg(&g.vxoff_hi[iy - 1]);
-  const int32_t xp = clamp_i((lx < hx) ? ix - 1 : ix, 1, g.xnum - 2);
-  const int32_t yp = clamp_i((ly < hy) ? iy - 1 : iy, 1, g.ynum - 2);
-  const float ox = (xp + 1 == ix) ? __ldg(&g.vyoff_lo[ix - 1]) : hx;
-  const float oy = (yp + 1 == iy) ? __ldg(&g.vxoff_lo[iy - 1]) : hy;
-  return gather4f(pg, g.ynum - 1, yp, xp, (lx - ox) * __ldg(&g.rsxvyf[xp]), (ly - oy) * __ldg(&g.rsyvxf[yp]));
-}
 
 __global__ void k_gather_temperature(DevMarkers mk, DevGrid g, const float* __restrict__ tk1) {
   const int64_t m = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;

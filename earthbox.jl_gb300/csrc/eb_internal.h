@@ -25,6 +25,18 @@ struct DevGrid {
   double xstpavg, ystpavg;
 };
 
+// Pressure-grid bilinear gather (GridToMarker.jl:104-153, MarkerGridMapping.jl:311-350)
+// on an FP32 mirror of the grid; (lx, ly) is the marker's offset from basic node (ix, iy).
+__device__ __forceinline__ float gather_p(const float* __restrict__ pg, const DevGrid& g, int32_t ix, int32_t iy,
+                                          float lx, float ly) {
+  const float hx = __ldg(&g.vyoff_hi[ix - 1]), hy = __ldg(&g.vxoff_hi[iy - 1]);
+  const int32_t xp = clamp_i((lx < hx) ? ix - 1 : ix, 1, g.xnum - 2);
+  const int32_t yp = clamp_i((ly < hy) ? iy - 1 : iy, 1, g.ynum - 2);
+  const float ox = (xp + 1 == ix) ? __ldg(&g.vyoff_lo[ix - 1]) : hx;
+  const float oy = (yp + 1 == iy) ? __ldg(&g.vxoff_lo[iy - 1]) : hy;
+  return gather4f(pg, g.ynum - 1, yp, xp, (lx - ox) * __ldg(&g.rsxvyf[xp]), (ly - oy) * __ldg(&g.rsyvxf[yp]));
+}
+
 struct DevMats {
   int32_t nmat;
   const double *mu, *hr, *flow, *plastic, *rho;
@@ -209,6 +221,9 @@ int launch_stress_correction(eb_ctx* c);
 int launch_add_remaining_dt(eb_ctx* c);
 int launch_advect(eb_ctx* c);
 int launch_update_strain(eb_ctx* c);
+// stress correction, remaining temperature change, advection + rotation and the strain
+// update in one marker pass (the four steps in that order; eb_advect.cu)
+int launch_marker_tail(eb_ctx* c);
 int launch_rheology(eb_ctx* c);
 int launch_viscoplastic(eb_ctx* c, int use_marker_plasticity);
 int launch_plastic_yielding(eb_ctx* c);

@@ -21,9 +21,11 @@
 namespace {
 
 // Steps of the cycle, in order.
+// (the stress correction, remaining temperature change, advection and strain update run
+// as one pass, eb_correct_advect_and_update_strain)
 enum Step {
-  ST_INSIDE = 0, ST_BILINEAR, ST_HEAT, ST_STOKES, ST_POST_STOKES, ST_SUBGRID_STRESS, ST_CORRECTION,
-  ST_SUBGRID_HEAT, ST_REMAINING_DT, ST_ADVECT, ST_STRAIN, ST_COUNT
+  ST_INSIDE = 0, ST_BILINEAR, ST_HEAT, ST_STOKES, ST_POST_STOKES, ST_SUBGRID_STRESS, ST_SUBGRID_HEAT, ST_TAIL,
+  ST_COUNT
 };
 
 // Upload group of an input field: 0 positions and material (locate), 1 heat scatter,
@@ -51,10 +53,7 @@ int final_step(int f) {
     case EB_M_XN: case EB_M_YN: case EB_M_XN_VY: case EB_M_YN_VY: return ST_BILINEAR;
     case EB_M_EXX: case EB_M_EXY: case EB_M_PR: case EB_M_SR_RATIO: return ST_POST_STOKES;
     case EB_M_SUBGRID_DT: return ST_SUBGRID_HEAT;
-    case EB_M_TK: return ST_REMAINING_DT;
-    case EB_M_X: case EB_M_Y: case EB_M_SXX: case EB_M_SXY: case EB_M_VX: case EB_M_VY: case EB_M_SPIN:
-      return ST_ADVECT;
-    default: return ST_STRAIN;  // gii, strain_plastic, strain_rate_plastic, and fields the cycle only reads
+    default: return ST_TAIL;  // tk, x, y, stresses, strains, velocities, and fields the cycle only reads
   }
 }
 
@@ -66,11 +65,8 @@ int run_step(eb_ctx* c, int s) {
     case ST_STOKES: return eb_interpolate_marker_stokes_parameters_to_grid(c);
     case ST_POST_STOKES: return eb_post_stokes_marker_gathers(c);
     case ST_SUBGRID_STRESS: return eb_update_subgrid_stress(c);
-    case ST_CORRECTION: return eb_apply_marker_stress_correction(c);
     case ST_SUBGRID_HEAT: return eb_subgrid_heat_diffusion_update(c);
-    case ST_REMAINING_DT: return eb_add_remaining_grid_change_to_marker_temperature(c);
-    case ST_ADVECT: return eb_advect_markers_and_rotate_stress(c);
-    default: return eb_update_marker_strain(c);
+    default: return eb_correct_advect_and_update_strain(c);
   }
 }
 
@@ -143,7 +139,7 @@ extern "C" int eb_marker_cycle_host(eb_ctx* c, const eb_marker_io* io) {
   for (int k = 0; k < io->n_out; ++k) outs[final_step(io->out_fields[k])].push_back(k);
 
   for (int s = 0; s < ST_COUNT; ++s) {
-    int g = s <= ST_BILINEAR ? 0 : (s == ST_HEAT ? 1 : (s < ST_STRAIN ? 2 : 3));
+    int g = s <= ST_BILINEAR ? 0 : (s == ST_HEAT ? 1 : (s < ST_TAIL ? 2 : 3));
     if (g == 2 && other_in) g = 3;  // an input of unknown first reader: wait for everything
     EB_CK(c, cudaStreamWaitEvent(c->stream, group_done[g], 0));
     if ((rc = run_step(c, s))) {

@@ -266,6 +266,15 @@ int eb_advect_markers_and_rotate_stress(eb_ctx* ctx);
 /* Advection.update_marker_strain!  (Advection.jl:169-178 -> MarkersStrain.jl:11-136) */
 int eb_update_marker_strain(eb_ctx* ctx);
 
+/* eb_apply_marker_stress_correction, eb_add_remaining_grid_change_to_marker_temperature,
+ * eb_advect_markers_and_rotate_stress and eb_update_marker_strain in one pass over the
+ * markers (each marker's fields read and written once), with the same results as the
+ * four calls in that order.  Between eb_subgrid_heat_diffusion_update and the next time
+ * step, the reference runs these four (StokesContinuitySolver.jl:365-381,
+ * HeatSolver.jl:94-122, TimeLoop.jl:261); nothing it does in between reads or writes the
+ * fields involved.                                                                  */
+int eb_correct_advect_and_update_strain(eb_ctx* ctx);
+
 /* ---- Stokes-continuity step --------------------------------------------------
  * The grid-side half of StokesContinuitySolver.solve_viscoelastic_stokes_continuity_equations!
  * (src/stokes_continuity_solver/StokesContinuitySolver.jl:68-110).  Inputs are

@@ -47,3 +47,20 @@ def test_cycle_from_host_rejects_bad_matid(eb):
     mic.marker_cycle_host({"matid": model.markers["matid"].astype(np.int16)}, {"x": np.zeros(model.marknum)})
     assert x0.shape == (model.marknum,)
     mic.close()
+
+
+@pytest.mark.parametrize("name", ["rift_small", "sinking_block"])
+def test_fused_tail_matches_the_four_calls(eb, name):
+    """eb_correct_advect_and_update_strain against stress correction, remaining temperature
+    change, advection and strain update called one by one: identical marker fields."""
+    model = eb.synthetic.config(name)
+    outs = []
+    for fused in (False, True):
+        mic = eb.MarkerInCell(0)
+        mic.load_model(model)
+        mic.marker_cycle(fused=fused)
+        outs.append({k: mic.download_marker(k) for k in ("x", "y", "sxx", "sxy", "tk", "gii", "strain_plastic",
+                                                         "strain_rate_plastic", "vx", "vy", "spin")})
+        mic.close()
+    for k in outs[0]:
+        assert np.array_equal(outs[0][k], outs[1][k]), k
