@@ -469,6 +469,18 @@ class MarkerInCell:
                 break
         return history
 
+    # --------------------------------------------------------- checkpoints --
+    def checkpoint_write(self, path) -> None:
+        """Every field the context holds, in one file (eb_checkpoint_write)."""
+        self._check(self._lib.eb_checkpoint_write(self._ctx, str(path).encode()))
+
+    def checkpoint_read(self, path) -> None:
+        """Restore the fields of eb_checkpoint_write (same grid; markers resized to the file's count)."""
+        self._check(self._lib.eb_checkpoint_read(self._ctx, str(path).encode()))
+        import struct
+        with open(path, "rb") as fh:
+            self.marknum = struct.unpack("<8x4q", fh.read(40))[3]
+
     # ------------------------------------------------------- step boundary --
     def set_rock_tables(self, mat_rho: np.ndarray, mat_cp: np.ndarray, mat_kt: np.ndarray) -> None:
         """Material tables of the rock-property models: mat_rho (nmat, 3), mat_cp (nmat),

@@ -213,7 +213,7 @@ ALL_SYMBOLS = [
     "eb_update_nodes_for_plastic_yielding", "eb_stokes_export_coo",
     "eb_marker_to_basic_grid_average_noalloc", "eb_marker_cycle_host", "eb_set_rock_tables",
     "eb_set_sediment_porosity", "eb_update_marker_rock_properties",
-    "eb_update_model_time_step_using_displacement_limit",
+    "eb_update_model_time_step_using_displacement_limit", "eb_checkpoint_write", "eb_checkpoint_read",
 ] + ENTRY_POINTS + STOKES_ENTRY_POINTS + HEAT_ENTRY_POINTS
 
 _lib = None
@@ -272,6 +272,8 @@ def load(path: pathlib.Path | str | None = None) -> C.CDLL:
     lib.eb_marker_to_basic_grid_average_noalloc.argtypes = [vp, vp, vp, C.c_int64, vp, C.c_int64, vp, C.c_int64,
                                                             vp, vp, vp, C.c_char_p, C.c_size_t]
     lib.eb_marker_cycle_host.argtypes = [vp, C.POINTER(MarkerIO)]
+    lib.eb_checkpoint_write.argtypes = [vp, C.c_char_p]
+    lib.eb_checkpoint_read.argtypes = [vp, C.c_char_p]
     lib.eb_set_rock_tables.argtypes = [vp, C.POINTER(RockDesc)]
     lib.eb_set_sediment_porosity.argtypes = [vp, C.POINTER(SedimentDesc)]
     lib.eb_update_marker_rock_properties.argtypes = [vp, C.POINTER(RockParams)]

@@ -709,3 +709,101 @@ extern "C" int eb_correct_advect_and_update_strain(eb_ctx* c) {
   if (rc) return rc;
   return finish(c, launch_marker_tail(c));
 }
+
+// ------------------------------------------------------------ checkpoints ---
+// File layout (little-endian host words): "EBGPUCK1", int64 version (1), xnum, ynum,
+// marknum, entry count; then per entry int32 kind (0 marker field, 1 grid field), int32
+// field id, int64 byte count and the bytes of the field in the layout eb_marker_download /
+// eb_grid_download return.  Every field the context holds is written; derived state (the
+// cell sort, FP32 mirrors, solver workspaces) is rebuilt by the next steps.
+namespace {
+constexpr char kCkMagic[8] = {'E', 'B', 'G', 'P', 'U', 'C', 'K', '1'};
+}  // namespace
+
+extern "C" int eb_checkpoint_write(eb_ctx* c, const char* path) {
+  if (!c || !path) return EB_BAD_INPUT;
+  if (!c->have_grid) return eb_fail(c, EB_NOT_READY, "eb_set_grid has not been called");
+  cudaSetDevice(c->device);
+  EB_CK(c, cudaStreamSynchronize(c->stream));
+  std::FILE* fp = std::fopen(path, "wb");
+  if (!fp) return eb_fail(c, EB_BAD_INPUT, std::string("cannot open ") + path + " for writing");
+  std::vector<std::pair<int, int>> entries;
+  for (int f = 0; f < EB_M_NFIELDS; ++f)
+    if (c->mf[f] && c->M > 0) entries.push_back({0, f});
+  for (int f = 0; f < EB_G_NFIELDS; ++f)
+    if (c->gf[f]) entries.push_back({1, f});
+  const int64_t head[5] = {1, c->xnum, c->ynum, c->M, (int64_t)entries.size()};
+  bool ok = std::fwrite(kCkMagic, 1, 8, fp) == 8 && std::fwrite(head, sizeof(head), 1, fp) == 1;
+  std::vector<char> buf;
+  for (auto [kind, f] : entries) {
+    if (!ok) break;
+    const int64_t bytes = kind == 0 ? c->M * (int64_t)marker_elem_size(f) : (int64_t)(grid_field_count(c, f) * sizeof(double));
+    buf.resize((size_t)bytes);
+    cudaError_t e = cudaMemcpy(buf.data(), kind == 0 ? c->mf[f] : (void*)c->gf[f], (size_t)bytes, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) {
+      std::fclose(fp);
+      return eb_cuda(c, e, "checkpoint read-back");
+    }
+    const int32_t kf[2] = {kind, f};
+    ok = std::fwrite(kf, sizeof(kf), 1, fp) == 1 && std::fwrite(&bytes, sizeof(bytes), 1, fp) == 1 &&
+         std::fwrite(buf.data(), 1, (size_t)bytes, fp) == (size_t)bytes;
+  }
+  if (std::fclose(fp) != 0) ok = false;
+  return ok ? EB_OK : eb_fail(c, EB_BAD_INPUT, std::string("writing ") + path + " failed");
+}
+
+extern "C" int eb_checkpoint_read(eb_ctx* c, const char* path) {
+  if (!c || !path) return EB_BAD_INPUT;
+  if (!c->have_grid) return eb_fail(c, EB_NOT_READY, "eb_set_grid has not been called");
+  cudaSetDevice(c->device);
+  std::FILE* fp = std::fopen(path, "rb");
+  if (!fp) return eb_fail(c, EB_BAD_INPUT, std::string("cannot open ") + path);
+  auto fail = [&](const std::string& m) { std::fclose(fp); return eb_fail(c, EB_BAD_INPUT, m); };
+  char magic[8];
+  int64_t head[5];
+  if (std::fread(magic, 1, 8, fp) != 8 || std::memcmp(magic, kCkMagic, 8) != 0 || std::fread(head, sizeof(head), 1, fp) != 1)
+    return fail(std::string(path) + " is not an eb checkpoint");
+  if (head[0] != 1) return fail("unsupported checkpoint version");
+  if (head[1] != c->xnum || head[2] != c->ynum) return fail("checkpoint grid differs from the context's grid");
+  if (head[3] != c->M) {
+    fclose(fp);
+    int rc = eb_resize_markers(c, head[3]);
+    if (rc) return rc;
+    fp = std::fopen(path, "rb");
+    if (!fp || std::fseek(fp, 8 + (long)sizeof(head), SEEK_SET) != 0) return fail("cannot reopen the checkpoint");
+  }
+  std::vector<char> buf;
+  bool matid = false;
+  for (int64_t k = 0; k < head[4]; ++k) {
+    int32_t kf[2];
+    int64_t bytes;
+    if (std::fread(kf, sizeof(kf), 1, fp) != 1 || std::fread(&bytes, sizeof(bytes), 1, fp) != 1)
+      return fail("truncated checkpoint");
+    const int kind = kf[0], f = kf[1];
+    if (kind != 0 && kind != 1) return fail("bad checkpoint entry");
+    if ((kind == 0 && (f < 0 || f >= EB_M_NFIELDS)) || (kind == 1 && (f < 0 || f >= EB_G_NFIELDS)))
+      return fail("checkpoint field id out of range");
+    const int64_t want = kind == 0 ? c->M * (int64_t)marker_elem_size(f) : (int64_t)(grid_field_count(c, f) * sizeof(double));
+    if (bytes != want) return fail("checkpoint field size differs from the context's");
+    buf.resize((size_t)bytes);
+    if (std::fread(buf.data(), 1, (size_t)bytes, fp) != (size_t)bytes) return fail("truncated checkpoint");
+    int rc = kind == 0 ? ensure_marker_field(c, f) : ensure_grid_field(c, f);
+    if (rc) { std::fclose(fp); return rc; }
+    cudaError_t e = cudaMemcpyAsync(kind == 0 ? c->mf[f] : (void*)c->gf[f], buf.data(), (size_t)bytes,
+                                    cudaMemcpyHostToDevice, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) { std::fclose(fp); return eb_cuda(c, e, "checkpoint upload"); }
+    if (kind == 0 && f == EB_M_MATID) matid = true;
+  }
+  std::fclose(fp);
+  c->located = false;  // the cell sort is rebuilt by the next bilinear set-up
+  if (matid && c->M > 0) {
+    c->matid_min = 0;
+    c->matid_max = 0;
+    int rc = launch_matid_range(c, c->stream);
+    if (rc) return rc;
+    EB_CK(c, cudaStreamSynchronize(c->stream));
+    return finish_matid_range(c);
+  }
+  return EB_OK;
+}

@@ -534,6 +534,18 @@ int eb_update_model_time_step_using_displacement_limit(eb_ctx* ctx, double marke
                                                        int32_t iuse_local_adaptive_time_stepping,
                                                        double* timestep, int32_t* timestep_update);
 
+/* ---- checkpoints -----------------------------------------------------------
+ * No counterpart in the reference, whose backups (model_manager/backup/core/MakeBackup.jl:22)
+ * and XDMF output (model_manager/xdmf/markers/core/TimeStep.jl) write the host arrays: those
+ * arrays are eb_marker_download / eb_grid_download in the reference's layout, and a resumed
+ * run uploads them again.  These two calls save and restore every field the context
+ * holds in one file (a header with the grid size and marknum, then each field's bytes in
+ * that same layout), so a GPU run can stop and resume without the host model.  Reading
+ * needs eb_set_grid with the same grid (markers are resized to the file's marknum); the
+ * next eb_initialize_bilinear_interpolation rebuilds the cell sort.                   */
+int eb_checkpoint_write(eb_ctx* ctx, const char* path);
+int eb_checkpoint_read(eb_ctx* ctx, const char* path);
+
 /* ---- one marker cycle from host arrays -------------------------------------
  * No single counterpart in the reference: the sequence of eb_get_marker_inside_flags,
  * eb_initialize_bilinear_interpolation, eb_interpolate_marker_heat_parameters_to_grid,
