@@ -47,7 +47,19 @@ ALGO_BYTES_PER_MARKER = {
     "k_advect": 8 + 8 + 1 + 16 + 16 + 24 + 32,             # xn/yn, fx/fy, flags, rw x/y, w vx/vy/spin, rw sxx/sxy
     "k_post_stokes": 8 + 8 + 1 + 4 + 8 + 4 * 8,
     "k_locate_count": 16 + 1 + 8 + 8 + 1 + 4,               # x,y, inside, w xn/yn, fx/fy, flags, count atomics
+    # flags, xn/yn, fx/fy, rw sxx/sxy/tk/x/y/gii, w vx/vy/spin, r exx/exy/pfailure; plastic markers
+    # (pfailure == 1) also read eta/eta_flow, rw strain_plastic, w strain_rate_plastic (+40 B)
+    "k_tail": 1 + 8 + 8 + 6 * 16 + 24 + 16 + 4,
 }
+TAIL_PLASTIC_BYTES = 8 + 8 + 16 + 8
+
+
+def algo_bytes_per_marker(kernel: str, model) -> float | None:
+    """Algorithmic bytes per marker of `kernel` on this workload."""
+    bpm = ALGO_BYTES_PER_MARKER.get(kernel)
+    if bpm is not None and kernel == "k_tail":
+        bpm += TAIL_PLASTIC_BYTES * float(np.mean(model.markers["pfailure"] == 1.0))
+    return bpm
 
 # DRAM bytes per marker (dram__bytes_read.sum + dram__bytes_write.sum) from one
 # `ncu --set full` capture of each kernel on the 2.56M-marker rift (801x201
@@ -361,7 +373,7 @@ def main():
     dom = max(prof, key=lambda k: prof[k][0])
     dom_ms, dom_n = kern[dom]
     peak, peak_kind = peaks()
-    bpm = ALGO_BYTES_PER_MARKER.get(dom)
+    bpm = algo_bytes_per_marker(dom, model)
     roofline = None
     if bpm is not None:
         achieved = bpm * M / (dom_ms * 1e-3) / 1e9

@@ -469,6 +469,30 @@ class MarkerInCell:
                 break
         return history
 
+    # ----------------------------------------------------- marker recycling --
+    def recycle_markers(self, matid_sticky_air: int, matid_sticky_water: int, matid_asthenosphere: int,
+                        xsize: float, ysize: float, velocity_y_upper: float, velocity_y_lower: float,
+                        temperature_bottom: float, seed: int, counter: int, iuse_random_fric: int = 0,
+                        delta_fric_coef: float = 0.0) -> tuple:
+        """MarkerRecycle.recycle_markers! for the extension models (types/Extension.jl:14-129);
+        returns (nrecycle_air, nrecycle_subsurface)."""
+        p = _abi.RecycleParams(1, matid_sticky_air, matid_sticky_water, matid_asthenosphere, xsize, ysize,
+                               velocity_y_upper, velocity_y_lower, temperature_bottom, iuse_random_fric,
+                               delta_fric_coef, seed, counter)
+        na, ns = C.c_int64(), C.c_int64()
+        self._check(self._lib.eb_recycle_markers(self._ctx, C.byref(p), C.byref(na), C.byref(ns)))
+        return na.value, ns.value
+
+    def recycled_markers(self) -> tuple:
+        """(1-based indices, flags: 0 sticky / 1 subsurface) of the last recycle_markers."""
+        n = C.c_int64()
+        self._check(self._lib.eb_recycled_markers(self._ctx, None, None, 0, C.byref(n)))
+        idx = np.zeros(n.value, np.int64)
+        fl = np.zeros(n.value, np.int8)
+        if n.value:
+            self._check(self._lib.eb_recycled_markers(self._ctx, _ptr(idx), _ptr(fl), n.value, C.byref(n)))
+        return idx, fl
+
     # --------------------------------------------------------- checkpoints --
     def checkpoint_write(self, path) -> None:
         """Every field the context holds, in one file (eb_checkpoint_write)."""

@@ -169,6 +169,14 @@ class RockParams(C.Structure):
                 ("iuse_sed_porosity", C.c_int32), ("maximum_heat_capacity", C.c_double)]
 
 
+class RecycleParams(C.Structure):
+    _fields_ = [("recycle_type", C.c_int32), ("matid_sticky_air", C.c_int32), ("matid_sticky_water", C.c_int32),
+                ("matid_asthenosphere", C.c_int32), ("xsize", C.c_double), ("ysize", C.c_double),
+                ("velocity_y_upper", C.c_double), ("velocity_y_lower", C.c_double),
+                ("temperature_bottom", C.c_double), ("iuse_random_fric", C.c_int32), ("delta_fric_coef", C.c_double),
+                ("seed", C.c_uint64), ("counter", C.c_int64)]
+
+
 class HeatParams(C.Structure):
     _fields_ = [("timestep", C.c_double), ("max_temp_change", C.c_double), ("gravity_x", C.c_double),
                 ("gravity_y", C.c_double), ("iuse_adiabatic_heating", C.c_int32), ("iuse_shear_heating", C.c_int32)]
@@ -214,6 +222,7 @@ ALL_SYMBOLS = [
     "eb_marker_to_basic_grid_average_noalloc", "eb_marker_cycle_host", "eb_set_rock_tables",
     "eb_set_sediment_porosity", "eb_update_marker_rock_properties",
     "eb_update_model_time_step_using_displacement_limit", "eb_checkpoint_write", "eb_checkpoint_read",
+    "eb_recycle_markers", "eb_recycled_markers", "eb_recycle_uniforms",
 ] + ENTRY_POINTS + STOKES_ENTRY_POINTS + HEAT_ENTRY_POINTS
 
 _lib = None
@@ -272,6 +281,11 @@ def load(path: pathlib.Path | str | None = None) -> C.CDLL:
     lib.eb_marker_to_basic_grid_average_noalloc.argtypes = [vp, vp, vp, C.c_int64, vp, C.c_int64, vp, C.c_int64,
                                                             vp, vp, vp, C.c_char_p, C.c_size_t]
     lib.eb_marker_cycle_host.argtypes = [vp, C.POINTER(MarkerIO)]
+    lib.eb_recycle_markers.argtypes = [vp, C.POINTER(RecycleParams), C.POINTER(C.c_int64), C.POINTER(C.c_int64)]
+    lib.eb_recycled_markers.argtypes = [vp, vp, vp, C.c_int64, C.POINTER(C.c_int64)]
+    lib.eb_recycle_uniforms.argtypes = [C.c_uint64, C.c_int64, C.c_uint32, C.c_int64, C.POINTER(C.c_double),
+                                        C.POINTER(C.c_double)]
+    lib.eb_recycle_uniforms.restype = None
     lib.eb_checkpoint_write.argtypes = [vp, C.c_char_p]
     lib.eb_checkpoint_read.argtypes = [vp, C.c_char_p]
     lib.eb_set_rock_tables.argtypes = [vp, C.POINTER(RockDesc)]
@@ -293,7 +307,7 @@ def load(path: pathlib.Path | str | None = None) -> C.CDLL:
     lib.eb_heat_size.restype = C.c_int64
     for name in ALL_SYMBOLS:
         if name not in ("eb_last_error", "eb_stream", "eb_launch_count", "eb_stokes_pscale", "eb_stokes_size",
-                        "eb_heat_size"):
+                        "eb_heat_size", "eb_recycle_uniforms"):
             getattr(lib, name).restype = C.c_int
     if path is None:
         _lib = lib

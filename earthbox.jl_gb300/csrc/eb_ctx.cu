@@ -300,6 +300,8 @@ extern "C" int eb_destroy(eb_ctx* c) {
   for (cudaEvent_t e : c->prof.pool) cudaEventDestroy(e);
   cudaFree(c->dflag);
   cudaFree(c->d_minmax);
+  cudaFree(c->recycle_list);
+  cudaFree(c->recycle_flags);
   if (c->h_pinned) cudaFreeHost(c->h_pinned);
   if (c->copy_in) cudaStreamDestroy(c->copy_in);
   if (c->copy_out) cudaStreamDestroy(c->copy_out);

@@ -135,6 +135,11 @@ struct eb_ctx {
   const double *sed_tx = nullptr, *sed_ty = nullptr;
   double sed_kw = 0.0, sed_rhow = 0.0, sed_cpw = 0.0;
   bool have_sed = false;
+  // the markers recycled by the last eb_recycle_markers (eb_recycle.cu)
+  int64_t* recycle_list = nullptr;
+  int8_t* recycle_flags = nullptr;
+  size_t recycle_cap = 0;
+  int64_t recycle_n = 0;
 };
 
 // Stokes system storage shared by the assembly (eb_stokes_build.cu) and the

@@ -1,0 +1,237 @@
+// eb_recycle.cu -- recycling of markers that left the domain.
+//
+// Reference: MarkerRecycle.recycle_markers! (boundary_conditions/marker_recycle/MarkerRecycle.jl)
+// for the extension models (LithosphericExtensionFixedBoundaries, ...Asymmetric,
+// ...DepthDependent -> types/Extension.jl:14-129):
+//   InitializeMarkerRecycling.initialize_recycling (utils/InitializeMarkerRecycling.jl): the
+//     outside markers in marker order (GridFuncs.get_indices_of_markers_outside_domain),
+//     split into sticky (air/water material) and subsurface;
+//   Extension.calculate_recycled_locations (types/Extension.jl:53-97): sticky markers re-enter
+//     at x = U xsize, y = U |vyu dt| (the top band), subsurface markers at x = U xsize,
+//     y = ysize - U |vyl dt| (the bottom band);
+//   Coordinates.reset_recycled_marker_coordinates (utils/Coordinates.jl): the k-th sticky
+//     outside marker takes the k-th sticky position, likewise for subsurface;
+//   ResetMarkers.reset_recycled_marker_properties! (utils/ResetMarkers.jl): sticky markers
+//     become sticky air at temperature_top with zero pressure, stress, strain rate, strain,
+//     melt and viscosity; subsurface markers become asthenosphere at temperature_bottom with
+//     pressure 3300 * 9.81 * gridy_b[ynum] (PressureReset.jl), stress 1.96e6 Pa, strain rate
+//     1e-14 1/s, viscosity 1e20 Pa s; both take fric_ini = fric = mat_plastic[matid, 3],
+//     minus delta_fric_coef when random friction is on and the marker's random number is
+//     <= 0.5 (FrictionRandomizer.randomize_initial_friction_coefficient).
+//
+// Random numbers.  The reference draws them from Julia's global generator (unseeded); here
+// every uniform comes from Philox-4x32-10 (Salmon, Moraes, Dror, Shaw, "Parallel random
+// numbers: as easy as 1, 2, 3", SC 2011) keyed by a caller seed, counter (j, stream, step):
+// stream 0 gives the j-th sticky position, stream 1 the j-th subsurface position, stream 2
+// marker j's friction number.  The same numbers in the oracle give the same results.
+// Built with -fmad=false: ysize + u * (-|vyl dt|) is rounded twice, as Julia evaluates it.
+#include "eb_internal.h"
+
+#include <cmath>
+#include <vector>
+
+namespace {
+
+constexpr int kB = 256;
+
+// Philox-4x32-10: ten rounds of two 32x32->64 multiplies and a Weyl-sequence key schedule.
+__host__ __device__ inline void philox4x32(uint32_t c[4], uint32_t k0, uint32_t k1) {
+  for (int r = 0; r < 10; ++r) {
+    const uint64_t p0 = (uint64_t)0xD2511F53u * c[0], p1 = (uint64_t)0xCD9E8D57u * c[2];
+    const uint32_t hi0 = (uint32_t)(p0 >> 32), lo0 = (uint32_t)p0, hi1 = (uint32_t)(p1 >> 32), lo1 = (uint32_t)p1;
+    const uint32_t n0 = hi1 ^ c[1] ^ k0, n1 = lo1, n2 = hi0 ^ c[3] ^ k1, n3 = lo0;
+    c[0] = n0; c[1] = n1; c[2] = n2; c[3] = n3;
+    k0 += 0x9E3779B9u;
+    k1 += 0xBB67AE85u;
+  }
+}
+// two uniforms in [0, 1) with 53 random bits each
+__host__ __device__ inline void uniforms(uint64_t seed, int64_t step, uint32_t stream, int64_t j, double& u0,
+                                        double& u1) {
+  uint32_t c[4] = {(uint32_t)j, (uint32_t)((uint64_t)j >> 32), stream, (uint32_t)step};
+  philox4x32(c, (uint32_t)seed, (uint32_t)(seed >> 32));
+  u0 = (double)((((uint64_t)c[0] << 32) | c[1]) >> 11) * 0x1p-53;
+  u1 = (double)((((uint64_t)c[2] << 32) | c[3]) >> 11) * 0x1p-53;
+}
+
+struct RecycleK {
+  int16_t sticky_air, sticky_water, asth;
+  double xsize, ysize, disp_top, disp_bottom;  // disp_top = |vyu dt|, disp_bottom = -|vyl dt|
+  double t_top, t_bottom, p_reset;
+  double fric_air, fric_asth;                   // mat_plastic[., 3]
+  int32_t random_fric;
+  double delta_fric;
+  uint64_t seed;
+  int64_t step;
+};
+
+__device__ __forceinline__ bool sticky(int16_t m, const RecycleK& p) { return m == p.sticky_air || m == p.sticky_water; }
+
+// per block: number of outside markers and of outside sticky markers
+__global__ void k_recycle_count(DevMarkers mk, RecycleK p, int32_t* __restrict__ counts, int32_t nblocks) {
+  const int64_t m = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const bool out = m < mk.M && mk.inside[m] != 1;
+  const bool st = out && sticky(mk.matid[m], p);
+  const int n_out = __syncthreads_count(out), n_st = __syncthreads_count(st);
+  if (threadIdx.x == 0) {
+    counts[blockIdx.x] = n_out;
+    counts[nblocks + blockIdx.x] = n_st;
+  }
+}
+
+// ranks in marker order, new positions and property resets; list[r] = 1-based index
+__global__ void k_recycle_apply(DevMarkers mk, RecycleK p, const int32_t* __restrict__ offsets, int32_t nblocks,
+                                int64_t n_air, int64_t* __restrict__ list, int8_t* __restrict__ flags) {
+  __shared__ int32_t s_out[kB / 32], s_st[kB / 32];
+  const int64_t m = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const bool out = m < mk.M && mk.inside[m] != 1;
+  const bool st = out && sticky(mk.matid[m], p);
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const unsigned b_out = __ballot_sync(0xffffffffu, out), b_st = __ballot_sync(0xffffffffu, st);
+  if (lane == 0) { s_out[w] = __popc(b_out); s_st[w] = __popc(b_st); }
+  __syncthreads();
+  if (!out) return;
+  int32_t r_out = offsets[blockIdx.x], r_st = offsets[nblocks + blockIdx.x];
+  for (int k = 0; k < w; ++k) { r_out += s_out[k]; r_st += s_st[k]; }
+  const unsigned below = (1u << lane) - 1u;
+  r_out += __popc(b_out & below);
+  r_st += __popc(b_st & below);
+  double ux, uy;
+  if (st && n_air > 0) {
+    uniforms(p.seed, p.step, 0u, r_st, ux, uy);
+    mk.x[m] = 0.0 + ux * p.xsize;
+    mk.y[m] = 0.0 + uy * p.disp_top;
+  } else {
+    const int64_t r_sub = (int64_t)r_out - r_st;
+    uniforms(p.seed, p.step, 1u, r_sub, ux, uy);
+    mk.x[m] = 0.0 + ux * p.xsize;
+    mk.y[m] = p.ysize + uy * p.disp_bottom;
+  }
+  list[r_out] = m + 1;
+  flags[r_out] = st ? 0 : 1;
+  double fric;
+  if (st) {
+    mk.matid[m] = p.sticky_air;
+    mk.tk[m] = p.t_top;
+    mk.pr[m] = 0.0;
+    mk.sxx[m] = 0.0; mk.sxy[m] = 0.0;
+    mk.exx[m] = 0.0; mk.exy[m] = 0.0;
+    mk.eta[m] = 0.0;
+    fric = p.fric_air;
+  } else {
+    mk.matid[m] = p.asth;
+    mk.tk[m] = p.t_bottom;
+    mk.pr[m] = p.p_reset;
+    mk.sxx[m] = 1.96e6; mk.sxy[m] = 1.96e6;
+    mk.exx[m] = 1e-14; mk.exy[m] = 1e-14;
+    mk.eta[m] = 1e20;
+    fric = p.fric_asth;
+    if (p.random_fric == 1) {
+      double r0, r1;
+      uniforms(p.seed, p.step, 2u, m, r0, r1);
+      if (r0 <= 0.5) fric = fric - p.delta_fric;
+    }
+  }
+  mk.sr_ratio[m] = 0.0;
+  mk.gii[m] = 0.0; mk.sp[m] = 0.0; mk.srp[m] = 0.0;
+  mk.melt[m] = 0.0;
+  mk.pfailure[m] = 0.0f;
+  mk.fric_ini[m] = fric;
+  mk.fric[m] = fric;
+}
+
+}  // namespace
+
+// shared with the oracle test: the uniforms of (seed, step, stream, j)
+extern "C" void eb_recycle_uniforms(uint64_t seed, int64_t step, uint32_t stream, int64_t j, double* u0, double* u1) {
+  uniforms(seed, step, stream, j, *u0, *u1);
+}
+
+extern "C" int eb_recycle_markers(eb_ctx* c, const eb_recycle_params* rp, int64_t* nrecycle_air,
+                                  int64_t* nrecycle_subsurface) {
+  if (!c || !rp) return EB_BAD_INPUT;
+  if (!c->have_grid || !c->have_params || !c->have_mats) return eb_fail(c, EB_NOT_READY, "grid, parameters and materials must be set");
+  if (rp->recycle_type != 1) return eb_fail(c, EB_BAD_INPUT, "recycle_type must be 1 (extension models)");
+  const int64_t nmat = c->mats.nmat;
+  for (int64_t id : {(int64_t)rp->matid_sticky_air, (int64_t)rp->matid_sticky_water, (int64_t)rp->matid_asthenosphere})
+    if (id < 1 || id > nmat) return eb_fail(c, EB_BAD_INPUT, "recycle material id outside the material table");
+  if (c->M > 0 && c->matid_min < 1) return eb_fail(c, EB_NOT_READY, "marker_matid has not been uploaded");
+  cudaSetDevice(c->device);
+  int rc;
+  const int need[] = {EB_M_INSIDE, EB_M_MATID, EB_M_X, EB_M_Y, EB_M_TK, EB_M_PR, EB_M_SXX, EB_M_SXY, EB_M_EXX, EB_M_EXY,
+                      EB_M_ETA, EB_M_SR_RATIO, EB_M_GII, EB_M_STRAIN_PLASTIC, EB_M_STRAIN_RATE_PLASTIC, EB_M_MELTFRAC,
+                      EB_M_PFAILURE, EB_M_FRIC_INI, EB_M_FRIC};
+  for (int f : need)
+    if ((rc = ensure_marker_field(c, f))) return rc;
+  if (nrecycle_air) *nrecycle_air = 0;
+  if (nrecycle_subsurface) *nrecycle_subsurface = 0;
+  c->recycle_n = 0;
+  if (c->M == 0) return EB_OK;
+  const int32_t nblocks = (int32_t)((c->M + kB - 1) / kB);
+  int32_t* d_counts = nullptr;
+  EB_CK(c, cudaMalloc(&d_counts, 2 * (size_t)nblocks * sizeof(int32_t)));
+  // mat_plastic[., 3] (sin of the initial friction angle) of the two reset materials
+  std::vector<double>& mp = c->h_mat_plastic;
+  RecycleK p{(int16_t)rp->matid_sticky_air, (int16_t)rp->matid_sticky_water, (int16_t)rp->matid_asthenosphere,
+             rp->xsize, rp->ysize, std::fabs(rp->velocity_y_upper * c->P.timestep),
+             -std::fabs(rp->velocity_y_lower * c->P.timestep), c->P.temperature_top, rp->temperature_bottom,
+             3300.0 * 9.81 * c->h_gy.back(), mp[2 * nmat + rp->matid_sticky_air - 1],
+             mp[2 * nmat + rp->matid_asthenosphere - 1], rp->iuse_random_fric, rp->delta_fric_coef, rp->seed,
+             rp->counter};
+  k_recycle_count<<<nblocks, kB, 0, c->stream>>>(dev_markers(c), p, d_counts, nblocks);
+  c->launches++;
+  std::vector<int32_t> h(2 * (size_t)nblocks);
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaMemcpyAsync(h.data(), d_counts, h.size() * sizeof(int32_t), cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) { cudaFree(d_counts); return eb_cuda(c, e, "recycle count"); }
+  int64_t n_out = 0, n_air = 0;
+  for (int32_t b = 0; b < nblocks; ++b) {
+    const int32_t o = h[b], s = h[nblocks + b];
+    h[b] = (int32_t)n_out;
+    h[nblocks + b] = (int32_t)n_air;
+    n_out += o;
+    n_air += s;
+  }
+  if (n_out > 0) {
+    if ((size_t)n_out > c->recycle_cap) {
+      cudaFree(c->recycle_list);
+      cudaFree(c->recycle_flags);
+      c->recycle_list = nullptr;
+      c->recycle_flags = nullptr;
+      c->recycle_cap = 0;
+      e = cudaMalloc(&c->recycle_list, n_out * sizeof(int64_t));
+      if (e == cudaSuccess) e = cudaMalloc(&c->recycle_flags, n_out * sizeof(int8_t));
+      if (e != cudaSuccess) { cudaFree(d_counts); return eb_cuda(c, e, "recycle list"); }
+      c->recycle_cap = (size_t)n_out;
+    }
+    e = cudaMemcpyAsync(d_counts, h.data(), h.size() * sizeof(int32_t), cudaMemcpyHostToDevice, c->stream);
+    if (e == cudaSuccess) {
+      EB_PROF(c, "k_recycle_apply");
+      k_recycle_apply<<<nblocks, kB, 0, c->stream>>>(dev_markers(c), p, d_counts, nblocks, n_air, c->recycle_list,
+                                                     c->recycle_flags);
+      c->launches++;
+      prof_end(c);
+      e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  }
+  cudaFree(d_counts);
+  if (e != cudaSuccess) return eb_cuda(c, e, "marker recycling");
+  c->recycle_n = n_out;
+  c->located = false;  // markers moved
+  if (nrecycle_air) *nrecycle_air = n_air;
+  if (nrecycle_subsurface) *nrecycle_subsurface = n_out - n_air;
+  return EB_OK;
+}
+
+extern "C" int eb_recycled_markers(eb_ctx* c, int64_t* indices, int8_t* flags, int64_t capacity, int64_t* n) {
+  if (!c) return EB_BAD_INPUT;
+  if (n) *n = c->recycle_n;
+  if (!indices || !flags || c->recycle_n == 0) return EB_OK;
+  if (capacity < c->recycle_n) return eb_fail(c, EB_BAD_INPUT, "recycled-marker arrays too small");
+  cudaSetDevice(c->device);
+  EB_CK(c, cudaMemcpy(indices, c->recycle_list, c->recycle_n * sizeof(int64_t), cudaMemcpyDeviceToHost));
+  EB_CK(c, cudaMemcpy(flags, c->recycle_flags, c->recycle_n * sizeof(int8_t), cudaMemcpyDeviceToHost));
+  return EB_OK;
+}

@@ -534,6 +534,36 @@ int eb_update_model_time_step_using_displacement_limit(eb_ctx* ctx, double marke
                                                        int32_t iuse_local_adaptive_time_stepping,
                                                        double* timestep, int32_t* timestep_update);
 
+/* ---- marker recycling ------------------------------------------------------
+ * MarkerRecycle.recycle_markers! for the extension models (boundary_conditions/marker_recycle/
+ * types/Extension.jl:14-129 with utils/{InitializeMarkerRecycling,Coordinates,ResetMarkers,
+ * PressureReset}.jl): the markers whose inside flag (eb_get_marker_inside_flags) is not +1,
+ * in marker order, re-enter in the top band (sticky-air/water material) or the bottom band
+ * (the rest) at uniformly random positions and have their properties reset (sticky air at
+ * temperature_top; asthenosphere at temperature_bottom with the lithostatic reset pressure,
+ * stress 1.96e6 Pa, strain rate 1e-14 1/s, viscosity 1e20 Pa s).  The uniforms come from
+ * Philox-4x32-10 keyed by `seed`, counter (index, stream, `counter`): the reference uses
+ * Julia's global generator, so positions match it in distribution, not value.  Fields the
+ * context does not hold (serpentinisation, extracted melt, stratigraphic age) are reset by
+ * the caller for the markers eb_recycled_markers lists.                            */
+typedef struct eb_recycle_params {
+  int32_t recycle_type;            /* 1: extension models (fixed boundaries, asymmetric, depth dependent) */
+  int32_t matid_sticky_air, matid_sticky_water, matid_asthenosphere;  /* material ids                 */
+  double  xsize, ysize;            /* model size (m); the domain starts at x = y = 0                    */
+  double  velocity_y_upper, velocity_y_lower;  /* vyu, vyl (m/s): band widths |v dt|                   */
+  double  temperature_bottom;      /* K (temperature_top comes from eb_params)                          */
+  int32_t iuse_random_fric;        /* 1: fric_ini - delta_fric_coef for half of the subsurface markers  */
+  double  delta_fric_coef;
+  uint64_t seed;                   /* Philox key                                                        */
+  int64_t counter;                 /* e.g. the time-step number: new numbers every call                 */
+} eb_recycle_params;
+int eb_recycle_markers(eb_ctx* ctx, const eb_recycle_params* p, int64_t* nrecycle_air, int64_t* nrecycle_subsurface);
+/* The markers of the last eb_recycle_markers: 1-based indices and flags (0 sticky, 1 subsurface),
+ * in marker order; with null arrays only *n is set.                                   */
+int eb_recycled_markers(eb_ctx* ctx, int64_t* indices, int8_t* flags, int64_t capacity, int64_t* n);
+/* The two uniforms of Philox-4x32-10 at (seed; j, stream, counter), as the recycling uses them. */
+void eb_recycle_uniforms(uint64_t seed, int64_t counter, uint32_t stream, int64_t j, double* u0, double* u1);
+
 /* ---- checkpoints -----------------------------------------------------------
  * No counterpart in the reference, whose backups (model_manager/backup/core/MakeBackup.jl:22)
  * and XDMF output (model_manager/xdmf/markers/core/TimeStep.jl) write the host arrays: those

@@ -1,6 +1,7 @@
 """CPU oracle (TEST INFRASTRUCTURE ONLY) for the step-boundary updates: the rock
 properties of the markers (rock_properties/RockProperties.jl:99-125) and the
-displacement-limited time step (time_step/update/Update.jl:16-219), restated in
+displacement-limited time step (time_step/update/Update.jl:16-219) and the marker recycling
+of the extension models (marker_recycle/types/Extension.jl:14-129), restated in
 boundary_oracle.c.  Only tests/ use it."""
 from __future__ import annotations
 
@@ -81,3 +82,44 @@ def rock_properties(mk: dict, mat_rho, mat_cp, mat_kt, density_model, rhocp_mode
                             C.c_int64(0 if tx is None else len(tx)), _p(ids), C.c_int64(0 if ids is None else len(ids)),
                             C.c_double(wk), C.c_double(wr), C.c_double(wc))
     return out
+
+
+RECYCLE_FIELDS = ("x", "y", "tk", "pr", "sxx", "sxy", "exx", "exy", "eta", "sr_ratio", "gii", "strain_plastic",
+                  "strain_rate_plastic", "meltfrac", "fric_ini", "fric")
+
+
+def philox4x32_10(ctr, key) -> tuple:
+    c = (C.c_uint32 * 4)(*[int(v) & 0xFFFFFFFF for v in ctr])
+    lib().o_philox4x32_10(c, C.c_uint32(key[0]), C.c_uint32(key[1]))
+    return tuple(c)
+
+
+def recycle_uniforms(seed: int, step: int, stream: int, j: int) -> tuple:
+    u0, u1 = C.c_double(), C.c_double()
+    lib().o_recycle_uniforms(C.c_uint64(seed), C.c_int64(step), C.c_uint32(stream), C.c_int64(j), C.byref(u0),
+                             C.byref(u1))
+    return u0.value, u1.value
+
+
+def recycle_extension(mk: dict, matid_sticky_air, matid_sticky_water, matid_asthenosphere, xsize, ysize,
+                      velocity_y_upper, velocity_y_lower, timestep, temperature_top, temperature_bottom, gridy_last,
+                      mat_plastic, iuse_random_fric, delta_fric_coef, seed, step) -> tuple:
+    """Returns (fields after recycling, 1-based indices, flags, n_air)."""
+    M = len(mk["x"])
+    out = {k: np.array(mk[k], dtype=np.float64, copy=True) for k in RECYCLE_FIELDS}
+    out["matid"] = np.array(mk["matid"], dtype=np.int16, copy=True)
+    out["pfailure"] = np.array(mk["pfailure"], dtype=np.float32, copy=True)
+    inside = np.ascontiguousarray(mk["inside"], dtype=np.int8)
+    ptrs = (C.c_void_p * len(RECYCLE_FIELDS))(*[out[k].ctypes.data for k in RECYCLE_FIELDS])
+    s = np.array([matid_sticky_air, matid_sticky_water, matid_asthenosphere], np.int16)
+    d = np.array([xsize, ysize, velocity_y_upper, velocity_y_lower, timestep, temperature_top, temperature_bottom,
+                  gridy_last, delta_fric_coef], np.float64)
+    mp = np.asfortranarray(mat_plastic, dtype=np.float64)
+    lst = np.zeros(max(M, 1), np.int64)
+    fl = np.zeros(max(M, 1), np.int8)
+    n_air = C.c_int64()
+    lib().o_recycle_extension.restype = C.c_int64
+    n = lib().o_recycle_extension(C.c_int64(M), _p(inside), _p(out["matid"]), ptrs, _p(out["pfailure"]), _p(s),
+                                  _p(d), C.c_int64(mp.shape[0]), _p(mp), C.c_int64(iuse_random_fric),
+                                  C.c_uint64(seed), C.c_int64(step), _p(lst), _p(fl), C.byref(n_air))
+    return out, lst[:n].copy(), fl[:n].copy(), n_air.value

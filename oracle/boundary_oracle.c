@@ -10,6 +10,11 @@
  *        thermal_conductivity}/types/*.jl, UpdateAdiabaticTerm.jl:19-33 and
  *        porosity/{PorosityUpdate,SedimentPorosity}.jl; topography depth by
  *        MathTools.linear_interp (utils/MathTools.jl:160-198)
+ *   o_recycle_extension             boundary_conditions/marker_recycle/types/Extension.jl:14-129
+ *       (recycle_markers! for the extension models: outside markers in marker order,
+ *        InitializeMarkerRecycling.jl:26-108; positions, Coordinates.jl:60-153; property
+ *        resets, ResetMarkers.jl:24-290; reset pressure, PressureReset.jl:20-26), with the
+ *        reference's rand() replaced by the Philox-4x32-10 stream of o_recycle_uniforms
  *
  * Grids are column-major (rows, cols).  Julia's x^2 and x^3 of a Float64 literal power
  * are x*x and x*x*x.
@@ -131,4 +136,97 @@ void o_rock_properties(int64_t M, const int8_t* inside, const int16_t* matid, co
       }
     }
   }
+}
+
+/* Philox-4x32-10 (Salmon, Moraes, Dror, Shaw, SC 2011): round function
+ * (c0,c1,c2,c3) -> (hi(M1 c2) ^ c1 ^ k0, lo(M1 c2), hi(M0 c0) ^ c3 ^ k1, lo(M0 c0)),
+ * M0 = 0xD2511F53, M1 = 0xCD9E8D57, key bumped by (0x9E3779B9, 0xBB67AE85) between rounds. */
+void o_philox4x32_10(uint32_t ctr[4], uint32_t k0, uint32_t k1) {
+  for (int round = 0; round < 10; ++round) {
+    if (round > 0) { k0 += 0x9E3779B9u; k1 += 0xBB67AE85u; }
+    const uint64_t a = (uint64_t)ctr[0] * 0xD2511F53u;
+    const uint64_t b = (uint64_t)ctr[2] * 0xCD9E8D57u;
+    const uint32_t out0 = (uint32_t)(b >> 32) ^ ctr[1] ^ k0;
+    const uint32_t out2 = (uint32_t)(a >> 32) ^ ctr[3] ^ k1;
+    ctr[1] = (uint32_t)b;
+    ctr[3] = (uint32_t)a;
+    ctr[0] = out0;
+    ctr[2] = out2;
+  }
+}
+
+/* counter (j lo, j hi, stream, step), key = seed; two doubles from the top 53 bits of
+ * (w0:w1) and (w2:w3) */
+void o_recycle_uniforms(uint64_t seed, int64_t step, uint32_t stream, int64_t j, double* u0, double* u1) {
+  uint32_t ctr[4] = {(uint32_t)(uint64_t)j, (uint32_t)((uint64_t)j >> 32), stream, (uint32_t)(uint64_t)step};
+  o_philox4x32_10(ctr, (uint32_t)seed, (uint32_t)(seed >> 32));
+  const uint64_t a = ((uint64_t)ctr[0] << 32) | ctr[1], b = ((uint64_t)ctr[2] << 32) | ctr[3];
+  *u0 = ldexp((double)(a >> 11), -53);
+  *u1 = ldexp((double)(b >> 11), -53);
+}
+
+/* Marker fields the recycling writes, in this order (f[k] points to M doubles). */
+enum { R_X, R_Y, R_TK, R_PR, R_SXX, R_SXY, R_EXX, R_EXY, R_ETA, R_SR_RATIO, R_GII, R_SP, R_SRP, R_MELT,
+       R_FRIC_INI, R_FRIC, R_NF };
+
+/* s[]: sticky_air, sticky_water, asthenosphere; d[]: xsize, ysize, vyu, vyl, timestep,
+ * temperature_top, temperature_bottom, gridy_b[ynum], delta_fric_coef; mat_plastic (nmat, 6)
+ * column-major.  Returns the number of recycled markers; list/flags (capacity M) get the
+ * 1-based indices and flags in marker order, *n_air the sticky count. */
+int64_t o_recycle_extension(int64_t M, const int8_t* inside, int16_t* matid, double** f, float* pfailure,
+                            const int16_t* s, const double* d, int64_t nmat, const double* mat_plastic,
+                            int64_t iuse_random_fric, uint64_t seed, int64_t step, int64_t* list, int8_t* flags,
+                            int64_t* n_air) {
+  const int16_t air = s[0], water = s[1], asth = s[2];
+  const double xsize = d[0], ysize = d[1], dt = d[4];
+  /* InitializeMarkerRecycling: outside indices in marker order, sticky count by material */
+  int64_t nout = 0, nair = 0, nsub = 0;
+  for (int64_t m = 0; m < M; ++m)
+    if (inside[m] != 1) {
+      list[nout++] = m;
+      if (matid[m] == air || matid[m] == water) ++nair; else ++nsub;
+    }
+  /* Extension.calculate_recycled_locations: band widths |vyu dt| and -|vyl dt| */
+  const double disp_upper = fabs(d[2] * dt), disp_lower = -fabs(d[3] * dt);
+  int64_t ia = 0, is = 0;
+  for (int64_t k = 0; k < nout; ++k) {
+    const int64_t m = list[k];
+    double u0, u1;
+    int flag;
+    if ((matid[m] == air || matid[m] == water) && nair > 0) {
+      o_recycle_uniforms(seed, step, 0u, ia++, &u0, &u1);
+      f[R_X][m] = 0.0 + u0 * xsize;
+      f[R_Y][m] = 0.0 + u1 * disp_upper;
+      flag = 0;
+    } else {
+      o_recycle_uniforms(seed, step, 1u, is++, &u0, &u1);
+      f[R_X][m] = 0.0 + u0 * xsize;
+      f[R_Y][m] = ysize + u1 * disp_lower;
+      flag = 1;
+    }
+    flags[k] = (int8_t)flag;
+    /* ResetMarkers.reset_marker!: sticky -> defaults (zero), subsurface -> asthenosphere */
+    const int16_t id = flag == 0 ? air : asth;
+    matid[m] = id;
+    f[R_TK][m] = flag == 0 ? d[5] : d[6];
+    f[R_PR][m] = flag == 0 ? 0.0 : 3300.0 * 9.81 * d[7];
+    f[R_SXX][m] = f[R_SXY][m] = flag == 0 ? 0.0 : 1.96e6;
+    f[R_EXX][m] = f[R_EXY][m] = flag == 0 ? 0.0 : 1e-14;
+    f[R_SR_RATIO][m] = 0.0;
+    f[R_GII][m] = f[R_SP][m] = f[R_SRP][m] = 0.0;
+    f[R_MELT][m] = 0.0;
+    f[R_ETA][m] = flag == 0 ? 0.0 : 1e20;
+    pfailure[m] = 0.0f;
+    double fric = mat_plastic[2 * nmat + (id - 1)];
+    if (flag == 1 && iuse_random_fric == 1) {
+      double r, unused;
+      o_recycle_uniforms(seed, step, 2u, m, &r, &unused);
+      if (r <= 0.5) fric = fric - d[8];
+    }
+    f[R_FRIC_INI][m] = fric;
+    f[R_FRIC][m] = fric;
+    list[k] = m + 1;
+  }
+  *n_air = nair;
+  return nout;
 }

@@ -93,3 +93,106 @@ def test_timestep_displacement_limit(eb, B, local):
             ly = np.where(vy != 0, displ * cy[:, None] / np.abs(vy), np.inf)
         want = min(dt_old, lx.min(), ly.min())
     assert got == want
+
+
+# Philox-4x32-10 known answers published with the Random123 library (Salmon, Moraes, Dror,
+# Shaw, SC 2011): (counter, key) -> output
+PHILOX_KAT = [
+    ((0, 0, 0, 0), (0, 0), (0x6627E8D5, 0xE169C58D, 0xBC57AC4C, 0x9B00DBD8)),
+    ((0xFFFFFFFF,) * 4, (0xFFFFFFFF,) * 2, (0x408F276D, 0x41C83B0E, 0xA20BC7C6, 0x6D5451FD)),
+    ((0x243F6A88, 0x85A308D3, 0x13198A2E, 0x03707344), (0xA4093822, 0x299F31D0),
+     (0xD16CFE09, 0x94FDCCEB, 0x5001E420, 0x24126EA1)),
+]
+
+
+@pytest.mark.parametrize("ctr,key,want", PHILOX_KAT)
+def test_philox_known_answers(B, ctr, key, want):
+    assert B.philox4x32_10(ctr, key) == want
+
+
+def test_recycle_uniforms_library_matches_oracle(eb, B):
+    """The product's host copy of the generator (eb_recycle_uniforms, a pure host function)
+    gives the oracle's numbers, including 64-bit indices."""
+    import ctypes as C
+    eb.build()
+    from earthbox_gb300 import _abi
+    lib = _abi.load()
+    for seed, step, stream, j in [(0, 0, 0, 0), (12345, 7, 1, 42), (2**63 + 5, 2**31 - 1, 2, 2**33 + 9),
+                                  (99, 3, 0, 10**6)]:
+        u0, u1 = C.c_double(), C.c_double()
+        lib.eb_recycle_uniforms(seed, step, stream, j, C.byref(u0), C.byref(u1))
+        w0, w1 = B.recycle_uniforms(seed, step, stream, j)
+        assert (u0.value, u1.value) == (w0, w1)
+        assert 0.0 <= w0 < 1.0 and 0.0 <= w1 < 1.0
+
+
+def reference_recycle(mk, s, xsize, ysize, vyu, vyl, dt, ttop, tbot, gy_last, mat_plastic, rf, dfric, U):
+    """The reference's loops written out in Python (InitializeMarkerRecycling.jl:26-108,
+    Extension.jl:53-97, Coordinates.jl:60-127, ResetMarkers.jl:24-268) with rand() taken
+    from U(stream, j)."""
+    out = {k: np.array(v, copy=True) for k, v in mk.items()}
+    air, water, asth = s
+    outside = [i for i in range(len(mk["x"])) if mk["inside"][i] != 1]
+    nair = sum(1 for i in outside if mk["matid"][i] in (air, water))
+    nsub = len(outside) - nair
+    newx_air = [0.0 + U(0, j)[0] * xsize for j in range(nair)]
+    newy_air = [0.0 + U(0, j)[1] * abs(vyu * dt) for j in range(nair)]
+    newx_sub = [0.0 + U(1, j)[0] * xsize for j in range(nsub)]
+    newy_sub = [ysize + U(1, j)[1] * -abs(vyl * dt) for j in range(nsub)]
+    ia = isub = 0
+    idx, flags = [], []
+    for i in outside:
+        if mk["matid"][i] in (air, water) and nair > 0:
+            out["x"][i], out["y"][i] = newx_air[ia], newy_air[ia]
+            ia += 1
+            flag = 0
+        else:
+            out["x"][i], out["y"][i] = newx_sub[isub], newy_sub[isub]
+            isub += 1
+            flag = 1
+        idx.append(i + 1)
+        flags.append(flag)
+    for i, flag in zip(idx, flags):
+        i -= 1
+        if flag == 0:
+            mid, T, P, S, E, V = air, ttop, 0.0, 0.0, 0.0, 0.0
+        else:
+            mid, T, P, S, E, V = asth, tbot, 3300.0 * 9.81 * gy_last, 1.96e6, 1e-14, 1e20
+        out["matid"][i] = mid
+        out["tk"][i], out["pr"][i] = T, P
+        out["sxx"][i] = out["sxy"][i] = S
+        out["exx"][i] = out["exy"][i] = E
+        out["sr_ratio"][i] = 0.0
+        out["gii"][i] = out["strain_plastic"][i] = out["strain_rate_plastic"][i] = 0.0
+        out["meltfrac"][i] = 0.0
+        out["eta"][i] = V
+        out["pfailure"][i] = np.float32(0.0)
+        f = mat_plastic[mid - 1, 2]
+        if flag == 1 and rf == 1 and U(2, i)[0] <= 0.5:
+            f = f - dfric
+        out["fric_ini"][i] = out["fric"][i] = f
+    return out, np.array(idx, np.int64), np.array(flags, np.int8), nair
+
+
+@pytest.mark.parametrize("water,rf", [(1, 0), (2, 1)])
+def test_recycle_oracle_matches_reference_loops(eb, B, water, rf):
+    rng = np.random.default_rng(21)
+    M = 1500
+    mk = {k: rng.uniform(-1.0, 1.0, M) for k in B.RECYCLE_FIELDS}
+    mk["matid"] = rng.integers(1, 5, M).astype(np.int16)
+    mk["pfailure"] = rng.uniform(0, 1, M).astype(np.float32)
+    mk["inside"] = np.where(rng.random(M) < 0.9, 1, rng.choice([0, -1], M)).astype(np.int8)
+    mp = np.asfortranarray(rng.uniform(0, 1, (4, 6)))
+    # sticky air, sticky water, asthenosphere; xsize, ysize, vyu, vyl, dt, T_top, T_bottom, gridy_b[ynum]
+    args = (1, water, 4, 500e3, 160e3, -2e-10, 3e-10, 3.15e11, 273.0, 1603.0, 160e3)
+    seed, step = 777, 3
+    got, idx, fl, nair = B.recycle_extension(mk, *args, mp, rf, 0.05, seed, step)
+    want, widx, wfl, wnair = reference_recycle(mk, args[:3], *args[3:11], mp, rf, 0.05,
+                                               lambda st, j: B.recycle_uniforms(seed, step, st, j))
+    assert nair == wnair and np.array_equal(idx, widx) and np.array_equal(fl, wfl)
+    assert len(idx) == int(np.sum(mk["inside"] != 1)) > 0
+    for k in (*B.RECYCLE_FIELDS, "matid", "pfailure"):
+        assert np.array_equal(got[k], want[k]), k
+    y = got["y"][idx - 1]
+    assert np.all(y[fl == 0] >= 0) and np.all(y[fl == 0] < 2e-10 * 3.15e11)
+    assert np.all(y[fl == 1] <= 160e3) and np.all(y[fl == 1] > 160e3 - 3e-10 * 3.15e11)

@@ -74,3 +74,47 @@ def test_timestep_matches_oracle(eb, local):
         want = B.timestep_displacement_limit(model.grid, vx, vy, 0.5, local, dt_old)
         assert got == want and upd == (want != dt_old)
     mic.close()
+
+
+@pytest.mark.parametrize("water,random_fric", [(1, 0), (2, 1)])
+def test_recycle_markers_match_oracle(eb, water, random_fric):
+    """Markers pushed out through all four sides re-enter bit-identically to the oracle:
+    positions, reset properties, the recycled list in marker order and the counts."""
+    from oracle import boundary as B
+    model = eb.synthetic.config("rift_small")
+    g = model.grid
+    mic = eb.MarkerInCell(0)
+    mic.load_model(model)
+    M = model.marknum
+    rng = np.random.default_rng(17)
+    x, y = mic.download_marker("x"), mic.download_marker("y")
+    out = rng.random(M) < 0.04
+    side = rng.integers(0, 4, M)
+    x = np.where(out & (side == 0), g.xmin - rng.uniform(1.0, 5e3, M), x)
+    x = np.where(out & (side == 1), g.xmax + rng.uniform(1.0, 5e3, M), x)
+    y = np.where(out & (side == 2), g.ymin - rng.uniform(1.0, 5e3, M), y)
+    y = np.where(out & (side == 3), g.ymax + rng.uniform(1.0, 5e3, M), y)
+    mic.upload_marker("x", x)
+    mic.upload_marker("y", y)
+    for k in B.RECYCLE_FIELDS[2:]:
+        mic.upload_marker(k, rng.uniform(0.5, 2.0, M))
+    mic.upload_marker("pfailure", rng.uniform(0, 1, M).astype(np.float32))
+    mic.get_marker_inside_flags()
+    mk = {k: mic.download_marker(k) for k in (*B.RECYCLE_FIELDS, "matid", "pfailure", "inside")}
+    assert np.sum(mk["inside"] != 1) > 100 and np.any(mk["matid"][mk["inside"] != 1] == 1)
+    vyu, vyl, tbot, seed, step = -1e-10, 2e-10, 1603.0, 2024, 9
+    p = model.params
+    want, widx, wfl, wnair = B.recycle_extension(mk, 1, water, 4, g.xmax, g.ymax, vyu, vyl, p["timestep"],
+                                                 p["temperature_top"], tbot, g.gridy_b[-1], model.mats.mat_plastic,
+                                                 random_fric, 0.1, seed, step)
+    nair, nsub = mic.recycle_markers(1, water, 4, g.xmax, g.ymax, vyu, vyl, tbot, seed, step,
+                                     iuse_random_fric=random_fric, delta_fric_coef=0.1)
+    assert (nair, nsub) == (wnair, len(widx) - wnair)
+    idx, fl = mic.recycled_markers()
+    assert np.array_equal(idx, widx) and np.array_equal(fl, wfl)
+    for k in (*B.RECYCLE_FIELDS, "matid", "pfailure"):
+        assert np.array_equal(mic.download_marker(k), want[k]), k
+    # every marker is back inside
+    mic.get_marker_inside_flags()
+    assert np.all(mic.download_marker("inside") == 1)
+    mic.close()
