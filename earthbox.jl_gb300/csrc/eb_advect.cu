@@ -128,23 +128,39 @@ struct TailGrids {
   const float *dsxy, *dsxx, *dtk1;  // FP32 mirrors
   double healing;
 };
+// Every marker field the pass reads is loaded before its first store: the stores could
+// alias the loads, so a load written after a store would wait for it and each marker
+// would pay several DRAM round trips in sequence.  Loading first puts all of them in
+// flight at once, and the plastic fields (10 % of markers or so) follow as soon as
+// pfailure arrives, overlapping the RK4 gathers.  Five blocks per SM (48 registers, a few
+// spilled) ran faster than four without spills (1.98 against 2.06 ms at 40M markers).
 template <bool kMove>
-__global__ void k_tail(DevMarkers mk, DevGrid g, VelGrids V, TailGrids T) {
+__global__ void __launch_bounds__(kBlock, 5) k_tail(DevMarkers mk, DevGrid g, VelGrids V, TailGrids T) {
   const int64_t m = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (m >= mk.M) return;
-  if (!(mk.mflags[m] & MF_INSIDE)) {
+  const uint8_t flags = __ldg(&mk.mflags[m]);
+  const int32_t ix0 = __ldg(&mk.xn[m]), iy0 = __ldg(&mk.yn[m]);
+  const float fx = __ldg(&mk.fx[m]), fy = __ldg(&mk.fy[m]);
+  double sxy = mk.sxy[m], sxx = mk.sxx[m];
+  const double tk = mk.tk[m], gii = mk.gii[m];
+  const double exx = __ldg(&mk.exx[m]), exy = __ldg(&mk.exy[m]);
+  const float pf = __ldg(&mk.pfailure[m]);
+  double x = 0.0, y = 0.0;
+  if (kMove) { x = mk.x[m]; y = mk.y[m]; }
+  if (!(flags & MF_INSIDE)) {
     if (kMove) { mk.vx[m] = 0.0; mk.vy[m] = 0.0; mk.spin[m] = 0.0; }
     return;
   }
-  const int32_t ix0 = mk.xn[m], iy0 = mk.yn[m];
-  const float fx = mk.fx[m], fy = mk.fy[m];
+  const bool plastic = pf == 1.0f;
+  double eta = 1.0, eta_flow = 1.0, sp0 = 0.0;
+  if (plastic) { eta = __ldg(&mk.eta[m]); eta_flow = __ldg(&mk.eta_flow[m]); sp0 = mk.sp[m]; }
   const float lx0 = fx * __ldg(&g.sxf[ix0 - 1]);
   const float ly0 = fy * __ldg(&g.syf[iy0 - 1]);
   // stress correction
-  double sxy = mk.sxy[m] + f2d(gather4f(T.dsxy, g.ynum, iy0, ix0, fx, fy));
-  double sxx = mk.sxx[m] + f2d(gather_p(T.dsxx, g, ix0, iy0, lx0, ly0));
+  sxy = sxy + f2d(gather4f(T.dsxy, g.ynum, iy0, ix0, fx, fy));
+  sxx = sxx + f2d(gather_p(T.dsxx, g, ix0, iy0, lx0, ly0));
   // remaining temperature change
-  mk.tk[m] = mk.tk[m] + f2d(gather4f(T.dtk1, g.ynum, iy0, ix0, fx, fy));
+  mk.tk[m] = tk + f2d(gather4f(T.dtk1, g.ynum, iy0, ix0, fx, fy));
   if (kMove) {
     const float h = V.dt;
     float v1x, v1y, s1;
@@ -170,8 +186,8 @@ __global__ void k_tail(DevMarkers mk, DevGrid g, VelGrids V, TailGrids T) {
     mk.vx[m] = vxd;
     mk.vy[m] = vyd;
     mk.spin[m] = f2d(spm);
-    mk.x[m] = fma(V.dtd, vxd, mk.x[m]);
-    mk.y[m] = fma(V.dtd, vyd, mk.y[m]);
+    mk.x[m] = fma(V.dtd, vxd, x);
+    mk.y[m] = fma(V.dtd, vyd, y);
     const float w = spm * V.dt;
     const float s2w = sinf(2.f * w), sw = sinf(w);
     const float c2m1 = -2.f * sw * sw;
@@ -184,15 +200,14 @@ __global__ void k_tail(DevMarkers mk, DevGrid g, VelGrids V, TailGrids T) {
   mk.sxx[m] = sxx;
   mk.sxy[m] = sxy;
   // strain update (inside markers only, as k_strain)
-  const float eii = hypotf(d2f(mk.exx[m]), d2f(mk.exy[m]));
-  mk.gii[m] = fma(V.dtd, f2d(eii), mk.gii[m]);
-  if (mk.pfailure[m] != 1.0f) return;
-  const double eta = mk.eta[m], eta_flow = mk.eta_flow[m];
+  const float eii = hypotf(d2f(exx), d2f(exy));
+  mk.gii[m] = fma(V.dtd, f2d(eii), gii);
+  if (!plastic) return;
   const float sii = hypotf(d2f(sxx), d2f(sxy));
   const float d = d2f(eta_flow - eta);
   float rate = 0.5f * sii * ((d / d2f(eta)) / d2f(eta_flow));
   rate = fmaxf(0.f, rate);
-  double sp = mk.sp[m] + V.dtd * f2d(rate) - T.healing * V.dtd;
+  double sp = sp0 + V.dtd * f2d(rate) - T.healing * V.dtd;
   mk.sp[m] = sp > 0.0 ? sp : 0.0;
   mk.srp[m] = f2d(rate);
 }

@@ -26,11 +26,17 @@ struct PostStokesGrids {
   float dt;
 };
 
+// The marker loads (flags, cell, offsets, material, viscosity) are all issued before the
+// first store, which could alias them: one DRAM round trip per marker instead of three.
 __global__ void k_post_stokes(DevMarkers mk, DevGrid g, PostStokesGrids G) {
   const int64_t m = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (m >= mk.M || !(mk.mflags[m] & MF_INSIDE)) return;
-  const int32_t ix = mk.xn[m], iy = mk.yn[m];
-  const float fx = mk.fx[m], fy = mk.fy[m];
+  if (m >= mk.M) return;
+  const uint8_t flags = __ldg(&mk.mflags[m]);
+  const int32_t ix = __ldg(&mk.xn[m]), iy = __ldg(&mk.yn[m]);
+  const float fx = __ldg(&mk.fx[m]), fy = __ldg(&mk.fy[m]);
+  const int16_t matid = __ldg(&mk.matid[m]);
+  const double eta64 = __ldg(&mk.eta[m]);
+  if (!(flags & MF_INSIDE)) return;
   const float lx = fx * __ldg(&g.sxf[ix - 1]), ly = fy * __ldg(&g.syf[iy - 1]);
   // MarkerStrainRate.calculate_marker_strain_rate!
   const float exx = gather_p(G.exx, g, ix, iy, lx, ly);
@@ -42,8 +48,8 @@ __global__ void k_post_stokes(DevMarkers mk, DevGrid g, PostStokesGrids G) {
   const float sxy2 = gather4f(G.sxy2, g.ynum, iy, ix, fx, fy);
   const float dsxx = gather_p(G.dsxx, g, ix, iy, lx, ly);
   const float dsxy = gather4f(G.dsxy, g.ynum, iy, ix, fx, fy);
-  const float mu = d2f(__ldg(&G.mat_mu[mk.matid[m] - 1]));
-  const float eta = d2f(mk.eta[m]);
+  const float mu = d2f(__ldg(&G.mat_mu[matid - 1]));
+  const float eta = d2f(eta64);
   const float eii = hypotf(exx, exy);
   float r = 1.f;
   if (eii > 0.f) {
