@@ -222,7 +222,7 @@ ALL_SYMBOLS = [
     "eb_marker_to_basic_grid_average_noalloc", "eb_marker_cycle_host", "eb_set_rock_tables",
     "eb_set_sediment_porosity", "eb_update_marker_rock_properties",
     "eb_update_model_time_step_using_displacement_limit", "eb_checkpoint_write", "eb_checkpoint_read",
-    "eb_recycle_markers", "eb_recycled_markers", "eb_recycle_uniforms",
+    "eb_recycle_markers", "eb_recycled_markers", "eb_recycle_uniforms", "eb_nn_gemm_bf16", "eb_nn_conv2d_bf16",
 ] + ENTRY_POINTS + STOKES_ENTRY_POINTS + HEAT_ENTRY_POINTS
 
 _lib = None
@@ -286,6 +286,8 @@ def load(path: pathlib.Path | str | None = None) -> C.CDLL:
     lib.eb_recycle_uniforms.argtypes = [C.c_uint64, C.c_int64, C.c_uint32, C.c_int64, C.POINTER(C.c_double),
                                         C.POINTER(C.c_double)]
     lib.eb_recycle_uniforms.restype = None
+    lib.eb_nn_gemm_bf16.argtypes = [C.c_int64, C.c_int32, C.c_int64, vp, vp, vp, C.c_int32]
+    lib.eb_nn_conv2d_bf16.argtypes = [C.c_int32] * 7 + [vp, vp, vp, C.c_int32, vp, vp]
     lib.eb_checkpoint_write.argtypes = [vp, C.c_char_p]
     lib.eb_checkpoint_read.argtypes = [vp, C.c_char_p]
     lib.eb_set_rock_tables.argtypes = [vp, C.POINTER(RockDesc)]

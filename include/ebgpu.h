@@ -564,6 +564,19 @@ int eb_recycled_markers(eb_ctx* ctx, int64_t* indices, int8_t* flags, int64_t ca
 /* The two uniforms of Philox-4x32-10 at (seed; j, stream, counter), as the recycling uses them. */
 void eb_recycle_uniforms(uint64_t seed, int64_t counter, uint32_t stream, int64_t j, double* u0, double* u1);
 
+/* ---- tensor-core building blocks of the learned preconditioner ----------------
+ * Host-array entry points (temporary device buffers) for one BF16 GEMM / convolution on the
+ * tcgen05 tensor cores with FP32 accumulation; BF16 values are passed as their uint16 bits.
+ * eb_nn_gemm_bf16: D[M x N] (FP32, row-major) = A[M x K] . B[N x K]^T, K a multiple of 8;
+ *   splits > 1 splits K across CTAs (partials summed on the host in split order).
+ * eb_nn_conv2d_bf16: y[B,H,W,Cout] = conv(x[B,H,W,C], w[Cout][taps*C]) with zero padding,
+ *   taps 9 (3x3, tap = 3(dy+1)+(dx+1)) or 1; flip 1 reads offset -d (input gradient);
+ *   mode 0: FP32 output y32; 1: BF16 y16 = relu(acc + bias); 2: BF16 y16 = acc + bias. */
+int eb_nn_gemm_bf16(int64_t M, int32_t N, int64_t K, const uint16_t* A, const uint16_t* B, float* D, int32_t splits);
+int eb_nn_conv2d_bf16(int32_t B, int32_t H, int32_t W, int32_t C, int32_t Cout, int32_t taps, int32_t flip,
+                      const uint16_t* x, const uint16_t* w, const float* bias, int32_t mode, float* y32,
+                      uint16_t* y16);
+
 /* ---- checkpoints -----------------------------------------------------------
  * No counterpart in the reference, whose backups (model_manager/backup/core/MakeBackup.jl:22)
  * and XDMF output (model_manager/xdmf/markers/core/TimeStep.jl) write the host arrays: those
