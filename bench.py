@@ -84,6 +84,8 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-stokes", action="store_true")
     ap.add_argument("--no-heat", action="store_true")
+    ap.add_argument("--no-learned", action="store_true")
+    ap.add_argument("--learned-steps", type=int, default=200)
     ap.add_argument("--circles", action="store_true",
                     help="also time the circles_1025 Stokes benchmark (200 inclusions, 1e-10)")
     ap.add_argument("--stokes-method", default="fgmres", choices=["fgmres", "bicgstab"])
@@ -103,6 +105,14 @@ def peaks():
         d = json.loads(p.read_text())
         return float(d["hbm_gbs"]), "measured"
     return 6800.0, "fallback"
+
+
+def peaks_bf16() -> float:
+    """Measured dense BF16 tensor throughput (TFLOP/s, burst), else the fallback figure."""
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        return float(json.loads(p.read_text()).get("bf16_tflops", 1900.0))
+    return 1900.0
 
 
 class Clocks:
@@ -183,7 +193,16 @@ STOKES_GRIDS = ("etas1", "etan1", "mus1", "mun1", "sxy1", "sxx1", "rho1", "rho1_
                 "brighty")
 
 
-def stokes_gpu(mic, reps: int = 2, method: str = "fgmres", rtol: float = 1e-8):
+def unet_flops_per_pixel() -> float:
+    """Forward FLOPs of the learned stage's U-Net per full-resolution pixel (2 per multiply-add
+    of each convolution, pixels of level l = 1 / 4^l of the full resolution)."""
+    layers = [(8, 32, 9, 0), (32, 32, 9, 0), (32, 64, 9, 1), (64, 64, 9, 1), (64, 128, 9, 2), (128, 128, 9, 2),
+              (128, 128, 9, 3), (128, 128, 9, 3), (256, 128, 9, 2), (128, 128, 9, 2), (192, 64, 9, 1),
+              (64, 64, 9, 1), (96, 32, 9, 0), (32, 32, 9, 0), (32, 16, 1, 0)]
+    return sum(2.0 * t * ci * co / 4 ** lv for ci, co, t, lv in layers)
+
+
+def stokes_gpu(mic, reps: int = 2, method: str = "fgmres", rtol: float = 1e-8, learned: bool = False):
     """The Stokes step on the grids the context holds: build steps, solve to 1e-8, unpack.
     One warm-up (level set-up, graph capture), then `reps` timed steps (wall clock: the
     FGMRES loop is host-driven)."""
@@ -193,7 +212,7 @@ def stokes_gpu(mic, reps: int = 2, method: str = "fgmres", rtol: float = 1e-8):
         mic.calc_viscoelastic_terms()
         mic.viscoelastic_rhs()
         mic.build_system_of_equations()
-        rep = mic.solve_system(rtol=rtol, check=False, method=method)
+        rep = mic.solve_system(rtol=rtol, check=False, method=method, learned=learned)
         mic.process_stokes_solution()
         return rep
 
@@ -490,6 +509,45 @@ def main():
             except Exception as exc:
                 stokes["cpu_baseline"] = {"value": None, "sample": f"failed: {exc}"}
 
+    # learned + MG against plain MG on the same system: the U-Net stage trained on the GPU on
+    # patches of this system (its own forward, backward and Adam kernels), then the solve with
+    # the stage after every V-cycle
+    learned = None
+    if stokes is not None and not args.no_learned:
+        try:
+            mic.learned_init(17)
+            patch, batch = 512, 4
+            tr = mic.learned_train(steps=args.learned_steps, batch=batch, patch=patch, patches_per_sample=4,
+                                   lr=1e-3, seed=23)
+            px = batch * tr["patch_h"] * tr["patch_w"]
+            train_flops = 3.0 * unet_flops_per_pixel() * px * args.learned_steps
+            mic.learned_stats()
+            l_dt, l_rep, l_prof = stokes_gpu(mic, reps=2, method="fgmres", learned=True)
+            st = mic.learned_stats()
+            calls = st["accepted"] + st["rejected"]
+            nc_cells = (model.grid.xnum - 1) * (model.grid.ynum - 1)
+            infer_px = ((model.grid.xnum - 1 + 7) // 8 * 8) * ((model.grid.ynum - 1 + 7) // 8 * 8)
+            l_kern = {k: (t / n, n) for k, (t, n) in l_prof.items()}
+            gemm_ms = sum(v[0] * v[1] for k, v in l_kern.items() if k.startswith("k_gemm_bf16")) / 2
+            infer_flops = unet_flops_per_pixel() * infer_px * calls / 3  # 3 solves counted (warm-up + 2)
+            learned = {"metric": "Stokes s/solve @1e-8 resid, learned+MG", "value": l_dt, "unit": "s/solve",
+                       "plain_mg_value": stokes["value"], "higher_is_better": False,
+                       "iterations": l_rep["iterations"], "plain_mg_iterations": stokes["iterations"],
+                       "rel_residual": l_rep["rel_residual"], "status": l_rep["status"],
+                       "stage": {"kept": st["accepted"], "rejected": st["rejected"],
+                                 "mean_removed_fraction": st["mean_removed"], "seconds_total": st["seconds"]},
+                       "training": {**tr, "tflops": train_flops / tr["seconds"] / 1e12,
+                                    "flops_per_step": train_flops / args.learned_steps},
+                       "network": "BF16 U-Net 32-64-128-128, 1.1M parameters, FP32 accumulation (tcgen05)",
+                       "inference": {"pixels": infer_px, "cells": nc_cells,
+                                     "gemm_ms_per_solve": gemm_ms,
+                                     "tensor_tflops": (infer_flops / (gemm_ms * 1e-3) / 1e12) if gemm_ms > 0 else None,
+                                     "peak_bf16_tflops": peaks_bf16()},
+                       "kernels_ms": {k: round(v[0] * v[1], 3) for k, v in
+                                      sorted(l_kern.items(), key=lambda kv: -kv[1][0] * kv[1][1])[:10]}}
+        except Exception as exc:
+            learned = {"value": None, "error": str(exc)}
+
     # the circles solver benchmark: 1025 x 1025 nodes, 200 inclusions (1e18-1e27 Pa s), to 1e-10
     stokes_circles = None
     if not args.no_stokes and args.circles:
@@ -583,7 +641,8 @@ def main():
                            "markers_per_cell": 25 if args.workload == "rift_40M" else None,
                            "l2": "inputs larger than L2 (each marker field 320 MB)", "parallelism": "replicas"},
                 "gpu_launches": launches, "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
-                "clocks": clk.summary(), "stokes": stokes, "stokes_circles": stokes_circles, "heat": heat,
+                "clocks": clk.summary(), "stokes": stokes, "stokes_learned": learned, "stokes_circles": stokes_circles,
+                "heat": heat,
                 "timestep": timestep,
                 "kernels_ms": {k: round(v[0], 4) for k, v in sorted(kern.items(), key=lambda kv: -kv[1][0] * kv[1][1])},
                 "generate_s": round(t_gen, 2)}

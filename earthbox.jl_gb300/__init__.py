@@ -289,11 +289,12 @@ class MarkerInCell:
         self._call("eb_build_stokes_system")
 
     def solve_system(self, rtol: float = 1e-8, max_iters: int = 0, restart: int = 0, mg_sweeps: int = 0,
-                     use_initial_guess: bool = False, method: str = "fgmres", check: bool = True) -> dict:
+                     use_initial_guess: bool = False, method: str = "fgmres", check: bool = True,
+                     learned: bool = False) -> dict:
         """The Stokes solve (replaces SystemSolver.solve_system_optimized, SystemSolver.jl:67-91);
-        method "fgmres" or "bicgstab"."""
+        method "fgmres" or "bicgstab"; learned: add the trained network's stage after each V-cycle."""
         o = _abi.SolveOpts(rtol, max_iters, restart, mg_sweeps, int(use_initial_guess),
-                           {"fgmres": 0, "bicgstab": 1}[method])
+                           {"fgmres": 0, "bicgstab": 1}[method], int(learned))
         r = _abi.SolveReport()
         rc = self._lib.eb_solve_stokes_system(self._ctx, C.byref(o), C.byref(r))
         rep = {"status": rc, "iterations": r.iterations, "levels": r.levels, "rel_residual": r.rel_residual,
@@ -469,6 +470,66 @@ class MarkerInCell:
                 break
         return history
 
+    # ------------------------------------------- learned preconditioner stage --
+    def learned_init(self, seed: int = 0) -> None:
+        """He-normal initial weights of the U-Net stage."""
+        self._check(self._lib.eb_learned_init(self._ctx, seed))
+
+    def learned_train(self, steps: int, batch: int = 4, patch: int = 512, patches_per_sample: int = 4,
+                      lr: float = 1e-3, seed: int = 0, mg_sweeps: int = 0) -> dict:
+        """Train the stage on the GPU on correction pairs of the current assembled system."""
+        o = _abi.LearnedOpts(batch, patch, steps, patches_per_sample, mg_sweeps, lr, seed)
+        r = _abi.LearnedReport()
+        self._check(self._lib.eb_learned_train(self._ctx, C.byref(o), C.byref(r)))
+        return {k: getattr(r, k) for k, _ in _abi.LearnedReport._fields_}
+
+    def learned_params(self, params: np.ndarray | None = None) -> np.ndarray:
+        """FP32 parameters (per layer [cout][taps][cin] weights, then [cout] biases); with an
+        array, upload it instead."""
+        n = C.c_int64()
+        self._check(self._lib.eb_learned_params(self._ctx, None, 0, C.byref(n), 0))
+        if params is not None:
+            p = np.ascontiguousarray(params, dtype=np.float32)
+            assert p.size == n.value
+            self._check(self._lib.eb_learned_params(self._ctx, _ptr(p), p.size, C.byref(n), 1))
+            return p
+        out = np.zeros(n.value, np.float32)
+        self._check(self._lib.eb_learned_params(self._ctx, _ptr(out), out.size, C.byref(n), 0))
+        return out
+
+    def learned_state(self, state: np.ndarray | None = None) -> np.ndarray:
+        """(eta mean, eta 1/std, rho mean, rho 1/std, kappa, trained) of the stage."""
+        st = np.zeros(6) if state is None else np.ascontiguousarray(state, dtype=np.float64)
+        self._check(self._lib.eb_learned_state(self._ctx, _ptr(st), 0 if state is None else 1))
+        return st
+
+    def learned_forward(self, x: np.ndarray) -> np.ndarray:
+        """The network on x [B][H][W][8] (FP32, rounded to BF16) -> [B][H][W][16] FP32."""
+        x = np.ascontiguousarray(x, dtype=np.float32)
+        B, H, W, _ = x.shape
+        y = np.zeros((B, H, W, 16), np.float32)
+        self._check(self._lib.eb_learned_forward(self._ctx, B, H, W, _ptr(x), _ptr(y)))
+        return y
+
+    def learned_loss_grad(self, x: np.ndarray, t: np.ndarray) -> tuple:
+        """(MSE loss against t [B][H][W][3], gradient of every parameter)."""
+        x = np.ascontiguousarray(x, dtype=np.float32)
+        t = np.ascontiguousarray(t, dtype=np.float32)
+        B, H, W, _ = x.shape
+        n = C.c_int64()
+        self._check(self._lib.eb_learned_params(self._ctx, None, 0, C.byref(n), 0))
+        g = np.zeros(n.value, np.float32)
+        loss = C.c_double()
+        self._check(self._lib.eb_learned_loss_grad(self._ctx, B, H, W, _ptr(x), _ptr(t), C.byref(loss), _ptr(g)))
+        return loss.value, g
+
+    def learned_stats(self) -> dict:
+        """Stage applications since the last call: kept, rejected, seconds and the mean fraction of
+        the squared preconditioner residual removed."""
+        a, r, s, m = C.c_int64(), C.c_int64(), C.c_double(), C.c_double()
+        self._check(self._lib.eb_learned_stats(self._ctx, C.byref(a), C.byref(r), C.byref(s), C.byref(m)))
+        return {"accepted": a.value, "rejected": r.value, "seconds": s.value, "mean_removed": m.value}
+
     # ----------------------------------------------------- marker recycling --
     def recycle_markers(self, matid_sticky_air: int, matid_sticky_water: int, matid_asthenosphere: int,
                         xsize: float, ysize: float, velocity_y_upper: float, velocity_y_lower: float,
@@ -571,7 +632,7 @@ class MarkerInCell:
                           use_initial_guess: bool = True, check: bool = True) -> dict:
         """The solve of SystemSolver.discretize_and_solve_conductive_heat_equation
         (heat_solver/solver/SystemSolver.jl:32-66) and reload_solu_temp: tk2."""
-        o = _abi.SolveOpts(rtol, max_iters, 0, mg_sweeps, int(use_initial_guess), 0)
+        o = _abi.SolveOpts(rtol, max_iters, 0, mg_sweeps, int(use_initial_guess), 0, 0)
         r = _abi.SolveReport()
         rc = self._lib.eb_solve_heat_system(self._ctx, C.byref(o), C.byref(r))
         if check:
@@ -587,7 +648,7 @@ class MarkerInCell:
                                         mg_sweeps: int = 0) -> dict:
         """HeatLoop.run_conductive_heat_solver_loop! (heat_loop/HeatLoop.jl:10-79)."""
         hp = self._heat(params)
-        o = _abi.SolveOpts(rtol, max_iters, 0, mg_sweeps, 1, 0)
+        o = _abi.SolveOpts(rtol, max_iters, 0, mg_sweeps, 1, 0, 0)
         r = _abi.HeatLoopReport()
         self._check(self._lib.eb_run_conductive_heat_solver_loop(self._ctx, C.byref(hp), C.byref(o), C.byref(r)))
         return {k: getattr(r, k) for k, _ in _abi.HeatLoopReport._fields_}

@@ -124,7 +124,17 @@ class StokesParams(C.Structure):
 
 class SolveOpts(C.Structure):
     _fields_ = [("rtol", C.c_double), ("max_iters", C.c_int32), ("restart", C.c_int32), ("mg_sweeps", C.c_int32),
-                ("use_initial_guess", C.c_int32), ("method", C.c_int32)]
+                ("use_initial_guess", C.c_int32), ("method", C.c_int32), ("learned", C.c_int32)]
+
+
+class LearnedOpts(C.Structure):
+    _fields_ = [("batch", C.c_int32), ("patch", C.c_int32), ("steps", C.c_int32), ("patches_per_sample", C.c_int32),
+                ("mg_sweeps", C.c_int32), ("lr", C.c_double), ("seed", C.c_uint64)]
+
+
+class LearnedReport(C.Structure):
+    _fields_ = [("steps", C.c_int32), ("patch_h", C.c_int32), ("patch_w", C.c_int32), ("loss_first", C.c_double),
+                ("loss_last", C.c_double), ("kappa", C.c_double), ("seconds", C.c_double)]
 
 
 class StokesNorms(C.Structure):
@@ -223,6 +233,8 @@ ALL_SYMBOLS = [
     "eb_set_sediment_porosity", "eb_update_marker_rock_properties",
     "eb_update_model_time_step_using_displacement_limit", "eb_checkpoint_write", "eb_checkpoint_read",
     "eb_recycle_markers", "eb_recycled_markers", "eb_recycle_uniforms", "eb_nn_gemm_bf16", "eb_nn_conv2d_bf16",
+    "eb_learned_init", "eb_learned_train", "eb_learned_params", "eb_learned_state", "eb_learned_forward",
+    "eb_learned_loss_grad", "eb_learned_stats",
 ] + ENTRY_POINTS + STOKES_ENTRY_POINTS + HEAT_ENTRY_POINTS
 
 _lib = None
@@ -288,6 +300,14 @@ def load(path: pathlib.Path | str | None = None) -> C.CDLL:
     lib.eb_recycle_uniforms.restype = None
     lib.eb_nn_gemm_bf16.argtypes = [C.c_int64, C.c_int32, C.c_int64, vp, vp, vp, C.c_int32]
     lib.eb_nn_conv2d_bf16.argtypes = [C.c_int32] * 7 + [vp, vp, vp, C.c_int32, vp, vp]
+    lib.eb_learned_init.argtypes = [vp, C.c_uint64]
+    lib.eb_learned_train.argtypes = [vp, C.POINTER(LearnedOpts), C.POINTER(LearnedReport)]
+    lib.eb_learned_params.argtypes = [vp, vp, C.c_int64, C.POINTER(C.c_int64), C.c_int32]
+    lib.eb_learned_state.argtypes = [vp, vp, C.c_int32]
+    lib.eb_learned_forward.argtypes = [vp, C.c_int32, C.c_int32, C.c_int32, vp, vp]
+    lib.eb_learned_loss_grad.argtypes = [vp, C.c_int32, C.c_int32, C.c_int32, vp, vp, C.POINTER(C.c_double), vp]
+    lib.eb_learned_stats.argtypes = [vp, C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.POINTER(C.c_double),
+                                     C.POINTER(C.c_double)]
     lib.eb_checkpoint_write.argtypes = [vp, C.c_char_p]
     lib.eb_checkpoint_read.argtypes = [vp, C.c_char_p]
     lib.eb_set_rock_tables.argtypes = [vp, C.POINTER(RockDesc)]

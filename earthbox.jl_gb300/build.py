@@ -18,7 +18,7 @@ BUILD = PKG / "_build"
 LIB = BUILD / "libebgpu.so"
 SOURCES = ["eb_ctx.cu", "eb_locate.cu", "eb_scatter.cu", "eb_gather.cu", "eb_advect.cu", "eb_rheology.cu",
            "eb_noalloc.cu", "eb_stokes_build.cu", "eb_stokes_solve.cu", "eb_heat.cu",
-           "eb_pipeline.cu", "eb_step_boundary.cu", "eb_recycle.cu", "eb_nn.cu"]
+           "eb_pipeline.cu", "eb_step_boundary.cu", "eb_recycle.cu", "eb_nn.cu", "eb_nn_net.cu"]
 # The Stokes assembly reproduces the reference's FP64 coefficients operation by
 # operation, so no multiply-add contraction there.
 EXTRA_FLAGS = {"eb_stokes_build.cu": ["-fmad=false"], "eb_heat.cu": ["-fmad=false"],

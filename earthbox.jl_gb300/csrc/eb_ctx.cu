@@ -294,6 +294,7 @@ extern "C" int eb_destroy(eb_ctx* c) {
   free_markers(c);
   stokes_free(c);
   heat_free(c);
+  nn_free(c);
   for (void* p : c->mat_allocs) cudaFree(p);
   for (void* p : c->rock_allocs) cudaFree(p);
   for (void* p : c->sed_allocs) cudaFree(p);

@@ -83,6 +83,7 @@ struct Profiler {
 
 struct StokesState;  // eb_stokes_solve.cu
 struct HeatState;    // eb_heat.cu
+namespace nn { struct Net; }  // eb_nn_net.cu: the learned preconditioner
 
 struct eb_ctx {
   int device = 0;
@@ -125,6 +126,7 @@ struct eb_ctx {
   StokesState* st = nullptr;
   // conductive heat step
   HeatState* ht = nullptr;
+  nn::Net* net = nullptr;
   // rock-property tables and sediment porosity inputs (eb_step_boundary.cu)
   std::vector<void*> rock_allocs;
   int64_t rock_nmat = 0;
@@ -175,6 +177,13 @@ int export_stokes_coo(eb_ctx* c, const StokesSystem* s, int64_t* Li, int64_t* Lj
                       int64_t* nnz);
 
 void heat_free(eb_ctx* c);  // eb_heat.cu
+// learned preconditioner (eb_nn_net.cu)
+void nn_free(eb_ctx* c);
+bool nn_trained(const eb_ctx* c);
+int nn_correction(eb_ctx* c, const double* t, double s, double* z_add);  // z_add = s kappa NN(t / s)
+// one learned-stage application: kept or not, its time, and the fraction of the squared
+// preconditioner residual it removed
+void nn_count(eb_ctx* c, bool accepted, double seconds, double removed);
 int launch_matid_range(eb_ctx* c, cudaStream_t s);  // eb_ctx.cu: marker_matid range check
 int finish_matid_range(eb_ctx* c);
 

@@ -121,6 +121,20 @@ __host__ __device__ constexpr size_t gemm_smem_bytes(int bn) {
 }
 
 // ---- operand loaders ----------------------------------------------------------------
+// A thread stages the same 16-byte chunk column (tid mod 8) of fixed tile rows in every
+// K-chunk, so each loader splits the address into a per-row part (computed once per CTA)
+// and a per-column part (once per K-chunk).
+struct RowAt {
+  int64_t pix;  // row index (matrix) or pixel index (convolution)
+  int32_t y, x;
+  bool ok;
+};
+struct ColAt {
+  int64_t k;    // column (matrix) or channel (convolution)
+  int32_t off;  // pixel offset of the tap (convolution)
+  int32_t dy, dx;
+  bool ok;
+};
 // Plain K-major matrix: row r at base + r * ld (elements), rows >= rows_valid and
 // columns >= k_valid read as zero.
 struct MatLoader {
@@ -128,9 +142,11 @@ struct MatLoader {
   int64_t ld;
   int64_t rows_valid;
   int64_t k_valid;
-  __device__ __forceinline__ const void* chunk(int64_t r, int64_t k, bool& ok) const {
-    ok = r < rows_valid && k < k_valid;
-    return ok ? (const void*)(base + r * ld + k) : (const void*)base;
+  __device__ __forceinline__ RowAt row(int64_t r) const { return RowAt{r, 0, 0, r < rows_valid}; }
+  __device__ __forceinline__ ColAt col(int64_t k) const { return ColAt{k, 0, 0, 0, k < k_valid}; }
+  __device__ __forceinline__ const void* at(const RowAt& R, const ColAt& K, bool& ok) const {
+    ok = R.ok && K.ok;
+    return ok ? (const void*)(base + R.pix * ld + K.k) : (const void*)base;
   }
 };
 // Implicit 3x3 (or 1x1) convolution, NHWC input [B][H][W][C] with C a multiple of 8:
@@ -140,20 +156,22 @@ struct ConvLoader {
   const uint16_t* x;
   int32_t B, H, W, C, taps;  // taps 9 or 1
   int32_t flip;
-  __device__ __forceinline__ const void* chunk(int64_t r, int64_t k, bool& ok) const {
+  __device__ __forceinline__ RowAt row(int64_t r) const {
     const int64_t P = (int64_t)B * H * W;
-    const int64_t kv = (int64_t)taps * C;
-    ok = false;
-    if (r >= P || k >= kv) return (const void*)x;
+    if (r >= P) return RowAt{0, 0, 0, false};
+    const int32_t rem = (int32_t)(r % ((int64_t)H * W));
+    return RowAt{r, rem / W, rem % W, true};
+  }
+  __device__ __forceinline__ ColAt col(int64_t k) const {
+    if (k >= (int64_t)taps * C) return ColAt{0, 0, 0, 0, false};
     const int32_t tap = (int32_t)(k / C), c = (int32_t)(k - (int64_t)tap * C);
     int32_t dy = 0, dx = 0;
     if (taps == 9) { dy = tap / 3 - 1; dx = tap % 3 - 1; if (flip) { dy = -dy; dx = -dx; } }
-    const int32_t b = (int32_t)(r / ((int64_t)H * W));
-    const int32_t rem = (int32_t)(r - (int64_t)b * H * W);
-    const int32_t y = rem / W + dy, xx = rem % W + dx;
-    if (y < 0 || y >= H || xx < 0 || xx >= W) return (const void*)x;
-    ok = true;
-    return (const void*)(x + (((int64_t)b * H + y) * W + xx) * C + c);
+    return ColAt{c, dy * W + dx, dy, dx, true};
+  }
+  __device__ __forceinline__ const void* at(const RowAt& R, const ColAt& K, bool& ok) const {
+    ok = R.ok && K.ok && R.y + K.dy >= 0 && R.y + K.dy < H && R.x + K.dx >= 0 && R.x + K.dx < W;
+    return ok ? (const void*)(x + (R.pix + K.off) * C + K.k) : (const void*)x;
   }
 };
 
@@ -211,20 +229,25 @@ __global__ void __launch_bounds__(kGemmThreads) k_gemm_bf16(ALoad A, MatLoader B
   tc_fence_after();
   const uint32_t tmem = *tslot_ptr;
 
+  // this thread's chunk column and rows: tile rows tid/8 + 16 i
+  const int cc = tid & 7, r0 = tid >> 3;
+  RowAt arow[kTileM / 16];
+#pragma unroll
+  for (int i = 0; i < kTileM / 16; ++i) arow[i] = A.row(m0 + r0 + 16 * i);
   auto load_stage = [&](int32_t j, int buf) {
-    const int64_t k0 = (kc0 + j) * kChunkK;
+    const int64_t k = (kc0 + j) * kChunkK + 8 * cc;
     const uint32_t sa = base + (uint32_t)buf * stage_bytes, sb = sa + a_bytes;
-    for (int q = tid; q < kTileM * 8; q += kGemmThreads) {
-      const int r = q >> 3, c = q & 7;
+    const ColAt ka = A.col(k), kb = Bm.col(k);
+#pragma unroll
+    for (int i = 0; i < kTileM / 16; ++i) {
       bool ok;
-      const void* src = A.chunk(m0 + r, k0 + 8 * c, ok);
-      cp_async16(sa + sw128_offset(r, c), src, ok);
+      const void* src = A.at(arow[i], ka, ok);
+      cp_async16(sa + sw128_offset(r0 + 16 * i, cc), src, ok);
     }
-    for (int q = tid; q < BN * 8; q += kGemmThreads) {
-      const int r = q >> 3, c = q & 7;
+    for (int r = r0; r < BN; r += 16) {
       bool ok;
-      const void* src = Bm.chunk(n0 + r, k0 + 8 * c, ok);
-      cp_async16(sb + sw128_offset(r, c), src, ok);
+      const void* src = Bm.at(Bm.row(n0 + r), kb, ok);
+      cp_async16(sb + sw128_offset(r, cc), src, ok);
     }
     cp_async_commit();
   };

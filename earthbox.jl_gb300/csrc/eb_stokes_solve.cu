@@ -582,6 +582,16 @@ __global__ void k_prec_out(const float* __restrict__ ux, const float* __restrict
   zt[nc + c] = (double)zy;
 }
 
+// Learned stage: zt += a z2, rounded once to FP32 (Zk) so that zt and Zk stay equal.
+__global__ void k_add_round(double* __restrict__ zt, float* __restrict__ Zk, const double* __restrict__ z2, double a,
+                            int64_t n) {
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  const float v = (float)(zt[k] + a * z2[k]);
+  Zk[k] = v;
+  zt[k] = (double)v;
+}
+
 // ------------------------------------------------------ host geometry ---
 std::vector<int32_t> coarse_nodes(int32_t n_cells) {
   const int32_t M = n_cells / 2;
@@ -712,6 +722,7 @@ struct StokesState {
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t gexec = nullptr;
   int64_t graph_kernels = 0;
+  double *nn_t = nullptr, *nn_q = nullptr, *nn_z = nullptr;  // learned-stage scratch: [t | q], z2
 };
 
 namespace {
@@ -1106,6 +1117,61 @@ int ensure_solver(eb_ctx* c, StokesState* st, int m) {
   return EB_OK;
 }
 
+// The learned stage after the V-cycle (z = zt): t = v - A z, z2 = NN(t), and z += a z2 with
+// the step a = <t, A z2> / |A z2|^2 that minimises |t - a A z2|; kept when a > 0, i.e. when
+// it lowers the preconditioner residual (the multigrid alone otherwise).
+int learned_stage(eb_ctx* c, StokesState* st, const double* v, double* zt, float* Zk) {
+  const auto t0 = std::chrono::steady_clock::now();
+  const StokesSystem& s = st->sys;
+  const int64_t n3 = 3 * s.nc;
+  int rc;
+  if (!st->nn_t) {  // t and q adjacent: one reduction gives t.q and q.q
+    if ((rc = dalloc(c, st->allocs, &st->nn_t, 2 * n3)) || (rc = dalloc(c, st->allocs, &st->nn_z, n3))) return rc;
+    st->nn_q = st->nn_t + n3;
+  }
+  if ((rc = apply_scaled(c, st, zt, st->nn_q))) return rc;
+  EB_PROF(c, "k_axpy");
+  k_sub<<<nblk(n3), kB, 0, c->stream>>>(st->nn_t, v, st->nn_q, n3);
+  EB_LAUNCHED(c);
+  double tt;
+  if ((rc = mdot(c, st, st->nn_t, 0, 1, st->nn_t, &tt))) return rc;
+  bool keep = false;
+  if (tt > 0.0 && std::isfinite(tt)) {
+    if ((rc = nn_correction(c, st->nn_t, std::sqrt(tt / n3), st->nn_z)) || (rc = apply_scaled(c, st, st->nn_z, st->nn_q)))
+      return rc;
+    double d[2];  // t.q, q.q
+    if ((rc = mdot(c, st, st->nn_t, n3, 2, st->nn_q, d))) return rc;
+    keep = std::isfinite(d[0]) && std::isfinite(d[1]) && d[1] > 0.0 && d[0] > 0.0;
+    if (keep) {
+      EB_PROF(c, "k_axpy");
+      k_add_round<<<nblk(n3), kB, 0, c->stream>>>(zt, Zk, st->nn_z, d[0] / d[1], n3);
+      EB_LAUNCHED(c);
+    }
+    nn_count(c, keep, std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count(),
+             keep ? d[0] * d[0] / (d[1] * tt) : 0.0);
+  } else {
+    nn_count(c, false, std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count(), 0.0);
+  }
+  return EB_OK;
+}
+
+// Scaling, multigrid hierarchy and captured V-cycle of the current system.
+int prepare(eb_ctx* c, StokesState* st, int sweeps, int m) {
+  int rc;
+  B2 b2;
+  if ((rc = ensure_solver(c, st, m)) || (rc = read_b2(c, &b2))) return rc;
+  if (st->levels.empty() || std::memcmp(&b2, &st->b2_levels, sizeof(B2)) != 0) {
+    if ((rc = setup_levels(c, st, b2))) return rc;
+    st->b2_levels = b2;
+  }
+  if ((rc = refresh_levels(c, st, b2)) || (rc = capture_vcycle(c, st, sweeps))) return rc;
+  const StokesSystem& s = st->sys;
+  EB_PROF(c, "k_scaling");
+  k_scaling<<<nblk(s.nc), kB, 0, c->stream>>>(s.coef, c->gf[EB_G_ETAN0], s.pscale, st->w, st->prep, s.nc);
+  EB_LAUNCHED(c);
+  return EB_OK;
+}
+
 }  // namespace
 
 // ------------------------------------------------------------ C-ABI ---
@@ -1132,16 +1198,10 @@ extern "C" int eb_solve_stokes_system(eb_ctx* c, const eb_solve_opts* o, eb_solv
   if (opt.method != 1) opt.method = 0;
   const int m = std::max(std::min(opt.restart, kMaxRestart), opt.method == 1 ? 6 : 1);
   const int64_t n3 = 3 * s.nc;
-  B2 b2;
-  if ((rc = ensure_solver(c, st, m)) || (rc = read_b2(c, &b2))) return rc;
-  if (st->levels.empty() || std::memcmp(&b2, &st->b2_levels, sizeof(B2)) != 0) {
-    if ((rc = setup_levels(c, st, b2))) return rc;
-    st->b2_levels = b2;
-  }
-  if ((rc = refresh_levels(c, st, b2)) || (rc = capture_vcycle(c, st, opt.mg_sweeps))) return rc;
-  EB_PROF(c, "k_scaling");
-  k_scaling<<<nblk(s.nc), kB, 0, c->stream>>>(s.coef, c->gf[EB_G_ETAN0], s.pscale, st->w, st->prep, s.nc);
-  EB_LAUNCHED(c);
+  if (opt.learned && !nn_trained(c))
+    return eb_fail(c, EB_NOT_READY, "learned stage requested but eb_learned_train has not run");
+  const bool use_nn = opt.learned != 0 && opt.method != 1;
+  if ((rc = prepare(c, st, opt.mg_sweeps, m))) return rc;
   // bhat = W R, xhat = W^-1 S0
   EB_PROF(c, "k_axpy");
   k_mul<<<nblk(n3), kB, 0, c->stream>>>(st->bs, s.rhs, st->w, n3, 0);
@@ -1238,6 +1298,7 @@ extern "C" int eb_solve_stokes_system(eb_ctx* c, const eb_solve_opts* o, eb_solv
       float* zk = st->Z + (size_t)k * n3;
       double* w = st->V + (size_t)(k + 1) * n3;
       if ((rc = precondition(c, st, vk, st->zt, zk))) return rc;
+      if (use_nn && (rc = learned_stage(c, st, vk, st->zt, zk))) return rc;
       // Shifted Arnoldi: with a good preconditioner A z_k is close to v_k, so the slot holds
       // d = A z_k - v_k and the projection starts from d (h_kk gets the 1 back below); the
       // cancellation that classical Gram-Schmidt suffers is then measured against |d|.
@@ -1676,3 +1737,14 @@ extern "C" double eb_stokes_pscale(const eb_ctx* c) { return (c && c->st) ? c->s
 extern "C" int64_t eb_stokes_size(const eb_ctx* c) {
   return (c && c->have_grid) ? 3 * (int64_t)(c->xnum - 1) * (c->ynum - 1) : 0;
 }
+
+// ------------------------------------------- services of the learned preconditioner ---
+int stokes_nn_ready(eb_ctx* c, int sweeps) {
+  int rc = need_system(c, true);
+  if (rc) return rc;
+  StokesState* st = c->st;
+  return prepare(c, st, sweeps, std::max(st->m, 1));
+}
+int stokes_nn_apply(eb_ctx* c, const double* x, double* y) { return apply_scaled(c, c->st, x, y); }
+int stokes_nn_precondition(eb_ctx* c, const double* r, double* z) { return precondition(c, c->st, r, z, c->st->Z); }
+int stokes_nn_dot(eb_ctx* c, const double* a, const double* b, double* out) { return mdot(c, c->st, a, 0, 1, b, out); }

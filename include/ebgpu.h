@@ -306,6 +306,9 @@ typedef struct eb_solve_opts {
   int32_t use_initial_guess; /* 1: start from the current device solution vector, 0: from zero         */
   int32_t method;            /* 0: FGMRES (long recurrence, robust); 1: BiCGStab (short recurrence, two
                                 preconditioner applications per iteration)                           */
+  int32_t learned;           /* 1: after each V-cycle, the learned stage (eb_learned_train) adds its
+                                correction when that lowers the preconditioner residual (FGMRES only;
+                                Stokes only)                                                        */
 } eb_solve_opts;
 
 typedef struct eb_solve_report {
@@ -576,6 +579,45 @@ int eb_nn_gemm_bf16(int64_t M, int32_t N, int64_t K, const uint16_t* A, const ui
 int eb_nn_conv2d_bf16(int32_t B, int32_t H, int32_t W, int32_t C, int32_t Cout, int32_t taps, int32_t flip,
                       const uint16_t* x, const uint16_t* w, const float* bias, int32_t mode, float* y32,
                       uint16_t* y16);
+
+/* ---- learned preconditioner stage --------------------------------------------
+ * A BF16 convolutional U-Net (FP32 accumulation, tcgen05 tensor cores; 4 levels of 32, 64,
+ * 128, 128 channels, 1.1M parameters) mapping (log10 viscosity, density, residual r / RMS(r))
+ * on the Stokes cells to the correction e with A e = r of the diagonally scaled system.
+ * eb_learned_train trains it on the GPU (forward, backward and Adam on the device) on pairs
+ * generated from the current assembled system: e = z - P(A z) for z = P(noise), r = A e (P the
+ * multigrid preconditioner), patches of patch x patch cells.  eb_solve_opts.learned = 1 then
+ * applies z += a NN(v - A z) after each V-cycle inside FGMRES, a minimising |v - A z| (kept
+ * when a > 0).                                                                             */
+typedef struct eb_learned_opts {
+  int32_t batch;             /* patches per optimizer step (1..16)                               */
+  int32_t patch;             /* patch side in cells (multiple of 8; clipped to the grid)           */
+  int32_t steps;             /* optimizer steps                                                   */
+  int32_t patches_per_sample;/* optimizer steps per generated full-grid sample                     */
+  int32_t mg_sweeps;         /* V-cycle sweeps of P (0 -> 3)                                       */
+  double  lr;                /* Adam learning rate                                                 */
+  uint64_t seed;             /* Philox noise and patch offsets                                     */
+} eb_learned_opts;
+typedef struct eb_learned_report {
+  int32_t steps, patch_h, patch_w;
+  double  loss_first, loss_last;  /* mean MSE of the first and of the last min(8, steps/2) steps */
+  double  kappa;                  /* RMS(e) / RMS(r) scale of the output                          */
+  double  seconds;
+} eb_learned_report;
+int eb_learned_init(eb_ctx* ctx, uint64_t seed);  /* He-normal weights                            */
+int eb_learned_train(eb_ctx* ctx, const eb_learned_opts* opts, eb_learned_report* report);
+/* FP32 parameters, per layer [cout][taps][cin] weights then [cout] biases; set 1 uploads.  */
+int eb_learned_params(eb_ctx* ctx, float* params, int64_t capacity, int64_t* n, int32_t set);
+/* state[6]: eta mean, eta 1/std, rho mean, rho 1/std, kappa, trained flag; set 1 uploads.   */
+int eb_learned_state(eb_ctx* ctx, double* state, int32_t set);
+/* Network on host arrays: x [B][H][W][8] FP32 (rounded to BF16), y [B][H][W][16] FP32.      */
+int eb_learned_forward(eb_ctx* ctx, int32_t B, int32_t H, int32_t W, const float* x, float* y);
+/* MSE loss against t [B][H][W][3] and the gradient of every parameter (layout as above).    */
+int eb_learned_loss_grad(eb_ctx* ctx, int32_t B, int32_t H, int32_t W, const float* x, const float* t, double* loss,
+                         float* grad);
+/* Learned-stage corrections kept / rejected by FGMRES since the last call, their time, and the
+ * mean fraction of the squared preconditioner residual they removed.                       */
+int eb_learned_stats(eb_ctx* ctx, int64_t* accepted, int64_t* rejected, double* seconds, double* mean_removed);
 
 /* ---- checkpoints -----------------------------------------------------------
  * No counterpart in the reference, whose backups (model_manager/backup/core/MakeBackup.jl:22)
