@@ -70,6 +70,7 @@ NCU_DRAM_BYTES_PER_MARKER = {
     "k_cells<subgrid_stress>": 57.3,
     "k_advect": 83.1,
     "k_post_stokes": 44.5,
+    "k_tail": 167.9,
 }
 
 
