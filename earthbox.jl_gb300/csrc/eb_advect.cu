@@ -51,17 +51,19 @@ __device__ __forceinline__ void walk_y(const DevGrid& g, int32_t iy0, float py, 
 // with offsets (ux, uy) inside basic cell (jx, jy).
 __device__ __forceinline__ void vel_spin(const DevGrid& g, const VelGrids& V, int32_t jx, int32_t jy, float ux,
                                          float uy, float& vx, float& vy, float& sp) {
-  const float dx = ux * __ldg(&g.rsxf[jx - 1]);
-  const float dy = uy * __ldg(&g.rsyf[jy - 1]);
+  const float4 cx0 = __ldg(&g.colx[2 * (jx - 1)]), cx1 = __ldg(&g.colx[2 * (jx - 1) + 1]);
+  const float4 ry0 = __ldg(&g.rowy[2 * (jy - 1)]), ry1 = __ldg(&g.rowy[2 * (jy - 1) + 1]);
+  const float dx = ux * cx0.y;
+  const float dy = uy * ry0.y;
   // vx grid: x from the basic cell, y row yi = jy + (y > gridy_vx[jy+1])
-  const float vhi = __ldg(&g.vxoff_hi[jy - 1]);
-  const int32_t yi = (uy > vhi) ? jy + 1 : jy;
-  const float dyv = (uy - ((yi == jy) ? __ldg(&g.vxoff_lo[jy - 1]) : vhi)) * __ldg(&g.rsyvxf[yi - 1]);
+  const bool ylo = !(uy > ry0.w);
+  const int32_t yi = ylo ? jy : jy + 1;
+  const float dyv = (uy - (ylo ? ry0.z : ry0.w)) * (ylo ? ry1.x : ry1.y);
   vx = gather4f(V.vx1, g.ynum + 1, yi, jx, dx, dyv);
   // vy grid: column xi = jx + (x > gridx_vy[jx+1]), y from the basic cell
-  const float hhi = __ldg(&g.vyoff_hi[jx - 1]);
-  const int32_t xi = (ux > hhi) ? jx + 1 : jx;
-  const float dxv = (ux - ((xi == jx) ? __ldg(&g.vyoff_lo[jx - 1]) : hhi)) * __ldg(&g.rsxvyf[xi - 1]);
+  const bool xlo = !(ux > cx0.w);
+  const int32_t xi = xlo ? jx : jx + 1;
+  const float dxv = (ux - (xlo ? cx0.z : cx0.w)) * (xlo ? cx1.x : cx1.y);
   vy = gather4f(V.vy1, g.ynum, jy, xi, dxv, dy);
   // basic grid spin
   sp = gather4f(V.esp, g.ynum, jy, jx, dx, dy);
@@ -132,10 +134,9 @@ struct TailGrids {
 // alias the loads, so a load written after a store would wait for it and each marker
 // would pay several DRAM round trips in sequence.  Loading first puts all of them in
 // flight at once, and the plastic fields (10 % of markers or so) follow as soon as
-// pfailure arrives, overlapping the RK4 gathers.  Five blocks per SM (48 registers, a few
-// spilled) ran faster than four without spills (1.98 against 2.06 ms at 40M markers).
+// pfailure arrives, overlapping the RK4 gathers.
 template <bool kMove>
-__global__ void __launch_bounds__(kBlock, 5) k_tail(DevMarkers mk, DevGrid g, VelGrids V, TailGrids T) {
+__global__ void __launch_bounds__(kBlock) k_tail(DevMarkers mk, DevGrid g, VelGrids V, TailGrids T) {
   const int64_t m = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (m >= mk.M) return;
   const uint8_t flags = __ldg(&mk.mflags[m]);

@@ -148,13 +148,14 @@ EB_DEV float gather4(const double* __restrict__ g, int32_t rows, int32_t iy, int
   v = fmaf(w.lr, d2f(__ldg(&g[o + rows + 1])), v);
   return v;
 }
+// (a grid holds fewer than 2^31 nodes: the offset is formed in 32 bits)
 EB_DEV float gather4f(const float* __restrict__ g, int32_t rows, int32_t iy, int32_t ix, float dx,
                       float dy) {
   const W4 w = wts(dx, dy);
-  const size_t o = (size_t)(ix - 1) * rows + (iy - 1);
-  float v = w.ul * __ldg(&g[o]);
-  v = fmaf(w.ll, __ldg(&g[o + 1]), v);
-  v = fmaf(w.ur, __ldg(&g[o + rows]), v);
-  v = fmaf(w.lr, __ldg(&g[o + rows + 1]), v);
+  const float* p = g + ((ix - 1) * rows + (iy - 1));
+  float v = w.ul * __ldg(p);
+  v = fmaf(w.ll, __ldg(p + 1), v);
+  v = fmaf(w.ur, __ldg(p + rows), v);
+  v = fmaf(w.lr, __ldg(p + rows + 1), v);
   return v;
 }

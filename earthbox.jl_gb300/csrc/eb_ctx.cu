@@ -411,6 +411,19 @@ extern "C" int eb_set_grid(eb_ctx* c, const eb_grid_desc* G) {
       (rc = upf(rsxvy, &g.rsxvyf)) || (rc = upf(syf, &g.syf)) || (rc = upf(rsyf, &g.rsyf)) || (rc = upf(vxlo, &g.vxoff_lo)) ||
       (rc = upf(vxhi, &g.vxoff_hi)) || (rc = upf(rsyvx, &g.rsyvxf)))
     return rc;
+  std::vector<float> colx(8 * (size_t)(X - 1), 0.f), rowy(8 * (size_t)(Y - 1), 0.f);
+  for (int32_t j = 0; j < X - 1; ++j) {
+    float* e = &colx[8 * (size_t)j];
+    e[0] = sxf[j]; e[1] = rsxf[j]; e[2] = vylo[j]; e[3] = vyhi[j]; e[4] = rsxvy[j]; e[5] = rsxvy[j + 1];
+  }
+  for (int32_t i = 0; i < Y - 1; ++i) {
+    float* e = &rowy[8 * (size_t)i];
+    e[0] = syf[i]; e[1] = rsyf[i]; e[2] = vxlo[i]; e[3] = vxhi[i]; e[4] = rsyvx[i]; e[5] = rsyvx[i + 1];
+  }
+  const float *pcx = nullptr, *pry = nullptr;
+  if ((rc = upf(colx, &pcx)) || (rc = upf(rowy, &pry))) return rc;
+  g.colx = reinterpret_cast<const float4*>(pcx);  // cudaMalloc storage: 256-byte aligned
+  g.rowy = reinterpret_cast<const float4*>(pry);
   // cell sort tables and partial-sum buffer
   CellSort& s = c->cs;
   s.ncells = (X - 1) * (Y - 1);

@@ -21,20 +21,28 @@ struct DevGrid {
   const float *vxoff_lo, *vxoff_hi;       // [ynum-1] gridy_vx[i]-gy[i], gridy_vx[i+1]-gy[i]
   const float *rsxvyf;                    // [xnum]   1/xstp_vy
   const float *rsyvxf;                    // [ynum]   1/ystp_vx
+  // the same FP32 tables packed per basic index j (1-based, entry 2(j-1) and 2(j-1)+1):
+  // {xstp_b, 1/xstp_b, vyoff_lo, vyoff_hi}, {1/xstp_vy[j], 1/xstp_vy[j+1], 0, 0}; rowy likewise
+  // for y with the vx-grid offsets: one cell's geometry in two 16-byte loads
+  const float4 *colx, *rowy;
   uint64_t kxmin, kxmax, kymin, kymax;    // order keys of the domain limits
   double xstpavg, ystpavg;
 };
 
 // Pressure-grid bilinear gather (GridToMarker.jl:104-153, MarkerGridMapping.jl:311-350)
 // on an FP32 mirror of the grid; (lx, ly) is the marker's offset from basic node (ix, iy).
+// xp is ix-1 or ix (after the clamp), so its staggered spacing is one of the pair at ix-1.
 __device__ __forceinline__ float gather_p(const float* __restrict__ pg, const DevGrid& g, int32_t ix, int32_t iy,
                                           float lx, float ly) {
-  const float hx = __ldg(&g.vyoff_hi[ix - 1]), hy = __ldg(&g.vxoff_hi[iy - 1]);
+  const float4 c0 = __ldg(&g.colx[2 * (ix - 1)]), c1 = __ldg(&g.colx[2 * (ix - 1) + 1]);
+  const float4 r0 = __ldg(&g.rowy[2 * (iy - 1)]), r1 = __ldg(&g.rowy[2 * (iy - 1) + 1]);
+  const float hx = c0.w, hy = r0.w;
   const int32_t xp = clamp_i((lx < hx) ? ix - 1 : ix, 1, g.xnum - 2);
   const int32_t yp = clamp_i((ly < hy) ? iy - 1 : iy, 1, g.ynum - 2);
-  const float ox = (xp + 1 == ix) ? __ldg(&g.vyoff_lo[ix - 1]) : hx;
-  const float oy = (yp + 1 == iy) ? __ldg(&g.vxoff_lo[iy - 1]) : hy;
-  return gather4f(pg, g.ynum - 1, yp, xp, (lx - ox) * __ldg(&g.rsxvyf[xp]), (ly - oy) * __ldg(&g.rsyvxf[yp]));
+  const bool xl = xp + 1 == ix, yl = yp + 1 == iy;
+  const float ox = xl ? c0.z : hx;
+  const float oy = yl ? r0.z : hy;
+  return gather4f(pg, g.ynum - 1, yp, xp, (lx - ox) * (xl ? c1.x : c1.y), (ly - oy) * (yl ? r1.x : r1.y));
 }
 
 struct DevMats {
