@@ -203,7 +203,8 @@ def unet_flops_per_pixel() -> float:
     return sum(2.0 * t * ci * co / 4 ** lv for ci, co, t, lv in layers)
 
 
-def stokes_gpu(mic, reps: int = 2, method: str = "fgmres", rtol: float = 1e-8, learned: bool = False):
+def stokes_gpu(mic, reps: int = 2, method: str = "fgmres", rtol: float = 1e-8, learned: bool = False,
+               precision: str = "mixed"):
     """The Stokes step on the grids the context holds: build steps, solve to 1e-8, unpack.
     One warm-up (level set-up, graph capture), then `reps` timed steps (wall clock: the
     FGMRES loop is host-driven)."""
@@ -213,7 +214,7 @@ def stokes_gpu(mic, reps: int = 2, method: str = "fgmres", rtol: float = 1e-8, l
         mic.calc_viscoelastic_terms()
         mic.viscoelastic_rhs()
         mic.build_system_of_equations()
-        rep = mic.solve_system(rtol=rtol, check=False, method=method, learned=learned)
+        rep = mic.solve_system(rtol=rtol, check=False, method=method, learned=learned, precision=precision)
         mic.process_stokes_solution()
         return rep
 
@@ -470,6 +471,11 @@ def main():
                   "reorthogonalisations": s_rep["reorthogonalisations"],
                   "kernels_ms": {k: round(v[0] * v[1], 3) for k, v in
                                  sorted(s_kern.items(), key=lambda kv: -kv[1][0] * kv[1][1])[:12]}}
+        # the plain method on the same system: FP64 V-cycle and FP64 stored directions
+        p_dt, p_rep, _ = stokes_gpu(mic, reps=2, method=args.stokes_method, precision="fp64")
+        stokes["plain_fp64"] = {"value": p_dt, "unit": "s/solve", "iterations": p_rep["iterations"],
+                                "rel_residual": p_rep["rel_residual"], "status": p_rep["status"],
+                                "mixed_speedup": p_dt / s_dt}
         # roofline of the Krylov-basis products (the solve's dominant kernels): per FGMRES
         # iteration k of a cycle, k_mdot reads the k+2 basis vectors and k_maxpy k+1 of them
         # plus the new direction (read and written); vectors are N doubles.
@@ -633,6 +639,11 @@ def main():
         timestep = {"metric": "per-timestep wall time", "value": (time.perf_counter() - t0) / 2, "unit": "s/step",
                     "higher_is_better": False,
                     "includes": "marker cycle (transfer + RK4), Stokes step (solve to 1e-8), heat step"}
+        if stokes is not None and "plain_fp64" in stokes:
+            # the same step with the plain FP64 multigrid solve in place of the mixed one
+            plain = timestep["value"] - stokes["value"] + stokes["plain_fp64"]["value"]
+            timestep["plain_fp64_mg_step"] = plain
+            timestep["speedup_vs_plain_fp64"] = plain / timestep["value"]
 
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,

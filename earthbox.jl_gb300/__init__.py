@@ -290,11 +290,12 @@ class MarkerInCell:
 
     def solve_system(self, rtol: float = 1e-8, max_iters: int = 0, restart: int = 0, mg_sweeps: int = 0,
                      use_initial_guess: bool = False, method: str = "fgmres", check: bool = True,
-                     learned: bool = False) -> dict:
+                     learned: bool = False, precision: str = "mixed") -> dict:
         """The Stokes solve (replaces SystemSolver.solve_system_optimized, SystemSolver.jl:67-91);
-        method "fgmres" or "bicgstab"; learned: add the trained network's stage after each V-cycle."""
+        method "fgmres" or "bicgstab"; learned: add the trained network's stage after each V-cycle;
+        precision "mixed" (FP32 V-cycle and stored directions) or "fp64" (the plain method)."""
         o = _abi.SolveOpts(rtol, max_iters, restart, mg_sweeps, int(use_initial_guess),
-                           {"fgmres": 0, "bicgstab": 1}[method], int(learned))
+                           {"fgmres": 0, "bicgstab": 1}[method], int(learned), {"mixed": 0, "fp64": 1}[precision])
         r = _abi.SolveReport()
         rc = self._lib.eb_solve_stokes_system(self._ctx, C.byref(o), C.byref(r))
         rep = {"status": rc, "iterations": r.iterations, "levels": r.levels, "rel_residual": r.rel_residual,
@@ -632,7 +633,7 @@ class MarkerInCell:
                           use_initial_guess: bool = True, check: bool = True) -> dict:
         """The solve of SystemSolver.discretize_and_solve_conductive_heat_equation
         (heat_solver/solver/SystemSolver.jl:32-66) and reload_solu_temp: tk2."""
-        o = _abi.SolveOpts(rtol, max_iters, 0, mg_sweeps, int(use_initial_guess), 0, 0)
+        o = _abi.SolveOpts(rtol, max_iters, 0, mg_sweeps, int(use_initial_guess), 0, 0, 0)
         r = _abi.SolveReport()
         rc = self._lib.eb_solve_heat_system(self._ctx, C.byref(o), C.byref(r))
         if check:
@@ -648,7 +649,7 @@ class MarkerInCell:
                                         mg_sweeps: int = 0) -> dict:
         """HeatLoop.run_conductive_heat_solver_loop! (heat_loop/HeatLoop.jl:10-79)."""
         hp = self._heat(params)
-        o = _abi.SolveOpts(rtol, max_iters, 0, mg_sweeps, 1, 0, 0)
+        o = _abi.SolveOpts(rtol, max_iters, 0, mg_sweeps, 1, 0, 0, 0)
         r = _abi.HeatLoopReport()
         self._check(self._lib.eb_run_conductive_heat_solver_loop(self._ctx, C.byref(hp), C.byref(o), C.byref(r)))
         return {k: getattr(r, k) for k, _ in _abi.HeatLoopReport._fields_}

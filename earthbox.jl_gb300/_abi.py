@@ -124,7 +124,8 @@ class StokesParams(C.Structure):
 
 class SolveOpts(C.Structure):
     _fields_ = [("rtol", C.c_double), ("max_iters", C.c_int32), ("restart", C.c_int32), ("mg_sweeps", C.c_int32),
-                ("use_initial_guess", C.c_int32), ("method", C.c_int32), ("learned", C.c_int32)]
+                ("use_initial_guess", C.c_int32), ("method", C.c_int32), ("learned", C.c_int32),
+                ("precision", C.c_int32)]
 
 
 class LearnedOpts(C.Structure):

@@ -262,16 +262,20 @@ __global__ void k_deinterleave(const double* __restrict__ il, double* __restrict
 }
 
 // ----------------------------------------------------------- multigrid ---
+// The V-cycle runs in FP32 (the mixed-precision method) or in FP64 (the plain method): every
+// multigrid kernel is a template on the level arithmetic T.  The transfer weights and the
+// boundary-condition coefficients of the coarse operators stay FP32 tables in both.
 struct Axis2 { int32_t* idx; float* w; };   // prolongation: 2 (coarse index, weight) per fine index
 struct AxisR { int32_t* idx; float* w; };   // restriction: kRmax (fine index, weight) per coarse index
 
+// Host view of one level; the arrays hold T = float or double (StokesState::mg64).
 struct Level {
   int32_t nx = 0, ny = 0;
   int64_t nc = 0;
-  float *X = nullptr, *Y = nullptr;                       // [9][nc]
-  float *ux = nullptr, *uy = nullptr, *fx = nullptr, *fy = nullptr, *rx = nullptr, *ry = nullptr;
-  float *etas = nullptr, *etan = nullptr;                 // [(ny+1)(nx+1)], [ny nx]
-  float *xstp = nullptr, *ystp = nullptr, *xstpc = nullptr, *ystpc = nullptr;
+  void *X = nullptr, *Y = nullptr;                        // [9][nc]
+  void *ux = nullptr, *uy = nullptr, *fx = nullptr, *fy = nullptr, *rx = nullptr, *ry = nullptr;
+  void *etas = nullptr, *etan = nullptr;                  // [(ny+1)(nx+1)], [ny nx]
+  void *xstp = nullptr, *ystp = nullptr, *xstpc = nullptr, *ystpc = nullptr;
   int32_t *kx = nullptr, *ky = nullptr;                   // nodes of this level in the finer level
   // transfers to the next coarser level
   Axis2 pvx_x{}, pvx_y{}, pvy_x{}, pvy_y{};
@@ -284,10 +288,10 @@ struct B2 { float topx, botx, topy, boty, leftx, rightx, lefty, righty; };
 
 // Coarse-level velocity stencil from averaged viscosity (same formulas as the
 // fine assembly, uniform boundary-condition coefficients, no stabilisation).
-__global__ void k_redisc(int32_t nx, int32_t ny, const float* __restrict__ etas, const float* __restrict__ etan,
-                         const float* __restrict__ xstp, const float* __restrict__ ystp,
-                         const float* __restrict__ xstpc, const float* __restrict__ ystpc, B2 b,
-                         float* __restrict__ X, float* __restrict__ Y) {
+template <class T>
+__global__ void k_redisc(int32_t nx, int32_t ny, const T* __restrict__ etas, const T* __restrict__ etan,
+                         const T* __restrict__ xstp, const T* __restrict__ ystp, const T* __restrict__ xstpc,
+                         const T* __restrict__ ystpc, B2 b, T* __restrict__ X, T* __restrict__ Y) {
   const int64_t nc = (int64_t)nx * ny;
   const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= nc) return;
@@ -295,93 +299,98 @@ __global__ void k_redisc(int32_t nx, int32_t ny, const float* __restrict__ etas,
   const int32_t xnum = nx + 1, ynum = ny + 1;
   auto eS = [&](int ii, int jj) { return etas[(int64_t)(jj - 1) * ynum + (ii - 1)]; };
   auto eN = [&](int ii, int jj) { return etan[(int64_t)(jj - 1) * ny + (ii - 1)]; };
-  float x[9] = {0}, y[9] = {0};
+  const T two = T(2);
+  T x[9] = {0}, y[9] = {0};
   if (j < xnum - 1) {
     const bool left = j == 1, right2 = j >= xnum - 2, top = i == 1, bot = i >= ynum - 1;
-    const float cL = 2.f * eN(i, j) / xstp[j - 1] / xstpc[j];
-    const float cR = 2.f * eN(i, j + 1) / xstp[j] / xstpc[j];
-    const float cU = eS(i, j + 1) / ystpc[i - 1] / ystp[i - 1];
-    const float cD = eS(i + 1, j + 1) / ystpc[i] / ystp[i - 1];
-    float C = -(cL + cR) - (cU + cD);
-    const float gUL = eS(i, j + 1) / xstpc[j] / ystp[i - 1], gUR = -gUL;
-    const float gLL = -eS(i + 1, j + 1) / xstpc[j] / ystp[i - 1], gLR = -gLL;
-    if (left) C += b.leftx * cL; else x[1] = cL;
-    if (right2) C += b.rightx * cR; else x[2] = cR;
-    if (top) C += b.topx * cU; else x[3] = cU;
-    if (bot) C += b.botx * cD; else x[4] = cD;
+    const T cL = two * eN(i, j) / xstp[j - 1] / xstpc[j];
+    const T cR = two * eN(i, j + 1) / xstp[j] / xstpc[j];
+    const T cU = eS(i, j + 1) / ystpc[i - 1] / ystp[i - 1];
+    const T cD = eS(i + 1, j + 1) / ystpc[i] / ystp[i - 1];
+    T C = -(cL + cR) - (cU + cD);
+    const T gUL = eS(i, j + 1) / xstpc[j] / ystp[i - 1], gUR = -gUL;
+    const T gLL = -eS(i + 1, j + 1) / xstpc[j] / ystp[i - 1], gLR = -gLL;
+    if (left) C += (T)b.leftx * cL; else x[1] = cL;
+    if (right2) C += (T)b.rightx * cR; else x[2] = cR;
+    if (top) C += (T)b.topx * cU; else x[3] = cU;
+    if (bot) C += (T)b.botx * cD; else x[4] = cD;
     x[0] = C;
-    float vUL = 0, vUR = 0, vLL = 0, vLR = 0;
-    if (!top) { vUL = gUL; vUR = gUR; } else { vLL = b.topy * gUL; vLR = b.topy * gUR; }
-    if (!bot) { vLL += gLL; vLR += gLR; } else { vUL += b.boty * gLL; vUR += b.boty * gLR; }
+    T vUL = 0, vUR = 0, vLL = 0, vLR = 0;
+    if (!top) { vUL = gUL; vUR = gUR; } else { vLL = (T)b.topy * gUL; vLR = (T)b.topy * gUR; }
+    if (!bot) { vLL += gLL; vLR += gLR; } else { vUL += (T)b.boty * gLL; vUR += (T)b.boty * gLR; }
     x[5] = vUL; x[6] = vUR; x[7] = vLL; x[8] = vLR;
   } else {
-    x[0] = 1.f;
+    x[0] = T(1);
   }
   if (i < ynum - 1) {
     const bool top = i == 1, bot2 = i >= ynum - 2, left = j == 1, right = j >= xnum - 1;
-    const float cU = 2.f * eN(i, j) / ystp[i - 1] / ystpc[i];
-    const float cD = 2.f * eN(i + 1, j) / ystp[i] / ystpc[i];
-    const float cL = eS(i + 1, j) / xstpc[j - 1] / xstp[j - 1];
-    const float cR = eS(i + 1, j + 1) / xstpc[j] / xstp[j - 1];
-    float C = -(cU + cD) - (cL + cR);
-    const float hUL = eS(i + 1, j) / ystpc[i] / xstp[j - 1], hLL = -hUL;
-    const float hUR = -eS(i + 1, j + 1) / ystpc[i] / xstp[j - 1], hLR = -hUR;
-    if (top) C += b.topy * cU; else y[1] = cU;
-    if (bot2) C += b.boty * cD; else y[2] = cD;
-    if (left) C += b.lefty * cL; else y[3] = cL;
-    if (right) C += b.righty * cR; else y[4] = cR;
+    const T cU = two * eN(i, j) / ystp[i - 1] / ystpc[i];
+    const T cD = two * eN(i + 1, j) / ystp[i] / ystpc[i];
+    const T cL = eS(i + 1, j) / xstpc[j - 1] / xstp[j - 1];
+    const T cR = eS(i + 1, j + 1) / xstpc[j] / xstp[j - 1];
+    T C = -(cU + cD) - (cL + cR);
+    const T hUL = eS(i + 1, j) / ystpc[i] / xstp[j - 1], hLL = -hUL;
+    const T hUR = -eS(i + 1, j + 1) / ystpc[i] / xstp[j - 1], hLR = -hUR;
+    if (top) C += (T)b.topy * cU; else y[1] = cU;
+    if (bot2) C += (T)b.boty * cD; else y[2] = cD;
+    if (left) C += (T)b.lefty * cL; else y[3] = cL;
+    if (right) C += (T)b.righty * cR; else y[4] = cR;
     y[0] = C;
-    float xUL = 0, xUR = 0, xLL = 0, xLR = 0;
-    if (!left) { xUL = hUL; xLL = hLL; } else { xUR = b.leftx * hUL; xLR = b.leftx * hLL; }
-    if (!right) { xUR += hUR; xLR += hLR; } else { xUL += b.rightx * hUR; xLL += b.rightx * hLR; }
+    T xUL = 0, xUR = 0, xLL = 0, xLR = 0;
+    if (!left) { xUL = hUL; xLL = hLL; } else { xUR = (T)b.leftx * hUL; xLR = (T)b.leftx * hLL; }
+    if (!right) { xUR += hUR; xLR += hLR; } else { xUL += (T)b.rightx * hUR; xLL += (T)b.rightx * hLR; }
     y[5] = xUL; y[6] = xUR; y[7] = xLL; y[8] = xLR;
   } else {
-    y[0] = 1.f;
+    y[0] = T(1);
   }
   for (int k = 0; k < 9; ++k) { X[(int64_t)k * nc + c] = x[k]; Y[(int64_t)k * nc + c] = y[k]; }
 }
 
 // Level 0 takes the assembled FP64 velocity block.
-__global__ void k_level0(const double* __restrict__ coef, float* __restrict__ X, float* __restrict__ Y, int64_t nc) {
+template <class T>
+__global__ void k_level0(const double* __restrict__ coef, T* __restrict__ X, T* __restrict__ Y, int64_t nc) {
   const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= nc) return;
   for (int k = 0; k < 9; ++k) {
-    X[(int64_t)k * nc + c] = (float)coef[(int64_t)k * nc + c];
-    Y[(int64_t)k * nc + c] = (float)coef[(int64_t)(11 + k) * nc + c];
+    X[(int64_t)k * nc + c] = (T)coef[(int64_t)k * nc + c];
+    Y[(int64_t)k * nc + c] = (T)coef[(int64_t)(11 + k) * nc + c];
   }
 }
-__global__ void k_to_f32(const double* __restrict__ a, float* __restrict__ b, int64_t n) {
+template <class T>
+__global__ void k_to_real(const double* __restrict__ a, T* __restrict__ b, int64_t n) {
   const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (k < n) b[k] = (float)a[k];
+  if (k < n) b[k] = (T)a[k];
 }
 // Arithmetic averages of the finer level's viscosity onto this level.
-__global__ void k_coarsen_eta(const float* __restrict__ es_f, const float* __restrict__ en_f, int32_t nxf, int32_t nyf,
-                              float* __restrict__ es_c, float* __restrict__ en_c, int32_t nxc, int32_t nyc,
+template <class T>
+__global__ void k_coarsen_eta(const T* __restrict__ es_f, const T* __restrict__ en_f, int32_t nxf, int32_t nyf,
+                              T* __restrict__ es_c, T* __restrict__ en_c, int32_t nxc, int32_t nyc,
                               const int32_t* __restrict__ kx, const int32_t* __restrict__ ky) {
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const int64_t nnode = (int64_t)(nxc + 1) * (nyc + 1);
   if (t < nnode) {
     const int32_t I = (int32_t)(t % (nyc + 1)), J = (int32_t)(t / (nyc + 1));
     const int32_t fi = ky[I], fj = kx[J];
-    float s = 0.f; int n = 0;
+    T s = 0; int n = 0;
     for (int32_t jj = max(fj - 1, 0); jj <= min(fj + 1, nxf); ++jj)
       for (int32_t ii = max(fi - 1, 0); ii <= min(fi + 1, nyf); ++ii) { s += es_f[(int64_t)jj * (nyf + 1) + ii]; ++n; }
-    es_c[t] = s / (float)n;
+    es_c[t] = s / (T)n;
   }
   if (t < (int64_t)nxc * nyc) {
     const int32_t I = (int32_t)(t % nyc), J = (int32_t)(t / nyc);
-    float s = 0.f; int n = 0;
+    T s = 0; int n = 0;
     for (int32_t jj = kx[J]; jj < kx[J + 1]; ++jj)
       for (int32_t ii = ky[I]; ii < ky[I + 1]; ++ii) { s += en_f[(int64_t)jj * nyf + ii]; ++n; }
-    en_c[t] = s / (float)n;
+    en_c[t] = s / (T)n;
   }
 }
 
 // Velocity-block product of one row kind at cell c.
-__device__ __forceinline__ float rowx(const float* __restrict__ X, const float* ux, const float* uy, int64_t c, int32_t i,
-                                      int32_t j, int32_t nx, int32_t ny, int64_t nc, bool skip_center) {
+template <class T>
+__device__ __forceinline__ T rowx(const T* __restrict__ X, const T* ux, const T* uy, int64_t c, int32_t i, int32_t j,
+                                  int32_t nx, int32_t ny, int64_t nc, bool skip_center) {
   const bool hu = i > 0, hd = i < ny - 1, hl = j > 0, hr = j < nx - 1;
-  float a = skip_center ? 0.f : X[c] * ux[c];
+  T a = skip_center ? T(0) : X[c] * ux[c];
   if (hl) a += X[nc + c] * ux[c - ny];
   if (hr) a += X[2 * nc + c] * ux[c + ny];
   if (hu) a += X[3 * nc + c] * ux[c - 1];
@@ -392,10 +401,11 @@ __device__ __forceinline__ float rowx(const float* __restrict__ X, const float* 
   if (hr) a += X[8 * nc + c] * uy[c + ny];
   return a;
 }
-__device__ __forceinline__ float rowy(const float* __restrict__ Y, const float* ux, const float* uy, int64_t c, int32_t i,
-                                      int32_t j, int32_t nx, int32_t ny, int64_t nc, bool skip_center) {
+template <class T>
+__device__ __forceinline__ T rowy(const T* __restrict__ Y, const T* ux, const T* uy, int64_t c, int32_t i, int32_t j,
+                                  int32_t nx, int32_t ny, int64_t nc, bool skip_center) {
   const bool hu = i > 0, hd = i < ny - 1, hl = j > 0, hr = j < nx - 1;
-  float a = skip_center ? 0.f : Y[c] * uy[c];
+  T a = skip_center ? T(0) : Y[c] * uy[c];
   if (hu) a += Y[nc + c] * uy[c - 1];
   if (hd) a += Y[2 * nc + c] * uy[c + 1];
   if (hl) a += Y[3 * nc + c] * uy[c - ny];
@@ -408,11 +418,12 @@ __device__ __forceinline__ float rowy(const float* __restrict__ Y, const float* 
 }
 
 // Device view of one multigrid level (transfer tables point to the next coarser level).
+template <class T>
 struct LevelDev {
   int32_t nx, ny;
   int64_t nc;
-  const float *X, *Y;
-  float *ux, *uy, *fx, *fy, *rx, *ry;
+  const T *X, *Y;
+  T *ux, *uy, *fx, *fy, *rx, *ry;
   Axis2 pvx_x, pvx_y, pvy_x, pvy_y;
   AxisR rvx_x, rvx_y, rvy_x, rvy_y;
 };
@@ -420,7 +431,8 @@ struct LevelDev {
 // Red-black Gauss-Seidel update of the t-th cell of one color: comp 0 updates vx,
 // 1 updates vy, on cells with (i + j) % 2 == color.  Column j holds the rows
 // i = 2q + ((j + color) & 1) of that color, q < ceil(ny / 2).
-__device__ __forceinline__ void d_rbgs(const LevelDev& v, int64_t t, int comp, int color) {
+template <class T>
+__device__ __forceinline__ void d_rbgs(const LevelDev<T>& v, int64_t t, int comp, int color) {
   const int32_t half = (v.ny + 1) / 2;
   const int32_t j = (int32_t)(t / half);
   if (j >= v.nx) return;
@@ -428,39 +440,42 @@ __device__ __forceinline__ void d_rbgs(const LevelDev& v, int64_t t, int comp, i
   if (i >= v.ny) return;
   const int64_t c = (int64_t)j * v.ny + i;
   if (comp == 0) {
-    const float s = rowx(v.X, v.ux, v.uy, c, i, j, v.nx, v.ny, v.nc, true);
+    const T s = rowx(v.X, v.ux, v.uy, c, i, j, v.nx, v.ny, v.nc, true);
     v.ux[c] = (v.fx[c] - s) / v.X[c];
   } else {
-    const float s = rowy(v.Y, v.ux, v.uy, c, i, j, v.nx, v.ny, v.nc, true);
+    const T s = rowy(v.Y, v.ux, v.uy, c, i, j, v.nx, v.ny, v.nc, true);
     v.uy[c] = (v.fy[c] - s) / v.Y[c];
   }
 }
-__device__ __forceinline__ int64_t rb_count(const LevelDev& v) { return (int64_t)v.nx * ((v.ny + 1) / 2); }
+template <class T>
+__device__ __forceinline__ int64_t rb_count(const LevelDev<T>& v) { return (int64_t)v.nx * ((v.ny + 1) / 2); }
 
-__device__ __forceinline__ void d_resid(const LevelDev& v, int64_t c) {
+template <class T>
+__device__ __forceinline__ void d_resid(const LevelDev<T>& v, int64_t c) {
   const int32_t i = (int32_t)(c % v.ny), j = (int32_t)(c / v.ny);
   v.rx[c] = v.fx[c] - rowx(v.X, v.ux, v.uy, c, i, j, v.nx, v.ny, v.nc, false);
   v.ry[c] = v.fy[c] - rowy(v.Y, v.ux, v.uy, c, i, j, v.nx, v.ny, v.nc, false);
 }
 // coarse f = R r at coarse cell c (tensor product of the axis tables of the fine level f)
-__device__ __forceinline__ void d_restrict(const LevelDev& f, const LevelDev& cl, int64_t c) {
+template <class T>
+__device__ __forceinline__ void d_restrict(const LevelDev<T>& f, const LevelDev<T>& cl, int64_t c) {
   const int32_t I = (int32_t)(c % cl.ny), J = (int32_t)(c / cl.ny);
-  float sx = 0.f, sy = 0.f;
+  T sx = 0, sy = 0;
   for (int a = 0; a < kRmax; ++a) {
-    const float wa = f.rvx_x.w[J * kRmax + a];
-    if (wa != 0.f) {
+    const T wa = (T)f.rvx_x.w[J * kRmax + a];
+    if (wa != T(0)) {
       const int64_t col = (int64_t)f.rvx_x.idx[J * kRmax + a] * f.ny;
       for (int b = 0; b < kRmax; ++b) {
-        const float wb = f.rvx_y.w[I * kRmax + b];
-        if (wb != 0.f) sx += wa * wb * f.rx[col + f.rvx_y.idx[I * kRmax + b]];
+        const T wb = (T)f.rvx_y.w[I * kRmax + b];
+        if (wb != T(0)) sx += wa * wb * f.rx[col + f.rvx_y.idx[I * kRmax + b]];
       }
     }
-    const float va = f.rvy_x.w[J * kRmax + a];
-    if (va != 0.f) {
+    const T va = (T)f.rvy_x.w[J * kRmax + a];
+    if (va != T(0)) {
       const int64_t col = (int64_t)f.rvy_x.idx[J * kRmax + a] * f.ny;
       for (int b = 0; b < kRmax; ++b) {
-        const float vb = f.rvy_y.w[I * kRmax + b];
-        if (vb != 0.f) sy += va * vb * f.ry[col + f.rvy_y.idx[I * kRmax + b]];
+        const T vb = (T)f.rvy_y.w[I * kRmax + b];
+        if (vb != T(0)) sy += va * vb * f.ry[col + f.rvy_y.idx[I * kRmax + b]];
       }
     }
   }
@@ -468,33 +483,38 @@ __device__ __forceinline__ void d_restrict(const LevelDev& f, const LevelDev& cl
   cl.fy[c] = sy;
 }
 // fine u += P e at fine cell c
-__device__ __forceinline__ void d_prolong(const LevelDev& f, const LevelDev& cl, int64_t c) {
+template <class T>
+__device__ __forceinline__ void d_prolong(const LevelDev<T>& f, const LevelDev<T>& cl, int64_t c) {
   const int32_t i = (int32_t)(c % f.ny), j = (int32_t)(c / f.ny);
-  float sx = 0.f, sy = 0.f;
+  T sx = 0, sy = 0;
   for (int a = 0; a < 2; ++a)
     for (int b = 0; b < 2; ++b) {
-      const float w1 = f.pvx_x.w[2 * j + a] * f.pvx_y.w[2 * i + b];
-      if (w1 != 0.f) sx += w1 * cl.ux[(int64_t)f.pvx_x.idx[2 * j + a] * cl.ny + f.pvx_y.idx[2 * i + b]];
-      const float w2 = f.pvy_x.w[2 * j + a] * f.pvy_y.w[2 * i + b];
-      if (w2 != 0.f) sy += w2 * cl.uy[(int64_t)f.pvy_x.idx[2 * j + a] * cl.ny + f.pvy_y.idx[2 * i + b]];
+      const T w1 = (T)f.pvx_x.w[2 * j + a] * (T)f.pvx_y.w[2 * i + b];
+      if (w1 != T(0)) sx += w1 * cl.ux[(int64_t)f.pvx_x.idx[2 * j + a] * cl.ny + f.pvx_y.idx[2 * i + b]];
+      const T w2 = (T)f.pvy_x.w[2 * j + a] * (T)f.pvy_y.w[2 * i + b];
+      if (w2 != T(0)) sy += w2 * cl.uy[(int64_t)f.pvy_x.idx[2 * j + a] * cl.ny + f.pvy_y.idx[2 * i + b]];
     }
   f.ux[c] += sx;
   f.uy[c] += sy;
 }
 
-__global__ void k_rbgs(LevelDev v, int comp, int color) {
+template <class T>
+__global__ void k_rbgs(LevelDev<T> v, int comp, int color) {
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (t < rb_count(v)) d_rbgs(v, t, comp, color);
 }
-__global__ void k_resid(LevelDev v) {
+template <class T>
+__global__ void k_resid(LevelDev<T> v) {
   const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (c < v.nc) d_resid(v, c);
 }
-__global__ void k_restrict(LevelDev f, LevelDev cl) {
+template <class T>
+__global__ void k_restrict(LevelDev<T> f, LevelDev<T> cl) {
   const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (c < cl.nc) d_restrict(f, cl, c);
 }
-__global__ void k_prolong(LevelDev f, LevelDev cl) {
+template <class T>
+__global__ void k_prolong(LevelDev<T> f, LevelDev<T> cl) {
   const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (c < f.nc) d_prolong(f, cl, c);
 }
@@ -502,9 +522,10 @@ __global__ void k_prolong(LevelDev f, LevelDev cl) {
 // The V-cycle below level l0 (all levels small) in one thread block:
 // every step is a block-stride loop followed by __syncthreads().
 constexpr int kCoarseThreads = 1024;
-__global__ void __launch_bounds__(kCoarseThreads) k_coarse_cycle(const LevelDev* __restrict__ lv, int l0, int nl,
-                                                                  int sweeps, const float* __restrict__ Ainv, int n) {
-  auto smooth = [&](const LevelDev& v, bool pre) {
+template <class T>
+__global__ void __launch_bounds__(kCoarseThreads) k_coarse_cycle(const LevelDev<T>* __restrict__ lv, int l0, int nl,
+                                                                  int sweeps, const T* __restrict__ Ainv, int n) {
+  auto smooth = [&](const LevelDev<T>& v, bool pre) {
     const int64_t cnt = rb_count(v);
     for (int s = 0; s < sweeps; ++s)
       for (int k = 0; k < 4; ++k) {
@@ -516,21 +537,21 @@ __global__ void __launch_bounds__(kCoarseThreads) k_coarse_cycle(const LevelDev*
       }
   };
   for (int l = l0; l < nl - 1; ++l) {
-    const LevelDev v = lv[l];
-    for (int64_t c = threadIdx.x; c < v.nc; c += blockDim.x) { v.ux[c] = 0.f; v.uy[c] = 0.f; }
+    const LevelDev<T> v = lv[l];
+    for (int64_t c = threadIdx.x; c < v.nc; c += blockDim.x) { v.ux[c] = T(0); v.uy[c] = T(0); }
     __syncthreads();
     smooth(v, true);
     for (int64_t c = threadIdx.x; c < v.nc; c += blockDim.x) d_resid(v, c);
     __syncthreads();
-    const LevelDev w = lv[l + 1];
+    const LevelDev<T> w = lv[l + 1];
     for (int64_t c = threadIdx.x; c < w.nc; c += blockDim.x) d_restrict(v, w, c);
     __syncthreads();
   }
   {  // coarsest: u = Ainv f
-    const LevelDev cl = lv[nl - 1];
+    const LevelDev<T> cl = lv[nl - 1];
     const int half = n / 2;
     for (int r = threadIdx.x; r < n; r += blockDim.x) {
-      float s = 0.f;
+      T s = 0;
       for (int k = 0; k < half; ++k) s += Ainv[(int64_t)r * n + k] * cl.fx[k];
       for (int k = 0; k < half; ++k) s += Ainv[(int64_t)r * n + half + k] * cl.fy[k];
       if (r < half) cl.ux[r] = s; else cl.uy[r - half] = s;
@@ -538,8 +559,8 @@ __global__ void __launch_bounds__(kCoarseThreads) k_coarse_cycle(const LevelDev*
     __syncthreads();
   }
   for (int l = nl - 2; l >= l0; --l) {
-    const LevelDev v = lv[l];
-    const LevelDev w = lv[l + 1];
+    const LevelDev<T> v = lv[l];
+    const LevelDev<T> w = lv[l + 1];
     for (int64_t c = threadIdx.x; c < v.nc; c += blockDim.x) d_prolong(v, w, c);
     __syncthreads();
     smooth(v, false);
@@ -547,39 +568,55 @@ __global__ void __launch_bounds__(kCoarseThreads) k_coarse_cycle(const LevelDev*
 }
 
 // Preconditioner input, on the scaled residual rhat (r = rhat ./ w):
-// z_p = prep r_p, stored scaled and rounded to FP32 (zhat_p = fl32(z_p / w_p));
-// level-0 right-hand side f = r_u - L_up z_p (FP32).
+// z_p = prep r_p, stored scaled (zhat_p = z_p / w_p); level-0 right-hand side f = r_u - L_up z_p.
+// FP32 method: zhat_p is rounded to FP32 (Zk, float) and zt holds the same value in FP64.
+// FP64 method: zt = zhat_p and Zk (double) repeats it.
+template <class T>
 __global__ void k_prec_in(const double* __restrict__ coef, const double* __restrict__ rhat,
                           const double* __restrict__ w, const double* __restrict__ prep, double* __restrict__ zt,
-                          float* __restrict__ Zk, float* __restrict__ fx, float* __restrict__ fy, int32_t nx,
-                          int32_t ny) {
+                          void* __restrict__ Zk, T* __restrict__ fx, T* __restrict__ fy, int32_t nx, int32_t ny) {
   const int64_t nc = (int64_t)nx * ny;
   const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= nc) return;
   const int32_t i = (int32_t)(c % ny), j = (int32_t)(c / ny);
   auto z = [&](int64_t k) { return prep[k] * (rhat[2 * nc + k] / w[2 * nc + k]); };
   const double zc = z(c);
-  const float zs = (float)(zc / w[2 * nc + c]);
-  Zk[2 * nc + c] = zs;
-  zt[2 * nc + c] = (double)zs;
+  if (sizeof(T) == 4) {
+    const float zs = (float)(zc / w[2 * nc + c]);
+    static_cast<float*>(Zk)[2 * nc + c] = zs;
+    zt[2 * nc + c] = (double)zs;
+  } else {
+    const double zs = zc / w[2 * nc + c];
+    static_cast<double*>(Zk)[2 * nc + c] = zs;
+    zt[2 * nc + c] = zs;
+  }
   double gx = coef[9 * nc + c] * zc;
   if (j < nx - 1) gx += coef[10 * nc + c] * z(c + ny);
   double gy = coef[20 * nc + c] * zc;
   if (i < ny - 1) gy += coef[21 * nc + c] * z(c + 1);
-  fx[c] = (float)(rhat[c] / w[c] - gx);
-  fy[c] = (float)(rhat[nc + c] / w[nc + c] - gy);
+  fx[c] = (T)(rhat[c] / w[c] - gx);
+  fy[c] = (T)(rhat[nc + c] / w[nc + c] - gy);
 }
-// Preconditioner output: zhat_u = fl32(u / w_u), kept in FP32 (Zk) and FP64 (zt).
-__global__ void k_prec_out(const float* __restrict__ ux, const float* __restrict__ uy, const double* __restrict__ w,
-                           double* __restrict__ zt, float* __restrict__ Zk, int64_t nc) {
+// Preconditioner output: zhat_u = u / w_u (rounded to FP32 in the FP32 method) into Zk and zt.
+template <class T>
+__global__ void k_prec_out(const T* __restrict__ ux, const T* __restrict__ uy, const double* __restrict__ w,
+                           double* __restrict__ zt, void* __restrict__ Zk, int64_t nc) {
   const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= nc) return;
-  const float zx = (float)((double)ux[c] / w[c]);
-  const float zy = (float)((double)uy[c] / w[nc + c]);
-  Zk[c] = zx;
-  Zk[nc + c] = zy;
-  zt[c] = (double)zx;
-  zt[nc + c] = (double)zy;
+  if (sizeof(T) == 4) {
+    const float zx = (float)((double)ux[c] / w[c]);
+    const float zy = (float)((double)uy[c] / w[nc + c]);
+    static_cast<float*>(Zk)[c] = zx;
+    static_cast<float*>(Zk)[nc + c] = zy;
+    zt[c] = (double)zx;
+    zt[nc + c] = (double)zy;
+  } else {
+    const double zx = (double)ux[c] / w[c], zy = (double)uy[c] / w[nc + c];
+    static_cast<double*>(Zk)[c] = zx;
+    static_cast<double*>(Zk)[nc + c] = zy;
+    zt[c] = zx;
+    zt[nc + c] = zy;
+  }
 }
 
 // Learned stage: zt += a z2, rounded once to FP32 (Zk) so that zt and Zk stay equal.
@@ -706,14 +743,16 @@ struct StokesState {
   std::vector<void*> allocs;         // system + solver buffers
   std::vector<void*> level_allocs;   // multigrid buffers
   std::vector<Level> levels;
-  float* Ainv = nullptr;
-  LevelDev* lv_dev = nullptr;        // device copies of the level descriptors
+  bool mg64 = false;                 // V-cycle arithmetic: FP32 (mixed method) or FP64 (plain method)
+  void* Ainv = nullptr;              // coarsest inverse (FP32 or FP64)
+  void* lv_dev = nullptr;            // device copies of the level descriptors
   int n_dense = 0;
   double *w = nullptr, *prep = nullptr;  // scaling and pressure factor
   // FGMRES workspace
   int m = 0;
   double *V = nullptr, *r = nullptr, *t = nullptr, *xs = nullptr, *bs = nullptr, *zp = nullptr, *zt = nullptr;
-  float* Z = nullptr;                // preconditioned directions, stored in FP32
+  float* Z = nullptr;                // preconditioned directions: FP32 (mixed method) ...
+  double* Zd = nullptr;              // ... or FP64 (plain method)
   double *partial = nullptr, *dots = nullptr, *hdev = nullptr;
   int nb_dot = 0;
   double* il = nullptr;              // interleaved staging vector (N)
@@ -739,6 +778,18 @@ int dupload(eb_ctx* c, std::vector<void*>& owner, T** p, const std::vector<T>& h
   if (rc) return rc;
   if (!h.empty()) EB_CK(c, cudaMemcpyAsync(*p, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice, c->stream));
   return EB_OK;
+}
+
+int dalloc_bytes(eb_ctx* c, std::vector<void*>& owner, void** p, size_t bytes) {
+  EB_CK(c, cudaMalloc(p, std::max<size_t>(bytes, 16)));
+  owner.push_back(*p);
+  return EB_OK;
+}
+// h converted to the level arithmetic and uploaded
+int upload_real(eb_ctx* c, std::vector<void*>& owner, void** p, const std::vector<double>& h, bool fp64) {
+  if (fp64) return dupload(c, owner, reinterpret_cast<double**>(p), h);
+  std::vector<float> f(h.begin(), h.end());
+  return dupload(c, owner, reinterpret_cast<float**>(p), f);
 }
 
 void free_levels(StokesState* st) {
@@ -804,7 +855,8 @@ int read_b2(eb_ctx* c, B2* b) {
 }
 
 // Build the level geometry, buffers and transfer tables (host), for the current grid and b2.
-LevelDev level_dev(const Level& v);
+template <class T>
+LevelDev<T> level_dev(const Level& v);
 
 int setup_levels(eb_ctx* c, StokesState* st, const B2& b2) {
   free_levels(st);
@@ -832,28 +884,29 @@ int setup_levels(eb_ctx* c, StokesState* st, const B2& b2) {
   if (st->n_dense > 2048)
     return eb_fail(c, EB_BAD_INPUT, "grid aspect ratio too large for the multigrid hierarchy (coarsest level has " +
                                         std::to_string(L.back().nc) + " cells)");
+  const size_t es = st->mg64 ? sizeof(double) : sizeof(float);
   for (int l = 0; l < nlev; ++l) {
     Level& v = L[l];
     const size_t nc = (size_t)v.nc;
     int rc;
-    if ((rc = dalloc(c, st->level_allocs, &v.X, 9 * nc)) || (rc = dalloc(c, st->level_allocs, &v.Y, 9 * nc)) ||
-        (rc = dalloc(c, st->level_allocs, &v.ux, nc)) || (rc = dalloc(c, st->level_allocs, &v.uy, nc)) ||
-        (rc = dalloc(c, st->level_allocs, &v.fx, nc)) || (rc = dalloc(c, st->level_allocs, &v.fy, nc)) ||
-        (rc = dalloc(c, st->level_allocs, &v.rx, nc)) || (rc = dalloc(c, st->level_allocs, &v.ry, nc)) ||
-        (rc = dalloc(c, st->level_allocs, &v.etas, (size_t)(v.nx + 1) * (v.ny + 1))) ||
-        (rc = dalloc(c, st->level_allocs, &v.etan, nc)))
+    auto A = [&](void** p, size_t n) { return dalloc_bytes(c, st->level_allocs, p, n * es); };
+    if ((rc = A(&v.X, 9 * nc)) || (rc = A(&v.Y, 9 * nc)) || (rc = A(&v.ux, nc)) || (rc = A(&v.uy, nc)) ||
+        (rc = A(&v.fx, nc)) || (rc = A(&v.fy, nc)) || (rc = A(&v.rx, nc)) || (rc = A(&v.ry, nc)) ||
+        (rc = A(&v.etas, (size_t)(v.nx + 1) * (v.ny + 1))) || (rc = A(&v.etan, nc)))
       return rc;
-    // spacing tables (FP32) for the rediscretisation
+    // spacing tables for the rediscretisation, in the level arithmetic
     std::vector<double> gxc, sxc, gyc, syc;
     stag(v.x, gxc, sxc);
     stag(v.y, gyc, syc);
-    std::vector<float> xs(v.nx), ys(v.ny), xsc(v.nx + 1), ysc(v.ny + 1);
-    for (int32_t j = 0; j < v.nx; ++j) xs[j] = (float)(v.x[j + 1] - v.x[j]);
-    for (int32_t i = 0; i < v.ny; ++i) ys[i] = (float)(v.y[i + 1] - v.y[i]);
-    for (int32_t j = 0; j <= v.nx; ++j) xsc[j] = (float)sxc[j];
-    for (int32_t i = 0; i <= v.ny; ++i) ysc[i] = (float)syc[i];
-    if ((rc = dupload(c, st->level_allocs, &v.xstp, xs)) || (rc = dupload(c, st->level_allocs, &v.ystp, ys)) ||
-        (rc = dupload(c, st->level_allocs, &v.xstpc, xsc)) || (rc = dupload(c, st->level_allocs, &v.ystpc, ysc)))
+    std::vector<double> xs(v.nx), ys(v.ny), xsc(v.nx + 1), ysc(v.ny + 1);
+    for (int32_t j = 0; j < v.nx; ++j) xs[j] = v.x[j + 1] - v.x[j];
+    for (int32_t i = 0; i < v.ny; ++i) ys[i] = v.y[i + 1] - v.y[i];
+    for (int32_t j = 0; j <= v.nx; ++j) xsc[j] = sxc[j];
+    for (int32_t i = 0; i <= v.ny; ++i) ysc[i] = syc[i];
+    if ((rc = upload_real(c, st->level_allocs, &v.xstp, xs, st->mg64)) ||
+        (rc = upload_real(c, st->level_allocs, &v.ystp, ys, st->mg64)) ||
+        (rc = upload_real(c, st->level_allocs, &v.xstpc, xsc, st->mg64)) ||
+        (rc = upload_real(c, st->level_allocs, &v.ystpc, ysc, st->mg64)))
       return rc;
   }
   // transfer tables between level l (fine) and l+1 (coarse)
@@ -904,45 +957,60 @@ int setup_levels(eb_ctx* c, StokesState* st, const B2& b2) {
         return rc;
     }
   }
-  int rc = dalloc(c, st->level_allocs, &st->Ainv, (size_t)st->n_dense * st->n_dense);
+  int rc = dalloc_bytes(c, st->level_allocs, &st->Ainv, (size_t)st->n_dense * st->n_dense * es);
   if (rc) return rc;
-  std::vector<LevelDev> lv;
-  for (const Level& v : L) lv.push_back(level_dev(v));
-  if ((rc = dupload(c, st->level_allocs, &st->lv_dev, lv))) return rc;
+  if (st->mg64) {
+    std::vector<LevelDev<double>> lv;
+    for (const Level& v : L) lv.push_back(level_dev<double>(v));
+    LevelDev<double>* d = nullptr;
+    if ((rc = dupload(c, st->level_allocs, &d, lv))) return rc;
+    st->lv_dev = d;
+  } else {
+    std::vector<LevelDev<float>> lv;
+    for (const Level& v : L) lv.push_back(level_dev<float>(v));
+    LevelDev<float>* d = nullptr;
+    if ((rc = dupload(c, st->level_allocs, &d, lv))) return rc;
+    st->lv_dev = d;
+  }
   EB_CK(c, cudaStreamSynchronize(c->stream));
   return EB_OK;
 }
 
 // Per-solve operators: level 0 from the FP64 stencil, coarse viscosity and stencils, coarsest inverse.
-int refresh_levels(eb_ctx* c, StokesState* st, const B2& b2) {
+template <class T>
+int refresh_levels_t(eb_ctx* c, StokesState* st, const B2& b2) {
   std::vector<Level>& L = st->levels;
   const StokesSystem& s = st->sys;
+  auto P = [](void* p) { return static_cast<T*>(p); };
   EB_PROF(c, "k_mg_setup");
-  k_level0<<<nblk(s.nc), kB, 0, c->stream>>>(s.coef, L[0].X, L[0].Y, s.nc);
+  k_level0<T><<<nblk(s.nc), kB, 0, c->stream>>>(s.coef, P(L[0].X), P(L[0].Y), s.nc);
   EB_LAUNCHED(c);
   EB_PROF(c, "k_mg_setup");
-  k_to_f32<<<nblk((int64_t)c->xnum * c->ynum), kB, 0, c->stream>>>(c->gf[EB_G_ETAS0], L[0].etas, (int64_t)c->xnum * c->ynum);
+  k_to_real<T><<<nblk((int64_t)c->xnum * c->ynum), kB, 0, c->stream>>>(c->gf[EB_G_ETAS0], P(L[0].etas),
+                                                                     (int64_t)c->xnum * c->ynum);
   EB_LAUNCHED(c);
   EB_PROF(c, "k_mg_setup");
-  k_to_f32<<<nblk(s.nc), kB, 0, c->stream>>>(c->gf[EB_G_ETAN0], L[0].etan, s.nc);
+  k_to_real<T><<<nblk(s.nc), kB, 0, c->stream>>>(c->gf[EB_G_ETAN0], P(L[0].etan), s.nc);
   EB_LAUNCHED(c);
   for (size_t l = 1; l < L.size(); ++l) {
     Level& f = L[l - 1];
     Level& v = L[l];
     const int64_t n = std::max<int64_t>((int64_t)(v.nx + 1) * (v.ny + 1), v.nc);
     EB_PROF(c, "k_mg_setup");
-    k_coarsen_eta<<<nblk(n), kB, 0, c->stream>>>(f.etas, f.etan, f.nx, f.ny, v.etas, v.etan, v.nx, v.ny, v.kx, v.ky);
+    k_coarsen_eta<T><<<nblk(n), kB, 0, c->stream>>>(P(f.etas), P(f.etan), f.nx, f.ny, P(v.etas), P(v.etan), v.nx, v.ny,
+                                                    v.kx, v.ky);
     EB_LAUNCHED(c);
     EB_PROF(c, "k_mg_setup");
-    k_redisc<<<nblk(v.nc), kB, 0, c->stream>>>(v.nx, v.ny, v.etas, v.etan, v.xstp, v.ystp, v.xstpc, v.ystpc, b2, v.X, v.Y);
+    k_redisc<T><<<nblk(v.nc), kB, 0, c->stream>>>(v.nx, v.ny, P(v.etas), P(v.etan), P(v.xstp), P(v.ystp), P(v.xstpc),
+                                                  P(v.ystpc), b2, P(v.X), P(v.Y));
     EB_LAUNCHED(c);
   }
   // coarsest velocity block as a dense matrix on the host, inverted in FP64
   const Level& cl = L.back();
   const int nc = (int)cl.nc, n = 2 * nc;
-  std::vector<float> hX(9 * (size_t)nc), hY(9 * (size_t)nc);
-  EB_CK(c, cudaMemcpyAsync(hX.data(), cl.X, hX.size() * sizeof(float), cudaMemcpyDeviceToHost, c->stream));
-  EB_CK(c, cudaMemcpyAsync(hY.data(), cl.Y, hY.size() * sizeof(float), cudaMemcpyDeviceToHost, c->stream));
+  std::vector<T> hX(9 * (size_t)nc), hY(9 * (size_t)nc);
+  EB_CK(c, cudaMemcpyAsync(hX.data(), cl.X, hX.size() * sizeof(T), cudaMemcpyDeviceToHost, c->stream));
+  EB_CK(c, cudaMemcpyAsync(hY.data(), cl.Y, hY.size() * sizeof(T), cudaMemcpyDeviceToHost, c->stream));
   EB_CK(c, cudaStreamSynchronize(c->stream));
   std::vector<double> A((size_t)n * n, 0.0), inv;
   const int32_t ny = cl.ny, nx = cl.nx;
@@ -973,20 +1041,23 @@ int refresh_levels(eb_ctx* c, StokesState* st, const B2& b2) {
     if (hd) put(r, cc + 1, Ys(8));
   }
   if (!invert_dense(A, n, inv)) return eb_fail(c, EB_NAN, "coarsest multigrid operator is singular");
-  std::vector<float> invf(inv.size());
-  for (size_t k = 0; k < inv.size(); ++k) invf[k] = (float)inv[k];
-  EB_CK(c, cudaMemcpyAsync(st->Ainv, invf.data(), invf.size() * sizeof(float), cudaMemcpyHostToDevice, c->stream));
+  std::vector<T> invf(inv.size());
+  for (size_t k = 0; k < inv.size(); ++k) invf[k] = (T)inv[k];
+  EB_CK(c, cudaMemcpyAsync(st->Ainv, invf.data(), invf.size() * sizeof(T), cudaMemcpyHostToDevice, c->stream));
   EB_CK(c, cudaStreamSynchronize(c->stream));
   return EB_OK;
 }
+int refresh_levels(eb_ctx* c, StokesState* st, const B2& b2) {
+  return st->mg64 ? refresh_levels_t<double>(c, st, b2) : refresh_levels_t<float>(c, st, b2);
+}
 
-// One V-cycle from level 0's f into level 0's u (launches on c->stream).
-// One V-cycle from level 0's f into level 0's u (launches on c->stream).
-LevelDev level_dev(const Level& v) {
-  LevelDev d;
+template <class T>
+LevelDev<T> level_dev(const Level& v) {
+  LevelDev<T> d;
+  auto P = [](void* p) { return static_cast<T*>(p); };
   d.nx = v.nx; d.ny = v.ny; d.nc = v.nc;
-  d.X = v.X; d.Y = v.Y;
-  d.ux = v.ux; d.uy = v.uy; d.fx = v.fx; d.fy = v.fy; d.rx = v.rx; d.ry = v.ry;
+  d.X = P(v.X); d.Y = P(v.Y);
+  d.ux = P(v.ux); d.uy = P(v.uy); d.fx = P(v.fx); d.fy = P(v.fy); d.rx = P(v.rx); d.ry = P(v.ry);
   d.pvx_x = v.pvx_x; d.pvx_y = v.pvx_y; d.pvy_x = v.pvy_x; d.pvy_y = v.pvy_y;
   d.rvx_x = v.rvx_x; d.rvx_y = v.rvx_y; d.rvy_x = v.rvy_x; d.rvy_y = v.rvy_y;
   return d;
@@ -995,32 +1066,34 @@ LevelDev level_dev(const Level& v) {
 // One V-cycle from level 0's f into level 0's u (launches on c->stream).  Levels
 // at or below l0 (the first with at most kCoarseCells cells) run in one block.
 constexpr int64_t kCoarseCells = 8192;
+template <class T>
 int vcycle_launch(eb_ctx* c, StokesState* st, int sweeps, int64_t* nk) {
   std::vector<Level>& L = st->levels;
   const int nl = (int)L.size();
   int l0 = 0;
   while (l0 < nl - 1 && L[l0].nc > kCoarseCells) ++l0;
-  auto rb = [&](const LevelDev& v, int comp, int color) {
+  auto rb = [&](const LevelDev<T>& v, int comp, int color) {
     const int64_t cnt = (int64_t)v.nx * ((v.ny + 1) / 2);
-    k_rbgs<<<nblk(cnt), kB, 0, c->stream>>>(v, comp, color);
+    k_rbgs<T><<<nblk(cnt), kB, 0, c->stream>>>(v, comp, color);
     ++*nk;
   };
   for (int l = 0; l < l0; ++l) {
-    const LevelDev v = level_dev(L[l]);
-    EB_CK(c, cudaMemsetAsync(L[l].ux, 0, v.nc * sizeof(float), c->stream));
-    EB_CK(c, cudaMemsetAsync(L[l].uy, 0, v.nc * sizeof(float), c->stream));
+    const LevelDev<T> v = level_dev<T>(L[l]);
+    EB_CK(c, cudaMemsetAsync(L[l].ux, 0, v.nc * sizeof(T), c->stream));
+    EB_CK(c, cudaMemsetAsync(L[l].uy, 0, v.nc * sizeof(T), c->stream));
     for (int s = 0; s < sweeps; ++s) { rb(v, 0, 0); rb(v, 0, 1); rb(v, 1, 0); rb(v, 1, 1); }
-    k_resid<<<nblk(v.nc), kB, 0, c->stream>>>(v);
-    const LevelDev w = level_dev(L[l + 1]);
-    k_restrict<<<nblk(w.nc), kB, 0, c->stream>>>(v, w);
+    k_resid<T><<<nblk(v.nc), kB, 0, c->stream>>>(v);
+    const LevelDev<T> w = level_dev<T>(L[l + 1]);
+    k_restrict<T><<<nblk(w.nc), kB, 0, c->stream>>>(v, w);
     *nk += 2;
   }
-  k_coarse_cycle<<<1, kCoarseThreads, 0, c->stream>>>(st->lv_dev, l0, nl, sweeps, st->Ainv, st->n_dense);
+  k_coarse_cycle<T><<<1, kCoarseThreads, 0, c->stream>>>(static_cast<const LevelDev<T>*>(st->lv_dev), l0, nl, sweeps,
+                                                        static_cast<const T*>(st->Ainv), st->n_dense);
   ++*nk;
   for (int l = l0 - 1; l >= 0; --l) {
-    const LevelDev v = level_dev(L[l]);
-    const LevelDev w = level_dev(L[l + 1]);
-    k_prolong<<<nblk(v.nc), kB, 0, c->stream>>>(v, w);
+    const LevelDev<T> v = level_dev<T>(L[l]);
+    const LevelDev<T> w = level_dev<T>(L[l + 1]);
+    k_prolong<T><<<nblk(v.nc), kB, 0, c->stream>>>(v, w);
     ++*nk;
     for (int s = 0; s < sweeps; ++s) { rb(v, 1, 1); rb(v, 1, 0); rb(v, 0, 1); rb(v, 0, 0); }
   }
@@ -1035,7 +1108,7 @@ int capture_vcycle(eb_ctx* c, StokesState* st, int sweeps) {
   c->prof.on = false;
   int64_t nk = 0;
   EB_CK(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
-  int rc = vcycle_launch(c, st, sweeps, &nk);
+  int rc = st->mg64 ? vcycle_launch<double>(c, st, sweeps, &nk) : vcycle_launch<float>(c, st, sweeps, &nk);
   cudaGraph_t g = nullptr;
   cudaError_t e = cudaStreamEndCapture(c->stream, &g);
   c->prof.on = prof;
@@ -1047,20 +1120,31 @@ int capture_vcycle(eb_ctx* c, StokesState* st, int sweeps) {
   return EB_OK;
 }
 
-// zhat = W^-1 M^-1 W^-1 rhat (rhat: SoA FP64 of 3 nc), rounded to FP32: kept in Zk (the
-// stored direction) and zt (its FP64 copy, the input of the operator product).
-int precondition(eb_ctx* c, StokesState* st, const double* rhat, double* zt, float* Zk) {
+// zhat = W^-1 M^-1 W^-1 rhat (rhat: SoA FP64 of 3 nc), kept in Zk (the stored direction:
+// FP32 in the mixed method, FP64 in the plain one) and zt (its FP64 value, the input of the
+// operator product).
+int precondition(eb_ctx* c, StokesState* st, const double* rhat, double* zt, void* Zk) {
   const StokesSystem& s = st->sys;
   Level& v = st->levels[0];
   EB_PROF(c, "k_precond");
-  k_prec_in<<<nblk(s.nc), kB, 0, c->stream>>>(s.coef, rhat, st->w, st->prep, zt, Zk, v.fx, v.fy, s.nx, s.ny);
+  if (st->mg64)
+    k_prec_in<double><<<nblk(s.nc), kB, 0, c->stream>>>(s.coef, rhat, st->w, st->prep, zt, Zk,
+                                                        static_cast<double*>(v.fx), static_cast<double*>(v.fy), s.nx, s.ny);
+  else
+    k_prec_in<float><<<nblk(s.nc), kB, 0, c->stream>>>(s.coef, rhat, st->w, st->prep, zt, Zk,
+                                                       static_cast<float*>(v.fx), static_cast<float*>(v.fy), s.nx, s.ny);
   EB_LAUNCHED(c);
   EB_PROF(c, "vcycle_graph");
   EB_CK(c, cudaGraphLaunch(st->gexec, c->stream));
   c->launches += st->graph_kernels - 1;
   EB_LAUNCHED(c);
   EB_PROF(c, "k_precond");
-  k_prec_out<<<nblk(s.nc), kB, 0, c->stream>>>(v.ux, v.uy, st->w, zt, Zk, s.nc);
+  if (st->mg64)
+    k_prec_out<double><<<nblk(s.nc), kB, 0, c->stream>>>(static_cast<double*>(v.ux), static_cast<double*>(v.uy), st->w,
+                                                         zt, Zk, s.nc);
+  else
+    k_prec_out<float><<<nblk(s.nc), kB, 0, c->stream>>>(static_cast<float*>(v.ux), static_cast<float*>(v.uy), st->w, zt,
+                                                        Zk, s.nc);
   EB_LAUNCHED(c);
   return EB_OK;
 }
@@ -1088,7 +1172,7 @@ int apply_scaled(eb_ctx* c, StokesState* st, const double* x, double* y) {
 }
 
 int ensure_solver(eb_ctx* c, StokesState* st, int m) {
-  if (st->m == m && st->V) return EB_OK;
+  if (st->m == m && st->V && (st->mg64 ? st->Zd != nullptr : st->Z != nullptr)) return EB_OK;
   // (re)allocate the Krylov workspace
   auto drop = [&](void* p) {
     if (!p) return;
@@ -1097,13 +1181,16 @@ int ensure_solver(eb_ctx* c, StokesState* st, int m) {
   };
   drop(st->V);
   drop(st->Z);
+  drop(st->Zd);
   st->V = nullptr;
   st->Z = nullptr;
+  st->Zd = nullptr;
   const size_t n3 = 3 * (size_t)st->sys.nc;
   st->m = m;
   st->nb_dot = kDotBlocks;
   int rc;
-  if ((rc = dalloc(c, st->allocs, &st->V, (size_t)(m + 2) * n3)) || (rc = dalloc(c, st->allocs, &st->Z, (size_t)m * n3)))
+  if ((rc = dalloc(c, st->allocs, &st->V, (size_t)(m + 2) * n3))) return rc;
+  if ((rc = st->mg64 ? dalloc(c, st->allocs, &st->Zd, (size_t)m * n3) : dalloc(c, st->allocs, &st->Z, (size_t)m * n3)))
     return rc;
   if (!st->r) {
     if ((rc = dalloc(c, st->allocs, &st->r, n3)) || (rc = dalloc(c, st->allocs, &st->t, n3)) ||
@@ -1120,7 +1207,7 @@ int ensure_solver(eb_ctx* c, StokesState* st, int m) {
 // The learned stage after the V-cycle (z = zt): t = v - A z, z2 = NN(t), and z += a z2 with
 // the step a = <t, A z2> / |A z2|^2 that minimises |t - a A z2|; kept when a > 0, i.e. when
 // it lowers the preconditioner residual (the multigrid alone otherwise).
-int learned_stage(eb_ctx* c, StokesState* st, const double* v, double* zt, float* Zk) {
+int learned_stage(eb_ctx* c, StokesState* st, const double* v, double* zt, float* Zk) {  // FP32 method only
   const auto t0 = std::chrono::steady_clock::now();
   const StokesSystem& s = st->sys;
   const int64_t n3 = 3 * s.nc;
@@ -1155,9 +1242,13 @@ int learned_stage(eb_ctx* c, StokesState* st, const double* v, double* zt, float
   return EB_OK;
 }
 
-// Scaling, multigrid hierarchy and captured V-cycle of the current system.
-int prepare(eb_ctx* c, StokesState* st, int sweeps, int m) {
+// Scaling, multigrid hierarchy and captured V-cycle of the current system, in FP32 or FP64.
+int prepare(eb_ctx* c, StokesState* st, int sweeps, int m, bool fp64) {
   int rc;
+  if (st->mg64 != fp64) {  // the level arrays and the stored directions change type
+    free_levels(st);
+    st->mg64 = fp64;
+  }
   B2 b2;
   if ((rc = ensure_solver(c, st, m)) || (rc = read_b2(c, &b2))) return rc;
   if (st->levels.empty() || std::memcmp(&b2, &st->b2_levels, sizeof(B2)) != 0) {
@@ -1201,7 +1292,9 @@ extern "C" int eb_solve_stokes_system(eb_ctx* c, const eb_solve_opts* o, eb_solv
   if (opt.learned && !nn_trained(c))
     return eb_fail(c, EB_NOT_READY, "learned stage requested but eb_learned_train has not run");
   const bool use_nn = opt.learned != 0 && opt.method != 1;
-  if ((rc = prepare(c, st, opt.mg_sweeps, m))) return rc;
+  if (opt.precision != 0 && opt.precision != 1) return eb_fail(c, EB_BAD_INPUT, "precision must be 0 (mixed) or 1 (FP64)");
+  if (use_nn && opt.precision == 1) return eb_fail(c, EB_BAD_INPUT, "the learned stage runs with the mixed method");
+  if ((rc = prepare(c, st, opt.mg_sweeps, m, opt.precision == 1))) return rc;
   // bhat = W R, xhat = W^-1 S0
   EB_PROF(c, "k_axpy");
   k_mul<<<nblk(n3), kB, 0, c->stream>>>(st->bs, s.rhs, st->w, n3, 0);
@@ -1253,14 +1346,15 @@ extern "C" int eb_solve_stokes_system(eb_ctx* c, const eb_solve_opts* o, eb_solv
       EB_PROF(c, "k_axpy");
       k_bicg_p<<<nblk(n3), kB, 0, c->stream>>>(p, r, v, beta, omega, n3);
       EB_LAUNCHED(c);
-      if ((rc = precondition(c, st, p, ph, st->Z)) || (rc = apply_scaled(c, st, ph, v))) return rc;
+      void* z0 = st->mg64 ? (void*)st->Zd : (void*)st->Z;
+      if ((rc = precondition(c, st, p, ph, z0)) || (rc = apply_scaled(c, st, ph, v))) return rc;
       double rv;
       if ((rc = mdot(c, st, rh0, 0, 1, v, &rv))) return rc;
       alpha = rho / rv;
       EB_PROF(c, "k_axpy");
       k_bicg_s<<<nblk(n3), kB, 0, c->stream>>>(sv, r, v, alpha, n3);
       EB_LAUNCHED(c);
-      if ((rc = precondition(c, st, sv, sh, st->Z)) || (rc = apply_scaled(c, st, sh, tv))) return rc;
+      if ((rc = precondition(c, st, sv, sh, z0)) || (rc = apply_scaled(c, st, sh, tv))) return rc;
       double st2[2];
       if ((rc = mdot(c, st, sv, n3, 2, tv, st2))) return rc;  // s.t, t.t
       omega = st2[1] > 0.0 ? st2[0] / st2[1] : 0.0;
@@ -1295,10 +1389,10 @@ extern "C" int eb_solve_stokes_system(eb_ctx* c, const eb_solve_opts* o, eb_solv
     int k = 0;
     for (; k < m && it < opt.max_iters; ++k) {
       double* vk = st->V + (size_t)k * n3;
-      float* zk = st->Z + (size_t)k * n3;
+      void* zk = st->mg64 ? (void*)(st->Zd + (size_t)k * n3) : (void*)(st->Z + (size_t)k * n3);
       double* w = st->V + (size_t)(k + 1) * n3;
       if ((rc = precondition(c, st, vk, st->zt, zk))) return rc;
-      if (use_nn && (rc = learned_stage(c, st, vk, st->zt, zk))) return rc;
+      if (use_nn && (rc = learned_stage(c, st, vk, st->zt, static_cast<float*>(zk)))) return rc;
       // Shifted Arnoldi: with a good preconditioner A z_k is close to v_k, so the slot holds
       // d = A z_k - v_k and the projection starts from d (h_kk gets the 1 back below); the
       // cancellation that classical Gram-Schmidt suffers is then measured against |d|.
@@ -1370,7 +1464,11 @@ extern "C" int eb_solve_stokes_system(eb_ctx* c, const eb_solve_opts* o, eb_solv
     for (int q = 0; q < k; ++q) negy[q] = -y[q];
     EB_CK(c, cudaMemcpyAsync(st->hdev, negy.data(), k * sizeof(double), cudaMemcpyHostToDevice, c->stream));
     EB_PROF(c, "k_maxpy");
-    k_maxpy_f32<<<nblk(n3), kB, 0, c->stream>>>(st->xs, st->Z, n3, st->hdev, k, n3);
+    if (st->mg64)
+      k_maxpy<<<(unsigned)((n3 + kAxTile - 1) / kAxTile), kAxThreads, (size_t)std::max(k, 1) * sizeof(double),
+                c->stream>>>(st->xs, st->Zd, n3, st->hdev, k, n3);
+    else
+      k_maxpy_f32<<<nblk(n3), kB, 0, c->stream>>>(st->xs, st->Z, n3, st->hdev, k, n3);
     EB_LAUNCHED(c);
     EB_CK(c, cudaStreamSynchronize(c->stream));
   }
@@ -1743,8 +1841,8 @@ int stokes_nn_ready(eb_ctx* c, int sweeps) {
   int rc = need_system(c, true);
   if (rc) return rc;
   StokesState* st = c->st;
-  return prepare(c, st, sweeps, std::max(st->m, 1));
+  return prepare(c, st, sweeps, std::max(st->m, 1), false);
 }
 int stokes_nn_apply(eb_ctx* c, const double* x, double* y) { return apply_scaled(c, c->st, x, y); }
-int stokes_nn_precondition(eb_ctx* c, const double* r, double* z) { return precondition(c, c->st, r, z, c->st->Z); }
+int stokes_nn_precondition(eb_ctx* c, const double* r, double* z) { return precondition(c, c->st, r, z, c->st->Z); }  // FP32 method
 int stokes_nn_dot(eb_ctx* c, const double* a, const double* b, double* out) { return mdot(c, c->st, a, 0, 1, b, out); }

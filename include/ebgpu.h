@@ -309,6 +309,8 @@ typedef struct eb_solve_opts {
   int32_t learned;           /* 1: after each V-cycle, the learned stage (eb_learned_train) adds its
                                 correction when that lowers the preconditioner residual (FGMRES only;
                                 Stokes only)                                                        */
+  int32_t precision;         /* 0: mixed (FP32 V-cycle, FP32 stored directions, FP64 FGMRES);
+                                1: plain FP64 (V-cycle and directions in FP64; Stokes only)          */
 } eb_solve_opts;
 
 typedef struct eb_solve_report {

@@ -109,10 +109,11 @@ def test_operator_apply_matches_coo_product(eb, case):
     mic.close()
 
 
-def solve_case(eb, model, rtol, method="fgmres"):
+def solve_case(eb, model, rtol, method="fgmres", precision="mixed"):
     o = oracle_for(model)
     mic = gpu_ctx(eb, model)
-    rep = mic.solve_viscoelastic_stokes_continuity_equations(rtol=rtol, max_iters=4000, method=method)
+    rep = mic.solve_viscoelastic_stokes_continuity_equations(rtol=rtol, max_iters=4000, method=method,
+                                                            precision=precision)
     S = mic.download_stokes_vector("solution")
     return o, mic, rep, S
 
@@ -128,11 +129,13 @@ def test_solve_reaches_metric_tolerance(eb, case, method):
     mic.close()
 
 
-@pytest.mark.parametrize("method", ["fgmres", "bicgstab"])
+@pytest.mark.parametrize("method,precision", [("fgmres", "mixed"), ("bicgstab", "mixed"), ("fgmres", "fp64"),
+                                              ("bicgstab", "fp64")])
 @pytest.mark.parametrize("case", ["rift_small", "sinking_block"])
-def test_solution_matches_superlu(eb, case, method):
+def test_solution_matches_superlu(eb, case, method, precision):
+    """Both the mixed method (FP32 V-cycle and stored directions) and the plain FP64 method."""
     model = marker_model(eb, case)
-    o, mic, rep, S = solve_case(eb, model, 1e-11, method)
+    o, mic, rep, S = solve_case(eb, model, 1e-11, method, precision)
     assert rep["status"] == 0, rep
     S_ref = o.solve_direct()
     for comp in range(3):
@@ -323,4 +326,18 @@ def test_circles_box_matches_superlu(eb):
     for k in range(3):
         err = np.max(np.abs(S[k::3] - S_ref[k::3])) / np.max(np.abs(S_ref[k::3]))
         assert err < 1e-6, (k, err)
+    mic.close()
+
+
+def test_mixed_and_fp64_methods_share_one_context(eb):
+    """Switching the V-cycle precision rebuilds the hierarchy; both reach the tolerance and the
+    FP64 V-cycle is no weaker a preconditioner than the FP32 one."""
+    model = marker_model(eb, "rift_small")
+    o, mic, rep32, S = solve_case(eb, model, 1e-8)
+    rep64 = mic.solve_viscoelastic_stokes_continuity_equations(rtol=1e-8, precision="fp64")
+    rep32b = mic.solve_viscoelastic_stokes_continuity_equations(rtol=1e-8, precision="mixed")
+    for r in (rep32, rep64, rep32b):
+        assert r["status"] == 0 and r["rel_residual"] <= 1e-8, r
+    assert rep64["iterations"] <= rep32["iterations"] + 2
+    assert rep32b["iterations"] == rep32["iterations"]
     mic.close()
