@@ -535,10 +535,11 @@ class MarkerInCell:
     def recycle_markers(self, matid_sticky_air: int, matid_sticky_water: int, matid_asthenosphere: int,
                         xsize: float, ysize: float, velocity_y_upper: float, velocity_y_lower: float,
                         temperature_bottom: float, seed: int, counter: int, iuse_random_fric: int = 0,
-                        delta_fric_coef: float = 0.0) -> tuple:
-        """MarkerRecycle.recycle_markers! for the extension models (types/Extension.jl:14-129);
-        returns (nrecycle_air, nrecycle_subsurface)."""
-        p = _abi.RecycleParams(1, matid_sticky_air, matid_sticky_water, matid_asthenosphere, xsize, ysize,
+                        delta_fric_coef: float = 0.0, recycle_type: int = 1) -> tuple:
+        """MarkerRecycle.recycle_markers!: recycle_type 1 extension models (types/Extension.jl:14-129),
+        2 extension without bottom inflow (types/ExtensionNoBottomInflow.jl), 3 channel
+        (types/Channel.jl); returns (nrecycle_air, nrecycle_subsurface)."""
+        p = _abi.RecycleParams(recycle_type, matid_sticky_air, matid_sticky_water, matid_asthenosphere, xsize, ysize,
                                velocity_y_upper, velocity_y_lower, temperature_bottom, iuse_random_fric,
                                delta_fric_coef, seed, counter)
         na, ns = C.c_int64(), C.c_int64()

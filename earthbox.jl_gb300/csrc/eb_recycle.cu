@@ -55,9 +55,11 @@ __host__ __device__ inline void uniforms(uint64_t seed, int64_t step, uint32_t s
 }
 
 struct RecycleK {
+  int32_t type;                                 // 1 extension, 2 extension without bottom inflow, 3 channel
   int16_t sticky_air, sticky_water, asth;
   double xsize, ysize, disp_top, disp_bottom;  // disp_top = |vyu dt|, disp_bottom = -|vyl dt|
   double t_top, t_bottom, p_reset;
+  double gridy_max, ysize_grid;                 // channel: gridy_b[ynum], gridy_b[ynum] - gridy_b[1]
   double fric_air, fric_asth;                   // mat_plastic[., 3]
   int32_t random_fric;
   double delta_fric;
@@ -66,12 +68,21 @@ struct RecycleK {
 };
 
 __device__ __forceinline__ bool sticky(int16_t m, const RecycleK& p) { return m == p.sticky_air || m == p.sticky_water; }
+// the markers a recycling type moves: outside the domain, or (channel) below the grid
+__device__ __forceinline__ bool selected(const DevMarkers& mk, int64_t m, const RecycleK& p) {
+  if (m >= mk.M) return false;
+  return p.type == 3 ? mk.y[m] > p.gridy_max : mk.inside[m] != 1;
+}
+// sticky rank (air/water positions): extension only; the other types treat every marker alike
+__device__ __forceinline__ bool sticky_sel(const DevMarkers& mk, int64_t m, const RecycleK& p) {
+  return p.type == 1 && sticky(mk.matid[m], p);
+}
 
 // per block: number of outside markers and of outside sticky markers
 __global__ void k_recycle_count(DevMarkers mk, RecycleK p, int32_t* __restrict__ counts, int32_t nblocks) {
   const int64_t m = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  const bool out = m < mk.M && mk.inside[m] != 1;
-  const bool st = out && sticky(mk.matid[m], p);
+  const bool out = selected(mk, m, p);
+  const bool st = out && sticky_sel(mk, m, p);
   const int n_out = __syncthreads_count(out), n_st = __syncthreads_count(st);
   if (threadIdx.x == 0) {
     counts[blockIdx.x] = n_out;
@@ -84,8 +95,8 @@ __global__ void k_recycle_apply(DevMarkers mk, RecycleK p, const int32_t* __rest
                                 int64_t n_air, int64_t* __restrict__ list, int8_t* __restrict__ flags) {
   __shared__ int32_t s_out[kB / 32], s_st[kB / 32];
   const int64_t m = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  const bool out = m < mk.M && mk.inside[m] != 1;
-  const bool st = out && sticky(mk.matid[m], p);
+  const bool out = selected(mk, m, p);
+  const bool st = out && sticky_sel(mk, m, p);
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const unsigned b_out = __ballot_sync(0xffffffffu, out), b_st = __ballot_sync(0xffffffffu, st);
   if (lane == 0) { s_out[w] = __popc(b_out); s_st[w] = __popc(b_st); }
@@ -96,7 +107,37 @@ __global__ void k_recycle_apply(DevMarkers mk, RecycleK p, const int32_t* __rest
   const unsigned below = (1u << lane) - 1u;
   r_out += __popc(b_out & below);
   r_st += __popc(b_st & below);
+  if (p.type == 3) {
+    // Channel.execute_recycle_steps (types/Channel.jl:20-54): wrap to the top, shift T
+    mk.y[m] = mk.y[m] - p.ysize_grid;
+    mk.tk[m] = mk.tk[m] + p.t_top - p.t_bottom;
+    list[r_out] = m + 1;
+    flags[r_out] = 1;
+    return;
+  }
   double ux, uy;
+  if (p.type == 2) {
+    // ExtensionNoBottomInflow (types/ExtensionNoBottomInflow.jl:25-123): every outside marker
+    // re-enters in the top band, one uniform for both coordinates, as sticky air
+    uniforms(p.seed, p.step, 0u, r_out, ux, uy);
+    mk.y[m] = ux * p.disp_top;
+    mk.x[m] = 0.0 + ux * p.xsize;
+    list[r_out] = m + 1;
+    flags[r_out] = 0;
+    mk.matid[m] = p.sticky_air;
+    mk.tk[m] = p.t_top;
+    mk.pr[m] = 0.0;
+    mk.sxx[m] = 0.0; mk.sxy[m] = 0.0;
+    mk.exx[m] = 0.0; mk.exy[m] = 0.0;
+    mk.eta[m] = 0.0;
+    mk.sr_ratio[m] = 0.0;
+    mk.gii[m] = 0.0; mk.sp[m] = 0.0; mk.srp[m] = 0.0;
+    mk.melt[m] = 0.0;
+    mk.pfailure[m] = 0.0f;
+    mk.fric_ini[m] = p.fric_air;
+    mk.fric[m] = p.fric_air;
+    return;
+  }
   if (st && n_air > 0) {
     uniforms(p.seed, p.step, 0u, r_st, ux, uy);
     mk.x[m] = 0.0 + ux * p.xsize;
@@ -151,7 +192,8 @@ extern "C" int eb_recycle_markers(eb_ctx* c, const eb_recycle_params* rp, int64_
                                   int64_t* nrecycle_subsurface) {
   if (!c || !rp) return EB_BAD_INPUT;
   if (!c->have_grid || !c->have_params || !c->have_mats) return eb_fail(c, EB_NOT_READY, "grid, parameters and materials must be set");
-  if (rp->recycle_type != 1) return eb_fail(c, EB_BAD_INPUT, "recycle_type must be 1 (extension models)");
+  if (rp->recycle_type < 1 || rp->recycle_type > 3)
+    return eb_fail(c, EB_BAD_INPUT, "recycle_type must be 1 (extension), 2 (extension without bottom inflow) or 3 (channel)");
   const int64_t nmat = c->mats.nmat;
   for (int64_t id : {(int64_t)rp->matid_sticky_air, (int64_t)rp->matid_sticky_water, (int64_t)rp->matid_asthenosphere})
     if (id < 1 || id > nmat) return eb_fail(c, EB_BAD_INPUT, "recycle material id outside the material table");
@@ -172,12 +214,15 @@ extern "C" int eb_recycle_markers(eb_ctx* c, const eb_recycle_params* rp, int64_
   EB_CK(c, cudaMalloc(&d_counts, 2 * (size_t)nblocks * sizeof(int32_t)));
   // mat_plastic[., 3] (sin of the initial friction angle) of the two reset materials
   std::vector<double>& mp = c->h_mat_plastic;
-  RecycleK p{(int16_t)rp->matid_sticky_air, (int16_t)rp->matid_sticky_water, (int16_t)rp->matid_asthenosphere,
-             rp->xsize, rp->ysize, std::fabs(rp->velocity_y_upper * c->P.timestep),
+  // top band: |vyu dt| (extension), vyu dt with its sign (no bottom inflow)
+  const double disp_top = rp->recycle_type == 2 ? rp->velocity_y_upper * c->P.timestep
+                                                : std::fabs(rp->velocity_y_upper * c->P.timestep);
+  RecycleK p{rp->recycle_type, (int16_t)rp->matid_sticky_air, (int16_t)rp->matid_sticky_water,
+             (int16_t)rp->matid_asthenosphere, rp->xsize, rp->ysize, disp_top,
              -std::fabs(rp->velocity_y_lower * c->P.timestep), c->P.temperature_top, rp->temperature_bottom,
-             3300.0 * 9.81 * c->h_gy.back(), mp[2 * nmat + rp->matid_sticky_air - 1],
-             mp[2 * nmat + rp->matid_asthenosphere - 1], rp->iuse_random_fric, rp->delta_fric_coef, rp->seed,
-             rp->counter};
+             3300.0 * 9.81 * c->h_gy.back(), c->h_gy.back(), c->h_gy.back() - c->h_gy.front(),
+             mp[2 * nmat + rp->matid_sticky_air - 1], mp[2 * nmat + rp->matid_asthenosphere - 1],
+             rp->iuse_random_fric, rp->delta_fric_coef, rp->seed, rp->counter};
   k_recycle_count<<<nblocks, kB, 0, c->stream>>>(dev_markers(c), p, d_counts, nblocks);
   c->launches++;
   std::vector<int32_t> h(2 * (size_t)nblocks);
@@ -220,6 +265,7 @@ extern "C" int eb_recycle_markers(eb_ctx* c, const eb_recycle_params* rp, int64_
   if (e != cudaSuccess) return eb_cuda(c, e, "marker recycling");
   c->recycle_n = n_out;
   c->located = false;  // markers moved
+  if (rp->recycle_type == 2) n_air = n_out;  // every recycled marker becomes sticky air
   if (nrecycle_air) *nrecycle_air = n_air;
   if (nrecycle_subsurface) *nrecycle_subsurface = n_out - n_air;
   return EB_OK;

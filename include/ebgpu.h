@@ -552,7 +552,14 @@ int eb_update_model_time_step_using_displacement_limit(eb_ctx* ctx, double marke
  * context does not hold (serpentinisation, extracted melt, stratigraphic age) are reset by
  * the caller for the markers eb_recycled_markers lists.                            */
 typedef struct eb_recycle_params {
-  int32_t recycle_type;            /* 1: extension models (fixed boundaries, asymmetric, depth dependent) */
+  int32_t recycle_type;            /* 1: extension models (fixed boundaries, asymmetric, depth dependent)
+                                      (types/Extension.jl:14-129); 2: extension without bottom inflow
+                                      (types/ExtensionNoBottomInflow.jl:8-123: every outside marker
+                                      re-enters in the top band as sticky air, one uniform for x and y,
+                                      band vyu dt with its sign); 3: channel (types/Channel.jl:20-54:
+                                      markers below gridy_b[ynum] move up by the grid height and
+                                      their temperature by temperature_top - temperature_bottom; the
+                                      inside flags are not used)                                     */
   int32_t matid_sticky_air, matid_sticky_water, matid_asthenosphere;  /* material ids                 */
   double  xsize, ysize;            /* model size (m); the domain starts at x = y = 0                    */
   double  velocity_y_upper, velocity_y_lower;  /* vyu, vyl (m/s): band widths |v dt|                   */

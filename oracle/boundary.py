@@ -123,3 +123,34 @@ def recycle_extension(mk: dict, matid_sticky_air, matid_sticky_water, matid_asth
                                   _p(d), C.c_int64(mp.shape[0]), _p(mp), C.c_int64(iuse_random_fric),
                                   C.c_uint64(seed), C.c_int64(step), _p(lst), _p(fl), C.byref(n_air))
     return out, lst[:n].copy(), fl[:n].copy(), n_air.value
+
+
+def recycle_no_bottom_inflow(mk: dict, matid_sticky_air, xsize, velocity_y_upper, timestep, temperature_top,
+                             mat_plastic, seed, step) -> tuple:
+    """ExtensionNoBottomInflow recycling; returns (fields, 1-based indices, flags)."""
+    M = len(mk["x"])
+    out = {k: np.array(mk[k], dtype=np.float64, copy=True) for k in RECYCLE_FIELDS}
+    out["matid"] = np.array(mk["matid"], dtype=np.int16, copy=True)
+    out["pfailure"] = np.array(mk["pfailure"], dtype=np.float32, copy=True)
+    inside = np.ascontiguousarray(mk["inside"], dtype=np.int8)
+    ptrs = (C.c_void_p * len(RECYCLE_FIELDS))(*[out[k].ctypes.data for k in RECYCLE_FIELDS])
+    d = np.array([xsize, velocity_y_upper, timestep, temperature_top], np.float64)
+    mp = np.asfortranarray(mat_plastic, dtype=np.float64)
+    lst = np.zeros(max(M, 1), np.int64)
+    fl = np.zeros(max(M, 1), np.int8)
+    lib().o_recycle_no_bottom_inflow.restype = C.c_int64
+    n = lib().o_recycle_no_bottom_inflow(C.c_int64(M), _p(inside), _p(out["matid"]), ptrs, _p(out["pfailure"]),
+                                         C.c_int16(matid_sticky_air), _p(d), C.c_int64(mp.shape[0]), _p(mp),
+                                         C.c_uint64(seed), C.c_int64(step), _p(lst), _p(fl))
+    return out, lst[:n].copy(), fl[:n].copy()
+
+
+def recycle_channel(y, tk, gridy_min, gridy_max, temperature_top, temperature_bottom) -> tuple:
+    """Channel recycling; returns (y, tk, 1-based indices)."""
+    y = np.array(y, dtype=np.float64, copy=True)
+    tk = np.array(tk, dtype=np.float64, copy=True)
+    lst = np.zeros(max(len(y), 1), np.int64)
+    lib().o_recycle_channel.restype = C.c_int64
+    n = lib().o_recycle_channel(C.c_int64(len(y)), _p(y), _p(tk), C.c_double(gridy_min), C.c_double(gridy_max),
+                                C.c_double(temperature_top), C.c_double(temperature_bottom), _p(lst))
+    return y, tk, lst[:n].copy()

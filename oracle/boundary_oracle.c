@@ -15,6 +15,8 @@
  *        InitializeMarkerRecycling.jl:26-108; positions, Coordinates.jl:60-153; property
  *        resets, ResetMarkers.jl:24-290; reset pressure, PressureReset.jl:20-26), with the
  *        reference's rand() replaced by the Philox-4x32-10 stream of o_recycle_uniforms
+ *   o_recycle_no_bottom_inflow      marker_recycle/types/ExtensionNoBottomInflow.jl:25-123
+ *   o_recycle_channel               marker_recycle/types/Channel.jl:20-54
  *
  * Grids are column-major (rows, cols).  Julia's x^2 and x^3 of a Float64 literal power
  * are x*x and x*x*x.
@@ -229,4 +231,52 @@ int64_t o_recycle_extension(int64_t M, const int8_t* inside, int16_t* matid, dou
   }
   *n_air = nair;
   return nout;
+}
+
+/* ExtensionNoBottomInflow: every outside marker (marker order, rank j) re-enters at
+ * y = u_j vyu dt, x = 0 + u_j xsize with ONE uniform u_j (stream 0, index j), and is reset as
+ * sticky air at temperature_top (reset_marker! defaults: zero pressure, stress, strain rate,
+ * strain, melt, viscosity; fric = mat_plastic[air, 3]).  d[]: xsize, vyu, dt, temperature_top. */
+int64_t o_recycle_no_bottom_inflow(int64_t M, const int8_t* inside, int16_t* matid, double** f, float* pfailure,
+                                   int16_t air, const double* d, int64_t nmat, const double* mat_plastic,
+                                   uint64_t seed, int64_t step, int64_t* list, int8_t* flags) {
+  const double displacement = d[1] * d[2];
+  int64_t n = 0;
+  for (int64_t m = 0; m < M; ++m) {
+    if (inside[m] == 1) continue;
+    double u, unused;
+    o_recycle_uniforms(seed, step, 0u, n, &u, &unused);
+    f[R_Y][m] = u * displacement;
+    f[R_X][m] = 0.0 + u * d[0];
+    matid[m] = air;
+    f[R_TK][m] = d[3];
+    f[R_PR][m] = 0.0;
+    f[R_SXX][m] = f[R_SXY][m] = 0.0;
+    f[R_EXX][m] = f[R_EXY][m] = 0.0;
+    f[R_SR_RATIO][m] = 0.0;
+    f[R_GII][m] = f[R_SP][m] = f[R_SRP][m] = 0.0;
+    f[R_MELT][m] = 0.0;
+    f[R_ETA][m] = 0.0;
+    pfailure[m] = 0.0f;
+    f[R_FRIC_INI][m] = f[R_FRIC][m] = mat_plastic[2 * nmat + (air - 1)];
+    list[n] = m + 1;
+    flags[n] = 0;
+    ++n;
+  }
+  return n;
+}
+
+/* Channel: markers with y > gridy_b[ynum] move up by the grid height and their temperature
+ * changes by temperature_top - temperature_bottom (evaluated as (T + T_top) - T_bottom). */
+int64_t o_recycle_channel(int64_t M, double* y, double* tk, double gridy_min, double gridy_max, double t_top,
+                          double t_bottom, int64_t* list) {
+  const double ysize = gridy_max - gridy_min;
+  int64_t n = 0;
+  for (int64_t m = 0; m < M; ++m)
+    if (y[m] > gridy_max) {
+      y[m] = y[m] - ysize;
+      tk[m] = tk[m] + t_top - t_bottom;
+      list[n++] = m + 1;
+    }
+  return n;
 }

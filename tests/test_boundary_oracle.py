@@ -196,3 +196,44 @@ def test_recycle_oracle_matches_reference_loops(eb, B, water, rf):
     y = got["y"][idx - 1]
     assert np.all(y[fl == 0] >= 0) and np.all(y[fl == 0] < 2e-10 * 3.15e11)
     assert np.all(y[fl == 1] <= 160e3) and np.all(y[fl == 1] > 160e3 - 3e-10 * 3.15e11)
+
+
+def test_recycle_no_bottom_inflow_oracle_matches_reference_loops(eb, B):
+    """ExtensionNoBottomInflow.jl:25-123 written out: outside markers in order, one rand() for
+    both coordinates, reset as sticky air."""
+    rng = np.random.default_rng(8)
+    M = 1200
+    mk = {k: rng.uniform(-1.0, 1.0, M) for k in B.RECYCLE_FIELDS}
+    mk["matid"] = rng.integers(1, 5, M).astype(np.int16)
+    mk["pfailure"] = rng.uniform(0, 1, M).astype(np.float32)
+    mk["inside"] = np.where(rng.random(M) < 0.9, 1, -1).astype(np.int8)
+    mp = np.asfortranarray(rng.uniform(0, 1, (4, 6)))
+    seed, step, vyu, dt = 99, 4, -3e-10, 3.15e11
+    got, idx, fl = B.recycle_no_bottom_inflow(mk, 1, 500e3, vyu, dt, 273.0, mp, seed, step)
+    want = {k: np.array(v, copy=True) for k, v in mk.items()}
+    outside = [i for i in range(M) if mk["inside"][i] != 1]
+    for j, i in enumerate(outside):
+        u = B.recycle_uniforms(seed, step, 0, j)[0]
+        want["y"][i] = u * (vyu * dt)
+        want["x"][i] = 0.0 + u * 500e3
+        want["matid"][i] = 1
+        want["tk"][i] = 273.0
+        for k in ("pr", "sxx", "sxy", "exx", "exy", "sr_ratio", "gii", "strain_plastic", "strain_rate_plastic",
+                  "meltfrac", "eta"):
+            want[k][i] = 0.0
+        want["pfailure"][i] = np.float32(0.0)
+        want["fric_ini"][i] = want["fric"][i] = mp[0, 2]
+    assert np.array_equal(idx, np.array(outside) + 1) and np.all(fl == 0)
+    for k in (*B.RECYCLE_FIELDS, "matid", "pfailure"):
+        assert np.array_equal(got[k], want[k]), k
+
+
+def test_recycle_channel_oracle(B):
+    rng = np.random.default_rng(9)
+    y = rng.uniform(-5e3, 165e3, 1000)
+    tk = rng.uniform(300, 1600, 1000)
+    y2, tk2, idx = B.recycle_channel(y, tk, 0.0, 160e3, 273.0, 1603.0)
+    moved = y > 160e3
+    assert np.array_equal(idx, np.nonzero(moved)[0] + 1)
+    assert np.array_equal(y2[moved], y[moved] - 160e3) and np.array_equal(y2[~moved], y[~moved])
+    assert np.array_equal(tk2[moved], tk[moved] + 273.0 - 1603.0) and np.array_equal(tk2[~moved], tk[~moved])

@@ -118,3 +118,47 @@ def test_recycle_markers_match_oracle(eb, water, random_fric):
     mic.get_marker_inside_flags()
     assert np.all(mic.download_marker("inside") == 1)
     mic.close()
+
+
+def test_recycle_no_bottom_inflow_and_channel_match_oracle(eb):
+    """Recycling types 2 (extension without bottom inflow) and 3 (channel) against the oracle."""
+    from oracle import boundary as B
+    model = eb.synthetic.config("rift_small")
+    g = model.grid
+    p = model.params
+    rng = np.random.default_rng(23)
+    # type 2: markers pushed out through the sides and the bottom
+    mic = eb.MarkerInCell(0)
+    mic.load_model(model)
+    M = model.marknum
+    x, y = mic.download_marker("x"), mic.download_marker("y")
+    out = rng.random(M) < 0.03
+    x = np.where(out & (rng.random(M) < 0.5), g.xmax + rng.uniform(1.0, 3e3, M), x)
+    y = np.where(out & (x <= g.xmax), g.ymax + rng.uniform(1.0, 3e3, M), y)
+    mic.upload_marker("x", x)
+    mic.upload_marker("y", y)
+    mic.get_marker_inside_flags()
+    mk = {k: mic.download_marker(k) for k in (*B.RECYCLE_FIELDS, "matid", "pfailure", "inside")}
+    want, widx, wfl = B.recycle_no_bottom_inflow(mk, 1, g.xmax, -2e-10, p["timestep"], p["temperature_top"],
+                                                 model.mats.mat_plastic, 77, 3)
+    nair, nsub = mic.recycle_markers(1, 1, 4, g.xmax, g.ymax, -2e-10, 0.0, 1603.0, 77, 3, recycle_type=2)
+    assert (nair, nsub) == (len(widx), 0) and nair > 50
+    idx, fl = mic.recycled_markers()
+    assert np.array_equal(idx, widx) and np.array_equal(fl, wfl)
+    for k in (*B.RECYCLE_FIELDS, "matid", "pfailure"):
+        assert np.array_equal(mic.download_marker(k), want[k]), k
+    mic.close()
+    # type 3: markers below the grid wrap to the top
+    mic = eb.MarkerInCell(0)
+    mic.load_model(model)
+    y = mic.download_marker("y")
+    y = np.where(rng.random(M) < 0.05, g.ymax + rng.uniform(1.0, 2e3, M), y)
+    mic.upload_marker("y", y)
+    tk = mic.download_marker("tk")
+    wy, wtk, widx = B.recycle_channel(y, tk, g.gridy_b[0], g.gridy_b[-1], p["temperature_top"], 1603.0)
+    nair, nsub = mic.recycle_markers(1, 1, 4, g.xmax, g.ymax, 0.0, 0.0, 1603.0, 0, 0, recycle_type=3)
+    assert (nair, nsub) == (0, len(widx)) and nsub > 50
+    idx, _ = mic.recycled_markers()
+    assert np.array_equal(idx, widx)
+    assert np.array_equal(mic.download_marker("y"), wy) and np.array_equal(mic.download_marker("tk"), wtk)
+    mic.close()
