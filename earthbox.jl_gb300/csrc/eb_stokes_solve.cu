@@ -1064,8 +1064,10 @@ LevelDev<T> level_dev(const Level& v) {
 }
 
 // One V-cycle from level 0's f into level 0's u (launches on c->stream).  Levels
-// at or below l0 (the first with at most kCoarseCells cells) run in one block.
-constexpr int64_t kCoarseCells = 8192;
+// at or below l0 (the first with at most kCoarseCells cells) run in one block.  Measured on
+// the 40M-marker rift (V-cycle time per solve): 8192 -> 107 ms, 2048 -> 95 ms, 1024 -> 98 ms,
+// 256 -> 102 ms (one 1024-thread block is slower than launches above a few thousand cells).
+constexpr int64_t kCoarseCells = 2048;
 template <class T>
 int vcycle_launch(eb_ctx* c, StokesState* st, int sweeps, int64_t* nk) {
   std::vector<Level>& L = st->levels;
