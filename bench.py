@@ -86,6 +86,7 @@ def parse():
     ap.add_argument("--no-stokes", action="store_true")
     ap.add_argument("--no-heat", action="store_true")
     ap.add_argument("--no-learned", action="store_true")
+    ap.add_argument("--no-rheology", action="store_true")
     ap.add_argument("--learned-steps", type=int, default=200)
     ap.add_argument("--circles", action="store_true",
                     help="also time the circles_1025 Stokes benchmark (200 inclusions, 1e-10)")
@@ -625,6 +626,7 @@ def main():
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         for _ in range(2):
+            mic.update_marker_rheology_and_viscoplastic_viscosity(True)
             step()
             mic.calc_viscoelastic_terms()
             mic.viscoelastic_rhs()
@@ -638,12 +640,46 @@ def main():
         torch.cuda.synchronize()
         timestep = {"metric": "per-timestep wall time", "value": (time.perf_counter() - t0) / 2, "unit": "s/step",
                     "higher_is_better": False,
-                    "includes": "marker cycle (transfer + RK4), Stokes step (solve to 1e-8), heat step"}
+                    "includes": "marker rheology (failure, flow viscosity, viscoplastic, yield; one fused pass), "
+                                "marker cycle (transfer + RK4), Stokes step (solve to 1e-8), heat step"}
         if stokes is not None and "plain_fp64" in stokes:
             # the same step with the plain FP64 multigrid solve in place of the mixed one
             plain = timestep["value"] - stokes["value"] + stokes["plain_fp64"]["value"]
             timestep["plain_fp64_mg_step"] = plain
             timestep["speedup_vs_plain_fp64"] = plain / timestep["value"]
+
+    # the per-marker rheology of TimeLoop.jl:222-223 (failure properties, composite-creep
+    # flow viscosity by bisection, viscoplastic viscosity, Drucker-Prager yielding) as one
+    # fused pass, against the two reference calls
+    rheology = None
+    if not args.no_rheology:
+        import torch
+        for _ in range(2):
+            mic.update_marker_rheology_and_viscoplastic_viscosity(True)
+        torch.cuda.synchronize()
+        mic.profile_enable(True)
+        for _ in range(3):
+            mic.update_marker_rheology_and_viscoplastic_viscosity(True)
+        pf = mic.profile()
+        for _ in range(3):
+            mic.update_marker_rheology()
+            mic.update_marker_viscoplastic_viscosity(True)
+        pt = mic.profile()
+        mic.profile_enable(False)
+        t_f = pf["k_rheology"][0] / pf["k_rheology"][1]
+        t_two = sum(pt[k][0] - pf.get(k, (0.0, 0))[0] for k in ("k_failure", "k_flow_viscosity", "k_viscoplastic",
+                                                                "k_yield") if k in pt) / 3
+        # reads inside, matid, strain_plastic, fric_ini, sxx, sxy, exx, exy, gii, pr, sr_ratio, tk,
+        # pfailure; writes cohesion, fric, eta_flow, preexp, eta, pfailure (yielding markers also
+        # rewrite sxx, sxy)
+        bpm = 1 + 2 + 10 * 8 + 4 + 5 * 8 + 4
+        peak, peak_kind = peaks()
+        rheology = {"metric": "markers/s (rheology: failure, flow viscosity, viscoplastic, yield)",
+                    "value": M / (t_f * 1e-3), "unit": "markers/s", "ms": t_f, "two_calls_ms": t_two,
+                    "bytes_per_marker": bpm,
+                    "roofline": {"bound": "fp64", "hbm_achieved": bpm * M / (t_f * 1e-3) / 1e9, "hbm_peak": peak,
+                                 "hbm_frac": bpm * M / (t_f * 1e-3) / 1e9 / peak, "peak_kind": peak_kind,
+                                 "note": "FP64 arithmetic bound: up to 20 bisection steps of exp/pow per marker"}}
 
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -655,7 +691,7 @@ def main():
                 "gpu_launches": launches, "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
                 "clocks": clk.summary(), "stokes": stokes, "stokes_learned": learned, "stokes_circles": stokes_circles,
                 "heat": heat,
-                "timestep": timestep,
+                "timestep": timestep, "rheology": rheology,
                 "kernels_ms": {k: round(v[0], 4) for k, v in sorted(kern.items(), key=lambda kv: -kv[1][0] * kv[1][1])},
                 "generate_s": round(t_gen, 2)}
         print(json.dumps(line))

@@ -242,6 +242,12 @@ class MarkerInCell:
         """Rheology.update_marker_viscoplastic_viscosity! (Rheology.jl:70-107)."""
         self._check(self._lib.eb_update_marker_viscoplastic_viscosity(self._ctx, int(bool(use_marker_plasticity))))
 
+    def update_marker_rheology_and_viscoplastic_viscosity(self, use_marker_plasticity: bool = True) -> None:
+        """Rheology.update_marker_rheology! then update_marker_viscoplastic_viscosity!
+        (TimeLoop.jl:222-223) as one fused marker pass (same results as the two calls)."""
+        self._check(self._lib.eb_update_marker_rheology_and_viscoplastic_viscosity(
+            self._ctx, int(bool(use_marker_plasticity))))
+
     def update_plastic_yielding(self) -> None:
         """MarkerPlasticity.update_plastic_yielding! (ViscoelasticForecast.jl:11-123)."""
         self._call("eb_update_plastic_yielding")

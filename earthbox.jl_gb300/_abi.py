@@ -235,7 +235,7 @@ ALL_SYMBOLS = [
     "eb_update_model_time_step_using_displacement_limit", "eb_checkpoint_write", "eb_checkpoint_read",
     "eb_recycle_markers", "eb_recycled_markers", "eb_recycle_uniforms", "eb_nn_gemm_bf16", "eb_nn_conv2d_bf16",
     "eb_learned_init", "eb_learned_train", "eb_learned_params", "eb_learned_state", "eb_learned_forward",
-    "eb_learned_loss_grad", "eb_learned_stats",
+    "eb_learned_loss_grad", "eb_learned_stats", "eb_update_marker_rheology_and_viscoplastic_viscosity",
 ] + ENTRY_POINTS + STOKES_ENTRY_POINTS + HEAT_ENTRY_POINTS
 
 _lib = None
@@ -301,6 +301,7 @@ def load(path: pathlib.Path | str | None = None) -> C.CDLL:
     lib.eb_recycle_uniforms.restype = None
     lib.eb_nn_gemm_bf16.argtypes = [C.c_int64, C.c_int32, C.c_int64, vp, vp, vp, C.c_int32]
     lib.eb_nn_conv2d_bf16.argtypes = [C.c_int32] * 7 + [vp, vp, vp, C.c_int32, vp, vp]
+    lib.eb_update_marker_rheology_and_viscoplastic_viscosity.argtypes = [vp, C.c_int]
     lib.eb_learned_init.argtypes = [vp, C.c_uint64]
     lib.eb_learned_train.argtypes = [vp, C.POINTER(LearnedOpts), C.POINTER(LearnedReport)]
     lib.eb_learned_params.argtypes = [vp, vp, C.c_int64, C.POINTER(C.c_int64), C.c_int32]

@@ -676,6 +676,11 @@ extern "C" int eb_update_marker_viscoplastic_viscosity(eb_ctx* c, int use_marker
   if (rc) return rc;
   return finish(c, launch_viscoplastic(c, use_marker_plasticity));
 }
+extern "C" int eb_update_marker_rheology_and_viscoplastic_viscosity(eb_ctx* c, int use_marker_plasticity) {
+  int rc = ready(c, true, false);
+  if (rc) return rc;
+  return finish(c, launch_rheology_fused(c, use_marker_plasticity));
+}
 extern "C" int eb_update_plastic_yielding(eb_ctx* c) {
   int rc = ready(c, true, false);
   if (rc) return rc;

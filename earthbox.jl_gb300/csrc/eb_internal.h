@@ -248,4 +248,5 @@ int launch_update_strain(eb_ctx* c);
 int launch_marker_tail(eb_ctx* c);
 int launch_rheology(eb_ctx* c);
 int launch_viscoplastic(eb_ctx* c, int use_marker_plasticity);
+int launch_rheology_fused(eb_ctx* c, int use_marker_plasticity);
 int launch_plastic_yielding(eb_ctx* c);

@@ -24,16 +24,28 @@ __device__ __forceinline__ double MATV(const double* t, int32_t nmat, int32_t m,
 }
 
 // Julia Float64^Float64 for the exponents on this path (2 -> x*x, 3 -> x*x*x, 1 -> x).
+// The flow-viscosity bisection evaluates a power law up to 20 times per marker and the FP64
+// pipe bounds the kernel (ncu: 86 % busy), so the other common exponents of the flow laws
+// (4, 3.5, 2.5, 1.5) are products and square roots, and any other exponent is
+// exp(y log x): within a few ulps of the correctly rounded power, like pow itself.
 __device__ __forceinline__ double jl_pow(double x, double y) {
   if (y == 2.0) return x * x;
   if (y == 3.0) return x * x * x;
   if (y == 1.0) return x;
+  if (x > 0.0 && x < INFINITY) {
+    if (y == 4.0) {
+      const double x2 = x * x;
+      return x2 * x2;
+    }
+    if (y == 3.5) return x * x * x * sqrt(x);
+    if (y == 2.5) return x * x * sqrt(x);
+    if (y == 1.5) return x * sqrt(x);
+    return exp(y * log(x));
+  }
   return pow(x, y);
 }
 
-__global__ void k_failure(DevMarkers mk, DevMats mt, int melt_damage) {
-  const int64_t m = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (m >= mk.M || mk.inside[m] != 1) return;
+__device__ __forceinline__ void d_failure(const DevMarkers& mk, const DevMats& mt, int melt_damage, int64_t m) {
   const int32_t id = mk.matid[m];
   const double strain = mk.sp[m], sfi_m = mk.fric_ini[m];
   const double ci = MATV(mt.plastic, mt.nmat, id, 1), cf = MATV(mt.plastic, mt.nmat, id, 2);
@@ -56,6 +68,11 @@ __global__ void k_failure(DevMarkers mk, DevMats mt, int melt_damage) {
   }
   mk.cohesion[m] = coh;
   mk.fric[m] = sf;
+}
+__global__ void k_failure(DevMarkers mk, DevMats mt, int melt_damage) {
+  const int64_t m = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= mk.M || mk.inside[m] != 1) return;
+  d_failure(mk, mt, melt_damage, m);
 }
 
 struct CreepRow {
@@ -100,9 +117,7 @@ struct RheoParams {
   int soft;
 };
 
-__global__ void k_flow_viscosity(DevMarkers mk, DevMats mt, RheoParams P) {
-  const int64_t m = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (m >= mk.M || mk.inside[m] != 1) return;
+__device__ __forceinline__ void d_flow_viscosity(const DevMarkers& mk, const DevMats& mt, const RheoParams& P, int64_t m) {
   const int32_t id = mk.matid[m];
   const int32_t ft = __ldg(&mt.flow_type[id - 1]);
   double eta = 0.0;
@@ -149,15 +164,23 @@ __global__ void k_flow_viscosity(DevMarkers mk, DevMats mt, RheoParams P) {
   mk.eta_flow[m] = eta;
   mk.preexp[m] = A;
 }
-
-__global__ void k_viscoplastic(DevMarkers mk, int64_t ntimestep, int64_t itype_global) {
+__global__ void k_flow_viscosity(DevMarkers mk, DevMats mt, RheoParams P) {
   const int64_t m = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (m >= mk.M || mk.inside[m] != 1) return;
+  d_flow_viscosity(mk, mt, P, m);
+}
+
+__device__ __forceinline__ void d_viscoplastic(const DevMarkers& mk, int64_t ntimestep, int64_t itype_global, int64_t m) {
   const double vf = mk.eta_flow[m];
   double vp = mk.eta[m];
   if (itype_global == 0) vp = vf;
   else if (itype_global == 1 && (ntimestep == 0 || vp == 0.0)) vp = vf;
   mk.eta[m] = vp;
+}
+__global__ void k_viscoplastic(DevMarkers mk, int64_t ntimestep, int64_t itype_global) {
+  const int64_t m = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= mk.M || mk.inside[m] != 1) return;
+  d_viscoplastic(mk, ntimestep, itype_global, m);
 }
 
 struct YieldParams {
@@ -167,9 +190,7 @@ struct YieldParams {
   int32_t id_air, id_wall, id_plate;
 };
 
-__global__ void k_yield(DevMarkers mk, DevMats mt, YieldParams P) {
-  const int64_t m = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (m >= mk.M || mk.inside[m] != 1) return;
+__device__ __forceinline__ void d_yield(const DevMarkers& mk, const DevMats& mt, const YieldParams& P, int64_t m) {
   const int32_t id = mk.matid[m];
   const double coh = mk.cohesion[m], sf = mk.fric[m];
   int yflag = 0;
@@ -215,6 +236,25 @@ __global__ void k_yield(DevMarkers mk, DevMats mt, YieldParams P) {
   }
   if (mk.pfailure[m] != 1.0f) mk.pfailure[m] = (float)yflag;
 }
+__global__ void k_yield(DevMarkers mk, DevMats mt, YieldParams P) {
+  const int64_t m = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= mk.M || mk.inside[m] != 1) return;
+  d_yield(mk, mt, P, m);
+}
+
+// Rheology.update_marker_rheology! followed by update_marker_viscoplastic_viscosity!
+// (TimeLoop.jl:222-223) in one pass: failure properties, flow viscosity, viscoplastic
+// viscosity and (marker plasticity) yielding of each marker, the same steps in the same order
+// as the four kernels above; the fields a step writes are read back by the next from L1.
+__global__ void k_rheology(DevMarkers mk, DevMats mt, int melt_damage, RheoParams R, int64_t ntimestep,
+                           int64_t itype_global, int yield, YieldParams Y) {
+  const int64_t m = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= mk.M || mk.inside[m] != 1) return;
+  d_failure(mk, mt, melt_damage, m);
+  d_flow_viscosity(mk, mt, R, m);
+  d_viscoplastic(mk, ntimestep, itype_global, m);
+  if (yield) d_yield(mk, mt, Y, m);
+}
 
 unsigned mblocks(const eb_ctx* c) { return (unsigned)((c->M + kBlock - 1) / kBlock); }
 
@@ -226,15 +266,23 @@ int ensure(eb_ctx* c, std::initializer_list<int> fs) {
   return EB_OK;
 }
 
+YieldParams yield_params(const eb_params& p) {
+  return YieldParams{p.ntimestep, p.timestep, p.y_sealevel, p.viscosity_min, p.viscosity_max, p.yield_stress_min,
+                     p.yield_stress_max, (int)(p.iuse_fluid_pressure_for_yield != 0),
+                     (int)(p.no_yielding_in_mobile_wall != 0), (int32_t)p.matid_sticky_air,
+                     (int32_t)p.matid_mobile_wall, (int32_t)p.matid_plate_extension};
+}
+RheoParams rheo_params(const eb_params& p) {
+  return RheoParams{p.timestep, p.temperature_top, p.viscosity_min, p.viscosity_max, p.powerlaw_stress_min,
+                    p.gas_constant, p.vsoftfac, (int)(p.iuse_viscous_strain_soft == 1)};
+}
+
 int yield_launch(eb_ctx* c) {
   int rc = ensure(c, {EB_M_INSIDE, EB_M_MATID, EB_M_COHESION, EB_M_FRIC, EB_M_ETA, EB_M_SXX, EB_M_SXY, EB_M_EXX,
                       EB_M_EXY, EB_M_SR_RATIO, EB_M_PR, EB_M_Y, EB_M_PFAILURE});
   if (rc) return rc;
   if (c->M == 0) return EB_OK;
-  const eb_params& p = c->P;
-  YieldParams Y{p.ntimestep, p.timestep, p.y_sealevel, p.viscosity_min, p.viscosity_max, p.yield_stress_min,
-                p.yield_stress_max, (int)(p.iuse_fluid_pressure_for_yield != 0), (int)(p.no_yielding_in_mobile_wall != 0),
-                (int32_t)p.matid_sticky_air, (int32_t)p.matid_mobile_wall, (int32_t)p.matid_plate_extension};
+  const YieldParams Y = yield_params(c->P);
   EB_PROF(c, "k_yield");
   k_yield<<<mblocks(c), kBlock, 0, c->stream>>>(dev_markers(c), c->mats, Y);
   EB_LAUNCHED(c);
@@ -254,9 +302,7 @@ int launch_rheology(eb_ctx* c) {
   EB_PROF(c, "k_failure");
   k_failure<<<mblocks(c), kBlock, 0, c->stream>>>(dev_markers(c), c->mats, melt);
   EB_LAUNCHED(c);
-  const eb_params& p = c->P;
-  RheoParams R{p.timestep, p.temperature_top, p.viscosity_min, p.viscosity_max, p.powerlaw_stress_min,
-               p.gas_constant, p.vsoftfac, (int)(p.iuse_viscous_strain_soft == 1)};
+  const RheoParams R = rheo_params(c->P);
   EB_PROF(c, "k_flow_viscosity");
   k_flow_viscosity<<<mblocks(c), kBlock, 0, c->stream>>>(dev_markers(c), c->mats, R);
   EB_LAUNCHED(c);
@@ -275,3 +321,18 @@ int launch_viscoplastic(eb_ctx* c, int use_marker_plasticity) {
 }
 
 int launch_plastic_yielding(eb_ctx* c) { return yield_launch(c); }
+
+int launch_rheology_fused(eb_ctx* c, int use_marker_plasticity) {
+  int rc = ensure(c, {EB_M_INSIDE, EB_M_MATID, EB_M_STRAIN_PLASTIC, EB_M_FRIC_INI, EB_M_COHESION, EB_M_FRIC,
+                      EB_M_SXX, EB_M_SXY, EB_M_EXX, EB_M_EXY, EB_M_TK, EB_M_PR, EB_M_GII, EB_M_SR_RATIO,
+                      EB_M_ETA_FLOW, EB_M_PREEXP, EB_M_ETA, EB_M_Y, EB_M_PFAILURE});
+  if (rc) return rc;
+  const int melt = c->P.iuse_melt_damage == 1;
+  if (melt && (rc = ensure_marker_field(c, EB_M_MELT_DAMAGE))) return rc;
+  if (c->M == 0) return EB_OK;
+  EB_PROF(c, "k_rheology");
+  k_rheology<<<mblocks(c), kBlock, 0, c->stream>>>(dev_markers(c), c->mats, melt, rheo_params(c->P), c->P.ntimestep,
+                                                  c->P.itype_global, use_marker_plasticity ? 1 : 0, yield_params(c->P));
+  EB_LAUNCHED(c);
+  return EB_OK;
+}

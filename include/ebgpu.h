@@ -233,6 +233,12 @@ int eb_update_marker_rheology(eb_ctx* ctx);
  * ViscoelasticForecast.update_plastic_yielding! (ViscoelasticForecast.jl:11-123). */
 int eb_update_marker_viscoplastic_viscosity(eb_ctx* ctx, int use_marker_plasticity);
 
+/* The two calls above as the time loop makes them (TimeLoop.jl:222-223), fused into one
+ * marker pass: failure properties, flow viscosity, viscoplastic viscosity and (when
+ * use_marker_plasticity != 0) yielding of each marker in turn.  Bit-identical to
+ * eb_update_marker_rheology followed by eb_update_marker_viscoplastic_viscosity.        */
+int eb_update_marker_rheology_and_viscoplastic_viscosity(eb_ctx* ctx, int use_marker_plasticity);
+
 /* MarkerPlasticity.update_plastic_yielding! alone (Picard iterations >= 2,
  * PlasticityLoopMarkers.jl:52-57) -> ViscoelasticForecast.jl:11-123.            */
 int eb_update_plastic_yielding(eb_ctx* ctx);

@@ -64,3 +64,27 @@ def test_fused_tail_matches_the_four_calls(eb, name):
         mic.close()
     for k in outs[0]:
         assert np.array_equal(outs[0][k], outs[1][k]), k
+
+
+@pytest.mark.parametrize("plasticity", [True, False])
+def test_fused_rheology_equals_the_two_calls(eb, plasticity):
+    """eb_update_marker_rheology_and_viscoplastic_viscosity gives, bit for bit, what
+    eb_update_marker_rheology followed by eb_update_marker_viscoplastic_viscosity gives."""
+    model = eb.synthetic.config("rift_small")
+    out = {}
+    for fused in (False, True):
+        mic = eb.MarkerInCell(0)
+        mic.load_model(model)
+        mic.marker_cycle()
+        if fused:
+            mic.update_marker_rheology_and_viscoplastic_viscosity(plasticity)
+        else:
+            mic.update_marker_rheology()
+            mic.update_marker_viscoplastic_viscosity(plasticity)
+        out[fused] = {k: mic.download_marker(k) for k in ("cohesion", "fric", "eta_flow", "preexp", "eta", "sxx",
+                                                          "sxy", "pfailure")}
+        mic.close()
+    for k in out[False]:
+        assert np.array_equal(out[False][k], out[True][k]), k
+    if plasticity:
+        assert np.any(out[True]["pfailure"] == 1.0)
