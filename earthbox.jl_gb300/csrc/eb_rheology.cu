@@ -79,15 +79,16 @@ struct CreepRow {
   double A_disl, n_disl, Ea_disl, Va_disl, A_p, m_p, n_p, s_p, A_diff, Ea_diff, Va_diff;
 };
 
-// CompositeCreep.calculate_composite_creep_viscosity_and_strain_rate
-__device__ double composite_viscosity(const CreepRow& r, double p_mpa, double T, double R, double preexp,
-                                      double s_mpa, bool use_old, double& e_disl, double& a_p, double& e_diff) {
+// CompositeCreep.calculate_composite_creep_viscosity_and_strain_rate: the total creep strain
+// rate at s_mpa (the viscosity is 0.5 s / rate); inv_sp = 1 / s_p of the Peierls law.
+__device__ double creep_rate(const CreepRow& r, double p_mpa, double T, double R, double preexp, double s_mpa,
+                             bool use_old, double inv_sp, double& e_disl, double& a_p, double& e_diff) {
   if (!use_old) e_disl = exp(-((r.Ea_disl * 1000.0 + r.Va_disl * p_mpa) * (1.0 / (R * T))));
   const double rd = preexp * e_disl * ((r.n_disl == 1.0) ? s_mpa : jl_pow(s_mpa, r.n_disl));
   double rp = 0.0;
   if (r.A_p > 0.0 && T < 1200.0) {
     if (!use_old) a_p = (r.Ea_disl * 1000.0 + r.Va_disl * p_mpa) * (1.0 / (R * T));
-    const double ratio = s_mpa / r.s_p;
+    const double ratio = s_mpa * inv_sp;
     const double tm = (r.m_p == 1.0) ? 1.0 - ratio : 1.0 - jl_pow(ratio, r.m_p);
     const double inner = (r.n_p == 2.0) ? tm * tm : jl_pow(tm, r.n_p);
     rp = r.A_p * exp(-a_p * inner) * (s_mpa * s_mpa);
@@ -97,8 +98,7 @@ __device__ double composite_viscosity(const CreepRow& r, double p_mpa, double T,
     if (!use_old) e_diff = exp(-((r.Ea_diff * 1000.0 + r.Va_diff * p_mpa) * (1.0 / (R * T))));
     rf = r.A_diff * e_diff * s_mpa;
   }
-  const double rate = ((rd > rp) ? rd : rp) + rf;
-  return 0.5 * (s_mpa * 1e6) / rate;
+  return ((rd > rp) ? rd : rp) + rf;
 }
 
 __device__ __forceinline__ double forecast_ve(double dt, double mu, double srr, double sxx, double sxy, double exx,
@@ -146,19 +146,36 @@ __device__ __forceinline__ void d_flow_viscosity(const DevMarkers& mk, const Dev
     double s0 = sqrt(sxx * sxx + sxy * sxy);
     if (s0 < P.s_min) s0 = P.s_min;
     double e_disl = 0.0, a_p = 0.0, e_diff = 0.0;
-    eta = composite_viscosity(r, p_mpa, T, P.R, A, s0 * kPaToMPa, false, e_disl, a_p, e_diff);
+    const double inv_sp = 1.0 / r.s_p;
+    double s_mpa = s0 * kPaToMPa;
+    double rate = creep_rate(r, p_mpa, T, P.R, A, s_mpa, false, inv_sp, e_disl, a_p, e_diff);
+    eta = 0.5 * (s_mpa * 1e6) / rate;
     double sf = forecast_ve(P.dt, mu, srr, sxx, sxy, exx, exy, P.s_min, eta);
     double delta = 1e39;
     int icount = 0;
+    // Each step needs only the side of savg the forecast falls on.  With eta = a / rate
+    // (a = s / 2) and D = mu dt rate + a, the forecast components are (a / D) c with
+    // c = 2 srr mu dt (exx, exy) + (sxx, sxy), fixed over the loop, and
+    // max(|forecast|, s_min) > savg >= s_min compares as a^2 |c|^2 > savg^2 D^2: no
+    // division or square root per step.  The viscosity of the last step is formed after
+    // the loop.
+    const double mdt = mu * P.dt;
+    const double cxx = 2.0 * srr * mdt * exx + sxx, cxy = 2.0 * srr * mdt * exy + sxy;
+    const double cc = cxx * cxx + cxy * cxy;
     while (icount < 20 && delta > 1.0) {
       ++icount;
       const double savg = (s0 + sf) / 2.0;
-      eta = composite_viscosity(r, p_mpa, T, P.R, A, savg * kPaToMPa, true, e_disl, a_p, e_diff);
-      const double sfu = forecast_ve(P.dt, mu, srr, sxx, sxy, exx, exy, P.s_min, eta);
-      if ((sf > s0 && sfu > savg) || (sf < s0 && sfu < savg)) s0 = savg;
+      s_mpa = savg * kPaToMPa;
+      rate = creep_rate(r, p_mpa, T, P.R, A, s_mpa, true, inv_sp, e_disl, a_p, e_diff);
+      const double a = 0.5 * (s_mpa * 1e6);
+      const double d = mdt * rate + a;
+      const double lhs = (a * a) * cc, rhs = (savg * savg) * (d * d);
+      const bool above = lhs > rhs, below = lhs < rhs && P.s_min < savg;
+      if ((sf > s0 && above) || (sf < s0 && below)) s0 = savg;
       else sf = savg;
       delta = fabs(sf - s0);
     }
+    if (icount > 0) eta = 0.5 * (s_mpa * 1e6) / rate;
     eta = fmin(fmax(eta, P.eta_min), P.eta_max);
   }
   mk.eta_flow[m] = eta;
