@@ -87,8 +87,10 @@ __global__ void k_apply64(const double* __restrict__ coef, const double* __restr
 }
 
 // W and the pressure preconditioner factor.
+// (winv = 1 / w: the preconditioner multiplies by it instead of dividing by w, the FP64
+// divisions having bound its two kernels)
 __global__ void k_scaling(const double* __restrict__ coef, const double* __restrict__ etan0, double pscale,
-                          double* __restrict__ w, double* __restrict__ prep, int64_t nc) {
+                          double* __restrict__ w, double* __restrict__ prep, double* __restrict__ winv, int64_t nc) {
   const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= nc) return;
   w[c] = 1.0 / sqrt(fabs(coef[c]));
@@ -102,6 +104,7 @@ __global__ void k_scaling(const double* __restrict__ coef, const double* __restr
     w[2 * nc + c] = sqrt(s);
     prep[c] = s;
   }
+  for (int k = 0; k < 3; ++k) winv[k * nc + c] = 1.0 / w[k * nc + c];
 }
 
 // ------------------------------------------------------ FGMRES helpers ---
@@ -573,20 +576,20 @@ __global__ void __launch_bounds__(kCoarseThreads) k_coarse_cycle(const LevelDev<
 // FP64 method: zt = zhat_p and Zk (double) repeats it.
 template <class T>
 __global__ void k_prec_in(const double* __restrict__ coef, const double* __restrict__ rhat,
-                          const double* __restrict__ w, const double* __restrict__ prep, double* __restrict__ zt,
+                          const double* __restrict__ winv, const double* __restrict__ prep, double* __restrict__ zt,
                           void* __restrict__ Zk, T* __restrict__ fx, T* __restrict__ fy, int32_t nx, int32_t ny) {
   const int64_t nc = (int64_t)nx * ny;
   const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= nc) return;
   const int32_t i = (int32_t)(c % ny), j = (int32_t)(c / ny);
-  auto z = [&](int64_t k) { return prep[k] * (rhat[2 * nc + k] / w[2 * nc + k]); };
+  auto z = [&](int64_t k) { return prep[k] * (rhat[2 * nc + k] * winv[2 * nc + k]); };
   const double zc = z(c);
   if (sizeof(T) == 4) {
-    const float zs = (float)(zc / w[2 * nc + c]);
+    const float zs = (float)(zc * winv[2 * nc + c]);
     static_cast<float*>(Zk)[2 * nc + c] = zs;
     zt[2 * nc + c] = (double)zs;
   } else {
-    const double zs = zc / w[2 * nc + c];
+    const double zs = zc * winv[2 * nc + c];
     static_cast<double*>(Zk)[2 * nc + c] = zs;
     zt[2 * nc + c] = zs;
   }
@@ -594,24 +597,24 @@ __global__ void k_prec_in(const double* __restrict__ coef, const double* __restr
   if (j < nx - 1) gx += coef[10 * nc + c] * z(c + ny);
   double gy = coef[20 * nc + c] * zc;
   if (i < ny - 1) gy += coef[21 * nc + c] * z(c + 1);
-  fx[c] = (T)(rhat[c] / w[c] - gx);
-  fy[c] = (T)(rhat[nc + c] / w[nc + c] - gy);
+  fx[c] = (T)(rhat[c] * winv[c] - gx);
+  fy[c] = (T)(rhat[nc + c] * winv[nc + c] - gy);
 }
 // Preconditioner output: zhat_u = u / w_u (rounded to FP32 in the FP32 method) into Zk and zt.
 template <class T>
-__global__ void k_prec_out(const T* __restrict__ ux, const T* __restrict__ uy, const double* __restrict__ w,
+__global__ void k_prec_out(const T* __restrict__ ux, const T* __restrict__ uy, const double* __restrict__ winv,
                            double* __restrict__ zt, void* __restrict__ Zk, int64_t nc) {
   const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= nc) return;
   if (sizeof(T) == 4) {
-    const float zx = (float)((double)ux[c] / w[c]);
-    const float zy = (float)((double)uy[c] / w[nc + c]);
+    const float zx = (float)((double)ux[c] * winv[c]);
+    const float zy = (float)((double)uy[c] * winv[nc + c]);
     static_cast<float*>(Zk)[c] = zx;
     static_cast<float*>(Zk)[nc + c] = zy;
     zt[c] = (double)zx;
     zt[nc + c] = (double)zy;
   } else {
-    const double zx = (double)ux[c] / w[c], zy = (double)uy[c] / w[nc + c];
+    const double zx = (double)ux[c] * winv[c], zy = (double)uy[c] * winv[nc + c];
     static_cast<double*>(Zk)[c] = zx;
     static_cast<double*>(Zk)[nc + c] = zy;
     zt[c] = zx;
@@ -738,16 +741,28 @@ bool invert_dense(std::vector<double>& A, int n, std::vector<double>& inv) {
 }  // namespace
 
 // ------------------------------------------------------------ state ---
-struct StokesState {
-  StokesSystem sys;
-  std::vector<void*> allocs;         // system + solver buffers
+// The multigrid hierarchy of one arithmetic (both are kept, so the two methods can alternate
+// on one system without rebuilding).
+struct Hierarchy {
   std::vector<void*> level_allocs;   // multigrid buffers
   std::vector<Level> levels;
-  bool mg64 = false;                 // V-cycle arithmetic: FP32 (mixed method) or FP64 (plain method)
   void* Ainv = nullptr;              // coarsest inverse (FP32 or FP64)
   void* lv_dev = nullptr;            // device copies of the level descriptors
   int n_dense = 0;
+  B2 b2_levels{};                    // boundary coefficients the transfer tables were built with
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t gexec = nullptr;
+  int64_t graph_kernels = 0;
+};
+
+struct StokesState {
+  StokesSystem sys;
+  std::vector<void*> allocs;         // system + solver buffers
+  Hierarchy hier[2];                 // [0] FP32 V-cycle (mixed method), [1] FP64 (plain method)
+  bool mg64 = false;                 // the hierarchy in use
+  Hierarchy& H() { return hier[mg64 ? 1 : 0]; }
   double *w = nullptr, *prep = nullptr;  // scaling and pressure factor
+  double* winv = nullptr;                // 1 / w
   // FGMRES workspace
   int m = 0;
   double *V = nullptr, *r = nullptr, *t = nullptr, *xs = nullptr, *bs = nullptr, *zp = nullptr, *zt = nullptr;
@@ -757,10 +772,6 @@ struct StokesState {
   int nb_dot = 0;
   double* il = nullptr;              // interleaved staging vector (N)
   double* tmp = nullptr;             // scratch vector (N)
-  B2 b2_levels{};                    // boundary coefficients the transfer tables were built with
-  cudaGraph_t graph = nullptr;
-  cudaGraphExec_t gexec = nullptr;
-  int64_t graph_kernels = 0;
   double *nn_t = nullptr, *nn_q = nullptr, *nn_z = nullptr;  // learned-stage scratch: [t | q], z2
 };
 
@@ -793,15 +804,15 @@ int upload_real(eb_ctx* c, std::vector<void*>& owner, void** p, const std::vecto
 }
 
 void free_levels(StokesState* st) {
-  for (void* p : st->level_allocs) cudaFree(p);
-  st->level_allocs.clear();
-  st->levels.clear();
-  st->Ainv = nullptr;
-  st->lv_dev = nullptr;
-  if (st->gexec) cudaGraphExecDestroy(st->gexec);
-  if (st->graph) cudaGraphDestroy(st->graph);
-  st->gexec = nullptr;
-  st->graph = nullptr;
+  for (void* p : st->H().level_allocs) cudaFree(p);
+  st->H().level_allocs.clear();
+  st->H().levels.clear();
+  st->H().Ainv = nullptr;
+  st->H().lv_dev = nullptr;
+  if (st->H().gexec) cudaGraphExecDestroy(st->H().gexec);
+  if (st->H().graph) cudaGraphDestroy(st->H().graph);
+  st->H().gexec = nullptr;
+  st->H().graph = nullptr;
 }
 
 }  // namespace
@@ -830,7 +841,10 @@ StokesSystem* stokes_system(eb_ctx* c) {
 
 void stokes_free(eb_ctx* c) {
   if (!c->st) return;
-  free_levels(c->st);
+  for (bool b : {false, true}) {
+    c->st->mg64 = b;
+    free_levels(c->st);
+  }
   for (void* p : c->st->allocs) cudaFree(p);
   delete c->st;
   c->st = nullptr;
@@ -860,7 +874,7 @@ LevelDev<T> level_dev(const Level& v);
 
 int setup_levels(eb_ctx* c, StokesState* st, const B2& b2) {
   free_levels(st);
-  std::vector<Level>& L = st->levels;
+  std::vector<Level>& L = st->H().levels;
   L.emplace_back();
   L[0].x = c->h_gx;
   L[0].y = c->h_gy;
@@ -877,11 +891,11 @@ int setup_levels(eb_ctx* c, StokesState* st, const B2& b2) {
     L.push_back(cl);
     Level& cc = L.back();
     int rc;
-    if ((rc = dupload(c, st->level_allocs, &cc.kx, kx)) || (rc = dupload(c, st->level_allocs, &cc.ky, ky))) return rc;
+    if ((rc = dupload(c, st->H().level_allocs, &cc.kx, kx)) || (rc = dupload(c, st->H().level_allocs, &cc.ky, ky))) return rc;
   }
   const int nlev = (int)L.size();
-  st->n_dense = 2 * (int)L.back().nc;
-  if (st->n_dense > 2048)
+  st->H().n_dense = 2 * (int)L.back().nc;
+  if (st->H().n_dense > 2048)
     return eb_fail(c, EB_BAD_INPUT, "grid aspect ratio too large for the multigrid hierarchy (coarsest level has " +
                                         std::to_string(L.back().nc) + " cells)");
   const size_t es = st->mg64 ? sizeof(double) : sizeof(float);
@@ -889,7 +903,7 @@ int setup_levels(eb_ctx* c, StokesState* st, const B2& b2) {
     Level& v = L[l];
     const size_t nc = (size_t)v.nc;
     int rc;
-    auto A = [&](void** p, size_t n) { return dalloc_bytes(c, st->level_allocs, p, n * es); };
+    auto A = [&](void** p, size_t n) { return dalloc_bytes(c, st->H().level_allocs, p, n * es); };
     if ((rc = A(&v.X, 9 * nc)) || (rc = A(&v.Y, 9 * nc)) || (rc = A(&v.ux, nc)) || (rc = A(&v.uy, nc)) ||
         (rc = A(&v.fx, nc)) || (rc = A(&v.fy, nc)) || (rc = A(&v.rx, nc)) || (rc = A(&v.ry, nc)) ||
         (rc = A(&v.etas, (size_t)(v.nx + 1) * (v.ny + 1))) || (rc = A(&v.etan, nc)))
@@ -903,10 +917,10 @@ int setup_levels(eb_ctx* c, StokesState* st, const B2& b2) {
     for (int32_t i = 0; i < v.ny; ++i) ys[i] = v.y[i + 1] - v.y[i];
     for (int32_t j = 0; j <= v.nx; ++j) xsc[j] = sxc[j];
     for (int32_t i = 0; i <= v.ny; ++i) ysc[i] = syc[i];
-    if ((rc = upload_real(c, st->level_allocs, &v.xstp, xs, st->mg64)) ||
-        (rc = upload_real(c, st->level_allocs, &v.ystp, ys, st->mg64)) ||
-        (rc = upload_real(c, st->level_allocs, &v.xstpc, xsc, st->mg64)) ||
-        (rc = upload_real(c, st->level_allocs, &v.ystpc, ysc, st->mg64)))
+    if ((rc = upload_real(c, st->H().level_allocs, &v.xstp, xs, st->mg64)) ||
+        (rc = upload_real(c, st->H().level_allocs, &v.ystp, ys, st->mg64)) ||
+        (rc = upload_real(c, st->H().level_allocs, &v.xstpc, xsc, st->mg64)) ||
+        (rc = upload_real(c, st->H().level_allocs, &v.ystpc, ysc, st->mg64)))
       return rc;
   }
   // transfer tables between level l (fine) and l+1 (coarse)
@@ -952,25 +966,25 @@ int setup_levels(eb_ctx* c, StokesState* st, const B2& b2) {
     AxisR* R[4] = {&f.rvx_x, &f.rvx_y, &f.rvy_x, &f.rvy_y};
     for (int a = 0; a < 4; ++a) {
       int rc;
-      if ((rc = dupload(c, st->level_allocs, &P[a]->idx, pi[a])) || (rc = dupload(c, st->level_allocs, &P[a]->w, pw[a])) ||
-          (rc = dupload(c, st->level_allocs, &R[a]->idx, ri[a])) || (rc = dupload(c, st->level_allocs, &R[a]->w, rw[a])))
+      if ((rc = dupload(c, st->H().level_allocs, &P[a]->idx, pi[a])) || (rc = dupload(c, st->H().level_allocs, &P[a]->w, pw[a])) ||
+          (rc = dupload(c, st->H().level_allocs, &R[a]->idx, ri[a])) || (rc = dupload(c, st->H().level_allocs, &R[a]->w, rw[a])))
         return rc;
     }
   }
-  int rc = dalloc_bytes(c, st->level_allocs, &st->Ainv, (size_t)st->n_dense * st->n_dense * es);
+  int rc = dalloc_bytes(c, st->H().level_allocs, &st->H().Ainv, (size_t)st->H().n_dense * st->H().n_dense * es);
   if (rc) return rc;
   if (st->mg64) {
     std::vector<LevelDev<double>> lv;
     for (const Level& v : L) lv.push_back(level_dev<double>(v));
     LevelDev<double>* d = nullptr;
-    if ((rc = dupload(c, st->level_allocs, &d, lv))) return rc;
-    st->lv_dev = d;
+    if ((rc = dupload(c, st->H().level_allocs, &d, lv))) return rc;
+    st->H().lv_dev = d;
   } else {
     std::vector<LevelDev<float>> lv;
     for (const Level& v : L) lv.push_back(level_dev<float>(v));
     LevelDev<float>* d = nullptr;
-    if ((rc = dupload(c, st->level_allocs, &d, lv))) return rc;
-    st->lv_dev = d;
+    if ((rc = dupload(c, st->H().level_allocs, &d, lv))) return rc;
+    st->H().lv_dev = d;
   }
   EB_CK(c, cudaStreamSynchronize(c->stream));
   return EB_OK;
@@ -979,7 +993,7 @@ int setup_levels(eb_ctx* c, StokesState* st, const B2& b2) {
 // Per-solve operators: level 0 from the FP64 stencil, coarse viscosity and stencils, coarsest inverse.
 template <class T>
 int refresh_levels_t(eb_ctx* c, StokesState* st, const B2& b2) {
-  std::vector<Level>& L = st->levels;
+  std::vector<Level>& L = st->H().levels;
   const StokesSystem& s = st->sys;
   auto P = [](void* p) { return static_cast<T*>(p); };
   EB_PROF(c, "k_mg_setup");
@@ -1043,7 +1057,7 @@ int refresh_levels_t(eb_ctx* c, StokesState* st, const B2& b2) {
   if (!invert_dense(A, n, inv)) return eb_fail(c, EB_NAN, "coarsest multigrid operator is singular");
   std::vector<T> invf(inv.size());
   for (size_t k = 0; k < inv.size(); ++k) invf[k] = (T)inv[k];
-  EB_CK(c, cudaMemcpyAsync(st->Ainv, invf.data(), invf.size() * sizeof(T), cudaMemcpyHostToDevice, c->stream));
+  EB_CK(c, cudaMemcpyAsync(st->H().Ainv, invf.data(), invf.size() * sizeof(T), cudaMemcpyHostToDevice, c->stream));
   EB_CK(c, cudaStreamSynchronize(c->stream));
   return EB_OK;
 }
@@ -1070,7 +1084,7 @@ LevelDev<T> level_dev(const Level& v) {
 constexpr int64_t kCoarseCells = 2048;
 template <class T>
 int vcycle_launch(eb_ctx* c, StokesState* st, int sweeps, int64_t* nk) {
-  std::vector<Level>& L = st->levels;
+  std::vector<Level>& L = st->H().levels;
   const int nl = (int)L.size();
   int l0 = 0;
   while (l0 < nl - 1 && L[l0].nc > kCoarseCells) ++l0;
@@ -1089,8 +1103,8 @@ int vcycle_launch(eb_ctx* c, StokesState* st, int sweeps, int64_t* nk) {
     k_restrict<T><<<nblk(w.nc), kB, 0, c->stream>>>(v, w);
     *nk += 2;
   }
-  k_coarse_cycle<T><<<1, kCoarseThreads, 0, c->stream>>>(static_cast<const LevelDev<T>*>(st->lv_dev), l0, nl, sweeps,
-                                                        static_cast<const T*>(st->Ainv), st->n_dense);
+  k_coarse_cycle<T><<<1, kCoarseThreads, 0, c->stream>>>(static_cast<const LevelDev<T>*>(st->H().lv_dev), l0, nl, sweeps,
+                                                        static_cast<const T*>(st->H().Ainv), st->H().n_dense);
   ++*nk;
   for (int l = l0 - 1; l >= 0; --l) {
     const LevelDev<T> v = level_dev<T>(L[l]);
@@ -1104,8 +1118,8 @@ int vcycle_launch(eb_ctx* c, StokesState* st, int sweeps, int64_t* nk) {
 }
 
 int capture_vcycle(eb_ctx* c, StokesState* st, int sweeps) {
-  if (st->gexec) { cudaGraphExecDestroy(st->gexec); st->gexec = nullptr; }
-  if (st->graph) { cudaGraphDestroy(st->graph); st->graph = nullptr; }
+  if (st->H().gexec) { cudaGraphExecDestroy(st->H().gexec); st->H().gexec = nullptr; }
+  if (st->H().graph) { cudaGraphDestroy(st->H().graph); st->H().graph = nullptr; }
   const bool prof = c->prof.on;
   c->prof.on = false;
   int64_t nk = 0;
@@ -1116,9 +1130,9 @@ int capture_vcycle(eb_ctx* c, StokesState* st, int sweeps) {
   c->prof.on = prof;
   if (rc) return rc;
   if (e != cudaSuccess) return eb_cuda(c, e, "cudaStreamEndCapture");
-  st->graph = g;
-  EB_CK(c, cudaGraphInstantiate(&st->gexec, g, 0));
-  st->graph_kernels = nk;
+  st->H().graph = g;
+  EB_CK(c, cudaGraphInstantiate(&st->H().gexec, g, 0));
+  st->H().graph_kernels = nk;
   return EB_OK;
 }
 
@@ -1127,25 +1141,25 @@ int capture_vcycle(eb_ctx* c, StokesState* st, int sweeps) {
 // operator product).
 int precondition(eb_ctx* c, StokesState* st, const double* rhat, double* zt, void* Zk) {
   const StokesSystem& s = st->sys;
-  Level& v = st->levels[0];
+  Level& v = st->H().levels[0];
   EB_PROF(c, "k_precond");
   if (st->mg64)
-    k_prec_in<double><<<nblk(s.nc), kB, 0, c->stream>>>(s.coef, rhat, st->w, st->prep, zt, Zk,
+    k_prec_in<double><<<nblk(s.nc), kB, 0, c->stream>>>(s.coef, rhat, st->winv, st->prep, zt, Zk,
                                                         static_cast<double*>(v.fx), static_cast<double*>(v.fy), s.nx, s.ny);
   else
-    k_prec_in<float><<<nblk(s.nc), kB, 0, c->stream>>>(s.coef, rhat, st->w, st->prep, zt, Zk,
+    k_prec_in<float><<<nblk(s.nc), kB, 0, c->stream>>>(s.coef, rhat, st->winv, st->prep, zt, Zk,
                                                        static_cast<float*>(v.fx), static_cast<float*>(v.fy), s.nx, s.ny);
   EB_LAUNCHED(c);
   EB_PROF(c, "vcycle_graph");
-  EB_CK(c, cudaGraphLaunch(st->gexec, c->stream));
-  c->launches += st->graph_kernels - 1;
+  EB_CK(c, cudaGraphLaunch(st->H().gexec, c->stream));
+  c->launches += st->H().graph_kernels - 1;
   EB_LAUNCHED(c);
   EB_PROF(c, "k_precond");
   if (st->mg64)
-    k_prec_out<double><<<nblk(s.nc), kB, 0, c->stream>>>(static_cast<double*>(v.ux), static_cast<double*>(v.uy), st->w,
+    k_prec_out<double><<<nblk(s.nc), kB, 0, c->stream>>>(static_cast<double*>(v.ux), static_cast<double*>(v.uy), st->winv,
                                                          zt, Zk, s.nc);
   else
-    k_prec_out<float><<<nblk(s.nc), kB, 0, c->stream>>>(static_cast<float*>(v.ux), static_cast<float*>(v.uy), st->w, zt,
+    k_prec_out<float><<<nblk(s.nc), kB, 0, c->stream>>>(static_cast<float*>(v.ux), static_cast<float*>(v.uy), st->winv, zt,
                                                         Zk, s.nc);
   EB_LAUNCHED(c);
   return EB_OK;
@@ -1174,31 +1188,33 @@ int apply_scaled(eb_ctx* c, StokesState* st, const double* x, double* y) {
 }
 
 int ensure_solver(eb_ctx* c, StokesState* st, int m) {
-  if (st->m == m && st->V && (st->mg64 ? st->Zd != nullptr : st->Z != nullptr)) return EB_OK;
-  // (re)allocate the Krylov workspace
   auto drop = [&](void* p) {
     if (!p) return;
     cudaFree(p);
     st->allocs.erase(std::remove(st->allocs.begin(), st->allocs.end(), p), st->allocs.end());
   };
-  drop(st->V);
-  drop(st->Z);
-  drop(st->Zd);
-  st->V = nullptr;
-  st->Z = nullptr;
-  st->Zd = nullptr;
   const size_t n3 = 3 * (size_t)st->sys.nc;
-  st->m = m;
-  st->nb_dot = kDotBlocks;
   int rc;
-  if ((rc = dalloc(c, st->allocs, &st->V, (size_t)(m + 2) * n3))) return rc;
-  if ((rc = st->mg64 ? dalloc(c, st->allocs, &st->Zd, (size_t)m * n3) : dalloc(c, st->allocs, &st->Z, (size_t)m * n3)))
-    return rc;
+  if (st->m != m || !st->V) {  // (re)allocate the Krylov workspace for m directions
+    drop(st->V);
+    drop(st->Z);
+    drop(st->Zd);
+    st->V = nullptr;
+    st->Z = nullptr;
+    st->Zd = nullptr;
+    st->m = m;
+    st->nb_dot = kDotBlocks;
+    if ((rc = dalloc(c, st->allocs, &st->V, (size_t)(m + 2) * n3))) return rc;
+  }
+  // stored directions of the method in use (FP32 mixed, FP64 plain), kept once allocated
+  if (st->mg64 && !st->Zd && (rc = dalloc(c, st->allocs, &st->Zd, (size_t)m * n3))) return rc;
+  if (!st->mg64 && !st->Z && (rc = dalloc(c, st->allocs, &st->Z, (size_t)m * n3))) return rc;
   if (!st->r) {
     if ((rc = dalloc(c, st->allocs, &st->r, n3)) || (rc = dalloc(c, st->allocs, &st->t, n3)) ||
         (rc = dalloc(c, st->allocs, &st->xs, n3)) || (rc = dalloc(c, st->allocs, &st->bs, n3)) ||
         (rc = dalloc(c, st->allocs, &st->zt, n3)) ||
-        (rc = dalloc(c, st->allocs, &st->w, n3)) || (rc = dalloc(c, st->allocs, &st->prep, (size_t)st->sys.nc)) ||
+        (rc = dalloc(c, st->allocs, &st->w, n3)) || (rc = dalloc(c, st->allocs, &st->winv, n3)) ||
+        (rc = dalloc(c, st->allocs, &st->prep, (size_t)st->sys.nc)) ||
         (rc = dalloc(c, st->allocs, &st->partial, (size_t)st->nb_dot * kMaxDots)) ||
         (rc = dalloc(c, st->allocs, &st->dots, kMaxDots)) || (rc = dalloc(c, st->allocs, &st->hdev, kMaxDots)))
       return rc;
@@ -1247,20 +1263,17 @@ int learned_stage(eb_ctx* c, StokesState* st, const double* v, double* zt, float
 // Scaling, multigrid hierarchy and captured V-cycle of the current system, in FP32 or FP64.
 int prepare(eb_ctx* c, StokesState* st, int sweeps, int m, bool fp64) {
   int rc;
-  if (st->mg64 != fp64) {  // the level arrays and the stored directions change type
-    free_levels(st);
-    st->mg64 = fp64;
-  }
+  st->mg64 = fp64;  // selects the hierarchy and the stored-direction buffer
   B2 b2;
   if ((rc = ensure_solver(c, st, m)) || (rc = read_b2(c, &b2))) return rc;
-  if (st->levels.empty() || std::memcmp(&b2, &st->b2_levels, sizeof(B2)) != 0) {
+  if (st->H().levels.empty() || std::memcmp(&b2, &st->H().b2_levels, sizeof(B2)) != 0) {
     if ((rc = setup_levels(c, st, b2))) return rc;
-    st->b2_levels = b2;
+    st->H().b2_levels = b2;
   }
   if ((rc = refresh_levels(c, st, b2)) || (rc = capture_vcycle(c, st, sweeps))) return rc;
   const StokesSystem& s = st->sys;
   EB_PROF(c, "k_scaling");
-  k_scaling<<<nblk(s.nc), kB, 0, c->stream>>>(s.coef, c->gf[EB_G_ETAN0], s.pscale, st->w, st->prep, s.nc);
+  k_scaling<<<nblk(s.nc), kB, 0, c->stream>>>(s.coef, c->gf[EB_G_ETAN0], s.pscale, st->w, st->prep, st->winv, s.nc);
   EB_LAUNCHED(c);
   return EB_OK;
 }
@@ -1502,7 +1515,7 @@ extern "C" int eb_solve_stokes_system(eb_ctx* c, const eb_solve_opts* o, eb_solv
   if (rep) {
     rep->iterations = it;
     rep->reorthogonalisations = reorth;
-    rep->levels = (int32_t)st->levels.size();
+    rep->levels = (int32_t)st->H().levels.size();
     rep->rel_residual = rel;
     rep->rel_residual_scaled = rel_s;
     rep->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
