@@ -205,7 +205,7 @@ def unet_flops_per_pixel() -> float:
 
 
 def stokes_gpu(mic, reps: int = 2, method: str = "fgmres", rtol: float = 1e-8, learned: bool = False,
-               precision: str = "mixed"):
+               precision: str = "mixed", gs_relax: float = 0.0):
     """The Stokes step on the grids the context holds: build steps, solve to 1e-8, unpack.
     One warm-up (level set-up, graph capture), then `reps` timed steps (wall clock: the
     FGMRES loop is host-driven)."""
@@ -215,7 +215,8 @@ def stokes_gpu(mic, reps: int = 2, method: str = "fgmres", rtol: float = 1e-8, l
         mic.calc_viscoelastic_terms()
         mic.viscoelastic_rhs()
         mic.build_system_of_equations()
-        rep = mic.solve_system(rtol=rtol, check=False, method=method, learned=learned, precision=precision)
+        rep = mic.solve_system(rtol=rtol, check=False, method=method, learned=learned, precision=precision,
+                               gs_relax=gs_relax)
         mic.process_stokes_solution()
         return rep
 
@@ -470,6 +471,7 @@ def main():
                   "rel_residual": s_rep["rel_residual"], "rel_residual_scaled": s_rep["rel_residual_scaled"],
                   "status": s_rep["status"], "solve_s": s_rep["seconds"],
                   "reorthogonalisations": s_rep["reorthogonalisations"],
+                  "fp32_gram_schmidt_iterations": s_rep["relaxed_iterations"],
                   "kernels_ms": {k: round(v[0] * v[1], 3) for k, v in
                                  sorted(s_kern.items(), key=lambda kv: -kv[1][0] * kv[1][1])[:12]}}
         # the plain method on the same system: FP64 V-cycle and FP64 stored directions
@@ -477,21 +479,32 @@ def main():
         stokes["plain_fp64"] = {"value": p_dt, "unit": "s/solve", "iterations": p_rep["iterations"],
                                 "rel_residual": p_rep["rel_residual"], "status": p_rep["status"],
                                 "mixed_speedup": p_dt / s_dt}
+        # the mixed method with its Gram-Schmidt kept in FP64 throughout (gs_relax < 0)
+        g_dt, g_rep, _ = stokes_gpu(mic, reps=2, method=args.stokes_method, gs_relax=-1.0)
+        stokes["mixed_fp64_gram_schmidt"] = {"value": g_dt, "unit": "s/solve", "iterations": g_rep["iterations"],
+                                             "rel_residual": g_rep["rel_residual"], "status": g_rep["status"]}
         # roofline of the Krylov-basis products (the solve's dominant kernels): per FGMRES
         # iteration k of a cycle, k_mdot reads the k+2 basis vectors and k_maxpy k+1 of them
-        # plus the new direction (read and written); vectors are N doubles.
+        # plus the new direction (read and written); vectors are N doubles.  The last
+        # `relaxed` iterations run the FP32 forms on N-float copies: k_mdot32 reads k+2 of
+        # them, k_maxpy32 k+1 plus the FP64 direction (read, written) and its FP32 copy.
         n_unk = 3 * (model.grid.xnum - 1) * (model.grid.ynum - 1)
         its, m = s_rep["iterations"], 250
         ks = [k for c0 in range(0, its, m) for k in range(min(m, its - c0))] if args.stokes_method == "fgmres" else []
+        n_rel = s_rep["relaxed_iterations"]
+        ks64, ks32 = ks[:len(ks) - n_rel], ks[len(ks) - n_rel:]
         vbytes = n_unk * 8.0
-        bytes_dot = sum(k + 2 for k in ks) * vbytes
-        bytes_axpy = sum(k + 3 for k in ks) * vbytes
+        bytes_dot = sum(k + 2 for k in ks64) * vbytes
+        bytes_axpy = sum(k + 3 for k in ks64) * vbytes
+        bytes_dot32 = sum(k + 2 for k in ks32) * n_unk * 4.0
+        bytes_axpy32 = sum((k + 1) * 4.0 + 20.0 for k in ks32) * n_unk
         peak, peak_kind = peaks()
         rl = {}
         nc_cells = n_unk // 3
         # operator product: 27 coefficients, x and the scaling w read, y written (FP64 per cell)
         bytes_apply = nc_cells * (27 + 3 + 3 + 3) * 8.0 * s_kern.get("k_apply64", (0, 0))[1] / 2
-        for kname, b in (("k_mdot", bytes_dot), ("k_maxpy", bytes_axpy), ("k_apply64", bytes_apply)):
+        for kname, b in (("k_mdot", bytes_dot), ("k_maxpy", bytes_axpy), ("k_mdot32", bytes_dot32),
+                         ("k_maxpy32", bytes_axpy32), ("k_apply64", bytes_apply)):
             if kname in s_kern and b > 0:
                 t = s_kern[kname][0] * s_kern[kname][1] / 2 * 1e-3  # seconds per solve (2 timed solves)
                 rl[kname] = {"achieved": b / t / 1e9, "bytes_per_solve": b, "s_per_solve": t}

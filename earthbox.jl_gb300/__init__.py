@@ -296,17 +296,19 @@ class MarkerInCell:
 
     def solve_system(self, rtol: float = 1e-8, max_iters: int = 0, restart: int = 0, mg_sweeps: int = 0,
                      use_initial_guess: bool = False, method: str = "fgmres", check: bool = True,
-                     learned: bool = False, precision: str = "mixed") -> dict:
+                     learned: bool = False, precision: str = "mixed", gs_relax: float = 0.0) -> dict:
         """The Stokes solve (replaces SystemSolver.solve_system_optimized, SystemSolver.jl:67-91);
         method "fgmres" or "bicgstab"; learned: add the trained network's stage after each V-cycle;
-        precision "mixed" (FP32 V-cycle and stored directions) or "fp64" (the plain method)."""
+        precision "mixed" (FP32 V-cycle and stored directions) or "fp64" (the plain method);
+        gs_relax (mixed only): FP32 Gram-Schmidt below gs_relax x the target (0: 1e3, <0: never)."""
         o = _abi.SolveOpts(rtol, max_iters, restart, mg_sweeps, int(use_initial_guess),
-                           {"fgmres": 0, "bicgstab": 1}[method], int(learned), {"mixed": 0, "fp64": 1}[precision])
+                           {"fgmres": 0, "bicgstab": 1}[method], int(learned), {"mixed": 0, "fp64": 1}[precision],
+                           gs_relax)
         r = _abi.SolveReport()
         rc = self._lib.eb_solve_stokes_system(self._ctx, C.byref(o), C.byref(r))
         rep = {"status": rc, "iterations": r.iterations, "levels": r.levels, "rel_residual": r.rel_residual,
                "rel_residual_scaled": r.rel_residual_scaled, "seconds": r.seconds,
-               "reorthogonalisations": r.reorthogonalisations}
+               "reorthogonalisations": r.reorthogonalisations, "relaxed_iterations": r.relaxed_iterations}
         if check:
             self._check(rc)
         return rep

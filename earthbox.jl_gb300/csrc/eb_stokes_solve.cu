@@ -33,6 +33,9 @@ constexpr int kMaxRestart = 500;
 // Classical Gram-Schmidt re-orthogonalises a new direction only when the projection
 // removed all but 5% of its norm (squared ratio below).
 constexpr double kReorth2 = 0.05 * 0.05;
+// Default residual level (relative to the target) below which the mixed method's
+// Gram-Schmidt runs in FP32 on the basis copies.
+constexpr double kGsRelax = 1e3;
 constexpr int kMaxDots = kMaxRestart + 8;  // dot products per reduction
 
 unsigned nblk(int64_t n) { return (unsigned)((n + kB - 1) / kB); }
@@ -41,7 +44,7 @@ unsigned nblk(int64_t n) { return (unsigned)((n + kB - 1) / kB); }
 // y = L x on SoA vectors; optional scaling: y = w .* L (w .* x); optional shift: y -= sub.
 __global__ void k_apply64(const double* __restrict__ coef, const double* __restrict__ x, double* __restrict__ y,
                           const double* __restrict__ w, int32_t nx, int32_t ny, int64_t nc,
-                          const double* __restrict__ sub = nullptr) {
+                          const double* __restrict__ sub = nullptr, float* __restrict__ y32 = nullptr) {
   const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= nc) return;
   const int32_t i = (int32_t)(c % ny), j = (int32_t)(c / ny);
@@ -84,6 +87,11 @@ __global__ void k_apply64(const double* __restrict__ coef, const double* __restr
   y[c] = ax;
   y[nc + c] = ay;
   y[2 * nc + c] = ap;
+  if (y32) {  // FP32 copy for the FP32 Gram-Schmidt products
+    y32[c] = (float)ax;
+    y32[nc + c] = (float)ay;
+    y32[2 * nc + c] = (float)ap;
+  }
 }
 
 // W and the pressure preconditioner factor.
@@ -213,6 +221,131 @@ __global__ void k_maxpy_f32(double* __restrict__ u, const float* __restrict__ Z,
   double s = u[k];
   for (int v = 0; v < nv; ++v) s -= h[v] * (double)Z[(int64_t)v * stride + k];
   u[k] = s;
+}
+// ---- Gram-Schmidt on FP32 copies of the basis (mixed method, late iterations) ----
+// Inexact Krylov theory (Simoncini & Szyld 2003; Bouras & Fraysse 2005) lets the error an
+// iteration adds to the Arnoldi relation grow like 1/|r| once the residual is small.  The
+// mixed method therefore keeps an FP32 copy of every basis vector (slots ld32 floats apart,
+// ld32 a multiple of 4, padding zero) and, below a residual threshold, projects with FP32
+// products on those copies: half the bytes, and the FP32 pipe instead of the FP64 one that
+// bounds k_mdot / k_maxpy.  The new direction itself stays FP64, and its norm is measured.
+//
+// dots: block (b, v) reduces a grid-stride slice of V32_v . u32 over float4 chunks
+// (n4 = ld32 / 4); four FP32 partial sums per thread (about 50 chunks each at 14M unknowns)
+// go to FP64 for the block reduction.
+__global__ void __launch_bounds__(kB) k_mdot32(const float* __restrict__ V, int64_t ld, const float* __restrict__ u,
+                                               int64_t n4, double* __restrict__ partial) {
+  const float4* a = reinterpret_cast<const float4*>(V + (int64_t)blockIdx.y * ld);
+  const float4* b = reinterpret_cast<const float4*>(u);
+  float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f;
+  const int64_t step = (int64_t)gridDim.x * blockDim.x;
+  int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  auto acc4 = [&](const float4 x, const float4 y) {
+    s0 = fmaf(x.x, y.x, s0);
+    s1 = fmaf(x.y, y.y, s1);
+    s2 = fmaf(x.z, y.z, s2);
+    s3 = fmaf(x.w, y.w, s3);
+  };
+  for (; k + 3 * step < n4; k += 4 * step) {  // eight 16-byte loads in flight
+    const float4 a0 = __ldcs(a + k), a1 = __ldcs(a + k + step), a2 = __ldcs(a + k + 2 * step),
+                 a3 = __ldcs(a + k + 3 * step);
+    const float4 u0 = __ldg(b + k), u1 = __ldg(b + k + step), u2 = __ldg(b + k + 2 * step), u3 = __ldg(b + k + 3 * step);
+    acc4(a0, u0);
+    acc4(a1, u1);
+    acc4(a2, u2);
+    acc4(a3, u3);
+  }
+  for (; k < n4; k += step) acc4(a[k], b[k]);
+  double s = ((double)s0 + (double)s1) + ((double)s2 + (double)s3);
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  __shared__ double sh[kB / 32];
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < kB / 32; ++w) t += sh[w];
+    partial[(int64_t)blockIdx.y * gridDim.x + blockIdx.x] = t;
+  }
+}
+// u -= sum_v h[v] V32_v, the sum formed in FP32 and subtracted from the FP64 u; u32 = float(u)
+// afterwards (the copy the second pass, or the normalisation, starts from); partial[block] =
+// the block's sum of u^2 in FP64 (the measured norm).  A thread owns kAx32Per float4 chunks of
+// consecutive elements and streams four basis vectors at a time (eight 16-byte loads in flight).
+constexpr int kAx32Per = 2, kAx32Chunks = kAxThreads * kAx32Per;  // chunks (4 elements) per block
+__global__ void __launch_bounds__(kAxThreads) k_maxpy32(double* __restrict__ u, float* __restrict__ u32,
+                                                        const float* __restrict__ V, int64_t ld,
+                                                        const double* __restrict__ h, int nv, int64_t n,
+                                                        double* __restrict__ partial) {
+  extern __shared__ float hs32[];
+  for (int v = threadIdx.x; v < nv; v += blockDim.x) hs32[v] = (float)h[v];
+  __syncthreads();
+  const int64_t n4 = ld >> 2;
+  int64_t ch[kAx32Per];
+  bool ok[kAx32Per];
+  float4 acc[kAx32Per];
+#pragma unroll
+  for (int q = 0; q < kAx32Per; ++q) {
+    ch[q] = (int64_t)blockIdx.x * kAx32Chunks + q * kAxThreads + threadIdx.x;
+    ok[q] = ch[q] < n4;
+    acc[q] = make_float4(0.f, 0.f, 0.f, 0.f);
+  }
+  const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
+  auto fma4 = [](float a, const float4 x, float4& s) {
+    s.x = fmaf(a, x.x, s.x);
+    s.y = fmaf(a, x.y, s.y);
+    s.z = fmaf(a, x.z, s.z);
+    s.w = fmaf(a, x.w, s.w);
+  };
+  int v = 0;
+  for (; v + 4 <= nv; v += 4) {
+    float4 x[4][kAx32Per];
+#pragma unroll
+    for (int g = 0; g < 4; ++g)
+#pragma unroll
+      for (int q = 0; q < kAx32Per; ++q)
+        x[g][q] = ok[q] ? __ldcs(reinterpret_cast<const float4*>(V + (int64_t)(v + g) * ld) + ch[q]) : zero;
+#pragma unroll
+    for (int g = 0; g < 4; ++g)
+#pragma unroll
+      for (int q = 0; q < kAx32Per; ++q) fma4(hs32[v + g], x[g][q], acc[q]);
+  }
+  for (; v < nv; ++v)
+#pragma unroll
+    for (int q = 0; q < kAx32Per; ++q)
+      if (ok[q]) fma4(hs32[v], __ldcs(reinterpret_cast<const float4*>(V + (int64_t)v * ld) + ch[q]), acc[q]);
+  double ss = 0.0;
+#pragma unroll
+  for (int q = 0; q < kAx32Per; ++q) {
+    if (!ok[q]) continue;
+    const float av[4] = {acc[q].x, acc[q].y, acc[q].z, acc[q].w};
+#pragma unroll
+    for (int l = 0; l < 4; ++l) {
+      const int64_t e = 4 * ch[q] + l;
+      if (e < n) {
+        const double r = u[e] - (double)av[l];
+        u[e] = r;
+        u32[e] = (float)r;
+        ss += r * r;
+      }
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) ss += __shfl_xor_sync(0xffffffffu, ss, o);
+  __shared__ double sh[kAxThreads / 32];
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = ss;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < kAxThreads / 32; ++w) t += sh[w];
+    partial[blockIdx.x] = t;
+  }
+}
+// dst = a src (dst may alias src), and the FP32 copy dst32 = float(dst) when given
+__global__ void k_scale_copy2(double* dst, float* __restrict__ dst32, const double* src, double a, int64_t n) {
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  const double r = a * src[k];
+  dst[k] = r;
+  if (dst32) dst32[k] = (float)r;
 }
 // BiCGStab vector updates
 __global__ void k_bicg_p(double* __restrict__ p, const double* __restrict__ r, const double* __restrict__ v, double beta,
@@ -770,6 +903,10 @@ struct StokesState {
   double* Zd = nullptr;              // ... or FP64 (plain method)
   double *partial = nullptr, *dots = nullptr, *hdev = nullptr;
   int nb_dot = 0;
+  float* V32 = nullptr;              // FP32 copies of the basis (mixed method), slots ld32 apart
+  int64_t ld32 = 0;
+  double* part32 = nullptr;          // per-block norms of k_maxpy32
+  int nb_ax32 = 0;
   double* il = nullptr;              // interleaved staging vector (N)
   double* tmp = nullptr;             // scratch vector (N)
   double *nn_t = nullptr, *nn_q = nullptr, *nn_z = nullptr;  // learned-stage scratch: [t | q], z2
@@ -1179,6 +1316,34 @@ int mdot(eb_ctx* c, StokesState* st, const double* V, int64_t stride, int nv, co
   return EB_OK;
 }
 
+// h[v] = V32_v . V32_{nv-1} for v < nv (the last slot holds the FP32 copy of the new direction)
+int mdot32(eb_ctx* c, StokesState* st, int nv, double* h) {
+  EB_PROF(c, "k_mdot32");
+  k_mdot32<<<dim3(st->nb_dot, nv), kB, 0, c->stream>>>(st->V32, st->ld32, st->V32 + (size_t)(nv - 1) * st->ld32,
+                                                       st->ld32 / 4, st->partial);
+  EB_LAUNCHED(c);
+  EB_PROF(c, "k_mdot_final");
+  k_mdot_final<<<nv, kB, 0, c->stream>>>(st->partial, st->nb_dot, st->dots);
+  EB_LAUNCHED(c);
+  EB_CK(c, cudaMemcpyAsync(h, st->dots, nv * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  EB_CK(c, cudaStreamSynchronize(c->stream));
+  return EB_OK;
+}
+// w -= sum_{v<nv} hdev[v] V32_v (w32 = its FP32 copy); *wn2 = |w|^2 measured in FP64
+int maxpy32(eb_ctx* c, StokesState* st, double* w, float* w32, int nv, double* wn2) {
+  const int64_t n3 = 3 * st->sys.nc;
+  EB_PROF(c, "k_maxpy32");
+  k_maxpy32<<<st->nb_ax32, kAxThreads, (size_t)nv * sizeof(float), c->stream>>>(w, w32, st->V32, st->ld32, st->hdev,
+                                                                                nv, n3, st->part32);
+  EB_LAUNCHED(c);
+  EB_PROF(c, "k_mdot_final");
+  k_mdot_final<<<1, kB, 0, c->stream>>>(st->part32, st->nb_ax32, st->dots);
+  EB_LAUNCHED(c);
+  EB_CK(c, cudaMemcpyAsync(wn2, st->dots, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  EB_CK(c, cudaStreamSynchronize(c->stream));
+  return EB_OK;
+}
+
 int apply_scaled(eb_ctx* c, StokesState* st, const double* x, double* y) {
   const StokesSystem& s = st->sys;
   EB_PROF(c, "k_apply64");
@@ -1199,9 +1364,11 @@ int ensure_solver(eb_ctx* c, StokesState* st, int m) {
     drop(st->V);
     drop(st->Z);
     drop(st->Zd);
+    drop(st->V32);
     st->V = nullptr;
     st->Z = nullptr;
     st->Zd = nullptr;
+    st->V32 = nullptr;
     st->m = m;
     st->nb_dot = kDotBlocks;
     if ((rc = dalloc(c, st->allocs, &st->V, (size_t)(m + 2) * n3))) return rc;
@@ -1209,6 +1376,14 @@ int ensure_solver(eb_ctx* c, StokesState* st, int m) {
   // stored directions of the method in use (FP32 mixed, FP64 plain), kept once allocated
   if (st->mg64 && !st->Zd && (rc = dalloc(c, st->allocs, &st->Zd, (size_t)m * n3))) return rc;
   if (!st->mg64 && !st->Z && (rc = dalloc(c, st->allocs, &st->Z, (size_t)m * n3))) return rc;
+  if (!st->mg64 && !st->V32) {  // FP32 basis copies, zero padding between the slots
+    st->ld32 = (int64_t)((n3 + 3) & ~(size_t)3);
+    st->nb_ax32 = (int)((st->ld32 / 4 + kAx32Chunks - 1) / kAx32Chunks);
+    if ((rc = dalloc(c, st->allocs, &st->V32, (size_t)(m + 2) * st->ld32))) return rc;
+    EB_CK(c, cudaMemsetAsync(st->V32, 0, (size_t)(m + 2) * st->ld32 * sizeof(float), c->stream));
+    drop(st->part32);
+    if ((rc = dalloc(c, st->allocs, &st->part32, (size_t)st->nb_ax32))) return rc;
+  }
   if (!st->r) {
     if ((rc = dalloc(c, st->allocs, &st->r, n3)) || (rc = dalloc(c, st->allocs, &st->t, n3)) ||
         (rc = dalloc(c, st->allocs, &st->xs, n3)) || (rc = dalloc(c, st->allocs, &st->bs, n3)) ||
@@ -1326,8 +1501,11 @@ extern "C" int eb_solve_stokes_system(eb_ctx* c, const eb_solve_opts* o, eb_solv
   const double bnorm = std::sqrt(bn2);
   if (!std::isfinite(bnorm)) return eb_fail(c, EB_NAN, "right-hand side has NaN/Inf");
   std::vector<double> H((size_t)(m + 1) * m), g(m + 1), cs(m), sn(m), hcol(m + 2), y(m);
-  int it = 0, reorth = 0;
+  int it = 0, reorth = 0, relaxed = 0;
   double est = 1.0;
+  // FP32 Gram-Schmidt (mixed method): from a residual estimate of gs_relax x the target on
+  const double relax_fac = opt.gs_relax == 0.0 ? kGsRelax : opt.gs_relax;
+  float* const V32 = (!st->mg64 && relax_fac > 0.0) ? st->V32 : nullptr;
   // The Krylov methods run on the scaled system, whose residual norm weights rows by W; the
   // tolerance is on the reference's (unscaled) residual ||R - L S|| / ||R||.  When the scaled
   // target is reached but the unscaled residual is still above rtol, the target is tightened
@@ -1397,7 +1575,7 @@ extern "C" int eb_solve_stokes_system(eb_ctx* c, const eb_solve_opts* o, eb_solv
     est = beta / bnorm;
     if (est <= target) { converged = true; break; }
     EB_PROF(c, "k_axpy");
-    k_scale_copy<<<nblk(n3), kB, 0, c->stream>>>(st->V, st->r, 1.0 / beta, n3);
+    k_scale_copy2<<<nblk(n3), kB, 0, c->stream>>>(st->V, V32, st->r, 1.0 / beta, n3);
     EB_LAUNCHED(c);
     std::fill(g.begin(), g.end(), 0.0);
     g[0] = beta;
@@ -1411,16 +1589,42 @@ extern "C" int eb_solve_stokes_system(eb_ctx* c, const eb_solve_opts* o, eb_solv
       // Shifted Arnoldi: with a good preconditioner A z_k is close to v_k, so the slot holds
       // d = A z_k - v_k and the projection starts from d (h_kk gets the 1 back below); the
       // cancellation that classical Gram-Schmidt suffers is then measured against |d|.
+      // FP32 products once the residual estimate |g_k| is below relax_tol (mixed method)
+      float* w32 = V32 ? V32 + (size_t)(k + 1) * st->ld32 : nullptr;
+      const bool relax = V32 && std::fabs(g[k]) <= relax_fac * target * bnorm;
       EB_PROF(c, "k_apply64");
-      k_apply64<<<nblk(s.nc), kB, 0, c->stream>>>(s.coef, st->zt, w, st->w, s.nx, s.ny, s.nc, vk);
+      k_apply64<<<nblk(s.nc), kB, 0, c->stream>>>(s.coef, st->zt, w, st->w, s.nx, s.ny, s.nc, vk,
+                                                  relax ? w32 : nullptr);
       EB_LAUNCHED(c);
       // Classical Gram-Schmidt.  One reduction gives V^T d and |d|^2 (d is the slot after V_k);
       // the projected norm follows from Pythagoras unless cancellation is large, in which
-      // case a second pass re-orthogonalises and the norm is measured.
+      // case a second pass re-orthogonalises and the norm is measured.  The FP32 form
+      // measures the norm every time (its products are only FP32-accurate).
       std::vector<double> h(k + 2);
-      if ((rc = mdot(c, st, st->V, n3, k + 2, w, h.data()))) return rc;
-      double wn2_before = h[k + 1];
-      for (int pass = 0; pass < 2; ++pass) {
+      if (relax) {
+        ++relaxed;
+        if ((rc = mdot32(c, st, k + 2, h.data()))) return rc;
+        double wn2_before = h[k + 1];
+        for (int pass = 0; pass < 2; ++pass) {
+          EB_CK(c, cudaMemcpyAsync(st->hdev, h.data(), (k + 1) * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+          double wn2 = 0.0;
+          if ((rc = maxpy32(c, st, w, w32, k + 1, &wn2))) return rc;
+          for (int q = 0; q <= k; ++q) hcol[q] = (pass == 0 ? 0.0 : hcol[q]) + h[q];
+          if (pass == 1 || wn2 > kReorth2 * wn2_before) {
+            hcol[k + 1] = std::sqrt(wn2);
+            break;
+          }
+          ++reorth;
+          if ((rc = mdot32(c, st, k + 2, h.data()))) return rc;
+          wn2_before = wn2;
+        }
+      }
+      double wn2_before = 0.0;
+      if (!relax) {
+        if ((rc = mdot(c, st, st->V, n3, k + 2, w, h.data()))) return rc;
+        wn2_before = h[k + 1];
+      }
+      for (int pass = 0; pass < 2 && !relax; ++pass) {
         EB_CK(c, cudaMemcpyAsync(st->hdev, h.data(), (k + 1) * sizeof(double), cudaMemcpyHostToDevice, c->stream));
         EB_PROF(c, "k_maxpy");
         k_maxpy<<<(unsigned)((n3 + kAxTile - 1) / kAxTile), kAxThreads, (size_t)(k + 1) * sizeof(double), c->stream>>>(
@@ -1464,7 +1668,7 @@ extern "C" int eb_solve_stokes_system(eb_ctx* c, const eb_solve_opts* o, eb_solv
       est = std::fabs(g[k + 1]) / bnorm;
       if (hk1 > 0.0) {
         EB_PROF(c, "k_axpy");
-        k_scale_copy<<<nblk(n3), kB, 0, c->stream>>>(w, w, 1.0 / hk1, n3);
+        k_scale_copy2<<<nblk(n3), kB, 0, c->stream>>>(w, w32, w, 1.0 / hk1, n3);
         EB_LAUNCHED(c);
       }
       if (est <= target || hk1 == 0.0) { ++k; break; }
@@ -1515,6 +1719,7 @@ extern "C" int eb_solve_stokes_system(eb_ctx* c, const eb_solve_opts* o, eb_solv
   if (rep) {
     rep->iterations = it;
     rep->reorthogonalisations = reorth;
+    rep->relaxed_iterations = relaxed;
     rep->levels = (int32_t)st->H().levels.size();
     rep->rel_residual = rel;
     rep->rel_residual_scaled = rel_s;

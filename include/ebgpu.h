@@ -317,6 +317,9 @@ typedef struct eb_solve_opts {
                                 Stokes only)                                                        */
   int32_t precision;         /* 0: mixed (FP32 V-cycle, FP32 stored directions, FP64 FGMRES);
                                 1: plain FP64 (V-cycle and directions in FP64; Stokes only)          */
+  double  gs_relax;          /* mixed method only: once the FGMRES residual estimate is below
+                                gs_relax x the target, Gram-Schmidt projects with FP32 products on
+                                FP32 copies of the basis; 0 -> 1e3, negative -> never (Stokes only) */
 } eb_solve_opts;
 
 typedef struct eb_solve_report {
@@ -326,6 +329,7 @@ typedef struct eb_solve_report {
   double  rel_residual_scaled; /* the same for the diagonally scaled system             */
   double  seconds;           /* wall time of the solve                                  */
   int32_t reorthogonalisations; /* Gram-Schmidt second passes (severe cancellation only) */
+  int32_t relaxed_iterations;   /* iterations whose Gram-Schmidt ran in FP32 (gs_relax)  */
 } eb_solve_report;
 
 enum eb_stokes_vector {

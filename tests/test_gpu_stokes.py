@@ -341,3 +341,31 @@ def test_mixed_and_fp64_methods_share_one_context(eb):
     assert rep64["iterations"] <= rep32["iterations"] + 2
     assert rep32b["iterations"] == rep32["iterations"]
     mic.close()
+
+
+@pytest.mark.parametrize("gs_relax", [1e3, 1e20])
+@pytest.mark.parametrize("case", ["rift_small", "sinking_block"])
+def test_fp32_gram_schmidt_matches_superlu(eb, case, gs_relax):
+    """The mixed method's FP32 Gram-Schmidt (projection on FP32 copies of the basis below
+    gs_relax x the target): at 1e20 every iteration takes that form (a residual gap left by the
+    FP32 products makes the method restart from its iterate), and the solution still meets 1e-11
+    and equals SuperLU's to 1e-6; gs_relax < 0 switches it off."""
+    model = marker_model(eb, case)
+    o = oracle_for(model)
+    mic = gpu_ctx(eb, model)
+    rep = mic.solve_viscoelastic_stokes_continuity_equations(rtol=1e-11, max_iters=4000, gs_relax=gs_relax)
+    assert rep["status"] == 0 and rep["rel_residual"] <= 1e-11, rep
+    assert rep["relaxed_iterations"] > 0
+    if gs_relax > 1e6:
+        assert rep["relaxed_iterations"] == rep["iterations"], rep
+    S = mic.download_stokes_vector("solution")
+    S_ref = o.solve_direct()
+    for comp in range(3):
+        a, b = S[comp::3], S_ref[comp::3]
+        assert np.abs(a - b).max() <= 1e-6 * np.abs(b).max(), (comp, np.abs(a - b).max() / np.abs(b).max())
+    off = mic.solve_viscoelastic_stokes_continuity_equations(rtol=1e-11, max_iters=4000, gs_relax=-1.0)
+    assert off["status"] == 0 and off["relaxed_iterations"] == 0, off
+    fp64 = mic.solve_viscoelastic_stokes_continuity_equations(rtol=1e-11, max_iters=4000, precision="fp64",
+                                                              gs_relax=1e20)
+    assert fp64["status"] == 0 and fp64["relaxed_iterations"] == 0, fp64   # plain method: never FP32
+    mic.close()
