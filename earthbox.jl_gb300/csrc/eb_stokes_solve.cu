@@ -41,56 +41,86 @@ constexpr int kMaxDots = kMaxRestart + 8;  // dot products per reduction
 unsigned nblk(int64_t n) { return (unsigned)((n + kB - 1) / kB); }
 
 // ------------------------------------------------------- FP64 operator ---
-// y = L x on SoA vectors; optional scaling: y = w .* L (w .* x); optional shift: y -= sub.
-__global__ void k_apply64(const double* __restrict__ coef, const double* __restrict__ x, double* __restrict__ y,
-                          const double* __restrict__ w, int32_t nx, int32_t ny, int64_t nc,
-                          const double* __restrict__ sub = nullptr, float* __restrict__ y32 = nullptr) {
-  const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+// y = L x on SoA vectors [vx | vy | p] (cell c = j ny + i), optionally y -= sub and an FP32
+// copy y32.  The FGMRES iteration passes the pre-scaled stencil W L W (k_prescale), the
+// residual checks the assembled one.  Cell indices fit 32 bits (27 nc doubles of stencil
+// would exceed the device's memory first).
+__global__ void __launch_bounds__(kB) k_apply64(const double* __restrict__ coef, const double* __restrict__ x,
+                                                double* __restrict__ y, int32_t nx, int32_t ny, int32_t nc,
+                                                const double* __restrict__ sub = nullptr,
+                                                float* __restrict__ y32 = nullptr) {
+  const int32_t c = (int32_t)(blockIdx.x * blockDim.x + threadIdx.x);
   if (c >= nc) return;
-  const int32_t i = (int32_t)(c % ny), j = (int32_t)(c / ny);
-  const double *vx = x, *vy = x + nc, *p = x + 2 * nc;
-  const double *wx = w, *wy = w ? w + nc : nullptr, *wp = w ? w + 2 * nc : nullptr;
-  auto X = [&](int64_t k) { return w ? vx[k] * wx[k] : vx[k]; };
-  auto Y = [&](int64_t k) { return w ? vy[k] * wy[k] : vy[k]; };
-  auto Pp = [&](int64_t k) { return w ? p[k] * wp[k] : p[k]; };
+  const int32_t j = c / ny, i = c - j * ny;
+  const double *vx = x, *vy = x + nc, *p = x + 2 * (int64_t)nc;
   const bool hu = i > 0, hd = i < ny - 1, hl = j > 0, hr = j < nx - 1;
   auto cf = [&](int s) { return __ldg(&coef[(int64_t)s * nc + c]); };
-  double ax = cf(0) * X(c);
-  if (hl) ax += cf(1) * X(c - ny);
-  if (hr) ax += cf(2) * X(c + ny);
-  if (hu) ax += cf(3) * X(c - 1);
-  if (hd) ax += cf(4) * X(c + 1);
-  if (hu) ax += cf(5) * Y(c - 1);
-  if (hu && hr) ax += cf(6) * Y(c + ny - 1);
-  ax += cf(7) * Y(c);
-  if (hr) ax += cf(8) * Y(c + ny);
-  ax += cf(9) * Pp(c);
-  if (hr) ax += cf(10) * Pp(c + ny);
-  double ay = cf(11) * Y(c);
-  if (hu) ay += cf(12) * Y(c - 1);
-  if (hd) ay += cf(13) * Y(c + 1);
-  if (hl) ay += cf(14) * Y(c - ny);
-  if (hr) ay += cf(15) * Y(c + ny);
-  if (hl) ay += cf(16) * X(c - ny);
-  ay += cf(17) * X(c);
-  if (hl && hd) ay += cf(18) * X(c + 1 - ny);
-  if (hd) ay += cf(19) * X(c + 1);
-  ay += cf(20) * Pp(c);
-  if (hd) ay += cf(21) * Pp(c + 1);
-  double ap = cf(22) * Pp(c);
-  if (hl) ap += cf(23) * X(c - ny);
-  ap += cf(24) * X(c);
-  if (hu) ap += cf(25) * Y(c - 1);
-  ap += cf(26) * Y(c);
-  if (w) { ax *= wx[c]; ay *= wy[c]; ap *= wp[c]; }
-  if (sub) { ax -= sub[c]; ay -= sub[nc + c]; ap -= sub[2 * nc + c]; }
+  double ax = cf(0) * vx[c];
+  if (hl) ax += cf(1) * vx[c - ny];
+  if (hr) ax += cf(2) * vx[c + ny];
+  if (hu) ax += cf(3) * vx[c - 1];
+  if (hd) ax += cf(4) * vx[c + 1];
+  if (hu) ax += cf(5) * vy[c - 1];
+  if (hu && hr) ax += cf(6) * vy[c + ny - 1];
+  ax += cf(7) * vy[c];
+  if (hr) ax += cf(8) * vy[c + ny];
+  ax += cf(9) * p[c];
+  if (hr) ax += cf(10) * p[c + ny];
+  double ay = cf(11) * vy[c];
+  if (hu) ay += cf(12) * vy[c - 1];
+  if (hd) ay += cf(13) * vy[c + 1];
+  if (hl) ay += cf(14) * vy[c - ny];
+  if (hr) ay += cf(15) * vy[c + ny];
+  if (hl) ay += cf(16) * vx[c - ny];
+  ay += cf(17) * vx[c];
+  if (hl && hd) ay += cf(18) * vx[c + 1 - ny];
+  if (hd) ay += cf(19) * vx[c + 1];
+  ay += cf(20) * p[c];
+  if (hd) ay += cf(21) * p[c + 1];
+  double ap = cf(22) * p[c];
+  if (hl) ap += cf(23) * vx[c - ny];
+  ap += cf(24) * vx[c];
+  if (hu) ap += cf(25) * vy[c - 1];
+  ap += cf(26) * vy[c];
+  if (sub) {
+    ax -= sub[c];
+    ay -= sub[nc + c];
+    ap -= sub[2 * (int64_t)nc + c];
+  }
   y[c] = ax;
   y[nc + c] = ay;
-  y[2 * nc + c] = ap;
+  y[2 * (int64_t)nc + c] = ap;
   if (y32) {  // FP32 copy for the FP32 Gram-Schmidt products
     y32[c] = (float)ax;
     y32[nc + c] = (float)ay;
-    y32[2 * nc + c] = (float)ap;
+    y32[2 * (int64_t)nc + c] = (float)ap;
+  }
+}
+// Stencil slots of k_apply64: row block (0 vx, 1 vy, 2 p), column block, and the neighbour
+// cell (i + di, j + dj) whose unknown the slot multiplies.
+struct StencilSlot {
+  int8_t row, col, di, dj;
+};
+__constant__ StencilSlot kSlots[27] = {
+    {0, 0, 0, 0},  {0, 0, 0, -1}, {0, 0, 0, 1},  {0, 0, -1, 0}, {0, 0, 1, 0},  {0, 1, -1, 0}, {0, 1, -1, 1},
+    {0, 1, 0, 0},  {0, 1, 0, 1},  {0, 2, 0, 0},  {0, 2, 0, 1},  {1, 1, 0, 0},  {1, 1, -1, 0}, {1, 1, 1, 0},
+    {1, 1, 0, -1}, {1, 1, 0, 1},  {1, 0, 0, -1}, {1, 0, 0, 0},  {1, 0, 1, -1}, {1, 0, 1, 0},  {1, 2, 0, 0},
+    {1, 2, 1, 0},  {2, 2, 0, 0},  {2, 0, 0, -1}, {2, 0, 0, 0},  {2, 1, -1, 0}, {2, 1, 0, 0}};
+// coefS[s][c] = w_row(c) coef[s][c] w_col(neighbour): the stencil of W L W, so that the
+// scaled product costs one FMA per slot (0 where the neighbour lies outside the grid).
+__global__ void k_prescale(const double* __restrict__ coef, const double* __restrict__ w,
+                           double* __restrict__ coefS, int32_t nx, int32_t ny, int32_t nc) {
+  const int32_t c = (int32_t)(blockIdx.x * blockDim.x + threadIdx.x);
+  if (c >= nc) return;
+  const int32_t j = c / ny, i = c - j * ny;
+#pragma unroll
+  for (int s = 0; s < 27; ++s) {
+    const StencilSlot q = kSlots[s];
+    const int32_t ii = i + q.di, jj = j + q.dj;
+    double v = 0.0;
+    if (ii >= 0 && ii < ny && jj >= 0 && jj < nx)
+      v = w[(int64_t)q.row * nc + c] * coef[(int64_t)s * nc + c] * w[(int64_t)q.col * nc + jj * ny + ii];
+    coefS[(int64_t)s * nc + c] = v;
   }
 }
 
@@ -230,41 +260,65 @@ __global__ void k_maxpy_f32(double* __restrict__ u, const float* __restrict__ Z,
 // products on those copies: half the bytes, and the FP32 pipe instead of the FP64 one that
 // bounds k_mdot / k_maxpy.  The new direction itself stays FP64, and its norm is measured.
 //
-// dots: block (b, v) reduces a grid-stride slice of V32_v . u32 over float4 chunks
-// (n4 = ld32 / 4); four FP32 partial sums per thread (about 50 chunks each at 14M unknowns)
-// go to FP64 for the block reduction.
+// dots: block (b, g) reduces a grid-stride slice of V32_v . u32 for the four vectors
+// v = 4g .. 4g+3 (< nv) over float4 chunks (n4 = ld32 / 4), so each chunk of u32 is read once
+// per four vectors; FP32 partial sums per thread (about 50 chunks each at 14M unknowns) go to
+// FP64 for the block reduction.  partial[v * gridDim.x + b].
+constexpr int kDot32Vecs = 4;
 __global__ void __launch_bounds__(kB) k_mdot32(const float* __restrict__ V, int64_t ld, const float* __restrict__ u,
-                                               int64_t n4, double* __restrict__ partial) {
-  const float4* a = reinterpret_cast<const float4*>(V + (int64_t)blockIdx.y * ld);
+                                               int64_t n4, int nv, double* __restrict__ partial) {
+  const int v0 = blockIdx.y * kDot32Vecs;
+  const int nvb = min(kDot32Vecs, nv - v0);
   const float4* b = reinterpret_cast<const float4*>(u);
-  float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f;
+  const float4* a[kDot32Vecs];
+#pragma unroll
+  for (int g = 0; g < kDot32Vecs; ++g)
+    a[g] = reinterpret_cast<const float4*>(V + (int64_t)(v0 + min(g, nvb - 1)) * ld);
+  float4 s[kDot32Vecs];
+#pragma unroll
+  for (int g = 0; g < kDot32Vecs; ++g) s[g] = make_float4(0.f, 0.f, 0.f, 0.f);
+  auto acc4 = [](const float4 x, const float4 y, float4& t) {
+    t.x = fmaf(x.x, y.x, t.x);
+    t.y = fmaf(x.y, y.y, t.y);
+    t.z = fmaf(x.z, y.z, t.z);
+    t.w = fmaf(x.w, y.w, t.w);
+  };
   const int64_t step = (int64_t)gridDim.x * blockDim.x;
   int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  auto acc4 = [&](const float4 x, const float4 y) {
-    s0 = fmaf(x.x, y.x, s0);
-    s1 = fmaf(x.y, y.y, s1);
-    s2 = fmaf(x.z, y.z, s2);
-    s3 = fmaf(x.w, y.w, s3);
-  };
-  for (; k + 3 * step < n4; k += 4 * step) {  // eight 16-byte loads in flight
-    const float4 a0 = __ldcs(a + k), a1 = __ldcs(a + k + step), a2 = __ldcs(a + k + 2 * step),
-                 a3 = __ldcs(a + k + 3 * step);
-    const float4 u0 = __ldg(b + k), u1 = __ldg(b + k + step), u2 = __ldg(b + k + 2 * step), u3 = __ldg(b + k + 3 * step);
-    acc4(a0, u0);
-    acc4(a1, u1);
-    acc4(a2, u2);
-    acc4(a3, u3);
+  for (; k + step < n4; k += 2 * step) {  // up to ten 16-byte loads in flight
+    const float4 u0 = __ldg(b + k), u1 = __ldg(b + k + step);
+    float4 x0[kDot32Vecs], x1[kDot32Vecs];
+#pragma unroll
+    for (int g = 0; g < kDot32Vecs; ++g)
+      if (g < nvb) {
+        x0[g] = __ldcs(a[g] + k);
+        x1[g] = __ldcs(a[g] + k + step);
+      }
+#pragma unroll
+    for (int g = 0; g < kDot32Vecs; ++g)
+      if (g < nvb) {
+        acc4(x0[g], u0, s[g]);
+        acc4(x1[g], u1, s[g]);
+      }
   }
-  for (; k < n4; k += step) acc4(a[k], b[k]);
-  double s = ((double)s0 + (double)s1) + ((double)s2 + (double)s3);
-  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-  __shared__ double sh[kB / 32];
-  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = s;
+  if (k < n4) {
+    const float4 u0 = __ldg(b + k);
+#pragma unroll
+    for (int g = 0; g < kDot32Vecs; ++g)
+      if (g < nvb) acc4(__ldcs(a[g] + k), u0, s[g]);
+  }
+  __shared__ double sh[kDot32Vecs][kB / 32];
+#pragma unroll
+  for (int g = 0; g < kDot32Vecs; ++g) {
+    double t = ((double)s[g].x + (double)s[g].y) + ((double)s[g].z + (double)s[g].w);
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+    if ((threadIdx.x & 31) == 0) sh[g][threadIdx.x >> 5] = t;
+  }
   __syncthreads();
-  if (threadIdx.x == 0) {
+  if ((int)threadIdx.x < nvb) {
     double t = 0.0;
-    for (int w = 0; w < kB / 32; ++w) t += sh[w];
-    partial[(int64_t)blockIdx.y * gridDim.x + blockIdx.x] = t;
+    for (int w = 0; w < kB / 32; ++w) t += sh[threadIdx.x][w];
+    partial[(int64_t)(v0 + threadIdx.x) * gridDim.x + blockIdx.x] = t;
   }
 }
 // u -= sum_v h[v] V32_v, the sum formed in FP32 and subtracted from the FP64 u; u32 = float(u)
@@ -896,6 +950,7 @@ struct StokesState {
   Hierarchy& H() { return hier[mg64 ? 1 : 0]; }
   double *w = nullptr, *prep = nullptr;  // scaling and pressure factor
   double* winv = nullptr;                // 1 / w
+  double* coefS = nullptr;               // stencil of W L W [27][nc]
   // FGMRES workspace
   int m = 0;
   double *V = nullptr, *r = nullptr, *t = nullptr, *xs = nullptr, *bs = nullptr, *zp = nullptr, *zt = nullptr;
@@ -1319,8 +1374,8 @@ int mdot(eb_ctx* c, StokesState* st, const double* V, int64_t stride, int nv, co
 // h[v] = V32_v . V32_{nv-1} for v < nv (the last slot holds the FP32 copy of the new direction)
 int mdot32(eb_ctx* c, StokesState* st, int nv, double* h) {
   EB_PROF(c, "k_mdot32");
-  k_mdot32<<<dim3(st->nb_dot, nv), kB, 0, c->stream>>>(st->V32, st->ld32, st->V32 + (size_t)(nv - 1) * st->ld32,
-                                                       st->ld32 / 4, st->partial);
+  k_mdot32<<<dim3(st->nb_dot, (nv + kDot32Vecs - 1) / kDot32Vecs), kB, 0, c->stream>>>(
+      st->V32, st->ld32, st->V32 + (size_t)(nv - 1) * st->ld32, st->ld32 / 4, nv, st->partial);
   EB_LAUNCHED(c);
   EB_PROF(c, "k_mdot_final");
   k_mdot_final<<<nv, kB, 0, c->stream>>>(st->partial, st->nb_dot, st->dots);
@@ -1347,7 +1402,7 @@ int maxpy32(eb_ctx* c, StokesState* st, double* w, float* w32, int nv, double* w
 int apply_scaled(eb_ctx* c, StokesState* st, const double* x, double* y) {
   const StokesSystem& s = st->sys;
   EB_PROF(c, "k_apply64");
-  k_apply64<<<nblk(s.nc), kB, 0, c->stream>>>(s.coef, x, y, st->w, s.nx, s.ny, s.nc);
+  k_apply64<<<nblk(s.nc), kB, 0, c->stream>>>(st->coefS, x, y, s.nx, s.ny, (int32_t)s.nc);
   EB_LAUNCHED(c);
   return EB_OK;
 }
@@ -1449,6 +1504,11 @@ int prepare(eb_ctx* c, StokesState* st, int sweeps, int m, bool fp64) {
   const StokesSystem& s = st->sys;
   EB_PROF(c, "k_scaling");
   k_scaling<<<nblk(s.nc), kB, 0, c->stream>>>(s.coef, c->gf[EB_G_ETAN0], s.pscale, st->w, st->prep, st->winv, s.nc);
+  EB_LAUNCHED(c);
+  if (s.nc >= (int64_t)1 << 30) return eb_fail(c, EB_BAD_INPUT, "Stokes grid exceeds 2^30 cells");
+  if (!st->coefS && (rc = dalloc(c, st->allocs, &st->coefS, (size_t)kStencilSlots * s.nc))) return rc;
+  EB_PROF(c, "k_scaling");
+  k_prescale<<<nblk(s.nc), kB, 0, c->stream>>>(s.coef, st->w, st->coefS, s.nx, s.ny, (int32_t)s.nc);
   EB_LAUNCHED(c);
   return EB_OK;
 }
@@ -1593,7 +1653,7 @@ extern "C" int eb_solve_stokes_system(eb_ctx* c, const eb_solve_opts* o, eb_solv
       float* w32 = V32 ? V32 + (size_t)(k + 1) * st->ld32 : nullptr;
       const bool relax = V32 && std::fabs(g[k]) <= relax_fac * target * bnorm;
       EB_PROF(c, "k_apply64");
-      k_apply64<<<nblk(s.nc), kB, 0, c->stream>>>(s.coef, st->zt, w, st->w, s.nx, s.ny, s.nc, vk,
+      k_apply64<<<nblk(s.nc), kB, 0, c->stream>>>(st->coefS, st->zt, w, s.nx, s.ny, (int32_t)s.nc, vk,
                                                   relax ? w32 : nullptr);
       EB_LAUNCHED(c);
       // Classical Gram-Schmidt.  One reduction gives V^T d and |d|^2 (d is the slot after V_k);
@@ -1696,7 +1756,7 @@ extern "C" int eb_solve_stokes_system(eb_ctx* c, const eb_solve_opts* o, eb_solv
   k_mul<<<nblk(n3), kB, 0, c->stream>>>(s.S, st->xs, st->w, n3, 0);
   EB_LAUNCHED(c);
   EB_PROF(c, "k_apply64");
-  k_apply64<<<nblk(s.nc), kB, 0, c->stream>>>(s.coef, s.S, st->t, nullptr, s.nx, s.ny, s.nc);
+  k_apply64<<<nblk(s.nc), kB, 0, c->stream>>>(s.coef, s.S, st->t, s.nx, s.ny, (int32_t)s.nc);
   EB_LAUNCHED(c);
   EB_PROF(c, "k_axpy");
   k_sub<<<nblk(n3), kB, 0, c->stream>>>(st->r, s.rhs, st->t, n3);
@@ -1874,7 +1934,7 @@ extern "C" int eb_stokes_nonlinear_residual(eb_ctx* c) {
   StokesSystem& s = c->st->sys;
   double* tmp = c->st->il;  // N doubles
   EB_PROF(c, "k_apply64");
-  k_apply64<<<nblk(s.nc), kB, 0, c->stream>>>(s.coef, s.S_old, tmp, nullptr, s.nx, s.ny, s.nc);
+  k_apply64<<<nblk(s.nc), kB, 0, c->stream>>>(s.coef, s.S_old, tmp, s.nx, s.ny, (int32_t)s.nc);
   EB_LAUNCHED(c);
   EB_PROF(c, "k_axpy");
   k_abs_sub<<<nblk(3 * s.nc), kB, 0, c->stream>>>(s.resnl, tmp, s.rhs, 3 * s.nc);
@@ -2024,7 +2084,7 @@ extern "C" int eb_stokes_apply(eb_ctx* c, const double* x, double* y) {
   k_deinterleave<<<nblk(s.nc), kB, 0, c->stream>>>(c->st->il, xin, s.nc);
   EB_LAUNCHED(c);
   EB_PROF(c, "k_apply64");
-  k_apply64<<<nblk(s.nc), kB, 0, c->stream>>>(s.coef, xin, c->st->il, nullptr, s.nx, s.ny, s.nc);
+  k_apply64<<<nblk(s.nc), kB, 0, c->stream>>>(s.coef, xin, c->st->il, s.nx, s.ny, (int32_t)s.nc);
   EB_LAUNCHED(c);
   EB_PROF(c, "k_interleave");
   k_interleave<<<nblk(s.nc), kB, 0, c->stream>>>(c->st->il, xin, s.nc);
