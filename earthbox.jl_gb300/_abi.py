@@ -186,7 +186,11 @@ class RecycleParams(C.Structure):
                 ("matid_asthenosphere", C.c_int32), ("xsize", C.c_double), ("ysize", C.c_double),
                 ("velocity_y_upper", C.c_double), ("velocity_y_lower", C.c_double),
                 ("temperature_bottom", C.c_double), ("iuse_random_fric", C.c_int32), ("delta_fric_coef", C.c_double),
-                ("seed", C.c_uint64), ("counter", C.c_int64)]
+                ("seed", C.c_uint64), ("counter", C.c_int64), ("asymmetric", C.c_int32),
+                ("full_velocity_contraction", C.c_double), ("sticky_thickness_left", C.c_double),
+                ("sticky_thickness_right", C.c_double), ("layer_thickness", C.c_double * 6),
+                ("x_left_strong", C.c_double), ("x_right_strong", C.c_double), ("matid_layers", C.c_int32 * 7),
+                ("matid_strong", C.c_int32 * 3)]
 
 
 class HeatParams(C.Structure):

@@ -55,7 +55,8 @@ __host__ __device__ inline void uniforms(uint64_t seed, int64_t step, uint32_t s
 }
 
 struct RecycleK {
-  int32_t type;                                 // 1 extension, 2 extension without bottom inflow, 3 channel
+  int32_t type;                                 // 1 extension, 2 extension without bottom inflow, 3 channel,
+                                                // 4 contraction
   int16_t sticky_air, sticky_water, asth;
   double xsize, ysize, disp_top, disp_bottom;  // disp_top = |vyu dt|, disp_bottom = -|vyl dt|
   double t_top, t_bottom, p_reset;
@@ -65,7 +66,42 @@ struct RecycleK {
   double delta_fric;
   uint64_t seed;
   int64_t step;
+  // contraction: side band, sticky thickness at the two sides, layer bases (cumulative
+  // thicknesses), strong-zone limits and the seven-layer / strong-zone material ids
+  int32_t asym;
+  double disp_side, sticky_l, sticky_r;
+  double depth[6];
+  double x_left_strong, x_right_strong;
+  int16_t layer_id[7], strong_id[3];
 };
+
+// SevenLayerEarthModel2D.define_material (marker_materials/init_manager/utils/
+// SevenLayerEarthModel2D.jl:20-62) followed by StrongRegions.define_material
+// (init_manager/utils/StrongRegions.jl:24-80), as ContractionViscoelastic.define_material
+// applies them (types/ContractionViscoelastic.jl:113-134, strong zones on).
+__device__ int16_t contraction_material(double x, double y, const RecycleK& p) {
+  const double* d = p.depth;
+  int16_t id = p.layer_id[6];
+  if (y <= d[0]) id = p.layer_id[0];
+  else if (y > d[0] && y <= d[1]) id = p.layer_id[1];
+  else if (y > d[1] && y <= d[2]) id = p.layer_id[2];
+  else if (y > d[2] && y <= d[3]) id = p.layer_id[3];
+  else if (y > d[3] && y <= d[4]) id = p.layer_id[4];
+  else if (y > d[4] && y <= d[5]) id = p.layer_id[5];
+  const bool outside = x < p.x_left_strong || x > p.x_right_strong;
+  if (d[0] < y && y <= d[1]) {
+    if (outside) id = p.strong_id[0];
+  } else if (d[1] < y && y <= d[2]) {
+    if (outside) id = p.strong_id[1];
+  } else if (d[2] < y && y <= d[3]) {
+    if (outside) id = p.strong_id[2];
+  } else if (d[3] < y && y <= d[4]) {
+    if (outside) id = p.strong_id[2];
+  } else if (d[4] < y && y <= d[5]) {
+    if (outside) id = p.strong_id[2];
+  }
+  return id;
+}
 
 __device__ __forceinline__ bool sticky(int16_t m, const RecycleK& p) { return m == p.sticky_air || m == p.sticky_water; }
 // the markers a recycling type moves: outside the domain, or (channel) below the grid
@@ -73,9 +109,10 @@ __device__ __forceinline__ bool selected(const DevMarkers& mk, int64_t m, const 
   if (m >= mk.M) return false;
   return p.type == 3 ? mk.y[m] > p.gridy_max : mk.inside[m] != 1;
 }
-// sticky rank (air/water positions): extension only; the other types treat every marker alike
+// sticky rank (air/water positions): extension and contraction; the other types treat every
+// marker alike
 __device__ __forceinline__ bool sticky_sel(const DevMarkers& mk, int64_t m, const RecycleK& p) {
-  return p.type == 1 && sticky(mk.matid[m], p);
+  return (p.type == 1 || p.type == 4) && sticky(mk.matid[m], p);
 }
 
 // per block: number of outside markers and of outside sticky markers
@@ -91,8 +128,9 @@ __global__ void k_recycle_count(DevMarkers mk, RecycleK p, int32_t* __restrict__
 }
 
 // ranks in marker order, new positions and property resets; list[r] = 1-based index
-__global__ void k_recycle_apply(DevMarkers mk, RecycleK p, const int32_t* __restrict__ offsets, int32_t nblocks,
-                                int64_t n_air, int64_t* __restrict__ list, int8_t* __restrict__ flags) {
+__global__ void k_recycle_apply(DevMarkers mk, DevMats mt, RecycleK p, const int32_t* __restrict__ offsets,
+                                int32_t nblocks, int64_t n_out, int64_t n_air, int64_t* __restrict__ list,
+                                int8_t* __restrict__ flags) {
   __shared__ int32_t s_out[kB / 32], s_st[kB / 32];
   const int64_t m = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const bool out = selected(mk, m, p);
@@ -136,6 +174,60 @@ __global__ void k_recycle_apply(DevMarkers mk, RecycleK p, const int32_t* __rest
     mk.pfailure[m] = 0.0f;
     mk.fric_ini[m] = p.fric_air;
     mk.fric[m] = p.fric_air;
+    return;
+  }
+  if (p.type == 4) {
+    // ContractionViscoelastic.execute_recycle_steps (types/ContractionViscoelastic.jl:60-111):
+    // the k-th sticky / subsurface marker takes the k-th position of its group; the first
+    // floor(n/2) of a group (none when asymmetric) enter at the left side, x = 0 + u d,
+    // the others at the right, x = xsize + u (-d) (ContractionRecycleLocations.jl:9-140);
+    // sticky markers in y = 0 + u h, subsurface ones in y = h + u (ysize - h), h the sticky
+    // thickness of that side.
+    const bool air = st;
+    const int64_t r = air ? (int64_t)r_st : (int64_t)r_out - r_st;
+    const int64_t ngrp = air ? n_air : n_out - n_air;
+    const int64_t nleft = p.asym ? 0 : ngrp / 2;
+    uniforms(p.seed, p.step, air ? 0u : 1u, r, ux, uy);
+    const bool left = r < nleft;
+    const double h = left ? p.sticky_l : p.sticky_r;
+    const double x = (left ? 0.0 : p.xsize) + ux * (left ? p.disp_side : -p.disp_side);
+    const double y = air ? 0.0 + uy * h : h + uy * (p.ysize - h);
+    mk.x[m] = x;
+    mk.y[m] = y;
+    list[r_out] = m + 1;
+    flags[r_out] = air ? 0 : 1;
+    double fric;
+    if (air) {
+      mk.matid[m] = p.sticky_air;
+      mk.tk[m] = p.t_top;
+      mk.pr[m] = 0.0;
+      mk.sxx[m] = 0.0; mk.sxy[m] = 0.0;
+      mk.exx[m] = 0.0; mk.exy[m] = 0.0;
+      mk.eta[m] = 0.0;
+      fric = p.fric_air;
+    } else {
+      // get_subsurface_reset_properties_viscoelastic_contraction (ContractionViscoelastic.jl:
+      // 69-111): material at the new position, pressure 3300 * 9.81 * y, temperature 0
+      const int16_t id = contraction_material(x, y, p);
+      mk.matid[m] = id;
+      mk.tk[m] = 0.0;
+      mk.pr[m] = 3300.0 * 9.81 * y;
+      mk.sxx[m] = 1.96e6; mk.sxy[m] = 1.96e6;
+      mk.exx[m] = 1e-14; mk.exy[m] = 1e-14;
+      mk.eta[m] = 1e20;
+      fric = __ldg(&mt.plastic[2 * (size_t)mt.nmat + (id - 1)]);  // mat_plastic[id, 3]
+      if (p.random_fric == 1) {
+        double r0, r1;
+        uniforms(p.seed, p.step, 2u, m, r0, r1);
+        if (r0 <= 0.5) fric = fric - p.delta_fric;
+      }
+    }
+    mk.sr_ratio[m] = 0.0;
+    mk.gii[m] = 0.0; mk.sp[m] = 0.0; mk.srp[m] = 0.0;
+    mk.melt[m] = 0.0;
+    mk.pfailure[m] = 0.0f;
+    mk.fric_ini[m] = fric;
+    mk.fric[m] = fric;
     return;
   }
   if (st && n_air > 0) {
@@ -192,10 +284,16 @@ extern "C" int eb_recycle_markers(eb_ctx* c, const eb_recycle_params* rp, int64_
                                   int64_t* nrecycle_subsurface) {
   if (!c || !rp) return EB_BAD_INPUT;
   if (!c->have_grid || !c->have_params || !c->have_mats) return eb_fail(c, EB_NOT_READY, "grid, parameters and materials must be set");
-  if (rp->recycle_type < 1 || rp->recycle_type > 3)
-    return eb_fail(c, EB_BAD_INPUT, "recycle_type must be 1 (extension), 2 (extension without bottom inflow) or 3 (channel)");
+  if (rp->recycle_type < 1 || rp->recycle_type > 4)
+    return eb_fail(c, EB_BAD_INPUT, "recycle_type must be 1 (extension), 2 (extension without bottom inflow), "
+                                    "3 (channel) or 4 (contraction)");
   const int64_t nmat = c->mats.nmat;
-  for (int64_t id : {(int64_t)rp->matid_sticky_air, (int64_t)rp->matid_sticky_water, (int64_t)rp->matid_asthenosphere})
+  std::vector<int64_t> ids = {rp->matid_sticky_air, rp->matid_sticky_water, rp->matid_asthenosphere};
+  if (rp->recycle_type == 4) {
+    ids.insert(ids.end(), rp->matid_layers, rp->matid_layers + 7);
+    ids.insert(ids.end(), rp->matid_strong, rp->matid_strong + 3);
+  }
+  for (int64_t id : ids)
     if (id < 1 || id > nmat) return eb_fail(c, EB_BAD_INPUT, "recycle material id outside the material table");
   if (c->M > 0 && c->matid_min < 1) return eb_fail(c, EB_NOT_READY, "marker_matid has not been uploaded");
   cudaSetDevice(c->device);
@@ -223,6 +321,22 @@ extern "C" int eb_recycle_markers(eb_ctx* c, const eb_recycle_params* rp, int64_
              3300.0 * 9.81 * c->h_gy.back(), c->h_gy.back(), c->h_gy.back() - c->h_gy.front(),
              mp[2 * nmat + rp->matid_sticky_air - 1], mp[2 * nmat + rp->matid_asthenosphere - 1],
              rp->iuse_random_fric, rp->delta_fric_coef, rp->seed, rp->counter};
+  if (rp->recycle_type == 4) {
+    // ContractionRecycleLocations.get_displacement_velocity: |v| dt / 2, or |v| dt asymmetric
+    p.asym = rp->asymmetric ? 1 : 0;
+    p.disp_side = p.asym ? std::fabs(rp->full_velocity_contraction) * c->P.timestep
+                         : std::fabs(rp->full_velocity_contraction) * c->P.timestep * 0.5;
+    p.sticky_l = rp->sticky_thickness_left;
+    p.sticky_r = rp->sticky_thickness_right;
+    // Layers.calc_depths_for_layers (markers/utils/Layers.jl:31-54): running sums
+    double base = rp->layer_thickness[0];
+    p.depth[0] = base;
+    for (int k = 1; k < 6; ++k) p.depth[k] = base = base + rp->layer_thickness[k];
+    p.x_left_strong = rp->x_left_strong;
+    p.x_right_strong = rp->x_right_strong;
+    for (int k = 0; k < 7; ++k) p.layer_id[k] = (int16_t)rp->matid_layers[k];
+    for (int k = 0; k < 3; ++k) p.strong_id[k] = (int16_t)rp->matid_strong[k];
+  }
   k_recycle_count<<<nblocks, kB, 0, c->stream>>>(dev_markers(c), p, d_counts, nblocks);
   c->launches++;
   std::vector<int32_t> h(2 * (size_t)nblocks);
@@ -253,8 +367,8 @@ extern "C" int eb_recycle_markers(eb_ctx* c, const eb_recycle_params* rp, int64_
     e = cudaMemcpyAsync(d_counts, h.data(), h.size() * sizeof(int32_t), cudaMemcpyHostToDevice, c->stream);
     if (e == cudaSuccess) {
       EB_PROF(c, "k_recycle_apply");
-      k_recycle_apply<<<nblocks, kB, 0, c->stream>>>(dev_markers(c), p, d_counts, nblocks, n_air, c->recycle_list,
-                                                     c->recycle_flags);
+      k_recycle_apply<<<nblocks, kB, 0, c->stream>>>(dev_markers(c), c->mats, p, d_counts, nblocks, n_out, n_air,
+                                                     c->recycle_list, c->recycle_flags);
       c->launches++;
       prof_end(c);
       e = cudaGetLastError();

@@ -569,7 +569,7 @@ typedef struct eb_recycle_params {
                                       band vyu dt with its sign); 3: channel (types/Channel.jl:20-54:
                                       markers below gridy_b[ynum] move up by the grid height and
                                       their temperature by temperature_top - temperature_bottom; the
-                                      inside flags are not used)                                     */
+                                      inside flags are not used); 4: contraction (fields below)      */
   int32_t matid_sticky_air, matid_sticky_water, matid_asthenosphere;  /* material ids                 */
   double  xsize, ysize;            /* model size (m); the domain starts at x = y = 0                    */
   double  velocity_y_upper, velocity_y_lower;  /* vyu, vyl (m/s): band widths |v dt|                   */
@@ -578,6 +578,20 @@ typedef struct eb_recycle_params {
   double  delta_fric_coef;
   uint64_t seed;                   /* Philox key                                                        */
   int64_t counter;                 /* e.g. the time-step number: new numbers every call                 */
+  /* recycle_type 4: contraction (ViscoelasticContraction -> types/ContractionViscoelastic.jl:20-134):
+     outside sticky and subsurface markers re-enter at the two sides (ContractionRecycleLocations.jl),
+     subsurface ones as the seven-layer / strong-zone material of their new position at pressure
+     3300 * 9.81 * y and temperature 0                                                              */
+  int32_t asymmetric;              /* 1: every marker enters at the right side (band |v| dt), 0: half at
+                                      each side (band |v| dt / 2)                                   */
+  double  full_velocity_contraction;  /* m/s                                                         */
+  double  sticky_thickness_left, sticky_thickness_right;  /* StickyThickness.get_sticky_thickness (m) */
+  double  layer_thickness[6];      /* thick_air, upper crust, lower crust, upper / middle / lower mantle
+                                      lithosphere (LithosphericExtension.get_layer_thickness)       */
+  double  x_left_strong, x_right_strong;  /* strong zones outside [x_left_strong, x_right_strong]     */
+  int32_t matid_layers[7];         /* Atmosphere, UpperContinentalCrust, LowerContinentalCrust,
+                                      Upper-, Middle-, LowerMantleLithosphere, Asthenosphere        */
+  int32_t matid_strong[3];         /* Upper-, LowerContinentalCrustStrongZone, LithosphericMantleStrongZone */
 } eb_recycle_params;
 int eb_recycle_markers(eb_ctx* ctx, const eb_recycle_params* p, int64_t* nrecycle_air, int64_t* nrecycle_subsurface);
 /* The markers of the last eb_recycle_markers: 1-based indices and flags (0 sticky, 1 subsurface),

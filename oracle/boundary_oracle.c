@@ -17,6 +17,10 @@
  *        reference's rand() replaced by the Philox-4x32-10 stream of o_recycle_uniforms
  *   o_recycle_no_bottom_inflow      marker_recycle/types/ExtensionNoBottomInflow.jl:25-123
  *   o_recycle_channel               marker_recycle/types/Channel.jl:20-54
+ *   o_recycle_contraction           marker_recycle/types/ContractionViscoelastic.jl:20-134 with
+ *       utils/ContractionRecycleLocations.jl:9-140, CountRecycle.jl:19-29, Coordinates.jl:223-293,
+ *       marker_materials/init_manager/utils/{SevenLayerEarthModel2D.jl:20-62,StrongRegions.jl:24-80},
+ *       markers/utils/Layers.jl:31-54
  *
  * Grids are column-major (rows, cols).  Julia's x^2 and x^3 of a Float64 literal power
  * are x*x and x*x*x.
@@ -279,4 +283,123 @@ int64_t o_recycle_channel(int64_t M, double* y, double* tk, double gridy_min, do
       list[n++] = m + 1;
     }
   return n;
+}
+
+/* SevenLayerEarthModel2D.define_material then StrongRegions.define_material with the layer
+ * bases of Layers.calc_depths_for_layers (base[k] = base[k-1] + thick[k]).
+ * ids: layers[0..6] (air, upper crust, lower crust, upper / middle / lower lithosphere,
+ * asthenosphere), strong[0..2] (upper crust, lower crust, lithosphere). */
+static int16_t contraction_define_material(double x, double y, const double* thick, double x_left, double x_right,
+                                           const int16_t* layers, const int16_t* strong) {
+  const double d1 = thick[0], d2 = d1 + thick[1], d3 = d2 + thick[2], d4 = d3 + thick[3], d5 = d4 + thick[4],
+               d6 = d5 + thick[5];
+  int16_t id = layers[6];
+  if (y <= d1) id = layers[0];
+  else if (y > d1 && y <= d2) id = layers[1];
+  else if (y > d2 && y <= d3) id = layers[2];
+  else if (y > d3 && y <= d4) id = layers[3];
+  else if (y > d4 && y <= d5) id = layers[4];
+  else if (y > d5 && y <= d6) id = layers[5];
+  if (d1 < y && y <= d2) {
+    if (x < x_left || x > x_right) id = strong[0];
+  } else if (d2 < y && y <= d3) {
+    if (x < x_left || x > x_right) id = strong[1];
+  } else if (d3 < y && y <= d4) {
+    if (x < x_left || x > x_right) id = strong[2];
+  } else if (d4 < y && y <= d5) {
+    if (x < x_left || x > x_right) id = strong[2];
+  } else if (d5 < y && y <= d6) {
+    if (x < x_left || x > x_right) id = strong[2];
+  }
+  return id;
+}
+
+/* ContractionRecycleLocations.calculate_recycled_*_locations for one group (n positions):
+ * the first nleft = floor(n/2) (0 when asymmetric; CountRecycle.get_left_and_right_recycle_counts)
+ * at the left side, the rest at the right; y = y0 + u_y height, x = x0 + u_x disp
+ * (Coordinates.update_recycled_coordinates_vertical_boundary!).  Uniform pair j of `stream`. */
+static void contraction_positions(int64_t n, int64_t asym, int air, double xsize, double ysize, double disp,
+                                  double h_left, double h_right, uint64_t seed, int64_t step, uint32_t stream,
+                                  double* newx, double* newy) {
+  const int64_t nleft = asym ? 0 : n / 2;
+  for (int64_t j = 0; j < n; ++j) {
+    double ux, uy;
+    o_recycle_uniforms(seed, step, stream, j, &ux, &uy);
+    const int left = j < nleft;
+    const double h = left ? h_left : h_right;
+    const double y_initial = air ? 0.0 : h, y_height = air ? h : ysize - h;
+    const double x_initial = left ? 0.0 : xsize, displacement_x = left ? disp : -disp;
+    newy[j] = y_initial + uy * y_height;
+    newx[j] = x_initial + ux * displacement_x;
+  }
+}
+
+/* ContractionViscoelastic.execute_recycle_steps (marker_recycle/types/ContractionViscoelastic.jl:
+ * 60-111): InitializeMarkerRecycling (outside markers in marker order, sticky by material),
+ * ContractionRecycleLocations (sticky positions from stream 0, subsurface from stream 1),
+ * Coordinates.reset_recycled_marker_coordinates (k-th marker of a group takes the k-th
+ * position), get_subsurface_reset_properties_viscoelastic_contraction (material of the new
+ * position, pressure PressureReset 3300 * 9.81 * y, temperature 0) and
+ * ResetMarkers.reset_recycled_marker_properties!.
+ * ids[]: sticky_air, sticky_water, layers[7], strong[3]; d[]: xsize, ysize,
+ * full_velocity_contraction, timestep, sticky_thickness_left, sticky_thickness_right,
+ * temperature_top, thick[6], x_left_strong, x_right_strong, delta_fric_coef.
+ * newx/newy: scratch of M doubles each (positions of the sticky group, then the subsurface). */
+int64_t o_recycle_contraction(int64_t M, const int8_t* inside, int16_t* matid, double** f, float* pfailure,
+                              const int16_t* ids, const double* d, int64_t asym, int64_t nmat,
+                              const double* mat_plastic, int64_t iuse_random_fric, uint64_t seed, int64_t step,
+                              int64_t* list, int8_t* flags, double* newx, double* newy, int64_t* n_air) {
+  const int16_t air = ids[0], water = ids[1];
+  const double xsize = d[0], ysize = d[1];
+  /* get_displacement_velocity: abs(v) * timestep * 0.5, or abs(v) * timestep */
+  const double disp = asym ? fabs(d[2]) * d[3] : fabs(d[2]) * d[3] * 0.5;
+  int64_t nout = 0, nair = 0, nsub = 0;
+  for (int64_t m = 0; m < M; ++m)
+    if (inside[m] != 1) {
+      list[nout++] = m;
+      if (matid[m] == air || matid[m] == water) ++nair; else ++nsub;
+    }
+  double *ax = newx, *ay = newy, *sx = newx + nair, *sy = newy + nair;
+  contraction_positions(nair, asym, 1, xsize, ysize, disp, d[4], d[5], seed, step, 0u, ax, ay);
+  contraction_positions(nsub, asym, 0, xsize, ysize, disp, d[4], d[5], seed, step, 1u, sx, sy);
+  int64_t ia = 0, is = 0;
+  for (int64_t k = 0; k < nout; ++k) {
+    const int64_t m = list[k];
+    const int sticky = (matid[m] == air || matid[m] == water) && nair > 0;
+    if (sticky) { f[R_X][m] = ax[ia]; f[R_Y][m] = ay[ia]; ++ia; }
+    else { f[R_X][m] = sx[is]; f[R_Y][m] = sy[is]; ++is; }
+    flags[k] = (int8_t)(sticky ? 0 : 1);
+    int16_t id;
+    if (sticky) {
+      id = air;
+      f[R_TK][m] = d[6];
+      f[R_PR][m] = 0.0;
+      f[R_SXX][m] = f[R_SXY][m] = 0.0;
+      f[R_EXX][m] = f[R_EXY][m] = 0.0;
+      f[R_ETA][m] = 0.0;
+    } else {
+      id = contraction_define_material(f[R_X][m], f[R_Y][m], d + 7, d[13], d[14], ids + 2, ids + 9);
+      f[R_TK][m] = 0.0;
+      f[R_PR][m] = 3300.0 * 9.81 * f[R_Y][m];
+      f[R_SXX][m] = f[R_SXY][m] = 1.96e6;
+      f[R_EXX][m] = f[R_EXY][m] = 1e-14;
+      f[R_ETA][m] = 1e20;
+    }
+    matid[m] = id;
+    f[R_SR_RATIO][m] = 0.0;
+    f[R_GII][m] = f[R_SP][m] = f[R_SRP][m] = 0.0;
+    f[R_MELT][m] = 0.0;
+    pfailure[m] = 0.0f;
+    double fric = mat_plastic[2 * nmat + (id - 1)];
+    if (!sticky && iuse_random_fric == 1) {
+      double r, unused;
+      o_recycle_uniforms(seed, step, 2u, m, &r, &unused);
+      if (r <= 0.5) fric = fric - d[15];
+    }
+    f[R_FRIC_INI][m] = fric;
+    f[R_FRIC][m] = fric;
+    list[k] = m + 1;
+  }
+  *n_air = nair;
+  return nout;
 }

@@ -237,3 +237,122 @@ def test_recycle_channel_oracle(B):
     assert np.array_equal(idx, np.nonzero(moved)[0] + 1)
     assert np.array_equal(y2[moved], y[moved] - 160e3) and np.array_equal(y2[~moved], y[~moved])
     assert np.array_equal(tk2[moved], tk[moved] + 273.0 - 1603.0) and np.array_equal(tk2[~moved], tk[~moved])
+
+
+def reference_contraction(mk, air, water, layers, strong, xsize, ysize, vfull, dt, h_left, h_right, ttop, thick,
+                          x_left, x_right, mat_plastic, rf, dfric, U, asym):
+    """ContractionViscoelastic.execute_recycle_steps written out in Python: outside markers in
+    order (InitializeMarkerRecycling.jl:26-108), side positions (ContractionRecycleLocations.jl:
+    9-140 with CountRecycle.jl:19-29; the y loop and the x loop of Coordinates.jl:223-293 take
+    rand() from U(stream, j)[1] and U(stream, j)[0]), the seven-layer and strong-zone material
+    of the new position (SevenLayerEarthModel2D.jl:20-62, StrongRegions.jl:24-80) and the
+    resets of ResetMarkers.jl:24-268."""
+    out = {k: np.array(v, copy=True) for k, v in mk.items()}
+    outside = [i for i in range(len(mk["x"])) if mk["inside"][i] != 1]
+    nair = sum(1 for i in outside if mk["matid"][i] in (air, water))
+    nsub = len(outside) - nair
+    disp = abs(vfull) * dt if asym else abs(vfull) * dt * 0.5
+
+    def positions(n, stream, is_air):
+        nleft = 0 if asym else n // 2
+        newx, newy = [0.0] * n, [0.0] * n
+        for start, cnt, h, x0, dx in ((0, nleft, h_left, 0.0, disp), (nleft, n - nleft, h_right, xsize, -disp)):
+            y0, yh = (0.0, h) if is_air else (h, ysize - h)
+            for j in range(cnt):
+                mm = j + start
+                newy[mm] = y0 + U(stream, mm)[1] * yh
+                newx[mm] = x0 + U(stream, mm)[0] * dx
+        return newx, newy
+
+    ax, ay = positions(nair, 0, True)
+    sx, sy = positions(nsub, 1, False)
+    d = [thick[0]]  # Layers.calc_depths_for_layers: running sums
+    for t in thick[1:]:
+        d.append(d[-1] + t)
+
+    def material(x, y):
+        mid = layers[6]
+        if y <= d[0]:
+            mid = layers[0]
+        else:
+            for k in range(1, 6):
+                if d[k - 1] < y <= d[k]:
+                    mid = layers[k]
+                    break
+        out_strong = x < x_left or x > x_right
+        for k, sid in ((1, strong[0]), (2, strong[1]), (3, strong[2]), (4, strong[2]), (5, strong[2])):
+            if d[k - 1] < y <= d[k]:
+                if out_strong:
+                    mid = sid
+                break
+        return mid
+
+    ia = isub = 0
+    idx, flags = [], []
+    for i in outside:
+        if mk["matid"][i] in (air, water) and nair > 0:
+            out["x"][i], out["y"][i] = ax[ia], ay[ia]
+            ia += 1
+            flag = 0
+        else:
+            out["x"][i], out["y"][i] = sx[isub], sy[isub]
+            isub += 1
+            flag = 1
+        idx.append(i + 1)
+        flags.append(flag)
+    for i, flag in zip(idx, flags):
+        i -= 1
+        if flag == 0:
+            mid, T, P, S, E, V = air, ttop, 0.0, 0.0, 0.0, 0.0
+        else:
+            mid = material(out["x"][i], out["y"][i])
+            T, P, S, E, V = 0.0, 3300.0 * 9.81 * out["y"][i], 1.96e6, 1e-14, 1e20
+        out["matid"][i] = mid
+        out["tk"][i], out["pr"][i] = T, P
+        out["sxx"][i] = out["sxy"][i] = S
+        out["exx"][i] = out["exy"][i] = E
+        out["sr_ratio"][i] = 0.0
+        out["gii"][i] = out["strain_plastic"][i] = out["strain_rate_plastic"][i] = 0.0
+        out["meltfrac"][i] = 0.0
+        out["eta"][i] = V
+        out["pfailure"][i] = np.float32(0.0)
+        f = mat_plastic[mid - 1, 2]
+        if flag == 1 and rf == 1 and U(2, i)[0] <= 0.5:
+            f = f - dfric
+        out["fric_ini"][i] = out["fric"][i] = f
+    return out, np.array(idx, np.int64), np.array(flags, np.int8), nair
+
+
+CONTRACTION = dict(layers=(1, 5, 6, 7, 8, 9, 10), strong=(11, 12, 4), thick=(10e3, 15e3, 10e3, 30e3, 20e3, 25e3))
+
+
+@pytest.mark.parametrize("asym,rf", [(0, 0), (1, 1), (0, 1)])
+def test_recycle_contraction_oracle_matches_reference_loops(eb, B, asym, rf):
+    rng = np.random.default_rng(31 + asym + 2 * rf)
+    M = 3000
+    mk = {k: rng.uniform(-1.0, 1.0, M) for k in B.RECYCLE_FIELDS}
+    mk["matid"] = rng.integers(1, 13, M).astype(np.int16)
+    mk["pfailure"] = rng.uniform(0, 1, M).astype(np.float32)
+    mk["inside"] = np.where(rng.random(M) < 0.7, 1, rng.choice([0, -1], M)).astype(np.int8)
+    mp = np.asfortranarray(rng.uniform(0, 1, (12, 6)))
+    c = CONTRACTION
+    xsize, ysize, vfull, dt, hl, hr, ttop = 500e3, 160e3, 3e-9, 3.15e13, 10e3, 12e3, 273.0
+    seed, step = 4242, 6
+    got, idx, fl, nair = B.recycle_contraction(mk, 1, 2, c["layers"], c["strong"], xsize, ysize, vfull, dt, hl, hr,
+                                               ttop, c["thick"], -1.0, 250e3, mp, rf, 0.07, seed, step, asym)
+    want, widx, wfl, wnair = reference_contraction(mk, 1, 2, c["layers"], c["strong"], xsize, ysize, vfull, dt, hl,
+                                                   hr, ttop, c["thick"], -1.0, 250e3, mp, rf, 0.07,
+                                                   lambda st, j: B.recycle_uniforms(seed, step, st, j), asym)
+    assert nair == wnair and np.array_equal(idx, widx) and np.array_equal(fl, wfl)
+    for k in (*B.RECYCLE_FIELDS, "matid", "pfailure"):
+        assert np.array_equal(got[k], want[k]), k
+    # positions: side bands of width |v| dt (/2); the left side (inside the strong-zone limits
+    # [-1, 250 km]) takes the seven-layer materials, the right side the strong-zone ones
+    x, sub = got["x"][idx - 1], fl == 1
+    band = abs(vfull) * dt * (1.0 if asym else 0.5)
+    assert np.all((x <= band) | (x >= xsize - band))
+    if asym:
+        assert np.all(x >= xsize - band)
+    ids = set(got["matid"][idx - 1][sub].tolist())
+    assert {10, 11, 12, 4}.issubset(ids)
+    assert {5, 6, 7, 8, 9}.issubset(ids) == (not asym)

@@ -162,3 +162,62 @@ def test_recycle_no_bottom_inflow_and_channel_match_oracle(eb):
     assert np.array_equal(idx, widx)
     assert np.array_equal(mic.download_marker("y"), wy) and np.array_equal(mic.download_marker("tk"), wtk)
     mic.close()
+
+
+@pytest.mark.parametrize("asym,random_fric", [(0, 1), (1, 0)])
+def test_recycle_contraction_matches_oracle(eb, asym, random_fric):
+    """Recycling type 4 (ContractionViscoelastic): markers pushed out through all four sides
+    re-enter at the two sides bit-identically to the oracle, subsurface ones as the seven-layer
+    or strong-zone material of their new position (12 materials, friction per material)."""
+    import dataclasses
+    from oracle import boundary as B
+    model = eb.synthetic.config("rift_small")
+    g = model.grid
+    p = model.params
+    rng = np.random.default_rng(41 + asym)
+    m0 = model.mats
+    rows = np.arange(12) % len(m0.mat_mu)
+    mp = np.asfortranarray(np.asarray(m0.mat_plastic)[rows].copy())
+    mp[:, 2] = rng.uniform(0.1, 0.6, 12)
+    mats = dataclasses.replace(m0, mat_mu=np.asarray(m0.mat_mu)[rows], mat_hr=np.asarray(m0.mat_hr)[rows],
+                               mat_flow_type=np.asarray(m0.mat_flow_type)[rows],
+                               mat_flow=np.asfortranarray(np.asarray(m0.mat_flow)[rows]), mat_plastic=mp,
+                               mat_rho=np.asarray(m0.mat_rho)[rows])
+    mic = eb.MarkerInCell(0)
+    mic.load_model(model)
+    mic.set_materials(mats)
+    M = model.marknum
+    x, y = mic.download_marker("x"), mic.download_marker("y")
+    out = rng.random(M) < 0.05
+    side = rng.integers(0, 4, M)
+    x = np.where(out & (side == 0), g.xmin - rng.uniform(1.0, 5e3, M), x)
+    x = np.where(out & (side == 1), g.xmax + rng.uniform(1.0, 5e3, M), x)
+    y = np.where(out & (side == 2), g.ymin - rng.uniform(1.0, 5e3, M), y)
+    y = np.where(out & (side == 3), g.ymax + rng.uniform(1.0, 5e3, M), y)
+    mic.upload_marker("x", x)
+    mic.upload_marker("y", y)
+    for k in B.RECYCLE_FIELDS[2:]:
+        mic.upload_marker(k, rng.uniform(0.5, 2.0, M))
+    mic.upload_marker("pfailure", rng.uniform(0, 1, M).astype(np.float32))
+    mic.get_marker_inside_flags()
+    mk = {k: mic.download_marker(k) for k in (*B.RECYCLE_FIELDS, "matid", "pfailure", "inside")}
+    layers, strong = (1, 5, 6, 7, 8, 9, 10), (11, 12, 4)
+    thick = (0.05 * g.ymax, 0.1 * g.ymax, 0.08 * g.ymax, 0.15 * g.ymax, 0.1 * g.ymax, 0.12 * g.ymax)
+    hl, hr, vfull, xl, xr, seed, step = 0.05 * g.ymax, 0.06 * g.ymax, 2e-9, -1.0, 0.5 * g.xmax, 515, 12
+    want, widx, wfl, wnair = B.recycle_contraction(mk, 1, 2, layers, strong, g.xmax, g.ymax, vfull, p["timestep"], hl,
+                                                   hr, p["temperature_top"], thick, xl, xr, mp, random_fric, 0.05,
+                                                   seed, step, asym)
+    con = dict(asymmetric=asym, full_velocity_contraction=vfull, sticky_thickness_left=hl, sticky_thickness_right=hr,
+               layer_thickness=thick, x_left_strong=xl, x_right_strong=xr, matid_layers=layers, matid_strong=strong)
+    nair, nsub = mic.recycle_markers(1, 2, 4, g.xmax, g.ymax, 0.0, 0.0, 1603.0, seed, step,
+                                     iuse_random_fric=random_fric, delta_fric_coef=0.05, recycle_type=4,
+                                     contraction=con)
+    assert (nair, nsub) == (wnair, len(widx) - wnair) and nair > 10 and nsub > 10
+    idx, fl = mic.recycled_markers()
+    assert np.array_equal(idx, widx) and np.array_equal(fl, wfl)
+    for k in (*B.RECYCLE_FIELDS, "matid", "pfailure"):
+        assert np.array_equal(mic.download_marker(k), want[k]), k
+    assert len(set(want["matid"][widx - 1][wfl == 1].tolist())) >= (4 if asym else 8)
+    mic.get_marker_inside_flags()
+    assert np.all(mic.download_marker("inside") == 1)
+    mic.close()
