@@ -543,13 +543,16 @@ class MarkerInCell:
     def recycle_markers(self, matid_sticky_air: int, matid_sticky_water: int, matid_asthenosphere: int,
                         xsize: float, ysize: float, velocity_y_upper: float, velocity_y_lower: float,
                         temperature_bottom: float, seed: int, counter: int, iuse_random_fric: int = 0,
-                        delta_fric_coef: float = 0.0, recycle_type: int = 1, contraction: dict | None = None) -> tuple:
+                        delta_fric_coef: float = 0.0, recycle_type: int = 1, contraction: dict | None = None,
+                        side_inflow: dict | None = None) -> tuple:
         """MarkerRecycle.recycle_markers!: recycle_type 1 extension models (types/Extension.jl:14-129),
         2 extension without bottom inflow (types/ExtensionNoBottomInflow.jl), 3 channel
         (types/Channel.jl), 4 contraction (types/ContractionViscoelastic.jl; `contraction` holds
         asymmetric, full_velocity_contraction, sticky_thickness_left/right, layer_thickness (6),
-        x_left_strong, x_right_strong, matid_layers (7), matid_strong (3));
-        returns (nrecycle_air, nrecycle_subsurface)."""
+        x_left_strong, x_right_strong, matid_layers (7), matid_strong (3)), 5 extension with side
+        inflow and outflow (types/ExtensionInflowAndOutflowAlongSides.jl; `side_inflow` holds
+        sticky_thickness_left/right, plate_thickness, smoothing_thickness, velocity_inflow_left/right,
+        adiabatic_gradient); returns (nrecycle_air, nrecycle_subsurface)."""
         p = _abi.RecycleParams(recycle_type, matid_sticky_air, matid_sticky_water, matid_asthenosphere, xsize, ysize,
                                velocity_y_upper, velocity_y_lower, temperature_bottom, iuse_random_fric,
                                delta_fric_coef, seed, counter)
@@ -562,6 +565,9 @@ class MarkerInCell:
             p.x_left_strong, p.x_right_strong = k["x_left_strong"], k["x_right_strong"]
             p.matid_layers[:] = list(k["matid_layers"])
             p.matid_strong[:] = list(k["matid_strong"])
+        if side_inflow:
+            for name, v in side_inflow.items():
+                setattr(p, name, v)
         na, ns = C.c_int64(), C.c_int64()
         self._check(self._lib.eb_recycle_markers(self._ctx, C.byref(p), C.byref(na), C.byref(ns)))
         return na.value, ns.value

@@ -190,7 +190,9 @@ class RecycleParams(C.Structure):
                 ("full_velocity_contraction", C.c_double), ("sticky_thickness_left", C.c_double),
                 ("sticky_thickness_right", C.c_double), ("layer_thickness", C.c_double * 6),
                 ("x_left_strong", C.c_double), ("x_right_strong", C.c_double), ("matid_layers", C.c_int32 * 7),
-                ("matid_strong", C.c_int32 * 3)]
+                ("matid_strong", C.c_int32 * 3), ("plate_thickness", C.c_double), ("smoothing_thickness", C.c_double),
+                ("velocity_inflow_left", C.c_double), ("velocity_inflow_right", C.c_double),
+                ("adiabatic_gradient", C.c_double)]
 
 
 class HeatParams(C.Structure):

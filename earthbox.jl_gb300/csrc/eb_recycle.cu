@@ -73,6 +73,9 @@ struct RecycleK {
   double depth[6];
   double x_left_strong, x_right_strong;
   int16_t layer_id[7], strong_id[3];
+  // side inflow: top of the inflow zone (= top of the ramp) and base of the ramp per side,
+  // inflow bands |v_left| dt and -|v_right| dt, adiabatic gradient (K/km)
+  double in_top_l, in_top_r, ramp_bot_l, ramp_bot_r, disp_in_l, disp_in_r, adiabatic;
 };
 
 // SevenLayerEarthModel2D.define_material (marker_materials/init_manager/utils/
@@ -112,7 +115,7 @@ __device__ __forceinline__ bool selected(const DevMarkers& mk, int64_t m, const 
 // sticky rank (air/water positions): extension and contraction; the other types treat every
 // marker alike
 __device__ __forceinline__ bool sticky_sel(const DevMarkers& mk, int64_t m, const RecycleK& p) {
-  return (p.type == 1 || p.type == 4) && sticky(mk.matid[m], p);
+  return (p.type == 1 || p.type == 4 || p.type == 5) && sticky(mk.matid[m], p);
 }
 
 // per block: number of outside markers and of outside sticky markers
@@ -230,6 +233,43 @@ __global__ void k_recycle_apply(DevMarkers mk, DevMats mt, RecycleK p, const int
     mk.fric[m] = fric;
     return;
   }
+  if (p.type == 5 && !st) {
+    // ExtensionInflowAndOutflowAlongSides (types/ExtensionInflowAndOutflowAlongSides.jl:
+    // 20-237): the first floor(n/2) subsurface markers enter at the left side, the others at
+    // the right, y = y0 + u (ysize - y0) below the plate and smoothing layer
+    // (InflowGeometry.jl), x = x0 + u d f with the ramp factor f of the new depth
+    // (InflowRamp.calculate_ramp_factor; Coordinates.jl:155-200); asthenosphere at pressure
+    // 3300 * 9.81 * y and T_bottom - gradient (ysize - y) / 1000.
+    const int64_t r = (int64_t)r_out - r_st, nleft = (n_out - n_air) / 2;
+    uniforms(p.seed, p.step, 1u, r, ux, uy);
+    const bool left = r < nleft;
+    const double y0 = left ? p.in_top_l : p.in_top_r, yb = left ? p.ramp_bot_l : p.ramp_bot_r;
+    const double y = y0 + uy * (p.ysize - y0);
+    const double f = (y0 <= y && y < yb) ? (y - y0) / (yb - y0) : 1.0;
+    mk.x[m] = (left ? 0.0 : p.xsize) + ux * (left ? p.disp_in_l : p.disp_in_r) * f;
+    mk.y[m] = y;
+    list[r_out] = m + 1;
+    flags[r_out] = 1;
+    mk.matid[m] = p.asth;
+    mk.tk[m] = p.t_bottom - p.adiabatic * ((p.ysize - y) / 1000.0);
+    mk.pr[m] = 3300.0 * 9.81 * y;
+    mk.sxx[m] = 1.96e6; mk.sxy[m] = 1.96e6;
+    mk.exx[m] = 1e-14; mk.exy[m] = 1e-14;
+    mk.eta[m] = 1e20;
+    double fric = p.fric_asth;
+    if (p.random_fric == 1) {
+      double r0, r1;
+      uniforms(p.seed, p.step, 2u, m, r0, r1);
+      if (r0 <= 0.5) fric = fric - p.delta_fric;
+    }
+    mk.sr_ratio[m] = 0.0;
+    mk.gii[m] = 0.0; mk.sp[m] = 0.0; mk.srp[m] = 0.0;
+    mk.melt[m] = 0.0;
+    mk.pfailure[m] = 0.0f;
+    mk.fric_ini[m] = fric;
+    mk.fric[m] = fric;
+    return;
+  }
   if (st && n_air > 0) {
     uniforms(p.seed, p.step, 0u, r_st, ux, uy);
     mk.x[m] = 0.0 + ux * p.xsize;
@@ -284,9 +324,9 @@ extern "C" int eb_recycle_markers(eb_ctx* c, const eb_recycle_params* rp, int64_
                                   int64_t* nrecycle_subsurface) {
   if (!c || !rp) return EB_BAD_INPUT;
   if (!c->have_grid || !c->have_params || !c->have_mats) return eb_fail(c, EB_NOT_READY, "grid, parameters and materials must be set");
-  if (rp->recycle_type < 1 || rp->recycle_type > 4)
+  if (rp->recycle_type < 1 || rp->recycle_type > 5)
     return eb_fail(c, EB_BAD_INPUT, "recycle_type must be 1 (extension), 2 (extension without bottom inflow), "
-                                    "3 (channel) or 4 (contraction)");
+                                    "3 (channel), 4 (contraction) or 5 (extension with side inflow and outflow)");
   const int64_t nmat = c->mats.nmat;
   std::vector<int64_t> ids = {rp->matid_sticky_air, rp->matid_sticky_water, rp->matid_asthenosphere};
   if (rp->recycle_type == 4) {
@@ -336,6 +376,17 @@ extern "C" int eb_recycle_markers(eb_ctx* c, const eb_recycle_params* rp, int64_
     p.x_right_strong = rp->x_right_strong;
     for (int k = 0; k < 7; ++k) p.layer_id[k] = (int16_t)rp->matid_layers[k];
     for (int k = 0; k < 3; ++k) p.strong_id[k] = (int16_t)rp->matid_strong[k];
+  }
+  if (rp->recycle_type == 5) {
+    // InflowGeometry.calculate_top_of_side_inflow / InflowRamp.get_top_and_bottom_of_inflow_ramp:
+    // (sticky + plate) + smoothing, and that + smoothing
+    p.in_top_l = rp->sticky_thickness_left + rp->plate_thickness + rp->smoothing_thickness;
+    p.in_top_r = rp->sticky_thickness_right + rp->plate_thickness + rp->smoothing_thickness;
+    p.ramp_bot_l = p.in_top_l + rp->smoothing_thickness;
+    p.ramp_bot_r = p.in_top_r + rp->smoothing_thickness;
+    p.disp_in_l = std::fabs(rp->velocity_inflow_left) * c->P.timestep;
+    p.disp_in_r = -std::fabs(rp->velocity_inflow_right) * c->P.timestep;
+    p.adiabatic = rp->adiabatic_gradient;
   }
   k_recycle_count<<<nblocks, kB, 0, c->stream>>>(dev_markers(c), p, d_counts, nblocks);
   c->launches++;

@@ -569,7 +569,8 @@ typedef struct eb_recycle_params {
                                       band vyu dt with its sign); 3: channel (types/Channel.jl:20-54:
                                       markers below gridy_b[ynum] move up by the grid height and
                                       their temperature by temperature_top - temperature_bottom; the
-                                      inside flags are not used); 4: contraction (fields below)      */
+                                      inside flags are not used); 4: contraction, 5: extension with
+                                      side inflow and outflow (fields below)                         */
   int32_t matid_sticky_air, matid_sticky_water, matid_asthenosphere;  /* material ids                 */
   double  xsize, ysize;            /* model size (m); the domain starts at x = y = 0                    */
   double  velocity_y_upper, velocity_y_lower;  /* vyu, vyl (m/s): band widths |v dt|                   */
@@ -592,6 +593,13 @@ typedef struct eb_recycle_params {
   int32_t matid_layers[7];         /* Atmosphere, UpperContinentalCrust, LowerContinentalCrust,
                                       Upper-, Middle-, LowerMantleLithosphere, Asthenosphere        */
   int32_t matid_strong[3];         /* Upper-, LowerContinentalCrustStrongZone, LithosphericMantleStrongZone */
+  /* recycle_type 5: extension with side inflow and outflow
+     (LithosphericExtensionInflowAndOutflowAlongSides -> types/ExtensionInflowAndOutflowAlongSides.jl):
+     sticky markers as type 1, subsurface ones at the two sides below sticky + plate + smoothing
+     (sticky_thickness_left/right above), as asthenosphere                                          */
+  double  plate_thickness, smoothing_thickness;          /* OutflowGeometry.get_outflow_geometry (m) */
+  double  velocity_inflow_left, velocity_inflow_right;   /* m/s                                      */
+  double  adiabatic_gradient;      /* K/km: T = temperature_bottom - gradient (ysize - y) / 1000     */
 } eb_recycle_params;
 int eb_recycle_markers(eb_ctx* ctx, const eb_recycle_params* p, int64_t* nrecycle_air, int64_t* nrecycle_subsurface);
 /* The markers of the last eb_recycle_markers: 1-based indices and flags (0 sticky, 1 subsurface),

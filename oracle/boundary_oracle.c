@@ -21,6 +21,8 @@
  *       utils/ContractionRecycleLocations.jl:9-140, CountRecycle.jl:19-29, Coordinates.jl:223-293,
  *       marker_materials/init_manager/utils/{SevenLayerEarthModel2D.jl:20-62,StrongRegions.jl:24-80},
  *       markers/utils/Layers.jl:31-54
+ *   o_recycle_side_inflow           marker_recycle/types/ExtensionInflowAndOutflowAlongSides.jl:20-237
+ *       with boundary_velocity/utils/{InflowGeometry.jl,InflowRamp.jl}, Coordinates.jl:155-200
  *
  * Grids are column-major (rows, cols).  Julia's x^2 and x^3 of a Float64 literal power
  * are x*x and x*x*x.
@@ -395,6 +397,104 @@ int64_t o_recycle_contraction(int64_t M, const int8_t* inside, int16_t* matid, d
       double r, unused;
       o_recycle_uniforms(seed, step, 2u, m, &r, &unused);
       if (r <= 0.5) fric = fric - d[15];
+    }
+    f[R_FRIC_INI][m] = fric;
+    f[R_FRIC][m] = fric;
+    list[k] = m + 1;
+  }
+  *n_air = nair;
+  return nout;
+}
+
+/* InflowRamp.calculate_ramp_factor: (y - top) / (bottom - top) inside [top, bottom), else 1 */
+static double ramp_factor(double y, double top, double bottom) {
+  return (top <= y && y < bottom) ? (y - top) / (bottom - top) : 1.0;
+}
+
+/* ExtensionInflowAndOutflowAlongSides.execute_recycling_steps (marker_recycle/types/
+ * ExtensionInflowAndOutflowAlongSides.jl:20-237): sticky markers at the Extension top-band
+ * positions (Extension.jl:58-73, stream 0), subsurface ones at the two sides (stream 1):
+ * the first floor(n/2) at x0 = 0 with band |v_left| dt, the rest at x0 = xsize with band
+ * -|v_right| dt; y0 = (sticky + plate) + smoothing of that side (InflowGeometry.jl), y = y0 +
+ * u_y (ysize - y0) and x = x0 + u_x band f(y), f the ramp factor over [y0, y0 + smoothing)
+ * (Coordinates.update_recycled_coordinates_vertical_inflow_outflow_boundary!).  Subsurface
+ * properties: asthenosphere, 3300 * 9.81 * y, T_bottom - gradient ((ysize - y) / 1000).
+ * d[]: xsize, ysize, vyu, timestep, temperature_top, temperature_bottom, sticky_left,
+ * sticky_right, plate, smoothing, v_inflow_left, v_inflow_right, adiabatic_gradient,
+ * delta_fric_coef; ids[]: sticky_air, sticky_water, asthenosphere. */
+int64_t o_recycle_side_inflow(int64_t M, const int8_t* inside, int16_t* matid, double** f, float* pfailure,
+                              const int16_t* ids, const double* d, int64_t nmat, const double* mat_plastic,
+                              int64_t iuse_random_fric, uint64_t seed, int64_t step, int64_t* list, int8_t* flags,
+                              double* newx, double* newy, int64_t* n_air) {
+  const int16_t air = ids[0], water = ids[1], asth = ids[2];
+  const double xsize = d[0], ysize = d[1], dt = d[3];
+  int64_t nout = 0, nair = 0, nsub = 0;
+  for (int64_t m = 0; m < M; ++m)
+    if (inside[m] != 1) {
+      list[nout++] = m;
+      if (matid[m] == air || matid[m] == water) ++nair; else ++nsub;
+    }
+  double *ax = newx, *ay = newy, *sx = newx + nair, *sy = newy + nair;
+  const double disp_upper = fabs(d[2] * dt);
+  for (int64_t j = 0; j < nair; ++j) {
+    double u0, u1;
+    o_recycle_uniforms(seed, step, 0u, j, &u0, &u1);
+    ay[j] = 0.0 + u1 * disp_upper;
+    ax[j] = 0.0 + u0 * xsize;
+  }
+  const int64_t nleft = nsub / 2;
+  for (int side = 0; side < 2; ++side) {
+    const double sticky = side == 0 ? d[6] : d[7];
+    const double y_initial = sticky + d[8] + d[9];           /* calculate_top_of_side_inflow */
+    const double y_smooth_top = sticky + d[8] + d[9], y_smooth_bottom = y_smooth_top + d[9];
+    const double y_height = ysize - y_initial;                /* get_y_height_of_inflow */
+    const double x_initial = side == 0 ? 0.0 : xsize;
+    const double displacement_x = side == 0 ? fabs(d[10]) * dt : -fabs(d[11]) * dt;
+    const int64_t start = side == 0 ? 0 : nleft, count = side == 0 ? nleft : nsub - nleft;
+    for (int64_t j = 0; j < count; ++j) {
+      double ux, uy;
+      o_recycle_uniforms(seed, step, 1u, start + j, &ux, &uy);
+      sy[start + j] = y_initial + uy * y_height;
+    }
+    for (int64_t j = 0; j < count; ++j) {
+      double ux, uy;
+      o_recycle_uniforms(seed, step, 1u, start + j, &ux, &uy);
+      const double rf = ramp_factor(sy[start + j], y_smooth_top, y_smooth_bottom);
+      sx[start + j] = x_initial + ux * displacement_x * rf;
+    }
+  }
+  int64_t ia = 0, is = 0;
+  for (int64_t k = 0; k < nout; ++k) {
+    const int64_t m = list[k];
+    const int sticky = (matid[m] == air || matid[m] == water) && nair > 0;
+    if (sticky) { f[R_X][m] = ax[ia]; f[R_Y][m] = ay[ia]; ++ia; }
+    else { f[R_X][m] = sx[is]; f[R_Y][m] = sy[is]; ++is; }
+    flags[k] = (int8_t)(sticky ? 0 : 1);
+    const int16_t id = sticky ? air : asth;
+    matid[m] = id;
+    if (sticky) {
+      f[R_TK][m] = d[4];
+      f[R_PR][m] = 0.0;
+      f[R_SXX][m] = f[R_SXY][m] = 0.0;
+      f[R_EXX][m] = f[R_EXY][m] = 0.0;
+      f[R_ETA][m] = 0.0;
+    } else {
+      const double dy_km = (ysize - f[R_Y][m]) / 1000.0;
+      f[R_TK][m] = d[5] - d[12] * dy_km;
+      f[R_PR][m] = 3300.0 * 9.81 * f[R_Y][m];
+      f[R_SXX][m] = f[R_SXY][m] = 1.96e6;
+      f[R_EXX][m] = f[R_EXY][m] = 1e-14;
+      f[R_ETA][m] = 1e20;
+    }
+    f[R_SR_RATIO][m] = 0.0;
+    f[R_GII][m] = f[R_SP][m] = f[R_SRP][m] = 0.0;
+    f[R_MELT][m] = 0.0;
+    pfailure[m] = 0.0f;
+    double fric = mat_plastic[2 * nmat + (id - 1)];
+    if (!sticky && iuse_random_fric == 1) {
+      double r, unused;
+      o_recycle_uniforms(seed, step, 2u, m, &r, &unused);
+      if (r <= 0.5) fric = fric - d[13];
     }
     f[R_FRIC_INI][m] = fric;
     f[R_FRIC][m] = fric;

@@ -356,3 +356,88 @@ def test_recycle_contraction_oracle_matches_reference_loops(eb, B, asym, rf):
     ids = set(got["matid"][idx - 1][sub].tolist())
     assert {10, 11, 12, 4}.issubset(ids)
     assert {5, 6, 7, 8, 9}.issubset(ids) == (not asym)
+
+
+def reference_side_inflow(mk, air, water, asth, xsize, ysize, vyu, dt, ttop, tbot, hl, hr, plate, smooth, vin_l,
+                          vin_r, grad, mat_plastic, rf, dfric, U):
+    """ExtensionInflowAndOutflowAlongSides.execute_recycling_steps written out in Python
+    (ExtensionInflowAndOutflowAlongSides.jl:20-237, Extension.jl:58-73, InflowGeometry.jl,
+    InflowRamp.jl, Coordinates.jl:155-200, ResetMarkers.jl:24-268), rand() from U(stream, j)."""
+    out = {k: np.array(v, copy=True) for k, v in mk.items()}
+    outside = [i for i in range(len(mk["x"])) if mk["inside"][i] != 1]
+    nair = sum(1 for i in outside if mk["matid"][i] in (air, water))
+    nsub = len(outside) - nair
+    newy_air = [0.0 + U(0, j)[1] * abs(vyu * dt) for j in range(nair)]
+    newx_air = [0.0 + U(0, j)[0] * xsize for j in range(nair)]
+    newx, newy = [0.0] * nsub, [0.0] * nsub
+    nleft = nsub // 2
+    for start, cnt, h, x0, disp in ((0, nleft, hl, 0.0, abs(vin_l) * dt), (nleft, nsub - nleft, hr, xsize,
+                                                                            -abs(vin_r) * dt)):
+        y0 = h + plate + smooth
+        top, bot = h + plate + smooth, h + plate + smooth + smooth
+        for j in range(cnt):
+            newy[start + j] = y0 + U(1, start + j)[1] * (ysize - y0)
+        for j in range(cnt):
+            y = newy[start + j]
+            ramp = (y - top) / (bot - top) if top <= y < bot else 1.0
+            newx[start + j] = x0 + U(1, start + j)[0] * disp * ramp
+    ia = isub = 0
+    idx, flags = [], []
+    for i in outside:
+        if mk["matid"][i] in (air, water) and nair > 0:
+            out["x"][i], out["y"][i] = newx_air[ia], newy_air[ia]
+            ia += 1
+            flag = 0
+        else:
+            out["x"][i], out["y"][i] = newx[isub], newy[isub]
+            isub += 1
+            flag = 1
+        idx.append(i + 1)
+        flags.append(flag)
+    for i, flag in zip(idx, flags):
+        i -= 1
+        if flag == 0:
+            mid, T, P, S, E, V = air, ttop, 0.0, 0.0, 0.0, 0.0
+        else:
+            y = out["y"][i]
+            mid, T, P, S, E, V = asth, tbot - grad * ((ysize - y) / 1000.0), 3300.0 * 9.81 * y, 1.96e6, 1e-14, 1e20
+        out["matid"][i] = mid
+        out["tk"][i], out["pr"][i] = T, P
+        out["sxx"][i] = out["sxy"][i] = S
+        out["exx"][i] = out["exy"][i] = E
+        out["sr_ratio"][i] = 0.0
+        out["gii"][i] = out["strain_plastic"][i] = out["strain_rate_plastic"][i] = 0.0
+        out["meltfrac"][i] = 0.0
+        out["eta"][i] = V
+        out["pfailure"][i] = np.float32(0.0)
+        f = mat_plastic[mid - 1, 2]
+        if flag == 1 and rf == 1 and U(2, i)[0] <= 0.5:
+            f = f - dfric
+        out["fric_ini"][i] = out["fric"][i] = f
+    return out, np.array(idx, np.int64), np.array(flags, np.int8), nair
+
+
+SIDE_INFLOW = (500e3, 160e3, -2e-10, 3.15e13, 273.0, 1603.0, 10e3, 12e3, 40e3, 15e3, 1e-9, 2e-9, 0.4)
+
+
+@pytest.mark.parametrize("rf", [0, 1])
+def test_recycle_side_inflow_oracle_matches_reference_loops(eb, B, rf):
+    rng = np.random.default_rng(61 + rf)
+    M = 3000
+    mk = {k: rng.uniform(-1.0, 1.0, M) for k in B.RECYCLE_FIELDS}
+    mk["matid"] = rng.integers(1, 5, M).astype(np.int16)
+    mk["pfailure"] = rng.uniform(0, 1, M).astype(np.float32)
+    mk["inside"] = np.where(rng.random(M) < 0.7, 1, rng.choice([0, -1], M)).astype(np.int8)
+    mp = np.asfortranarray(rng.uniform(0, 1, (4, 6)))
+    seed, step = 1717, 5
+    got, idx, fl, nair = B.recycle_side_inflow(mk, 1, 2, 4, *SIDE_INFLOW, mp, rf, 0.03, seed, step)
+    want, widx, wfl, wnair = reference_side_inflow(mk, 1, 2, 4, *SIDE_INFLOW, mp, rf, 0.03,
+                                                   lambda st, j: B.recycle_uniforms(seed, step, st, j))
+    assert nair == wnair and np.array_equal(idx, widx) and np.array_equal(fl, wfl)
+    for k in (*B.RECYCLE_FIELDS, "matid", "pfailure"):
+        assert np.array_equal(got[k], want[k]), k
+    # subsurface markers sit below the inflow top of their side; some inside the ramp
+    x, y, sub = got["x"][idx - 1], got["y"][idx - 1], fl == 1
+    assert np.all(y[sub] >= 10e3 + 40e3 + 15e3)
+    ramp = sub & (y < 12e3 + 40e3 + 30e3) & (y > 12e3 + 40e3 + 15e3)
+    assert ramp.sum() > 5

@@ -221,3 +221,51 @@ def test_recycle_contraction_matches_oracle(eb, asym, random_fric):
     mic.get_marker_inside_flags()
     assert np.all(mic.download_marker("inside") == 1)
     mic.close()
+
+
+@pytest.mark.parametrize("random_fric", [0, 1])
+def test_recycle_side_inflow_matches_oracle(eb, random_fric):
+    """Recycling type 5 (ExtensionInflowAndOutflowAlongSides): sticky markers in the top band,
+    subsurface ones at the two sides below the plate with the ramp factor, as asthenosphere with
+    the adiabatic temperature; bit-identical to the oracle."""
+    from oracle import boundary as B
+    model = eb.synthetic.config("rift_small")
+    g = model.grid
+    p = model.params
+    rng = np.random.default_rng(71 + random_fric)
+    mic = eb.MarkerInCell(0)
+    mic.load_model(model)
+    M = model.marknum
+    x, y = mic.download_marker("x"), mic.download_marker("y")
+    out = rng.random(M) < 0.05
+    side = rng.integers(0, 4, M)
+    x = np.where(out & (side == 0), g.xmin - rng.uniform(1.0, 5e3, M), x)
+    x = np.where(out & (side == 1), g.xmax + rng.uniform(1.0, 5e3, M), x)
+    y = np.where(out & (side == 2), g.ymin - rng.uniform(1.0, 5e3, M), y)
+    y = np.where(out & (side == 3), g.ymax + rng.uniform(1.0, 5e3, M), y)
+    mic.upload_marker("x", x)
+    mic.upload_marker("y", y)
+    for k in B.RECYCLE_FIELDS[2:]:
+        mic.upload_marker(k, rng.uniform(0.5, 2.0, M))
+    mic.upload_marker("pfailure", rng.uniform(0, 1, M).astype(np.float32))
+    mic.get_marker_inside_flags()
+    mk = {k: mic.download_marker(k) for k in (*B.RECYCLE_FIELDS, "matid", "pfailure", "inside")}
+    hl, hr, plate, smooth = 0.05 * g.ymax, 0.06 * g.ymax, 0.25 * g.ymax, 0.1 * g.ymax
+    vyu, vin_l, vin_r, grad, tbot, seed, step = -1e-10, 1e-9, 2e-9, 0.4, 1603.0, 3131, 2
+    want, widx, wfl, wnair = B.recycle_side_inflow(mk, 1, 2, 4, g.xmax, g.ymax, vyu, p["timestep"],
+                                                   p["temperature_top"], tbot, hl, hr, plate, smooth, vin_l, vin_r,
+                                                   grad, model.mats.mat_plastic, random_fric, 0.05, seed, step)
+    side_in = dict(sticky_thickness_left=hl, sticky_thickness_right=hr, plate_thickness=plate,
+                   smoothing_thickness=smooth, velocity_inflow_left=vin_l, velocity_inflow_right=vin_r,
+                   adiabatic_gradient=grad)
+    nair, nsub = mic.recycle_markers(1, 2, 4, g.xmax, g.ymax, vyu, 0.0, tbot, seed, step,
+                                     iuse_random_fric=random_fric, delta_fric_coef=0.05, recycle_type=5,
+                                     side_inflow=side_in)
+    assert (nair, nsub) == (wnair, len(widx) - wnair) and nair > 10 and nsub > 10
+    idx, fl = mic.recycled_markers()
+    assert np.array_equal(idx, widx) and np.array_equal(fl, wfl)
+    for k in (*B.RECYCLE_FIELDS, "matid", "pfailure"):
+        assert np.array_equal(mic.download_marker(k), want[k]), k
+    mic.get_marker_inside_flags()
+    assert np.all(mic.download_marker("inside") == 1)
+    mic.close()
