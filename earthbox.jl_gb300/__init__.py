@@ -544,7 +544,7 @@ class MarkerInCell:
                         xsize: float, ysize: float, velocity_y_upper: float, velocity_y_lower: float,
                         temperature_bottom: float, seed: int, counter: int, iuse_random_fric: int = 0,
                         delta_fric_coef: float = 0.0, recycle_type: int = 1, contraction: dict | None = None,
-                        side_inflow: dict | None = None) -> tuple:
+                        side_inflow: dict | None = None, fracture_zone: dict | None = None) -> tuple:
         """MarkerRecycle.recycle_markers!: recycle_type 1 extension models (types/Extension.jl:14-129),
         2 extension without bottom inflow (types/ExtensionNoBottomInflow.jl), 3 channel
         (types/Channel.jl), 4 contraction (types/ContractionViscoelastic.jl; `contraction` holds
@@ -552,22 +552,19 @@ class MarkerInCell:
         x_left_strong, x_right_strong, matid_layers (7), matid_strong (3)), 5 extension with side
         inflow and outflow (types/ExtensionInflowAndOutflowAlongSides.jl; `side_inflow` holds
         sticky_thickness_left/right, plate_thickness, smoothing_thickness, velocity_inflow_left/right,
-        adiabatic_gradient); returns (nrecycle_air, nrecycle_subsurface)."""
+        adiabatic_gradient), 6 fracture-zone contraction (types/ContractionFractureZone.jl; the
+        `contraction` position fields plus `fracture_zone`: fz_thickness (7), x_fracture_zone_start/end,
+        matid_fz (7), age_lithosphere_left/right (Myr), thermal_lithosphere_depth_left/right,
+        thermal_diffusivity, adiabatic_gradient); returns (nrecycle_air, nrecycle_subsurface)."""
         p = _abi.RecycleParams(recycle_type, matid_sticky_air, matid_sticky_water, matid_asthenosphere, xsize, ysize,
                                velocity_y_upper, velocity_y_lower, temperature_bottom, iuse_random_fric,
                                delta_fric_coef, seed, counter)
-        if contraction:
-            k = contraction
-            p.asymmetric = int(k.get("asymmetric", 0))
-            p.full_velocity_contraction = k["full_velocity_contraction"]
-            p.sticky_thickness_left, p.sticky_thickness_right = k["sticky_thickness_left"], k["sticky_thickness_right"]
-            p.layer_thickness[:] = list(k["layer_thickness"])
-            p.x_left_strong, p.x_right_strong = k["x_left_strong"], k["x_right_strong"]
-            p.matid_layers[:] = list(k["matid_layers"])
-            p.matid_strong[:] = list(k["matid_strong"])
-        if side_inflow:
-            for name, v in side_inflow.items():
-                setattr(p, name, v)
+        for group in (contraction, side_inflow, fracture_zone):
+            for name, v in (group or {}).items():
+                if name in ("layer_thickness", "matid_layers", "matid_strong", "fz_thickness", "matid_fz"):
+                    getattr(p, name)[:] = list(v)
+                else:
+                    setattr(p, name, int(v) if name == "asymmetric" else v)
         na, ns = C.c_int64(), C.c_int64()
         self._check(self._lib.eb_recycle_markers(self._ctx, C.byref(p), C.byref(na), C.byref(ns)))
         return na.value, ns.value

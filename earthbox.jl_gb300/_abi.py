@@ -192,7 +192,11 @@ class RecycleParams(C.Structure):
                 ("x_left_strong", C.c_double), ("x_right_strong", C.c_double), ("matid_layers", C.c_int32 * 7),
                 ("matid_strong", C.c_int32 * 3), ("plate_thickness", C.c_double), ("smoothing_thickness", C.c_double),
                 ("velocity_inflow_left", C.c_double), ("velocity_inflow_right", C.c_double),
-                ("adiabatic_gradient", C.c_double)]
+                ("adiabatic_gradient", C.c_double), ("fz_thickness", C.c_double * 7),
+                ("x_fracture_zone_start", C.c_double), ("x_fracture_zone_end", C.c_double),
+                ("matid_fz", C.c_int32 * 7), ("age_lithosphere_left", C.c_double),
+                ("age_lithosphere_right", C.c_double), ("thermal_lithosphere_depth_left", C.c_double),
+                ("thermal_lithosphere_depth_right", C.c_double), ("thermal_diffusivity", C.c_double)]
 
 
 class HeatParams(C.Structure):

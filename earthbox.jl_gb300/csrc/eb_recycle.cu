@@ -76,7 +76,49 @@ struct RecycleK {
   // side inflow: top of the inflow zone (= top of the ramp) and base of the ramp per side,
   // inflow bands |v_left| dt and -|v_right| dt, adiabatic gradient (K/km)
   double in_top_l, in_top_r, ramp_bot_l, ramp_bot_r, disp_in_l, disp_in_r, adiabatic;
+  // fracture zone: layer bases (sticky air, sediments, basaltic crust, gabbroic crust, younger,
+  // older and weak lithosphere), zone limits, material ids, and the thermal model
+  double fz_base[7], x_fz_start, x_fz_end;
+  int16_t fz_id[7];  // air, sediment, basaltic, gabbroic, mantle lithosphere, weak mantle, asthenosphere
+  double kappa, age_l, age_r, tld_l, tld_r, t_top_fz;
 };
+
+// FractureZone.define_material (marker_materials/init_manager/types/FractureZone.jl:103-299):
+// asthenosphere, then each rule in turn overrides the id where it applies.
+__device__ int16_t fz_material(double x, double y, const RecycleK& p) {
+  const double* b = p.fz_base;
+  int16_t id = p.fz_id[6];
+  if (y <= b[0]) id = p.fz_id[0];
+  if (b[0] < y && y <= b[1]) id = p.fz_id[1];
+  if (b[1] < y && y <= b[2]) id = p.fz_id[2];
+  if (b[2] < y && y <= b[3]) id = p.fz_id[3];
+  const bool younger = x < p.x_fz_end && b[3] < y && y <= b[4];
+  const bool older = x >= p.x_fz_end && b[3] < y && y <= b[5];
+  if (younger || older) id = p.fz_id[4];
+  // weak gabbroic crust: basaltic-crust material up to x_end + (base of gabbro - y) * 25
+  const double x_weak_end = p.x_fz_end + (b[3] - y) * 25.0;
+  if (p.x_fz_start < x && x < x_weak_end && b[2] < y && y <= b[3]) id = p.fz_id[2];
+  if (p.x_fz_start < x && x < p.x_fz_end && b[3] < y && y <= b[6]) id = p.fz_id[5];
+  return id;
+}
+// FractureZone.calculate_temperature (markers/temperature/init_manager/types/FractureZone.jl:
+// 107-202): adiabat, T_top in the sticky layer, half-space cooling of the plate's age on either
+// side of x_end (sqrt(kappa age) for the reference's (kappa age)^0.5)
+__device__ double fz_lith_temperature(const RecycleK& p, double asth_thickness, double depth, double age) {
+  const double t_base = p.t_bottom - p.adiabatic * asth_thickness / 1000.0;
+  return t_base + (p.t_top_fz - t_base) * (1 - erf(depth / (2 * sqrt(p.kappa * age))));
+}
+__device__ double fz_temperature(double x, double y, const RecycleK& p) {
+  const double sticky = p.fz_base[0];
+  const double sub = y - sticky;
+  double t = p.t_bottom - (p.adiabatic * (p.ysize - y) / 1000.0);
+  if (y <= sticky) t = p.t_top_fz;
+  else if (0 < x && x < p.x_fz_end && sticky < y && y < p.tld_l)
+    t = fz_lith_temperature(p, p.ysize - p.tld_l, sub, p.age_l);
+  else if (x > p.x_fz_end && sticky < y && y < p.tld_r)
+    t = fz_lith_temperature(p, p.ysize - p.tld_r, sub, p.age_r);
+  return t;
+}
 
 // SevenLayerEarthModel2D.define_material (marker_materials/init_manager/utils/
 // SevenLayerEarthModel2D.jl:20-62) followed by StrongRegions.define_material
@@ -115,7 +157,7 @@ __device__ __forceinline__ bool selected(const DevMarkers& mk, int64_t m, const 
 // sticky rank (air/water positions): extension and contraction; the other types treat every
 // marker alike
 __device__ __forceinline__ bool sticky_sel(const DevMarkers& mk, int64_t m, const RecycleK& p) {
-  return (p.type == 1 || p.type == 4 || p.type == 5) && sticky(mk.matid[m], p);
+  return (p.type == 1 || p.type >= 4) && sticky(mk.matid[m], p);
 }
 
 // per block: number of outside markers and of outside sticky markers
@@ -179,8 +221,8 @@ __global__ void k_recycle_apply(DevMarkers mk, DevMats mt, RecycleK p, const int
     mk.fric[m] = p.fric_air;
     return;
   }
-  if (p.type == 4) {
-    // ContractionViscoelastic.execute_recycle_steps (types/ContractionViscoelastic.jl:60-111):
+  if (p.type == 4 || p.type == 6) {
+    // ContractionViscoelastic / ContractionFractureZone .execute_recycle_steps (types/ContractionViscoelastic.jl:60-111):
     // the k-th sticky / subsurface marker takes the k-th position of its group; the first
     // floor(n/2) of a group (none when asymmetric) enter at the left side, x = 0 + u d,
     // the others at the right, x = xsize + u (-d) (ContractionRecycleLocations.jl:9-140);
@@ -211,9 +253,11 @@ __global__ void k_recycle_apply(DevMarkers mk, DevMats mt, RecycleK p, const int
     } else {
       // get_subsurface_reset_properties_viscoelastic_contraction (ContractionViscoelastic.jl:
       // 69-111): material at the new position, pressure 3300 * 9.81 * y, temperature 0
-      const int16_t id = contraction_material(x, y, p);
+      // (fracture zone: FractureZoneProperties.jl:17-55, material and temperature of the
+      // fracture-zone initial model)
+      const int16_t id = p.type == 4 ? contraction_material(x, y, p) : fz_material(x, y, p);
       mk.matid[m] = id;
-      mk.tk[m] = 0.0;
+      mk.tk[m] = p.type == 4 ? 0.0 : fz_temperature(x, y, p);
       mk.pr[m] = 3300.0 * 9.81 * y;
       mk.sxx[m] = 1.96e6; mk.sxy[m] = 1.96e6;
       mk.exx[m] = 1e-14; mk.exy[m] = 1e-14;
@@ -324,15 +368,17 @@ extern "C" int eb_recycle_markers(eb_ctx* c, const eb_recycle_params* rp, int64_
                                   int64_t* nrecycle_subsurface) {
   if (!c || !rp) return EB_BAD_INPUT;
   if (!c->have_grid || !c->have_params || !c->have_mats) return eb_fail(c, EB_NOT_READY, "grid, parameters and materials must be set");
-  if (rp->recycle_type < 1 || rp->recycle_type > 5)
+  if (rp->recycle_type < 1 || rp->recycle_type > 6)
     return eb_fail(c, EB_BAD_INPUT, "recycle_type must be 1 (extension), 2 (extension without bottom inflow), "
-                                    "3 (channel), 4 (contraction) or 5 (extension with side inflow and outflow)");
+                                    "3 (channel), 4 (contraction), 5 (extension with side inflow and outflow) "
+                                    "or 6 (fracture-zone contraction)");
   const int64_t nmat = c->mats.nmat;
   std::vector<int64_t> ids = {rp->matid_sticky_air, rp->matid_sticky_water, rp->matid_asthenosphere};
   if (rp->recycle_type == 4) {
     ids.insert(ids.end(), rp->matid_layers, rp->matid_layers + 7);
     ids.insert(ids.end(), rp->matid_strong, rp->matid_strong + 3);
   }
+  if (rp->recycle_type == 6) ids.insert(ids.end(), rp->matid_fz, rp->matid_fz + 7);
   for (int64_t id : ids)
     if (id < 1 || id > nmat) return eb_fail(c, EB_BAD_INPUT, "recycle material id outside the material table");
   if (c->M > 0 && c->matid_min < 1) return eb_fail(c, EB_NOT_READY, "marker_matid has not been uploaded");
@@ -361,7 +407,7 @@ extern "C" int eb_recycle_markers(eb_ctx* c, const eb_recycle_params* rp, int64_
              3300.0 * 9.81 * c->h_gy.back(), c->h_gy.back(), c->h_gy.back() - c->h_gy.front(),
              mp[2 * nmat + rp->matid_sticky_air - 1], mp[2 * nmat + rp->matid_asthenosphere - 1],
              rp->iuse_random_fric, rp->delta_fric_coef, rp->seed, rp->counter};
-  if (rp->recycle_type == 4) {
+  if (rp->recycle_type == 4 || rp->recycle_type == 6) {
     // ContractionRecycleLocations.get_displacement_velocity: |v| dt / 2, or |v| dt asymmetric
     p.asym = rp->asymmetric ? 1 : 0;
     p.disp_side = p.asym ? std::fabs(rp->full_velocity_contraction) * c->P.timestep
@@ -376,6 +422,29 @@ extern "C" int eb_recycle_markers(eb_ctx* c, const eb_recycle_params* rp, int64_
     p.x_right_strong = rp->x_right_strong;
     for (int k = 0; k < 7; ++k) p.layer_id[k] = (int16_t)rp->matid_layers[k];
     for (int k = 0; k < 3; ++k) p.strong_id[k] = (int16_t)rp->matid_strong[k];
+  }
+  if (rp->recycle_type == 6) {
+    // FractureZone.define_geometry: bases as running sums from the sticky layer / gabbro base
+    const double* t = rp->fz_thickness;
+    p.fz_base[0] = t[0];
+    p.fz_base[1] = p.fz_base[0] + t[1];
+    p.fz_base[2] = p.fz_base[1] + t[2];
+    p.fz_base[3] = p.fz_base[2] + t[3];
+    p.fz_base[4] = p.fz_base[3] + t[4];
+    p.fz_base[5] = p.fz_base[3] + t[5];
+    p.fz_base[6] = p.fz_base[3] + t[6];
+    p.x_fz_start = rp->x_fracture_zone_start;
+    p.x_fz_end = rp->x_fracture_zone_end;
+    for (int k = 0; k < 7; ++k) p.fz_id[k] = (int16_t)rp->matid_fz[k];
+    // get_thermal_parameters: ages in Myr -> s (ConversionFuncs.millions_of_years_to_seconds)
+    const double seconds_per_year = 365.25 * 24.0 * 3600.0;
+    p.age_l = (rp->age_lithosphere_left * 1e6) * seconds_per_year;
+    p.age_r = (rp->age_lithosphere_right * 1e6) * seconds_per_year;
+    p.tld_l = rp->thermal_lithosphere_depth_left;
+    p.tld_r = rp->thermal_lithosphere_depth_right;
+    p.kappa = rp->thermal_diffusivity;
+    p.adiabatic = rp->adiabatic_gradient;
+    p.t_top_fz = c->P.temperature_top;
   }
   if (rp->recycle_type == 5) {
     // InflowGeometry.calculate_top_of_side_inflow / InflowRamp.get_top_and_bottom_of_inflow_ramp:

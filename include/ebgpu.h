@@ -570,7 +570,8 @@ typedef struct eb_recycle_params {
                                       markers below gridy_b[ynum] move up by the grid height and
                                       their temperature by temperature_top - temperature_bottom; the
                                       inside flags are not used); 4: contraction, 5: extension with
-                                      side inflow and outflow (fields below)                         */
+                                      side inflow and outflow, 6: fracture-zone contraction (fields
+                                      below)                                                        */
   int32_t matid_sticky_air, matid_sticky_water, matid_asthenosphere;  /* material ids                 */
   double  xsize, ysize;            /* model size (m); the domain starts at x = y = 0                    */
   double  velocity_y_upper, velocity_y_lower;  /* vyu, vyl (m/s): band widths |v dt|                   */
@@ -600,6 +601,20 @@ typedef struct eb_recycle_params {
   double  plate_thickness, smoothing_thickness;          /* OutflowGeometry.get_outflow_geometry (m) */
   double  velocity_inflow_left, velocity_inflow_right;   /* m/s                                      */
   double  adiabatic_gradient;      /* K/km: T = temperature_bottom - gradient (ysize - y) / 1000     */
+  /* recycle_type 6: fracture-zone contraction (FractureZoneContractionFixedBoundaries[Asymmetric] ->
+     types/ContractionFractureZone.jl): positions as type 4 (asymmetric, full_velocity_contraction,
+     sticky_thickness_left/right); subsurface markers take the material and the temperature of the
+     fracture-zone initial model (FractureZoneProperties.jl), pressure 3300 * 9.81 * y;
+     adiabatic_gradient as above                                                                    */
+  double  fz_thickness[7];         /* thick_air, sediment, basaltic crust, gabbroic crust, younger /
+                                      older / weak lithosphere (FractureZone.define_geometry)       */
+  double  x_fracture_zone_start, x_fracture_zone_end;
+  int32_t matid_fz[7];             /* Atmosphere, SedimentaryBasin, BasalticOceanicCrust,
+                                      GabbroicOceanicCrust, MantleLithosphere, WeakMantleLithosphere,
+                                      Asthenosphere                                                 */
+  double  age_lithosphere_left, age_lithosphere_right;   /* Myr                                      */
+  double  thermal_lithosphere_depth_left, thermal_lithosphere_depth_right;  /* m                      */
+  double  thermal_diffusivity;     /* m^2/s                                                          */
 } eb_recycle_params;
 int eb_recycle_markers(eb_ctx* ctx, const eb_recycle_params* p, int64_t* nrecycle_air, int64_t* nrecycle_subsurface);
 /* The markers of the last eb_recycle_markers: 1-based indices and flags (0 sticky, 1 subsurface),

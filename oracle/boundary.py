@@ -1,9 +1,8 @@
 """CPU oracle (TEST INFRASTRUCTURE ONLY) for the step-boundary updates: the rock
 properties of the markers (rock_properties/RockProperties.jl:99-125) and the
 displacement-limited time step (time_step/update/Update.jl:16-219) and the marker recycling
-of the extension, no-bottom-inflow, channel, contraction and side-inflow models
-(marker_recycle/types/{Extension,ExtensionNoBottomInflow,Channel,ContractionViscoelastic,
-ExtensionInflowAndOutflowAlongSides}.jl),
+of every model type (marker_recycle/types/{Extension,ExtensionNoBottomInflow,Channel,
+ContractionViscoelastic,ExtensionInflowAndOutflowAlongSides,ContractionFractureZone}.jl),
 restated in boundary_oracle.c.  Only tests/ use it."""
 from __future__ import annotations
 
@@ -181,6 +180,39 @@ def recycle_side_inflow(mk: dict, matid_sticky_air, matid_sticky_water, matid_as
                                     _p(d), C.c_int64(mp.shape[0]), _p(mp), C.c_int64(iuse_random_fric),
                                     C.c_uint64(seed), C.c_int64(step), _p(lst), _p(fl), _p(nx), _p(ny),
                                     C.byref(n_air))
+    return out, lst[:n].copy(), fl[:n].copy(), n_air.value
+
+
+def recycle_fracture_zone(mk: dict, matid_sticky_air, matid_sticky_water, matid_fz, xsize, ysize,
+                          full_velocity_contraction, timestep, sticky_thickness_left, sticky_thickness_right,
+                          temperature_top, temperature_bottom, adiabatic_gradient, fz_thickness,
+                          x_fracture_zone_start, x_fracture_zone_end, age_lithosphere_left, age_lithosphere_right,
+                          thermal_lithosphere_depth_left, thermal_lithosphere_depth_right, thermal_diffusivity,
+                          mat_plastic, iuse_random_fric, delta_fric_coef, seed, step, asymmetric=0) -> tuple:
+    """ContractionFractureZone recycling; returns (fields, 1-based indices, flags, n_air)."""
+    M = len(mk["x"])
+    out = {k: np.array(mk[k], dtype=np.float64, copy=True) for k in RECYCLE_FIELDS}
+    out["matid"] = np.array(mk["matid"], dtype=np.int16, copy=True)
+    out["pfailure"] = np.array(mk["pfailure"], dtype=np.float32, copy=True)
+    inside = np.ascontiguousarray(mk["inside"], dtype=np.int8)
+    ptrs = (C.c_void_p * len(RECYCLE_FIELDS))(*[out[k].ctypes.data for k in RECYCLE_FIELDS])
+    ids = np.array([matid_sticky_air, matid_sticky_water, *matid_fz], np.int16)
+    assert len(ids) == 9 and len(fz_thickness) == 7
+    d = np.array([xsize, ysize, full_velocity_contraction, timestep, sticky_thickness_left, sticky_thickness_right,
+                  temperature_top, temperature_bottom, adiabatic_gradient, *fz_thickness, x_fracture_zone_start,
+                  x_fracture_zone_end, age_lithosphere_left, age_lithosphere_right, thermal_lithosphere_depth_left,
+                  thermal_lithosphere_depth_right, thermal_diffusivity, delta_fric_coef], np.float64)
+    assert len(d) == 24
+    mp = np.asfortranarray(mat_plastic, dtype=np.float64)
+    lst = np.zeros(max(M, 1), np.int64)
+    fl = np.zeros(max(M, 1), np.int8)
+    nx, ny = np.zeros(max(M, 1)), np.zeros(max(M, 1))
+    n_air = C.c_int64()
+    lib().o_recycle_fracture_zone.restype = C.c_int64
+    n = lib().o_recycle_fracture_zone(C.c_int64(M), _p(inside), _p(out["matid"]), ptrs, _p(out["pfailure"]),
+                                      _p(ids), _p(d), C.c_int64(int(asymmetric)), C.c_int64(mp.shape[0]), _p(mp),
+                                      C.c_int64(iuse_random_fric), C.c_uint64(seed), C.c_int64(step), _p(lst),
+                                      _p(fl), _p(nx), _p(ny), C.byref(n_air))
     return out, lst[:n].copy(), fl[:n].copy(), n_air.value
 
 

@@ -23,6 +23,9 @@
  *       markers/utils/Layers.jl:31-54
  *   o_recycle_side_inflow           marker_recycle/types/ExtensionInflowAndOutflowAlongSides.jl:20-237
  *       with boundary_velocity/utils/{InflowGeometry.jl,InflowRamp.jl}, Coordinates.jl:155-200
+ *   o_recycle_fracture_zone         marker_recycle/types/ContractionFractureZone.jl:11-61 with
+ *       utils/FractureZoneProperties.jl:17-55, marker_materials/init_manager/types/FractureZone.jl:
+ *       63-299 and temperature/init_manager/types/FractureZone.jl:86-202 (erf from libm)
  *
  * Grids are column-major (rows, cols).  Julia's x^2 and x^3 of a Float64 literal power
  * are x*x and x*x*x.
@@ -495,6 +498,128 @@ int64_t o_recycle_side_inflow(int64_t M, const int8_t* inside, int16_t* matid, d
       double r, unused;
       o_recycle_uniforms(seed, step, 2u, m, &r, &unused);
       if (r <= 0.5) fric = fric - d[13];
+    }
+    f[R_FRIC_INI][m] = fric;
+    f[R_FRIC][m] = fric;
+    list[k] = m + 1;
+  }
+  *n_air = nair;
+  return nout;
+}
+
+/* FractureZone.define_material: the set_* rules in order, each overriding the previous id.
+ * b[]: bases of sticky air, sediments, basaltic crust, gabbroic crust, younger, older and weak
+ * lithosphere (define_geometry); id[]: air, sediment, basaltic, gabbroic, mantle lithosphere,
+ * weak mantle lithosphere, asthenosphere. */
+static int16_t fz_define_material(double x, double y, const double* b, double x_start, double x_end,
+                                  const int16_t* id) {
+  int16_t m = id[6];                                             /* set_asthenosphere */
+  if (y <= b[0]) m = id[0];                                      /* set_sticky_air */
+  if (b[0] < y && y <= b[1]) m = id[1];                          /* set_sediments */
+  if (b[1] < y && y <= b[2]) m = id[2];                          /* set_basaltic_crust */
+  if (b[2] < y && y <= b[3]) m = id[3];                          /* set_gabbroic_crust */
+  const int younger = x < x_end && b[3] < y && y <= b[4];        /* in_younger_lithosphere */
+  const int older = x >= x_end && b[3] < y && y <= b[5];         /* in_older_lithosphere */
+  if (younger || older) m = id[4];                               /* set_lithosphere */
+  const double x_weak_end = x_end + (b[3] - y) * 25.0;           /* get_x_end_of_weak_oceanic_crust */
+  if (x_start < x && x < x_weak_end && (b[2] < y && y <= b[3])) m = id[2];
+  if (x_start < x && x < x_end && b[3] < y && y <= b[6]) m = id[5];  /* set_weak_mantle_of_fracture_zone */
+  return m;
+}
+
+/* calc_lithosphere_temperature with (kappa age)^0.5 as sqrt */
+static double fz_lith_temp(double t_top, double t_bottom, double grad, double asth, double kappa, double depth,
+                           double age) {
+  const double t_base = t_bottom - grad * asth / 1000.0;
+  return t_base + (t_top - t_base) * (1 - erf(depth / (2 * sqrt(kappa * age))));
+}
+
+/* FractureZone.calculate_temperature(y, x, thermal_parameters); th[]: t_top, t_bottom, gradient,
+ * x_end, age_left (s), age_right (s), sticky thickness, lithosphere depth left, right, kappa, ysize */
+static double fz_calculate_temperature(double y, double x, const double* th) {
+  const double t_top = th[0], t_bottom = th[1], grad = th[2], x_end = th[3], sticky = th[6];
+  const double ysize = th[10], kappa = th[9];
+  const double sub_sticky_depth = y - sticky;
+  const double left_asth = ysize - th[7], right_asth = ysize - th[8];
+  double t = t_bottom - (grad * (ysize - y) / 1000.0);
+  if (y <= sticky) t = t_top;
+  else if (0 < x && x < x_end && sticky < y && y < th[7])
+    t = fz_lith_temp(t_top, t_bottom, grad, left_asth, kappa, sub_sticky_depth, th[4]);
+  else if (x > x_end && sticky < y && y < th[8])
+    t = fz_lith_temp(t_top, t_bottom, grad, right_asth, kappa, sub_sticky_depth, th[5]);
+  return t;
+}
+
+/* ContractionFractureZone.execute_recycle_steps (marker_recycle/types/ContractionFractureZone.jl:
+ * 11-61): positions as o_recycle_contraction, subsurface properties from
+ * FractureZoneProperties.get_subsurface_reset_properties_fracture_zone (FractureZoneProperties.jl:
+ * 17-55).  ids[]: sticky_air, sticky_water, fz ids[7]; d[]: xsize, ysize,
+ * full_velocity_contraction, timestep, sticky_thickness_left, sticky_thickness_right,
+ * temperature_top, temperature_bottom, adiabatic_gradient, fz thickness[7], x_fz_start, x_fz_end,
+ * age_left (Myr), age_right (Myr), lithosphere depth left, right, kappa, delta_fric_coef. */
+int64_t o_recycle_fracture_zone(int64_t M, const int8_t* inside, int16_t* matid, double** f, float* pfailure,
+                                const int16_t* ids, const double* d, int64_t asym, int64_t nmat,
+                                const double* mat_plastic, int64_t iuse_random_fric, uint64_t seed, int64_t step,
+                                int64_t* list, int8_t* flags, double* newx, double* newy, int64_t* n_air) {
+  const int16_t air = ids[0], water = ids[1];
+  const double xsize = d[0], ysize = d[1];
+  const double disp = asym ? fabs(d[2]) * d[3] : fabs(d[2]) * d[3] * 0.5;
+  const double* t = d + 9;
+  /* FractureZone.define_geometry */
+  double b[7];
+  b[0] = t[0];
+  b[1] = b[0] + t[1];
+  b[2] = b[1] + t[2];
+  b[3] = b[2] + t[3];
+  b[4] = b[3] + t[4];
+  b[5] = b[3] + t[5];
+  b[6] = b[3] + t[6];
+  /* get_thermal_parameters (millions_of_years_to_seconds: (t 1e6) (365.25 24 3600)) */
+  const double spy = 365.25 * 24.0 * 3600.0;
+  const double th[11] = {d[6], d[7], d[8], d[17], (d[18] * 1e6) * spy, (d[19] * 1e6) * spy, t[0], d[20], d[21],
+                         d[22], ysize};
+  int64_t nout = 0, nair = 0, nsub = 0;
+  for (int64_t m = 0; m < M; ++m)
+    if (inside[m] != 1) {
+      list[nout++] = m;
+      if (matid[m] == air || matid[m] == water) ++nair; else ++nsub;
+    }
+  double *ax = newx, *ay = newy, *sx = newx + nair, *sy = newy + nair;
+  contraction_positions(nair, asym, 1, xsize, ysize, disp, d[4], d[5], seed, step, 0u, ax, ay);
+  contraction_positions(nsub, asym, 0, xsize, ysize, disp, d[4], d[5], seed, step, 1u, sx, sy);
+  int64_t ia = 0, is = 0;
+  for (int64_t k = 0; k < nout; ++k) {
+    const int64_t m = list[k];
+    const int sticky = (matid[m] == air || matid[m] == water) && nair > 0;
+    if (sticky) { f[R_X][m] = ax[ia]; f[R_Y][m] = ay[ia]; ++ia; }
+    else { f[R_X][m] = sx[is]; f[R_Y][m] = sy[is]; ++is; }
+    flags[k] = (int8_t)(sticky ? 0 : 1);
+    int16_t id;
+    if (sticky) {
+      id = air;
+      f[R_TK][m] = d[6];
+      f[R_PR][m] = 0.0;
+      f[R_SXX][m] = f[R_SXY][m] = 0.0;
+      f[R_EXX][m] = f[R_EXY][m] = 0.0;
+      f[R_ETA][m] = 0.0;
+    } else {
+      id = fz_define_material(f[R_X][m], f[R_Y][m], b, d[16], d[17], ids + 2);
+      f[R_TK][m] = fz_calculate_temperature(f[R_Y][m], f[R_X][m], th);
+      f[R_PR][m] = 3300.0 * 9.81 * f[R_Y][m];
+      f[R_SXX][m] = f[R_SXY][m] = 1.96e6;
+      f[R_EXX][m] = f[R_EXY][m] = 1e-14;
+      f[R_ETA][m] = 1e20;
+    }
+    matid[m] = id;
+    f[R_SR_RATIO][m] = 0.0;
+    f[R_GII][m] = f[R_SP][m] = f[R_SRP][m] = 0.0;
+    f[R_MELT][m] = 0.0;
+    pfailure[m] = 0.0f;
+    double fric = mat_plastic[2 * nmat + (id - 1)];
+    if (!sticky && iuse_random_fric == 1) {
+      double r, unused;
+      o_recycle_uniforms(seed, step, 2u, m, &r, &unused);
+      if (r <= 0.5) fric = fric - d[23];
     }
     f[R_FRIC_INI][m] = fric;
     f[R_FRIC][m] = fric;

@@ -441,3 +441,95 @@ def test_recycle_side_inflow_oracle_matches_reference_loops(eb, B, rf):
     assert np.all(y[sub] >= 10e3 + 40e3 + 15e3)
     ramp = sub & (y < 12e3 + 40e3 + 30e3) & (y > 12e3 + 40e3 + 15e3)
     assert ramp.sum() > 5
+
+
+def reference_fz_material(x, y, b, x_start, x_end, ids):
+    """FractureZone.define_material (marker_materials/init_manager/types/FractureZone.jl:103-299)."""
+    m = ids[6]
+    if y <= b[0]:
+        m = ids[0]
+    if b[0] < y <= b[1]:
+        m = ids[1]
+    if b[1] < y <= b[2]:
+        m = ids[2]
+    if b[2] < y <= b[3]:
+        m = ids[3]
+    if (x < x_end and b[3] < y <= b[4]) or (x >= x_end and b[3] < y <= b[5]):
+        m = ids[4]
+    if x_start < x < x_end + (b[3] - y) * 25.0 and b[2] < y <= b[3]:
+        m = ids[2]
+    if x_start < x < x_end and b[3] < y <= b[6]:
+        m = ids[5]
+    return m
+
+
+def reference_fz_temperature(y, x, ttop, tbot, grad, x_end, age_l, age_r, sticky, tld_l, tld_r, kappa, ysize):
+    """FractureZone.calculate_temperature (temperature/init_manager/types/FractureZone.jl:107-202)."""
+    import math
+
+    def lith(asth, depth, age):
+        tb = tbot - grad * asth / 1000.0
+        return tb + (ttop - tb) * (1 - math.erf(depth / (2 * (kappa * age) ** 0.5)))
+    t = tbot - (grad * (ysize - y) / 1000.0)
+    if y <= sticky:
+        t = ttop
+    elif 0 < x < x_end and sticky < y < tld_l:
+        t = lith(ysize - tld_l, y - sticky, age_l)
+    elif x > x_end and sticky < y < tld_r:
+        t = lith(ysize - tld_r, y - sticky, age_r)
+    return t
+
+
+FZ = dict(ids=(1, 5, 6, 7, 8, 9, 10), thick=(10e3, 1e3, 2e3, 4e3, 40e3, 70e3, 20e3), x_start=-1.0, x_end=30e3,
+          ages=(10.0, 40.0), tld=(60e3, 100e3), kappa=1e-6, grad=0.4)
+
+
+@pytest.mark.parametrize("asym", [0, 1])
+def test_recycle_fracture_zone_oracle(eb, B, asym):
+    """Positions are the contraction ones (the viscoelastic-contraction test pins them); the
+    fracture-zone material and temperature of each subsurface marker equal the reference's
+    functions written out in Python (temperature within 1e-14: libm's erf against Python's)."""
+    rng = np.random.default_rng(81 + asym)
+    M = 3000
+    mk = {k: rng.uniform(-1.0, 1.0, M) for k in B.RECYCLE_FIELDS}
+    mk["matid"] = rng.integers(1, 13, M).astype(np.int16)
+    mk["pfailure"] = rng.uniform(0, 1, M).astype(np.float32)
+    mk["inside"] = np.where(rng.random(M) < 0.7, 1, rng.choice([0, -1], M)).astype(np.int8)
+    mp = np.asfortranarray(rng.uniform(0, 1, (12, 6)))
+    z = FZ
+    xsize, ysize, vfull, dt, hl, hr, ttop, tbot = 500e3, 160e3, 3e-9, 3.15e13, 10e3, 12e3, 273.0, 1603.0
+    seed, step = 5151, 8
+    got, idx, fl, nair = B.recycle_fracture_zone(mk, 1, 2, z["ids"], xsize, ysize, vfull, dt, hl, hr, ttop, tbot,
+                                                 z["grad"], z["thick"], z["x_start"], z["x_end"], *z["ages"],
+                                                 *z["tld"], z["kappa"], mp, 1, 0.02, seed, step, asym)
+    ref, ridx, rfl, rnair = B.recycle_contraction(mk, 1, 2, (1,) * 7, (1,) * 3, xsize, ysize, vfull, dt, hl, hr,
+                                                  ttop, (1.0,) * 6, -1.0, 1e30, mp, 1, 0.02, seed, step, asym)
+    assert nair == rnair and np.array_equal(idx, ridx) and np.array_equal(fl, rfl)
+    assert np.array_equal(got["x"], ref["x"]) and np.array_equal(got["y"], ref["y"])
+    t = z["thick"]
+    b = [t[0]]
+    for v in t[1:4]:
+        b.append(b[-1] + v)
+    b += [b[3] + t[4], b[3] + t[5], b[3] + t[6]]
+    spy = 365.25 * 24.0 * 3600.0
+    ages = [(a * 1e6) * spy for a in z["ages"]]
+    mats, sub = set(), 0
+    for i, flag in zip(idx - 1, fl):
+        if flag == 0:
+            assert got["matid"][i] == 1 and got["tk"][i] == ttop
+            continue
+        sub += 1
+        x, y = got["x"][i], got["y"][i]
+        m = reference_fz_material(x, y, b, z["x_start"], z["x_end"], z["ids"])
+        assert got["matid"][i] == m
+        mats.add(m)
+        want_t = reference_fz_temperature(y, x, ttop, tbot, z["grad"], z["x_end"], *ages, t[0], *z["tld"],
+                                          z["kappa"], ysize)
+        assert abs(got["tk"][i] - want_t) <= 1e-14 * abs(want_t)
+        assert got["pr"][i] == 3300.0 * 9.81 * y
+        f = mp[m - 1, 2]
+        if B.recycle_uniforms(seed, step, 2, i)[0] <= 0.5:
+            f = f - 0.02
+        assert got["fric"][i] == f
+    # (the right side's 12 km sticky layer lies below the sediments' base: no sediment there)
+    assert sub > 100 and {6, 7, 8, 10}.issubset(mats) and (5 in mats) == (not asym)

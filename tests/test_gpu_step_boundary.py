@@ -269,3 +269,69 @@ def test_recycle_side_inflow_matches_oracle(eb, random_fric):
     mic.get_marker_inside_flags()
     assert np.all(mic.download_marker("inside") == 1)
     mic.close()
+
+
+@pytest.mark.parametrize("asym", [0, 1])
+def test_recycle_fracture_zone_matches_oracle(eb, asym):
+    """Recycling type 6 (ContractionFractureZone): contraction positions, fracture-zone material
+    and temperature; bit-identical to the oracle except the temperature, within 1e-14 (CUDA's
+    erf against libm's)."""
+    import dataclasses
+    from oracle import boundary as B
+    model = eb.synthetic.config("rift_small")
+    g = model.grid
+    p = model.params
+    rng = np.random.default_rng(91 + asym)
+    m0 = model.mats
+    rows = np.arange(12) % len(m0.mat_mu)
+    mp = np.asfortranarray(np.asarray(m0.mat_plastic)[rows].copy())
+    mp[:, 2] = rng.uniform(0.1, 0.6, 12)
+    mats = dataclasses.replace(m0, mat_mu=np.asarray(m0.mat_mu)[rows], mat_hr=np.asarray(m0.mat_hr)[rows],
+                               mat_flow_type=np.asarray(m0.mat_flow_type)[rows],
+                               mat_flow=np.asfortranarray(np.asarray(m0.mat_flow)[rows]), mat_plastic=mp,
+                               mat_rho=np.asarray(m0.mat_rho)[rows])
+    mic = eb.MarkerInCell(0)
+    mic.load_model(model)
+    mic.set_materials(mats)
+    M = model.marknum
+    x, y = mic.download_marker("x"), mic.download_marker("y")
+    out = rng.random(M) < 0.05
+    side = rng.integers(0, 4, M)
+    x = np.where(out & (side == 0), g.xmin - rng.uniform(1.0, 5e3, M), x)
+    x = np.where(out & (side == 1), g.xmax + rng.uniform(1.0, 5e3, M), x)
+    y = np.where(out & (side == 2), g.ymin - rng.uniform(1.0, 5e3, M), y)
+    y = np.where(out & (side == 3), g.ymax + rng.uniform(1.0, 5e3, M), y)
+    mic.upload_marker("x", x)
+    mic.upload_marker("y", y)
+    for k in B.RECYCLE_FIELDS[2:]:
+        mic.upload_marker(k, rng.uniform(0.5, 2.0, M))
+    mic.upload_marker("pfailure", rng.uniform(0, 1, M).astype(np.float32))
+    mic.get_marker_inside_flags()
+    mk = {k: mic.download_marker(k) for k in (*B.RECYCLE_FIELDS, "matid", "pfailure", "inside")}
+    fz_ids = (1, 5, 6, 7, 8, 9, 10)
+    thick = (0.05 * g.ymax, 0.01 * g.ymax, 0.02 * g.ymax, 0.03 * g.ymax, 0.25 * g.ymax, 0.45 * g.ymax, 0.15 * g.ymax)
+    hl, hr, vfull, seed, step, tbot = 0.04 * g.ymax, 0.06 * g.ymax, 2e-9, 616, 4, 1603.0
+    x_start, x_end, ages, tld, kappa, grad = -1.0, 0.2 * g.xmax, (15.0, 45.0), (0.4 * g.ymax, 0.6 * g.ymax), 1e-6, 0.4
+    want, widx, wfl, wnair = B.recycle_fracture_zone(mk, 1, 2, fz_ids, g.xmax, g.ymax, vfull, p["timestep"], hl, hr,
+                                                     p["temperature_top"], tbot, grad, thick, x_start, x_end, *ages,
+                                                     *tld, kappa, mp, 1, 0.05, seed, step, asym)
+    con = dict(asymmetric=asym, full_velocity_contraction=vfull, sticky_thickness_left=hl, sticky_thickness_right=hr)
+    fz = dict(fz_thickness=thick, x_fracture_zone_start=x_start, x_fracture_zone_end=x_end, matid_fz=fz_ids,
+              age_lithosphere_left=ages[0], age_lithosphere_right=ages[1], thermal_lithosphere_depth_left=tld[0],
+              thermal_lithosphere_depth_right=tld[1], thermal_diffusivity=kappa, adiabatic_gradient=grad)
+    nair, nsub = mic.recycle_markers(1, 2, 4, g.xmax, g.ymax, 0.0, 0.0, tbot, seed, step, iuse_random_fric=1,
+                                     delta_fric_coef=0.05, recycle_type=6, contraction=con, fracture_zone=fz)
+    assert (nair, nsub) == (wnair, len(widx) - wnair) and nair > 10 and nsub > 10
+    idx, fl = mic.recycled_markers()
+    assert np.array_equal(idx, widx) and np.array_equal(fl, wfl)
+    for k in (*B.RECYCLE_FIELDS, "matid", "pfailure"):
+        got = mic.download_marker(k)
+        if k == "tk":
+            np.testing.assert_allclose(got, want[k], rtol=1e-14, atol=0)
+        else:
+            assert np.array_equal(got, want[k]), k
+    lith = (wfl == 1) & np.isin(want["matid"][widx - 1], (8,))
+    assert lith.sum() > 5  # markers in the cooling plate (the erf branch)
+    mic.get_marker_inside_flags()
+    assert np.all(mic.download_marker("inside") == 1)
+    mic.close()
