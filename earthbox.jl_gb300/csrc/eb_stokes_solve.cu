@@ -737,13 +737,17 @@ __global__ void __launch_bounds__(kCoarseThreads) k_coarse_cycle(const LevelDev<
     for (int64_t c = threadIdx.x; c < w.nc; c += blockDim.x) d_restrict(v, w, c);
     __syncthreads();
   }
-  {  // coarsest: u = Ainv f
+  {  // coarsest: u = Ainv f, the inverse stored by columns (AinvT[k n + r]) so that the warp's
+     // rows r read one contiguous line per k
     const LevelDev<T> cl = lv[nl - 1];
     const int half = n / 2;
     for (int r = threadIdx.x; r < n; r += blockDim.x) {
-      T s = 0;
-      for (int k = 0; k < half; ++k) s += Ainv[(int64_t)r * n + k] * cl.fx[k];
-      for (int k = 0; k < half; ++k) s += Ainv[(int64_t)r * n + half + k] * cl.fy[k];
+      T s0 = 0, s1 = 0;
+      for (int k = 0; k < half; ++k) {
+        s0 += Ainv[(int64_t)k * n + r] * cl.fx[k];
+        s1 += Ainv[(int64_t)(half + k) * n + r] * cl.fy[k];
+      }
+      const T s = s0 + s1;
       if (r < half) cl.ux[r] = s; else cl.uy[r - half] = s;
     }
     __syncthreads();
@@ -1247,8 +1251,9 @@ int refresh_levels_t(eb_ctx* c, StokesState* st, const B2& b2) {
     if (hd) put(r, cc + 1, Ys(8));
   }
   if (!invert_dense(A, n, inv)) return eb_fail(c, EB_NAN, "coarsest multigrid operator is singular");
-  std::vector<T> invf(inv.size());
-  for (size_t k = 0; k < inv.size(); ++k) invf[k] = (T)inv[k];
+  std::vector<T> invf(inv.size());  // transposed: column k of the inverse is contiguous
+  for (int r = 0; r < n; ++r)
+    for (int k = 0; k < n; ++k) invf[(size_t)k * n + r] = (T)inv[(size_t)r * n + k];
   EB_CK(c, cudaMemcpyAsync(st->H().Ainv, invf.data(), invf.size() * sizeof(T), cudaMemcpyHostToDevice, c->stream));
   EB_CK(c, cudaStreamSynchronize(c->stream));
   return EB_OK;
