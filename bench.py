@@ -91,6 +91,9 @@ def parse():
     ap.add_argument("--circles", action="store_true",
                     help="also time the circles_1025 Stokes benchmark (200 inclusions, 1e-10)")
     ap.add_argument("--stokes-method", default="fgmres", choices=["fgmres", "bicgstab"])
+    ap.add_argument("--stokes-only", action="store_true",
+                    help="after the warm-up marker cycles run ONE mixed Stokes step and print its line "
+                         "(a small launch list for ncu; not the bench line)")
     return ap.parse_args()
 
 
@@ -369,6 +372,23 @@ def main():
 
     for _ in range(max(args.warmup, 3)):
         step()
+    if args.stokes_only:
+        # one Stokes step (terms, RHS, assembly, mixed FGMRES + MG solve, unpacking), no warm-up
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        mic.calc_viscoelastic_terms()
+        mic.viscoelastic_rhs()
+        mic.build_system_of_equations()
+        rep = mic.solve_system(rtol=1e-8, check=True, method=args.stokes_method)
+        mic.process_stokes_solution()
+        torch.cuda.synchronize()
+        if rank == 0:
+            print(json.dumps({"metric": "one Stokes step (profiling run)", "value": time.perf_counter() - t0,
+                              "unit": "s", "workload": args.workload, "iterations": rep["iterations"],
+                              "fp32_gram_schmidt_iterations": rep["relaxed_iterations"],
+                              "rel_residual": rep["rel_residual"]}))
+        mic.close()
+        return
     if world > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()
