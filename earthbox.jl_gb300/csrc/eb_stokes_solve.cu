@@ -624,9 +624,9 @@ struct LevelDev {
 template <class T>
 __device__ __forceinline__ void d_rbgs(const LevelDev<T>& v, int64_t t, int comp, int color) {
   const int32_t half = (v.ny + 1) / 2;
-  const int32_t j = (int32_t)(t / half);
+  const int32_t j = (int32_t)t / half;  // t < nx * half < 2^31
   if (j >= v.nx) return;
-  const int32_t i = 2 * (int32_t)(t - (int64_t)j * half) + ((j + color) & 1);
+  const int32_t i = 2 * ((int32_t)t - j * half) + ((j + color) & 1);
   if (i >= v.ny) return;
   const int64_t c = (int64_t)j * v.ny + i;
   if (comp == 0) {
@@ -642,14 +642,14 @@ __device__ __forceinline__ int64_t rb_count(const LevelDev<T>& v) { return (int6
 
 template <class T>
 __device__ __forceinline__ void d_resid(const LevelDev<T>& v, int64_t c) {
-  const int32_t i = (int32_t)(c % v.ny), j = (int32_t)(c / v.ny);
+  const int32_t j = (int32_t)c / v.ny, i = (int32_t)c - j * v.ny;  // cell indices fit 32 bits
   v.rx[c] = v.fx[c] - rowx(v.X, v.ux, v.uy, c, i, j, v.nx, v.ny, v.nc, false);
   v.ry[c] = v.fy[c] - rowy(v.Y, v.ux, v.uy, c, i, j, v.nx, v.ny, v.nc, false);
 }
 // coarse f = R r at coarse cell c (tensor product of the axis tables of the fine level f)
 template <class T>
 __device__ __forceinline__ void d_restrict(const LevelDev<T>& f, const LevelDev<T>& cl, int64_t c) {
-  const int32_t I = (int32_t)(c % cl.ny), J = (int32_t)(c / cl.ny);
+  const int32_t J = (int32_t)c / cl.ny, I = (int32_t)c - J * cl.ny;
   T sx = 0, sy = 0;
   for (int a = 0; a < kRmax; ++a) {
     const T wa = (T)f.rvx_x.w[J * kRmax + a];
@@ -675,7 +675,7 @@ __device__ __forceinline__ void d_restrict(const LevelDev<T>& f, const LevelDev<
 // fine u += P e at fine cell c
 template <class T>
 __device__ __forceinline__ void d_prolong(const LevelDev<T>& f, const LevelDev<T>& cl, int64_t c) {
-  const int32_t i = (int32_t)(c % f.ny), j = (int32_t)(c / f.ny);
+  const int32_t j = (int32_t)c / f.ny, i = (int32_t)c - j * f.ny;
   T sx = 0, sy = 0;
   for (int a = 0; a < 2; ++a)
     for (int b = 0; b < 2; ++b) {
@@ -772,7 +772,7 @@ __global__ void k_prec_in(const double* __restrict__ coef, const double* __restr
   const int64_t nc = (int64_t)nx * ny;
   const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= nc) return;
-  const int32_t i = (int32_t)(c % ny), j = (int32_t)(c / ny);
+  const int32_t j = (int32_t)c / ny, i = (int32_t)c - j * ny;
   auto z = [&](int64_t k) { return prep[k] * (rhat[2 * nc + k] * winv[2 * nc + k]); };
   const double zc = z(c);
   if (sizeof(T) == 4) {
