@@ -252,6 +252,12 @@ class MarkerInCell:
         """MarkerPlasticity.update_plastic_yielding! (ViscoelasticForecast.jl:11-123)."""
         self._call("eb_update_plastic_yielding")
 
+    def calc_marker_viscoplastic_viscosity(self) -> None:
+        """GridViscoplasticityToMarkers.calc_marker_viscoplastic_viscosity!
+        (src/rheology/plastic_failure/nodes/GridViscoplasticityToMarkers.jl:7-118): the nodal
+        Picard variant's grid viscoplastic viscosity back to the markers (eta, pfailure)."""
+        self._call("eb_calc_marker_viscoplastic_viscosity")
+
     def post_stokes_marker_gathers(self) -> None:
         """Marker part of StokesContinuitySolver.execute_post_stokes_solver_steps! (StokesContinuitySolver.jl:283-290)."""
         self._call("eb_post_stokes_marker_gathers")
@@ -296,19 +302,22 @@ class MarkerInCell:
 
     def solve_system(self, rtol: float = 1e-8, max_iters: int = 0, restart: int = 0, mg_sweeps: int = 0,
                      use_initial_guess: bool = False, method: str = "fgmres", check: bool = True,
-                     learned: bool = False, precision: str = "mixed", gs_relax: float = 0.0) -> dict:
+                     learned: bool = False, precision: str = "mixed", gs_relax: float = 0.0,
+                     fallback: bool = True) -> dict:
         """The Stokes solve (replaces SystemSolver.solve_system_optimized, SystemSolver.jl:67-91);
         method "fgmres" or "bicgstab"; learned: add the trained network's stage after each V-cycle;
         precision "mixed" (FP32 V-cycle and stored directions) or "fp64" (the plain method);
-        gs_relax (mixed only): FP32 Gram-Schmidt below gs_relax x the target (0: 1e3, <0: never)."""
+        gs_relax (mixed only): FP32 Gram-Schmidt below gs_relax x the target (0: 1e3, <0: never);
+        fallback (mixed only): the plain method takes over when the mixed residual stops falling."""
         o = _abi.SolveOpts(rtol, max_iters, restart, mg_sweeps, int(use_initial_guess),
                            {"fgmres": 0, "bicgstab": 1}[method], int(learned), {"mixed": 0, "fp64": 1}[precision],
-                           gs_relax)
+                           gs_relax, 0 if fallback else -1)
         r = _abi.SolveReport()
         rc = self._lib.eb_solve_stokes_system(self._ctx, C.byref(o), C.byref(r))
         rep = {"status": rc, "iterations": r.iterations, "levels": r.levels, "rel_residual": r.rel_residual,
                "rel_residual_scaled": r.rel_residual_scaled, "seconds": r.seconds,
-               "reorthogonalisations": r.reorthogonalisations, "relaxed_iterations": r.relaxed_iterations}
+               "reorthogonalisations": r.reorthogonalisations, "relaxed_iterations": r.relaxed_iterations,
+               "fallback_used": r.fallback_used, "precision_used": ("mixed", "fp64")[r.precision_used]}
         if check:
             self._check(rc)
         return rep

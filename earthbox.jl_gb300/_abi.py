@@ -125,7 +125,7 @@ class StokesParams(C.Structure):
 class SolveOpts(C.Structure):
     _fields_ = [("rtol", C.c_double), ("max_iters", C.c_int32), ("restart", C.c_int32), ("mg_sweeps", C.c_int32),
                 ("use_initial_guess", C.c_int32), ("method", C.c_int32), ("learned", C.c_int32),
-                ("precision", C.c_int32), ("gs_relax", C.c_double)]
+                ("precision", C.c_int32), ("gs_relax", C.c_double), ("fallback", C.c_int32)]
 
 
 class LearnedOpts(C.Structure):
@@ -155,7 +155,7 @@ class MobileWall(C.Structure):
 class SolveReport(C.Structure):
     _fields_ = [("iterations", C.c_int32), ("levels", C.c_int32), ("rel_residual", C.c_double),
                 ("rel_residual_scaled", C.c_double), ("seconds", C.c_double), ("reorthogonalisations", C.c_int32),
-                ("relaxed_iterations", C.c_int32)]
+                ("relaxed_iterations", C.c_int32), ("fallback_used", C.c_int32), ("precision_used", C.c_int32)]
 
 
 STOKES_VECTORS = {"solution": 0, "rhs": 1, "solution_old": 2, "resnl": 3}
@@ -231,6 +231,7 @@ ENTRY_POINTS = [
     "eb_post_stokes_marker_gathers", "eb_update_subgrid_stress", "eb_apply_marker_stress_correction",
     "eb_subgrid_heat_diffusion_update", "eb_add_remaining_grid_change_to_marker_temperature",
     "eb_advect_markers_and_rotate_stress", "eb_update_marker_strain", "eb_correct_advect_and_update_strain",
+    "eb_calc_marker_viscoplastic_viscosity",
 ]
 ALL_SYMBOLS = [
     "eb_create", "eb_destroy", "eb_last_error", "eb_set_grid", "eb_set_materials", "eb_set_params",

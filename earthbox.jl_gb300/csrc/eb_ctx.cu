@@ -691,6 +691,11 @@ extern "C" int eb_post_stokes_marker_gathers(eb_ctx* c) {
   if (rc) return rc;
   return finish(c, launch_post_stokes_gathers(c));
 }
+extern "C" int eb_calc_marker_viscoplastic_viscosity(eb_ctx* c) {
+  int rc = ready(c, false, true);
+  if (rc) return rc;
+  return finish(c, launch_marker_viscoplastic_viscosity(c));
+}
 extern "C" int eb_update_subgrid_stress(eb_ctx* c) {
   int rc = ready(c, true, true);
   if (rc) return rc;

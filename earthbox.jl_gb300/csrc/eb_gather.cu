@@ -80,6 +80,40 @@ __global__ void k_add_dt(DevMarkers mk, DevGrid g, const float* __restrict__ dtk
   mk.tk[m] = mk.tk[m] + f2d(gather4f(dtk1, g.ynum, mk.yn[m], mk.xn[m], mk.fx[m], mk.fy[m]));
 }
 
+// GridViscoplasticityToMarkers.calc_marker_viscoplastic_viscosity!
+// (src/rheology/plastic_failure/nodes/GridViscoplasticityToMarkers.jl:7-118): a marker whose
+// basic cell has a yielding corner takes the harmonic average of etas1 over the yielding
+// corners (weights plastic_yield x bilinear weight, numerator their sum) when that is below
+// its flow viscosity, and is marked as failed; every other inside marker takes its flow
+// viscosity.  Run once per time step of the nodal Picard variant, so it is done in FP64
+// (the comparison with the flow viscosity decides the failure flag).
+__global__ void k_marker_eta_vp(DevMarkers mk, int32_t ynum, const double* __restrict__ plastic_yield,
+                                const double* __restrict__ etas1) {
+  const int64_t m = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= mk.M || !(mk.mflags[m] & MF_INSIDE)) return;
+  const int32_t ix = mk.xn[m], iy = mk.yn[m];
+  const size_t o = (size_t)(ix - 1) * ynum + (iy - 1);
+  const double pul = __ldg(&plastic_yield[o]), pll = __ldg(&plastic_yield[o + 1]);
+  const double pur = __ldg(&plastic_yield[o + ynum]), plr = __ldg(&plastic_yield[o + ynum + 1]);
+  const double vflow = mk.eta_flow[m];
+  if (!(pul > 0.0 || pll > 0.0 || pur > 0.0 || plr > 0.0)) {
+    mk.eta[m] = vflow;
+    return;
+  }
+  const double dx = f2d(mk.fx[m]), dy = f2d(mk.fy[m]);
+  const double wul = (1.0 - dx) * (1.0 - dy), wll = (1.0 - dx) * dy, wur = dx * (1.0 - dy), wlr = dx * dy;
+  const double denom = pul / __ldg(&etas1[o]) * wul + pll / __ldg(&etas1[o + 1]) * wll +
+                       pur / __ldg(&etas1[o + ynum]) * wur + plr / __ldg(&etas1[o + ynum + 1]) * wlr;
+  const double numer = pul * wul + pll * wll + pur * wur + plr * wlr;
+  const double vvp = numer / denom;
+  if (vvp >= vflow) {
+    mk.eta[m] = vflow;
+  } else {
+    mk.eta[m] = vvp;
+    mk.pfailure[m] = 1.0f;
+  }
+}
+
 unsigned mblocks(const eb_ctx* c) { return (unsigned)((c->M + kBlock - 1) / kBlock); }
 
 }  // namespace
@@ -134,6 +168,19 @@ int launch_add_remaining_dt(eb_ctx* c) {
   if ((rc = grid_f32(c, {EB_G_DTK1}, &dtk1))) return rc;
   EB_PROF(c, "k_add_dt");
   k_add_dt<<<mblocks(c), kBlock, 0, c->stream>>>(dev_markers(c), c->g, dtk1);
+  EB_LAUNCHED(c);
+  return EB_OK;
+}
+
+int launch_marker_viscoplastic_viscosity(eb_ctx* c) {
+  int rc;
+  const int mf[] = {EB_M_ETA, EB_M_ETA_FLOW, EB_M_PFAILURE};
+  for (int f : mf) if ((rc = ensure_marker_field(c, f))) return rc;
+  if ((rc = ensure_grid_field(c, EB_G_PLASTIC_YIELD)) || (rc = ensure_grid_field(c, EB_G_ETAS1))) return rc;
+  if (c->M == 0) return EB_OK;
+  EB_PROF(c, "k_marker_eta_vp");
+  k_marker_eta_vp<<<mblocks(c), kBlock, 0, c->stream>>>(dev_markers(c), c->g.ynum, c->gf[EB_G_PLASTIC_YIELD],
+                                                         c->gf[EB_G_ETAS1]);
   EB_LAUNCHED(c);
   return EB_OK;
 }

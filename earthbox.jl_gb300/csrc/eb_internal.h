@@ -239,6 +239,7 @@ int launch_subgrid_stress(eb_ctx* c);
 int launch_subgrid_heat(eb_ctx* c);
 int launch_gather_temperature(eb_ctx* c);
 int launch_post_stokes_gathers(eb_ctx* c);
+int launch_marker_viscoplastic_viscosity(eb_ctx* c);
 int launch_stress_correction(eb_ctx* c);
 int launch_add_remaining_dt(eb_ctx* c);
 int launch_advect(eb_ctx* c);

@@ -25,17 +25,29 @@ namespace {
 
 constexpr int64_t kMaxMarkers = 1 << 19;  // 524,288 markers
 constexpr int64_t kMaxCells = 1 << 17;    // 131,072 basic cells
-// Scratch layout (bytes): per marker key/fx/fy/perm_tmp/perm (5 x 4), per cell
-// count/start/cursor (3 x 4, plus one) and 8 partial sums (8 x 4).
+// Stable LSD radix sort of the markers by cell key: two passes of 9 bits cover keys
+// 0..nc (nc <= 2^17; key nc marks a marker outside the grid), 2048-marker tiles.
+constexpr int kDigitBits = 9;
+constexpr int kDigits = 1 << kDigitBits;
+constexpr int kSortThreads = 256;
+constexpr int kSortItems = 8;
+constexpr int kTile = kSortThreads * kSortItems;
+constexpr int64_t kMaxTiles = (kMaxMarkers + kTile - 1) / kTile;
+// Scratch layout (bytes): per marker key/fx/fy/perm_tmp/perm (5 x 4); per cell count/start
+// (2 x 4, plus one) and 8 partial sums (8 x 4).  The radix sort's second key buffer and its
+// per-tile digit counts live in the partial-sum region, which is written only after the sort.
 constexpr size_t kMarkerBytes = (size_t)kMaxMarkers * 5 * 4;
-constexpr size_t kCellBytes = (size_t)(kMaxCells + 1) * 3 * 4 + (size_t)kMaxCells * 8 * 4;
+constexpr size_t kCellBytes = (size_t)(kMaxCells + 1) * 2 * 4 + (size_t)kMaxCells * 8 * 4;
 constexpr size_t kNoAllocScratchBytes = 16u << 20;
-static_assert(kMarkerBytes + kCellBytes + 1024 <= kNoAllocScratchBytes, "scratch layout exceeds the array");
+static_assert(kMarkerBytes + kCellBytes + 2048 <= kNoAllocScratchBytes, "scratch layout exceeds the array");
+static_assert((size_t)kMaxMarkers * 4 + 256 + (size_t)kDigits * kMaxTiles * 4 + 4 <= (size_t)kMaxCells * 8 * 4,
+              "radix buffers exceed the partial-sum region they share");
 
 static __device__ __align__(256) unsigned char g_scratch[kNoAllocScratchBytes];
 
 struct Scratch {
-  int32_t *key, *perm_tmp, *perm, *count, *start, *cursor;
+  int32_t *key, *perm_tmp, *perm, *count, *start;
+  int32_t *key2, *hist;  // alias `part` (used only before the cell folds)
   float *fx, *fy, *part;
 };
 
@@ -50,8 +62,9 @@ Scratch carve(unsigned char* base) {
   s.perm = (int32_t*)take(kMaxMarkers * 4);
   s.count = (int32_t*)take((kMaxCells + 1) * 4);
   s.start = (int32_t*)take((kMaxCells + 1) * 4);
-  s.cursor = (int32_t*)take((kMaxCells + 1) * 4);
   s.part = (float*)take(kMaxCells * 8 * 4);
+  s.key2 = (int32_t*)s.part;
+  s.hist = (int32_t*)((unsigned char*)s.part + (((size_t)kMaxMarkers * 4 + 255) & ~size_t(255)));
   return s;
 }
 
@@ -66,11 +79,14 @@ __device__ int32_t search(const double* __restrict__ v, int32_t n, double x) {
   return lo;
 }
 
+// Cell key (column-major basic cell, 0-based; nc for a marker outside the grid), offsets and
+// the per-cell marker counts.
 __global__ void k_na_locate(const double* __restrict__ x, const double* __restrict__ y, int32_t M,
                             const double* __restrict__ gx, int32_t xnum, const double* __restrict__ gy, int32_t ynum,
                             Scratch s) {
   const int32_t m = blockIdx.x * blockDim.x + threadIdx.x;
-  int32_t key = -1;
+  const int32_t nc = (xnum - 1) * (ynum - 1);
+  int32_t key = nc;
   if (m < M) {
     const double xm = x[m], ym = y[m];
     const uint64_t kx = dkey(xm), ky = dkey(ym);
@@ -86,11 +102,12 @@ __global__ void k_na_locate(const double* __restrict__ x, const double* __restri
     s.key[m] = key;
   }
   const unsigned peers = __match_any_sync(0xffffffffu, key);
-  if (key >= 0 && (int)(threadIdx.x & 31) == __ffs(peers) - 1) atomicAdd(&s.count[key], __popc(peers));
+  if (key < nc && (int)(threadIdx.x & 31) == __ffs(peers) - 1) atomicAdd(&s.count[key], __popc(peers));
 }
 
-// Exclusive scan of count[0..n) into start[0..n] by one block (n <= kMaxCells + 1).
-__global__ void k_na_scan(Scratch s, int32_t n) {
+// Exclusive scan of in[0..n) into out[0..n] by one block; in and out may be the same array
+// (each thread reads in[i] before it writes out[i], and no other thread reads index i).
+__global__ void k_na_scan(const int32_t* in, int32_t* out, int32_t n) {
   __shared__ int32_t warp_sums[32];
   __shared__ int32_t carry;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
@@ -98,7 +115,7 @@ __global__ void k_na_scan(Scratch s, int32_t n) {
   __syncthreads();
   for (int32_t base = 0; base < n; base += blockDim.x) {
     const int32_t i = base + threadIdx.x;
-    const int32_t v = i < n ? s.count[i] : 0;
+    const int32_t v = i < n ? in[i] : 0;
     int32_t inc = v;
     for (int o = 1; o < 32; o <<= 1) {
       const int32_t t = __shfl_up_sync(0xffffffffu, inc, o);
@@ -116,35 +133,76 @@ __global__ void k_na_scan(Scratch s, int32_t n) {
     }
     __syncthreads();
     const int32_t c0 = carry;
-    if (i < n) s.start[i] = c0 + (wid ? warp_sums[wid - 1] : 0) + inc - v;
+    if (i < n) out[i] = c0 + (wid ? warp_sums[wid - 1] : 0) + inc - v;
     __syncthreads();
     if (threadIdx.x == 0) carry = c0 + warp_sums[nw - 1];
     __syncthreads();
   }
-  if (threadIdx.x == 0) s.start[n] = carry;
+  if (threadIdx.x == 0) out[n] = carry;
 }
 
-__global__ void k_na_place(int32_t M, Scratch s) {
-  const int32_t m = blockIdx.x * blockDim.x + threadIdx.x;
-  const int32_t key = m < M ? s.key[m] : -1;
-  const unsigned peers = __match_any_sync(0xffffffffu, key);
-  const int lane = threadIdx.x & 31, leader = __ffs(peers) - 1;
-  int32_t base = 0;
-  if (key >= 0 && lane == leader) base = atomicAdd(&s.cursor[key], __popc(peers));
-  base = __shfl_sync(0xffffffffu, base, leader);
-  if (key >= 0) s.perm_tmp[s.start[key] + base + __popc(peers & ((1u << lane) - 1u))] = m;
+// Radix pass, step 1: digit counts of one tile of kTile markers, stored digit-major
+// (hist[d * ntiles + tile]) so that one exclusive scan gives every (digit, tile) its offset.
+__global__ void __launch_bounds__(kSortThreads) k_na_digit_count(const int32_t* __restrict__ key, int32_t M,
+                                                                 int shift, int32_t ntiles,
+                                                                 int32_t* __restrict__ hist) {
+  __shared__ int32_t cnt[kDigits];
+  for (int d = threadIdx.x; d < kDigits; d += kSortThreads) cnt[d] = 0;
+  __syncthreads();
+  const int32_t base = blockIdx.x * kTile;
+  for (int r = 0; r < kSortItems; ++r) {
+    const int32_t i = base + r * kSortThreads + threadIdx.x;
+    if (i < M) atomicAdd(&cnt[(key[i] >> shift) & (kDigits - 1)], 1);
+  }
+  __syncthreads();
+  for (int d = threadIdx.x; d < kDigits; d += kSortThreads) hist[(size_t)d * ntiles + blockIdx.x] = cnt[d];
 }
 
-__global__ void k_na_sort(int32_t nc, Scratch s) {
-  const int32_t cell = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int lane = threadIdx.x & 31;
-  if (cell >= nc) return;
-  const int32_t beg = s.start[cell], n = s.start[cell + 1] - beg;
-  for (int32_t i = lane; i < n; i += 32) {
-    const int32_t v = s.perm_tmp[beg + i];
-    int32_t r = 0;
-    for (int32_t j = 0; j < n; ++j) r += (s.perm_tmp[beg + j] < v);
-    s.perm[beg + r] = v;
+// Radix pass, step 2: stable scatter.  A marker's place is its (digit, tile) offset plus the
+// markers of its tile with the same digit that come before it: those of earlier rounds
+// (cnt), of earlier warps of its round (wcnt) and of lower lanes of its warp.  Pass 0 reads
+// the markers in index order (val_in == nullptr: the value is the index itself).
+__global__ void __launch_bounds__(kSortThreads) k_na_digit_scatter(const int32_t* __restrict__ key_in,
+                                                                   const int32_t* __restrict__ val_in, int32_t M,
+                                                                   int shift, int32_t ntiles,
+                                                                   const int32_t* __restrict__ hoff,
+                                                                   int32_t* __restrict__ key_out,
+                                                                   int32_t* __restrict__ val_out) {
+  constexpr int kWarps = kSortThreads / 32;
+  __shared__ int32_t cnt[kDigits];
+  __shared__ int32_t wcnt[kWarps][kDigits];
+  for (int d = threadIdx.x; d < kDigits; d += kSortThreads) {
+    cnt[d] = 0;
+    for (int w = 0; w < kWarps; ++w) wcnt[w][d] = 0;
+  }
+  __syncthreads();
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int32_t base = blockIdx.x * kTile;
+  for (int r = 0; r < kSortItems; ++r) {
+    const int32_t i = base + r * kSortThreads + threadIdx.x;
+    const bool valid = i < M;
+    const int32_t k = valid ? key_in[i] : 0;
+    const int d = valid ? (k >> shift) & (kDigits - 1) : -1;
+    const unsigned peers = __match_any_sync(0xffffffffu, d);
+    if (valid && lane == __ffs(peers) - 1) wcnt[warp][d] = __popc(peers);
+    __syncthreads();
+    if (valid) {
+      int32_t pre = cnt[d];
+      for (int w = 0; w < warp; ++w) pre += wcnt[w][d];
+      const int32_t pos = hoff[(size_t)d * ntiles + blockIdx.x] + pre + __popc(peers & ((1u << lane) - 1u));
+      if (key_out) key_out[pos] = k;
+      val_out[pos] = val_in ? val_in[i] : i;
+    }
+    __syncthreads();
+    for (int dd = threadIdx.x; dd < kDigits; dd += kSortThreads) {
+      int32_t add = 0;
+      for (int w = 0; w < kWarps; ++w) {
+        add += wcnt[w][dd];
+        wcnt[w][dd] = 0;
+      }
+      cnt[dd] += add;
+    }
+    __syncthreads();
   }
 }
 
@@ -226,14 +284,22 @@ extern "C" int eb_marker_to_basic_grid_average_noalloc(const double* d_marker_x,
   cudaStream_t st = (cudaStream_t)stream;
   const int32_t M = (int32_t)marknum, X = (int32_t)xnum, Y = (int32_t)ynum, nc = (X - 1) * (Y - 1);
   // the array keeps the previous call's contents: clear the counters this call accumulates into
-  if (cudaMemsetAsync(s.count, 0, (nc + 1) * sizeof(int32_t), st) != cudaSuccess ||
-      cudaMemsetAsync(s.cursor, 0, (nc + 1) * sizeof(int32_t), st) != cudaSuccess)
+  if (cudaMemsetAsync(s.count, 0, (nc + 1) * sizeof(int32_t), st) != cudaSuccess)
     return fail(EB_CUDA_ERROR, "cudaMemsetAsync failed");
   const unsigned mb = (unsigned)((M + 255) / 256);
   if (M > 0) k_na_locate<<<mb, 256, 0, st>>>(d_marker_x, d_marker_y, M, d_gridx_b, X, d_gridy_b, Y, s);
-  k_na_scan<<<1, 1024, 0, st>>>(s, nc);
-  if (M > 0) k_na_place<<<mb, 256, 0, st>>>(M, s);
-  k_na_sort<<<(unsigned)(((int64_t)nc * 32 + 255) / 256), 256, 0, st>>>(nc, s);
+  k_na_scan<<<1, 1024, 0, st>>>(s.count, s.start, nc);
+  if (M > 0) {
+    // markers ordered by (cell, marker index): two stable passes over the cell key
+    const int32_t ntiles = (M + kTile - 1) / kTile;
+    k_na_digit_count<<<ntiles, kSortThreads, 0, st>>>(s.key, M, 0, ntiles, s.hist);
+    k_na_scan<<<1, 1024, 0, st>>>(s.hist, s.hist, kDigits * ntiles);
+    k_na_digit_scatter<<<ntiles, kSortThreads, 0, st>>>(s.key, nullptr, M, 0, ntiles, s.hist, s.key2, s.perm_tmp);
+    k_na_digit_count<<<ntiles, kSortThreads, 0, st>>>(s.key2, M, kDigitBits, ntiles, s.hist);
+    k_na_scan<<<1, 1024, 0, st>>>(s.hist, s.hist, kDigits * ntiles);
+    k_na_digit_scatter<<<ntiles, kSortThreads, 0, st>>>(s.key2, s.perm_tmp, M, kDigitBits, ntiles, s.hist, nullptr,
+                                                        s.perm);
+  }
   k_na_cells<<<(unsigned)((nc + 255) / 256), 256, 0, st>>>(d_marker_value, nc, s);
   k_na_finish<<<(unsigned)((X * Y + 255) / 256), 256, 0, st>>>(X, Y, s, d_avg, d_wsum);
   const cudaError_t e = cudaGetLastError();

@@ -36,6 +36,9 @@ constexpr double kReorth2 = 0.05 * 0.05;
 // Default residual level (relative to the target) below which the mixed method's
 // Gram-Schmidt runs in FP32 on the basis copies.
 constexpr double kGsRelax = 1e3;
+// The mixed method's FP64 residual "fails to fall" when an FGMRES cycle leaves the true
+// residual above this fraction of its value at the start of the cycle.
+constexpr double kStallFactor = 0.5;
 constexpr int kMaxDots = kMaxRestart + 8;  // dot products per reduction
 
 unsigned nblk(int64_t n) { return (unsigned)((n + kB - 1) / kB); }
@@ -1530,13 +1533,15 @@ static int need_system(eb_ctx* c, bool built) {
   return EB_OK;
 }
 
-extern "C" int eb_solve_stokes_system(eb_ctx* c, const eb_solve_opts* o, eb_solve_report* rep) {
-  int rc = need_system(c, true);
-  if (rc) return rc;
+// One solve with one method.  With `stall_check` (the mixed method when the fallback is on),
+// the solve also stops when the true FP64 residual at the start of an FGMRES cycle is not
+// below kStallFactor times its value at the start of the previous cycle, and reports that
+// as EB_NOT_CONVERGED: the residual has stopped falling.
+static int solve_once(eb_ctx* c, eb_solve_opts opt, bool stall_check, eb_solve_report* rep, bool* input_nan) {
+  int rc;
   const auto t0 = std::chrono::steady_clock::now();
   StokesState* st = c->st;
   StokesSystem& s = st->sys;
-  eb_solve_opts opt = o ? *o : eb_solve_opts{};
   if (opt.rtol <= 0) opt.rtol = 1e-8;
   if (opt.max_iters <= 0) opt.max_iters = 3000;
   if (opt.restart <= 0) opt.restart = 250;
@@ -1564,7 +1569,10 @@ extern "C" int eb_solve_stokes_system(eb_ctx* c, const eb_solve_opts* o, eb_solv
   double bn2;
   if ((rc = mdot(c, st, st->bs, 0, 1, st->bs, &bn2))) return rc;
   const double bnorm = std::sqrt(bn2);
-  if (!std::isfinite(bnorm)) return eb_fail(c, EB_NAN, "right-hand side has NaN/Inf");
+  if (!std::isfinite(bnorm)) {
+    *input_nan = true;
+    return eb_fail(c, EB_NAN, "right-hand side has NaN/Inf");
+  }
   std::vector<double> H((size_t)(m + 1) * m), g(m + 1), cs(m), sn(m), hcol(m + 2), y(m);
   int it = 0, reorth = 0, relaxed = 0;
   double est = 1.0;
@@ -1576,6 +1584,8 @@ extern "C" int eb_solve_stokes_system(eb_ctx* c, const eb_solve_opts* o, eb_solv
   // target is reached but the unscaled residual is still above rtol, the target is tightened
   // by their ratio and the method restarts from the current iterate.
   double target = opt.rtol, rel = 0.0, rel_s = 0.0;
+  double prev_beta = HUGE_VAL;
+  bool stalled = false;
   for (int outer = 0;; ++outer) {
   bool converged = (bnorm == 0.0);
   if (opt.method == 1 && !converged) {
@@ -1639,6 +1649,8 @@ extern "C" int eb_solve_stokes_system(eb_ctx* c, const eb_solve_opts* o, eb_solv
     if (!std::isfinite(beta)) return eb_fail(c, EB_NAN, "FGMRES residual became NaN/Inf");
     est = beta / bnorm;
     if (est <= target) { converged = true; break; }
+    if (stall_check && beta > kStallFactor * prev_beta) { stalled = true; break; }
+    prev_beta = beta;
     EB_PROF(c, "k_axpy");
     k_scale_copy2<<<nblk(n3), kB, 0, c->stream>>>(st->V, V32, st->r, 1.0 / beta, n3);
     EB_LAUNCHED(c);
@@ -1777,7 +1789,7 @@ extern "C" int eb_solve_stokes_system(eb_ctx* c, const eb_solve_opts* o, eb_solv
   rel = RR > 0 ? std::sqrt(rr / RR) : std::sqrt(rr);
   rel_s = bnorm > 0 ? std::sqrt(sr2) / bnorm : std::sqrt(sr2);
   if (!std::isfinite(rel)) break;
-  if (rel <= opt.rtol || it >= opt.max_iters || outer >= 8 || bnorm == 0.0) break;
+  if (stalled || rel <= opt.rtol || it >= opt.max_iters || outer >= 8 || bnorm == 0.0) break;
   target = std::min(target, rel_s) * std::max(0.5 * opt.rtol / rel, 1e-4);
   }  // outer
   prof_resolve(c);
@@ -1789,12 +1801,48 @@ extern "C" int eb_solve_stokes_system(eb_ctx* c, const eb_solve_opts* o, eb_solv
     rep->rel_residual = rel;
     rep->rel_residual_scaled = rel_s;
     rep->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    rep->fallback_used = 0;
+    rep->precision_used = opt.precision;
   }
   if (!std::isfinite(rel)) return eb_fail(c, EB_NAN, "Stokes solution has NaN/Inf");
   if (rel > opt.rtol * 1.0000001)
-    return eb_fail(c, EB_NOT_CONVERGED, "Stokes solve stopped at relative residual " + std::to_string(rel) +
-                                            " after " + std::to_string(it) + " iterations");
+    return eb_fail(c, EB_NOT_CONVERGED, std::string(stalled ? "Stokes residual stopped falling at " :
+                                                              "Stokes solve stopped at relative residual ") +
+                                            std::to_string(rel) + " after " + std::to_string(it) + " iterations");
   return EB_OK;
+}
+
+// The mixed method falls back to the plain FP64 method whenever its FP64 residual fails to
+// fall: when it stops without meeting the tolerance (iteration limit, or a cycle that did not
+// lower the true residual), the plain method continues from its iterate with a budget of
+// max_iters iterations of its own; when it produced NaN/Inf, the plain method starts from
+// zero.  The report then sums both attempts and names the method that finished.
+extern "C" int eb_solve_stokes_system(eb_ctx* c, const eb_solve_opts* o, eb_solve_report* rep) {
+  int rc = need_system(c, true);
+  if (rc) return rc;
+  const eb_solve_opts opt = o ? *o : eb_solve_opts{};
+  const bool fallback = opt.precision == 0 && opt.fallback >= 0;
+  eb_solve_report r1{};
+  bool input_nan = false;
+  rc = solve_once(c, opt, fallback, &r1, &input_nan);
+  if (rep) *rep = r1;
+  if (!fallback || input_nan || (rc != EB_NOT_CONVERGED && rc != EB_NAN)) return rc;
+  eb_solve_opts o2 = opt;
+  o2.precision = 1;
+  o2.learned = 0;
+  o2.use_initial_guess = rc == EB_NAN ? 0 : 1;
+  eb_solve_report r2{};
+  const int rc2 = solve_once(c, o2, false, &r2, &input_nan);
+  if (rep) {
+    *rep = r2;
+    rep->iterations = r1.iterations + r2.iterations;
+    rep->reorthogonalisations = r1.reorthogonalisations + r2.reorthogonalisations;
+    rep->relaxed_iterations = r1.relaxed_iterations;
+    rep->seconds = r1.seconds + r2.seconds;
+    rep->fallback_used = 1;
+    rep->precision_used = 1;
+  }
+  return rc2;
 }
 
 extern "C" int eb_set_stokes_params(eb_ctx* c, const eb_stokes_params* p) {

@@ -248,6 +248,13 @@ int eb_update_plastic_yielding(eb_ctx* ctx);
  * MarkerStrainRateRatio.jl:191-271, MarkerPressure.jl:17-54, fused in one pass. */
 int eb_post_stokes_marker_gathers(eb_ctx* ctx);
 
+/* GridViscoplasticityToMarkers.calc_marker_viscoplastic_viscosity!
+ *   (src/rheology/plastic_failure/nodes/GridViscoplasticityToMarkers.jl:7-118), reached through
+ * StokesContinuitySolver.interpolate_grid_viscoplastic_viscosity_to_markers! (StokesContinuitySolver.jl:256-266)
+ * after the nodal Picard loop (itype_global = 1): plastic_yield and etas1 -> marker_eta, marker_pfailure.
+ * Needs located markers (eb_initialize_bilinear_interpolation). */
+int eb_calc_marker_viscoplastic_viscosity(eb_ctx* ctx);
+
 /* SubGridStress.Update.update_subgrid_stress!  (subgrid_stress/update/Update.jl:69-87) */
 int eb_update_subgrid_stress(eb_ctx* ctx);
 
@@ -307,7 +314,8 @@ typedef struct eb_solve_opts {
                                 iteration runs on the W-scaled system and tightens its own target
                                 until this holds); 0 -> 1e-8                                     */
   int32_t max_iters;         /* FGMRES iterations; 0 -> 3000                                          */
-  int32_t restart;           /* Krylov basis size; 0 -> 40                                             */
+  int32_t restart;           /* Krylov basis size (FGMRES restarts after this many iterations); 0 -> 250;
+                                at most 500 (Stokes; unused by the heat solve)                       */
   int32_t mg_sweeps;         /* red-black Gauss-Seidel sweeps before/after each coarse correction; 0 -> 3 */
   int32_t use_initial_guess; /* 1: start from the current device solution vector, 0: from zero         */
   int32_t method;            /* 0: FGMRES (long recurrence, robust); 1: BiCGStab (short recurrence, two
@@ -320,6 +328,11 @@ typedef struct eb_solve_opts {
   double  gs_relax;          /* mixed method only: once the FGMRES residual estimate is below
                                 gs_relax x the target, Gram-Schmidt projects with FP32 products on
                                 FP32 copies of the basis; 0 -> 1e3, negative -> never (Stokes only) */
+  int32_t fallback;          /* mixed method only: 0 -> the plain FP64 method takes over whenever the
+                                mixed method's FP64 residual fails to fall (an FGMRES cycle that does
+                                not halve the true residual, the iteration limit reached, or NaN/Inf),
+                                continuing from the mixed iterate (from zero after NaN/Inf) with
+                                max_iters iterations of its own; negative -> no fallback (Stokes only) */
 } eb_solve_opts;
 
 typedef struct eb_solve_report {
@@ -330,6 +343,9 @@ typedef struct eb_solve_report {
   double  seconds;           /* wall time of the solve                                  */
   int32_t reorthogonalisations; /* Gram-Schmidt second passes (severe cancellation only) */
   int32_t relaxed_iterations;   /* iterations whose Gram-Schmidt ran in FP32 (gs_relax)  */
+  int32_t fallback_used;     /* 1: the mixed method's residual stopped falling and the plain FP64
+                                method finished the solve (iterations and seconds cover both)  */
+  int32_t precision_used;    /* method that produced S: 0 mixed, 1 plain FP64                  */
 } eb_solve_report;
 
 enum eb_stokes_vector {
@@ -355,8 +371,10 @@ int eb_build_stokes_system(eb_ctx* ctx);
 /* Replaces SystemSolver.solve_system_optimized (SystemSolver.jl:67-91), whose direct
  * sparse solve (MUMPS, ParallelSolver.jl:52-126, or UMFPACK) becomes FGMRES in FP64,
  * preconditioned by a block-triangular split: FP32 geometric multigrid on the velocity
- * block and a viscosity-scaled diagonal on the pressure.  EB_NOT_CONVERGED when the
- * tolerance is not met in max_iters (S then holds the last iterate), EB_NAN on NaN. */
+ * block and a viscosity-scaled diagonal on the pressure.  The mixed method falls back to the
+ * plain FP64 method when its residual stops falling (opts->fallback).  EB_NOT_CONVERGED when
+ * the tolerance is not met (S then holds the last iterate), EB_NAN on NaN/Inf in the
+ * right-hand side or a solution that the fallback could not repair. */
 int eb_solve_stokes_system(eb_ctx* ctx, const eb_solve_opts* opts, eb_solve_report* report);
 
 /* SystemSolver.process_stokes_solution!  (SystemSolver.jl:141-271: reload_solu_vel!, apply_vel_bc!) */
@@ -725,9 +743,14 @@ int eb_marker_cycle_host(eb_ctx* ctx, const eb_marker_io* io);
  * (xnum-1)*(ynum-1) <= EB_NOALLOC_MAX_CELLS, else EB_BAD_INPUT with a message
  * in errbuf.  The first call on a device resolves the array's device address
  * (cudaGetSymbolAddress) with that device current; make that first call
- * before any stream capture.  Work is queued on `stream` (a cudaStream_t, 0 =
+ * before any stream capture.  That address is kept for the life of the
+ * process: after cudaDeviceReset on a device, this entry point must not be
+ * called on it again.  Work is queued on `stream` (a cudaStream_t, 0 =
  * default) without synchronising.  All calls share the one array, so calls
- * that overlap on the GPU (different streams, or another host thread) race.  */
+ * that overlap on the GPU (different streams, or another host thread) race.
+ * Cost is linear in marknum however the markers cluster: they are ordered by
+ * (cell, marker index) with a stable radix sort, and each cell folds its own
+ * markers in that order.  */
 #define EB_NOALLOC_MAX_MARKERS 524288
 #define EB_NOALLOC_MAX_CELLS   131072
 int eb_marker_to_basic_grid_average_noalloc(

@@ -993,3 +993,42 @@ void o_plastic_yielding(int64_t M, const int8_t* flags, int64_t ntimestep, doubl
     if (m_pfailure[m] != 1.0f) m_pfailure[m] = (float)yflag;
   }
 }
+
+/* GridViscoplasticityToMarkers.calc_marker_viscoplastic_viscosity!
+ * (src/rheology/plastic_failure/nodes/GridViscoplasticityToMarkers.jl:7-62), with
+ * check_basic_grid_for_yielding (:64-74) and interpolate_grid_viscosity_to_marker (:76-118,
+ * use_sum_for_numerator = true): markers of a cell with a yielding corner take the
+ * plastic-flag-weighted harmonic average of etas1 when it is below their flow viscosity,
+ * and are then marked as failed.  A serial marker loop, as in the reference. */
+void o_marker_viscoplastic_viscosity_from_grid(int64_t M, const int8_t* flags, int64_t ynum,
+                                               const int32_t* xn, const int32_t* yn, const double* mdx,
+                                               const double* mdy, const double* plastic_yield,
+                                               const double* etas1, const double* m_eta_flow, double* m_eta,
+                                               float* m_pfailure) {
+  for (int64_t m = 0; m < M; ++m) {
+    if (flags[m] != 1) continue;
+    const int32_t ix = xn[m], iy = yn[m];
+    const double pul = plastic_yield[IDX(iy, ix, ynum)], pll = plastic_yield[IDX(iy + 1, ix, ynum)];
+    const double pur = plastic_yield[IDX(iy, ix + 1, ynum)], plr = plastic_yield[IDX(iy + 1, ix + 1, ynum)];
+    const int yielding = pul > 0.0 || pll > 0.0 || pur > 0.0 || plr > 0.0;
+    const double vflow = m_eta_flow[m];
+    if (!yielding) {
+      m_eta[m] = vflow;
+      continue;
+    }
+    const double dx = mdx[m], dy = mdy[m];
+    const double wul = (1.0 - dx) * (1.0 - dy), wll = (1.0 - dx) * dy;
+    const double wur = dx * (1.0 - dy), wlr = dx * dy;
+    const double eul = etas1[IDX(iy, ix, ynum)], ell = etas1[IDX(iy + 1, ix, ynum)];
+    const double eur = etas1[IDX(iy, ix + 1, ynum)], elr = etas1[IDX(iy + 1, ix + 1, ynum)];
+    const double denom = pul / eul * wul + pll / ell * wll + pur / eur * wur + plr / elr * wlr;
+    const double numer = pul * wul + pll * wll + pur * wur + plr * wlr;
+    const double vvp = numer / denom;
+    if (vvp >= vflow) {
+      m_eta[m] = vflow;
+    } else {
+      m_eta[m] = vvp;
+      m_pfailure[m] = 1.0f;
+    }
+  }
+}

@@ -266,6 +266,14 @@ class OracleMIC:
             P(k["cohesion"]), P(k["fric"]), P(k["exx"]), P(k["exy"]), P(k["sr_ratio"]), P(k["pr"]), P(k["sxx"]),
             P(k["sxy"]), P(k["eta"]), P(k["pfailure"]))
 
+    def calc_marker_viscoplastic_viscosity(self):
+        """GridViscoplasticityToMarkers.calc_marker_viscoplastic_viscosity! (plastic_yield, etas1 -> eta)."""
+        k, gr = self.mk, self.gr
+        lib().o_marker_viscoplastic_viscosity_from_grid(
+            I(self.M), P(k["inside"]), I(self.g.ynum), P(k["xn"]), P(k["yn"]), P(k["dx"]), P(k["dy"]),
+            P(np.asfortranarray(gr["plastic_yield"])), P(np.asfortranarray(gr["etas1"])), P(k["eta_flow"]),
+            P(k["eta"]), P(k["pfailure"]))
+
     def marker_cycle(self):
         self.get_marker_inside_flags()
         self.initialize_bilinear_interpolation()

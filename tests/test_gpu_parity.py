@@ -412,3 +412,65 @@ def test_errors_are_reported_not_raised_on_device(eb):
     with pytest.raises(eb.EarthBoxGPUError):
         mic.upload_marker("matid", bad)
     mic.close()
+
+
+def test_grid_viscoplastic_viscosity_to_markers(eb, oracle):
+    """GridViscoplasticityToMarkers.calc_marker_viscoplastic_viscosity!: yielding cells take the
+    plastic-flag-weighted harmonic average of etas1 when it is below the flow viscosity (eta
+    within 1e-6, the failure flags exact); cells without a yielding corner keep eta_flow."""
+    model = eb.synthetic.config("rift_small")
+    Y, X = model.grid.ynum, model.grid.xnum
+    rng = np.random.default_rng(11)
+    model.grids["plastic_yield"] = np.asfortranarray((rng.random((Y, X)) < 0.25).astype(float))
+    model.grids["etas1"] = np.asfortranarray(10.0 ** rng.uniform(19.0, 24.0, (Y, X)))
+    mic, ref = fresh(eb, oracle, model)
+    locate_both(mic, ref)
+    mic.calc_marker_viscoplastic_viscosity()
+    ref.calc_marker_viscoplastic_viscosity()
+    sel = ref.mk["inside"] == 1
+    close(mic.download_marker("eta")[sel], ref.mk["eta"][sel], "eta")
+    pf = mic.download_marker("pfailure")
+    assert np.array_equal(pf, ref.mk["pfailure"])
+    newly = (ref.mk["pfailure"] == 1) & (model.markers["pfailure"] == 0)
+    assert newly.sum() > 100, "the case must make markers fail"
+    keep = sel & (ref.mk["eta"] == ref.mk["eta_flow"])
+    assert keep.sum() > 100
+    mic.close()
+
+
+def topo_model(eb):
+    """rift_small with the topography model on: two extra materials stand for the sticky air
+    (1.2 kg/m^3) and sticky water (1025 kg/m^3) of FlattenDensity, and sea level sits 7 km above
+    the rock surface, so that both the air and the water branch replace node densities."""
+    model = eb.synthetic.config("rift_small")
+    m = model.mats
+    pad = lambda a, v: np.concatenate([a, np.array(v, dtype=a.dtype)])
+    mats = eb.synthetic.Materials(
+        mat_mu=pad(m.mat_mu, [1e20, 1e20]), mat_hr=pad(m.mat_hr, [0.0, 0.0]),
+        mat_flow_type=pad(m.mat_flow_type, [0, 0]),
+        mat_flow=np.asfortranarray(np.vstack([m.mat_flow, np.zeros((2, 12))])),
+        mat_plastic=np.asfortranarray(np.vstack([m.mat_plastic, np.zeros((2, 6))])),
+        mat_rho=pad(m.mat_rho, [1.2, 1025.0]))
+    mats.mat_flow[4:, 0] = 1e18
+    model.mats = mats
+    model.params.update(iuse_topo=1, y_sealevel=3e3, matid_sticky_air_rho=5, matid_sticky_water_rho=6)
+    return model
+
+
+def test_sticky_layer_density_flattening(eb, oracle):
+    """FlattenDensity.flatten_staggered_grid_density_in_sticky_air_layer! (iuse_topo = 1): rho1 and
+    rho1_vy of nodes at or below 1100 kg/m^3 become the sticky-air density above sea level and
+    the sticky-water density below it (rho1 only where hr1 == 0)."""
+    model = topo_model(eb)
+    mic = fresh(eb, oracle, model)[0]
+    steps = ["get_marker_inside_flags", "initialize_bilinear_interpolation",
+             "interpolate_marker_heat_parameters_to_grid", "interpolate_marker_stokes_parameters_to_grid"]
+    for st in steps:
+        getattr(mic, st)()
+    ref, refa = oracle_pair(oracle, model, steps)
+    for f in ("rho1", "rho1_vy"):
+        got = mic.download_grid(f)
+        close(got, ref.gr[f], f, scale=refa.gr[f])
+        assert np.sum(ref.gr[f] == 1.2) >= 50 and np.sum(ref.gr[f] == 1025.0) >= 50, f
+        assert np.array_equal(got == 1.2, ref.gr[f] == 1.2) and np.array_equal(got == 1025.0, ref.gr[f] == 1025.0), f
+    mic.close()
