@@ -488,6 +488,47 @@ class MarkerInCell:
                 break
         return history
 
+    def time_step(self, nglobal: int = 5, tolerance_picard: float = 1e-3, iuse_harmonic: int = 1,
+                  heat: bool = False, **solve_kw) -> dict:
+        """One pass of TimeLoop.run_loop!'s body (src/time_loop/TimeLoop.jl:181-194) restricted to the
+        hot path, with a fixed time step:
+          execute_pre_solver_steps! (:203-230): initialize_bilinear_interpolation!, the heat-parameter
+            averages, update_marker_rheology! + update_marker_viscoplastic_viscosity! (marker
+            plasticity when itype_global == 0; one fused pass), the Stokes-parameter averages and the
+            harmonic normal viscosity;
+          execute_stokes_continuity_solver_steps! (:232-248): the Picard loop of itype_global (markers
+            or nodes), the staggered velocity on basic nodes, the nodal variant's grid viscoplastic
+            viscosity back to the markers, the post-Stokes grid and marker steps, and
+            update_marker_stress_for_grid_and_subgrid_changes! (StokesContinuitySolver.jl:365-381);
+          execute_heat_solver_steps! (:250-259) when `heat`;
+          execute_advection_steps! (:261-273): RK4 advection with stress rotation, strain update;
+          and the inside flags of the moved markers.
+        Returns {"picard": per-iteration records, "heat": heat-loop report or None}."""
+        p = getattr(self, "_params", {})
+        nodes = int(p.get("itype_global", 0)) == 1
+        self.get_marker_inside_flags()
+        self.initialize_bilinear_interpolation()
+        self.interpolate_marker_heat_parameters_to_grid()
+        self.update_marker_rheology_and_viscoplastic_viscosity(use_marker_plasticity=not nodes)
+        self.interpolate_marker_stokes_parameters_to_grid()
+        self.interpolate_basic_viscoplastic_viscosity_to_pressure_grid(iuse_harmonic)
+        loop = self.picard_loop_nodes if nodes else self.picard_loop_markers
+        hist = loop(nglobal, tolerance_picard, iuse_harmonic, **solve_kw)
+        self.interpolate_stag_velocity_to_basic_grid()
+        if nodes:
+            self.calc_marker_viscoplastic_viscosity()
+        self.forecast_viscoelastic_grid_stress()
+        self.calculate_deviatoric_grid_stress_change()
+        self.post_stokes_marker_gathers()
+        if float(p.get("subgrid_diff_coef_stress", 1.0)) > 0:
+            self.update_subgrid_stress()
+        self.apply_marker_stress_correction()
+        hrep = self.update_marker_temp_for_grid_and_subgrid_changes() if heat else None
+        self.advect_markers_and_rotate_stress()
+        self.update_marker_strain()
+        self.get_marker_inside_flags()
+        return {"picard": hist, "heat": hrep}
+
     # ------------------------------------------- learned preconditioner stage --
     def learned_init(self, seed: int = 0) -> None:
         """He-normal initial weights of the U-Net stage."""

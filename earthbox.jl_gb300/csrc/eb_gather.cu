@@ -86,11 +86,15 @@ __global__ void k_add_dt(DevMarkers mk, DevGrid g, const float* __restrict__ dtk
 // corners (weights plastic_yield x bilinear weight, numerator their sum) when that is below
 // its flow viscosity, and is marked as failed; every other inside marker takes its flow
 // viscosity.  Run once per time step of the nodal Picard variant, so it is done in FP64
-// (the comparison with the flow viscosity decides the failure flag).
-__global__ void k_marker_eta_vp(DevMarkers mk, int32_t ynum, const double* __restrict__ plastic_yield,
+// with the reference's normalised distances (MarkerGridMapping.jl:185-219): the harmonic
+// average over corners whose viscosities differ by orders of magnitude amplifies an error in
+// the weight of the weakest corner, and the comparison with the flow viscosity decides the
+// failure flag.
+__global__ void k_marker_eta_vp(DevMarkers mk, DevGrid g, const double* __restrict__ plastic_yield,
                                 const double* __restrict__ etas1) {
   const int64_t m = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (m >= mk.M || !(mk.mflags[m] & MF_INSIDE)) return;
+  const int32_t ynum = g.ynum;
   const int32_t ix = mk.xn[m], iy = mk.yn[m];
   const size_t o = (size_t)(ix - 1) * ynum + (iy - 1);
   const double pul = __ldg(&plastic_yield[o]), pll = __ldg(&plastic_yield[o + 1]);
@@ -100,7 +104,8 @@ __global__ void k_marker_eta_vp(DevMarkers mk, int32_t ynum, const double* __res
     mk.eta[m] = vflow;
     return;
   }
-  const double dx = f2d(mk.fx[m]), dy = f2d(mk.fy[m]);
+  const double dx = (mk.x[m] - __ldg(&g.gx[ix - 1])) / __ldg(&g.sx[ix - 1]);
+  const double dy = (mk.y[m] - __ldg(&g.gy[iy - 1])) / __ldg(&g.sy[iy - 1]);
   const double wul = (1.0 - dx) * (1.0 - dy), wll = (1.0 - dx) * dy, wur = dx * (1.0 - dy), wlr = dx * dy;
   const double denom = pul / __ldg(&etas1[o]) * wul + pll / __ldg(&etas1[o + 1]) * wll +
                        pur / __ldg(&etas1[o + ynum]) * wur + plr / __ldg(&etas1[o + ynum + 1]) * wlr;
@@ -179,7 +184,7 @@ int launch_marker_viscoplastic_viscosity(eb_ctx* c) {
   if ((rc = ensure_grid_field(c, EB_G_PLASTIC_YIELD)) || (rc = ensure_grid_field(c, EB_G_ETAS1))) return rc;
   if (c->M == 0) return EB_OK;
   EB_PROF(c, "k_marker_eta_vp");
-  k_marker_eta_vp<<<mblocks(c), kBlock, 0, c->stream>>>(dev_markers(c), c->g.ynum, c->gf[EB_G_PLASTIC_YIELD],
+  k_marker_eta_vp<<<mblocks(c), kBlock, 0, c->stream>>>(dev_markers(c), c->g, c->gf[EB_G_PLASTIC_YIELD],
                                                          c->gf[EB_G_ETAS1]);
   EB_LAUNCHED(c);
   return EB_OK;

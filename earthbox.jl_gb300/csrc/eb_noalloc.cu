@@ -13,9 +13,9 @@
 // It computes one inclusive bilinear average on the basic grid, the operation
 // of BilinearNumerator (update_weight_inclusive!) + BilinearAverage
 // (calc_bilinear_average_arithmetic!) for a field such as density or
-// temperature, deterministically: markers are grouped by cell with their
-// marker order kept, each cell folds its markers in that order, and nodes sum
-// their four cells in a fixed order.
+// temperature, in FP64 and deterministically: markers are grouped by cell with
+// their marker order kept, each cell folds its markers in that order, and nodes
+// sum their four cells in a fixed order.
 #include <cstdio>
 #include <cstring>
 #include <mutex>
@@ -33,14 +33,14 @@ constexpr int kSortThreads = 256;
 constexpr int kSortItems = 8;
 constexpr int kTile = kSortThreads * kSortItems;
 constexpr int64_t kMaxTiles = (kMaxMarkers + kTile - 1) / kTile;
-// Scratch layout (bytes): per marker key/fx/fy/perm_tmp/perm (5 x 4); per cell count/start
-// (2 x 4, plus one) and 8 partial sums (8 x 4).  The radix sort's second key buffer and its
+// Scratch layout (bytes): per marker key/perm_tmp/perm (3 x 4); per cell count/start (2 x 4,
+// plus one) and 8 FP64 partial sums (8 x 8).  The radix sort's second key buffer and its
 // per-tile digit counts live in the partial-sum region, which is written only after the sort.
-constexpr size_t kMarkerBytes = (size_t)kMaxMarkers * 5 * 4;
-constexpr size_t kCellBytes = (size_t)(kMaxCells + 1) * 2 * 4 + (size_t)kMaxCells * 8 * 4;
+constexpr size_t kMarkerBytes = (size_t)kMaxMarkers * 3 * 4;
+constexpr size_t kCellBytes = (size_t)(kMaxCells + 1) * 2 * 4 + (size_t)kMaxCells * 8 * 8;
 constexpr size_t kNoAllocScratchBytes = 16u << 20;
 static_assert(kMarkerBytes + kCellBytes + 2048 <= kNoAllocScratchBytes, "scratch layout exceeds the array");
-static_assert((size_t)kMaxMarkers * 4 + 256 + (size_t)kDigits * kMaxTiles * 4 + 4 <= (size_t)kMaxCells * 8 * 4,
+static_assert((size_t)kMaxMarkers * 4 + 256 + (size_t)kDigits * kMaxTiles * 4 + 4 <= (size_t)kMaxCells * 8 * 8,
               "radix buffers exceed the partial-sum region they share");
 
 static __device__ __align__(256) unsigned char g_scratch[kNoAllocScratchBytes];
@@ -48,7 +48,7 @@ static __device__ __align__(256) unsigned char g_scratch[kNoAllocScratchBytes];
 struct Scratch {
   int32_t *key, *perm_tmp, *perm, *count, *start;
   int32_t *key2, *hist;  // alias `part` (used only before the cell folds)
-  float *fx, *fy, *part;
+  double* part;
 };
 
 Scratch carve(unsigned char* base) {
@@ -56,13 +56,11 @@ Scratch carve(unsigned char* base) {
   size_t o = 0;
   auto take = [&](size_t bytes) { unsigned char* p = base + o; o += (bytes + 255) & ~size_t(255); return p; };
   s.key = (int32_t*)take(kMaxMarkers * 4);
-  s.fx = (float*)take(kMaxMarkers * 4);
-  s.fy = (float*)take(kMaxMarkers * 4);
   s.perm_tmp = (int32_t*)take(kMaxMarkers * 4);
   s.perm = (int32_t*)take(kMaxMarkers * 4);
   s.count = (int32_t*)take((kMaxCells + 1) * 4);
   s.start = (int32_t*)take((kMaxCells + 1) * 4);
-  s.part = (float*)take(kMaxCells * 8 * 4);
+  s.part = (double*)take(kMaxCells * 8 * 8);
   s.key2 = (int32_t*)s.part;
   s.hist = (int32_t*)((unsigned char*)s.part + (((size_t)kMaxMarkers * 4 + 255) & ~size_t(255)));
   return s;
@@ -79,8 +77,8 @@ __device__ int32_t search(const double* __restrict__ v, int32_t n, double x) {
   return lo;
 }
 
-// Cell key (column-major basic cell, 0-based; nc for a marker outside the grid), offsets and
-// the per-cell marker counts.
+// Cell key (column-major basic cell, 0-based; nc for a marker outside the grid) and the
+// per-cell marker counts.
 __global__ void k_na_locate(const double* __restrict__ x, const double* __restrict__ y, int32_t M,
                             const double* __restrict__ gx, int32_t xnum, const double* __restrict__ gy, int32_t ynum,
                             Scratch s) {
@@ -94,9 +92,6 @@ __global__ void k_na_locate(const double* __restrict__ x, const double* __restri
     if (in) {
       const int32_t ix = clamp_i(search(gx, xnum, xm), 1, xnum - 1);
       const int32_t iy = clamp_i(search(gy, ynum, ym), 1, ynum - 1);
-      const double x0 = gx[ix - 1], y0 = gy[iy - 1];
-      s.fx[m] = (float)((xm - x0) / (gx[ix] - x0));
-      s.fy[m] = (float)((ym - y0) / (gy[iy] - y0));
       key = (ix - 1) * (ynum - 1) + (iy - 1);
     }
     s.key[m] = key;
@@ -206,21 +201,27 @@ __global__ void __launch_bounds__(kSortThreads) k_na_digit_scatter(const int32_t
   }
 }
 
-// One thread per cell: fold the cell's markers in marker order into the four
-// corners' w*value and w sums.
-__global__ void k_na_cells(const double* __restrict__ value, int32_t nc, Scratch s) {
+// One thread per cell: fold the cell's markers in marker order into the four corners'
+// w*value and w sums.  Offsets and weights are the reference's FP64 expressions
+// (MarkerGridMapping.jl:185-219, MarkerGridNodeWeights.jl:68-101): a marker within an FP32
+// rounding of the far grid line still gives that node its (tiny) weight, as in the reference.
+__global__ void k_na_cells(const double* __restrict__ x, const double* __restrict__ y,
+                           const double* __restrict__ value, const double* __restrict__ gx,
+                           const double* __restrict__ gy, int32_t ynum, int32_t nc, Scratch s) {
   const int32_t cell = blockIdx.x * blockDim.x + threadIdx.x;
   if (cell >= nc) return;
-  KSum a[8];
-  for (int k = 0; k < 8; ++k) a[k].init();
+  const int32_t ix = cell / (ynum - 1) + 1, iy = cell % (ynum - 1) + 1;
+  const double x0 = gx[ix - 1], hx = gx[ix] - x0, y0 = gy[iy - 1], hy = gy[iy] - y0;
+  double a[8] = {0, 0, 0, 0, 0, 0, 0, 0};
   for (int32_t k = s.start[cell]; k < s.start[cell + 1]; ++k) {
     const int32_t m = s.perm[k];
-    const W4 w = wts(s.fx[m], s.fy[m]);
-    const float v = (float)value[m];
-    a[0].add(w.ul * v); a[1].add(w.ll * v); a[2].add(w.ur * v); a[3].add(w.lr * v);
-    a[4].add(w.ul); a[5].add(w.ll); a[6].add(w.ur); a[7].add(w.lr);
+    const double dx = (x[m] - x0) / hx, dy = (y[m] - y0) / hy;
+    const double wul = (1.0 - dx) * (1.0 - dy), wll = (1.0 - dx) * dy, wur = dx * (1.0 - dy), wlr = dx * dy;
+    const double v = value[m];
+    a[0] += wul * v; a[1] += wll * v; a[2] += wur * v; a[3] += wlr * v;
+    a[4] += wul; a[5] += wll; a[6] += wur; a[7] += wlr;
   }
-  for (int k = 0; k < 8; ++k) s.part[(size_t)k * nc + cell] = a[k].get();
+  for (int k = 0; k < 8; ++k) s.part[(size_t)k * nc + cell] = a[k];
 }
 
 // Node (i, j) is UL of cell (i, j), LL of (i-1, j), UR of (i, j-1), LR of (i-1, j-1).
@@ -229,21 +230,18 @@ __global__ void k_na_finish(int32_t xnum, int32_t ynum, Scratch s, double* __res
   const int32_t t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= xnum * ynum) return;
   const int32_t i = t % ynum + 1, j = t / ynum + 1, nc = (xnum - 1) * (ynum - 1);
-  KSum num, den;
-  num.init();
-  den.init();
+  double n = 0.0, d = 0.0;
   auto add = [&](int32_t ci, int32_t cj, int corner) {
     const int32_t c = (cj - 1) * (ynum - 1) + (ci - 1);
-    num.add(s.part[(size_t)corner * nc + c]);
-    den.add(s.part[(size_t)(4 + corner) * nc + c]);
+    n += s.part[(size_t)corner * nc + c];
+    d += s.part[(size_t)(4 + corner) * nc + c];
   };
   if (i > 1 && j > 1) add(i - 1, j - 1, 3);
   if (i < ynum && j > 1) add(i, j - 1, 2);
   if (i > 1 && j < xnum) add(i - 1, j, 1);
   if (i < ynum && j < xnum) add(i, j, 0);
-  const float n = num.get(), d = den.get();
-  wsum[t] = (double)d;
-  if (d != 0.f) avg[t] = (double)(n / d);  // else: keep the caller's previous value (the backup)
+  wsum[t] = d;
+  if (d != 0.0) avg[t] = n / d;  // else: keep the caller's previous value (the backup)
 }
 
 std::mutex g_mutex;
@@ -300,7 +298,8 @@ extern "C" int eb_marker_to_basic_grid_average_noalloc(const double* d_marker_x,
     k_na_digit_scatter<<<ntiles, kSortThreads, 0, st>>>(s.key2, s.perm_tmp, M, kDigitBits, ntiles, s.hist, nullptr,
                                                         s.perm);
   }
-  k_na_cells<<<(unsigned)((nc + 255) / 256), 256, 0, st>>>(d_marker_value, nc, s);
+  k_na_cells<<<(unsigned)((nc + 255) / 256), 256, 0, st>>>(d_marker_x, d_marker_y, d_marker_value, d_gridx_b,
+                                                          d_gridy_b, Y, nc, s);
   k_na_finish<<<(unsigned)((X * Y + 255) / 256), 256, 0, st>>>(X, Y, s, d_avg, d_wsum);
   const cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return fail(EB_CUDA_ERROR, cudaGetErrorString(e));

@@ -129,3 +129,43 @@ def test_direct_solve_of_marker_model(eb, S_mod):
     o.stokes_steps()
     S = o.solve_direct()
     assert o.residual(S) < 1e-12
+
+
+def test_solution_sensitivity_to_averaging_precision(eb):
+    """How far the Stokes solution moves when its averaged input grids move by 1e-6 relative.
+
+    The GPU's marker->grid averages agree with the oracle's within 1e-6 (FP32 weights and sums),
+    so this sets how closely anything computed from a GPU velocity field can follow the oracle
+    through a Picard loop or a time step (tests/test_gpu_picard.py, tests/test_gpu_rift_2p5M.py).
+    On the weak-crust rift after one time step (1e18 Pa s sticky air over up to 1e26 Pa s rock),
+    random perturbations of 1e-6 move the oracle's own direct solution by well over 1e-6 of
+    max|v| (about 2-6e-5), and by less than the 1e-4 those tests allow."""
+    import test_gpu_picard as tp
+    from oracle.picard import OraclePicard
+    from oracle.stokes import StokesOracle
+    model = tp.weak_rift(eb, 0)
+    op = OraclePicard(model)
+    op.time_step(6, 1e-3)
+    m = op.mic
+    for st in ("get_marker_inside_flags", "initialize_bilinear_interpolation",
+               "interpolate_marker_heat_parameters_to_grid", "update_marker_rheology"):
+        getattr(m, st)()
+    m.update_marker_viscoplastic_viscosity(True)
+    m.interpolate_marker_stokes_parameters_to_grid()
+    base = {k: v.copy(order="F") for k, v in op.gr.items()}
+
+    def solve(gr):
+        so = StokesOracle(model, gr)
+        so.stokes_steps()
+        return so.solve_direct()
+
+    S0 = solve(base)
+    rng = np.random.default_rng(0)
+    moves = []
+    for _ in range(2):
+        g = {k: v.copy(order="F") for k, v in base.items()}
+        for k in ("etas1", "etan1", "rho1", "rho1_vy", "mus1", "mun1", "sxy1", "sxx1"):
+            g[k] = np.asfortranarray(g[k] * (1 + 1e-6 * rng.uniform(-1, 1, g[k].shape)))
+        S = solve(g)
+        moves.append(max(np.abs(S[c::3] - S0[c::3]).max() / np.abs(S0[c::3]).max() for c in (0, 1)))
+    assert 5e-6 < max(moves) < 1e-4, moves
