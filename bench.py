@@ -318,7 +318,7 @@ def stokes_leg(eb, model, local, args, rank, world):
            "mixed_speedup": p_dt / m_dt}
     # Krylov-basis product roofline of the mixed solve (its HBM-bound kernels)
     kern = {k: (t / n, n) for k, (t, n) in prof.items()}
-    its, m = m_rep["iterations"], 250
+    its, m = m_rep["iterations"], 500   # FGMRES restart length (the solver default)
     ks = [k for c0 in range(0, its, m) for k in range(min(m, its - c0))]
     n_rel = m_rep["relaxed_iterations"]
     ks64, ks32 = ks[:len(ks) - n_rel], ks[len(ks) - n_rel:]

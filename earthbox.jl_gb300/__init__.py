@@ -303,21 +303,24 @@ class MarkerInCell:
     def solve_system(self, rtol: float = 1e-8, max_iters: int = 0, restart: int = 0, mg_sweeps: int = 0,
                      use_initial_guess: bool = False, method: str = "fgmres", check: bool = True,
                      learned: bool = False, precision: str = "mixed", gs_relax: float = 0.0,
-                     fallback: bool = True) -> dict:
+                     fallback: bool = True, mg_inner: int = 0, mg_inner_tol: float = 0.0) -> dict:
         """The Stokes solve (replaces SystemSolver.solve_system_optimized, SystemSolver.jl:67-91);
         method "fgmres" or "bicgstab"; learned: add the trained network's stage after each V-cycle;
         precision "mixed" (FP32 V-cycle and stored directions) or "fp64" (the plain method);
         gs_relax (mixed only): FP32 Gram-Schmidt below gs_relax x the target (0: 1e3, <0: never);
-        fallback (mixed only): the plain method takes over when the mixed residual stops falling."""
+        fallback (mixed only): the plain method takes over when the mixed residual stops falling;
+        mg_inner: the velocity stage's GCR steps (1: a single V-cycle), mg_inner_tol its stopping
+        residual reduction."""
         o = _abi.SolveOpts(rtol, max_iters, restart, mg_sweeps, int(use_initial_guess),
                            {"fgmres": 0, "bicgstab": 1}[method], int(learned), {"mixed": 0, "fp64": 1}[precision],
-                           gs_relax, 0 if fallback else -1)
+                           gs_relax, 0 if fallback else -1, mg_inner, mg_inner_tol)
         r = _abi.SolveReport()
         rc = self._lib.eb_solve_stokes_system(self._ctx, C.byref(o), C.byref(r))
         rep = {"status": rc, "iterations": r.iterations, "levels": r.levels, "rel_residual": r.rel_residual,
                "rel_residual_scaled": r.rel_residual_scaled, "seconds": r.seconds,
                "reorthogonalisations": r.reorthogonalisations, "relaxed_iterations": r.relaxed_iterations,
-               "fallback_used": r.fallback_used, "precision_used": ("mixed", "fp64")[r.precision_used]}
+               "fallback_used": r.fallback_used, "precision_used": ("mixed", "fp64")[r.precision_used],
+               "vcycles": r.vcycles}
         if check:
             self._check(rc)
         return rep

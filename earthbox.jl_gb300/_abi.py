@@ -125,7 +125,8 @@ class StokesParams(C.Structure):
 class SolveOpts(C.Structure):
     _fields_ = [("rtol", C.c_double), ("max_iters", C.c_int32), ("restart", C.c_int32), ("mg_sweeps", C.c_int32),
                 ("use_initial_guess", C.c_int32), ("method", C.c_int32), ("learned", C.c_int32),
-                ("precision", C.c_int32), ("gs_relax", C.c_double), ("fallback", C.c_int32)]
+                ("precision", C.c_int32), ("gs_relax", C.c_double), ("fallback", C.c_int32),
+                ("mg_inner", C.c_int32), ("mg_inner_tol", C.c_double)]
 
 
 class LearnedOpts(C.Structure):
@@ -155,7 +156,8 @@ class MobileWall(C.Structure):
 class SolveReport(C.Structure):
     _fields_ = [("iterations", C.c_int32), ("levels", C.c_int32), ("rel_residual", C.c_double),
                 ("rel_residual_scaled", C.c_double), ("seconds", C.c_double), ("reorthogonalisations", C.c_int32),
-                ("relaxed_iterations", C.c_int32), ("fallback_used", C.c_int32), ("precision_used", C.c_int32)]
+                ("relaxed_iterations", C.c_int32), ("fallback_used", C.c_int32), ("precision_used", C.c_int32),
+                ("vcycles", C.c_int64)]
 
 
 STOKES_VECTORS = {"solution": 0, "rhs": 1, "solution_old": 2, "resnl": 3}

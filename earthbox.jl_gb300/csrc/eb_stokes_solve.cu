@@ -39,6 +39,10 @@ constexpr double kGsRelax = 1e3;
 // The mixed method's FP64 residual "fails to fall" when an FGMRES cycle leaves the true
 // residual above this fraction of its value at the start of the cycle.
 constexpr double kStallFactor = 0.5;
+// Velocity stage of the block preconditioner: GCR steps (each one V-cycle) at most, and the
+// velocity residual reduction at which they stop.
+constexpr int kGcrDefaultSteps = 1;
+constexpr double kGcrDefaultTol = 0.1;
 constexpr int kMaxDots = kMaxRestart + 8;  // dot products per reduction
 
 unsigned nblk(int64_t n) { return (unsigned)((n + kB - 1) / kB); }
@@ -554,7 +558,9 @@ __global__ void k_to_real(const double* __restrict__ a, T* __restrict__ b, int64
   const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (k < n) b[k] = (T)a[k];
 }
-// Arithmetic averages of the finer level's viscosity onto this level.
+// Arithmetic averages of the finer level's viscosity onto this level.  (Geometric and harmonic
+// averages, for the node or the cell viscosity or both, all needed more FGMRES iterations on the
+// rift's systems, or failed to converge.)
 template <class T>
 __global__ void k_coarsen_eta(const T* __restrict__ es_f, const T* __restrict__ en_f, int32_t nxf, int32_t nyf,
                               T* __restrict__ es_c, T* __restrict__ en_c, int32_t nxc, int32_t nyc,
@@ -826,6 +832,68 @@ __global__ void k_add_round(double* __restrict__ zt, float* __restrict__ Zk, con
   zt[k] = (double)v;
 }
 
+// ------------------------------------- velocity-block GCR (inner solve) ---
+// The velocity stage of the block preconditioner can run a few steps of GCR on the velocity
+// block A_uu (the unscaled level-0 stencil), each step preconditioned by one V-cycle: the
+// residual-minimising combination of the V-cycle corrections removes the few error modes that
+// the multigrid alone handles poorly (thin low-viscosity layers at sharp viscosity jumps that
+// coarse levels cannot represent).  Vectors are [ux | uy] (2 nc values, level arithmetic T).
+constexpr int kGcrMax = 8;
+
+struct GcrPtrs { const void* v[kGcrMax + 2]; };
+struct GcrCoef { double beta[kGcrMax]; double inv, alpha; int nprev; };
+
+// q = A_uu z on level 0
+template <class T>
+__global__ void k_vel_apply(LevelDev<T> v, const T* __restrict__ z, T* __restrict__ q) {
+  const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= v.nc) return;
+  const int32_t j = (int32_t)c / v.ny, i = (int32_t)c - j * v.ny;
+  q[c] = rowx(v.X, z, z + v.nc, c, i, j, v.nx, v.ny, v.nc, false);
+  q[v.nc + c] = rowy(v.Y, z, z + v.nc, c, i, j, v.nx, v.ny, v.nc, false);
+}
+// partial[w][block] = sum over the block's elements of a . b_w / |diag A_uu| (FP64 accumulation).
+// The inner product weights each row by the inverse of its diagonal, as the outer iteration's
+// symmetric scaling does: unweighted, the stiff rows (1e23 Pa s rock) would hide the residual of
+// the soft ones (1e18 Pa s sticky air) by five orders of magnitude.
+template <class T>
+__global__ void __launch_bounds__(kB) k_gcr_dots(LevelDev<T> v, const T* __restrict__ a, GcrPtrs b, int64_t n,
+                                                 double* __restrict__ partial) {
+  const T* bw = static_cast<const T*>(b.v[blockIdx.y]);
+  double s = 0.0;
+  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
+    const double d = k < v.nc ? (double)v.X[k] : (double)v.Y[k - v.nc];
+    s += (double)a[k] * (double)bw[k] / fabs(d);
+  }
+  __shared__ double sh[kB];
+  sh[threadIdx.x] = s;
+  __syncthreads();
+  for (int o = kB / 2; o > 0; o >>= 1) {
+    if ((int)threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) partial[(int64_t)blockIdx.y * gridDim.x + blockIdx.x] = sh[0];
+}
+// zk = (zk - sum_j beta_j z_j) inv, qk likewise (orthonormal against the earlier q_j);
+// u += alpha zk, r -= alpha qk
+template <class T>
+__global__ void k_gcr_update(T* __restrict__ zk, T* __restrict__ qk, GcrPtrs zp, GcrPtrs qp, GcrCoef cf,
+                             T* __restrict__ u, T* __restrict__ r, int64_t n) {
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  double z = zk[k], q = qk[k];
+  for (int j = 0; j < cf.nprev; ++j) {
+    z -= cf.beta[j] * (double)static_cast<const T*>(zp.v[j])[k];
+    q -= cf.beta[j] * (double)static_cast<const T*>(qp.v[j])[k];
+  }
+  z *= cf.inv;
+  q *= cf.inv;
+  zk[k] = (T)z;
+  qk[k] = (T)q;
+  u[k] = (T)((double)u[k] + cf.alpha * z);
+  r[k] = (T)((double)r[k] - cf.alpha * q);
+}
+
 // ------------------------------------------------------ host geometry ---
 std::vector<int32_t> coarse_nodes(int32_t n_cells) {
   const int32_t M = n_cells / 2;
@@ -947,6 +1015,7 @@ struct Hierarchy {
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t gexec = nullptr;
   int64_t graph_kernels = 0;
+  void* gcr = nullptr;               // velocity GCR vectors: r, u, z[kGcrMax], q[kGcrMax]
 };
 
 struct StokesState {
@@ -972,6 +1041,9 @@ struct StokesState {
   double* il = nullptr;              // interleaved staging vector (N)
   double* tmp = nullptr;             // scratch vector (N)
   double *nn_t = nullptr, *nn_q = nullptr, *nn_z = nullptr;  // learned-stage scratch: [t | q], z2
+  int gcr_steps = 1;                 // velocity stage: 1 V-cycle, or up to this many GCR steps
+  double gcr_tol = 0.1;              // ... until the velocity residual falls below this fraction
+  int64_t gcr_total = 0;             // GCR steps run in the current solve
 };
 
 namespace {
@@ -1003,6 +1075,7 @@ int upload_real(eb_ctx* c, std::vector<void*>& owner, void** p, const std::vecto
 }
 
 void free_levels(StokesState* st) {
+  st->H().gcr = nullptr;  // one of level_allocs
   for (void* p : st->H().level_allocs) cudaFree(p);
   st->H().level_allocs.clear();
   st->H().levels.clear();
@@ -1336,6 +1409,97 @@ int capture_vcycle(eb_ctx* c, StokesState* st, int sweeps) {
   return EB_OK;
 }
 
+// Velocity stage by GCR: the level-0 right-hand side (fx, fy) in, the solution (ux, uy) out.
+// Each step runs the captured V-cycle on the current residual, applies A_uu to the correction,
+// orthonormalises it against the earlier steps' products (one fused reduction, Pythagorean
+// norm) and moves the solution and the residual along it.  Stops after gcr_steps steps, or when
+// |r| <= gcr_tol |f| (|r| follows from the same reduction), or when a correction adds nothing.
+template <class T>
+int velocity_gcr(eb_ctx* c, StokesState* st) {
+  Hierarchy& H = st->H();
+  Level& L0 = H.levels[0];
+  const LevelDev<T> v = level_dev<T>(L0);
+  const int64_t nc = v.nc, n = 2 * nc;
+  const int K = std::min(st->gcr_steps, kGcrMax);
+  int rc;
+  if (!H.gcr && (rc = dalloc_bytes(c, H.level_allocs, &H.gcr, (size_t)(2 + 2 * kGcrMax) * n * sizeof(T)))) return rc;
+  T* R = static_cast<T*>(H.gcr);
+  T* U = R + n;
+  auto Zs = [&](int k) { return U + n + (size_t)k * n; };
+  auto Qs = [&](int k) { return U + n + (size_t)(kGcrMax + k) * n; };
+  const size_t hb = nc * sizeof(T);
+  EB_CK(c, cudaMemcpyAsync(R, L0.fx, hb, cudaMemcpyDeviceToDevice, c->stream));
+  EB_CK(c, cudaMemcpyAsync(R + nc, L0.fy, hb, cudaMemcpyDeviceToDevice, c->stream));
+  EB_CK(c, cudaMemsetAsync(U, 0, n * sizeof(T), c->stream));
+  double rr0 = 0.0, rr = 0.0;
+  int done = 0;
+  for (int k = 0; k < K; ++k) {
+    if (k > 0) {
+      EB_CK(c, cudaMemcpyAsync(L0.fx, R, hb, cudaMemcpyDeviceToDevice, c->stream));
+      EB_CK(c, cudaMemcpyAsync(L0.fy, R + nc, hb, cudaMemcpyDeviceToDevice, c->stream));
+    }
+    EB_PROF(c, "vcycle_graph");
+    EB_CK(c, cudaGraphLaunch(H.gexec, c->stream));
+    c->launches += H.graph_kernels - 1;
+    EB_LAUNCHED(c);
+    EB_CK(c, cudaMemcpyAsync(Zs(k), L0.ux, hb, cudaMemcpyDeviceToDevice, c->stream));
+    EB_CK(c, cudaMemcpyAsync(Zs(k) + nc, L0.uy, hb, cudaMemcpyDeviceToDevice, c->stream));
+    EB_PROF(c, "k_vel_apply");
+    k_vel_apply<T><<<nblk(nc), kB, 0, c->stream>>>(v, Zs(k), Qs(k));
+    EB_LAUNCHED(c);
+    // dots: q_k.q_j (j < k), q_k.q_k, q_k.r, and r.r at the first step
+    GcrPtrs b{};
+    int nv = 0;
+    for (int j = 0; j < k; ++j) b.v[nv++] = Qs(j);
+    b.v[nv++] = Qs(k);
+    b.v[nv++] = R;
+    EB_PROF(c, "k_gcr_dots");
+    k_gcr_dots<T><<<dim3(st->nb_dot, nv), kB, 0, c->stream>>>(v, Qs(k), b, n, st->partial);
+    EB_LAUNCHED(c);
+    int nall = nv;
+    if (k == 0) {
+      GcrPtrs br{};
+      br.v[0] = R;
+      k_gcr_dots<T><<<dim3(st->nb_dot, 1), kB, 0, c->stream>>>(v, R, br, n, st->partial + (size_t)nv * st->nb_dot);
+      EB_LAUNCHED(c);
+      ++nall;
+    }
+    k_mdot_final<<<nall, kB, 0, c->stream>>>(st->partial, st->nb_dot, st->dots);
+    EB_LAUNCHED(c);
+    double h[kGcrMax + 3];
+    EB_CK(c, cudaMemcpyAsync(h, st->dots, nall * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    EB_CK(c, cudaStreamSynchronize(c->stream));
+    if (k == 0) rr0 = rr = h[nv];
+    double qq = h[k];
+    GcrCoef cf{};
+    cf.nprev = k;
+    for (int j = 0; j < k; ++j) {
+      cf.beta[j] = h[j];
+      qq -= h[j] * h[j];
+    }
+    if (!(qq > 1e-12 * h[k]) || !std::isfinite(qq) || !(rr0 > 0.0)) break;
+    const double nrm = std::sqrt(qq);
+    cf.inv = 1.0 / nrm;
+    cf.alpha = h[k + 1] / nrm;
+    EB_PROF(c, "k_gcr_update");
+    k_gcr_update<T><<<nblk(n), kB, 0, c->stream>>>(Zs(k), Qs(k), GcrPtrs{{Zs(0), Zs(1), Zs(2), Zs(3), Zs(4), Zs(5),
+                                                                         Zs(6), Zs(7)}},
+                                                   GcrPtrs{{Qs(0), Qs(1), Qs(2), Qs(3), Qs(4), Qs(5), Qs(6), Qs(7)}},
+                                                   cf, U, R, n);
+    EB_LAUNCHED(c);
+    ++done;
+    ++st->gcr_total;
+    rr -= cf.alpha * cf.alpha;
+    if (rr <= st->gcr_tol * st->gcr_tol * rr0) break;
+  }
+  if (done == 0) {  // no usable step: the V-cycle's correction as it is
+    EB_CK(c, cudaMemcpyAsync(U, Zs(0), n * sizeof(T), cudaMemcpyDeviceToDevice, c->stream));
+  }
+  EB_CK(c, cudaMemcpyAsync(L0.ux, U, hb, cudaMemcpyDeviceToDevice, c->stream));
+  EB_CK(c, cudaMemcpyAsync(L0.uy, U + nc, hb, cudaMemcpyDeviceToDevice, c->stream));
+  return EB_OK;
+}
+
 // zhat = W^-1 M^-1 W^-1 rhat (rhat: SoA FP64 of 3 nc), kept in Zk (the stored direction:
 // FP32 in the mixed method, FP64 in the plain one) and zt (its FP64 value, the input of the
 // operator product).
@@ -1350,10 +1514,15 @@ int precondition(eb_ctx* c, StokesState* st, const double* rhat, double* zt, voi
     k_prec_in<float><<<nblk(s.nc), kB, 0, c->stream>>>(s.coef, rhat, st->winv, st->prep, zt, Zk,
                                                        static_cast<float*>(v.fx), static_cast<float*>(v.fy), s.nx, s.ny);
   EB_LAUNCHED(c);
-  EB_PROF(c, "vcycle_graph");
-  EB_CK(c, cudaGraphLaunch(st->H().gexec, c->stream));
-  c->launches += st->H().graph_kernels - 1;
-  EB_LAUNCHED(c);
+  if (st->gcr_steps > 1) {
+    const int rc = st->mg64 ? velocity_gcr<double>(c, st) : velocity_gcr<float>(c, st);
+    if (rc) return rc;
+  } else {
+    EB_PROF(c, "vcycle_graph");
+    EB_CK(c, cudaGraphLaunch(st->H().gexec, c->stream));
+    c->launches += st->H().graph_kernels - 1;
+    EB_LAUNCHED(c);
+  }
   EB_PROF(c, "k_precond");
   if (st->mg64)
     k_prec_out<double><<<nblk(s.nc), kB, 0, c->stream>>>(static_cast<double*>(v.ux), static_cast<double*>(v.uy), st->winv,
@@ -1544,8 +1713,11 @@ static int solve_once(eb_ctx* c, eb_solve_opts opt, bool stall_check, eb_solve_r
   StokesSystem& s = st->sys;
   if (opt.rtol <= 0) opt.rtol = 1e-8;
   if (opt.max_iters <= 0) opt.max_iters = 3000;
-  if (opt.restart <= 0) opt.restart = 250;
+  if (opt.restart <= 0) opt.restart = kMaxRestart;
   if (opt.mg_sweeps <= 0) opt.mg_sweeps = 3;
+  st->gcr_steps = opt.mg_inner <= 0 ? kGcrDefaultSteps : std::min(opt.mg_inner, kGcrMax);
+  st->gcr_tol = opt.mg_inner_tol > 0.0 ? opt.mg_inner_tol : kGcrDefaultTol;
+  st->gcr_total = 0;
   if (opt.method != 1) opt.method = 0;
   const int m = std::max(std::min(opt.restart, kMaxRestart), opt.method == 1 ? 6 : 1);
   const int64_t n3 = 3 * s.nc;
@@ -1803,6 +1975,7 @@ static int solve_once(eb_ctx* c, eb_solve_opts opt, bool stall_check, eb_solve_r
     rep->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     rep->fallback_used = 0;
     rep->precision_used = opt.precision;
+    rep->vcycles = st->gcr_steps > 1 ? st->gcr_total : it;
   }
   if (!std::isfinite(rel)) return eb_fail(c, EB_NAN, "Stokes solution has NaN/Inf");
   if (rel > opt.rtol * 1.0000001)
@@ -1841,6 +2014,7 @@ extern "C" int eb_solve_stokes_system(eb_ctx* c, const eb_solve_opts* o, eb_solv
     rep->seconds = r1.seconds + r2.seconds;
     rep->fallback_used = 1;
     rep->precision_used = 1;
+    rep->vcycles = r1.vcycles + r2.vcycles;
   }
   return rc2;
 }

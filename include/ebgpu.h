@@ -314,8 +314,9 @@ typedef struct eb_solve_opts {
                                 iteration runs on the W-scaled system and tightens its own target
                                 until this holds); 0 -> 1e-8                                     */
   int32_t max_iters;         /* FGMRES iterations; 0 -> 3000                                          */
-  int32_t restart;           /* Krylov basis size (FGMRES restarts after this many iterations); 0 -> 250;
-                                at most 500 (Stokes; unused by the heat solve)                       */
+  int32_t restart;           /* Krylov basis size (FGMRES restarts after this many iterations); 0 -> 500,
+                                the most allowed (Stokes; unused by the heat solve): restarting after
+                                250 stalled on systems that converge within 550 unrestarted          */
   int32_t mg_sweeps;         /* red-black Gauss-Seidel sweeps before/after each coarse correction; 0 -> 3 */
   int32_t use_initial_guess; /* 1: start from the current device solution vector, 0: from zero         */
   int32_t method;            /* 0: FGMRES (long recurrence, robust); 1: BiCGStab (short recurrence, two
@@ -333,6 +334,11 @@ typedef struct eb_solve_opts {
                                 not halve the true residual, the iteration limit reached, or NaN/Inf),
                                 continuing from the mixed iterate (from zero after NaN/Inf) with
                                 max_iters iterations of its own; negative -> no fallback (Stokes only) */
+  int32_t mg_inner;          /* velocity stage of the preconditioner: 1 -> one V-cycle; k > 1 -> up to k
+                                steps of GCR on the velocity block, each preconditioned by one V-cycle,
+                                until the velocity residual falls below mg_inner_tol of its start
+                                (at most 8); 0 -> 1 (Stokes only)                                    */
+  double  mg_inner_tol;      /* 0 -> 0.1 */
 } eb_solve_opts;
 
 typedef struct eb_solve_report {
@@ -346,6 +352,7 @@ typedef struct eb_solve_report {
   int32_t fallback_used;     /* 1: the mixed method's residual stopped falling and the plain FP64
                                 method finished the solve (iterations and seconds cover both)  */
   int32_t precision_used;    /* method that produced S: 0 mixed, 1 plain FP64                  */
+  int64_t vcycles;           /* V-cycles run (one per iteration, or the GCR steps of mg_inner) */
 } eb_solve_report;
 
 enum eb_stokes_vector {
