@@ -9,9 +9,11 @@
 //   ViscoplasticViscosity.update_marker_viscoplastic_viscosity!  viscoplastic_viscosity/ViscoplasticViscosity.jl:21-60
 //   ViscoelasticForecast.update_plastic_yielding!            plastic_failure/markers/update/types/ViscoelasticForecast.jl:11-181
 //   YieldStress / FluidPressure / Limits / YieldCheck / CheckYield   plastic_failure/utils/*.jl, markers/update/utils/*.jl
-// These kernels run in FP64 end to end: the bisection's stopping test
-// (|dsigma| <= 1 Pa) and its branch decisions must follow the reference's
-// FP64 path to keep the flow viscosity within tolerance.
+// The arithmetic is FP64 where results are formed: the bisection's stopping test
+// (|dsigma| <= 1 Pa), its midpoints and its final viscosity follow the reference's FP64
+// path.  Its branch decisions come from the root of the decision function, found once per
+// marker (FP32 search, two FP64 Newton steps), with the reference's FP64 test wherever a
+// midpoint lies too close to that root to decide by comparison.
 #include "eb_internal.h"
 
 namespace {
@@ -117,6 +119,131 @@ struct RheoParams {
   int soft;
 };
 
+// ---- root-guided bisection --------------------------------------------------------------
+// Each step of the reference's bisection (CompositeViscosity.jl:133-284) asks on which side of
+// the visco-elastic forecast the midpoint savg lies.  With a = savg / 2 (the reference's
+// 0.5 (s_mpa 1e6)) and D = mu dt rate(savg) + a, the forecast exceeds savg exactly when
+//   phi(savg) = 2 mu dt rate(savg) + savg - |c| < 0,   c = 2 srr mu dt (exx, exy) + (sxx, sxy),
+// and phi increases with the stress (every creep rate does), so every decision is "savg below
+// the root s* of phi".  s* is found once: a bracketed search on log(s) in FP32, then two FP64
+// Newton steps on phi.  The bisection then runs with its exact FP64 midpoints, deciding each
+// step by comparing the midpoint's bit pattern with s*'s (both positive, so integer order is
+// numeric order); a midpoint within kBandUlps of s* (relative 3e-11, far above the ~1e-15 of
+// either evaluation) takes the reference's own FP64 test.  The decisions, the step count and
+// the final midpoint are therefore those of the plain FP64 loop, with one FP64 creep-rate
+// evaluation at the end instead of one per step.  A marker whose Newton steps do not settle
+// (a kink of max(dislocation, Peierls) at the root) runs the plain loop.
+constexpr int64_t kBandUlps = 1 << 17;
+
+struct FlowLaw {
+  CreepRow r;
+  double A, p_mpa, T, R, inv_sp, e_disl, a_p, e_diff;
+};
+
+__device__ __forceinline__ double rate_at(const FlowLaw& f, double s_mpa) {
+  double ed = f.e_disl, ap = f.a_p, ef = f.e_diff;
+  return creep_rate(f.r, f.p_mpa, f.T, f.R, f.A, s_mpa, true, f.inv_sp, ed, ap, ef);
+}
+
+// rate and d rate / d s (s in Pa) of the reference's composite law at s
+__device__ double rate_and_slope(const FlowLaw& f, double s, double& slope) {
+  const double s_mpa = s * kPaToMPa;
+  const double inv_s = 1.0 / s;
+  const double rd = f.A * f.e_disl * ((f.r.n_disl == 1.0) ? s_mpa : jl_pow(s_mpa, f.r.n_disl));
+  const double drd = f.r.n_disl * rd * inv_s;
+  double rp = 0.0, drp = 0.0;
+  if (f.r.A_p > 0.0 && f.T < 1200.0) {
+    const double ratio = s_mpa * f.inv_sp;
+    const double rm = (f.r.m_p == 1.0) ? ratio : jl_pow(ratio, f.r.m_p);
+    const double tm = 1.0 - rm;
+    const double inner = (f.r.n_p == 2.0) ? tm * tm : jl_pow(tm, f.r.n_p);
+    rp = f.r.A_p * exp(-f.a_p * inner) * (s_mpa * s_mpa);
+    const double tpow = (f.r.n_p == 2.0) ? tm : jl_pow(tm, f.r.n_p - 1.0);
+    drp = rp * (2.0 + f.a_p * f.r.n_p * tpow * f.r.m_p * rm) * inv_s;
+  }
+  double rf = 0.0, drf = 0.0;
+  if (f.r.A_diff > 0.0) {
+    rf = f.r.A_diff * f.e_diff * s_mpa;
+    drf = rf * inv_s;
+  }
+  slope = ((rd > rp) ? drd : drp) + drf;
+  return ((rd > rp) ? rd : rp) + rf;
+}
+
+// psi(u) = log(2 mdt rate(e^u)) - log(|c| - e^u) in FP32 (increasing in u); +inf past |c|
+struct LogLaw {
+  float ld, lp, lf, n, a_p, m_p, n_p, inv_sp, l2mdt, cabs;
+  bool peierls, diff;
+  __device__ float psi(float u) const {
+    const float e = __expf(u);
+    if (!(e < cabs)) return INFINITY;
+    const float lsm = u - 13.815510558f;  // log(s_mpa) = log(s) - log(1e6)
+    float L = ld + n * lsm;
+    if (peierls) {
+      const float ratio = __expf(lsm) * inv_sp;
+      const float rm = (m_p == 1.f) ? ratio : __powf(ratio, m_p);
+      const float tm = 1.f - rm;
+      const float inner = (n_p == 2.f) ? tm * tm : __powf(tm, n_p);
+      L = fmaxf(L, lp - a_p * inner + 2.f * lsm);
+    }
+    if (diff) {
+      const float lrf = lf + lsm;
+      const float hi = fmaxf(L, lrf), lo = fminf(L, lrf);
+      L = hi + log1pf(__expf(lo - hi));
+    }
+    return l2mdt + L - __logf(cabs - e);
+  }
+};
+
+// The root s* of phi (see above); false when the Newton steps do not settle.  Roots far
+// outside [lo, hi] (every midpoint on one side by a wide margin) return 0 or +inf.
+__device__ bool flow_root(const FlowLaw& f, double mdt, double cabs, double lo, double hi, double& sstar) {
+  if (!(cabs > 0.0)) {  // phi > 0 everywhere: every midpoint lies above the root
+    sstar = 0.0;
+    return true;
+  }
+  LogLaw g;
+  g.ld = __logf((float)f.A) - (float)((f.r.Ea_disl * 1000.0 + f.r.Va_disl * f.p_mpa) * (1.0 / (f.R * f.T)));
+  g.n = (float)f.r.n_disl;
+  g.peierls = f.r.A_p > 0.0 && f.T < 1200.0;
+  g.lp = g.peierls ? __logf((float)f.r.A_p) : 0.f;
+  g.a_p = (float)f.a_p;
+  g.m_p = (float)f.r.m_p;
+  g.n_p = (float)f.r.n_p;
+  g.inv_sp = (float)f.inv_sp;
+  g.diff = f.r.A_diff > 0.0;
+  g.lf = g.diff ? __logf((float)f.r.A_diff) -
+                      (float)((f.r.Ea_diff * 1000.0 + f.r.Va_diff * f.p_mpa) * (1.0 / (f.R * f.T)))
+                : 0.f;
+  g.l2mdt = __logf((float)(2.0 * mdt));
+  g.cabs = (float)cabs;
+  // The shortcuts below trust psi's sign only where |c| - s does not cancel in FP32 (s at
+  // least 1 % below |c|; at or above |c|, phi > 0 holds exactly).
+  constexpr float kMargin = 1e-3f;  // far above the FP32 evaluation error of psi there
+  float ul = __logf((float)lo), uh = __logf((float)hi);
+  const float pl = g.psi(ul), ph = g.psi(uh);
+  if (lo >= cabs || (lo < 0.99 * cabs && pl > kMargin)) { sstar = 0.0; return true; }  // root well below lo
+  if (hi < 0.99 * cabs && ph < -kMargin) { sstar = INFINITY; return true; }           // ... well above hi
+  ul -= 1e-3f;
+  uh = fminf(uh + 1e-3f, __logf(g.cabs) - 1e-6f);
+  if (!(g.psi(ul) <= 0.f)) ul -= 0.1f;
+  for (int k = 0; k < 26; ++k) {
+    const float um = 0.5f * (ul + uh);
+    if (g.psi(um) > 0.f) uh = um; else ul = um;
+  }
+  double s = (double)__expf(0.5f * (ul + uh));
+  double step = 0.0;
+  for (int k = 0; k < 2; ++k) {
+    double slope;
+    const double rate = rate_and_slope(f, s, slope);
+    const double phi = 2.0 * mdt * rate + s - cabs;
+    step = phi / (2.0 * mdt * slope + 1.0);
+    s -= step;
+  }
+  sstar = s;
+  return isfinite(s) && s > 0.0 && fabs(step) <= 1e-9 * s;
+}
+
 __device__ __forceinline__ void d_flow_viscosity(const DevMarkers& mk, const DevMats& mt, const RheoParams& P, int64_t m) {
   const int32_t id = mk.matid[m];
   const int32_t ft = __ldg(&mt.flow_type[id - 1]);
@@ -162,7 +289,38 @@ __device__ __forceinline__ void d_flow_viscosity(const DevMarkers& mk, const Dev
     const double mdt = mu * P.dt;
     const double cxx = 2.0 * srr * mdt * exx + sxx, cxy = 2.0 * srr * mdt * exy + sxy;
     const double cc = cxx * cxx + cxy * cxy;
-    while (icount < 20 && delta > 1.0) {
+    FlowLaw fl{r, A, p_mpa, T, P.R, inv_sp, e_disl, a_p, e_diff};
+    double sstar;
+    if (flow_root(fl, mdt, sqrt(cc), fmin(s0, sf), fmax(s0, sf), sstar)) {
+      const int64_t kr = __double_as_longlong(sstar);
+      double savg = s0;
+      while (icount < 20 && delta > 1.0) {
+        ++icount;
+        savg = (s0 + sf) / 2.0;
+        const int64_t dist = __double_as_longlong(savg) - kr;
+        bool above, below;
+        if (dist > kBandUlps) {
+          above = false;
+          below = P.s_min < savg;
+        } else if (dist < -kBandUlps) {
+          above = true;
+          below = false;
+        } else {  // within the band: the reference's own test
+          s_mpa = savg * kPaToMPa;
+          rate = rate_at(fl, s_mpa);
+          const double a = 0.5 * (s_mpa * 1e6);
+          const double d = mdt * rate + a;
+          const double lhs = (a * a) * cc, rhs = (savg * savg) * (d * d);
+          above = lhs > rhs;
+          below = lhs < rhs && P.s_min < savg;
+        }
+        if ((sf > s0 && above) || (sf < s0 && below)) s0 = savg;
+        else sf = savg;
+        delta = fabs(sf - s0);
+      }
+      s_mpa = savg * kPaToMPa;
+      rate = rate_at(fl, s_mpa);
+    } else while (icount < 20 && delta > 1.0) {
       ++icount;
       const double savg = (s0 + sf) / 2.0;
       s_mpa = savg * kPaToMPa;

@@ -342,6 +342,36 @@ def test_rheology(eb, oracle):
     mic.close()
 
 
+@pytest.mark.parametrize("name", ["rift_small", "rift_2p5M"])
+def test_flow_viscosity_bisection_follows_the_reference(eb, oracle, name):
+    """CompositeViscosity.update_marker_flow_viscosity!: the GPU decides each bisection step from
+    the root of the decision function and evaluates the creep law only at the last midpoint; the
+    decisions, the step count and that midpoint must be the reference's, so eta_flow agrees with
+    the oracle's plain FP64 bisection to 1e-11: the last bits of exp and pow differ between CUDA and
+    the host's C library (up to ~1.5e-12 here), while one different decision or step would move it
+    by at least the final half-interval over the stress, 1e-9 or more.  Checked on the markers as
+    generated and after they took the strain rates and pressures of a real Stokes solution."""
+    model = eb.synthetic.config(name)
+    for stage in ("initial", "after one time step"):
+        mic, ref = fresh(eb, oracle, model)
+        for o in (mic, ref):
+            o.get_marker_inside_flags()
+            o.update_marker_rheology()
+        sel = ref.mk["inside"] == 1
+        got, want = mic.download_marker("eta_flow")[sel], ref.mk["eta_flow"][sel]
+        rel = np.abs(got - want) / want
+        print(f"{name} {stage}: worst relative eta_flow error {rel.max():.3g}; oracle bisection steps "
+              f"{np.bincount(ref.iters[sel])}")
+        assert np.all(rel <= 1e-11), (stage, int(np.sum(rel > 1e-11)), rel.max())
+        assert np.array_equal(mic.download_marker("preexp"), ref.mk["preexp"])
+        if stage == "initial":
+            mic.time_step(3, 1e-3, rtol=1e-10)
+            model = model.copy()
+            for f in ("x", "y", "sxx", "sxy", "exx", "exy", "pr", "sr_ratio", "gii", "strain_plastic", "tk", "eta"):
+                model.markers[f] = mic.download_marker(f)
+        mic.close()
+
+
 def test_full_marker_cycle(eb, oracle, pair):
     model, _, _ = pair
     mic = fresh(eb, oracle, model)[0]
