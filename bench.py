@@ -363,19 +363,35 @@ def stokes_leg(eb, model, local, args, rank, world):
     return out
 
 
-def run_time_steps(eb, model, local, nsteps: int, precision: str, heat: bool, nglobal: int = 5):
-    """`nsteps` hot-path time steps (MarkerInCell.time_step) of a fresh context, wall-timed."""
+def run_time_steps(eb, model, local, nsteps: int, precision: str, heat: bool, nglobal: int = 5,
+                   learned_steps: int = 0):
+    """`nsteps` hot-path time steps (MarkerInCell.time_step, every solve warm-started) of a fresh
+    context, wall-timed.  With learned_steps > 0 the learned stage is first trained (untimed) on the
+    model's first Stokes system and then used inside FGMRES and as the warm start of every solve."""
     import torch
-    mic = fresh_context(eb, model, local)
+    mic = fresh_context(eb, model, local) if not learned_steps else stokes_state(eb, model, local)
+    extra, train = {}, None
+    if learned_steps:
+        mic.learned_init(17)
+        train = mic.learned_train(steps=learned_steps, batch=4, patch=512, patches_per_sample=4, lr=1e-3, seed=23)
+        extra = {"learned": True, "learned_warm": True}
+        mic.learned_stats()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     recs = []
     for _ in range(nsteps):
-        recs.append(mic.time_step(nglobal, 1e-3, heat=heat, rtol=1e-8, precision=precision, check=False))
+        recs.append(mic.time_step(nglobal, 1e-3, heat=heat, rtol=1e-8, precision=precision, check=False, **extra))
     torch.cuda.synchronize()
     dt = (time.perf_counter() - t0) / nsteps
+    st = mic.learned_stats() if learned_steps else None
     mic.close()
     pic = [r["picard"] for r in recs]
+    if learned_steps:
+        return {"s_per_step": dt, "picard_iterations": [len(p) for p in pic],
+                "fgmres_iterations": [[h["iterations"] for h in p] for p in pic],
+                "solve_s": sum(h["seconds"] for p in pic for h in p) / nsteps,
+                "status_ok": all(h["status"] == 0 for p in pic for h in p),
+                "training_s": train["seconds"], "stage_kept": st["accepted"], "stage_rejected": st["rejected"]}
     return {"s_per_step": dt, "picard_iterations": [len(p) for p in pic],
             "fgmres_iterations": [[h["iterations"] for h in p] for p in pic],
             "solve_s": sum(h["seconds"] for p in pic for h in p) / nsteps,
@@ -384,18 +400,25 @@ def run_time_steps(eb, model, local, nsteps: int, precision: str, heat: bool, ng
             "status_ok": all(h["status"] == 0 for p in pic for h in p)}
 
 
-def timestep_leg(eb, model, local, nsteps: int, heat: bool, workload: str):
+def timestep_leg(eb, model, local, nsteps: int, heat: bool, workload: str, learned_steps: int = 0):
     """Whole hot-path time steps, the mixed method against the plain FP64 method, each on a
     freshly loaded copy of the model (one untimed warm-up step per method first)."""
     out = {"metric": "per-timestep wall time", "unit": "s/step", "higher_is_better": False, "workload": workload,
            "steps": nsteps,
            "includes": "rheology (one fused pass), marker->grid averages, Picard loop (nglobal 5, tol 1e-3) of "
-                       "Stokes solves to 1e-8, post-Stokes grid/marker steps, subgrid stress"
+                       "warm-started Stokes solves to 1e-8, post-Stokes grid/marker steps, subgrid stress"
                        + (", heat step" if heat else "") + ", RK4 advection, strain"}
     for prec in ("mixed", "fp64"):   # the context keeps its own copy of the model: `model` is not changed
         run_time_steps(eb, model, local, 1, prec, heat)          # warm-up (set-up, graph capture)
         out["mixed" if prec == "mixed" else "plain_fp64"] = run_time_steps(eb, model, local, nsteps, prec, heat)
     out["speedup_vs_plain_fp64"] = out["plain_fp64"]["s_per_step"] / out["mixed"]["s_per_step"]
+    if learned_steps:
+        try:
+            ml = run_time_steps(eb, model, local, nsteps, "mixed", heat, learned_steps=learned_steps)
+            ml["speedup_vs_plain_fp64"] = out["plain_fp64"]["s_per_step"] / ml["s_per_step"]
+            out["mixed_learned"] = ml
+        except Exception as exc:  # reported, not required
+            out["mixed_learned"] = {"s_per_step": None, "error": str(exc)[:200]}
     return out
 
 
@@ -634,7 +657,8 @@ def main():
     timestep = None
     if not args.no_stokes and not args.no_timestep:
         timestep = timestep_leg(eb, model, local, args.timesteps, heat=not args.no_heat,
-                                workload=f"{args.workload} (time steps 1-{args.timesteps} from the initial state)")
+                                workload=f"{args.workload} (time steps 1-{args.timesteps} from the initial state)",
+                                learned_steps=0 if args.no_learned else args.learned_steps)
     config2 = None
     if not args.no_stokes and not args.no_config2:
         m2 = eb.synthetic.config("rift_2p5M", seed=100 + rank)

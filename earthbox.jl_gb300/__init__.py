@@ -303,17 +303,19 @@ class MarkerInCell:
     def solve_system(self, rtol: float = 1e-8, max_iters: int = 0, restart: int = 0, mg_sweeps: int = 0,
                      use_initial_guess: bool = False, method: str = "fgmres", check: bool = True,
                      learned: bool = False, precision: str = "mixed", gs_relax: float = 0.0,
-                     fallback: bool = True, mg_inner: int = 0, mg_inner_tol: float = 0.0) -> dict:
+                     fallback: bool = True, mg_inner: int = 0, mg_inner_tol: float = 0.0,
+                     learned_warm: bool = False) -> dict:
         """The Stokes solve (replaces SystemSolver.solve_system_optimized, SystemSolver.jl:67-91);
         method "fgmres" or "bicgstab"; learned: add the trained network's stage after each V-cycle;
         precision "mixed" (FP32 V-cycle and stored directions) or "fp64" (the plain method);
         gs_relax (mixed only): FP32 Gram-Schmidt below gs_relax x the target (0: 1e3, <0: never);
         fallback (mixed only): the plain method takes over when the mixed residual stops falling;
         mg_inner: the velocity stage's GCR steps (1: a single V-cycle), mg_inner_tol its stopping
-        residual reduction."""
+        residual reduction; learned_warm (with learned and use_initial_guess): the learned stage
+        also corrects the initial guess."""
         o = _abi.SolveOpts(rtol, max_iters, restart, mg_sweeps, int(use_initial_guess),
                            {"fgmres": 0, "bicgstab": 1}[method], int(learned), {"mixed": 0, "fp64": 1}[precision],
-                           gs_relax, 0 if fallback else -1, mg_inner, mg_inner_tol)
+                           gs_relax, 0 if fallback else -1, mg_inner, mg_inner_tol, int(learned_warm))
         r = _abi.SolveReport()
         rc = self._lib.eb_solve_stokes_system(self._ctx, C.byref(o), C.byref(r))
         rep = {"status": rc, "iterations": r.iterations, "levels": r.levels, "rel_residual": r.rel_residual,
@@ -424,16 +426,30 @@ class MarkerInCell:
         """The etas1 / plastic_yield / plastic strain-rate updates of PlasticityLoopNodes.picard_loop."""
         self._call("eb_apply_nodal_plastic_yielding")
 
+    @staticmethod
+    def _warm_kw(solve_kw: dict, warm: bool) -> dict:
+        """Solve options starting from the current solution vector when `warm` (an explicit
+        use_initial_guess in solve_kw wins)."""
+        kw = dict(solve_kw)
+        if warm:
+            kw.setdefault("use_initial_guess", True)
+        return kw
+
     def picard_loop_nodes(self, nglobal: int, tolerance_picard: float, iuse_harmonic: int = 1,
-                          wall: dict | None = None, **solve_kw) -> list:
+                          wall: dict | None = None, warm_start: bool = True, warm_first: bool = False,
+                          **solve_kw) -> list:
         """PlasticityLoopNodes.picard_loop (plasticity_loop_nodes/PlasticityLoopNodes.jl:36-92): solve,
         process, nodal yield, apply it when nodes yield; stop when no node yields, at nglobal, or when
-        the yield error or dvxy_rel_L2 drops below the tolerance (check_stop_global_loop_nodes)."""
+        the yield error or dvxy_rel_L2 drops below the tolerance (check_stop_global_loop_nodes).
+        warm_start: each solve after the first starts from the previous iterate (the reference's
+        direct solve needs no start; the iterative one reaches the same residual tolerance in fewer
+        iterations); warm_first: the first one too (from the solution the context holds)."""
         history = []
         for iglobal in range(1, nglobal + 1):
             if iglobal > 1:
                 self.interpolate_basic_viscoplastic_viscosity_to_pressure_grid(iuse_harmonic)
-            rep = self.solve_viscoelastic_stokes_continuity_equations(**solve_kw)
+            rep = self.solve_viscoelastic_stokes_continuity_equations(
+                **self._warm_kw(solve_kw, warm_start and (iglobal > 1 or warm_first)))
             norms = self.stokes_solution_processing()
             nnode, gerr = self.update_nodes_for_plastic_yielding(wall)
             if nnode > 0:
@@ -471,11 +487,12 @@ class MarkerInCell:
         return norms
 
     def picard_loop_markers(self, nglobal: int, tolerance_picard: float, iuse_harmonic: int = 1,
-                            **solve_kw) -> list:
+                            warm_start: bool = True, warm_first: bool = False, **solve_kw) -> list:
         """PlasticityLoopMarkers.picard_loop (global_plasticity_loop/plasticity_loop/
         plasticity_loop_markers/PlasticityLoopMarkers.jl:36-73): from the second iteration on,
         re-yield the markers and re-average the viscosity; solve; process; stop at nglobal or when
         dvxy_rel_L2 < tolerance_picard (LoopTermination.check_stop_global_loop_markers).
+        warm_start / warm_first as in picard_loop_nodes.
         Returns one record per iteration (solve report and norms)."""
         history = []
         for iglobal in range(1, nglobal + 1):
@@ -484,7 +501,8 @@ class MarkerInCell:
                 self.update_plastic_yielding()
                 self.interpolate_viscosity_to_transport_arrays()
                 self.interpolate_basic_viscoplastic_viscosity_to_pressure_grid(iuse_harmonic)
-            rep = self.solve_viscoelastic_stokes_continuity_equations(**solve_kw)
+            rep = self.solve_viscoelastic_stokes_continuity_equations(
+                **self._warm_kw(solve_kw, warm_start and (iglobal > 1 or warm_first)))
             norms = self.stokes_solution_processing()
             history.append({"iglobal": iglobal, **rep, **norms})
             if iglobal == nglobal or norms["dvxy_rel_L2"] < tolerance_picard:
@@ -492,7 +510,7 @@ class MarkerInCell:
         return history
 
     def time_step(self, nglobal: int = 5, tolerance_picard: float = 1e-3, iuse_harmonic: int = 1,
-                  heat: bool = False, **solve_kw) -> dict:
+                  heat: bool = False, warm_start: bool = True, **solve_kw) -> dict:
         """One pass of TimeLoop.run_loop!'s body (src/time_loop/TimeLoop.jl:181-194) restricted to the
         hot path, with a fixed time step:
           execute_pre_solver_steps! (:203-230): initialize_bilinear_interpolation!, the heat-parameter
@@ -506,6 +524,8 @@ class MarkerInCell:
           execute_heat_solver_steps! (:250-259) when `heat`;
           execute_advection_steps! (:261-273): RK4 advection with stress rotation, strain update;
           and the inside flags of the moved markers.
+        warm_start: every Stokes solve starts from the latest solution (the previous Picard iterate,
+        or the previous time step's solution for the first solve of a step).
         Returns {"picard": per-iteration records, "heat": heat-loop report or None}."""
         p = getattr(self, "_params", {})
         nodes = int(p.get("itype_global", 0)) == 1
@@ -516,7 +536,9 @@ class MarkerInCell:
         self.interpolate_marker_stokes_parameters_to_grid()
         self.interpolate_basic_viscoplastic_viscosity_to_pressure_grid(iuse_harmonic)
         loop = self.picard_loop_nodes if nodes else self.picard_loop_markers
-        hist = loop(nglobal, tolerance_picard, iuse_harmonic, **solve_kw)
+        hist = loop(nglobal, tolerance_picard, iuse_harmonic, warm_start=warm_start,
+                    warm_first=warm_start and getattr(self, "_solved", False), **solve_kw)
+        self._solved = True
         self.interpolate_stag_velocity_to_basic_grid()
         if nodes:
             self.calc_marker_viscoplastic_viscosity()

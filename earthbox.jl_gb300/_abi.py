@@ -126,7 +126,7 @@ class SolveOpts(C.Structure):
     _fields_ = [("rtol", C.c_double), ("max_iters", C.c_int32), ("restart", C.c_int32), ("mg_sweeps", C.c_int32),
                 ("use_initial_guess", C.c_int32), ("method", C.c_int32), ("learned", C.c_int32),
                 ("precision", C.c_int32), ("gs_relax", C.c_double), ("fallback", C.c_int32),
-                ("mg_inner", C.c_int32), ("mg_inner_tol", C.c_double)]
+                ("mg_inner", C.c_int32), ("mg_inner_tol", C.c_double), ("learned_warm", C.c_int32)]
 
 
 class LearnedOpts(C.Structure):

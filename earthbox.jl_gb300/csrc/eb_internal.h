@@ -166,6 +166,7 @@ struct StokesSystem {
   double* S_old = nullptr; // [3][nc]
   double* resnl = nullptr; // [3][nc]
   double pscale = 0.0;
+  double S_pscale = 0.0;   // pscale of the system S was solved for (its pressure unknowns are p / S_pscale)
   bool built = false;
 };
 StokesSystem* stokes_system(eb_ctx* c);            // allocated on first use for the current grid

@@ -1732,6 +1732,14 @@ static int solve_once(eb_ctx* c, eb_solve_opts opt, bool stall_check, eb_solve_r
   k_mul<<<nblk(n3), kB, 0, c->stream>>>(st->bs, s.rhs, st->w, n3, 0);
   EB_LAUNCHED(c);
   if (opt.use_initial_guess) {
+    // S from an earlier system keeps the velocities, and its pressure unknowns p / pscale are
+    // brought to this system's pressure scale
+    if (s.S_pscale > 0.0 && s.S_pscale != s.pscale) {
+      EB_PROF(c, "k_axpy");
+      k_scale_copy<<<nblk(s.nc), kB, 0, c->stream>>>(s.S + 2 * s.nc, s.S + 2 * s.nc, s.S_pscale / s.pscale, s.nc);
+      EB_LAUNCHED(c);
+      s.S_pscale = s.pscale;
+    }
     EB_PROF(c, "k_axpy");
     k_mul<<<nblk(n3), kB, 0, c->stream>>>(st->xs, s.S, st->w, n3, 1);
     EB_LAUNCHED(c);
@@ -1740,6 +1748,12 @@ static int solve_once(eb_ctx* c, eb_solve_opts opt, bool stall_check, eb_solve_r
   }
   double bn2;
   if ((rc = mdot(c, st, st->bs, 0, 1, st->bs, &bn2))) return rc;
+  if (use_nn && opt.use_initial_guess && opt.learned_warm) {
+    // the learned stage as a warm start: xhat += a NN(bhat - Khat xhat) when that lowers the
+    // residual (the stage's own step and acceptance test); the first stored-direction slot is
+    // scratch here
+    if ((rc = learned_stage(c, st, st->bs, st->xs, st->Z))) return rc;
+  }
   const double bnorm = std::sqrt(bn2);
   if (!std::isfinite(bnorm)) {
     *input_nan = true;
@@ -1944,6 +1958,7 @@ static int solve_once(eb_ctx* c, eb_solve_opts opt, bool stall_check, eb_solve_r
   EB_PROF(c, "k_axpy");
   k_mul<<<nblk(n3), kB, 0, c->stream>>>(s.S, st->xs, st->w, n3, 0);
   EB_LAUNCHED(c);
+  s.S_pscale = s.pscale;
   EB_PROF(c, "k_apply64");
   k_apply64<<<nblk(s.nc), kB, 0, c->stream>>>(s.coef, s.S, st->t, s.nx, s.ny, (int32_t)s.nc);
   EB_LAUNCHED(c);
@@ -2280,6 +2295,7 @@ extern "C" int eb_stokes_vector_upload(eb_ctx* c, int which, const double* host)
   EB_PROF(c, "k_interleave");
   k_deinterleave<<<nblk(s.nc), kB, 0, c->stream>>>(c->st->il, d, s.nc);
   EB_LAUNCHED(c);
+  if (which == EB_SV_SOLUTION) s.S_pscale = s.pscale;  // an uploaded S is in the current system's scale
   EB_CK(c, cudaStreamSynchronize(c->stream));
   prof_resolve(c);
   return EB_OK;

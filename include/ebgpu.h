@@ -318,7 +318,9 @@ typedef struct eb_solve_opts {
                                 the most allowed (Stokes; unused by the heat solve): restarting after
                                 250 stalled on systems that converge within 550 unrestarted          */
   int32_t mg_sweeps;         /* red-black Gauss-Seidel sweeps before/after each coarse correction; 0 -> 3 */
-  int32_t use_initial_guess; /* 1: start from the current device solution vector, 0: from zero         */
+  int32_t use_initial_guess; /* 1: start from the current device solution vector (a solution of an
+                                earlier system has its pressure unknowns rescaled to this system's
+                                pscale), 0: from zero                                                */
   int32_t method;            /* 0: FGMRES (long recurrence, robust); 1: BiCGStab (short recurrence, two
                                 preconditioner applications per iteration)                           */
   int32_t learned;           /* 1: after each V-cycle, the learned stage (eb_learned_train) adds its
@@ -339,6 +341,9 @@ typedef struct eb_solve_opts {
                                 until the velocity residual falls below mg_inner_tol of its start
                                 (at most 8); 0 -> 1 (Stokes only)                                    */
   double  mg_inner_tol;      /* 0 -> 0.1 */
+  int32_t learned_warm;      /* with learned = 1 and use_initial_guess = 1: the learned stage also corrects
+                                the initial guess, xhat += a NN(residual) when that lowers the residual
+                                (the Picard warm start); Stokes only                                  */
 } eb_solve_opts;
 
 typedef struct eb_solve_report {
@@ -447,7 +452,9 @@ int eb_apply_nodal_plastic_yielding(eb_ctx* ctx);
 /* No counterpart in the reference (its COO product): y = L x for host vectors of N doubles. */
 int eb_stokes_apply(eb_ctx* ctx, const double* x, double* y);
 
-/* Copies of the N-vectors named by enum eb_stokes_vector (host arrays, interleaved layout). */
+/* Copies of the N-vectors named by enum eb_stokes_vector (host arrays, interleaved layout).  An
+ * uploaded solution is taken to be in the current system's pressure scale (its pressure unknowns
+ * p / pscale of the last assembled system). */
 int eb_stokes_vector_upload(eb_ctx* ctx, int which, const double* host);
 int eb_stokes_vector_download(eb_ctx* ctx, int which, double* host);
 

@@ -86,3 +86,36 @@ def test_training_lowers_loss_and_solve_still_converges(eb):
           f"{plain['seconds']:.3f} -> {learned['seconds']:.3f} s, corrections kept {stats['accepted']} of "
           f"{stats['accepted'] + stats['rejected']}; training {rep}")
     mic.close()
+
+
+def test_learned_warm_start_of_a_picard_iteration(eb):
+    """The learned stage as a Picard warm start: the second Picard iteration's solve starts from the
+    first one's solution, corrected by the network where that lowers the residual (the stage's own
+    step and acceptance test).  The solve must meet the tolerance either way; the test records the
+    iterations with and without the corrected start (on this model the network gains nothing)."""
+    mic = stokes_system(eb)
+    mic.learned_init(4)
+    mic.learned_train(steps=40, batch=2, patch=32, patches_per_sample=4, lr=1e-3, seed=9)
+    mic.solve_system(rtol=1e-8)
+    S1 = mic.download_stokes_vector("solution")
+    # the second Picard iteration's system: markers re-yielded, viscosity re-averaged
+    mic.backup_and_clear_viscosity_transport_arrays()
+    mic.update_plastic_yielding()
+    mic.interpolate_viscosity_to_transport_arrays()
+    mic.interpolate_basic_viscoplastic_viscosity_to_pressure_grid(1)
+    mic.calc_viscoelastic_terms()
+    mic.viscoelastic_rhs()
+    mic.build_system_of_equations()
+    out = {}
+    for warm in (False, True):
+        mic.upload_stokes_vector("solution", S1)
+        mic.learned_stats()
+        rep = mic.solve_system(rtol=1e-8, use_initial_guess=True, learned=True, learned_warm=warm)
+        st = mic.learned_stats()
+        assert rep["status"] == 0 and rep["rel_residual"] <= 1e-8, rep
+        assert st["accepted"] + st["rejected"] == rep["iterations"] + (1 if warm else 0), (st, rep)
+        out[warm] = rep["iterations"]
+    cold = mic.solve_system(rtol=1e-8, learned=True)["iterations"]
+    print(f"\nsecond Picard solve: {cold} iterations cold, {out[False]} from the previous solution, "
+          f"{out[True]} from the previous solution corrected by the network")
+    mic.close()

@@ -369,3 +369,37 @@ def test_fp32_gram_schmidt_matches_superlu(eb, case, gs_relax):
                                                               gs_relax=1e20)
     assert fp64["status"] == 0 and fp64["relaxed_iterations"] == 0, fp64   # plain method: never FP32
     mic.close()
+
+
+def test_warm_start_rescales_pressure_to_the_new_system(eb):
+    """A solve that starts from the solution of an earlier system: the pressure unknowns are
+    p / pscale, and pscale = 2 etan0[1,1] / (xstpavg + ystpavg) changes between systems, so the
+    start is rescaled to the new pscale.  Ten times the viscosity of the upper-left cell alone moves
+    pscale by ten and the solution only near that corner, so the warm start's residual is small:
+    to a loose tolerance (1e-4) it must need far fewer iterations than a cold start (an unscaled
+    start, every pressure unknown off by ten, would not), and to 1e-10 both must reach the same
+    solution."""
+    model = marker_model(eb, "rift_small")
+    mic = gpu_ctx(eb, model)
+    mic.solve_viscoelastic_stokes_continuity_equations(rtol=1e-10)
+    p0 = mic.pscale
+    etan1 = model.grids["etan1"].copy(order="F")
+    etan1[0, 0] *= 10.0
+    mic.upload_grid("etan1", etan1)
+    mic.calc_viscoelastic_terms()
+    mic.viscoelastic_rhs()
+    mic.build_system_of_equations()
+    assert mic.pscale == pytest.approx(10.0 * p0, rel=1e-6)
+    warm4 = mic.solve_system(rtol=1e-4, use_initial_guess=True)   # from the first system's solution
+    warm = mic.solve_system(rtol=1e-10, use_initial_guess=True)   # ... continued to 1e-10
+    S_warm = mic.download_stokes_vector("solution")
+    cold4 = mic.solve_system(rtol=1e-4)
+    cold = mic.solve_system(rtol=1e-10)
+    S_cold = mic.download_stokes_vector("solution")
+    print(f"\nto 1e-4: warm start {warm4['iterations']} iterations, cold start {cold4['iterations']}")
+    assert warm4["iterations"] <= 0.5 * cold4["iterations"], (warm4["iterations"], cold4["iterations"])
+    assert warm["rel_residual"] <= 1e-10 and cold["rel_residual"] <= 1e-10
+    for comp in range(3):
+        a, b = S_warm[comp::3], S_cold[comp::3]
+        assert np.abs(a - b).max() <= 1e-6 * np.abs(b).max(), comp
+    mic.close()
