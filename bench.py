@@ -100,6 +100,9 @@ def parse():
     ap.add_argument("--learned-steps", type=int, default=200)
     ap.add_argument("--circles", action="store_true",
                     help="also time the circles_1025 Stokes benchmark (200 inclusions, 1e-10)")
+    ap.add_argument("--rheology-only", action="store_true",
+                    help="run one time step of the workload, then three fused rheology passes, and print their "
+                         "time (a small case for ncu; not the bench line)")
     ap.add_argument("--stokes-only", action="store_true",
                     help="after the warm-up marker cycles run ONE mixed Stokes step and print its line "
                          "(a small launch list for ncu; not the bench line)")
@@ -549,6 +552,20 @@ def main():
     def step():
         mic.marker_cycle()
 
+    if args.rheology_only:
+        # markers with the strain rates and pressures of a real solution, then the fused pass
+        mic.time_step(3, 1e-3, rtol=1e-8)
+        torch.cuda.synchronize()
+        mic.profile_enable(True)
+        for _ in range(3):
+            mic.update_marker_rheology_and_viscoplastic_viscosity(True)
+        pr = mic.profile()
+        if rank == 0:
+            ms = pr["k_rheology"][0] / pr["k_rheology"][1]
+            print(json.dumps({"metric": "fused rheology pass (profiling run)", "value": ms, "unit": "ms",
+                              "workload": args.workload, "markers": M}))
+        mic.close()
+        return
     for _ in range(max(args.warmup, 3)):
         step()
     if args.stokes_only:

@@ -203,7 +203,8 @@ __device__ bool flow_root(const FlowLaw& f, double mdt, double cabs, double lo, 
     return true;
   }
   LogLaw g;
-  g.ld = __logf((float)f.A) - (float)((f.r.Ea_disl * 1000.0 + f.r.Va_disl * f.p_mpa) * (1.0 / (f.R * f.T)));
+  const float inv_rt = 1.f / ((float)f.R * (float)f.T);  // FP32: this stage only brackets the root
+  g.ld = __logf((float)f.A) - ((float)f.r.Ea_disl * 1000.f + (float)f.r.Va_disl * (float)f.p_mpa) * inv_rt;
   g.n = (float)f.r.n_disl;
   g.peierls = f.r.A_p > 0.0 && f.T < 1200.0;
   g.lp = g.peierls ? __logf((float)f.r.A_p) : 0.f;
@@ -212,8 +213,7 @@ __device__ bool flow_root(const FlowLaw& f, double mdt, double cabs, double lo, 
   g.n_p = (float)f.r.n_p;
   g.inv_sp = (float)f.inv_sp;
   g.diff = f.r.A_diff > 0.0;
-  g.lf = g.diff ? __logf((float)f.r.A_diff) -
-                      (float)((f.r.Ea_diff * 1000.0 + f.r.Va_diff * f.p_mpa) * (1.0 / (f.R * f.T)))
+  g.lf = g.diff ? __logf((float)f.r.A_diff) - ((float)f.r.Ea_diff * 1000.f + (float)f.r.Va_diff * (float)f.p_mpa) * inv_rt
                 : 0.f;
   g.l2mdt = __logf((float)(2.0 * mdt));
   g.cabs = (float)cabs;
@@ -273,7 +273,7 @@ __device__ __forceinline__ void d_flow_viscosity(const DevMarkers& mk, const Dev
     double s0 = sqrt(sxx * sxx + sxy * sxy);
     if (s0 < P.s_min) s0 = P.s_min;
     double e_disl = 0.0, a_p = 0.0, e_diff = 0.0;
-    const double inv_sp = 1.0 / r.s_p;
+    const double inv_sp = (r.A_p > 0.0 && T < 1200.0) ? 1.0 / r.s_p : 0.0;  // Peierls creep only
     double s_mpa = s0 * kPaToMPa;
     double rate = creep_rate(r, p_mpa, T, P.R, A, s_mpa, false, inv_sp, e_disl, a_p, e_diff);
     eta = 0.5 * (s_mpa * 1e6) / rate;
@@ -374,7 +374,10 @@ __device__ __forceinline__ void d_yield(const DevMarkers& mk, const DevMats& mt,
     const double mu = __ldg(&mt.mu[id - 1]);
     double sxx = mk.sxx[m], sxy = mk.sxy[m];
     const double exx = mk.exx[m], exy = mk.exy[m], srr = mk.sr_ratio[m], p = mk.pr[m];
-    const double cphi = cos(asin(sf));
+    // cos(asin(sf)) of YieldStress.calc_yield_stress, as the identity sqrt(1 - sf^2) for
+    // sf in [-1, 1]: one square root instead of two FP64 transcendentals (they differ by a few
+    // ulps of cos(phi), which moves the yield test only for a stress within ~1e-16 of yield)
+    const double cphi = sqrt(fmax(0.0, 1.0 - sf * sf));
     double sy;
     if (P.fluid == 0) {
       sy = coh * cphi + sf * p;
