@@ -250,15 +250,6 @@ __global__ void k_scale_copy(double* dst, const double* src, double a, int64_t n
   const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (k < n) dst[k] = a * src[k];
 }
-// u -= sum_v h[v] Z_v (FP32 directions)
-__global__ void k_maxpy_f32(double* __restrict__ u, const float* __restrict__ Z, int64_t stride,
-                            const double* __restrict__ h, int nv, int64_t n) {
-  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= n) return;
-  double s = u[k];
-  for (int v = 0; v < nv; ++v) s -= h[v] * (double)Z[(int64_t)v * stride + k];
-  u[k] = s;
-}
 // ---- Gram-Schmidt on FP32 copies of the basis (mixed method, late iterations) ----
 // Inexact Krylov theory (Simoncini & Szyld 2003; Bouras & Fraysse 2005) lets the error an
 // iteration adds to the Arnoldi relation grow like 1/|r| once the residual is small.  The
@@ -328,19 +319,317 @@ __global__ void __launch_bounds__(kB) k_mdot32(const float* __restrict__ V, int6
     partial[(int64_t)(v0 + threadIdx.x) * gridDim.x + blockIdx.x] = t;
   }
 }
-// u -= sum_v h[v] V32_v, the sum formed in FP32 and subtracted from the FP64 u; u32 = float(u)
-// afterwards (the copy the second pass, or the normalisation, starts from); partial[block] =
-// the block's sum of u^2 in FP64 (the measured norm).  A thread owns kAx32Per float4 chunks of
-// consecutive elements and streams four basis vectors at a time (eight 16-byte loads in flight).
-constexpr int kAx32Per = 2, kAx32Chunks = kAxThreads * kAx32Per;  // chunks (4 elements) per block
-__global__ void __launch_bounds__(kAxThreads) k_maxpy32(double* __restrict__ u, float* __restrict__ u32,
-                                                        const float* __restrict__ V, int64_t ld,
-                                                        const double* __restrict__ h, int nv, int64_t n,
-                                                        double* __restrict__ partial) {
-  extern __shared__ float hs32[];
-  for (int v = threadIdx.x; v < nv; v += blockDim.x) hs32[v] = (float)h[v];
+constexpr int kAx32Per = 2, kAx32Chunks = kAxThreads * kAx32Per;  // float4 chunks per thread / block
+
+// ---- The mixed method's Arnoldi step in double-float ----
+// On this part the FP64 pipe (about 1.6 FMA per SM per clock, measured) also executes the
+// FP64 <-> FP32 conversion instructions (about 2 per SM per clock), so FP64 arithmetic and
+// conversions, not HBM, bound elementwise kernels on FP64 vectors.  The mixed method therefore
+// keeps each Krylov vector as the unevaluated sum hi + lo of two FP32 vectors (about 2^-47
+// relative), forms the operator product and the Gram-Schmidt products from FMA-based exact
+// products (TwoProduct: p + e = a b exactly with e = fma(a, b, -p)) summed with Knuth's TwoSum
+// (the Dot2 scheme of Ogita, Rump & Oishi, SIAM J. Sci. Comput. 26, 2005), and converts with
+// integer operations; once its residual is small (gs_relax) it drops to plain FP32 vectors.
+// Every kernel of the step then runs on the FP32 pipe and streams HBM; the Hessenberg matrix
+// and the Givens rotations stay FP64 on the host.  The _rn intrinsics keep the compiler from
+// contracting a product into a following sum, which would break the error-free transforms.
+
+// x = hi + lo: hi = x rounded to FP32 (d2f), lo = x - hi rounded to FP32, by integer
+// operations; |x - hi - lo| <= 2^-48 |x|.  Magnitudes below 2^-74 keep hi alone (the
+// dropped lo is below 2^-98), below FLT_MIN both are zero; above FLT_MAX, and NaN, hi is
+// infinite.
+EB_DEV void split_df(double x, float& hi, float& lo) {
+  const uint32_t H = (uint32_t)__double2hiint(x), L = (uint32_t)__double2loint(x);
+  const uint32_t e = (H >> 20) & 0x7FFu;
+  hi = d2f(x);
+  // the 29 significand bits below hi's last place, as a signed count of units 2^(e - 1075):
+  // r, or r - 2^29 when d2f rounded the magnitude up (bit 28 set)
+  const int32_t r = (int32_t)(L & 0x1FFFFFFFu);
+  const int32_t t = ((L >> 28) & 1u) ? r - (1 << 29) : r;
+  const float mag = __fmul_rn(__int2float_rn(t), __uint_as_float((e - 948u) << 23));  // exact: power of 2
+  lo = (e >= 949u && e <= 1150u) ? __uint_as_float(__float_as_uint(mag) ^ (H & 0x80000000u)) : 0.f;
+}
+// (s, c) += p + e (TwoSum of s and p; e and the rounding error go to c)
+EB_DEV void two_sum_acc(float p, float e, float& s, float& c) {
+  const float t = __fadd_rn(s, p);
+  const float z = __fsub_rn(t, s);
+  c = __fadd_rn(c, __fadd_rn(__fadd_rn(__fsub_rn(s, __fsub_rn(t, z)), __fsub_rn(p, z)), e));
+  s = t;
+}
+// (s, c) += (ah + al) x for an FP32 x
+EB_DEV void df_axpy_acc(float ah, float al, float x, float& s, float& c) {
+  const float p = __fmul_rn(ah, x);
+  const float e = fmaf(al, x, fmaf(ah, x, -p));
+  two_sum_acc(p, e, s, c);
+}
+// (s, c) += (ah + al)(bh + bl), the al bl term dropped
+EB_DEV void df_fma_acc(float ah, float al, float bh, float bl, float& s, float& c) {
+  const float p = __fmul_rn(ah, bh);
+  const float e = fmaf(al, bh, fmaf(ah, bl, fmaf(ah, bh, -p)));
+  two_sum_acc(p, e, s, c);
+}
+// normalised pair h + l = s + c with |l| <= ulp(h) / 2 (TwoSum)
+EB_DEV void df_norm(float s, float c, float& h, float& l) {
+  h = __fadd_rn(s, c);
+  const float z = __fsub_rn(h, s);
+  l = __fadd_rn(__fsub_rn(s, __fsub_rn(h, z)), __fsub_rn(c, z));
+}
+
+// d = (W L W) x - v_k for the mixed method: x = Z_k (FP32, exact), the stencil as the pair
+// ch + cl, v_k = vh + vl; d is written as the normalised pair (dh, dl).  Same cells, slots
+// and neighbour order as k_apply64.
+__global__ void __launch_bounds__(kB) k_apply_df(const float* __restrict__ ch, const float* __restrict__ cl,
+                                                 const float* __restrict__ x, const float* __restrict__ vh,
+                                                 const float* __restrict__ vl, float* __restrict__ dh,
+                                                 float* __restrict__ dl, int32_t nx, int32_t ny, int32_t nc) {
+  const int32_t c = (int32_t)(blockIdx.x * blockDim.x + threadIdx.x);
+  if (c >= nc) return;
+  const int32_t j = c / ny, i = c - j * ny;
+  const float *vx = x, *vy = x + nc, *p = x + 2 * (int64_t)nc;
+  const bool hu = i > 0, hd = i < ny - 1, hl = j > 0, hr = j < nx - 1;
+  float s, e;
+  auto t = [&](int slot, float xv) {
+    df_axpy_acc(__ldg(&ch[(int64_t)slot * nc + c]), __ldg(&cl[(int64_t)slot * nc + c]), xv, s, e);
+  };
+  auto out = [&](int64_t o) {
+    two_sum_acc(-vh[o], -vl[o], s, e);
+    float h, l;
+    df_norm(s, e, h, l);
+    dh[o] = h;
+    dl[o] = l;
+  };
+  s = e = 0.f;
+  t(0, vx[c]);
+  if (hl) t(1, vx[c - ny]);
+  if (hr) t(2, vx[c + ny]);
+  if (hu) t(3, vx[c - 1]);
+  if (hd) t(4, vx[c + 1]);
+  if (hu) t(5, vy[c - 1]);
+  if (hu && hr) t(6, vy[c + ny - 1]);
+  t(7, vy[c]);
+  if (hr) t(8, vy[c + ny]);
+  t(9, p[c]);
+  if (hr) t(10, p[c + ny]);
+  out(c);
+  s = e = 0.f;
+  t(11, vy[c]);
+  if (hu) t(12, vy[c - 1]);
+  if (hd) t(13, vy[c + 1]);
+  if (hl) t(14, vy[c - ny]);
+  if (hr) t(15, vy[c + ny]);
+  if (hl) t(16, vx[c - ny]);
+  t(17, vx[c]);
+  if (hl && hd) t(18, vx[c + 1 - ny]);
+  if (hd) t(19, vx[c + 1]);
+  t(20, p[c]);
+  if (hd) t(21, p[c + 1]);
+  out(nc + (int64_t)c);
+  s = e = 0.f;
+  t(22, p[c]);
+  if (hl) t(23, vx[c - ny]);
+  t(24, vx[c]);
+  if (hu) t(25, vy[c - 1]);
+  t(26, vy[c]);
+  out(2 * (int64_t)nc + c);
+}
+// The same in FP32 once the residual is small: d = ch x - vh, FP32 arithmetic.
+__global__ void __launch_bounds__(kB) k_apply32(const float* __restrict__ ch, const float* __restrict__ x,
+                                                const float* __restrict__ vh, float* __restrict__ dh, int32_t nx,
+                                                int32_t ny, int32_t nc) {
+  const int32_t c = (int32_t)(blockIdx.x * blockDim.x + threadIdx.x);
+  if (c >= nc) return;
+  const int32_t j = c / ny, i = c - j * ny;
+  const float *vx = x, *vy = x + nc, *p = x + 2 * (int64_t)nc;
+  const bool hu = i > 0, hd = i < ny - 1, hl = j > 0, hr = j < nx - 1;
+  auto cf = [&](int slot) { return __ldg(&ch[(int64_t)slot * nc + c]); };
+  float ax = cf(0) * vx[c];
+  if (hl) ax = fmaf(cf(1), vx[c - ny], ax);
+  if (hr) ax = fmaf(cf(2), vx[c + ny], ax);
+  if (hu) ax = fmaf(cf(3), vx[c - 1], ax);
+  if (hd) ax = fmaf(cf(4), vx[c + 1], ax);
+  if (hu) ax = fmaf(cf(5), vy[c - 1], ax);
+  if (hu && hr) ax = fmaf(cf(6), vy[c + ny - 1], ax);
+  ax = fmaf(cf(7), vy[c], ax);
+  if (hr) ax = fmaf(cf(8), vy[c + ny], ax);
+  ax = fmaf(cf(9), p[c], ax);
+  if (hr) ax = fmaf(cf(10), p[c + ny], ax);
+  float ay = cf(11) * vy[c];
+  if (hu) ay = fmaf(cf(12), vy[c - 1], ay);
+  if (hd) ay = fmaf(cf(13), vy[c + 1], ay);
+  if (hl) ay = fmaf(cf(14), vy[c - ny], ay);
+  if (hr) ay = fmaf(cf(15), vy[c + ny], ay);
+  if (hl) ay = fmaf(cf(16), vx[c - ny], ay);
+  ay = fmaf(cf(17), vx[c], ay);
+  if (hl && hd) ay = fmaf(cf(18), vx[c + 1 - ny], ay);
+  if (hd) ay = fmaf(cf(19), vx[c + 1], ay);
+  ay = fmaf(cf(20), p[c], ay);
+  if (hd) ay = fmaf(cf(21), p[c + 1], ay);
+  float ap = cf(22) * p[c];
+  if (hl) ap = fmaf(cf(23), vx[c - ny], ap);
+  ap = fmaf(cf(24), vx[c], ap);
+  if (hu) ap = fmaf(cf(25), vy[c - 1], ap);
+  ap = fmaf(cf(26), vy[c], ap);
+  dh[c] = ax - vh[c];
+  dh[nc + c] = ay - vh[nc + c];
+  dh[2 * (int64_t)nc + c] = ap - vh[2 * (int64_t)nc + c];
+}
+// dots: block (b, g) reduces a grid-stride slice of (Vh_v + Vl_v) . (Vh_{nv-1} + Vl_{nv-1}) for
+// v = G g .. G g + G - 1 (< nv) over float4 chunks, U chunks per thread and step; the last slot
+// holds the new direction, so its own product is |d|^2.  partial[v * gridDim.x + b].
+constexpr int kDfVecs = 2, kDfUnroll = 2;
+__global__ void __launch_bounds__(kB) k_mdot_df(const float* __restrict__ Vh, const float* __restrict__ Vl, int64_t ld,
+                                                int64_t n4, int nv, double* __restrict__ partial) {
+  constexpr int G = kDfVecs, U = kDfUnroll;
+  const int v0 = blockIdx.y * G;
+  const int nvb = min(G, nv - v0);
+  const float4* bh = reinterpret_cast<const float4*>(Vh + (int64_t)(nv - 1) * ld);
+  const float4* bl = reinterpret_cast<const float4*>(Vl + (int64_t)(nv - 1) * ld);
+  const float4 *ah[G], *al[G];
+#pragma unroll
+  for (int g = 0; g < G; ++g) {
+    ah[g] = reinterpret_cast<const float4*>(Vh + (int64_t)(v0 + min(g, nvb - 1)) * ld);
+    al[g] = reinterpret_cast<const float4*>(Vl + (int64_t)(v0 + min(g, nvb - 1)) * ld);
+  }
+  float4 s[G], cs[G];
+#pragma unroll
+  for (int g = 0; g < G; ++g) s[g] = cs[g] = make_float4(0.f, 0.f, 0.f, 0.f);
+  auto acc4 = [](const float4 xh, const float4 xl, const float4 yh, const float4 yl, float4& s, float4& c) {
+    df_fma_acc(xh.x, xl.x, yh.x, yl.x, s.x, c.x);
+    df_fma_acc(xh.y, xl.y, yh.y, yl.y, s.y, c.y);
+    df_fma_acc(xh.z, xl.z, yh.z, yl.z, s.z, c.z);
+    df_fma_acc(xh.w, xl.w, yh.w, yl.w, s.w, c.w);
+  };
+  const int64_t step = (int64_t)gridDim.x * blockDim.x;
+  int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  for (; k + (U - 1) * step < n4; k += U * step) {
+    float4 yh[U], yl[U], xh[U][G], xl[U][G];
+#pragma unroll
+    for (int q = 0; q < U; ++q) {
+      yh[q] = __ldg(bh + k + q * step);
+      yl[q] = __ldg(bl + k + q * step);
+#pragma unroll
+      for (int g = 0; g < G; ++g)
+        if (g < nvb) {
+          xh[q][g] = __ldcs(ah[g] + k + q * step);
+          xl[q][g] = __ldcs(al[g] + k + q * step);
+        }
+    }
+#pragma unroll
+    for (int q = 0; q < U; ++q)
+#pragma unroll
+      for (int g = 0; g < G; ++g)
+        if (g < nvb) acc4(xh[q][g], xl[q][g], yh[q], yl[q], s[g], cs[g]);
+  }
+  for (; k < n4; k += step) {
+    const float4 yh = __ldg(bh + k), yl = __ldg(bl + k);
+#pragma unroll
+    for (int g = 0; g < G; ++g)
+      if (g < nvb) acc4(__ldcs(ah[g] + k), __ldcs(al[g] + k), yh, yl, s[g], cs[g]);
+  }
+  __shared__ double sh[G][kB / 32];
+#pragma unroll
+  for (int g = 0; g < G; ++g) {
+    double t = ((f2d(s[g].x) + f2d(cs[g].x)) + (f2d(s[g].y) + f2d(cs[g].y))) +
+               ((f2d(s[g].z) + f2d(cs[g].z)) + (f2d(s[g].w) + f2d(cs[g].w)));
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+    if ((threadIdx.x & 31) == 0) sh[g][threadIdx.x >> 5] = t;
+  }
+  __syncthreads();
+  if ((int)threadIdx.x < nvb) {
+    double t = 0.0;
+    for (int w = 0; w < kB / 32; ++w) t += sh[threadIdx.x][w];
+    partial[(int64_t)(v0 + threadIdx.x) * gridDim.x + blockIdx.x] = t;
+  }
+}
+// u = (uh + ul) - sum_v h[v] (Vh_v + Vl_v) in place (u the slot after the nv basis vectors),
+// normalised; partial[block] = the block's sum of u^2.  A thread owns kAx32Per float4 chunks of
+// consecutive elements and streams four basis vectors at a time.
+__global__ void __launch_bounds__(kAxThreads) k_maxpy_df(const float* __restrict__ Vh, const float* __restrict__ Vl,
+                                                         int64_t ld, const double* __restrict__ h, int nv,
+                                                         float* __restrict__ uhp, float* __restrict__ ulp,
+                                                         double* __restrict__ partial) {
+  extern __shared__ float hsd[];  // hi parts at [0, nv), lo parts at [nv, 2 nv)
+  for (int v = threadIdx.x; v < nv; v += blockDim.x) split_df(h[v], hsd[v], hsd[nv + v]);
   __syncthreads();
   const int64_t n4 = ld >> 2;
+  float4* uh = reinterpret_cast<float4*>(uhp);
+  float4* ul = reinterpret_cast<float4*>(ulp);
+  int64_t ch[kAx32Per];
+  bool ok[kAx32Per];
+  float4 as[kAx32Per], ac[kAx32Per];
+#pragma unroll
+  for (int q = 0; q < kAx32Per; ++q) {
+    ch[q] = (int64_t)blockIdx.x * kAx32Chunks + q * kAxThreads + threadIdx.x;
+    ok[q] = ch[q] < n4;
+    as[q] = ac[q] = make_float4(0.f, 0.f, 0.f, 0.f);
+  }
+  const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
+  auto acc4 = [](float bh, float bl, const float4 xh, const float4 xl, float4& s, float4& c) {
+    df_fma_acc(xh.x, xl.x, bh, bl, s.x, c.x);
+    df_fma_acc(xh.y, xl.y, bh, bl, s.y, c.y);
+    df_fma_acc(xh.z, xl.z, bh, bl, s.z, c.z);
+    df_fma_acc(xh.w, xl.w, bh, bl, s.w, c.w);
+  };
+  int v = 0;
+  for (; v + 4 <= nv; v += 4) {
+    float4 xh[4][kAx32Per], xl[4][kAx32Per];
+#pragma unroll
+    for (int g = 0; g < 4; ++g)
+#pragma unroll
+      for (int q = 0; q < kAx32Per; ++q) {
+        xh[g][q] = ok[q] ? __ldcs(reinterpret_cast<const float4*>(Vh + (int64_t)(v + g) * ld) + ch[q]) : zero;
+        xl[g][q] = ok[q] ? __ldcs(reinterpret_cast<const float4*>(Vl + (int64_t)(v + g) * ld) + ch[q]) : zero;
+      }
+#pragma unroll
+    for (int g = 0; g < 4; ++g)
+#pragma unroll
+      for (int q = 0; q < kAx32Per; ++q) acc4(hsd[v + g], hsd[nv + v + g], xh[g][q], xl[g][q], as[q], ac[q]);
+  }
+  for (; v < nv; ++v)
+#pragma unroll
+    for (int q = 0; q < kAx32Per; ++q)
+      if (ok[q])
+        acc4(hsd[v], hsd[nv + v], __ldcs(reinterpret_cast<const float4*>(Vh + (int64_t)v * ld) + ch[q]),
+             __ldcs(reinterpret_cast<const float4*>(Vl + (int64_t)v * ld) + ch[q]), as[q], ac[q]);
+  float sh2 = 0.f, sl2 = 0.f;  // sum of u^2 as a pair
+  auto fin = [&](float& xh, float& xl, float s, float c) {
+    float t = 0.f, e = 0.f;
+    two_sum_acc(xh, xl, t, e);
+    two_sum_acc(-s, -c, t, e);
+    df_norm(t, e, xh, xl);
+    df_fma_acc(xh, xl, xh, xl, sh2, sl2);
+  };
+#pragma unroll
+  for (int q = 0; q < kAx32Per; ++q) {
+    if (!ok[q]) continue;
+    float4 xh = uh[ch[q]], xl = ul[ch[q]];
+    fin(xh.x, xl.x, as[q].x, ac[q].x);
+    fin(xh.y, xl.y, as[q].y, ac[q].y);
+    fin(xh.z, xl.z, as[q].z, ac[q].z);
+    fin(xh.w, xl.w, as[q].w, ac[q].w);
+    uh[ch[q]] = xh;
+    ul[ch[q]] = xl;
+  }
+  double ss = f2d(sh2) + f2d(sl2);
+  for (int o = 16; o > 0; o >>= 1) ss += __shfl_xor_sync(0xffffffffu, ss, o);
+  __shared__ double sh[kAxThreads / 32];
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = ss;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < kAxThreads / 32; ++w) t += sh[w];
+    partial[blockIdx.x] = t;
+  }
+}
+// FP32 form: u = uh - sum_v h[v] Vh_v in place (u the slot after the nv basis vectors);
+// partial[block] = the block's sum of u^2.
+__global__ void __launch_bounds__(kAxThreads) k_maxpy32(float* __restrict__ V, int64_t ld, const double* __restrict__ h,
+                                                        int nv, double* __restrict__ partial) {
+  extern __shared__ float hs32[];
+  for (int v = threadIdx.x; v < nv; v += blockDim.x) hs32[v] = d2f(h[v]);
+  __syncthreads();
+  const int64_t n4 = ld >> 2;
+  float4* u = reinterpret_cast<float4*>(V + (int64_t)nv * ld);
   int64_t ch[kAx32Per];
   bool ok[kAx32Per];
   float4 acc[kAx32Per];
@@ -374,25 +663,22 @@ __global__ void __launch_bounds__(kAxThreads) k_maxpy32(double* __restrict__ u, 
 #pragma unroll
     for (int q = 0; q < kAx32Per; ++q)
       if (ok[q]) fma4(hs32[v], __ldcs(reinterpret_cast<const float4*>(V + (int64_t)v * ld) + ch[q]), acc[q]);
-  double ss = 0.0;
+  float ss = 0.f;
 #pragma unroll
   for (int q = 0; q < kAx32Per; ++q) {
     if (!ok[q]) continue;
-    const float av[4] = {acc[q].x, acc[q].y, acc[q].z, acc[q].w};
-#pragma unroll
-    for (int l = 0; l < 4; ++l) {
-      const int64_t e = 4 * ch[q] + l;
-      if (e < n) {
-        const double r = u[e] - (double)av[l];
-        u[e] = r;
-        u32[e] = (float)r;
-        ss += r * r;
-      }
-    }
+    float4 x = u[ch[q]];
+    x.x -= acc[q].x;
+    x.y -= acc[q].y;
+    x.z -= acc[q].z;
+    x.w -= acc[q].w;
+    u[ch[q]] = x;
+    ss += (x.x * x.x + x.y * x.y) + (x.z * x.z + x.w * x.w);
   }
-  for (int o = 16; o > 0; o >>= 1) ss += __shfl_xor_sync(0xffffffffu, ss, o);
+  double sd = f2d(ss);
+  for (int o = 16; o > 0; o >>= 1) sd += __shfl_xor_sync(0xffffffffu, sd, o);
   __shared__ double sh[kAxThreads / 32];
-  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = ss;
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = sd;
   __syncthreads();
   if (threadIdx.x == 0) {
     double t = 0.0;
@@ -400,13 +686,95 @@ __global__ void __launch_bounds__(kAxThreads) k_maxpy32(double* __restrict__ u, 
     partial[blockIdx.x] = t;
   }
 }
-// dst = a src (dst may alias src), and the FP32 copy dst32 = float(dst) when given
-__global__ void k_scale_copy2(double* dst, float* __restrict__ dst32, const double* src, double a, int64_t n) {
+// (vh + vl) *= ah + al in place, normalised; vl == nullptr: vh *= ah in FP32
+__global__ void k_scale_df(float* __restrict__ vh, float* __restrict__ vl, float ah, float al, int64_t n) {
   const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= n) return;
-  const double r = a * src[k];
-  dst[k] = r;
-  if (dst32) dst32[k] = (float)r;
+  if (!vl) {
+    vh[k] *= ah;
+    return;
+  }
+  const float xh = vh[k], xl = vl[k];
+  const float p = __fmul_rn(xh, ah);
+  const float e = fmaf(xl, ah, fmaf(xh, al, fmaf(xh, ah, -p)));
+  float h, l;
+  df_norm(p, e, h, l);
+  vh[k] = h;
+  vl[k] = l;
+}
+// (vh, vl) = split(a src) (the first basis vector of a cycle, from the FP64 residual)
+__global__ void k_split_scale(float* __restrict__ vh, float* __restrict__ vl, const double* __restrict__ src, double a,
+                              int64_t n) {
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < n) split_df(a * src[k], vh[k], vl[k]);
+}
+// u -= sum_v h[v] Z_v (FP32 directions): the sum in double-float, subtracted from the FP64 u
+constexpr int kUpdVecs = 8;
+__global__ void k_update_df(double* __restrict__ u, const float* __restrict__ Z, int64_t stride,
+                            const double* __restrict__ h, int nv, int64_t n) {
+  extern __shared__ float ysd[];  // hi parts at [0, nv), lo parts at [nv, 2 nv)
+  for (int v = threadIdx.x; v < nv; v += blockDim.x) split_df(h[v], ysd[v], ysd[nv + v]);
+  __syncthreads();
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  float s = 0.f, c = 0.f;
+  int v = 0;
+  for (; v + kUpdVecs <= nv; v += kUpdVecs) {
+    float z[kUpdVecs];
+#pragma unroll
+    for (int g = 0; g < kUpdVecs; ++g) z[g] = __ldcs(Z + (int64_t)(v + g) * stride + k);
+#pragma unroll
+    for (int g = 0; g < kUpdVecs; ++g) df_axpy_acc(ysd[v + g], ysd[nv + v + g], z[g], s, c);
+  }
+  for (; v < nv; ++v) df_axpy_acc(ysd[v], ysd[nv + v], Z[(int64_t)v * stride + k], s, c);
+  u[k] -= f2d(s) + f2d(c);
+}
+// The mixed method's FP32 copies of the scaled system: the W L W stencil as pairs (ch, cl),
+// the four pressure-coupling slots 9, 10, 20, 21 of the assembled stencil (cq), 1/w (winv32)
+// and prep * winv_p (pw32), the pressure factor of the preconditioner's input.
+__global__ void k_split_setup(const double* __restrict__ coefS, const double* __restrict__ coef,
+                              const double* __restrict__ winv, const double* __restrict__ prep,
+                              float* __restrict__ ch, float* __restrict__ cl, float* __restrict__ cq,
+                              float* __restrict__ winv32, float* __restrict__ pw32, int64_t nc) {
+  const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= nc) return;
+  for (int s = 0; s < 27; ++s) split_df(coefS[s * nc + c], ch[s * nc + c], cl[s * nc + c]);
+  const int slots[4] = {9, 10, 20, 21};
+  for (int q = 0; q < 4; ++q) cq[q * nc + c] = d2f(coef[slots[q] * nc + c]);
+  for (int k = 0; k < 3; ++k) winv32[k * nc + c] = d2f(winv[k * nc + c]);
+  pw32[c] = d2f(prep[c] * winv[2 * nc + c]);
+}
+// FP32 preconditioner input of the mixed method from the basis vector's hi part rh:
+// zhat_p = (prep winv_p rh_p) winv_p into Z_k, and the velocity right-hand sides
+// f = winv_u rh_u - L_up z_p for the V-cycle (as k_prec_in, in FP32).
+__global__ void k_prec_in32(const float* __restrict__ cq, const float* __restrict__ rh, const float* __restrict__ winv32,
+                            const float* __restrict__ pw32, float* __restrict__ Zk, float* __restrict__ fx,
+                            float* __restrict__ fy, int32_t nx, int32_t ny) {
+  const int64_t nc = (int64_t)nx * ny;
+  const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= nc) return;
+  const int32_t j = (int32_t)c / ny, i = (int32_t)c - j * ny;
+  auto z = [&](int64_t k) { return pw32[k] * rh[2 * nc + k]; };
+  const float zc = z(c);
+  Zk[2 * nc + c] = zc * winv32[2 * nc + c];
+  float gx = cq[c] * zc;
+  if (j < nx - 1) gx = fmaf(cq[nc + c], z(c + ny), gx);
+  float gy = cq[2 * nc + c] * zc;
+  if (i < ny - 1) gy = fmaf(cq[3 * nc + c], z(c + 1), gy);
+  fx[c] = rh[c] * winv32[c] - gx;
+  fy[c] = rh[nc + c] * winv32[nc + c] - gy;
+}
+__global__ void k_prec_out32(const float* __restrict__ ux, const float* __restrict__ uy,
+                             const float* __restrict__ winv32, float* __restrict__ Zk, int64_t nc) {
+  const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= nc) return;
+  Zk[c] = ux[c] * winv32[c];
+  Zk[nc + c] = uy[c] * winv32[nc + c];
+}
+// dst = a src (dst may alias src)
+__global__ void k_scale_copy2(double* dst, const double* src, double a, int64_t n) {
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < n) dst[k] = a * src[k];
 }
 // BiCGStab vector updates
 __global__ void k_bicg_p(double* __restrict__ p, const double* __restrict__ r, const double* __restrict__ v, double beta,
@@ -1041,6 +1409,8 @@ struct StokesState {
   double *w = nullptr, *prep = nullptr;  // scaling and pressure factor
   double* winv = nullptr;                // 1 / w
   double* coefS = nullptr;               // stencil of W L W [27][nc]
+  // mixed method: coefS as FP32 pairs, FP32 pressure-coupling slots, 1/w and prep * winv_p
+  float *coefH = nullptr, *coefL = nullptr, *cq32 = nullptr, *winv32 = nullptr, *pw32 = nullptr;
   // FGMRES workspace
   int m = 0;
   double *V = nullptr, *r = nullptr, *t = nullptr, *xs = nullptr, *bs = nullptr, *zp = nullptr, *zt = nullptr;
@@ -1048,9 +1418,10 @@ struct StokesState {
   double* Zd = nullptr;              // ... or FP64 (plain method)
   double *partial = nullptr, *dots = nullptr, *hdev = nullptr;
   int nb_dot = 0;
-  float* V32 = nullptr;              // FP32 copies of the basis (mixed method), slots ld32 apart
+  float* V32 = nullptr;              // the basis as FP32 hi parts (mixed method), slots ld32 apart
+  float* V32lo = nullptr;            // their remainders: the basis as double-float pairs
   int64_t ld32 = 0;
-  double* part32 = nullptr;          // per-block norms of k_maxpy32
+  double* part32 = nullptr;          // per-block norms of k_maxpy32 / k_maxpy_df
   int nb_ax32 = 0;
   double* il = nullptr;              // interleaved staging vector (N)
   double* tmp = nullptr;             // scratch vector (N)
@@ -1579,6 +1950,26 @@ int precondition(eb_ctx* c, StokesState* st, const double* rhat, double* zt, voi
   return EB_OK;
 }
 
+// The mixed method's preconditioner on a split basis vector (its FP32 hi part rh): FP32 input
+// and output kernels around the captured FP32 V-cycle; the direction goes to Zk only.
+int precondition32(eb_ctx* c, StokesState* st, const float* rh, float* Zk) {
+  const StokesSystem& s = st->sys;
+  Level& v = st->H().levels[0];
+  EB_PROF(c, "k_precond");
+  k_prec_in32<<<nblk(s.nc), kB, 0, c->stream>>>(st->cq32, rh, st->winv32, st->pw32, Zk, static_cast<float*>(v.fx),
+                                                static_cast<float*>(v.fy), s.nx, s.ny);
+  EB_LAUNCHED(c);
+  EB_PROF(c, "vcycle_graph");
+  EB_CK(c, cudaGraphLaunch(st->H().gexec, c->stream));
+  c->launches += st->H().graph_kernels - 1;
+  EB_LAUNCHED(c);
+  EB_PROF(c, "k_precond");
+  k_prec_out32<<<nblk(s.nc), kB, 0, c->stream>>>(static_cast<float*>(v.ux), static_cast<float*>(v.uy), st->winv32, Zk,
+                                                 s.nc);
+  EB_LAUNCHED(c);
+  return EB_OK;
+}
+
 // dots[v] = V_v . u for v < nv (device), copied to host h
 int mdot(eb_ctx* c, StokesState* st, const double* V, int64_t stride, int nv, const double* u, double* h) {
   const int64_t n3 = 3 * st->sys.nc;
@@ -1606,12 +1997,38 @@ int mdot32(eb_ctx* c, StokesState* st, int nv, double* h) {
   EB_CK(c, cudaStreamSynchronize(c->stream));
   return EB_OK;
 }
-// w -= sum_{v<nv} hdev[v] V32_v (w32 = its FP32 copy); *wn2 = |w|^2 measured in FP64
-int maxpy32(eb_ctx* c, StokesState* st, double* w, float* w32, int nv, double* wn2) {
-  const int64_t n3 = 3 * st->sys.nc;
+// h[v] = V_v . V_{nv-1} for v < nv on the split basis (slot nv-1 holds the new direction)
+int mdot_df(eb_ctx* c, StokesState* st, int nv, double* h) {
+  EB_PROF(c, "k_mdot_df");
+  k_mdot_df<<<dim3(st->nb_dot, (nv + kDfVecs - 1) / kDfVecs), kB, 0, c->stream>>>(st->V32, st->V32lo, st->ld32,
+                                                                                  st->ld32 / 4, nv, st->partial);
+  EB_LAUNCHED(c);
+  EB_PROF(c, "k_mdot_final");
+  k_mdot_final<<<nv, kB, 0, c->stream>>>(st->partial, st->nb_dot, st->dots);
+  EB_LAUNCHED(c);
+  EB_CK(c, cudaMemcpyAsync(h, st->dots, nv * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  EB_CK(c, cudaStreamSynchronize(c->stream));
+  return EB_OK;
+}
+// slot nv -= sum_{v<nv} hdev[v] V_v on the split basis (double-float); *wn2 = |slot nv|^2
+int maxpy_df(eb_ctx* c, StokesState* st, int nv, double* wn2) {
+  EB_PROF(c, "k_maxpy_df");
+  k_maxpy_df<<<st->nb_ax32, kAxThreads, (size_t)2 * nv * sizeof(float), c->stream>>>(
+      st->V32, st->V32lo, st->ld32, st->hdev, nv, st->V32 + (size_t)nv * st->ld32, st->V32lo + (size_t)nv * st->ld32,
+      st->part32);
+  EB_LAUNCHED(c);
+  EB_PROF(c, "k_mdot_final");
+  k_mdot_final<<<1, kB, 0, c->stream>>>(st->part32, st->nb_ax32, st->dots);
+  EB_LAUNCHED(c);
+  EB_CK(c, cudaMemcpyAsync(wn2, st->dots, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  EB_CK(c, cudaStreamSynchronize(c->stream));
+  return EB_OK;
+}
+// the same on the FP32 hi parts in FP32
+int maxpy32(eb_ctx* c, StokesState* st, int nv, double* wn2) {
   EB_PROF(c, "k_maxpy32");
-  k_maxpy32<<<st->nb_ax32, kAxThreads, (size_t)nv * sizeof(float), c->stream>>>(w, w32, st->V32, st->ld32, st->hdev,
-                                                                                nv, n3, st->part32);
+  k_maxpy32<<<st->nb_ax32, kAxThreads, (size_t)nv * sizeof(float), c->stream>>>(st->V32, st->ld32, st->hdev, nv,
+                                                                                st->part32);
   EB_LAUNCHED(c);
   EB_PROF(c, "k_mdot_final");
   k_mdot_final<<<1, kB, 0, c->stream>>>(st->part32, st->nb_ax32, st->dots);
@@ -1642,6 +2059,8 @@ int ensure_solver(eb_ctx* c, StokesState* st, int m) {
     drop(st->Z);
     drop(st->Zd);
     drop(st->V32);
+    drop(st->V32lo);
+    st->V32lo = nullptr;
     st->V = nullptr;
     st->Z = nullptr;
     st->Zd = nullptr;
@@ -1658,6 +2077,9 @@ int ensure_solver(eb_ctx* c, StokesState* st, int m) {
     st->nb_ax32 = (int)((st->ld32 / 4 + kAx32Chunks - 1) / kAx32Chunks);
     if ((rc = dalloc(c, st->allocs, &st->V32, (size_t)(m + 2) * st->ld32))) return rc;
     EB_CK(c, cudaMemsetAsync(st->V32, 0, (size_t)(m + 2) * st->ld32 * sizeof(float), c->stream));
+    drop(st->V32lo);
+    if ((rc = dalloc(c, st->allocs, &st->V32lo, (size_t)(m + 2) * st->ld32))) return rc;
+    EB_CK(c, cudaMemsetAsync(st->V32lo, 0, (size_t)(m + 2) * st->ld32 * sizeof(float), c->stream));
     drop(st->part32);
     if ((rc = dalloc(c, st->allocs, &st->part32, (size_t)st->nb_ax32))) return rc;
   }
@@ -1732,6 +2154,18 @@ int prepare(eb_ctx* c, StokesState* st, int sweeps, int m, bool fp64) {
   EB_PROF(c, "k_scaling");
   k_prescale<<<nblk(s.nc), kB, 0, c->stream>>>(s.coef, st->w, st->coefS, s.nx, s.ny, (int32_t)s.nc);
   EB_LAUNCHED(c);
+  if (!fp64) {
+    if (!st->coefH && ((rc = dalloc(c, st->allocs, &st->coefH, (size_t)kStencilSlots * s.nc)) ||
+                       (rc = dalloc(c, st->allocs, &st->coefL, (size_t)kStencilSlots * s.nc)) ||
+                       (rc = dalloc(c, st->allocs, &st->cq32, (size_t)4 * s.nc)) ||
+                       (rc = dalloc(c, st->allocs, &st->winv32, (size_t)3 * s.nc)) ||
+                       (rc = dalloc(c, st->allocs, &st->pw32, (size_t)s.nc))))
+      return rc;
+    EB_PROF(c, "k_scaling");
+    k_split_setup<<<nblk(s.nc), kB, 0, c->stream>>>(st->coefS, s.coef, st->winv, st->prep, st->coefH, st->coefL,
+                                                    st->cq32, st->winv32, st->pw32, s.nc);
+    EB_LAUNCHED(c);
+  }
   return EB_OK;
 }
 
@@ -1807,9 +2241,11 @@ static int solve_once(eb_ctx* c, eb_solve_opts opt, bool stall_check, eb_solve_r
   std::vector<double> H((size_t)(m + 1) * m), g(m + 1), cs(m), sn(m), hcol(m + 2), y(m);
   int it = 0, reorth = 0, relaxed = 0;
   double est = 1.0;
-  // FP32 Gram-Schmidt (mixed method): from a residual estimate of gs_relax x the target on
+  // The mixed method's FGMRES (without the learned stage or the GCR velocity stage) runs its
+  // Arnoldi step on split vectors: double-float until the residual estimate falls below
+  // gs_relax x the target, FP32 after that.  gs_relax < 0 keeps the FP64 step.
   const double relax_fac = opt.gs_relax == 0.0 ? kGsRelax : opt.gs_relax;
-  float* const V32 = (!st->mg64 && relax_fac > 0.0) ? st->V32 : nullptr;
+  const bool split = !st->mg64 && relax_fac > 0.0 && !use_nn && st->gcr_steps <= 1;
   // The Krylov methods run on the scaled system, whose residual norm weights rows by W; the
   // tolerance is on the reference's (unscaled) residual ||R - L S|| / ||R||.  When the scaled
   // target is reached but the unscaled residual is still above rtol, the target is tightened
@@ -1883,7 +2319,10 @@ static int solve_once(eb_ctx* c, eb_solve_opts opt, bool stall_check, eb_solve_r
     if (stall_check && beta > kStallFactor * prev_beta) { stalled = true; break; }
     prev_beta = beta;
     EB_PROF(c, "k_axpy");
-    k_scale_copy2<<<nblk(n3), kB, 0, c->stream>>>(st->V, V32, st->r, 1.0 / beta, n3);
+    if (split)
+      k_split_scale<<<nblk(n3), kB, 0, c->stream>>>(st->V32, st->V32lo, st->r, 1.0 / beta, n3);
+    else
+      k_scale_copy2<<<nblk(n3), kB, 0, c->stream>>>(st->V, st->r, 1.0 / beta, n3);
     EB_LAUNCHED(c);
     std::fill(g.begin(), g.end(), 0.0);
     g[0] = beta;
@@ -1892,69 +2331,82 @@ static int solve_once(eb_ctx* c, eb_solve_opts opt, bool stall_check, eb_solve_r
       double* vk = st->V + (size_t)k * n3;
       void* zk = st->mg64 ? (void*)(st->Zd + (size_t)k * n3) : (void*)(st->Z + (size_t)k * n3);
       double* w = st->V + (size_t)(k + 1) * n3;
-      if ((rc = precondition(c, st, vk, st->zt, zk))) return rc;
-      if (use_nn && (rc = learned_stage(c, st, vk, st->zt, static_cast<float*>(zk)))) return rc;
-      // Shifted Arnoldi: with a good preconditioner A z_k is close to v_k, so the slot holds
-      // d = A z_k - v_k and the projection starts from d (h_kk gets the 1 back below); the
-      // cancellation that classical Gram-Schmidt suffers is then measured against |d|.
-      // FP32 products once the residual estimate |g_k| is below relax_tol (mixed method)
-      float* w32 = V32 ? V32 + (size_t)(k + 1) * st->ld32 : nullptr;
-      const bool relax = V32 && std::fabs(g[k]) <= relax_fac * target * bnorm;
-      EB_PROF(c, "k_apply64");
-      k_apply64<<<nblk(s.nc), kB, 0, c->stream>>>(st->coefS, st->zt, w, s.nx, s.ny, (int32_t)s.nc, vk,
-                                                  relax ? w32 : nullptr);
-      EB_LAUNCHED(c);
-      // Classical Gram-Schmidt.  One reduction gives V^T d and |d|^2 (d is the slot after V_k);
-      // the projected norm follows from Pythagoras unless cancellation is large, in which
-      // case a second pass re-orthogonalises and the norm is measured.  The FP32 form
-      // measures the norm every time (its products are only FP32-accurate).
+      float* const vh = st->V32 + (size_t)k * st->ld32;
+      float* const vl = st->V32lo + (size_t)k * st->ld32;
+      float* const wh = vh + st->ld32;
+      float* const wl = vl + st->ld32;
+      const bool relax = split && std::fabs(g[k]) <= relax_fac * target * bnorm;
       std::vector<double> h(k + 2);
-      if (relax) {
-        ++relaxed;
-        if ((rc = mdot32(c, st, k + 2, h.data()))) return rc;
+      if (split) {
+        // Shifted Arnoldi (see the FP64 form below) on split vectors; classical Gram-Schmidt
+        // with the norm measured in the update's pass, a second pass if the projection removed
+        // all but 5% of the norm
+        if ((rc = precondition32(c, st, vh, static_cast<float*>(zk)))) return rc;
+        if (relax) {
+          ++relaxed;
+          EB_PROF(c, "k_apply32");
+          k_apply32<<<nblk(s.nc), kB, 0, c->stream>>>(st->coefH, static_cast<float*>(zk), vh, wh, s.nx, s.ny,
+                                                      (int32_t)s.nc);
+        } else {
+          EB_PROF(c, "k_apply_df");
+          k_apply_df<<<nblk(s.nc), kB, 0, c->stream>>>(st->coefH, st->coefL, static_cast<float*>(zk), vh, vl, wh, wl,
+                                                       s.nx, s.ny, (int32_t)s.nc);
+        }
+        EB_LAUNCHED(c);
+        auto dots = [&]() { return relax ? mdot32(c, st, k + 2, h.data()) : mdot_df(c, st, k + 2, h.data()); };
+        if ((rc = dots())) return rc;
         double wn2_before = h[k + 1];
         for (int pass = 0; pass < 2; ++pass) {
           EB_CK(c, cudaMemcpyAsync(st->hdev, h.data(), (k + 1) * sizeof(double), cudaMemcpyHostToDevice, c->stream));
           double wn2 = 0.0;
-          if ((rc = maxpy32(c, st, w, w32, k + 1, &wn2))) return rc;
+          if ((rc = relax ? maxpy32(c, st, k + 1, &wn2) : maxpy_df(c, st, k + 1, &wn2))) return rc;
           for (int q = 0; q <= k; ++q) hcol[q] = (pass == 0 ? 0.0 : hcol[q]) + h[q];
           if (pass == 1 || wn2 > kReorth2 * wn2_before) {
             hcol[k + 1] = std::sqrt(wn2);
             break;
           }
           ++reorth;
-          if ((rc = mdot32(c, st, k + 2, h.data()))) return rc;
+          if ((rc = dots())) return rc;
           wn2_before = wn2;
         }
-      }
-      double wn2_before = 0.0;
-      if (!relax) {
-        if ((rc = mdot(c, st, st->V, n3, k + 2, w, h.data()))) return rc;
-        wn2_before = h[k + 1];
-      }
-      for (int pass = 0; pass < 2 && !relax; ++pass) {
-        EB_CK(c, cudaMemcpyAsync(st->hdev, h.data(), (k + 1) * sizeof(double), cudaMemcpyHostToDevice, c->stream));
-        EB_PROF(c, "k_maxpy");
-        k_maxpy<<<(unsigned)((n3 + kAxTile - 1) / kAxTile), kAxThreads, (size_t)(k + 1) * sizeof(double), c->stream>>>(
-            w, st->V, n3, st->hdev, k + 1, n3);
+      } else {
+        if ((rc = precondition(c, st, vk, st->zt, zk))) return rc;
+        if (use_nn && (rc = learned_stage(c, st, vk, st->zt, static_cast<float*>(zk)))) return rc;
+        // Shifted Arnoldi: with a good preconditioner A z_k is close to v_k, so the slot holds
+        // d = A z_k - v_k and the projection starts from d (h_kk gets the 1 back below); the
+        // cancellation that classical Gram-Schmidt suffers is then measured against |d|.
+        EB_PROF(c, "k_apply64");
+        k_apply64<<<nblk(s.nc), kB, 0, c->stream>>>(st->coefS, st->zt, w, s.nx, s.ny, (int32_t)s.nc, vk);
         EB_LAUNCHED(c);
-        double proj = 0.0;
-        for (int q = 0; q <= k; ++q) {
-          hcol[q] = (pass == 0 ? 0.0 : hcol[q]) + h[q];
-          proj += h[q] * h[q];
-        }
-        const double est = wn2_before - proj;
-        if (pass == 0 && est > kReorth2 * wn2_before) {  // no severe cancellation: keep
-          hcol[k + 1] = std::sqrt(est);
-          break;
-        }
-        ++reorth;
+        // Classical Gram-Schmidt.  One reduction gives V^T d and |d|^2 (d is the slot after V_k);
+        // the projected norm follows from Pythagoras unless cancellation is large, in which
+        // case a second pass re-orthogonalises and the norm is measured.
         if ((rc = mdot(c, st, st->V, n3, k + 2, w, h.data()))) return rc;
-        if (pass == 1) {
-          hcol[k + 1] = std::sqrt(h[k + 1]);
-          break;
+        double wn2_before = h[k + 1];
+        for (int pass = 0; pass < 2; ++pass) {
+          EB_CK(c, cudaMemcpyAsync(st->hdev, h.data(), (k + 1) * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+          EB_PROF(c, "k_maxpy");
+          k_maxpy<<<(unsigned)((n3 + kAxTile - 1) / kAxTile), kAxThreads, (size_t)(k + 1) * sizeof(double),
+                    c->stream>>>(w, st->V, n3, st->hdev, k + 1, n3);
+          EB_LAUNCHED(c);
+          double proj = 0.0;
+          for (int q = 0; q <= k; ++q) {
+            hcol[q] = (pass == 0 ? 0.0 : hcol[q]) + h[q];
+            proj += h[q] * h[q];
+          }
+          const double est = wn2_before - proj;
+          if (pass == 0 && est > kReorth2 * wn2_before) {  // no severe cancellation: keep
+            hcol[k + 1] = std::sqrt(est);
+            break;
+          }
+          ++reorth;
+          if ((rc = mdot(c, st, st->V, n3, k + 2, w, h.data()))) return rc;
+          if (pass == 1) {
+            hcol[k + 1] = std::sqrt(h[k + 1]);
+            break;
+          }
+          wn2_before = h[k + 1];
         }
-        wn2_before = h[k + 1];
       }
       hcol[k] += 1.0;
       if (!std::isfinite(hcol[k + 1])) return eb_fail(c, EB_NAN, "FGMRES basis became NaN/Inf");
@@ -1976,7 +2428,14 @@ static int solve_once(eb_ctx* c, eb_solve_opts opt, bool stall_check, eb_solve_r
       est = std::fabs(g[k + 1]) / bnorm;
       if (hk1 > 0.0) {
         EB_PROF(c, "k_axpy");
-        k_scale_copy2<<<nblk(n3), kB, 0, c->stream>>>(w, w32, w, 1.0 / hk1, n3);
+        if (split) {
+          // 1 / hk1 as an FP32 pair (the FP32 form uses its hi part)
+          const double a = 1.0 / hk1;
+          const float ah = (float)a, al = (float)(a - (double)ah);
+          k_scale_df<<<nblk(n3), kB, 0, c->stream>>>(wh, relax ? nullptr : wl, ah, al, n3);
+        } else {
+          k_scale_copy2<<<nblk(n3), kB, 0, c->stream>>>(w, w, 1.0 / hk1, n3);
+        }
         EB_LAUNCHED(c);
       }
       if (est <= target || hk1 == 0.0) { ++k; break; }
@@ -1995,7 +2454,8 @@ static int solve_once(eb_ctx* c, eb_solve_opts opt, bool stall_check, eb_solve_r
       k_maxpy<<<(unsigned)((n3 + kAxTile - 1) / kAxTile), kAxThreads, (size_t)std::max(k, 1) * sizeof(double),
                 c->stream>>>(st->xs, st->Zd, n3, st->hdev, k, n3);
     else
-      k_maxpy_f32<<<nblk(n3), kB, 0, c->stream>>>(st->xs, st->Z, n3, st->hdev, k, n3);
+      k_update_df<<<nblk(n3), kB, (size_t)2 * std::max(k, 1) * sizeof(float), c->stream>>>(st->xs, st->Z, n3, st->hdev,
+                                                                                          k, n3);
     EB_LAUNCHED(c);
     EB_CK(c, cudaStreamSynchronize(c->stream));
   }

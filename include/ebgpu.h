@@ -330,7 +330,9 @@ typedef struct eb_solve_opts {
                                 1: plain FP64 (V-cycle and directions in FP64; Stokes only)          */
   double  gs_relax;          /* mixed method only: once the FGMRES residual estimate is below
                                 gs_relax x the target, Gram-Schmidt projects with FP32 products on
-                                FP32 copies of the basis; 0 -> 1e3, negative -> never (Stokes only) */
+                                FP32 copies of the basis, before that with double-float products
+                                (Dot2) on the basis split into FP32 hi + lo; 0 -> 1e3, negative ->
+                                FP64 products throughout (Stokes only)                               */
   int32_t fallback;          /* mixed method only: 0 -> the plain FP64 method takes over whenever the
                                 mixed method's FP64 residual fails to fall (an FGMRES cycle that does
                                 not halve the true residual, the iteration limit reached, or NaN/Inf),
