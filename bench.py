@@ -326,17 +326,16 @@ def stokes_leg(eb, model, local, args, rank, world):
     n_rel = m_rep["relaxed_iterations"]
     ks64, ks32 = ks[:len(ks) - n_rel], ks[len(ks) - n_rel:]
     rl = {}
-    # the mixed method's Arnoldi step: double-float pairs (8 bytes per element and vector) before
-    # the FP32 threshold, FP32 after it; k_apply64 remains for the residuals of each cycle
+    # the mixed method's Arnoldi step: double-float pairs (8 bytes per element and vector); below
+    # the FP32 threshold the products read the FP32 hi parts; k_apply64 remains for the
+    # residuals of each cycle
     nc = n_unk // 3
     n_df = kern.get("k_apply_df", (0, 0))[1] / 3
-    n_32 = kern.get("k_apply32", (0, 0))[1] / 3
     for kname, b in (("k_mdot_df", sum(k + 2 for k in ks64) * n_unk * 8.0),
                      ("k_maxpy_df", sum((k + 1) * 8.0 + 16.0 for k in ks64) * n_unk),
                      ("k_mdot32", sum(k + 2 for k in ks32) * n_unk * 4.0),
-                     ("k_maxpy32", sum((k + 1) * 4.0 + 8.0 for k in ks32) * n_unk),
+                     ("k_maxpy32", sum((k + 1) * 4.0 + 16.0 for k in ks32) * n_unk),
                      ("k_apply_df", nc * (27 * 8.0 + 12 + 24 + 24) * n_df),
-                     ("k_apply32", nc * (27 * 4.0 + 12 + 12 + 12) * n_32),
                      ("k_apply64", nc * 36 * 8.0 * kern.get("k_apply64", (0, 0))[1] / 3)):
         if kname in kern and b > 0:
             t = kern[kname][0] * kern[kname][1] / 3 * 1e-3   # 3 mixed solves were profiled

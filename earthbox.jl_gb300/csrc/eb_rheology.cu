@@ -202,25 +202,27 @@ __device__ bool flow_root(const FlowLaw& f, double mdt, double cabs, double lo, 
     sstar = 0.0;
     return true;
   }
+  // FP32 copies by integer conversion (d2f): the F2F instructions would issue on the FP64 pipe
+  // that bounds this kernel
   LogLaw g;
-  const float inv_rt = 1.f / ((float)f.R * (float)f.T);  // FP32: this stage only brackets the root
-  g.ld = __logf((float)f.A) - ((float)f.r.Ea_disl * 1000.f + (float)f.r.Va_disl * (float)f.p_mpa) * inv_rt;
-  g.n = (float)f.r.n_disl;
+  const float inv_rt = 1.f / (d2f(f.R) * d2f(f.T));  // FP32: this stage only brackets the root
+  const float p32 = d2f(f.p_mpa);
+  g.ld = __logf(d2f(f.A)) - (d2f(f.r.Ea_disl) * 1000.f + d2f(f.r.Va_disl) * p32) * inv_rt;
+  g.n = d2f(f.r.n_disl);
   g.peierls = f.r.A_p > 0.0 && f.T < 1200.0;
-  g.lp = g.peierls ? __logf((float)f.r.A_p) : 0.f;
-  g.a_p = (float)f.a_p;
-  g.m_p = (float)f.r.m_p;
-  g.n_p = (float)f.r.n_p;
-  g.inv_sp = (float)f.inv_sp;
+  g.lp = g.peierls ? __logf(d2f(f.r.A_p)) : 0.f;
+  g.a_p = d2f(f.a_p);
+  g.m_p = d2f(f.r.m_p);
+  g.n_p = d2f(f.r.n_p);
+  g.inv_sp = d2f(f.inv_sp);
   g.diff = f.r.A_diff > 0.0;
-  g.lf = g.diff ? __logf((float)f.r.A_diff) - ((float)f.r.Ea_diff * 1000.f + (float)f.r.Va_diff * (float)f.p_mpa) * inv_rt
-                : 0.f;
-  g.l2mdt = __logf((float)(2.0 * mdt));
-  g.cabs = (float)cabs;
+  g.lf = g.diff ? __logf(d2f(f.r.A_diff)) - (d2f(f.r.Ea_diff) * 1000.f + d2f(f.r.Va_diff) * p32) * inv_rt : 0.f;
+  g.l2mdt = __logf(2.f * d2f(mdt));
+  g.cabs = d2f(cabs);
   // The shortcuts below trust psi's sign only where |c| - s does not cancel in FP32 (s at
   // least 1 % below |c|; at or above |c|, phi > 0 holds exactly).
   constexpr float kMargin = 1e-3f;  // far above the FP32 evaluation error of psi there
-  float ul = __logf((float)lo), uh = __logf((float)hi);
+  float ul = __logf(d2f(lo)), uh = __logf(d2f(hi));
   const float pl = g.psi(ul), ph = g.psi(uh);
   if (lo >= cabs || (lo < 0.99 * cabs && pl > kMargin)) { sstar = 0.0; return true; }  // root well below lo
   if (hi < 0.99 * cabs && ph < -kMargin) { sstar = INFINITY; return true; }           // ... well above hi
@@ -231,7 +233,7 @@ __device__ bool flow_root(const FlowLaw& f, double mdt, double cabs, double lo, 
     const float um = 0.5f * (ul + uh);
     if (g.psi(um) > 0.f) uh = um; else ul = um;
   }
-  double s = (double)__expf(0.5f * (ul + uh));
+  double s = f2d(__expf(0.5f * (ul + uh)));
   double step = 0.0;
   for (int k = 0; k < 2; ++k) {
     double slope;

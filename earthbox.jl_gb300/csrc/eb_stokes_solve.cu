@@ -329,7 +329,8 @@ constexpr int kAx32Per = 2, kAx32Chunks = kAxThreads * kAx32Per;  // float4 chun
 // relative), forms the operator product and the Gram-Schmidt products from FMA-based exact
 // products (TwoProduct: p + e = a b exactly with e = fma(a, b, -p)) summed with Knuth's TwoSum
 // (the Dot2 scheme of Ogita, Rump & Oishi, SIAM J. Sci. Comput. 26, 2005), and converts with
-// integer operations; once its residual is small (gs_relax) it drops to plain FP32 vectors.
+// integer operations; once its residual is small (gs_relax) the Gram-Schmidt products drop to
+// FP32 on the hi parts.
 // Every kernel of the step then runs on the FP32 pipe and streams HBM; the Hessenberg matrix
 // and the Givens rotations stay FP64 on the host.  The _rn intrinsics keep the compiler from
 // contracting a product into a following sum, which would break the error-free transforms.
@@ -431,47 +432,6 @@ __global__ void __launch_bounds__(kB) k_apply_df(const float* __restrict__ ch, c
   if (hu) t(25, vy[c - 1]);
   t(26, vy[c]);
   out(2 * (int64_t)nc + c);
-}
-// The same in FP32 once the residual is small: d = ch x - vh, FP32 arithmetic.
-__global__ void __launch_bounds__(kB) k_apply32(const float* __restrict__ ch, const float* __restrict__ x,
-                                                const float* __restrict__ vh, float* __restrict__ dh, int32_t nx,
-                                                int32_t ny, int32_t nc) {
-  const int32_t c = (int32_t)(blockIdx.x * blockDim.x + threadIdx.x);
-  if (c >= nc) return;
-  const int32_t j = c / ny, i = c - j * ny;
-  const float *vx = x, *vy = x + nc, *p = x + 2 * (int64_t)nc;
-  const bool hu = i > 0, hd = i < ny - 1, hl = j > 0, hr = j < nx - 1;
-  auto cf = [&](int slot) { return __ldg(&ch[(int64_t)slot * nc + c]); };
-  float ax = cf(0) * vx[c];
-  if (hl) ax = fmaf(cf(1), vx[c - ny], ax);
-  if (hr) ax = fmaf(cf(2), vx[c + ny], ax);
-  if (hu) ax = fmaf(cf(3), vx[c - 1], ax);
-  if (hd) ax = fmaf(cf(4), vx[c + 1], ax);
-  if (hu) ax = fmaf(cf(5), vy[c - 1], ax);
-  if (hu && hr) ax = fmaf(cf(6), vy[c + ny - 1], ax);
-  ax = fmaf(cf(7), vy[c], ax);
-  if (hr) ax = fmaf(cf(8), vy[c + ny], ax);
-  ax = fmaf(cf(9), p[c], ax);
-  if (hr) ax = fmaf(cf(10), p[c + ny], ax);
-  float ay = cf(11) * vy[c];
-  if (hu) ay = fmaf(cf(12), vy[c - 1], ay);
-  if (hd) ay = fmaf(cf(13), vy[c + 1], ay);
-  if (hl) ay = fmaf(cf(14), vy[c - ny], ay);
-  if (hr) ay = fmaf(cf(15), vy[c + ny], ay);
-  if (hl) ay = fmaf(cf(16), vx[c - ny], ay);
-  ay = fmaf(cf(17), vx[c], ay);
-  if (hl && hd) ay = fmaf(cf(18), vx[c + 1 - ny], ay);
-  if (hd) ay = fmaf(cf(19), vx[c + 1], ay);
-  ay = fmaf(cf(20), p[c], ay);
-  if (hd) ay = fmaf(cf(21), p[c + 1], ay);
-  float ap = cf(22) * p[c];
-  if (hl) ap = fmaf(cf(23), vx[c - ny], ap);
-  ap = fmaf(cf(24), vx[c], ap);
-  if (hu) ap = fmaf(cf(25), vy[c - 1], ap);
-  ap = fmaf(cf(26), vy[c], ap);
-  dh[c] = ax - vh[c];
-  dh[nc + c] = ay - vh[nc + c];
-  dh[2 * (int64_t)nc + c] = ap - vh[2 * (int64_t)nc + c];
 }
 // dots: block (b, g) reduces a grid-stride slice of (Vh_v + Vl_v) . (Vh_{nv-1} + Vl_{nv-1}) for
 // v = G g .. G g + G - 1 (< nv) over float4 chunks, U chunks per thread and step; the last slot
@@ -621,10 +581,14 @@ __global__ void __launch_bounds__(kAxThreads) k_maxpy_df(const float* __restrict
     partial[blockIdx.x] = t;
   }
 }
-// FP32 form: u = uh - sum_v h[v] Vh_v in place (u the slot after the nv basis vectors);
+// FP32 projection once the residual is small: u = (uh + ul) - sum_v h[v] Vh_v in place (u the
+// slot after the nv basis vectors), the sum over the FP32 hi parts in FP32 and the update in
+// double-float, so that u keeps the accuracy of the operator product (d = A z - v cancels most
+// of A z: rounding d's own terms to FP32 first cost FGMRES iterations);
 // partial[block] = the block's sum of u^2.
-__global__ void __launch_bounds__(kAxThreads) k_maxpy32(float* __restrict__ V, int64_t ld, const double* __restrict__ h,
-                                                        int nv, double* __restrict__ partial) {
+__global__ void __launch_bounds__(kAxThreads) k_maxpy32(float* __restrict__ V, float* __restrict__ ulp, int64_t ld,
+                                                        const double* __restrict__ h, int nv,
+                                                        double* __restrict__ partial) {
   extern __shared__ float hs32[];
   for (int v = threadIdx.x; v < nv; v += blockDim.x) hs32[v] = d2f(h[v]);
   __syncthreads();
@@ -663,19 +627,27 @@ __global__ void __launch_bounds__(kAxThreads) k_maxpy32(float* __restrict__ V, i
 #pragma unroll
     for (int q = 0; q < kAx32Per; ++q)
       if (ok[q]) fma4(hs32[v], __ldcs(reinterpret_cast<const float4*>(V + (int64_t)v * ld) + ch[q]), acc[q]);
-  float ss = 0.f;
+  float4* ul = reinterpret_cast<float4*>(ulp);
+  float sh2 = 0.f, sl2 = 0.f;  // sum of u^2 as a pair
+  auto fin = [&](float& xh, float& xl, float a) {
+    float t = 0.f, e = 0.f;
+    two_sum_acc(xh, xl, t, e);
+    two_sum_acc(-a, 0.f, t, e);
+    df_norm(t, e, xh, xl);
+    df_fma_acc(xh, xl, xh, xl, sh2, sl2);
+  };
 #pragma unroll
   for (int q = 0; q < kAx32Per; ++q) {
     if (!ok[q]) continue;
-    float4 x = u[ch[q]];
-    x.x -= acc[q].x;
-    x.y -= acc[q].y;
-    x.z -= acc[q].z;
-    x.w -= acc[q].w;
-    u[ch[q]] = x;
-    ss += (x.x * x.x + x.y * x.y) + (x.z * x.z + x.w * x.w);
+    float4 xh = u[ch[q]], xl = ul[ch[q]];
+    fin(xh.x, xl.x, acc[q].x);
+    fin(xh.y, xl.y, acc[q].y);
+    fin(xh.z, xl.z, acc[q].z);
+    fin(xh.w, xl.w, acc[q].w);
+    u[ch[q]] = xh;
+    ul[ch[q]] = xl;
   }
-  double sd = f2d(ss);
+  double sd = f2d(sh2) + f2d(sl2);
   for (int o = 16; o > 0; o >>= 1) sd += __shfl_xor_sync(0xffffffffu, sd, o);
   __shared__ double sh[kAxThreads / 32];
   if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = sd;
@@ -686,14 +658,10 @@ __global__ void __launch_bounds__(kAxThreads) k_maxpy32(float* __restrict__ V, i
     partial[blockIdx.x] = t;
   }
 }
-// (vh + vl) *= ah + al in place, normalised; vl == nullptr: vh *= ah in FP32
+// (vh + vl) *= ah + al in place, normalised
 __global__ void k_scale_df(float* __restrict__ vh, float* __restrict__ vl, float ah, float al, int64_t n) {
   const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= n) return;
-  if (!vl) {
-    vh[k] *= ah;
-    return;
-  }
   const float xh = vh[k], xl = vl[k];
   const float p = __fmul_rn(xh, ah);
   const float e = fmaf(xl, ah, fmaf(xh, al, fmaf(xh, ah, -p)));
@@ -2024,11 +1992,11 @@ int maxpy_df(eb_ctx* c, StokesState* st, int nv, double* wn2) {
   EB_CK(c, cudaStreamSynchronize(c->stream));
   return EB_OK;
 }
-// the same on the FP32 hi parts in FP32
+// the same with the sum over the FP32 hi parts in FP32
 int maxpy32(eb_ctx* c, StokesState* st, int nv, double* wn2) {
   EB_PROF(c, "k_maxpy32");
-  k_maxpy32<<<st->nb_ax32, kAxThreads, (size_t)nv * sizeof(float), c->stream>>>(st->V32, st->ld32, st->hdev, nv,
-                                                                                st->part32);
+  k_maxpy32<<<st->nb_ax32, kAxThreads, (size_t)nv * sizeof(float), c->stream>>>(
+      st->V32, st->V32lo + (size_t)nv * st->ld32, st->ld32, st->hdev, nv, st->part32);
   EB_LAUNCHED(c);
   EB_PROF(c, "k_mdot_final");
   k_mdot_final<<<1, kB, 0, c->stream>>>(st->part32, st->nb_ax32, st->dots);
@@ -2242,8 +2210,8 @@ static int solve_once(eb_ctx* c, eb_solve_opts opt, bool stall_check, eb_solve_r
   int it = 0, reorth = 0, relaxed = 0;
   double est = 1.0;
   // The mixed method's FGMRES (without the learned stage or the GCR velocity stage) runs its
-  // Arnoldi step on split vectors: double-float until the residual estimate falls below
-  // gs_relax x the target, FP32 after that.  gs_relax < 0 keeps the FP64 step.
+  // Arnoldi step on split vectors in double-float; once the residual estimate falls below
+  // gs_relax x the target its Gram-Schmidt products are FP32.  gs_relax < 0 keeps the FP64 step.
   const double relax_fac = opt.gs_relax == 0.0 ? kGsRelax : opt.gs_relax;
   const bool split = !st->mg64 && relax_fac > 0.0 && !use_nn && st->gcr_steps <= 1;
   // The Krylov methods run on the scaled system, whose residual norm weights rows by W; the
@@ -2342,16 +2310,10 @@ static int solve_once(eb_ctx* c, eb_solve_opts opt, bool stall_check, eb_solve_r
         // with the norm measured in the update's pass, a second pass if the projection removed
         // all but 5% of the norm
         if ((rc = precondition32(c, st, vh, static_cast<float*>(zk)))) return rc;
-        if (relax) {
-          ++relaxed;
-          EB_PROF(c, "k_apply32");
-          k_apply32<<<nblk(s.nc), kB, 0, c->stream>>>(st->coefH, static_cast<float*>(zk), vh, wh, s.nx, s.ny,
-                                                      (int32_t)s.nc);
-        } else {
-          EB_PROF(c, "k_apply_df");
-          k_apply_df<<<nblk(s.nc), kB, 0, c->stream>>>(st->coefH, st->coefL, static_cast<float*>(zk), vh, vl, wh, wl,
-                                                       s.nx, s.ny, (int32_t)s.nc);
-        }
+        if (relax) ++relaxed;
+        EB_PROF(c, "k_apply_df");
+        k_apply_df<<<nblk(s.nc), kB, 0, c->stream>>>(st->coefH, st->coefL, static_cast<float*>(zk), vh, vl, wh, wl, s.nx,
+                                                     s.ny, (int32_t)s.nc);
         EB_LAUNCHED(c);
         auto dots = [&]() { return relax ? mdot32(c, st, k + 2, h.data()) : mdot_df(c, st, k + 2, h.data()); };
         if ((rc = dots())) return rc;
@@ -2429,10 +2391,9 @@ static int solve_once(eb_ctx* c, eb_solve_opts opt, bool stall_check, eb_solve_r
       if (hk1 > 0.0) {
         EB_PROF(c, "k_axpy");
         if (split) {
-          // 1 / hk1 as an FP32 pair (the FP32 form uses its hi part)
-          const double a = 1.0 / hk1;
+          const double a = 1.0 / hk1;  // as an FP32 pair
           const float ah = (float)a, al = (float)(a - (double)ah);
-          k_scale_df<<<nblk(n3), kB, 0, c->stream>>>(wh, relax ? nullptr : wl, ah, al, n3);
+          k_scale_df<<<nblk(n3), kB, 0, c->stream>>>(wh, wl, ah, al, n3);
         } else {
           k_scale_copy2<<<nblk(n3), kB, 0, c->stream>>>(w, w, 1.0 / hk1, n3);
         }
