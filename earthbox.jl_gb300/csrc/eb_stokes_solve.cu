@@ -319,7 +319,9 @@ __global__ void __launch_bounds__(kB) k_mdot32(const float* __restrict__ V, int6
     partial[(int64_t)(v0 + threadIdx.x) * gridDim.x + blockIdx.x] = t;
   }
 }
-constexpr int kAx32Per = 2, kAx32Chunks = kAxThreads * kAx32Per;  // float4 chunks per thread / block
+// float4 chunks per thread of the split-basis updates (template parameter P): 2 on long vectors,
+// 1 where two would leave the GPU's 152 SMs with few blocks
+constexpr int64_t kAxP2Chunks = (int64_t)152 * 8 * kAxThreads * 2;  // n/4 from which P = 2
 
 // ---- The mixed method's Arnoldi step in double-float ----
 // On this part the FP64 pipe (about 1.6 FMA per SM per clock, measured) also executes the
@@ -502,8 +504,9 @@ __global__ void __launch_bounds__(kB) k_mdot_df(const float* __restrict__ Vh, co
   }
 }
 // u = (uh + ul) - sum_v h[v] (Vh_v + Vl_v) in place (u the slot after the nv basis vectors),
-// normalised; partial[block] = the block's sum of u^2.  A thread owns kAx32Per float4 chunks of
+// normalised; partial[block] = the block's sum of u^2.  A thread owns P float4 chunks of
 // consecutive elements and streams four basis vectors at a time.
+template <int P>
 __global__ void __launch_bounds__(kAxThreads) k_maxpy_df(const float* __restrict__ Vh, const float* __restrict__ Vl,
                                                          int64_t ld, const double* __restrict__ h, int nv,
                                                          float* __restrict__ uhp, float* __restrict__ ulp,
@@ -514,12 +517,12 @@ __global__ void __launch_bounds__(kAxThreads) k_maxpy_df(const float* __restrict
   const int64_t n4 = ld >> 2;
   float4* uh = reinterpret_cast<float4*>(uhp);
   float4* ul = reinterpret_cast<float4*>(ulp);
-  int64_t ch[kAx32Per];
-  bool ok[kAx32Per];
-  float4 as[kAx32Per], ac[kAx32Per];
+  int64_t ch[P];
+  bool ok[P];
+  float4 as[P], ac[P];
 #pragma unroll
-  for (int q = 0; q < kAx32Per; ++q) {
-    ch[q] = (int64_t)blockIdx.x * kAx32Chunks + q * kAxThreads + threadIdx.x;
+  for (int q = 0; q < P; ++q) {
+    ch[q] = (int64_t)blockIdx.x * (kAxThreads * P) + q * kAxThreads + threadIdx.x;
     ok[q] = ch[q] < n4;
     as[q] = ac[q] = make_float4(0.f, 0.f, 0.f, 0.f);
   }
@@ -532,22 +535,22 @@ __global__ void __launch_bounds__(kAxThreads) k_maxpy_df(const float* __restrict
   };
   int v = 0;
   for (; v + 4 <= nv; v += 4) {
-    float4 xh[4][kAx32Per], xl[4][kAx32Per];
+    float4 xh[4][P], xl[4][P];
 #pragma unroll
     for (int g = 0; g < 4; ++g)
 #pragma unroll
-      for (int q = 0; q < kAx32Per; ++q) {
+      for (int q = 0; q < P; ++q) {
         xh[g][q] = ok[q] ? __ldcs(reinterpret_cast<const float4*>(Vh + (int64_t)(v + g) * ld) + ch[q]) : zero;
         xl[g][q] = ok[q] ? __ldcs(reinterpret_cast<const float4*>(Vl + (int64_t)(v + g) * ld) + ch[q]) : zero;
       }
 #pragma unroll
     for (int g = 0; g < 4; ++g)
 #pragma unroll
-      for (int q = 0; q < kAx32Per; ++q) acc4(hsd[v + g], hsd[nv + v + g], xh[g][q], xl[g][q], as[q], ac[q]);
+      for (int q = 0; q < P; ++q) acc4(hsd[v + g], hsd[nv + v + g], xh[g][q], xl[g][q], as[q], ac[q]);
   }
   for (; v < nv; ++v)
 #pragma unroll
-    for (int q = 0; q < kAx32Per; ++q)
+    for (int q = 0; q < P; ++q)
       if (ok[q])
         acc4(hsd[v], hsd[nv + v], __ldcs(reinterpret_cast<const float4*>(Vh + (int64_t)v * ld) + ch[q]),
              __ldcs(reinterpret_cast<const float4*>(Vl + (int64_t)v * ld) + ch[q]), as[q], ac[q]);
@@ -560,7 +563,7 @@ __global__ void __launch_bounds__(kAxThreads) k_maxpy_df(const float* __restrict
     df_fma_acc(xh, xl, xh, xl, sh2, sl2);
   };
 #pragma unroll
-  for (int q = 0; q < kAx32Per; ++q) {
+  for (int q = 0; q < P; ++q) {
     if (!ok[q]) continue;
     float4 xh = uh[ch[q]], xl = ul[ch[q]];
     fin(xh.x, xl.x, as[q].x, ac[q].x);
@@ -586,6 +589,7 @@ __global__ void __launch_bounds__(kAxThreads) k_maxpy_df(const float* __restrict
 // double-float, so that u keeps the accuracy of the operator product (d = A z - v cancels most
 // of A z: rounding d's own terms to FP32 first cost FGMRES iterations);
 // partial[block] = the block's sum of u^2.
+template <int P>
 __global__ void __launch_bounds__(kAxThreads) k_maxpy32(float* __restrict__ V, float* __restrict__ ulp, int64_t ld,
                                                         const double* __restrict__ h, int nv,
                                                         double* __restrict__ partial) {
@@ -594,12 +598,12 @@ __global__ void __launch_bounds__(kAxThreads) k_maxpy32(float* __restrict__ V, f
   __syncthreads();
   const int64_t n4 = ld >> 2;
   float4* u = reinterpret_cast<float4*>(V + (int64_t)nv * ld);
-  int64_t ch[kAx32Per];
-  bool ok[kAx32Per];
-  float4 acc[kAx32Per];
+  int64_t ch[P];
+  bool ok[P];
+  float4 acc[P];
 #pragma unroll
-  for (int q = 0; q < kAx32Per; ++q) {
-    ch[q] = (int64_t)blockIdx.x * kAx32Chunks + q * kAxThreads + threadIdx.x;
+  for (int q = 0; q < P; ++q) {
+    ch[q] = (int64_t)blockIdx.x * (kAxThreads * P) + q * kAxThreads + threadIdx.x;
     ok[q] = ch[q] < n4;
     acc[q] = make_float4(0.f, 0.f, 0.f, 0.f);
   }
@@ -612,20 +616,20 @@ __global__ void __launch_bounds__(kAxThreads) k_maxpy32(float* __restrict__ V, f
   };
   int v = 0;
   for (; v + 4 <= nv; v += 4) {
-    float4 x[4][kAx32Per];
+    float4 x[4][P];
 #pragma unroll
     for (int g = 0; g < 4; ++g)
 #pragma unroll
-      for (int q = 0; q < kAx32Per; ++q)
+      for (int q = 0; q < P; ++q)
         x[g][q] = ok[q] ? __ldcs(reinterpret_cast<const float4*>(V + (int64_t)(v + g) * ld) + ch[q]) : zero;
 #pragma unroll
     for (int g = 0; g < 4; ++g)
 #pragma unroll
-      for (int q = 0; q < kAx32Per; ++q) fma4(hs32[v + g], x[g][q], acc[q]);
+      for (int q = 0; q < P; ++q) fma4(hs32[v + g], x[g][q], acc[q]);
   }
   for (; v < nv; ++v)
 #pragma unroll
-    for (int q = 0; q < kAx32Per; ++q)
+    for (int q = 0; q < P; ++q)
       if (ok[q]) fma4(hs32[v], __ldcs(reinterpret_cast<const float4*>(V + (int64_t)v * ld) + ch[q]), acc[q]);
   float4* ul = reinterpret_cast<float4*>(ulp);
   float sh2 = 0.f, sl2 = 0.f;  // sum of u^2 as a pair
@@ -637,7 +641,7 @@ __global__ void __launch_bounds__(kAxThreads) k_maxpy32(float* __restrict__ V, f
     df_fma_acc(xh, xl, xh, xl, sh2, sl2);
   };
 #pragma unroll
-  for (int q = 0; q < kAx32Per; ++q) {
+  for (int q = 0; q < P; ++q) {
     if (!ok[q]) continue;
     float4 xh = u[ch[q]], xl = ul[ch[q]];
     fin(xh.x, xl.x, acc[q].x);
@@ -1390,7 +1394,8 @@ struct StokesState {
   float* V32lo = nullptr;            // their remainders: the basis as double-float pairs
   int64_t ld32 = 0;
   double* part32 = nullptr;          // per-block norms of k_maxpy32 / k_maxpy_df
-  int nb_ax32 = 0;
+  int nb_ax32 = 0, ax_p = 2;          // blocks and float4 chunks per thread of the split updates
+  int nb_split = 0;                  // blocks per vector group of the split dot products
   double* il = nullptr;              // interleaved staging vector (N)
   double* tmp = nullptr;             // scratch vector (N)
   double *nn_t = nullptr, *nn_q = nullptr, *nn_z = nullptr;  // learned-stage scratch: [t | q], z2
@@ -1941,11 +1946,13 @@ int precondition32(eb_ctx* c, StokesState* st, const float* rh, float* Zk) {
 // dots[v] = V_v . u for v < nv (device), copied to host h
 int mdot(eb_ctx* c, StokesState* st, const double* V, int64_t stride, int nv, const double* u, double* h) {
   const int64_t n3 = 3 * st->sys.nc;
+  // blocks per vector: at least 8 elements per thread, at most kDotBlocks
+  const int nb = (int)std::min<int64_t>(st->nb_dot, std::max<int64_t>(1, (n3 + 8 * kB - 1) / (8 * kB)));
   EB_PROF(c, "k_mdot");
-  k_mdot<<<dim3(st->nb_dot, nv), kB, 0, c->stream>>>(V, stride, u, n3, st->partial);
+  k_mdot<<<dim3(nb, nv), kB, 0, c->stream>>>(V, stride, u, n3, st->partial);
   EB_LAUNCHED(c);
   EB_PROF(c, "k_mdot");
-  k_mdot_final<<<nv, kB, 0, c->stream>>>(st->partial, st->nb_dot, st->dots);
+  k_mdot_final<<<nv, kB, 0, c->stream>>>(st->partial, nb, st->dots);
   EB_LAUNCHED(c);
   EB_CK(c, cudaMemcpyAsync(h, st->dots, nv * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
   EB_CK(c, cudaStreamSynchronize(c->stream));
@@ -1955,11 +1962,11 @@ int mdot(eb_ctx* c, StokesState* st, const double* V, int64_t stride, int nv, co
 // h[v] = V32_v . V32_{nv-1} for v < nv (the last slot holds the FP32 copy of the new direction)
 int mdot32(eb_ctx* c, StokesState* st, int nv, double* h) {
   EB_PROF(c, "k_mdot32");
-  k_mdot32<<<dim3(st->nb_dot, (nv + kDot32Vecs - 1) / kDot32Vecs), kB, 0, c->stream>>>(
+  k_mdot32<<<dim3(st->nb_split, (nv + kDot32Vecs - 1) / kDot32Vecs), kB, 0, c->stream>>>(
       st->V32, st->ld32, st->V32 + (size_t)(nv - 1) * st->ld32, st->ld32 / 4, nv, st->partial);
   EB_LAUNCHED(c);
   EB_PROF(c, "k_mdot_final");
-  k_mdot_final<<<nv, kB, 0, c->stream>>>(st->partial, st->nb_dot, st->dots);
+  k_mdot_final<<<nv, kB, 0, c->stream>>>(st->partial, st->nb_split, st->dots);
   EB_LAUNCHED(c);
   EB_CK(c, cudaMemcpyAsync(h, st->dots, nv * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
   EB_CK(c, cudaStreamSynchronize(c->stream));
@@ -1968,11 +1975,11 @@ int mdot32(eb_ctx* c, StokesState* st, int nv, double* h) {
 // h[v] = V_v . V_{nv-1} for v < nv on the split basis (slot nv-1 holds the new direction)
 int mdot_df(eb_ctx* c, StokesState* st, int nv, double* h) {
   EB_PROF(c, "k_mdot_df");
-  k_mdot_df<<<dim3(st->nb_dot, (nv + kDfVecs - 1) / kDfVecs), kB, 0, c->stream>>>(st->V32, st->V32lo, st->ld32,
-                                                                                  st->ld32 / 4, nv, st->partial);
+  k_mdot_df<<<dim3(st->nb_split, (nv + kDfVecs - 1) / kDfVecs), kB, 0, c->stream>>>(st->V32, st->V32lo, st->ld32,
+                                                                                    st->ld32 / 4, nv, st->partial);
   EB_LAUNCHED(c);
   EB_PROF(c, "k_mdot_final");
-  k_mdot_final<<<nv, kB, 0, c->stream>>>(st->partial, st->nb_dot, st->dots);
+  k_mdot_final<<<nv, kB, 0, c->stream>>>(st->partial, st->nb_split, st->dots);
   EB_LAUNCHED(c);
   EB_CK(c, cudaMemcpyAsync(h, st->dots, nv * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
   EB_CK(c, cudaStreamSynchronize(c->stream));
@@ -1981,7 +1988,8 @@ int mdot_df(eb_ctx* c, StokesState* st, int nv, double* h) {
 // slot nv -= sum_{v<nv} hdev[v] V_v on the split basis (double-float); *wn2 = |slot nv|^2
 int maxpy_df(eb_ctx* c, StokesState* st, int nv, double* wn2) {
   EB_PROF(c, "k_maxpy_df");
-  k_maxpy_df<<<st->nb_ax32, kAxThreads, (size_t)2 * nv * sizeof(float), c->stream>>>(
+  auto kern = st->ax_p == 2 ? k_maxpy_df<2> : k_maxpy_df<1>;
+  kern<<<st->nb_ax32, kAxThreads, (size_t)2 * nv * sizeof(float), c->stream>>>(
       st->V32, st->V32lo, st->ld32, st->hdev, nv, st->V32 + (size_t)nv * st->ld32, st->V32lo + (size_t)nv * st->ld32,
       st->part32);
   EB_LAUNCHED(c);
@@ -1995,7 +2003,8 @@ int maxpy_df(eb_ctx* c, StokesState* st, int nv, double* wn2) {
 // the same with the sum over the FP32 hi parts in FP32
 int maxpy32(eb_ctx* c, StokesState* st, int nv, double* wn2) {
   EB_PROF(c, "k_maxpy32");
-  k_maxpy32<<<st->nb_ax32, kAxThreads, (size_t)nv * sizeof(float), c->stream>>>(
+  auto kern = st->ax_p == 2 ? k_maxpy32<2> : k_maxpy32<1>;
+  kern<<<st->nb_ax32, kAxThreads, (size_t)nv * sizeof(float), c->stream>>>(
       st->V32, st->V32lo + (size_t)nv * st->ld32, st->ld32, st->hdev, nv, st->part32);
   EB_LAUNCHED(c);
   EB_PROF(c, "k_mdot_final");
@@ -2042,7 +2051,11 @@ int ensure_solver(eb_ctx* c, StokesState* st, int m) {
   if (!st->mg64 && !st->Z && (rc = dalloc(c, st->allocs, &st->Z, (size_t)m * n3))) return rc;
   if (!st->mg64 && !st->V32) {  // FP32 basis copies, zero padding between the slots
     st->ld32 = (int64_t)((n3 + 3) & ~(size_t)3);
-    st->nb_ax32 = (int)((st->ld32 / 4 + kAx32Chunks - 1) / kAx32Chunks);
+    const int64_t n4 = st->ld32 / 4;
+    st->ax_p = n4 >= kAxP2Chunks ? 2 : 1;
+    st->nb_ax32 = (int)((n4 + kAxThreads * st->ax_p - 1) / (kAxThreads * st->ax_p));
+    // dot-product blocks per group of basis vectors: at least 8 float4 chunks per thread
+    st->nb_split = (int)std::min<int64_t>(kDotBlocks, std::max<int64_t>(1, (n4 + 8 * kB - 1) / (8 * kB)));
     if ((rc = dalloc(c, st->allocs, &st->V32, (size_t)(m + 2) * st->ld32))) return rc;
     EB_CK(c, cudaMemsetAsync(st->V32, 0, (size_t)(m + 2) * st->ld32 * sizeof(float), c->stream));
     drop(st->V32lo);
