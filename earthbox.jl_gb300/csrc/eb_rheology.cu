@@ -246,6 +246,34 @@ __device__ bool flow_root(const FlowLaw& f, double mdt, double cabs, double lo, 
   return isfinite(s) && s > 0.0 && fabs(step) <= 1e-9 * s;
 }
 
+// The bisection's bookkeeping on positive finite doubles in integer form, decided exactly as
+// the FP64 operations would be: the comparisons compare bit patterns (integer order is numeric
+// order for positive doubles), halving a sum subtracts one from its exponent, and
+// |b - a| > 1 uses the exact difference (Sterbenz: within a factor of 2 the FP64 difference is
+// exact; farther apart it exceeds b / 2, above 1 once b >= 4).  Comparisons, multiplications
+// and differences of doubles all issue on the FP64 pipe, which bounds this kernel.
+__device__ __forceinline__ int64_t dbits(double x) { return __double_as_longlong(x); }
+__device__ __forceinline__ bool gap_above_one(double a, double b) {
+  int64_t ia = dbits(a), ib = dbits(b);
+  if (ia > ib) {
+    const int64_t t = ia; ia = ib; ib = t;
+  }
+  // below Sterbenz's range (2a < b) the difference exceeds b / 2
+  if (ia + ((int64_t)1 << 52) < ib) return ib >= 0x4010000000000000LL /* 4.0 */ || fabs(b - a) > 1.0;
+  const int32_t ea = (int32_t)(ia >> 52), eb = (int32_t)(ib >> 52);
+  const int64_t one = (int64_t)1 << 52;
+  const int64_t ma = (ia & (one - 1)) | one, mb = (ib & (one - 1)) | one;
+  const int64_t D = (mb << (eb - ea)) - ma;  // b - a in units of 2^(ea - 1075), exact
+  const int sh = 1075 - ea;                  // D 2^-sh > 1  <=>  D > 2^sh
+  if (sh < 0) return D > 0;
+  if (sh >= 62) return false;
+  return D > ((int64_t)1 << sh);
+}
+__device__ __forceinline__ bool pos_normal(double x) {
+  const int64_t b = dbits(x);
+  return b >= ((int64_t)1 << 52) && b < 0x7FF0000000000000LL;
+}
+
 __device__ __forceinline__ void d_flow_viscosity(const DevMarkers& mk, const DevMats& mt, const RheoParams& P, int64_t m) {
   const int32_t id = mk.matid[m];
   const int32_t ft = __ldg(&mt.flow_type[id - 1]);
@@ -293,21 +321,26 @@ __device__ __forceinline__ void d_flow_viscosity(const DevMarkers& mk, const Dev
     const double cc = cxx * cxx + cxy * cxy;
     FlowLaw fl{r, A, p_mpa, T, P.R, inv_sp, e_disl, a_p, e_diff};
     double sstar;
-    if (flow_root(fl, mdt, sqrt(cc), fmin(s0, sf), fmax(s0, sf), sstar)) {
-      const int64_t kr = __double_as_longlong(sstar);
-      double savg = s0;
-      while (icount < 20 && delta > 1.0) {
+    if (pos_normal(s0) && pos_normal(sf) && P.s_min >= 0.0 &&
+        flow_root(fl, mdt, sqrt(cc), fmin(s0, sf), fmax(s0, sf), sstar)) {
+      const int64_t kr = dbits(sstar), kmin = dbits(P.s_min);
+      int64_t i0 = dbits(s0), i1 = dbits(sf);
+      bool more = true;  // delta = 1e39 > 1 before the first step
+      int64_t iavg = i0;
+      while (icount < 20 && more) {
         ++icount;
-        savg = (s0 + sf) / 2.0;
-        const int64_t dist = __double_as_longlong(savg) - kr;
+        // (s0 + sf) / 2: the sum in FP64, halved exactly in the exponent
+        iavg = dbits(__longlong_as_double(i0) + __longlong_as_double(i1)) - ((int64_t)1 << 52);
+        const int64_t dist = iavg - kr;
         bool above, below;
         if (dist > kBandUlps) {
           above = false;
-          below = P.s_min < savg;
+          below = kmin < iavg;
         } else if (dist < -kBandUlps) {
           above = true;
           below = false;
         } else {  // within the band: the reference's own test
+          const double savg = __longlong_as_double(iavg);
           s_mpa = savg * kPaToMPa;
           rate = rate_at(fl, s_mpa);
           const double a = 0.5 * (s_mpa * 1e6);
@@ -316,11 +349,11 @@ __device__ __forceinline__ void d_flow_viscosity(const DevMarkers& mk, const Dev
           above = lhs > rhs;
           below = lhs < rhs && P.s_min < savg;
         }
-        if ((sf > s0 && above) || (sf < s0 && below)) s0 = savg;
-        else sf = savg;
-        delta = fabs(sf - s0);
+        if ((i1 > i0 && above) || (i1 < i0 && below)) i0 = iavg;
+        else i1 = iavg;
+        more = gap_above_one(__longlong_as_double(i0), __longlong_as_double(i1));
       }
-      s_mpa = savg * kPaToMPa;
+      s_mpa = __longlong_as_double(iavg) * kPaToMPa;
       rate = rate_at(fl, s_mpa);
     } else while (icount < 20 && delta > 1.0) {
       ++icount;
