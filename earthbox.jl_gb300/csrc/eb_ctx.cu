@@ -791,13 +791,34 @@ extern "C" int eb_checkpoint_read(eb_ctx* c, const char* path) {
     return fail(std::string(path) + " is not an eb checkpoint");
   if (head[0] != 1) return fail("unsupported checkpoint version");
   if (head[1] != c->xnum || head[2] != c->ynum) return fail("checkpoint grid differs from the context's grid");
-  if (head[3] != c->M) {
-    fclose(fp);
-    int rc = eb_resize_markers(c, head[3]);
-    if (rc) return rc;
-    fp = std::fopen(path, "rb");
-    if (!fp || std::fseek(fp, 8 + (long)sizeof(head), SEEK_SET) != 0) return fail("cannot reopen the checkpoint");
+  // Validate every entry header and size before the context changes: a truncated or
+  // mismatched file then leaves the context as it was.
+  if (std::fseek(fp, 0, SEEK_END) != 0) return fail("cannot read the checkpoint");
+  const long fsize = std::ftell(fp);
+  const long data0 = 8 + (long)sizeof(head);
+  if (fsize < data0 || std::fseek(fp, data0, SEEK_SET) != 0) return fail("truncated checkpoint");
+  const int64_t Mck = head[3];
+  if (Mck < 0) return fail("bad checkpoint marker count");
+  for (int64_t k = 0; k < head[4]; ++k) {
+    int32_t kf[2];
+    int64_t bytes;
+    if (std::fread(kf, sizeof(kf), 1, fp) != 1 || std::fread(&bytes, sizeof(bytes), 1, fp) != 1)
+      return fail("truncated checkpoint");
+    const int kind = kf[0], f = kf[1];
+    if (kind != 0 && kind != 1) return fail("bad checkpoint entry");
+    if ((kind == 0 && (f < 0 || f >= EB_M_NFIELDS)) || (kind == 1 && (f < 0 || f >= EB_G_NFIELDS)))
+      return fail("checkpoint field id out of range");
+    const int64_t want = kind == 0 ? Mck * (int64_t)marker_elem_size(f) : (int64_t)(grid_field_count(c, f) * sizeof(double));
+    if (bytes != want) return fail("checkpoint field size differs from the context's");
+    const long pos = std::ftell(fp);
+    if (pos < 0 || bytes > (int64_t)(fsize - pos) || std::fseek(fp, (long)bytes, SEEK_CUR) != 0)
+      return fail("truncated checkpoint");
   }
+  if (head[3] != c->M) {
+    int rc = eb_resize_markers(c, head[3]);
+    if (rc) { std::fclose(fp); return rc; }
+  }
+  if (std::fseek(fp, data0, SEEK_SET) != 0) return fail("cannot reread the checkpoint");
   std::vector<char> buf;
   bool matid = false;
   for (int64_t k = 0; k < head[4]; ++k) {

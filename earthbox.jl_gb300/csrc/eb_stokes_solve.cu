@@ -1051,6 +1051,29 @@ __global__ void k_rbgs(LevelDev<T> v, int comp, int color) {
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (t < rb_count(v)) d_rbgs(v, t, comp, color);
 }
+// The first half-sweep of a level (vx, red) from a zero start: u_x = f_x / diag on the red
+// cells (every neighbour is zero), and the zero start written to the rest of u_x and u_y, so
+// that no memset precedes the sweep.  Thread t owns the t-th red and the t-th black cell.
+template <class T>
+__global__ void k_rbgs_first(LevelDev<T> v) {
+  wait_prior_grid();
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= rb_count(v)) return;
+  const int32_t half = (v.ny + 1) / 2;
+  const int32_t j = (int32_t)t / half;
+  const int32_t q = (int32_t)t - j * half;
+  const int32_t ir = 2 * q + (j & 1), ib = 2 * q + ((j + 1) & 1);
+  if (ir < v.ny) {
+    const int64_t c = (int64_t)j * v.ny + ir;
+    v.ux[c] = v.fx[c] / v.X[c];
+    v.uy[c] = T(0);
+  }
+  if (ib < v.ny) {
+    const int64_t c = (int64_t)j * v.ny + ib;
+    v.ux[c] = T(0);
+    v.uy[c] = T(0);
+  }
+}
 template <class T>
 __global__ void k_resid(LevelDev<T> v) {
   wait_prior_grid();
@@ -1740,10 +1763,15 @@ int vcycle_launch(eb_ctx* c, StokesState* st, int sweeps, int64_t* nk, bool pdl)
   };
   for (int l = 0; l < l0; ++l) {
     const LevelDev<T> v = level_dev<T>(L[l]);
-    EB_CK(c, cudaMemsetAsync(L[l].ux, 0, v.nc * sizeof(T), c->stream));
-    EB_CK(c, cudaMemsetAsync(L[l].uy, 0, v.nc * sizeof(T), c->stream));
     for (int s = 0; s < sweeps; ++s)
-      for (int k = 0; k < 4; ++k) EB_CK(c, rb(v, k >> 1, k & 1));
+      for (int k = 0; k < 4; ++k) {
+        if (s == 0 && k == 0) {  // zero start folded into the first half-sweep
+          const int64_t cnt = (int64_t)v.nx * ((v.ny + 1) / 2);
+          EB_CK(c, launch(k_rbgs_first<T>, nblk(cnt), kB, v));
+        } else {
+          EB_CK(c, rb(v, k >> 1, k & 1));
+        }
+      }
     EB_CK(c, launch(k_resid<T>, nblk(v.nc), kB, v));
     const LevelDev<T> w = level_dev<T>(L[l + 1]);
     EB_CK(c, launch(k_restrict<T>, nblk(w.nc), kB, v, w));

@@ -717,7 +717,10 @@ int eb_learned_stats(eb_ctx* ctx, int64_t* accepted, int64_t* rejected, double* 
  * holds in one file (a header with the grid size and marknum, then each field's bytes in
  * that same layout), so a GPU run can stop and resume without the host model.  Reading
  * needs eb_set_grid with the same grid (markers are resized to the file's marknum); the
- * next eb_initialize_bilinear_interpolation rebuilds the cell sort.                   */
+ * next eb_initialize_bilinear_interpolation rebuilds the cell sort.  The file's headers
+ * and sizes are all checked before anything changes: a truncated or mismatched file
+ * returns EB_BAD_INPUT with the context untouched.  Fields the context holds that the file
+ * does not are left as they were (a file written by eb_checkpoint_write holds them all). */
 int eb_checkpoint_write(eb_ctx* ctx, const char* path);
 int eb_checkpoint_read(eb_ctx* ctx, const char* path);
 

@@ -46,3 +46,27 @@ def test_checkpoint_of_another_grid_is_refused(eb, tmp_path):
         b.checkpoint_read(tmp_path / "junk")
     a.close()
     b.close()
+
+
+def test_truncated_checkpoint_leaves_the_context_untouched(eb, tmp_path):
+    """Every entry header and size is checked before the context changes: a file cut short
+    (here in its last field) is refused, and the context keeps its markers and fields."""
+    a = eb.MarkerInCell(0)
+    a.load_model(eb.synthetic.config("rift_small"))
+    path = tmp_path / "state.ebck"
+    a.checkpoint_write(path)
+    data = path.read_bytes()
+    cut = tmp_path / "cut.ebck"
+    cut.write_bytes(data[:-100])
+    b = eb.MarkerInCell(0)
+    small = eb.synthetic.config("rift_small")
+    b.load_model(small)
+    b.marker_cycle()
+    before = {k: b.download_marker(k) for k in FIELDS}
+    with pytest.raises(RuntimeError, match="truncated"):
+        b.checkpoint_read(cut)
+    assert b.marknum == small.marknum
+    for k in FIELDS:
+        assert np.array_equal(b.download_marker(k), before[k]), k
+    a.close()
+    b.close()
