@@ -47,6 +47,49 @@ constexpr int kMaxDots = kMaxRestart + 8;  // dot products per reduction
 
 unsigned nblk(int64_t n) { return (unsigned)((n + kB - 1) / kB); }
 
+// ---- double-float helpers (the mixed method's Krylov vectors, below) ----
+// x = hi + lo: hi = x rounded to FP32 (d2f), lo = x - hi rounded to FP32, by integer
+// operations; |x - hi - lo| <= 2^-48 |x|.  Magnitudes below 2^-74 keep hi alone (the
+// dropped lo is below 2^-98), below FLT_MIN both are zero; above FLT_MAX, and NaN, hi is
+// infinite.
+EB_DEV void split_df(double x, float& hi, float& lo) {
+  const uint32_t H = (uint32_t)__double2hiint(x), L = (uint32_t)__double2loint(x);
+  const uint32_t e = (H >> 20) & 0x7FFu;
+  hi = d2f(x);
+  // the 29 significand bits below hi's last place, as a signed count of units 2^(e - 1075):
+  // r, or r - 2^29 when d2f rounded the magnitude up (bit 28 set)
+  const int32_t r = (int32_t)(L & 0x1FFFFFFFu);
+  const int32_t t = ((L >> 28) & 1u) ? r - (1 << 29) : r;
+  const float mag = __fmul_rn(__int2float_rn(t), __uint_as_float((e - 948u) << 23));  // exact: power of 2
+  lo = (e >= 949u && e <= 1150u) ? __uint_as_float(__float_as_uint(mag) ^ (H & 0x80000000u)) : 0.f;
+}
+// (s, c) += p + e (TwoSum of s and p; e and the rounding error go to c)
+EB_DEV void two_sum_acc(float p, float e, float& s, float& c) {
+  const float t = __fadd_rn(s, p);
+  const float z = __fsub_rn(t, s);
+  c = __fadd_rn(c, __fadd_rn(__fadd_rn(__fsub_rn(s, __fsub_rn(t, z)), __fsub_rn(p, z)), e));
+  s = t;
+}
+// (s, c) += (ah + al) x for an FP32 x
+EB_DEV void df_axpy_acc(float ah, float al, float x, float& s, float& c) {
+  const float p = __fmul_rn(ah, x);
+  const float e = fmaf(al, x, fmaf(ah, x, -p));
+  two_sum_acc(p, e, s, c);
+}
+// (s, c) += (ah + al)(bh + bl), the al bl term dropped
+EB_DEV void df_fma_acc(float ah, float al, float bh, float bl, float& s, float& c) {
+  const float p = __fmul_rn(ah, bh);
+  const float e = fmaf(al, bh, fmaf(ah, bl, fmaf(ah, bh, -p)));
+  two_sum_acc(p, e, s, c);
+}
+// normalised pair h + l = s + c with |l| <= ulp(h) / 2 (TwoSum)
+EB_DEV void df_norm(float s, float c, float& h, float& l) {
+  h = __fadd_rn(s, c);
+  const float z = __fsub_rn(h, s);
+  l = __fadd_rn(__fsub_rn(s, __fsub_rn(h, z)), __fsub_rn(c, z));
+}
+
+
 // ------------------------------------------------------- FP64 operator ---
 // y = L x on SoA vectors [vx | vy | p] (cell c = j ny + i), optionally y -= sub and an FP32
 // copy y32.  The FGMRES iteration passes the pre-scaled stencil W L W (k_prescale), the
@@ -305,12 +348,20 @@ __global__ void __launch_bounds__(kB) k_mdot32(const float* __restrict__ V, int6
     for (int g = 0; g < kDot32Vecs; ++g)
       if (g < nvb) acc4(__ldcs(a[g] + k), u0, s[g]);
   }
+  // lanes and warp reduced as double-float pairs on the FP32 pipe (an FP64 reduction would
+  // convert on the FP64 pipe); the block's eight warp sums are added in FP64
   __shared__ double sh[kDot32Vecs][kB / 32];
 #pragma unroll
   for (int g = 0; g < kDot32Vecs; ++g) {
-    double t = ((double)s[g].x + (double)s[g].y) + ((double)s[g].z + (double)s[g].w);
-    for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
-    if ((threadIdx.x & 31) == 0) sh[g][threadIdx.x >> 5] = t;
+    float S = s[g].x, C = 0.f;
+    two_sum_acc(s[g].y, 0.f, S, C);
+    two_sum_acc(s[g].z, 0.f, S, C);
+    two_sum_acc(s[g].w, 0.f, S, C);
+    for (int o = 16; o > 0; o >>= 1) {
+      const float s2 = __shfl_xor_sync(0xffffffffu, S, o), c2 = __shfl_xor_sync(0xffffffffu, C, o);
+      two_sum_acc(s2, c2, S, C);
+    }
+    if ((threadIdx.x & 31) == 0) sh[g][threadIdx.x >> 5] = f2d(S) + f2d(C);
   }
   __syncthreads();
   if ((int)threadIdx.x < nvb) {
@@ -336,47 +387,6 @@ constexpr int64_t kAxP2Chunks = (int64_t)152 * 8 * kAxThreads * 2;  // n/4 from 
 // Every kernel of the step then runs on the FP32 pipe and streams HBM; the Hessenberg matrix
 // and the Givens rotations stay FP64 on the host.  The _rn intrinsics keep the compiler from
 // contracting a product into a following sum, which would break the error-free transforms.
-
-// x = hi + lo: hi = x rounded to FP32 (d2f), lo = x - hi rounded to FP32, by integer
-// operations; |x - hi - lo| <= 2^-48 |x|.  Magnitudes below 2^-74 keep hi alone (the
-// dropped lo is below 2^-98), below FLT_MIN both are zero; above FLT_MAX, and NaN, hi is
-// infinite.
-EB_DEV void split_df(double x, float& hi, float& lo) {
-  const uint32_t H = (uint32_t)__double2hiint(x), L = (uint32_t)__double2loint(x);
-  const uint32_t e = (H >> 20) & 0x7FFu;
-  hi = d2f(x);
-  // the 29 significand bits below hi's last place, as a signed count of units 2^(e - 1075):
-  // r, or r - 2^29 when d2f rounded the magnitude up (bit 28 set)
-  const int32_t r = (int32_t)(L & 0x1FFFFFFFu);
-  const int32_t t = ((L >> 28) & 1u) ? r - (1 << 29) : r;
-  const float mag = __fmul_rn(__int2float_rn(t), __uint_as_float((e - 948u) << 23));  // exact: power of 2
-  lo = (e >= 949u && e <= 1150u) ? __uint_as_float(__float_as_uint(mag) ^ (H & 0x80000000u)) : 0.f;
-}
-// (s, c) += p + e (TwoSum of s and p; e and the rounding error go to c)
-EB_DEV void two_sum_acc(float p, float e, float& s, float& c) {
-  const float t = __fadd_rn(s, p);
-  const float z = __fsub_rn(t, s);
-  c = __fadd_rn(c, __fadd_rn(__fadd_rn(__fsub_rn(s, __fsub_rn(t, z)), __fsub_rn(p, z)), e));
-  s = t;
-}
-// (s, c) += (ah + al) x for an FP32 x
-EB_DEV void df_axpy_acc(float ah, float al, float x, float& s, float& c) {
-  const float p = __fmul_rn(ah, x);
-  const float e = fmaf(al, x, fmaf(ah, x, -p));
-  two_sum_acc(p, e, s, c);
-}
-// (s, c) += (ah + al)(bh + bl), the al bl term dropped
-EB_DEV void df_fma_acc(float ah, float al, float bh, float bl, float& s, float& c) {
-  const float p = __fmul_rn(ah, bh);
-  const float e = fmaf(al, bh, fmaf(ah, bl, fmaf(ah, bh, -p)));
-  two_sum_acc(p, e, s, c);
-}
-// normalised pair h + l = s + c with |l| <= ulp(h) / 2 (TwoSum)
-EB_DEV void df_norm(float s, float c, float& h, float& l) {
-  h = __fadd_rn(s, c);
-  const float z = __fsub_rn(h, s);
-  l = __fadd_rn(__fsub_rn(s, __fsub_rn(h, z)), __fsub_rn(c, z));
-}
 
 // d = (W L W) x - v_k for the mixed method: x = Z_k (FP32, exact), the stencil as the pair
 // ch + cl, v_k = vh + vl; d is written as the normalised pair (dh, dl).  Same cells, slots
@@ -488,13 +498,20 @@ __global__ void __launch_bounds__(kB) k_mdot_df(const float* __restrict__ Vh, co
     for (int g = 0; g < G; ++g)
       if (g < nvb) acc4(__ldcs(ah[g] + k), __ldcs(al[g] + k), yh, yl, s[g], cs[g]);
   }
+  // the thread's four lanes and then the warp reduced as double-float pairs (FP32 pipe); only
+  // the eight warp sums of the block are added in FP64
   __shared__ double sh[G][kB / 32];
 #pragma unroll
   for (int g = 0; g < G; ++g) {
-    double t = ((f2d(s[g].x) + f2d(cs[g].x)) + (f2d(s[g].y) + f2d(cs[g].y))) +
-               ((f2d(s[g].z) + f2d(cs[g].z)) + (f2d(s[g].w) + f2d(cs[g].w)));
-    for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
-    if ((threadIdx.x & 31) == 0) sh[g][threadIdx.x >> 5] = t;
+    float S = s[g].x, C = cs[g].x;
+    two_sum_acc(s[g].y, cs[g].y, S, C);
+    two_sum_acc(s[g].z, cs[g].z, S, C);
+    two_sum_acc(s[g].w, cs[g].w, S, C);
+    for (int o = 16; o > 0; o >>= 1) {
+      const float s2 = __shfl_xor_sync(0xffffffffu, S, o), c2 = __shfl_xor_sync(0xffffffffu, C, o);
+      two_sum_acc(s2, c2, S, C);
+    }
+    if ((threadIdx.x & 31) == 0) sh[g][threadIdx.x >> 5] = f2d(S) + f2d(C);
   }
   __syncthreads();
   if ((int)threadIdx.x < nvb) {
@@ -573,10 +590,12 @@ __global__ void __launch_bounds__(kAxThreads) k_maxpy_df(const float* __restrict
     uh[ch[q]] = xh;
     ul[ch[q]] = xl;
   }
-  double ss = f2d(sh2) + f2d(sl2);
-  for (int o = 16; o > 0; o >>= 1) ss += __shfl_xor_sync(0xffffffffu, ss, o);
+  for (int o = 16; o > 0; o >>= 1) {
+    const float s2 = __shfl_xor_sync(0xffffffffu, sh2, o), c2 = __shfl_xor_sync(0xffffffffu, sl2, o);
+    two_sum_acc(s2, c2, sh2, sl2);
+  }
   __shared__ double sh[kAxThreads / 32];
-  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = ss;
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = f2d(sh2) + f2d(sl2);
   __syncthreads();
   if (threadIdx.x == 0) {
     double t = 0.0;
@@ -651,10 +670,12 @@ __global__ void __launch_bounds__(kAxThreads) k_maxpy32(float* __restrict__ V, f
     u[ch[q]] = xh;
     ul[ch[q]] = xl;
   }
-  double sd = f2d(sh2) + f2d(sl2);
-  for (int o = 16; o > 0; o >>= 1) sd += __shfl_xor_sync(0xffffffffu, sd, o);
+  for (int o = 16; o > 0; o >>= 1) {
+    const float s2 = __shfl_xor_sync(0xffffffffu, sh2, o), c2 = __shfl_xor_sync(0xffffffffu, sl2, o);
+    two_sum_acc(s2, c2, sh2, sl2);
+  }
   __shared__ double sh[kAxThreads / 32];
-  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = sd;
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = f2d(sh2) + f2d(sl2);
   __syncthreads();
   if (threadIdx.x == 0) {
     double t = 0.0;
