@@ -307,8 +307,9 @@ class MarkerInCell:
                      learned_warm: bool = False) -> dict:
         """The Stokes solve (replaces SystemSolver.solve_system_optimized, SystemSolver.jl:67-91);
         method "fgmres" or "bicgstab"; learned: add the trained network's stage after each V-cycle;
-        precision "mixed" (FP32 V-cycle and stored directions) or "fp64" (the plain method);
-        gs_relax (mixed only): FP32 Gram-Schmidt below gs_relax x the target (0: 1e3, <0: never);
+        precision "mixed" (FP32 V-cycle and stored directions, the Arnoldi step on double-float
+        FP32 pairs) or "fp64" (the plain method); gs_relax (mixed only): FP32 Gram-Schmidt
+        products below gs_relax x the target (0: 1e3; <0: the FP64 Arnoldi step throughout);
         fallback (mixed only): the plain method takes over when the mixed residual stops falling;
         mg_inner: the velocity stage's GCR steps (1: a single V-cycle), mg_inner_tol its stopping
         residual reduction; learned_warm (with learned and use_initial_guess): the learned stage

@@ -371,6 +371,29 @@ def test_fp32_gram_schmidt_matches_superlu(eb, case, gs_relax):
     mic.close()
 
 
+@pytest.mark.parametrize("case", ["rift_small", "sinking_block"])
+def test_double_float_arnoldi_step_matches_the_fp64_step(eb, case):
+    """The mixed method's Arnoldi step on FP32 pairs (double-float operator product and
+    Gram-Schmidt, FP32 preconditioner input and output), with the FP32 products disabled
+    (gs_relax tiny): against the FP64 Arnoldi step with the same FP32 V-cycle (gs_relax < 0),
+    the same number of FGMRES iterations to within one (the reductions sum in another order)
+    and the same solution to 1e-9 of each field's maximum at rtol 1e-11."""
+    model = marker_model(eb, case)
+    mic = gpu_ctx(eb, model)
+    out = {}
+    for name, relax in (("split", 1e-30), ("fp64_step", -1.0)):
+        rep = mic.solve_viscoelastic_stokes_continuity_equations(rtol=1e-11, max_iters=4000, gs_relax=relax)
+        assert rep["status"] == 0 and rep["rel_residual"] <= 1e-11 and rep["relaxed_iterations"] == 0, rep
+        out[name] = (rep["iterations"], mic.download_stokes_vector("solution"))
+    print(f"\n{case}: FGMRES iterations, double-float step {out['split'][0]}, FP64 step {out['fp64_step'][0]}")
+    assert abs(out["split"][0] - out["fp64_step"][0]) <= 1, out
+    a, b = out["split"][1], out["fp64_step"][1]
+    for comp in range(3):
+        x, y = a[comp::3], b[comp::3]
+        assert np.abs(x - y).max() <= 1e-9 * np.abs(y).max(), (comp, np.abs(x - y).max() / np.abs(y).max())
+    mic.close()
+
+
 def test_warm_start_rescales_pressure_to_the_new_system(eb):
     """A solve that starts from the solution of an earlier system: the pressure unknowns are
     p / pscale, and pscale = 2 etan0[1,1] / (xstpavg + ystpavg) changes between systems, so the
