@@ -3,7 +3,7 @@ numpy transcriptions of the reference's formulas."""
 import numpy as np
 import pytest
 
-from boundary_cases import porosity_fields, rock_tables, sediment
+from boundary_cases import porosity_fields, rock_golden_markers, rock_tables, sediment
 
 
 @pytest.fixture(scope="module")
@@ -533,3 +533,15 @@ def test_recycle_fracture_zone_oracle(eb, B, asym):
         assert got["fric"][i] == f
     # (the right side's 12 km sticky layer lies below the sediments' base: no sediment there)
     assert sub > 100 and {6, 7, 8, 10}.issubset(mats) and (5 in mats) == (not asym)
+
+
+def test_rock_property_laws_match_reference_known_answers(B):
+    """The oracle's heat capacity (Waples) and conductivities (Liao14, Sekiguchi-Waples) against
+    the reference's own test values (rock_props_tests.jl, tolerance 1e-9 as there)."""
+    g, mk, tabs, (nw, nl, ns) = rock_golden_markers()
+    cp = B.rock_properties(mk, *tabs, 0, 1, 0, 273.0, 1e30)["rhocp"][:nw]
+    np.testing.assert_allclose(cp, g["waples"]["expected_cp"], rtol=0, atol=1e-9)
+    k_liao = B.rock_properties(mk, *tabs, 0, 0, 0, 273.0, 1e30)["kt"][nw:nw + nl]
+    np.testing.assert_allclose(k_liao, g["liao14"]["expected_k"], rtol=0, atol=1e-9)
+    k_sw = B.rock_properties(mk, *tabs, 0, 0, 5, 273.0, 1e30)["kt"][nw + nl:]
+    np.testing.assert_allclose(k_sw, g["sekiguchi_waples"]["expected_k"], rtol=0, atol=1e-9)

@@ -335,3 +335,30 @@ def test_recycle_fracture_zone_matches_oracle(eb, asym):
     mic.get_marker_inside_flags()
     assert np.all(mic.download_marker("inside") == 1)
     mic.close()
+
+
+def test_rock_property_laws_match_reference_known_answers(eb):
+    """The GPU's heat capacity (Waples) and conductivities (Liao14, Sekiguchi-Waples) at the
+    conditions of the reference's own rock-property test values (rock_props_tests.jl,
+    tolerance 1e-9 as there), on inside markers of a model whose fields are overwritten."""
+    from boundary_cases import rock_golden_markers
+    g, mk, tabs, (nw, nl, ns) = rock_golden_markers()
+    model = eb.synthetic.config("rift_small")
+    mic = eb.MarkerInCell(0)
+    mic.load_model(model)
+    mic.get_marker_inside_flags()
+    idx = np.flatnonzero(mic.download_marker("inside") == 1)[:nw + nl + ns]
+    for k in ("tk", "pr", "matid"):
+        a = mic.download_marker(k)
+        if k == "matid":
+            a[:] = 1
+        a[idx] = mk[k]
+        mic.upload_marker(k, a)
+    mic.set_rock_tables(*tabs)
+    mic.update_marker_rock_properties(0, 1, 0, 0, 1e30)
+    np.testing.assert_allclose(mic.download_marker("rhocp")[idx[:nw]], g["waples"]["expected_cp"], rtol=0, atol=1e-9)
+    np.testing.assert_allclose(mic.download_marker("kt")[idx[nw:nw + nl]], g["liao14"]["expected_k"], rtol=0, atol=1e-9)
+    mic.update_marker_rock_properties(0, 0, 5, 0, 1e30)
+    np.testing.assert_allclose(mic.download_marker("kt")[idx[nw + nl:]], g["sekiguchi_waples"]["expected_k"], rtol=0,
+                               atol=1e-9)
+    mic.close()
