@@ -89,6 +89,14 @@ RECYCLE_FIELDS = ("x", "y", "tk", "pr", "sxx", "sxy", "exx", "exy", "eta", "sr_r
                   "strain_rate_plastic", "meltfrac", "fric_ini", "fric")
 
 
+def fz_lithosphere_temperature(t_top, t_bottom, grad, asth, kappa, depth, age) -> float:
+    """FractureZone.calc_lithosphere_temperature (the half-space cooling erf law) of the
+    oracle's fracture-zone recycling."""
+    f = lib().o_fz_lithosphere_temperature
+    f.restype = C.c_double
+    return f(*[C.c_double(v) for v in (t_top, t_bottom, grad, asth, kappa, depth, age)])
+
+
 def philox4x32_10(ctr, key) -> tuple:
     c = (C.c_uint32 * 4)(*[int(v) & 0xFFFFFFFF for v in ctr])
     lib().o_philox4x32_10(c, C.c_uint32(key[0]), C.c_uint32(key[1]))

@@ -534,6 +534,12 @@ static double fz_lith_temp(double t_top, double t_bottom, double grad, double as
   return t_base + (t_top - t_base) * (1 - erf(depth / (2 * sqrt(kappa * age))));
 }
 
+/* exported for the known-answer test of the erf law (HalfSpaceCooling's form) */
+double o_fz_lithosphere_temperature(double t_top, double t_bottom, double grad, double asth, double kappa,
+                                    double depth, double age) {
+  return fz_lith_temp(t_top, t_bottom, grad, asth, kappa, depth, age);
+}
+
 /* FractureZone.calculate_temperature(y, x, thermal_parameters); th[]: t_top, t_bottom, gradient,
  * x_end, age_left (s), age_right (s), sticky thickness, lithosphere depth left, right, kappa, ysize */
 static double fz_calculate_temperature(double y, double x, const double* th) {

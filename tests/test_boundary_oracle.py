@@ -545,3 +545,16 @@ def test_rock_property_laws_match_reference_known_answers(B):
     np.testing.assert_allclose(k_liao, g["liao14"]["expected_k"], rtol=0, atol=1e-9)
     k_sw = B.rock_properties(mk, *tabs, 0, 0, 5, 273.0, 1e30)["kt"][nw + nl:]
     np.testing.assert_allclose(k_sw, g["sekiguchi_waples"]["expected_k"], rtol=0, atol=1e-9)
+
+
+def test_fracture_zone_erf_law_matches_reference_half_space_cooling(B):
+    """The erf law of the oracle's fracture-zone lithosphere temperature, with the mantle base at
+    the asthenosphere temperature and age = distance / half spreading rate, against the
+    reference's own half-space cooling test values (half_space_cooling_tests.jl, 1e-9)."""
+    import json
+    import pathlib
+    g = json.loads((pathlib.Path(__file__).parent / "golden" / "half_space_reference.json").read_text())
+    age = g["distance_from_ridge_meters"] / g["half_spreading_rate_m_s"]
+    got = [B.fz_lithosphere_temperature(g["surface_temperature_kelvin"], g["asthenosphere_temperature_kelvin"], 0.0, 0.0,
+                                        g["thermal_diffusivity_m2_s"], d, age) for d in g["depths_m"]]
+    np.testing.assert_allclose(got, g["expected_temperature_kelvin"], rtol=0, atol=1e-9)
