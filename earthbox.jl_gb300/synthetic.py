@@ -385,6 +385,69 @@ def circles(n: int = 1025, ncircles: int = 200, seed: int = 4, width: float = 10
     return Model(f"circles_{n}", grid, None, params, {}, gr)
 
 
+def rayleigh_taylor(xnum: int = 51, ynum: int = 51, mpc: int = 5) -> Model:
+    """The reference's Rayleigh-Taylor instability benchmark (Ramberg 1968), as configured in
+    src/benchmarks/models/rayleigh_taylor_instability/{model,materials}.yml and the benchmark
+    material library: an 8 x 3 km uniform grid, 5 x 5 markers per cell on a regular lattice, a
+    dense weak layer (3000 kg/m^3, 1e13 Pa s) over a light viscous one (2900 kg/m^3, 1e19 Pa s)
+    with the interface at 1500 m depth, shear modulus 1e20 Pa, a 100 kyr time step, no slip on
+    top and bottom and free slip on the sides, pressure fixed at the upper-left cell, interface
+    stabilisation off.  Material ids follow the marker's depth before the perturbation; every
+    marker is then moved up by cos(2 pi (x - xsize/2) / lambda) A (markers/utils/RayleighTaylor.jl),
+    lambda = 4 km, A = 10 m, so the interface peaks at x = xsize/2."""
+    W, H, h1, lam, amp = 8000.0, 3000.0, 1500.0, 4000.0, 10.0
+    grid = staggered_grid(np.linspace(0.0, W, xnum), np.linspace(0.0, H, ynum))
+    mx, my = (xnum - 1) * mpc, (ynum - 1) * mpc
+    x = np.repeat((np.arange(mx) + 0.5) * (W / mx), my)
+    y0 = np.tile((np.arange(my) + 0.5) * (H / my), mx)
+    matid = np.where(y0 >= h1, 2, 1).astype(np.int16)
+    y = y0 - np.cos(2.0 * math.pi * (x - W / 2.0) / lam) * amp
+    n = len(x)
+    rho_l, eta_l = np.array([3000.0, 2900.0]), np.array([1e13, 1e19])
+    mats = Materials(
+        mat_mu=np.array([1e20, 1e20]), mat_hr=np.zeros(2), mat_flow_type=np.array([0, 0], np.int64),
+        mat_flow=np.asfortranarray(np.zeros((2, 12))), mat_plastic=np.asfortranarray(np.zeros((2, 6))),
+        mat_rho=rho_l.copy())
+    mats.mat_flow[:, 0] = eta_l
+    k = matid - 1
+    m = {"x": x, "y": y, "matid": matid, "rho": rho_l[k], "eta": eta_l[k], "eta_flow": eta_l[k].copy()}
+    for f in ("cohesion", "fric", "fric_ini", "preexp", "sxx", "sxy", "exx", "exy", "pr", "gii", "strain_plastic"):
+        m[f] = np.zeros(n)
+    m["sr_ratio"] = np.ones(n)
+    m["tk"] = np.full(n, 273.0)
+    m["kt"] = np.full(n, 2e-6)
+    m["rhocp"] = m["rho"] * 1000.0
+    m["ha"] = np.zeros(n)
+    _fields_common(np.random.Generator(np.random.Philox(0)), n, m)
+    m["pfailure"][:] = 0.0
+    grids = _analytic_grids(grid, v0=0.0, eta_ref=1e19, rho_ref=2900.0, T0=273.0, T1=273.0, depth_T1=H, y_surface=0.0)
+    grids.update(velocity_bcs(grid, 0.0, free_slip_bottom=False))
+    grids["btopx"] = np.asfortranarray(np.column_stack([np.zeros(xnum), -np.ones(xnum)]))  # no slip on top
+    params = default_params(timestep=1e5 * YEAR, viscosity_min=1e13, viscosity_max=1e25, ntimestep=1,
+                            temperature_top=273.0)
+    params.update(stokes_params(iuse_interface_stabilization=0, pressure_bc=0.0))
+    return Model("rayleigh_taylor", grid, mats, params, m, grids)
+
+
+def ramberg_wave_velocity(h1: float, h2: float, rho1: float, rho2: float, eta1: float, eta2: float, amp: float,
+                          lam: float, g: float = 9.81) -> float:
+    """Ramberg's (1968) analytical vertical velocity at the crest of a sinusoidal interface
+    between a top layer (thickness h1, density rho1, viscosity eta1) and a bottom layer (h2, rho2,
+    eta2) between no-slip walls, as the reference's benchmark evaluates it
+    (post_processing/analytical/RayleighTaylorInstabilityManager.jl): the growth factor
+    K = -d12 / (c11 j22 - d12 j21) and v = -K (rho1 - rho2) h2 g / (2 eta2) A."""
+    t1, t2 = 2.0 * math.pi * h1 / lam, 2.0 * math.pi * h2 / lam
+    r = eta1 / eta2
+    den1 = math.cosh(2.0 * t1) - 1.0 - 2.0 * t1 ** 2
+    den2 = math.cosh(2.0 * t2) - 1.0 - 2.0 * t2 ** 2
+    c11 = r * 2.0 * t1 ** 2 / den1 - 2.0 * t2 ** 2 / den2
+    d12 = r * (math.sinh(2.0 * t1) - 2.0 * t1) / den1 + (math.sinh(2.0 * t2) - 2.0 * t2) / den2
+    j21 = r * t2 * (math.sinh(2.0 * t1) + 2.0 * t1) / den1 + t2 * (math.sinh(2.0 * t2) + 2.0 * t2) / den2
+    j22 = r * 2.0 * t1 ** 2 * t2 / den1 - 2.0 * t2 ** 3 / den2
+    K = -d12 / (c11 * j22 - d12 * j21)
+    return -K * (rho1 - rho2) * h2 * g / 2.0 / eta2 * amp
+
+
 def config(name: str, seed: int | None = None) -> Model:
     """Named workloads: sinking_block, rift_small, rift_2p5M, rift_40M, rift_40M_strip, circles_1025."""
     kw = {} if seed is None else {"seed": seed}

@@ -63,3 +63,13 @@ def marker_model(eb, name: str, **kw):
     grids = {k: np.asfortranarray(o.gr[k]) for k in STOKES_GRIDS}
     model.grids.update(grids)
     return model
+
+
+def bilinear_basic(grid, field, x, y):
+    """Bilinear value of a basic-grid field (ynum x xnum) at (x, y)."""
+    j = int(np.clip(np.searchsorted(grid.gridx_b, x, side="right") - 1, 0, grid.xnum - 2))
+    i = int(np.clip(np.searchsorted(grid.gridy_b, y, side="right") - 1, 0, grid.ynum - 2))
+    dx = (x - grid.gridx_b[j]) / (grid.gridx_b[j + 1] - grid.gridx_b[j])
+    dy = (y - grid.gridy_b[i]) / (grid.gridy_b[i + 1] - grid.gridy_b[i])
+    return ((1 - dx) * (1 - dy) * field[i, j] + dx * (1 - dy) * field[i, j + 1] + (1 - dx) * dy * field[i + 1, j]
+            + dx * dy * field[i + 1, j + 1])

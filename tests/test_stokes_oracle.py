@@ -169,3 +169,28 @@ def test_solution_sensitivity_to_averaging_precision(eb):
         S = solve(g)
         moves.append(max(np.abs(S[c::3] - S0[c::3]).max() / np.abs(S0[c::3]).max() for c in (0, 1)))
     assert 5e-6 < max(moves) < 1e-4, moves
+
+
+def test_oracle_rayleigh_taylor_matches_ramberg(eb):
+    """The reference's Rayleigh-Taylor benchmark (Ramberg 1968) through the oracle: marker
+    averages, assembly, a direct solve, the basic-node velocity (mean of the two vy nodes
+    beside each basic node), and the crest velocity within the reference's 3.5 % limit of the
+    analytic value (RayleighTaylorInstabilityManager.jl)."""
+    from oracle.oracle import OracleMIC
+    from oracle.stokes import StokesOracle
+    from stokes_cases import bilinear_basic
+    model = eb.synthetic.rayleigh_taylor()
+    ref = OracleMIC(model)
+    ref.get_marker_inside_flags()
+    ref.initialize_bilinear_interpolation()
+    ref.interpolate_marker_stokes_parameters_to_grid()
+    model.grids.update({k: np.asfortranarray(v) for k, v in ref.gr.items()})
+    o = StokesOracle(model)
+    o.stokes_steps()
+    S = o.solve_direct()
+    o.process_stokes_solution(S)
+    vyb = 0.5 * (o.gr["vy1"][:, :-1] + o.gr["vy1"][:, 1:])
+    g = model.grid
+    v = bilinear_basic(g, vyb, 0.5 * (g.xmax - g.xmin), 1500.0 - 10.0)
+    va = eb.synthetic.ramberg_wave_velocity(1500.0, 1500.0, 3000.0, 2900.0, 1e13, 1e19, 10.0, 4000.0)
+    assert abs(v - va) / abs(va) < 0.035, (v, va)
