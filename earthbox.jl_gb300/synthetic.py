@@ -429,6 +429,54 @@ def rayleigh_taylor(xnum: int = 51, ynum: int = 51, mpc: int = 5) -> Model:
     return Model("rayleigh_taylor", grid, mats, params, m, grids)
 
 
+def stress_buildup(xnum: int = 51, ynum: int = 51, mpc: int = 4) -> Model:
+    """The reference's viscoelastic stress-buildup benchmark, as configured in
+    src/benchmarks/models/viscoelastic_stress_buildup/{model,materials}.yml and the benchmark
+    material library (Viscoelastic_Material): a 100 x 100 km uniform grid, 4 x 4 markers per
+    cell on a regular lattice, one isoviscous material (1e21 Pa s, shear modulus 1e10 Pa,
+    4000 kg/m^3), no gravity, a 10 yr time step, and pure shear at 1e-14 1/s
+    (PureShearDeformationBC.jl with VelocityFromStrainRate.jl: full extension velocity
+    strain rate x width, half of it out through each side and in through the top and the
+    bottom, tangential components free).  The deviatoric stress builds up as a Maxwell body:
+    sxx(t) = 2 eta edot (1 - exp(-mu t / eta))."""
+    W = H = 100e3
+    edot = 1e-14
+    grid = staggered_grid(np.linspace(0.0, W, xnum), np.linspace(0.0, H, ynum))
+    mx, my = (xnum - 1) * mpc, (ynum - 1) * mpc
+    x = np.repeat((np.arange(mx) + 0.5) * (W / mx), my)
+    y = np.tile((np.arange(my) + 0.5) * (H / my), mx)
+    n = len(x)
+    eta, mu, rho = 1e21, 1e10, 4000.0
+    mats = Materials(
+        mat_mu=np.array([mu]), mat_hr=np.zeros(1), mat_flow_type=np.array([0], np.int64),
+        mat_flow=np.asfortranarray(np.zeros((1, 12))), mat_plastic=np.asfortranarray(np.zeros((1, 6))),
+        mat_rho=np.array([rho]))
+    mats.mat_flow[0, 0] = eta
+    m = {"x": x, "y": y, "matid": np.ones(n, np.int16), "rho": np.full(n, rho), "eta": np.full(n, eta),
+         "eta_flow": np.full(n, eta)}
+    for f in ("cohesion", "fric", "fric_ini", "preexp", "sxx", "sxy", "exx", "exy", "pr", "gii", "strain_plastic"):
+        m[f] = np.zeros(n)
+    m["sr_ratio"] = np.ones(n)
+    m["tk"] = np.full(n, 273.0)
+    m["kt"] = np.full(n, 2.0)
+    m["rhocp"] = m["rho"] * 1000.0
+    m["ha"] = np.zeros(n)
+    _fields_common(np.random.Generator(np.random.Philox(0)), n, m)
+    m["pfailure"][:] = 0.0
+    grids = _analytic_grids(grid, v0=0.0, eta_ref=eta, rho_ref=rho, T0=273.0, T1=273.0, depth_T1=H, y_surface=0.0)
+    grids.update(velocity_bcs(grid))
+    v = edot * W
+    F = np.asfortranarray
+    grids["btopy"] = F(np.column_stack([np.full(xnum + 1, 0.5 * v), np.zeros(xnum + 1)]))
+    grids["bbottomy"] = F(np.column_stack([np.full(xnum + 1, -0.5 * v), np.zeros(xnum + 1)]))
+    grids["bleftx"] = F(np.column_stack([np.full(ynum + 1, -0.5 * v), np.zeros(ynum + 1)]))
+    grids["brightx"] = F(np.column_stack([np.full(ynum + 1, 0.5 * v), np.zeros(ynum + 1)]))
+    params = default_params(timestep=10.0 * YEAR, viscosity_min=1e18, viscosity_max=1e25, ntimestep=1,
+                            temperature_top=273.0)
+    params.update(stokes_params(iuse_interface_stabilization=0, pressure_bc=0.0, gravity_y=0.0))
+    return Model("stress_buildup", grid, mats, params, m, grids)
+
+
 def ramberg_wave_velocity(h1: float, h2: float, rho1: float, rho2: float, eta1: float, eta2: float, amp: float,
                           lam: float, g: float = 9.81) -> float:
     """Ramberg's (1968) analytical vertical velocity at the crest of a sinusoidal interface

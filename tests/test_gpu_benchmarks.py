@@ -6,7 +6,11 @@ RayleighTaylorInstabilityManager.jl): markers of two layers with a sinusoidal in
 averaged to the grid, the Stokes system is assembled and solved, the velocity is moved to the
 basic nodes, and its vertical component at the interface crest (x = xsize/2, y = h1 - A,
 bilinear on the basic grid) must agree with Ramberg's analytic crest velocity within the
-reference's relative error limit of 3.5 %."""
+reference's relative error limit of 3.5 %.
+
+Viscoelastic stress buildup (src/benchmarks/models/viscoelastic_stress_buildup): whole time
+steps of a Maxwell body in pure shear, held to the reference's discrete stress update and to the
+continuous Maxwell curve."""
 import pytest
 
 from stokes_cases import bilinear_basic
@@ -38,4 +42,45 @@ def test_rayleigh_taylor_crest_velocity_matches_ramberg(eb, precision):
     print(f"\nRayleigh-Taylor crest velocity ({precision}): GPU {v_num:.5e} m/s, Ramberg {v_ana:.5e} m/s, "
           f"relative error {100 * err:.2f} % (limit {100 * RELATIVE_ERROR_LIMIT:.1f} %)")
     assert err < RELATIVE_ERROR_LIMIT, (v_num, v_ana, err)
+    mic.close()
+
+
+def test_viscoelastic_stress_buildup_matches_maxwell(eb):
+    """The reference's viscoelastic stress-buildup benchmark (models/viscoelastic_stress_buildup,
+    post_processing/analytical/ViscoElasticStressBuildupManager.jl) through whole GPU time steps:
+    pure shear at 1e-14 1/s of a Maxwell body (1e21 Pa s, 1e10 Pa) for 2500 steps of 10 yr,
+    the largest grid sxx read at every 1000 yr output.
+
+    The reference steps the stress with the backward-Euler factor f = eta / (eta + mu dt)
+    (src/utils/ViscoelasticFactor.jl:24), so after n steps sxx_n = 2 eta edot (1 - f^n) exactly;
+    the GPU must reproduce that within 1e-6.  Against the continuous curve
+    2 eta edot (1 - exp(-mu t / eta)) the scheme itself is first-order in dt/tau: 0.134 % low
+    at 1000 yr, falling below the reference's 0.1 % limit from 3000 yr on.  So the continuous
+    curve is held to the scheme's own deviation (plus 1e-6) at every output and to the 0.1 %
+    limit from 3000 yr."""
+    import math
+    syn = eb.synthetic
+    model = syn.stress_buildup()
+    mic = eb.MarkerInCell(0)
+    mic.load_model(model)
+    dt = model.params["timestep"]
+    eta, mu, edot = 1e21, 1e10, 1e-14
+    f = eta / (eta + dt * mu)
+    rows = []
+    for n in range(1, 2501):
+        hist = mic.time_step(1, 1e-3, iuse_harmonic=0, rtol=1e-10)["picard"]
+        assert hist[-1]["status"] == 0, hist
+        if n % 100 == 0:
+            s = float(mic.download_grid("sxx2").max())
+            disc = 2.0 * eta * edot * (1.0 - f ** n)
+            ana = 2.0 * eta * edot * (1.0 - math.exp(-n * dt * mu / eta))
+            rows.append((n * 10, s, disc, ana))
+    print("\nstress buildup (t yr, GPU MPa, discrete MPa, Maxwell MPa, vs discrete, vs Maxwell):",
+          ", ".join(f"({t}, {s / 1e6:.6f}, {d / 1e6:.6f}, {a / 1e6:.6f}, {abs(s - d) / d:.1e}, {abs(s - a) / a:.2e})"
+                    for t, s, d, a in rows[::4]))
+    for t, s, d, a in rows:
+        assert abs(s - d) / d < 1e-6, (t, s, d)
+        assert abs(s - a) / a < abs(d - a) / a + 1e-6, (t, s, a)
+        if t >= 3000:
+            assert abs(s - a) / a < 1e-3, (t, s, a)
     mic.close()
