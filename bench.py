@@ -47,6 +47,7 @@ ALGO_BYTES_PER_MARKER = {
     "k_cells<stokes>": 4 + 4 + 8 + 1 + 4 + 8 * 8 + 4 + 4,   # perm, xn, fx/fy, flags, matid, 8 f64, 2 f32
     "k_cells<heat>": 4 + 8 + 1 + 4 + 5 * 8,
     "k_cells<denominators>": 4 + 4 + 8 + 1,
+    "k_cells<heat+denominators>": 4 + 4 + 8 + 1 + 4 + 5 * 8,
     "k_cells<subgrid_stress>": 4 + 8 + 8 + 1 + 4 + 8 + 2 * 16,
     "k_cells<subgrid_heat>": 4 + 8 + 8 + 1 + 16 + 8,
     "k_advect": 8 + 8 + 1 + 16 + 16 + 24 + 32,             # xn/yn, fx/fy, flags, rw x/y, w vx/vy/spin, rw sxx/sxy
@@ -148,8 +149,40 @@ def r3(v):
     return float(f"{v:.3g}") if np.isfinite(v) else None
 
 
+class _Nvml:
+    """Read-only NVML queries through ctypes: SM clock, its maximum and the active clock-event
+    reasons of one device.  Nothing here changes a setting."""
+
+    SM = 1  # NVML_CLOCK_SM
+    REASONS = {0x4: "sw_power_cap", 0x8: "hw_slowdown", 0x20: "sw_thermal_slowdown",
+               0x40: "hw_thermal_slowdown", 0x80: "hw_power_brake_slowdown"}
+
+    def __init__(self, index: int):
+        import ctypes
+        self.c = ctypes
+        self.lib = ctypes.CDLL("libnvidia-ml.so.1")
+        if self.lib.nvmlInit_v2() != 0:
+            raise OSError("nvmlInit_v2 failed")
+        self.h = ctypes.c_void_p()
+        if self.lib.nvmlDeviceGetHandleByIndex_v2(ctypes.c_uint(index), ctypes.byref(self.h)) != 0:
+            raise OSError("nvmlDeviceGetHandleByIndex_v2 failed")
+        self.reasons_fn = getattr(self.lib, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
+            self.lib.nvmlDeviceGetCurrentClocksThrottleReasons
+
+    def sample(self):
+        c = self.c
+        clk, mx, rs = c.c_uint(), c.c_uint(), c.c_ulonglong()
+        if self.lib.nvmlDeviceGetClockInfo(self.h, self.SM, c.byref(clk)) != 0:
+            return None
+        self.lib.nvmlDeviceGetMaxClockInfo(self.h, self.SM, c.byref(mx))
+        self.reasons_fn(self.h, c.byref(rs))
+        return float(clk.value), float(mx.value), {nm for bit, nm in self.REASONS.items() if rs.value & bit}
+
+
 class Clocks:
-    """nvidia-smi sampling of SM clocks and throttle reasons during the timed region."""
+    """SM clock and throttle-reason samples taken during the timed region: NVML polled every
+    10 ms from a host thread (the timed regions last a fraction of a second), else nvidia-smi at
+    its 200 ms period."""
 
     FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
               "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
@@ -158,18 +191,42 @@ class Clocks:
     def __init__(self, index: int):
         self.index = index
         self.proc = None
+        self.thread = None
+        self.samples = []
+        self.source = None
 
     def __enter__(self):
+        import threading
+        try:
+            nv = _Nvml(self.index)
+            self.stop = threading.Event()
+
+            def poll():
+                while True:
+                    s = nv.sample()
+                    if s is not None:
+                        self.samples.append(s)
+                    if self.stop.wait(0.01):
+                        break
+            self.source = "nvml"
+            self.thread = threading.Thread(target=poll, daemon=True)
+            self.thread.start()
+            return self
+        except (OSError, AttributeError):
+            pass
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
                  "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.source = "nvidia-smi"
         except OSError:
             self.proc = None
         return self
 
     def __exit__(self, *a):
-        self.lines = []
+        if self.thread is not None:
+            self.stop.set()
+            self.thread.join(timeout=5)
         if self.proc:
             self.proc.terminate()
             try:
@@ -177,26 +234,25 @@ class Clocks:
             except subprocess.TimeoutExpired:
                 self.proc.kill()
                 out, _ = self.proc.communicate()
-            self.lines = [ln for ln in out.splitlines() if ln.strip()]
+            names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+            for ln in out.splitlines():
+                parts = [p.strip() for p in ln.split(",")]
+                if len(parts) < 7:
+                    continue
+                try:
+                    sm, mx = float(parts[0]), float(parts[1])
+                except ValueError:
+                    continue
+                self.samples.append((sm, mx, {nm for nm, v in zip(names, parts[3:7])
+                                              if v.lower().startswith("active")}))
 
     def summary(self):
-        sm, mx, reasons = [], None, set()
-        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for ln in getattr(self, "lines", []):
-            parts = [p.strip() for p in ln.split(",")]
-            if len(parts) < 7:
-                continue
-            try:
-                sm.append(float(parts[0]))
-                mx = float(parts[1])
-            except ValueError:
-                continue
-            for nm, v in zip(names, parts[3:7]):
-                if v.lower().startswith("active"):
-                    reasons.add(nm)
-        if not sm:
-            return {"sm_mhz": None, "sm_max_mhz": mx, "reasons": ["unsampled"]}
-        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        reasons = set().union(*(r for _, _, r in self.samples))
+        return {"sm_mhz": float(np.median([s for s, _, _ in self.samples])), "sm_max_mhz": self.samples[-1][1],
+                "sm_min_mhz": min(s for s, _, _ in self.samples), "reasons": sorted(reasons),
+                "samples": len(self.samples), "source": self.source}
 
 
 E2E_IN = ["x", "y", "matid", "rho", "cohesion", "fric", "eta", "eta_flow", "sxx", "sxy", "pfailure", "dilatation",
@@ -724,7 +780,9 @@ def main():
                 "vs_baseline": None, "dtype": "f64 storage, f32 weights/sums", "data": "synthetic",
                 "config": {"workload": args.workload, "markers": M, "xnum": model.grid.xnum, "ynum": model.grid.ynum,
                            "markers_per_cell": 25 if args.workload == "rift_40M" else None,
-                           "l2": "inputs larger than L2 (each marker field 320 MB)", "parallelism": "replicas"},
+                           "l2": (f"inputs larger than L2 (each marker field {M * 8 / 1e6:.0f} MB)" if M * 8 > 129e6
+                                  else f"marker fields ({M * 8 / 1e6:.0f} MB each) fit in L2: a profiling case"),
+                           "parallelism": "replicas"},
                 "gpu_launches": launches, "roofline": r3(roofline), "cycle_GBps": r3(cycle_gbs),
                 "cpu_baseline": cpu, "e2e": r3(e2e), "clocks": clk.summary(),
                 "kernels_ms": {k: r3(v[0]) for k, v in top},

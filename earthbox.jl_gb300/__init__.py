@@ -514,8 +514,8 @@ class MarkerInCell:
                   heat: bool = False, warm_start: bool = True, **solve_kw) -> dict:
         """One pass of TimeLoop.run_loop!'s body (src/time_loop/TimeLoop.jl:181-194) restricted to the
         hot path, with a fixed time step:
-          execute_pre_solver_steps! (:203-230): initialize_bilinear_interpolation!, the heat-parameter
-            averages, update_marker_rheology! + update_marker_viscoplastic_viscosity! (marker
+          execute_pre_solver_steps! (:203-230): initialize_bilinear_interpolation! and the
+            heat-parameter averages (one walk of the cell lists), update_marker_rheology! + update_marker_viscoplastic_viscosity! (marker
             plasticity when itype_global == 0; one fused pass), the Stokes-parameter averages and the
             harmonic normal viscosity;
           execute_stokes_continuity_solver_steps! (:232-248): the Picard loop of itype_global (markers
@@ -531,8 +531,7 @@ class MarkerInCell:
         p = getattr(self, "_params", {})
         nodes = int(p.get("itype_global", 0)) == 1
         self.get_marker_inside_flags()
-        self.initialize_bilinear_interpolation()
-        self.interpolate_marker_heat_parameters_to_grid()
+        self.initialize_bilinear_interpolation_and_heat_scatter()
         self.update_marker_rheology_and_viscoplastic_viscosity(use_marker_plasticity=not nodes)
         self.interpolate_marker_stokes_parameters_to_grid()
         self.interpolate_basic_viscoplastic_viscosity_to_pressure_grid(iuse_harmonic)
@@ -815,14 +814,23 @@ class MarkerInCell:
         and the strain update in one marker pass (eb_correct_advect_and_update_strain)."""
         self._call("eb_correct_advect_and_update_strain")
 
+    def initialize_bilinear_interpolation_and_heat_scatter(self) -> None:
+        """The bilinear set-up followed by the heat scatter, with the weight denominators summed in
+        the heat scatter's walk of the cell lists (same results as the two calls in sequence)."""
+        self._call("eb_initialize_bilinear_interpolation_and_heat_scatter")
+
     def marker_cycle(self, fused: bool = True) -> None:
         """The marker-in-cell transfer + RK4 sequence of one time step (no Stokes/heat solve):
         locate, heat and Stokes scatters, post-Stokes gathers, subgrid stress and temperature,
         stress and temperature corrections, RK4 advection and the strain update.  With
-        fused=True the last four run as one pass (same results)."""
+        fused=True the bilinear set-up shares the heat scatter's cell walk and the last four
+        steps run as one pass (same results)."""
         self.get_marker_inside_flags()
-        self.initialize_bilinear_interpolation()
-        self.interpolate_marker_heat_parameters_to_grid()
+        if fused:
+            self.initialize_bilinear_interpolation_and_heat_scatter()
+        else:
+            self.initialize_bilinear_interpolation()
+            self.interpolate_marker_heat_parameters_to_grid()
         self.interpolate_marker_stokes_parameters_to_grid()
         self.post_stokes_marker_gathers()
         self.update_subgrid_stress()

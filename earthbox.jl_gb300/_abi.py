@@ -233,7 +233,7 @@ ENTRY_POINTS = [
     "eb_post_stokes_marker_gathers", "eb_update_subgrid_stress", "eb_apply_marker_stress_correction",
     "eb_subgrid_heat_diffusion_update", "eb_add_remaining_grid_change_to_marker_temperature",
     "eb_advect_markers_and_rotate_stress", "eb_update_marker_strain", "eb_correct_advect_and_update_strain",
-    "eb_calc_marker_viscoplastic_viscosity",
+    "eb_calc_marker_viscoplastic_viscosity", "eb_initialize_bilinear_interpolation_and_heat_scatter",
 ]
 ALL_SYMBOLS = [
     "eb_create", "eb_destroy", "eb_last_error", "eb_set_grid", "eb_set_materials", "eb_set_params",

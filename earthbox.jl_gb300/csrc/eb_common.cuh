@@ -148,6 +148,17 @@ EB_DEV float gather4(const double* __restrict__ g, int32_t rows, int32_t iy, int
   v = fmaf(w.lr, d2f(__ldg(&g[o + rows + 1])), v);
   return v;
 }
+// The 4-point gather from the four node values (UL, LL, UR, LR) already in registers
+// (the arithmetic of gather4f below).
+EB_DEV float gather4v(float n0, float n1, float n2, float n3, float dx, float dy) {
+  const W4 w = wts(dx, dy);
+  float v = w.ul * n0;
+  v = fmaf(w.ll, n1, v);
+  v = fmaf(w.ur, n2, v);
+  v = fmaf(w.lr, n3, v);
+  return v;
+}
+
 // (a grid holds fewer than 2^31 nodes: the offset is formed in 32 bits)
 EB_DEV float gather4f(const float* __restrict__ g, int32_t rows, int32_t iy, int32_t ix, float dx,
                       float dy) {

@@ -621,16 +621,43 @@ extern "C" int eb_get_marker_inside_flags(eb_ctx* c) {
   return finish(c, launch_inside_flags(c));
 }
 
-extern "C" int eb_initialize_bilinear_interpolation(eb_ctx* c) {
-  int rc = ready(c, false, false);
-  if (rc) return rc;
+// cell location and the cell-sorted list: eb_initialize_bilinear_interpolation without its
+// denominator pass
+static int bilinear_locate(eb_ctx* c) {
+  int rc;
   const int need[] = {EB_M_X, EB_M_Y, EB_M_INSIDE, EB_M_XN, EB_M_YN};
   for (int f : need) if ((rc = ensure_marker_field(c, f))) return rc;
   const int grids[] = {EB_G_WTNODES, EB_G_WTETAS, EB_G_WTETAN, EB_G_WTNODES_VY};
   for (int f : grids) if ((rc = ensure_grid_field(c, f))) return rc;
   if (c->M > 0 && (rc = launch_locate_and_sort(c))) return rc;
   c->located = true;
+  return EB_OK;
+}
+
+extern "C" int eb_initialize_bilinear_interpolation(eb_ctx* c) {
+  int rc = ready(c, false, false);
+  if (rc) return rc;
+  if ((rc = bilinear_locate(c))) return rc;
   return finish(c, launch_denominators(c));
+}
+
+int cycle_bilinear_setup(eb_ctx* c) {
+  int rc = ready(c, false, false);
+  if (rc) return rc;
+  return finish(c, bilinear_locate(c));
+}
+
+int cycle_heat_and_denominators(eb_ctx* c) {
+  int rc = ready(c, true, true);
+  if (rc) return rc;
+  return finish(c, launch_scatter_heat(c, true));
+}
+
+extern "C" int eb_initialize_bilinear_interpolation_and_heat_scatter(eb_ctx* c) {
+  int rc = ready(c, true, false);
+  if (rc) return rc;
+  if ((rc = bilinear_locate(c))) return rc;
+  return finish(c, launch_scatter_heat(c, true));
 }
 
 extern "C" int eb_interpolate_marker_stokes_parameters_to_grid(eb_ctx* c) {

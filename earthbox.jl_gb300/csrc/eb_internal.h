@@ -234,7 +234,10 @@ int launch_inside_flags(eb_ctx* c);
 int launch_locate_and_sort(eb_ctx* c);
 int launch_denominators(eb_ctx* c);
 int launch_scatter_stokes(eb_ctx* c);
-int launch_scatter_heat(eb_ctx* c);
+// with_denominators: the same fold also sums the weight denominators (wtnodes, wtetas, wtetan,
+// wtnodes_vy) that launch_denominators would (bit-identical), for a heat scatter that directly
+// follows the bilinear set-up
+int launch_scatter_heat(eb_ctx* c, bool with_denominators = false);
 int launch_scatter_viscosity(eb_ctx* c);
 int launch_subgrid_stress(eb_ctx* c);
 int launch_subgrid_heat(eb_ctx* c);
@@ -248,6 +251,12 @@ int launch_update_strain(eb_ctx* c);
 // stress correction, remaining temperature change, advection + rotation and the strain
 // update in one marker pass (the four steps in that order; eb_advect.cu)
 int launch_marker_tail(eb_ctx* c);
+// The bilinear set-up without its denominator pass and the heat scatter that sums them; run
+// back to back they equal eb_initialize_bilinear_interpolation followed by
+// eb_interpolate_marker_heat_parameters_to_grid (eb_ctx.cu; the host pipeline runs them as two
+// steps so the heat fields' upload can overlap the locate and sort).
+int cycle_bilinear_setup(eb_ctx* c);
+int cycle_heat_and_denominators(eb_ctx* c);
 int launch_rheology(eb_ctx* c);
 int launch_viscoplastic(eb_ctx* c, int use_marker_plasticity);
 int launch_rheology_fused(eb_ctx* c, int use_marker_plasticity);

@@ -1,9 +1,9 @@
 // eb_pipeline.cu -- one marker cycle with the host copies overlapped with the steps.
 //
 // The cycle is MarkerInCell.marker_cycle's sequence of entry points (inside flags,
-// bilinear set-up, heat and Stokes scatters, post-Stokes gathers, subgrid stress,
-// stress correction, subgrid heat, remaining temperature change, RK4 advection,
-// strain update), each of which the reference calls from its time loop
+// bilinear set-up, heat scatter -- the weight denominators summed in the heat fold --,
+// Stokes scatter, post-Stokes gathers, subgrid stress, stress correction, subgrid heat,
+// remaining temperature change, RK4 advection, strain update), each of which the reference calls from its time loop
 // (TimeLoop.jl; the call sites are listed beside each entry point in the header).
 // Here the caller's host arrays go in and out inside the same call:
 //   * uploads run on a copy stream in the order the steps first read them, in four
@@ -60,8 +60,8 @@ int final_step(int f) {
 int run_step(eb_ctx* c, int s) {
   switch (s) {
     case ST_INSIDE: return eb_get_marker_inside_flags(c);
-    case ST_BILINEAR: return eb_initialize_bilinear_interpolation(c);
-    case ST_HEAT: return eb_interpolate_marker_heat_parameters_to_grid(c);
+    case ST_BILINEAR: return cycle_bilinear_setup(c);
+    case ST_HEAT: return cycle_heat_and_denominators(c);
     case ST_STOKES: return eb_interpolate_marker_stokes_parameters_to_grid(c);
     case ST_POST_STOKES: return eb_post_stokes_marker_gathers(c);
     case ST_SUBGRID_STRESS: return eb_update_subgrid_stress(c);

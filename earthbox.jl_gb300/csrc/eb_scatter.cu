@@ -28,6 +28,15 @@ __device__ __forceinline__ int32_t cell_id(int32_t ci, int32_t cj, int32_t ynum)
   return (cj - 1) * (ynum - 1) + (ci - 1);
 }
 
+// Geometry of one basic-cell column ix (1-based), loaded once per staging thread: every
+// marker of a cell lies in the cell's column, so the cell-sorted folds need no per-marker
+// xn load and no per-marker geometry gathers.
+struct ColW { float vlo, vhi, sx, r0, r1; };  // vyoff_lo/hi[ix-1], sxf[ix-1], rsxvyf[ix-1], rsxvyf[ix]
+__device__ __forceinline__ ColW col_weights(const DevGrid& g, int32_t ix) {
+  const float4 c0 = __ldg(&g.colx[2 * (ix - 1)]), c1 = __ldg(&g.colx[2 * (ix - 1) + 1]);
+  return ColW{c0.z, c0.w, c0.x, c1.x, c1.y};
+}
+
 // Weights of one marker from its stored FP32 normalised offsets.
 struct MW {
   W4 b;       // basic UL, LL, UR, LR
@@ -35,13 +44,13 @@ struct MW {
   W4 vy;      // vy-grid corners
   int half;   // 0: vy cell = xn, 1: vy cell = xn + 1
 };
-__device__ __forceinline__ MW marker_weights(const DevGrid& g, int32_t ix, float fx, float fy, uint8_t fl) {
+__device__ __forceinline__ MW marker_weights(const ColW& c, float fx, float fy, uint8_t fl) {
   MW w;
   w.b = wts(fx, fy);
   w.wc = (1.f - fabsf(0.5f - fx)) * (1.f - fabsf(0.5f - fy));
   w.half = (fl & MF_VYRIGHT) ? 1 : 0;
-  const float off = w.half ? __ldg(&g.vyoff_hi[ix - 1]) : __ldg(&g.vyoff_lo[ix - 1]);
-  const float dxv = (fx * __ldg(&g.sxf[ix - 1]) - off) * __ldg(&g.rsxvyf[ix - 1 + w.half]);
+  const float off = w.half ? c.vhi : c.vlo;
+  const float dxv = (fx * c.sx - off) * (w.half ? c.r1 : c.r0);
   w.vy = wts(dxv, fy);
   return w;
 }
@@ -93,9 +102,11 @@ __device__ __forceinline__ void stage_weights(float (*sv)[kChunk], int t, const 
 // ------------------------------------------------------------------ specs ---
 // Each spec defines: kRoles (folding warps, <= 8), kNV (staged rows), kAcc
 // (register accumulator pairs KSum2 per folding thread), kSlots (shared-memory
-// accumulator slots, SAcc, each a pair), a Raw record of the marker fields it
-// reads, load() (the global loads only, issued one pass ahead), put() (arithmetic
-// on a loaded Raw, marker write-backs, staging), accum() and store().  Every
+// accumulator slots, SAcc, each a pair), a Cell record of per-cell constants and
+// cell() that loads them (once per staging thread: a thread stages the same cell in
+// every pass), a Raw record of the marker fields it reads, load() (the global loads
+// only, issued one pass ahead), put() (arithmetic on a loaded Raw and the cell's
+// constants, marker write-backs, staging), accum() and store().  Every
 // accumulator receives its cell's markers in slot (marker) order; accumulators
 // travel in pairs through packed FP32x2 arithmetic where two share a role.
 
@@ -107,12 +118,15 @@ struct DenomSpec {
   //        slot q), 3 central node (registers), 4-5 vy corners {0,1} / {2,3} (shared pair
   //        slot 4 + 2*half + pair)
   static constexpr int kRoles = 6, kNV = S_V0, kAcc = 1, kSlots = 8;
-  struct Raw { int32_t xn; float fx, fy; uint8_t fl; };
+  using Cell = ColW;
+  __device__ Cell cell(const DevGrid& g, int32_t, int32_t ix) const { return col_weights(g, ix); }
+  struct Raw { float fx, fy; uint8_t fl; };
   __device__ Raw load(const DevMarkers& mk, int32_t m) const {
-    return Raw{mk.xn[m], mk.fx[m], mk.fy[m], mk.mflags[m]};
+    return Raw{mk.fx[m], mk.fy[m], mk.mflags[m]};
   }
-  __device__ void put(const Raw& r, const DevMarkers&, const DevGrid& g, int t, float (*sv)[kChunk], uint8_t* sfl) const {
-    stage_weights(sv, t, marker_weights(g, r.xn, r.fx, r.fy, r.fl));
+  __device__ void put(const Raw& r, const Cell& cc, const DevMarkers&, const DevGrid&, int t, float (*sv)[kChunk],
+                      uint8_t* sfl) const {
+    stage_weights(sv, t, marker_weights(cc, r.fx, r.fy, r.fl));
     sfl[t] = r.fl;
   }
   __device__ void accum(int role, int lane, int t, float (*sv)[kChunk], const uint8_t* sfl, KSum2* a, SAcc sa) const {
@@ -164,6 +178,10 @@ struct StokesSpec {
   static constexpr int kRoles = 8, kNV = V_END, kAcc = 2, kSlots = 20;
   const double* mat_mu;
   int32_t* dflag;
+  // (the column geometry is loaded per marker here: held per cell it costs this fold its
+  // fourth resident block at 64 registers)
+  struct Cell {};
+  __device__ Cell cell(const DevGrid&, int32_t, int32_t) const { return Cell{}; }
   struct Raw {
     double rho, coh, fric, etaf, eta, sxy, melt, sxx;
     float fx, fy, plast, dil;
@@ -178,8 +196,9 @@ struct StokesSpec {
     r.melt = mk.melt[m]; r.sxx = mk.sxx[m];
     return r;
   }
-  __device__ void put(const Raw& r, const DevMarkers&, const DevGrid& g, int t, float (*sv)[kChunk], uint8_t* sfl) const {
-    stage_weights(sv, t, marker_weights(g, r.xn, r.fx, r.fy, r.fl));
+  __device__ void put(const Raw& r, const Cell&, const DevMarkers&, const DevGrid& g, int t, float (*sv)[kChunk],
+                      uint8_t* sfl) const {
+    stage_weights(sv, t, marker_weights(col_weights(g, r.xn), r.fx, r.fy, r.fl));
     sfl[t] = r.fl;
     const double mu = __ldg(&mat_mu[r.mt - 1]);
     if ((__double_as_longlong(mu) << 1) == 0) atomicOr(dflag, 2);  // reference raises on a zero shear modulus
@@ -258,24 +277,45 @@ struct StokesSpec {
   }
 };
 
-// Heat numerators (BilinearNumerator.jl:31-141): tk, kt, rhocp, hr(+serp), ha; part slots 5*corner + f
-struct HeatSpec {
-  static constexpr const char* kName = "k_cells<heat>";
-  // roles: corner (role & 3) x field pairs {tk, kt} + {ha} (role < 4) or {rhocp, hr} (role >= 4)
-  static constexpr int kRoles = 8, kNV = S_V0 + 5, kAcc = 2, kSlots = 0;
+// Heat numerators (BilinearNumerator.jl:31-141): tk, kt, rhocp, hr(+serp), ha; part slots 5*corner + f.
+// With kDen the same fold also sums the weight denominators of DenomSpec (BilinearDenominator.jl:34-157)
+// into part slots kDenBase + DenomSpec's slot: the bilinear set-up and the heat scatter of a marker
+// cycle then walk the cell lists once.  Every sum receives the same terms in the same order as in
+// DenomSpec (a term of 0 leaves a compensated sum unchanged), so the denominators are bit-identical.
+constexpr int kDenBase = 20;
+template <bool kDen>
+struct HeatSpecT {
+  static constexpr const char* kName = kDen ? "k_cells<heat+denominators>" : "k_cells<heat>";
+  // roles: corner (role & 3) x field pairs {tk, kt} + {ha, incl weight} (role < 4) or {rhocp, hr}
+  //        (role >= 4); with kDen roles >= 4 also sum {excl weight of quadrant k, vy weight half 0}
+  //        and {vy weight half 1, central weight (role 4)}
+  static constexpr int kRoles = 8, kNV = S_V0 + 5, kAcc = kDen ? 3 : 2, kSlots = 0;
   const double* mat_hr;
   int use_serp;
-  struct Raw { double tk, kt, rhocp, ha, serp; float fx, fy; int32_t mt; };
+  struct Cell { ColW col; };
+  __device__ Cell cell(const DevGrid& g, int32_t, int32_t ix) const {
+    Cell c{};
+    if (kDen) c.col = col_weights(g, ix);
+    return c;
+  }
+  struct Raw { double tk, kt, rhocp, ha, serp; float fx, fy; int32_t mt; uint8_t fl; };
   __device__ Raw load(const DevMarkers& mk, int32_t m) const {
     Raw r;
     r.fx = mk.fx[m]; r.fy = mk.fy[m]; r.mt = mk.matid[m];
     r.tk = mk.tk[m]; r.kt = mk.kt[m]; r.rhocp = mk.rhocp[m]; r.ha = mk.ha[m];
     r.serp = use_serp ? mk.serp_hr[m] : 0.0;
+    if (kDen) r.fl = mk.mflags[m];
     return r;
   }
-  __device__ void put(const Raw& r, const DevMarkers&, const DevGrid&, int t, float (*sv)[kChunk], uint8_t*) const {
-    const W4 w = wts(r.fx, r.fy);
-    sv[S_UL][t] = w.ul; sv[S_LL][t] = w.ll; sv[S_UR][t] = w.ur; sv[S_LR][t] = w.lr;
+  __device__ void put(const Raw& r, const Cell& cc, const DevMarkers&, const DevGrid&, int t, float (*sv)[kChunk],
+                      uint8_t* sfl) const {
+    if (kDen) {
+      stage_weights(sv, t, marker_weights(cc.col, r.fx, r.fy, r.fl));
+      sfl[t] = r.fl;
+    } else {
+      const W4 w = wts(r.fx, r.fy);
+      sv[S_UL][t] = w.ul; sv[S_LL][t] = w.ll; sv[S_UR][t] = w.ur; sv[S_LR][t] = w.lr;
+    }
     double hr = __ldg(&mat_hr[r.mt - 1]);
     if (use_serp) hr = hr + r.serp;
     sv[S_V0 + 0][t] = d2f(r.tk);
@@ -284,14 +324,21 @@ struct HeatSpec {
     sv[S_V0 + 3][t] = d2f(hr);
     sv[S_V0 + 4][t] = d2f(r.ha);
   }
-  __device__ void accum(int role, int, int t, float (*sv)[kChunk], const uint8_t*, KSum2* a, SAcc) const {
-    const float w = sv[S_UL + (role & 3)][t];
+  __device__ void accum(int role, int, int t, float (*sv)[kChunk], const uint8_t* sfl, KSum2* a, SAcc) const {
+    const int k = role & 3;
+    const float w = sv[S_UL + k][t];
     const float2 w2 = make_float2(w, w);
     if (role < 4) {
       a[0].add(__fmul2_rn(w2, make_float2(sv[S_V0 + 0][t], sv[S_V0 + 1][t])));
-      a[1].add(make_float2(w * sv[S_V0 + 4][t], 0.f));
+      a[1].add(make_float2(w * sv[S_V0 + 4][t], kDen ? w : 0.f));
     } else {
       a[0].add(__fmul2_rn(w2, make_float2(sv[S_V0 + 2][t], sv[S_V0 + 3][t])));
+      if (kDen) {
+        const float wv = sv[S_VUL + k][t];
+        const bool h1 = sv[S_HALF][t] != 0.f;
+        a[1].add(make_float2(((quadrant_mask(sfl[t]) >> k) & 1u) ? w : 0.f, h1 ? 0.f : wv));
+        a[2].add(make_float2(h1 ? wv : 0.f, k == 0 ? sv[S_WC][t] : 0.f));
+      }
     }
   }
   __device__ void store(int role, int, int32_t cell, int32_t nc, const KSum2* a, SAcc, float* part) const {
@@ -300,23 +347,34 @@ struct HeatSpec {
       part[(size_t)(5 * k + 0) * nc + cell] = a[0].x();
       part[(size_t)(5 * k + 1) * nc + cell] = a[0].y();
       part[(size_t)(5 * k + 4) * nc + cell] = a[1].x();
+      if (kDen) part[(size_t)(kDenBase + k) * nc + cell] = a[1].y();
     } else {
       part[(size_t)(5 * k + 2) * nc + cell] = a[0].x();
       part[(size_t)(5 * k + 3) * nc + cell] = a[0].y();
+      if (kDen) {
+        part[(size_t)(kDenBase + 4 + k) * nc + cell] = a[1].x();
+        part[(size_t)(kDenBase + 9 + k) * nc + cell] = a[1].y();
+        part[(size_t)(kDenBase + 13 + k) * nc + cell] = a[2].x();
+        if (k == 0) part[(size_t)(kDenBase + 8) * nc + cell] = a[2].y();
+      }
     }
   }
 };
+using HeatSpec = HeatSpecT<false>;
 
 // Viscosity re-scatter (BilinearNumerator.jl:470-533): part slots 0-3 excl eta, 4 central eta
 // roles: 0 exclusive quadrants (shared slot q), 1 central node (registers)
 struct ViscSpec {
   static constexpr const char* kName = "k_cells<viscosity>";
   static constexpr int kRoles = 2, kNV = S_V0 + 1, kAcc = 1, kSlots = 4;
+  struct Cell {};
+  __device__ Cell cell(const DevGrid&, int32_t, int32_t) const { return Cell{}; }
   struct Raw { double eta; float fx, fy; uint8_t fl; };
   __device__ Raw load(const DevMarkers& mk, int32_t m) const {
     return Raw{mk.eta[m], mk.fx[m], mk.fy[m], mk.mflags[m]};
   }
-  __device__ void put(const Raw& r, const DevMarkers&, const DevGrid&, int t, float (*sv)[kChunk], uint8_t* sfl) const {
+  __device__ void put(const Raw& r, const Cell&, const DevMarkers&, const DevGrid&, int t, float (*sv)[kChunk],
+                      uint8_t* sfl) const {
     const W4 w = wts(r.fx, r.fy);
     sv[S_UL][t] = w.ul; sv[S_LL][t] = w.ll; sv[S_UR][t] = w.ur; sv[S_LR][t] = w.lr;
     sv[S_WC][t] = (1.f - fabsf(0.5f - r.fx)) * (1.f - fabsf(0.5f - r.fy));
@@ -370,14 +428,21 @@ struct SubgridStressSpec {
   const float *sxy1, *sxx1;  // FP32 mirrors
   const double* mat_mu;
   float dt, coef;
-  struct Raw { double eta, sxy, sxx; int32_t m, xn, yn, mt; float fx, fy; uint8_t fl; };
+  // the cell's basic indices and its four sxy1 nodes (UL, LL, UR, LR)
+  struct Cell { int32_t iy, ix; float n0, n1, n2, n3; };
+  __device__ Cell cell(const DevGrid& g, int32_t iy, int32_t ix) const {
+    const float* p = sxy1 + ((ix - 1) * g.ynum + (iy - 1));
+    return Cell{iy, ix, __ldg(p), __ldg(p + 1), __ldg(p + g.ynum), __ldg(p + g.ynum + 1)};
+  }
+  struct Raw { double eta, sxy, sxx; int32_t m, mt; float fx, fy; uint8_t fl; };
   __device__ Raw load(const DevMarkers& mk, int32_t m) const {
     Raw r;
-    r.m = m; r.fl = mk.mflags[m]; r.xn = mk.xn[m]; r.yn = mk.yn[m]; r.fx = mk.fx[m]; r.fy = mk.fy[m];
+    r.m = m; r.fl = mk.mflags[m]; r.fx = mk.fx[m]; r.fy = mk.fy[m];
     r.mt = mk.matid[m]; r.eta = mk.eta[m]; r.sxy = mk.sxy[m]; r.sxx = mk.sxx[m];
     return r;
   }
-  __device__ void put(const Raw& r, const DevMarkers& mk, const DevGrid& g, int t, float (*sv)[kChunk], uint8_t* sfl) const {
+  __device__ void put(const Raw& r, const Cell& cc, const DevMarkers& mk, const DevGrid& g, int t, float (*sv)[kChunk],
+                      uint8_t* sfl) const {
     const W4 w = wts(r.fx, r.fy);
     sv[S_UL][t] = w.ul; sv[S_LL][t] = w.ll; sv[S_UR][t] = w.ur; sv[S_LR][t] = w.lr;
     sv[S_WC][t] = (1.f - fabsf(0.5f - r.fx)) * (1.f - fabsf(0.5f - r.fy));
@@ -387,10 +452,10 @@ struct SubgridStressSpec {
     const float maxwell = d2f(r.eta) / mu;
     const float sdif = fmaxf(-coef * dt / maxwell, -30.f);
     const float term = -expm1f(sdif);  // 1 - exp(sdif), accurate for small |sdif|
-    const float sxy_g = gather4f(sxy1, g.ynum, r.yn, r.xn, r.fx, r.fy);
+    const float sxy_g = gather4v(cc.n0, cc.n1, cc.n2, cc.n3, r.fx, r.fy);
     const float rxy = (sxy_g - d2f(r.sxy)) * term;
     mk.sxy[r.m] = r.sxy + f2d(rxy);
-    const float sxx_g = gather_pressure_grid(sxx1, g, r.xn, r.yn, r.fx, r.fy);
+    const float sxx_g = gather_pressure_grid(sxx1, g, cc.ix, cc.iy, r.fx, r.fy);
     const float rxx = (sxx_g - d2f(r.sxx)) * term;
     mk.sxx[r.m] = r.sxx + f2d(rxx);
     sv[S_V0][t] = rxy;
@@ -429,16 +494,26 @@ struct SubgridHeatSpec {
   static constexpr int kRoles = 4, kNV = S_V0 + 1, kAcc = 1, kSlots = 0;
   const float *tk1, *kt1, *rhocp1;  // FP32 mirrors
   float dt, coef, inv_ts;  // inv_ts = 2/xstpavg^2 + 2/ystpavg^2
-  struct Raw { double tk; int32_t m, xn, yn; float fx, fy; };
-  __device__ Raw load(const DevMarkers& mk, int32_t m) const {
-    return Raw{mk.tk[m], m, mk.xn[m], mk.yn[m], mk.fx[m], mk.fy[m]};
+  // the four nodes (UL, LL, UR, LR) of the cell in tk1, kt1 and rhocp1
+  struct Cell { float4 tk, kt, rc; };
+  __device__ static float4 nodes(const float* f, const DevGrid& g, int32_t iy, int32_t ix) {
+    const float* p = f + ((ix - 1) * g.ynum + (iy - 1));
+    return make_float4(__ldg(p), __ldg(p + 1), __ldg(p + g.ynum), __ldg(p + g.ynum + 1));
   }
-  __device__ void put(const Raw& r, const DevMarkers& mk, const DevGrid& g, int t, float (*sv)[kChunk], uint8_t*) const {
+  __device__ Cell cell(const DevGrid& g, int32_t iy, int32_t ix) const {
+    return Cell{nodes(tk1, g, iy, ix), nodes(kt1, g, iy, ix), nodes(rhocp1, g, iy, ix)};
+  }
+  struct Raw { double tk; int32_t m; float fx, fy; };
+  __device__ Raw load(const DevMarkers& mk, int32_t m) const {
+    return Raw{mk.tk[m], m, mk.fx[m], mk.fy[m]};
+  }
+  __device__ void put(const Raw& r, const Cell& cc, const DevMarkers& mk, const DevGrid&, int t, float (*sv)[kChunk],
+                      uint8_t*) const {
     const W4 w = wts(r.fx, r.fy);
     sv[S_UL][t] = w.ul; sv[S_LL][t] = w.ll; sv[S_UR][t] = w.ur; sv[S_LR][t] = w.lr;
-    const float tn = gather4f(tk1, g.ynum, r.yn, r.xn, r.fx, r.fy);
-    const float k = gather4f(kt1, g.ynum, r.yn, r.xn, r.fx, r.fy);
-    const float rc = gather4f(rhocp1, g.ynum, r.yn, r.xn, r.fx, r.fy);
+    const float tn = gather4v(cc.tk.x, cc.tk.y, cc.tk.z, cc.tk.w, r.fx, r.fy);
+    const float k = gather4v(cc.kt.x, cc.kt.y, cc.kt.z, cc.kt.w, r.fx, r.fy);
+    const float rc = gather4v(cc.rc.x, cc.rc.y, cc.rc.z, cc.rc.w, r.fx, r.fy);
     const float tsg = rc / k / inv_ts;
     const float term = fmaxf(-coef * dt / tsg, -30.f);
     const float d = (tn - d2f(r.tk)) * (-expm1f(term));
@@ -473,7 +548,7 @@ static_assert(kChunk >= 32 * kSlotStride, "staging table too small");
 static_assert(kThreads == 32 * kPer, "one staged marker per thread per pass");
 
 template <class S>
-__global__ void __launch_bounds__(kThreads) k_cells(S spec, DevMarkers mk, DevGrid g,
+__global__ void __launch_bounds__(kThreads, 4) k_cells(S spec, DevMarkers mk, DevGrid g,
                                                     const int32_t* __restrict__ start,
                                                     const int32_t* __restrict__ perm, int32_t nc,
                                                     float* __restrict__ part) {
@@ -501,6 +576,13 @@ __global__ void __launch_bounds__(kThreads) k_cells(S spec, DevMarkers mk, DevGr
   const int32_t nmax = s_max;
   const int32_t my_cnt = s_cnt[lane];
   const int32_t st_beg = s_beg[sj], st_cnt = s_cnt[sj];
+  // constants of this thread's staging cell (basic indices iy, ix; markers of the cell-sorted
+  // list of a cell carry exactly these indices)
+  typename S::Cell cc{};
+  if (st_cnt > 0) {
+    const int32_t cell = c0 + sj, rows = g.ynum - 1;
+    cc = spec.cell(g, cell % rows + 1, cell / rows + 1);
+  }
   KSum2 acc[S::kAcc];
 #pragma unroll
   for (int k = 0; k < S::kAcc; ++k) acc[k].init();
@@ -512,7 +594,7 @@ __global__ void __launch_bounds__(kThreads) k_cells(S spec, DevMarkers mk, DevGr
   if (have) r = spec.load(mk, __ldg(&perm[st_beg + si]));
   for (int32_t base = 0; base < nmax; base += kPer) {
     __syncthreads();
-    if (have) spec.put(r, mk, g, sj * kSlotStride + si, sv, sfl);
+    if (have) spec.put(r, cc, mk, g, sj * kSlotStride + si, sv, sfl);
     __syncthreads();
     have = m_next >= 0;
     if (have) r = spec.load(mk, m_next);
@@ -570,19 +652,20 @@ struct NodeCtx {
   }
 };
 
-__global__ void k_finish_denoms(NodeCtx n, double* wtnodes, double* wtetas, double* wtetan, double* wtnodes_vy) {
+__global__ void k_finish_denoms(NodeCtx n, int base, double* wtnodes, double* wtetas, double* wtetan,
+                                double* wtnodes_vy) {
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const int64_t nb = (int64_t)n.ynum * n.xnum, np = (int64_t)(n.ynum - 1) * (n.xnum - 1),
                 nv = (int64_t)n.ynum * (n.xnum + 1);
   if (t < nb) {
     const int32_t i = (int32_t)(t % n.ynum) + 1, j = (int32_t)(t / n.ynum) + 1;
-    wtnodes[t] = f2d(n.basic(i, j, 0, 1));
-    wtetas[t] = f2d(n.basic(i, j, 4, 1));
+    wtnodes[t] = f2d(n.basic(i, j, base + 0, 1));
+    wtetas[t] = f2d(n.basic(i, j, base + 4, 1));
   }
-  if (t < np) wtetan[t] = f2d(n.part[(size_t)8 * n.nc + t]);
+  if (t < np) wtetan[t] = f2d(n.part[(size_t)(base + 8) * n.nc + t]);
   if (t < nv) {
     const int32_t i = (int32_t)(t % n.ynum) + 1, jv = (int32_t)(t / n.ynum) + 1;
-    wtnodes_vy[t] = f2d(n.vy(i, jv, 9));
+    wtnodes_vy[t] = f2d(n.vy(i, jv, base + 9));
   }
 }
 
@@ -761,6 +844,18 @@ int ensure_markers(eb_ctx* c, std::initializer_list<int> fields) {
 
 }  // namespace
 
+namespace {
+int finish_denominators(eb_ctx* c, int base) {
+  const int64_t n = (int64_t)c->ynum * (c->xnum + 1);
+  EB_PROF(c, "k_finish_denoms");
+  k_finish_denoms<<<node_blocks(c, n), 256, 0, c->stream>>>(node_ctx(c), base, c->gf[EB_G_WTNODES],
+                                                            c->gf[EB_G_WTETAS], c->gf[EB_G_WTETAN],
+                                                            c->gf[EB_G_WTNODES_VY]);
+  EB_LAUNCHED(c);
+  return EB_OK;
+}
+}  // namespace
+
 int launch_denominators(eb_ctx* c) {
   if (c->M > 0) {
     int rc = run_cells(c, DenomSpec{});
@@ -768,12 +863,7 @@ int launch_denominators(eb_ctx* c) {
   } else {
     EB_CK(c, cudaMemsetAsync(c->part, 0, (size_t)kMaxSlots * c->cs.ncells * sizeof(float), c->stream));
   }
-  const int64_t n = (int64_t)c->ynum * (c->xnum + 1);
-  EB_PROF(c, "k_finish_denoms");
-  k_finish_denoms<<<node_blocks(c, n), 256, 0, c->stream>>>(node_ctx(c), c->gf[EB_G_WTNODES], c->gf[EB_G_WTETAS],
-                                                            c->gf[EB_G_WTETAN], c->gf[EB_G_WTNODES_VY]);
-  EB_LAUNCHED(c);
-  return EB_OK;
+  return finish_denominators(c, 0);
 }
 
 int launch_scatter_stokes(eb_ctx* c) {
@@ -824,18 +914,20 @@ int launch_scatter_stokes(eb_ctx* c) {
   return EB_OK;
 }
 
-int launch_scatter_heat(eb_ctx* c) {
+int launch_scatter_heat(eb_ctx* c, bool with_denominators) {
   int rc = ensure_markers(c, {EB_M_MATID, EB_M_TK, EB_M_KT, EB_M_RHOCP, EB_M_HA, EB_M_SERP_HR});
   if (rc) return rc;
   rc = ensure_grids(c, {EB_G_TK1, EB_G_TK0, EB_G_TK2, EB_G_KT1, EB_G_KT0, EB_G_RHOCP1, EB_G_RHOCP0, EB_G_HR1, EB_G_HR0,
                         EB_G_HA1, EB_G_HA0, EB_G_BTOPT, EB_G_BBOTTOMT, EB_G_BLEFTT, EB_G_BRIGHTT});
   if (rc) return rc;
   if (c->M > 0) {
-    rc = run_cells(c, HeatSpec{c->mats.hr, (int)(c->P.iuse_serpentinization == 1)});
+    const int serp = (int)(c->P.iuse_serpentinization == 1);
+    rc = with_denominators ? run_cells(c, HeatSpecT<true>{c->mats.hr, serp}) : run_cells(c, HeatSpec{c->mats.hr, serp});
     if (rc) return rc;
   } else {
     EB_CK(c, cudaMemsetAsync(c->part, 0, (size_t)kMaxSlots * c->cs.ncells * sizeof(float), c->stream));
   }
+  if (with_denominators && (rc = finish_denominators(c, kDenBase))) return rc;  // k_finish_heat reads wtnodes
   double** gf = c->gf;
   HeatGrids G{gf[EB_G_TK1], gf[EB_G_TK0], gf[EB_G_KT1], gf[EB_G_KT0], gf[EB_G_RHOCP1], gf[EB_G_RHOCP0],
               gf[EB_G_HR1], gf[EB_G_HR0], gf[EB_G_HA1], gf[EB_G_HA0], gf[EB_G_TK2], gf[EB_G_WTNODES]};

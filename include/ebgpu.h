@@ -200,6 +200,13 @@ int eb_get_marker_inside_flags(eb_ctx* ctx);
  * weight-sum denominators wtnodes/wtetas/wtetan/wtnodes_vy (BilinearDenominator.jl:34-157). */
 int eb_initialize_bilinear_interpolation(eb_ctx* ctx);
 
+/* eb_initialize_bilinear_interpolation followed by eb_interpolate_marker_heat_parameters_to_grid
+ * (the order of MarkerInCell's marker cycle), with the weight denominators summed in the heat
+ * scatter's walk of the cell lists instead of a walk of their own.  Every output (cell indices,
+ * wtnodes/wtetas/wtetan/wtnodes_vy, the heat transport arrays and their backups) is
+ * bit-identical to the two calls in sequence.  Needs the materials (as the heat scatter does). */
+int eb_initialize_bilinear_interpolation_and_heat_scatter(eb_ctx* ctx);
+
 /* MarkersToStokesArrays.interpolate_markers_to_transport_arrays!
  *   (src/interpolation/utils/MarkersToStokesArrays.jl:39-45): backup+clear
  * (BackupTransportArrays.jl:33-98), numerators (BilinearNumerator.jl:205-454),

@@ -88,3 +88,51 @@ def test_fused_rheology_equals_the_two_calls(eb, plasticity):
         assert np.array_equal(out[False][k], out[True][k]), k
     if plasticity:
         assert np.any(out[True]["pfailure"] == 1.0)
+
+
+def _on_lines(eb):
+    """sinking_block with markers exactly on basic and staggered grid lines (two or four exclusive
+    quadrants at once), on the domain edges and outside it."""
+    model = eb.synthetic.config("sinking_block")
+    g = model.grid
+    rng = np.random.default_rng(11)
+    xs = np.concatenate([g.gridx_b, g.gridx_vy[1:-1], np.nextafter(g.gridx_b, np.inf)[:-1]])
+    ys = np.concatenate([g.gridy_b, g.gridy_vx[1:-1], np.nextafter(g.gridy_b, np.inf)[:-1]])
+    n = model.marknum
+    x, y = model.markers["x"].copy(), model.markers["y"].copy()
+    pick = rng.random(n) < 0.3
+    x[pick] = rng.choice(xs, int(pick.sum()))
+    y[pick] = rng.choice(ys, int(pick.sum()))
+    x[:4] = [g.xmin, g.xmax, g.xmin - 1.0, g.xmax + 1e-9]
+    y[:4] = [g.ymin, g.ymax, g.ymax, g.ymin]
+    model.markers["x"], model.markers["y"] = x, y
+    return model
+
+
+@pytest.mark.parametrize("name", ["rift_small", "sinking_block", "on_lines"])
+def test_bilinear_setup_and_heat_scatter_equal_the_two_calls(eb, name):
+    """eb_initialize_bilinear_interpolation_and_heat_scatter (denominators summed in the heat
+    fold) gives, bit for bit, what eb_initialize_bilinear_interpolation followed by
+    eb_interpolate_marker_heat_parameters_to_grid gives: cell indices, the four weight sums and
+    the heat transport arrays with their backups."""
+    model = _on_lines(eb) if name == "on_lines" else eb.synthetic.config(name)
+    grids = ("wtnodes", "wtetas", "wtetan", "wtnodes_vy", "tk1", "kt1", "rhocp1", "hr1", "ha1",
+             "tk0", "kt0", "rhocp0", "hr0", "ha0")
+    out = {}
+    for fused in (False, True):
+        mic = eb.MarkerInCell(0)
+        mic.load_model(model)
+        mic.get_marker_inside_flags()
+        if fused:
+            mic.initialize_bilinear_interpolation_and_heat_scatter()
+        else:
+            mic.initialize_bilinear_interpolation()
+            mic.interpolate_marker_heat_parameters_to_grid()
+        out[fused] = {k: mic.download_grid(k) for k in grids}
+        out[fused].update({k: mic.download_marker(k) for k in ("xn", "yn", "inside")})
+        mic.close()
+    for k in out[False]:
+        assert np.array_equal(out[False][k], out[True][k]), k
+    assert np.any(out[True]["wtetas"] != out[True]["wtnodes"])  # exclusive and inclusive sums differ
+    if name == "on_lines":
+        assert np.any(out[True]["inside"] != 1)  # some markers outside the domain
