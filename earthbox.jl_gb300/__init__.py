@@ -511,7 +511,8 @@ class MarkerInCell:
         return history
 
     def time_step(self, nglobal: int = 5, tolerance_picard: float = 1e-3, iuse_harmonic: int = 1,
-                  heat: bool = False, warm_start: bool = True, **solve_kw) -> dict:
+                  heat: bool = False, warm_start: bool = True, marker_cell_displ_max: float | None = None,
+                  **solve_kw) -> dict:
         """One pass of TimeLoop.run_loop!'s body (src/time_loop/TimeLoop.jl:181-194) restricted to the
         hot path, with a fixed time step:
           execute_pre_solver_steps! (:203-230): initialize_bilinear_interpolation! and the
@@ -527,9 +528,21 @@ class MarkerInCell:
           and the inside flags of the moved markers.
         warm_start: every Stokes solve starts from the latest solution (the previous Picard iterate,
         or the previous time step's solution for the first solve of a step).
-        Returns {"picard": per-iteration records, "heat": heat-loop report or None}."""
+        marker_cell_displ_max: when given, the step runs as the reference's time loop does with a
+        displacement limit: it starts from the viscoelastic time step (params "timestep_viscoelastic",
+        else the time step the parameters were set with; TimeLoop.update_model_time_step!, :138) and,
+        after the Picard loop, TimeStep.adjust_time_step_using_displacement_limit! (:244) shortens it
+        so that no marker moves more than that fraction of a cell; the post-Stokes steps and the
+        advection then use the shortened step.
+        Returns {"picard": per-iteration records, "heat": heat-loop report or None, "timestep": s}."""
         p = getattr(self, "_params", {})
         nodes = int(p.get("itype_global", 0)) == 1
+        if marker_cell_displ_max is not None:
+            if "timestep_viscoelastic" not in p:
+                p["timestep_viscoelastic"] = float(p["timestep"])
+            if p["timestep"] != p["timestep_viscoelastic"]:
+                p["timestep"] = float(p["timestep_viscoelastic"])
+                self.set_params(p)
         self.get_marker_inside_flags()
         self.initialize_bilinear_interpolation_and_heat_scatter()
         self.update_marker_rheology_and_viscoplastic_viscosity(use_marker_plasticity=not nodes)
@@ -542,6 +555,11 @@ class MarkerInCell:
         self.interpolate_stag_velocity_to_basic_grid()
         if nodes:
             self.calc_marker_viscoplastic_viscosity()
+        if marker_cell_displ_max is not None:
+            dt, updated = self.update_model_time_step_using_displacement_limit(p["timestep"], marker_cell_displ_max)
+            if updated:
+                p["timestep"] = float(dt)
+                self.set_params(p)
         self.forecast_viscoelastic_grid_stress()
         self.calculate_deviatoric_grid_stress_change()
         self.post_stokes_marker_gathers()
@@ -552,7 +570,7 @@ class MarkerInCell:
         self.advect_markers_and_rotate_stress()
         self.update_marker_strain()
         self.get_marker_inside_flags()
-        return {"picard": hist, "heat": hrep}
+        return {"picard": hist, "heat": hrep, "timestep": float(p.get("timestep", 0.0))}
 
     # ------------------------------------------- learned preconditioner stage --
     def learned_init(self, seed: int = 0) -> None:

@@ -477,6 +477,67 @@ def stress_buildup(xnum: int = 51, ynum: int = 51, mpc: int = 4) -> Model:
     return Model("stress_buildup", grid, mats, params, m, grids)
 
 
+def channel_flow_non_newtonian(xnum: int = 51, ynum: int = 21, mpc: int = 5) -> Model:
+    """The reference's non-Newtonian channel-flow benchmark, as configured in
+    src/benchmarks/models/channel_flow_non_newtonian/{model,materials}.yml and the benchmark
+    material library (NonNewtonianMaterialChannelFlowBenchmark): a 10 x 10 km vertical channel on
+    51 x 21 nodes with 5 x 5 markers per cell on a regular lattice, one dislocation-creep material
+    (5e-20 1/s/MPa^n, n = 3, no activation energy or volume; 3200 kg/m^3; shear modulus 1e21 Pa),
+    no gravity, the nodal plasticity loop with one Picard iteration per step, and a 100 kyr time
+    step limited to half a cell of marker displacement.  VerticalChannelFlowNonNewtonianBC.jl:
+    pressure 1e9 Pa on the top row of pressure cells and 0 on the bottom row (pressure condition
+    mode 1), zero vertical gradients of vx and vy through the top and bottom (VerticalChannelBC.jl),
+    no slip on both sides."""
+    W = H = 10e3
+    grid = staggered_grid(np.linspace(0.0, W, xnum), np.linspace(0.0, H, ynum))
+    mx, my = (xnum - 1) * mpc, (ynum - 1) * mpc
+    x = np.repeat((np.arange(mx) + 0.5) * (W / mx), my)
+    y = np.tile((np.arange(my) + 0.5) * (H / my), mx)
+    n = len(x)
+    mat_flow = np.zeros((1, 12))
+    mat_flow[0, [1, 2, 3, 4]] = [5e-20, 3.0, 0.0, 0.0]
+    mats = Materials(
+        mat_mu=np.array([1e21]), mat_hr=np.zeros(1), mat_flow_type=np.array([1], np.int64),
+        mat_flow=np.asfortranarray(mat_flow), mat_plastic=np.asfortranarray(np.zeros((1, 6))),
+        mat_rho=np.array([3200.0]))
+    T0 = 273.15
+    m = {"x": x, "y": y, "matid": np.ones(n, np.int16), "rho": np.full(n, 3200.0), "eta": np.full(n, 1e21),
+         "eta_flow": np.full(n, 1e21), "preexp": np.full(n, 5e-20), "sr_ratio": np.ones(n), "tk": np.full(n, T0),
+         "kt": np.full(n, 3.0), "rhocp": np.full(n, 3200.0 * 3000.0), "ha": np.zeros(n)}
+    for f in ("cohesion", "fric", "fric_ini", "sxx", "sxy", "exx", "exy", "pr", "gii", "strain_plastic"):
+        m[f] = np.zeros(n)
+    _fields_common(np.random.Generator(np.random.Philox(0)), n, m)
+    m["pfailure"][:] = 0.0
+    grids = _analytic_grids(grid, v0=0.0, eta_ref=1e21, rho_ref=3200.0, T0=T0, T1=T0, depth_T1=H, y_surface=0.0)
+    grids.update(velocity_bcs(grid))
+    F = np.asfortranarray
+    X, Y = xnum, ynum
+    grids["btopx"] = F(np.column_stack([np.zeros(X), np.ones(X)]))
+    grids["bbottomx"] = F(np.column_stack([np.zeros(X), np.ones(X)]))
+    grids["btopy"] = F(np.column_stack([np.zeros(X + 1), np.ones(X + 1)]))
+    grids["bbottomy"] = F(np.column_stack([np.zeros(X + 1), np.ones(X + 1)]))
+    grids["bleftx"] = F(np.zeros((Y + 1, 2)))
+    grids["brightx"] = F(np.zeros((Y + 1, 2)))
+    grids["blefty"] = F(np.column_stack([np.zeros(Y), -np.ones(Y)]))
+    grids["brighty"] = F(np.column_stack([np.zeros(Y), -np.ones(Y)]))
+    params = default_params(timestep=1e5 * YEAR, viscosity_min=1e18, viscosity_max=1e25, powerlaw_stress_min=1e4,
+                            itype_global=1, temperature_top=T0, ntimestep=1)
+    params.update(stokes_params(pressure_bc_mode=1, pressure_bc=1e9, gravity_y=0.0, iuse_interface_stabilization=0))
+    params["marker_cell_displ_max"] = 0.5
+    return Model("channel_flow_non_newtonian", grid, mats, params, m, grids)
+
+
+def channel_flow_velocity(x: np.ndarray, width: float, ydim: float, top_pressure: float, pre_exponential_dc: float,
+                          n: float) -> np.ndarray:
+    """Analytic vertical velocity of pressure-driven power-law flow between no-slip walls, as the
+    reference's benchmark evaluates it (post_processing/analytical/ChannelFlowNonNewtonianManager.jl):
+    C1 = 2 A / (1e6)^n from the MPa-based pre-exponential factor A, dp/dy = -top_pressure / ydim and
+    v(x) = C1 / (n + 1) (-dp/dy)^n ((W/2)^(n+1) - (x - W/2)^(n+1)) (m/s, positive downwards)."""
+    c1 = pre_exponential_dc * 2.0 / (1e6 ** n)
+    grad = -top_pressure / ydim
+    return c1 / (n + 1.0) * (-grad) ** n * ((width / 2.0) ** (n + 1.0) - np.abs(x - width / 2.0) ** (n + 1.0))
+
+
 def ramberg_wave_velocity(h1: float, h2: float, rho1: float, rho2: float, eta1: float, eta2: float, amp: float,
                           lam: float, g: float = 9.81) -> float:
     """Ramberg's (1968) analytical vertical velocity at the crest of a sinusoidal interface

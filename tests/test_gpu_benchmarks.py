@@ -10,7 +10,11 @@ reference's relative error limit of 3.5 %.
 
 Viscoelastic stress buildup (src/benchmarks/models/viscoelastic_stress_buildup): whole time
 steps of a Maxwell body in pure shear, held to the reference's discrete stress update and to the
-continuous Maxwell curve."""
+continuous Maxwell curve.
+
+Non-Newtonian channel flow (src/benchmarks/models/channel_flow_non_newtonian): sixty time steps
+of pressure-driven power-law flow against the analytic profile and the oracle."""
+import numpy as np
 import pytest
 
 from stokes_cases import bilinear_basic
@@ -83,4 +87,35 @@ def test_viscoelastic_stress_buildup_matches_maxwell(eb):
         assert abs(s - a) / a < abs(d - a) / a + 1e-6, (t, s, a)
         if t >= 3000:
             assert abs(s - a) / a < 1e-3, (t, s, a)
+    mic.close()
+
+
+def test_non_newtonian_channel_flow_matches_the_power_law_profile(eb):
+    """The reference's non-Newtonian channel-flow benchmark (models/channel_flow_non_newtonian,
+    post_processing/analytical/ChannelFlowNonNewtonianManager.jl) through sixty GPU time steps:
+    composite-creep rheology, one nodal Picard iteration per step, the displacement-limited time
+    step, RK4 advection and the channel recycling.  The basic-node vy profile of row 11 must lie
+    within the reference's 1.1 % limit of the analytic power-law flow, and within 0.3 % of the
+    oracle's profile after the same sixty steps (FP32 weights and gathers carried through sixty
+    nonlinear steps; 1.7e-3 measured)."""
+    from test_stokes_oracle import channel_flow_error, channel_flow_oracle
+    syn = eb.synthetic
+    model = syn.channel_flow_non_newtonian()
+    g = model.grid
+    mic = eb.MarkerInCell(0)
+    mic.load_model(model)
+    displ = model.params["marker_cell_displ_max"]
+    for _ in range(60):
+        rep = mic.time_step(1, 1e-3, iuse_harmonic=0, marker_cell_displ_max=displ, rtol=1e-10)
+        assert rep["picard"][-1]["status"] == 0, rep["picard"]
+        mic.recycle_markers(1, 1, 1, g.xmax, g.ymax, 0.0, 0.0, model.params["temperature_top"], 0, 0, recycle_type=3)
+    vyb = mic.download_grid("vyb")
+    err = channel_flow_error(eb, model, vyb)
+    ref_model, ref_vyb = channel_flow_oracle(eb)
+    dev = float(np.max(np.abs(vyb[10] - ref_vyb[10])) / np.max(np.abs(ref_vyb[10])))
+    print(f"\nnon-Newtonian channel flow: last time step {rep['timestep'] / 3.15576e7:.1f} yr, peak "
+          f"{vyb[10].max() * 3.15576e9:.3f} cm/yr; largest relative error against the analytic profile "
+          f"{100 * err:.3f} % (limit 1.1 %); against the oracle {dev:.2e}")
+    assert err < 0.011, err
+    assert dev < 3e-3, dev
     mic.close()

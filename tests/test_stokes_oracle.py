@@ -194,3 +194,59 @@ def test_oracle_rayleigh_taylor_matches_ramberg(eb):
     v = bilinear_basic(g, vyb, 0.5 * (g.xmax - g.xmin), 1500.0 - 10.0)
     va = eb.synthetic.ramberg_wave_velocity(1500.0, 1500.0, 3000.0, 2900.0, 1e13, 1e19, 10.0, 4000.0)
     assert abs(v - va) / abs(va) < 0.035, (v, va)
+
+
+def channel_flow_oracle(eb, nsteps: int = 60):
+    """The reference's non-Newtonian channel-flow benchmark through the oracle: per step the
+    pre-solver averages and rheology, one nodal Picard iteration (direct solve), the
+    displacement-limited time step (TimeLoop.jl:244), the post-Stokes steps, RK4 advection and
+    the channel recycling (MarkerRecycle types/Channel.jl).  Returns (model, basic-node vy)."""
+    from oracle.picard import OraclePicard
+    from oracle import boundary as B
+    model = eb.synthetic.channel_flow_non_newtonian()
+    op = OraclePicard(model)
+    p, g, m = op.model.params, model.grid, op.mic
+    dt_ve = p["timestep"]
+    for _ in range(nsteps):
+        p["timestep"] = dt_ve
+        m.get_marker_inside_flags()
+        m.initialize_bilinear_interpolation()
+        m.interpolate_marker_heat_parameters_to_grid()
+        m.update_marker_rheology()
+        m.update_marker_viscoplastic_viscosity(use_marker_plasticity=False)
+        m.interpolate_marker_stokes_parameters_to_grid()
+        op.so.interpolate_basic_viscoplastic_viscosity_to_pressure_grid(0)
+        op.picard_loop_nodes(1, 1e-3, 0)
+        op.so.interpolate_stag_velocity_to_basic_grid()
+        m.calc_marker_viscoplastic_viscosity()
+        p["timestep"] = B.timestep_displacement_limit(g, op.gr["vx1"], op.gr["vy1"], p["marker_cell_displ_max"], 0,
+                                                      dt_ve)
+        op.so.forecast_viscoelastic_grid_stress()
+        m.post_stokes_marker_gathers()
+        m.update_subgrid_stress()
+        m.apply_marker_stress_correction()
+        m.advect_markers_and_rotate_stress()
+        m.update_marker_strain()
+        y, tk, _ = B.recycle_channel(m.mk["y"], m.mk["tk"], g.ymin, g.ymax, p["temperature_top"], p["temperature_top"])
+        m.mk["y"][:] = y
+        m.mk["tk"][:] = tk
+    return model, op.gr["vyb"].copy()
+
+
+def channel_flow_error(eb, model, vyb) -> float:
+    """The reference's check (ChannelFlowNonNewtonianManager.jl, Options.jl y_index = 11): the
+    basic-node vy profile of row 11 against the analytic profile, largest relative error over the
+    nodes where the analytic velocity is not zero."""
+    g = model.grid
+    ana = eb.synthetic.channel_flow_velocity(g.gridx_b, g.xmax - g.xmin, (g.ymax - g.ymin) - g.ystp_b[0], 1e9, 5e-20,
+                                             3.0)
+    nz = ana != 0.0
+    return float(np.max(np.abs(vyb[10, nz] - ana[nz]) / np.abs(ana[nz])))
+
+
+def test_oracle_channel_flow_non_newtonian_matches_the_power_law(eb):
+    """Sixty steps as the reference runs the benchmark (Options.jl time_steps = [60]): the
+    velocity profile within the reference's 1.1 % limit of the analytic power-law flow."""
+    model, vyb = channel_flow_oracle(eb)
+    err = channel_flow_error(eb, model, vyb)
+    assert err < 0.011, err
