@@ -538,6 +538,74 @@ def channel_flow_velocity(x: np.ndarray, width: float, ydim: float, top_pressure
     return c1 / (n + 1.0) * (-grad) ** n * ((width / 2.0) ** (n + 1.0) - np.abs(x - width / 2.0) ** (n + 1.0))
 
 
+def solid_body_rotation(xnum: int = 51, ynum: int = 51, mpc: int = 5) -> Model:
+    """The reference's solid-body-rotation benchmark, as configured in
+    src/benchmarks/models/solid_body_rotation/{model,materials}.yml and the benchmark material
+    library (MaterialForSolidBodyRotation): a 50 x 50 km box on 51 x 51 nodes with 5 x 5 markers per
+    cell on a regular lattice, one isoviscous material (1e19 Pa s, shear modulus 1e20 Pa, 3000 kg/m^3,
+    1000 J/kg/K, conductivity 2e-6 W/m/K), 727 C everywhere but the temperature wave
+    (TemperatureWave.jl: 1500 K where 0.4 <= x/xsize <= 0.6 and 0.1 <= y/ysize <= 0.3), the
+    kinematic velocity of solid_body_rotation_velocity (3.1536 cm/yr at the box's half width),
+    SolidBodyRotationBC.jl's thermal conditions (zero flux through the top and the bottom, 727 C on
+    both sides), subgrid temperature diffusion on and subgrid stress diffusion off, and a
+    55344.0275 yr time step: one rotation takes 90 steps."""
+    W = H = 50e3
+    grid = staggered_grid(np.linspace(0.0, W, xnum), np.linspace(0.0, H, ynum))
+    mx, my = (xnum - 1) * mpc, (ynum - 1) * mpc
+    x = np.repeat((np.arange(mx) + 0.5) * (W / mx), my)
+    y = np.tile((np.arange(my) + 0.5) * (H / my), mx)
+    n = len(x)
+    T0 = 727.0 + 273.15
+    T = np.full(n, T0)
+    T[(0.4 <= x / W) & (x / W <= 0.6) & (0.1 <= y / H) & (y / H <= 0.3)] = 1500.0
+    mats = Materials(
+        mat_mu=np.array([1e20]), mat_hr=np.zeros(1), mat_flow_type=np.array([0], np.int64),
+        mat_flow=np.asfortranarray(np.zeros((1, 12))), mat_plastic=np.asfortranarray(np.zeros((1, 6))),
+        mat_rho=np.array([3000.0]))
+    mats.mat_flow[0, 0] = 1e19
+    m = {"x": x, "y": y, "matid": np.ones(n, np.int16), "rho": np.full(n, 3000.0), "eta": np.full(n, 1e19),
+         "eta_flow": np.full(n, 1e19), "sr_ratio": np.ones(n), "tk": T, "kt": np.full(n, 2e-6),
+         "rhocp": np.full(n, 3000.0 * 1000.0), "ha": np.zeros(n)}
+    for f in ("cohesion", "fric", "fric_ini", "preexp", "sxx", "sxy", "exx", "exy", "pr", "gii", "strain_plastic"):
+        m[f] = np.zeros(n)
+    _fields_common(np.random.Generator(np.random.Philox(0)), n, m)
+    m["pfailure"][:] = 0.0
+    grids = _analytic_grids(grid, v0=0.0, eta_ref=1e19, rho_ref=3000.0, T0=T0, T1=T0, depth_T1=H, y_surface=0.0)
+    grids.update(velocity_bcs(grid))
+    F = np.asfortranarray
+    X, Y = xnum, ynum
+    grids["btopt"] = F(np.column_stack([np.zeros(X), np.ones(X)]))
+    grids["bbottomt"] = F(np.column_stack([np.zeros(X), np.ones(X)]))
+    grids["bleftt"] = F(np.column_stack([np.full(Y, T0), np.zeros(Y)]))
+    grids["brightt"] = F(np.column_stack([np.full(Y, T0), np.zeros(Y)]))
+    vx1, vy1 = solid_body_rotation_velocity(grid, 3.1536e-2 / YEAR)
+    grids["vx1"], grids["vy1"] = vx1, vy1
+    params = default_params(timestep=55344.0275 * YEAR, viscosity_min=1e18, viscosity_max=1e25, temperature_top=T0,
+                            subgrid_diff_coef_stress=0.0, subgrid_diff_coef_temp=1.0)
+    params.update(stokes_params(gravity_y=0.0, iuse_interface_stabilization=0))
+    params.update(max_temp_change=20.0, iuse_adiabatic_heating=0, iuse_shear_heating=0, iuse_heat=1,
+                  velocity_rotation=3.1536e-2 / YEAR)
+    return Model("solid_body_rotation", grid, mats, params, m, grids)
+
+
+def solid_body_rotation_velocity(grid: Grid, vrotation: float) -> tuple:
+    """Kinematics.solid_body_rotation! (src/kinematics/Kinematics.jl): the staggered velocities
+    of a rigid rotation about the box centre, vrotation at half the box width:
+    vx1[i, j] = -vrotation ((i - 1.5) dy - ysize/2) / (xsize/2) and
+    vy1[i, j] = vrotation ((j - 1.5) dx - xsize/2) / (xsize/2) (1-based i, j, mean spacings)."""
+    X, Y = grid.xnum, grid.ynum
+    W, H = grid.xmax - grid.xmin, grid.ymax - grid.ymin
+    i = np.arange(1, Y + 2, dtype=np.float64)[:, None]
+    j = np.arange(1, X + 1, dtype=np.float64)[None, :]
+    dy = ((i - 1.0) - 0.5) * grid.ystpavg - H / 2.0
+    vx1 = np.broadcast_to(-vrotation * (dy / (W / 2.0)), (Y + 1, X))
+    i = np.arange(1, Y + 1, dtype=np.float64)[:, None]
+    j = np.arange(1, X + 2, dtype=np.float64)[None, :]
+    dx = (j - 1.0 - 0.5) * grid.xstpavg - W / 2.0
+    vy1 = np.broadcast_to(vrotation * (dx / (W / 2.0)), (Y, X + 1))
+    return np.asfortranarray(vx1), np.asfortranarray(vy1)
+
+
 def ramberg_wave_velocity(h1: float, h2: float, rho1: float, rho2: float, eta1: float, eta2: float, amp: float,
                           lam: float, g: float = 9.81) -> float:
     """Ramberg's (1968) analytical vertical velocity at the crest of a sinusoidal interface

@@ -13,7 +13,10 @@ steps of a Maxwell body in pure shear, held to the reference's discrete stress u
 continuous Maxwell curve.
 
 Non-Newtonian channel flow (src/benchmarks/models/channel_flow_non_newtonian): sixty time steps
-of pressure-driven power-law flow against the analytic profile and the oracle."""
+of pressure-driven power-law flow against the analytic profile and the oracle.
+
+Solid-body rotation (src/benchmarks/models/solid_body_rotation): one rotation of a hot square in
+a kinematic velocity field (advection and the heat step), back on its initial profile."""
 import numpy as np
 import pytest
 
@@ -118,4 +121,40 @@ def test_non_newtonian_channel_flow_matches_the_power_law_profile(eb):
           f"{100 * err:.3f} % (limit 1.1 %); against the oracle {dev:.2e}")
     assert err < 0.011, err
     assert dev < 3e-3, dev
+    mic.close()
+
+
+def test_solid_body_rotation_returns_the_temperature_wave(eb):
+    """The reference's solid-body-rotation benchmark (models/solid_body_rotation,
+    post_processing/analytical/SolidBodyRotationManager.jl) through ninety GPU steps (one
+    rotation): inside flags, bilinear set-up with the heat averages, the kinematic velocity's
+    strain rate and spin, the heat step with subgrid diffusion, and RK4 advection.  The row-11
+    grid temperature must come back to its step-1 profile within the reference's 2 % (Celsius),
+    and agree with the oracle's after the same steps within 0.05 K."""
+    from benchmark_cases import ROTATION_STEPS, Y_INDEX, rotation_check, solid_body_rotation_oracle
+    syn = eb.synthetic
+    model = syn.solid_body_rotation()
+    mic = eb.MarkerInCell(0)
+    mic.load_model(model)
+    rows = []
+    for step in range(1, ROTATION_STEPS + 2):
+        mic.get_marker_inside_flags()
+        mic.initialize_bilinear_interpolation_and_heat_scatter()
+        if step in (1, ROTATION_STEPS + 1):
+            rows.append(mic.download_grid("tk1")[Y_INDEX - 1, :].copy())
+        if step == ROTATION_STEPS + 1:
+            break
+        mic.update_grid_strain_rate_and_spin()
+        rep = mic.update_marker_temp_for_grid_and_subgrid_changes(model.params)
+        assert rep is not None
+        mic.advect_markers_and_rotate_stress()
+    err = rotation_check(model, rows[0], rows[1])
+    _, o0, o1 = solid_body_rotation_oracle(eb)
+    dev = float(np.max(np.abs(rows[1] - o1)))
+    print(f"\nsolid body rotation: one rotation in {ROTATION_STEPS} steps, largest relative change of the "
+          f"row-{Y_INDEX} profile {100 * err:.4f} % (limit 2 %); against the oracle {dev:.2e} K")
+    assert rows[0].max() > 1400.0
+    assert float(np.max(np.abs(rows[0] - o0) / o0)) < 1e-6  # step 1: FP32 weight sums, 3e-8 measured
+    assert err < 0.02, err
+    assert dev < 0.05, dev
     mic.close()
