@@ -117,9 +117,13 @@ class MarkerInCell:
         self.xnum, self.ynum = int(g.xnum), int(g.ynum)
 
     def set_materials(self, m: "synthetic.Materials") -> None:
+        """The material tables; mat_flow may hold the first 12 columns of the reference's
+        nmat x 17 flow-law table (the composite-creep laws), the rest is then zero."""
+        flow = np.zeros((len(m.mat_mu), 17))
+        flow[:, :np.shape(m.mat_flow)[1]] = m.mat_flow
         keep = [np.ascontiguousarray(m.mat_mu, np.float64), np.ascontiguousarray(m.mat_hr, np.float64),
                 np.ascontiguousarray(m.mat_flow_type, np.int64),
-                np.asfortranarray(m.mat_flow, np.float64).ravel(order="F"),
+                np.asfortranarray(flow).ravel(order="F"),
                 np.asfortranarray(m.mat_plastic, np.float64).ravel(order="F"),
                 np.ascontiguousarray(m.mat_rho, np.float64)]
         d = _abi.MaterialDesc(len(keep[0]), *[_ptr(a) for a in keep])
@@ -566,6 +570,8 @@ class MarkerInCell:
         if float(p.get("subgrid_diff_coef_stress", 1.0)) > 0:
             self.update_subgrid_stress()
         self.apply_marker_stress_correction()
+        if heat and getattr(self, "heat", None) is not None:
+            self.heat = dict(self.heat, timestep=float(p.get("timestep", self.heat["timestep"])))
         hrep = self.update_marker_temp_for_grid_and_subgrid_changes() if heat else None
         self.advect_markers_and_rotate_stress()
         self.update_marker_strain()

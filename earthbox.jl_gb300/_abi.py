@@ -112,7 +112,7 @@ class Params(C.Structure):
         ("subgrid_diff_coef_temp", C.c_double), ("iuse_melt_damage", C.c_int64),
         ("iuse_serpentinization", C.c_int64), ("iuse_topo", C.c_int64),
         ("matid_sticky_air_rho", C.c_int64), ("matid_sticky_water_rho", C.c_int64),
-        ("runge_kutta_order", C.c_int64),
+        ("runge_kutta_order", C.c_int64), ("temperature_bottom", C.c_double), ("temperature_left", C.c_double),
     ]
 
 

@@ -447,6 +447,10 @@ extern "C" int eb_set_materials(eb_ctx* c, const eb_material_desc* m) {
   if (m->nmat < 1 || m->nmat > 32767) return eb_fail(c, EB_BAD_INPUT, "nmat out of range");
   if (!m->mat_mu || !m->mat_hr || !m->mat_flow_type || !m->mat_flow || !m->mat_plastic)
     return eb_fail(c, EB_BAD_INPUT, "null material array");
+  int64_t option = m->mat_flow_type[0];
+  for (int64_t i = 1; i < m->nmat; ++i) option = std::max<int64_t>(option, m->mat_flow_type[i]);
+  if (!(option == -1 || option == 0 || option == 1 || option == 2 || option == 4 || option == 5))
+    return eb_fail(c, EB_BAD_INPUT, "flow law type (largest mat_flow_type) must be -1, 0, 1, 2, 4 or 5");
   cudaSetDevice(c->device);
   cudaStreamSynchronize(c->stream);
   for (void* p : c->mat_allocs) cudaFree(p);
@@ -458,12 +462,13 @@ extern "C" int eb_set_materials(eb_ctx* c, const eb_material_desc* m) {
   d.nmat = n;
   std::vector<int32_t> ft(n);
   for (int32_t i = 0; i < n; ++i) ft[i] = (int32_t)m->mat_flow_type[i];
+  d.option = (int32_t)option;
   std::vector<double> rho(n, -1.0);
   if (m->mat_rho) rho.assign(m->mat_rho, m->mat_rho + n);
   int rc;
   if ((rc = upload_vec(c, c->mat_allocs, std::vector<double>(m->mat_mu, m->mat_mu + n), &d.mu)) ||
       (rc = upload_vec(c, c->mat_allocs, std::vector<double>(m->mat_hr, m->mat_hr + n), &d.hr)) ||
-      (rc = upload_vec(c, c->mat_allocs, std::vector<double>(m->mat_flow, m->mat_flow + 12 * (size_t)n), &d.flow)) ||
+      (rc = upload_vec(c, c->mat_allocs, std::vector<double>(m->mat_flow, m->mat_flow + (size_t)kFlowCols * n), &d.flow)) ||
       (rc = upload_vec(c, c->mat_allocs, std::vector<double>(m->mat_plastic, m->mat_plastic + 6 * (size_t)n), &d.plastic)) ||
       (rc = upload_vec(c, c->mat_allocs, rho, &d.rho)) || (rc = upload_vec(c, c->mat_allocs, ft, &d.flow_type)))
     return rc;

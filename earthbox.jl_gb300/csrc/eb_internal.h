@@ -45,8 +45,10 @@ __device__ __forceinline__ float gather_p(const float* __restrict__ pg, const De
   return gather4f(pg, g.ynum - 1, yp, xp, (lx - ox) * (xl ? c1.x : c1.y), (ly - oy) * (yl ? r1.x : r1.y));
 }
 
+constexpr int kFlowCols = 17;  // columns of the reference's mat_flow table
 struct DevMats {
   int32_t nmat;
+  int32_t option;  // the model's flow law: the largest mat_flow_type (FlowViscosity.jl:21-44)
   const double *mu, *hr, *flow, *plastic, *rho;
   const int32_t* flow_type;
 };

@@ -117,6 +117,7 @@ __device__ __forceinline__ double forecast_ve(double dt, double mu, double srr, 
 struct RheoParams {
   double dt, T_top, eta_min, eta_max, s_min, R, vsoftfac;
   int soft;
+  double T_bottom, T_left, ysize;  // the Blankenbach and Couette flow laws
 };
 
 // ---- root-guided bisection --------------------------------------------------------------
@@ -274,7 +275,48 @@ __device__ __forceinline__ bool pos_normal(double x) {
   return b >= ((int64_t)1 << 52) && b < 0x7FF0000000000000LL;
 }
 
+// The flow laws other than composite creep; the model's law is its largest mat_flow_type
+// (FlowViscosity.jl:21-44, UpdateManager.jl).  Each sets eta_flow and preexp as the
+// reference's module does, with the same operations in the same order.
+__device__ __forceinline__ bool d_flow_viscosity_other(const DevMarkers& mk, const DevMats& mt, const RheoParams& P,
+                                                       int64_t m) {
+  const int32_t id = mk.matid[m];
+  double eta, pre;
+  switch (mt.option) {
+    case 0:  // Isoviscous.jl
+      eta = MATV(mt.flow, mt.nmat, id, 1);
+      pre = eta;
+      break;
+    case 4: {  // CouetteFlowBenchmark.jl: temperature limited below by the left wall's
+      const double T = fmax(mk.tk[m], P.T_left);
+      pre = MATV(mt.flow, mt.nmat, id, 13);
+      const double ea = MATV(mt.flow, mt.nmat, id, 14);
+      eta = pre * exp(ea * 1000.0 / P.R / P.T_left * (1.0 - (T - P.T_left) / P.T_left));
+      break;
+    }
+    case 5: {  // Blankenback89.jl: temperature limited below by the top's
+      const double T = fmax(mk.tk[m], P.T_top);
+      pre = MATV(mt.flow, mt.nmat, id, 15);
+      const double b = MATV(mt.flow, mt.nmat, id, 16), cy = MATV(mt.flow, mt.nmat, id, 17);
+      eta = pre * exp(-b * (T - P.T_top) / (P.T_bottom - P.T_top) + cy * mk.y[m] / P.ysize);
+      break;
+    }
+    case -1: {  // Xdependent.jl: the analytic viscosity of the non-Newtonian channel
+      const double pgrad = -1e9 / 9500.0, dx = mk.x[m] - 10000.0 / 2.0;
+      eta = fabs(dx) > 0.0 ? 1.0 / 1e-37 * pow(-pgrad, 1.0 - 3.0) * pow(dx, 1.0 - 3.0) : P.eta_max;
+      pre = MATV(mt.flow, mt.nmat, id, 1);
+      break;
+    }
+    default:
+      return false;
+  }
+  mk.eta_flow[m] = eta;
+  mk.preexp[m] = pre;
+  return true;
+}
+
 __device__ __forceinline__ void d_flow_viscosity(const DevMarkers& mk, const DevMats& mt, const RheoParams& P, int64_t m) {
+  if (d_flow_viscosity_other(mk, mt, P, m)) return;
   const int32_t id = mk.matid[m];
   const int32_t ft = __ldg(&mt.flow_type[id - 1]);
   double eta = 0.0;
@@ -485,9 +527,12 @@ YieldParams yield_params(const eb_params& p) {
                      (int)(p.no_yielding_in_mobile_wall != 0), (int32_t)p.matid_sticky_air,
                      (int32_t)p.matid_mobile_wall, (int32_t)p.matid_plate_extension};
 }
-RheoParams rheo_params(const eb_params& p) {
+RheoParams rheo_params(const eb_ctx* c) {
+  const eb_params& p = c->P;
+  const double ysize = c->h_gy.empty() ? 0.0 : c->h_gy.back() - c->h_gy.front();
   return RheoParams{p.timestep, p.temperature_top, p.viscosity_min, p.viscosity_max, p.powerlaw_stress_min,
-                    p.gas_constant, p.vsoftfac, (int)(p.iuse_viscous_strain_soft == 1)};
+                    p.gas_constant, p.vsoftfac, (int)(p.iuse_viscous_strain_soft == 1), p.temperature_bottom,
+                    p.temperature_left, ysize};
 }
 
 int yield_launch(eb_ctx* c) {
@@ -507,7 +552,7 @@ int yield_launch(eb_ctx* c) {
 int launch_rheology(eb_ctx* c) {
   int rc = ensure(c, {EB_M_INSIDE, EB_M_MATID, EB_M_STRAIN_PLASTIC, EB_M_FRIC_INI, EB_M_COHESION, EB_M_FRIC,
                       EB_M_SXX, EB_M_SXY, EB_M_EXX, EB_M_EXY, EB_M_TK, EB_M_PR, EB_M_GII, EB_M_SR_RATIO,
-                      EB_M_ETA_FLOW, EB_M_PREEXP});
+                      EB_M_ETA_FLOW, EB_M_PREEXP, EB_M_X, EB_M_Y});
   if (rc) return rc;
   const int melt = c->P.iuse_melt_damage == 1;
   if (melt && (rc = ensure_marker_field(c, EB_M_MELT_DAMAGE))) return rc;
@@ -515,7 +560,7 @@ int launch_rheology(eb_ctx* c) {
   EB_PROF(c, "k_failure");
   k_failure<<<mblocks(c), kBlock, 0, c->stream>>>(dev_markers(c), c->mats, melt);
   EB_LAUNCHED(c);
-  const RheoParams R = rheo_params(c->P);
+  const RheoParams R = rheo_params(c);
   EB_PROF(c, "k_flow_viscosity");
   k_flow_viscosity<<<mblocks(c), kBlock, 0, c->stream>>>(dev_markers(c), c->mats, R);
   EB_LAUNCHED(c);
@@ -538,13 +583,13 @@ int launch_plastic_yielding(eb_ctx* c) { return yield_launch(c); }
 int launch_rheology_fused(eb_ctx* c, int use_marker_plasticity) {
   int rc = ensure(c, {EB_M_INSIDE, EB_M_MATID, EB_M_STRAIN_PLASTIC, EB_M_FRIC_INI, EB_M_COHESION, EB_M_FRIC,
                       EB_M_SXX, EB_M_SXY, EB_M_EXX, EB_M_EXY, EB_M_TK, EB_M_PR, EB_M_GII, EB_M_SR_RATIO,
-                      EB_M_ETA_FLOW, EB_M_PREEXP, EB_M_ETA, EB_M_Y, EB_M_PFAILURE});
+                      EB_M_ETA_FLOW, EB_M_PREEXP, EB_M_ETA, EB_M_X, EB_M_Y, EB_M_PFAILURE});
   if (rc) return rc;
   const int melt = c->P.iuse_melt_damage == 1;
   if (melt && (rc = ensure_marker_field(c, EB_M_MELT_DAMAGE))) return rc;
   if (c->M == 0) return EB_OK;
   EB_PROF(c, "k_rheology");
-  k_rheology<<<mblocks(c), kBlock, 0, c->stream>>>(dev_markers(c), c->mats, melt, rheo_params(c->P), c->P.ntimestep,
+  k_rheology<<<mblocks(c), kBlock, 0, c->stream>>>(dev_markers(c), c->mats, melt, rheo_params(c), c->P.ntimestep,
                                                   c->P.itype_global, use_marker_plasticity ? 1 : 0, yield_params(c->P));
   EB_LAUNCHED(c);
   return EB_OK;

@@ -606,6 +606,104 @@ def solid_body_rotation_velocity(grid: Grid, vrotation: float) -> tuple:
     return np.asfortranarray(vx1), np.asfortranarray(vy1)
 
 
+def couette_flow_viscous_heating(xnum: int = 51, ynum: int = 11, mpc: int = 5) -> Model:
+    """The reference's Couette-flow viscous-heating benchmark, as configured in
+    src/benchmarks/models/couette_flow_viscous_heating/{model,materials}.yml and the benchmark
+    material library (TempDependentViscosityCouetteFlowBenchmark): a 30 x 12.5 km vertical shear
+    zone on 51 x 11 nodes with 5 x 5 markers per cell on a regular lattice, the
+    temperature-dependent Couette flow law (mat_flow_type 4: 1e15 Pa s, 150 kJ/mol about the left
+    wall's 727 C), 3000 kg/m^3, 1000 J/kg/K, conductivity 2 W/m/K, shear heating on,
+    VerticalCouetteFlowBC.jl: the open channel of VerticalChannelBC.jl with no pressure drop, no
+    slip on the left wall, vy ghost = 6.3072 cm/yr - vy interior on the right wall
+    (NoSlipBC.set_vy_for_no_slip_with_shear_at_right_boundary!), zero vertical temperature
+    gradient through the top and the bottom, 727 C on the left wall and no heat flux through the
+    right one; nodal plasticity loop with one Picard iteration, harmonic normal viscosity, and a
+    5 Myr time step limited to five cells of marker displacement."""
+    W, H = 30e3, 12.5e3
+    grid = staggered_grid(np.linspace(0.0, W, xnum), np.linspace(0.0, H, ynum))
+    mx, my = (xnum - 1) * mpc, (ynum - 1) * mpc
+    x = np.repeat((np.arange(mx) + 0.5) * (W / mx), my)
+    y = np.tile((np.arange(my) + 0.5) * (H / my), mx)
+    n = len(x)
+    T0 = 727.0 + 273.15
+    flow = np.zeros((1, 17))
+    flow[0, 12], flow[0, 13] = 1e15, 150.0
+    mats = Materials(
+        mat_mu=np.array([1e20]), mat_hr=np.zeros(1), mat_flow_type=np.array([4], np.int64),
+        mat_flow=np.asfortranarray(flow), mat_plastic=np.asfortranarray(np.zeros((1, 6))),
+        mat_rho=np.array([3000.0]))
+    m = {"x": x, "y": y, "matid": np.ones(n, np.int16), "rho": np.full(n, 3000.0), "eta": np.full(n, 1e21),
+         "eta_flow": np.full(n, 1e21), "sr_ratio": np.ones(n), "tk": np.full(n, T0), "kt": np.full(n, 2.0),
+         "rhocp": np.full(n, 3000.0 * 1000.0), "ha": np.zeros(n)}
+    for f in ("cohesion", "fric", "fric_ini", "preexp", "sxx", "sxy", "exx", "exy", "pr", "gii", "strain_plastic"):
+        m[f] = np.zeros(n)
+    _fields_common(np.random.Generator(np.random.Philox(0)), n, m)
+    m["pfailure"][:] = 0.0
+    grids = _analytic_grids(grid, v0=0.0, eta_ref=1e21, rho_ref=3000.0, T0=T0, T1=T0, depth_T1=H, y_surface=0.0)
+    grids.update(velocity_bcs(grid))
+    F = np.asfortranarray
+    X, Y = xnum, ynum
+    vshear = 6.3072e-2 / YEAR
+    grids["btopx"] = F(np.column_stack([np.zeros(X), np.ones(X)]))
+    grids["bbottomx"] = F(np.column_stack([np.zeros(X), np.ones(X)]))
+    grids["btopy"] = F(np.column_stack([np.zeros(X + 1), np.ones(X + 1)]))
+    grids["bbottomy"] = F(np.column_stack([np.zeros(X + 1), np.ones(X + 1)]))
+    grids["bleftx"] = F(np.zeros((Y + 1, 2)))
+    grids["brightx"] = F(np.zeros((Y + 1, 2)))
+    grids["blefty"] = F(np.column_stack([np.zeros(Y), -np.ones(Y)]))
+    grids["brighty"] = F(np.column_stack([np.full(Y, vshear), -np.ones(Y)]))
+    grids["btopt"] = F(np.column_stack([np.zeros(X), np.ones(X)]))
+    grids["bbottomt"] = F(np.column_stack([np.zeros(X), np.ones(X)]))
+    grids["bleftt"] = F(np.column_stack([np.full(Y, T0), np.zeros(Y)]))
+    grids["brightt"] = F(np.column_stack([np.zeros(Y), np.ones(Y)]))
+    params = default_params(timestep=5e6 * YEAR, viscosity_min=1e18, viscosity_max=1e25, temperature_top=T0,
+                            itype_global=1, ntimestep=1, temperature_bottom=T0, temperature_left=T0)
+    params.update(stokes_params(pressure_bc_mode=1, pressure_bc=0.0, gravity_y=0.0, iuse_interface_stabilization=0))
+    params.update(max_temp_change=10.0, iuse_adiabatic_heating=0, iuse_shear_heating=1, iuse_heat=1,
+                  marker_cell_displ_max=5.0)
+    return Model("couette_flow_viscous_heating", grid, mats, params, m, grids)
+
+
+def couette_temperature_profile(t_left: float, t_right: float, width: float, activation_energy: float,
+                                gas_constant: float = 8.314, npoints: int = 100) -> tuple:
+    """Steady temperature across a Couette shear zone with the temperature-dependent viscosity,
+    as the reference's benchmark evaluates it (post_processing/analytical/
+    CouetteFlowViscousHeatingManager.jl, after Gerya 2010): phi1 = exp(Ea (T_right - T_left) /
+    (R T_left^2)); the Brinkman number from the bisection on b in [1e-6, 10] with
+    Br = b^2/2 (1 - tanh(b/2)^2) and phi1 = b^2 / (2 Br); then for phi from 1 to phi1 the
+    position x(phi) and T = T_left + log(phi) R T_left^2 / Ea.  Returns (x m, T K)."""
+    def br_of(b):
+        return b ** 2.0 / 2.0 * (1.0 - ((math.exp(b) - 1.0) / (math.exp(b) + 1.0)) ** 2.0)
+
+    def phi_of(b, br):
+        return b ** 2.0 / 2.0 / br
+    phi1 = math.exp(activation_energy * (t_right - t_left) / gas_constant / t_left ** 2)
+    lo, hi = 1e-6, 10.0
+    br, ph = 0.0, 0.0
+    if phi_of(lo, br_of(lo)) - phi1 <= 0.0 <= phi_of(hi, br_of(hi)) - phi1:
+        d = 1e6
+        while abs(d) > 1e-6:
+            b = (lo + hi) / 2.0
+            br = br_of(b)
+            ph = phi_of(b, br)
+            d = ph - phi1
+            if d <= 0.0:
+                lo = b
+            else:
+                hi = b
+    phi1 = ph
+    xs, ts = np.zeros(npoints), np.zeros(npoints)
+    dphi = (phi1 - 1.0) / (npoints - 1)
+    for j in range(npoints):
+        phi = 1.0 + j * dphi
+        c = math.sqrt(2.0 * br * (phi1 - phi))
+        bb = math.sqrt(2.0 * br * phi1)
+        dd = math.sqrt(2.0 * br * (phi1 - 1.0))
+        xs[j] = width * (1.0 / math.sqrt(2.0 * br * phi1)) * math.log((dd + bb) / (dd - bb) * ((c - bb) / (c + bb)))
+        ts[j] = t_left + math.log(phi) * gas_constant * t_left ** 2.0 / activation_energy
+    return xs, ts
+
+
 def ramberg_wave_velocity(h1: float, h2: float, rho1: float, rho2: float, eta1: float, eta2: float, amp: float,
                           lam: float, g: float = 9.81) -> float:
     """Ramberg's (1968) analytical vertical velocity at the crest of a sinusoidal interface

@@ -14,7 +14,7 @@
  *   - marker cell indices (marker_xn/yn, marker_xn_vy/yn_vy) are 1-based Int32;
  *   - marker_matid is Int16 (the reference's storage type) on the host and on
  *     the device; its upload checks 1 <= matid (<= nmat once materials are set);
- *   - material tables mat_flow (nmat x 12) and mat_plastic (nmat x 6) are
+ *   - material tables mat_flow (nmat x 17) and mat_plastic (nmat x 6) are
  *     column-major, indexed by the 1-based material id.
  * All calls are synchronous with respect to the host on return, on the
  * context's own CUDA stream.
@@ -59,8 +59,15 @@ typedef struct eb_material_desc {
   int64_t nmat;
   const double*  mat_mu;        /* [nmat]      shear modulus (Pa)                     */
   const double*  mat_hr;        /* [nmat]      radiogenic heat production (W/m^3)     */
-  const int64_t* mat_flow_type; /* [nmat]      0 isoviscous, 1/2 composite creep     */
-  const double*  mat_flow;      /* [nmat x 12] column-major flow-law table            */
+  /* mat_flow_type: the flow law of each material.  As in FlowViscosity.jl:21-44, the
+   * largest value in the table selects the law of the whole model: -1 x-dependent
+   * (Xdependent.jl), 0 isoviscous (Isoviscous.jl), 1 or 2 composite creep with the
+   * materials of type 0 isoviscous (CompositeViscosity.jl), 4 the temperature-dependent
+   * Couette-flow law (CouetteFlowBenchmark.jl: mat_flow columns 13-14), 5 the
+   * Blankenbach (1989) convection law (Blankenback89.jl: columns 15-17).          */
+  const int64_t* mat_flow_type; /* [nmat]                                            */
+  const double*  mat_flow;      /* [nmat x 17] column-major flow-law table (the
+                                 * reference's model.materials.arrays.mat_flow)       */
   const double*  mat_plastic;   /* [nmat x 6]  column-major plasticity table          */
   const double*  mat_rho;       /* [nmat]      first column of mat_rho (sticky flatten)*/
 } eb_material_desc;
@@ -86,6 +93,8 @@ typedef struct eb_params {
   int64_t iuse_topo;                /* sticky-layer density flattening switch          */
   int64_t matid_sticky_air_rho, matid_sticky_water_rho; /* ids for flattening, -1 none */
   int64_t runge_kutta_order;        /* 1 or 4 (0 = markers do not move)                */
+  double  temperature_bottom;       /* K (Blankenbach flow law, mat_flow_type 5)        */
+  double  temperature_left;         /* K (Couette flow law, mat_flow_type 4)            */
 } eb_params;
 
 /* ---- marker fields ----------------------------------------------------------

@@ -854,6 +854,52 @@ static inline double forecast_ve(double dt, double mu, double srr, double sxx, d
   return (s > smin) ? s : smin;
 }
 
+/* The flow laws other than composite creep, selected as FlowViscosity.update_marker_flow_viscosity!
+ * selects them (FlowViscosity.jl:21-44): option = the largest mat_flow_type of the model.
+ *   0  Isoviscous.update_marker_flow_viscosity! (types/isoviscous/Isoviscous.jl):
+ *      eta_flow = preexp = mat_flow[mat, 1];
+ *   4  CouetteFlowBenchmark.update_marker_flow_viscosity! (types/couette_flow_benchmark/
+ *      CouetteFlowBenchmark.jl): T = max(TK, T_left), eta = A exp(Ea 1000 / R / T_left
+ *      (1 - (T - T_left) / T_left)) with A, Ea = mat_flow[mat, 13], [mat, 14]; preexp = A;
+ *   5  Blankenback89.update_marker_flow_viscosity! (types/blankenbach89/Blankenback89.jl):
+ *      T = max(TK, T_top), eta = eta0 exp(-b (T - T_top) / (T_bottom - T_top) + c y / ysize)
+ *      with eta0, b, c = mat_flow[mat, 15:17]; preexp = eta0;
+ *  -1  Xdependent.update_marker_flow_viscosity! (types/x_dependent/Xdependent.jl): the
+ *      analytic viscosity of the 10 x 9.5 km non-Newtonian channel (n = 3, C = 1e-37,
+ *      1e9 Pa), eta_max on the centre line; preexp = mat_flow[mat, 1].
+ * mat_flow is the reference's nmat x 17 table.  Markers outside the domain are skipped. */
+void o_flow_viscosity_other(int64_t M, const int8_t* flags, const int16_t* matid, int64_t nmat, int64_t option,
+                            const double* mat_flow, double T_top, double T_bottom, double T_left, double R,
+                            double ysize, double eta_max, const double* m_x, const double* m_y,
+                            const double* m_tk, double* m_eta_flow, double* m_preexp) {
+  OMP_FOR
+  for (int64_t m = 0; m < M; ++m) {
+    if (flags[m] != 1) continue;
+    int mt = matid[m];
+    double eta = 0.0, pre = 0.0;
+    if (option == 0) {
+      eta = MAT(mat_flow, nmat, mt, 1);
+      pre = eta;
+    } else if (option == 4) {
+      double T = m_tk[m] > T_left ? m_tk[m] : T_left;
+      pre = MAT(mat_flow, nmat, mt, 13);
+      double ea = MAT(mat_flow, nmat, mt, 14);
+      eta = pre * exp(ea * 1000.0 / R / T_left * (1.0 - (T - T_left) / T_left));
+    } else if (option == 5) {
+      double T = m_tk[m] > T_top ? m_tk[m] : T_top;
+      pre = MAT(mat_flow, nmat, mt, 15);
+      double b = MAT(mat_flow, nmat, mt, 16), cy = MAT(mat_flow, nmat, mt, 17);
+      eta = pre * exp(-b * (T - T_top) / (T_bottom - T_top) + cy * m_y[m] / ysize);
+    } else if (option == -1) {
+      double pg = -1e9 / 9500.0, dx = m_x[m] - 10000.0 / 2.0;
+      eta = fabs(dx) > 0.0 ? 1.0 / 1e-37 * pow(-pg, 1.0 - 3.0) * pow(dx, 1.0 - 3.0) : eta_max;
+      pre = MAT(mat_flow, nmat, mt, 1);
+    }
+    m_eta_flow[m] = eta;
+    m_preexp[m] = pre;
+  }
+}
+
 /* CompositeViscosity.update_marker_flow_viscosity! (flow_viscosity/update/types/composite_viscosity/
  * CompositeViscosity.jl:133-284) incl. apply_strain_softening (:286-297, ViscousStrainSoftening.jl:14-39),
  * calc_initial_stress_invariant (:299-306), update_bisection_limits (:403-418).

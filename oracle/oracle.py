@@ -83,7 +83,10 @@ class OracleMIC:
             self.mk[k] = np.zeros(self.M)
         self._gx = [np.ascontiguousarray(getattr(self.g, n), dtype=np.float64) for n in
                     ("gridx_b", "gridy_b", "xstp_b", "ystp_b", "gridx_vy", "xstp_vy", "gridy_vx", "ystp_vx")]
-        self.mat_flow = np.asfortranarray(self.mats.mat_flow).ravel(order="F").copy()
+        flow = np.zeros((self.mats.mat_flow.shape[0], 17))  # the reference's nmat x 17 table
+        flow[:, :self.mats.mat_flow.shape[1]] = self.mats.mat_flow
+        self.mat_flow = np.asfortranarray(flow).ravel(order="F").copy()
+        self.flow_option = int(np.max(self.mats.mat_flow_type))
         self.mat_plastic = np.asfortranarray(self.mats.mat_plastic).ravel(order="F").copy()
         self.mat_mu = np.ascontiguousarray(self.mats.mat_mu, np.float64)
         self.mat_hr = np.ascontiguousarray(self.mats.mat_hr, np.float64)
@@ -242,6 +245,14 @@ class OracleMIC:
         lib().o_failure_properties(I(self.M), P(k["inside"]), P(k["matid"]), I(self.mats.nmat), P(self.mat_plastic),
                                    P(k["strain_plastic"]), P(k["fric_ini"]), I(p["iuse_melt_damage"]),
                                    P(k["melt_damage"]), P(k["cohesion"]), P(k["fric"]))
+        if self.flow_option in (-1, 0, 4, 5):
+            g = self.g
+            lib().o_flow_viscosity_other(
+                I(self.M), P(k["inside"]), P(k["matid"]), I(self.mats.nmat), I(self.flow_option), P(self.mat_flow),
+                D(p["temperature_top"]), D(p.get("temperature_bottom", 0.0)), D(p.get("temperature_left", 0.0)),
+                D(p["gas_constant"]), D(g.ymax - g.ymin), D(p["viscosity_max"]), P(k["x"]), P(k["y"]), P(k["tk"]),
+                P(k["eta_flow"]), P(k["preexp"]))
+            return
         lib().o_composite_viscosity(
             I(self.M), P(k["inside"]), P(k["matid"]), I(self.mats.nmat), P(self.mat_ft), P(self.mat_flow),
             P(self.mat_plastic), P(self.mat_mu), D(p["timestep"]), D(p["temperature_top"]), D(p["viscosity_min"]),

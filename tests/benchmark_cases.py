@@ -46,3 +46,66 @@ def solid_body_rotation_oracle(eb, nsteps: int = ROTATION_STEPS):
         mic.add_remaining_grid_change_to_marker_temperature()
         mic.advect_markers_and_rotate_stress()
     return model, rows[0], rows[1]
+
+
+COUETTE_STEPS = 99   # Options.jl: output 100 (its grid temperature is the one after 99 steps)
+COUETTE_ROW = 11     # Options.jl: y_index
+
+
+def couette_error(eb, model, row) -> float:
+    """CouetteFlowViscousHeatingManager.get_test_results: the numerical profile (row 11 of the grid
+    temperature) interpolated linearly at the analytic profile's positions, against the steady
+    analytic temperature built from its own wall temperatures; largest relative error in K."""
+    g = model.grid
+    xs, ts = eb.synthetic.couette_temperature_profile(row[0], row[-1], g.xmax - g.xmin, 150e3)
+    num = np.interp(xs, g.gridx_b, row)
+    return float(np.max(np.abs(num - ts) / ts))
+
+
+def couette_oracle(eb, nsteps: int = COUETTE_STEPS):
+    """The Couette viscous-heating benchmark through the oracle, step by step as
+    TimeLoop.run_loop! runs it (src/time_loop/TimeLoop.jl:181-194): pre-solver averages and the
+    temperature-dependent flow law, one nodal Picard iteration with harmonic normal viscosity,
+    the displacement-limited time step, post-Stokes steps, the heat step with shear heating and
+    subgrid diffusion, RK4 advection and the channel recycling.  Returns (model, row-11 grid
+    temperature after nsteps)."""
+    from oracle import boundary as B
+    from oracle.heat import HeatOracle
+    from oracle.picard import OraclePicard
+    model = eb.synthetic.couette_flow_viscous_heating()
+    op = OraclePicard(model)
+    p, g, m = op.model.params, model.grid, op.mic
+    dt_ve = p["timestep"]
+    for _ in range(nsteps):
+        p["timestep"] = dt_ve
+        m.get_marker_inside_flags()
+        m.initialize_bilinear_interpolation()
+        m.interpolate_marker_heat_parameters_to_grid()
+        m.update_marker_rheology()
+        m.update_marker_viscoplastic_viscosity(use_marker_plasticity=False)
+        m.interpolate_marker_stokes_parameters_to_grid()
+        op.so.interpolate_basic_viscoplastic_viscosity_to_pressure_grid(1)
+        op.picard_loop_nodes(1, 1e-3, 1)
+        op.so.interpolate_stag_velocity_to_basic_grid()
+        m.calc_marker_viscoplastic_viscosity()
+        p["timestep"] = B.timestep_displacement_limit(g, op.gr["vx1"], op.gr["vy1"], p["marker_cell_displ_max"], 0,
+                                                      dt_ve)
+        op.so.forecast_viscoelastic_grid_stress()
+        m.post_stokes_marker_gathers()
+        m.update_subgrid_stress()
+        m.apply_marker_stress_correction()
+        ho = HeatOracle(op.model, grids=op.gr)
+        ho.heat_step()
+        for k in ("dtk1", "tk2"):
+            op.gr[k] = np.asfortranarray(ho.gr[k])
+        m.subgrid_heat_diffusion_update()
+        m.add_remaining_grid_change_to_marker_temperature()
+        m.advect_markers_and_rotate_stress()
+        m.update_marker_strain()
+        y, tk, _ = B.recycle_channel(m.mk["y"], m.mk["tk"], g.ymin, g.ymax, p["temperature_top"], p["temperature_top"])
+        m.mk["y"][:] = y
+        m.mk["tk"][:] = tk
+    m.get_marker_inside_flags()
+    m.initialize_bilinear_interpolation()
+    m.interpolate_marker_heat_parameters_to_grid()
+    return model, op.gr["tk1"][COUETTE_ROW - 1, :].copy()

@@ -158,3 +158,39 @@ def test_solid_body_rotation_returns_the_temperature_wave(eb):
     assert err < 0.02, err
     assert dev < 0.05, dev
     mic.close()
+
+
+def test_couette_flow_matches_the_steady_viscous_heating_profile(eb):
+    """The reference's Couette viscous-heating benchmark (models/couette_flow_viscous_heating,
+    post_processing/analytical/CouetteFlowViscousHeatingManager.jl) through 99 GPU time steps:
+    the temperature-dependent Couette flow law, one nodal Picard iteration with harmonic normal
+    viscosity, the displacement-limited step, the heat step with shear heating and subgrid
+    diffusion, RK4 advection and the channel recycling.  The row-11 grid temperature of output
+    100 must lie within the reference's 0.3 % of the steady analytic profile, and within 0.1 K of
+    the oracle's after the same steps.  The Stokes solves run to 1e-12 (the reference solves
+    directly): the flow is driven by the wall alone and its lateral velocity is pure solver
+    error, which at 1e-10 moves the markers sideways enough to shift the wall temperature by
+    about 0.5 K over the 99 steps."""
+    from benchmark_cases import COUETTE_ROW, COUETTE_STEPS, couette_error, couette_oracle
+    syn = eb.synthetic
+    model = syn.couette_flow_viscous_heating()
+    g = model.grid
+    mic = eb.MarkerInCell(0)
+    mic.load_model(model)
+    displ = model.params["marker_cell_displ_max"]
+    for _ in range(COUETTE_STEPS):
+        rep = mic.time_step(1, 1e-3, iuse_harmonic=1, heat=True, marker_cell_displ_max=displ, rtol=1e-12)
+        assert rep["picard"][-1]["status"] == 0, rep["picard"]
+        mic.recycle_markers(1, 1, 1, g.xmax, g.ymax, 0.0, 0.0, model.params["temperature_top"], 0, 0, recycle_type=3)
+    mic.get_marker_inside_flags()
+    mic.initialize_bilinear_interpolation_and_heat_scatter()
+    row = mic.download_grid("tk1")[COUETTE_ROW - 1, :].copy()
+    err = couette_error(eb, model, row)
+    _, orow = couette_oracle(eb)
+    dev = float(np.max(np.abs(row - orow)))
+    print(f"\nCouette viscous heating: right wall {row[-1]:.2f} K (left {row[0]:.2f} K), largest relative error "
+          f"against the steady analytic profile {100 * err:.4f} % (limit 0.3 %); against the oracle {dev:.3f} K")
+    assert row[-1] > row[0] + 100.0
+    assert err < 0.003, err
+    assert dev < 0.1, dev
+    mic.close()

@@ -513,3 +513,40 @@ def test_sticky_layer_density_flattening(eb, oracle):
         assert np.sum(ref.gr[f] == 1.2) >= 50 and np.sum(ref.gr[f] == 1025.0) >= 50, f
         assert np.array_equal(got == 1.2, ref.gr[f] == 1.2) and np.array_equal(got == 1025.0, ref.gr[f] == 1025.0), f
     mic.close()
+
+
+@pytest.mark.parametrize("option", [0, 4, 5, -1])
+def test_other_flow_laws_match_oracle(eb, oracle, option):
+    """The flow laws the model's largest mat_flow_type selects besides composite creep
+    (FlowViscosity.jl:21-44): isoviscous (preexp = viscosity), the temperature-dependent Couette
+    law (mat_flow columns 13-14), the Blankenbach law (columns 15-17) and the x-dependent channel
+    law, through the rheology entry point and the fused pass, against the oracle."""
+    import copy
+    model = eb.synthetic.config("rift_small")
+    mats = copy.deepcopy(model.mats)
+    n = len(mats.mat_mu)
+    flow = np.zeros((n, 17))
+    flow[:, :12] = mats.mat_flow
+    flow[:, 0] = 1e21 * (1.0 + np.arange(n))
+    flow[:, 12] = 1e15 * (1.0 + np.arange(n))
+    flow[:, 13] = 150.0
+    flow[:, 14] = 1e23
+    flow[:, 15] = np.log(1000.0)
+    flow[:, 16] = 0.5
+    mats.mat_flow = np.asfortranarray(flow)
+    mats.mat_flow_type = np.full(n, option, np.int64)
+    model.mats = mats
+    model.params = dict(model.params, temperature_bottom=1603.15, temperature_left=1000.15)
+    mic, ref = fresh(eb, oracle, model)
+    for o in (mic, ref):
+        o.get_marker_inside_flags()
+        o.update_marker_rheology()
+    close(mic.download_marker("preexp"), ref.mk["preexp"], "preexp", rtol=0.0)
+    close(mic.download_marker("eta_flow"), ref.mk["eta_flow"], "eta_flow", rtol=1e-12)
+    fused = eb.MarkerInCell(0)
+    fused.load_model(model)
+    fused.get_marker_inside_flags()
+    fused.update_marker_rheology_and_viscoplastic_viscosity(True)
+    close(fused.download_marker("eta_flow"), mic.download_marker("eta_flow"), "fused eta_flow", rtol=0.0)
+    for m in (mic, fused):
+        m.close()
