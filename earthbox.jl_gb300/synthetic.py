@@ -704,6 +704,74 @@ def couette_temperature_profile(t_left: float, t_right: float, width: float, act
     return xs, ts
 
 
+def channel_flow_variable_conductivity(xnum: int = 51, ynum: int = 11, mpc: int = 5) -> Model:
+    """The reference's variable-conductivity channel-flow benchmark, as configured in
+    src/benchmarks/models/channel_flow_variable_conductivity/{model,materials}.yml and the
+    benchmark material library (ConstantViscosityChannelVariableThermalConductivity): a 30 x 12.5 km
+    vertical channel on 51 x 11 nodes with 5 x 5 markers per cell on a regular lattice that do not
+    move (NoMotion), an isoviscous material (1e19 Pa s, 3000 kg/m^3, 1000 J/kg/K) with the
+    temperature-dependent conductivity k = k0 / (1 + a (T - T_top) / T_top), k0 = 8 W/m/K, a = 1
+    (rock-property conductivity model 2; params["rock_tables"] holds the tables), shear heating on,
+    VerticalChannelFlowShearHeatingBC.jl: the open channel with 3e7 Pa on the top row of pressure
+    cells, no slip on both walls, 25 C on both walls and zero vertical temperature gradient through
+    the top and the bottom; nodal plasticity loop with one Picard iteration, 100 kyr steps."""
+    W, H = 30e3, 12.5e3
+    grid = staggered_grid(np.linspace(0.0, W, xnum), np.linspace(0.0, H, ynum))
+    mx, my = (xnum - 1) * mpc, (ynum - 1) * mpc
+    x = np.repeat((np.arange(mx) + 0.5) * (W / mx), my)
+    y = np.tile((np.arange(my) + 0.5) * (H / my), mx)
+    n = len(x)
+    T0 = 25.0 + 273.15
+    mats = Materials(
+        mat_mu=np.array([1e20]), mat_hr=np.zeros(1), mat_flow_type=np.array([0], np.int64),
+        mat_flow=np.asfortranarray(np.zeros((1, 12))), mat_plastic=np.asfortranarray(np.zeros((1, 6))),
+        mat_rho=np.array([3000.0]))
+    mats.mat_flow[0, 0] = 1e19
+    m = {"x": x, "y": y, "matid": np.ones(n, np.int16), "rho": np.full(n, 3000.0), "eta": np.full(n, 1e19),
+         "eta_flow": np.full(n, 1e19), "sr_ratio": np.ones(n), "tk": np.full(n, T0), "kt": np.full(n, 8.0),
+         "rhocp": np.full(n, 3000.0 * 1000.0), "ha": np.zeros(n)}
+    for f in ("cohesion", "fric", "fric_ini", "preexp", "sxx", "sxy", "exx", "exy", "pr", "gii", "strain_plastic"):
+        m[f] = np.zeros(n)
+    _fields_common(np.random.Generator(np.random.Philox(0)), n, m)
+    m["pfailure"][:] = 0.0
+    grids = _analytic_grids(grid, v0=0.0, eta_ref=1e19, rho_ref=3000.0, T0=T0, T1=T0, depth_T1=H, y_surface=0.0)
+    grids.update(velocity_bcs(grid))
+    F = np.asfortranarray
+    X, Y = xnum, ynum
+    grids["btopx"] = F(np.column_stack([np.zeros(X), np.ones(X)]))
+    grids["bbottomx"] = F(np.column_stack([np.zeros(X), np.ones(X)]))
+    grids["btopy"] = F(np.column_stack([np.zeros(X + 1), np.ones(X + 1)]))
+    grids["bbottomy"] = F(np.column_stack([np.zeros(X + 1), np.ones(X + 1)]))
+    grids["bleftx"] = F(np.zeros((Y + 1, 2)))
+    grids["brightx"] = F(np.zeros((Y + 1, 2)))
+    grids["blefty"] = F(np.column_stack([np.zeros(Y), -np.ones(Y)]))
+    grids["brighty"] = F(np.column_stack([np.zeros(Y), -np.ones(Y)]))
+    grids["btopt"] = F(np.column_stack([np.zeros(X), np.ones(X)]))
+    grids["bbottomt"] = F(np.column_stack([np.zeros(X), np.ones(X)]))
+    grids["bleftt"] = F(np.column_stack([np.full(Y, T0), np.zeros(Y)]))
+    grids["brightt"] = F(np.column_stack([np.full(Y, T0), np.zeros(Y)]))
+    params = default_params(timestep=1e5 * YEAR, viscosity_min=1e18, viscosity_max=1e25, temperature_top=T0,
+                            itype_global=1, ntimestep=1, runge_kutta_order=0, temperature_bottom=T0)
+    params.update(stokes_params(pressure_bc_mode=1, pressure_bc=3e7, gravity_y=0.0, iuse_interface_stabilization=0))
+    params.update(max_temp_change=10.0, iuse_adiabatic_heating=0, iuse_shear_heating=1, iuse_heat=1)
+    params["rock_tables"] = {"mat_rho": np.array([[3000.0, 0.0, 0.0]]), "mat_cp": np.array([1000.0]),
+                             "mat_kt": np.array([[8.0, 1.0]]), "density_model": 0, "rhocp_model": 0,
+                             "conductivity_model": 2}
+    return Model("channel_flow_variable_conductivity", grid, mats, params, m, grids)
+
+
+def channel_flow_variable_conductivity_temperature(x: np.ndarray, width: float, height: float, t_wall: float,
+                                                   top_pressure: float, viscosity: float, k0: float,
+                                                   b: float) -> np.ndarray:
+    """Steady temperature of shear-heated Poiseuille flow with k = k0 / (1 + b (T - T_wall) / T_wall),
+    as the reference's benchmark evaluates it (post_processing/analytical/
+    ChannelFlowVariableConductivityManager.jl, after Gerya 2010): dp/dy = -top_pressure / height,
+    t1 = W^4 b / 192 / k0 / T_wall / eta (dp/dy)^2, T = T_wall / b (exp(t1 (1 - (2x/W - 1)^4)) + b - 1)."""
+    grad = -top_pressure / height
+    t1 = width ** 4.0 * b / 192.0 / k0 / t_wall / viscosity * grad ** 2.0
+    return t_wall / b * (np.exp(t1 * (1.0 - (2.0 * x / width - 1.0) ** 4.0)) + b - 1.0)
+
+
 def ramberg_wave_velocity(h1: float, h2: float, rho1: float, rho2: float, eta1: float, eta2: float, amp: float,
                           lam: float, g: float = 9.81) -> float:
     """Ramberg's (1968) analytical vertical velocity at the crest of a sinusoidal interface

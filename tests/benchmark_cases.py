@@ -15,12 +15,13 @@ def rotation_check(model, t_initial, t_final) -> float:
     return float(np.max(np.abs(b[nz] - a[nz]) / np.abs(a[nz])))
 
 
-def solid_body_rotation_oracle(eb, nsteps: int = ROTATION_STEPS):
+def solid_body_rotation_oracle(eb, rotations: int = 3):
     """TimeLoop.run_loop!'s body for the benchmark (src/time_loop/TimeLoop.jl:181-194) through the
     oracle: inside flags, bilinear set-up and heat averages (the output's TempC is this grid
     temperature), the kinematic velocity (Kinematics.solid_body_rotation!) with its spin, the heat
     step (RHS, heat loop, grid change, subgrid diffusion, remaining change to the markers) and RK4
-    advection.  Returns (model, row-11 grid temperature at step 1, at step nsteps + 1)."""
+    advection.  Returns (model, {step: row-11 grid temperature}) for step 1 and the steps that
+    follow each full rotation (the reference's outputs 1, 91, 181, 271)."""
     from oracle.heat import HeatOracle
     from oracle.oracle import OracleMIC
     model = eb.synthetic.solid_body_rotation()
@@ -29,14 +30,16 @@ def solid_body_rotation_oracle(eb, nsteps: int = ROTATION_STEPS):
     # spin of the rigid rotation: 0.5 (dvy/dx - dvx/dy) = vrotation / (xsize / 2) everywhere
     omega = model.params["velocity_rotation"] / (0.5 * (g.xmax - g.xmin))
     mic.gr["esp"] = np.asfortranarray(np.full((g.ynum, g.xnum), omega))
-    rows = []
-    for step in range(1, nsteps + 2):
+    marks = {1 + k * ROTATION_STEPS for k in range(rotations + 1)}
+    last = max(marks)
+    rows = {}
+    for step in range(1, last + 1):
         mic.get_marker_inside_flags()
         mic.initialize_bilinear_interpolation()
         mic.interpolate_marker_heat_parameters_to_grid()
-        if step in (1, nsteps + 1):
-            rows.append(mic.gr["tk1"][Y_INDEX - 1, :].copy())
-        if step == nsteps + 1:
+        if step in marks:
+            rows[step] = mic.gr["tk1"][Y_INDEX - 1, :].copy()
+        if step == last:
             break
         ho = HeatOracle(model, grids=mic.gr)
         ho.heat_step()
@@ -45,7 +48,7 @@ def solid_body_rotation_oracle(eb, nsteps: int = ROTATION_STEPS):
         mic.subgrid_heat_diffusion_update()
         mic.add_remaining_grid_change_to_marker_temperature()
         mic.advect_markers_and_rotate_stress()
-    return model, rows[0], rows[1]
+    return model, rows
 
 
 COUETTE_STEPS = 99   # Options.jl: output 100 (its grid temperature is the one after 99 steps)
@@ -109,3 +112,64 @@ def couette_oracle(eb, nsteps: int = COUETTE_STEPS):
     m.initialize_bilinear_interpolation()
     m.interpolate_marker_heat_parameters_to_grid()
     return model, op.gr["tk1"][COUETTE_ROW - 1, :].copy()
+
+
+VCOND_STEPS = 495    # output 100 at 0.5 Myr per output with 100 kyr steps: 49.5 Myr
+VCOND_ROW = 11
+
+
+def vcond_error(eb, model, row) -> float:
+    """ChannelFlowVariableConductivityManager.get_test_results: row 11 of the grid temperature
+    against the steady analytic profile built from its wall temperature, relative error in
+    Celsius (largest over the nodes)."""
+    g = model.grid
+    ana = eb.synthetic.channel_flow_variable_conductivity_temperature(
+        g.gridx_b, g.xmax - g.xmin, (g.ymax - g.ymin) - g.ystp_b[0], row[0], 3e7, 1e19, 8.0, 1.0)
+    a, n = ana - 273.15, row - 273.15
+    return float(np.max(np.abs(n - a) / np.abs(a)))
+
+
+def vcond_oracle(eb, nsteps: int = VCOND_STEPS):
+    """The variable-conductivity channel benchmark through the oracle: per step the rock
+    properties (temperature-dependent conductivity), the pre-solver averages, one nodal Picard
+    iteration, the post-Stokes steps and the heat step with shear heating (markers do not
+    move).  Returns (model, row-11 grid temperature after nsteps)."""
+    from oracle import boundary as B
+    from oracle.heat import HeatOracle
+    from oracle.picard import OraclePicard
+    model = eb.synthetic.channel_flow_variable_conductivity()
+    op = OraclePicard(model)
+    p, m = op.model.params, op.mic
+    rt = p["rock_tables"]
+
+    def pre():
+        m.get_marker_inside_flags()
+        upd = B.rock_properties(m.mk, rt["mat_rho"], rt["mat_cp"], rt["mat_kt"], rt["density_model"],
+                                rt["rhocp_model"], rt["conductivity_model"], p["temperature_top"], 1200.0)
+        for k, v in upd.items():
+            m.mk[k][:] = v
+        m.initialize_bilinear_interpolation()
+        m.interpolate_marker_heat_parameters_to_grid()
+    for _ in range(nsteps):
+        pre()
+        m.update_marker_rheology()
+        m.update_marker_viscoplastic_viscosity(use_marker_plasticity=False)
+        m.interpolate_marker_stokes_parameters_to_grid()
+        op.so.interpolate_basic_viscoplastic_viscosity_to_pressure_grid(0)
+        op.picard_loop_nodes(1, 1e-3, 0)
+        op.so.interpolate_stag_velocity_to_basic_grid()
+        m.calc_marker_viscoplastic_viscosity()
+        op.so.forecast_viscoelastic_grid_stress()
+        m.post_stokes_marker_gathers()
+        m.update_subgrid_stress()
+        m.apply_marker_stress_correction()
+        ho = HeatOracle(op.model, grids=op.gr)
+        ho.heat_step()
+        for k in ("dtk1", "tk2"):
+            op.gr[k] = np.asfortranarray(ho.gr[k])
+        m.subgrid_heat_diffusion_update()
+        m.add_remaining_grid_change_to_marker_temperature()
+        m.advect_markers_and_rotate_stress()
+        m.update_marker_strain()
+    pre()
+    return model, op.gr["tk1"][VCOND_ROW - 1, :].copy()

@@ -1,19 +1,26 @@
 """The reference's heat-path benchmarks through the oracle.
 
 Solid-body rotation (src/benchmarks/models/solid_body_rotation, post_processing/analytical/
-SolidBodyRotationManager.jl): one rotation of a hot square in a kinematic velocity field, the
-grid temperature profile of row 11 back on its initial profile within the reference's 2 % limit.
+SolidBodyRotationManager.jl): three rotations of a hot square in a kinematic velocity field, the
+grid temperature profile of row 11 back on its initial profile after each within the reference's
+2 % limit.
 
 Couette viscous heating (src/benchmarks/models/couette_flow_viscous_heating): a shear zone with a
-temperature-dependent viscosity heating itself, against the steady analytic profile."""
+temperature-dependent viscosity heating itself, against the steady analytic profile.
+
+Variable-conductivity channel (src/benchmarks/models/channel_flow_variable_conductivity):
+shear-heated Poiseuille flow with a temperature-dependent conductivity, against the steady
+analytic profile."""
 from benchmark_cases import rotation_check, solid_body_rotation_oracle
 
 
 def test_oracle_solid_body_rotation_returns_the_temperature_wave(eb):
-    model, t0, t1 = solid_body_rotation_oracle(eb)
-    assert t0.max() > 1400.0  # the profile crosses the hot square
-    err = rotation_check(model, t0, t1)
-    assert err < 0.02, err
+    """Outputs 91, 181 and 271 (one, two and three rotations) against output 1."""
+    model, rows = solid_body_rotation_oracle(eb)
+    assert rows[1].max() > 1400.0  # the profile crosses the hot square
+    for step in (91, 181, 271):
+        err = rotation_check(model, rows[1], rows[step])
+        assert err < 0.02, (step, err)
 
 
 def test_oracle_couette_flow_matches_the_steady_viscous_heating_profile(eb):
@@ -25,3 +32,15 @@ def test_oracle_couette_flow_matches_the_steady_viscous_heating_profile(eb):
     assert row[-1] > row[0] + 100.0  # the shear zone heated up
     err = couette_error(eb, model, row)
     assert err < 0.003, err
+
+
+def test_oracle_variable_conductivity_channel_matches_the_steady_profile(eb):
+    """The reference's variable-conductivity channel benchmark
+    (models/channel_flow_variable_conductivity, ChannelFlowVariableConductivityManager.jl):
+    after 495 steps (output 100) the shear-heated temperature across the channel within the
+    reference's 2.2 % (Celsius) of the steady analytic profile."""
+    from benchmark_cases import vcond_error, vcond_oracle
+    model, row = vcond_oracle(eb)
+    assert row.max() > 1000.0  # the channel centre heated from 298 K
+    err = vcond_error(eb, model, row)
+    assert err < 0.022, err

@@ -15,8 +15,11 @@ continuous Maxwell curve.
 Non-Newtonian channel flow (src/benchmarks/models/channel_flow_non_newtonian): sixty time steps
 of pressure-driven power-law flow against the analytic profile and the oracle.
 
-Solid-body rotation (src/benchmarks/models/solid_body_rotation): one rotation of a hot square in
-a kinematic velocity field (advection and the heat step), back on its initial profile."""
+Solid-body rotation (src/benchmarks/models/solid_body_rotation): three rotations of a hot square
+in a kinematic velocity field (advection and the heat step), back on its initial profile.
+
+Couette viscous heating and the variable-conductivity channel: shear heating against steady
+analytic profiles."""
 import numpy as np
 import pytest
 
@@ -126,37 +129,39 @@ def test_non_newtonian_channel_flow_matches_the_power_law_profile(eb):
 
 def test_solid_body_rotation_returns_the_temperature_wave(eb):
     """The reference's solid-body-rotation benchmark (models/solid_body_rotation,
-    post_processing/analytical/SolidBodyRotationManager.jl) through ninety GPU steps (one
-    rotation): inside flags, bilinear set-up with the heat averages, the kinematic velocity's
+    post_processing/analytical/SolidBodyRotationManager.jl) through 270 GPU steps (three
+    rotations): inside flags, bilinear set-up with the heat averages, the kinematic velocity's
     strain rate and spin, the heat step with subgrid diffusion, and RK4 advection.  The row-11
-    grid temperature must come back to its step-1 profile within the reference's 2 % (Celsius),
-    and agree with the oracle's after the same steps within 0.05 K."""
+    grid temperature of outputs 91, 181 and 271 must come back to output 1's profile within the
+    reference's 2 % (Celsius), and agree with the oracle's within 0.05 K."""
     from benchmark_cases import ROTATION_STEPS, Y_INDEX, rotation_check, solid_body_rotation_oracle
     syn = eb.synthetic
     model = syn.solid_body_rotation()
     mic = eb.MarkerInCell(0)
     mic.load_model(model)
-    rows = []
-    for step in range(1, ROTATION_STEPS + 2):
+    marks = {1 + k * ROTATION_STEPS for k in range(4)}
+    rows = {}
+    for step in range(1, max(marks) + 1):
         mic.get_marker_inside_flags()
         mic.initialize_bilinear_interpolation_and_heat_scatter()
-        if step in (1, ROTATION_STEPS + 1):
-            rows.append(mic.download_grid("tk1")[Y_INDEX - 1, :].copy())
-        if step == ROTATION_STEPS + 1:
+        if step in marks:
+            rows[step] = mic.download_grid("tk1")[Y_INDEX - 1, :].copy()
+        if step == max(marks):
             break
         mic.update_grid_strain_rate_and_spin()
         rep = mic.update_marker_temp_for_grid_and_subgrid_changes(model.params)
         assert rep is not None
         mic.advect_markers_and_rotate_stress()
-    err = rotation_check(model, rows[0], rows[1])
-    _, o0, o1 = solid_body_rotation_oracle(eb)
-    dev = float(np.max(np.abs(rows[1] - o1)))
-    print(f"\nsolid body rotation: one rotation in {ROTATION_STEPS} steps, largest relative change of the "
-          f"row-{Y_INDEX} profile {100 * err:.4f} % (limit 2 %); against the oracle {dev:.2e} K")
-    assert rows[0].max() > 1400.0
-    assert float(np.max(np.abs(rows[0] - o0) / o0)) < 1e-6  # step 1: FP32 weight sums, 3e-8 measured
-    assert err < 0.02, err
-    assert dev < 0.05, dev
+    _, orows = solid_body_rotation_oracle(eb)
+    assert rows[1].max() > 1400.0
+    assert float(np.max(np.abs(rows[1] - orows[1]) / orows[1])) < 1e-6  # FP32 weight sums, 3e-8 measured
+    for step in sorted(marks - {1}):
+        err = rotation_check(model, rows[1], rows[step])
+        dev = float(np.max(np.abs(rows[step] - orows[step])))
+        print(f"\nsolid body rotation, output {step} ({(step - 1) // ROTATION_STEPS} rotations): largest relative "
+              f"change of the row-{Y_INDEX} profile {100 * err:.4f} % (limit 2 %); against the oracle {dev:.2e} K")
+        assert err < 0.02, (step, err)
+        assert dev < 0.05, (step, dev)
     mic.close()
 
 
@@ -193,4 +198,40 @@ def test_couette_flow_matches_the_steady_viscous_heating_profile(eb):
     assert row[-1] > row[0] + 100.0
     assert err < 0.003, err
     assert dev < 0.1, dev
+    mic.close()
+
+
+def test_variable_conductivity_channel_matches_the_steady_profile(eb):
+    """The reference's variable-conductivity channel benchmark
+    (models/channel_flow_variable_conductivity, ChannelFlowVariableConductivityManager.jl)
+    through 495 GPU time steps: the rock-property update with the temperature-dependent
+    conductivity, one nodal Picard iteration, and the heat step with shear heating (markers do
+    not move).  Output 100's row-11 temperature must lie within the reference's 2.2 % (Celsius)
+    of the steady analytic profile, and within 0.05 K of the oracle's."""
+    from benchmark_cases import VCOND_ROW, VCOND_STEPS, vcond_error, vcond_oracle
+    syn = eb.synthetic
+    model = syn.channel_flow_variable_conductivity()
+    rt = model.params["rock_tables"]
+    mic = eb.MarkerInCell(0)
+    mic.load_model(model)
+    mic.set_rock_tables(rt["mat_rho"], rt["mat_cp"], rt["mat_kt"])
+
+    def rock():
+        mic.get_marker_inside_flags()
+        mic.update_marker_rock_properties(rt["density_model"], rt["rhocp_model"], rt["conductivity_model"])
+    for _ in range(VCOND_STEPS):
+        rock()
+        rep = mic.time_step(1, 1e-3, iuse_harmonic=0, heat=True, rtol=1e-12)
+        assert rep["picard"][-1]["status"] == 0, rep["picard"]
+    rock()
+    mic.initialize_bilinear_interpolation_and_heat_scatter()
+    row = mic.download_grid("tk1")[VCOND_ROW - 1, :].copy()
+    err = vcond_error(eb, model, row)
+    _, orow = vcond_oracle(eb)
+    dev = float(np.max(np.abs(row - orow)))
+    print(f"\nvariable-conductivity channel: centre {row.max():.2f} K, largest relative error against the "
+          f"steady analytic profile {100 * err:.4f} % (limit 2.2 %); against the oracle {dev:.3f} K")
+    assert row.max() > 1000.0
+    assert err < 0.022, err
+    assert dev < 0.05, dev
     mic.close()
