@@ -772,6 +772,65 @@ def channel_flow_variable_conductivity_temperature(x: np.ndarray, width: float, 
     return t_wall / b * (np.exp(t1 * (1.0 - (2.0 * x / width - 1.0) ** 4.0)) + b - 1.0)
 
 
+def elastic_slab(xnum: int = 51, ynum: int = 51, mpc: int = 5) -> Model:
+    """The reference's elastic-slab benchmark, as configured in
+    src/benchmarks/models/elastic_slab/{model,materials}.yml and the benchmark material library:
+    a 1000 x 1000 km box on 51 x 51 nodes with 5 x 5 markers per cell on a regular lattice; the
+    slab 0.2 < y/ysize < 0.8, x/xsize < 0.8 (ElasticSlab.in_elastic_slab) of 4000 kg/m^3,
+    1e27 Pa s, shear modulus 1e10 Pa, attached to the left wall, in a medium of 1 kg/m^3, 1e21 Pa s,
+    1e20 Pa; both split into the reference's checkerboard of material ids 2-5
+    (ElasticSlab.define_material, 20 x 20 squares).  ElasticSlabBC.jl: no slip on the left wall,
+    free slip elsewhere, pressure fixed in the upper-left cell.  Gravity 10 m/s^2 for the first
+    100 steps (GravityFuncs.turn_off_gravity!), 200 yr steps multiplied by 10 after step 250
+    (TimeStepIncrease single increase), subgrid stress diffusion off, heat on with uniform 0 C."""
+    W = H = 1000e3
+    grid = staggered_grid(np.linspace(0.0, W, xnum), np.linspace(0.0, H, ynum))
+    mx, my = (xnum - 1) * mpc, (ynum - 1) * mpc
+    x = np.repeat((np.arange(mx) + 0.5) * (W / mx), my)
+    y = np.tile((np.arange(my) + 0.5) * (H / my), mx)
+    n = len(x)
+
+    def check(v, size):
+        c = np.ceil(v / (size / 20.0)) + 1.0
+        return c - np.ceil(c / 2.0) * 2.0
+    matid = np.where(check(y, H) == check(x, W), 3, 2)
+    slab = (0.2 < y / H) & (y / H < 0.8) & (x / W < 0.8)
+    matid = np.where(slab, np.where(matid == 2, 4, 5), matid).astype(np.int16)
+    # material ids 1-5 (id 1 unused, as in the reference's material model)
+    eta = np.array([1e21, 1e21, 1e21, 1e27, 1e27])
+    mu = np.array([1e20, 1e20, 1e20, 1e10, 1e10])
+    rho = np.array([1.0, 1.0, 1.0, 4000.0, 4000.0])
+    mats = Materials(
+        mat_mu=mu, mat_hr=np.zeros(5), mat_flow_type=np.zeros(5, np.int64),
+        mat_flow=np.asfortranarray(np.zeros((5, 12))), mat_plastic=np.asfortranarray(np.zeros((5, 6))), mat_rho=rho)
+    mats.mat_flow[:, 0] = eta
+    mi = matid.astype(np.int64) - 1
+    T0 = 273.15
+    m = {"x": x, "y": y, "matid": matid, "rho": rho[mi].copy(), "eta": eta[mi].copy(), "eta_flow": eta[mi].copy(),
+         "sr_ratio": np.ones(n), "tk": np.full(n, T0), "kt": np.full(n, 3.0), "rhocp": rho[mi] * 1000.0,
+         "ha": np.zeros(n)}
+    for f in ("cohesion", "fric", "fric_ini", "preexp", "sxx", "sxy", "exx", "exy", "pr", "gii", "strain_plastic"):
+        m[f] = np.zeros(n)
+    _fields_common(np.random.Generator(np.random.Philox(0)), n, m)
+    m["pfailure"][:] = 0.0
+    grids = _analytic_grids(grid, v0=0.0, eta_ref=1e21, rho_ref=1.0, T0=T0, T1=T0, depth_T1=H, y_surface=0.0)
+    grids.update(velocity_bcs(grid))
+    F = np.asfortranarray
+    X, Y = xnum, ynum
+    grids["bleftx"] = F(np.zeros((Y + 1, 2)))
+    grids["blefty"] = F(np.column_stack([np.zeros(Y), -np.ones(Y)]))
+    grids["bleftt"] = F(np.column_stack([np.zeros(Y), np.ones(Y)]))
+    grids["brightt"] = F(np.column_stack([np.zeros(Y), np.ones(Y)]))
+    params = default_params(timestep=200.0 * YEAR, viscosity_min=1e18, viscosity_max=1e27, temperature_top=T0,
+                            itype_global=1, ntimestep=1, subgrid_diff_coef_stress=0.0, subgrid_diff_coef_temp=1.0,
+                            temperature_bottom=T0)
+    params.update(stokes_params(pressure_bc_mode=0, pressure_bc=0.0, gravity_y=10.0, iuse_interface_stabilization=0))
+    params.update(max_temp_change=20.0, iuse_adiabatic_heating=0, iuse_shear_heating=0, iuse_heat=1,
+                  marker_cell_displ_max=0.3333, nsteps_turn_off_gravity=100, ntime_increase=250,
+                  time_increase_factor=10.0, nskip_output=50)
+    return Model("elastic_slab", grid, mats, params, m, grids)
+
+
 def ramberg_wave_velocity(h1: float, h2: float, rho1: float, rho2: float, eta1: float, eta2: float, amp: float,
                           lam: float, g: float = 9.81) -> float:
     """Ramberg's (1968) analytical vertical velocity at the crest of a sinusoidal interface

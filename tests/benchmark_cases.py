@@ -173,3 +173,51 @@ def vcond_oracle(eb, nsteps: int = VCOND_STEPS):
         m.update_marker_strain()
     pre()
     return model, op.gr["tk1"][VCOND_ROW - 1, :].copy()
+
+
+SLAB_OUTPUTS = (80, 100, 120, 140, 160)
+
+
+def elastic_slab_oracle(eb, outputs=SLAB_OUTPUTS):
+    """The elastic-slab benchmark through the oracle (about 8 minutes on one core: 7950 steps with
+    a direct Stokes solve each, so no CPU test runs it): gravity off after step 100, the step
+    multiplied by 10 after step 250, one output per 50 steps.  Returns {output: largest relative
+    change of a slab marker's distance from the origin}."""
+    from oracle import boundary as B
+    from oracle.picard import OraclePicard
+    model = eb.synthetic.elastic_slab()
+    op = OraclePicard(model)
+    p, g, m = op.model.params, model.grid, op.mic
+    W, H = g.xmax - g.xmin, g.ymax - g.ymin
+    x0, y0 = m.mk["x"].copy(), m.mk["y"].copy()
+    slab = (0.2 < y0 / H) & (y0 / H < 0.8) & (x0 / W < 0.8)
+    d0 = np.hypot(x0[slab], y0[slab])
+    dt, nskip, worst = p["timestep"], p["nskip_output"], {}
+    for step in range(1, 1 + (max(outputs) - 1) * nskip + 1):
+        out = (step - 1) // nskip + 1
+        if (step - 1) % nskip == 0 and out in outputs:
+            worst[out] = float(np.max(np.abs(np.hypot(m.mk["x"][slab], m.mk["y"][slab]) - d0) / d0))
+            if out == max(outputs):
+                break
+        p["timestep"] = dt
+        m.get_marker_inside_flags()
+        m.initialize_bilinear_interpolation()
+        m.interpolate_marker_heat_parameters_to_grid()
+        m.update_marker_rheology()
+        m.update_marker_viscoplastic_viscosity(use_marker_plasticity=False)
+        m.interpolate_marker_stokes_parameters_to_grid()
+        op.so.interpolate_basic_viscoplastic_viscosity_to_pressure_grid(0)
+        op.picard_loop_nodes(1, 1e-3, 0)
+        op.so.interpolate_stag_velocity_to_basic_grid()
+        m.calc_marker_viscoplastic_viscosity()
+        p["timestep"] = B.timestep_displacement_limit(g, op.gr["vx1"], op.gr["vy1"], p["marker_cell_displ_max"], 0, dt)
+        op.so.forecast_viscoelastic_grid_stress()
+        m.post_stokes_marker_gathers()
+        m.apply_marker_stress_correction()
+        m.advect_markers_and_rotate_stress()
+        m.update_marker_strain()
+        if step == p["nsteps_turn_off_gravity"]:
+            p["gravity_y"] = 0.0
+        if step == p["ntime_increase"]:
+            dt = dt * p["time_increase_factor"]
+    return worst

@@ -235,3 +235,46 @@ def test_variable_conductivity_channel_matches_the_steady_profile(eb):
     assert err < 0.022, err
     assert dev < 0.05, dev
     mic.close()
+
+
+def test_elastic_slab_recovers_its_shape(eb):
+    """The reference's elastic-slab benchmark (models/elastic_slab,
+    post_processing/analytical/ElasticSlabManager.jl) through 7950 GPU time steps: a
+    visco-elastic slab attached to the left wall bends under gravity for 100 steps, gravity is
+    switched off (GravityFuncs.turn_off_gravity!), the 200 yr step grows tenfold after step 250
+    (TimeStepIncrease), and the slab springs back.  With the reference's fixed output counter
+    (one output per 50 steps), outputs 80, 100, 120, 140 and 160 must each put every slab marker
+    within the reference's 0.3 % of its initial distance from the origin."""
+    syn = eb.synthetic
+    model = syn.elastic_slab()
+    p = dict(model.params)
+    W = model.grid.xmax - model.grid.xmin
+    H = model.grid.ymax - model.grid.ymin
+    mic = eb.MarkerInCell(0)
+    mic.load_model(model)
+    x0, y0 = model.markers["x"], model.markers["y"]
+    slab = (0.2 < y0 / H) & (y0 / H < 0.8) & (x0 / W < 0.8)
+    d0 = np.hypot(x0[slab], y0[slab])
+    outputs = (80, 100, 120, 140, 160)
+    worst = {}
+    nskip = p["nskip_output"]
+    for step in range(1, 1 + (max(outputs) - 1) * nskip + 1):
+        out = (step - 1) // nskip + 1
+        if (step - 1) % nskip == 0 and out in outputs:
+            d = np.hypot(mic.download_marker("x")[slab], mic.download_marker("y")[slab])
+            worst[out] = float(np.max(np.abs(d - d0) / d0))
+            if out == max(outputs):
+                break
+        rep = mic.time_step(1, 1e-3, iuse_harmonic=0, marker_cell_displ_max=p["marker_cell_displ_max"], rtol=1e-10)
+        assert rep["picard"][-1]["status"] == 0, (step, rep["picard"])
+        mp = mic._params
+        if step == p["nsteps_turn_off_gravity"]:
+            mp["gravity_y"] = 0.0
+            mic.set_stokes_params(mp)
+        if step == p["ntime_increase"]:
+            mp["timestep_viscoelastic"] = mp["timestep_viscoelastic"] * p["time_increase_factor"]
+    print("\nelastic slab: largest relative change of a slab marker's distance from the origin "
+          + ", ".join(f"output {k}: {100 * v:.4f} %" for k, v in sorted(worst.items())) + " (limit 0.3 %)")
+    for k, v in worst.items():
+        assert v < 0.003, (k, v)
+    mic.close()
