@@ -831,6 +831,86 @@ def elastic_slab(xnum: int = 51, ynum: int = 51, mpc: int = 5) -> Model:
     return Model("elastic_slab", grid, mats, params, m, grids)
 
 
+def box_convection(mpc: int = 4) -> Model:
+    """The reference's isoviscous box-convection benchmark, Blankenbach et al. (1989) case 1a, as
+    configured in src/benchmarks/models/box_convection_isoviscous_1a/{model,materials}.yml and the
+    benchmark material library (IsoviscousFluidBlankenbach89): a 1000 x 1000 km box on the
+    reference's 51 x 51 grid refined along the sides (sides_with_highres/core/Initialization.jl:
+    10 km cells, a 1.2407234 geometric transition, 30 km cells in the middle), 4 x 4 markers per
+    (average) cell on a regular lattice, the Blankenbach flow law (1e23 Pa s, b = c = 0) and
+    density rho0 (1 - alpha (T - T_top)) (4000 kg/m^3, 2.5e-5 1/K; rock-property density model 1,
+    rhocp constant with 1250 J/kg/K, uniform conductivity 5 W/m/K: params["rock_tables"]),
+    gravity 10 m/s^2, free slip on every side, 0 C at the top, 1000 C at the bottom, no heat flux
+    through the sides, the BoxConvection initial temperature, and 0.5 Myr steps limited to half a
+    cell of marker displacement: Ra = 1e4."""
+    X = Y = 51
+    W = H = 1000e3
+    gy = np.zeros(Y)
+    for i in range(2, 12):
+        gy[i - 1] = gy[i - 2] + 10000.0
+    for i in range(12, 17):
+        gy[i - 1] = gy[i - 2] + 10000.0 * 1.2407234 ** float(i - 10)
+    for i in range(17, 37):
+        gy[i - 1] = gy[i - 2] + 30000.0
+    for i in range(37, 42):
+        gy[i - 1] = gy[i - 2] + 10000.0 * 1.2407234 ** float(41 - i)
+    for i in range(42, Y + 1):
+        gy[i - 1] = gy[i - 2] + 10000.0
+    gy[Y - 1] = H
+    gx = gy * W / H
+    grid = staggered_grid(gx, gy)
+    mx, my = (X - 1) * mpc, (Y - 1) * mpc
+    x = np.repeat((np.arange(mx) + 0.5) * (W / mx), my)
+    y = np.tile((np.arange(my) + 0.5) * (H / my), mx)
+    n = len(x)
+    t_top, t_bot = 273.15, 1273.15
+    xw, yw = x / W, y / H
+    yw = np.where(yw > 0.5, 0.5 + 0.5 * (np.abs(yw - 0.5) / 0.5) ** 10, 0.5 - 0.5 * (np.abs(yw - 0.5) / 0.5) ** 10)
+    T = (t_top + (t_bot - t_top) * yw ** (2.0 + xw) + t_bot + (t_top - t_bot) * (1.0 - yw) ** (3.0 - xw)) / 2.0
+    flow = np.zeros((1, 17))
+    flow[0, 14] = 1e23
+    mats = Materials(
+        mat_mu=np.array([1e28]), mat_hr=np.zeros(1), mat_flow_type=np.array([5], np.int64),
+        mat_flow=np.asfortranarray(flow), mat_plastic=np.asfortranarray(np.zeros((1, 6))), mat_rho=np.array([4000.0]))
+    rho = 4000.0 * (1.0 - 2.5e-5 * (T - t_top))
+    m = {"x": x, "y": y, "matid": np.ones(n, np.int16), "rho": rho, "eta": np.full(n, 1e23),
+         "eta_flow": np.full(n, 1e23), "sr_ratio": np.ones(n), "tk": T, "kt": np.full(n, 5.0),
+         "rhocp": rho * 1250.0, "ha": np.zeros(n)}
+    for f in ("cohesion", "fric", "fric_ini", "preexp", "sxx", "sxy", "exx", "exy", "pr", "gii", "strain_plastic"):
+        m[f] = np.zeros(n)
+    _fields_common(np.random.Generator(np.random.Philox(0)), n, m)
+    m["pfailure"][:] = 0.0
+    grids = _analytic_grids(grid, v0=0.0, eta_ref=1e23, rho_ref=4000.0, T0=t_top, T1=t_bot, depth_T1=H, y_surface=0.0)
+    grids.update(velocity_bcs(grid))
+    F = np.asfortranarray
+    grids["btopt"] = F(np.column_stack([np.full(X, t_top), np.zeros(X)]))
+    grids["bbottomt"] = F(np.column_stack([np.full(X, t_bot), np.zeros(X)]))
+    grids["bleftt"] = F(np.column_stack([np.zeros(Y), np.ones(Y)]))
+    grids["brightt"] = F(np.column_stack([np.zeros(Y), np.ones(Y)]))
+    params = default_params(timestep=0.5e6 * YEAR, viscosity_min=1e18, viscosity_max=1e27, temperature_top=t_top,
+                            temperature_bottom=t_bot, itype_global=1, ntimestep=1, subgrid_diff_coef_stress=0.0,
+                            subgrid_diff_coef_temp=1.0)
+    params.update(stokes_params(pressure_bc_mode=0, pressure_bc=0.0, gravity_y=10.0, iuse_interface_stabilization=0))
+    params.update(max_temp_change=20.0, iuse_adiabatic_heating=0, iuse_shear_heating=0, iuse_heat=1,
+                  marker_cell_displ_max=0.5, nskip_output=100)
+    params["rock_tables"] = {"mat_rho": np.array([[4000.0, 2.5e-5, 0.0]]), "mat_cp": np.array([1250.0]),
+                             "mat_kt": np.array([[5.0, 0.0]]), "density_model": 1, "rhocp_model": 0,
+                             "conductivity_model": 1}
+    return Model("box_convection_isoviscous_1a", grid, mats, params, m, grids)
+
+
+def box_convection_vrms(grid: Grid, vx1: np.ndarray, vy1: np.ndarray, conductivity: float, heat_capacity: float,
+                        density: float) -> float:
+    """BoxConvection.calculate_nondimensional_rms_velocity (post_processing/numerical/box_convection/
+    BoxConvection.jl:66-88): the cell-weighted mean of (vx^2 at the cell's two vx nodes + vy^2 at
+    its two vy nodes) / 2, its square root scaled by ysize / kappa."""
+    xs, ys = grid.xstp_b, grid.ystp_b
+    W, H = grid.xmax - grid.xmin, grid.ymax - grid.ymin
+    a = (vx1[1:-1, :-1] ** 2 + vx1[1:-1, 1:] ** 2 + vy1[:-1, 1:-1] ** 2 + vy1[1:, 1:-1] ** 2) / 2.0
+    v = float(np.sum(a * ys[:, None] * xs[None, :]))
+    return math.sqrt(v / W / H) * H / (conductivity / heat_capacity / density)
+
+
 def ramberg_wave_velocity(h1: float, h2: float, rho1: float, rho2: float, eta1: float, eta2: float, amp: float,
                           lam: float, g: float = 9.81) -> float:
     """Ramberg's (1968) analytical vertical velocity at the crest of a sinusoidal interface

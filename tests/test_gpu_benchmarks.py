@@ -278,3 +278,39 @@ def test_elastic_slab_recovers_its_shape(eb):
     for k, v in worst.items():
         assert v < 0.003, (k, v)
     mic.close()
+
+
+def test_box_convection_reaches_blankenbach_case_1a(eb):
+    """The reference's isoviscous box-convection benchmark (models/box_convection_isoviscous_1a,
+    post_processing/numerical/box_convection/BoxConvectionManager.jl): Blankenbach et al. (1989)
+    case 1a, Ra = 1e4, run as the reference runs it for output 100 of its fixed output counter
+    (one output per 100 steps): 9900 GPU time steps of rock properties (the Blankenbach density),
+    the Blankenbach flow law, one nodal Picard iteration, the heat step and RK4 advection, after
+    the initial grid-to-marker temperature interpolation.  The dimensionless RMS velocity of the
+    last solution must lie within the reference's 0.2 % of the benchmark value 42.865."""
+    syn = eb.synthetic
+    model = syn.box_convection()
+    rt = model.params["rock_tables"]
+    mic = eb.MarkerInCell(0)
+    mic.load_model(model)
+    mic.set_rock_tables(rt["mat_rho"], rt["mat_cp"], rt["mat_kt"])
+    mic.get_marker_inside_flags()
+    mic.initialize_bilinear_interpolation_and_heat_scatter()
+    mic.interpolate_temperature_to_markers()  # iuse_initial_temp_interp
+    nsteps = 99 * model.params["nskip_output"]
+    history = []
+    for step in range(1, nsteps + 1):
+        mic.get_marker_inside_flags()
+        mic.update_marker_rock_properties(rt["density_model"], rt["rhocp_model"], rt["conductivity_model"])
+        rep = mic.time_step(1, 1e-3, iuse_harmonic=0, heat=True, marker_cell_displ_max=model.params["marker_cell_displ_max"],
+                            rtol=1e-10)
+        assert rep["picard"][-1]["status"] == 0, (step, rep["picard"])
+        if step % 1000 == 0 or step == nsteps:
+            history.append((step, syn.box_convection_vrms(model.grid, mic.download_grid("vx1"), mic.download_grid("vy1"),
+                                                          5.0, 1250.0, 4000.0)))
+    vrms = history[-1][1]
+    err = abs(vrms - 42.865) / 42.865
+    print("\nbox convection (Blankenbach 1a): vrms by step " + ", ".join(f"{s}: {v:.3f}" for s, v in history)
+          + f"; final {vrms:.3f} against 42.865, relative error {100 * err:.3f} % (limit 0.2 %)")
+    assert err < 0.002, (vrms, history)
+    mic.close()
