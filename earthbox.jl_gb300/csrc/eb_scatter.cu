@@ -366,7 +366,9 @@ using HeatSpec = HeatSpecT<false>;
 // roles: 0 exclusive quadrants (shared slot q), 1 central node (registers)
 struct ViscSpec {
   static constexpr const char* kName = "k_cells<viscosity>";
-  static constexpr int kRoles = 2, kNV = S_V0 + 1, kAcc = 1, kSlots = 4;
+  // roles 0-3: the exclusive quadrant of that index (registers), 4: the central node; one warp
+  // per quadrant keeps the fold short (a marker usually lies in one quadrant)
+  static constexpr int kRoles = 5, kNV = S_V0 + 1, kAcc = 1, kSlots = 0;
   struct Cell {};
   __device__ Cell cell(const DevGrid&, int32_t, int32_t) const { return Cell{}; }
   struct Raw { double eta; float fx, fy; uint8_t fl; };
@@ -383,18 +385,14 @@ struct ViscSpec {
   }
   __device__ void accum(int role, int lane, int t, float (*sv)[kChunk], const uint8_t* sfl, KSum2* a, SAcc sa) const {
     const float e = sv[S_V0][t];
-    if (role == 0) {
-      for (uint32_t m = quadrant_mask(sfl[t]); m; m &= m - 1) {
-        const int q = __ffs(m) - 1;
-        sa.add1(q, lane, sv[S_UL + q][t] * e);
-      }
+    if (role < 4) {
+      if ((quadrant_mask(sfl[t]) >> role) & 1u) a[0].add(make_float2(sv[S_UL + role][t] * e, 0.f));
     } else {
       a[0].add(make_float2(sv[S_WC][t] * e, 0.f));
     }
   }
-  __device__ void store(int role, int lane, int32_t cell, int32_t nc, const KSum2* a, SAcc sa, float* part) const {
-    if (role == 0) for (int q = 0; q < 4; ++q) part[(size_t)q * nc + cell] = sa.get0(q, lane);
-    else part[(size_t)4 * nc + cell] = a[0].x();
+  __device__ void store(int role, int, int32_t cell, int32_t nc, const KSum2* a, SAcc, float* part) const {
+    part[(size_t)role * nc + cell] = a[0].x();
   }
 };
 
@@ -421,10 +419,11 @@ __device__ __forceinline__ float gather_pressure_grid(const float* __restrict__ 
 // Subgrid stress (SubgridShearStress.jl:27-96, SubgridNormalStress.jl:27-89):
 // put() relaxes the marker stress, writes it back and stages the relaxed change.
 // part slots: 0-3 excl relax_xy*w, 4-7 excl w, 8 central relax_xx*wc, 9 central wc
-// roles: 0 exclusive quadrants (shared pair slot q: {relax_xy*w, w}), 1 central node (registers)
+// roles 0-3: the exclusive quadrant of that index ({relax_xy*w, w} in registers), 4: the central
+// node; one warp per quadrant keeps the fold, which the staging warps wait for, short
 struct SubgridStressSpec {
   static constexpr const char* kName = "k_cells<subgrid_stress>";
-  static constexpr int kRoles = 2, kNV = S_V0 + 2, kAcc = 1, kSlots = 4;
+  static constexpr int kRoles = 5, kNV = S_V0 + 2, kAcc = 1, kSlots = 0;
   const float *sxy1, *sxx1;  // FP32 mirrors
   const double* mat_mu;
   float dt, coef;
@@ -462,28 +461,20 @@ struct SubgridStressSpec {
     sv[S_V0 + 1][t] = rxx;
   }
   __device__ void accum(int role, int lane, int t, float (*sv)[kChunk], const uint8_t* sfl, KSum2* a, SAcc sa) const {
-    if (role == 0) {
-      const float r = sv[S_V0][t];
-      for (uint32_t m = quadrant_mask(sfl[t]); m; m &= m - 1) {
-        const int q = __ffs(m) - 1;
-        const float w = sv[S_UL + q][t];
-        sa.add2(q, lane, make_float2(w * r, w));
+    if (role < 4) {
+      if ((quadrant_mask(sfl[t]) >> role) & 1u) {
+        const float w = sv[S_UL + role][t];
+        a[0].add(make_float2(w * sv[S_V0][t], w));
       }
     } else {
       const float w = sv[S_WC][t];
       a[0].add(make_float2(w * sv[S_V0 + 1][t], w));
     }
   }
-  __device__ void store(int role, int lane, int32_t cell, int32_t nc, const KSum2* a, SAcc sa, float* part) const {
-    if (role == 0) {
-      for (int q = 0; q < 4; ++q) {
-        part[(size_t)q * nc + cell] = sa.get0(q, lane);
-        part[(size_t)(4 + q) * nc + cell] = sa.get1(q, lane);
-      }
-    } else {
-      part[(size_t)8 * nc + cell] = a[0].x();
-      part[(size_t)9 * nc + cell] = a[0].y();
-    }
+  __device__ void store(int role, int, int32_t cell, int32_t nc, const KSum2* a, SAcc, float* part) const {
+    const int q = role < 4 ? role : 8;
+    part[(size_t)q * nc + cell] = a[0].x();
+    part[(size_t)(q < 4 ? 4 + q : 9) * nc + cell] = a[0].y();
   }
 };
 
