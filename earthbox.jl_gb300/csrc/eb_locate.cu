@@ -102,7 +102,9 @@ __global__ void k_place(const int32_t* __restrict__ xn, const int32_t* __restric
   }
 }
 
-// One warp per cell: order the cell's marker indices ascending (rank by count).
+// One warp per cell: order the cell's marker indices ascending.  Up to 32 markers: a bitonic
+// network across the warp's lanes (15 compare-exchange stages; the padding INT32_MAX sorts last
+// and every index is distinct); more: rank by count.
 __global__ void k_sort_segments(const int32_t* __restrict__ start, int32_t ncells,
                                 const int32_t* __restrict__ perm_tmp, int32_t* __restrict__ perm) {
   const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -110,11 +112,17 @@ __global__ void k_sort_segments(const int32_t* __restrict__ start, int32_t ncell
   if (warp >= ncells) return;
   const int32_t beg = start[warp], n = start[warp + 1] - beg;
   if (n <= 32) {
-    const int32_t v = lane < n ? perm_tmp[beg + lane] : INT32_MAX;
-    int r = 0;
-#pragma unroll 8
-    for (int j = 0; j < 32; ++j) r += (__shfl_sync(0xffffffffu, v, j) < v);
-    if (lane < n) perm[beg + r] = v;
+    int32_t v = lane < n ? perm_tmp[beg + lane] : INT32_MAX;
+#pragma unroll
+    for (int k = 2; k <= 32; k <<= 1) {
+#pragma unroll
+      for (int j = k >> 1; j > 0; j >>= 1) {
+        const int32_t o = __shfl_xor_sync(0xffffffffu, v, j);
+        const bool keep_min = ((lane & j) == 0) == ((lane & k) == 0);
+        v = keep_min ? min(v, o) : max(v, o);
+      }
+    }
+    if (lane < n) perm[beg + lane] = v;
   } else {
     for (int i = lane; i < n; i += 32) {
       const int32_t v = perm_tmp[beg + i];
