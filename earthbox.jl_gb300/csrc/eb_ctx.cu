@@ -274,9 +274,9 @@ static void free_grid_tables(eb_ctx* c) {
     c->gf[f] = nullptr;
     c->gf32[f] = nullptr;
   }
-  cudaFree(c->cs.count); cudaFree(c->cs.start); cudaFree(c->cs.cursor); cudaFree(c->cs.scan_tmp);
+  cudaFree(c->cs.count); cudaFree(c->cs.start); cudaFree(c->cs.scan_tmp);
   cudaFree(c->part);
-  c->cs.count = c->cs.start = c->cs.cursor = c->cs.scan_tmp = nullptr;
+  c->cs.count = c->cs.start = c->cs.scan_tmp = nullptr;
   c->part = nullptr;
 }
 
@@ -430,7 +430,6 @@ extern "C" int eb_set_grid(eb_ctx* c, const eb_grid_desc* G) {
   s.scan_blocks = (s.ncells + 1 + 1023) / 1024;
   EB_CK(c, cudaMalloc(&s.count, (s.ncells + 1) * sizeof(int32_t)));
   EB_CK(c, cudaMalloc(&s.start, (s.ncells + 1) * sizeof(int32_t)));
-  EB_CK(c, cudaMalloc(&s.cursor, (s.ncells + 1) * sizeof(int32_t)));
   EB_CK(c, cudaMalloc(&s.scan_tmp, (s.scan_blocks + 1) * sizeof(int32_t)));
   EB_CK(c, cudaMalloc(&c->part, (size_t)kMaxSlots * s.ncells * sizeof(float)));
   g.kxmin = dkey(G->xmin); g.kxmax = dkey(G->xmax);

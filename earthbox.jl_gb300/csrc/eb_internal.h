@@ -74,7 +74,6 @@ struct CellSort {
   int32_t ncells;        // (ynum-1)*(xnum-1)
   int32_t* count;        // [ncells+1]
   int32_t* start;        // [ncells+1] exclusive scan of count
-  int32_t* cursor;       // [ncells]
   int32_t* perm;         // [M] marker indices grouped by cell, ascending within a cell
   int32_t* perm_tmp;     // [M] placement buffer before the per-cell sort
   int32_t* scan_tmp;     // block sums for the scan

@@ -43,8 +43,11 @@ __device__ __forceinline__ uint32_t half_bits(float f, double d,
   return exact_half_bits(d, __ldg(&s_tab[k]));
 }
 
+// rank[m]: the marker's slot within its cell's segment, from the histogram's own atomics (the
+// order of the warps' groups within a cell is the atomics' order; k_sort_segments restores
+// marker order).
 __global__ void k_locate_count(DevMarkers mk, DevGrid g, int32_t* __restrict__ count,
-                               int32_t* __restrict__ dflag) {
+                               int32_t* __restrict__ dflag, int32_t* __restrict__ rank) {
   int64_t m = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   int32_t key = -1;
   if (m < mk.M) {
@@ -79,27 +82,22 @@ __global__ void k_locate_count(DevMarkers mk, DevGrid g, int32_t* __restrict__ c
   }
   // warp-aggregated histogram: one atomic per distinct cell per warp
   const unsigned peers = __match_any_sync(0xffffffffu, key);
+  const int lane = threadIdx.x & 31;
   const int leader = __ffs(peers) - 1;
-  if (key >= 0 && (int)(threadIdx.x & 31) == leader) atomicAdd(&count[key], __popc(peers));
+  int32_t base = 0;
+  if (key >= 0 && lane == leader) base = atomicAdd(&count[key], __popc(peers));
+  base = __shfl_sync(0xffffffffu, base, leader);
+  if (key >= 0) rank[m] = base + __popc(peers & ((1u << lane) - 1u));
 }
 
 __global__ void k_place(const int32_t* __restrict__ xn, const int32_t* __restrict__ yn,
                         const uint8_t* __restrict__ mflags, int64_t M, int32_t ynum,
-                        const int32_t* __restrict__ start, int32_t* __restrict__ cursor,
+                        const int32_t* __restrict__ start, const int32_t* __restrict__ rank,
                         int32_t* __restrict__ perm_tmp) {
-  int64_t m = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  int32_t key = -1;
-  if (m < M && (mflags[m] & MF_INSIDE)) key = (xn[m] - 1) * (ynum - 1) + (yn[m] - 1);
-  const unsigned peers = __match_any_sync(0xffffffffu, key);
-  const int lane = threadIdx.x & 31;
-  const int leader = __ffs(peers) - 1;
-  int32_t base = 0;
-  if (key >= 0 && lane == leader) base = atomicAdd(&cursor[key], __popc(peers));
-  base = __shfl_sync(0xffffffffu, base, leader);
-  if (key >= 0) {
-    const int r = __popc(peers & ((1u << lane) - 1u));
-    perm_tmp[start[key] + base + r] = (int32_t)m;
-  }
+  const int64_t m = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= M || !(mflags[m] & MF_INSIDE)) return;
+  const int32_t key = (xn[m] - 1) * (ynum - 1) + (yn[m] - 1);
+  perm_tmp[start[key] + rank[m]] = (int32_t)m;
 }
 
 // One warp per cell: order the cell's marker indices ascending.  Up to 32 markers: a bitonic
@@ -209,11 +207,11 @@ int launch_locate_and_sort(eb_ctx* c) {
   CellSort& s = c->cs;
   const int32_t n = s.ncells + 1;
   EB_CK(c, cudaMemsetAsync(s.count, 0, n * sizeof(int32_t), c->stream));
-  EB_CK(c, cudaMemsetAsync(s.cursor, 0, n * sizeof(int32_t), c->stream));
   EB_CK(c, cudaMemsetAsync(c->dflag, 0, sizeof(int32_t), c->stream));
   const unsigned mblocks = (unsigned)((c->M + kBlock - 1) / kBlock);
   EB_PROF(c, "k_locate_count");
-  k_locate_count<<<mblocks, kBlock, 0, c->stream>>>(mk, c->g, s.count, c->dflag);
+  // s.perm holds each marker's slot in its cell until k_sort_segments writes the sorted list
+  k_locate_count<<<mblocks, kBlock, 0, c->stream>>>(mk, c->g, s.count, c->dflag, s.perm);
   EB_LAUNCHED(c);
   EB_PROF(c, "k_scan_blocks");
   k_scan_blocks<<<s.scan_blocks, 1024, 0, c->stream>>>(s.count, n, s.start, s.scan_tmp);
@@ -225,7 +223,7 @@ int launch_locate_and_sort(eb_ctx* c) {
   k_scan_add<<<s.scan_blocks, 1024, 0, c->stream>>>(s.start, n, s.scan_tmp);
   EB_LAUNCHED(c);
   EB_PROF(c, "k_place");
-  k_place<<<mblocks, kBlock, 0, c->stream>>>(mk.xn, mk.yn, mk.mflags, c->M, c->ynum, s.start, s.cursor, s.perm_tmp);
+  k_place<<<mblocks, kBlock, 0, c->stream>>>(mk.xn, mk.yn, mk.mflags, c->M, c->ynum, s.start, s.perm, s.perm_tmp);
   EB_LAUNCHED(c);
   const unsigned sblocks = (unsigned)(((int64_t)s.ncells * 32 + kBlock - 1) / kBlock);
   EB_PROF(c, "k_sort_segments");
