@@ -911,6 +911,93 @@ def box_convection_vrms(grid: Grid, vx1: np.ndarray, vy1: np.ndarray, conductivi
     return math.sqrt(v / W / H) * H / (conductivity / heat_capacity / density)
 
 
+def channel_flow_non_steady_temperature(xnum: int = 51, ynum: int = 11, mpc: int = 5) -> Model:
+    """The reference's non-steady channel-temperature benchmark, as configured in
+    src/benchmarks/models/channel_flow_non_steady_temperature/{model,materials}.yml and the
+    benchmark material library (ConstantViscosityChannel): a 30 x 12.5 km vertical channel on
+    51 x 11 nodes with 5 x 5 markers per cell on a regular lattice, an isoviscous material
+    (1e19 Pa s, 3000 kg/m^3, 1000 J/kg/K, 2 W/m/K), the linear initial temperature from 727 C at
+    the top to 1227 C at the bottom, VerticalChannelFlowIsoviscousBC.jl: the open channel with
+    1e5 Pa on the top row of pressure cells, no slip on both walls, the initial linear profile held
+    on both walls (TemperatureBC.set_variable_temperature_at_*_boundary!) and its gradient through
+    the top and the bottom (ConstantGradientBC.jl); subgrid diffusion on, 1 Myr steps limited to a
+    tenth of a cell of displacement, the channel recycling."""
+    W, H = 30e3, 12.5e3
+    grid = staggered_grid(np.linspace(0.0, W, xnum), np.linspace(0.0, H, ynum))
+    mx, my = (xnum - 1) * mpc, (ynum - 1) * mpc
+    x = np.repeat((np.arange(mx) + 0.5) * (W / mx), my)
+    y = np.tile((np.arange(my) + 0.5) * (H / my), mx)
+    n = len(x)
+    t_top, t_bot = 727.0 + 273.15, 1227.0 + 273.15
+    T = t_top + (t_bot - t_top) * y / H
+    mats = Materials(
+        mat_mu=np.array([1e20]), mat_hr=np.zeros(1), mat_flow_type=np.array([0], np.int64),
+        mat_flow=np.asfortranarray(np.zeros((1, 12))), mat_plastic=np.asfortranarray(np.zeros((1, 6))),
+        mat_rho=np.array([3000.0]))
+    mats.mat_flow[0, 0] = 1e19
+    m = {"x": x, "y": y, "matid": np.ones(n, np.int16), "rho": np.full(n, 3000.0), "eta": np.full(n, 1e19),
+         "eta_flow": np.full(n, 1e19), "sr_ratio": np.ones(n), "tk": T, "kt": np.full(n, 2.0),
+         "rhocp": np.full(n, 3000.0 * 1000.0), "ha": np.zeros(n)}
+    for f in ("cohesion", "fric", "fric_ini", "preexp", "sxx", "sxy", "exx", "exy", "pr", "gii", "strain_plastic"):
+        m[f] = np.zeros(n)
+    _fields_common(np.random.Generator(np.random.Philox(0)), n, m)
+    m["pfailure"][:] = 0.0
+    grids = _analytic_grids(grid, v0=0.0, eta_ref=1e19, rho_ref=3000.0, T0=t_top, T1=t_bot, depth_T1=H,
+                            y_surface=0.0)
+    grids.update(velocity_bcs(grid))
+    F = np.asfortranarray
+    X, Y = xnum, ynum
+    ystp, dtdy = H / (Y - 1), (t_bot - t_top) / H
+    grids["btopx"] = F(np.column_stack([np.zeros(X), np.ones(X)]))
+    grids["bbottomx"] = F(np.column_stack([np.zeros(X), np.ones(X)]))
+    grids["btopy"] = F(np.column_stack([np.zeros(X + 1), np.ones(X + 1)]))
+    grids["bbottomy"] = F(np.column_stack([np.zeros(X + 1), np.ones(X + 1)]))
+    grids["bleftx"] = F(np.zeros((Y + 1, 2)))
+    grids["brightx"] = F(np.zeros((Y + 1, 2)))
+    grids["blefty"] = F(np.column_stack([np.zeros(Y), -np.ones(Y)]))
+    grids["brighty"] = F(np.column_stack([np.zeros(Y), -np.ones(Y)]))
+    grids["btopt"] = F(np.column_stack([np.full(X, -ystp * dtdy), np.ones(X)]))
+    grids["bbottomt"] = F(np.column_stack([np.full(X, ystp * dtdy), np.ones(X)]))
+    wall = t_top + np.arange(Y) * ystp * dtdy
+    grids["bleftt"] = F(np.column_stack([wall, np.zeros(Y)]))
+    grids["brightt"] = F(np.column_stack([wall, np.zeros(Y)]))
+    params = default_params(timestep=1e6 * YEAR, viscosity_min=1e18, viscosity_max=1e25, temperature_top=t_top,
+                            temperature_bottom=t_bot, itype_global=1, ntimestep=1)
+    params.update(stokes_params(pressure_bc_mode=1, pressure_bc=1e5, gravity_y=0.0, iuse_interface_stabilization=0))
+    params.update(max_temp_change=10.0, iuse_adiabatic_heating=0, iuse_shear_heating=0, iuse_heat=1,
+                  marker_cell_displ_max=0.1, nskip_output=5)
+    return Model("channel_flow_non_steady_temperature", grid, mats, params, m, grids)
+
+
+def channel_flow_non_steady_temperature_profile(x: np.ndarray, tmyr: float, width: float, ysize: float, ynum: int,
+                                                y_index: int, t_top_c: float, t_bottom_c: float,
+                                                top_pressure: float, viscosity: float, conductivity: float,
+                                                density: float, heat_capacity: float) -> np.ndarray:
+    """Temperature (C) across the channel at the row y_index after tmyr Myr, as the reference's
+    benchmark evaluates it (post_processing/analytical/ChannelFlowNonSteadyTemperatureManager.jl,
+    after Gerya 2010 with its 1/4 factor): T0 = T_top + y G at the row (Celsius + 273.0, the
+    reference's conversion), dp/dy = -top_pressure / (ysize - dy), e = -dp/dy G / (4 eta), and
+    100 terms m = 1..100 of F_m E_m sin(pi (2m' - 1) x / W) with m' = m - 1 (the reference's
+    indexing), F_m = -8 e W^2 / (pi (2m' - 1))^3, E_m = W^2 (1 - exp(-kappa t (pi (2m' - 1))^2 / W^2))
+    / (kappa (pi (2m' - 1))^2) and t = tmyr in 365-day years."""
+    t_top, t_bot = t_top_c + 273.0, t_bottom_c + 273.0
+    grad_t = (t_bot - t_top) / ysize
+    y_test = (y_index - 1) * ysize / (ynum - 1)
+    t0 = t_top + y_test * grad_t
+    grad_p = -top_pressure / (ysize - ysize / (ynum - 1))
+    tsec = tmyr * 1e6 * 365.0 * 24.0 * 60.0 * 60.0
+    ep = -1.0 / 4.0 / viscosity * grad_p * grad_t
+    kappa = conductivity / density / heat_capacity
+    dT = np.zeros_like(np.asarray(x, dtype=np.float64))
+    for mm in range(1, 101):
+        mf = float(mm - 1)
+        a = math.pi * (2.0 * mf - 1.0)
+        emt = width * width * (1.0 - math.exp(-kappa * tsec / width / width * a ** 2.0)) / (kappa * a ** 2.0)
+        fm = -8.0 * ep * width * width / a ** 3.0
+        dT = dT + fm * emt * np.sin(a * np.asarray(x) / width)
+    return t0 + dT - 273.0
+
+
 def ramberg_wave_velocity(h1: float, h2: float, rho1: float, rho2: float, eta1: float, eta2: float, amp: float,
                           lam: float, g: float = 9.81) -> float:
     """Ramberg's (1968) analytical vertical velocity at the crest of a sinusoidal interface

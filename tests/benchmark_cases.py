@@ -221,3 +221,78 @@ def elastic_slab_oracle(eb, outputs=SLAB_OUTPUTS):
         if step == p["ntime_increase"]:
             dt = dt * p["time_increase_factor"]
     return worst
+
+
+NST_OUTPUTS = (1, 10, 20, 30, 40, 50, 60, 70, 80, 100, 120, 140, 160, 180, 200, 220, 240)
+NST_ROW = 11
+
+
+def nst_error(eb, model, row_k, tmyr) -> float:
+    """ChannelFlowNonSteadyTemperatureManager.get_test_results for one output: row 11 of the grid
+    temperature (Celsius) against the transient analytic profile at the output's time; largest
+    relative error."""
+    g = model.grid
+    ana = eb.synthetic.channel_flow_non_steady_temperature_profile(
+        g.gridx_b, tmyr, g.xmax - g.xmin, g.ymax - g.ymin, g.ynum, NST_ROW, 727.0, 1227.0, 1e5, 1e19, 2.0, 3000.0,
+        1000.0)
+    num = row_k - 273.15
+    return float(np.max(np.abs(num - ana) / np.abs(ana)))
+
+
+def nst_oracle(eb):
+    """The non-steady channel benchmark through the oracle, run as the reference's time loop runs
+    it: the initial grid temperature interpolated back to the markers, then per step the
+    pre-solver averages, one nodal Picard iteration, the displacement-limited step, the
+    post-Stokes steps, the heat step, RK4 advection and the channel recycling (which shifts a
+    recycled marker's temperature by T_top - T_bottom).  Returns (model, {output: (time in Myr,
+    row-11 grid temperature)}) for the reference's outputs (one per 5 steps)."""
+    from oracle import boundary as B
+    from oracle.heat import HeatOracle
+    from oracle.picard import OraclePicard
+    model = eb.synthetic.channel_flow_non_steady_temperature()
+    op = OraclePicard(model)
+    p, g, m = op.model.params, model.grid, op.mic
+    dt_ve, nskip = p["timestep"], p["nskip_output"]
+
+    def pre():
+        m.get_marker_inside_flags()
+        m.initialize_bilinear_interpolation()
+        m.interpolate_marker_heat_parameters_to_grid()
+    pre()
+    m.interpolate_temperature_to_markers()
+    tsum, rows = 0.0, {}
+    for step in range(1, 1 + (max(NST_OUTPUTS) - 1) * nskip + 1):
+        p["timestep"] = dt_ve
+        pre()
+        out = (step - 1) // nskip + 1
+        if (step - 1) % nskip == 0 and out in NST_OUTPUTS:
+            rows[out] = (tsum / (1e6 * 365.25 * 24.0 * 3600.0), m.gr["tk1"][NST_ROW - 1, :].copy())
+            if out == max(NST_OUTPUTS):
+                break
+        m.update_marker_rheology()
+        m.update_marker_viscoplastic_viscosity(use_marker_plasticity=False)
+        m.interpolate_marker_stokes_parameters_to_grid()
+        op.so.interpolate_basic_viscoplastic_viscosity_to_pressure_grid(0)
+        op.picard_loop_nodes(1, 1e-3, 0)
+        op.so.interpolate_stag_velocity_to_basic_grid()
+        m.calc_marker_viscoplastic_viscosity()
+        p["timestep"] = B.timestep_displacement_limit(g, op.gr["vx1"], op.gr["vy1"], p["marker_cell_displ_max"], 0,
+                                                      dt_ve)
+        tsum += p["timestep"]
+        op.so.forecast_viscoelastic_grid_stress()
+        m.post_stokes_marker_gathers()
+        m.update_subgrid_stress()
+        m.apply_marker_stress_correction()
+        ho = HeatOracle(op.model, grids=op.gr)
+        ho.heat_step()
+        for k in ("dtk1", "tk2"):
+            op.gr[k] = np.asfortranarray(ho.gr[k])
+        m.subgrid_heat_diffusion_update()
+        m.add_remaining_grid_change_to_marker_temperature()
+        m.advect_markers_and_rotate_stress()
+        m.update_marker_strain()
+        y, tk, _ = B.recycle_channel(m.mk["y"], m.mk["tk"], g.ymin, g.ymax, p["temperature_top"],
+                                     p["temperature_bottom"])
+        m.mk["y"][:] = y
+        m.mk["tk"][:] = tk
+    return model, rows

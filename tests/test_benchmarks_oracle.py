@@ -10,7 +10,11 @@ temperature-dependent viscosity heating itself, against the steady analytic prof
 
 Variable-conductivity channel (src/benchmarks/models/channel_flow_variable_conductivity):
 shear-heated Poiseuille flow with a temperature-dependent conductivity, against the steady
-analytic profile."""
+analytic profile.
+
+Non-steady channel temperature (src/benchmarks/models/channel_flow_non_steady_temperature):
+advection of a vertical temperature gradient by Poiseuille flow with conduction to the walls,
+against the transient analytic profile at every output."""
 from benchmark_cases import rotation_check, solid_body_rotation_oracle
 
 
@@ -44,3 +48,16 @@ def test_oracle_variable_conductivity_channel_matches_the_steady_profile(eb):
     assert row.max() > 1000.0  # the channel centre heated from 298 K
     err = vcond_error(eb, model, row)
     assert err < 0.022, err
+
+
+def test_oracle_non_steady_channel_temperature_follows_the_transient_solution(eb):
+    """The reference's non-steady channel-temperature benchmark
+    (models/channel_flow_non_steady_temperature, ChannelFlowNonSteadyTemperatureManager.jl):
+    every output from 1 to 240 (one per 5 steps) within the reference's 0.7 % (Celsius) of the
+    transient analytic profile."""
+    from benchmark_cases import nst_error, nst_oracle
+    model, rows = nst_oracle(eb)
+    assert rows[240][1].min() < 1000.0  # the channel cooled from its initial 1227 C
+    for out, (tmyr, row) in rows.items():
+        err = nst_error(eb, model, row, tmyr)
+        assert err < 0.007, (out, tmyr, err)

@@ -314,3 +314,49 @@ def test_box_convection_reaches_blankenbach_case_1a(eb):
           + f"; final {vrms:.3f} against 42.865, relative error {100 * err:.3f} % (limit 0.2 %)")
     assert err < 0.002, (vrms, history)
     mic.close()
+
+
+def test_non_steady_channel_temperature_follows_the_transient_solution(eb):
+    """The reference's non-steady channel-temperature benchmark
+    (models/channel_flow_non_steady_temperature, ChannelFlowNonSteadyTemperatureManager.jl)
+    through 1195 GPU time steps: the initial grid temperature interpolated back to the markers,
+    one nodal Picard iteration per step, the displacement-limited step, the heat step with
+    subgrid diffusion, RK4 advection and the channel recycling.  Every output from 1 to 240 must
+    lie within the reference's 0.7 % (Celsius) of the transient analytic profile, and within
+    0.05 K of the oracle's (under 0.001 K measured)."""
+    from benchmark_cases import NST_OUTPUTS, NST_ROW, nst_error, nst_oracle
+    syn = eb.synthetic
+    model = syn.channel_flow_non_steady_temperature()
+    p, g = model.params, model.grid
+    mic = eb.MarkerInCell(0)
+    mic.load_model(model)
+    mic.get_marker_inside_flags()
+    mic.initialize_bilinear_interpolation_and_heat_scatter()
+    mic.interpolate_temperature_to_markers()  # iuse_initial_temp_interp
+    nskip, tsum, rows = p["nskip_output"], 0.0, {}
+    for step in range(1, 1 + (max(NST_OUTPUTS) - 1) * nskip + 1):
+        out = (step - 1) // nskip + 1
+        if (step - 1) % nskip == 0 and out in NST_OUTPUTS:
+            mic.get_marker_inside_flags()
+            mic.initialize_bilinear_interpolation_and_heat_scatter()
+            rows[out] = (tsum / (1e6 * 365.25 * 24.0 * 3600.0), mic.download_grid("tk1")[NST_ROW - 1, :].copy())
+            if out == max(NST_OUTPUTS):
+                break
+        rep = mic.time_step(1, 1e-3, iuse_harmonic=0, heat=True, marker_cell_displ_max=p["marker_cell_displ_max"],
+                            rtol=1e-12)
+        assert rep["picard"][-1]["status"] == 0, (step, rep["picard"])
+        tsum += rep["timestep"]
+        mic.recycle_markers(1, 1, 1, g.xmax, g.ymax, 0.0, 0.0, p["temperature_bottom"], 0, 0, recycle_type=3)
+    _, orows = nst_oracle(eb)
+    worst, dev = 0.0, 0.0
+    for out, (tmyr, row) in rows.items():
+        # the displacement-limited steps follow the solved velocity: 4e-9 relative measured
+        assert abs(tmyr - orows[out][0]) <= 1e-6 * max(tmyr, 1.0), (out, tmyr, orows[out][0])
+        err = nst_error(eb, model, row, tmyr)
+        worst = max(worst, err)
+        dev = max(dev, float(np.max(np.abs(row - orows[out][1]))))
+        assert err < 0.007, (out, tmyr, err)
+    print(f"\nnon-steady channel temperature: 17 outputs to {rows[240][0]:.1f} Myr, largest relative error "
+          f"against the transient analytic profile {100 * worst:.3f} % (limit 0.7 %); against the oracle {dev:.3f} K")
+    assert dev < 0.05, dev
+    mic.close()
