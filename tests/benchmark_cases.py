@@ -296,3 +296,56 @@ def nst_oracle(eb):
         m.mk["y"][:] = y
         m.mk["tk"][:] = tk
     return model, rows
+
+
+def box_convection_oracle(eb, every: int = 1000):
+    """The box-convection benchmark through the oracle (about 12.5 minutes on one core for the
+    9900 steps, so no CPU test runs it): the initial grid temperature interpolated back to the
+    markers, then per step the rock properties, the pre-solver averages, one nodal Picard
+    iteration, the displacement-limited step, the post-Stokes steps, the heat step and RK4
+    advection.  Returns {step: dimensionless RMS velocity} every `every` steps and at the last."""
+    from oracle import boundary as B
+    from oracle.heat import HeatOracle
+    from oracle.picard import OraclePicard
+    syn = eb.synthetic
+    model = syn.box_convection()
+    op = OraclePicard(model)
+    p, g, m = op.model.params, model.grid, op.mic
+    rt, dt_ve = p["rock_tables"], p["timestep"]
+    m.get_marker_inside_flags()
+    m.initialize_bilinear_interpolation()
+    m.interpolate_marker_heat_parameters_to_grid()
+    m.interpolate_temperature_to_markers()
+    nsteps, out = 99 * p["nskip_output"], {}
+    for step in range(1, nsteps + 1):
+        p["timestep"] = dt_ve
+        m.get_marker_inside_flags()
+        upd = B.rock_properties(m.mk, rt["mat_rho"], rt["mat_cp"], rt["mat_kt"], rt["density_model"],
+                                rt["rhocp_model"], rt["conductivity_model"], p["temperature_top"], 1200.0)
+        for k, v in upd.items():
+            m.mk[k][:] = v
+        m.initialize_bilinear_interpolation()
+        m.interpolate_marker_heat_parameters_to_grid()
+        m.update_marker_rheology()
+        m.update_marker_viscoplastic_viscosity(use_marker_plasticity=False)
+        m.interpolate_marker_stokes_parameters_to_grid()
+        op.so.interpolate_basic_viscoplastic_viscosity_to_pressure_grid(0)
+        op.picard_loop_nodes(1, 1e-3, 0)
+        op.so.interpolate_stag_velocity_to_basic_grid()
+        m.calc_marker_viscoplastic_viscosity()
+        p["timestep"] = B.timestep_displacement_limit(g, op.gr["vx1"], op.gr["vy1"], p["marker_cell_displ_max"], 0,
+                                                      dt_ve)
+        op.so.forecast_viscoelastic_grid_stress()
+        m.post_stokes_marker_gathers()
+        m.apply_marker_stress_correction()
+        ho = HeatOracle(op.model, grids=op.gr)
+        ho.heat_step()
+        for k in ("dtk1", "tk2"):
+            op.gr[k] = np.asfortranarray(ho.gr[k])
+        m.subgrid_heat_diffusion_update()
+        m.add_remaining_grid_change_to_marker_temperature()
+        m.advect_markers_and_rotate_stress()
+        m.update_marker_strain()
+        if step % every == 0 or step == nsteps:
+            out[step] = syn.box_convection_vrms(g, op.gr["vx1"], op.gr["vy1"], 5.0, 1250.0, 4000.0)
+    return out
