@@ -998,6 +998,153 @@ def channel_flow_non_steady_temperature_profile(x: np.ndarray, tmyr: float, widt
     return t0 + dT - 273.0
 
 
+def plasticity_benchmark_kaus10(xnum: int = 401, ynum: int = 101, mpc: int = 3) -> Model:
+    """The reference's Kaus (2010) plasticity benchmark, as configured in
+    src/benchmarks/models/plasticity_benchmark_kaus10/{model,materials}.yml and the benchmark
+    material library (Plasticity_Benchmark_Kaus10): a 40 x 12 km box on 401 x 101 nodes with
+    3 x 3 markers per cell on a regular lattice; 2 km of sticky air (1 kg/m^3, 1e19 Pa s, shear
+    modulus 1e21 Pa) over a visco-elasto-plastic layer (1e25 Pa s, 5e10 Pa, cohesion 40 MPa
+    softening to 5 MPa between plastic strains 0 and 0.1, friction angle 30 degrees), the
+    layer split into the seven-layer model's material ids 3-8 (SevenLayerEarthModel2D, all of
+    them CrustKaus10), with a weak notch of 1e20 Pa s at the bottom centre
+    (WeakNotch.get_seed_limits_weak_notch with the model height as its base: 800 m wide,
+    400 m high, material id 9).  Density: DensityLiao14 at the uniform 273 K,
+    rho0 (1 - alpha (T - 298.15)).  ExtensionNoBottomInflowBC.jl: the sides move apart at half of
+    the full extension velocity strain_rate_bc x xsize = 1e-15 1/s x 40 km
+    (VelocityFromStrainRate.jl), the top lets in vyu = v_full ysize / xsize
+    (ExtensionFreeSlipAlongBottom.calc_velocity!), free slip on the bottom, pressure 1e5 Pa in
+    the upper-left cell; nodal plasticity loop (up to 100 iterations, tolerance 1e-3), 15 kyr
+    viscoelastic steps with the 0.5-cell displacement limit, viscosity 1e19-1e25 Pa s, yield
+    stress 20 MPa-1 GPa, gravity 10 m/s^2.  The reference stops at an extensional strain
+    v_full t / xsize of 0.02 (Stopping.check_extensional_strain_stopping).  The heat solve is
+    on in the reference but leaves the uniform temperature unchanged (equal top and bottom
+    temperatures, no shear, adiabatic or radiogenic heating)."""
+    W, H = 40000.0, 12000.0
+    grid = staggered_grid(np.linspace(0.0, W, xnum), np.linspace(0.0, H, ynum))
+    mx, my = (xnum - 1) * mpc, (ynum - 1) * mpc
+    x = np.repeat((np.arange(mx) + 0.5) * (W / mx), my)
+    y = np.tile((np.arange(my) + 0.5) * (H / my), mx)
+    n = len(x)
+    thick_air, thick_layer = 2000.0, 1666.67
+    tops = thick_air + thick_layer * np.arange(1, 6)
+    matid = np.where(y <= thick_air, 1, 3 + np.searchsorted(tops, y, side="left")).astype(np.int16)
+    matid = np.minimum(matid, 8).astype(np.int16)
+    w_seed, x_seed = 800.0, 20000.0
+    notch = (H - w_seed / 2.0 <= y) & (y <= H) & (x_seed - w_seed / 2.0 <= x) & (x <= x_seed + w_seed / 2.0)
+    matid[notch] = 9
+    T0 = 273.0
+    nmat = 9
+    rock = np.zeros(nmat, bool)
+    rock[2:8] = True
+    rho_rock = 2700.0 * (1.0 - 3.0e-5 * (T0 - 298.15))
+    rho = np.where(np.arange(nmat) >= 2, rho_rock, 1.0)
+    eta = np.where(rock, 1e25, 1e19)
+    eta[8] = 1e20
+    mu = np.where(np.arange(nmat) >= 2, 5e10, 1e21)
+    cp = np.where(np.arange(nmat) >= 2, 1200.0, 100.0)
+    kt = np.where(np.arange(nmat) >= 2, 3.0, 20.0)
+    sin30 = math.sin(math.radians(30.0))
+    mat_plastic = np.zeros((nmat, 6))
+    mat_plastic[rock, :] = [40e6, 5e6, sin30, sin30, 0.0, 0.1]
+    mat_flow = np.zeros((nmat, 12))
+    mat_flow[:, 0] = eta
+    mats = Materials(mat_mu=mu, mat_hr=np.zeros(nmat), mat_flow_type=np.zeros(nmat, np.int64),
+                     mat_flow=np.asfortranarray(mat_flow), mat_plastic=np.asfortranarray(mat_plastic), mat_rho=rho)
+    mi = matid.astype(np.int64) - 1
+    m = {"x": x, "y": y, "matid": matid, "rho": rho[mi].copy(), "eta": eta[mi].copy(), "eta_flow": eta[mi].copy(),
+         "sr_ratio": np.ones(n), "tk": np.full(n, T0), "kt": kt[mi].copy(), "rhocp": rho[mi] * cp[mi],
+         "ha": np.zeros(n)}
+    m["cohesion"] = mat_plastic[mi, 0].copy()
+    m["fric_ini"] = mat_plastic[mi, 2].copy()
+    m["fric"] = m["fric_ini"].copy()
+    for f in ("preexp", "sxx", "sxy", "exx", "exy", "pr", "gii", "strain_plastic"):
+        m[f] = np.zeros(n)
+    _fields_common(np.random.Generator(np.random.Philox(0)), n, m)
+    m["pfailure"][:] = 0.0
+    grids = _analytic_grids(grid, v0=0.0, eta_ref=1e25, rho_ref=rho_rock, T0=T0, T1=T0, depth_T1=H,
+                            y_surface=thick_air)
+    edot = 1e-15
+    v_full = edot * W
+    vyu = v_full * H / W
+    grids.update(velocity_bcs(grid, v_ext=0.5 * v_full))
+    F = np.asfortranarray
+    grids["btopy"] = F(np.column_stack([np.full(xnum + 1, vyu), np.zeros(xnum + 1)]))
+    grids["bbottomy"] = F(np.zeros((xnum + 1, 2)))
+    params = default_params(timestep=15e3 * YEAR, viscosity_min=1e19, viscosity_max=1e25, yield_stress_min=2e7,
+                            yield_stress_max=1e9, temperature_top=T0, temperature_bottom=T0, itype_global=1,
+                            matid_sticky_air=1, subgrid_diff_coef_stress=1.0, subgrid_diff_coef_temp=1.0)
+    params.update(stokes_params(pressure_bc_mode=0, pressure_bc=1e5, gravity_y=10.0, iuse_interface_stabilization=0))
+    params.update(nglobal=100, tolerance_picard=1e-3, marker_cell_displ_max=0.5, strain_rate_bc=edot,
+                  full_velocity_extension=v_full, velocity_y_upper=vyu, strain_limit=0.02, thick_air=thick_air,
+                  w_seed=w_seed, x_seed=x_seed, friction_angle=30.0, dilation_angle=0.0)
+    return Model("plasticity_benchmark_kaus10", grid, mats, params, m, grids)
+
+
+def pressure_grid_value(grid: Grid, arr: np.ndarray, x: float, y: float) -> float:
+    """GridToMarker.get_marker_value_from_pressure_grid_without_mapping_input
+    (interpolation/utils/GridToMarker.jl:51-79 with MarkerGridMapping.upr_left_index_pressure and
+    upr_left_dist_pressure, :311-350): the basic cell holding the point, the pressure node up and
+    to the left of it (clamped to the interior cells), and bilinear weights from the staggered
+    coordinates; arr is a (ynum-1, xnum-1) pressure-grid array."""
+    def axis(b, stag, sstag, v, nn):
+        i = int(np.clip(np.searchsorted(b, v, side="right") - 1, 0, nn - 2))
+        p = i - 1 if v < stag[i + 1] else i
+        p = min(max(p, 0), nn - 3)
+        return p, (v - stag[p + 1]) / sstag[p + 1]
+    yn, dy = axis(grid.gridy_b, grid.gridy_vx, grid.ystp_vx, y, grid.ynum)
+    xn, dx = axis(grid.gridx_b, grid.gridx_vy, grid.xstp_vy, x, grid.xnum)
+    return float((1.0 - dx) * (1.0 - dy) * arr[yn, xn] + (1.0 - dx) * dy * arr[yn + 1, xn]
+                 + dx * (1.0 - dy) * arr[yn, xn + 1] + dx * dy * arr[yn + 1, xn + 1])
+
+
+def kaus10_measurement_lines(grid: Grid, params: dict) -> tuple:
+    """The sample points of the reference's shear-zone measurement
+    (post_processing/numerical/PlasticityBenchmarkK10.jl:325-400): four vertical lines, at w_seed/4
+    and w_seed/4 + 2 km outside the left and the right edge of the notch (left near, left far,
+    right near, right far), each sampled at ynum x 10 points between the bottom of the sticky air
+    and the top of the notch.  Returns (x of the four lines, y of the samples)."""
+    H = grid.ymax
+    w_seed, x_seed = params["w_seed"], params["x_seed"]
+    xmin_n, xmax_n = x_seed - w_seed / 2.0, x_seed + w_seed / 2.0
+    notch_thick = w_seed / 2.0
+    y0 = params["thick_air"]
+    npoints = grid.ynum * 10
+    ys = y0 + (H - y0 - notch_thick) / (npoints - 1) * np.arange(npoints)
+    xs = (xmin_n - w_seed / 4.0, xmin_n - (w_seed / 4.0 + 2000.0), xmax_n + w_seed / 4.0,
+          xmax_n + (w_seed / 4.0 + 2000.0))
+    return xs, ys
+
+
+def kaus10_fault_dip(grid: Grid, eii: np.ndarray, params: dict) -> dict:
+    """The reference's measurement of the shear-zone dip
+    (post_processing/numerical/PlasticityBenchmarkK10.jl:200-245 and 325-450): on each of the
+    lines of kaus10_measurement_lines the depth of the largest strain-rate invariant (the first
+    of equal maxima) gives one end of a fault stick; each side's dip is atan(|dy| / |dx|) of its
+    stick, and the mean of the two dips is compared with the target, the mean of the Coulomb
+    (45 + phi/2) and Arthur (45 + (phi + psi)/4) angles.  Returns the dips (degrees), the target
+    and the relative error."""
+    xs, ys = kaus10_measurement_lines(grid, params)
+
+    def ymax_at(xp):
+        best, ybest = -1e32, -1e32
+        for yp in ys:
+            v = pressure_grid_value(grid, eii, xp, yp)
+            if v > best:
+                best, ybest = v, yp
+        return ybest
+    x1l, x2l, x1r, x2r = xs
+    y1l, y2l, y1r, y2r = (ymax_at(x) for x in xs)
+    th_l = math.degrees(math.atan(abs(y2l - y1l) / abs(x2l - x1l)))
+    th_r = math.degrees(math.atan(abs(y2r - y1r) / abs(x2r - x1r)))
+    phi, psi = params["friction_angle"], params["dilation_angle"]
+    coulomb, arthur = 45.0 + phi / 2.0, 45.0 + (phi + psi) / 4.0
+    target = (coulomb + arthur) / 2.0
+    theta = (th_l + th_r) / 2.0
+    return {"theta_left": th_l, "theta_right": th_r, "theta": theta, "target": target,
+            "relative_error": abs(theta - target) / abs(target),
+            "sticks": {"left": ((x1l, y1l), (x2l, y2l)), "right": ((x1r, y1r), (x2r, y2r))}}
+
+
 def ramberg_wave_velocity(h1: float, h2: float, rho1: float, rho2: float, eta1: float, eta2: float, amp: float,
                           lam: float, g: float = 9.81) -> float:
     """Ramberg's (1968) analytical vertical velocity at the crest of a sinusoidal interface

@@ -349,3 +349,60 @@ def box_convection_oracle(eb, every: int = 1000):
         if step % every == 0 or step == nsteps:
             out[step] = syn.box_convection_vrms(g, op.gr["vx1"], op.gr["vy1"], 5.0, 1250.0, 4000.0)
     return out
+
+
+KAUS10_SEED = 10
+
+
+def kaus10_oracle(eb, nsteps: int | None = None, log=None):
+    """The Kaus (2010) plasticity benchmark through the oracle (tens of minutes on the host's
+    cores: a direct Stokes solve per nodal Picard iteration, so no CPU test runs it).  Per step,
+    as TimeLoop.run_loop! does for this model: inside flags, the pre-solver averages and rheology,
+    the nodal Picard loop (PlasticityLoopNodes.jl:36-92; up to nglobal iterations), the staggered
+    velocity on basic nodes, the nodal viscoplastic viscosity back to the markers, the
+    displacement-limited step, the post-Stokes steps with the subgrid stress diffusion, RK4
+    advection, the strain update, and the ExtensionNoBottomInflow recycling of the markers that
+    left the box.  The heat solve is left out: the temperature is uniform and stays so.  Stops at
+    the reference's extensional-strain limit (v_full t / xsize >= 0.02) or after nsteps.
+    log(step, Picard records, model time, pressure-grid strain-rate invariant) runs after each step.
+    Returns (model, final pressure-grid strain-rate invariant, per-step Picard iteration counts)."""
+    from oracle import boundary as B
+    from oracle.picard import OraclePicard
+    model = eb.synthetic.plasticity_benchmark_kaus10()
+    op = OraclePicard(model)
+    p, g, m = op.model.params, model.grid, op.mic
+    W = g.xmax - g.xmin
+    dt_ve, timesum, step, iters = p["timestep"], 0.0, 0, []
+    while True:
+        step += 1
+        p["timestep"] = dt_ve
+        m.get_marker_inside_flags()
+        m.initialize_bilinear_interpolation()
+        m.interpolate_marker_heat_parameters_to_grid()
+        m.update_marker_rheology()
+        m.update_marker_viscoplastic_viscosity(use_marker_plasticity=False)
+        m.interpolate_marker_stokes_parameters_to_grid()
+        op.so.interpolate_basic_viscoplastic_viscosity_to_pressure_grid(1)
+        hist = op.picard_loop_nodes(int(p["nglobal"]), p["tolerance_picard"], 1)
+        iters.append(len(hist))
+        op.so.interpolate_stag_velocity_to_basic_grid()
+        m.calc_marker_viscoplastic_viscosity()
+        p["timestep"] = B.timestep_displacement_limit(g, op.gr["vx1"], op.gr["vy1"], p["marker_cell_displ_max"], 0,
+                                                      dt_ve)
+        op.so.forecast_viscoelastic_grid_stress()
+        m.post_stokes_marker_gathers()
+        m.update_subgrid_stress()
+        m.apply_marker_stress_correction()
+        m.advect_markers_and_rotate_stress()
+        m.update_marker_strain()
+        m.get_marker_inside_flags()
+        out, _, _ = B.recycle_no_bottom_inflow(m.mk, 1, W, p["velocity_y_upper"], p["timestep"],
+                                               p["temperature_top"], model.mats.mat_plastic, KAUS10_SEED, step)
+        for k, v in out.items():
+            m.mk[k][:] = v
+        timesum += p["timestep"]
+        if log is not None:
+            log(step, hist, timesum, op.gr["eii"])
+        if p["full_velocity_extension"] * timesum / W >= p["strain_limit"] or (nsteps and step >= nsteps):
+            break
+    return model, np.array(op.gr["eii"]), iters
