@@ -14,7 +14,10 @@ analytic profile.
 
 Non-steady channel temperature (src/benchmarks/models/channel_flow_non_steady_temperature):
 advection of a vertical temperature gradient by Poiseuille flow with conduction to the walls,
-against the transient analytic profile at every output."""
+against the transient analytic profile at every output.
+
+Kaus (2010) plasticity (src/benchmarks/models/plasticity_benchmark_kaus10): the first two steps
+of the nodal Picard loop against the oracle's own nine-step record, which the GPU test reads."""
 from benchmark_cases import rotation_check, solid_body_rotation_oracle
 
 
@@ -61,3 +64,21 @@ def test_oracle_non_steady_channel_temperature_follows_the_transient_solution(eb
     for out, (tmyr, row) in rows.items():
         err = nst_error(eb, model, row, tmyr)
         assert err < 0.007, (out, tmyr, err)
+
+
+def test_oracle_kaus10_first_steps_reproduce_its_record(eb):
+    """The Kaus (2010) benchmark's first two steps through the oracle (about ten seconds) give the
+    Picard iterations and yielding-node counts recorded in tests/golden/kaus10_oracle_9steps.npz,
+    the record the GPU test compares its nine steps against."""
+    import pathlib
+
+    import numpy as np
+
+    from benchmark_cases import kaus10_oracle
+    g = np.load(pathlib.Path(__file__).resolve().parent / "golden" / "kaus10_oracle_9steps.npz")
+    counts = []
+    _, eii, iters = kaus10_oracle(eb, nsteps=2, log=lambda s, h, t, e: counts.append([r["nnode_yield"] for r in h]))
+    assert iters == g["iters"][:2].tolist()
+    for s, c in enumerate(counts, start=1):
+        assert c == g[f"nnode_{s}"].tolist(), (s, c)
+    assert np.all(np.isfinite(eii)) and eii.max() > 0.0
